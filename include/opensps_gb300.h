@@ -1,0 +1,37 @@
+/*
+ * opensps_gb300.h — entry points of libopensps_gb300.so that OpenSPS does not have.
+ *
+ * They serve callers that keep their inputs on the GPU (a fitting loop that draws its weights on the device, the
+ * benchmark's device-resident timing). They have no counterpart in OpenSPS's include/opensps.h.
+ */
+#ifndef OPENSPS_GB300_H
+#define OPENSPS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Number of doubles per model in the device parameter table of opensps_gb300_batch_device, and their order:
+ * dust1, dust2, dust3, dust_index, dust1_index, frac_nodust, frac_obrun, zred, igm_factor, sigma_smooth,
+ * dust_tesc. */
+#define OPENSPS_GB300_DEVICE_PARAMS 11
+
+/* A batch of n models whose inputs are already in device memory: d_params (OPENSPS_GB300_DEVICE_PARAMS x n
+ * doubles, column-major) and d_wz (ntfull x nz x n doubles, the ssp_weights_z of the C API). The context's
+ * settings and its min/max_wave_smooth apply. Outputs stay on the device: the spectra in the context's buffer
+ * (opensps_context_batch_spec_device) and, when d_mags is not NULL, the magnitudes (nbands x n doubles) in d_mags.
+ * Asynchronous on the context's stream unless sync != 0. Status as opensps_context_compute_csp_batch. */
+void opensps_gb300_batch_device(int handle, int n, const double *d_params, const double *d_wz, double *d_mags,
+                                int sync, int *status);
+
+/* The context's CUDA stream (cudaStream_t) and the device it runs on. */
+void opensps_gb300_context_stream(int handle, void **stream, int *device, int *status);
+
+/* Kernel launches of the last batch on the handle (for the benchmark's launch count). */
+void opensps_gb300_last_launches(int handle, int *launches, int *status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENSPS_GB300_H */

@@ -1,0 +1,252 @@
+"""ctypes binding of libopensps_gb300.so: the OpenSPS C API entry points of this path.
+
+This is the binding an OpenSPS Python caller would add (the external ``opensps-python`` binds the same symbols
+through ctypes/cffi): every function takes and returns what ``include/opensps.h`` declares, and a nonzero status
+raises :class:`OpenSPSError` with the library's last-error message.
+
+The library is the product: it must be built (``libopensps_gb300.build.build()``) and there is no fallback; importing
+this module without it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import synthdata
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libopensps_gb300.so"
+_lib = None
+
+NBGRAD = 44
+DEVICE_PARAMS = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
+                 "igm_factor", "sigma_smooth", "dust_tesc")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes): every symbol of include/opensps.h and include/opensps_gb300.h
+SIGNATURES = {
+    "opensps_clear_error": (None, []),
+    "opensps_get_last_error": (None, [_ip, C.c_char_p, C.c_int]),
+    "opensps_get_nbgrad": (None, [_ip]),
+    "opensps_get_grad_param_name": (None, [C.c_int, C.c_char_p, C.c_int, _ip]),
+    "opensps_context_create": (None, [_ip, _ip]),
+    "opensps_context_destroy": (None, [C.c_int, _ip]),
+    "opensps_context_setup": (None, [C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, _ip]),
+    "opensps_context_set_int": (None, [C.c_int, C.c_char_p, C.c_int, _ip]),
+    "opensps_context_set_float": (None, [C.c_int, C.c_char_p, C.c_double, _ip]),
+    "opensps_context_set_str": (None, [C.c_int, C.c_char_p, C.c_char_p, _ip]),
+    "opensps_context_set_fast_mode": (None, [C.c_int, C.c_int, _ip]),
+    "opensps_context_get_dims": (None, [C.c_int, _ip, _ip, _ip]),
+    "opensps_context_get_nspec": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_get_ntfull": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_get_nbands": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_get_nz": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_get_nemline": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_get_zsol": (None, [C.c_int, _dp, _ip]),
+    "opensps_context_get_lambda": (None, [C.c_int, _dp, _ip]),
+    "opensps_context_get_ages": (None, [C.c_int, _dp, _ip]),
+    "opensps_context_get_zlegend": (None, [C.c_int, _dp, _ip]),
+    "opensps_context_get_emlambda": (None, [C.c_int, _dp, _ip]),
+    "opensps_context_set_filters_library": (None, [C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, _ip]),
+    "opensps_context_set_mag_compute": (None, [C.c_int, C.c_int, _ip, _ip]),
+    "opensps_context_compute_csp_batch": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp] + [_dp] * 8
+                                          + [_ip]),
+    "opensps_context_compute_csp_batch_parts": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp]
+                                                + [_dp] * 14 + [_ip]),
+    "opensps_context_batch_spec_device": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip, _ip, _ip]),
+    "opensps_context_batch_spec_host": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip, _ip, _ip]),
+    "opensps_context_compute_csp_batch_grad": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp, _dp,
+                                                      _dp, _dp, _dp, _dp, _dp] + [_dp] * 8 + [_dp, _dp, _dp, _ip]),
+    "opensps_context_compute_csp_batch_grad_rows": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp,
+                                                           _dp, _dp, _dp, _dp, _dp, _dp] + [_dp] * 8
+                                                    + [_dp, C.c_int, _dp, _dp, _ip]),
+    "opensps_gb300_batch_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
+    "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
+    "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
+}
+
+
+class OpenSPSError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads the C-ABI library (built in-tree); raises if it is missing. No CUDA call is made here."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else _LIB_PATH
+    if not p.exists():
+        raise OSError(f"{p} is not built: run libopensps_gb300.build.build() (python -c 'import __graft_entry__ as g; "
+                      f"g.build()')")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def _check(status: C.c_int, lib: C.CDLL):
+    if status.value != 0:
+        st = C.c_int(0)
+        buf = C.create_string_buffer(512)
+        lib.opensps_get_last_error(C.byref(st), buf, 512)
+        raise OpenSPSError(status.value, buf.value.decode(errors="replace"))
+
+
+def _names_values(params: dict[str, np.ndarray], n: int):
+    names = list(params.keys())
+    arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(params[k], dtype=np.float64), (n,))) for k in names]
+    c_names = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+    c_vals = (_dp * max(1, len(names)))(*[a.ctypes.data_as(_dp) for a in arrs])
+    return len(names), c_names, c_vals, arrs
+
+
+class Context:
+    """One OpenSPS context (a handle), set up on the synthetic libraries of the data root."""
+
+    def __init__(self, data_root: str | os.PathLike | None = None, setup: bool = True):
+        self.lib = load_library()
+        root = Path(data_root) if data_root else synthdata.default_root()
+        synthdata.generate(root)
+        os.environ["OPENSPS_DATA_HOME"] = str(root)
+        h, st = C.c_int(0), C.c_int(0)
+        self.lib.opensps_context_create(C.byref(h), C.byref(st))
+        _check(st, self.lib)
+        self.handle = h.value
+        if setup:
+            self.setup()
+
+    # -- lifecycle
+    def setup(self, isoc: str = "synthetic", spec: str = "synthetic", dust: str = "none"):
+        st = C.c_int(0)
+        self.lib.opensps_context_setup(-1, isoc.encode(), spec.encode(), dust.encode(), self.handle, C.byref(st))
+        _check(st, self.lib)
+
+    def close(self):
+        if getattr(self, "handle", 0):
+            st = C.c_int(0)
+            self.lib.opensps_context_destroy(self.handle, C.byref(st))
+            self.handle = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- settings
+    def set_int(self, key: str, value: int):
+        st = C.c_int(0)
+        self.lib.opensps_context_set_int(self.handle, key.encode(), int(value), C.byref(st))
+        _check(st, self.lib)
+
+    def set_float(self, key: str, value: float):
+        st = C.c_int(0)
+        self.lib.opensps_context_set_float(self.handle, key.encode(), float(value), C.byref(st))
+        _check(st, self.lib)
+
+    def set_filters_library(self, name: str):
+        st = C.c_int(0)
+        self.lib.opensps_context_set_filters_library(self.handle, name.encode(), 0, 2, 0, C.byref(st))
+        _check(st, self.lib)
+
+    def _get_int(self, fn) -> int:
+        v, st = C.c_int(0), C.c_int(0)
+        getattr(self.lib, fn)(self.handle, C.byref(v), C.byref(st))
+        _check(st, self.lib)
+        return v.value
+
+    @property
+    def nspec(self) -> int: return self._get_int("opensps_context_get_nspec")
+    @property
+    def ntfull(self) -> int: return self._get_int("opensps_context_get_ntfull")
+    @property
+    def nbands(self) -> int: return self._get_int("opensps_context_get_nbands")
+    @property
+    def nz(self) -> int: return self._get_int("opensps_context_get_nz")
+    @property
+    def nemline(self) -> int: return self._get_int("opensps_context_get_nemline")
+
+    def _get_arr(self, fn, n) -> np.ndarray:
+        out, st = np.empty(n), C.c_int(0)
+        getattr(self.lib, fn)(self.handle, _ptr(out), C.byref(st))
+        _check(st, self.lib)
+        return out
+
+    def wavelengths(self) -> np.ndarray: return self._get_arr("opensps_context_get_lambda", self.nspec)
+    def ages(self) -> np.ndarray: return self._get_arr("opensps_context_get_ages", self.ntfull)
+    def zlegend(self) -> np.ndarray: return self._get_arr("opensps_context_get_zlegend", self.nz)
+
+    # -- batches
+    def csp_batch(self, params: dict, ssp_weights_z: np.ndarray | None = None, ssp_weights: np.ndarray | None = None,
+                  spec: bool = True, mass: bool = True, lbol: bool = True) -> dict:
+        """compute_csp_batch_grad with no cotangents (the forward batch): weights (n, nz, nt) or (n, nt)."""
+        if ssp_weights_z is not None:
+            w = np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
+            n = w.shape[0]
+        else:
+            w = np.ascontiguousarray(ssp_weights, dtype=np.float64)
+            n = w.shape[0]
+        ns, nb = self.nspec, self.nbands
+        k, c_names, c_vals, keep = _names_values(params, n)
+        out = {"mags": np.empty((n, nb))}
+        if spec: out["spec"] = np.empty((n, ns))
+        if mass: out["mass"] = np.empty(n)
+        if lbol: out["lbol"] = np.empty(n)
+        st = C.c_int(0)
+        if ssp_weights_z is not None:
+            self.lib.opensps_context_compute_csp_batch_grad(
+                self.handle, n, k, c_names, c_vals, None, _ptr(w), None, None, None, None, None,
+                _ptr(out["mags"]), _ptr(out.get("spec")), _ptr(out.get("mass")), _ptr(out.get("lbol")), None, None,
+                None, None, None, None, None, C.byref(st))
+        else:
+            self.lib.opensps_context_compute_csp_batch(
+                self.handle, n, k, c_names, c_vals, _ptr(w), _ptr(out["mags"]), _ptr(out.get("spec")),
+                _ptr(out.get("mass")), _ptr(out.get("lbol")), None, None, None, None, C.byref(st))
+        _check(st, self.lib)
+        del keep
+        return out
+
+    def batch_device(self, n: int, d_params: int, d_wz: int, d_mags: int | None, sync: bool = True):
+        """opensps_gb300_batch_device with device pointers (integers, e.g. torch.Tensor.data_ptr())."""
+        st = C.c_int(0)
+        self.lib.opensps_gb300_batch_device(self.handle, n, C.c_void_p(d_params), C.c_void_p(d_wz),
+                                            C.c_void_p(d_mags) if d_mags else None, 1 if sync else 0, C.byref(st))
+        _check(st, self.lib)
+
+    def spec_device(self):
+        p, ns, n, b, st = C.c_void_p(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self.lib.opensps_context_batch_spec_device(self.handle, C.byref(p), C.byref(ns), C.byref(n), C.byref(b),
+                                                   C.byref(st))
+        _check(st, self.lib)
+        return p.value, ns.value, n.value, b.value
+
+    def stream(self) -> int:
+        s, d, st = C.c_void_p(), C.c_int(), C.c_int()
+        self.lib.opensps_gb300_context_stream(self.handle, C.byref(s), C.byref(d), C.byref(st))
+        _check(st, self.lib)
+        return s.value or 0
+
+    def last_launches(self) -> int:
+        return self._get_int("opensps_gb300_last_launches")

@@ -1,0 +1,524 @@
+// The batch driver: per-model parameters and checks on the host, then the device pipeline
+//   weights_prep -> model_params -> contraction (+ fused epilogue) -> bands / magnitudes
+// on the context's stream (OpenSPS compute_csp_batch, src/physics/opensps_csp_batch.f90:431-1214).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "context.h"
+
+namespace sps {
+
+// ---------------------------------------------------------------------------------------------- find_interval
+// 0-based index i with a[i] <= v < a[i + 1] for ascending or descending a (bisection over 0..n+1 as the reference's
+// find_interval, src/math/opensps_interpolation.f90:152-197, with its end cases), as the reference's 1-based
+// result minus one (so -1 below an ascending table).
+__host__ __device__ static int find_interval0(const double *a, int n, double v) {
+    if (n < 2) return 0;
+    const bool asc = a[n - 1] >= a[0];
+    int lower = 0, upper = n + 1;
+    while (upper - lower > 1) {
+        const int mid = (upper + lower) / 2;
+        const bool ge = v >= a[mid - 1];
+        if (asc == ge) lower = mid; else upper = mid;
+    }
+    if (v == a[0]) return 0;
+    if (v == a[n - 1]) return n - 2;
+    return lower - 1;
+}
+
+// ---------------------------------------------------------------------------------------------- model params
+struct ModelParamArgs {
+    int n, nspec, jtop, add_igm, smooth, i0;   // i0: the pixel whose smoothing row gives the model's taps
+    const double *par;       // PAR_DEVICE x n
+    const float *igm_a;      // jtop x 6
+    const double *lam;       // nspec
+    const double *zt, *dl;   // 500
+    double dlnl;
+    float *mpar;             // n x MODEL_PAR_FLOATS
+    double *zshift;          // n x 4
+    double *dist;            // n
+};
+
+__global__ void model_params_kernel(ModelParamArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double *p = a.par + (size_t)PAR_DEVICE * m;
+    float *o = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    for (int i = 0; i < MODEL_PAR_FLOATS; ++i) o[i] = 0.f;
+    const double d1 = p[PF_DUST1], d2 = p[PF_DUST2], d3 = p[PF_DUST3], fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
+    // attenuate_batch / pixel_transmissions (src/physics/opensps_csp_batch.f90:3576-3660, 3765-3818)
+    o[MP_DUST2] = (float)d2;
+    if (1.0 - fnd <= SAFE_FLOOR) { o[MP_ONE_M_FND] = 0.f; o[MP_FND] = 1.f; }
+    else { o[MP_ONE_M_FND] = (float)(1.0 - fnd); o[MP_FND] = (float)fnd; }
+    o[MP_DUST_INDEX] = (float)p[PF_DUST_INDEX];
+    o[MP_DUST1] = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)d1;
+    o[MP_DUST1_INDEX] = (float)p[PF_DUST1_INDEX];
+    o[MP_ONE_M_FO] = (float)(1.0 - fo);
+    o[MP_FO] = (float)fo;
+    o[MP_DUST3] = (fabs(d3) <= SAFE_FLOOR) ? 0.f : (float)d3;
+    // IGM (apply_igm_z :4205-4299): redshift factors and the short-wavelength cap
+    const double z = p[PF_ZRED];
+    o[MP_IGM_JMAX] = __int_as_float(0);
+    o[MP_SMOOTH_R] = __int_as_float(-1);
+    if (a.add_igm && z > SAFE_FLOOR && a.jtop > 0) {
+        const double opz = 1.0 + z;
+        float b[6];
+        b[0] = (float)pow(opz, 3.46);
+        b[1] = (float)pow(opz, 1.68);
+        b[2] = (float)pow(opz, 3.0 + 0.46);
+        b[3] = (float)pow(opz, 1.5 + 0.18);
+        b[4] = (float)pow(opz, 3.0 - 1.32);
+        b[5] = (float)pow(opz, 1.68);
+        float tmax = 0.f;
+        int jmax = 1;
+        for (int j = 0; j < a.jtop; ++j) {
+            const float *ia = a.igm_a + (size_t)j * 6;
+            const float t = ia[0] * b[0] + ia[1] * b[1] + ia[2] * b[2] + ia[3] * b[3] + ia[4] * b[4] + ia[5] * b[5];
+            if (t > tmax) { tmax = t; jmax = j + 1; }
+        }
+        for (int k = 0; k < 6; ++k) o[MP_IGM_B + k] = b[k];
+        o[MP_IGM_FACTOR] = (float)p[PF_IGM_FACTOR];
+        o[MP_IGM_TMAX] = tmax;
+        o[MP_IGM_JMAX] = __int_as_float(jmax);
+        o[MP_IGM_ON] = 1.f;
+    }
+    // velocity smoothing taps: row i0 of build_velocity_kernel (src/spectra/opensps_smoothing.f90:553-633)
+    const double sig = p[PF_SIGMA_SMOOTH];
+    if (a.smooth && sig > SAFE_FLOOR && a.i0 >= 0) {
+        const int n = a.nspec, i = a.i0;
+        const double sb = sig / (C_LIGHT * 1.0e-13);
+        const double inv2s2 = 0.5 * (1.0 / sb) * (1.0 / sb);
+        const double vl = a.lam[i] * exp(-4.0 * sb), vh = a.lam[i] * exp(4.0 * sb);
+        // il: first pixel >= vl, one lower when it lies above vl; ih: first pixel >= vh
+        int lo = 0, hi = n;
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vl) lo = md + 1; else hi = md; }
+        int il = lo < n ? lo : n - 1;
+        if (il > 0 && a.lam[il] > vl) il--;
+        lo = il; hi = n;
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vh) lo = md + 1; else hi = md; }
+        int ih = lo < n ? lo : n - 1;
+        if (ih < il) ih = il;
+        if (ih - il + 1 >= 2 && i - il <= 4 && ih - i <= 4) {
+            double w[9], tw = 0.0;
+            const double lli = log(a.lam[i]);
+            for (int j = il; j <= ih; ++j) {
+                const double d = lli - log(a.lam[j]);
+                double wj = exp(-inv2s2 * d * d) / a.lam[j];
+                const double dlft = (j > il) ? a.lam[j] - a.lam[j - 1] : 0.0;
+                const double drgt = (j < ih) ? a.lam[j + 1] - a.lam[j] : 0.0;
+                wj = 0.5 * wj * (dlft + drgt);
+                w[j - il] = wj;
+                tw += wj;
+            }
+            if (tw > SAFE_FLOOR) {
+                for (int j = il; j <= ih; ++j) o[MP_TAPS + 4 + (j - i)] = (float)(w[j - il] / tw);
+                o[MP_SMOOTH_R] = __int_as_float(max(i - il, ih - i));
+            }
+        }
+    }
+    // observed frame: the shift of lambda / (1 + z) on the log-uniform grid, in pixels
+    double *zs = a.zshift + (size_t)4 * m;
+    if (fabs(z) > SAFE_FLOOR) {
+        const double s = log1p(z) / a.dlnl;
+        const double n0 = floor(s), phi = s - n0;
+        zs[0] = n0;
+        zs[1] = phi > 0.0 ? expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl) : 0.0;
+        zs[2] = s;
+        zs[3] = 1.0;
+    } else {
+        zs[0] = 0.0; zs[1] = 0.0; zs[2] = 0.0; zs[3] = 0.0;
+    }
+    // distance term (distance_term, src/spectra/opensps_batch_photometry.f90:784-794)
+    double dd = 0.0;
+    if (fabs(z) > SAFE_FLOOR) {
+        int idx = find_interval0(a.zt, 500, z);
+        idx = max(0, min(idx, 498));
+        const double slope = (a.dl[idx + 1] - a.dl[idx]) / (a.zt[idx + 1] - a.zt[idx]);
+        const double dm = a.dl[idx] + slope * (z - a.zt[idx]);
+        if (dm == dm && dm > SAFE_FLOOR) dd = 5.0 * log10(dm / 10.0) - 2.5 * log10(1.0 + z);
+    }
+    a.dist[m] = dd;
+}
+
+// ---------------------------------------------------------------------------------------------- basis operand
+// The line profile of one line (compute_line_gaussians src/physics/opensps_gas.f90:303-340, windowed as
+// add_lines_to_spectrum :364-390): prof[j] for j in [jlo, jhi].
+static void line_profile(const Context &c, double pos, double sigma_kms, std::vector<double> &prof, int &jlo,
+                         int &jhi) {
+    const int n = c.nspec;
+    int j = find_interval0(c.lam.data(), n, pos) + 1;   // 1-based as the reference
+    j = std::max(1, std::min(j, n - 1));
+    const double res_min = c.lam[j] - c.lam[j - 1];
+    double sig = pos * sigma_kms * (1.0e13 / C_LIGHT);
+    sig = std::max(sig, 2.0 * res_min);
+    const double norm = (1.0 / (std::sqrt(2.0 * M_PI) * sig)) * (pos * pos / C_LIGHT);
+    prof.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        const double x = (c.lam[i] - pos) / sig;
+        prof[i] = norm * std::exp(-0.5 * x * x);
+    }
+    int jc = find_interval0(c.lam.data(), n, pos) + 1;
+    jc = std::max(1, std::min(jc, n));
+    int jh = std::min(jc + 1, n);
+    const double cut = 1.0e-14 * std::max(prof[jc - 1], prof[jh - 1]);
+    int jl = jc;
+    while (jl > 1 && prof[jl - 2] > cut) jl--;
+    while (jh < n && prof[jh] > cut) jh++;
+    jlo = jl - 1;
+    jhi = jh - 1;
+    if (cut <= 0.0) { jlo = 0; jhi = -1; }
+}
+
+// True when every line's width at sigma_kms is the grid floor (2 pixels' width at the line).
+static bool lines_floor_limited(const Context &c, double sigma_kms) {
+    for (int l = 0; l < c.nline; ++l) {
+        const double pos = c.line_lambda[l];
+        int j = find_interval0(c.lam.data(), c.nspec, pos) + 1;
+        j = std::max(1, std::min(j, c.nspec - 1));
+        const double res_min = c.lam[j] - c.lam[j - 1];
+        if (pos * sigma_kms * (1.0e13 / C_LIGHT) > 2.0 * res_min) return false;
+    }
+    return true;
+}
+
+static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double line_sigma, std::string &err) {
+    union { double d; long long i; } u;
+    u.d = neb ? line_sigma : -1.0;
+    const long long key = (u.i * 31 + (long long)nacc) * 1009 + itesc;
+    auto it = c.basis_cache.find(key);
+    if (it != c.basis_cache.end()) return it->second;
+    const int ns = c.nspec, nt = c.nt, nz = c.nz;
+    std::vector<double> b(c.ssp);
+    if (neb) {
+        // the young SSPs with their lines (add_neb_emission: linear in the weights, so part of the basis)
+        std::vector<double> prof;
+        for (int l = 0; l < c.nline; ++l) {
+            int jlo, jhi;
+            line_profile(c, c.line_lambda[l], line_sigma, prof, jlo, jhi);
+            for (int z = 0; z < nz; ++z)
+                for (int t = 0; t < nt; ++t) {
+                    const double L = c.line_lum[l + (size_t)c.nline * (t + (size_t)nt * z)];
+                    if (L == 0.0) continue;
+                    double *col = b.data() + (size_t)ns * (t + (size_t)nt * z);
+                    for (int j = jlo; j <= jhi; ++j) col[j] += prof[j] * L;
+                }
+        }
+    }
+    BasisOperand *op = new BasisOperand();
+    op->nacc = nacc;
+    op->itesc = itesc;
+    const int BK = contract_bk();
+    auto pad = [BK](int k) { return (k + BK - 1) / BK * BK; };
+    if (nacc == 1) {
+        op->nty = 0;
+        op->ky_pad = 0;
+        op->kpad = pad(nt * nz);
+    } else {
+        op->nty = itesc;
+        op->ky_pad = pad(itesc * nz);
+        op->kpad = op->ky_pad + pad((nt - itesc) * nz);
+    }
+    const int kpad = op->kpad;
+    std::vector<uint16_t> hi((size_t)ns * kpad, 0), lo((size_t)ns * kpad, 0);
+    for (int k = 0; k < kpad; ++k) {
+        int t = -1, z = -1;
+        if (nacc == 1) {
+            if (k < nt * nz) { t = k % nt; z = k / nt; }
+        } else if (k < op->ky_pad) {
+            if (itesc > 0 && k < itesc * nz) { t = k % itesc; z = k / itesc; }
+        } else {
+            const int kk = k - op->ky_pad, nto = nt - itesc;
+            if (nto > 0 && kk < nto * nz) { t = itesc + kk % nto; z = kk / nto; }
+        }
+        if (t < 0) continue;
+        const double *col = b.data() + (size_t)ns * (t + (size_t)nt * z);
+        for (int j = 0; j < ns; ++j) {
+            const float f = (float)col[j];
+            const uint16_t h = f32_to_bf16_bits(f);
+            hi[(size_t)j * kpad + k] = h;
+            lo[(size_t)j * kpad + k] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));
+        }
+    }
+    cudaError_t e;
+    if ((e = op->hi.reserve(hi.size())) != cudaSuccess || (e = op->lo.reserve(lo.size())) != cudaSuccess ||
+        (e = cudaMemcpy(op->hi.p, hi.data(), hi.size() * 2, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(op->lo.p, lo.data(), lo.size() * 2, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&op->tm_hi, op->hi.p, kpad, ns, BK, contract_bm())) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&op->tm_lo, op->lo.p, kpad, ns, BK, contract_bm())) != cudaSuccess) {
+        err = std::string("basis operand: ") + cudaGetErrorString(e);
+        op->hi.release(); op->lo.release();
+        delete op;
+        return nullptr;
+    }
+    c.basis_cache[key] = op;
+    return op;
+}
+
+// ---------------------------------------------------------------------------------------------- the batch
+static std::string cuda_msg(const char *what, cudaError_t e) { return std::string(what) + ": " + cudaGetErrorString(e); }
+
+int run_batch(Context &c, const BatchIO &io, std::string &err) {
+    const int n = io.n, ns = c.nspec, nt = c.nt, nz = c.nz, nb = c.nbands;
+    if (n <= 0) return 0;
+    const double *P = io.params;   // PF_COUNT x n
+    auto par = [&](int m, int id) { return P[(size_t)PF_COUNT * m + id]; };
+
+    // ---- checks shared by the batch (the reference's batch_check_models / plan_smoothing rules)
+    if (c.dust_type != 0) { err = "dust_type " + std::to_string(c.dust_type) + ": only the power law (0) on this path"; return ST_UNSUPPORTED; }
+    if (c.compute_vega_mags != 0) { err = "compute_vega_mags = 1 is not supported on this path"; return ST_UNSUPPORTED; }
+    if (c.smooth_velocity != 1) { err = "smooth_velocity = 0 is not supported on this path"; return ST_UNSUPPORTED; }
+    const double minl = par(0, PF_MIN_WAVE_SMOOTH), maxl = par(0, PF_MAX_WAVE_SMOOTH);
+    int itesc = -1;
+    bool nacc2 = false, any_smooth = false;
+    for (int m = 0; m < n; ++m) {
+        const double dla = par(m, PF_DUST_TESC) > SAFE_FLOOR ? par(m, PF_DUST_TESC) : 7.0;
+        int it = find_interval0(c.log_age.data(), nt, dla) + 1;
+        it = std::max(1, std::min(it, nt));
+        if (itesc < 0) itesc = it;
+        else if (it != itesc) { err = "dust_tesc must select the same age for every model of a batch on this path"; return ST_UNSUPPORTED; }
+        if (par(m, PF_MIN_WAVE_SMOOTH) != minl || par(m, PF_MAX_WAVE_SMOOTH) != maxl) {
+            err = "models must share min_wave_smooth and max_wave_smooth";
+            return ST_UNSUPPORTED;
+        }
+        const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
+        if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
+        const double sig = par(m, PF_SIGMA_SMOOTH);
+        if (sig > SAFE_FLOOR) {
+            any_smooth = true;
+            const double x = 4.0 * (sig / (C_LIGHT * 1.0e-13)) / c.dlnl;
+            if (x > 4.0 - 1e-9) {
+                err = "sigma_smooth above ~350 km/s (a window wider than +-4 pixels) is not supported on this path";
+                return ST_UNSUPPORTED;
+            }
+        }
+    }
+    // smoothing rows must keep their whole window inside the grid
+    int i0 = -1;
+    if (any_smooth) {
+        for (int j = 0; j < ns; ++j)
+            if (c.lam[j] >= minl && c.lam[j] <= maxl) { i0 = j; break; }
+        if (i0 >= 0 && (minl <= c.lam[contract_halo()] || maxl >= c.lam[ns - 1 - contract_halo()])) {
+            err = "the smoothing range must lie inside the wavelength grid's interior";
+            return ST_UNSUPPORTED;
+        }
+    }
+    // nebular lines: one profile table per batch, from the first model's sigma (prepare_line_gaussians(ctx,
+    // psets(1)), src/physics/opensps_csp_batch.f90:1733); a model whose own sigma would give other widths is
+    // unsupported, as in the reference (:747-751)
+    const bool neb = c.add_neb_emission == 1 && c.nebemlineinspec == 1 && c.nline > 0;
+    double line_sigma = 0.0;
+    if (neb) {
+        const double s1 = par(0, PF_SIGMA_SMOOTH);
+        const bool f1 = lines_floor_limited(c, s1);
+        line_sigma = f1 ? 0.0 : s1;
+        for (int m = 1; m < n; ++m) {
+            const double sm = par(m, PF_SIGMA_SMOOTH);
+            if (sm == s1) continue;
+            if (!(f1 && lines_floor_limited(c, sm))) {
+                err = "nebular lines with a sigma_smooth of each model's own (above the grid's line width) are unsupported";
+                return ST_UNSUPPORTED;
+            }
+        }
+    }
+    const int nacc = nacc2 ? 2 : 1;
+    BasisOperand *bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
+    if (!bop) return ST_DATA_MISSING;
+
+    // ---- per-pixel table (smoothing range)
+    {
+        std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
+        for (int j = 0; j < ns; ++j) {
+            float *px = pix.data() + (size_t)j * PIX_FLOATS;
+            px[PIX_LTAB] = (float)std::log(c.lam[j] / 5500.0);
+            if (j < c.jtop)
+                for (int k = 0; k < 6; ++k) px[PIX_IGM_A + k] = c.igm_a[(size_t)j * 6 + k];
+            px[PIX_SMOOTH] = (c.lam[j] >= minl && c.lam[j] <= maxl) ? 1.f : 0.f;
+        }
+        cudaError_t e;
+        if ((e = c.d_pix.reserve(pix.size())) != cudaSuccess ||
+            (e = cudaMemcpy(c.d_pix.p, pix.data(), sizeof(float) * pix.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            err = cuda_msg("pixel table", e);
+            return ST_DATA_MISSING;
+        }
+    }
+
+    // ---- scratch
+    const int bn = contract_models_per_tile(nacc);
+    const int n_mtiles = (n + bn - 1) / bn;
+    const int kpad = bop->kpad;
+    cudaError_t e;
+    const size_t nwz = (size_t)n * nt * nz;
+    if ((!io.dev_inputs && (e = c.d_wz.reserve(nwz)) != cudaSuccess) ||
+        (e = c.d_params.reserve((size_t)PAR_DEVICE * n)) != cudaSuccess ||
+        (e = c.d_whi.reserve((size_t)n * kpad)) != cudaSuccess || (e = c.d_wlo.reserve((size_t)n * kpad)) != cudaSuccess ||
+        (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess || (e = c.d_mpar.reserve((size_t)MODEL_PAR_FLOATS * n)) != cudaSuccess ||
+        (e = c.d_zshift.reserve((size_t)4 * n)) != cudaSuccess || (e = c.d_dist.reserve(n)) != cudaSuccess ||
+        (e = c.d_spec.reserve((size_t)n * ns)) != cudaSuccess || (e = c.d_mags.reserve((size_t)n * nb)) != cudaSuccess) {
+        err = cuda_msg("device memory", e);
+        return ST_DATA_MISSING;
+    }
+    cudaStream_t st = c.stream;
+    const double *d_wz = io.wz;
+    const double *d_par = nullptr;
+    std::vector<double> hp;
+    if (io.dev_inputs) {
+        d_par = io.dev_params;   // already PAR_DEVICE x n on the device
+    } else {
+        if ((e = cudaMemcpyAsync(c.d_wz.p, io.wz, sizeof(double) * nwz, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            err = cuda_msg("weights copy", e);
+            return ST_DATA_MISSING;
+        }
+        d_wz = c.d_wz.p;
+        hp.resize((size_t)PAR_DEVICE * n);
+        for (int m = 0; m < n; ++m)
+            for (int k = 0; k < PAR_DEVICE; ++k) hp[(size_t)PAR_DEVICE * m + k] = par(m, k);
+        if ((e = cudaMemcpyAsync(c.d_params.p, hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            err = cuda_msg("parameter copy", e);
+            return ST_DATA_MISSING;
+        }
+        d_par = c.d_params.p;
+    }
+    cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
+
+    // ---- weights
+    WeightsArgs wa;
+    wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.nty_young = bop->nty; wa.ky_pad = bop->ky_pad;
+    wa.wz = d_wz; wa.mass = c.d_mass.p; wa.llin = c.d_llin.p; wa.w_hi = c.d_whi.p; wa.w_lo = c.d_wlo.p;
+    wa.sums = c.d_sums.p; wa.itesc = itesc;
+    if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
+
+    // ---- per-model parameters
+    ModelParamArgs ma;
+    ma.n = n; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
+    ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
+    ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zshift = c.d_zshift.p; ma.dist = c.d_dist.p;
+    model_params_kernel<<<(n + 127) / 128, 128, 0, st>>>(ma);
+    if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
+
+    // ---- contraction + epilogue
+    ContractPlan pl;
+    pl.tm_a_hi = bop->tm_hi;
+    pl.tm_a_lo = bop->tm_lo;
+    pl.num_sms = c.num_sms;
+    if ((e = encode_tmap_2d_bf16(&pl.tm_b_hi, c.d_whi.p, kpad, n, contract_bk(), bn)) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&pl.tm_b_lo, c.d_wlo.p, kpad, n, contract_bk(), bn)) != cudaSuccess) {
+        err = cuda_msg("weights tensor map", e);
+        return ST_DATA_MISSING;
+    }
+    ContractArgs ca;
+    ca.nspec = ns; ca.n_models = n;
+    ca.n_ptiles = (ns + contract_out_rows() - 1) / contract_out_rows();
+    ca.n_mtiles = n_mtiles;
+    ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
+    ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
+    ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
+    ca.status = c.d_status.p;
+    if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
+    int launches = 3;   // weights, model parameters, contraction
+
+    // ---- bands and magnitudes
+    const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
+    if (want_mags) {
+        std::vector<int> do_band(nb, 1);
+        for (int b = 0; b < nb && b < (int)c.mag_mask.size(); ++b) do_band[b] = c.mag_mask[b];
+        if ((e = c.d_do_band.reserve(nb)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c.d_do_band.p, do_band.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            err = cuda_msg("band mask", e);
+            return ST_DATA_MISSING;
+        }
+        BandArgs ba;
+        ba.nspec = ns; ba.nbands = nb; ba.n_models = n; ba.ld_spec = ns; ba.spec = c.d_spec.p; ba.cmat = c.d_cmat.p;
+        ba.jr = c.d_jr.p; ba.wl = c.d_wl.p; ba.zshift = c.d_zshift.p; ba.dlnl = c.dlnl; ba.dist = c.d_dist.p;
+        ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
+        ba.do_band = c.d_do_band.p; ba.fband = nullptr; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
+        if ((e = run_bands(ba, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+        ++launches;
+    }
+    c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
+    if (io.dev_inputs) {
+        c.last_n = n;
+        if (!io.dev_sync) return 0;
+        int kstatus = 0;
+        if ((e = cudaMemcpyAsync(&kstatus, c.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            err = cuda_msg("batch", e);
+            return ST_DATA_MISSING;
+        }
+        if (kstatus != 0) {
+            char buf[96];
+            std::snprintf(buf, sizeof buf, "a device wait gave up (code 0x%x)", kstatus);
+            err = buf;
+            return ST_DATA_MISSING;
+        }
+        return 0;
+    }
+
+    // ---- outputs
+    if (io.spec && !io.dev_inputs) {
+        if ((e = c.d_spec64.reserve((size_t)n * ns)) != cudaSuccess ||
+            (e = run_spec_to_f64(c.d_spec.p, ns, ns, n, c.d_spec64.p, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(io.spec, c.d_spec64.p, sizeof(double) * n * ns, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("spectra copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+    if (want_mags && !io.dev_inputs) {
+        if ((e = cudaMemcpyAsync(io.mags, c.d_mags.p, sizeof(double) * n * nb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("magnitudes copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+    std::vector<double> sums;
+    const bool want_sums = io.mass || io.lbol || io.mass_young || io.mass_old || io.lbol_young || io.lbol_old;
+    if (want_sums && !io.dev_inputs) {
+        sums.resize((size_t)6 * n);
+        if ((e = cudaMemcpyAsync(sums.data(), c.d_sums.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("sums copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+    int kstatus = 0;
+    if ((e = cudaMemcpyAsync(&kstatus, c.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        err = cuda_msg("batch", e);
+        return ST_DATA_MISSING;
+    }
+    if (kstatus != 0) {
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "a device wait gave up (code 0x%x)", kstatus);
+        err = buf;
+        return ST_DATA_MISSING;
+    }
+    c.last_n = n;
+    if (want_sums && !io.dev_inputs) {
+        for (int m = 0; m < n; ++m) {
+            const double *s = sums.data() + (size_t)6 * m;
+            if (io.mass) io.mass[m] = s[0];
+            if (io.lbol) io.lbol[m] = s[1] > SAFE_FLOOR ? std::log10(s[1]) : 0.0;
+            if (io.mass_young) io.mass_young[m] = s[2];
+            if (io.mass_old) io.mass_old[m] = s[3];
+            if (io.lbol_young) io.lbol_young[m] = std::log10(std::max(s[4], SAFE_FLOOR));
+            if (io.lbol_old) io.lbol_old[m] = std::log10(std::max(s[5], SAFE_FLOOR));
+        }
+    }
+    if (io.sfr) for (int m = 0; m < n; ++m) io.sfr[m] = std::nan("");
+    if (io.mdust) for (int m = 0; m < n; ++m) io.mdust[m] = SAFE_FLOOR;
+    return 0;
+}
+
+}  // namespace sps
+
+namespace sps {
+// The reverse pass (compute_csp_batch_grad): not built yet on this path.
+int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
+                   const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
+                   double *weights_z_bar, std::string &err) {
+    (void)mags_bar; (void)spec_bar; (void)mass_bar; (void)lbol_bar; (void)params_bar; (void)params_bar_rows;
+    (void)weights_z_bar;
+    if (!mags_bar && !spec_bar && !mass_bar && !lbol_bar && !params_bar && !weights_z_bar) return run_batch(c, io, err);
+    err = "gradients are not available on this path yet";
+    return ST_UNSUPPORTED;
+}
+}  // namespace sps

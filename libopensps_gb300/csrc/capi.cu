@@ -1,0 +1,480 @@
+// The extern "C" entry points of include/opensps.h and include/opensps_gb300.h: a handle table over contexts, the
+// parameter plumbing of the batch calls (names / values -> one parameter row per model, as OpenSPS's batch_handle,
+// src/bindings/c/opensps_c_api.f90:663-961) and the status / last-error convention (never abort).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+#include "context.h"
+#include "../../include/opensps.h"
+#include "../../include/opensps_gb300.h"
+
+namespace sps {
+void get_error(int *status, std::string *msg);
+void clear_error();
+int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
+                   const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
+                   double *weights_z_bar, std::string &err);
+}  // namespace sps
+
+using namespace sps;
+
+namespace {
+
+std::mutex g_pool_mu;
+std::vector<std::unique_ptr<Context>> g_pool;   // handle h -> g_pool[h - 1]
+
+Context *lookup(int handle) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (handle < 1 || handle > (int)g_pool.size()) return nullptr;
+    return g_pool[handle - 1].get();
+}
+
+void fail(int *status, int code, const std::string &msg) {
+    if (status) *status = code;
+    set_error(code, msg);
+}
+
+// The gradient rows' names (params_bar rows 0..43), as opensps_get_grad_param_name.
+const char *const GRAD_NAMES[OPENSPS_NBGRAD] = {
+    "fagn", "dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_obrun", "frac_nodust", "mwr", "uvb",
+    "duste_qpah", "duste_umin", "duste_gamma", "gas_logz", "gas_logu", "logzsol", "tage", "tau", "const", "fburst",
+    "tburst", "sf_start", "zred", "sigma_smooth", "sf_trunc", "sf_slope", "imf1", "imf2", "imf3", "vdmc", "mdave",
+    "agn_tau", "igm_factor", "gas_logn", "gas_logno", "gas_logco", "afe", "fbhb", "sbss", "agb", "pagb", "redgb",
+    "delt", "dell"};
+
+// names / values -> PF_COUNT x n rows (the context's values, with the named ones per model). 0, or a status.
+int build_params(Context &c, int n, int n_params, const char *const *names, const double *const *values,
+                 std::vector<double> &rows, std::string &err) {
+    rows.resize((size_t)PF_COUNT * n);
+    for (int m = 0; m < n; ++m) std::memcpy(rows.data() + (size_t)PF_COUNT * m, c.pdef, sizeof(double) * PF_COUNT);
+    if (n_params < 0) { err = "n_params < 0"; return ST_BAD_ARG; }
+    if (n_params > 0 && (!names || !values)) { err = "names / values are NULL"; return ST_BAD_ARG; }
+    for (int i = 0; i < n_params; ++i) {
+        const ParamInfo *pi = find_param(names[i]);
+        if (!pi) { err = std::string("compute_csp_batch: unknown parameter ") + (names[i] ? names[i] : "(null)"); return ST_BAD_ARG; }
+        if (pi->id < 0) {
+            err = std::string("compute_csp_batch: ") + pi->name + " cannot vary per model on this path";
+            return ST_UNSUPPORTED;
+        }
+        if (!values[i]) { err = std::string("compute_csp_batch: no values for ") + pi->name; return ST_BAD_ARG; }
+        for (int m = 0; m < n; ++m) rows[(size_t)PF_COUNT * m + pi->id] = values[i][m];
+    }
+    return 0;
+}
+
+// ssp_weights (ntfull x n) at each model's logzsol -> weights over ages and metallicities: the two bracketing
+// metallicities at (1 - dz) and dz (metallicity_interval, src/physics/opensps_csp_batch.f90:2071-2085; linear in the
+// spectra as compute_interpolated_ssp, not clamped).
+void blend_weights(const Context &c, int n, const double *w, const std::vector<double> &rows, std::vector<double> &wz) {
+    const int nt = c.nt, nz = c.nz;
+    wz.assign((size_t)n * nt * nz, 0.0);
+    std::vector<double> lz(nz);
+    for (int z = 0; z < nz; ++z) lz[z] = std::log10(c.zlegend[z] / c.zsol);
+    for (int m = 0; m < n; ++m) {
+        const double x = rows[(size_t)PF_COUNT * m + PF_LOGZSOL];
+        int zlo = 0;
+        // find_interval clamped to 1..nz-1 (1-based)
+        int lower = 0, upper = nz + 1;
+        while (upper - lower > 1) { const int mid = (upper + lower) / 2; if (x >= lz[mid - 1]) lower = mid; else upper = mid; }
+        int idx = lower;
+        if (x == lz[0]) idx = 1; else if (x == lz[nz - 1]) idx = nz - 1;
+        zlo = std::max(1, std::min(idx, nz - 1)) - 1;
+        const double dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
+        double *o = wz.data() + (size_t)m * nt * nz;
+        for (int t = 0; t < nt; ++t) {
+            o[t + (size_t)nt * zlo] = (1.0 - dz) * w[(size_t)nt * m + t];
+            o[t + (size_t)nt * (zlo + 1)] = dz * w[(size_t)nt * m + t];
+        }
+    }
+}
+
+// The common body of the batch entry points.
+void batch_entry(int handle, int n, int n_params, const char *const *names, const double *const *values,
+                 const double *ssp_weights, const double *ssp_weights_z, const double *zred_mags,
+                 const double *mags_bar, const double *spec_bar, const double *mass_bar, const double *lbol_bar,
+                 double *mags, double *spec, double *mass, double *lbol, double *mdust, double *sfr, double *emlines,
+                 double *indx, double *young, double *old, double *mass_young, double *mass_old, double *lbol_young,
+                 double *lbol_old, double *params_bar, int params_bar_rows, double *weights_bar,
+                 double *weights_z_bar, int *status) {
+    if (!status) return;
+    *status = 0;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (n <= 0) return;
+    if (params_bar && params_bar_rows < OPENSPS_NBGRAD)
+        return fail(status, ST_BAD_ARG, "compute_csp_batch_grad: params_bar has " + std::to_string(params_bar_rows) +
+                                            " rows, the library writes " + std::to_string(OPENSPS_NBGRAD) +
+                                            " (opensps_get_nbgrad)");
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    if (!mags && !c->fast_mode) return fail(status, ST_BAD_ARG, "mags is required");
+    if (indx) return fail(status, ST_UNSUPPORTED, "spectral indices are not computed on this path");
+    if (zred_mags) return fail(status, ST_UNSUPPORTED, "zred_mags is not supported on this path");
+    std::string err;
+    std::vector<double> rows;
+    int st = build_params(*c, n, n_params, names, values, rows, err);
+    if (st) return fail(status, st, err);
+    std::vector<double> wz_blend;
+    const double *wz = ssp_weights_z;
+    if (!wz) {
+        if (!ssp_weights)
+            return fail(status, ST_UNSUPPORTED, "SFH parameters without a weight matrix are not supported on this path");
+        blend_weights(*c, n, ssp_weights, rows, wz_blend);
+        wz = wz_blend.data();
+    }
+    if (emlines) std::fill(emlines, emlines + (size_t)c->nline * n, 0.0);
+    BatchIO io;
+    io.n = n; io.params = rows.data(); io.wz = wz;
+    io.mags = mags; io.spec = spec; io.mass = mass; io.lbol = lbol; io.emlines = emlines; io.sfr = sfr;
+    io.mdust = mdust; io.young = young; io.old = old; io.mass_young = mass_young; io.mass_old = mass_old;
+    io.lbol_young = lbol_young; io.lbol_old = lbol_old;
+    const bool grad = mags_bar || spec_bar || mass_bar || lbol_bar || params_bar || weights_bar || weights_z_bar;
+    if (grad) {
+        if (weights_bar && !ssp_weights_z)
+            return fail(status, ST_UNSUPPORTED, "weights_bar with ssp_weights is not supported on this path");
+        st = run_grad_batch(*c, io, mags_bar, spec_bar, mass_bar, lbol_bar, params_bar, params_bar_rows,
+                            weights_z_bar, err);
+        if (weights_bar) std::fill(weights_bar, weights_bar + (size_t)c->nt * n, 0.0);
+    } else {
+        st = run_batch(*c, io, err);
+    }
+    if (st) return fail(status, st, err);
+}
+
+}  // namespace
+
+extern "C" {
+
+void opensps_clear_error(void) { clear_error(); }
+
+void opensps_get_last_error(int *status, char *message, int message_len) {
+    std::string msg;
+    int st = 0;
+    get_error(&st, &msg);
+    if (status) *status = st;
+    if (message && message_len > 0) {
+        const int k = std::min((int)msg.size(), message_len - 1);
+        std::memcpy(message, msg.data(), k);
+        message[k] = '\0';
+    }
+}
+
+void opensps_get_nbgrad(int *nbgrad) { if (nbgrad) *nbgrad = OPENSPS_NBGRAD; }
+
+void opensps_get_grad_param_name(int grad_idx, char *name, int max_len, int *status) {
+    if (grad_idx < 0 || grad_idx >= OPENSPS_NBGRAD) { if (status) *status = ST_BAD_ARG; return; }
+    if (name && max_len > 0) {
+        const int k = std::min((int)std::strlen(GRAD_NAMES[grad_idx]), max_len - 1);
+        std::memcpy(name, GRAD_NAMES[grad_idx], k);
+        name[k] = '\0';
+    }
+    if (status) *status = 0;
+}
+
+void opensps_context_create(int *handle, int *status) {
+    std::unique_ptr<Context> c(new Context());
+    for (int i = 0; i < PF_COUNT; ++i) c->pdef[i] = 0.0;
+    // the defaults of the parameters this path reads
+    const char *names[] = {"dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun",
+                           "zred", "igm_factor", "sigma_smooth", "dust_tesc", "logzsol", "tage", "tau",
+                           "min_wave_smooth", "max_wave_smooth"};
+    for (const char *nm : names) {
+        const ParamInfo *p = find_param(nm);
+        c->pdef[p->id] = p->def;
+    }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (size_t i = 0; i < g_pool.size(); ++i)
+        if (!g_pool[i]) {
+            g_pool[i] = std::move(c);
+            if (handle) *handle = (int)i + 1;
+            if (status) *status = 0;
+            return;
+        }
+    g_pool.push_back(std::move(c));
+    if (handle) *handle = (int)g_pool.size();
+    if (status) *status = 0;
+}
+
+void opensps_context_destroy(int handle, int *status) {
+    std::unique_ptr<Context> victim;
+    {
+        std::lock_guard<std::mutex> lk(g_pool_mu);
+        if (handle < 1 || handle > (int)g_pool.size() || !g_pool[handle - 1]) {
+            if (status) *status = ST_BAD_HANDLE;
+            return;
+        }
+        victim = std::move(g_pool[handle - 1]);
+    }
+    { std::lock_guard<std::mutex> lk(victim->mu); }
+    victim.reset();
+    if (status) *status = 0;
+}
+
+void opensps_context_setup(int zin, const char *isoc_type, const char *spec_type, const char *dust_type, int handle,
+                           int *status) {
+    (void)zin;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::string err;
+    const int st = context_setup(*c, isoc_type, spec_type, dust_type, err);
+    if (st) return fail(status, st, err);
+    if (status) *status = 0;
+}
+
+void opensps_context_set_int(int handle, const char *key, int value, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (!key) return fail(status, 101, "NULL key");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const std::string k(key);
+    if (k == "add_neb_emission") c->add_neb_emission = value;
+    else if (k == "add_igm_absorption") c->add_igm_absorption = value;
+    else if (k == "smooth_velocity") c->smooth_velocity = value;
+    else if (k == "dust_type") c->dust_type = value;
+    else if (k == "compute_vega_mags") c->compute_vega_mags = value;
+    else if (k == "sfh") c->sfh = value;
+    else if (k == "nebemlineinspec") c->nebemlineinspec = value;
+    else if (k == "keep_maggies") c->keep_maggies = value;
+    else if (k == "add_dust_emission" || k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_stellar_remnants" ||
+             k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" || k == "zmet" || k == "imf_type" ||
+             k == "redshift_colors" || k == "cloudy_dust" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
+             k == "vactoair_flag") {
+        // known settings this path keeps at the values it implements; other values are refused at batch time
+        if ((k == "add_dust_emission" || k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_xrb_emission" ||
+             k == "redshift_colors") && value != 0)
+            return fail(status, 104, k + " = 1 is not supported on this path");
+    } else {
+        return fail(status, 101, "unknown integer parameter " + k);
+    }
+    if (status) *status = 0;
+}
+
+void opensps_context_set_float(int handle, const char *key, double value, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (!key) return fail(status, 102, "NULL key");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const std::string k(key);
+    if (k == "H0") c->h0 = value;
+    else if (k == "om0") c->om0 = value;
+    else if (k == "ol0") c->ol0 = value;
+    else {
+        const ParamInfo *p = find_param(key);
+        if (!p) return fail(status, 102, "unknown float parameter " + k);
+        if (p->id >= 0) c->pdef[p->id] = value;
+    }
+    if (status) *status = 0;
+}
+
+void opensps_context_set_str(int handle, const char *key, const char *value, int *status) {
+    (void)value;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (!key) return fail(status, 103, "NULL key");
+    const std::string k(key);
+    if (k == "imf_filename" || k == "sfh_filename") return fail(status, 104, k + " is not supported on this path");
+    return fail(status, 103, "unknown string parameter " + k);
+}
+
+void opensps_context_set_fast_mode(int handle, int fast_mode, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    c->fast_mode = fast_mode;
+    if (status) *status = 0;
+}
+
+#define GETTER(fn, type, expr)                                                         \
+    void fn(int handle, type *out, int *status) {                                      \
+        Context *c = lookup(handle);                                                   \
+        if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");          \
+        if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");     \
+        if (out) *out = (expr);                                                        \
+        if (status) *status = 0;                                                       \
+    }
+GETTER(opensps_context_get_nspec, int, c->nspec)
+GETTER(opensps_context_get_ntfull, int, c->nt)
+GETTER(opensps_context_get_nbands, int, c->nbands)
+GETTER(opensps_context_get_nz, int, c->nz)
+GETTER(opensps_context_get_nemline, int, c->nline)
+GETTER(opensps_context_get_zsol, double, c->zsol)
+#undef GETTER
+
+void opensps_context_get_dims(int handle, int *n_spec, int *n_time, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    if (n_spec) *n_spec = c->nspec;
+    if (n_time) *n_time = c->nt;
+    if (status) *status = 0;
+}
+
+#define ARRAY_GETTER(fn, vec)                                                          \
+    void fn(int handle, double *out, int *status) {                                    \
+        Context *c = lookup(handle);                                                   \
+        if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");          \
+        if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");     \
+        if (out) std::copy(c->vec.begin(), c->vec.end(), out);                         \
+        if (status) *status = 0;                                                       \
+    }
+ARRAY_GETTER(opensps_context_get_lambda, lam)
+ARRAY_GETTER(opensps_context_get_ages, log_age)
+ARRAY_GETTER(opensps_context_get_zlegend, zlegend)
+ARRAY_GETTER(opensps_context_get_emlambda, line_lambda)
+#undef ARRAY_GETTER
+
+void opensps_context_set_filters_library(int handle, const char *name, int resample, int grid_policy,
+                                         int vega_ref_band, int *status) {
+    (void)resample; (void)grid_policy; (void)vega_ref_band;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    std::string err;
+    const int st = context_load_filters(*c, name ? name : "", err);
+    if (st) return fail(status, st, err);
+    if (status) *status = 0;
+}
+
+void opensps_context_set_mag_compute(int handle, int n_bands, const int *mask, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    if (!mask) { c->mag_mask.clear(); if (status) *status = 0; return; }
+    if (n_bands < 1 || n_bands > c->nbands) return fail(status, ST_BAD_ARG, "n_bands out of range");
+    c->mag_mask.assign(c->nbands, 0);
+    for (int b = 0; b < n_bands; ++b) c->mag_mask[b] = mask[b] != 0;
+    if (status) *status = 0;
+}
+
+void opensps_context_compute_csp_batch(int handle, int n, int n_params, const char *const *names,
+                                       const double *const *values, const double *ssp_weights, double *mags,
+                                       double *spec, double *mass, double *lbol, double *mdust, double *sfr,
+                                       double *emlines, double *indx, int *status) {
+    batch_entry(handle, n, n_params, names, values, ssp_weights, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                mags, spec, mass, lbol, mdust, sfr, emlines, indx, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                nullptr, OPENSPS_NBGRAD, nullptr, nullptr, status);
+}
+
+void opensps_context_compute_csp_batch_parts(int handle, int n, int n_params, const char *const *names,
+                                             const double *const *values, const double *ssp_weights, double *mags,
+                                             double *spec, double *mass, double *lbol, double *mdust, double *sfr,
+                                             double *emlines, double *indx, double *young, double *old,
+                                             double *mass_young, double *mass_old, double *lbol_young,
+                                             double *lbol_old, int *status) {
+    if (!young || !old) return fail(status, ST_BAD_ARG, "compute_csp_batch_parts: young and old are required");
+    batch_entry(handle, n, n_params, names, values, ssp_weights, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                mags, spec, mass, lbol, mdust, sfr, emlines, indx, young, old, mass_young, mass_old, lbol_young,
+                lbol_old, nullptr, OPENSPS_NBGRAD, nullptr, nullptr, status);
+}
+
+void opensps_context_batch_spec_device(int handle, void **ptr, int *nspec, int *n, int *bytes, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (ptr) *ptr = c->last_n > 0 ? (void *)c->d_spec.p : nullptr;
+    if (nspec) *nspec = c->nspec;
+    if (n) *n = c->last_n;
+    if (bytes) *bytes = 4;
+    if (status) *status = 0;
+}
+
+void opensps_context_batch_spec_host(int handle, void **ptr, int *nspec, int *n, int *bytes, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (ptr) *ptr = nullptr;
+    if (nspec) *nspec = c->nspec;
+    if (n) *n = c->last_n;
+    if (bytes) *bytes = 4;
+    if (c->last_n <= 0) { if (status) *status = 0; return; }
+    const size_t need = sizeof(float) * (size_t)c->nspec * c->last_n;
+    if (c->pinned_bytes < need) {
+        if (c->pinned_spec) cudaFreeHost(c->pinned_spec);
+        c->pinned_spec = nullptr;
+        c->pinned_bytes = 0;
+        cudaError_t e = cudaMallocHost(&c->pinned_spec, need);
+        if (e != cudaSuccess) return fail(status, ST_DATA_MISSING, std::string("pinned buffer: ") + cudaGetErrorString(e));
+        c->pinned_bytes = need;
+    }
+    cudaError_t e = cudaMemcpyAsync(c->pinned_spec, c->d_spec.p, need, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail(status, ST_DATA_MISSING, std::string("spectra copy: ") + cudaGetErrorString(e));
+    if (ptr) *ptr = c->pinned_spec;
+    if (status) *status = 0;
+}
+
+void opensps_context_compute_csp_batch_grad(int handle, int n, int n_params, const char *const *names,
+                                            const double *const *values, const double *ssp_weights,
+                                            const double *ssp_weights_z, const double *zred_mags,
+                                            const double *mags_bar, const double *spec_bar, const double *mass_bar,
+                                            const double *lbol_bar, double *mags, double *spec, double *mass,
+                                            double *lbol, double *mdust, double *sfr, double *emlines, double *indx,
+                                            double *params_bar, double *weights_bar, double *weights_z_bar,
+                                            int *status) {
+    batch_entry(handle, n, n_params, names, values, ssp_weights, ssp_weights_z, zred_mags, mags_bar, spec_bar,
+                mass_bar, lbol_bar, mags, spec, mass, lbol, mdust, sfr, emlines, indx, nullptr, nullptr, nullptr,
+                nullptr, nullptr, nullptr, params_bar, OPENSPS_NBGRAD, weights_bar, weights_z_bar, status);
+}
+
+void opensps_context_compute_csp_batch_grad_rows(int handle, int n, int n_params, const char *const *names,
+                                                 const double *const *values, const double *ssp_weights,
+                                                 const double *ssp_weights_z, const double *zred_mags,
+                                                 const double *mags_bar, const double *spec_bar,
+                                                 const double *mass_bar, const double *lbol_bar, double *mags,
+                                                 double *spec, double *mass, double *lbol, double *mdust, double *sfr,
+                                                 double *emlines, double *indx, double *params_bar,
+                                                 int params_bar_rows, double *weights_bar, double *weights_z_bar,
+                                                 int *status) {
+    batch_entry(handle, n, n_params, names, values, ssp_weights, ssp_weights_z, zred_mags, mags_bar, spec_bar,
+                mass_bar, lbol_bar, mags, spec, mass, lbol, mdust, sfr, emlines, indx, nullptr, nullptr, nullptr,
+                nullptr, nullptr, nullptr, params_bar, params_bar_rows, weights_bar, weights_z_bar, status);
+}
+
+// ---------------------------------------------------------------------------------------------- extensions
+void opensps_gb300_batch_device(int handle, int n, const double *d_params, const double *d_wz, double *d_mags,
+                                int sync, int *status) {
+    if (!status) return;
+    *status = 0;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    if (n <= 0) return;
+    // the batch-wide settings come from the context; the per-model table is on the device (a copy is read here
+    // for the batch's checks: 88 bytes per model)
+    std::vector<double> rows((size_t)PF_COUNT * n), dp((size_t)PAR_DEVICE * n);
+    cudaError_t e = cudaMemcpy(dp.data(), d_params, sizeof(double) * dp.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(status, ST_BAD_ARG, std::string("d_params: ") + cudaGetErrorString(e));
+    for (int m = 0; m < n; ++m) {
+        std::memcpy(rows.data() + (size_t)PF_COUNT * m, c->pdef, sizeof(double) * PF_COUNT);
+        std::memcpy(rows.data() + (size_t)PF_COUNT * m, dp.data() + (size_t)PAR_DEVICE * m, sizeof(double) * PAR_DEVICE);
+    }
+    BatchIO io;
+    io.n = n; io.params = rows.data(); io.wz = d_wz; io.dev_inputs = true; io.dev_params = d_params;
+    io.mags = d_mags; io.dev_sync = sync != 0;
+    std::string err;
+    const int st = run_batch(*c, io, err);
+    if (st) return fail(status, st, err);
+}
+
+void opensps_gb300_context_stream(int handle, void **stream, int *device, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (stream) *stream = (void *)c->stream;
+    if (device) *device = c->device;
+    if (status) *status = 0;
+}
+
+void opensps_gb300_last_launches(int handle, int *launches, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (launches) *launches = c->last_launches;
+    if (status) *status = 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,374 @@
+// Context setup: the libraries of the data root, their device tables, the contraction's basis operand, and the
+// parameter table of the C API.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include "context.h"
+
+namespace sps {
+
+// ---------------------------------------------------------------------------------------------- parameters
+// The float parameters of the reference's parameter registry (src/core/opensps_batch_registry.f90:103-115) with
+// their defaults (src/core/opensps_types.f90:32-45); id >= 0 for those this path takes per model.
+static const ParamInfo PARAMS[] = {
+    {"dust1", PF_DUST1, 0.0}, {"dust2", PF_DUST2, 0.0}, {"dust3", PF_DUST3, 0.0},
+    {"dust_index", PF_DUST_INDEX, -0.7}, {"dust1_index", PF_DUST1_INDEX, -1.0},
+    {"frac_nodust", PF_FRAC_NODUST, 0.0}, {"frac_obrun", PF_FRAC_OBRUN, 0.0}, {"zred", PF_ZRED, 0.0},
+    {"igm_factor", PF_IGM_FACTOR, 1.0}, {"sigma_smooth", PF_SIGMA_SMOOTH, 0.0}, {"dust_tesc", PF_DUST_TESC, 7.0},
+    {"logzsol", PF_LOGZSOL, 0.0}, {"tage", PF_TAGE, 0.0}, {"tau", PF_TAU, 1.0},
+    {"min_wave_smooth", PF_MIN_WAVE_SMOOTH, 1.0e3}, {"max_wave_smooth", PF_MAX_WAVE_SMOOTH, 1.0e4},
+    // known to the reference, not varied per model by this path
+    {"const", -1, 0.0}, {"fburst", -1, 0.0}, {"tburst", -1, 11.0}, {"sf_start", -1, 0.0}, {"sf_trunc", -1, 0.0},
+    {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
+    {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"imf1", -1, 1.3},
+    {"imf2", -1, 2.3}, {"imf3", -1, 2.3}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
+    {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
+    {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
+    {"duste_gamma", -1, 0.01}, {"duste_umin", -1, 1.0}, {"duste_qpah", -1, 3.5}, {"gas_logu", -1, -2.0},
+    {"gas_logz", -1, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
+    {"fagn", -1, 0.0}, {"agn_tau", -1, 10.0}, {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
+    {"wgp1", -1, 1.0}, {"wgp2", -1, 1.0}, {"wgp3", -1, 1.0}, {"compute_mags", -1, 1.0},
+    {"compute_indices", -1, 1.0},
+};
+
+const ParamInfo *find_param(const char *name) {
+    if (!name) return nullptr;
+    for (const auto &p : PARAMS)
+        if (std::strcmp(p.name, name) == 0) return &p;
+    return nullptr;
+}
+
+// ---------------------------------------------------------------------------------------------- errors
+static std::mutex g_err_mu;
+static int g_err_status = 0;
+static std::string g_err_msg;
+
+void set_error(int status, const std::string &msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err_status = status;
+    g_err_msg = msg;
+}
+void get_error(int *status, std::string *msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    *status = g_err_status;
+    *msg = g_err_msg;
+}
+void clear_error() {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err_status = 0;
+    g_err_msg.clear();
+}
+
+// ---------------------------------------------------------------------------------------------- bf16
+uint16_t f32_to_bf16_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40);   // NaN
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+float bf16_bits_to_f32(uint16_t b) {
+    uint32_t u = (uint32_t)b << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// ---------------------------------------------------------------------------------------------- TMA maps
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled get_encode_fn() {
+    static PFN_encodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_encodeTiled>(p);
+    });
+    return fn;
+}
+
+// A 2-D bf16 tensor map over a row-major [outer][inner] array, box box_outer x box_inner with the 128-byte swizzle;
+// elements outside the array read as zero.
+cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                                uint32_t box_outer) {
+    PFN_encodeTiled fn = get_encode_fn();
+    if (!fn) return cudaErrorNotSupported;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {inner * 2};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// ---------------------------------------------------------------------------------------------- data root
+std::string data_root() {
+    const char *e = std::getenv("OPENSPS_DATA_HOME");
+    if (e && *e) return std::string(e);
+    return std::string();
+}
+
+static bool read_f64(const std::string &path, std::vector<double> &out, size_t count) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    out.resize(count);
+    f.read(reinterpret_cast<char *>(out.data()), (std::streamsize)(count * sizeof(double)));
+    return (size_t)f.gcount() == count * sizeof(double);
+}
+
+// A minimal reader of the manifest's integer fields ("key": value).
+static bool manifest_int(const std::string &text, const char *key, long long &v) {
+    std::string k = std::string("\"") + key + "\"";
+    size_t p = text.find(k);
+    if (p == std::string::npos) return false;
+    p = text.find(':', p);
+    if (p == std::string::npos) return false;
+    v = std::strtoll(text.c_str() + p + 1, nullptr, 10);
+    return true;
+}
+static bool manifest_double(const std::string &text, const char *key, double &v) {
+    std::string k = std::string("\"") + key + "\"";
+    size_t p = text.find(k);
+    if (p == std::string::npos) return false;
+    p = text.find(':', p);
+    if (p == std::string::npos) return false;
+    v = std::strtod(text.c_str() + p + 1, nullptr);
+    return true;
+}
+
+Context::~Context() {
+    for (auto &kv : basis_cache) {
+        kv.second->hi.release();
+        kv.second->lo.release();
+        delete kv.second;
+    }
+    d_pix.release(); d_cmat.release(); d_wl.release(); d_igm_a.release(); d_jr.release(); d_do_band.release();
+    d_lam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
+    d_wz.release(); d_params.release(); d_sums.release(); d_zshift.release(); d_dist.release(); d_fband.release();
+    d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
+    d_status.release();
+    if (pinned_spec) cudaFreeHost(pinned_spec);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+// Madau (1995) wavelength factors of the IGM optical depth (src/physics/opensps_cosmology.f90:466-494).
+static void igm_pixel_terms(double w, double *a) {
+    static const double LYW[17] = {1215.67, 1025.72, 972.537, 949.743, 937.803, 930.748, 926.226, 923.150, 920.963,
+                                   919.352, 918.129, 917.181, 916.429, 915.824, 915.329, 914.919, 914.576};
+    static const double LYC[17] = {0.0036, 0.0017, 0.0011846, 0.0009410, 0.0007960, 0.0006967, 0.0006236, 0.0005665,
+                                   0.0005200, 0.0004817, 0.0004487, 0.0004200, 0.0003947, 0.000372, 0.000352,
+                                   0.0003334, 0.00031644};
+    for (int k = 0; k < 6; ++k) a[k] = 0.0;
+    if (w < LYW[0]) {
+        double ser = 0.0;
+        for (int i = 0; i < 17; ++i)
+            if (w < LYW[i]) ser += LYC[i] * std::pow(LYW[i], -3.46);
+        a[0] = ser * std::pow(w, 3.46);
+        a[1] = 0.0017 * std::pow(w / LYW[0], 1.68);
+    }
+    if (w < 911.75) {
+        const double s = w / 911.75;
+        a[2] = 0.25 * std::pow(s, 3.0) * (1.0 - std::pow(s, 0.46));
+        a[3] = 9.4 * std::pow(s, 1.5) * (1.0 - std::pow(s, 0.18));
+        a[4] = -0.7 * std::pow(s, 3.0) * (std::pow(s, -1.32) - 1.0);
+        a[5] = -0.023 * (1.0 - std::pow(s, 1.68));
+    }
+}
+
+// The cosmology table of update_cosmology_table (src/physics/opensps_cosmology.f90:244-300): 500 scale factors,
+// luminosity distance [pc] by a 10000-point trapezoid.
+static void cosmology_table(double h0, double om0, double ol0, std::vector<double> &zt, std::vector<double> &dl) {
+    zt.resize(500);
+    dl.resize(500);
+    const double dh = ((C_LIGHT * 1.0e-13) / h0) * 1.0e6;
+    for (int i = 1; i <= 500; ++i) {
+        const double a = (double)(i - 1) / 499.0 * (1.0 - 1.0 / 1001.0) + 1.0 / 1001.0;
+        const double z = 1.0 / a - 1.0;
+        zt[i - 1] = z;
+        double d = 0.0;
+        if (z > 0.0) {
+            const int N = 10000;
+            const double dz = z / (double)(N - 1);
+            double prev = 1.0 / std::sqrt(om0 + ol0), sum = 0.0;
+            for (int k = 2; k <= N; ++k) {
+                const double zc = (double)(k - 1) * dz;
+                const double now = 1.0 / std::sqrt(om0 * std::pow(1.0 + zc, 3) + ol0);
+                sum += 0.5 * dz * (prev + now);
+                prev = now;
+            }
+            d = (1.0 + z) * dh * sum;
+        }
+        dl[i - 1] = d;
+    }
+}
+
+template <class T>
+static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
+    cudaError_t e = b.reserve(n);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+}
+
+int context_load_filters(Context &c, const std::string &name, std::string &err) {
+    int nb = 0;
+    if (name == "gauss20") nb = 20;
+    else if (name == "gauss40") nb = 40;
+    else { err = "unknown filter library " + name; return 324; }
+    const std::string dir = data_root() + "/synthetic/";
+    std::vector<double> bands, centers;
+    if (!read_f64(dir + "filters_" + std::to_string(nb) + ".f64", bands, (size_t)nb * c.nspec) ||
+        !read_f64(dir + "filters_" + std::to_string(nb) + "_center.f64", centers, nb)) {
+        err = "filter library " + name + " missing under " + dir;
+        return 324;
+    }
+    c.bands.swap(bands);
+    c.band_center.swap(centers);
+    c.nbands = nb;
+    c.filter_set = name;
+    c.mag_mask.clear();
+    // The band matrix of the split-K product (prepare_batch_grid src/spectra/opensps_batch_photometry.f90:375-392):
+    // C(j, b) = band(j, b) (wtl(j - 1) + wtl(j)), wtl(j) = |lambda(j + 1) - lambda(j)| / 2, formed in FP64.
+    const int ns = c.nspec;
+    std::vector<double> wtl(ns, 0.0);
+    for (int j = 0; j + 1 < ns; ++j) wtl[j] = 0.5 * std::fabs(c.lam[j + 1] - c.lam[j]);
+    std::vector<float> cm((size_t)nb * ns, 0.f);
+    std::vector<int> jr(2 * nb);
+    for (int b = 0; b < nb; ++b) {
+        const double *bd = c.bands.data() + (size_t)b * ns;
+        int ilo = ns, ihi = -1;
+        for (int j = 0; j < ns; ++j)
+            if (bd[j] != 0.0) { ilo = std::min(ilo, j); ihi = std::max(ihi, j); }
+        // trapezoid intervals touching the support: j = ilo - 1 .. ihi (0-based), last interval ns - 2
+        int jlo = std::max(0, ilo - 1), jhi = std::min(ns - 2, ihi);
+        if (ilo > ihi) { jlo = 0; jhi = -1; }
+        for (int j = 0; j < ns; ++j) {
+            double cw = 0.0;
+            if (j >= jlo && j <= jhi) cw += wtl[j];
+            if (j - 1 >= jlo && j - 1 <= jhi) cw += wtl[j - 1];
+            cm[(size_t)b * ns + j] = (float)(bd[j] * cw);
+        }
+        // pixels whose weight can be nonzero: jlo .. jhi + 1
+        jr[2 * b] = jlo;
+        jr[2 * b + 1] = (jhi >= jlo) ? jhi + 1 : jlo - 1;
+    }
+    cudaError_t e;
+    if ((e = upload(c.d_cmat, cm.data(), cm.size())) != cudaSuccess ||
+        (e = upload(c.d_jr, jr.data(), jr.size())) != cudaSuccess) {
+        err = std::string("device upload failed: ") + cudaGetErrorString(e);
+        return ST_BAD_ARG;
+    }
+    return 0;
+}
+
+int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err) {
+    (void)dust;
+    const std::string iso = isoc ? isoc : "", sp = spec ? spec : "";
+    if (!(iso.empty() || iso == "synthetic") || !(sp.empty() || sp == "synthetic")) {
+        err = "only the synthetic libraries of the data root are available (isoc_type / spec_type \"synthetic\")";
+        return ST_DATA_MISSING;
+    }
+    const std::string root = data_root();
+    if (root.empty()) {
+        err = "OPENSPS_DATA_HOME is not set";
+        return ST_DATA_MISSING;
+    }
+    const std::string dir = root + "/synthetic/";
+    std::ifstream mf(dir + "manifest.json");
+    if (!mf) {
+        err = "no synthetic library under " + dir;
+        return ST_DATA_MISSING;
+    }
+    std::stringstream ss;
+    ss << mf.rdbuf();
+    const std::string man = ss.str();
+    long long ns = 0, nt = 0, nz = 0, nl = 0;
+    if (!manifest_int(man, "nspec", ns) || !manifest_int(man, "ntfull", nt) || !manifest_int(man, "nz", nz) ||
+        !manifest_int(man, "nline", nl)) {
+        err = "bad manifest " + dir + "manifest.json";
+        return ST_DATA_MISSING;
+    }
+    manifest_double(man, "zsol", c.zsol);
+    c.nspec = (int)ns; c.nt = (int)nt; c.nz = (int)nz; c.nline = (int)nl;
+    if (!read_f64(dir + "lambda.f64", c.lam, ns) || !read_f64(dir + "log_age.f64", c.log_age, nt) ||
+        !read_f64(dir + "zlegend.f64", c.zlegend, nz) || !read_f64(dir + "ssp_spec.f64", c.ssp, ns * nt * nz) ||
+        !read_f64(dir + "ssp_mass.f64", c.mass, nt * nz) || !read_f64(dir + "ssp_lbol.f64", c.lbol, nt * nz) ||
+        !read_f64(dir + "line_lambda.f64", c.line_lambda, nl) ||
+        !read_f64(dir + "line_lum.f64", c.line_lum, nl * nt * nz)) {
+        err = "missing or short array under " + dir;
+        return ST_DATA_MISSING;
+    }
+    c.llin.resize(c.lbol.size());
+    for (size_t i = 0; i < c.lbol.size(); ++i) c.llin[i] = std::pow(10.0, c.lbol[i]);
+    // the observed-frame resampling and the smoothing taps take the grid as log-uniform: check it
+    c.dlnl = (std::log(c.lam[ns - 1]) - std::log(c.lam[0])) / (double)(ns - 1);
+    for (int j = 0; j < ns; ++j) {
+        const double dev = std::log(c.lam[j]) - std::log(c.lam[0]) - j * c.dlnl;
+        if (std::fabs(dev) > 1e-9 * c.dlnl) {
+            err = "the wavelength grid is not log-uniform";
+            return ST_UNSUPPORTED;
+        }
+    }
+
+    cudaError_t e = cudaGetDevice(&c.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device);
+    int major = 0, minor = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, c.device);
+    if (e != cudaSuccess) {
+        err = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        return ST_DATA_MISSING;
+    }
+    if (major != 10 || minor != 3) {
+        err = "this library is built for sm_103a (GB300); device is sm_" + std::to_string(major) + std::to_string(minor);
+        return ST_UNSUPPORTED;
+    }
+    if (!c.stream && (e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        err = std::string("stream: ") + cudaGetErrorString(e);
+        return ST_DATA_MISSING;
+    }
+
+    // per-pixel table
+    c.jtop = 0;
+    for (int j = 0; j < ns; ++j)
+        if (c.lam[j] < 1215.67) c.jtop = j + 1;
+    std::vector<float> wl(ns), igm_a((size_t)std::max(c.jtop, 1) * 6, 0.f);
+    for (int j = 0; j < ns; ++j) wl[j] = c.lam[j] > 2.2250738585072014e-308 ? (float)(1.0 / c.lam[j]) : 0.f;
+    for (int j = 0; j < c.jtop; ++j) {
+        double a[6];
+        igm_pixel_terms(c.lam[j], a);
+        for (int k = 0; k < 6; ++k) igm_a[(size_t)j * 6 + k] = (float)a[k];
+    }
+    c.igm_a = igm_a;
+    cosmology_table(c.h0, c.om0, c.ol0, c.zt, c.dl);
+    if ((e = upload(c.d_wl, wl.data(), wl.size())) != cudaSuccess ||
+        (e = upload(c.d_igm_a, igm_a.data(), igm_a.size())) != cudaSuccess ||
+        (e = upload(c.d_lam, c.lam.data(), c.lam.size())) != cudaSuccess ||
+        (e = upload(c.d_mass, c.mass.data(), c.mass.size())) != cudaSuccess ||
+        (e = upload(c.d_llin, c.llin.data(), c.llin.size())) != cudaSuccess ||
+        (e = upload(c.d_zt, c.zt.data(), c.zt.size())) != cudaSuccess ||
+        (e = upload(c.d_dl, c.dl.data(), c.dl.size())) != cudaSuccess ||
+        (e = c.d_status.reserve(4)) != cudaSuccess) {
+        err = std::string("device upload failed: ") + cudaGetErrorString(e);
+        return ST_DATA_MISSING;
+    }
+    c.d_pix.release();   // rebuilt per batch (smoothing range)
+    int st = context_load_filters(c, c.filter_set, err);
+    if (st != 0) return st;
+    for (auto &kv : c.basis_cache) { kv.second->hi.release(); kv.second->lo.release(); delete kv.second; }
+    c.basis_cache.clear();
+    c.is_setup = true;
+    return 0;
+}
+
+}  // namespace sps

@@ -1,0 +1,135 @@
+// Host-side state of a context: the libraries read at setup, their device copies, the per-model parameter table
+// and the scratch of the batch calls.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "csp_kernels.h"
+
+namespace sps {
+
+constexpr double SAFE_FLOOR = 2.2250738585072014e-308;   // tiny(1.0_wp)
+constexpr double C_LIGHT = 2.99792458e18;                 // A / s
+
+// The float parameters of a model that this path reads, in the order of the per-model table handed to the device
+// (the first PAR_DEVICE of them), with the defaults of OpenSPS's PARAMS_CORE (src/core/opensps_types.f90:32-45).
+enum ParamId {
+    PF_DUST1 = 0, PF_DUST2, PF_DUST3, PF_DUST_INDEX, PF_DUST1_INDEX, PF_FRAC_NODUST, PF_FRAC_OBRUN, PF_ZRED,
+    PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC,
+    PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
+    PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH,
+    PF_COUNT
+};
+
+struct ParamInfo {
+    const char *name;
+    int id;           // ParamId, or -1: a parameter of the reference that this path does not vary per model
+    double def;
+};
+const ParamInfo *find_param(const char *name);
+extern const char *const REFERENCE_FLOAT_PARAMS[];
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr; n = 0;
+        cudaError_t e = cudaMalloc(&p, sizeof(T) * (count > 0 ? count : 1));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+// The contraction's basis operand for one K order (bf16 hi and lo, pixels x kpad).
+struct BasisOperand {
+    int nacc = 0, itesc = 0, kpad = 0, ky_pad = 0, nty = 0;
+    DevBuf<__nv_bfloat16> hi, lo;
+    CUtensorMap tm_hi, tm_lo;
+};
+
+struct Context {
+    std::mutex mu;
+    bool is_setup = false;
+    // settings (set_int / set_float)
+    int add_neb_emission = 0, add_igm_absorption = 0, smooth_velocity = 1, dust_type = 0, compute_vega_mags = 0;
+    int sfh = 0, nebemlineinspec = 1, fast_mode = 0;
+    double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
+    double pdef[PF_COUNT];
+    std::string filter_set = "gauss40";
+    std::vector<int> mag_mask;   // empty: all bands
+
+    // libraries (host, FP64)
+    int nspec = 0, nt = 0, nz = 0, nline = 0, nbands = 0;
+    double zsol = 0.0142, dlnl = 0.0;
+    std::vector<double> lam, log_age, zlegend, ssp, mass, lbol, line_lambda, line_lum, bands, band_center;
+    std::vector<double> llin;    // 10^lbol
+    std::vector<double> zt, dl;  // cosmology table (500)
+    std::vector<float> igm_a;    // jtop x 6 Madau wavelength factors
+    int jtop = 0;
+
+    // device copies
+    int device = 0, num_sms = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf<float> d_pix, d_cmat, d_wl, d_igm_a;
+    DevBuf<int> d_jr, d_do_band;
+    DevBuf<double> d_lam, d_mass, d_llin, d_zt, d_dl;
+    std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
+    double basis_sigma = -1.0;
+
+    // batch scratch
+    DevBuf<double> d_wz, d_params, d_sums, d_zshift, d_dist, d_fband, d_mags, d_spec64;
+    DevBuf<__nv_bfloat16> d_whi, d_wlo;
+    DevBuf<float> d_mpar, d_spec;
+    DevBuf<int> d_status;
+    int last_n = 0;              // models of the last batch (device spectra valid for these)
+    int last_launches = 0;       // kernels launched by the last batch
+    void *pinned_spec = nullptr; size_t pinned_bytes = 0;
+    std::vector<double> last_maggies;
+    int keep_maggies = 0;
+
+    ~Context();
+};
+
+// status codes of opensps.h
+enum { ST_OK = 0, ST_BAD_HANDLE = 1, ST_UNSUPPORTED = 2, ST_BAD_ARG = 3, ST_DATA_MISSING = 4,
+       ST_NOT_SETUP = 301, ST_NO_OPERATOR = 303 };
+
+void set_error(int status, const std::string &msg);
+int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err);
+int context_load_filters(Context &c, const std::string &name, std::string &err);
+std::string data_root();
+
+// Host-side bf16 conversion, round to nearest even (the device's __float2bfloat16_rn).
+uint16_t f32_to_bf16_bits(float f);
+float bf16_bits_to_f32(uint16_t b);
+
+// The batch driver (batch.cu). Inputs are host pointers (the C API) unless dev_inputs, in which case wz and params
+// are device pointers and the spectra stay on the device.
+struct BatchIO {
+    int n = 0;
+    // per-model parameters: PF_COUNT x n (host), built from names / values and the context's defaults
+    const double *params = nullptr;
+    const double *wz = nullptr;      // nt x nz x n
+    bool dev_inputs = false;         // wz, dev_params and mags are device pointers; outputs stay on the device
+    const double *dev_params = nullptr;   // PAR_DEVICE x n on the device (dev_inputs)
+    bool dev_sync = true;            // dev_inputs: wait for the batch before returning
+    // outputs (host, may be null)
+    double *mags = nullptr, *spec = nullptr, *mass = nullptr, *lbol = nullptr, *emlines = nullptr;
+    double *young = nullptr, *old = nullptr, *mass_young = nullptr, *mass_old = nullptr, *lbol_young = nullptr,
+           *lbol_old = nullptr, *sfr = nullptr, *mdust = nullptr;
+};
+int run_batch(Context &c, const BatchIO &io, std::string &err);
+
+cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                                uint32_t box_outer);
+
+}  // namespace sps

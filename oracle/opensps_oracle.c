@@ -1,0 +1,460 @@
+/*
+ * FP64 CPU oracle of the batched CSP hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the checker for the GPU path: only the tests, the smoke
+ * check and the CPU-baseline leg of the benchmark load it. The product (libopensps_gb300) never
+ * links, loads or calls it, and has no CPU fallback.
+ *
+ * It restates, in plain C with FP64 arithmetic (the reference's FP64 build, KP = WP), the algorithm
+ * of OpenSPS's compute_csp_batch for the path it covers. Every function names the reference
+ * routine (file:line, paths inside the OpenSPS source tree) that it follows. OpenMP parallelises
+ * over models (each model is independent, as in the reference).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+
+#define SAFE_FLOOR DBL_MIN                 /* src/core/opensps_constants.f90:192 tiny(1.0_wp) */
+#define C_LIGHT 2.99792458e18              /* src/core/opensps_constants.f90:41 [A/s] */
+#define V_BAND 5500.0                      /* src/physics/opensps_dust.f90:47 */
+#define AB_ZEROPOINT 48.60                 /* src/spectra/opensps_batch_photometry.f90:40 */
+#define LINE_PROFILE_CUT 1.0e-14           /* src/physics/opensps_gas.f90:354 */
+#define N_SIGMA_RANGE 4.0                  /* src/spectra/opensps_smoothing.f90:28 */
+
+/* Madau (1995) IGM constants as tabulated in src/physics/opensps_cosmology.f90:65-95 (published values). */
+#define N_LYMAN 17
+static const double LY_WAVE[N_LYMAN] = {1215.67, 1025.72, 972.537, 949.743, 937.803, 930.748, 926.226, 923.150,
+                                        920.963, 919.352, 918.129, 917.181, 916.429, 915.824, 915.329, 914.919,
+                                        914.576};
+static const double LY_COEFF[N_LYMAN] = {0.0036, 0.0017, 0.0011846, 0.0009410, 0.0007960, 0.0006967, 0.0006236,
+                                         0.0005665, 0.0005200, 0.0004817, 0.0004487, 0.0004200, 0.0003947,
+                                         0.000372, 0.000352, 0.0003334, 0.00031644};
+#define LYMAN_LIMIT 911.75
+#define A_METAL 0.0017
+#define MADAU_C1 0.25
+#define MADAU_C2 9.4
+#define MADAU_C3 0.7
+#define MADAU_C4 0.023
+#define MADAU_P1 0.46
+#define MADAU_P2 0.18
+#define MADAU_P3 1.32
+#define MADAU_P4 1.68
+
+/* log10(L_sun / (4 pi (10 pc)^2)), src/core/opensps_constants.f90:87 */
+static double abs_mag_zeropoint_log(void) {
+    const double pi = acos(-1.0);
+    const double pc = (648000.0 / pi) * 1.495978707e13;
+    return log10(3.828e33 / (4.0 * pi * (10.0 * pc) * (10.0 * pc)));
+}
+
+/* find_interval (src/math/opensps_interpolation.f90:152-197): 1-based i with a(i) <= v < a(i+1)
+ * by bisection over 0..n+1, ascending or descending; the legacy end cases v == a(1) -> 1 and
+ * v == a(n) -> n-1. Returned 1-based like the reference (0 = below an ascending table). */
+int oracle_find_interval(const double *a, int n, double v) {
+    if (n < 2) return 1;
+    int asc = a[n - 1] >= a[0];
+    int lower = 0, upper = n + 1;
+    while (upper - lower > 1) {
+        int mid = (upper + lower) / 2;
+        int ge = v >= a[mid - 1];
+        if (asc == ge) lower = mid; else upper = mid;
+    }
+    if (v == a[0]) return 1;
+    if (v == a[n - 1]) return n - 1;
+    return lower;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Nebular lines folded into the young SSPs.                                                  */
+/* ------------------------------------------------------------------------------------------ */
+
+/* The line profile table gaussnebarr(:, i) of compute_line_gaussians (src/physics/opensps_gas.f90:303-340)
+ * with neb_res_min of compute_nebular_kernels (src/core/opensps_initialization.f90:1377-1385), restricted to the
+ * window of add_lines_to_spectrum (src/physics/opensps_gas.f90:364-390; the batch path's nebular_setup uses the
+ * same cut, src/physics/opensps_csp_batch.f90:1636-1640). Writes prof (nspec) and the 0-based window [*jlo, *jhi]. */
+static void line_profile(int nspec, const double *lam, double line_pos, double sigma_kms, double *prof,
+                         int *jlo, int *jhi) {
+    int j = oracle_find_interval(lam, nspec, line_pos);
+    if (j < 1) j = 1;
+    if (j > nspec - 1) j = nspec - 1;
+    double res_min = lam[j] - lam[j - 1];
+    double sig = line_pos * sigma_kms * (1.0e13 / C_LIGHT);
+    if (sig < 2.0 * res_min) sig = 2.0 * res_min;
+    double norm = (1.0 / (sqrt(2.0 * acos(-1.0)) * sig)) * (line_pos * line_pos / C_LIGHT);
+    for (int i = 0; i < nspec; ++i) {
+        double x = (lam[i] - line_pos) / sig;
+        prof[i] = norm * exp(-0.5 * x * x);
+    }
+    int jc = oracle_find_interval(lam, nspec, line_pos);
+    if (jc < 1) jc = 1;
+    if (jc > nspec) jc = nspec;
+    int jh = jc + 1 < nspec ? jc + 1 : nspec;   /* 1-based */
+    double pk = prof[jc - 1] > prof[jh - 1] ? prof[jc - 1] : prof[jh - 1];
+    double cut = LINE_PROFILE_CUT * pk;
+    int jl = jc;
+    while (jl > 1 && prof[jl - 2] > cut) jl--;
+    while (jh < nspec && prof[jh] > cut) jh++;
+    *jlo = jl - 1;
+    *jhi = jh - 1;
+    if (cut <= 0.0) { *jlo = 0; *jhi = -1; }
+}
+
+/* The SSP basis with the nebular lines added to every age that has line luminosity (apply_nebular_emission
+ * adds the lines of each young SSP before the age sum; the batch path adds the same sum after it,
+ * src/physics/opensps_csp_batch.f90:2565-2610 and line_profiles :3133-3166: linear in the weights, so both are
+ * the same sums). ssp_in / ssp_out: nspec x nt x nz (pixel fastest); line_lum: nline x nt x nz. */
+void oracle_line_basis(int nspec, int nt, int nz, const double *lam, int nline, const double *line_pos,
+                       const double *line_lum, double sigma_kms, const double *ssp_in, double *ssp_out) {
+    memcpy(ssp_out, ssp_in, sizeof(double) * (size_t)nspec * nt * nz);
+    double *prof = (double *)malloc(sizeof(double) * nspec);
+    for (int l = 0; l < nline; ++l) {
+        int jlo, jhi;
+        line_profile(nspec, lam, line_pos[l], sigma_kms, prof, &jlo, &jhi);
+        for (int z = 0; z < nz; ++z)
+            for (int t = 0; t < nt; ++t) {
+                double L = line_lum[l + (size_t)nline * (t + (size_t)nt * z)];
+                if (L == 0.0) continue;
+                double *col = ssp_out + (size_t)nspec * (t + (size_t)nt * z);
+                for (int j = jlo; j <= jhi; ++j) col[j] += prof[j] * L;
+            }
+    }
+    free(prof);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Cosmology: distance term of the magnitudes.                                                */
+/* ------------------------------------------------------------------------------------------ */
+
+/* get_luminosity_distance (src/physics/opensps_cosmology.f90:244-276): trapezoid over 10000 points, [pc]. */
+static double lum_distance_pc(double h0, double om0, double ol0, double z) {
+    if (z <= 0.0) return 0.0;
+    const int N = 10000;
+    double dh = ((C_LIGHT * 1.0e-13) / h0) * 1.0e6;
+    double dz = z / (double)(N - 1);
+    double prev = 1.0 / sqrt(om0 + ol0), sum = 0.0;
+    for (int i = 2; i <= N; ++i) {
+        double zc = (double)(i - 1) * dz;
+        double now = 1.0 / sqrt(om0 * pow(1.0 + zc, 3) + ol0);
+        sum += 0.5 * dz * (prev + now);
+        prev = now;
+    }
+    return (1.0 + z) * dh * sum;
+}
+
+/* update_cosmology_table (src/physics/opensps_cosmology.f90:286-300): 500 scale factors; zt decreasing. */
+void oracle_cosmo_table(double h0, double om0, double ol0, double *zt, double *dl) {
+    for (int i = 1; i <= 500; ++i) {
+        double a = (double)(i - 1) / 499.0 * (1.0 - 1.0 / 1001.0) + 1.0 / 1001.0;
+        zt[i - 1] = 1.0 / a - 1.0;
+        dl[i - 1] = lum_distance_pc(h0, om0, ol0, zt[i - 1]);
+    }
+}
+
+/* distance_term (src/spectra/opensps_batch_photometry.f90:784-794) with interpolate_linear_scalar
+ * (src/math/opensps_interpolation.f90:45-72). */
+double oracle_distance_term(const double *zt, const double *dl, double z) {
+    if (fabs(z) <= SAFE_FLOOR) return 0.0;
+    int idx = oracle_find_interval(zt, 500, z);
+    if (idx < 1) idx = 1;
+    if (idx > 499) idx = 499;
+    double slope = (dl[idx] - dl[idx - 1]) / (zt[idx] - zt[idx - 1]);
+    double dm = dl[idx - 1] + slope * (z - zt[idx - 1]);
+    if (dm != dm || dm <= SAFE_FLOOR) return 0.0;
+    double mz = 1.0 + z;
+    return 5.0 * log10(dm / 10.0) + (mz > 0.0 ? -2.5 * log10(mz) : NAN);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* IGM                                                                                         */
+/* ------------------------------------------------------------------------------------------ */
+
+/* igm_tau_pixel_terms (src/physics/opensps_cosmology.f90:466-494) */
+void oracle_igm_pixel_terms(double w, double *a) {
+    for (int k = 0; k < 6; ++k) a[k] = 0.0;
+    if (w < LY_WAVE[0]) {
+        double ser = 0.0;
+        for (int i = 0; i < N_LYMAN; ++i)
+            if (w < LY_WAVE[i]) ser += LY_COEFF[i] * pow(LY_WAVE[i], -3.46);
+        a[0] = ser * pow(w, 3.46);
+        a[1] = A_METAL * pow(w / LY_WAVE[0], 1.68);
+    }
+    if (w < LYMAN_LIMIT) {
+        double s = w / LYMAN_LIMIT;
+        a[2] = MADAU_C1 * pow(s, 3.0) * (1.0 - pow(s, MADAU_P1));
+        a[3] = MADAU_C2 * pow(s, 1.5) * (1.0 - pow(s, MADAU_P2));
+        a[4] = -MADAU_C3 * pow(s, 3.0) * (pow(s, -MADAU_P3) - 1.0);
+        a[5] = -MADAU_C4 * (1.0 - pow(s, MADAU_P4));
+    }
+}
+
+/* igm_tau_z_terms (src/physics/opensps_cosmology.f90:497-508) */
+void oracle_igm_z_terms(double opz, double *b) {
+    b[0] = pow(opz, 3.46);
+    b[1] = pow(opz, 1.68);
+    b[2] = pow(opz, 3.0 + MADAU_P1);
+    b[3] = pow(opz, 1.5 + MADAU_P2);
+    b[4] = pow(opz, 3.0 - MADAU_P3);
+    b[5] = pow(opz, MADAU_P4);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Velocity smoothing operator                                                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct {
+    int *lo, *hi, *off;   /* 0-based; lo = -1: pixel unchanged */
+    double *coef;
+} vkernel_t;
+
+/* build_velocity_kernel (src/spectra/opensps_smoothing.f90:553-633) */
+static void build_velocity_kernel(int n, const double *lam, double sigma, double minl, double maxl, vkernel_t *k) {
+    k->lo = (int *)malloc(sizeof(int) * n);
+    k->hi = (int *)malloc(sizeof(int) * n);
+    k->off = (int *)malloc(sizeof(int) * n);
+    int *wlo = (int *)malloc(sizeof(int) * n), *whi = (int *)malloc(sizeof(int) * n);
+    for (int i = 0; i < n; ++i) { k->lo[i] = -1; k->hi[i] = -2; k->off[i] = 0; wlo[i] = -1; whi[i] = -2; }
+    k->coef = NULL;
+    if (n < 2 || sigma <= SAFE_FLOOR) { free(wlo); free(whi); return; }
+    double sb = sigma / (C_LIGHT * 1.0e-13);
+    double inv2s2 = 0.5 * (1.0 / sb) * (1.0 / sb);
+    double fb = exp(-N_SIGMA_RANGE * sb), fr = exp(N_SIGMA_RANGE * sb);
+    int il = 1, ih = 1, ntot = 0;   /* 1-based as the reference */
+    for (int i = 1; i <= n; ++i) {
+        double li = lam[i - 1];
+        if (li < minl || li > maxl) continue;
+        double vl = li * fb, vh = li * fr;
+        while (il > 1 && lam[il - 1] > vl) il--;
+        while (il < n && lam[il - 1] < vl) il++;
+        if (il > 1 && lam[il - 1] > vl) il--;
+        if (ih < il) ih = il;
+        while (ih > il && lam[ih - 1] > vh) ih--;
+        while (ih < n && lam[ih - 1] < vh) ih++;
+        if (ih - il + 1 < 2) continue;
+        wlo[i - 1] = il;
+        whi[i - 1] = ih;
+        ntot += ih - il + 1;
+    }
+    k->coef = (double *)malloc(sizeof(double) * (ntot > 0 ? ntot : 1));
+    double *w = (double *)malloc(sizeof(double) * n);
+    ntot = 0;
+    for (int i = 1; i <= n; ++i) {
+        if (wlo[i - 1] < 0) continue;
+        int l0 = wlo[i - 1], h0 = whi[i - 1], nw = h0 - l0 + 1;
+        double lli = log(lam[i - 1]);
+        for (int m = 0; m < nw; ++m) {
+            double d = lli - log(lam[l0 - 1 + m]);
+            w[m] = exp(-inv2s2 * d * d) / lam[l0 - 1 + m];
+        }
+        double tw = 0.0;
+        for (int m = 1; m <= nw; ++m) {
+            double dl = 0.0, dr = 0.0;
+            if (m > 1) dl = lam[l0 + m - 2] - lam[l0 + m - 3];
+            if (m < nw) dr = lam[l0 + m - 1] - lam[l0 + m - 2];
+            w[m - 1] = 0.5 * w[m - 1] * (dl + dr);
+            tw += w[m - 1];
+        }
+        if (tw <= SAFE_FLOOR) continue;
+        k->lo[i - 1] = l0 - 1;
+        k->hi[i - 1] = h0 - 1;
+        k->off[i - 1] = ntot;
+        for (int m = 0; m < nw; ++m) k->coef[ntot + m] = w[m] / tw;
+        ntot += nw;
+    }
+    free(w); free(wlo); free(whi);
+}
+
+static void free_vkernel(vkernel_t *k) { free(k->lo); free(k->hi); free(k->off); free(k->coef); }
+
+/* apply_velocity_kernel: smoothed(i) = sum coef * spec(lo..hi) for active rows, unchanged otherwise. */
+static void apply_vkernel(const vkernel_t *k, int n, const double *in, double *out) {
+    for (int i = 0; i < n; ++i) {
+        if (k->lo[i] < 0) { out[i] = in[i]; continue; }
+        double s = 0.0;
+        const double *c = k->coef + k->off[i];
+        for (int j = k->lo[i]; j <= k->hi[i]; ++j) s += c[j - k->lo[i]] * in[j];
+        out[i] = s;
+    }
+}
+
+/* The smoothing coefficient rows of pixel i for sigma (tests compare the GPU's per-model taps with these). */
+int oracle_velocity_row(int n, const double *lam, double sigma, double minl, double maxl, int i, int *lo,
+                        double *coef, int maxtaps) {
+    vkernel_t k;
+    build_velocity_kernel(n, lam, sigma, minl, maxl, &k);
+    int nt = 0;
+    *lo = k.lo[i];
+    if (k.lo[i] >= 0) {
+        nt = k.hi[i] - k.lo[i] + 1;
+        for (int m = 0; m < nt && m < maxtaps; ++m) coef[m] = k.coef[k.off[i] + m];
+    }
+    free_vkernel(&k);
+    return nt;
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* The batch                                                                                   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Per-model parameters, in this order (doubles): */
+enum { P_DUST1, P_DUST2, P_DUST3, P_DUST_INDEX, P_DUST1_INDEX, P_FRAC_NODUST, P_FRAC_OBRUN, P_ZRED,
+       P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_NPAR };
+
+typedef struct {
+    int nspec, nt, nz, nbands;
+    const double *lam;       /* nspec */
+    const double *log_age;   /* nt */
+    const double *basis;     /* nspec x nt x nz, lines already folded in (oracle_line_basis) */
+    const double *mass;      /* nt x nz */
+    const double *lbol;      /* nt x nz (log10) */
+    const double *bands;     /* nspec x nbands */
+    const double *zt, *dl;   /* cosmology table (500) */
+    int nline;
+    const double *line_lum;  /* nline x nt x nz, or NULL */
+    int add_igm;             /* add_igm_absorption */
+    int smooth;              /* velocity smoothing on (smooth_velocity = 1, smoothspec_fast = 1) */
+    double min_wave_smooth, max_wave_smooth;
+} oracle_grid_t;
+
+/* One model of compute_csp_batch (src/physics/opensps_csp_batch.f90:431-1214) with a weight matrix over
+ * ages and metallicities (weights_over_z):
+ *   model_sums_zw           :2090-2120   mass, L_bol, weights floored at SAFE_FLOOR, young/old at it_tesc
+ *   age_sums_w (CPU order)  :2269-2293   metallicities outer, ages inner
+ *   attenuate_batch         :3576-3660 with pixel_transmissions :3765-3818 (power-law curve, dust_type 0)
+ *   apply_igm_z             :4205-4299   Madau terms, the short-wavelength cap, exp(-tau igm_factor)
+ *   smooth_columns / apply_velocity_kernel (src/spectra/opensps_smoothing.f90)
+ *   compute_magnitudes_columns (src/spectra/opensps_batch_photometry.f90:53-180): observed_frame_z :819-903,
+ *   band_fluxes :1049-1171 (trapezoid per band support), magnitudes_from_fluxes :185-232 (AB, distance term).
+ * work: 4 * nspec doubles. */
+static void csp_one(const oracle_grid_t *g, const double *wz, const double *par, double *spec, double *mags,
+                    double *mass, double *lbol, double *emlines, double *young, double *old, double *fband_out,
+                    double *work, int ab_only) {
+    const int ns = g->nspec, nt = g->nt, nz = g->nz;
+    double *y = work, *o = work + ns, *tot = work + 2 * ns, *tmp = work + 3 * ns;
+    /* it_tesc: batch_model_indices :1554-1560 */
+    double dla = par[P_DUST_TESC] > SAFE_FLOOR ? par[P_DUST_TESC] : 7.0;
+    int itesc = oracle_find_interval(g->log_age, nt, dla);
+    if (itesc < 1) itesc = 1;
+    if (itesc > nt) itesc = nt;
+    double ms = 0.0, ls = 0.0;
+    for (int i = 0; i < ns; ++i) { y[i] = 0.0; o[i] = 0.0; }
+    if (emlines) for (int l = 0; l < g->nline; ++l) emlines[l] = 0.0;
+    for (int z = 0; z < nz; ++z)
+        for (int k = 0; k < nt; ++k) {
+            double w = wz[k + (size_t)nt * z];
+            if (!(w > SAFE_FLOOR)) continue;
+            ms += w * g->mass[k + (size_t)nt * z];
+            ls += w * pow(10.0, g->lbol[k + (size_t)nt * z]);
+            const double *b = g->basis + (size_t)ns * (k + (size_t)nt * z);
+            double *col = (k + 1 <= itesc) ? y : o;
+            for (int i = 0; i < ns; ++i) col[i] += w * b[i];
+            if (emlines && g->line_lum)
+                for (int l = 0; l < g->nline; ++l) emlines[l] += w * g->line_lum[l + (size_t)g->nline * (k + (size_t)nt * z)];
+        }
+    if (mass) *mass = ms;
+    if (lbol) *lbol = ls > SAFE_FLOOR ? log10(ls) : 0.0;
+    if (young) memcpy(young, y, sizeof(double) * ns);
+    if (old) memcpy(old, o, sizeof(double) * ns);
+
+    /* attenuation, dust_type 0 (power law) */
+    double d1 = par[P_DUST1], d2 = par[P_DUST2], d3 = par[P_DUST3], di = par[P_DUST_INDEX], d1i = par[P_DUST1_INDEX];
+    double fnd = par[P_FRAC_NODUST], fo = par[P_FRAC_OBRUN];
+    for (int i = 0; i < ns; ++i) {
+        double ltab = log(g->lam[i] / V_BAND);
+        double curve = 1.0;
+        if (di != 0.0) curve = curve * exp(di * ltab);
+        double tau_d = d2 * curve, td = exp(-tau_d);
+        double tb = 1.0, too = 1.0;
+        if (!(d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR)) tb = exp(-(d1 * exp(d1i * ltab)));
+        if (!(fabs(d3) <= SAFE_FLOOR)) too = exp(-(d3 * curve));
+        double ss = (y[i] * tb * (1.0 - fo) + y[i] * fo) + o[i] * too;
+        tot[i] = (1.0 - fnd <= SAFE_FLOOR) ? ss : ss * (td * (1.0 - fnd) + fnd);
+    }
+    /* IGM per model */
+    double zr = par[P_ZRED];
+    if (g->add_igm && zr > SAFE_FLOOR) {
+        int jtop = 0;
+        for (int j = 0; j < ns; ++j) if (g->lam[j] < 1215.67) jtop = j + 1;
+        if (jtop > 0) {
+            double b[6], a[6];
+            oracle_igm_z_terms(1.0 + zr, b);
+            double tmax = 0.0;
+            int jmax = 1;
+            for (int j = 0; j < jtop; ++j) {
+                oracle_igm_pixel_terms(g->lam[j], a);
+                tmp[j] = a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3] + a[4] * b[4] + a[5] * b[5];
+                if (tmp[j] > tmax) { tmax = tmp[j]; jmax = j + 1; }
+            }
+            if (jmax > 1) for (int j = 0; j < jmax; ++j) tmp[j] = tmax;
+            for (int j = 0; j < jtop; ++j) tot[j] *= exp(-tmp[j] * par[P_IGM_FACTOR]);
+        }
+    }
+    /* velocity smoothing */
+    double *fin = tot;
+    if (g->smooth && par[P_SIGMA_SMOOTH] > SAFE_FLOOR) {
+        vkernel_t vk;
+        build_velocity_kernel(ns, g->lam, par[P_SIGMA_SMOOTH], g->min_wave_smooth, g->max_wave_smooth, &vk);
+        apply_vkernel(&vk, ns, tot, tmp);
+        free_vkernel(&vk);
+        fin = tmp;
+    }
+    if (spec) memcpy(spec, fin, sizeof(double) * ns);
+
+    /* magnitudes */
+    if (mags || fband_out) {
+        double *fobs = (fin == tmp) ? tot : tmp;   /* reuse the free buffer */
+        for (int j = 0; j < ns; ++j) {
+            double v;
+            if (fabs(zr) > SAFE_FLOOR) {
+                double target = g->lam[j] / (1.0 + zr);
+                int il = oracle_find_interval(g->lam, ns, target);
+                if (il < 1) il = 1;
+                if (il > ns - 1) il = ns - 1;
+                double t = (target - g->lam[il - 1]) / (g->lam[il] - g->lam[il - 1]);
+                v = fin[il - 1] + t * (fin[il] - fin[il - 1]);
+            } else {
+                v = fin[j];
+            }
+            if (v != v) v = 0.0;
+            fobs[j] = (v > 0.0 ? v : 0.0) * (g->lam[j] > DBL_MIN ? 1.0 / g->lam[j] : 0.0);
+        }
+        double dist = oracle_distance_term(g->zt, g->dl, zr);
+        double zp = AB_ZEROPOINT + 2.5 * abs_mag_zeropoint_log();
+        for (int b = 0; b < g->nbands; ++b) {
+            const double *bd = g->bands + (size_t)ns * b;
+            int ilo = ns, ihi = 1;
+            for (int j = 1; j <= ns; ++j) if (bd[j - 1] != 0.0) { if (j < ilo) ilo = j; if (j > ihi) ihi = j; }
+            int jlo = ilo - 1 > 1 ? ilo - 1 : 1, jhi = ihi < ns - 1 ? ihi : ns - 1;
+            if (ilo > ihi) { jlo = 1; jhi = 0; }
+            double s = 0.0;
+            for (int j = jlo; j <= jhi; ++j) {
+                double wtl = 0.5 * fabs(g->lam[j] - g->lam[j - 1]);
+                s += wtl * (fobs[j - 1] * bd[j - 1] + fobs[j] * bd[j]);
+            }
+            if (fband_out) fband_out[b] = s;
+            if (mags) mags[b] = (s > 0.0 ? -2.5 * log10(s) : NAN) - zp + dist;
+        }
+        (void)ab_only;
+    }
+}
+
+/* The batch: n models, wz (nt x nz x n), par (P_NPAR x n). Any output may be NULL. */
+void oracle_csp_batch(const oracle_grid_t *g, int n, const double *wz, const double *par, double *spec, double *mags,
+                      double *mass, double *lbol, double *emlines, double *young, double *old, double *fband) {
+    const int ns = g->nspec;
+#pragma omp parallel
+    {
+        double *work = (double *)malloc(sizeof(double) * 4 * (size_t)ns);
+#pragma omp for schedule(dynamic, 4)
+        for (int m = 0; m < n; ++m) {
+            csp_one(g, wz + (size_t)g->nt * g->nz * m, par + (size_t)P_NPAR * m, spec ? spec + (size_t)ns * m : NULL,
+                    mags ? mags + (size_t)g->nbands * m : NULL, mass ? mass + m : NULL, lbol ? lbol + m : NULL,
+                    emlines ? emlines + (size_t)g->nline * m : NULL, young ? young + (size_t)ns * m : NULL,
+                    old ? old + (size_t)ns * m : NULL, fband ? fband + (size_t)g->nbands * m : NULL, work, 0);
+        }
+        free(work);
+    }
+}
+
+int oracle_npar(void) { return P_NPAR; }
+double oracle_abs_mag_zeropoint_log(void) { return abs_mag_zeropoint_log(); }

@@ -1,0 +1,135 @@
+"""Python driver of the FP64 CPU oracle (opensps_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by the tests, the smoke check and the benchmark's CPU-baseline leg, never by
+the product. It restates OpenSPS's batched CSP in FP64 on the CPU (see the C file for the reference routines each
+function follows) on the same synthetic libraries the product reads.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+PAR_NAMES = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
+             "igm_factor", "sigma_smooth", "dust_tesc")
+PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
+                "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
+                "dust_tesc": 7.0}
+_dp = C.POINTER(C.c_double)
+
+
+def build() -> Path:
+    if not LIB.exists() or LIB.stat().st_mtime < (HERE / "opensps_oracle.c").stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nspec", C.c_int), ("nt", C.c_int), ("nz", C.c_int), ("nbands", C.c_int),
+                ("lam", _dp), ("log_age", _dp), ("basis", _dp), ("mass", _dp), ("lbol", _dp), ("bands", _dp),
+                ("zt", _dp), ("dl", _dp), ("nline", C.c_int), ("line_lum", _dp), ("add_igm", C.c_int),
+                ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB))
+        _lib.oracle_find_interval.restype = C.c_int
+        _lib.oracle_find_interval.argtypes = [_dp, C.c_int, C.c_double]
+        _lib.oracle_line_basis.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, C.c_double, _dp, _dp]
+        _lib.oracle_cosmo_table.argtypes = [C.c_double, C.c_double, C.c_double, _dp, _dp]
+        _lib.oracle_distance_term.restype = C.c_double
+        _lib.oracle_distance_term.argtypes = [_dp, _dp, C.c_double]
+        _lib.oracle_igm_pixel_terms.argtypes = [C.c_double, _dp]
+        _lib.oracle_igm_z_terms.argtypes = [C.c_double, _dp]
+        _lib.oracle_velocity_row.restype = C.c_int
+        _lib.oracle_velocity_row.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, C.c_int,
+                                             C.POINTER(C.c_int), _dp, C.c_int]
+        _lib.oracle_csp_batch.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _dp] + [_dp] * 8
+        _lib.oracle_npar.restype = C.c_int
+        _lib.oracle_abs_mag_zeropoint_log.restype = C.c_double
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+class Oracle:
+    """The oracle over one synthetic library and filter set, with a context's batch-wide settings."""
+
+    def __init__(self, data: dict, nbands: int = 40, add_neb: bool = True, add_igm: bool = True,
+                 smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
+                 line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73):
+        L = lib()
+        self.d = data
+        self.lam = np.ascontiguousarray(data["lambda"])
+        self.log_age = np.ascontiguousarray(data["log_age"])
+        ns, nt, nz = self.lam.size, self.log_age.size, data["zlegend"].size
+        self.nspec, self.nt, self.nz = ns, nt, nz
+        ssp = np.ascontiguousarray(data["ssp_spec"])          # (nz, nt, ns)
+        self.line_lum = np.ascontiguousarray(data["line_lum"])
+        nl = data["line_lambda"].size
+        if add_neb:
+            self.basis = np.empty_like(ssp)
+            L.oracle_line_basis(ns, nt, nz, _p(self.lam), nl, _p(np.ascontiguousarray(data["line_lambda"])),
+                                _p(self.line_lum), float(line_sigma), _p(ssp), _p(self.basis))
+        else:
+            self.basis = ssp
+        self.mass = np.ascontiguousarray(data["ssp_mass"])
+        self.lbol = np.ascontiguousarray(data["ssp_lbol"])
+        self.bands = np.ascontiguousarray(data[f"filters_{nbands}"])
+        self.nbands = nbands
+        self.zt, self.dl = np.empty(500), np.empty(500)
+        L.oracle_cosmo_table(h0, om0, ol0, _p(self.zt), _p(self.dl))
+        g = _Grid()
+        g.nspec, g.nt, g.nz, g.nbands = ns, nt, nz, nbands
+        g.lam, g.log_age, g.basis = _p(self.lam), _p(self.log_age), _p(self.basis)
+        g.mass, g.lbol, g.bands = _p(self.mass), _p(self.lbol), _p(self.bands)
+        g.zt, g.dl = _p(self.zt), _p(self.dl)
+        g.nline = nl
+        g.line_lum = _p(self.line_lum) if add_neb else None
+        g.add_igm, g.smooth = int(add_igm), int(smooth)
+        g.min_wave_smooth, g.max_wave_smooth = min_wave_smooth, max_wave_smooth
+        self.grid = g
+        self.nline = nl
+
+    def pack_params(self, params: dict, n: int) -> np.ndarray:
+        out = np.empty((n, len(PAR_NAMES)))
+        for i, k in enumerate(PAR_NAMES):
+            out[:, i] = np.broadcast_to(np.asarray(params.get(k, PAR_DEFAULTS[k]), dtype=np.float64), (n,))
+        return np.ascontiguousarray(out)
+
+    def csp_batch(self, params: dict, wz: np.ndarray, spec=True, young=False, fband=False, emlines=False) -> dict:
+        """wz: (n, nz, nt) weights over metallicities and ages."""
+        wz = np.ascontiguousarray(wz, dtype=np.float64)
+        n = wz.shape[0]
+        par = self.pack_params(params, n)
+        out = {"mags": np.empty((n, self.nbands)), "mass": np.empty(n), "lbol": np.empty(n)}
+        if spec: out["spec"] = np.empty((n, self.nspec))
+        if young:
+            out["young"] = np.empty((n, self.nspec))
+            out["old"] = np.empty((n, self.nspec))
+        if fband: out["fband"] = np.empty((n, self.nbands))
+        if emlines: out["emlines"] = np.empty((n, self.nline))
+        lib().oracle_csp_batch(C.byref(self.grid), n, _p(wz), _p(par), _p(out.get("spec")), _p(out["mags"]),
+                               _p(out["mass"]), _p(out["lbol"]), _p(out.get("emlines")), _p(out.get("young")),
+                               _p(out.get("old")), _p(out.get("fband")))
+        return out
+
+    def velocity_row(self, sigma: float, i: int, minl: float = 1.0e3, maxl: float = 1.0e4):
+        lo, coef = C.c_int(0), np.zeros(64)
+        nt = lib().oracle_velocity_row(self.nspec, _p(self.lam), sigma, minl, maxl, i, C.byref(lo), _p(coef), 64)
+        return lo.value, coef[:nt].copy()
+
+    def distance_term(self, z: float) -> float:
+        return lib().oracle_distance_term(_p(self.zt), _p(self.dl), z)
