@@ -1,0 +1,278 @@
+"""Benchmark of the batched mixed-precision CSP (models/s) on GB300.
+
+Workload (one step = one batch): the mixed-precision batched CSP at B = 65536 models: weights over 107 ages x 12
+metallicities per model, split-BF16 contraction with a 1284 x 5994 SSP basis (nebular lines in the young SSPs),
+power-law dust (tau_V uniform 0-3), redshift uniform 0-6 with the Madau IGM, velocity smoothing sigma uniform
+50-300 km/s, 40 filters; seeded synthetic inputs (libopensps_gb300.workloads.mixed_csp).
+
+* ``value``: models/s with the inputs resident in HBM (opensps_gb300_batch_device), timed with CUDA events on the
+  library's stream over ``--steps`` batches after ``--warmup`` (the 673 MB FP64 weight input of a step is larger than
+  L2, so no flush is needed between steps).
+* ``e2e``: the same through the OpenSPS C API (opensps_context_compute_csp_batch_grad with ssp_weights_z, no
+  cotangents) from pinned host buffers: the weights and per-model parameters are copied in and the magnitudes,
+  masses and L_bol copied out inside the timed region.
+* ``roofline``: the contraction kernel (split-BF16 tcgen05 GEMM with its fused epilogue): 3 x 2 K P B executed
+  bf16 FLOPs per launch over its mean CUDA-event duration, against the measured sustained bf16 peak.
+* ``cpu_baseline`` / ``--impl reference``: the FP64 CPU oracle (a restatement of OpenSPS's compute_csp_batch,
+  the reference being Fortran with no compiler in this image) with OpenMP on all host cores, on a bounded sample.
+
+With ``--gpus N`` under torchrun each rank runs its own batch (replicas: the models of different ranks are
+independent; no collective on the data path) and ``value`` is the models of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+K_AGES, N_Z, N_PIX = 107, 12, 5994
+METRIC = "CSP models/s at B=65536: mixed vs FP64 at <=1e-4 rel; emulator speedup @0.01 mag"
+WORKLOAD = ("mixed-precision batched CSP (split-BF16 contraction 1284x5994, nebular lines, power-law dust, "
+            "Madau IGM z 0-6, velocity smoothing 50-300 km/s, 40 filters)")
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "src": "fallback"}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, path: Path):
+        self.path = path
+        self.proc = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", str(int(os.environ.get("LOCAL_RANK", "0")))],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_rate(n_sample: int, seed: int = 5) -> dict:
+    """The FP64 CPU oracle on n_sample models of the workload: models/s on all host cores."""
+    from libopensps_gb300 import synthdata, workloads
+    from oracle.oracle import Oracle
+    o = Oracle(synthdata.load(), nbands=40)
+    wz, params = workloads.mixed_csp(n_sample, seed=seed)
+    o.csp_batch({k: v[:8] for k, v in params.items()}, wz[:8])   # warm
+    t0 = time.perf_counter()
+    o.csp_batch(params, wz)
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n_sample / dt, "unit": "models/s", "cores": cores, "kind": "port",
+            "sample": f"{n_sample} models of the B=65536 workload (FP64 oracle, OpenMP), {dt:.2f} s"}
+
+
+def run_reference(args) -> None:
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    n_sample = args.cpu_sample
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_oracle_rate(n_sample, seed=100 + i)
+        if i >= args.warmup:
+            vals.append(r)
+    v = float(np.mean([r["value"] for r in vals]))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "models/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.batch / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": args.batch, "sample_per_step": n_sample,
+                       "note": "OpenSPS is Fortran (no Fortran compiler in this image): the FP64 C oracle restating "
+                               "its compute_csp_batch is the CPU implementation timed"},
+            "cpu_baseline": {"value": v, "unit": "models/s", "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "models/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from libopensps_gb300 import workloads
+    from libopensps_gb300.capi import Context
+
+    n = args.batch
+    ctx = Context()
+    ctx.set_int("add_neb_emission", 1)
+    ctx.set_int("add_igm_absorption", 1)
+    nb = ctx.nbands
+
+    # inputs: pinned host copies (for e2e) and device-resident copies (for value)
+    h_wz = torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True)
+    _, params = workloads.mixed_csp(n, seed=1000 + rank, out=h_wz.numpy())
+    h_par = torch.from_numpy(workloads.device_param_table(params, n)).pin_memory()
+    d_wz = h_wz.to("cuda", non_blocking=False)
+    d_par = h_par.to("cuda", non_blocking=False)
+    d_mags = torch.empty((n, nb), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def step():
+        ctx.batch_device(n, d_par.data_ptr(), d_wz.data_ptr(), d_mags.data_ptr(), sync=False)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").exists() else \
+        ClockSampler(Path("/tmp") / f"opensps_clocks_{rank}.csv")
+    clocks.start()
+    time.sleep(0.3)
+    ctx.set_profiling(True)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    ktimes = ctx.kernel_times()
+    ctx.set_profiling(False)
+    launches = ctx.last_launches()
+    clk = clocks.stop()
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = ws * n / (ms_step * 1e-3)
+
+    # e2e through the C API from pinned host buffers (magnitudes, mass and L_bol back to the host)
+    e2e_ms = None
+    h_wz_np = h_wz.numpy()
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            barrier()
+            t0 = time.perf_counter()
+        ctx.csp_batch(params, ssp_weights_z=h_wz_np, spec=False)
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = h_wz.numel() * 8 + n * 11 * 8 + 3 * n * 8
+    d2h = n * nb * 8 + 6 * n * 8
+
+    # roofline of the contraction
+    pk = _peaks()
+    flops = 3.0 * 2.0 * (K_AGES * N_Z) * N_PIX * n
+    t_contract = ktimes[2] if len(ktimes) > 2 else None
+    achieved = flops / (t_contract * 1e-3) / 1e12 if t_contract else None
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("csp_contract_kernel_bytes_per_launch_at_65536")
+
+    if rank == 0:
+        cpu = cpu_oracle_rate(args.cpu_sample) if args.cpu_sample > 0 else None
+        line = {
+            "metric": METRIC, "value": value, "unit": "models/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 (split-BF16, f32 accumulate; FP64 sums)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch": n, "ages": K_AGES, "metallicities": N_Z, "pixels": N_PIX,
+                       "filters": nb, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (673 MB of FP64 weights per step)"},
+            "e2e": {"value": ws * n / (e2e_ms * 1e-3), "unit": "models/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "outputs": "mags, mass, lbol (spectra stay on the device)"},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"],
+                         "unit": "TFLOP/s", "frac": (achieved / pk["bf16_tflops_sustained"]) if achieved else None,
+                         "traffic": traffic, "kernel": "csp_contract_kernel<1>",
+                         "peak_src": f"{pk['src']} sustained bf16",
+                         "stage_ms": {"weights": ktimes[0] if len(ktimes) > 0 else None,
+                                      "model_params": ktimes[1] if len(ktimes) > 1 else None,
+                                      "contract": t_contract,
+                                      "bands": ktimes[3] if len(ktimes) > 3 else None}},
+            "cpu_baseline": cpu,
+            "gpu_launches": launches * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=65536)
+    ap.add_argument("--cpu-sample", type=int, default=4096)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

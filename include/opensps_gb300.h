@@ -27,6 +27,12 @@ void opensps_gb300_batch_device(int handle, int n, const double *d_params, const
 /* The context's CUDA stream (cudaStream_t) and the device it runs on. */
 void opensps_gb300_context_stream(int handle, void **stream, int *device, int *status);
 
+/* With on != 0, CUDA events are recorded between the kernels of every batch on the handle; afterwards
+ * opensps_gb300_kernel_times gives the device time of each stage of the last batch in milliseconds, in order: the
+ * weights prologue, the per-model parameters, the contraction with its epilogue, the band fluxes and magnitudes. */
+void opensps_gb300_set_profiling(int handle, int on, int *status);
+void opensps_gb300_kernel_times(int handle, double *ms, int max_n, int *n, int *status);
+
 /* Kernel launches of the last batch on the handle (for the benchmark's launch count). */
 void opensps_gb300_last_launches(int handle, int *launches, int *status);
 

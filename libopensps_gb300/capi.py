@@ -67,6 +67,8 @@ SIGNATURES = {
     "opensps_gb300_batch_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
+    "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
+    "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
 }
 
 
@@ -250,3 +252,15 @@ class Context:
 
     def last_launches(self) -> int:
         return self._get_int("opensps_gb300_last_launches")
+
+    def set_profiling(self, on: bool):
+        st = C.c_int(0)
+        self.lib.opensps_gb300_set_profiling(self.handle, 1 if on else 0, C.byref(st))
+        _check(st, self.lib)
+
+    def kernel_times(self) -> list[float]:
+        """Device ms of the last batch's stages: weights, model parameters, contraction, bands."""
+        buf, n, st = np.zeros(8), C.c_int(0), C.c_int(0)
+        self.lib.opensps_gb300_kernel_times(self.handle, _ptr(buf), 8, C.byref(n), C.byref(st))
+        _check(st, self.lib)
+        return buf[:n.value].tolist()

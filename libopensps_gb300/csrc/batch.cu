@@ -257,6 +257,35 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
 }
 
 // ---------------------------------------------------------------------------------------------- the batch
+// Profiling marks: with profiling on, event k is recorded on the stream after stage k (0 = before the first kernel),
+// so that the kernels' device times can be read back after the batch (opensps_gb300_kernel_times).
+// Two event sets alternate between batches; a set is read back (and its times added to the running sums) when it
+// is about to be reused, so that up to two profiled batches can be in flight.
+void prof_harvest(Context &c, int s) {
+    if (!c.prof_pending[s]) return;
+    cudaEventSynchronize(c.prof_ev[s][c.prof_used[s] - 1]);
+    for (int i = 1; i < c.prof_used[s]; ++i) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, c.prof_ev[s][i - 1], c.prof_ev[s][i]) == cudaSuccess) c.prof_acc[i - 1] += t;
+    }
+    c.prof_nstage = std::max(c.prof_nstage, c.prof_used[s] - 1);
+    c.prof_count += 1;
+    c.prof_pending[s] = false;
+}
+
+static void prof_mark(Context &c, int k) {
+    if (!c.profile || k >= Context::NPROF) return;
+    if (k == 0) {
+        c.prof_set ^= 1;
+        prof_harvest(c, c.prof_set);
+    }
+    const int s = c.prof_set;
+    if (!c.prof_ev[s][k]) cudaEventCreate(&c.prof_ev[s][k]);
+    cudaEventRecord(c.prof_ev[s][k], c.stream);
+    c.prof_used[s] = k + 1;
+    c.prof_pending[s] = k > 0;
+}
+
 static std::string cuda_msg(const char *what, cudaError_t e) { return std::string(what) + ": " + cudaGetErrorString(e); }
 
 int run_batch(Context &c, const BatchIO &io, std::string &err) {
@@ -326,8 +355,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     BasisOperand *bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
     if (!bop) return ST_DATA_MISSING;
 
-    // ---- per-pixel table (smoothing range)
-    {
+    // ---- per-pixel table (rebuilt when the smoothing range changes)
+    if (!(c.d_pix.p && c.pix_minl == minl && c.pix_maxl == maxl)) {
         std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
         for (int j = 0; j < ns; ++j) {
             float *px = pix.data() + (size_t)j * PIX_FLOATS;
@@ -342,6 +371,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("pixel table", e);
             return ST_DATA_MISSING;
         }
+        c.pix_minl = minl;
+        c.pix_maxl = maxl;
     }
 
     // ---- scratch
@@ -387,7 +418,9 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.nty_young = bop->nty; wa.ky_pad = bop->ky_pad;
     wa.wz = d_wz; wa.mass = c.d_mass.p; wa.llin = c.d_llin.p; wa.w_hi = c.d_whi.p; wa.w_lo = c.d_wlo.p;
     wa.sums = c.d_sums.p; wa.itesc = itesc;
+    prof_mark(c, 0);
     if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
+    prof_mark(c, 1);
 
     // ---- per-model parameters
     ModelParamArgs ma;
@@ -395,6 +428,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
     ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zshift = c.d_zshift.p; ma.dist = c.d_dist.p;
     model_params_kernel<<<(n + 127) / 128, 128, 0, st>>>(ma);
+    prof_mark(c, 2);
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
 
     // ---- contraction + epilogue
@@ -416,6 +450,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
+    prof_mark(c, 3);
     int launches = 3;   // weights, model parameters, contraction
 
     // ---- bands and magnitudes
@@ -434,6 +469,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
         ba.do_band = c.d_do_band.p; ba.fband = nullptr; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
         if ((e = run_bands(ba, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+        prof_mark(c, 4);
         ++launches;
     }
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);

@@ -14,6 +14,7 @@
 namespace sps {
 void get_error(int *status, std::string *msg);
 void clear_error();
+void prof_harvest(Context &c, int s);
 int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
                    const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
                    double *weights_z_bar, std::string &err);
@@ -467,6 +468,31 @@ void opensps_gb300_context_stream(int handle, void **stream, int *device, int *s
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
     if (stream) *stream = (void *)c->stream;
     if (device) *device = c->device;
+    if (status) *status = 0;
+}
+
+void opensps_gb300_set_profiling(int handle, int on, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (int s = 0; s < 2; ++s) prof_harvest(*c, s);
+    c->profile = on;
+    c->prof_count = 0;
+    c->prof_nstage = 0;
+    for (int i = 0; i < Context::NPROF; ++i) c->prof_acc[i] = 0.0;
+    if (status) *status = 0;
+}
+
+// Mean device time of each stage over the profiled batches since profiling was switched on.
+void opensps_gb300_kernel_times(int handle, double *ms, int max_n, int *n, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (int s = 0; s < 2; ++s) prof_harvest(*c, s);
+    int k = 0;
+    for (; k < c->prof_nstage && k < max_n; ++k)
+        if (ms) ms[k] = c->prof_count > 0 ? c->prof_acc[k] / c->prof_count : 0.0;
+    if (n) *n = k;
     if (status) *status = 0;
 }
 

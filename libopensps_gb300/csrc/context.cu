@@ -159,6 +159,8 @@ Context::~Context() {
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
     d_status.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
+    for (int s = 0; s < 2; ++s)
+        for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -362,7 +364,8 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         err = std::string("device upload failed: ") + cudaGetErrorString(e);
         return ST_DATA_MISSING;
     }
-    c.d_pix.release();   // rebuilt per batch (smoothing range)
+    c.d_pix.release();   // rebuilt by the next batch (smoothing range)
+    c.pix_minl = c.pix_maxl = -1.0;
     int st = context_load_filters(c, c.filter_set, err);
     if (st != 0) return st;
     for (auto &kv : c.basis_cache) { kv.second->hi.release(); kv.second->lo.release(); delete kv.second; }

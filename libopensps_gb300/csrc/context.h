@@ -83,7 +83,7 @@ struct Context {
     DevBuf<int> d_jr, d_do_band;
     DevBuf<double> d_lam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
-    double basis_sigma = -1.0;
+    double pix_minl = -1.0, pix_maxl = -1.0;   // smoothing range of the device pixel table
 
     // batch scratch
     DevBuf<double> d_wz, d_params, d_sums, d_zshift, d_dist, d_fband, d_mags, d_spec64;
@@ -92,6 +92,12 @@ struct Context {
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch
+    // profiling: events recorded between the kernels of a batch (opensps_gb300_set_profiling)
+    static constexpr int NPROF = 8;
+    int profile = 0, prof_set = 0, prof_used[2] = {0, 0}, prof_count = 0, prof_nstage = 0;
+    bool prof_pending[2] = {false, false};
+    double prof_acc[NPROF] = {};
+    cudaEvent_t prof_ev[2][NPROF] = {};
     void *pinned_spec = nullptr; size_t pinned_bytes = 0;
     std::vector<double> last_maggies;
     int keep_maggies = 0;
