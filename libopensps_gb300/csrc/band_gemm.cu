@@ -1,0 +1,193 @@
+// Band fluxes and AB magnitudes as a tensor-core GEMM: fband(m, b) = sum_j Fobs(m, j) C(j, b).
+//
+// compute_magnitudes_columns (OpenSPS src/spectra/opensps_batch_photometry.f90:53-180): each model's rest-frame
+// spectrum resampled to the observed frame at its redshift, divided by lambda (observed_frame_z :819-903), then the
+// trapezoid filter integrals regrouped by pixel, C(j, b) = band(j, b) (wtl(j - 1) + wtl(j)) (the split-K product
+// :1002-1044, prepare_batch_grid :375-392), then magnitudes_from_fluxes :185-232 (AB, distance term, NaN for bands
+// not computed).
+//
+// Per CTA: 128 models (MMA M). K = the pixels that any band reaches, 64 per stage. The A operand (observed frame
+// of 128 models x 64 pixels) is built by the CTA's threads in shared memory from the spectra, in the 128-byte
+// swizzled K-major layout, split into bf16 hi and lo; the B operand (band matrix, hi and lo, bands x pixels) comes
+// by TMA. fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes.
+// Two stages: the threads build stage s + 1 while the tensor core works on stage s.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include "sm103_ptx.cuh"
+#include "csp_kernels.h"
+
+namespace sps {
+
+constexpr int BG_M = 128;
+constexpr int BG_K = 64;
+constexpr int BG_THREADS = 256;
+constexpr int BG_A_BYTES = BG_M * BG_K * 2;   // 16 KB
+
+struct BandGemmSmem {
+    static int b_bytes(int npad) { return npad * BG_K * 2; }
+    static int total(int npad) { return 2 * (2 * BG_A_BYTES + 2 * b_bytes(npad)) + 256 + 1024; }
+};
+
+__global__ void __launch_bounds__(BG_THREADS)
+band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_constant__ CUtensorMap tm_c_lo,
+                 BandGemmArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int npad = a.npad;
+    const int b_bytes = npad * BG_K * 2;
+    const int stage_bytes = 2 * BG_A_BYTES + 2 * b_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * stage_bytes);
+    uint64_t *bar_tma = bars;        // [2]
+    uint64_t *bar_mma = bars + 2;    // [2]
+    uint64_t *bar_done = bars + 4;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 5);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * BG_M;
+    int *status = a.status;
+    const uint32_t tcols = npad <= 32 ? 32 : (npad <= 64 ? 64 : (npad <= 128 ? 128 : 256));
+
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) { mbar_init(&bar_tma[s], 1); mbar_init(&bar_mma[s], 1); }
+        mbar_init(bar_done, 1);
+        fence_mbar_init();
+        tma_prefetch_desc(&tm_c_hi);
+        tma_prefetch_desc(&tm_c_lo);
+    }
+    if (warp == 0) { tmem_alloc(tmem_slot, tcols); tmem_relinquish(); }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
+    const float em1 = expm1f((float)a.dlnl);
+
+    // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
+    for (int kb = 0; kb < a.nkb; ++kb) {
+        const int s = kb & 1;
+        uint8_t *st = smem + s * stage_bytes;
+        if (kb >= 2) mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+        if (tid == 0) {
+            mbar_arrive_expect_tx(&bar_tma[s], 2 * b_bytes);
+            tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &bar_tma[s]);
+            tma_load_2d(st + 2 * BG_A_BYTES + b_bytes, &tm_c_lo, kb * BG_K, 0, &bar_tma[s]);
+        }
+        const int j = a.j0 + kb * BG_K + 2 * lane;       // observed pixel of this lane (and j + 1)
+        float wl0 = 0.f, wl1 = 0.f;
+        if (j < a.nspec) wl0 = a.wl[j];
+        if (j + 1 < a.nspec) wl1 = a.wl[j + 1];
+        for (int rr = 0; rr < 16; ++rr) {
+            const int r = warp * 16 + rr;
+            const int m = m0 + r;
+            float f0 = 0.f, f1 = 0.f;
+            if (m < a.n_models) {
+                const float *sp = a.spec + (size_t)m * a.ld_spec;
+                const float4 zs = reinterpret_cast<const float4 *>(a.zinfo)[m];   // n0, t, s, rest flag
+                const int n0 = __float_as_int(zs.x);
+                float v0, v1;
+                if (zs.w == 0.f) {
+                    v0 = (j < a.nspec) ? sp[j] : 0.f;
+                    v1 = (j + 1 < a.nspec) ? sp[j + 1] : 0.f;
+                } else {
+                    const int sub = (zs.y > 0.f) ? 1 : 0;
+                    int il0 = j - n0 - sub, il1 = il0 + 1;
+                    float t0 = zs.y, t1 = zs.y;
+                    if (il0 < 0 || il0 > a.nspec - 2) {
+                        const int c = il0 < 0 ? 0 : a.nspec - 2;
+                        t0 = expm1f(((float)(j - c) - zs.z) * (float)a.dlnl) / em1;
+                        il0 = c;
+                    }
+                    if (il1 < 0 || il1 > a.nspec - 2) {
+                        const int c = il1 < 0 ? 0 : a.nspec - 2;
+                        t1 = expm1f(((float)(j + 1 - c) - zs.z) * (float)a.dlnl) / em1;
+                        il1 = c;
+                    }
+                    const float s00 = sp[il0], s01 = sp[il0 + 1];
+                    const float s10 = sp[il1], s11 = sp[il1 + 1];
+                    v0 = fmaf(t0, s01 - s00, s00);
+                    v1 = fmaf(t1, s11 - s10, s10);
+                }
+                if (v0 != v0) v0 = 0.f;
+                if (v1 != v1) v1 = 0.f;
+                f0 = fmaxf(v0, 0.f) * wl0;
+                f1 = fmaxf(v1, 0.f) * wl1;
+            }
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
+            const uint32_t off = r * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2);
+            __nv_bfloat162 hh, ll;
+            hh.x = h0; hh.y = h1;
+            ll.x = l0; ll.y = l1;
+            *reinterpret_cast<__nv_bfloat162 *>(st + off) = hh;
+            *reinterpret_cast<__nv_bfloat162 *>(st + BG_A_BYTES + off) = ll;
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            mbar_wait(&bar_tma[s], (kb >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+            tc_fence_after();
+            const uint32_t sa = smem_u32(st);
+            const uint32_t ahi = sa, alo = sa + BG_A_BYTES, bhi = sa + 2 * BG_A_BYTES, blo = bhi + b_bytes;
+#pragma unroll
+            for (int k = 0; k < BG_K / 16; ++k) {
+                const uint32_t o = k * 32;
+                mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
+                mma_bf16(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+            }
+            mma_commit(&bar_mma[s]);
+        }
+    }
+    if (tid == 0) mma_commit(bar_done);
+    mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
+    tc_fence_after();
+
+    // epilogue: warps 0..3 read their lane quarter (one model per thread)
+    if (warp < 4) {
+        const int r = warp * 32 + lane, m = m0 + r;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < npad; c0 += 32) {
+            float v[32];
+            tmem_ld32(trow + c0, v);
+            if (m < a.n_models) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int b = c0 + i;
+                    if (b < a.nbands) {
+                        const double f = (double)v[i];
+                        if (a.fband) a.fband[(size_t)m * a.nbands + b] = f;
+                        if (a.mags) {
+                            double mg = __longlong_as_double(0x7ff8000000000000LL);
+                            if (a.do_band == nullptr || a.do_band[b] != 0)
+                                mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) - a.zp +
+                                     a.dist[m];
+                            a.mags[(size_t)m * a.nbands + b] = mg;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, tcols);
+    }
+}
+
+int band_gemm_npad(int nbands) { return (nbands + 15) / 16 * 16 < 32 ? 32 : (nbands + 15) / 16 * 16; }
+
+cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
+                          cudaStream_t st) {
+    if (a.n_models <= 0 || a.nkb <= 0) return cudaSuccess;
+    const int smem = BandGemmSmem::total(a.npad);
+    cudaError_t e = cudaFuncSetAttribute(band_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = (a.n_models + BG_M - 1) / BG_M;
+    band_gemm_kernel<<<grid, BG_THREADS, smem, st>>>(tm_hi, tm_lo, a);
+    return cudaGetLastError();
+}
+
+}  // namespace sps

@@ -37,7 +37,7 @@ struct ModelParamArgs {
     const double *zt, *dl;   // 500
     double dlnl;
     float *mpar;             // n x MODEL_PAR_FLOATS
-    double *zshift;          // n x 4
+    float4 *zinfo;           // n: the observed-frame shift (band_gemm.cu)
     double *dist;            // n
 };
 
@@ -119,17 +119,17 @@ __global__ void model_params_kernel(ModelParamArgs a) {
         }
     }
     // observed frame: the shift of lambda / (1 + z) on the log-uniform grid, in pixels
-    double *zs = a.zshift + (size_t)4 * m;
+    // (observed pixel j reads rest pixels j - n0 - 1 and j - n0 at t, the same t for every interior pixel)
+    float4 zi = make_float4(__int_as_float(0), 0.f, 0.f, 0.f);
     if (fabs(z) > SAFE_FLOOR) {
         const double s = log1p(z) / a.dlnl;
         const double n0 = floor(s), phi = s - n0;
-        zs[0] = n0;
-        zs[1] = phi > 0.0 ? expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl) : 0.0;
-        zs[2] = s;
-        zs[3] = 1.0;
-    } else {
-        zs[0] = 0.0; zs[1] = 0.0; zs[2] = 0.0; zs[3] = 0.0;
+        zi.x = __int_as_float((int)n0);
+        zi.y = phi > 0.0 ? (float)(expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl)) : 0.f;
+        zi.z = (float)s;
+        zi.w = 1.f;
     }
+    a.zinfo[m] = zi;
     // distance term (distance_term, src/spectra/opensps_batch_photometry.f90:784-794)
     double dd = 0.0;
     if (fabs(z) > SAFE_FLOOR) {
@@ -342,9 +342,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         const double s1 = par(0, PF_SIGMA_SMOOTH);
         const bool f1 = lines_floor_limited(c, s1);
         line_sigma = f1 ? 0.0 : s1;
+        // below 0.999 of the smallest line's threshold every line is at the floor (no per-line test needed)
+        double thr = 1e300;
+        for (int l = 0; l < c.nline; ++l) {
+            const double pos = c.line_lambda[l];
+            int j = find_interval0(c.lam.data(), c.nspec, pos) + 1;
+            j = std::max(1, std::min(j, c.nspec - 1));
+            thr = std::min(thr, 2.0 * (c.lam[j] - c.lam[j - 1]) / (pos * (1.0e13 / C_LIGHT)));
+        }
         for (int m = 1; m < n; ++m) {
             const double sm = par(m, PF_SIGMA_SMOOTH);
             if (sm == s1) continue;
+            if (f1 && sm < 0.999 * thr) continue;
             if (!(f1 && lines_floor_limited(c, sm))) {
                 err = "nebular lines with a sigma_smooth of each model's own (above the grid's line width) are unsupported";
                 return ST_UNSUPPORTED;
@@ -385,7 +394,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         (e = c.d_params.reserve((size_t)PAR_DEVICE * n)) != cudaSuccess ||
         (e = c.d_whi.reserve((size_t)n * kpad)) != cudaSuccess || (e = c.d_wlo.reserve((size_t)n * kpad)) != cudaSuccess ||
         (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess || (e = c.d_mpar.reserve((size_t)MODEL_PAR_FLOATS * n)) != cudaSuccess ||
-        (e = c.d_zshift.reserve((size_t)4 * n)) != cudaSuccess || (e = c.d_dist.reserve(n)) != cudaSuccess ||
+        (e = c.d_zinfo.reserve((size_t)n)) != cudaSuccess || (e = c.d_dist.reserve(n)) != cudaSuccess ||
         (e = c.d_spec.reserve((size_t)n * ns)) != cudaSuccess || (e = c.d_mags.reserve((size_t)n * nb)) != cudaSuccess) {
         err = cuda_msg("device memory", e);
         return ST_DATA_MISSING;
@@ -426,7 +435,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ModelParamArgs ma;
     ma.n = n; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
     ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
-    ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zshift = c.d_zshift.p; ma.dist = c.d_dist.p;
+    ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zinfo = c.d_zinfo.p; ma.dist = c.d_dist.p;
     model_params_kernel<<<(n + 127) / 128, 128, 0, st>>>(ma);
     prof_mark(c, 2);
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
@@ -463,12 +472,14 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("band mask", e);
             return ST_DATA_MISSING;
         }
-        BandArgs ba;
-        ba.nspec = ns; ba.nbands = nb; ba.n_models = n; ba.ld_spec = ns; ba.spec = c.d_spec.p; ba.cmat = c.d_cmat.p;
-        ba.jr = c.d_jr.p; ba.wl = c.d_wl.p; ba.zshift = c.d_zshift.p; ba.dlnl = c.dlnl; ba.dist = c.d_dist.p;
+        BandGemmArgs ba;
+        ba.n_models = n; ba.nspec = ns; ba.nbands = nb; ba.npad = c.band_npad; ba.nkb = c.band_nkb; ba.j0 = c.band_j0;
+        ba.ld_spec = ns; ba.spec = c.d_spec.p; ba.zinfo = c.d_zinfo.p; ba.wl = c.d_wl.p; ba.dlnl = c.dlnl;
+        ba.dist = c.d_dist.p;
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
-        ba.do_band = c.d_do_band.p; ba.fband = nullptr; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
-        if ((e = run_bands(ba, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+        ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
+        ba.status = c.d_status.p;
+        if ((e = run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
         prof_mark(c, 4);
         ++launches;
     }

@@ -143,6 +143,38 @@ void batch_entry(int handle, int n, int n_params, const char *const *names, cons
         st = run_batch(*c, io, err);
     }
     if (st) return fail(status, st, err);
+    if (!ssp_weights_z && (lbol || lbol_young || lbol_old)) {
+        // With one weight per age blended at logzsol, L_bol follows the SSP's own interpolation: log L_bol is blended
+        // between the bracketing metallicities, then exponentiated (model_sums MSUMS_BLEND,
+        // src/physics/opensps_csp_batch.f90:2129-2176), which is not the sum over the two slabs' linear L_bol.
+        const int nt = c->nt, nz = c->nz;
+        std::vector<double> lz(nz);
+        for (int z = 0; z < nz; ++z) lz[z] = std::log10(c->zlegend[z] / c->zsol);
+        for (int m = 0; m < n; ++m) {
+            const double x = rows[(size_t)PF_COUNT * m + PF_LOGZSOL];
+            int lower = 0, upper = nz + 1;
+            while (upper - lower > 1) { const int mid = (upper + lower) / 2; if (x >= lz[mid - 1]) lower = mid; else upper = mid; }
+            int idx = lower;
+            if (x == lz[0]) idx = 1; else if (x == lz[nz - 1]) idx = nz - 1;
+            const int zlo = std::max(1, std::min(idx, nz - 1)) - 1;
+            const double dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
+            const double dla = rows[(size_t)PF_COUNT * m + PF_DUST_TESC] > SAFE_FLOOR ? rows[(size_t)PF_COUNT * m + PF_DUST_TESC] : 7.0;
+            int it = 0;
+            while (it < nt && c->log_age[it] <= dla) ++it;   // ages <= dust_tesc
+            it = std::max(1, std::min(it, nt));
+            double ls = 0.0, ly = 0.0, lo = 0.0;
+            for (int t = 0; t < nt; ++t) {
+                const double w = ssp_weights[(size_t)nt * m + t];
+                if (!(w > SAFE_FLOOR)) continue;
+                const double lk = w * std::pow(10.0, (1.0 - dz) * c->lbol[t + (size_t)nt * zlo] + dz * c->lbol[t + (size_t)nt * (zlo + 1)]);
+                ls += lk;
+                if (t + 1 <= it) ly += lk; else lo += lk;
+            }
+            if (lbol) lbol[m] = ls > SAFE_FLOOR ? std::log10(ls) : 0.0;
+            if (lbol_young) lbol_young[m] = std::log10(std::max(ly, SAFE_FLOOR));
+            if (lbol_old) lbol_old[m] = std::log10(std::max(lo, SAFE_FLOOR));
+        }
+    }
 }
 
 }  // namespace

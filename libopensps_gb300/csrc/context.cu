@@ -153,9 +153,9 @@ Context::~Context() {
         kv.second->lo.release();
         delete kv.second;
     }
-    d_pix.release(); d_cmat.release(); d_wl.release(); d_igm_a.release(); d_jr.release(); d_do_band.release();
+    d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
     d_lam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
-    d_wz.release(); d_params.release(); d_sums.release(); d_zshift.release(); d_dist.release(); d_fband.release();
+    d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
     d_status.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
@@ -244,8 +244,8 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
     const int ns = c.nspec;
     std::vector<double> wtl(ns, 0.0);
     for (int j = 0; j + 1 < ns; ++j) wtl[j] = 0.5 * std::fabs(c.lam[j + 1] - c.lam[j]);
-    std::vector<float> cm((size_t)nb * ns, 0.f);
-    std::vector<int> jr(2 * nb);
+    std::vector<double> cm((size_t)nb * ns, 0.0);
+    int j0 = ns, j1 = -1;
     for (int b = 0; b < nb; ++b) {
         const double *bd = c.bands.data() + (size_t)b * ns;
         int ilo = ns, ihi = -1;
@@ -253,23 +253,43 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
             if (bd[j] != 0.0) { ilo = std::min(ilo, j); ihi = std::max(ihi, j); }
         // trapezoid intervals touching the support: j = ilo - 1 .. ihi (0-based), last interval ns - 2
         int jlo = std::max(0, ilo - 1), jhi = std::min(ns - 2, ihi);
-        if (ilo > ihi) { jlo = 0; jhi = -1; }
+        if (ilo > ihi) continue;
         for (int j = 0; j < ns; ++j) {
             double cw = 0.0;
             if (j >= jlo && j <= jhi) cw += wtl[j];
             if (j - 1 >= jlo && j - 1 <= jhi) cw += wtl[j - 1];
-            cm[(size_t)b * ns + j] = (float)(bd[j] * cw);
+            cm[(size_t)b * ns + j] = bd[j] * cw;
         }
         // pixels whose weight can be nonzero: jlo .. jhi + 1
-        jr[2 * b] = jlo;
-        jr[2 * b + 1] = (jhi >= jlo) ? jhi + 1 : jlo - 1;
+        j0 = std::min(j0, jlo);
+        j1 = std::max(j1, jhi + 1);
     }
+    if (j1 < j0) { j0 = 0; j1 = -1; }
+    // the band GEMM's B operand: rows = bands (padded to npad), columns = pixels j0 .. j0 + 64 nkb - 1, bf16 hi + lo
+    const int npad = band_gemm_npad(nb);
+    if (npad > 256) { err = "more than 256 bands"; return ST_BAD_ARG; }
+    const int nkb = (j1 - j0 + 1 + 63) / 64, kpad = 64 * nkb;
+    std::vector<uint16_t> hi((size_t)npad * std::max(kpad, 64), 0), lo(hi.size(), 0);
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < kpad; ++k) {
+            const int j = j0 + k;
+            if (j >= ns) break;
+            const float f = (float)cm[(size_t)b * ns + j];
+            const uint16_t h = f32_to_bf16_bits(f);
+            hi[(size_t)b * kpad + k] = h;
+            lo[(size_t)b * kpad + k] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));
+        }
     cudaError_t e;
-    if ((e = upload(c.d_cmat, cm.data(), cm.size())) != cudaSuccess ||
-        (e = upload(c.d_jr, jr.data(), jr.size())) != cudaSuccess) {
-        err = std::string("device upload failed: ") + cudaGetErrorString(e);
+    if ((e = upload(c.d_cb_hi, reinterpret_cast<const __nv_bfloat16 *>(hi.data()), hi.size())) != cudaSuccess ||
+        (e = upload(c.d_cb_lo, reinterpret_cast<const __nv_bfloat16 *>(lo.data()), lo.size())) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&c.tm_cb_hi, c.d_cb_hi.p, std::max(kpad, 64), npad, 64, npad)) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&c.tm_cb_lo, c.d_cb_lo.p, std::max(kpad, 64), npad, 64, npad)) != cudaSuccess) {
+        err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
         return ST_BAD_ARG;
     }
+    c.band_j0 = j0;
+    c.band_nkb = nkb;
+    c.band_npad = npad;
     return 0;
 }
 

@@ -79,14 +79,19 @@ struct Context {
     // device copies
     int device = 0, num_sms = 0;
     cudaStream_t stream = nullptr;
-    DevBuf<float> d_pix, d_cmat, d_wl, d_igm_a;
-    DevBuf<int> d_jr, d_do_band;
+    DevBuf<float> d_pix, d_wl, d_igm_a;
+    DevBuf<int> d_do_band;
+    // band matrix of the band GEMM: bf16 hi / lo, band_npad rows x 64 band_nkb pixels from pixel band_j0
+    DevBuf<__nv_bfloat16> d_cb_hi, d_cb_lo;
+    CUtensorMap tm_cb_hi, tm_cb_lo;
+    int band_j0 = 0, band_nkb = 0, band_npad = 0;
     DevBuf<double> d_lam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
     double pix_minl = -1.0, pix_maxl = -1.0;   // smoothing range of the device pixel table
 
     // batch scratch
-    DevBuf<double> d_wz, d_params, d_sums, d_zshift, d_dist, d_fband, d_mags, d_spec64;
+    DevBuf<double> d_wz, d_params, d_sums, d_dist, d_fband, d_mags, d_spec64;
+    DevBuf<float4> d_zinfo;
     DevBuf<__nv_bfloat16> d_whi, d_wlo;
     DevBuf<float> d_mpar, d_spec;
     DevBuf<int> d_status;
@@ -128,6 +133,7 @@ struct BatchIO {
     bool dev_inputs = false;         // wz, dev_params and mags are device pointers; outputs stay on the device
     const double *dev_params = nullptr;   // PAR_DEVICE x n on the device (dev_inputs)
     bool dev_sync = true;            // dev_inputs: wait for the batch before returning
+    double *fband_dev = nullptr;     // device n x nbands band fluxes (the reverse pass), or null
     // outputs (host, may be null)
     double *mags = nullptr, *spec = nullptr, *mass = nullptr, *lbol = nullptr, *emlines = nullptr;
     double *young = nullptr, *old = nullptr, *mass_young = nullptr, *mass_old = nullptr, *lbol_young = nullptr,

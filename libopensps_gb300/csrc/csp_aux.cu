@@ -3,10 +3,6 @@
 // weights_prep: model_sums_zw (OpenSPS src/physics/opensps_csp_batch.f90:2090-2120) per model: the weights floored
 //   at SAFE_FLOOR, the FP64 mass and L_bol sums (young and old parts apart), and the weights cast once to the
 //   contraction's operand (bf16 hi + lo, in its K order).
-// bands: compute_magnitudes_columns (src/spectra/opensps_batch_photometry.f90:53-180) per model: the rest-frame
-//   spectrum resampled to the observed frame at the model's redshift (observed_frame_z :819-903), divided by lambda,
-//   the trapezoid filter integrals (band_fluxes :1049-1171, regrouped by pixel as the split-K form :1002-1044) and
-//   the AB magnitudes with the distance term (magnitudes_from_fluxes :185-232).
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cfloat>
@@ -71,75 +67,6 @@ cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st) {
     const int threads = 256, per_block = threads / 32;
     const int blocks = (a.n_models + per_block - 1) / per_block;
     weights_prep_kernel<<<blocks, threads, 0, st>>>(a);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------------------------- bands
-constexpr int BAND_THREADS = 256;
-
-__global__ void __launch_bounds__(BAND_THREADS) bands_kernel(BandArgs a) {
-    extern __shared__ float fobs[];   // nspec
-    const int m = blockIdx.x;
-    if (m >= a.n_models) return;
-    const float *s = a.spec + (size_t)m * a.ld_spec;
-    const double *zs = a.zshift + (size_t)m * 4;
-    const int n0 = (int)zs[0];
-    const float tin = (float)zs[1];
-    const double sh = zs[2];
-    const bool rest = zs[3] == 0.0;
-    const int ns = a.nspec;
-    const float em1 = (float)expm1(a.dlnl);
-    for (int j = threadIdx.x; j < ns; j += BAND_THREADS) {
-        float v;
-        if (rest) {
-            v = s[j];
-        } else {
-            // rest-frame interval il and position t of lambda_j / (1 + z) on the log-uniform grid
-            int il = j - n0 - (tin > 0.f ? 1 : 0);
-            float t = tin;
-            if (il < 0 || il > ns - 2) {
-                const int ilc = il < 0 ? 0 : ns - 2;
-                const double x = (double)(j - ilc) - sh;   // position relative to pixel ilc, in pixels
-                t = (float)(expm1(x * a.dlnl)) / em1;
-                il = ilc;
-            }
-            const float s0 = s[il], s1 = s[il + 1];
-            v = fmaf(t, s1 - s0, s0);
-        }
-        if (v != v) v = 0.f;
-        fobs[j] = fmaxf(v, 0.f) * a.wl[j];
-    }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int b = warp; b < a.nbands; b += BAND_THREADS / 32) {
-        const int j0 = a.jr[2 * b], j1 = a.jr[2 * b + 1];
-        const float *c = a.cmat + (size_t)b * ns;
-        float acc = 0.f;
-        for (int j = j0 + lane; j <= j1; j += 32) acc = fmaf(__ldg(c + j), fobs[j], acc);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        if (lane == 0) {
-            const double f = (double)acc;
-            if (a.fband) a.fband[(size_t)m * a.nbands + b] = f;
-            if (a.mags) {
-                double mg = __longlong_as_double(0x7ff8000000000000LL);
-                if (a.do_band == nullptr || a.do_band[b] != 0) {
-                    mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) - a.zp + a.dist[m];
-                }
-                a.mags[(size_t)m * a.nbands + b] = mg;
-            }
-        }
-    }
-}
-
-cudaError_t run_bands(const BandArgs &a, cudaStream_t st) {
-    if (a.n_models <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * a.nspec;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(bands_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    bands_kernel<<<a.n_models, BAND_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 

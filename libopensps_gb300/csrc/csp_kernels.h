@@ -63,23 +63,24 @@ struct WeightsArgs {
 };
 cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st);
 
-// Band fluxes (observed frame at each model's redshift, trapezoid filter integrals) and AB magnitudes.
-struct BandArgs {
-    int nspec, nbands, n_models, ld_spec;
+// Band fluxes (observed frame at each model's redshift, trapezoid filter integrals) and AB magnitudes, as a
+// tensor-core GEMM over the pixels any band reaches (band_gemm.cu).
+struct BandGemmArgs {
+    int n_models, nspec, nbands, npad, nkb, j0, ld_spec;
     const float *spec;      // n_models x ld_spec rest-frame spectra
-    const float *cmat;      // nbands x nspec: band(j) (wtl(j - 1) + wtl(j)), FP32
-    const int *jr;          // nbands x 2: first and last pixel of each band's nonzero weights (0-based)
+    const float4 *zinfo;    // n_models: (n0 as int bits, t of the interior interpolation, shift s in pixels, 0 at z = 0)
     const float *wl;        // nspec: 1 / lambda
-    const double *zshift;   // n_models x 4: n0 (floor of the shift), t of the interior interpolation, s (the shift
-                            // in pixels), z flag (0: rest frame)
     double dlnl;            // grid step in ln lambda
     const double *dist;     // n_models: distance term
     double zp;              // 48.60 + 2.5 ABS_MAG_ZEROPOINT_LOG
     const int *do_band;     // nbands
     double *fband;          // n_models x nbands (may be null)
     double *mags;           // n_models x nbands (may be null)
+    int *status;
 };
-cudaError_t run_bands(const BandArgs &a, cudaStream_t st);
+int band_gemm_npad(int nbands);
+cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
+                          cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

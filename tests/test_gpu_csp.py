@@ -71,3 +71,42 @@ def test_no_dust_is_sum_of_ssps(ctx, data):
     ref = np.einsum("mzt,zts->ms", wz, data["ssp_spec"])
     assert rel_err_spec(got["spec"], ref) <= 1e-4
     c.close()
+
+
+def test_twenty_filters(data, built_lib):
+    """The band GEMM with another band count (20 filters: 32 padded rows)."""
+    from libopensps_gb300.capi import Context
+    from oracle.oracle import Oracle
+    c = Context()
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    c.set_filters_library("gauss20")
+    assert c.nbands == 20
+    n = 70
+    wz, params = config3_inputs(n, seed=21)
+    _compare(c.csp_batch(params, ssp_weights_z=wz), Oracle(data, nbands=20).csp_batch(params, wz))
+    c.close()
+
+
+def test_weights_over_ages_blended_at_logzsol(ctx, oracle40, data):
+    """ssp_weights (one weight per age) with logzsol per model: the two bracketing metallicities, linear in the
+    spectra and the mass, log-linear in L_bol (compute_interpolated_ssp)."""
+    n = 33
+    rng = np.random.default_rng(17)
+    w = rng.dirichlet(np.ones(107), size=n)
+    logzsol = rng.uniform(-1.9, 0.4, n)
+    _, params = config3_inputs(n, seed=18)
+    params = dict(params, logzsol=logzsol)
+    got = ctx.csp_batch(params, ssp_weights=w)
+    lz = np.log10(data["zlegend"] / 0.0142)
+    wz = np.zeros((n, 12, 107))
+    lbol = np.empty(n)
+    for m in range(n):
+        zlo = min(max(np.searchsorted(lz, logzsol[m], side="right") - 1, 0), 10)
+        dz = (logzsol[m] - lz[zlo]) / (lz[zlo + 1] - lz[zlo])
+        wz[m, zlo] = (1 - dz) * w[m]
+        wz[m, zlo + 1] = dz * w[m]
+        lbol[m] = np.log10(np.sum(w[m] * 10.0 ** ((1 - dz) * data["ssp_lbol"][zlo] + dz * data["ssp_lbol"][zlo + 1])))
+    ora = oracle40.csp_batch({k: v for k, v in params.items() if k != "logzsol"}, wz)
+    ora["lbol"] = lbol
+    _compare(got, ora)
