@@ -48,16 +48,17 @@ __global__ void model_params_kernel(ModelParamArgs a) {
     float *o = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
     for (int i = 0; i < MODEL_PAR_FLOATS; ++i) o[i] = 0.f;
     const double d1 = p[PF_DUST1], d2 = p[PF_DUST2], d3 = p[PF_DUST3], fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
+    const double LOG2E = 1.4426950408889634;
     // attenuate_batch / pixel_transmissions (src/physics/opensps_csp_batch.f90:3576-3660, 3765-3818)
-    o[MP_DUST2] = (float)d2;
+    o[MP_KD2] = (float)(-d2 * LOG2E);
     if (1.0 - fnd <= SAFE_FLOOR) { o[MP_ONE_M_FND] = 0.f; o[MP_FND] = 1.f; }
     else { o[MP_ONE_M_FND] = (float)(1.0 - fnd); o[MP_FND] = (float)fnd; }
     o[MP_DUST_INDEX] = (float)p[PF_DUST_INDEX];
-    o[MP_DUST1] = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)d1;
+    o[MP_KD1] = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)(-d1 * LOG2E);
     o[MP_DUST1_INDEX] = (float)p[PF_DUST1_INDEX];
     o[MP_ONE_M_FO] = (float)(1.0 - fo);
     o[MP_FO] = (float)fo;
-    o[MP_DUST3] = (fabs(d3) <= SAFE_FLOOR) ? 0.f : (float)d3;
+    o[MP_KD3] = (fabs(d3) <= SAFE_FLOOR) ? 0.f : (float)(-d3 * LOG2E);
     // IGM (apply_igm_z :4205-4299): redshift factors and the short-wavelength cap
     const double z = p[PF_ZRED];
     o[MP_IGM_JMAX] = __int_as_float(0);
@@ -78,9 +79,9 @@ __global__ void model_params_kernel(ModelParamArgs a) {
             const float t = ia[0] * b[0] + ia[1] * b[1] + ia[2] * b[2] + ia[3] * b[3] + ia[4] * b[4] + ia[5] * b[5];
             if (t > tmax) { tmax = t; jmax = j + 1; }
         }
-        for (int k = 0; k < 6; ++k) o[MP_IGM_B + k] = b[k];
-        o[MP_IGM_FACTOR] = (float)p[PF_IGM_FACTOR];
-        o[MP_IGM_TMAX] = tmax;
+        const double kf = -p[PF_IGM_FACTOR] * LOG2E;
+        for (int k = 0; k < 6; ++k) o[MP_IGM_KB + k] = (float)((double)b[k] * kf);
+        o[MP_IGM_KCAP] = (float)((double)tmax * kf);
         o[MP_IGM_JMAX] = __int_as_float(jmax);
         o[MP_IGM_ON] = 1.f;
     }
@@ -222,6 +223,7 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
     }
     const int kpad = op->kpad;
     std::vector<uint16_t> hi((size_t)ns * kpad, 0), lo((size_t)ns * kpad, 0);
+    std::vector<int> kmap(kpad, -1);   // operand column -> source index t + nt z, bit 30: a young age
     for (int k = 0; k < kpad; ++k) {
         int t = -1, z = -1;
         if (nacc == 1) {
@@ -233,6 +235,7 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
             if (nto > 0 && kk < nto * nz) { t = itesc + kk % nto; z = kk / nto; }
         }
         if (t < 0) continue;
+        kmap[k] = (t + nt * z) | ((t < itesc) ? 0x40000000 : 0);
         const double *col = b.data() + (size_t)ns * (t + (size_t)nt * z);
         for (int j = 0; j < ns; ++j) {
             const float f = (float)col[j];
@@ -245,10 +248,12 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
     if ((e = op->hi.reserve(hi.size())) != cudaSuccess || (e = op->lo.reserve(lo.size())) != cudaSuccess ||
         (e = cudaMemcpy(op->hi.p, hi.data(), hi.size() * 2, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(op->lo.p, lo.data(), lo.size() * 2, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = op->kmap.reserve(kpad)) != cudaSuccess ||
+        (e = cudaMemcpy(op->kmap.p, kmap.data(), sizeof(int) * kpad, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = encode_tmap_2d_bf16(&op->tm_hi, op->hi.p, kpad, ns, BK, contract_bm())) != cudaSuccess ||
         (e = encode_tmap_2d_bf16(&op->tm_lo, op->lo.p, kpad, ns, BK, contract_bm())) != cudaSuccess) {
         err = std::string("basis operand: ") + cudaGetErrorString(e);
-        op->hi.release(); op->lo.release();
+        op->hi.release(); op->lo.release(); op->kmap.release();
         delete op;
         return nullptr;
     }
@@ -364,15 +369,21 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     BasisOperand *bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
     if (!bop) return ST_DATA_MISSING;
 
-    // ---- per-pixel table (rebuilt when the smoothing range changes)
-    if (!(c.d_pix.p && c.pix_minl == minl && c.pix_maxl == maxl)) {
+    // ---- per-pixel table (rebuilt when the batch's shared dust_index changes): ln(lambda / 5500) log2(e), the
+    // diffuse curve (lambda / 5500)^dust_index in FP64 (exp_kp of the reference: the argument formed in FP64), the
+    // Madau wavelength factors
+    const double idx0 = par(0, PF_DUST_INDEX);
+    bool uniform_index = true;
+    for (int m = 1; m < n && uniform_index; ++m) uniform_index = par(m, PF_DUST_INDEX) == idx0;
+    if (!c.d_pix.p || (uniform_index && c.pix_index != idx0)) {
         std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
         for (int j = 0; j < ns; ++j) {
             float *px = pix.data() + (size_t)j * PIX_FLOATS;
-            px[PIX_LTAB] = (float)std::log(c.lam[j] / 5500.0);
+            const double ltab = std::log(c.lam[j] / 5500.0);
+            px[PIX_LTAB2] = (float)(ltab * 1.4426950408889634);
+            px[PIX_CURVE] = (float)(idx0 != 0.0 ? std::exp(idx0 * ltab) : 1.0);
             if (j < c.jtop)
                 for (int k = 0; k < 6; ++k) px[PIX_IGM_A + k] = c.igm_a[(size_t)j * 6 + k];
-            px[PIX_SMOOTH] = (c.lam[j] >= minl && c.lam[j] <= maxl) ? 1.f : 0.f;
         }
         cudaError_t e;
         if ((e = c.d_pix.reserve(pix.size())) != cudaSuccess ||
@@ -380,9 +391,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("pixel table", e);
             return ST_DATA_MISSING;
         }
-        c.pix_minl = minl;
-        c.pix_maxl = maxl;
+        c.pix_index = idx0;
     }
+    // the smoothed pixels: lambda within [min_wave_smooth, max_wave_smooth]
+    int sm_lo = ns, sm_hi = -1;
+    for (int j = 0; j < ns; ++j)
+        if (c.lam[j] >= minl && c.lam[j] <= maxl) { sm_lo = std::min(sm_lo, j); sm_hi = std::max(sm_hi, j); }
 
     // ---- scratch
     const int bn = contract_models_per_tile(nacc);
@@ -424,9 +438,10 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
 
     // ---- weights
     WeightsArgs wa;
-    wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.nty_young = bop->nty; wa.ky_pad = bop->ky_pad;
+    wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.kmap = bop->kmap.p;
     wa.wz = d_wz; wa.mass = c.d_mass.p; wa.llin = c.d_llin.p; wa.w_hi = c.d_whi.p; wa.w_lo = c.d_wlo.p;
-    wa.sums = c.d_sums.p; wa.itesc = itesc;
+    wa.sums = c.d_sums.p;
+    wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     prof_mark(c, 0);
     if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 1);
@@ -457,6 +472,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
     ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
     ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
+    ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);

@@ -151,6 +151,7 @@ Context::~Context() {
     for (auto &kv : basis_cache) {
         kv.second->hi.release();
         kv.second->lo.release();
+        kv.second->kmap.release();
         delete kv.second;
     }
     d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
@@ -385,7 +386,7 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         return ST_DATA_MISSING;
     }
     c.d_pix.release();   // rebuilt by the next batch (smoothing range)
-    c.pix_minl = c.pix_maxl = -1.0;
+    c.pix_index = -1e300;
     int st = context_load_filters(c, c.filter_set, err);
     if (st != 0) return st;
     for (auto &kv : c.basis_cache) { kv.second->hi.release(); kv.second->lo.release(); delete kv.second; }

@@ -53,6 +53,7 @@ struct DevBuf {
 struct BasisOperand {
     int nacc = 0, itesc = 0, kpad = 0, ky_pad = 0, nty = 0;
     DevBuf<__nv_bfloat16> hi, lo;
+    DevBuf<int> kmap;            // operand column -> source (age, metallicity) of the weights, bit 30: young
     CUtensorMap tm_hi, tm_lo;
 };
 
@@ -87,7 +88,7 @@ struct Context {
     int band_j0 = 0, band_nkb = 0, band_npad = 0;
     DevBuf<double> d_lam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
-    double pix_minl = -1.0, pix_maxl = -1.0;   // smoothing range of the device pixel table
+    double pix_index = -1e300;   // dust_index of the device pixel table's curve
 
     // batch scratch
     DevBuf<double> d_wz, d_params, d_sums, d_dist, d_fband, d_mags, d_spec64;

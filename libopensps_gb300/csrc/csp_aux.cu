@@ -1,8 +1,8 @@
-// The prologue and photometry kernels of the batched CSP path.
+// The prologue kernels of the batched CSP path.
 //
 // weights_prep: model_sums_zw (OpenSPS src/physics/opensps_csp_batch.f90:2090-2120) per model: the weights floored
-//   at SAFE_FLOOR, the FP64 mass and L_bol sums (young and old parts apart), and the weights cast once to the
-//   contraction's operand (bf16 hi + lo, in its K order).
+//   at SAFE_FLOOR, the FP64 mass and L_bol sums (young and old parts apart when asked), and the weights cast once to
+//   the contraction's operand (bf16 hi + lo, in its K order, through the operand's column map).
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cfloat>
@@ -12,34 +12,29 @@
 namespace sps {
 
 // ---------------------------------------------------------------------------------------------- weights
-__global__ void weights_prep_kernel(WeightsArgs a) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One warp per model; lane l takes operand columns l, l + 32, ...
+template <bool PARTS>
+__global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
+    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= a.n_models) return;
-    const int m = warp;
-    const int ntz = a.nt * a.nz;
-    const double *w = a.wz + (size_t)m * ntz;
-    double ms = 0.0, ls = 0.0, msy = 0.0, mso = 0.0, lsy = 0.0, lso = 0.0;
+    if (m >= a.n_models) return;
+    const double *w = a.wz + (size_t)m * a.nt * a.nz;
+    double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
     __nv_bfloat16 *hi = a.w_hi + (size_t)m * a.kpad, *lo = a.w_lo + (size_t)m * a.kpad;
-    const int nty = a.nty_young, nto = a.nt - a.nty_young;
+#pragma unroll 4
     for (int k = lane; k < a.kpad; k += 32) {
-        // the (age, metallicity) of operand column k
-        int t = -1, z = -1;
-        if (nty == 0) {
-            if (k < ntz) { t = k % a.nt; z = k / a.nt; }
-        } else if (k < a.ky_pad) {
-            if (k < nty * a.nz) { t = k % nty; z = k / nty; }
-        } else {
-            const int kk = k - a.ky_pad;
-            if (nto > 0 && kk < nto * a.nz) { t = nty + kk % nto; z = kk / nto; }
-        }
+        const int code = __ldg(a.kmap + k);
         float wf = 0.f;
-        if (t >= 0) {
-            double wv = w[t + a.nt * z];
+        if (code >= 0) {
+            const int src = code & 0x3fffffff;
+            const double wv = w[src];
             if (wv > DBL_MIN) {
-                const double mk = wv * a.mass[t + a.nt * z], lk = wv * a.llin[t + a.nt * z];
-                ms += mk; ls += lk;
-                if (t + 1 <= a.itesc) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
+                const double mk = wv * __ldg(a.mass + src), lk = wv * __ldg(a.llin + src);
+                ms += mk;
+                ls += lk;
+                if (PARTS) {
+                    if (code & 0x40000000) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
+                }
                 wf = (float)wv;
             }
         }
@@ -51,14 +46,17 @@ __global__ void weights_prep_kernel(WeightsArgs a) {
     for (int off = 16; off > 0; off >>= 1) {
         ms += __shfl_xor_sync(0xffffffffu, ms, off);
         ls += __shfl_xor_sync(0xffffffffu, ls, off);
-        msy += __shfl_xor_sync(0xffffffffu, msy, off);
-        mso += __shfl_xor_sync(0xffffffffu, mso, off);
-        lsy += __shfl_xor_sync(0xffffffffu, lsy, off);
-        lso += __shfl_xor_sync(0xffffffffu, lso, off);
+        if (PARTS) {
+            msy += __shfl_xor_sync(0xffffffffu, msy, off);
+            lsy += __shfl_xor_sync(0xffffffffu, lsy, off);
+            mso += __shfl_xor_sync(0xffffffffu, mso, off);
+            lso += __shfl_xor_sync(0xffffffffu, lso, off);
+        }
     }
     if (lane == 0 && a.sums) {
         double *o = a.sums + (size_t)m * 6;
-        o[0] = ms; o[1] = ls; o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso;
+        o[0] = ms; o[1] = ls;
+        if (PARTS) { o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso; }
     }
 }
 
@@ -66,7 +64,8 @@ cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st) {
     if (a.n_models <= 0) return cudaSuccess;
     const int threads = 256, per_block = threads / 32;
     const int blocks = (a.n_models + per_block - 1) / per_block;
-    weights_prep_kernel<<<blocks, threads, 0, st>>>(a);
+    if (a.parts) weights_prep_kernel<true><<<blocks, threads, 0, st>>>(a);
+    else weights_prep_kernel<false><<<blocks, threads, 0, st>>>(a);
     return cudaGetLastError();
 }
 

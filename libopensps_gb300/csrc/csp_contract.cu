@@ -13,8 +13,13 @@
 // pixels x BN models x 64 K per stage; the 128 pixel rows of a tile are 120 output pixels with a halo of 4 on each
 // side for the smoothing. One CTA per SM, persistent over tiles (model tile outer, pixel tile inner, so that the
 // CTAs running together share the weights of a model tile in L2). Warp roles: warp 0 = TMA producer, warp 1 = MMA
-// issuer (and TMEM owner), warps 2..5 = epilogue (TMEM lanes 32 (warp % 4) ..). Accumulators are double-buffered in
-// TMEM so that the epilogue of a tile overlaps the MMAs of the next.
+// issuer (and TMEM owner), warps 2..9 = epilogue in two groups of four (group g takes the models of column half g;
+// in a group, warp w reads TMEM lanes 32 (w % 4) ..). Accumulators are double-buffered in TMEM so that the
+// epilogue of a tile overlaps the MMAs of the next.
+//
+// Epilogue of a chunk of 16 models, per group: phase 1, thread = pixel row: the attenuated, IGM-absorbed spectrum
+// of the 16 models into a staging tile; phase 2, thread = 4 consecutive output pixels of one model: the velocity
+// smoothing (taps in registers) and the store.
 //
 // NACC = 1: one accumulator (no birth-cloud or old-star screen in the batch: young and old are only ever summed).
 // NACC = 2: young and old accumulators (the K range is ordered young block first, then old block).
@@ -31,9 +36,11 @@ constexpr int BK = 64;           // K per stage (one 128-byte swizzled row of bf
 constexpr int HALO = 4;          // smoothing halo (taps -4 .. 4)
 constexpr int OUT_ROWS = BM - 2 * HALO;
 constexpr int NSTAGE = 2;
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_GROUPS = 2;
+constexpr int EPI_WARPS = 4 * EPI_GROUPS;
 constexpr int NTHREADS = (2 + EPI_WARPS) * 32;
-constexpr int TROW = BM + 4;     // epilogue staging row (floats), padded
+constexpr int CHUNK = 16;        // models per epilogue chunk
+constexpr int TROW = BM + 4;     // staging row (floats): 16-byte aligned rows, and room for the phase-2 reads
 
 template <int NACC>
 struct ContractCfg {
@@ -43,13 +50,33 @@ struct ContractCfg {
     static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
     static constexpr int ACC_COLS = NACC * BN;                    // TMEM columns of one accumulator set
     static constexpr int TMEM_COLS = 2 * ACC_COLS;                // double-buffered (= 512)
-    static constexpr int STAGE_T_BYTES = 32 * TROW * 4;           // epilogue staging, 32 models
-    static constexpr int PAR_BYTES = 2 * 32 * MODEL_PAR_FLOATS * 4;
-    static constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + STAGE_T_BYTES + PAR_BYTES + 256 + 1024;
+    static constexpr int GROUP_COLS = BN / EPI_GROUPS;            // models per epilogue group
+    static constexpr int STAGE_T_FLOATS = CHUNK * TROW;           // per group
+    static constexpr int PAR_FLOATS = 2 * CHUNK * MODEL_PAR_FLOATS;   // per group, double-buffered
+    static constexpr int EPI_BYTES = EPI_GROUPS * (STAGE_T_FLOATS + PAR_FLOATS) * 4;
+    static constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + EPI_BYTES + 256 + 1024;
     static constexpr uint32_t IDESC = idesc_bf16_f32(BM, BN);
 };
 
-__device__ __forceinline__ float fast_exp(float x) { return exp2f(x * 1.4426950408889634f); }
+// 2^x by the SFU (relative error ~2^-22; flushes results below the smallest normal to zero).
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
 
 template <int NACC>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -60,9 +87,8 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *stage_base = smem;
-    float *stageT = reinterpret_cast<float *>(smem + NSTAGE * C::STAGE_BYTES);
-    float *parbuf = reinterpret_cast<float *>(smem + NSTAGE * C::STAGE_BYTES + C::STAGE_T_BYTES);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * C::STAGE_BYTES + C::STAGE_T_BYTES + C::PAR_BYTES);
+    float *epi_base = reinterpret_cast<float *>(smem + NSTAGE * C::STAGE_BYTES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * C::STAGE_BYTES + C::EPI_BYTES);
     uint64_t *full = bars;                 // [NSTAGE]
     uint64_t *empty = bars + NSTAGE;       // [NSTAGE]
     uint64_t *tfull = bars + 2 * NSTAGE;   // [2]
@@ -157,10 +183,17 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
             mbar_wait(mma_done, 0, status, ERR_TIMEOUT_MMA, false);
         }
     } else {
-        // ------------------------------------------------------------------ epilogue (warps 2..5)
+        // ------------------------------------------------------------------ epilogue (warps 2..9)
+        const int ew = warp - 2;                // 0..7
+        const int g = ew >> 2;                  // group: column half
+        const int wg = ew & 3;                  // warp within the group (phase 2: models 4 wg .. 4 wg + 3)
         const int q = warp & 3;                 // TMEM lane quarter this warp may access
-        const int r = q * 32 + lane;            // pixel row of the tile
-        const int et = threadIdx.x - 64;        // 0..127
+        const int r = q * 32 + lane;            // pixel row of the tile (phase 1)
+        const int et = wg * 32 + lane;          // 0..127 within the group
+        const int bar_id = 1 + g;
+        float *stageT = epi_base + g * (C::STAGE_T_FLOATS + C::PAR_FLOATS);
+        float *parbuf = stageT + C::STAGE_T_FLOATS;
+        const bool vec_store = (args.ld_spec & 1) == 0;
         int acc = 0; uint32_t aph = 0;
         int pb = 0;
         for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
@@ -168,97 +201,131 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
             const int p0 = pt * OUT_ROWS - HALO, m0 = mt * C::BN;
             const int p = p0 + r;
             const bool inpix = (p >= 0 && p < args.nspec);
-            // per-pixel data
-            float ltab = 0.f, ia[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            bool sm_active = false;
+            // per-pixel data of this thread's row (phase 1)
+            float ltab2 = 0.f, curve_u = 1.f, ia[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (inpix) {
-                const float *px = args.pix + (size_t)p * PIX_FLOATS;
-                ltab = px[PIX_LTAB];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) ia[k] = px[PIX_IGM_A + k];
-                sm_active = px[PIX_SMOOTH] != 0.f;
+                const float4 *px = reinterpret_cast<const float4 *>(args.pix + (size_t)p * PIX_FLOATS);
+                const float4 v0 = px[0], v1 = px[1];
+                ltab2 = v0.x; curve_u = v0.y; ia[0] = v0.z; ia[1] = v0.w;
+                ia[2] = v1.x; ia[3] = v1.y; ia[4] = v1.z; ia[5] = v1.w;
             }
-            const bool out_row = (r >= HALO && r < BM - HALO && inpix);
             const bool igm_pix = inpix && p < args.jtop;
 
             mbar_wait(&tfull[acc], aph, status, ERR_TIMEOUT_EPILOGUE);
-            // all epilogue threads agree on whether to go on (a thread that gave up set the status first)
-            named_bar_sync(1, 128);
+            // the group agrees on whether to go on (a thread that gave up set the status first)
+            named_bar_sync(bar_id, 128);
             if (*(volatile int *)status != 0) break;
             tc_fence_after();
             const uint32_t t_row = tmem_base + ((uint32_t)(q * 32) << 16) + acc * C::ACC_COLS;
 
-            for (int c = 0; c < C::BN / 32; ++c) {
-                // model parameters of this chunk of 32 models (double-buffered)
-                float *par = parbuf + pb * 32 * MODEL_PAR_FLOATS;
-                for (int i = et; i < 32 * MODEL_PAR_FLOATS; i += 128) {
-                    const int mm = m0 + c * 32 + i / MODEL_PAR_FLOATS;
-                    par[i] = (mm < args.n_models) ? args.mpar[(size_t)mm * MODEL_PAR_FLOATS + (i % MODEL_PAR_FLOATS)] : 0.f;
+            for (int c = 0; c < C::GROUP_COLS / CHUNK; ++c) {
+                const int col0 = g * C::GROUP_COLS + c * CHUNK;      // first model of the chunk in the tile
+                // model parameters of the chunk (double-buffered)
+                float *par = parbuf + pb * CHUNK * MODEL_PAR_FLOATS;
+                for (int i = et; i < CHUNK * MODEL_PAR_FLOATS / 4; i += 128) {
+                    const int mm = m0 + col0 + (i * 4) / MODEL_PAR_FLOATS;
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (mm < args.n_models)
+                        v = reinterpret_cast<const float4 *>(args.mpar + (size_t)mm * MODEL_PAR_FLOATS)[(i * 4) % MODEL_PAR_FLOATS / 4];
+                    reinterpret_cast<float4 *>(par)[i] = v;
                 }
-                float y[32];
-                tmem_ld32(t_row + c * 32, y);
-                float o[32];
+                float y[16];
+                tmem_ld16(t_row + col0, y);
+                float o[16];
                 if constexpr (NACC == 2) {
-                    tmem_ld32(t_row + C::BN + c * 32, o);
+                    tmem_ld16(t_row + C::BN + col0, o);
                     if (args.nkb_young == 0) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) y[j] = 0.f;
+                        for (int j = 0; j < 16; ++j) y[j] = 0.f;
                     }
                     if (args.nkb_old == 0) {
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) o[j] = 0.f;
+                        for (int j = 0; j < 16; ++j) o[j] = 0.f;
                     }
                 }
-                if (c == C::BN / 32 - 1) {
-                    // all of this accumulator has been read: hand it back to the MMA warp
+                if (c == C::GROUP_COLS / CHUNK - 1) {
+                    // all of this group's accumulator columns have been read: hand them back to the MMA warp
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[acc]);
                 }
-                named_bar_sync(1, 128);
+                named_bar_sync(bar_id, 128);
+                // ---- phase 1: thread = pixel row r, 16 models
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
+                for (int j = 0; j < 16; ++j) {
                     const float *mp = par + j * MODEL_PAR_FLOATS;
-                    const float ed = mp[MP_DUST_INDEX];
-                    const float curve = (ed != 0.f) ? fast_exp(ed * ltab) : 1.f;
-                    const float td = fast_exp(-mp[MP_DUST2] * curve);
+                    const float4 d0 = *reinterpret_cast<const float4 *>(mp);          // kd2, 1-fnd, fnd, index
+                    const float curve = args.uniform_index ? curve_u : ex2(d0.w * ltab2);
                     float ss;
                     if constexpr (NACC == 2) {
-                        float tb = 1.f, to = 1.f;
-                        if (mp[MP_DUST1] != 0.f) tb = fast_exp(-mp[MP_DUST1] * fast_exp(mp[MP_DUST1_INDEX] * ltab));
-                        if (mp[MP_DUST3] != 0.f) to = fast_exp(-mp[MP_DUST3] * curve);
-                        ss = (y[j] * tb * mp[MP_ONE_M_FO] + y[j] * mp[MP_FO]) + o[j] * to;
+                        const float4 d1 = *reinterpret_cast<const float4 *>(mp + 4);  // kd1, d1 index, 1-fo, fo
+                        const float kd3 = mp[MP_KD3];
+                        const float tb = (d1.x != 0.f) ? ex2(d1.x * ex2(d1.y * ltab2)) : 1.f;
+                        const float to = (kd3 != 0.f) ? ex2(kd3 * curve) : 1.f;
+                        ss = (y[j] * tb * d1.z + y[j] * d1.w) + o[j] * to;
                     } else {
                         ss = y[j];
                     }
-                    float tot = ss * (td * mp[MP_ONE_M_FND] + mp[MP_FND]);
-                    if (igm_pix && mp[MP_IGM_ON] != 0.f) {
-                        const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
-                        float tau;
-                        if (p < jmax) tau = mp[MP_IGM_TMAX];
-                        else tau = ia[0] * mp[MP_IGM_B + 0] + ia[1] * mp[MP_IGM_B + 1] + ia[2] * mp[MP_IGM_B + 2] +
-                                   ia[3] * mp[MP_IGM_B + 3] + ia[4] * mp[MP_IGM_B + 4] + ia[5] * mp[MP_IGM_B + 5];
-                        tot *= fast_exp(-tau * mp[MP_IGM_FACTOR]);
+                    float tot = ss * fmaf(ex2(d0.x * curve), d0.y, d0.z);
+                    if (igm_pix) {
+                        const float4 g0 = *reinterpret_cast<const float4 *>(mp + MP_IGM_ON);   // on, jmax, kcap, kd3
+                        if (g0.x != 0.f) {
+                            float arg;
+                            if (p < __float_as_int(g0.y)) {
+                                arg = g0.z;
+                            } else {
+                                const float4 g1 = *reinterpret_cast<const float4 *>(mp + MP_IGM_KB);   // kb0..kb3
+                                const float2 g2 = *reinterpret_cast<const float2 *>(mp + MP_IGM_KB + 4);  // kb4, kb5
+                                arg = ia[0] * g1.x + ia[1] * g1.y + ia[2] * g1.z + ia[3] * g1.w + ia[4] * g2.x +
+                                      ia[5] * g2.y;
+                            }
+                            tot *= ex2(arg);
+                        }
                     }
                     stageT[j * TROW + r] = tot;
                 }
-                named_bar_sync(1, 128);
-                if (out_row) {
-#pragma unroll 4
-                    for (int j = 0; j < 32; ++j) {
-                        const int mm = m0 + c * 32 + j;
-                        if (mm >= args.n_models) break;
+                named_bar_sync(bar_id, 128);
+                // ---- phase 2: warp wg takes models 4 wg .. 4 wg + 3; lane l the output rows 4 + 4l .. 7 + 4l
+                if (lane < OUT_ROWS / 4) {
+                    const int row0 = HALO + 4 * lane;
+                    const int pq = p0 + row0;                      // first output pixel of this lane
+#pragma unroll 1
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const int j = wg * 4 + jj;
+                        const int mm = m0 + col0 + j;
+                        if (mm >= args.n_models || pq >= args.nspec) continue;
                         const float *mp = par + j * MODEL_PAR_FLOATS;
-                        const float *row = stageT + j * TROW + r;
-                        float v = row[0];
+                        const float *row = stageT + j * TROW + row0 - HALO;   // 16-byte aligned
+                        const float4 w0 = *reinterpret_cast<const float4 *>(row);
+                        const float4 w1 = *reinterpret_cast<const float4 *>(row + 4);
+                        const float4 w2 = *reinterpret_cast<const float4 *>(row + 8);
+                        const float win[12] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y, w2.z, w2.w};
+                        float out[4] = {win[4], win[5], win[6], win[7]};
                         const int R = __float_as_int(mp[MP_SMOOTH_R]);
-                        if (R >= 0 && sm_active) {
-                            float s = 0.f;
+                        if (R >= 0 && pq + 3 >= args.sm_lo && pq <= args.sm_hi) {
+                            const float4 ta = *reinterpret_cast<const float4 *>(mp + MP_TAPS);
+                            const float4 tb = *reinterpret_cast<const float4 *>(mp + MP_TAPS + 4);
+                            const float tc = mp[MP_TAPS + 8];
+                            const float tap[9] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w, tc};
 #pragma unroll
-                            for (int d = -HALO; d <= HALO; ++d) s = fmaf(mp[MP_TAPS + HALO + d], row[d], s);
-                            v = s;
+                            for (int u = 0; u < 4; ++u) {
+                                const int pu = pq + u;
+                                if (pu < args.sm_lo || pu > args.sm_hi) continue;
+                                float s = 0.f;
+#pragma unroll
+                                for (int d = 0; d < 9; ++d) s = fmaf(tap[d], win[u + d], s);
+                                out[u] = s;
+                            }
                         }
-                        args.spec[(size_t)mm * args.ld_spec + p] = v;
+                        float *dst = args.spec + (size_t)mm * args.ld_spec + pq;
+                        if (vec_store && pq + 3 < args.nspec) {
+                            reinterpret_cast<float2 *>(dst)[0] = make_float2(out[0], out[1]);
+                            reinterpret_cast<float2 *>(dst)[1] = make_float2(out[2], out[3]);
+                        } else {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (pq + u < args.nspec) dst[u] = out[u];
+                        }
                     }
                 }
                 pb ^= 1;

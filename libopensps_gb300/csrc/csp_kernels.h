@@ -15,23 +15,35 @@ enum {
     ERR_TIMEOUT_BAND = 0x104,
 };
 
-// Per-pixel table (floats per pixel): ln(lambda / 5500 A), the six Madau wavelength factors a_k, smoothing on/off.
-enum { PIX_LTAB = 0, PIX_IGM_A = 1, PIX_SMOOTH = 7, PIX_FLOATS = 8 };
+// Per-pixel table (floats per pixel): ln(lambda / 5500 A) log2(e), the diffuse curve (lambda / 5500)^dust_index of
+// the batch's shared dust_index (used when uniform_index), the six Madau wavelength factors a_k.
+enum { PIX_LTAB2 = 0, PIX_CURVE = 1, PIX_IGM_A = 2, PIX_FLOATS = 8 };
 
-// Per-model parameter block (floats), written by the model-parameter prologue.
+// Per-model parameter block (floats), written by the model-parameter prologue; exponents are pre-scaled by
+// log2(e) so that every transmission is one exp2. Groups of four start on 16-byte boundaries (vector loads).
 enum {
-    MP_DUST2 = 0, MP_ONE_M_FND, MP_FND, MP_DUST_INDEX, MP_DUST1, MP_DUST1_INDEX, MP_ONE_M_FO, MP_FO, MP_DUST3,
-    MP_IGM_B,                      // 6 redshift factors b_k(1 + z)
-    MP_IGM_FACTOR = MP_IGM_B + 6,  // 15
-    MP_IGM_TMAX, MP_IGM_JMAX,      // capped optical depth and the (1-based) pixel of the maximum (int bits)
-    MP_IGM_ON,                     // 18
-    MP_SMOOTH_R,                   // smoothing half-width in pixels (int bits), -1: none
-    MP_TAPS,                       // 9 normalised taps, offsets -4 .. 4 (zero beyond R)
+    MP_KD2 = 0,          // -dust2 log2(e):            T_diffuse = exp2(MP_KD2 curve)
+    MP_ONE_M_FND = 1,    // 1 - frac_nodust (0 when frac_nodust = 1)
+    MP_FND = 2,          // frac_nodust (1 when frac_nodust = 1)
+    MP_DUST_INDEX = 3,   // dust_index (curve = exp2(dust_index ln(lambda/5500) log2 e) when not uniform)
+    MP_KD1 = 4,          // -dust1 log2(e) (0: no birth-cloud screen)
+    MP_DUST1_INDEX = 5,
+    MP_ONE_M_FO = 6,     // 1 - frac_obrun
+    MP_FO = 7,           // frac_obrun
+    MP_IGM_ON = 8,       // 1: IGM for this model
+    MP_IGM_JMAX = 9,     // (1-based) pixel of the maximum optical depth (int bits): pixels below are capped
+    MP_IGM_KCAP = 10,    // -tmax igm_factor log2(e)
+    MP_KD3 = 11,         // -dust3 log2(e) (0: no old-star screen)
+    MP_IGM_KB = 12,      // 6 redshift factors b_k(1 + z) times -igm_factor log2(e) (12..17)
+    MP_SMOOTH_R = 18,    // smoothing half-width in pixels (int bits), -1: none
+    MP_TAPS = 20,        // 9 normalised taps, offsets -4 .. 4 (zero beyond R)
     MODEL_PAR_FLOATS = 32
 };
 
 struct ContractArgs {
     int nspec, n_models, n_ptiles, n_mtiles, nkb_young, nkb_old, jtop, ld_spec;
+    int sm_lo, sm_hi;    // pixels smoothed (lambda within [min_wave_smooth, max_wave_smooth]); sm_lo > sm_hi: none
+    int uniform_index;   // every model has the dust_index of the pixel table's curve
     const float *pix;    // nspec x PIX_FLOATS
     const float *mpar;   // n_models x MODEL_PAR_FLOATS
     float *spec;         // n_models x ld_spec (pixel fastest)
@@ -53,13 +65,14 @@ cudaError_t run_contract(int nacc, const ContractPlan &pl, const ContractArgs &a
 // Weights prologue: FP64 weights (ntfull x nz per model) -> bf16 hi / lo in the contraction's K order, and the FP64
 // per-model sums (mass, L_bol linear, young and old parts).
 struct WeightsArgs {
-    int n_models, nt, nz, kpad, nty_young, ky_pad;   // nty_young: ages in the young block (NACC = 2); 0 for NACC = 1
+    int n_models, nt, nz, kpad;
+    const int *kmap;        // kpad: source index t + nt z of operand column k (bit 30 set: a young age), -1: padding
     const double *wz;       // n_models x (nt x nz), age fastest
     const double *mass;     // nt x nz
     const double *llin;     // nt x nz: 10^log L_bol
     __nv_bfloat16 *w_hi, *w_lo;   // n_models x kpad
     double *sums;           // n_models x 6: mass, lsum, mass_young, mass_old, lsum_young, lsum_old
-    int itesc;              // ages <= itesc (1-based count) are young
+    int parts;              // also the young and old sums
 };
 cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st);
 

@@ -50,7 +50,8 @@ def test_birth_cloud_and_old_screen(ctx, oracle40):
     wz, params = config3_inputs(n, seed=7)
     rng = np.random.default_rng(8)
     params = dict(params, dust1=rng.uniform(0.0, 2.0, n), dust3=rng.uniform(0.0, 0.5, n),
-                  frac_obrun=rng.uniform(0.0, 0.3, n), frac_nodust=rng.uniform(0.0, 0.2, n))
+                  frac_obrun=rng.uniform(0.0, 0.3, n), frac_nodust=rng.uniform(0.0, 0.2, n),
+                  dust_index=rng.uniform(-1.2, -0.3, n), dust1_index=rng.uniform(-1.5, -0.5, n))
     _compare(ctx.csp_batch(params, ssp_weights_z=wz), oracle40.csp_batch(params, wz))
 
 
