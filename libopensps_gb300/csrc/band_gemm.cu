@@ -61,6 +61,11 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     const uint32_t tmem = *tmem_slot;
     const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
     const float em1 = expm1f((float)a.dlnl);
+    // the observed-frame shift of the CTA's models (w = 2: no model in this row)
+    __shared__ float4 zsm[BG_M];
+    for (int i = tid; i < BG_M; i += BG_THREADS)
+        zsm[i] = (m0 + i < a.n_models) ? a.zinfo[m0 + i] : make_float4(0.f, 0.f, 0.f, 2.f);
+    __syncthreads();
 
     // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
     for (int kb = 0; kb < a.nkb; ++kb) {
@@ -74,44 +79,50 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         }
         const int j = a.j0 + kb * BG_K + 2 * lane;       // observed pixel of this lane (and j + 1)
         float wl0 = 0.f, wl1 = 0.f;
-        if (j < a.nspec) wl0 = a.wl[j];
-        if (j + 1 < a.nspec) wl1 = a.wl[j + 1];
+        if (j < a.nspec) wl0 = __ldg(a.wl + j);
+        if (j + 1 < a.nspec) wl1 = __ldg(a.wl + j + 1);
+        // all 16 rows' loads are issued before any is used (the rows are independent)
+        float s00[16], s01[16], s10[16], s11[16], t0v[16], t1v[16];
+#pragma unroll
         for (int rr = 0; rr < 16; ++rr) {
             const int r = warp * 16 + rr;
-            const int m = m0 + r;
-            float f0 = 0.f, f1 = 0.f;
-            if (m < a.n_models) {
-                const float *sp = a.spec + (size_t)m * a.ld_spec;
-                const float4 zs = reinterpret_cast<const float4 *>(a.zinfo)[m];   // n0, t, s, rest flag
+            const float4 zs = zsm[r];                     // n0, t, s, (0: rest frame, 2: no model)
+            const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec;
+            s00[rr] = s01[rr] = s10[rr] = s11[rr] = 0.f;
+            t0v[rr] = t1v[rr] = 0.f;
+            if (zs.w == 1.f) {
                 const int n0 = __float_as_int(zs.x);
-                float v0, v1;
-                if (zs.w == 0.f) {
-                    v0 = (j < a.nspec) ? sp[j] : 0.f;
-                    v1 = (j + 1 < a.nspec) ? sp[j + 1] : 0.f;
-                } else {
-                    const int sub = (zs.y > 0.f) ? 1 : 0;
-                    int il0 = j - n0 - sub, il1 = il0 + 1;
-                    float t0 = zs.y, t1 = zs.y;
-                    if (il0 < 0 || il0 > a.nspec - 2) {
-                        const int c = il0 < 0 ? 0 : a.nspec - 2;
-                        t0 = expm1f(((float)(j - c) - zs.z) * (float)a.dlnl) / em1;
-                        il0 = c;
-                    }
-                    if (il1 < 0 || il1 > a.nspec - 2) {
-                        const int c = il1 < 0 ? 0 : a.nspec - 2;
-                        t1 = expm1f(((float)(j + 1 - c) - zs.z) * (float)a.dlnl) / em1;
-                        il1 = c;
-                    }
-                    const float s00 = sp[il0], s01 = sp[il0 + 1];
-                    const float s10 = sp[il1], s11 = sp[il1 + 1];
-                    v0 = fmaf(t0, s01 - s00, s00);
-                    v1 = fmaf(t1, s11 - s10, s10);
+                const int sub = (zs.y > 0.f) ? 1 : 0;
+                int il0 = j - n0 - sub, il1 = il0 + 1;
+                float t0 = zs.y, t1 = zs.y;
+                if (il0 < 0 || il0 > a.nspec - 2) {
+                    const int c = il0 < 0 ? 0 : a.nspec - 2;
+                    t0 = expm1f(((float)(j - c) - zs.z) * (float)a.dlnl) / em1;
+                    il0 = c;
                 }
-                if (v0 != v0) v0 = 0.f;
-                if (v1 != v1) v1 = 0.f;
-                f0 = fmaxf(v0, 0.f) * wl0;
-                f1 = fmaxf(v1, 0.f) * wl1;
+                if (il1 < 0 || il1 > a.nspec - 2) {
+                    const int c = il1 < 0 ? 0 : a.nspec - 2;
+                    t1 = expm1f(((float)(j + 1 - c) - zs.z) * (float)a.dlnl) / em1;
+                    il1 = c;
+                }
+                s00[rr] = __ldg(sp + il0); s01[rr] = __ldg(sp + il0 + 1);
+                s10[rr] = __ldg(sp + il1); s11[rr] = __ldg(sp + il1 + 1);
+                t0v[rr] = t0; t1v[rr] = t1;
+            } else if (zs.w == 0.f) {
+                // rest frame: v = s00 (t = 0)
+                if (j < a.nspec) s00[rr] = __ldg(sp + j);
+                if (j + 1 < a.nspec) s10[rr] = __ldg(sp + j + 1);
             }
+        }
+#pragma unroll
+        for (int rr = 0; rr < 16; ++rr) {
+            const int r = warp * 16 + rr;
+            float v0 = fmaf(t0v[rr], s01[rr] - s00[rr], s00[rr]);
+            float v1 = fmaf(t1v[rr], s11[rr] - s10[rr], s10[rr]);
+            if (v0 != v0) v0 = 0.f;
+            if (v1 != v1) v1 = 0.f;
+            const float f0 = fmaxf(v0, 0.f) * wl0;
+            const float f1 = fmaxf(v1, 0.f) * wl1;
             const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
             const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
             const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
