@@ -245,10 +245,8 @@ def run_ours(args) -> None:
                          "unit": "TFLOP/s", "frac": (achieved / pk["bf16_tflops_sustained"]) if achieved else None,
                          "traffic": traffic, "kernel": "csp_contract_kernel<1>",
                          "peak_src": f"{pk['src']} sustained bf16",
-                         "stage_ms": {"weights": ktimes[0] if len(ktimes) > 0 else None,
-                                      "model_params": ktimes[1] if len(ktimes) > 1 else None,
-                                      "contract": t_contract,
-                                      "bands": ktimes[3] if len(ktimes) > 3 else None}},
+                         "stage_ms": dict(zip(["weight_operand", "wait_model_params", "contract", "bands",
+                                               "wait_fp64_sums"], ktimes))},
             "cpu_baseline": cpu,
             "gpu_launches": launches * args.steps,
             "clocks": clk,

@@ -29,6 +29,14 @@ struct BandGemmSmem {
     static int total(int npad) { return 2 * (2 * BG_A_BYTES + 2 * b_bytes(npad)) + 256 + 1024; }
 };
 
+// The rest-frame interval of observed pixel j when it falls outside the grid (extrapolation from the first or
+// the last interval, as the reference's clamped find_interval): *il and the position t.
+__device__ __noinline__ void clamped_interval(int j, float shift, float dlnl, float em1, int nspec, int *il, float *t) {
+    const int c = (*il < 0) ? 0 : nspec - 2;
+    *t = expm1f(((float)(j - c) - shift) * dlnl) / em1;
+    *il = c;
+}
+
 __global__ void __launch_bounds__(BG_THREADS)
 band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_constant__ CUtensorMap tm_c_lo,
                  BandGemmArgs a) {
@@ -60,7 +68,8 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
-    const float em1 = expm1f((float)a.dlnl);
+    const float dlnl_f = (float)a.dlnl;
+    const float em1 = expm1f(dlnl_f);
     // the observed-frame shift of the CTA's models (w = 2: no model in this row)
     __shared__ float4 zsm[BG_M];
     for (int i = tid; i < BG_M; i += BG_THREADS)
@@ -95,16 +104,8 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                 const int sub = (zs.y > 0.f) ? 1 : 0;
                 int il0 = j - n0 - sub, il1 = il0 + 1;
                 float t0 = zs.y, t1 = zs.y;
-                if (il0 < 0 || il0 > a.nspec - 2) {
-                    const int c = il0 < 0 ? 0 : a.nspec - 2;
-                    t0 = expm1f(((float)(j - c) - zs.z) * (float)a.dlnl) / em1;
-                    il0 = c;
-                }
-                if (il1 < 0 || il1 > a.nspec - 2) {
-                    const int c = il1 < 0 ? 0 : a.nspec - 2;
-                    t1 = expm1f(((float)(j + 1 - c) - zs.z) * (float)a.dlnl) / em1;
-                    il1 = c;
-                }
+                if (il0 < 0 || il0 > a.nspec - 2) clamped_interval(j, zs.z, dlnl_f, em1, a.nspec, &il0, &t0);
+                if (il1 < 0 || il1 > a.nspec - 2) clamped_interval(j + 1, zs.z, dlnl_f, em1, a.nspec, &il1, &t1);
                 s00[rr] = __ldg(sp + il0); s01[rr] = __ldg(sp + il0 + 1);
                 s10[rr] = __ldg(sp + il1); s11[rr] = __ldg(sp + il1 + 1);
                 t0v[rr] = t0; t1v[rr] = t1;

@@ -162,6 +162,10 @@ Context::~Context() {
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_params) cudaEventDestroy(ev_params);
+    if (ev_sums) cudaEventDestroy(ev_sums);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -356,7 +360,11 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         err = "this library is built for sm_103a (GB300); device is sm_" + std::to_string(major) + std::to_string(minor);
         return ST_UNSUPPORTED;
     }
-    if (!c.stream && (e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    if ((!c.stream && (e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.side && (e = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.ev_fork && (e = cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming)) != cudaSuccess) ||
+        (!c.ev_params && (e = cudaEventCreateWithFlags(&c.ev_params, cudaEventDisableTiming)) != cudaSuccess) ||
+        (!c.ev_sums && (e = cudaEventCreateWithFlags(&c.ev_sums, cudaEventDisableTiming)) != cudaSuccess)) {
         err = std::string("stream: ") + cudaGetErrorString(e);
         return ST_DATA_MISSING;
     }

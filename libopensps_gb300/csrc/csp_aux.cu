@@ -12,7 +12,47 @@
 namespace sps {
 
 // ---------------------------------------------------------------------------------------------- weights
-// One warp per model; lane l takes operand columns l, l + 32, ...
+// The weight as an FP32 value, 0 unless it is above SAFE_FLOOR (model_sums_zw's floor): the FP64 -> FP32 rounding
+// done on the integer pipes (round to nearest even on the 29 dropped mantissa bits) so that the cast keeps off the
+// FP64 unit, which GB300 has little of. Weights below FP32's smallest normal also give 0.
+__device__ __forceinline__ float weight_to_f32(double w) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+    const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
+    if (b <= 0x0010000000000000ull || (hi32 >> 31)) return 0.f;       // <= DBL_MIN, or negative
+    const int fe = (int)((hi32 >> 20) & 0x7ff) - 896;                  // FP32 biased exponent
+    if (fe < 1) return 0.f;
+    if (fe > 254) return __int_as_float(0x7f800000);
+    uint32_t m = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+    const uint32_t rem = lo32 & 0x1fffffffu;
+    m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(((uint32_t)fe << 23) + m);                  // a mantissa carry moves into the exponent
+}
+
+// The contraction's weight operand: one warp per model, lane l takes operand columns l, l + 32, ...
+__global__ void __launch_bounds__(256) weights_convert_kernel(WeightsArgs a) {
+    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (m >= a.n_models) return;
+    const double *w = a.wz + (size_t)m * a.nt * a.nz;
+    __nv_bfloat16 *hi = a.w_hi + (size_t)m * a.kpad, *lo = a.w_lo + (size_t)m * a.kpad;
+#pragma unroll 4
+    for (int k = lane; k < a.kpad; k += 32) {
+        const int code = __ldg(a.kmap + k);
+        const float wf = (code >= 0) ? weight_to_f32(__ldg(w + (code & 0x3fffffff))) : 0.f;
+        const __nv_bfloat16 h = __float2bfloat16_rn(wf);
+        hi[k] = h;
+        lo[k] = __float2bfloat16_rn(wf - __bfloat162float(h));
+    }
+}
+
+cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st) {
+    if (a.n_models <= 0) return cudaSuccess;
+    const int threads = 256, per_block = threads / 32;
+    weights_convert_kernel<<<(a.n_models + per_block - 1) / per_block, threads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// The FP64 sums of model_sums_zw: one warp per model over the source weights (age fastest).
 template <bool PARTS>
 __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -20,27 +60,20 @@ __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
     if (m >= a.n_models) return;
     const double *w = a.wz + (size_t)m * a.nt * a.nz;
     double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
-    __nv_bfloat16 *hi = a.w_hi + (size_t)m * a.kpad, *lo = a.w_lo + (size_t)m * a.kpad;
+    const int ntz = a.nt * a.nz;
+    int t = lane % a.nt;
 #pragma unroll 4
-    for (int k = lane; k < a.kpad; k += 32) {
-        const int code = __ldg(a.kmap + k);
-        float wf = 0.f;
-        if (code >= 0) {
-            const int src = code & 0x3fffffff;
-            const double wv = w[src];
-            if (wv > DBL_MIN) {
-                const double mk = wv * __ldg(a.mass + src), lk = wv * __ldg(a.llin + src);
-                ms += mk;
-                ls += lk;
-                if (PARTS) {
-                    if (code & 0x40000000) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
-                }
-                wf = (float)wv;
+    for (int k = lane; k < ntz; k += 32) {
+        const double wv = __ldg(w + k);
+        if (wv > DBL_MIN) {
+            const double mk = wv * __ldg(a.mass + k), lk = wv * __ldg(a.llin + k);
+            ms += mk;
+            ls += lk;
+            if (PARTS) {
+                if (t < a.itesc) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
             }
         }
-        const __nv_bfloat16 h = __float2bfloat16_rn(wf);
-        hi[k] = h;
-        lo[k] = __float2bfloat16_rn(wf - __bfloat162float(h));
+        if (PARTS) { t += 32; while (t >= a.nt) t -= a.nt; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {

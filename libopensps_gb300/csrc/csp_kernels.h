@@ -73,7 +73,10 @@ struct WeightsArgs {
     __nv_bfloat16 *w_hi, *w_lo;   // n_models x kpad
     double *sums;           // n_models x 6: mass, lsum, mass_young, mass_old, lsum_young, lsum_old
     int parts;              // also the young and old sums
+    int itesc;              // ages t < itesc (0-based) are young
 };
+// the bf16 hi / lo operand (no FP64 arithmetic), and the FP64 sums (run beside the contraction)
+cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st);
 cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st);
 
 // Band fluxes (observed frame at each model's redshift, trapezoid filter integrals) and AB magnitudes, as a
