@@ -469,8 +469,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
 
-    // ---- fork: the per-model parameters, then the FP64 mass / L_bol sums, on the side stream (the sums overlap the
-    // contraction, which leaves the FP64 pipes idle)
+    // ---- fork: the per-model parameters on a side stream (beside the weight operand); the FP64 mass / L_bol sums on
+    // a second one once the contraction is done (beside the band GEMM, which leaves the FP64 pipes idle)
     if ((e = cudaEventRecord(c.ev_fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side, c.ev_fork, 0)) != cudaSuccess) {
         err = cuda_msg("fork", e);
         return ST_DATA_MISSING;
@@ -490,10 +490,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.sums = c.d_sums.p;
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
-    if ((e = run_weights_prep(wa, c.side)) != cudaSuccess || (e = cudaEventRecord(c.ev_sums, c.side)) != cudaSuccess) {
-        err = cuda_msg("weights sums kernel", e);
-        return ST_DATA_MISSING;
-    }
     // ---- main stream: the weight operand, then the contraction once the parameters are there
     prof_mark(c, 0);
     if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
@@ -522,6 +518,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);
+    if ((e = cudaEventRecord(c.ev_contract, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side2, c.ev_contract, 0)) != cudaSuccess ||
+        (e = run_weights_prep(wa, c.side2)) != cudaSuccess || (e = cudaEventRecord(c.ev_sums, c.side2)) != cudaSuccess) {
+        err = cuda_msg("weights sums kernel", e);
+        return ST_DATA_MISSING;
+    }
     int launches = 4;   // weight operand, model parameters, FP64 sums, contraction
 
     // ---- bands and magnitudes

@@ -165,7 +165,9 @@ Context::~Context() {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_params) cudaEventDestroy(ev_params);
     if (ev_sums) cudaEventDestroy(ev_sums);
+    if (ev_contract) cudaEventDestroy(ev_contract);
     if (side) cudaStreamDestroy(side);
+    if (side2) cudaStreamDestroy(side2);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -362,6 +364,8 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     }
     if ((!c.stream && (e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.side && (e = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.side2 && (e = cudaStreamCreateWithFlags(&c.side2, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.ev_contract && (e = cudaEventCreateWithFlags(&c.ev_contract, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_fork && (e = cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_params && (e = cudaEventCreateWithFlags(&c.ev_params, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_sums && (e = cudaEventCreateWithFlags(&c.ev_sums, cudaEventDisableTiming)) != cudaSuccess)) {

@@ -80,8 +80,9 @@ struct Context {
     // device copies
     int device = 0, num_sms = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;                 // the per-model parameters and the FP64 sums run here
-    cudaEvent_t ev_fork = nullptr, ev_params = nullptr, ev_sums = nullptr;
+    cudaStream_t side = nullptr;                 // the per-model parameters run here
+    cudaStream_t side2 = nullptr;                // the FP64 sums run here (after the contraction)
+    cudaEvent_t ev_fork = nullptr, ev_params = nullptr, ev_contract = nullptr, ev_sums = nullptr;
     DevBuf<float> d_pix, d_wl, d_igm_a;
     DevBuf<int> d_do_band;
     // band matrix of the band GEMM: bf16 hi / lo, band_npad rows x 64 band_nkb pixels from pixel band_j0
