@@ -34,6 +34,7 @@ struct ModelParamArgs {
     const double *par;       // PAR_DEVICE x n
     const float *igm_a;      // jtop x 6
     const double *lam;       // nspec
+    const double *lnlam;     // nspec: ln lambda
     const double *zt, *dl;   // 500
     double dlnl;
     float *mpar;             // n x MODEL_PAR_FLOATS
@@ -41,53 +42,43 @@ struct ModelParamArgs {
     double *dist;            // n
 };
 
-// One warp per model: the lanes share the IGM scan (the cap's maximum over the pixels below Lyman alpha) and the
-// smoothing taps; lane 0 writes the scalars.
+// One thread per model for the FP64 scalars (GB300's FP64 rate is low: a warp instruction serves 32 models); the IGM
+// cap's search for the largest optical depth over the pixels below Lyman alpha is shared by the warp's lanes, model
+// after model.
 __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
-    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    if (m >= a.n) return;
-    const double *p = a.par + (size_t)PAR_DEVICE * m;
-    float *o = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    const bool live = m < a.n;
     const double LOG2E = 1.4426950408889634;
-    const double z = p[PF_ZRED];
-    float val = 0.f;     // this lane's word of the parameter block
-    // attenuate_batch / pixel_transmissions (src/physics/opensps_csp_batch.f90:3576-3660, 3765-3818)
-    if (lane < 12) {
-        const double d1 = p[PF_DUST1], d2 = p[PF_DUST2], d3 = p[PF_DUST3], fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
-        const bool nodiff = 1.0 - fnd <= SAFE_FLOOR;
-        switch (lane) {
-            case MP_KD2: val = (float)(-d2 * LOG2E); break;
-            case MP_ONE_M_FND: val = nodiff ? 0.f : (float)(1.0 - fnd); break;
-            case MP_FND: val = nodiff ? 1.f : (float)fnd; break;
-            case MP_DUST_INDEX: val = (float)p[PF_DUST_INDEX]; break;
-            case MP_KD1: val = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)(-d1 * LOG2E); break;
-            case MP_DUST1_INDEX: val = (float)p[PF_DUST1_INDEX]; break;
-            case MP_ONE_M_FO: val = (float)(1.0 - fo); break;
-            case MP_FO: val = (float)fo; break;
-            case MP_KD3: val = (fabs(d3) <= SAFE_FLOOR) ? 0.f : (float)(-d3 * LOG2E); break;
-            default: break;
-        }
-    }
-    // IGM (apply_igm_z :4205-4299): redshift factors and the short-wavelength cap
-    const bool igm = a.add_igm && z > SAFE_FLOOR && a.jtop > 0;
-    if (lane == MP_IGM_JMAX) val = __int_as_float(0);
+    const double *p = a.par + (size_t)PAR_DEVICE * (live ? m : 0);
+    const double z = live ? p[PF_ZRED] : 0.0;
+    const bool igm = live && a.add_igm && z > SAFE_FLOOR && a.jtop > 0;
+    // redshift factors b_k = (1 + z)^p_k (igm_tau_z_terms, src/physics/opensps_cosmology.f90:497-508)
+    float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (igm) {
-        // lane k < 6 forms b_k = (1 + z)^p_k; every lane gets all six
         const double opz = 1.0 + z;
-        // exponents of igm_tau_z_terms (src/physics/opensps_cosmology.f90:497-508), formed as there
-        const double pw = lane == 0 ? 3.46 : lane == 1 ? 1.68 : lane == 2 ? 3.0 + 0.46 : lane == 3 ? 1.5 + 0.18
-                        : lane == 4 ? 3.0 - 1.32 : 1.68;
-        const float bk = lane < 6 ? (float)pow(opz, pw) : 0.f;
-        float b[6];
+        b[0] = (float)pow(opz, 3.46);
+        b[1] = (float)pow(opz, 1.68);
+        b[2] = (float)pow(opz, 3.0 + 0.46);
+        b[3] = (float)pow(opz, 1.5 + 0.18);
+        b[4] = (float)pow(opz, 3.0 - 1.32);
+        b[5] = (float)pow(opz, 1.68);
+    }
+    // the cap (apply_igm_z :4272-4299): the first pixel of the largest optical depth, searched by the whole warp for
+    // each of its models in turn
+    float my_tmax = 0.f;
+    int my_jmax = 1;
+    const unsigned todo = __ballot_sync(0xffffffffu, igm);
+    for (int i = 0; i < 32; ++i) {
+        if (!((todo >> i) & 1u)) continue;
+        float bb[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) b[k] = __shfl_sync(0xffffffffu, bk, k);
-        // the first pixel of the largest optical depth (strictly greater: the first of equal maxima)
+        for (int k = 0; k < 6; ++k) bb[k] = __shfl_sync(0xffffffffu, b[k], i);
         float tmax = 0.f;
         int jmax = 1;
         for (int j = lane; j < a.jtop; j += 32) {
             const float *ia = a.igm_a + (size_t)j * 6;
-            const float t = ia[0] * b[0] + ia[1] * b[1] + ia[2] * b[2] + ia[3] * b[3] + ia[4] * b[4] + ia[5] * b[5];
+            const float t = ia[0] * bb[0] + ia[1] * bb[1] + ia[2] * bb[2] + ia[3] * bb[3] + ia[4] * bb[4] + ia[5] * bb[5];
             if (t > tmax) { tmax = t; jmax = j + 1; }
         }
 #pragma unroll
@@ -96,84 +87,101 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
             const int j2 = __shfl_xor_sync(0xffffffffu, jmax, off);
             if (t2 > tmax || (t2 == tmax && j2 < jmax)) { tmax = t2; jmax = j2; }
         }
-        if (tmax <= 0.f) jmax = 1;
+        if (lane == i) { my_tmax = tmax; my_jmax = tmax > 0.f ? jmax : 1; }
+    }
+    if (!live) return;
+
+    float *o = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    float blk[MODEL_PAR_FLOATS];
+#pragma unroll
+    for (int i = 0; i < MODEL_PAR_FLOATS; ++i) blk[i] = 0.f;
+    const double d1 = p[PF_DUST1], d2 = p[PF_DUST2], d3 = p[PF_DUST3], fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
+    // attenuate_batch / pixel_transmissions (src/physics/opensps_csp_batch.f90:3576-3660, 3765-3818)
+    blk[MP_KD2] = (float)(-d2 * LOG2E);
+    if (1.0 - fnd <= SAFE_FLOOR) { blk[MP_ONE_M_FND] = 0.f; blk[MP_FND] = 1.f; }
+    else { blk[MP_ONE_M_FND] = (float)(1.0 - fnd); blk[MP_FND] = (float)fnd; }
+    blk[MP_DUST_INDEX] = (float)p[PF_DUST_INDEX];
+    blk[MP_KD1] = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)(-d1 * LOG2E);
+    blk[MP_DUST1_INDEX] = (float)p[PF_DUST1_INDEX];
+    blk[MP_ONE_M_FO] = (float)(1.0 - fo);
+    blk[MP_FO] = (float)fo;
+    blk[MP_KD3] = (fabs(d3) <= SAFE_FLOOR) ? 0.f : (float)(-d3 * LOG2E);
+    blk[MP_IGM_JMAX] = __int_as_float(0);
+    if (igm) {
         const double kf = -p[PF_IGM_FACTOR] * LOG2E;
-        if (lane >= MP_IGM_KB && lane < MP_IGM_KB + 6) val = (float)((double)b[lane - MP_IGM_KB] * kf);
-        if (lane == MP_IGM_KCAP) val = (float)((double)tmax * kf);
-        if (lane == MP_IGM_JMAX) val = __int_as_float(jmax);
-        if (lane == MP_IGM_ON) val = 1.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) blk[MP_IGM_KB + k] = (float)((double)b[k] * kf);
+        blk[MP_IGM_KCAP] = (float)((double)my_tmax * kf);
+        blk[MP_IGM_JMAX] = __int_as_float(my_jmax);
+        blk[MP_IGM_ON] = 1.f;
     }
     // velocity smoothing taps: row i0 of build_velocity_kernel (src/spectra/opensps_smoothing.f90:553-633)
-    if (lane == MP_SMOOTH_R) val = __int_as_float(-1);
+    blk[MP_SMOOTH_R] = __int_as_float(-1);
     const double sig = p[PF_SIGMA_SMOOTH];
     if (a.smooth && sig > SAFE_FLOOR && a.i0 >= 0) {
         const int n = a.nspec, i = a.i0;
         const double sb = sig / (C_LIGHT * 1.0e-13);
         const double inv2s2 = 0.5 * (1.0 / sb) * (1.0 / sb);
-        int il = 0, ih = 0;
-        if (lane == 0) {
-            const double vl = a.lam[i] * exp(-4.0 * sb), vh = a.lam[i] * exp(4.0 * sb);
-            // il: first pixel >= vl, one lower when it lies above vl; ih: first pixel >= vh
-            int lo = 0, hi = n;
-            while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vl) lo = md + 1; else hi = md; }
-            il = lo < n ? lo : n - 1;
-            if (il > 0 && a.lam[il] > vl) il--;
-            lo = il; hi = n;
-            while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vh) lo = md + 1; else hi = md; }
-            ih = lo < n ? lo : n - 1;
-            if (ih < il) ih = il;
-        }
-        il = __shfl_sync(0xffffffffu, il, 0);
-        ih = __shfl_sync(0xffffffffu, ih, 0);
+        const double vl = a.lam[i] * exp(-4.0 * sb), vh = a.lam[i] * exp(4.0 * sb);
+        // il: first pixel >= vl, one lower when it lies above vl; ih: first pixel >= vh
+        int lo = 0, hi = n;
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vl) lo = md + 1; else hi = md; }
+        int il = lo < n ? lo : n - 1;
+        if (il > 0 && a.lam[il] > vl) il--;
+        lo = il; hi = n;
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vh) lo = md + 1; else hi = md; }
+        int ih = lo < n ? lo : n - 1;
+        if (ih < il) ih = il;
         if (ih - il + 1 >= 2 && i - il <= 4 && ih - i <= 4) {
-            // lane u < 9 takes window pixel j = il + u
-            const int j = il + lane;
-            double wj = 0.0;
-            if (lane < 9 && j <= ih) {
-                const double d = log(a.lam[i]) - log(a.lam[j]);
-                wj = exp(-inv2s2 * d * d) / a.lam[j];
-                const double dlft = (j > il) ? a.lam[j] - a.lam[j - 1] : 0.0;
-                const double drgt = (j < ih) ? a.lam[j + 1] - a.lam[j] : 0.0;
-                wj = 0.5 * wj * (dlft + drgt);
-            }
-            // total weight summed in window order, as the reference
-            double tw = 0.0;
-            for (int u = 0; u < 9; ++u) tw += __shfl_sync(0xffffffffu, wj, u);
-            if (tw > SAFE_FLOOR) {
-                // tap of offset d (d = -4..4) lives on lane MP_TAPS + 4 + d: its window pixel is i + d
-                const int src = (lane >= MP_TAPS && lane < MP_TAPS + 9) ? (i + lane - MP_TAPS - 4) - il : 31;
-                const double wsrc = __shfl_sync(0xffffffffu, wj, (src >= 0 && src < 9) ? src : 31);
-                if (lane >= MP_TAPS && lane < MP_TAPS + 9) {
-                    const int jw = i + lane - MP_TAPS - 4;
-                    val = (jw >= il && jw <= ih) ? (float)(wsrc / tw) : 0.f;
+            double w[9], tw = 0.0;
+            const double lli = a.lnlam[i];
+#pragma unroll
+            for (int u = 0; u < 9; ++u) {
+                const int j = il + u;
+                double wj = 0.0;
+                if (j <= ih) {
+                    const double d = lli - a.lnlam[j];
+                    wj = exp(-inv2s2 * d * d) / a.lam[j];
+                    const double dlft = (j > il) ? a.lam[j] - a.lam[j - 1] : 0.0;
+                    const double drgt = (j < ih) ? a.lam[j + 1] - a.lam[j] : 0.0;
+                    wj = 0.5 * wj * (dlft + drgt);
                 }
-                if (lane == MP_SMOOTH_R) val = __int_as_float(max(i - il, ih - i));
+                w[u] = wj;
+                tw += wj;
+            }
+            if (tw > SAFE_FLOOR) {
+#pragma unroll
+                for (int d = -4; d <= 4; ++d) {
+                    const int u = i + d - il;
+                    blk[MP_TAPS + 4 + d] = (u >= 0 && u <= ih - il && u < 9) ? (float)(w[u] / tw) : 0.f;
+                }
+                blk[MP_SMOOTH_R] = __int_as_float(max(i - il, ih - i));
             }
         }
     }
-    o[lane] = val;
-    if (lane == 0) {
-        // observed frame: the shift of lambda / (1 + z) on the log-uniform grid, in pixels
-        // (observed pixel j reads rest pixels j - n0 - 1 and j - n0 at t, the same t for every interior pixel)
-        float4 zi = make_float4(__int_as_float(0), 0.f, 0.f, 0.f);
-        double dd = 0.0;
-        if (fabs(z) > SAFE_FLOOR) {
-            const double s = log1p(z) / a.dlnl;
-            const double n0 = floor(s), phi = s - n0;
-            zi.x = __int_as_float((int)n0);
-            zi.y = phi > 0.0 ? (float)(expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl)) : 0.f;
-            zi.z = (float)s;
-            zi.w = 1.f;
-            // distance term (distance_term, src/spectra/opensps_batch_photometry.f90:784-794)
-            int idx = find_interval0(a.zt, 500, z);
-            idx = max(0, min(idx, 498));
-            const double slope = (a.dl[idx + 1] - a.dl[idx]) / (a.zt[idx + 1] - a.zt[idx]);
-            const double dm = a.dl[idx] + slope * (z - a.zt[idx]);
-            if (dm == dm && dm > SAFE_FLOOR) dd = 5.0 * log10(dm / 10.0) - 2.5 * log10(1.0 + z);
-        }
-        a.zinfo[m] = zi;
-        a.dist[m] = dd;
+#pragma unroll
+    for (int i = 0; i < MODEL_PAR_FLOATS; i += 4)
+        reinterpret_cast<float4 *>(o)[i / 4] = make_float4(blk[i], blk[i + 1], blk[i + 2], blk[i + 3]);
+    // observed frame: the shift of lambda / (1 + z) on the log-uniform grid, in pixels
+    // (observed pixel j reads rest pixels j - n0 - 1 and j - n0 at t, the same t for every interior pixel)
+    float4 zi = make_float4(__int_as_float(0), 0.f, 0.f, 0.f);
+    double dd = 0.0;
+    if (fabs(z) > SAFE_FLOOR) {
+        const double s = log1p(z) / a.dlnl;
+        const double n0 = floor(s), phi = s - n0;
+        zi.x = __int_as_float((int)n0);
+        zi.y = phi > 0.0 ? (float)(expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl)) : 0.f;
+        zi.z = (float)s;
+        zi.w = 1.f;
+        // distance term (distance_term, src/spectra/opensps_batch_photometry.f90:784-794)
+        int idx = find_interval0(a.zt, 500, z);
+        idx = max(0, min(idx, 498));
+        const double slope = (a.dl[idx + 1] - a.dl[idx]) / (a.zt[idx + 1] - a.zt[idx]);
+        const double dm = a.dl[idx] + slope * (z - a.zt[idx]);
+        if (dm == dm && dm > SAFE_FLOOR) dd = 5.0 * log10(dm / 10.0) - 2.5 * log10(1.0 + z);
     }
+    a.zinfo[m] = zi;
+    a.dist[m] = dd;
 }
 
 // ---------------------------------------------------------------------------------------------- basis operand
@@ -479,7 +487,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ma.n = n; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
     ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
     ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zinfo = c.d_zinfo.p; ma.dist = c.d_dist.p;
-    model_params_kernel<<<(n + 7) / 8, 256, 0, c.side>>>(ma);
+    ma.lnlam = c.d_lnlam.p;
+    model_params_kernel<<<(n + 255) / 256, 256, 0, c.side>>>(ma);
     if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(c.ev_params, c.side)) != cudaSuccess) {
         err = cuda_msg("model parameter kernel", e);
         return ST_DATA_MISSING;

@@ -155,7 +155,7 @@ Context::~Context() {
         delete kv.second;
     }
     d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
-    d_lam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
+    d_lam.release(); d_lnlam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
     d_status.release();
@@ -385,10 +385,13 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         for (int k = 0; k < 6; ++k) igm_a[(size_t)j * 6 + k] = (float)a[k];
     }
     c.igm_a = igm_a;
+    std::vector<double> lnlam(ns);
+    for (int j = 0; j < ns; ++j) lnlam[j] = std::log(c.lam[j]);
     cosmology_table(c.h0, c.om0, c.ol0, c.zt, c.dl);
     if ((e = upload(c.d_wl, wl.data(), wl.size())) != cudaSuccess ||
         (e = upload(c.d_igm_a, igm_a.data(), igm_a.size())) != cudaSuccess ||
         (e = upload(c.d_lam, c.lam.data(), c.lam.size())) != cudaSuccess ||
+        (e = upload(c.d_lnlam, lnlam.data(), lnlam.size())) != cudaSuccess ||
         (e = upload(c.d_mass, c.mass.data(), c.mass.size())) != cudaSuccess ||
         (e = upload(c.d_llin, c.llin.data(), c.llin.size())) != cudaSuccess ||
         (e = upload(c.d_zt, c.zt.data(), c.zt.size())) != cudaSuccess ||

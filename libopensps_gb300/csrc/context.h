@@ -89,7 +89,7 @@ struct Context {
     DevBuf<__nv_bfloat16> d_cb_hi, d_cb_lo;
     CUtensorMap tm_cb_hi, tm_cb_lo;
     int band_j0 = 0, band_nkb = 0, band_npad = 0;
-    DevBuf<double> d_lam, d_mass, d_llin, d_zt, d_dl;
+    DevBuf<double> d_lam, d_lnlam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
     double pix_index = -1e300;   // dust_index of the device pixel table's curve
 
