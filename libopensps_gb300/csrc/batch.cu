@@ -56,13 +56,14 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     // redshift factors b_k = (1 + z)^p_k (igm_tau_z_terms, src/physics/opensps_cosmology.f90:497-508)
     float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (igm) {
-        const double opz = 1.0 + z;
-        b[0] = (float)pow(opz, 3.46);
-        b[1] = (float)pow(opz, 1.68);
-        b[2] = (float)pow(opz, 3.0 + 0.46);
-        b[3] = (float)pow(opz, 1.5 + 0.18);
-        b[4] = (float)pow(opz, 3.0 - 1.32);
-        b[5] = (float)pow(opz, 1.68);
+        // (1 + z)^p as exp(p ln(1 + z)): one FP64 logarithm for the six powers
+        const double l1z = log1p(z);
+        b[0] = (float)exp(3.46 * l1z);
+        b[1] = (float)exp(1.68 * l1z);
+        b[2] = (float)exp((3.0 + 0.46) * l1z);
+        b[3] = (float)exp((1.5 + 0.18) * l1z);
+        b[4] = (float)exp((3.0 - 1.32) * l1z);
+        b[5] = b[1];
     }
     // the cap (apply_igm_z :4272-4299): the first pixel of the largest optical depth, searched by the whole warp for
     // each of its models in turn
@@ -122,38 +123,41 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
         const int n = a.nspec, i = a.i0;
         const double sb = sig / (C_LIGHT * 1.0e-13);
         const double inv2s2 = 0.5 * (1.0 / sb) * (1.0 / sb);
-        const double vl = a.lam[i] * exp(-4.0 * sb), vh = a.lam[i] * exp(4.0 * sb);
+        // the window in ln lambda: lambda_j vs lambda_i exp(-+4 sigma / c) compared as logarithms
+        const double vl = a.lnlam[i] - 4.0 * sb, vh = a.lnlam[i] + 4.0 * sb;
         // il: first pixel >= vl, one lower when it lies above vl; ih: first pixel >= vh
         int lo = 0, hi = n;
-        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vl) lo = md + 1; else hi = md; }
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lnlam[md] < vl) lo = md + 1; else hi = md; }
         int il = lo < n ? lo : n - 1;
-        if (il > 0 && a.lam[il] > vl) il--;
+        if (il > 0 && a.lnlam[il] > vl) il--;
         lo = il; hi = n;
-        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lam[md] < vh) lo = md + 1; else hi = md; }
+        while (lo < hi) { const int md = (lo + hi) / 2; if (a.lnlam[md] < vh) lo = md + 1; else hi = md; }
         int ih = lo < n ? lo : n - 1;
         if (ih < il) ih = il;
         if (ih - il + 1 >= 2 && i - il <= 4 && ih - i <= 4) {
-            double w[9], tw = 0.0;
+            // Gaussian weights / lambda_j times the trapezoid widths, normalised: the exponent is formed in FP64
+            // (differences of ln lambda), the exponential and the normalisation in FP32 (the taps are stored so)
+            float w[9], tw = 0.f;
             const double lli = a.lnlam[i];
 #pragma unroll
             for (int u = 0; u < 9; ++u) {
                 const int j = il + u;
-                double wj = 0.0;
+                float wj = 0.f;
                 if (j <= ih) {
                     const double d = lli - a.lnlam[j];
-                    wj = exp(-inv2s2 * d * d) / a.lam[j];
-                    const double dlft = (j > il) ? a.lam[j] - a.lam[j - 1] : 0.0;
-                    const double drgt = (j < ih) ? a.lam[j + 1] - a.lam[j] : 0.0;
-                    wj = 0.5 * wj * (dlft + drgt);
+                    const float dlft = (j > il) ? (float)(a.lam[j] - a.lam[j - 1]) : 0.f;
+                    const float drgt = (j < ih) ? (float)(a.lam[j + 1] - a.lam[j]) : 0.f;
+                    wj = expf((float)(-inv2s2 * d * d)) / (float)a.lam[j] * 0.5f * (dlft + drgt);
                 }
                 w[u] = wj;
                 tw += wj;
             }
-            if (tw > SAFE_FLOOR) {
+            if (tw > 0.f) {
+                const float inv = 1.f / tw;
 #pragma unroll
                 for (int d = -4; d <= 4; ++d) {
                     const int u = i + d - il;
-                    blk[MP_TAPS + 4 + d] = (u >= 0 && u <= ih - il && u < 9) ? (float)(w[u] / tw) : 0.f;
+                    blk[MP_TAPS + 4 + d] = (u >= 0 && u <= ih - il && u < 9) ? w[u] * inv : 0.f;
                 }
                 blk[MP_SMOOTH_R] = __int_as_float(max(i - il, ih - i));
             }
@@ -499,6 +503,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.sums = c.d_sums.p;
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
+    wa.grid = c.num_sms;   // a few warps per SM: the sums run in the background of the other kernels
+    if ((e = cudaStreamWaitEvent(c.side2, c.ev_fork, 0)) != cudaSuccess || (e = run_weights_prep(wa, c.side2)) != cudaSuccess ||
+        (e = cudaEventRecord(c.ev_sums, c.side2)) != cudaSuccess) {
+        err = cuda_msg("weights sums kernel", e);
+        return ST_DATA_MISSING;
+    }
     // ---- main stream: the weight operand, then the contraction once the parameters are there
     prof_mark(c, 0);
     if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
@@ -527,11 +537,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);
-    if ((e = cudaEventRecord(c.ev_contract, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side2, c.ev_contract, 0)) != cudaSuccess ||
-        (e = run_weights_prep(wa, c.side2)) != cudaSuccess || (e = cudaEventRecord(c.ev_sums, c.side2)) != cudaSuccess) {
-        err = cuda_msg("weights sums kernel", e);
-        return ST_DATA_MISSING;
-    }
     int launches = 4;   // weight operand, model parameters, FP64 sums, contraction
 
     // ---- bands and magnitudes

@@ -55,9 +55,9 @@ cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st) {
 // The FP64 sums of model_sums_zw: one warp per model over the source weights (age fastest).
 template <bool PARTS>
 __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
-    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (m >= a.n_models) return;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; m < a.n_models; m += nwarps) {
     const double *w = a.wz + (size_t)m * a.nt * a.nz;
     double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
     const int ntz = a.nt * a.nz;
@@ -91,12 +91,13 @@ __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
         o[0] = ms; o[1] = ls;
         if (PARTS) { o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso; }
     }
+    }
 }
 
 cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st) {
     if (a.n_models <= 0) return cudaSuccess;
-    const int threads = 256, per_block = threads / 32;
-    const int blocks = (a.n_models + per_block - 1) / per_block;
+    const int threads = a.grid > 0 ? 64 : 256, per_block = threads / 32;
+    const int blocks = a.grid > 0 ? a.grid : (a.n_models + per_block - 1) / per_block;
     if (a.parts) weights_prep_kernel<true><<<blocks, threads, 0, st>>>(a);
     else weights_prep_kernel<false><<<blocks, threads, 0, st>>>(a);
     return cudaGetLastError();

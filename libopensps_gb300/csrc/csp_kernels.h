@@ -74,6 +74,7 @@ struct WeightsArgs {
     double *sums;           // n_models x 6: mass, lsum, mass_young, mass_old, lsum_young, lsum_old
     int parts;              // also the young and old sums
     int itesc;              // ages t < itesc (0-based) are young
+    int grid;               // blocks of the FP64 sums kernel (0: one warp per model)
 };
 // the bf16 hi / lo operand (no FP64 arithmetic), and the FP64 sums (run beside the contraction)
 cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st);
