@@ -481,8 +481,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
 
-    // ---- fork: the per-model parameters on a side stream (beside the weight operand); the FP64 mass / L_bol sums on
-    // a second one once the contraction is done (beside the band GEMM, which leaves the FP64 pipes idle)
+    // ---- fork: the per-model parameters on a side stream, beside the weight operand
     if ((e = cudaEventRecord(c.ev_fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side, c.ev_fork, 0)) != cudaSuccess) {
         err = cuda_msg("fork", e);
         return ST_DATA_MISSING;
@@ -503,12 +502,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.sums = c.d_sums.p;
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
-    wa.grid = c.num_sms;   // a few warps per SM: the sums run in the background of the other kernels
-    if ((e = cudaStreamWaitEvent(c.side2, c.ev_fork, 0)) != cudaSuccess || (e = run_weights_prep(wa, c.side2)) != cudaSuccess ||
-        (e = cudaEventRecord(c.ev_sums, c.side2)) != cudaSuccess) {
-        err = cuda_msg("weights sums kernel", e);
-        return ST_DATA_MISSING;
-    }
+    wa.grid = 0;
     // ---- main stream: the weight operand, then the contraction once the parameters are there
     prof_mark(c, 0);
     if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
@@ -560,8 +554,9 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ++launches;
     }
     prof_mark(c, 4);
-    // join the side stream: the batch is complete when the main stream is
-    if ((e = cudaStreamWaitEvent(st, c.ev_sums, 0)) != cudaSuccess) { err = cuda_msg("join", e); return ST_DATA_MISSING; }
+    // the FP64 mass and L_bol sums (alone: a kernel beside the contraction or the band GEMM slows them more than it
+    // takes itself)
+    if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 5);
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {
