@@ -1,4 +1,5 @@
-// Band fluxes and AB magnitudes as a tensor-core GEMM: fband(m, b) = sum_j Fobs(m, j) C(j, b).
+// Band fluxes and AB magnitudes as a tensor-core GEMM: fband(m, b) = sum_j Fobs(m, j) C(j, b); with, beside them,
+// the FP64 mass and L_bol sums of the same models.
 //
 // compute_magnitudes_columns (OpenSPS src/spectra/opensps_batch_photometry.f90:53-180): each model's rest-frame
 // spectrum resampled to the observed frame at its redshift, divided by lambda (observed_frame_z :819-903), then the
@@ -7,12 +8,16 @@
 // not computed).
 //
 // Per CTA: 128 models (MMA M). K = the pixels that any band reaches, 64 per stage. The A operand (observed frame
-// of 128 models x 64 pixels) is built by the CTA's threads in shared memory from the spectra, in the 128-byte
-// swizzled K-major layout, split into bf16 hi and lo; the B operand (band matrix, hi and lo, bands x pixels) comes
-// by TMA. fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes.
-// Two stages: the threads build stage s + 1 while the tensor core works on stage s.
+// of 128 models x 64 pixels) is built by warps 0..7 in shared memory from the spectra, in the 128-byte swizzled
+// K-major layout, split into bf16 hi and lo; the B operand (band matrix, hi and lo, bands x pixels) comes by TMA.
+// fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes. Two stages:
+// the builders fill stage s + 1 while the tensor core works on stage s.
+//
+// Warps 8 and 9 meanwhile form the FP64 sums of model_sums_zw (src/physics/opensps_csp_batch.f90:2090-2120) for the
+// CTA's 128 models: the band GEMM waits on memory and leaves the FP64 pipes idle, which GB300 has few of.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cfloat>
 #include <cstdint>
 #include "sm103_ptx.cuh"
 #include "csp_kernels.h"
@@ -21,7 +26,10 @@ namespace sps {
 
 constexpr int BG_M = 128;
 constexpr int BG_K = 64;
-constexpr int BG_THREADS = 256;
+constexpr int BG_BUILD_WARPS = 8;
+constexpr int BG_BUILD_THREADS = BG_BUILD_WARPS * 32;
+constexpr int BG_SUM_WARPS = 2;
+constexpr int BG_THREADS = BG_BUILD_THREADS + BG_SUM_WARPS * 32;
 constexpr int BG_A_BYTES = BG_M * BG_K * 2;   // 16 KB
 
 struct BandGemmSmem {
@@ -29,15 +37,51 @@ struct BandGemmSmem {
     static int total(int npad) { return 2 * (2 * BG_A_BYTES + 2 * b_bytes(npad)) + 256 + 1024; }
 };
 
-// The rest-frame interval of observed pixel j when it falls outside the grid (extrapolation from the first or
-// the last interval, as the reference's clamped find_interval): *il and the position t.
-__device__ __noinline__ void clamped_interval(int j, float shift, float dlnl, float em1, int nspec, int *il, float *t) {
-    const int c = (*il < 0) ? 0 : nspec - 2;
-    *t = expm1f(((float)(j - c) - shift) * dlnl) / em1;
-    *il = c;
+// 2^x by the SFU
+__device__ __forceinline__ float bg_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-__global__ void __launch_bounds__(BG_THREADS)
+// The FP64 sums of one model (one warp): mass and L_bol over the weights above SAFE_FLOOR (the comparison on the
+// bit pattern: positive doubles order as their bits), young and old apart with parts.
+__device__ __forceinline__ void model_sums_warp(const BandGemmArgs &a, int m, int lane) {
+    const double *w = a.wz + (size_t)m * a.ntz;
+    double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
+    int t = lane % a.nt;
+#pragma unroll 4
+    for (int k = lane; k < a.ntz; k += 32) {
+        const double wv = __ldg(w + k);
+        if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
+            const double mk = wv * __ldg(a.mass + k), lk = wv * __ldg(a.llin + k);
+            ms += mk;
+            ls += lk;
+            if (a.parts) {
+                if (t < a.itesc) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
+            }
+        }
+        if (a.parts) { t += 32; while (t >= a.nt) t -= a.nt; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ms += __shfl_xor_sync(0xffffffffu, ms, off);
+        ls += __shfl_xor_sync(0xffffffffu, ls, off);
+        if (a.parts) {
+            msy += __shfl_xor_sync(0xffffffffu, msy, off);
+            lsy += __shfl_xor_sync(0xffffffffu, lsy, off);
+            mso += __shfl_xor_sync(0xffffffffu, mso, off);
+            lso += __shfl_xor_sync(0xffffffffu, lso, off);
+        }
+    }
+    if (lane == 0) {
+        double *o = a.sums + (size_t)m * 6;
+        o[0] = ms; o[1] = ls;
+        if (a.parts) { o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso; }
+    }
+}
+
+__global__ void __launch_bounds__(BG_THREADS, 2)
 band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_constant__ CUtensorMap tm_c_lo,
                  BandGemmArgs a) {
     extern __shared__ uint8_t smem_raw[];
@@ -54,6 +98,7 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     const int m0 = blockIdx.x * BG_M;
     int *status = a.status;
     const uint32_t tcols = npad <= 32 ? 32 : (npad <= 64 ? 64 : (npad <= 128 ? 128 : 256));
+    __shared__ float4 zsm[BG_M];     // the observed-frame shift of the CTA's models (w = 2: no model in this row)
 
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) { mbar_init(&bar_tma[s], 1); mbar_init(&bar_mma[s], 1); }
@@ -63,118 +108,129 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         tma_prefetch_desc(&tm_c_lo);
     }
     if (warp == 0) { tmem_alloc(tmem_slot, tcols); tmem_relinquish(); }
+    for (int i = tid; i < BG_M; i += BG_THREADS)
+        zsm[i] = (m0 + i < a.n_models) ? a.zinfo[m0 + i] : make_float4(0.f, 0.f, 0.f, 2.f);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
-    const float dlnl_f = (float)a.dlnl;
-    const float em1 = expm1f(dlnl_f);
-    // the observed-frame shift of the CTA's models (w = 2: no model in this row)
-    __shared__ float4 zsm[BG_M];
-    for (int i = tid; i < BG_M; i += BG_THREADS)
-        zsm[i] = (m0 + i < a.n_models) ? a.zinfo[m0 + i] : make_float4(0.f, 0.f, 0.f, 2.f);
-    __syncthreads();
 
-    // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
-    for (int kb = 0; kb < a.nkb; ++kb) {
-        const int s = kb & 1;
-        uint8_t *st = smem + s * stage_bytes;
-        if (kb >= 2) mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
-        if (tid == 0) {
-            mbar_arrive_expect_tx(&bar_tma[s], 2 * b_bytes);
-            tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &bar_tma[s]);
-            tma_load_2d(st + 2 * BG_A_BYTES + b_bytes, &tm_c_lo, kb * BG_K, 0, &bar_tma[s]);
+    if (warp >= BG_BUILD_WARPS) {
+        // ---------------------------------------------------------------- FP64 sums of the CTA's models
+        if (a.sums) {
+            for (int r = warp - BG_BUILD_WARPS; r < BG_M; r += BG_SUM_WARPS)
+                if (m0 + r < a.n_models) model_sums_warp(a, m0 + r, lane);
         }
-        const int j = a.j0 + kb * BG_K + 2 * lane;       // observed pixel of this lane (and j + 1)
-        float wl0 = 0.f, wl1 = 0.f;
-        if (j < a.nspec) wl0 = __ldg(a.wl + j);
-        if (j + 1 < a.nspec) wl1 = __ldg(a.wl + j + 1);
-        // all 16 rows' loads are issued before any is used (the rows are independent)
-        float s00[16], s01[16], s10[16], s11[16], t0v[16], t1v[16];
+    } else {
+        // ---------------------------------------------------------------- band GEMM (warps 0..7)
+        const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
+        const float dl2 = (float)(a.dlnl * 1.4426950408889634);   // grid step in log2 units
+        const float inv_em1 = (float)(1.0 / expm1(a.dlnl));
+        // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
+        for (int kb = 0; kb < a.nkb; ++kb) {
+            const int s = kb & 1;
+            uint8_t *st = smem + s * stage_bytes;
+            if (kb >= 2) mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+            if (tid == 0) {
+                mbar_arrive_expect_tx(&bar_tma[s], 2 * b_bytes);
+                tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &bar_tma[s]);
+                tma_load_2d(st + 2 * BG_A_BYTES + b_bytes, &tm_c_lo, kb * BG_K, 0, &bar_tma[s]);
+            }
+            const int j = a.j0 + kb * BG_K + 2 * lane;       // observed pixel of this lane (and j + 1)
+            float wl0 = 0.f, wl1 = 0.f;
+            if (j < a.nspec) wl0 = __ldg(a.wl + j);
+            if (j + 1 < a.nspec) wl1 = __ldg(a.wl + j + 1);
+            // rows in two halves of 8: each half's loads are all issued before any is used
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+            float s00[8], s01[8], s10[8], s11[8], t0v[8], t1v[8];
 #pragma unroll
-        for (int rr = 0; rr < 16; ++rr) {
-            const int r = warp * 16 + rr;
-            const float4 zs = zsm[r];                     // n0, t, s, (0: rest frame, 2: no model)
-            const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec;
-            s00[rr] = s01[rr] = s10[rr] = s11[rr] = 0.f;
-            t0v[rr] = t1v[rr] = 0.f;
-            if (zs.w == 1.f) {
-                const int n0 = __float_as_int(zs.x);
-                const int sub = (zs.y > 0.f) ? 1 : 0;
-                int il0 = j - n0 - sub, il1 = il0 + 1;
-                float t0 = zs.y, t1 = zs.y;
-                if (il0 < 0 || il0 > a.nspec - 2) clamped_interval(j, zs.z, dlnl_f, em1, a.nspec, &il0, &t0);
-                if (il1 < 0 || il1 > a.nspec - 2) clamped_interval(j + 1, zs.z, dlnl_f, em1, a.nspec, &il1, &t1);
-                s00[rr] = __ldg(sp + il0); s01[rr] = __ldg(sp + il0 + 1);
-                s10[rr] = __ldg(sp + il1); s11[rr] = __ldg(sp + il1 + 1);
-                t0v[rr] = t0; t1v[rr] = t1;
-            } else if (zs.w == 0.f) {
-                // rest frame: v = s00 (t = 0)
-                if (j < a.nspec) s00[rr] = __ldg(sp + j);
-                if (j + 1 < a.nspec) s10[rr] = __ldg(sp + j + 1);
+            for (int rr = 0; rr < 8; ++rr) {
+                const int r = warp * 16 + h * 8 + rr;
+                const float4 zs = zsm[r];                     // n0, t, s, (0: rest frame, 2: no model)
+                const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec;
+                s00[rr] = s01[rr] = s10[rr] = s11[rr] = 0.f;
+                t0v[rr] = t1v[rr] = 0.f;
+                if (zs.w == 1.f) {
+                    const int n0 = __float_as_int(zs.x);
+                    const int sub = (zs.y > 0.f) ? 1 : 0;
+                    const int il0 = j - n0 - sub, il1 = il0 + 1;
+                    // intervals outside the grid extrapolate from the first / last one (the reference's clamped
+                    // find_interval): position t = (e^(x dlnl) - 1) / (e^dlnl - 1), x pixels from the interval start
+                    const int c0 = min(max(il0, 0), a.nspec - 2), c1 = min(max(il1, 0), a.nspec - 2);
+                    const float t0 = (c0 == il0) ? zs.y : (bg_ex2(((float)(j - c0) - zs.z) * dl2) - 1.f) * inv_em1;
+                    const float t1 = (c1 == il1) ? zs.y : (bg_ex2(((float)(j + 1 - c1) - zs.z) * dl2) - 1.f) * inv_em1;
+                    s00[rr] = __ldg(sp + c0); s01[rr] = __ldg(sp + c0 + 1);
+                    s10[rr] = __ldg(sp + c1); s11[rr] = __ldg(sp + c1 + 1);
+                    t0v[rr] = t0; t1v[rr] = t1;
+                } else if (zs.w == 0.f) {
+                    // rest frame: v = s00 (t = 0)
+                    if (j < a.nspec) s00[rr] = __ldg(sp + j);
+                    if (j + 1 < a.nspec) s10[rr] = __ldg(sp + j + 1);
+                }
+            }
+#pragma unroll
+            for (int rr = 0; rr < 8; ++rr) {
+                const int r = warp * 16 + h * 8 + rr;
+                float v0 = fmaf(t0v[rr], s01[rr] - s00[rr], s00[rr]);
+                float v1 = fmaf(t1v[rr], s11[rr] - s10[rr], s10[rr]);
+                if (v0 != v0) v0 = 0.f;
+                if (v1 != v1) v1 = 0.f;
+                const float f0 = fmaxf(v0, 0.f) * wl0;
+                const float f1 = fmaxf(v1, 0.f) * wl1;
+                const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
+                const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
+                const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
+                const uint32_t off = r * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2);
+                __nv_bfloat162 hh, ll;
+                hh.x = h0; hh.y = h1;
+                ll.x = l0; ll.y = l1;
+                *reinterpret_cast<__nv_bfloat162 *>(st + off) = hh;
+                *reinterpret_cast<__nv_bfloat162 *>(st + BG_A_BYTES + off) = ll;
+            }
+            }
+            fence_proxy_async_smem();
+            named_bar_sync(1, BG_BUILD_THREADS);
+            if (tid == 0) {
+                mbar_wait(&bar_tma[s], (kb >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+                tc_fence_after();
+                const uint32_t sa = smem_u32(st);
+                const uint32_t ahi = sa, alo = sa + BG_A_BYTES, bhi = sa + 2 * BG_A_BYTES, blo = bhi + b_bytes;
+#pragma unroll
+                for (int k = 0; k < BG_K / 16; ++k) {
+                    const uint32_t o = k * 32;
+                    mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                    mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
+                    mma_bf16(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
+                }
+                mma_commit(&bar_mma[s]);
             }
         }
-#pragma unroll
-        for (int rr = 0; rr < 16; ++rr) {
-            const int r = warp * 16 + rr;
-            float v0 = fmaf(t0v[rr], s01[rr] - s00[rr], s00[rr]);
-            float v1 = fmaf(t1v[rr], s11[rr] - s10[rr], s10[rr]);
-            if (v0 != v0) v0 = 0.f;
-            if (v1 != v1) v1 = 0.f;
-            const float f0 = fmaxf(v0, 0.f) * wl0;
-            const float f1 = fmaxf(v1, 0.f) * wl1;
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
-            const uint32_t off = r * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2);
-            __nv_bfloat162 hh, ll;
-            hh.x = h0; hh.y = h1;
-            ll.x = l0; ll.y = l1;
-            *reinterpret_cast<__nv_bfloat162 *>(st + off) = hh;
-            *reinterpret_cast<__nv_bfloat162 *>(st + BG_A_BYTES + off) = ll;
-        }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            mbar_wait(&bar_tma[s], (kb >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
-            tc_fence_after();
-            const uint32_t sa = smem_u32(st);
-            const uint32_t ahi = sa, alo = sa + BG_A_BYTES, bhi = sa + 2 * BG_A_BYTES, blo = bhi + b_bytes;
-#pragma unroll
-            for (int k = 0; k < BG_K / 16; ++k) {
-                const uint32_t o = k * 32;
-                mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, (kb > 0 || k > 0) ? 1u : 0u);
-                mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
-                mma_bf16(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
-            }
-            mma_commit(&bar_mma[s]);
-        }
-    }
-    if (tid == 0) mma_commit(bar_done);
-    mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
-    tc_fence_after();
+        if (tid == 0) mma_commit(bar_done);
+        mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
+        tc_fence_after();
 
-    // epilogue: warps 0..3 read their lane quarter (one model per thread)
-    if (warp < 4) {
-        const int r = warp * 32 + lane, m = m0 + r;
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int c0 = 0; c0 < npad; c0 += 32) {
-            float v[32];
-            tmem_ld32(trow + c0, v);
-            if (m < a.n_models) {
+        // epilogue: warps 0..3 read their lane quarter (one model per thread)
+        if (warp < 4) {
+            const int r = warp * 32 + lane, m = m0 + r;
+            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+            for (int c0 = 0; c0 < npad; c0 += 32) {
+                float v[32];
+                tmem_ld32(trow + c0, v);
+                if (m < a.n_models) {
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int b = c0 + i;
-                    if (b < a.nbands) {
-                        const double f = (double)v[i];
-                        if (a.fband) a.fband[(size_t)m * a.nbands + b] = f;
-                        if (a.mags) {
-                            double mg = __longlong_as_double(0x7ff8000000000000LL);
-                            if (a.do_band == nullptr || a.do_band[b] != 0)
-                                mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) - a.zp +
-                                     a.dist[m];
-                            a.mags[(size_t)m * a.nbands + b] = mg;
+                    for (int i = 0; i < 32; ++i) {
+                        const int b = c0 + i;
+                        if (b < a.nbands) {
+                            const double f = (double)v[i];
+                            if (a.fband) a.fband[(size_t)m * a.nbands + b] = f;
+                            if (a.mags) {
+                                double mg = __longlong_as_double(0x7ff8000000000000LL);
+                                if (a.do_band == nullptr || a.do_band[b] != 0)
+                                    mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) -
+                                         a.zp + a.dist[m];
+                                a.mags[(size_t)m * a.nbands + b] = mg;
+                            }
                         }
                     }
                 }

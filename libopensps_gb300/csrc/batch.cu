@@ -66,7 +66,14 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
         b[5] = b[1];
     }
     // the cap (apply_igm_z :4272-4299): the first pixel of the largest optical depth, searched by the whole warp for
-    // each of its models in turn
+    // each of its models in turn, over the wavelength factors staged in shared memory (one array per factor)
+    extern __shared__ float sa[];    // 6 x jtop
+    const int nj = a.add_igm ? a.jtop : 0;
+    for (int i = threadIdx.x; i < 6 * nj; i += blockDim.x) {
+        const int j = i / 6, k = i % 6;
+        sa[k * nj + j] = a.igm_a[i];
+    }
+    __syncthreads();
     float my_tmax = 0.f;
     int my_jmax = 1;
     const unsigned todo = __ballot_sync(0xffffffffu, igm);
@@ -77,9 +84,9 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
         for (int k = 0; k < 6; ++k) bb[k] = __shfl_sync(0xffffffffu, b[k], i);
         float tmax = 0.f;
         int jmax = 1;
-        for (int j = lane; j < a.jtop; j += 32) {
-            const float *ia = a.igm_a + (size_t)j * 6;
-            const float t = ia[0] * bb[0] + ia[1] * bb[1] + ia[2] * bb[2] + ia[3] * bb[3] + ia[4] * bb[4] + ia[5] * bb[5];
+        for (int j = lane; j < nj; j += 32) {
+            const float t = sa[j] * bb[0] + sa[nj + j] * bb[1] + sa[2 * nj + j] * bb[2] + sa[3 * nj + j] * bb[3] +
+                            sa[4 * nj + j] * bb[4] + sa[5 * nj + j] * bb[5];
             if (t > tmax) { tmax = t; jmax = j + 1; }
         }
 #pragma unroll
@@ -491,7 +498,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
     ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zinfo = c.d_zinfo.p; ma.dist = c.d_dist.p;
     ma.lnlam = c.d_lnlam.p;
-    model_params_kernel<<<(n + 255) / 256, 256, 0, c.side>>>(ma);
+    {
+        const int smem = (c.add_igm_absorption == 1 ? c.jtop : 0) * 6 * (int)sizeof(float);
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(model_params_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) {
+            err = cuda_msg("model parameter kernel", e);
+            return ST_DATA_MISSING;
+        }
+        model_params_kernel<<<(n + 255) / 256, 256, smem, c.side>>>(ma);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(c.ev_params, c.side)) != cudaSuccess) {
         err = cuda_msg("model parameter kernel", e);
         return ST_DATA_MISSING;
@@ -531,7 +546,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);
-    int launches = 4;   // weight operand, model parameters, FP64 sums, contraction
+    int launches = 3;   // weight operand, model parameters, contraction
 
     // ---- bands and magnitudes
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
@@ -550,13 +565,17 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
         ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
         ba.status = c.d_status.p;
+        ba.wz = d_wz; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = c.d_sums.p; ba.nt = nt; ba.ntz = nt * nz;
+        ba.parts = wa.parts; ba.itesc = itesc;
         if ((e = run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
         ++launches;
     }
     prof_mark(c, 4);
-    // the FP64 mass and L_bol sums (alone: a kernel beside the contraction or the band GEMM slows them more than it
-    // takes itself)
-    if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+    // the FP64 mass and L_bol sums: formed by the band GEMM's spare warps, or here when there are no magnitudes
+    if (!want_mags) {
+        if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+        ++launches;
+    }
     prof_mark(c, 5);
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {

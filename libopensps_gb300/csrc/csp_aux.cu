@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
 #pragma unroll 4
     for (int k = lane; k < ntz; k += 32) {
         const double wv = __ldg(w + k);
-        if (wv > DBL_MIN) {
+        if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
             const double mk = wv * __ldg(a.mass + k), lk = wv * __ldg(a.llin + k);
             ms += mk;
             ls += lk;

@@ -94,6 +94,11 @@ struct BandGemmArgs {
     double *fband;          // n_models x nbands (may be null)
     double *mags;           // n_models x nbands (may be null)
     int *status;
+    // the FP64 mass / L_bol sums formed beside the GEMM (sums null: none)
+    const double *wz;       // n_models x ntz, age fastest
+    const double *mass, *llin;   // ntz
+    double *sums;           // n_models x 6 (as WeightsArgs::sums)
+    int nt, ntz, parts, itesc;
 };
 int band_gemm_npad(int nbands);
 cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
