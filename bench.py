@@ -246,7 +246,7 @@ def run_ours(args) -> None:
                          "traffic": traffic, "kernel": "csp_contract_kernel<1>",
                          "peak_src": f"{pk['src']} sustained bf16",
                          "stage_ms": dict(zip(["weight_operand", "wait_model_params", "contract", "bands",
-                                               "fp64_sums_alone"], ktimes))},
+                                               "fp64_sums"], ktimes))},
             "cpu_baseline": cpu,
             "gpu_launches": launches * args.steps,
             "clocks": clk,

@@ -13,8 +13,8 @@
 // fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes. Two stages:
 // the builders fill stage s + 1 while the tensor core works on stage s.
 //
-// Warps 8 and 9 meanwhile form the FP64 sums of model_sums_zw (src/physics/opensps_csp_batch.f90:2090-2120) for the
-// CTA's 128 models: the band GEMM waits on memory and leaves the FP64 pipes idle, which GB300 has few of.
+// With args.sums set, warps 8 and 9 form the FP64 sums of model_sums_zw (src/physics/opensps_csp_batch.f90:2090-2120)
+// for the CTA's 128 models (measured slower than the separate sums kernel; the batch does not set it).
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cfloat>

@@ -565,17 +565,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
         ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
         ba.status = c.d_status.p;
-        ba.wz = d_wz; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = c.d_sums.p; ba.nt = nt; ba.ntz = nt * nz;
+        ba.wz = d_wz; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = nullptr; ba.nt = nt; ba.ntz = nt * nz;
         ba.parts = wa.parts; ba.itesc = itesc;
         if ((e = run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
         ++launches;
     }
     prof_mark(c, 4);
-    // the FP64 mass and L_bol sums: formed by the band GEMM's spare warps, or here when there are no magnitudes
-    if (!want_mags) {
-        if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
-        ++launches;
-    }
+    // the FP64 mass and L_bol sums (alone: beside the contraction or the band GEMM they slow those more than they take)
+    if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+    ++launches;
     prof_mark(c, 5);
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {
