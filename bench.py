@@ -245,7 +245,7 @@ def run_ours(args) -> None:
                          "unit": "TFLOP/s", "frac": (achieved / pk["bf16_tflops_sustained"]) if achieved else None,
                          "traffic": traffic, "kernel": "csp_contract_kernel<1>",
                          "peak_src": f"{pk['src']} sustained bf16",
-                         "stage_ms": dict(zip(["weight_operand", "wait_model_params", "contract", "bands",
+                         "stage_ms": dict(zip(["model_params", "weight_operand", "contract", "bands",
                                                "fp64_sums"], ktimes))},
             "cpu_baseline": cpu,
             "gpu_launches": launches * args.steps,

@@ -488,11 +488,9 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
 
-    // ---- fork: the per-model parameters on a side stream, beside the weight operand
-    if ((e = cudaEventRecord(c.ev_fork, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side, c.ev_fork, 0)) != cudaSuccess) {
-        err = cuda_msg("fork", e);
-        return ST_DATA_MISSING;
-    }
+    // ---- the per-model parameters, then the weight operand (one stream: run side by side they took longer than in
+    // turn)
+    prof_mark(c, 0);
     ModelParamArgs ma;
     ma.n = n; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
     ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
@@ -505,12 +503,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("model parameter kernel", e);
             return ST_DATA_MISSING;
         }
-        model_params_kernel<<<(n + 255) / 256, 256, smem, c.side>>>(ma);
+        model_params_kernel<<<(n + 255) / 256, 256, smem, st>>>(ma);
     }
-    if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaEventRecord(c.ev_params, c.side)) != cudaSuccess) {
+    if ((e = cudaGetLastError()) != cudaSuccess) {
         err = cuda_msg("model parameter kernel", e);
         return ST_DATA_MISSING;
     }
+    prof_mark(c, 1);
     WeightsArgs wa;
     wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.kmap = bop->kmap.p;
     wa.wz = d_wz; wa.mass = c.d_mass.p; wa.llin = c.d_llin.p; wa.w_hi = c.d_whi.p; wa.w_lo = c.d_wlo.p;
@@ -518,11 +517,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
     wa.grid = 0;
-    // ---- main stream: the weight operand, then the contraction once the parameters are there
-    prof_mark(c, 0);
     if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
-    prof_mark(c, 1);
-    if ((e = cudaStreamWaitEvent(st, c.ev_params, 0)) != cudaSuccess) { err = cuda_msg("join", e); return ST_DATA_MISSING; }
     prof_mark(c, 2);
 
     // ---- contraction + epilogue
