@@ -259,7 +259,7 @@ class Context:
         _check(st, self.lib)
 
     def kernel_times(self) -> list[float]:
-        """Device ms of the last batch's stages: weights, model parameters, contraction, bands."""
+        """Mean device ms of the profiled batches' stages: model parameters, weight operand, contraction, bands, FP64 sums."""
         buf, n, st = np.zeros(8), C.c_int(0), C.c_int(0)
         self.lib.opensps_gb300_kernel_times(self.handle, _ptr(buf), 8, C.byref(n), C.byref(st))
         _check(st, self.lib)

@@ -458,3 +458,47 @@ void oracle_csp_batch(const oracle_grid_t *g, int n, const double *wz, const dou
 
 int oracle_npar(void) { return P_NPAR; }
 double oracle_abs_mag_zeropoint_log(void) { return abs_mag_zeropoint_log(); }
+
+/* ------------------------------------------------------------------------------------------ */
+/* IMF bin integrals                                                                           */
+/* ------------------------------------------------------------------------------------------ */
+
+/* exp(y) - 1 by the Taylor series to y^13 below |y| = 1/4, exp(y) - 1 above (expm1_series,
+ * src/physics/opensps_imf.f90:624-650; the same nested multiply-adds). */
+double oracle_expm1_series(double y) {
+    if (fabs(y) < 0.25) {
+        double r = 1.0 + y * (1.0 / 13);
+        r = 1.0 + y * (1.0 / 12) * r;
+        r = 1.0 + y * (1.0 / 11) * r;
+        r = 1.0 + y * (1.0 / 10) * r;
+        r = 1.0 + y * (1.0 / 9) * r;
+        r = 1.0 + y * (1.0 / 8) * r;
+        r = 1.0 + y * (1.0 / 7) * r;
+        r = 1.0 + y * (1.0 / 6) * r;
+        r = 1.0 + y * (1.0 / 5) * r;
+        r = 1.0 + y * (1.0 / 4) * r;
+        r = 1.0 + y * (1.0 / 3) * r;
+        r = 1.0 + y * (1.0 / 2) * r;
+        return y * r;
+    }
+    return exp(y) - 1.0;
+}
+
+/* ln(m2 / m1) as log1p((m2 - m1) / m1) in Kahan's form (imf_bin_logs, src/physics/opensps_imf.f90:564-580). */
+double oracle_bin_dl(double m1, double m2) {
+    if (m1 <= 0.0 || m2 <= m1) return 0.0;
+    double x = (m2 - m1) / m1, u = 1.0 + x;
+    return (u == 1.0) ? x : log(u) * x / (u - 1.0);
+}
+
+/* The number of stars of a power-law bin, int_lo^hi c m^-alpha dm, in the table form of imf_bin_weights_tab
+ * (src/physics/opensps_imf.f90:519-548, FP64 build): c / e * lo^e * expm1(e dl) with e = 1 - alpha, dl = ln(hi/lo);
+ * c dl at e = 0. */
+double oracle_powerlaw_bin(double alpha, double c, double lo, double hi) {
+    double e = 1.0 - alpha;
+    double dl = oracle_bin_dl(lo, hi);
+    if (e == 0.0) return c * dl;
+    double ce = c / e;
+    double plo = exp(e * log(lo));
+    return ce * plo * oracle_expm1_series(e * dl);
+}

@@ -1,0 +1,91 @@
+"""The FP64 oracle pinned against the reference's known answers and identities (CPU only).
+
+* the IMF power-law bin integrals against the reference's 60-digit known-answer table
+  (tests/golden/imf_powerlaw_bins.txt, made by the reference's own generator), within 1e-14 as the reference's
+  test_powerlaw_bin_worst_cases;
+* identities the reference's batch tests use (tests/test_csp_batch.f90): with no dust, IGM, lines or smoothing the
+  spectrum is sum_k w_k SSP_k; linearity in the weights; the velocity-smoothing rows sum to one; the distance term.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def olib():
+    from oracle import oracle
+    L = oracle.lib()
+    L.oracle_powerlaw_bin.restype = C.c_double
+    L.oracle_powerlaw_bin.argtypes = [C.c_double] * 4
+    return L
+
+
+def test_imf_powerlaw_bins_known_answers(olib):
+    lines = (GOLDEN / "imf_powerlaw_bins.txt").read_text().splitlines()
+    n = int(lines[1])
+    rows = [tuple(float(x) for x in l.split()) for l in lines[2:2 + n]]
+    assert len(rows) == n == 444
+    worst = 0.0
+    for alpha, lo, hi, ref in rows:
+        got = olib.oracle_powerlaw_bin(alpha, 1.0, lo, hi)
+        worst = max(worst, abs(got / ref - 1.0))
+    assert worst <= 1e-14, worst
+
+
+def _oracle(data, **kw):
+    from oracle.oracle import Oracle
+    return Oracle(data, **kw)
+
+
+def test_no_dust_sum_of_ssps(data):
+    o = _oracle(data, add_neb=False, add_igm=False, smooth=False)
+    rng = np.random.default_rng(0)
+    wz = rng.dirichlet(np.ones(12 * 107), size=5).reshape(5, 12, 107)
+    r = o.csp_batch({}, wz)
+    ref = np.einsum("mzt,zts->ms", wz, data["ssp_spec"])
+    np.testing.assert_allclose(r["spec"], ref, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(r["mass"], np.einsum("mzt,zt->m", wz, data["ssp_mass"]), rtol=1e-12)
+
+
+def test_linear_in_weights(data):
+    o = _oracle(data)
+    rng = np.random.default_rng(1)
+    w1 = rng.dirichlet(np.ones(1284), size=3).reshape(3, 12, 107)
+    w2 = rng.dirichlet(np.ones(1284), size=3).reshape(3, 12, 107)
+    p = {"dust2": np.array([0.3, 1.0, 2.0]), "zred": np.array([0.5, 2.0, 4.0]), "sigma_smooth": [100.0, 150.0, 250.0]}
+    a, b, ab = o.csp_batch(p, w1), o.csp_batch(p, w2), o.csp_batch(p, w1 + 2.0 * w2)
+    np.testing.assert_allclose(ab["spec"], a["spec"] + 2.0 * b["spec"], rtol=1e-11, atol=1e-300)
+
+
+def test_velocity_rows_normalised(data):
+    o = _oracle(data)
+    for sigma in (50.0, 150.0, 300.0):
+        i = int(np.searchsorted(o.lam, 5000.0))
+        lo, coef = o.velocity_row(sigma, i)
+        assert coef.size in (3, 5, 7, 9)
+        assert lo == i - coef.size // 2
+        assert abs(coef.sum() - 1.0) < 1e-14
+        # nearly symmetric on a log-uniform grid (the trapezoid widths grow by e^dlnl per pixel)
+        np.testing.assert_allclose(coef, coef[::-1], rtol=3e-3)
+
+
+def test_distance_term(data):
+    o = _oracle(data)
+    assert o.distance_term(0.0) == 0.0
+    d1, d2 = o.distance_term(1.0), o.distance_term(2.0)
+    assert 43.0 < d1 < 44.5 and d2 > d1
+
+
+def test_igm_only_below_lyman_alpha(data):
+    o = _oracle(data, add_neb=False, smooth=False)
+    rng = np.random.default_rng(2)
+    wz = rng.dirichlet(np.ones(1284), size=2).reshape(2, 12, 107)
+    a = o.csp_batch({"zred": np.array([3.0, 3.0])}, wz)
+    b = _oracle(data, add_neb=False, add_igm=False, smooth=False).csp_batch({"zred": np.array([3.0, 3.0])}, wz)
+    red = o.lam >= 1215.67
+    np.testing.assert_array_equal(a["spec"][:, red], b["spec"][:, red])
+    assert np.all(a["spec"][:, ~red] <= b["spec"][:, ~red])
