@@ -230,6 +230,27 @@ class Context:
         del keep
         return out
 
+    def csp_batch_parts(self, params: dict, ssp_weights: np.ndarray, emlines: bool = True) -> dict:
+        """compute_csp_batch_parts: the batch with the intrinsic young and old age sums (weights (n, nt))."""
+        w = np.ascontiguousarray(ssp_weights, dtype=np.float64)
+        n = w.shape[0]
+        ns, nb, nl = self.nspec, self.nbands, self.nemline
+        k, c_names, c_vals, keep = _names_values(params, n)
+        out = {"mags": np.empty((n, nb)), "spec": np.empty((n, ns)), "mass": np.empty(n), "lbol": np.empty(n),
+               "young": np.empty((n, ns)), "old": np.empty((n, ns)), "mass_young": np.empty(n),
+               "mass_old": np.empty(n), "lbol_young": np.empty(n), "lbol_old": np.empty(n)}
+        if emlines:
+            out["emlines"] = np.empty((n, nl))
+        st = C.c_int(0)
+        self.lib.opensps_context_compute_csp_batch_parts(
+            self.handle, n, k, c_names, c_vals, _ptr(w), _ptr(out["mags"]), _ptr(out["spec"]), _ptr(out["mass"]),
+            _ptr(out["lbol"]), None, None, _ptr(out.get("emlines")), None, _ptr(out["young"]), _ptr(out["old"]),
+            _ptr(out["mass_young"]), _ptr(out["mass_old"]), _ptr(out["lbol_young"]), _ptr(out["lbol_old"]),
+            C.byref(st))
+        _check(st, self.lib)
+        del keep
+        return out
+
     def batch_device(self, n: int, d_params: int, d_wz: int, d_mags: int | None, sync: bool = True):
         """opensps_gb300_batch_device with device pointers (integers, e.g. torch.Tensor.data_ptr())."""
         st = C.c_int(0)

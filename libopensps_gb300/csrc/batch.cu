@@ -370,6 +370,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
         if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
+        if (io.young || io.old) nacc2 = true;   // the parts need the young and old sums apart
         const double sig = par(m, PF_SIGMA_SMOOTH);
         if (sig > SAFE_FLOOR) {
             any_smooth = true;
@@ -538,6 +539,16 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
     ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
     ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
+    ca.young = ca.old = nullptr;
+    const bool parts = (io.young || io.old) && !io.dev_inputs;
+    if (parts) {
+        if ((e = c.d_young.reserve((size_t)n * ns)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns)) != cudaSuccess) {
+            err = cuda_msg("device memory", e);
+            return ST_DATA_MISSING;
+        }
+        ca.young = c.d_young.p;
+        ca.old = c.d_old.p;
+    }
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);
@@ -589,6 +600,55 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return 0;
     }
 
+    // ---- emission-line luminosities (with nebular emission)
+    const bool want_eml = io.emlines && neb && !io.dev_inputs;
+    if (want_eml) {
+        if (c.eml_nnz < 0) {
+            // the (age, metallicity) entries with lines, and their luminosities as FP32 (once per context)
+            std::vector<int> kidx;
+            std::vector<float> lum;
+            for (int k = 0; k < nt * nz; ++k) {
+                bool any = false;
+                for (int l = 0; l < c.nline; ++l) any = any || c.line_lum[l + (size_t)c.nline * k] != 0.0;
+                if (!any) continue;
+                kidx.push_back(k);
+                for (int l = 0; l < c.nline; ++l) lum.push_back((float)c.line_lum[l + (size_t)c.nline * k]);
+            }
+            if ((e = c.d_eml_kidx.reserve(std::max<size_t>(kidx.size(), 1))) != cudaSuccess ||
+                (e = c.d_eml_lum.reserve(std::max<size_t>(lum.size(), 1))) != cudaSuccess ||
+                (!kidx.empty() && (e = cudaMemcpy(c.d_eml_kidx.p, kidx.data(), sizeof(int) * kidx.size(), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+                (!lum.empty() && (e = cudaMemcpy(c.d_eml_lum.p, lum.data(), sizeof(float) * lum.size(), cudaMemcpyHostToDevice)) != cudaSuccess)) {
+                err = cuda_msg("line table", e);
+                return ST_DATA_MISSING;
+            }
+            c.eml_nnz = (int)kidx.size();
+        }
+        EmlineArgs ea;
+        ea.n_models = n; ea.nline = c.nline; ea.ntz = nt * nz; ea.nnz = c.eml_nnz; ea.wz = d_wz;
+        ea.kidx = c.d_eml_kidx.p; ea.lum = c.d_eml_lum.p;
+        if ((e = c.d_eml.reserve((size_t)n * c.nline)) != cudaSuccess) { err = cuda_msg("device memory", e); return ST_DATA_MISSING; }
+        ea.eml = c.d_eml.p;
+        if ((e = run_emlines(ea, st)) != cudaSuccess) { err = cuda_msg("line kernel", e); return ST_DATA_MISSING; }
+        ++c.last_launches;
+    }
+    std::vector<float> eml_h, young_h, old_h;
+    if (want_eml) {
+        eml_h.resize((size_t)n * c.nline);
+        if ((e = cudaMemcpyAsync(eml_h.data(), c.d_eml.p, sizeof(float) * eml_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("line copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+    if (parts) {
+        young_h.resize((size_t)n * ns);
+        old_h.resize((size_t)n * ns);
+        if ((e = cudaMemcpyAsync(young_h.data(), c.d_young.p, sizeof(float) * young_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(old_h.data(), c.d_old.p, sizeof(float) * old_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("parts copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+
     // ---- outputs
     if (io.spec && !io.dev_inputs) {
         if ((e = c.d_spec64.reserve((size_t)n * ns)) != cudaSuccess ||
@@ -635,6 +695,14 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if (io.mass_old) io.mass_old[m] = s[3];
             if (io.lbol_young) io.lbol_young[m] = std::log10(std::max(s[4], SAFE_FLOOR));
             if (io.lbol_old) io.lbol_old[m] = std::log10(std::max(s[5], SAFE_FLOOR));
+        }
+    }
+    if (want_eml)
+        for (size_t i = 0; i < eml_h.size(); ++i) io.emlines[i] = (double)eml_h[i];
+    if (parts) {
+        for (size_t i = 0; i < young_h.size(); ++i) {
+            if (io.young) io.young[i] = (double)young_h[i];
+            if (io.old) io.old[i] = (double)old_h[i];
         }
     }
     if (io.sfr) for (int m = 0; m < n; ++m) io.sfr[m] = std::nan("");

@@ -158,7 +158,7 @@ Context::~Context() {
     d_lam.release(); d_lnlam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
-    d_status.release();
+    d_status.release(); d_young.release(); d_old.release(); d_eml.release(); d_eml_lum.release(); d_eml_kidx.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
@@ -406,6 +406,7 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     if (st != 0) return st;
     for (auto &kv : c.basis_cache) { kv.second->hi.release(); kv.second->lo.release(); delete kv.second; }
     c.basis_cache.clear();
+    c.eml_nnz = -1;
     c.is_setup = true;
     return 0;
 }

@@ -97,7 +97,9 @@ struct Context {
     DevBuf<double> d_wz, d_params, d_sums, d_dist, d_fband, d_mags, d_spec64;
     DevBuf<float4> d_zinfo;
     DevBuf<__nv_bfloat16> d_whi, d_wlo;
-    DevBuf<float> d_mpar, d_spec;
+    DevBuf<float> d_mpar, d_spec, d_young, d_old, d_eml, d_eml_lum;
+    DevBuf<int> d_eml_kidx;
+    int eml_nnz = -1;            // entries of the line table (-1: not built)
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch

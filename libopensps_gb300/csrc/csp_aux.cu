@@ -103,6 +103,28 @@ cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------- emission lines
+// line_profiles' luminosities (src/physics/opensps_csp_batch.f90:3133-3166 with the line table of the ages that have
+// lines): one block per model, one thread per line, over the (age, metallicity) entries with lines.
+__global__ void emlines_kernel(EmlineArgs a) {
+    const int m = blockIdx.x;
+    const double *w = a.wz + (size_t)m * a.ntz;
+    for (int l = threadIdx.x; l < a.nline; l += blockDim.x) {
+        float s = 0.f;
+        for (int i = 0; i < a.nnz; ++i) {
+            const float wv = weight_to_f32(__ldg(w + __ldg(a.kidx + i)));
+            s = fmaf(wv, __ldg(a.lum + (size_t)i * a.nline + l), s);
+        }
+        a.eml[(size_t)m * a.nline + l] = s;
+    }
+}
+
+cudaError_t run_emlines(const EmlineArgs &a, cudaStream_t st) {
+    if (a.n_models <= 0 || a.nline <= 0) return cudaSuccess;
+    emlines_kernel<<<a.n_models, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------- casts
 __global__ void spec_to_f64_kernel(const float *src, int ld, int nspec, int n_models, double *dst) {
     const size_t total = (size_t)nspec * n_models;

@@ -258,6 +258,11 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
                     const float curve = args.uniform_index ? curve_u : ex2(d0.w * ltab2);
                     float ss;
                     if constexpr (NACC == 2) {
+                        if (args.young && inpix && r >= HALO && r < BM - HALO && m0 + col0 + j < args.n_models) {
+                            // the parts: young and old age sums before dust (compute_csp_batch_parts)
+                            args.young[(size_t)(m0 + col0 + j) * args.ld_spec + p] = y[j];
+                            args.old[(size_t)(m0 + col0 + j) * args.ld_spec + p] = o[j];
+                        }
                         const float4 d1 = *reinterpret_cast<const float4 *>(mp + 4);  // kd1, d1 index, 1-fo, fo
                         const float kd3 = mp[MP_KD3];
                         const float tb = (d1.x != 0.f) ? ex2(d1.x * ex2(d1.y * ltab2)) : 1.f;

@@ -47,6 +47,7 @@ struct ContractArgs {
     const float *pix;    // nspec x PIX_FLOATS
     const float *mpar;   // n_models x MODEL_PAR_FLOATS
     float *spec;         // n_models x ld_spec (pixel fastest)
+    float *young, *old;  // NACC = 2 only, may be null: the age sums before dust (n_models x ld_spec)
     int *status;
 };
 
@@ -103,6 +104,16 @@ struct BandGemmArgs {
 int band_gemm_npad(int nbands);
 cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
                           cudaStream_t st);
+
+// Emission-line luminosities: eml(l, m) = sum_k w(k, m) L(l, k) over the (age, metallicity) entries with lines.
+struct EmlineArgs {
+    int n_models, nline, ntz, nnz;
+    const double *wz;       // n_models x ntz
+    const int *kidx;        // nnz source indices k with line luminosity
+    const float *lum;       // nnz x nline: L(l, kidx[i])
+    float *eml;             // n_models x nline
+};
+cudaError_t run_emlines(const EmlineArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

@@ -111,3 +111,31 @@ def test_weights_over_ages_blended_at_logzsol(ctx, oracle40, data):
     ora = oracle40.csp_batch({k: v for k, v in params.items() if k != "logzsol"}, wz)
     ora["lbol"] = lbol
     _compare(got, ora)
+
+
+def test_parts_and_emission_lines(ctx, oracle40, data):
+    """compute_csp_batch_parts: the young and old age sums (nebular lines in the young), their masses and L_bol, and
+    the emission-line luminosities."""
+    n = 45
+    rng = np.random.default_rng(31)
+    w = rng.dirichlet(np.ones(107), size=n)
+    logzsol = rng.uniform(-1.9, 0.4, n)
+    _, params = config3_inputs(n, seed=32)
+    params = dict(params, logzsol=logzsol, dust1=rng.uniform(0.0, 1.0, n))
+    got = ctx.csp_batch_parts(params, w)
+    lz = np.log10(data["zlegend"] / 0.0142)
+    wz = np.zeros((n, 12, 107))
+    for m in range(n):
+        zlo = min(max(np.searchsorted(lz, logzsol[m], side="right") - 1, 0), 10)
+        dz = (logzsol[m] - lz[zlo]) / (lz[zlo + 1] - lz[zlo])
+        wz[m, zlo] = (1 - dz) * w[m]
+        wz[m, zlo + 1] = dz * w[m]
+    ora = oracle40.csp_batch({k: v for k, v in params.items() if k != "logzsol"}, wz, young=True, emlines=True)
+    assert rel_err_spec(got["young"], ora["young"]) <= 1e-4
+    assert rel_err_spec(got["old"], ora["old"]) <= 1e-4
+    assert rel_err_spec(got["spec"], ora["spec"]) <= 1e-4
+    young_ages = data["log_age"] <= 7.0
+    np.testing.assert_allclose(got["mass_young"], np.einsum("mzt,zt->m", wz[:, :, young_ages],
+                                                            data["ssp_mass"][:, young_ages]), rtol=1e-12)
+    np.testing.assert_allclose(got["mass_young"] + got["mass_old"], got["mass"], rtol=1e-12)
+    np.testing.assert_allclose(got["emlines"], ora["emlines"], rtol=1e-5)
