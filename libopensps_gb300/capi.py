@@ -108,6 +108,14 @@ def _ptr(a):
     return a.ctypes.data_as(_dp)
 
 
+def nbgrad(lib: C.CDLL | None = None) -> int:
+    """opensps_get_nbgrad: the rows of params_bar the gradient entry points write."""
+    lib = lib or load_library()
+    v = C.c_int(0)
+    lib.opensps_get_nbgrad(C.byref(v))
+    return v.value
+
+
 def _check(status: C.c_int, lib: C.CDLL):
     if status.value != 0:
         st = C.c_int(0)
@@ -226,6 +234,36 @@ class Context:
             self.lib.opensps_context_compute_csp_batch(
                 self.handle, n, k, c_names, c_vals, _ptr(w), _ptr(out["mags"]), _ptr(out.get("spec")),
                 _ptr(out.get("mass")), _ptr(out.get("lbol")), None, None, None, None, C.byref(st))
+        _check(st, self.lib)
+        del keep
+        return out
+
+    def csp_batch_grad(self, params: dict, ssp_weights_z: np.ndarray, mags_bar: np.ndarray | None = None,
+                       spec_bar: np.ndarray | None = None, mass_bar: np.ndarray | None = None,
+                       lbol_bar: np.ndarray | None = None, params_bar_rows: int | None = None,
+                       weights_z_bar: bool = True) -> dict:
+        """compute_csp_batch_grad_rows: the forward batch and the reverse pass for the given cotangents (arrays
+        (n, nbands), (n, nspec), (n,), (n,)). Returns the forward outputs, params_bar (n, rows) and weights_z_bar
+        (n, nz, nt)."""
+        w = np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
+        n = w.shape[0]
+        ns, nb, nt, nz = self.nspec, self.nbands, self.ntfull, self.nz
+        rows = params_bar_rows if params_bar_rows is not None else nbgrad(self.lib)
+        k, c_names, c_vals, keep = _names_values(params, n)
+        cot = {}
+        for name, arr in (("mags_bar", mags_bar), ("spec_bar", spec_bar), ("mass_bar", mass_bar),
+                          ("lbol_bar", lbol_bar)):
+            cot[name] = None if arr is None else np.ascontiguousarray(arr, dtype=np.float64)
+        out = {"mags": np.empty((n, nb)), "spec": np.empty((n, ns)), "mass": np.empty(n), "lbol": np.empty(n),
+               "params_bar": np.full((n, rows), np.nan)}
+        if weights_z_bar:
+            out["weights_z_bar"] = np.empty((n, nz, nt))
+        st = C.c_int(0)
+        self.lib.opensps_context_compute_csp_batch_grad_rows(
+            self.handle, n, k, c_names, c_vals, None, _ptr(w), None, _ptr(cot["mags_bar"]), _ptr(cot["spec_bar"]),
+            _ptr(cot["mass_bar"]), _ptr(cot["lbol_bar"]), _ptr(out["mags"]), _ptr(out["spec"]), _ptr(out["mass"]),
+            _ptr(out["lbol"]), None, None, None, None, _ptr(out["params_bar"]), rows, None,
+            _ptr(out.get("weights_z_bar")), C.byref(st))
         _check(st, self.lib)
         del keep
         return out

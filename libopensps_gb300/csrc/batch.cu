@@ -10,24 +10,6 @@
 
 namespace sps {
 
-// ---------------------------------------------------------------------------------------------- find_interval
-// 0-based index i with a[i] <= v < a[i + 1] for ascending or descending a (bisection over 0..n+1 as the reference's
-// find_interval, src/math/opensps_interpolation.f90:152-197, with its end cases), as the reference's 1-based
-// result minus one (so -1 below an ascending table).
-__host__ __device__ static int find_interval0(const double *a, int n, double v) {
-    if (n < 2) return 0;
-    const bool asc = a[n - 1] >= a[0];
-    int lower = 0, upper = n + 1;
-    while (upper - lower > 1) {
-        const int mid = (upper + lower) / 2;
-        const bool ge = v >= a[mid - 1];
-        if (asc == ge) lower = mid; else upper = mid;
-    }
-    if (v == a[0]) return 0;
-    if (v == a[n - 1]) return n - 2;
-    return lower - 1;
-}
-
 // ---------------------------------------------------------------------------------------------- model params
 struct ModelParamArgs {
     int n, nspec, jtop, add_igm, smooth, i0;   // i0: the pixel whose smoothing row gives the model's taps
@@ -370,7 +352,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
         if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
-        if (io.young || io.old) nacc2 = true;   // the parts need the young and old sums apart
+        if (io.young || io.old || io.keep_parts) nacc2 = true;   // the parts need the young and old sums apart
         const double sig = par(m, PF_SIGMA_SMOOTH);
         if (sig > SAFE_FLOOR) {
             any_smooth = true;
@@ -450,6 +432,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     int sm_lo = ns, sm_hi = -1;
     for (int j = 0; j < ns; ++j)
         if (c.lam[j] >= minl && c.lam[j] <= maxl) { sm_lo = std::min(sm_lo, j); sm_hi = std::max(sm_hi, j); }
+
+    c.geom.bop = bop;
+    c.geom.nacc = nacc;
+    c.geom.sm_lo = any_smooth ? sm_lo : ns;
+    c.geom.sm_hi = any_smooth ? sm_hi : -1;
+    c.geom.uniform_index = uniform_index ? 1 : 0;
+    c.geom.n = 0;
 
     // ---- scratch
     const int bn = contract_models_per_tile(nacc);
@@ -540,7 +529,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
     ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
     ca.young = ca.old = nullptr;
-    const bool parts = (io.young || io.old) && !io.dev_inputs;
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
     if (parts) {
         if ((e = c.d_young.reserve((size_t)n * ns)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns)) != cudaSuccess) {
             err = cuda_msg("device memory", e);
@@ -584,6 +573,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {
         c.last_n = n;
+        c.geom.n = n;
         if (!io.dev_sync) return 0;
         int kstatus = 0;
         if ((e = cudaMemcpyAsync(&kstatus, c.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
@@ -639,7 +629,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             return ST_DATA_MISSING;
         }
     }
-    if (parts) {
+    const bool parts_out = (io.young || io.old) && !io.dev_inputs;
+    if (parts_out) {
         young_h.resize((size_t)n * ns);
         old_h.resize((size_t)n * ns);
         if ((e = cudaMemcpyAsync(young_h.data(), c.d_young.p, sizeof(float) * young_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
@@ -686,6 +677,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return ST_DATA_MISSING;
     }
     c.last_n = n;
+    c.geom.n = n;
     if (want_sums && !io.dev_inputs) {
         for (int m = 0; m < n; ++m) {
             const double *s = sums.data() + (size_t)6 * m;
@@ -699,7 +691,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     if (want_eml)
         for (size_t i = 0; i < eml_h.size(); ++i) io.emlines[i] = (double)eml_h[i];
-    if (parts) {
+    if (parts_out) {
         for (size_t i = 0; i < young_h.size(); ++i) {
             if (io.young) io.young[i] = (double)young_h[i];
             if (io.old) io.old[i] = (double)old_h[i];
@@ -710,17 +702,4 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     return 0;
 }
 
-}  // namespace sps
-
-namespace sps {
-// The reverse pass (compute_csp_batch_grad): not built yet on this path.
-int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
-                   const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
-                   double *weights_z_bar, std::string &err) {
-    (void)mags_bar; (void)spec_bar; (void)mass_bar; (void)lbol_bar; (void)params_bar; (void)params_bar_rows;
-    (void)weights_z_bar;
-    if (!mags_bar && !spec_bar && !mass_bar && !lbol_bar && !params_bar && !weights_z_bar) return run_batch(c, io, err);
-    err = "gradients are not available on this path yet";
-    return ST_UNSUPPORTED;
-}
 }  // namespace sps

@@ -134,8 +134,9 @@ void batch_entry(int handle, int n, int n_params, const char *const *names, cons
     io.lbol_young = lbol_young; io.lbol_old = lbol_old;
     const bool grad = mags_bar || spec_bar || mass_bar || lbol_bar || params_bar || weights_bar || weights_z_bar;
     if (grad) {
-        if (weights_bar && !ssp_weights_z)
-            return fail(status, ST_UNSUPPORTED, "weights_bar with ssp_weights is not supported on this path");
+        // (with ssp_weights the metallicity blend at logzsol would add logzsol's row and weights_bar's chain rule)
+        if (!ssp_weights_z)
+            return fail(status, ST_UNSUPPORTED, "gradients need ssp_weights_z on this path (ssp_weights is forward only)");
         st = run_grad_batch(*c, io, mags_bar, spec_bar, mass_bar, lbol_bar, params_bar, params_bar_rows,
                             weights_z_bar, err);
         if (weights_bar) std::fill(weights_bar, weights_bar + (size_t)c->nt * n, 0.0);

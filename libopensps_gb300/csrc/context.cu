@@ -149,9 +149,7 @@ static bool manifest_double(const std::string &text, const char *key, double &v)
 
 Context::~Context() {
     for (auto &kv : basis_cache) {
-        kv.second->hi.release();
-        kv.second->lo.release();
-        kv.second->kmap.release();
+        kv.second->release();
         delete kv.second;
     }
     d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
@@ -159,6 +157,9 @@ Context::~Context() {
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
     d_status.release(); d_young.release(); d_old.release(); d_eml.release(); d_eml_lum.release(); d_eml_kidx.release();
+    d_bptr.release(); d_bidx.release(); d_bw.release(); d_mags_bar.release(); d_spec_bar.release(); d_mass_bar.release();
+    d_lbol_bar.release(); d_cscale.release(); d_pbar.release(); d_wzbar.release(); d_ybh.release(); d_ybl.release();
+    d_obh.release(); d_obl.release(); d_wzb32.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
@@ -294,7 +295,27 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
         err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
         return ST_BAD_ARG;
     }
+    // the same matrix by pixel for the reverse pass (CSR over pixels j0 .. j1: the bands reaching each, FP32 weights)
+    std::vector<int> bptr(1, 0), bidx;
+    std::vector<float> bw;
+    for (int j = j0; j <= j1; ++j) {
+        for (int b = 0; b < nb; ++b) {
+            const double w = cm[(size_t)b * ns + j];
+            if (w == 0.0) continue;
+            bidx.push_back(b);
+            bw.push_back((float)w);
+        }
+        bptr.push_back((int)bidx.size());
+    }
+    if (bidx.empty()) { bidx.push_back(0); bw.push_back(0.f); }
+    if ((e = upload(c.d_bptr, bptr.data(), bptr.size())) != cudaSuccess ||
+        (e = upload(c.d_bidx, bidx.data(), bidx.size())) != cudaSuccess ||
+        (e = upload(c.d_bw, bw.data(), bw.size())) != cudaSuccess) {
+        err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
+        return ST_BAD_ARG;
+    }
     c.band_j0 = j0;
+    c.band_j1 = j1;
     c.band_nkb = nkb;
     c.band_npad = npad;
     return 0;
@@ -404,7 +425,7 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     c.pix_index = -1e300;
     int st = context_load_filters(c, c.filter_set, err);
     if (st != 0) return st;
-    for (auto &kv : c.basis_cache) { kv.second->hi.release(); kv.second->lo.release(); delete kv.second; }
+    for (auto &kv : c.basis_cache) { kv.second->release(); delete kv.second; }
     c.basis_cache.clear();
     c.eml_nnz = -1;
     c.is_setup = true;

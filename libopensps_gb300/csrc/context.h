@@ -55,6 +55,20 @@ struct BasisOperand {
     DevBuf<__nv_bfloat16> hi, lo;
     DevBuf<int> kmap;            // operand column -> source (age, metallicity) of the weights, bit 30: young
     CUtensorMap tm_hi, tm_lo;
+    // the reverse pass's copy, transposed (kpad x ppad, pixels padded to ppad with zeros), made on first use
+    int ppad = 0;
+    DevBuf<__nv_bfloat16> thi, tlo;
+    DevBuf<int> col_of;          // source index t + nt z -> operand column
+    CUtensorMap tm_thi, tm_tlo;
+    void release() {
+        hi.release(); lo.release(); kmap.release(); thi.release(); tlo.release(); col_of.release();
+    }
+};
+
+// What the reverse pass needs of the forward batch it follows.
+struct BatchGeom {
+    BasisOperand *bop = nullptr;
+    int nacc = 0, sm_lo = 0, sm_hi = -1, uniform_index = 0, n = 0;
 };
 
 struct Context {
@@ -100,6 +114,14 @@ struct Context {
     DevBuf<float> d_mpar, d_spec, d_young, d_old, d_eml, d_eml_lum;
     DevBuf<int> d_eml_kidx;
     int eml_nnz = -1;            // entries of the line table (-1: not built)
+    BatchGeom geom;              // of the last batch
+    // reverse pass: the band matrix by pixel (CSR over pixels band_j0 .. band_j1), cotangents and results
+    int band_j1 = -1;
+    DevBuf<int> d_bptr, d_bidx;
+    DevBuf<float> d_bw;
+    DevBuf<double> d_mags_bar, d_spec_bar, d_mass_bar, d_lbol_bar, d_cscale, d_pbar, d_wzbar;
+    DevBuf<__nv_bfloat16> d_ybh, d_ybl, d_obh, d_obl;
+    DevBuf<float> d_wzb32;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch
@@ -140,6 +162,7 @@ struct BatchIO {
     const double *dev_params = nullptr;   // PAR_DEVICE x n on the device (dev_inputs)
     bool dev_sync = true;            // dev_inputs: wait for the batch before returning
     double *fband_dev = nullptr;     // device n x nbands band fluxes (the reverse pass), or null
+    bool keep_parts = false;         // the reverse pass: the young and old sums kept on the device (d_young, d_old)
     // outputs (host, may be null)
     double *mags = nullptr, *spec = nullptr, *mass = nullptr, *lbol = nullptr, *emlines = nullptr;
     double *young = nullptr, *old = nullptr, *mass_young = nullptr, *mass_old = nullptr, *lbol_young = nullptr,

@@ -7,6 +7,23 @@
 
 namespace sps {
 
+// 0-based index i with a[i] <= v < a[i + 1] for ascending or descending a (bisection over 0..n+1 as the reference's
+// find_interval, src/math/opensps_interpolation.f90:152-197, with its end cases), as the reference's 1-based
+// result minus one (so -1 below an ascending table).
+__host__ __device__ inline int find_interval0(const double *a, int n, double v) {
+    if (n < 2) return 0;
+    const bool asc = a[n - 1] >= a[0];
+    int lower = 0, upper = n + 1;
+    while (upper - lower > 1) {
+        const int mid = (upper + lower) / 2;
+        const bool ge = v >= a[mid - 1];
+        if (asc == ge) lower = mid; else upper = mid;
+    }
+    if (v == a[0]) return 0;
+    if (v == a[n - 1]) return n - 2;
+    return lower - 1;
+}
+
 // Error codes a kernel writes into its status word (0 = ok). A bounded wait that gave up records which role.
 enum {
     ERR_TIMEOUT_PRODUCER = 0x101,
@@ -114,6 +131,47 @@ struct EmlineArgs {
     float *eml;             // n_models x nline
 };
 cudaError_t run_emlines(const EmlineArgs &a, cudaStream_t st);
+
+// Split-BF16 GEMM D(M x N) = A(M x K) B(N x K)^T, f32 out (gemm_bf16x3.cu). B's rows start at b_row0.
+struct GemmArgs {
+    int M, N, K, ldd, b_row0;
+    float *D;
+    int *status;
+};
+struct GemmPlan {
+    CUtensorMap tm_a_hi, tm_a_lo, tm_b_hi, tm_b_lo;
+    int num_sms;
+};
+int gemm_bk();
+int gemm_bm();
+int gemm_bn();
+cudaError_t run_gemm_bf16x3(const GemmPlan &pl, const GemmArgs &g, cudaStream_t st);
+
+// The reverse pass per model (adjoint.cu): from the forward's young / old sums, band fluxes and the cotangents, the
+// cotangents of the young and old sums (bf16 hi / lo operands of the weight GEMM) and the parameter gradients.
+struct AdjointArgs {
+    int n_models, nspec, ppad, nbands, jtop, j0, j1, sm_lo, sm_hi, uniform_index;
+    double dlnl;
+    const float *young, *old;        // n_models x nspec: the forward's age sums before dust
+    const float *mpar;               // n_models x MODEL_PAR_FLOATS
+    const double *par;               // n_models x PAR_DEVICE (dust1 .. dust_tesc)
+    const float4 *zinfo;             // n_models: the observed-frame shift
+    const double *fband;             // n_models x nbands
+    const double *mags_bar;          // n_models x nbands, or null
+    const double *spec_bar;          // n_models x nspec, or null
+    const int *do_band;              // nbands, or null: every band
+    const float *pix;                // nspec x PIX_FLOATS
+    const double *lam, *lnlam;       // nspec
+    const float *wl;                 // nspec: 1 / lambda
+    const int *bptr;                 // j1 - j0 + 2: the bands reaching pixel j0 + i are bidx[bptr[i] .. bptr[i+1]-1]
+    const int *bidx;
+    const float *bw;                 // the band matrix C(j, b) of those entries
+    const double *zt, *dl;           // cosmology table (500)
+    __nv_bfloat16 *ybar_hi, *ybar_lo, *obar_hi, *obar_lo;   // n_models x ppad (zero beyond nspec)
+    double *cscale;                  // n_models: the cotangent scale (the A operands are divided by it)
+    double *params_bar;              // n_models x 44
+};
+cudaError_t run_adjoint(const AdjointArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);
