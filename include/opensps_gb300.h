@@ -37,6 +37,21 @@ void opensps_gb300_kernel_times(int handle, double *ms, int max_n, int *n, int *
 /* Kernel launches of the last batch on the handle (for the benchmark's launch count). */
 void opensps_gb300_last_launches(int handle, int *launches, int *status);
 
+/* Maximum n of opensps_gb300_spec_mags_noalloc. */
+#define OPENSPS_GB300_NOALLOC_MAX_MODELS 65536
+
+/* The magnitudes (nbands x n doubles, d_mags) of n rest-frame spectra already on the device (d_spec: nspec x n
+ * floats, column-major, as opensps_context_batch_spec_device gives them) at redshifts d_zred (n doubles), through
+ * the band GEMM of the batch, with no allocation: the call's scratch (observed-frame shifts, distance terms, band
+ * mask, status word) is a fixed 2 MiB device array of the library, held on every device that loads the library
+ * until the process exits. No counterpart in OpenSPS: it serves callers that may not allocate device memory.
+ * n > OPENSPS_GB300_NOALLOC_MAX_MODELS: status 3 and nothing runs. The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress) and should come before any stream capture. Every call shares the array:
+ * calls whose kernels overlap on the GPU (other streams, contexts or threads) race. Runs on the context's stream;
+ * asynchronous unless sync != 0. The context's filter library and magnitude mask apply. */
+void opensps_gb300_spec_mags_noalloc(int handle, int n, const float *d_spec, const double *d_zred, double *d_mags,
+                                     int sync, int *status);
+
 #ifdef __cplusplus
 }
 #endif

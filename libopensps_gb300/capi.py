@@ -67,6 +67,7 @@ SIGNATURES = {
     "opensps_gb300_batch_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
+    "opensps_gb300_spec_mags_noalloc": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
     "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
 }
@@ -302,6 +303,14 @@ class Context:
                                                    C.byref(st))
         _check(st, self.lib)
         return p.value, ns.value, n.value, b.value
+
+    def spec_mags_noalloc(self, n: int, d_spec: int, d_zred: int, d_mags: int, sync: bool = True):
+        """opensps_gb300_spec_mags_noalloc: magnitudes of device spectra (nspec x n floats) at device redshifts (n
+        doubles) into d_mags (nbands x n doubles), with no allocation (device pointers as integers)."""
+        st = C.c_int(0)
+        self.lib.opensps_gb300_spec_mags_noalloc(self.handle, n, C.c_void_p(d_spec), C.c_void_p(d_zred),
+                                                 C.c_void_p(d_mags), 1 if sync else 0, C.byref(st))
+        _check(st, self.lib)
 
     def stream(self) -> int:
         s, d, st = C.c_void_p(), C.c_int(), C.c_int()

@@ -18,6 +18,8 @@ void prof_harvest(Context &c, int s);
 int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
                    const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
                    double *weights_z_bar, std::string &err);
+int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zred, double *d_mags, bool sync,
+                     std::string &err);
 }  // namespace sps
 
 using namespace sps;
@@ -493,6 +495,19 @@ void opensps_gb300_batch_device(int handle, int n, const double *d_params, const
     io.mags = d_mags; io.dev_sync = sync != 0;
     std::string err;
     const int st = run_batch(*c, io, err);
+    if (st) return fail(status, st, err);
+}
+
+void opensps_gb300_spec_mags_noalloc(int handle, int n, const float *d_spec, const double *d_zred, double *d_mags,
+                                     int sync, int *status) {
+    if (!status) return;
+    *status = 0;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    std::string err;
+    const int st = run_mags_noalloc(*c, n, d_spec, d_zred, d_mags, sync != 0, err);
     if (st) return fail(status, st, err);
 }
 
