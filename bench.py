@@ -13,6 +13,8 @@ power-law dust (tau_V uniform 0-3), redshift uniform 0-6 with the Madau IGM, vel
   masses and L_bol copied out inside the timed region.
 * ``roofline``: the contraction kernel (split-BF16 tcgen05 GEMM with its fused epilogue): 3 x 2 K P B executed
   bf16 FLOPs per launch over its mean CUDA-event duration, against the measured sustained bf16 peak.
+* ``adjoint``: the reverse pass (compute_csp_batch_grad_rows) at B = 16384 with cotangents on 40 magnitudes and
+  512 spectral bins, through the C API from page-locked host buffers (wall time), with its device stage times.
 * ``cpu_baseline`` / ``--impl reference``: the FP64 CPU oracle (a restatement of OpenSPS's compute_csp_batch,
   the reference being Fortran with no compiler in this image) with OpenMP on all host cores, on a bounded sample.
 
@@ -141,6 +143,53 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def adjoint_measure(ctx, args, rank, torch, barrier) -> dict | None:
+    """The reverse pass (compute_csp_batch_grad_rows) at B = --adjoint-batch through the C API from page-locked host
+    buffers: weights, magnitude and spectrum cotangents (N(0, 1) on 40 magnitudes and 512 spectral bins) in;
+    magnitudes, mass, L_bol, params_bar and weights_z_bar out. Wall time per call, and the device time of its
+    stages (CUDA events on the library's stream)."""
+    from libopensps_gb300 import workloads
+    n = args.adjoint_batch
+    if n <= 0:
+        return None
+    ns, nb = ctx.nspec, ctx.nbands
+    h_wz = torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True)
+    _, params = workloads.mixed_csp(n, seed=2000 + rank, out=h_wz.numpy())
+    mb, sb = workloads.adjoint_cotangents(n, ns, nb, seed=4)
+    h_mb = torch.from_numpy(mb).pin_memory().numpy()
+    h_sb = torch.from_numpy(sb).pin_memory().numpy()
+    out = {"mags": (n, nb), "mass": (n,), "lbol": (n,), "params_bar": (n, 44), "weights_z_bar": (n, N_Z, K_AGES)}
+    out = {k: torch.empty(v, dtype=torch.float64, pin_memory=True).numpy() for k, v in out.items()}
+    wz = h_wz.numpy()
+    steps, warm = args.adjoint_steps, max(args.warmup, 1)
+
+    def call():
+        ctx.csp_batch_grad(params, wz, mags_bar=h_mb, spec_bar=h_sb, spec=False, out=out)
+
+    for _ in range(warm):
+        call()
+    barrier()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    barrier()
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    kt = ctx.kernel_times()
+    ctx.set_profiling(False)
+    names = ["model_params", "weight_operand", "contract", "bands", "fp64_sums", "copies_host", "adjoint",
+             "weights_gemm", "weights_cotangent"]
+    stages = dict(zip(names, kt))
+    dev = sum(v for k, v in stages.items() if k != "copies_host")
+    h2d = wz.nbytes + h_mb.nbytes + h_sb.nbytes + n * 11 * 8
+    d2h = sum(a.nbytes for a in out.values())
+    return {"batch": n, "value": n / (ms * 1e-3), "unit": "models/s", "ms_per_step": ms, "steps": steps,
+            "device_ms": dev, "device_value": n / (dev * 1e-3) if dev > 0 else None, "stage_ms": stages,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "cotangents": "N(0,1) on 40 magnitudes and 512 spectral bins (FP32 values)",
+            "outputs": "mags, mass, lbol, params_bar (44 rows), weights_z_bar"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -218,6 +267,7 @@ def run_ours(args) -> None:
         e2e_ms = float(t.item())
     h2d = h_wz.numel() * 8 + n * 11 * 8 + 3 * n * 8
     d2h = n * nb * 8 + 6 * n * 8
+    adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
 
     # roofline of the contraction
     pk = _peaks()
@@ -248,6 +298,7 @@ def run_ours(args) -> None:
                          "stage_ms": dict(zip(["model_params", "weight_operand", "contract", "bands",
                                                "fp64_sums"], ktimes))},
             "cpu_baseline": cpu,
+            "adjoint": adjoint,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -265,6 +316,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--adjoint-batch", type=int, default=16384)
+    ap.add_argument("--adjoint-steps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -30,7 +30,9 @@ void opensps_gb300_context_stream(int handle, void **stream, int *device, int *s
 /* With on != 0, CUDA events are recorded between the kernels of every batch on the handle; afterwards
  * opensps_gb300_kernel_times gives the device time of each stage of the last batch in milliseconds, in order: the
  * per-model parameters, the weight operand, the contraction with its epilogue, the band fluxes and magnitudes, the
- * FP64 mass and L_bol sums (mean over the batches since profiling was switched on). */
+ * FP64 mass and L_bol sums; after a gradient call also the forward's output copies with the cotangents' copies
+ * (host time included), the per-model adjoint, the weights' GEMMs and the weights' cotangent kernel (mean over the
+ * batches since profiling was switched on). At most 9 stages. */
 void opensps_gb300_set_profiling(int handle, int on, int *status);
 void opensps_gb300_kernel_times(int handle, double *ms, int max_n, int *n, int *status);
 

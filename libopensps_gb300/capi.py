@@ -242,10 +242,11 @@ class Context:
     def csp_batch_grad(self, params: dict, ssp_weights_z: np.ndarray, mags_bar: np.ndarray | None = None,
                        spec_bar: np.ndarray | None = None, mass_bar: np.ndarray | None = None,
                        lbol_bar: np.ndarray | None = None, params_bar_rows: int | None = None,
-                       weights_z_bar: bool = True) -> dict:
+                       weights_z_bar: bool = True, spec: bool = True, out: dict | None = None) -> dict:
         """compute_csp_batch_grad_rows: the forward batch and the reverse pass for the given cotangents (arrays
-        (n, nbands), (n, nspec), (n,), (n,)). Returns the forward outputs, params_bar (n, rows) and weights_z_bar
-        (n, nz, nt)."""
+        (n, nbands), (n, nspec), (n,), (n,)). Returns the forward outputs (mags, mass, lbol, and spec unless
+        spec=False), params_bar (n, rows) and weights_z_bar (n, nz, nt). ``out`` may hold preallocated C-contiguous
+        float64 arrays for any of these (e.g. page-locked ones)."""
         w = np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
         n = w.shape[0]
         ns, nb, nt, nz = self.nspec, self.nbands, self.ntfull, self.nz
@@ -255,19 +256,29 @@ class Context:
         for name, arr in (("mags_bar", mags_bar), ("spec_bar", spec_bar), ("mass_bar", mass_bar),
                           ("lbol_bar", lbol_bar)):
             cot[name] = None if arr is None else np.ascontiguousarray(arr, dtype=np.float64)
-        out = {"mags": np.empty((n, nb)), "spec": np.empty((n, ns)), "mass": np.empty(n), "lbol": np.empty(n),
-               "params_bar": np.full((n, rows), np.nan)}
+        shapes = {"mags": (n, nb), "mass": (n,), "lbol": (n,), "params_bar": (n, rows)}
+        if spec:
+            shapes["spec"] = (n, ns)
         if weights_z_bar:
-            out["weights_z_bar"] = np.empty((n, nz, nt))
+            shapes["weights_z_bar"] = (n, nz, nt)
+        given = out or {}
+        res = {}
+        for name, shp in shapes.items():
+            a = given.get(name)
+            if a is None:
+                a = np.empty(shp)
+            elif a.shape != shp or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"out[{name!r}] must be a C-contiguous float64 array of shape {shp}")
+            res[name] = a
         st = C.c_int(0)
         self.lib.opensps_context_compute_csp_batch_grad_rows(
             self.handle, n, k, c_names, c_vals, None, _ptr(w), None, _ptr(cot["mags_bar"]), _ptr(cot["spec_bar"]),
-            _ptr(cot["mass_bar"]), _ptr(cot["lbol_bar"]), _ptr(out["mags"]), _ptr(out["spec"]), _ptr(out["mass"]),
-            _ptr(out["lbol"]), None, None, None, None, _ptr(out["params_bar"]), rows, None,
-            _ptr(out.get("weights_z_bar")), C.byref(st))
+            _ptr(cot["mass_bar"]), _ptr(cot["lbol_bar"]), _ptr(res["mags"]), _ptr(res.get("spec")),
+            _ptr(res["mass"]), _ptr(res["lbol"]), None, None, None, None, _ptr(res["params_bar"]), rows, None,
+            _ptr(res.get("weights_z_bar")), C.byref(st))
         _check(st, self.lib)
         del keep
-        return out
+        return res
 
     def csp_batch_parts(self, params: dict, ssp_weights: np.ndarray, emlines: bool = True) -> dict:
         """compute_csp_batch_parts: the batch with the intrinsic young and old age sums (weights (n, nt))."""
@@ -327,8 +338,9 @@ class Context:
         _check(st, self.lib)
 
     def kernel_times(self) -> list[float]:
-        """Mean device ms of the profiled batches' stages: model parameters, weight operand, contraction, bands, FP64 sums."""
-        buf, n, st = np.zeros(8), C.c_int(0), C.c_int(0)
-        self.lib.opensps_gb300_kernel_times(self.handle, _ptr(buf), 8, C.byref(n), C.byref(st))
+        """Mean device ms of the profiled batches' stages: model parameters, weight operand, contraction, bands, FP64 sums
+        (and after gradient calls: output and cotangent copies, adjoint, weights GEMMs, weights cotangent)."""
+        buf, n, st = np.zeros(10), C.c_int(0), C.c_int(0)
+        self.lib.opensps_gb300_kernel_times(self.handle, _ptr(buf), 10, C.byref(n), C.byref(st))
         _check(st, self.lib)
         return buf[:n.value].tolist()

@@ -10,8 +10,8 @@
 // adjoint_kernel: one CTA per model. Shared memory holds the model's recomputed pre-smoothing spectrum (TOT, later
 // the cotangent of TOT), its smoothed spectrum (S), the cotangent of S (SB) and the observed-frame cotangent (VB).
 // The cotangents of the young and old sums leave as the bf16 hi / lo A operands of the weight GEMM; the parameter
-// gradients are block reductions. Every cotangent is divided by the model's largest one (cscale) so that the FP32
-// arithmetic stays in range; the results are multiplied back in FP64.
+// gradients are block reductions. Every cotangent is divided by a power of two at least the model's largest one
+// (cscale) so that the FP32 arithmetic stays in range; the results are multiplied back in FP64.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -22,10 +22,12 @@
 #include <string>
 #include <vector>
 #include "context.h"
+#include "sm103_ptx.cuh"
 
 namespace sps {
 
-constexpr int ADJ_THREADS = 256;
+constexpr int ADJ_THREADS = 384;
+constexpr int ADJ_WARPS = ADJ_THREADS / 32;
 constexpr int ADJ_MAX_BANDS = 256;
 constexpr double ADJ_C_KMS = 2.99792458e5;           // C_LIGHT 1e-13: km/s
 constexpr double DMAG_DF = -1.0857362047581294;       // -2.5 / ln 10
@@ -34,7 +36,13 @@ constexpr int NBGRAD = 44;
 // gradient rows of params_bar (opensps.h)
 enum { R_DUST1 = 1, R_DUST2 = 2, R_DUST3 = 3, R_DUST_INDEX = 4, R_DUST1_INDEX = 5, R_FRAC_OBRUN = 6,
        R_FRAC_NODUST = 7, R_ZRED = 22, R_SIGMA = 23, R_IGM_FACTOR = 32 };
-enum { G_DUST2 = 0, G_DUST_INDEX, G_FNODUST, G_DUST1, G_DUST1_INDEX, G_FOBRUN, G_DUST3, G_ZRED, G_IGMF, G_SIGMA, NG };
+enum { G_DUST2 = 0, G_DUST_INDEX, G_FNODUST, G_DUST1, G_DUST1_INDEX, G_FOBRUN, G_DUST3, G_ZRED, G_IGMF, G_SIGMA,
+       G_OBS, NG };
+
+// The per-model block of the reverse pass (floats; KOBS and DDIST are doubles at 8-byte offsets), written by
+// adjoint_prep_kernel: the redshift factors b_k = (1 + z)^p_k and d b_k / dz, the smoothing taps' d / dsigma, the
+// observed frame's d t / dz factor and the distance term's d / dz.
+enum { AP_B = 0, AP_DB = 6, AP_DTAP = 12, AP_KOBS = 22, AP_DDIST = 24, AP_FLOATS = 32 };
 
 __device__ __forceinline__ float adj_ex2(float x) {
     float y;
@@ -42,6 +50,83 @@ __device__ __forceinline__ float adj_ex2(float x) {
     return y;
 }
 
+// x 2^-k as FP32 on the integer pipes (GB300 has little FP64): round to nearest even on the dropped mantissa bits; a
+// result below FP32's smallest normal is a signed 0, above its largest an infinity; infinities and NaNs carry over.
+__device__ __forceinline__ float scaled_to_f32(double x, int k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
+    const uint32_t sign = hi32 & 0x80000000u;
+    const int de = (int)((hi32 >> 20) & 0x7ff);
+    if (de == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (((hi32 & 0xfffffu) | lo32) ? 0x400000u : 0u));
+    const int fe = de - 896 - k;                                        // FP32 biased exponent of x 2^-k
+    if (de == 0 || fe < 1) return __uint_as_float(sign);
+    if (fe > 254) return __uint_as_float(sign | 0x7f800000u);
+    uint32_t m = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+    const uint32_t rem = lo32 & 0x1fffffffu;
+    m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign | (((uint32_t)fe << 23) + m));         // a mantissa carry moves into the exponent
+}
+
+// ---------------------------------------------------------------------------------------------- per-model scalars
+// One thread per model, FP64 (igm_tau_z_terms_dz src/physics/opensps_cosmology.f90:511-522; smooth_sigma_adjoint's
+// d C / d sigma = C (x^2 - <x^2>) / (sigma_beta^3 c); backward_observed_frame's d t / dz; distance_term_dz).
+__global__ void __launch_bounds__(256) adjoint_prep_kernel(AdjointPrepArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n_models) return;
+    const double *pr = a.par + (size_t)PAR_DEVICE * m;
+    const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    float blk[AP_FLOATS];
+#pragma unroll
+    for (int i = 0; i < AP_FLOATS; ++i) blk[i] = 0.f;
+    const double z = pr[PF_ZRED];
+    if (mp[MP_IGM_ON] != 0.f) {
+        const double pk[6] = {3.46, 1.68, 3.0 + 0.46, 1.5 + 0.18, 3.0 - 1.32, 1.68};
+        const double l1z = log1p(z);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const double bk = exp(pk[k] * l1z);
+            blk[AP_B + k] = (float)bk;
+            blk[AP_DB + k] = (float)(pk[k] * bk / (1.0 + z));
+        }
+    }
+    const int R = __float_as_int(mp[MP_SMOOTH_R]);
+    const double sig = pr[PF_SIGMA_SMOOTH];
+    if (R >= 0 && sig > 0.0) {
+        const double sb = sig / ADJ_C_KMS;
+        const double inv = 1.0 / (sb * sb * sb * ADJ_C_KMS);
+        double av[9], mean = 0.0;
+#pragma unroll
+        for (int d = -4; d <= 4; ++d) {
+            const int j = min(max(a.sm_lo + d, 0), a.nspec - 1);
+            const double dd = a.lnlam[a.sm_lo] - a.lnlam[j];
+            av[d + 4] = dd * dd * inv;
+            mean += (double)mp[MP_TAPS + d + 4] * av[d + 4];
+        }
+#pragma unroll
+        for (int d = 0; d < 9; ++d) blk[AP_DTAP + d] = (float)((double)mp[MP_TAPS + d] * (av[d] - mean));
+    }
+    double kobs = 0.0, ddist = 0.0;
+    const float4 zi = a.zinfo[m];
+    if (zi.w == 1.f) {
+        // t = (lambda_j / (1 + z) - lambda_il) / (lambda_(il+1) - lambda_il): dt/dz = -lambda_j / ((1 + z)^2 dlambda_il),
+        // lambda_j / dlambda_il = e^((j - il) dlnl) / (e^dlnl - 1), j - il = nsh on the grid's interior
+        const int nsh = __float_as_int(zi.x) + ((zi.y > 0.f) ? 1 : 0);
+        const double opz = 1.0 + z;
+        kobs = -exp((double)nsh * a.dlnl) / (opz * opz * a.em1);
+        const int idx = max(0, min(find_interval0(a.zt, 500, z), 498));
+        const double slope = (a.dl[idx + 1] - a.dl[idx]) / (a.zt[idx + 1] - a.zt[idx]);
+        const double dm = a.dl[idx] + slope * (z - a.zt[idx]);
+        if (dm == dm && dm > SAFE_FLOOR) ddist = 5.0 / log(10.0) * slope / dm - 2.5 / (log(10.0) * opz);
+    }
+    float *o = a.apar + (size_t)AP_FLOATS * m;
+#pragma unroll
+    for (int i = 0; i < AP_FLOATS; i += 4)
+        reinterpret_cast<float4 *>(o)[i / 4] = make_float4(blk[i], blk[i + 1], blk[i + 2], blk[i + 3]);
+    reinterpret_cast<double *>(o)[AP_KOBS / 2] = kobs;
+    reinterpret_cast<double *>(o)[AP_DDIST / 2] = ddist;
+}
+
+// ---------------------------------------------------------------------------------------------- the adjoint
 // The forward's per-pixel factors of a model (as the contraction's epilogue forms them).
 struct PixFwd {
     float curve, ltab, td, c1, tb, to, D, ssfac_y;
@@ -49,112 +134,182 @@ struct PixFwd {
     bool igm;
 };
 
-__device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const float *mp, int p, bool igm_model, int jmax,
-                                              const float *b, const float *db) {
+struct ModelConst {
+    float kd2, one_m_fnd, fnd, dust_index, kd1, dust1_index, one_m_fo, fo, kd3;
+    float b[6], db[6];
+    int jmax;
+    bool igm_model;
+};
+
+__device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const ModelConst &mc, int p) {
     PixFwd f;
-    const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
-    const float ltab2 = v0.x;
+    const float ltab2 = fmaf((float)p, a.lt_step, a.lt_base);   // ln(lambda / 5500) log2(e) on the log-uniform grid
     f.ltab = ltab2 * 0.6931471805599453f;                        // ln(lambda / 5500)
-    f.curve = a.uniform_index ? v0.y : adj_ex2(mp[MP_DUST_INDEX] * ltab2);
-    f.td = adj_ex2(mp[MP_KD2] * f.curve);
-    f.c1 = adj_ex2(mp[MP_DUST1_INDEX] * ltab2);
-    f.tb = (mp[MP_KD1] != 0.f) ? adj_ex2(mp[MP_KD1] * f.c1) : 1.f;
-    f.to = (mp[MP_KD3] != 0.f) ? adj_ex2(mp[MP_KD3] * f.curve) : 1.f;
-    f.D = fmaf(f.td, mp[MP_ONE_M_FND], mp[MP_FND]);
-    f.ssfac_y = f.tb * mp[MP_ONE_M_FO] + mp[MP_FO];
-    f.igm = igm_model && p < a.jtop;
+    f.curve = adj_ex2(mc.dust_index * ltab2);
+    f.td = adj_ex2(mc.kd2 * f.curve);
+    f.c1 = adj_ex2(mc.dust1_index * ltab2);
+    f.tb = (mc.kd1 != 0.f) ? adj_ex2(mc.kd1 * f.c1) : 1.f;
+    f.to = (mc.kd3 != 0.f) ? adj_ex2(mc.kd3 * f.curve) : 1.f;
+    f.D = fmaf(f.td, mc.one_m_fnd, mc.fnd);
+    f.ssfac_y = f.tb * mc.one_m_fo + mc.fo;
+    f.igm = mc.igm_model && p < a.jtop;
     f.tau = 0.f;
     f.dtau = 0.f;
     if (f.igm) {
         // pixels below the one of the largest depth take its depth (apply_igm_z's cap)
-        const int jc = (p < jmax) ? jmax - 1 : p;
-        const float4 w0 = reinterpret_cast<const float4 *>(a.pix + (size_t)jc * PIX_FLOATS)[0];
-        const float4 w1 = reinterpret_cast<const float4 *>(a.pix + (size_t)jc * PIX_FLOATS)[1];
+        const int jc = (p < mc.jmax) ? mc.jmax - 1 : p;
+        const float4 w0 = __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)jc * PIX_FLOATS));
+        const float4 w1 = __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)jc * PIX_FLOATS) + 1);
         const float ia[6] = {w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            f.tau = fmaf(ia[k], b[k], f.tau);
-            f.dtau = fmaf(ia[k], db[k], f.dtau);
+            f.tau = fmaf(ia[k], mc.b[k], f.tau);
+            f.dtau = fmaf(ia[k], mc.db[k], f.dtau);
         }
     }
     return f;
 }
 
+// The reverse pass of one pixel: from dL / dTOT (tb), the forward's sums (y, o), the gradient accumulators and the
+// cotangents of y and o.
+__device__ __forceinline__ void pixel_adjoint(const AdjointArgs &a, const ModelConst &mc, int p, float y, float o,
+                                              float tb, float f_igm, float kf, float d1, float d2, float d3, float *g,
+                                              float &yb, float &ob) {
+    const PixFwd f = pix_forward(a, mc, p);
+    const float ss = y * f.ssfac_y + o * f.to;
+    const float pre = ss * f.D;
+    float pb = tb;
+    if (f.igm) {
+        // T = exp(-igm_factor tau): dT/dz = -igm_factor T dtau/dz, dT/d igm_factor = -tau T
+        const float T = adj_ex2(f.tau * kf);
+        const float gT = pb * pre;
+        g[G_ZRED] = fmaf(gT, -f_igm * T * f.dtau, g[G_ZRED]);
+        g[G_IGMF] = fmaf(gT, -f.tau * T, g[G_IGMF]);
+        pb *= T;
+    }
+    // pre = ss D, D = T_d (1 - fnd) + fnd, ss = y (T_b (1 - fo) + fo) + o T_o
+    const float dcurve = f.curve * f.ltab;   // d curve / d dust_index
+    g[G_DUST2] = fmaf(pb * ss * mc.one_m_fnd, -f.td * f.curve, g[G_DUST2]);
+    g[G_DUST_INDEX] = fmaf(pb, ss * mc.one_m_fnd * f.td * (-d2 * dcurve) + f.D * o * f.to * (-d3 * dcurve),
+                           g[G_DUST_INDEX]);
+    g[G_FNODUST] = fmaf(pb * ss, 1.f - f.td, g[G_FNODUST]);
+    const float ybase = pb * f.D * y;
+    g[G_DUST1] = fmaf(ybase * mc.one_m_fo, -f.tb * f.c1, g[G_DUST1]);
+    g[G_DUST1_INDEX] = fmaf(ybase * mc.one_m_fo, -f.tb * d1 * f.c1 * f.ltab, g[G_DUST1_INDEX]);
+    g[G_FOBRUN] = fmaf(ybase, 1.f - f.tb, g[G_FOBRUN]);
+    g[G_DUST3] = fmaf(pb * f.D * o, -f.to * f.curve, g[G_DUST3]);
+    yb = pb * f.D * f.ssfac_y;
+    ob = pb * f.D * f.to;
+}
+
+__device__ __forceinline__ __nv_bfloat162 bf16_hi2(float a, float b) { return __floats2bfloat162_rn(a, b); }
+__device__ __forceinline__ __nv_bfloat162 bf16_lo2(float a, float b, __nv_bfloat162 h) {
+    return __floats2bfloat162_rn(a - __low2float(h), b - __high2float(h));
+}
+
+// floats per staged row: the row plus the unit offsets at either end, in 16-byte units
+__host__ __device__ int adj_row_pad(int ns);
+
 __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) {
-    extern __shared__ float sh[];
+    extern __shared__ __align__(16) float sh[];
     const int ns = a.nspec;
-    float *TOT = sh, *S = sh + ns, *SB = sh + 2 * ns, *VB = sh + 3 * ns;   // VB: pixels j0 .. j1
+    const int rowpad = adj_row_pad(ns);
+    // YS, OS: the model's young and old sums (bulk copies of the 16-byte units that hold the rows); TOT: the
+    // pre-smoothing spectrum, later dL / dTOT; S: the smoothed spectrum, later dL / dS; VB: pixels j0 .. j1
+    float *YS = sh, *OS = sh + rowpad, *TOT = sh + 2 * rowpad, *S = TOT + ns, *VB = S + ns;
     __shared__ float fbs[ADJ_MAX_BANDS];
-    __shared__ float red[NG][ADJ_THREADS / 32];
-    __shared__ double cred[ADJ_THREADS / 32];
-    __shared__ float b_s[6], db_s[6];
-    __shared__ double s_c, s_msum;
+    __shared__ uint64_t rows_bar;
+    __shared__ float red[NG][ADJ_WARPS];
+    __shared__ unsigned long long wmax[ADJ_WARPS];
+    __shared__ double wsum[ADJ_WARPS];
     const int m = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    const float *ap = a.apar + (size_t)AP_FLOATS * m;
     const double *pr = a.par + (size_t)PAR_DEVICE * m;
-    const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
-    const double z = pr[PF_ZRED];
-    const bool igm_model = mp[MP_IGM_ON] != 0.f;
-    const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
+    // the rows' 16-byte units: from the unit holding the first pixel through the one holding the last
+    const uintptr_t y0 = reinterpret_cast<uintptr_t>(a.young + (size_t)m * ns);
+    const uintptr_t o0 = reinterpret_cast<uintptr_t>(a.old + (size_t)m * ns);
+    const uintptr_t yb0 = y0 & ~uintptr_t(15), ob0 = o0 & ~uintptr_t(15);
+    const uint32_t ybytes = (uint32_t)(((y0 + 4 * (uintptr_t)ns + 15) & ~uintptr_t(15)) - yb0);
+    const uint32_t obytes = (uint32_t)(((o0 + 4 * (uintptr_t)ns + 15) & ~uintptr_t(15)) - ob0);
+    if (tid == 0) {
+        mbar_init(&rows_bar, 1);
+        fence_mbar_init();
+        mbar_arrive_expect_tx(&rows_bar, ybytes + obytes);
+        bulk_load(YS, reinterpret_cast<const void *>(yb0), ybytes, &rows_bar);
+        bulk_load(OS, reinterpret_cast<const void *>(ob0), obytes, &rows_bar);
+    }
+    const float *yv = YS + (y0 - yb0) / 4, *ov = OS + (o0 - ob0) / 4;
     const double *mb = a.mags_bar ? a.mags_bar + (size_t)m * a.nbands : nullptr;
     const double *fbd = a.fband + (size_t)m * a.nbands;
     const double *sbar = a.spec_bar ? a.spec_bar + (size_t)m * ns : nullptr;
+    const bool even = (ns & 1) == 0;   // rows start on 8-byte (float2) and 16-byte (double2) boundaries
 
-    // ---- the cotangent scale: the largest band-flux cotangent and spectrum cotangent of the model
-    double cm = 0.0;
+    // ---- the cotangent scale 2^ks >= the largest band-flux and spectrum cotangent of the model (a power of two, so
+    // that scaling is exact); magnitudes of doubles compared as their bit patterns
+    unsigned long long amax = 0ull;
+    double msum = 0.0;   // the magnitudes' cotangents over the bands computed (the distance term's share of d / dz)
     if (mb)
         for (int b = tid; b < a.nbands; b += ADJ_THREADS) {
             const double f = fbd[b];
-            if ((a.do_band == nullptr || a.do_band[b] != 0) && f > 0.0) cm = fmax(cm, fabs(mb[b] * DMAG_DF / f));
+            if ((a.do_band == nullptr || a.do_band[b] != 0) && f > 0.0) {
+                amax = max(amax, (unsigned long long)__double_as_longlong(mb[b] * DMAG_DF / f) & 0x7fffffffffffffffull);
+                msum += mb[b];
+            }
         }
-    if (sbar)
-        for (int p = tid; p < ns; p += ADJ_THREADS) cm = fmax(cm, fabs(sbar[p]));
+    if (sbar) {
+        if (even) {
+            const double2 *s2 = reinterpret_cast<const double2 *>(sbar);
+#pragma unroll 4
+            for (int i = tid; i < ns / 2; i += ADJ_THREADS) {
+                const double2 v = __ldg(s2 + i);
+                amax = max(amax, (unsigned long long)__double_as_longlong(v.x) & 0x7fffffffffffffffull);
+                amax = max(amax, (unsigned long long)__double_as_longlong(v.y) & 0x7fffffffffffffffull);
+            }
+        } else {
+            for (int i = tid; i < ns; i += ADJ_THREADS)
+                amax = max(amax, (unsigned long long)__double_as_longlong(sbar[i]) & 0x7fffffffffffffffull);
+        }
+    }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) cm = fmax(cm, __shfl_xor_sync(0xffffffffu, cm, off));
-    if (lane == 0) cred[warp] = cm;
-    if (tid == 0) {
-        // the redshift factors b_k = (1 + z)^p_k and d b_k / dz (igm_tau_z_terms, src/physics/opensps_cosmology.f90:
-        // 497-522), as the forward forms them
-        const double pk[6] = {3.46, 1.68, 3.0 + 0.46, 1.5 + 0.18, 3.0 - 1.32, 1.68};
-        const double l1z = igm_model ? log1p(z) : 0.0;
-        for (int k = 0; k < 6; ++k) {
-            const double bk = igm_model ? exp(pk[k] * l1z) : 0.0;
-            b_s[k] = (float)bk;
-            db_s[k] = igm_model ? (float)(pk[k] * bk / (1.0 + z)) : 0.f;
-        }
+    for (int off = 16; off > 0; off >>= 1) {
+        amax = max(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+        msum += __shfl_xor_sync(0xffffffffu, msum, off);
+    }
+    if (lane == 0) { wmax[warp] = amax; wsum[warp] = msum; }
+    ModelConst mc;
+    {
+        const float4 d0 = __ldg(reinterpret_cast<const float4 *>(mp));        // kd2, 1 - fnd, fnd, dust_index
+        const float4 d1v = __ldg(reinterpret_cast<const float4 *>(mp) + 1);   // kd1, dust1_index, 1 - fo, fo
+        const float4 d2v = __ldg(reinterpret_cast<const float4 *>(mp) + 2);   // igm on, jmax, kcap, kd3
+        mc.kd2 = d0.x; mc.one_m_fnd = d0.y; mc.fnd = d0.z; mc.dust_index = d0.w;
+        mc.kd1 = d1v.x; mc.dust1_index = d1v.y; mc.one_m_fo = d1v.z; mc.fo = d1v.w;
+        mc.igm_model = d2v.x != 0.f; mc.jmax = __float_as_int(d2v.y); mc.kd3 = d2v.w;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { mc.b[k] = __ldg(ap + AP_B + k); mc.db[k] = __ldg(ap + AP_DB + k); }
     }
     __syncthreads();
-    if (tid == 0) {
-        double c = 0.0;
-        for (int w = 0; w < ADJ_THREADS / 32; ++w) c = fmax(c, cred[w]);
-        if (!(c > 0.0) || c > DBL_MAX) c = 1.0;
-        s_c = c;
-        a.cscale[m] = c;
-        // the magnitudes' cotangents over the bands computed (the distance term's share of d / dz)
-        double ms = 0.0;
-        if (mb)
-            for (int b = 0; b < a.nbands; ++b)
-                if ((a.do_band == nullptr || a.do_band[b] != 0) && fbd[b] > 0.0) ms += mb[b];
-        s_msum = ms;
-    }
-    __syncthreads();
-    const double c = s_c;
+    unsigned long long u = 0ull;
+#pragma unroll
+    for (int w = 0; w < ADJ_WARPS; ++w) u = max(u, wmax[w]);
+    // 2^ks with ks = the exponent of frexp (2^ks >= the maximum); 1 for a zero or non-finite maximum
+    const int de = (int)(u >> 52);
+    const int ks = (u == 0ull || de == 0x7ff) ? 0 : de - 1022;
     if (mb)
         for (int b = tid; b < a.nbands; b += ADJ_THREADS) {
             const double f = fbd[b];
-            fbs[b] = ((a.do_band == nullptr || a.do_band[b] != 0) && f > 0.0) ? (float)(mb[b] * DMAG_DF / f / c) : 0.f;
+            fbs[b] = ((a.do_band == nullptr || a.do_band[b] != 0) && f > 0.0) ? scaled_to_f32(mb[b] * DMAG_DF / f, ks)
+                                                                              : 0.f;
         }
-    float b[6], db[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) { b[k] = b_s[k]; db[k] = db_s[k]; }
     const float f_igm = (float)pr[PF_IGM_FACTOR];
     const float kf = -f_igm * 1.4426950408889634f;
 
     // ---- pass 0: the pre-smoothing spectrum TOT = ss D T_igm (the forward's epilogue, recomputed)
+    mbar_wait(&rows_bar, 0, a.status, ERR_TIMEOUT_ADJOINT, false);
+#pragma unroll 2
     for (int p = tid; p < ns; p += ADJ_THREADS) {
-        const PixFwd f = pix_forward(a, mp, p, igm_model, jmax, b, db);
-        const float ss = yv[p] * f.ssfac_y + ov[p] * f.to;
-        float tot = ss * f.D;
+        const PixFwd f = pix_forward(a, mc, p);
+        float tot = (yv[p] * f.ssfac_y + ov[p] * f.to) * f.D;
         if (f.igm) tot *= adj_ex2(f.tau * kf);
         TOT[p] = tot;
     }
@@ -163,7 +318,7 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     const int R = __float_as_int(mp[MP_SMOOTH_R]);
     float tap[9];
 #pragma unroll
-    for (int d = 0; d < 9; ++d) tap[d] = mp[MP_TAPS + d];
+    for (int d = 0; d < 9; ++d) tap[d] = __ldg(mp + MP_TAPS + d);
     for (int p = tid; p < ns; p += ADJ_THREADS) {
         float v = TOT[p];
         if (R >= 0 && p >= a.sm_lo && p <= a.sm_hi) {
@@ -181,13 +336,17 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     const bool shifted = zi.w == 1.f;
     const int nsh = __float_as_int(zi.x) + ((zi.y > 0.f) ? 1 : 0);   // observed pixel j reads interval j - nsh
     const float tin = zi.y;
-    const float dl2 = (float)(a.dlnl * 1.4426950408889634), inv_em1 = (float)(1.0 / expm1(a.dlnl));
-    float gz = 0.f;   // sum of VB_j (S(il + 1) - S(il)) lambda_j / lambda_(il + nsh)
+    float gobs = 0.f;   // sum of VB_j (S(il + 1) - S(il)) lambda_j / lambda_(il + nsh)
     if (mb) {
         for (int j = a.j0 + tid; j <= a.j1; j += ADJ_THREADS) {
+            // dL / dFobs_j = sum over the bands reaching j of C(j, b) dL / dfband_b: the warp's 32 pixels form one
+            // chunk, whose bands are read as coalesced rows of the band-major matrix
             float fo_bar = 0.f;
-            const int e1 = a.bptr[j - a.j0 + 1];
-            for (int e = a.bptr[j - a.j0]; e < e1; ++e) fo_bar = fmaf(a.bw[e], fbs[a.bidx[e]], fo_bar);
+            const int2 br = __ldg(a.bchunk + ((j - a.j0) >> 5));
+            for (int b = br.x; b <= br.y; ++b) {
+                const int4 bm = __ldg(a.bmeta + b);
+                if (j >= bm.x && j <= bm.y) fo_bar = fmaf(__ldg(a.bc + bm.z + (j - bm.x)), fbs[b], fo_bar);
+            }
             float v;
             int cl = j;
             float xf = 1.f;
@@ -197,92 +356,95 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
                 float t = tin;
                 if (cl != il) {
                     // outside the grid: the first / last interval extrapolated
-                    t = (adj_ex2(((float)(j - cl) - zi.z) * dl2) - 1.f) * inv_em1;
-                    xf = adj_ex2((float)(il - cl) * dl2);
+                    t = (adj_ex2(((float)(j - cl) - zi.z) * a.dl2) - 1.f) * a.inv_em1;
+                    xf = adj_ex2((float)(il - cl) * a.dl2);
                 }
                 v = fmaf(t, S[cl + 1] - S[cl], S[cl]);
             } else {
                 v = S[j];
             }
-            const float vb = (v > 0.f) ? fo_bar * a.wl[j] : 0.f;   // (NaN v: 0, as the forward)
+            const float vb = (v > 0.f) ? fo_bar * __ldg(a.wl + j) : 0.f;   // (NaN v: 0, as the forward)
             VB[j - a.j0] = vb;
-            if (shifted && vb != 0.f) gz = fmaf(vb * (S[cl + 1] - S[cl]), xf, gz);
+            if (shifted && vb != 0.f) gobs = fmaf(vb * (S[cl + 1] - S[cl]), xf, gobs);
         }
     }
     __syncthreads();
-    // ---- pass 3: SB = dL / dS: the spectrum's own cotangent and the transpose of the observed-frame interpolation
-    for (int p = tid; p < ns; p += ADJ_THREADS) {
-        float sb = sbar ? (float)(sbar[p] / c) : 0.f;
-        if (mb) {
-            if (!shifted) {
-                if (p >= a.j0 && p <= a.j1) sb += VB[p - a.j0];
+    // ---- pass 3: dL / dS (into S): the spectrum's own cotangent and the transpose of the observed-frame
+    // interpolation
+    for (int p = 2 * tid; p < ns; p += 2 * ADJ_THREADS) {
+        float sb[2] = {0.f, 0.f};
+        if (sbar) {
+            if (even && p + 1 < ns) {
+                const double2 v = __ldg(reinterpret_cast<const double2 *>(sbar + p));
+                sb[0] = scaled_to_f32(v.x, ks);
+                sb[1] = scaled_to_f32(v.y, ks);
             } else {
-                const int ja = p + nsh;        // interval p, weight 1 - t
-                const int jb = p - 1 + nsh;    // interval p - 1, weight t
-                if (p <= ns - 2 && ja >= a.j0 && ja <= a.j1) sb = fmaf(1.f - tin, VB[ja - a.j0], sb);
-                if (p >= 1 && jb >= a.j0 && jb <= a.j1) sb = fmaf(tin, VB[jb - a.j0], sb);
+                sb[0] = scaled_to_f32(sbar[p], ks);
+                if (p + 1 < ns) sb[1] = scaled_to_f32(sbar[p + 1], ks);
             }
         }
-        SB[p] = sb;
+#pragma unroll
+        for (int u2 = 0; u2 < 2; ++u2) {
+            const int q = p + u2;
+            if (q >= ns) break;
+            float x = sb[u2];
+            if (mb) {
+                if (!shifted) {
+                    if (q >= a.j0 && q <= a.j1) x += VB[q - a.j0];
+                } else {
+                    const int ja = q + nsh;        // interval q, weight 1 - t
+                    const int jb = q - 1 + nsh;    // interval q - 1, weight t
+                    if (q <= ns - 2 && ja >= a.j0 && ja <= a.j1) x = fmaf(1.f - tin, VB[ja - a.j0], x);
+                    if (q >= 1 && jb >= a.j0 && jb <= a.j1) x = fmaf(tin, VB[jb - a.j0], x);
+                }
+            }
+            S[q] = x;
+        }
     }
     __syncthreads();
     if (tid == 0 && mb && shifted) {
         // observed pixels whose interval lies outside the grid (extrapolated from the first / last interval)
         const int lo_end = min(a.j1, nsh - 1), hi_beg = max(a.j0, ns - 1 + nsh);
         for (int j = a.j0; j <= lo_end; ++j) {
-            const float t = (adj_ex2(((float)j - zi.z) * dl2) - 1.f) * inv_em1;
-            SB[0] = fmaf(1.f - t, VB[j - a.j0], SB[0]);
-            SB[1] = fmaf(t, VB[j - a.j0], SB[1]);
+            const float t = (adj_ex2(((float)j - zi.z) * a.dl2) - 1.f) * a.inv_em1;
+            S[0] = fmaf(1.f - t, VB[j - a.j0], S[0]);
+            S[1] = fmaf(t, VB[j - a.j0], S[1]);
         }
         for (int j = hi_beg; j <= a.j1; ++j) {
             const int cl = ns - 2;
-            const float t = (adj_ex2(((float)(j - cl) - zi.z) * dl2) - 1.f) * inv_em1;
-            SB[cl] = fmaf(1.f - t, VB[j - a.j0], SB[cl]);
-            SB[cl + 1] = fmaf(t, VB[j - a.j0], SB[cl + 1]);
+            const float t = (adj_ex2(((float)(j - cl) - zi.z) * a.dl2) - 1.f) * a.inv_em1;
+            S[cl] = fmaf(1.f - t, VB[j - a.j0], S[cl]);
+            S[cl + 1] = fmaf(t, VB[j - a.j0], S[cl + 1]);
         }
     }
     __syncthreads();
-    // ---- pass 4: the smoothing's transpose (dL / dTOT, into S) and d / dsigma of its taps:
-    // dc_d / dsigma = c_d (a_d - sum_u c_u a_u), a_d = (ln lambda_i0 - ln lambda_(i0 + d))^2 / (s^3 c), s = sigma / c
+    // ---- pass 4: d / dsigma of the taps (dtap from the per-model block; they sum to zero, so the differences from
+    // the centre keep the FP32 sum clear of cancellation), then the smoothing's transpose into TOT
     float gs = 0.f;
-    float dtap[9];
+    if (R >= 0) {
+        float dtap[9];
 #pragma unroll
-    for (int d = 0; d < 9; ++d) dtap[d] = 0.f;
-    {
-        const double sig = pr[PF_SIGMA_SMOOTH];
-        if (R >= 0 && sig > 0.0) {
-            const double sb = sig / ADJ_C_KMS;
-            const double inv = 1.0 / (sb * sb * sb * ADJ_C_KMS);
-            float av[9], mean = 0.f;
+        for (int d = 0; d < 9; ++d) dtap[d] = __ldg(ap + AP_DTAP + d);
+        for (int p = max(a.sm_lo, 0) + tid; p <= a.sm_hi; p += ADJ_THREADS) {
+            const float t0 = TOT[p];
+            float ds = 0.f;
 #pragma unroll
-            for (int d = -4; d <= 4; ++d) {
-                const int j = min(max(a.sm_lo + d, 0), ns - 1);
-                const double dd = a.lnlam[a.sm_lo] - a.lnlam[j];
-                av[d + 4] = (float)(dd * dd * inv);
-                mean = fmaf(tap[d + 4], av[d + 4], mean);
-            }
-#pragma unroll
-            for (int d = 0; d < 9; ++d) dtap[d] = tap[d] * (av[d] - mean);
+            for (int d = -4; d <= 4; ++d) ds = fmaf(dtap[d + 4], TOT[p + d] - t0, ds);
+            gs = fmaf(S[p], ds, gs);
         }
     }
-    // the cotangent of TOT goes to S (S is not read after pass 2)
+    __syncthreads();
     for (int p = tid; p < ns; p += ADJ_THREADS) {
         const bool act = R >= 0 && p >= a.sm_lo && p <= a.sm_hi;
-        float tb = act ? 0.f : SB[p];
+        float tb = act ? 0.f : S[p];
         if (R >= 0) {
 #pragma unroll
             for (int d = -4; d <= 4; ++d) {
                 const int r = p - d;   // S(r) reads TOT(r + d) = TOT(p)
-                if (r >= a.sm_lo && r <= a.sm_hi) tb = fmaf(tap[d + 4], SB[r], tb);
+                if (r >= a.sm_lo && r <= a.sm_hi) tb = fmaf(tap[d + 4], S[r], tb);
             }
         }
-        if (act) {
-            float ds = 0.f;
-#pragma unroll
-            for (int d = -4; d <= 4; ++d) ds = fmaf(dtap[d + 4], TOT[p + d], ds);
-            gs = fmaf(SB[p], ds, gs);
-        }
-        S[p] = tb;
+        TOT[p] = tb;
     }
     __syncthreads();
     // ---- pass 5: the IGM and attenuation adjoints; the young / old cotangents (bf16 hi / lo); parameter gradients
@@ -290,51 +452,28 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
 #pragma unroll
     for (int k = 0; k < NG; ++k) g[k] = 0.f;
     const float d2 = (float)pr[PF_DUST2], d3 = (float)pr[PF_DUST3], d1 = (float)pr[PF_DUST1];
-    const float one_m_fnd = mp[MP_ONE_M_FND], one_m_fo = mp[MP_ONE_M_FO];
-    float gz_igm = 0.f;
-    for (int p = tid; p < a.ppad; p += ADJ_THREADS) {
-        float yb = 0.f, ob = 0.f;
+    __nv_bfloat162 *yh = reinterpret_cast<__nv_bfloat162 *>(a.ybar_hi + (size_t)m * a.ppad);
+    __nv_bfloat162 *yl = reinterpret_cast<__nv_bfloat162 *>(a.ybar_lo + (size_t)m * a.ppad);
+    __nv_bfloat162 *oh = reinterpret_cast<__nv_bfloat162 *>(a.obar_hi + (size_t)m * a.ppad);
+    __nv_bfloat162 *ol = reinterpret_cast<__nv_bfloat162 *>(a.obar_lo + (size_t)m * a.ppad);
+    for (int p = 2 * tid; p < a.ppad; p += 2 * ADJ_THREADS) {
+        float yb[2] = {0.f, 0.f}, ob[2] = {0.f, 0.f};
         if (p < ns) {
-            const PixFwd f = pix_forward(a, mp, p, igm_model, jmax, b, db);
-            const float y = yv[p], o = ov[p];
-            const float ss = y * f.ssfac_y + o * f.to;
-            const float pre = ss * f.D;
-            float pb = S[p];
-            if (f.igm) {
-                // T = exp(-igm_factor tau): dT/dz = -igm_factor T dtau/dz, dT/d igm_factor = -tau T
-                const float T = adj_ex2(f.tau * kf);
-                const float gT = pb * pre;
-                gz_igm = fmaf(gT, -f_igm * T * f.dtau, gz_igm);
-                g[G_IGMF] = fmaf(gT, -f.tau * T, g[G_IGMF]);
-                pb *= T;
-            }
-            // pre = ss D, D = T_d (1 - fnd) + fnd, ss = y (T_b (1 - fo) + fo) + o T_o
-            const float dcurve = f.curve * f.ltab;   // d curve / d dust_index
-            g[G_DUST2] = fmaf(pb * ss * one_m_fnd, -f.td * f.curve, g[G_DUST2]);
-            g[G_DUST_INDEX] = fmaf(pb, ss * one_m_fnd * f.td * (-d2 * dcurve) + f.D * o * f.to * (-d3 * dcurve),
-                                   g[G_DUST_INDEX]);
-            g[G_FNODUST] = fmaf(pb * ss, 1.f - f.td, g[G_FNODUST]);
-            const float ybase = pb * f.D * y;
-            g[G_DUST1] = fmaf(ybase * one_m_fo, -f.tb * f.c1, g[G_DUST1]);
-            g[G_DUST1_INDEX] = fmaf(ybase * one_m_fo, -f.tb * d1 * f.c1 * f.ltab, g[G_DUST1_INDEX]);
-            g[G_FOBRUN] = fmaf(ybase, 1.f - f.tb, g[G_FOBRUN]);
-            g[G_DUST3] = fmaf(pb * f.D * o, -f.to * f.curve, g[G_DUST3]);
-            yb = pb * f.D * f.ssfac_y;
-            ob = pb * f.D * f.to;
-        }
-        const size_t q = (size_t)m * a.ppad + p;
-        const __nv_bfloat16 yh = __float2bfloat16_rn(yb), oh = __float2bfloat16_rn(ob);
-        a.ybar_hi[q] = yh;
-        a.ybar_lo[q] = __float2bfloat16_rn(yb - __bfloat162float(yh));
-        a.obar_hi[q] = oh;
-        a.obar_lo[q] = __float2bfloat16_rn(ob - __bfloat162float(oh));
-    }
-    g[G_ZRED] = gz_igm;
-    g[G_SIGMA] = gs;
-    // the observed frame's d / dz (kept apart: its factor is applied in FP64 below)
-    float gobs = gz;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) gobs += __shfl_xor_sync(0xffffffffu, gobs, off);
+            for (int u2 = 0; u2 < 2; ++u2) {
+                const int q = p + u2;
+                if (q >= ns) break;
+                pixel_adjoint(a, mc, q, yv[q], ov[q], TOT[q], f_igm, kf, d1, d2, d3, g, yb[u2], ob[u2]);
+            }
+        }
+        const __nv_bfloat162 hy = bf16_hi2(yb[0], yb[1]), ho = bf16_hi2(ob[0], ob[1]);
+        yh[p >> 1] = hy;
+        yl[p >> 1] = bf16_lo2(yb[0], yb[1], hy);
+        oh[p >> 1] = ho;
+        ol[p >> 1] = bf16_lo2(ob[0], ob[1], ho);
+    }
+    g[G_SIGMA] = gs;
+    g[G_OBS] = gobs;
 #pragma unroll
     for (int k = 0; k < NG; ++k) {
         float v = g[k];
@@ -342,40 +481,38 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if (lane == 0) red[k][warp] = v;
     }
-    if (lane == 0) cred[warp] = (double)gobs;   // (cred's first use ended before the syncs above)
     __syncthreads();
     if (tid < NBGRAD) {
-        const int row_of[NG] = {R_DUST2, R_DUST_INDEX, R_FRAC_NODUST, R_DUST1, R_DUST1_INDEX, R_FRAC_OBRUN,
-                                R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA};
+        const double c = ldexp(1.0, ks);
+        const int row_of[NG - 1] = {R_DUST2, R_DUST_INDEX, R_FRAC_NODUST, R_DUST1, R_DUST1_INDEX, R_FRAC_OBRUN,
+                                    R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA};
         double v = 0.0;
         int k = -1;
 #pragma unroll
-        for (int i = 0; i < NG; ++i)
+        for (int i = 0; i < NG - 1; ++i)
             if (row_of[i] == tid) k = i;
         if (k >= 0) {
-            for (int w = 0; w < ADJ_THREADS / 32; ++w) v += (double)red[k][w];
+            for (int w = 0; w < ADJ_WARPS; ++w) v += (double)red[k][w];
             v *= c;
         }
         if (tid == R_ZRED) {
-            if (shifted) {
-                // dt/dz = -lambda_j / ((1 + z)^2 (lambda_(il+1) - lambda_il)) on the log-uniform grid
-                double go = 0.0;
-                for (int w = 0; w < ADJ_THREADS / 32; ++w) go += cred[w];
-                const double opz = 1.0 + z;
-                v += c * go * (-exp((double)nsh * a.dlnl) / (opz * opz * expm1(a.dlnl)));
-            }
-            if (mb && fabs(z) > SAFE_FLOOR) {
-                // the distance term's derivative, d_L linear in the cosmology table
-                const int idx = max(0, min(find_interval0(a.zt, 500, z), 498));
-                const double slope = (a.dl[idx + 1] - a.dl[idx]) / (a.zt[idx + 1] - a.zt[idx]);
-                const double dm = a.dl[idx] + slope * (z - a.zt[idx]);
-                if (dm == dm && dm > SAFE_FLOOR)
-                    v += s_msum * (5.0 / log(10.0) * slope / dm - 2.5 / (log(10.0) * (1.0 + z)));
-            }
+            // the observed frame's share (its factor formed in FP64 per model) and the distance term's
+            double go = 0.0, ms = 0.0;
+            for (int w = 0; w < ADJ_WARPS; ++w) { go += (double)red[G_OBS][w]; ms += wsum[w]; }
+            const double *apd = reinterpret_cast<const double *>(ap);
+            v += c * go * apd[AP_KOBS / 2];
+            if (mb) v += ms * apd[AP_DDIST / 2];
         }
         a.params_bar[(size_t)m * NBGRAD + tid] = v;
     }
+    if (tid == 0) {
+        a.cscale[m] = ldexp(1.0, ks);
+        // (a wait above that gave up leaves the bulk copies to be waited for here, before the CTA exits)
+        mbar_wait(&rows_bar, 0, a.status, ERR_TIMEOUT_ADJOINT, false);
+    }
 }
+
+__host__ __device__ int adj_row_pad(int ns) { return (ns + 8 + 3) / 4 * 4; }
 
 // ---------------------------------------------------------------------------------------------- transposed basis
 // t(k, p) = basis(p, k): kpad x ppad from ns x kpad (zero for p >= ns), 32 x 32 tiles through shared memory.
@@ -418,11 +555,14 @@ __global__ void wzbar_kernel(WzbArgs a) {
     a.wzb[i] = v;
 }
 
-cudaError_t run_adjoint(const AdjointArgs &a, cudaStream_t st) {
+cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st) {
     if (a.n_models <= 0) return cudaSuccess;
+    adjoint_prep_kernel<<<(pa.n_models + 255) / 256, 256, 0, st>>>(pa);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     const int nj = a.j1 - a.j0 + 1;
-    const size_t smem = sizeof(float) * (3 * (size_t)a.nspec + (size_t)(nj > 0 ? nj : 1));
-    cudaError_t e = cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = sizeof(float) * (2 * (size_t)adj_row_pad(a.nspec) + 2 * (size_t)a.nspec + (size_t)(nj > 0 ? nj : 1));
+    e = cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     adjoint_kernel<<<a.n_models, ADJ_THREADS, smem, st>>>(a);
     return cudaGetLastError();
@@ -508,22 +648,30 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), s);
 
     // ---- the per-model adjoint
+    if ((e = c.d_apar.reserve((size_t)32 * n)) != cudaSuccess) { err = msg("device memory", e); return ST_DATA_MISSING; }
+    AdjointPrepArgs pa;
+    pa.n_models = n; pa.nspec = ns; pa.sm_lo = c.geom.sm_lo; pa.dlnl = c.dlnl; pa.em1 = std::expm1(c.dlnl);
+    pa.par = c.d_params.p; pa.mpar = c.d_mpar.p; pa.zinfo = c.d_zinfo.p; pa.lnlam = c.d_lnlam.p;
+    pa.zt = c.d_zt.p; pa.dl = c.d_dl.p; pa.apar = c.d_apar.p;
     AdjointArgs a;
     a.n_models = n; a.nspec = ns; a.ppad = ppad; a.nbands = nb; a.jtop = c.jtop;
     a.j0 = c.band_j0; a.j1 = nb > 0 ? c.band_j1 : c.band_j0 - 1;
     a.sm_lo = c.geom.sm_lo; a.sm_hi = c.geom.sm_hi; a.uniform_index = c.geom.uniform_index;
-    a.dlnl = c.dlnl;
-    a.young = c.d_young.p; a.old = c.d_old.p; a.mpar = c.d_mpar.p; a.par = c.d_params.p; a.zinfo = c.d_zinfo.p;
-    a.fband = c.d_fband.p;
+    a.dl2 = (float)(c.dlnl * 1.4426950408889634); a.inv_em1 = (float)(1.0 / std::expm1(c.dlnl));
+    a.young = c.d_young.p; a.old = c.d_old.p; a.mpar = c.d_mpar.p; a.apar = c.d_apar.p; a.par = c.d_params.p;
+    a.zinfo = c.d_zinfo.p; a.fband = c.d_fband.p;
     a.mags_bar = mags_bar ? c.d_mags_bar.p : nullptr;
     a.spec_bar = spec_bar ? c.d_spec_bar.p : nullptr;
     a.do_band = c.mag_mask.empty() ? nullptr : c.d_do_band.p;
-    a.pix = c.d_pix.p; a.lam = c.d_lam.p; a.lnlam = c.d_lnlam.p; a.wl = c.d_wl.p;
-    a.bptr = c.d_bptr.p; a.bidx = c.d_bidx.p; a.bw = c.d_bw.p; a.zt = c.d_zt.p; a.dl = c.d_dl.p;
+    a.pix = c.d_pix.p; a.wl = c.d_wl.p; a.bc = c.d_bc.p; a.bmeta = c.d_bmeta.p; a.bchunk = c.d_bchunk.p;
+    a.lt_base = (float)(std::log(c.lam[0] / 5500.0) * 1.4426950408889634);
+    a.lt_step = (float)(c.dlnl * 1.4426950408889634);
     a.ybar_hi = c.d_ybh.p; a.ybar_lo = c.d_ybl.p; a.obar_hi = c.d_obh.p; a.obar_lo = c.d_obl.p;
-    a.cscale = c.d_cscale.p; a.params_bar = c.d_pbar.p;
-    if ((e = run_adjoint(a, s)) != cudaSuccess) { err = msg("adjoint kernel", e); return ST_DATA_MISSING; }
-    int launches = 1;
+    a.cscale = c.d_cscale.p; a.params_bar = c.d_pbar.p; a.status = c.d_status.p;
+    prof_mark(c, 6);
+    if ((e = run_adjoint(pa, a, s)) != cudaSuccess) { err = msg("adjoint kernel", e); return ST_DATA_MISSING; }
+    prof_mark(c, 7);
+    int launches = 2;
 
     // ---- the weights' cotangent: young and old pixel cotangents against the transposed basis
     if (weights_z_bar) {
@@ -551,6 +699,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
             if ((e = run_gemm_bf16x3(pl, g, s)) != cudaSuccess) { err = msg("weights GEMM", e); return ST_DATA_MISSING; }
             ++launches;
         }
+        prof_mark(c, 8);
         WzbArgs w;
         w.n_models = n; w.ntz = ntz; w.ldd = kpad; w.D = c.d_wzb32.p; w.col_of = bop->col_of.p;
         w.cscale = c.d_cscale.p; w.mass_bar = mass_bar ? c.d_mass_bar.p : nullptr;
@@ -559,6 +708,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         const size_t tot = (size_t)n * ntz;
         wzbar_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(w);
         if ((e = cudaGetLastError()) != cudaSuccess) { err = msg("weights cotangent kernel", e); return ST_DATA_MISSING; }
+        prof_mark(c, 9);
         ++launches;
         if ((e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
             err = msg("weights cotangent copy", e);

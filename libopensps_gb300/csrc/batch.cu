@@ -312,7 +312,7 @@ void prof_harvest(Context &c, int s) {
     c.prof_pending[s] = false;
 }
 
-static void prof_mark(Context &c, int k) {
+void prof_mark(Context &c, int k) {
     if (!c.profile || k >= Context::NPROF) return;
     if (k == 0) {
         c.prof_set ^= 1;
@@ -531,7 +531,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.young = ca.old = nullptr;
     const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
     if (parts) {
-        if ((e = c.d_young.reserve((size_t)n * ns)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns)) != cudaSuccess) {
+        // (4 floats of padding: the reverse pass copies whole 16-byte units of each row)
+        if ((e = c.d_young.reserve((size_t)n * ns + 4)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns + 4)) != cudaSuccess) {
             err = cuda_msg("device memory", e);
             return ST_DATA_MISSING;
         }

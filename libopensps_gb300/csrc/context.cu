@@ -157,9 +157,9 @@ Context::~Context() {
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
     d_status.release(); d_young.release(); d_old.release(); d_eml.release(); d_eml_lum.release(); d_eml_kidx.release();
-    d_bptr.release(); d_bidx.release(); d_bw.release(); d_mags_bar.release(); d_spec_bar.release(); d_mass_bar.release();
+    d_bc.release(); d_bmeta.release(); d_bchunk.release(); d_mags_bar.release(); d_spec_bar.release(); d_mass_bar.release();
     d_lbol_bar.release(); d_cscale.release(); d_pbar.release(); d_wzbar.release(); d_ybh.release(); d_ybl.release();
-    d_obh.release(); d_obl.release(); d_wzb32.release();
+    d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
@@ -295,22 +295,32 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
         err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
         return ST_BAD_ARG;
     }
-    // the same matrix by pixel for the reverse pass (CSR over pixels j0 .. j1: the bands reaching each, FP32 weights)
-    std::vector<int> bptr(1, 0), bidx;
-    std::vector<float> bw;
-    for (int j = j0; j <= j1; ++j) {
-        for (int b = 0; b < nb; ++b) {
-            const double w = cm[(size_t)b * ns + j];
-            if (w == 0.0) continue;
-            bidx.push_back(b);
-            bw.push_back((float)w);
-        }
-        bptr.push_back((int)bidx.size());
+    // the same matrix by band for the reverse pass: each band's nonzero pixel range as a dense row, and per chunk of 32
+    // pixels from j0 the first and last band reaching it
+    std::vector<float> bc;
+    std::vector<int4> bmeta(nb);
+    for (int b = 0; b < nb; ++b) {
+        int lo = ns, hi = -1;
+        for (int j = 0; j < ns; ++j)
+            if (cm[(size_t)b * ns + j] != 0.0) { lo = std::min(lo, j); hi = std::max(hi, j); }
+        bmeta[b] = make_int4(lo, hi, (int)bc.size(), 0);
+        for (int j = lo; j <= hi; ++j) bc.push_back((float)cm[(size_t)b * ns + j]);
     }
-    if (bidx.empty()) { bidx.push_back(0); bw.push_back(0.f); }
-    if ((e = upload(c.d_bptr, bptr.data(), bptr.size())) != cudaSuccess ||
-        (e = upload(c.d_bidx, bidx.data(), bidx.size())) != cudaSuccess ||
-        (e = upload(c.d_bw, bw.data(), bw.size())) != cudaSuccess) {
+    const int nchunk = std::max(1, (j1 - j0 + 1 + 31) / 32);
+    std::vector<int2> bchunk(nchunk, make_int2(1, 0));
+    for (int k = 0; k < nchunk; ++k) {
+        const int a0 = j0 + 32 * k, a1 = a0 + 31;
+        for (int b = 0; b < nb; ++b) {
+            if (bmeta[b].y < a0 || bmeta[b].x > a1 || bmeta[b].y < bmeta[b].x) continue;
+            if (bchunk[k].x > bchunk[k].y) bchunk[k] = make_int2(b, b);
+            else bchunk[k].y = b;
+        }
+    }
+    if (bc.empty()) bc.push_back(0.f);
+    if (bmeta.empty()) bmeta.push_back(make_int4(ns, -1, 0, 0));
+    if ((e = upload(c.d_bc, bc.data(), bc.size())) != cudaSuccess ||
+        (e = upload(c.d_bmeta, bmeta.data(), bmeta.size())) != cudaSuccess ||
+        (e = upload(c.d_bchunk, bchunk.data(), bchunk.size())) != cudaSuccess) {
         err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
         return ST_BAD_ARG;
     }

@@ -115,18 +115,20 @@ struct Context {
     DevBuf<int> d_eml_kidx;
     int eml_nnz = -1;            // entries of the line table (-1: not built)
     BatchGeom geom;              // of the last batch
-    // reverse pass: the band matrix by pixel (CSR over pixels band_j0 .. band_j1), cotangents and results
+    // reverse pass: the band matrix by band (band b's nonzero pixels lo .. hi as a dense row at off), the bands
+    // reaching each 32-pixel chunk from band_j0 (first, last), cotangents and results
     int band_j1 = -1;
-    DevBuf<int> d_bptr, d_bidx;
-    DevBuf<float> d_bw;
+    DevBuf<float> d_bc;
+    DevBuf<int4> d_bmeta;        // (lo, hi, off, 0) per band
+    DevBuf<int2> d_bchunk;       // (first, last) band per chunk; first > last: none
     DevBuf<double> d_mags_bar, d_spec_bar, d_mass_bar, d_lbol_bar, d_cscale, d_pbar, d_wzbar;
     DevBuf<__nv_bfloat16> d_ybh, d_ybl, d_obh, d_obl;
-    DevBuf<float> d_wzb32;
+    DevBuf<float> d_wzb32, d_apar;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch
     // profiling: events recorded between the kernels of a batch (opensps_gb300_set_profiling)
-    static constexpr int NPROF = 8;
+    static constexpr int NPROF = 10;
     int profile = 0, prof_set = 0, prof_used[2] = {0, 0}, prof_count = 0, prof_nstage = 0;
     bool prof_pending[2] = {false, false};
     double prof_acc[NPROF] = {};
@@ -169,6 +171,8 @@ struct BatchIO {
            *lbol_old = nullptr, *sfr = nullptr, *mdust = nullptr;
 };
 int run_batch(Context &c, const BatchIO &io, std::string &err);
+// With profiling on: records event k on the context's stream (0 starts a batch's set).
+void prof_mark(Context &c, int k);
 
 cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
                                 uint32_t box_outer);

@@ -30,6 +30,7 @@ enum {
     ERR_TIMEOUT_MMA = 0x102,
     ERR_TIMEOUT_EPILOGUE = 0x103,
     ERR_TIMEOUT_BAND = 0x104,
+    ERR_TIMEOUT_ADJOINT = 0x105,
 };
 
 // Per-pixel table (floats per pixel): ln(lambda / 5500 A) log2(e), the diffuse curve (lambda / 5500)^dust_index of
@@ -149,11 +150,22 @@ cudaError_t run_gemm_bf16x3(const GemmPlan &pl, const GemmArgs &g, cudaStream_t 
 
 // The reverse pass per model (adjoint.cu): from the forward's young / old sums, band fluxes and the cotangents, the
 // cotangents of the young and old sums (bf16 hi / lo operands of the weight GEMM) and the parameter gradients.
+struct AdjointPrepArgs {
+    int n_models, nspec, sm_lo;
+    double dlnl, em1;                // grid step in ln lambda, e^dlnl - 1
+    const double *par;               // n_models x PAR_DEVICE
+    const float *mpar;               // n_models x MODEL_PAR_FLOATS
+    const float4 *zinfo;
+    const double *lnlam;             // nspec
+    const double *zt, *dl;           // cosmology table (500)
+    float *apar;                     // n_models x 32: the per-model block of the reverse pass
+};
 struct AdjointArgs {
     int n_models, nspec, ppad, nbands, jtop, j0, j1, sm_lo, sm_hi, uniform_index;
-    double dlnl;
-    const float *young, *old;        // n_models x nspec: the forward's age sums before dust
+    float dl2, inv_em1;              // dlnl log2(e), 1 / (e^dlnl - 1)
+    const float *young, *old;        // n_models x nspec (+ 4 floats of padding): the forward's age sums before dust
     const float *mpar;               // n_models x MODEL_PAR_FLOATS
+    const float *apar;               // n_models x 32 (AdjointPrepArgs::apar)
     const double *par;               // n_models x PAR_DEVICE (dust1 .. dust_tesc)
     const float4 *zinfo;             // n_models: the observed-frame shift
     const double *fband;             // n_models x nbands
@@ -161,17 +173,17 @@ struct AdjointArgs {
     const double *spec_bar;          // n_models x nspec, or null
     const int *do_band;              // nbands, or null: every band
     const float *pix;                // nspec x PIX_FLOATS
-    const double *lam, *lnlam;       // nspec
     const float *wl;                 // nspec: 1 / lambda
-    const int *bptr;                 // j1 - j0 + 2: the bands reaching pixel j0 + i are bidx[bptr[i] .. bptr[i+1]-1]
-    const int *bidx;
-    const float *bw;                 // the band matrix C(j, b) of those entries
-    const double *zt, *dl;           // cosmology table (500)
+    const float *bc;                 // the band matrix C(j, b) by band: band b's pixels lo .. hi at bc + off
+    const int4 *bmeta;               // nbands: (lo, hi, off, 0)
+    const int2 *bchunk;              // per 32 pixels from j0: the first and last band reaching them
+    float lt_base, lt_step;          // ln(lambda_p / 5500) log2(e) = lt_base + p lt_step (the log-uniform grid)
     __nv_bfloat16 *ybar_hi, *ybar_lo, *obar_hi, *obar_lo;   // n_models x ppad (zero beyond nspec)
     double *cscale;                  // n_models: the cotangent scale (the A operands are divided by it)
     double *params_bar;              // n_models x 44
+    int *status;
 };
-cudaError_t run_adjoint(const AdjointArgs &a, cudaStream_t st);
+cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

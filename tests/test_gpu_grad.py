@@ -127,3 +127,24 @@ def test_mass_and_lbol_cotangents_alone(gctx, data):
     want = massb[:, None, None] * data["ssp_mass"][None] + (lbolb / (np.log(10.0) * lsum))[:, None, None] * llin[None]
     np.testing.assert_allclose(got["weights_z_bar"], want, rtol=1e-6, atol=1e-12 * np.max(np.abs(want)))
     np.testing.assert_allclose(got["params_bar"], 0.0)
+
+
+def test_sigma_smooth_gradient_from_spectrum_cotangents(gctx, oracle40, data):
+    """sigma_smooth alone: spectrum cotangents only inside the smoothing range, where the gradient is a second
+    difference of the spectrum. Within 2e-3 of the central difference (floor 1e-3 of the batch's largest)."""
+    n, seed = 8, 90
+    wz, params = _inputs(data, n, seed)
+    lam = data["lambda"]
+    rng = np.random.default_rng(seed)
+    sel = (lam >= 1e3) & (lam <= 1e4)
+    sb = np.zeros((n, lam.size))
+    sb[:, sel] = rng.standard_normal((n, int(sel.sum())))
+    got = gctx.csp_batch_grad(params, wz, spec_bar=sb)
+    k = "sigma_smooth"
+    h = H_REL * np.abs(params[k])
+    up = oracle40.csp_batch(dict(params, **{k: params[k] + h}), wz)
+    dn = oracle40.csp_batch(dict(params, **{k: params[k] - h}), wz)
+    fd = (np.sum(sb * up["spec"], axis=1) - np.sum(sb * dn["spec"], axis=1)) / (2.0 * h)
+    g = got["params_bar"][:, ROWS[k]]
+    err = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd)))
+    assert float(err.max()) <= RTOL, (g, fd)
