@@ -239,16 +239,25 @@ class Context:
         del keep
         return out
 
-    def csp_batch_grad(self, params: dict, ssp_weights_z: np.ndarray, mags_bar: np.ndarray | None = None,
+    def csp_batch_grad(self, params: dict, ssp_weights_z: np.ndarray | None = None, mags_bar: np.ndarray | None = None,
                        spec_bar: np.ndarray | None = None, mass_bar: np.ndarray | None = None,
                        lbol_bar: np.ndarray | None = None, params_bar_rows: int | None = None,
-                       weights_z_bar: bool = True, spec: bool = True, out: dict | None = None) -> dict:
+                       weights_z_bar: bool = True, spec: bool = True, out: dict | None = None,
+                       ssp_weights: np.ndarray | None = None, n: int | None = None) -> dict:
         """compute_csp_batch_grad_rows: the forward batch and the reverse pass for the given cotangents (arrays
-        (n, nbands), (n, nspec), (n,), (n,)). Returns the forward outputs (mags, mass, lbol, and spec unless
-        spec=False), params_bar (n, rows) and weights_z_bar (n, nz, nt). ``out`` may hold preallocated C-contiguous
-        float64 arrays for any of these (e.g. page-locked ones)."""
-        w = np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
-        n = w.shape[0]
+        (n, nbands), (n, nspec), (n,), (n,)). Weights: ssp_weights_z (n, nz, nt), or ssp_weights (n, nt) blended at
+        logzsol, or neither (the context's SFH from the per-model SFH parameters; give n). Returns the forward
+        outputs (mags, mass, lbol, and spec unless spec=False), params_bar (n, rows) and weights_z_bar (n, nz, nt)
+        with ssp_weights_z, weights_bar (n, nt) otherwise. ``out`` may hold preallocated C-contiguous float64 arrays
+        for any of these (e.g. page-locked ones)."""
+        w = None if ssp_weights_z is None else np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
+        wa = None if ssp_weights is None else np.ascontiguousarray(ssp_weights, dtype=np.float64)
+        if w is not None:
+            n = w.shape[0]
+        elif wa is not None:
+            n = wa.shape[0]
+        elif n is None:
+            raise ValueError("give n with SFH parameters (no weights)")
         ns, nb, nt, nz = self.nspec, self.nbands, self.ntfull, self.nz
         rows = params_bar_rows if params_bar_rows is not None else nbgrad(self.lib)
         k, c_names, c_vals, keep = _names_values(params, n)
@@ -259,8 +268,10 @@ class Context:
         shapes = {"mags": (n, nb), "mass": (n,), "lbol": (n,), "params_bar": (n, rows)}
         if spec:
             shapes["spec"] = (n, ns)
-        if weights_z_bar:
+        if weights_z_bar and w is not None:
             shapes["weights_z_bar"] = (n, nz, nt)
+        if weights_z_bar and w is None:
+            shapes["weights_bar"] = (n, nt)
         given = out or {}
         res = {}
         for name, shp in shapes.items():
@@ -272,10 +283,10 @@ class Context:
             res[name] = a
         st = C.c_int(0)
         self.lib.opensps_context_compute_csp_batch_grad_rows(
-            self.handle, n, k, c_names, c_vals, None, _ptr(w), None, _ptr(cot["mags_bar"]), _ptr(cot["spec_bar"]),
+            self.handle, n, k, c_names, c_vals, _ptr(wa), _ptr(w), None, _ptr(cot["mags_bar"]), _ptr(cot["spec_bar"]),
             _ptr(cot["mass_bar"]), _ptr(cot["lbol_bar"]), _ptr(res["mags"]), _ptr(res.get("spec")),
-            _ptr(res["mass"]), _ptr(res["lbol"]), None, None, None, None, _ptr(res["params_bar"]), rows, None,
-            _ptr(res.get("weights_z_bar")), C.byref(st))
+            _ptr(res["mass"]), _ptr(res["lbol"]), None, None, None, None, _ptr(res["params_bar"]), rows,
+            _ptr(res.get("weights_bar")), _ptr(res.get("weights_z_bar")), C.byref(st))
         _check(st, self.lib)
         del keep
         return res

@@ -573,8 +573,8 @@ static std::string msg(const char *what, cudaError_t e) { return std::string(wha
 
 int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, const double *spec_bar,
                    const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
-                   double *weights_z_bar, std::string &err) {
-    if (!mags_bar && !spec_bar && !mass_bar && !lbol_bar && !params_bar && !weights_z_bar) return run_batch(c, io_in, err);
+                   double *weights_z_bar, double *weights_bar, std::string &err) {
+    if (!params_bar && !weights_z_bar && !weights_bar) return run_batch(c, io_in, err);
     const int n = io_in.n, ns = c.nspec, nb = c.nbands, ntz = c.nt * c.nz;
     if (mags_bar && (c.fast_mode || nb == 0)) {
         err = "mags_bar needs the magnitudes (fast mode off, a filter library)";
@@ -673,8 +673,11 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     prof_mark(c, 7);
     int launches = 2;
 
-    // ---- the weights' cotangent: young and old pixel cotangents against the transposed basis
-    if (weights_z_bar) {
+    // ---- the weights' cotangent: young and old pixel cotangents against the transposed basis (over ages and
+    // metallicities; with weights formed on the device, then through the blend and the SFH below)
+    const bool dev_blend = io_in.sfh_par != nullptr;
+    const bool sfh_rev = dev_blend && (weights_bar || params_bar);
+    if (weights_z_bar || sfh_rev) {
         if ((e = c.d_wzb32.reserve((size_t)n * kpad)) != cudaSuccess || (e = c.d_wzbar.reserve((size_t)n * ntz)) != cudaSuccess) {
             err = msg("device memory", e);
             return ST_DATA_MISSING;
@@ -703,14 +706,41 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         WzbArgs w;
         w.n_models = n; w.ntz = ntz; w.ldd = kpad; w.D = c.d_wzb32.p; w.col_of = bop->col_of.p;
         w.cscale = c.d_cscale.p; w.mass_bar = mass_bar ? c.d_mass_bar.p : nullptr;
-        w.lbol_bar = lbol_bar ? c.d_lbol_bar.p : nullptr; w.sums = c.d_sums.p; w.mass = c.d_mass.p; w.llin = c.d_llin.p;
+        // (the log-blended L_bol of weights formed on the device has its own cotangent, in the SFH reverse pass)
+        w.lbol_bar = (lbol_bar && !dev_blend) ? c.d_lbol_bar.p : nullptr;
+        w.sums = c.d_sums.p; w.mass = c.d_mass.p; w.llin = c.d_llin.p;
         w.wzb = c.d_wzbar.p;
         const size_t tot = (size_t)n * ntz;
         wzbar_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(w);
         if ((e = cudaGetLastError()) != cudaSuccess) { err = msg("weights cotangent kernel", e); return ST_DATA_MISSING; }
         prof_mark(c, 9);
         ++launches;
-        if ((e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+        if (weights_z_bar &&
+            (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+            err = msg("weights cotangent copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
+    // ---- weights formed on the device: the cotangent of the weights over ages, logzsol's row and the SFH rows
+    if (sfh_rev) {
+        const int nt = c.nt;
+        const bool tangents = io_in.given_w == nullptr && params_bar != nullptr;
+        if ((e = c.d_wbar.reserve((size_t)nt * n)) != cudaSuccess ||
+            (tangents && (e = c.d_dual.reserve((size_t)3 * nt * n * sfh_dual_bytes())) != cudaSuccess)) {
+            err = msg("device memory", e);
+            return ST_DATA_MISSING;
+        }
+        SfhRevArgs r;
+        r.n = n; r.nt = nt; r.nz = c.nz; r.sfh = io_in.sfh_type; r.rows = NBGRAD; r.has_logzsol = 1;
+        r.sfh_tangents = tangents ? 1 : 0;
+        r.tf = c.d_logage.p; r.lz = c.d_lz.p; r.lbol = c.d_lbol.p; r.par = c.d_sfhpar.p; r.w = c.d_w.p;
+        r.lblend = c.d_lblend.p; r.lbol_bar = lbol_bar ? c.d_lbol_bar.p : nullptr; r.wzb = c.d_wzbar.p;
+        r.weights_bar = c.d_wbar.p; r.scratch = c.d_sfh_scratch.p; r.params_bar = c.d_pbar.p;
+        r.dual = tangents ? (void *)c.d_dual.p : nullptr;
+        if ((e = run_sfh_reverse(r, s)) != cudaSuccess) { err = msg("SFH reverse kernel", e); return ST_DATA_MISSING; }
+        ++launches;
+        if (weights_bar &&
+            (e = cudaMemcpyAsync(weights_bar, c.d_wbar.p, sizeof(double) * nt * n, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
             err = msg("weights cotangent copy", e);
             return ST_DATA_MISSING;
         }

@@ -461,12 +461,32 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     std::vector<double> hp;
     if (io.dev_inputs) {
         d_par = io.dev_params;   // already PAR_DEVICE x n on the device
+    } else if (io.sfh_par) {
+        // the weights over ages (the SFH's, or the caller's) and their blend at logzsol, formed on the device
+        if ((e = c.d_sfhpar.reserve((size_t)SFH_NCOL * n)) != cudaSuccess || (e = c.d_w.reserve((size_t)nt * n)) != cudaSuccess ||
+            (e = c.d_sfh_scratch.reserve((size_t)2 * nt * n)) != cudaSuccess ||
+            (e = c.d_lblend.reserve((size_t)3 * n)) != cudaSuccess || (e = c.d_sfr.reserve(n)) != cudaSuccess ||
+            (io.given_w && (e = c.d_wgiven.reserve((size_t)nt * n)) != cudaSuccess) ||
+            (e = cudaMemcpyAsync(c.d_sfhpar.p, io.sfh_par, sizeof(double) * SFH_NCOL * n, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (io.given_w && (e = cudaMemcpyAsync(c.d_wgiven.p, io.given_w, sizeof(double) * nt * n, cudaMemcpyHostToDevice, st)) != cudaSuccess)) {
+            err = cuda_msg("SFH inputs", e);
+            return ST_DATA_MISSING;
+        }
+        SfhArgs sa;
+        sa.n = n; sa.nt = nt; sa.nz = nz; sa.sfh = io.sfh_type; sa.itesc = itesc;
+        sa.tf = c.d_logage.p; sa.lz = c.d_lz.p; sa.lbol = c.d_lbol.p; sa.par = c.d_sfhpar.p;
+        sa.given = io.given_w ? c.d_wgiven.p : nullptr;
+        sa.w = c.d_w.p; sa.scratch = c.d_sfh_scratch.p; sa.wz = c.d_wz.p; sa.lblend = c.d_lblend.p; sa.sfr = c.d_sfr.p;
+        if ((e = run_sfh_forward(sa, st)) != cudaSuccess) { err = cuda_msg("SFH weights kernel", e); return ST_DATA_MISSING; }
+        d_wz = c.d_wz.p;
     } else {
         if ((e = cudaMemcpyAsync(c.d_wz.p, io.wz, sizeof(double) * nwz, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
             err = cuda_msg("weights copy", e);
             return ST_DATA_MISSING;
         }
         d_wz = c.d_wz.p;
+    }
+    if (!io.dev_inputs) {
         hp.resize((size_t)PAR_DEVICE * n);
         for (int m = 0; m < n; ++m)
             for (int k = 0; k < PAR_DEVICE; ++k) hp[(size_t)PAR_DEVICE * m + k] = par(m, k);
@@ -665,6 +685,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             return ST_DATA_MISSING;
         }
     }
+    // weights formed on the device: L_bol blended in log between the slabs (model_sums MSUMS_BLEND,
+    // src/physics/opensps_csp_batch.f90:2129-2176), not the sum over the two slabs' linear L_bol; the SFH's SFR
+    std::vector<double> lblend, sfr_h;
+    if (io.sfh_par && !io.dev_inputs) {
+        lblend.resize((size_t)3 * n);
+        sfr_h.resize(n);
+        if ((e = cudaMemcpyAsync(lblend.data(), c.d_lblend.p, sizeof(double) * lblend.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(sfr_h.data(), c.d_sfr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+            err = cuda_msg("SFH outputs copy", e);
+            return ST_DATA_MISSING;
+        }
+    }
     int kstatus = 0;
     if ((e = cudaMemcpyAsync(&kstatus, c.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
         (e = cudaStreamSynchronize(st)) != cudaSuccess) {
@@ -698,7 +730,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if (io.old) io.old[i] = (double)old_h[i];
         }
     }
-    if (io.sfr) for (int m = 0; m < n; ++m) io.sfr[m] = std::nan("");
+    if (!lblend.empty()) {
+        for (int m = 0; m < n; ++m) {
+            const double *l = lblend.data() + (size_t)3 * m;
+            if (io.lbol) io.lbol[m] = l[0] > SAFE_FLOOR ? std::log10(l[0]) : 0.0;
+            if (io.lbol_young) io.lbol_young[m] = std::log10(std::max(l[1], SAFE_FLOOR));
+            if (io.lbol_old) io.lbol_old[m] = std::log10(std::max(l[2], SAFE_FLOOR));
+        }
+    }
+    if (io.sfr) for (int m = 0; m < n; ++m) io.sfr[m] = sfr_h.empty() ? std::nan("") : sfr_h[m];
     if (io.mdust) for (int m = 0; m < n; ++m) io.mdust[m] = SAFE_FLOOR;
     return 0;
 }

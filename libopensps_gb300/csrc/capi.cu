@@ -17,7 +17,7 @@ void clear_error();
 void prof_harvest(Context &c, int s);
 int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const double *spec_bar,
                    const double *mass_bar, const double *lbol_bar, double *params_bar, int params_bar_rows,
-                   double *weights_z_bar, std::string &err);
+                   double *weights_z_bar, double *weights_bar, std::string &err);
 int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zred, double *d_mags, bool sync,
                      std::string &err);
 }  // namespace sps
@@ -68,32 +68,6 @@ int build_params(Context &c, int n, int n_params, const char *const *names, cons
     return 0;
 }
 
-// ssp_weights (ntfull x n) at each model's logzsol -> weights over ages and metallicities: the two bracketing
-// metallicities at (1 - dz) and dz (metallicity_interval, src/physics/opensps_csp_batch.f90:2071-2085; linear in the
-// spectra as compute_interpolated_ssp, not clamped).
-void blend_weights(const Context &c, int n, const double *w, const std::vector<double> &rows, std::vector<double> &wz) {
-    const int nt = c.nt, nz = c.nz;
-    wz.assign((size_t)n * nt * nz, 0.0);
-    std::vector<double> lz(nz);
-    for (int z = 0; z < nz; ++z) lz[z] = std::log10(c.zlegend[z] / c.zsol);
-    for (int m = 0; m < n; ++m) {
-        const double x = rows[(size_t)PF_COUNT * m + PF_LOGZSOL];
-        int zlo = 0;
-        // find_interval clamped to 1..nz-1 (1-based)
-        int lower = 0, upper = nz + 1;
-        while (upper - lower > 1) { const int mid = (upper + lower) / 2; if (x >= lz[mid - 1]) lower = mid; else upper = mid; }
-        int idx = lower;
-        if (x == lz[0]) idx = 1; else if (x == lz[nz - 1]) idx = nz - 1;
-        zlo = std::max(1, std::min(idx, nz - 1)) - 1;
-        const double dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
-        double *o = wz.data() + (size_t)m * nt * nz;
-        for (int t = 0; t < nt; ++t) {
-            o[t + (size_t)nt * zlo] = (1.0 - dz) * w[(size_t)nt * m + t];
-            o[t + (size_t)nt * (zlo + 1)] = dz * w[(size_t)nt * m + t];
-        }
-    }
-}
-
 // The common body of the batch entry points.
 void batch_entry(int handle, int n, int n_params, const char *const *names, const double *const *values,
                  const double *ssp_weights, const double *ssp_weights_z, const double *zred_mags,
@@ -120,64 +94,40 @@ void batch_entry(int handle, int n, int n_params, const char *const *names, cons
     std::vector<double> rows;
     int st = build_params(*c, n, n_params, names, values, rows, err);
     if (st) return fail(status, st, err);
-    std::vector<double> wz_blend;
-    const double *wz = ssp_weights_z;
-    if (!wz) {
-        if (!ssp_weights)
-            return fail(status, ST_UNSUPPORTED, "SFH parameters without a weight matrix are not supported on this path");
-        blend_weights(*c, n, ssp_weights, rows, wz_blend);
-        wz = wz_blend.data();
+    // weights: the caller's over ages and metallicities, or over ages (blended at logzsol on the device), or the
+    // SFH's (formed on the device, then blended)
+    std::vector<double> sfhp;
+    if (!ssp_weights_z) {
+        if (!ssp_weights) {
+            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4)
+                return fail(status, ST_UNSUPPORTED, "sfh = " + std::to_string(c->sfh) +
+                                                        ": only 0 (SSP), 1 (tau) and 4 (delayed tau) on this path");
+            for (int m = 0; m < n; ++m)
+                if (!(rows[(size_t)PF_COUNT * m + PF_TAGE] > 0.0))
+                    return fail(status, ST_UNSUPPORTED, "models with tage <= 0 are not supported");
+        }
+        sfhp.resize((size_t)SFH_NCOL * n);
+        const int ids[SFH_NCOL] = {PF_TAGE, PF_TAU, PF_CONST, PF_FBURST, PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_LOGZSOL};
+        for (int m = 0; m < n; ++m)
+            for (int k = 0; k < SFH_NCOL; ++k) sfhp[(size_t)SFH_NCOL * m + k] = rows[(size_t)PF_COUNT * m + ids[k]];
     }
     if (emlines) std::fill(emlines, emlines + (size_t)c->nline * n, 0.0);
     BatchIO io;
-    io.n = n; io.params = rows.data(); io.wz = wz;
+    io.n = n; io.params = rows.data(); io.wz = ssp_weights_z;
+    if (!ssp_weights_z) { io.sfh_par = sfhp.data(); io.given_w = ssp_weights; io.sfh_type = c->sfh; }
     io.mags = mags; io.spec = spec; io.mass = mass; io.lbol = lbol; io.emlines = emlines; io.sfr = sfr;
     io.mdust = mdust; io.young = young; io.old = old; io.mass_young = mass_young; io.mass_old = mass_old;
     io.lbol_young = lbol_young; io.lbol_old = lbol_old;
     const bool grad = mags_bar || spec_bar || mass_bar || lbol_bar || params_bar || weights_bar || weights_z_bar;
     if (grad) {
-        // (with ssp_weights the metallicity blend at logzsol would add logzsol's row and weights_bar's chain rule)
-        if (!ssp_weights_z)
-            return fail(status, ST_UNSUPPORTED, "gradients need ssp_weights_z on this path (ssp_weights is forward only)");
+        // weights over ages and metallicities: weights_bar is zero (the reference's wbl with weights_over_z)
+        if (ssp_weights_z && weights_bar) std::fill(weights_bar, weights_bar + (size_t)c->nt * n, 0.0);
         st = run_grad_batch(*c, io, mags_bar, spec_bar, mass_bar, lbol_bar, params_bar, params_bar_rows,
-                            weights_z_bar, err);
-        if (weights_bar) std::fill(weights_bar, weights_bar + (size_t)c->nt * n, 0.0);
+                            ssp_weights_z ? weights_z_bar : nullptr, ssp_weights_z ? nullptr : weights_bar, err);
     } else {
         st = run_batch(*c, io, err);
     }
     if (st) return fail(status, st, err);
-    if (!ssp_weights_z && (lbol || lbol_young || lbol_old)) {
-        // With one weight per age blended at logzsol, L_bol follows the SSP's own interpolation: log L_bol is blended
-        // between the bracketing metallicities, then exponentiated (model_sums MSUMS_BLEND,
-        // src/physics/opensps_csp_batch.f90:2129-2176), which is not the sum over the two slabs' linear L_bol.
-        const int nt = c->nt, nz = c->nz;
-        std::vector<double> lz(nz);
-        for (int z = 0; z < nz; ++z) lz[z] = std::log10(c->zlegend[z] / c->zsol);
-        for (int m = 0; m < n; ++m) {
-            const double x = rows[(size_t)PF_COUNT * m + PF_LOGZSOL];
-            int lower = 0, upper = nz + 1;
-            while (upper - lower > 1) { const int mid = (upper + lower) / 2; if (x >= lz[mid - 1]) lower = mid; else upper = mid; }
-            int idx = lower;
-            if (x == lz[0]) idx = 1; else if (x == lz[nz - 1]) idx = nz - 1;
-            const int zlo = std::max(1, std::min(idx, nz - 1)) - 1;
-            const double dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
-            const double dla = rows[(size_t)PF_COUNT * m + PF_DUST_TESC] > SAFE_FLOOR ? rows[(size_t)PF_COUNT * m + PF_DUST_TESC] : 7.0;
-            int it = 0;
-            while (it < nt && c->log_age[it] <= dla) ++it;   // ages <= dust_tesc
-            it = std::max(1, std::min(it, nt));
-            double ls = 0.0, ly = 0.0, lo = 0.0;
-            for (int t = 0; t < nt; ++t) {
-                const double w = ssp_weights[(size_t)nt * m + t];
-                if (!(w > SAFE_FLOOR)) continue;
-                const double lk = w * std::pow(10.0, (1.0 - dz) * c->lbol[t + (size_t)nt * zlo] + dz * c->lbol[t + (size_t)nt * (zlo + 1)]);
-                ls += lk;
-                if (t + 1 <= it) ly += lk; else lo += lk;
-            }
-            if (lbol) lbol[m] = ls > SAFE_FLOOR ? std::log10(ls) : 0.0;
-            if (lbol_young) lbol_young[m] = std::log10(std::max(ly, SAFE_FLOOR));
-            if (lbol_old) lbol_old[m] = std::log10(std::max(lo, SAFE_FLOOR));
-        }
-    }
 }
 
 }  // namespace

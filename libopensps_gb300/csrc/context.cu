@@ -20,8 +20,9 @@ static const ParamInfo PARAMS[] = {
     {"igm_factor", PF_IGM_FACTOR, 1.0}, {"sigma_smooth", PF_SIGMA_SMOOTH, 0.0}, {"dust_tesc", PF_DUST_TESC, 7.0},
     {"logzsol", PF_LOGZSOL, 0.0}, {"tage", PF_TAGE, 0.0}, {"tau", PF_TAU, 1.0},
     {"min_wave_smooth", PF_MIN_WAVE_SMOOTH, 1.0e3}, {"max_wave_smooth", PF_MAX_WAVE_SMOOTH, 1.0e4},
+    {"const", PF_CONST, 0.0}, {"fburst", PF_FBURST, 0.0}, {"tburst", PF_TBURST, 11.0},
+    {"sf_start", PF_SF_START, 0.0}, {"sf_trunc", PF_SF_TRUNC, 0.0},
     // known to the reference, not varied per model by this path
-    {"const", -1, 0.0}, {"fburst", -1, 0.0}, {"tburst", -1, 11.0}, {"sf_start", -1, 0.0}, {"sf_trunc", -1, 0.0},
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
     {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"imf1", -1, 1.3},
     {"imf2", -1, 2.3}, {"imf3", -1, 2.3}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
@@ -160,6 +161,8 @@ Context::~Context() {
     d_bc.release(); d_bmeta.release(); d_bchunk.release(); d_mags_bar.release(); d_spec_bar.release(); d_mass_bar.release();
     d_lbol_bar.release(); d_cscale.release(); d_pbar.release(); d_wzbar.release(); d_ybh.release(); d_ybl.release();
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
+    d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
+    d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
@@ -418,6 +421,8 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     c.igm_a = igm_a;
     std::vector<double> lnlam(ns);
     for (int j = 0; j < ns; ++j) lnlam[j] = std::log(c.lam[j]);
+    std::vector<double> lzv(c.nz);
+    for (int z = 0; z < c.nz; ++z) lzv[z] = std::log10(c.zlegend[z] / c.zsol);
     cosmology_table(c.h0, c.om0, c.ol0, c.zt, c.dl);
     if ((e = upload(c.d_wl, wl.data(), wl.size())) != cudaSuccess ||
         (e = upload(c.d_igm_a, igm_a.data(), igm_a.size())) != cudaSuccess ||
@@ -425,6 +430,9 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         (e = upload(c.d_lnlam, lnlam.data(), lnlam.size())) != cudaSuccess ||
         (e = upload(c.d_mass, c.mass.data(), c.mass.size())) != cudaSuccess ||
         (e = upload(c.d_llin, c.llin.data(), c.llin.size())) != cudaSuccess ||
+        (e = upload(c.d_logage, c.log_age.data(), c.log_age.size())) != cudaSuccess ||
+        (e = upload(c.d_lz, lzv.data(), lzv.size())) != cudaSuccess ||
+        (e = upload(c.d_lbol, c.lbol.data(), c.lbol.size())) != cudaSuccess ||
         (e = upload(c.d_zt, c.zt.data(), c.zt.size())) != cudaSuccess ||
         (e = upload(c.d_dl, c.dl.data(), c.dl.size())) != cudaSuccess ||
         (e = c.d_status.reserve(4)) != cudaSuccess) {

@@ -22,7 +22,8 @@ enum ParamId {
     PF_DUST1 = 0, PF_DUST2, PF_DUST3, PF_DUST_INDEX, PF_DUST1_INDEX, PF_FRAC_NODUST, PF_FRAC_OBRUN, PF_ZRED,
     PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC,
     PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
-    PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH,
+    PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
+    PF_TBURST, PF_SF_START, PF_SF_TRUNC,
     PF_COUNT
 };
 
@@ -124,6 +125,10 @@ struct Context {
     DevBuf<double> d_mags_bar, d_spec_bar, d_mass_bar, d_lbol_bar, d_cscale, d_pbar, d_wzbar;
     DevBuf<__nv_bfloat16> d_ybh, d_ybl, d_obh, d_obl;
     DevBuf<float> d_wzb32, d_apar;
+    // SFH weights: grid tables, per-model parameters, weights over ages, log-blended L_bol, SFR; reverse-pass scratch
+    DevBuf<double> d_logage, d_lz, d_lbol;
+    DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
+    DevBuf<unsigned char> d_dual;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch
@@ -165,6 +170,11 @@ struct BatchIO {
     bool dev_sync = true;            // dev_inputs: wait for the batch before returning
     double *fband_dev = nullptr;     // device n x nbands band fluxes (the reverse pass), or null
     bool keep_parts = false;         // the reverse pass: the young and old sums kept on the device (d_young, d_old)
+    // weights formed on the device (wz unused): per-model SFH columns (SFH_NCOL x n, host) with the SFH type, or the
+    // caller's weights over ages (nt x n, host) blended at logzsol
+    const double *sfh_par = nullptr;
+    const double *given_w = nullptr;
+    int sfh_type = 0;
     // outputs (host, may be null)
     double *mags = nullptr, *spec = nullptr, *mass = nullptr, *lbol = nullptr, *emlines = nullptr;
     double *young = nullptr, *old = nullptr, *mass_young = nullptr, *mass_old = nullptr, *lbol_young = nullptr,

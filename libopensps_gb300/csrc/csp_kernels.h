@@ -185,6 +185,38 @@ struct AdjointArgs {
 };
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 
+// SFH weights (sfh.cu). Per-model FP64 columns: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr), logzsol.
+enum { SFH_TAGE = 0, SFH_TAU, SFH_CONST, SFH_FBURST, SFH_TBURST, SFH_SF_START, SFH_SF_TRUNC, SFH_NPAR = 7,
+       SFH_LOGZSOL = 7, SFH_NCOL = 8 };
+// their params_bar rows (opensps.h)
+enum { PB_LOGZSOL = 15, PB_TAGE = 16, PB_TAU = 17, PB_CONST = 18, PB_FBURST = 19, PB_TBURST = 20, PB_SF_START = 21,
+       PB_SF_TRUNC = 24 };
+struct SfhArgs {
+    int n, nt, nz, sfh, itesc;
+    const double *tf;        // nt: log10(age / yr) of the grid
+    const double *lz;        // nz: log10(Z / Zsun)
+    const double *lbol;      // nz x nt: log10 L_bol of the SSPs (age fastest)
+    const double *par;       // n x SFH_NCOL
+    const double *given;     // n x nt weights over ages given by the caller, or null: the SFH's
+    double *w;               // n x nt: the weights over ages
+    double *scratch;         // n x 2 nt
+    double *wz;              // n x nt x nz: the weights over ages and metallicities
+    double *lblend;          // n x 3: log-blended L_bol (total, young, old)
+    double *sfr;             // n, or null
+};
+cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st);
+struct SfhRevArgs {
+    int n, nt, nz, sfh, rows, has_logzsol, sfh_tangents;
+    const double *tf, *lz, *lbol, *par, *w, *lblend, *lbol_bar;
+    const double *wzb;       // n x nt x nz: dL / dwz without the L_bol term
+    double *weights_bar;     // n x nt, or null
+    double *scratch;         // n x nt
+    double *params_bar;      // n x rows
+    void *dual;              // n x 3 nt dual numbers (sfh_dual_bytes() each)
+};
+cudaError_t run_sfh_reverse(const SfhRevArgs &a, cudaStream_t st);
+size_t sfh_dual_bytes();
+
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);
 

@@ -1,0 +1,420 @@
+// SFH weights on the device, one thread per model in FP64 (OpenSPS batch_sfh_weights → sfh_weights_core,
+// src/physics/opensps_csp_batch.f90:1865-1917, src/physics/opensps_sfh.f90:1077-1160, compute_ssp_weights :97-257):
+// the mass formed against the hat kernel of each grid age for SFH types 0 (SSP), 1 (tau) and 4 (delayed tau), with
+// the constant and burst components, normalised to one solar mass formed. Then the models' metallicity blend at
+// logzsol into the weights over ages and metallicities, the log-blended L_bol (model_sums MSUMS_BLEND :2129-2176) and
+// the current SFR (get_sfh_properties_at_age :281-486 over the mass fraction, batch_model_indices :1558-1567).
+//
+// The weights are written once as templates over the scalar type: double for the forward, Dual (value and seven
+// derivatives: tage, tau, const, fburst, tburst, sf_start, sf_trunc) for the tangents of the reverse pass
+// (sfh_weights_tangent, src/physics/opensps_sfh_tangent.f90:61-198, forward mode; d Ei(x)/dx = e^x / x).
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cfloat>
+#include "context.h"
+
+namespace sps {
+
+constexpr double SFH_LOG_E = 0.43429448190325182765;   // log10(e)
+constexpr double SFH_LN10 = 2.302585092994045684;
+constexpr double SFH_EULER_GAMMA = 0.57721566490153286060651209008240243104215933593992;
+
+// ---------------------------------------------------------------------------------------------- dual numbers
+struct Dual {
+    double v;
+    double d[SFH_NPAR];
+};
+__device__ __forceinline__ Dual dconst(double v) {
+    Dual r;
+    r.v = v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = 0.0;
+    return r;
+}
+__device__ __forceinline__ Dual operator+(const Dual &a, const Dual &b) {
+    Dual r; r.v = a.v + b.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual operator-(const Dual &a, const Dual &b) {
+    Dual r; r.v = a.v - b.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual operator-(const Dual &a) {
+    Dual r; r.v = -a.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual operator*(const Dual &a, const Dual &b) {
+    Dual r; r.v = a.v * b.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual operator/(const Dual &a, const Dual &b) {
+    Dual r; r.v = a.v / b.v;
+    const double ib = 1.0 / b.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+    return r;
+}
+__device__ __forceinline__ Dual operator+(const Dual &a, double b) { Dual r = a; r.v += b; return r; }
+__device__ __forceinline__ Dual operator+(double b, const Dual &a) { return a + b; }
+__device__ __forceinline__ Dual operator-(const Dual &a, double b) { Dual r = a; r.v -= b; return r; }
+__device__ __forceinline__ Dual operator-(double b, const Dual &a) { return -a + b; }
+__device__ __forceinline__ Dual operator*(const Dual &a, double b) {
+    Dual r; r.v = a.v * b;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = a.d[i] * b;
+    return r;
+}
+__device__ __forceinline__ Dual operator*(double b, const Dual &a) { return a * b; }
+__device__ __forceinline__ Dual operator/(const Dual &a, double b) { return a * (1.0 / b); }
+
+__device__ __forceinline__ double val(double x) { return x; }
+__device__ __forceinline__ double val(const Dual &x) { return x.v; }
+template <class T> __device__ __forceinline__ T lift(double v);
+template <> __device__ __forceinline__ double lift<double>(double v) { return v; }
+template <> __device__ __forceinline__ Dual lift<Dual>(double v) { return dconst(v); }
+
+// a smooth function f applied to x, with its derivative df at x
+__device__ __forceinline__ double chain(double, double f, double) { return f; }
+__device__ __forceinline__ Dual chain(const Dual &x, double f, double df) {
+    Dual r; r.v = f;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = df * x.d[i];
+    return r;
+}
+template <class T> __device__ __forceinline__ T sexp(const T &x) { const double e = exp(val(x)); return chain(x, e, e); }
+template <class T> __device__ __forceinline__ T spow10(const T &x) {
+    const double e = pow(10.0, val(x));
+    return chain(x, e, e * SFH_LN10);
+}
+template <class T> __device__ __forceinline__ T slog10(const T &x) {
+    return chain(x, log10(val(x)), 1.0 / (val(x) * SFH_LN10));
+}
+template <class T> __device__ __forceinline__ T smax(const T &a, const T &b) { return val(a) >= val(b) ? a : b; }
+template <class T> __device__ __forceinline__ T smin(const T &a, const T &b) { return val(a) <= val(b) ? a : b; }
+
+// Ei(x) (expi, src/math/opensps_special_functions.f90:62-122): the power series about 0 for x <= 40, the
+// asymptotic series (20 terms) beyond; d Ei / dx = e^x / x.
+__device__ double expi_d(double x) {
+    if (x == 0.0) return -INFINITY;
+    if (x < 0.0) return NAN;
+    if (fabs(x) <= 40.0) {
+        double res = 1.0, r = 1.0;
+        for (int k = 1; k <= 1000; ++k) {
+            const double dd = (double)k + 1.0;
+            r = (r * (double)k * x) / (dd * dd);
+            res += r;
+            if (fabs(r) <= 1.0e-20 * fabs(res)) break;
+            if (k == 1000) return NAN;
+        }
+        return SFH_EULER_GAMMA + log(x) + x * res;
+    }
+    double res = 1.0, r = 1.0;
+    const double inv = 1.0 / x;
+    for (int k = 1; k <= 20; ++k) {
+        r *= (double)k * inv;
+        res += r;
+    }
+    return exp(x) * inv * res;
+}
+template <class T> __device__ __forceinline__ T sexpi(const T &x, bool &finite) {
+    const double e = expi_d(val(x));
+    finite = isfinite(e);
+    return chain(x, finite ? e : 0.0, finite ? exp(val(x)) / val(x) : 0.0);
+}
+
+// ---------------------------------------------------------------------------------------------- the weights
+template <class T>
+struct SfhT {
+    int type;         // -1 burst, 0 constant, 1 tau, 4 delayed tau
+    T tage, tau, tb, tq;
+};
+
+// eval_indefinite_moments_log (src/physics/opensps_sfh.f90:852-905): M0 = int SFR dt, M1 = int SFR log10(t) dt
+template <class T>
+__device__ void moments_log(const T &log_t, const SfhT<T> &s, T &m0, T &m1) {
+    const T t = spow10(log_t);
+    if (s.type == 0) {
+        m0 = t;
+        m1 = t * (log_t - SFH_LOG_E);
+        return;
+    }
+    if (s.type == 1 || s.type == 4) {
+        if (val(s.tau) <= SAFE_FLOOR) { m0 = lift<T>(0.0); m1 = lift<T>(0.0); return; }
+        const T tt = smax(t / s.tau, lift<T>(SAFE_FLOOR));
+        bool fin;
+        const T ei = sexpi(tt, fin);
+        const T e = sexp(tt);
+        if (s.type == 1) {
+            m0 = e;
+            m1 = log_t * m0 - SFH_LOG_E * ei;
+        } else {
+            const T a = t - s.tage - s.tau;
+            m0 = -(a * e);
+            m1 = -((a * log_t - s.tau * SFH_LOG_E) * e) - (s.tage + s.tau) * SFH_LOG_E * ei;
+        }
+        return;
+    }
+    m0 = lift<T>(0.0);
+    m1 = lift<T>(0.0);
+}
+
+// compute_ssp_weights (src/physics/opensps_sfh.f90:97-257) with log-age interpolation: w (nt, strided) += the hat
+// kernel masses; idx_min / idx_max 1-based as the reference's. w must start at zero.
+template <class T>
+__device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_min, int idx_max, T *w, int ws) {
+    const double tiny_logt = 0.0;
+    if (s.type == -1) {
+        if (val(s.tb) < 0.0) return;
+        const T log_tb = slog10(smax(s.tb, lift<T>(pow(10.0, tiny_logt))));
+        if (val(log_tb) <= tf[0]) { w[0] = w[0] + 1.0; return; }
+        int j = find_interval0(tf, nt, val(log_tb)) + 1;
+        j = j < 1 ? 1 : (j > nt - 1 ? nt - 1 : j);
+        const double dt = tf[j] - tf[j - 1];
+        w[(j - 1) * ws] = w[(j - 1) * ws] + (tf[j] - log_tb) / dt;
+        w[j * ws] = w[j * ws] + (log_tb - tf[j - 1]) / dt;
+        return;
+    }
+    const T lmin = lift<T>(pow(10.0, tiny_logt));
+    const T lts = slog10(smax(s.tq, lmin)), lte = slog10(smax(s.tage, lmin));
+    int js = find_interval0(tf, nt, val(lts)) + 1;
+    int je = find_interval0(tf, nt, val(lte)) + 2;
+    const int lo_bound = idx_min > 1 ? idx_min : 1, hi_bound = idx_max < nt - 1 ? idx_max : nt - 1;
+    if (js < lo_bound) js = lo_bound;
+    if (je > hi_bound) je = hi_bound;
+    T lim_prev = smin(smax(lift<T>(tf[js - 1]), lts), lte);
+    T m0p, m1p;
+    moments_log(lim_prev, s, m0p, m1p);
+    for (int j = js; j <= je; ++j) {
+        const T lim2 = smin(smax(lift<T>(tf[j]), lts), lte);
+        if (val(lim2) <= val(lim_prev)) { lim_prev = lim2; continue; }
+        T m0c, m1c;
+        moments_log(lim2, s, m0c, m1c);
+        const T m0 = m0c - m0p, m1 = m1c - m1p;
+        m0p = m0c;
+        m1p = m1c;
+        const double lo = tf[j - 1], hi = tf[j], inv = 1.0 / (hi - lo);
+        w[(j - 1) * ws] = w[(j - 1) * ws] + (hi * m0 - m1) * inv;
+        w[j * ws] = w[j * ws] + (m1 - lo * m0) * inv;
+        lim_prev = lim2;
+    }
+    if (idx_min == 0) {
+        const T l1 = smin(smax(lift<T>(tiny_logt), lts), lte), l2 = smin(smax(lift<T>(tf[0]), lts), lte);
+        if (val(l1) < val(l2)) {
+            T a0, a1, b0, b1;
+            moments_log(l2, s, a0, a1);
+            moments_log(l1, s, b0, b1);
+            w[0] = w[0] + (a0 - b0);
+        }
+    }
+}
+
+// sfh_weights_core_pc for one metallicity (src/physics/opensps_sfh.f90:1077-1160; convert_sfhparams_pc :1306-1360).
+// p: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr). w, t1, t2: nt entries at stride ws, zeroed here.
+template <class T>
+__device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, T *w, T *t1, T *t2, int ws) {
+    for (int i = 0; i < nt; ++i) { w[i * ws] = lift<T>(0.0); t1[i * ws] = lift<T>(0.0); t2[i * ws] = lift<T>(0.0); }
+    SfhT<T> s;
+    const T start = (sfh == 1 || sfh == 4) ? p[SFH_SF_START] * 1.0e9 : lift<T>(0.0);
+    s.tage = p[SFH_TAGE] * 1.0e9 - start;
+    const T tburst = p[SFH_TBURST] * 1.0e9 - start;
+    const T trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
+    s.tau = p[SFH_TAU] * 1.0e9;
+    s.tb = s.tage - tburst;
+    s.tq = (val(trunc) <= 0.0 || val(trunc) > val(s.tage)) ? lift<T>(0.0) : s.tage - trunc;
+    int imax = find_interval0(tf, nt, log10(val(s.tage))) + 1 + 2;
+    imax = imax < 1 ? 1 : (imax > nt ? nt : imax);
+    if (sfh == 0) {
+        s.type = -1;
+        s.tb = s.tage;
+        ssp_weights(tf, nt, s, imax - 2 > 1 ? imax - 2 : 1, imax, w, ws);
+        return;
+    }
+    s.type = sfh;
+    ssp_weights(tf, nt, s, 0, imax, w, ws);
+    T mass1 = lift<T>(0.0);
+    for (int i = 0; i < imax; ++i) mass1 = mass1 + w[i * ws];
+    if (val(mass1) < SAFE_FLOOR) mass1 = lift<T>(1.0);
+    for (int i = 0; i < nt; ++i) w[i * ws] = w[i * ws] / mass1;
+    const T cst = p[SFH_CONST], fb_in = p[SFH_FBURST];
+    if (val(cst) > 0.0 || val(fb_in) > SAFE_FLOOR) {
+        s.type = 0;
+        ssp_weights(tf, nt, s, 0, imax, t1, ws);
+        T m1 = lift<T>(0.0);
+        for (int i = 0; i < imax; ++i) m1 = m1 + t1[i * ws];
+        if (val(m1) < SAFE_FLOOR) m1 = lift<T>(1.0);
+        T fb = lift<T>(0.0);
+        if (val(s.tb) >= 0.0) {
+            s.type = -1;
+            ssp_weights(tf, nt, s, 0, imax, t2, ws);
+            fb = fb_in;
+        }
+        for (int i = 0; i < nt; ++i)
+            w[i * ws] = (1.0 - cst - fb) * w[i * ws] + cst * (t1[i * ws] / m1) + fb * t2[i * ws];
+    }
+}
+
+// The current SFR per unit mass formed over the mass fraction formed by tage (per yr), sfh 0, 1, 4.
+__device__ double sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
+    double mass_frac = 1.0, sfr = 0.0;
+    if (sfh == 1 || sfh == 4) {
+        const double tage = p[SFH_TAGE], tau = p[SFH_TAU], cst = p[SFH_CONST], fburst = p[SFH_FBURST];
+        const double tburst = p[SFH_TBURST], start = p[SFH_SF_START], trunc = p[SFH_SF_TRUNC];
+        const double t_max = pow(10.0, tf[nt - 1] - 9.0) - start;
+        const double t_prime = tage - start;
+        const double t_trunc = (trunc < SAFE_FLOOR || trunc < start) ? t_max : trunc - start;
+        const double tau_g = fmax(tau, SAFE_FLOOR);
+        const bool one = sfh == 1;
+        const double rt = fmin(t_max, t_trunc) / tau_g;
+        const double total = tau_g * (one ? -expm1(-rt) : -expm1(-rt) - rt * exp(-rt));
+        double mass_tau = 0.0, sfr_tau = 0.0;
+        if (t_prime >= 0.0) {
+            const double r = fmin(t_prime, t_trunc) / tau_g;
+            mass_tau = tau_g * (one ? -expm1(-r) : -expm1(-r) - r * exp(-r));
+            sfr_tau = (one ? 1.0 : r) * exp(-r);
+        }
+        const double mfrac_burst = (t_prime > tburst - start) ? 1.0 : 0.0;
+        double sfr_const = 0.0, mass_const = 0.0;
+        if (t_prime > 0.0) {
+            sfr_const = 1.0 / fmin(t_max, t_trunc);
+            mass_const = fmax(fmin(t_prime, t_trunc), 0.0) * sfr_const;
+        }
+        const double norm = 1.0 - cst - fburst;
+        mass_frac = norm * mass_tau / total + cst * mass_const + fburst * mfrac_burst;
+        sfr = (t_prime > t_trunc) ? 0.0 : norm * sfr_tau / total + cst * sfr_const;
+    }
+    sfr /= 1.0e9;
+    if (mass_frac > SAFE_FLOOR) sfr /= mass_frac;
+    return sfr;
+}
+
+// The metallicity interval of logzsol: zlo (0-based) and dz, not clamped (metallicity_interval,
+// src/physics/opensps_csp_batch.f90:2071-2085).
+__device__ __forceinline__ void zinterval(const double *lz, int nz, double x, int &zlo, double &dz) {
+    int idx = find_interval0(lz, nz, x) + 1;
+    idx = idx < 1 ? 1 : (idx > nz - 1 ? nz - 1 : idx);
+    zlo = idx - 1;
+    dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
+}
+
+// One thread per model: the weights over ages (w, n x nt), the SFR, the blend over metallicities (wz, n x nt x nz,
+// age fastest: the other slabs are zeroed) and the log-blended L_bol sums (total, young, old).
+__global__ void __launch_bounds__(128) sfh_forward_kernel(SfhArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double *p = a.par + (size_t)SFH_NCOL * m;
+    const int nt = a.nt, nz = a.nz;
+    double *w = a.w + (size_t)nt * m;
+    double *t1 = a.scratch + (size_t)2 * nt * m, *t2 = t1 + nt;
+    if (a.given == nullptr) {
+        sfh_weights_core<double>(a.tf, nt, a.sfh, p, w, t1, t2, 1);
+        if (a.sfr) a.sfr[m] = sfh_sfr(a.tf, nt, a.sfh, p);
+    } else {
+        for (int i = 0; i < nt; ++i) w[i] = a.given[(size_t)nt * m + i];
+        if (a.sfr) a.sfr[m] = NAN;
+    }
+    int zlo;
+    double dz;
+    zinterval(a.lz, nz, p[SFH_LOGZSOL], zlo, dz);
+    double *wz = a.wz + (size_t)nt * nz * m;
+    double ls = 0.0, ly = 0.0, lo = 0.0;
+    for (int z = 0; z < nz; ++z)
+        for (int t = 0; t < nt; ++t) {
+            const double wt = w[t];
+            double v = 0.0;
+            if (z == zlo) v = (1.0 - dz) * wt;
+            else if (z == zlo + 1) v = dz * wt;
+            wz[t + (size_t)nt * z] = v;
+        }
+    // log L_bol blended between the slabs, then exponentiated (the SSP's own interpolation); ages <= dust_tesc young
+    for (int t = 0; t < nt; ++t) {
+        const double wt = w[t];
+        if (!(wt > SAFE_FLOOR)) continue;
+        const double lk = wt * pow(10.0, (1.0 - dz) * a.lbol[t + (size_t)nt * zlo] + dz * a.lbol[t + (size_t)nt * (zlo + 1)]);
+        ls += lk;
+        if (t < a.itesc) ly += lk; else lo += lk;
+    }
+    a.lblend[3 * m] = ls;
+    a.lblend[3 * m + 1] = ly;
+    a.lblend[3 * m + 2] = lo;
+}
+
+cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    sfh_forward_kernel<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------- reverse pass
+// One thread per model: dL / dw_t = (1 - dz) wzb(t, zlo) + dz wzb(t, zlo + 1) + lbol_bar L~_t / (ln 10 L~) (wzb
+// without the linear L_bol term; L~ the log-blended L_bol), the weights' cotangent (weights_bar); the SFH
+// parameters' rows sum_t dL/dw_t dw_t/dtheta with the tangents of the weights (batch_sfh_gradients,
+// src/physics/opensps_csp_batch.f90:5198-5218); logzsol's row through dz (dchain(7) = 1 / (lz(zlo+1) - lz(zlo))).
+__global__ void __launch_bounds__(64) sfh_reverse_kernel(SfhRevArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const int nt = a.nt, nz = a.nz;
+    const double *p = a.par + (size_t)SFH_NCOL * m;
+    const double *w = a.w + (size_t)nt * m;
+    const double *wzb = a.wzb + (size_t)nt * nz * m;
+    int zlo;
+    double dz;
+    zinterval(a.lz, nz, p[SFH_LOGZSOL], zlo, dz);
+    const double ls = a.lblend[3 * m];
+    const double lbar = (a.lbol_bar && ls > SAFE_FLOOR) ? a.lbol_bar[m] / (ls * SFH_LN10) : 0.0;
+    double gz = 0.0;   // dL / d dz
+    double *wb = a.weights_bar ? a.weights_bar + (size_t)nt * m : nullptr;
+    for (int t = 0; t < nt; ++t) {
+        const double b0 = wzb[t + (size_t)nt * zlo], b1 = wzb[t + (size_t)nt * (zlo + 1)];
+        double g = (1.0 - dz) * b0 + dz * b1;
+        gz += w[t] * (b1 - b0);
+        if (lbar != 0.0 && w[t] > SAFE_FLOOR) {
+            const double l0 = a.lbol[t + (size_t)nt * zlo], l1 = a.lbol[t + (size_t)nt * (zlo + 1)];
+            const double lt = pow(10.0, (1.0 - dz) * l0 + dz * l1);
+            g += lbar * lt;
+            gz += lbar * w[t] * lt * SFH_LN10 * (l1 - l0);
+        }
+        if (wb) wb[t] = g;
+        a.scratch[(size_t)nt * m + t] = g;
+    }
+    double *pb = a.params_bar + (size_t)a.rows * m;
+    pb[PB_LOGZSOL] = a.has_logzsol ? gz / (a.lz[zlo + 1] - a.lz[zlo]) : 0.0;
+    if (!a.sfh_tangents) return;
+    // the tangents of the weights (all seven directions in one pass)
+    Dual pd[SFH_NPAR];
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) {
+        pd[i] = dconst(p[i]);
+        pd[i].d[i] = 1.0;
+    }
+    Dual *dw = reinterpret_cast<Dual *>(a.dual) + (size_t)3 * nt * m;
+    sfh_weights_core<Dual>(a.tf, nt, a.sfh, pd, dw, dw + nt, dw + 2 * nt, 1);
+    double acc[SFH_NPAR];
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) acc[i] = 0.0;
+    for (int t = 0; t < nt; ++t) {
+        const double g = a.scratch[(size_t)nt * m + t];
+#pragma unroll
+        for (int i = 0; i < SFH_NPAR; ++i) acc[i] += g * dw[t].d[i];
+    }
+    const int row[SFH_NPAR] = {PB_TAGE, PB_TAU, PB_CONST, PB_FBURST, PB_TBURST, PB_SF_START, PB_SF_TRUNC};
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) pb[row[i]] = acc[i];
+}
+
+cudaError_t run_sfh_reverse(const SfhRevArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    sfh_reverse_kernel<<<(a.n + 63) / 64, 64, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+size_t sfh_dual_bytes() { return sizeof(Dual); }
+
+}  // namespace sps

@@ -23,7 +23,8 @@ _dp = C.POINTER(C.c_double)
 
 
 def build() -> Path:
-    if not LIB.exists() or LIB.stat().st_mtime < (HERE / "opensps_oracle.c").stat().st_mtime:
+    srcs = [HERE / "opensps_oracle.c", HERE / "sfh_oracle.c"]
+    if not LIB.exists() or any(LIB.stat().st_mtime < s.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
 
@@ -56,12 +57,37 @@ def lib() -> C.CDLL:
                                              C.POINTER(C.c_int), _dp, C.c_int]
         _lib.oracle_csp_batch.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _dp] + [_dp] * 8
         _lib.oracle_npar.restype = C.c_int
+        _lib.oracle_expi.restype = C.c_double
+        _lib.oracle_expi.argtypes = [C.c_double]
+        _lib.oracle_sfh_batch.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
         _lib.oracle_abs_mag_zeropoint_log.restype = C.c_double
     return _lib
 
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(_dp)
+
+
+SFH_NAMES = ("tage", "tau", "const", "fburst", "tburst", "sf_start", "sf_trunc")
+SFH_DEFAULTS = {"tage": 0.0, "tau": 1.0, "const": 0.0, "fburst": 0.0, "tburst": 11.0, "sf_start": 0.0,
+                "sf_trunc": 0.0}
+
+
+def sfh_weights(log_age: np.ndarray, sfh: int, params: dict, n: int):
+    """The SFH weights over the ages (n, nt) and the current SFR per unit mass formed (n,) of SFH type sfh (0, 1, 4)
+    for per-model parameters (sfh_oracle.c)."""
+    tf = np.ascontiguousarray(log_age, dtype=np.float64)
+    p = np.empty((n, len(SFH_NAMES)))
+    for i, k in enumerate(SFH_NAMES):
+        p[:, i] = np.broadcast_to(np.asarray(params.get(k, SFH_DEFAULTS[k]), dtype=np.float64), (n,))
+    w = np.empty((n, tf.size))
+    sfr = np.empty(n)
+    lib().oracle_sfh_batch(_p(tf), tf.size, int(sfh), n, _p(p), _p(w), _p(sfr))
+    return w, sfr
+
+
+def expi(x: float) -> float:
+    return lib().oracle_expi(float(x))
 
 
 class Oracle:

@@ -57,3 +57,38 @@ def rel_err_spec(got: np.ndarray, ref: np.ndarray, floor: float = 1e-6) -> float
     mask = np.abs(ref) >= floor * peak
     err = np.abs(got - ref) / np.where(mask, np.abs(ref), 1.0)
     return float(np.max(np.where(mask, err, 0.0)))
+
+
+def blend_at_logzsol(data, w, logzsol):
+    """Weights over ages (n, nt) blended between the two metallicities bracketing logzsol (not clamped), and the
+    log-blended L_bol (total, young ages <= 7.0 dex, old) of the model_sums MSUMS_BLEND form."""
+    n, nt = w.shape
+    lz = np.log10(data["zlegend"] / 0.0142)
+    nz = lz.size
+    wz = np.zeros((n, nz, nt))
+    lb = np.zeros((n, 3))
+    young = data["log_age"] <= 7.0
+    for m in range(n):
+        zlo = min(max(np.searchsorted(lz, logzsol[m], side="right") - 1, 0), nz - 2)
+        dz = (logzsol[m] - lz[zlo]) / (lz[zlo + 1] - lz[zlo])
+        wz[m, zlo] = (1 - dz) * w[m]
+        wz[m, zlo + 1] = dz * w[m]
+        lk = np.where(w[m] > 0, w[m] * 10.0 ** ((1 - dz) * data["ssp_lbol"][zlo] + dz * data["ssp_lbol"][zlo + 1]), 0.0)
+        lb[m] = [lk.sum(), lk[young].sum(), lk[~young].sum()]
+    return wz, lb
+
+
+def oracle_sfh_csp(oracle, data, sfh, params):
+    """The oracle's batch for SFH parameters: its SFH weights, blended at logzsol, through its CSP; L_bol
+    log-blended; the SFR per unit mass formed."""
+    from oracle.oracle import SFH_NAMES, sfh_weights
+    n = len(np.atleast_1d(params["tage"]))
+    w, sfr = sfh_weights(data["log_age"], sfh, params, n)
+    logzsol = np.broadcast_to(np.asarray(params.get("logzsol", 0.0), dtype=np.float64), (n,))
+    wz, lb = blend_at_logzsol(data, w, logzsol)
+    out = oracle.csp_batch({k: v for k, v in params.items() if k not in SFH_NAMES and k != "logzsol"}, wz)
+    out["lbol"] = np.log10(lb[:, 0])
+    out["sfr"] = sfr
+    out["w"] = w
+    out["wz"] = wz
+    return out

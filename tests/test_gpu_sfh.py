@@ -1,0 +1,96 @@
+"""SFH weights formed on the device (sfh 0, 1, 4 with the constant and burst components), blended at logzsol,
+through the batch, against the FP64 oracle: spectra <= 1e-4 relative, magnitudes <= 1e-3 mag, mass <= 1e-12
+relative, log L_bol <= 1e-9 relative, the SFR per unit mass formed <= 1e-12 relative.
+
+(L_bol is set by the youngest ages, whose weights are differences of the closed-form moments ~ e^(t/tau) over bins
+short against tau: a 1-ulp difference between the host's and the device's exp / pow grows by ~tau / dt there, up
+to ~1e-10 relative in those weights; the mass is set by the old ages and keeps 1e-12.)"""
+import numpy as np
+import pytest
+
+from conftest import oracle_sfh_csp, rel_err_spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(sfh, nbands=40, neb=False, igm=False):
+    from libopensps_gb300.capi import Context
+    c = Context()
+    c.set_int("sfh", sfh)
+    if neb:
+        c.set_int("add_neb_emission", 1)
+    if igm:
+        c.set_int("add_igm_absorption", 1)
+    if nbands == 20:
+        c.set_filters_library("gauss20")
+    return c
+
+
+def _forward(c, params, n):
+    import ctypes as C
+    from libopensps_gb300 import capi
+    k, names, vals, keep = capi._names_values(params, n)
+    out = {"mags": np.empty((n, c.nbands)), "spec": np.empty((n, c.nspec)), "mass": np.empty(n),
+           "lbol": np.empty(n), "sfr": np.empty(n)}
+    st = C.c_int(0)
+    c.lib.opensps_context_compute_csp_batch(c.handle, n, k, names, vals, None, capi._ptr(out["mags"]),
+                                            capi._ptr(out["spec"]), capi._ptr(out["mass"]), capi._ptr(out["lbol"]),
+                                            None, capi._ptr(out["sfr"]), None, None, C.byref(st))
+    capi._check(st, c.lib)
+    del keep
+    return out
+
+
+def _check(got, ora):
+    assert rel_err_spec(got["spec"], ora["spec"]) <= 1e-4
+    assert np.array_equal(np.isnan(got["mags"]), np.isnan(ora["mags"]))
+    assert float(np.nanmax(np.abs(got["mags"] - ora["mags"]))) <= 1e-3
+    np.testing.assert_allclose(got["mass"], ora["mass"], rtol=1e-12)
+    np.testing.assert_allclose(got["lbol"], ora["lbol"], rtol=1e-9)
+    np.testing.assert_allclose(got["sfr"], ora["sfr"], rtol=1e-12)
+
+
+def test_delayed_tau_plain_config(data, built_lib):
+    """The plain-CSP workload: delayed tau, tau log-uniform 0.1-10 Gyr, age 1-13.7 Gyr, logZ on the grid's range,
+    power-law dust, z = 0, no nebular emission, 20 filters."""
+    from oracle.oracle import Oracle
+    n = 64
+    rng = np.random.default_rng(0)
+    params = {"tau": 10.0 ** rng.uniform(-1.0, 1.0, n), "tage": rng.uniform(1.0, 13.7, n),
+              "logzsol": rng.uniform(-2.0, 0.5, n), "dust2": rng.uniform(0.0, 2.0, n)}
+    c = _ctx(4, nbands=20)
+    got = _forward(c, params, n)
+    _check(got, oracle_sfh_csp(Oracle(data, nbands=20, add_neb=False, add_igm=False), data, 4, params))
+    c.close()
+
+
+@pytest.mark.parametrize("sfh", [0, 1, 4])
+def test_sfh_types_with_constant_and_burst(data, built_lib, sfh):
+    from oracle.oracle import Oracle
+    n = 40
+    rng = np.random.default_rng(10 + sfh)
+    params = {"tau": 10.0 ** rng.uniform(-0.5, 1.0, n), "tage": rng.uniform(0.5, 13.0, n),
+              "logzsol": rng.uniform(-1.5, 0.3, n), "dust2": rng.uniform(0.0, 1.0, n),
+              "zred": rng.uniform(0.1, 3.0, n), "sigma_smooth": rng.uniform(60.0, 250.0, n)}
+    if sfh != 0:
+        params.update({"const": rng.uniform(0.0, 0.3, n), "fburst": rng.uniform(0.0, 0.2, n),
+                       "tburst": rng.uniform(0.2, 10.0, n), "sf_trunc": np.where(rng.uniform(size=n) < 0.5, 0.0,
+                                                                                  rng.uniform(0.5, 12.0, n)),
+                       "sf_start": rng.uniform(0.0, 0.3, n)})
+    c = _ctx(sfh, neb=True, igm=True)
+    got = _forward(c, params, n)
+    _check(got, oracle_sfh_csp(Oracle(data, nbands=40), data, sfh, params))
+    c.close()
+
+
+def test_sfh_rejects_nonpositive_age_and_tabular(data, built_lib):
+    from libopensps_gb300.capi import OpenSPSError
+    c = _ctx(4)
+    with pytest.raises(OpenSPSError) as e:
+        _forward(c, {"tage": np.array([1.0, 0.0]), "tau": np.array([1.0, 1.0])}, 2)
+    assert e.value.status == 2
+    c.set_int("sfh", 3)
+    with pytest.raises(OpenSPSError) as e:
+        _forward(c, {"tage": np.array([1.0]), "tau": np.array([1.0])}, 1)
+    assert e.value.status == 2
+    c.close()
