@@ -167,6 +167,20 @@ static inline void opensps_context_compute_csp_batch_ext(int handle, const opens
         status);
 }
 
+/* SSP operators (opensps.h:424-455): the SSP as an operator applied to a per-model IMF. With operators on the
+ * context, imf1, imf2 and imf3 (Kroupa, imf_type 2) vary per model in the batch calls. all_metallicities: every
+ * metallicity of the context is built (logzsol varies per model either way on this path). */
+void opensps_context_build_ssp_ops(int handle, int all_metallicities, int *status);            /* opensps.h:430 */
+/* The isochrone modification groups as free parameters (opensps.h:440): status 2 on this path. */
+void opensps_context_build_ssp_ops_free_mods(int handle, int all_metallicities, int *status);  /* opensps.h:440 */
+void opensps_context_free_ssp_ops(int handle, int *status);                                    /* opensps.h:443 */
+void opensps_context_has_ssp_ops(int handle, int *has_ops, int *status);                       /* opensps.h:446 */
+/* One IMF's SSP grid at the context's metallicity (zmet): imf_params [imf1, imf2, imf3, vdmc, mdave] or NULL
+ * (the context's); mass_grid, lbol_grid (log10): ntfull; spec_grid: nspec x ntfull column-major
+ * (opensps.h:451-455). */
+void opensps_context_evaluate_ssp_op(int handle, int imf_type, const double *imf_params, double *mass_grid,
+                                     double *lbol_grid, double *spec_grid, int *status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_lib"
 LIB = OUT / "libopensps_gb300.so"
 SOURCES = ["capi.cu", "context.cu", "batch.cu", "csp_contract.cu", "csp_aux.cu", "band_gemm.cu", "gemm_bf16x3.cu",
-           "adjoint.cu", "noalloc.cu", "sfh.cu"]
+           "adjoint.cu", "noalloc.cu", "sfh.cu", "ssp_op.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

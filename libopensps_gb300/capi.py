@@ -64,6 +64,11 @@ SIGNATURES = {
     "opensps_context_compute_csp_batch_grad_rows": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp,
                                                            _dp, _dp, _dp, _dp, _dp, _dp] + [_dp] * 8
                                                     + [_dp, C.c_int, _dp, _dp, _ip]),
+    "opensps_context_build_ssp_ops": (None, [C.c_int, C.c_int, _ip]),
+    "opensps_context_build_ssp_ops_free_mods": (None, [C.c_int, C.c_int, _ip]),
+    "opensps_context_free_ssp_ops": (None, [C.c_int, _ip]),
+    "opensps_context_has_ssp_ops": (None, [C.c_int, _ip, _ip]),
+    "opensps_context_evaluate_ssp_op": (None, [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip]),
     "opensps_gb300_batch_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
@@ -325,6 +330,39 @@ class Context:
                                                    C.byref(st))
         _check(st, self.lib)
         return p.value, ns.value, n.value, b.value
+
+    # -- SSP operators (the IMF per model)
+    def build_ssp_ops(self, all_metallicities: bool = True):
+        """opensps_context_build_ssp_ops over the data root's operator dataset (written first if missing)."""
+        from . import synth_ops
+        synth_ops.generate(Path(os.environ["OPENSPS_DATA_HOME"]))
+        st = C.c_int(0)
+        self.lib.opensps_context_build_ssp_ops(self.handle, 1 if all_metallicities else 0, C.byref(st))
+        _check(st, self.lib)
+
+    def free_ssp_ops(self):
+        st = C.c_int(0)
+        self.lib.opensps_context_free_ssp_ops(self.handle, C.byref(st))
+        _check(st, self.lib)
+
+    @property
+    def has_ssp_ops(self) -> bool:
+        h, st = C.c_int(0), C.c_int(0)
+        self.lib.opensps_context_has_ssp_ops(self.handle, C.byref(h), C.byref(st))
+        _check(st, self.lib)
+        return bool(h.value)
+
+    def evaluate_ssp_op(self, imf_params=None, imf_type: int = 2) -> dict:
+        """opensps_context_evaluate_ssp_op: one IMF's SSP grid at the context's zmet: mass, lbol (ntfull,) and spec
+        (ntfull, nspec)."""
+        nt, ns = self.ntfull, self.nspec
+        out = {"mass": np.empty(nt), "lbol": np.empty(nt), "spec": np.empty((nt, ns))}
+        p = None if imf_params is None else np.ascontiguousarray(imf_params, dtype=np.float64)
+        st = C.c_int(0)
+        self.lib.opensps_context_evaluate_ssp_op(self.handle, imf_type, _ptr(p), _ptr(out["mass"]), _ptr(out["lbol"]),
+                                                 _ptr(out["spec"]), C.byref(st))
+        _check(st, self.lib)
+        return out
 
     def spec_mags_noalloc(self, n: int, d_spec: int, d_zred: int, d_mags: int, sync: bool = True):
         """opensps_gb300_spec_mags_noalloc: magnitudes of device spectra (nspec x n floats) at device redshifts (n

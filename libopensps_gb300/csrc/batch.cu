@@ -400,9 +400,28 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
         }
     }
+    // with SSP operators on the context (opensps_context_build_ssp_ops) the age sums come from the operator applied
+    // to each model's IMF; else from the resident basis, whose IMF is fixed
+    const bool ops = c.ops.ready;
+    if (ops) {
+        if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts) { err = "gradients with the SSP operators are not supported on this path"; return ST_UNSUPPORTED; }
+        if (c.imf_type != 2) { err = "imf_type " + std::to_string(c.imf_type) + ": only 2 (Kroupa) with the operators"; return ST_UNSUPPORTED; }
+        nacc2 = true;
+    } else {
+        for (int m = 0; m < n; ++m)
+            for (int id : {PF_IMF1, PF_IMF2, PF_IMF3})
+                if (par(m, id) != c.pdef[id]) {
+                    err = "an IMF per model needs the SSP operators (opensps_context_build_ssp_ops)";
+                    return ST_UNSUPPORTED;
+                }
+    }
     const int nacc = nacc2 ? 2 : 1;
-    BasisOperand *bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
-    if (!bop) return ST_DATA_MISSING;
+    BasisOperand *bop = nullptr;
+    if (!ops) {
+        bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
+        if (!bop) return ST_DATA_MISSING;
+    }
 
     // ---- per-pixel table (rebuilt when the batch's shared dust_index changes): ln(lambda / 5500) log2(e), the
     // diffuse curve (lambda / 5500)^dust_index in FP64 (exp_kp of the reference: the argument formed in FP64), the
@@ -443,7 +462,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // ---- scratch
     const int bn = contract_models_per_tile(nacc);
     const int n_mtiles = (n + bn - 1) / bn;
-    const int kpad = bop->kpad;
+    const int kpad = ops ? 64 : bop->kpad;
     cudaError_t e;
     const size_t nwz = (size_t)n * nt * nz;
     if ((!io.dev_inputs && (e = c.d_wz.reserve(nwz)) != cudaSuccess) ||
@@ -520,13 +539,40 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return ST_DATA_MISSING;
     }
     prof_mark(c, 1);
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
+    int launches = 0;
     WeightsArgs wa;
-    wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.kmap = bop->kmap.p;
+    wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.kmap = bop ? bop->kmap.p : nullptr;
     wa.wz = d_wz; wa.mass = c.d_mass.p; wa.llin = c.d_llin.p; wa.w_hi = c.d_whi.p; wa.w_lo = c.d_wlo.p;
     wa.sums = c.d_sums.p;
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
     wa.grid = 0;
+    float *d_y = c.d_young.p, *d_o = c.d_old.p;
+    if (ops) {
+        // ---- the operator: the IMF weights folded with the SFH weights, the template GEMM, then the epilogue
+        std::vector<double> al((size_t)3 * n);
+        for (int m = 0; m < n; ++m) {
+            al[3 * m] = par(m, PF_IMF1); al[3 * m + 1] = par(m, PF_IMF2); al[3 * m + 2] = par(m, PF_IMF3);
+        }
+        if ((e = c.d_alpha.reserve(al.size())) != cudaSuccess || (e = c.d_yo.reserve((size_t)2 * n * ns + 4)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c.d_alpha.p, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            err = cuda_msg("operator inputs", e);
+            return ST_DATA_MISSING;
+        }
+        d_y = c.d_yo.p;
+        d_o = c.d_yo.p + (size_t)n * ns;
+        const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, itesc, d_y, d_o, err);
+        if (rc) return rc;
+        prof_mark(c, 2);
+        PartsEpilogueArgs pe;
+        pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
+        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = d_y; pe.old = d_o;
+        pe.spec = c.d_spec.p;
+        if ((e = run_parts_epilogue(pe, st)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+        prof_mark(c, 3);
+        launches = 5;   // model parameters, fold, template GEMM, epilogue (+ the parameter upload)
+    } else {
     if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 2);
 
@@ -549,7 +595,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
     ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
     ca.young = ca.old = nullptr;
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
     if (parts) {
         // (4 floats of padding: the reverse pass copies whole 16-byte units of each row)
         if ((e = c.d_young.reserve((size_t)n * ns + 4)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns + 4)) != cudaSuccess) {
@@ -558,11 +603,14 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         ca.young = c.d_young.p;
         ca.old = c.d_old.p;
+        d_y = c.d_young.p;
+        d_o = c.d_old.p;
     }
     ca.status = c.d_status.p;
     if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 3);
-    int launches = 3;   // weight operand, model parameters, contraction
+    launches = 3;   // weight operand, model parameters, contraction
+    }
 
     // ---- bands and magnitudes
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
@@ -587,9 +635,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ++launches;
     }
     prof_mark(c, 4);
-    // the FP64 mass and L_bol sums (alone: beside the contraction or the band GEMM they slow those more than they take)
-    if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
-    ++launches;
+    // the FP64 mass and L_bol sums (alone: beside the contraction or the band GEMM they slow those more than they take;
+    // the operator's fold forms its own)
+    if (!ops) {
+        if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+        ++launches;
+    }
     prof_mark(c, 5);
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {
@@ -654,8 +705,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     if (parts_out) {
         young_h.resize((size_t)n * ns);
         old_h.resize((size_t)n * ns);
-        if ((e = cudaMemcpyAsync(young_h.data(), c.d_young.p, sizeof(float) * young_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(old_h.data(), c.d_old.p, sizeof(float) * old_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+        if ((e = cudaMemcpyAsync(young_h.data(), d_y, sizeof(float) * young_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(old_h.data(), d_o, sizeof(float) * old_h.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
             err = cuda_msg("parts copy", e);
             return ST_DATA_MISSING;
         }
@@ -686,12 +737,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
     }
     // weights formed on the device: L_bol blended in log between the slabs (model_sums MSUMS_BLEND,
-    // src/physics/opensps_csp_batch.f90:2129-2176), not the sum over the two slabs' linear L_bol; the SFH's SFR
+    // src/physics/opensps_csp_batch.f90:2129-2176), not the sum over the two slabs' linear L_bol (with the operators
+    // L_bol is their linear L_bol row); the SFH's SFR
     std::vector<double> lblend, sfr_h;
     if (io.sfh_par && !io.dev_inputs) {
-        lblend.resize((size_t)3 * n);
         sfr_h.resize(n);
-        if ((e = cudaMemcpyAsync(lblend.data(), c.d_lblend.p, sizeof(double) * lblend.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        if (!ops) lblend.resize((size_t)3 * n);
+        if ((!ops && (e = cudaMemcpyAsync(lblend.data(), c.d_lblend.p, sizeof(double) * lblend.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
             (e = cudaMemcpyAsync(sfr_h.data(), c.d_sfr.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
             err = cuda_msg("SFH outputs copy", e);
             return ST_DATA_MISSING;

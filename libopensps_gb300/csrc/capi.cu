@@ -224,9 +224,11 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "compute_vega_mags") c->compute_vega_mags = value;
     else if (k == "sfh") c->sfh = value;
     else if (k == "nebemlineinspec") c->nebemlineinspec = value;
+    else if (k == "zmet") c->zmet = value;
+    else if (k == "imf_type") c->imf_type = value;
     else if (k == "keep_maggies") c->keep_maggies = value;
     else if (k == "add_dust_emission" || k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_stellar_remnants" ||
-             k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" || k == "zmet" || k == "imf_type" ||
+             k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" ||
              k == "redshift_colors" || k == "cloudy_dust" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
              k == "vactoair_flag") {
         // known settings this path keeps at the values it implements; other values are refused at batch time
@@ -446,6 +448,51 @@ void opensps_gb300_batch_device(int handle, int n, const double *d_params, const
     std::string err;
     const int st = run_batch(*c, io, err);
     if (st) return fail(status, st, err);
+}
+
+void opensps_context_build_ssp_ops(int handle, int all_metallicities, int *status) {
+    (void)all_metallicities;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    std::string err;
+    const int st = ops_build(*c, err);
+    if (st) return fail(status, st, err);
+    if (status) *status = 0;
+}
+
+void opensps_context_build_ssp_ops_free_mods(int handle, int all_metallicities, int *status) {
+    (void)all_metallicities;
+    if (!lookup(handle)) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    fail(status, ST_UNSUPPORTED, "isochrone modification groups are not supported on this path");
+}
+
+void opensps_context_free_ssp_ops(int handle, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->ops.release();
+    if (status) *status = 0;
+}
+
+void opensps_context_has_ssp_ops(int handle, int *has_ops, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (has_ops) *has_ops = c->ops.ready ? 1 : 0;
+    if (status) *status = 0;
+}
+
+void opensps_context_evaluate_ssp_op(int handle, int imf_type, const double *imf_params, double *mass_grid,
+                                     double *lbol_grid, double *spec_grid, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
+    std::string err;
+    const int st = ops_evaluate(*c, imf_type, imf_params, mass_grid, lbol_grid, spec_grid, err);
+    if (st) return fail(status, st, err);
+    if (status) *status = 0;
 }
 
 void opensps_gb300_spec_mags_noalloc(int handle, int n, const float *d_spec, const double *d_zred, double *d_mags,

@@ -21,11 +21,11 @@ static const ParamInfo PARAMS[] = {
     {"logzsol", PF_LOGZSOL, 0.0}, {"tage", PF_TAGE, 0.0}, {"tau", PF_TAU, 1.0},
     {"min_wave_smooth", PF_MIN_WAVE_SMOOTH, 1.0e3}, {"max_wave_smooth", PF_MAX_WAVE_SMOOTH, 1.0e4},
     {"const", PF_CONST, 0.0}, {"fburst", PF_FBURST, 0.0}, {"tburst", PF_TBURST, 11.0},
-    {"sf_start", PF_SF_START, 0.0}, {"sf_trunc", PF_SF_TRUNC, 0.0},
+    {"sf_start", PF_SF_START, 0.0}, {"sf_trunc", PF_SF_TRUNC, 0.0}, {"imf1", PF_IMF1, 1.3},
+    {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3},
     // known to the reference, not varied per model by this path
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
-    {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"imf1", -1, 1.3},
-    {"imf2", -1, 2.3}, {"imf3", -1, 2.3}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
+    {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
     {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
     {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
     {"duste_gamma", -1, 0.01}, {"duste_umin", -1, 1.0}, {"duste_qpah", -1, 3.5}, {"gas_logu", -1, -2.0},
@@ -163,6 +163,7 @@ Context::~Context() {
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
+    ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);

@@ -23,7 +23,7 @@ enum ParamId {
     PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC,
     PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
-    PF_TBURST, PF_SF_START, PF_SF_TRUNC,
+    PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3,
     PF_COUNT
 };
 
@@ -66,6 +66,20 @@ struct BasisOperand {
     }
 };
 
+// The SSP operator on the device (opensps_context_build_ssp_ops): points, sorted entries, the library as the
+// template GEMM's B operand (pixels x ntpad, bf16 hi / lo).
+struct SspOps {
+    bool ready = false;
+    int ntempl = 0, ntpad = 0, npt = 0, nent = 0;
+    double lower_bound = 0.08;
+    DevBuf<OpsPoint> pts;
+    DevBuf<uint32_t> ent;
+    DevBuf<float> ent_c;
+    DevBuf<__nv_bfloat16> lib_hi, lib_lo;
+    CUtensorMap tm_lib_hi, tm_lib_lo;
+    void release() { pts.release(); ent.release(); ent_c.release(); lib_hi.release(); lib_lo.release(); ready = false; }
+};
+
 // What the reverse pass needs of the forward batch it follows.
 struct BatchGeom {
     BasisOperand *bop = nullptr;
@@ -77,7 +91,7 @@ struct Context {
     bool is_setup = false;
     // settings (set_int / set_float)
     int add_neb_emission = 0, add_igm_absorption = 0, smooth_velocity = 1, dust_type = 0, compute_vega_mags = 0;
-    int sfh = 0, nebemlineinspec = 1, fast_mode = 0;
+    int sfh = 0, nebemlineinspec = 1, fast_mode = 0, zmet = 1, imf_type = 2;
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];
     std::string filter_set = "gauss40";
@@ -129,6 +143,10 @@ struct Context {
     DevBuf<double> d_logage, d_lz, d_lbol;
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
     DevBuf<unsigned char> d_dual;
+    SspOps ops;
+    DevBuf<double> d_alpha;
+    DevBuf<__nv_bfloat16> d_vhi, d_vlo;
+    DevBuf<float> d_yo;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch
@@ -181,6 +199,12 @@ struct BatchIO {
            *lbol_old = nullptr, *sfr = nullptr, *mdust = nullptr;
 };
 int run_batch(Context &c, const BatchIO &io, std::string &err);
+// The SSP operator (ssp_op.cu): build from the data root, the young / old sums of a batch, one IMF's SSP grid.
+int ops_build(Context &c, std::string &err);
+int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, float *d_young,
+                  float *d_old, std::string &err);
+int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
+                 double *spec_grid, std::string &err);
 // With profiling on: records event k on the context's stream (0 starts a batch's set).
 void prof_mark(Context &c, int k);
 

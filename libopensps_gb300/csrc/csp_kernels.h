@@ -217,6 +217,34 @@ struct SfhRevArgs {
 cudaError_t run_sfh_reverse(const SfhRevArgs &a, cudaStream_t st);
 size_t sfh_dual_bytes();
 
+// The SSP operator applied to per-model IMFs (ssp_op.cu). A point of the isochrones of one grid point: the IMF bin
+// [lo, hi] (ln lo and ln(hi / lo) for the bins inside one power-law segment of the IMF), the Kroupa segment (1 .. 3,
+// 0: the bin crosses a segment boundary, -1: no stars), the star's current mass and L_bol.
+struct OpsPoint {
+    float ln_lo, dl, mcur, lum, lo, hi;
+    int seg, pad;
+};
+struct OpsFoldArgs {
+    int n, nt, nz, npt, nent, ntpad, itesc;
+    float lower_bound, lim_lo, lim_hi;
+    const double *wz;         // n x nt x nz SFH weights (age fastest)
+    const double *alpha;      // n x 3: the Kroupa slopes (imf1, imf2, imf3)
+    const OpsPoint *pts;      // (nt x nz) x npt
+    const uint32_t *ent;      // (nt x nz) x nent: template << 16 | point, sorted by template within a grid point
+    const float *ent_c;       // the entries' coefficients
+    __nv_bfloat16 *v_hi, *v_lo;   // 2n x ntpad template weights: rows 0 .. n-1 young, n .. 2n-1 old
+    double *sums;             // n x 6: mass, L_bol, young mass, old mass, young L_bol, old L_bol
+};
+cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
+// The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).
+struct PartsEpilogueArgs {
+    int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
+    const float *pix, *mpar;
+    const float *young, *old;     // n x nspec
+    float *spec;                  // n x nspec
+};
+cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
+
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);
 

@@ -1,0 +1,442 @@
+// The SSP operator applied to a free IMF per model (OpenSPS opensps_ssp_operator.f90 and opensps_ssp_batch.f90):
+// the template weights V = S . (w_IMF x SFH weight) of every model, young and old apart, then spectra = library . V
+// as a split-BF16 tcgen05 GEMM.
+//
+//   IMF bin weights  compute_imf_weights / imf_bin_weights_tab (src/physics/opensps_imf.f90:111-172, 439-559): per
+//                    isochrone point the Kroupa IMF's number of stars over its mass bin, over the IMF's mass between
+//                    its limits; inside one power-law segment c lo^e expm1(e ln(hi / lo)) / e (e = 1 - alpha), in FP32
+//                    with the segment's constants (FP64) formed once per model, as the reference's FP32 kernels do.
+//   fold             fold_multi (src/physics/opensps_ssp_batch.f90:3095-3188): V(e, m) = sum over points of S(e, p)
+//                    w_IMF(p, m) wsfh(age(p), m), young ages and old apart, with the mass and L_bol rows.
+//   template product template_columns (:3247-3385): spectra(pixel, m) = sum_e library(pixel, e) V(e, m).
+//
+// The fold: one CTA per model, over the grid points with an SFH weight. Per grid point the IMF weights of its 1500
+// points go to shared memory, then its entries, sorted by template on the host, are summed in runs of one template
+// per thread and added to the template vector in shared memory (one atomic per run). The mass and L_bol rows are
+// summed per grid point in FP32 and over grid points in FP64.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <string>
+#include <vector>
+#include "context.h"
+
+namespace sps {
+
+constexpr int OPS_THREADS = 256;
+
+__device__ __forceinline__ float ops_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// e^y - 1: the Taylor series to y^6 below |y| = 1/8 (FP32: terms beyond are below its rounding), e^y - 1 above
+__device__ __forceinline__ float ops_expm1(float y) {
+    if (fabsf(y) < 0.125f) {
+        float r = 1.f + y * (1.f / 6.f);
+        r = 1.f + y * (1.f / 5.f) * r;
+        r = 1.f + y * (1.f / 4.f) * r;
+        r = 1.f + y * (1.f / 3.f) * r;
+        r = 1.f + y * (1.f / 2.f) * r;
+        return y * r;
+    }
+    return ops_ex2(y * 1.4426950408889634f) - 1.f;
+}
+
+struct KroupaSeg {
+    float e[3], ce[3], c[3];
+    float lo[3], hi[3];
+};
+
+// c lo^e expm1(e dl) / e over one segment (e = 0: c dl)
+__device__ __forceinline__ float seg_piece(const KroupaSeg &k, int s, float ln_lo, float dl) {
+    if (k.e[s] == 0.f) return k.c[s] * dl;
+    return k.ce[s] * ops_ex2(k.e[s] * ln_lo * 1.4426950408889634f) * ops_expm1(k.e[s] * dl);
+}
+
+__device__ __forceinline__ float imf_weight(const KroupaSeg &k, const OpsPoint &q) {
+    if (q.seg > 0) return seg_piece(k, q.seg - 1, q.ln_lo, q.dl);
+    if (q.seg < 0) return 0.f;
+    // a bin across a segment boundary: its pieces in each segment
+    float v = 0.f;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
+        if (hi > lo) v += seg_piece(k, s, logf(lo), logf(hi / lo));
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(OPS_THREADS) ops_fold_kernel(OpsFoldArgs a) {
+    extern __shared__ float osm[];
+    float *V = osm;                          // 2 x ntpad: young, old
+    float *W = osm + 2 * a.ntpad;            // npt IMF weights of the current grid point
+    __shared__ double red[4][OPS_THREADS / 32];
+    __shared__ KroupaSeg kseg;
+    __shared__ float s_inv_total;
+    const int m = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < 2 * a.ntpad; i += OPS_THREADS) V[i] = 0.f;
+    if (tid == 0) {
+        // the segments' constants and the IMF's mass over its limits (imf_integral, mass-weighted), in FP64
+        const double a1 = a.alpha[3 * m], a2 = a.alpha[3 * m + 1], a3 = a.alpha[3 * m + 2];
+        const double c2 = pow(0.5, -a1 + a2);
+        const double al[3] = {a1, a2, a3}, cs[3] = {1.0, c2, c2};
+        const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
+        double total = 0.0;
+        const double llo = a.lim_lo, lhi = a.lim_hi;
+        for (int s = 0; s < 3; ++s) {
+            const double e = 1.0 - al[s];
+            kseg.e[s] = (float)e;
+            kseg.c[s] = (float)cs[s];
+            kseg.ce[s] = e != 0.0 ? (float)(cs[s] / e) : 0.f;
+            kseg.lo[s] = (float)slo[s];
+            kseg.hi[s] = (float)shi[s];
+            const double lo = fmax(llo, slo[s]), hi = fmin(lhi, shi[s]);
+            if (hi > lo) {
+                const double em = 2.0 - al[s];   // mass-weighted: int c m^(1 - alpha) dm
+                total += (em == 0.0) ? cs[s] * log(hi / lo) : cs[s] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
+            }
+        }
+        s_inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
+    }
+    __syncthreads();
+    const KroupaSeg k = kseg;
+    const float inv_total = s_inv_total;
+    const int ng = a.nt * a.nz;
+    const double *wzm = a.wz + (size_t)ng * m;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};   // mass young, mass old, L_bol young, L_bol old
+    const int per = (a.nent + OPS_THREADS - 1) / OPS_THREADS;
+    for (int g = 0; g < ng; ++g) {
+        const double sw = wzm[g];
+        if (!(sw > SAFE_FLOOR)) continue;                 // (the same for every thread)
+        const int part = (g % a.nt) < a.itesc ? 0 : 1;
+        const OpsPoint *pts = a.pts + (size_t)g * a.npt;
+        float ma = 0.f, la = 0.f;
+        for (int p = tid; p < a.npt; p += OPS_THREADS) {
+            const OpsPoint q = pts[p];
+            const float w = imf_weight(k, q) * inv_total;
+            W[p] = w;
+            ma = fmaf(w, q.mcur, ma);
+            la = fmaf(w, q.lum, la);
+        }
+        acc[part] += sw * (double)ma;
+        acc[2 + part] += sw * (double)la;
+        __syncthreads();
+        // runs of one template within this thread's entries: one shared-memory add per run
+        const uint32_t *en = a.ent + (size_t)g * a.nent;
+        const float *ec = a.ent_c + (size_t)g * a.nent;
+        const float swf = (float)sw;
+        float *Vp = V + part * a.ntpad;
+        const int e0 = tid * per, e1 = min(e0 + per, a.nent);
+        int cur = -1;
+        float run = 0.f;
+        for (int i = e0; i < e1; ++i) {
+            const uint32_t key = __ldg(en + i);
+            const int t = (int)(key >> 16);
+            const float v = W[key & 0xffffu] * __ldg(ec + i);
+            if (t != cur) {
+                if (cur >= 0 && run != 0.f) atomicAdd(Vp + cur, run * swf);
+                cur = t;
+                run = v;
+            } else {
+                run += v;
+            }
+        }
+        if (cur >= 0 && run != 0.f) atomicAdd(Vp + cur, run * swf);
+        __syncthreads();
+    }
+    // the template weights as the GEMM's A operand rows (bf16 hi / lo): young row m, old row n + m
+    for (int i = tid; i < 2 * a.ntpad; i += OPS_THREADS) {
+        const int part = i / a.ntpad, e = i % a.ntpad;
+        const float v = V[i];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const size_t row = (size_t)(part == 0 ? m : a.n + m) * a.ntpad + e;
+        a.v_hi[row] = h;
+        a.v_lo[row] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        double v = acc[j];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) red[j][warp] = v;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int j = 0; j < 4; ++j)
+            for (int w = 0; w < OPS_THREADS / 32; ++w) s[j] += red[j][w];
+        double *o = a.sums + (size_t)6 * m;
+        o[0] = s[0] + s[1];
+        o[1] = s[2] + s[3];
+        o[2] = s[0]; o[3] = s[1]; o[4] = s[2]; o[5] = s[3];
+    }
+}
+
+cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    const size_t smem = sizeof(float) * (2 * (size_t)a.ntpad + (size_t)a.npt);
+    cudaError_t e = cudaFuncSetAttribute(ops_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ops_fold_kernel<<<a.n, OPS_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------- the epilogue
+__global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a) {
+    extern __shared__ float tsm[];
+    const int ns = a.nspec, m = blockIdx.x;
+    const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
+    const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
+    const float kd2 = mp[MP_KD2], one_m_fnd = mp[MP_ONE_M_FND], fnd = mp[MP_FND], di = mp[MP_DUST_INDEX];
+    const float kd1 = mp[MP_KD1], d1i = mp[MP_DUST1_INDEX], one_m_fo = mp[MP_ONE_M_FO], fo = mp[MP_FO];
+    const float kd3 = mp[MP_KD3], igm_on = mp[MP_IGM_ON], kcap = mp[MP_IGM_KCAP];
+    const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
+    float kb[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) kb[k] = mp[MP_IGM_KB + k];
+    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
+        const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
+        const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
+        const float tb = (kd1 != 0.f) ? ops_ex2(kd1 * ops_ex2(d1i * v0.x)) : 1.f;
+        const float to = (kd3 != 0.f) ? ops_ex2(kd3 * curve) : 1.f;
+        const float y = yv[p];
+        const float ss = (y * tb * one_m_fo + y * fo) + ov[p] * to;
+        float tot = ss * fmaf(ops_ex2(kd2 * curve), one_m_fnd, fnd);
+        if (igm_on != 0.f && p < a.jtop) {
+            float arg;
+            if (p < jmax) {
+                arg = kcap;
+            } else {
+                const float4 v1 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[1];
+                arg = v0.z * kb[0] + v0.w * kb[1] + v1.x * kb[2] + v1.y * kb[3] + v1.z * kb[4] + v1.w * kb[5];
+            }
+            tot *= ops_ex2(arg);
+        }
+        tsm[p] = tot;
+    }
+    __syncthreads();
+    const int R = __float_as_int(mp[MP_SMOOTH_R]);
+    float tap[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) tap[d] = mp[MP_TAPS + d];
+    float *out = a.spec + (size_t)m * ns;
+    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
+        float v = tsm[p];
+        if (R >= 0 && p >= a.sm_lo && p <= a.sm_hi) {
+            float s = 0.f;
+#pragma unroll
+            for (int d = -4; d <= 4; ++d) s = fmaf(tap[d + 4], tsm[p + d], s);
+            v = s;
+        }
+        out[p] = v;
+    }
+}
+
+cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    const size_t smem = sizeof(float) * (size_t)a.nspec;
+    cudaError_t e = cudaFuncSetAttribute(parts_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    parts_epilogue_kernel<<<a.n, 256, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------- host side
+template <class T>
+static bool read_raw(const std::string &path, std::vector<T> &out, size_t count) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    out.resize(count);
+    f.read(reinterpret_cast<char *>(out.data()), (std::streamsize)(count * sizeof(T)));
+    return (size_t)f.gcount() == count * sizeof(T);
+}
+
+static std::string cmsg(const char *what, cudaError_t e) { return std::string(what) + ": " + cudaGetErrorString(e); }
+
+// The operator from the data root's ssp_op dataset (the reference's ssp_operator_build from isochrones and
+// libraries; here its synthetic stand-in): points with their bins and Kroupa segments, entries sorted by template per
+// grid point, the library transposed to pixels x ntpad in bf16 hi / lo.
+int ops_build(Context &c, std::string &err) {
+    const std::string dir = data_root() + "/ssp_op/";
+    std::ifstream mf(dir + "manifest.json");
+    if (!mf) { err = "SSP operator data missing under " + dir; return ST_DATA_MISSING; }
+    const int ns = c.nspec, nt = c.nt, nz = c.nz, ng = nt * nz;
+    const int npt = 1500, ntempl = 2000;
+    std::vector<float> lib;
+    std::vector<double> mini, coef, mcur, lum;
+    std::vector<int> idx;
+    const size_t np = (size_t)ng * npt;
+    if (!read_raw(dir + "lib.f32", lib, (size_t)ntempl * ns) || !read_raw(dir + "pt_mini.f64", mini, np) ||
+        !read_raw(dir + "pt_idx.i32", idx, np * 4) || !read_raw(dir + "pt_coef.f64", coef, np * 4) ||
+        !read_raw(dir + "pt_mcur.f64", mcur, np) || !read_raw(dir + "pt_lum.f64", lum, np)) {
+        err = "SSP operator data under " + dir + " does not match the context's grid";
+        return ST_DATA_MISSING;
+    }
+    const double lower_bound = 0.08, lim_lo = 0.08, lim_hi = 120.0;
+    // data layout: grid point (z, t) z-major in the files: g_file = z nt + t == t + nt z (age fastest)
+    std::vector<OpsPoint> pts(np);
+    const int nent = 4 * npt;
+    std::vector<uint32_t> ent((size_t)ng * nent);
+    std::vector<float> ent_c((size_t)ng * nent);
+    std::vector<std::pair<uint32_t, float>> tmp(nent);
+    for (int g = 0; g < ng; ++g) {
+        const double *mi = mini.data() + (size_t)g * npt;
+        for (int i = 0; i < npt; ++i) {
+            OpsPoint &q = pts[(size_t)g * npt + i];
+            const double m1 = (i == 0) ? lower_bound : mi[i] - 0.5 * (mi[i] - mi[i - 1]);
+            const double m2 = (i == npt - 1) ? mi[i] : mi[i] + 0.5 * (mi[i + 1] - mi[i]);
+            q.mcur = (float)mcur[(size_t)g * npt + i];
+            q.lum = (float)lum[(size_t)g * npt + i];
+            q.lo = (float)m1;
+            q.hi = (float)m2;
+            q.ln_lo = (float)std::log(m1);
+            q.dl = (float)std::log1p((m2 - m1) / m1);
+            q.pad = 0;
+            if (mi[i] < lim_lo || mi[i] > lim_hi || m2 <= m1) q.seg = -1;
+            else if (m1 >= 0.08 && m2 <= 0.5) q.seg = 1;
+            else if (m1 >= 0.5 && m2 <= 1.0) q.seg = 2;
+            else if (m1 >= 1.0) q.seg = 3;
+            else q.seg = 0;
+        }
+        for (int i = 0; i < npt; ++i)
+            for (int k = 0; k < 4; ++k) {
+                const size_t s = ((size_t)g * npt + i) * 4 + k;
+                tmp[4 * i + k] = {((uint32_t)idx[s] << 16) | (uint32_t)i, (float)coef[s]};
+            }
+        std::sort(tmp.begin(), tmp.end(), [](const std::pair<uint32_t, float> &x, const std::pair<uint32_t, float> &y) {
+            return x.first < y.first;
+        });
+        for (int i = 0; i < nent; ++i) {
+            ent[(size_t)g * nent + i] = tmp[i].first;
+            ent_c[(size_t)g * nent + i] = tmp[i].second;
+        }
+    }
+    const int ntpad = (ntempl + 63) / 64 * 64;
+    std::vector<uint16_t> lh((size_t)ns * ntpad, 0), ll((size_t)ns * ntpad, 0);
+    for (int e = 0; e < ntempl; ++e)
+        for (int p = 0; p < ns; ++p) {
+            const float f = lib[(size_t)e * ns + p];
+            const uint16_t h = f32_to_bf16_bits(f);
+            lh[(size_t)p * ntpad + e] = h;
+            ll[(size_t)p * ntpad + e] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));
+        }
+    SspOps &o = c.ops;
+    cudaError_t e;
+    if ((e = o.pts.reserve(np)) != cudaSuccess || (e = o.ent.reserve(ent.size())) != cudaSuccess ||
+        (e = o.ent_c.reserve(ent_c.size())) != cudaSuccess || (e = o.lib_hi.reserve(lh.size())) != cudaSuccess ||
+        (e = o.lib_lo.reserve(ll.size())) != cudaSuccess ||
+        (e = cudaMemcpy(o.pts.p, pts.data(), sizeof(OpsPoint) * np, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o.ent.p, ent.data(), sizeof(uint32_t) * ent.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o.ent_c.p, ent_c.data(), sizeof(float) * ent_c.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o.lib_hi.p, lh.data(), 2 * lh.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o.lib_lo.p, ll.data(), 2 * ll.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&o.tm_lib_hi, o.lib_hi.p, ntpad, ns, gemm_bk(), gemm_bn())) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&o.tm_lib_lo, o.lib_lo.p, ntpad, ns, gemm_bk(), gemm_bn())) != cudaSuccess) {
+        err = cmsg("SSP operator upload", e);
+        o.release();
+        return ST_DATA_MISSING;
+    }
+    o.ntempl = ntempl;
+    o.ntpad = ntpad;
+    o.npt = npt;
+    o.nent = nent;
+    o.lower_bound = lower_bound;
+    o.ready = true;
+    return 0;
+}
+
+// The young and old sums of n models (d_wz: their SFH weights over ages and metallicities, d_alpha: n x 3 Kroupa
+// slopes) through the operator: the fold, then the template GEMM into d_young / d_old (n x nspec each, contiguous:
+// d_old = d_young + n nspec); the mass and L_bol sums into the context's sums (n x 6).
+int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, float *d_young,
+                  float *d_old, std::string &err) {
+    SspOps &o = c.ops;
+    cudaStream_t st = c.stream;
+    cudaError_t e;
+    if ((e = c.d_vhi.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
+        (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess) {
+        err = cmsg("device memory", e);
+        return ST_DATA_MISSING;
+    }
+    OpsFoldArgs fa;
+    fa.n = n; fa.nt = c.nt; fa.nz = c.nz; fa.npt = o.npt; fa.nent = o.nent; fa.ntpad = o.ntpad; fa.itesc = itesc;
+    fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;
+    fa.wz = d_wz; fa.alpha = d_alpha; fa.pts = o.pts.p; fa.ent = o.ent.p; fa.ent_c = o.ent_c.p;
+    fa.v_hi = c.d_vhi.p; fa.v_lo = c.d_vlo.p; fa.sums = c.d_sums.p;
+    if ((e = run_ops_fold(fa, st)) != cudaSuccess) { err = cmsg("operator fold kernel", e); return ST_DATA_MISSING; }
+    GemmPlan pl;
+    pl.num_sms = c.num_sms;
+    pl.tm_b_hi = o.tm_lib_hi;
+    pl.tm_b_lo = o.tm_lib_lo;
+    if ((e = encode_tmap_2d_bf16(&pl.tm_a_hi, c.d_vhi.p, o.ntpad, 2 * n, gemm_bk(), gemm_bm())) != cudaSuccess ||
+        (e = encode_tmap_2d_bf16(&pl.tm_a_lo, c.d_vlo.p, o.ntpad, 2 * n, gemm_bk(), gemm_bm())) != cudaSuccess) {
+        err = cmsg("template tensor map", e);
+        return ST_DATA_MISSING;
+    }
+    GemmArgs g;
+    g.M = 2 * n; g.N = c.nspec; g.K = o.ntpad; g.ldd = c.nspec; g.b_row0 = 0; g.D = d_young; g.status = c.d_status.p;
+    if (d_old != d_young + (size_t)n * c.nspec) { err = "operator parts: the old sums must follow the young"; return ST_BAD_ARG; }
+    if ((e = run_gemm_bf16x3(pl, g, st)) != cudaSuccess) { err = cmsg("template GEMM", e); return ST_DATA_MISSING; }
+    return 0;
+}
+
+// One IMF's SSP grid at the context's metallicity zmet: every age as a "model" with a unit weight there.
+int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
+                 double *spec_grid, std::string &err) {
+    if (!c.ops.ready) { err = "no SSP operators on the context (opensps_context_build_ssp_ops)"; return ST_NO_OPERATOR; }
+    if (imf_type != 2) { err = "imf_type " + std::to_string(imf_type) + ": only 2 (Kroupa) on this path"; return ST_UNSUPPORTED; }
+    const int nt = c.nt, nz = c.nz, ns = c.nspec;
+    const int z = std::max(1, std::min(c.zmet, nz)) - 1;
+    std::vector<double> wz((size_t)nt * nt * nz, 0.0), alpha((size_t)3 * nt);
+    const double a1 = imf_params ? imf_params[0] : c.pdef[PF_IMF1], a2 = imf_params ? imf_params[1] : c.pdef[PF_IMF2];
+    const double a3 = imf_params ? imf_params[2] : c.pdef[PF_IMF3];
+    for (int t = 0; t < nt; ++t) {
+        wz[(size_t)nt * nz * t + t + (size_t)nt * z] = 1.0;
+        alpha[3 * t] = a1; alpha[3 * t + 1] = a2; alpha[3 * t + 2] = a3;
+    }
+    cudaError_t e;
+    cudaStream_t st = c.stream;
+    if ((e = c.d_wz.reserve(wz.size())) != cudaSuccess || (e = c.d_alpha.reserve(alpha.size())) != cudaSuccess ||
+        (e = c.d_yo.reserve((size_t)2 * nt * ns + 4)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(c.d_wz.p, wz.data(), sizeof(double) * wz.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(c.d_alpha.p, alpha.data(), sizeof(double) * alpha.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+        err = cmsg("operator inputs", e);
+        return ST_DATA_MISSING;
+    }
+    cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
+    // every age young (itesc = nt): the spectra are the young sums
+    int rc = run_ops_parts(c, nt, c.d_wz.p, c.d_alpha.p, nt, c.d_yo.p, c.d_yo.p + (size_t)nt * ns, err);
+    if (rc) return rc;
+    std::vector<float> y((size_t)nt * ns);
+    std::vector<double> sums((size_t)6 * nt);
+    int kstatus = 0;
+    if ((e = cudaMemcpyAsync(y.data(), c.d_yo.p, sizeof(float) * y.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(sums.data(), c.d_sums.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&kstatus, c.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        err = cmsg("operator evaluation", e);
+        return ST_DATA_MISSING;
+    }
+    if (kstatus != 0) {
+        char buf[96];
+        std::snprintf(buf, sizeof buf, "a device wait gave up (code 0x%x)", kstatus);
+        err = buf;
+        return ST_DATA_MISSING;
+    }
+    for (int t = 0; t < nt; ++t) {
+        if (mass_grid) mass_grid[t] = sums[(size_t)6 * t];
+        if (lbol_grid) lbol_grid[t] = sums[(size_t)6 * t + 1] > SAFE_FLOOR ? std::log10(sums[(size_t)6 * t + 1]) : 0.0;
+        if (spec_grid)
+            for (int p = 0; p < ns; ++p) spec_grid[(size_t)ns * t + p] = (double)y[(size_t)ns * t + p];
+    }
+    return 0;
+}
+
+}  // namespace sps

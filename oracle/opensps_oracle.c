@@ -326,6 +326,9 @@ typedef struct {
  *   compute_magnitudes_columns (src/spectra/opensps_batch_photometry.f90:53-180): observed_frame_z :819-903,
  *   band_fluxes :1049-1171 (trapezoid per band support), magnitudes_from_fluxes :185-232 (AB, distance term).
  * work: 4 * nspec doubles. */
+static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double *spec,
+                       double *mags, double *fband_out, double *tot, double *tmp);
+
 static void csp_one(const oracle_grid_t *g, const double *wz, const double *par, double *spec, double *mags,
                     double *mass, double *lbol, double *emlines, double *young, double *old, double *fband_out,
                     double *work, int ab_only) {
@@ -355,7 +358,15 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
     if (lbol) *lbol = ls > SAFE_FLOOR ? log10(ls) : 0.0;
     if (young) memcpy(young, y, sizeof(double) * ns);
     if (old) memcpy(old, o, sizeof(double) * ns);
+    post_parts(g, y, o, par, spec, mags, fband_out, tot, tmp);
+    (void)ab_only;
+}
 
+/* From the young and old age sums of a model: attenuation, IGM, smoothing, the spectrum and the magnitudes
+ * (the stages of compute_csp_batch after the age sums). tot, tmp: nspec doubles of work. */
+static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double *spec,
+                       double *mags, double *fband_out, double *tot, double *tmp) {
+    const int ns = g->nspec;
     /* attenuation, dust_type 0 (power law) */
     double d1 = par[P_DUST1], d2 = par[P_DUST2], d3 = par[P_DUST3], di = par[P_DUST_INDEX], d1i = par[P_DUST1_INDEX];
     double fnd = par[P_FRAC_NODUST], fo = par[P_FRAC_OBRUN];
@@ -434,7 +445,22 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
             if (fband_out) fband_out[b] = s;
             if (mags) mags[b] = (s > 0.0 ? -2.5 * log10(s) : NAN) - zp + dist;
         }
-        (void)ab_only;
+    }
+}
+
+/* The batch from given young and old age sums (young, old: nspec x n): spectra, magnitudes, band fluxes. */
+void oracle_csp_from_parts(const oracle_grid_t *g, int n, const double *young, const double *old, const double *par,
+                           double *spec, double *mags, double *fband) {
+    const int ns = g->nspec;
+#pragma omp parallel
+    {
+        double *work = (double *)malloc(sizeof(double) * 2 * (size_t)ns);
+#pragma omp for schedule(dynamic, 4)
+        for (int m = 0; m < n; ++m)
+            post_parts(g, young + (size_t)ns * m, old + (size_t)ns * m, par + (size_t)P_NPAR * m,
+                       spec ? spec + (size_t)ns * m : NULL, mags ? mags + (size_t)g->nbands * m : NULL,
+                       fband ? fband + (size_t)g->nbands * m : NULL, work, work + ns);
+        free(work);
     }
 }
 

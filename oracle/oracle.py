@@ -23,7 +23,7 @@ _dp = C.POINTER(C.c_double)
 
 
 def build() -> Path:
-    srcs = [HERE / "opensps_oracle.c", HERE / "sfh_oracle.c"]
+    srcs = [HERE / "opensps_oracle.c", HERE / "sfh_oracle.c", HERE / "ops_oracle.c"]
     if not LIB.exists() or any(LIB.stat().st_mtime < s.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
@@ -34,6 +34,13 @@ class _Grid(C.Structure):
                 ("lam", _dp), ("log_age", _dp), ("basis", _dp), ("mass", _dp), ("lbol", _dp), ("bands", _dp),
                 ("zt", _dp), ("dl", _dp), ("nline", C.c_int), ("line_lum", _dp), ("add_igm", C.c_int),
                 ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double)]
+
+
+class _OpsT(C.Structure):
+    _fields_ = [("nspec", C.c_int), ("nt", C.c_int), ("nz", C.c_int), ("npt", C.c_int), ("ntempl", C.c_int),
+                ("lib", C.POINTER(C.c_float)), ("mini", _dp), ("idx", C.POINTER(C.c_int)), ("coef", _dp),
+                ("mcur", _dp), ("lum", _dp), ("lower_bound", C.c_double), ("lim_lo", C.c_double),
+                ("lim_hi", C.c_double)]
 
 
 _lib = None
@@ -60,6 +67,10 @@ def lib() -> C.CDLL:
         _lib.oracle_expi.restype = C.c_double
         _lib.oracle_expi.argtypes = [C.c_double]
         _lib.oracle_sfh_batch.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        _lib.oracle_csp_from_parts.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        _lib.oracle_ops_csp.argtypes = [C.POINTER(_OpsT), C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp]
+        _lib.oracle_kroupa_integral.restype = C.c_double
+        _lib.oracle_kroupa_integral.argtypes = [_dp, C.c_double, C.c_double, C.c_int]
         _lib.oracle_abs_mag_zeropoint_log.restype = C.c_double
     return _lib
 
@@ -152,6 +163,18 @@ class Oracle:
                                _p(out.get("old")), _p(out.get("fband")))
         return out
 
+    def csp_from_parts(self, params: dict, young: np.ndarray, old: np.ndarray) -> dict:
+        """The batch's stages after the age sums (attenuation, IGM, smoothing, magnitudes) from given young and old
+        spectra (n, nspec)."""
+        y = np.ascontiguousarray(young, dtype=np.float64)
+        o = np.ascontiguousarray(old, dtype=np.float64)
+        n = y.shape[0]
+        par = self.pack_params(params, n)
+        out = {"mags": np.empty((n, self.nbands)), "spec": np.empty((n, self.nspec)), "fband": np.empty((n, self.nbands))}
+        lib().oracle_csp_from_parts(C.byref(self.grid), n, _p(y), _p(o), _p(par), _p(out["spec"]), _p(out["mags"]),
+                                    _p(out["fband"]))
+        return out
+
     def velocity_row(self, sigma: float, i: int, minl: float = 1.0e3, maxl: float = 1.0e4):
         lo, coef = C.c_int(0), np.zeros(64)
         nt = lib().oracle_velocity_row(self.nspec, _p(self.lam), sigma, minl, maxl, i, C.byref(lo), _p(coef), 64)
@@ -159,3 +182,36 @@ class Oracle:
 
     def distance_term(self, z: float) -> float:
         return lib().oracle_distance_term(_p(self.zt), _p(self.dl), z)
+
+
+class OpsOracle:
+    """The SSP operator applied to per-model Kroupa IMFs (ops_oracle.c) over the operator dataset (synth_ops)."""
+
+    def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0):
+        self.ops = ops
+        man = ops["manifest"]
+        self.nspec, self.nt, self.nz, self.npt, self.ntempl = man["nspec"], man["nt"], man["nz"], man["npt"], man["ntempl"]
+        self._keep = [np.ascontiguousarray(ops[k]) for k in ("lib", "mini", "idx", "coef", "mcur", "lum")]
+        lb, mi, ix, co, mc, lu = self._keep
+        t = _OpsT()
+        t.nspec, t.nt, t.nz, t.npt, t.ntempl = self.nspec, self.nt, self.nz, self.npt, self.ntempl
+        t.lib = lb.ctypes.data_as(C.POINTER(C.c_float))
+        t.mini, t.coef, t.mcur, t.lum = _p(mi), _p(co), _p(mc), _p(lu)
+        t.idx = ix.ctypes.data_as(C.POINTER(C.c_int))
+        t.lower_bound, t.lim_lo, t.lim_hi = man["imf_lower_bound"], lim_lo, lim_hi
+        self.t = t
+
+    def parts(self, alpha: np.ndarray, wz: np.ndarray, itesc: int):
+        """alpha (n, 3) Kroupa slopes, wz (n, nz, nt): young, old (n, nspec), mass and linear L_bol (n,)."""
+        a = np.ascontiguousarray(alpha, dtype=np.float64)
+        w = np.ascontiguousarray(wz, dtype=np.float64)
+        n = a.shape[0]
+        y, o = np.empty((n, self.nspec)), np.empty((n, self.nspec))
+        mass, ls = np.empty(n), np.empty(n)
+        lib().oracle_ops_csp(C.byref(self.t), n, _p(a), _p(w), int(itesc), _p(y), _p(o), _p(mass), _p(ls))
+        return y, o, mass, ls
+
+
+def kroupa_integral(alpha, m1: float, m2: float, mass_weighted: bool) -> float:
+    a = np.ascontiguousarray(alpha, dtype=np.float64)
+    return lib().oracle_kroupa_integral(_p(a), float(m1), float(m2), int(mass_weighted))
