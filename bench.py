@@ -15,6 +15,8 @@ power-law dust (tau_V uniform 0-3), redshift uniform 0-6 with the Madau IGM, vel
   bf16 FLOPs per launch over its mean CUDA-event duration, against the measured sustained bf16 peak.
 * ``adjoint``: the reverse pass (compute_csp_batch_grad_rows) at B = 16384 with cotangents on 40 magnitudes and
   512 spectral bins, through the C API from page-locked host buffers (wall time), with its device stage times.
+* ``ssp_operator``: the IMF-free batch through the SSP operator (a Kroupa IMF per model) at B = 1024, through the C
+  API, with its device stage times.
 * ``cpu_baseline`` / ``--impl reference``: the FP64 CPU oracle (a restatement of OpenSPS's compute_csp_batch,
   the reference being Fortran with no compiler in this image) with OpenMP on all host cores, on a bounded sample.
 
@@ -190,6 +192,45 @@ def adjoint_measure(ctx, args, rank, torch, barrier) -> dict | None:
             "outputs": "mags, mass, lbol, params_bar (44 rows), weights_z_bar"}
 
 
+def ssp_operator_measure(args, torch, barrier) -> dict | None:
+    """The SSP operator with a Kroupa IMF per model (slopes uniform in [0.3, 1.8], [1.3, 2.8], [1.8, 3.3]) at B =
+    --ops-batch through the C API (weights over ages and metallicities of the mixed workload: every grid point holds
+    weight, so 1284 x 1500 IMF bin weights per model), wall time per call with its device stage times."""
+    from libopensps_gb300 import workloads
+    from libopensps_gb300.capi import Context
+    n = args.ops_batch
+    if n <= 0:
+        return None
+    ctx = Context()
+    ctx.set_int("add_igm_absorption", 1)
+    ctx.build_ssp_ops()
+    h_wz = torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True)
+    _, params = workloads.mixed_csp(n, seed=3000, out=h_wz.numpy())
+    rng = np.random.default_rng(3001)
+    params = dict(params, imf1=rng.uniform(0.3, 1.8, n), imf2=rng.uniform(1.3, 2.8, n), imf3=rng.uniform(1.8, 3.3, n))
+    wz = h_wz.numpy()
+    for _ in range(max(args.warmup, 1)):
+        ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    barrier()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(args.ops_steps):
+        ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    barrier()
+    ms = (time.perf_counter() - t0) * 1e3 / args.ops_steps
+    kt = ctx.kernel_times()
+    ctx.set_profiling(False)
+    ctx.close()
+    names = ["model_params", "fold_and_template_gemm", "epilogue", "bands"]
+    stages = dict(zip(names, kt))
+    dev = sum(stages.values())
+    return {"batch": n, "value": n / (ms * 1e-3), "unit": "models/s", "ms_per_step": ms, "steps": args.ops_steps,
+            "device_ms": dev, "device_value": n / (dev * 1e-3) if dev > 0 else None, "stage_ms": stages,
+            "imf_bin_weights_per_model": K_AGES * N_Z * 1500, "operator_entries": K_AGES * N_Z * 1500 * 4,
+            "workload": "IMF-free CSP through the SSP operator (Kroupa slopes per model), mixed-workload weights, "
+                        "power-law dust, z 0-6 with IGM, smoothing 50-300 km/s, 40 filters"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -268,6 +309,7 @@ def run_ours(args) -> None:
     h2d = h_wz.numel() * 8 + n * 11 * 8 + 3 * n * 8
     d2h = n * nb * 8 + 6 * n * 8
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
+    ssp_ops = ssp_operator_measure(args, torch, barrier)
 
     # roofline of the contraction
     pk = _peaks()
@@ -299,6 +341,7 @@ def run_ours(args) -> None:
                                                "fp64_sums"], ktimes))},
             "cpu_baseline": cpu,
             "adjoint": adjoint,
+            "ssp_operator": ssp_ops,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -318,6 +361,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--adjoint-batch", type=int, default=16384)
     ap.add_argument("--adjoint-steps", type=int, default=10)
+    ap.add_argument("--ops-batch", type=int, default=1024)
+    ap.add_argument("--ops-steps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -163,7 +163,8 @@ Context::~Context() {
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
-    ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release();
+    ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
+    d_spart.release(); d_vflag.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);

@@ -146,7 +146,9 @@ struct Context {
     SspOps ops;
     DevBuf<double> d_alpha;
     DevBuf<__nv_bfloat16> d_vhi, d_vlo;
-    DevBuf<float> d_yo;
+    DevBuf<float> d_yo, d_vpart;
+    DevBuf<double> d_spart;
+    DevBuf<int> d_vflag;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)
     int last_launches = 0;       // kernels launched by the last batch

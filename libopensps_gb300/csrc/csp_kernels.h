@@ -234,6 +234,9 @@ struct OpsFoldArgs {
     const float *ent_c;       // the entries' coefficients
     __nv_bfloat16 *v_hi, *v_lo;   // 2n x ntpad template weights: rows 0 .. n-1 young, n .. 2n-1 old
     double *sums;             // n x 6: mass, L_bol, young mass, old mass, young L_bol, old L_bol
+    float *vpart;             // nz x 2n x ntpad: each metallicity slab's template weights
+    double *spart;            // nz x n x 4: each slab's mass and L_bol rows (young, old)
+    int *flag;                // nz x ceil(n / 4): the slab has weight for some model of the group
 };
 cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
 // The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).

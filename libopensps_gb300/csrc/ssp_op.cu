@@ -10,10 +10,11 @@
 //                    w_IMF(p, m) wsfh(age(p), m), young ages and old apart, with the mass and L_bol rows.
 //   template product template_columns (:3247-3385): spectra(pixel, m) = sum_e library(pixel, e) V(e, m).
 //
-// The fold: one CTA per model, over the grid points with an SFH weight. Per grid point the IMF weights of its 1500
-// points go to shared memory, then its entries, sorted by template on the host, are summed in runs of one template
-// per thread and added to the template vector in shared memory (one atomic per run). The mass and L_bol rows are
-// summed per grid point in FP32 and over grid points in FP64.
+// The fold: four models and one metallicity slab per CTA (every point record and entry read once for the four), over
+// the slab's grid points any of them weighs; the slabs' template vectors are then summed in slab order. Per grid point the IMF weights of its 1500 points go to shared memory, then its entries, sorted by
+// template on the host, are summed in runs of one template per thread and added to the template vectors in shared
+// memory (one atomic per run and model). The mass and L_bol rows are summed per grid point in FP32 and over grid
+// points in FP64.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -73,118 +74,250 @@ __device__ __forceinline__ float imf_weight(const KroupaSeg &k, const OpsPoint &
     return v;
 }
 
-__global__ void __launch_bounds__(OPS_THREADS) ops_fold_kernel(OpsFoldArgs a) {
-    extern __shared__ float osm[];
-    float *V = osm;                          // 2 x ntpad: young, old
-    float *W = osm + 2 * a.ntpad;            // npt IMF weights of the current grid point
-    __shared__ double red[4][OPS_THREADS / 32];
-    __shared__ KroupaSeg kseg;
-    __shared__ float s_inv_total;
-    const int m = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < 2 * a.ntpad; i += OPS_THREADS) V[i] = 0.f;
-    if (tid == 0) {
+// OPS_K models per CTA: every point record and entry is read once for all of them. A CTA takes one metallicity slab
+// (blockIdx.y) of its OPS_K models; the slabs' template weights are summed after (ops_reduce_kernel), in slab order.
+constexpr int OPS_K = 4;
+constexpr int OPS_PT_PER = 6;     // point records per thread and grid point (npt <= OPS_THREADS x OPS_PT_PER)
+constexpr int OPS_ENT_PER = 24;   // entries per thread and grid point (nent <= OPS_THREADS x OPS_ENT_PER)
+
+constexpr int OPS_MAXT = 128;     // ages per slab (nt <= OPS_MAXT)
+constexpr int OPS_NBUF = 3;       // IMF-weight buffers (phase A of i + 1 beside phase B of i)
+
+__global__ void __launch_bounds__(OPS_THREADS, 2) ops_fold_kernel(OpsFoldArgs a) {
+    extern __shared__ float4 osm4[];
+    // OPS_NBUF x npt: the IMF weights of a grid point, one per model. Phase B of grid point i runs beside phase A of
+    // i + 1 (no barrier between them), and the barrier after phase A of i + 1 orders phase B of i before phase A of
+    // i + 2: three buffers keep the three apart.
+    float4 *W4 = osm4;
+    float *V = reinterpret_cast<float *>(osm4 + OPS_NBUF * a.npt);   // OPS_K x ntpad: per model, the current part
+    __shared__ KroupaSeg kseg[OPS_K];
+    __shared__ float inv_total[OPS_K];
+    __shared__ float sw_s[OPS_MAXT][OPS_K];           // the models' SFH weights at the slab's ages
+    __shared__ int tlist[OPS_MAXT];                   // the ages any model weighs
+    __shared__ int n_active;
+    __shared__ float gsum[OPS_NBUF][OPS_THREADS / 32][OPS_K][2];   // per warp: sum of w mcur, w L of its points
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = blockIdx.x, z = blockIdx.y;
+    const int m0 = grp * OPS_K;
+    const int nk = min(OPS_K, a.n - m0);
+    const int ngroups = (a.n + OPS_K - 1) / OPS_K;
+    const int ng = a.nt * a.nz;
+    for (int i = tid; i < OPS_K * a.ntpad; i += OPS_THREADS) V[i] = 0.f;
+    for (int i = tid; i < a.nt * OPS_K; i += OPS_THREADS) {
+        const int t = i / OPS_K, k = i % OPS_K;
+        const double sw = k < nk ? a.wz[(size_t)ng * (m0 + k) + t + (size_t)a.nt * z] : 0.0;
+        sw_s[t][k] = (sw > SAFE_FLOOR) ? (float)sw : 0.f;
+    }
+    if (tid < OPS_K) {
+        const int k = tid;
         // the segments' constants and the IMF's mass over its limits (imf_integral, mass-weighted), in FP64
+        const int m = min(m0 + k, a.n - 1);
         const double a1 = a.alpha[3 * m], a2 = a.alpha[3 * m + 1], a3 = a.alpha[3 * m + 2];
         const double c2 = pow(0.5, -a1 + a2);
         const double al[3] = {a1, a2, a3}, cs[3] = {1.0, c2, c2};
         const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
         double total = 0.0;
-        const double llo = a.lim_lo, lhi = a.lim_hi;
-        for (int s = 0; s < 3; ++s) {
-            const double e = 1.0 - al[s];
-            kseg.e[s] = (float)e;
-            kseg.c[s] = (float)cs[s];
-            kseg.ce[s] = e != 0.0 ? (float)(cs[s] / e) : 0.f;
-            kseg.lo[s] = (float)slo[s];
-            kseg.hi[s] = (float)shi[s];
-            const double lo = fmax(llo, slo[s]), hi = fmin(lhi, shi[s]);
+        for (int sg = 0; sg < 3; ++sg) {
+            const double e = 1.0 - al[sg];
+            kseg[k].e[sg] = (float)e;
+            kseg[k].c[sg] = (float)cs[sg];
+            kseg[k].ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
+            kseg[k].lo[sg] = (float)slo[sg];
+            kseg[k].hi[sg] = (float)shi[sg];
+            const double lo = fmax((double)a.lim_lo, slo[sg]), hi = fmin((double)a.lim_hi, shi[sg]);
             if (hi > lo) {
-                const double em = 2.0 - al[s];   // mass-weighted: int c m^(1 - alpha) dm
-                total += (em == 0.0) ? cs[s] * log(hi / lo) : cs[s] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
+                const double em = 2.0 - al[sg];   // mass-weighted: int c m^(1 - alpha) dm
+                total += (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
             }
         }
-        s_inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
-    }
-    __syncthreads();
-    const KroupaSeg k = kseg;
-    const float inv_total = s_inv_total;
-    const int ng = a.nt * a.nz;
-    const double *wzm = a.wz + (size_t)ng * m;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};   // mass young, mass old, L_bol young, L_bol old
-    const int per = (a.nent + OPS_THREADS - 1) / OPS_THREADS;
-    for (int g = 0; g < ng; ++g) {
-        const double sw = wzm[g];
-        if (!(sw > SAFE_FLOOR)) continue;                 // (the same for every thread)
-        const int part = (g % a.nt) < a.itesc ? 0 : 1;
-        const OpsPoint *pts = a.pts + (size_t)g * a.npt;
-        float ma = 0.f, la = 0.f;
-        for (int p = tid; p < a.npt; p += OPS_THREADS) {
-            const OpsPoint q = pts[p];
-            const float w = imf_weight(k, q) * inv_total;
-            W[p] = w;
-            ma = fmaf(w, q.mcur, ma);
-            la = fmaf(w, q.lum, la);
-        }
-        acc[part] += sw * (double)ma;
-        acc[2 + part] += sw * (double)la;
-        __syncthreads();
-        // runs of one template within this thread's entries: one shared-memory add per run
-        const uint32_t *en = a.ent + (size_t)g * a.nent;
-        const float *ec = a.ent_c + (size_t)g * a.nent;
-        const float swf = (float)sw;
-        float *Vp = V + part * a.ntpad;
-        const int e0 = tid * per, e1 = min(e0 + per, a.nent);
-        int cur = -1;
-        float run = 0.f;
-        for (int i = e0; i < e1; ++i) {
-            const uint32_t key = __ldg(en + i);
-            const int t = (int)(key >> 16);
-            const float v = W[key & 0xffffu] * __ldg(ec + i);
-            if (t != cur) {
-                if (cur >= 0 && run != 0.f) atomicAdd(Vp + cur, run * swf);
-                cur = t;
-                run = v;
-            } else {
-                run += v;
-            }
-        }
-        if (cur >= 0 && run != 0.f) atomicAdd(Vp + cur, run * swf);
-        __syncthreads();
-    }
-    // the template weights as the GEMM's A operand rows (bf16 hi / lo): young row m, old row n + m
-    for (int i = tid; i < 2 * a.ntpad; i += OPS_THREADS) {
-        const int part = i / a.ntpad, e = i % a.ntpad;
-        const float v = V[i];
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        const size_t row = (size_t)(part == 0 ? m : a.n + m) * a.ntpad + e;
-        a.v_hi[row] = h;
-        a.v_lo[row] = __float2bfloat16_rn(v - __bfloat162float(h));
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        double v = acc[j];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        if (lane == 0) red[j][warp] = v;
+        inv_total[k] = total > 0.0 ? (float)(1.0 / total) : 1.f;
     }
     __syncthreads();
     if (tid == 0) {
-        double s[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int j = 0; j < 4; ++j)
-            for (int w = 0; w < OPS_THREADS / 32; ++w) s[j] += red[j][w];
-        double *o = a.sums + (size_t)6 * m;
-        o[0] = s[0] + s[1];
-        o[1] = s[2] + s[3];
-        o[2] = s[0]; o[3] = s[1]; o[4] = s[2]; o[5] = s[3];
+        int na = 0;
+        for (int t = 0; t < a.nt; ++t) {
+            bool any = false;
+            for (int k = 0; k < OPS_K; ++k) any = any || sw_s[t][k] != 0.f;
+            if (any) tlist[na++] = t;
+        }
+        n_active = na;
+    }
+    __syncthreads();
+    const int na = n_active;
+    // threads 0 .. 15: one FP64 accumulator each: (model k, mass / L_bol, young / old)
+    double acc = 0.0;
+    const int ak = tid >> 2, aq = (tid >> 1) & 1, ap = tid & 1;
+    float run[OPS_K];
+    // the template vectors hold one part at a time (the ages ascend: young, then old); flushed to this slab's rows
+    auto flush = [&](int part) {
+        for (int i = tid; i < nk * a.ntpad; i += OPS_THREADS) {
+            const int k = i / a.ntpad, e = i % a.ntpad;
+            a.vpart[((size_t)z * 2 * a.n + (part == 0 ? m0 + k : a.n + m0 + k)) * a.ntpad + e] = V[i];
+            V[i] = 0.f;
+        }
+    };
+    int vpart_of = -1;          // the part V holds (-1: none yet)
+    bool flushed[2] = {false, false};
+    for (int it = 0; it <= na; ++it) {
+        const int buf = it % OPS_NBUF;
+        // ---- phase A of grid point it (IMF weights into W4[buf], per-warp mass / L_bol partials into gsum[buf])
+        if (it < na) {
+            const int t = tlist[it];
+            const OpsPoint *pts = a.pts + ((size_t)t + (size_t)a.nt * z) * a.npt;
+            float4 *Wb = W4 + buf * a.npt;
+            float ma[OPS_K] = {0.f, 0.f, 0.f, 0.f}, la[OPS_K] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
+            for (int u = 0; u < OPS_PT_PER; ++u) {
+                const int p = tid + u * OPS_THREADS;
+                if (p >= a.npt) break;
+                const OpsPoint q = pts[p];
+                float w[OPS_K];
+#pragma unroll
+                for (int k = 0; k < OPS_K; ++k) {
+                    w[k] = imf_weight(kseg[k], q) * inv_total[k];
+                    ma[k] = fmaf(w[k], q.mcur, ma[k]);
+                    la[k] = fmaf(w[k], q.lum, la[k]);
+                }
+                Wb[p] = make_float4(w[0], w[1], w[2], w[3]);
+            }
+#pragma unroll
+            for (int k = 0; k < OPS_K; ++k) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    ma[k] += __shfl_xor_sync(0xffffffffu, ma[k], off);
+                    la[k] += __shfl_xor_sync(0xffffffffu, la[k], off);
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < OPS_K; ++k) { gsum[buf][warp][k][0] = ma[k]; gsum[buf][warp][k][1] = la[k]; }
+            }
+        }
+        __syncthreads();   // W4[buf] and gsum[buf] of it complete; every thread done with phase B of it - 2
+        if (it == 0) continue;
+        // ---- phase B of grid point it - 1 (reads W4[(it - 1) % OPS_NBUF], written before the previous barrier)
+        const int ip = it - 1, pb = (it - 1) % OPS_NBUF;
+        const int t = tlist[ip];
+        const int part = t < a.itesc ? 0 : 1;
+        if (part != vpart_of) {
+            if (vpart_of >= 0) {
+                __syncthreads();            // (the previous part's adds are complete; part is the same for all)
+                flush(vpart_of);
+                flushed[vpart_of] = true;
+                __syncthreads();
+            }
+            vpart_of = part;
+        }
+        const float sw[OPS_K] = {sw_s[t][0], sw_s[t][1], sw_s[t][2], sw_s[t][3]};
+        if (tid < 16 && ap == part) {
+            float s = 0.f;
+#pragma unroll
+            for (int w = 0; w < OPS_THREADS / 32; ++w) s += gsum[pb][w][ak][aq];
+            acc += (double)sw[ak] * (double)s;
+        }
+        const size_t g = (size_t)t + (size_t)a.nt * z;
+        const float4 *Wb = W4 + pb * a.npt;
+        const int e0 = tid * OPS_ENT_PER;
+        const uint32_t *en = a.ent + g * a.nent;
+        const float *ec = a.ent_c + g * a.nent;
+        uint32_t key[OPS_ENT_PER];
+        float cf[OPS_ENT_PER];
+        if (e0 + OPS_ENT_PER <= a.nent) {
+#pragma unroll
+            for (int u = 0; u < OPS_ENT_PER / 4; ++u) {
+                const uint4 kk = __ldg(reinterpret_cast<const uint4 *>(en + e0) + u);
+                const float4 cc = __ldg(reinterpret_cast<const float4 *>(ec + e0) + u);
+                key[4 * u] = kk.x; key[4 * u + 1] = kk.y; key[4 * u + 2] = kk.z; key[4 * u + 3] = kk.w;
+                cf[4 * u] = cc.x; cf[4 * u + 1] = cc.y; cf[4 * u + 2] = cc.z; cf[4 * u + 3] = cc.w;
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < OPS_ENT_PER; ++u) {
+                const bool in = e0 + u < a.nent;
+                key[u] = in ? __ldg(en + e0 + u) : 0xffffffffu;
+                cf[u] = in ? __ldg(ec + e0 + u) : 0.f;
+            }
+        }
+        float *Vp = V;
+        int cur = -1;
+#pragma unroll
+        for (int k = 0; k < OPS_K; ++k) run[k] = 0.f;
+#pragma unroll
+        for (int u = 0; u < OPS_ENT_PER; ++u) {
+            if (key[u] == 0xffffffffu) continue;
+            const int te = (int)(key[u] >> 16);
+            const float4 w4 = Wb[key[u] & 0xffffu];
+            if (te != cur) {
+                if (cur >= 0) {
+#pragma unroll
+                    for (int k = 0; k < OPS_K; ++k)
+                        if (run[k] != 0.f) atomicAdd(Vp + (size_t)k * a.ntpad + cur, run[k] * sw[k]);
+                }
+                cur = te;
+                run[0] = w4.x * cf[u]; run[1] = w4.y * cf[u]; run[2] = w4.z * cf[u]; run[3] = w4.w * cf[u];
+            } else {
+                run[0] = fmaf(w4.x, cf[u], run[0]); run[1] = fmaf(w4.y, cf[u], run[1]);
+                run[2] = fmaf(w4.z, cf[u], run[2]); run[3] = fmaf(w4.w, cf[u], run[3]);
+            }
+        }
+        if (cur >= 0) {
+#pragma unroll
+            for (int k = 0; k < OPS_K; ++k)
+                if (run[k] != 0.f) atomicAdd(Vp + (size_t)k * a.ntpad + cur, run[k] * sw[k]);
+        }
+    }
+    __syncthreads();
+    // this slab's template weights (each part once: the one held, the other zero if it had no age) and sums, read
+    // back in slab order by ops_reduce_kernel
+    if (tid == 0) a.flag[(size_t)z * ngroups + grp] = na > 0 ? 1 : 0;
+    if (na == 0) return;
+    flush(vpart_of);
+    flushed[vpart_of] = true;
+    for (int part = 0; part < 2; ++part)
+        if (!flushed[part]) flush(part);   // (V is zero after the flush above)
+    // spart (model, 4): mass young, mass old, L_bol young, L_bol old  <-  accumulator (k, quantity aq, part ap)
+    if (tid < 16 && ak < nk) a.spart[((size_t)z * a.n + m0 + ak) * 4 + 2 * aq + ap] = acc;
+}
+
+// The slabs' template weights summed in slab order, as the template GEMM's bf16 hi / lo A operand, and the sums.
+__global__ void ops_reduce_kernel(OpsFoldArgs a) {
+    const int ngroups = (a.n + OPS_K - 1) / OPS_K;
+    const size_t total = (size_t)2 * a.n * a.ntpad;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int row = (int)(i / a.ntpad);
+        const int m = row < a.n ? row : row - a.n;
+        const int grp = m / OPS_K;
+        float v = 0.f;
+        for (int z = 0; z < a.nz; ++z)
+            if (a.flag[(size_t)z * ngroups + grp]) v += a.vpart[(size_t)z * total + i];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        a.v_hi[i] = h;
+        a.v_lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+        if (i < (size_t)a.n) {
+            const int mm = (int)i, gg = mm / OPS_K;
+            double s[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int z = 0; z < a.nz; ++z)
+                if (a.flag[(size_t)z * ngroups + gg])
+                    for (int j = 0; j < 4; ++j) s[j] += a.spart[((size_t)z * a.n + mm) * 4 + j];
+            double *o = a.sums + (size_t)6 * mm;
+            o[0] = s[0] + s[1];
+            o[1] = s[2] + s[3];
+            o[2] = s[0]; o[3] = s[1]; o[4] = s[2]; o[5] = s[3];
+        }
     }
 }
 
 cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (2 * (size_t)a.ntpad + (size_t)a.npt);
+    if (a.npt > OPS_THREADS * OPS_PT_PER || a.nent > OPS_THREADS * OPS_ENT_PER) return cudaErrorInvalidValue;
+    if (a.nt > OPS_MAXT) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float4) * OPS_NBUF * (size_t)a.npt + sizeof(float) * (size_t)OPS_K * a.ntpad;
     cudaError_t e = cudaFuncSetAttribute(ops_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    ops_fold_kernel<<<a.n, OPS_THREADS, smem, st>>>(a);
+    const dim3 grid((a.n + OPS_K - 1) / OPS_K, a.nz);
+    ops_fold_kernel<<<grid, OPS_THREADS, smem, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ops_reduce_kernel<<<1024, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -360,8 +493,12 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     SspOps &o = c.ops;
     cudaStream_t st = c.stream;
     cudaError_t e;
+    const int ngroups = (n + 3) / 4;
     if ((e = c.d_vhi.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
-        (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess) {
+        (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess ||
+        (e = c.d_vpart.reserve((size_t)c.nz * 2 * n * o.ntpad)) != cudaSuccess ||
+        (e = c.d_spart.reserve((size_t)c.nz * n * 4)) != cudaSuccess ||
+        (e = c.d_vflag.reserve((size_t)c.nz * ngroups)) != cudaSuccess) {
         err = cmsg("device memory", e);
         return ST_DATA_MISSING;
     }
@@ -370,6 +507,7 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;
     fa.wz = d_wz; fa.alpha = d_alpha; fa.pts = o.pts.p; fa.ent = o.ent.p; fa.ent_c = o.ent_c.p;
     fa.v_hi = c.d_vhi.p; fa.v_lo = c.d_vlo.p; fa.sums = c.d_sums.p;
+    fa.vpart = c.d_vpart.p; fa.spart = c.d_spart.p; fa.flag = c.d_vflag.p;
     if ((e = run_ops_fold(fa, st)) != cudaSuccess) { err = cmsg("operator fold kernel", e); return ST_DATA_MISSING; }
     GemmPlan pl;
     pl.num_sms = c.num_sms;
