@@ -17,6 +17,8 @@ power-law dust (tau_V uniform 0-3), redshift uniform 0-6 with the Madau IGM, vel
   512 spectral bins, through the C API from page-locked host buffers (wall time), with its device stage times.
 * ``ssp_operator``: the IMF-free batch through the SSP operator (a Kroupa IMF per model) at B = 1024, through the C
   API, with its device stage times.
+* ``fp64_path`` / ``mixed_over_fp64``: the same workload through the plain FP64 GPU path (DGEMM age sums, every
+  later stage in FP64) at B = 65536, and the mixed path's device models/s over it.
 * ``cpu_baseline`` / ``--impl reference``: the FP64 CPU oracle (a restatement of OpenSPS's compute_csp_batch,
   the reference being Fortran with no compiler in this image) with OpenMP on all host cores, on a bounded sample.
 
@@ -231,6 +233,39 @@ def ssp_operator_measure(args, torch, barrier) -> dict | None:
                         "power-law dust, z 0-6 with IGM, smoothing 50-300 km/s, 40 filters"}
 
 
+def fp64_measure(args, torch, barrier) -> dict | None:
+    """The plain FP64 path of the same workload ("gb300_fp64": DGEMM age sums, every later stage in FP64) at B =
+    --fp64-batch through the C API: the denominator of the mixed path's speed-up (device stage times alongside)."""
+    from libopensps_gb300 import workloads
+    from libopensps_gb300.capi import Context
+    n = args.fp64_batch
+    if n <= 0:
+        return None
+    ctx = Context()
+    ctx.set_int("add_neb_emission", 1)
+    ctx.set_int("add_igm_absorption", 1)
+    ctx.set_int("gb300_fp64", 1)
+    h_wz = torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True)
+    _, params = workloads.mixed_csp(n, seed=4000, out=h_wz.numpy())
+    wz = h_wz.numpy()
+    ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    barrier()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(args.fp64_steps):
+        ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    barrier()
+    ms = (time.perf_counter() - t0) * 1e3 / args.fp64_steps
+    kt = ctx.kernel_times()
+    ctx.set_profiling(False)
+    ctx.close()
+    dev = sum(kt[:5])
+    return {"batch": n, "value": n / (ms * 1e-3), "unit": "models/s", "ms_per_step": ms, "steps": args.fp64_steps,
+            "device_ms": dev, "device_value": n / (dev * 1e-3) if dev > 0 else None,
+            "stage_ms": dict(zip(["model_params", "age_sums_dgemm_and_fp64_tail", "-", "-", "fp64_sums"], kt)),
+            "dtype": "f64"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -310,6 +345,7 @@ def run_ours(args) -> None:
     d2h = n * nb * 8 + 6 * n * 8
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
+    fp64 = fp64_measure(args, torch, barrier)
 
     # roofline of the contraction
     pk = _peaks()
@@ -342,6 +378,8 @@ def run_ours(args) -> None:
             "cpu_baseline": cpu,
             "adjoint": adjoint,
             "ssp_operator": ssp_ops,
+            "fp64_path": fp64,
+            "mixed_over_fp64": (value / fp64["device_value"]) if fp64 and fp64.get("device_value") else None,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -363,6 +401,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=10)
     ap.add_argument("--ops-batch", type=int, default=1024)
     ap.add_argument("--ops-steps", type=int, default=10)
+    ap.add_argument("--fp64-batch", type=int, default=65536)
+    ap.add_argument("--fp64-steps", type=int, default=2)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -18,8 +18,9 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_lib"
 LIB = OUT / "libopensps_gb300.so"
 SOURCES = ["capi.cu", "context.cu", "batch.cu", "csp_contract.cu", "csp_aux.cu", "band_gemm.cu", "gemm_bf16x3.cu",
-           "adjoint.cu", "noalloc.cu", "sfh.cu", "ssp_op.cu"]
+           "adjoint.cu", "noalloc.cu", "sfh.cu", "ssp_op.cu", "fp64_path.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_LIB = "/usr/local/cuda/lib64"   # cuBLAS (the plain FP64 path's DGEMM)
 
 
 def nvcc() -> str:
@@ -62,8 +63,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         objs = [o for _, o in ex.map(compile_one, SOURCES)]
     if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [cc, "-shared", "-o", str(tmp)] + [str(o) for o in objs] + ARCH + ["-lcudart_static", "-lrt",
-                                                                                   "-lpthread", "-ldl"]
+        cmd = [cc, "-shared", "-o", str(tmp)] + [str(o) for o in objs] + ARCH + [
+            "-lcudart_static", "-lrt", "-lpthread", "-ldl", "-lcublas", "-Xlinker", "-rpath=" + CUDA_LIB]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -218,14 +218,10 @@ static bool lines_floor_limited(const Context &c, double sigma_kms) {
     return true;
 }
 
-static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double line_sigma, std::string &err) {
-    union { double d; long long i; } u;
-    u.d = neb ? line_sigma : -1.0;
-    const long long key = (u.i * 31 + (long long)nacc) * 1009 + itesc;
-    auto it = c.basis_cache.find(key);
-    if (it != c.basis_cache.end()) return it->second;
+// The SSP basis (nspec x nt x nz, FP64) with the nebular lines folded into the young SSPs.
+void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<double> &b) {
     const int ns = c.nspec, nt = c.nt, nz = c.nz;
-    std::vector<double> b(c.ssp);
+    b = c.ssp;
     if (neb) {
         // the young SSPs with their lines (add_neb_emission: linear in the weights, so part of the basis)
         std::vector<double> prof;
@@ -241,7 +237,20 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
                 }
         }
     }
+}
+
+static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double line_sigma, std::string &err) {
+    union { double d; long long i; } u;
+    u.d = neb ? line_sigma : -1.0;
+    const long long key = (u.i * 31 + (long long)nacc) * 1009 + itesc;
+    auto it = c.basis_cache.find(key);
+    if (it != c.basis_cache.end()) return it->second;
+    const int ns = c.nspec, nt = c.nt, nz = c.nz;
+    std::vector<double> b;
+    line_basis_host(c, neb, line_sigma, b);
     BasisOperand *op = new BasisOperand();
+    op->neb = neb;
+    op->line_sigma = line_sigma;
     op->nacc = nacc;
     op->itesc = itesc;
     const int BK = contract_bk();
@@ -403,6 +412,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // with SSP operators on the context (opensps_context_build_ssp_ops) the age sums come from the operator applied
     // to each model's IMF; else from the resident basis, whose IMF is fixed
     const bool ops = c.ops.ready;
+    const bool fp64 = c.fp64 != 0 && !ops;
+    if (fp64 && (io.dev_inputs || io.keep_parts || io.young || io.old)) {
+        err = "the plain FP64 path computes host-input batches' outputs only (no parts, device inputs or gradients)";
+        return ST_UNSUPPORTED;
+    }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
         if (io.keep_parts) { err = "gradients with the SSP operators are not supported on this path"; return ST_UNSUPPORTED; }
@@ -549,7 +563,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.itesc = itesc;
     wa.grid = 0;
     float *d_y = c.d_young.p, *d_o = c.d_old.p;
-    if (ops) {
+    if (fp64) {
+        // ---- the plain FP64 path: DGEMM age sums, then the rest in FP64 (spectra into d_spec64, magnitudes)
+        const int rc = run_fp64_tail(c, io, bop, d_wz, d_par, nacc, any_smooth ? sm_lo : ns, any_smooth ? sm_hi : -1,
+                                     i0, err);
+        if (rc) return rc;
+        prof_mark(c, 2);
+        prof_mark(c, 3);
+        launches = 5;   // model parameters, weights gather, two DGEMMs, the FP64 tail
+    } else if (ops) {
         // ---- the operator: the IMF weights folded with the SFH weights, the template GEMM, then the epilogue
         std::vector<double> al((size_t)3 * n);
         for (int m = 0; m < n; ++m) {
@@ -614,7 +636,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
 
     // ---- bands and magnitudes
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
-    if (want_mags) {
+    if (want_mags && !fp64) {
         std::vector<int> do_band(nb, 1);
         for (int b = 0; b < nb && b < (int)c.mag_mask.size(); ++b) do_band[b] = c.mag_mask[b];
         if ((e = c.d_do_band.reserve(nb)) != cudaSuccess ||
@@ -715,7 +737,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // ---- outputs
     if (io.spec && !io.dev_inputs) {
         if ((e = c.d_spec64.reserve((size_t)n * ns)) != cudaSuccess ||
-            (e = run_spec_to_f64(c.d_spec.p, ns, ns, n, c.d_spec64.p, st)) != cudaSuccess ||
+            (!fp64 && (e = run_spec_to_f64(c.d_spec.p, ns, ns, n, c.d_spec64.p, st)) != cudaSuccess) ||
             (e = cudaMemcpyAsync(io.spec, c.d_spec64.p, sizeof(double) * n * ns, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
             err = cuda_msg("spectra copy", e);
             return ST_DATA_MISSING;

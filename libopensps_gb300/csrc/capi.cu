@@ -225,6 +225,7 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "sfh") c->sfh = value;
     else if (k == "nebemlineinspec") c->nebemlineinspec = value;
     else if (k == "zmet") c->zmet = value;
+    else if (k == "gb300_fp64") c->fp64 = value;   // extension: the plain FP64 path
     else if (k == "imf_type") c->imf_type = value;
     else if (k == "keep_maggies") c->keep_maggies = value;
     else if (k == "add_dust_emission" || k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_stellar_remnants" ||

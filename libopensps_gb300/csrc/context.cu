@@ -164,7 +164,8 @@ Context::~Context() {
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
     ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
-    d_spart.release(); d_vflag.release();
+    d_spart.release(); d_vflag.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
+    fp64_release(*this);
     if (pinned_spec) cudaFreeHost(pinned_spec);
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
@@ -303,13 +304,17 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
     // the same matrix by band for the reverse pass: each band's nonzero pixel range as a dense row, and per chunk of 32
     // pixels from j0 the first and last band reaching it
     std::vector<float> bc;
+    std::vector<double> bc64;
     std::vector<int4> bmeta(nb);
     for (int b = 0; b < nb; ++b) {
         int lo = ns, hi = -1;
         for (int j = 0; j < ns; ++j)
             if (cm[(size_t)b * ns + j] != 0.0) { lo = std::min(lo, j); hi = std::max(hi, j); }
         bmeta[b] = make_int4(lo, hi, (int)bc.size(), 0);
-        for (int j = lo; j <= hi; ++j) bc.push_back((float)cm[(size_t)b * ns + j]);
+        for (int j = lo; j <= hi; ++j) {
+            bc.push_back((float)cm[(size_t)b * ns + j]);
+            bc64.push_back(cm[(size_t)b * ns + j]);
+        }
     }
     const int nchunk = std::max(1, (j1 - j0 + 1 + 31) / 32);
     std::vector<int2> bchunk(nchunk, make_int2(1, 0));
@@ -321,10 +326,11 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
             else bchunk[k].y = b;
         }
     }
-    if (bc.empty()) bc.push_back(0.f);
+    if (bc.empty()) { bc.push_back(0.f); bc64.push_back(0.0); }
     if (bmeta.empty()) bmeta.push_back(make_int4(ns, -1, 0, 0));
     if ((e = upload(c.d_bc, bc.data(), bc.size())) != cudaSuccess ||
         (e = upload(c.d_bmeta, bmeta.data(), bmeta.size())) != cudaSuccess ||
+        (e = upload(c.d_bc64, bc64.data(), bc64.size())) != cudaSuccess ||
         (e = upload(c.d_bchunk, bchunk.data(), bchunk.size())) != cudaSuccess) {
         err = std::string("band matrix upload failed: ") + cudaGetErrorString(e);
         return ST_BAD_ARG;
@@ -421,6 +427,8 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         for (int k = 0; k < 6; ++k) igm_a[(size_t)j * 6 + k] = (float)a[k];
     }
     c.igm_a = igm_a;
+    std::vector<double> igm_a64((size_t)std::max(c.jtop, 1) * 6, 0.0);
+    for (int j = 0; j < c.jtop; ++j) igm_pixel_terms(c.lam[j], igm_a64.data() + (size_t)j * 6);
     std::vector<double> lnlam(ns);
     for (int j = 0; j < ns; ++j) lnlam[j] = std::log(c.lam[j]);
     std::vector<double> lzv(c.nz);
@@ -428,6 +436,7 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     cosmology_table(c.h0, c.om0, c.ol0, c.zt, c.dl);
     if ((e = upload(c.d_wl, wl.data(), wl.size())) != cudaSuccess ||
         (e = upload(c.d_igm_a, igm_a.data(), igm_a.size())) != cudaSuccess ||
+        (e = upload(c.d_igm_a64, igm_a64.data(), igm_a64.size())) != cudaSuccess ||
         (e = upload(c.d_lam, c.lam.data(), c.lam.size())) != cudaSuccess ||
         (e = upload(c.d_lnlam, lnlam.data(), lnlam.size())) != cudaSuccess ||
         (e = upload(c.d_mass, c.mass.data(), c.mass.size())) != cudaSuccess ||

@@ -56,13 +56,17 @@ struct BasisOperand {
     DevBuf<__nv_bfloat16> hi, lo;
     DevBuf<int> kmap;            // operand column -> source (age, metallicity) of the weights, bit 30: young
     CUtensorMap tm_hi, tm_lo;
+    bool neb = false;
+    double line_sigma = 0.0;
+    // the plain FP64 path's copy (nspec x kpad, column-major, the same K order), made on first use
+    DevBuf<double> b64;
     // the reverse pass's copy, transposed (kpad x ppad, pixels padded to ppad with zeros), made on first use
     int ppad = 0;
     DevBuf<__nv_bfloat16> thi, tlo;
     DevBuf<int> col_of;          // source index t + nt z -> operand column
     CUtensorMap tm_thi, tm_tlo;
     void release() {
-        hi.release(); lo.release(); kmap.release(); thi.release(); tlo.release(); col_of.release();
+        hi.release(); lo.release(); kmap.release(); thi.release(); tlo.release(); col_of.release(); b64.release();
     }
 };
 
@@ -92,6 +96,8 @@ struct Context {
     // settings (set_int / set_float)
     int add_neb_emission = 0, add_igm_absorption = 0, smooth_velocity = 1, dust_type = 0, compute_vega_mags = 0;
     int sfh = 0, nebemlineinspec = 1, fast_mode = 0, zmet = 1, imf_type = 2;
+    int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
+    void *cublas = nullptr;      // cublasHandle_t of the FP64 path
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];
     std::string filter_set = "gauss40";
@@ -144,6 +150,7 @@ struct Context {
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
     DevBuf<unsigned char> d_dual;
     SspOps ops;
+    DevBuf<double> d_w64, d_y64, d_bc64, d_igm_a64;
     DevBuf<double> d_alpha;
     DevBuf<__nv_bfloat16> d_vhi, d_vlo;
     DevBuf<float> d_yo, d_vpart;
@@ -203,6 +210,11 @@ struct BatchIO {
 int run_batch(Context &c, const BatchIO &io, std::string &err);
 // The SSP operator (ssp_op.cu): build from the data root, the young / old sums of a batch, one IMF's SSP grid.
 int ops_build(Context &c, std::string &err);
+// The plain FP64 path (fp64_path.cu): the age sums by DGEMM and the rest in FP64, into the host outputs of io.
+void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<double> &b);
+int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,
+                  int sm_lo, int sm_hi, int i0, std::string &err);
+void fp64_release(Context &c);
 int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, float *d_young,
                   float *d_old, std::string &err);
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
