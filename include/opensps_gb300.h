@@ -54,6 +54,59 @@ void opensps_gb300_last_launches(int handle, int *launches, int *status);
 void opensps_gb300_spec_mags_noalloc(int handle, int n, const float *d_spec, const double *d_zred, double *d_mags,
                                      int sync, int *status);
 
+/* ---- The learned emulator (no counterpart in OpenSPS, whose only network is the cue nebular MLP) ----------------
+ * An ensemble of five MLPs, 10 inputs -> 4 x 512 SiLU -> the first 64 PCA coefficients of log10 of the spectrum and
+ * the magnitudes less the distance term (bf16 weights and activations, f32 accumulation), trained on this
+ * library's own CSP through the SSP operators: a Kroupa IMF per model and the delayed-tau SFH (sfh = 4) on the
+ * device. Inputs, column-major OPENSPS_GB300_EMU_INPUTS x n doubles, in this order: tau [Gyr], tage [Gyr], logzsol,
+ * dust2, dust_index, zred, sigma_smooth [km/s], imf1, imf2, imf3. The training box: log10 tau in [-1, 1], tage in
+ * [1, 13.7], logzsol in [-2, 0.5], dust2 in [0, 3], dust_index in [-1, -0.4], zred in [0, 6], sigma_smooth in
+ * [50, 300], imf1 in [0.3, 1.8], imf2 in [1.3, 2.8], imf3 in [1.8, 3.3]. A model outside the box, or whose
+ * ensemble spread (the members' standard deviation, the largest over the bands less than 15 mag fainter than its
+ * brightest) exceeds 0.01 mag, is flagged and, with fallback, computed by the plain CSP. */
+#define OPENSPS_GB300_EMU_INPUTS 10
+#define OPENSPS_GB300_EMU_NPC 64
+
+/* Generates n_train + n_val models with the context's CSP (SSP operators built, sfh = 4, the context's other
+ * settings), fits the PCA and trains the ensemble (epochs over n_train, minibatch `batch`, a multiple of 128, per
+ * member), validates on the n_val models, writes the weights to path (unless path is NULL or empty) and leaves the
+ * emulator on the context. Progress lines go to stderr. */
+void opensps_gb300_emulator_train(int handle, const char *path, long long n_train, int n_val, int epochs, int batch,
+                                  int seed, int *status);
+/* Loads an emulator written by opensps_gb300_emulator_train (same band set and wavelength grid). */
+void opensps_gb300_emulator_load(int handle, const char *path, int *status);
+void opensps_gb300_emulator_free(int handle, int *status);
+/* Training and validation figures: n_train, n_val, epochs, batch, seed, training-set seconds, training seconds,
+ * validation RMS error [mag], maximum error, 99th percentile of the per-model maximum error, flagged fraction,
+ * maximum error of the unflagged models, the PCA's explained variance. */
+void opensps_gb300_emulator_info(int handle, double *info, int max_n, int *n, int *status);
+/* Magnitudes (nbands x n, column-major), optionally the PCA coefficients (64 x n), the spread (n) and the source
+ * of each model (0 emulator; 1 outside the box, 2 spread, 3 not finite: computed by the plain CSP when
+ * fallback != 0). *n_fallback: the flagged count. */
+void opensps_gb300_emulator_predict(int handle, int n, const double *inputs, int fallback, double *mags, double *pca,
+                                    double *spread, int *source, int *n_fallback, int *status);
+/* The ensemble on device inputs (n x OPENSPS_GB300_EMU_INPUTS floats, row-major): d_mags (n x nbands floats),
+ * d_pca (n x 64 floats, or NULL), d_spread (n floats, or NULL), d_flag (n ints), d_flagged (the flagged models'
+ * indices, at most n ints); no fallback. With n_flagged not NULL the call waits and returns the flagged count;
+ * otherwise it is asynchronous on the context's stream unless sync != 0. */
+void opensps_gb300_emulator_predict_device(int handle, int n, const float *d_inputs, float *d_mags, float *d_pca,
+                                           float *d_spread, int *d_flag, int *d_flagged, int *n_flagged, int sync,
+                                           int *status);
+/* The fallback thresholds: spread_max [mag] and the faint-band cut [mag]. */
+void opensps_gb300_emulator_set_threshold(int handle, double spread_max, double faint, int *status);
+/* An untrained ensemble with random weights (seed), for checks of the training kernels. */
+void opensps_gb300_emulator_init(int handle, int seed, int *status);
+/* Number of FP32 parameters of the ensemble: weights [w0 | wh | w4] then biases (see libopensps_gb300 docs). */
+void opensps_gb300_emulator_param_count(long long *count);
+/* Gets (set = 0) or sets (set = 1) the FP32 parameters of a trainable emulator. */
+void opensps_gb300_emulator_params(int handle, int set, float *params, int *status);
+/* The training kernels' loss (5 floats, one per member) and gradients (param_count floats) on one minibatch given
+ * as standardised network features x_std (n x 12 floats: the ten inputs' features, then the two grid clocks) and
+ * targets y_std (n x 128 floats) with output weights
+ * loss_weights (128 floats); n a multiple of 128. Every member sees the same rows. No update. */
+void opensps_gb300_emulator_grads(int handle, int n, const float *x_std, const float *y_std,
+                                  const float *loss_weights, float *loss, float *grads, int *status);
+
 #ifdef __cplusplus
 }
 #endif

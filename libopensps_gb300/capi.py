@@ -75,7 +75,26 @@ SIGNATURES = {
     "opensps_gb300_spec_mags_noalloc": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
     "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
+    "opensps_gb300_emulator_train": (None, [C.c_int, C.c_char_p, C.c_longlong, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            _ip]),
+    "opensps_gb300_emulator_load": (None, [C.c_int, C.c_char_p, _ip]),
+    "opensps_gb300_emulator_free": (None, [C.c_int, _ip]),
+    "opensps_gb300_emulator_info": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
+    "opensps_gb300_emulator_predict": (None, [C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, _dp, _ip, _ip, _ip]),
+    "opensps_gb300_emulator_predict_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_void_p, C.c_void_p, _ip, C.c_int, _ip]),
+    "opensps_gb300_emulator_set_threshold": (None, [C.c_int, C.c_double, C.c_double, _ip]),
+    "opensps_gb300_emulator_init": (None, [C.c_int, C.c_int, _ip]),
+    "opensps_gb300_emulator_param_count": (None, [C.POINTER(C.c_longlong)]),
+    "opensps_gb300_emulator_params": (None, [C.c_int, C.c_int, C.c_void_p, _ip]),
+    "opensps_gb300_emulator_grads": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, _ip]),
 }
+
+# the emulator's inputs, in the order of opensps_gb300_emulator_predict
+EMU_INPUTS = ("tau", "tage", "logzsol", "dust2", "dust_index", "zred", "sigma_smooth", "imf1", "imf2", "imf3")
+EMU_INFO = ("n_train", "n_val", "epochs", "batch", "seed", "t_generate_s", "t_train_s", "val_rms_mag",
+            "val_max_mag", "val_p99_mag", "val_flagged_frac", "val_max_unflagged_mag", "pca_explained")
 
 
 class OpenSPSError(RuntimeError):
@@ -217,13 +236,17 @@ class Context:
     # -- batches
     def csp_batch(self, params: dict, ssp_weights_z: np.ndarray | None = None, ssp_weights: np.ndarray | None = None,
                   spec: bool = True, mass: bool = True, lbol: bool = True) -> dict:
-        """compute_csp_batch_grad with no cotangents (the forward batch): weights (n, nz, nt) or (n, nt)."""
+        """compute_csp_batch_grad with no cotangents (the forward batch): weights (n, nz, nt) or (n, nt), or none
+        (the context's SFH from the parameters tage, tau, ...; n from the parameter arrays)."""
         if ssp_weights_z is not None:
             w = np.ascontiguousarray(ssp_weights_z, dtype=np.float64)
             n = w.shape[0]
-        else:
+        elif ssp_weights is not None:
             w = np.ascontiguousarray(ssp_weights, dtype=np.float64)
             n = w.shape[0]
+        else:
+            w = None
+            n = max(np.size(v) for v in params.values())
         ns, nb = self.nspec, self.nbands
         k, c_names, c_vals, keep = _names_values(params, n)
         out = {"mags": np.empty((n, nb))}
@@ -393,3 +416,104 @@ class Context:
         self.lib.opensps_gb300_kernel_times(self.handle, _ptr(buf), 10, C.byref(n), C.byref(st))
         _check(st, self.lib)
         return buf[:n.value].tolist()
+
+    # -- the learned emulator (include/opensps_gb300.h)
+    def emulator_train(self, path: str | os.PathLike | None, n_train: int = 4194304, n_val: int = 32768,
+                       epochs: int = 60, batch: int = 8192, seed: int = 1):
+        """opensps_gb300_emulator_train on this context's CSP: builds the SSP operators and sets sfh = 4 first."""
+        if not self.has_ssp_ops:
+            self.build_ssp_ops()
+        self.set_int("sfh", 4)
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_train(self.handle, str(path).encode() if path else None, n_train, n_val,
+                                              epochs, batch, seed, C.byref(st))
+        _check(st, self.lib)
+
+    def emulator_load(self, path: str | os.PathLike):
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_load(self.handle, str(path).encode(), C.byref(st))
+        _check(st, self.lib)
+
+    def emulator_free(self):
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_free(self.handle, C.byref(st))
+        _check(st, self.lib)
+
+    def emulator_info(self) -> dict:
+        buf, n, st = np.zeros(32), C.c_int(0), C.c_int(0)
+        self.lib.opensps_gb300_emulator_info(self.handle, _ptr(buf), 32, C.byref(n), C.byref(st))
+        _check(st, self.lib)
+        return dict(zip(EMU_INFO, buf[:n.value].tolist()))
+
+    def emulator_set_threshold(self, spread_max: float = 0.01, faint: float = 15.0):
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_set_threshold(self.handle, spread_max, faint, C.byref(st))
+        _check(st, self.lib)
+
+    def emulator_predict(self, inputs: dict | np.ndarray, fallback: bool = True, pca: bool = False) -> dict:
+        """opensps_gb300_emulator_predict. inputs: a dict of the EMU_INPUTS arrays or an (n, 10) array. Returns mags
+        (n, nbands), spread (n,), source (n,) and n_fallback (and pca (n, 64))."""
+        if isinstance(inputs, dict):
+            x = np.stack([np.asarray(inputs[k], dtype=np.float64) for k in EMU_INPUTS], axis=1)
+        else:
+            x = np.asarray(inputs, dtype=np.float64)
+        x = np.ascontiguousarray(x)
+        n, nb = x.shape[0], self.nbands
+        out = {"mags": np.empty((n, nb)), "spread": np.empty(n), "source": np.empty(n, dtype=np.int32)}
+        if pca:
+            out["pca"] = np.empty((n, 64))
+        nf, st = C.c_int(0), C.c_int(0)
+        self.lib.opensps_gb300_emulator_predict(self.handle, n, _ptr(x), 1 if fallback else 0, _ptr(out["mags"]),
+                                                _ptr(out.get("pca")), _ptr(out["spread"]),
+                                                out["source"].ctypes.data_as(_ip), C.byref(nf), C.byref(st))
+        _check(st, self.lib)
+        out["n_fallback"] = nf.value
+        return out
+
+    def emulator_predict_device(self, n: int, d_inputs: int, d_mags: int, d_flag: int, d_flagged: int,
+                                d_pca: int = 0, d_spread: int = 0, count: bool = True, sync: bool = True) -> int:
+        """opensps_gb300_emulator_predict_device on device pointers (integers); returns the flagged count (or -1)."""
+        nf, st = C.c_int(0), C.c_int(0)
+        self.lib.opensps_gb300_emulator_predict_device(self.handle, n, C.c_void_p(d_inputs), C.c_void_p(d_mags),
+                                                       C.c_void_p(d_pca or None), C.c_void_p(d_spread or None),
+                                                       C.c_void_p(d_flag), C.c_void_p(d_flagged),
+                                                       C.byref(nf) if count else None, 1 if sync else 0, C.byref(st))
+        _check(st, self.lib)
+        return nf.value if count else -1
+
+    def emulator_init(self, seed: int = 0):
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_init(self.handle, seed, C.byref(st))
+        _check(st, self.lib)
+
+    def emulator_param_count(self) -> int:
+        v = C.c_longlong(0)
+        self.lib.opensps_gb300_emulator_param_count(C.byref(v))
+        return v.value
+
+    def emulator_params(self, values: np.ndarray | None = None) -> np.ndarray:
+        """Gets (values None) or sets the FP32 parameters [w0 | wh | w4 | bias]."""
+        st = C.c_int(0)
+        if values is None:
+            buf = np.empty(self.emulator_param_count(), dtype=np.float32)
+            self.lib.opensps_gb300_emulator_params(self.handle, 0, C.c_void_p(buf.ctypes.data), C.byref(st))
+            _check(st, self.lib)
+            return buf
+        buf = np.ascontiguousarray(values, dtype=np.float32)
+        self.lib.opensps_gb300_emulator_params(self.handle, 1, C.c_void_p(buf.ctypes.data), C.byref(st))
+        _check(st, self.lib)
+        return buf
+
+    def emulator_grads(self, x_std: np.ndarray, y_std: np.ndarray, loss_weights: np.ndarray):
+        """opensps_gb300_emulator_grads: (loss (5,), grads (param_count,)) of the training kernels on one minibatch."""
+        x = np.ascontiguousarray(x_std, dtype=np.float32)
+        y = np.ascontiguousarray(y_std, dtype=np.float32)
+        w = np.ascontiguousarray(loss_weights, dtype=np.float32)
+        loss = np.zeros(5, dtype=np.float32)
+        g = np.zeros(self.emulator_param_count(), dtype=np.float32)
+        st = C.c_int(0)
+        self.lib.opensps_gb300_emulator_grads(self.handle, x.shape[0], C.c_void_p(x.ctypes.data),
+                                              C.c_void_p(y.ctypes.data), C.c_void_p(w.ctypes.data),
+                                              C.c_void_p(loss.ctypes.data), C.c_void_p(g.ctypes.data), C.byref(st))
+        _check(st, self.lib)
+        return loss, g

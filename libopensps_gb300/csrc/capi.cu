@@ -20,6 +20,17 @@ int run_grad_batch(Context &c, const BatchIO &io, const double *mags_bar, const 
                    double *weights_z_bar, double *weights_bar, std::string &err);
 int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zred, double *d_mags, bool sync,
                      std::string &err);
+int emu_train(Context &c, long long n_train, int n_val, int epochs, int batch, int seed, const std::string &path,
+              std::string &err);
+int emu_load(Context &c, const std::string &path, std::string &err);
+int emu_predict(Context &c, int n, const double *inputs, int fallback, double *mags, double *pca, double *spread,
+                int *source, int *n_fallback, std::string &err);
+int emu_infer_device(Context &c, int n, const float *d_x, float *d_mags, float *d_coef, float *d_spread, int *d_flag,
+                     int *d_nflag, int *d_flagged, std::string &err);
+int emu_init(Context &c, int seed, std::string &err);
+int emu_params(Context &c, int set, float *host, std::string &err);
+int emu_grads(Context &c, int n, const float *x_std, const float *y_std, const float *lossw, float *loss, float *grads,
+              std::string &err);
 }  // namespace sps
 
 using namespace sps;
@@ -68,43 +79,46 @@ int build_params(Context &c, int n, int n_params, const char *const *names, cons
     return 0;
 }
 
-// The common body of the batch entry points.
-void batch_entry(int handle, int n, int n_params, const char *const *names, const double *const *values,
-                 const double *ssp_weights, const double *ssp_weights_z, const double *zred_mags,
-                 const double *mags_bar, const double *spec_bar, const double *mass_bar, const double *lbol_bar,
-                 double *mags, double *spec, double *mass, double *lbol, double *mdust, double *sfr, double *emlines,
-                 double *indx, double *young, double *old, double *mass_young, double *mass_old, double *lbol_young,
-                 double *lbol_old, double *params_bar, int params_bar_rows, double *weights_bar,
-                 double *weights_z_bar, int *status) {
-    if (!status) return;
-    *status = 0;
-    Context *c = lookup(handle);
-    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
-    std::lock_guard<std::mutex> lk(c->mu);
-    if (n <= 0) return;
-    if (params_bar && params_bar_rows < OPENSPS_NBGRAD)
-        return fail(status, ST_BAD_ARG, "compute_csp_batch_grad: params_bar has " + std::to_string(params_bar_rows) +
-                                            " rows, the library writes " + std::to_string(OPENSPS_NBGRAD) +
-                                            " (opensps_get_nbgrad)");
-    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
-    if (!mags && !c->fast_mode) return fail(status, ST_BAD_ARG, "mags is required");
-    if (indx) return fail(status, ST_UNSUPPORTED, "spectral indices are not computed on this path");
-    if (zred_mags) return fail(status, ST_UNSUPPORTED, "zred_mags is not supported on this path");
-    std::string err;
+
+}  // namespace
+
+namespace sps {
+// The common body of the batch entry points, on a context the caller has locked: 0 or a status (err).
+int batch_core(Context &cref, int n, int n_params, const char *const *names, const double *const *values,
+               const double *ssp_weights, const double *ssp_weights_z, const double *zred_mags,
+               const double *mags_bar, const double *spec_bar, const double *mass_bar, const double *lbol_bar,
+               double *mags, double *spec, double *mass, double *lbol, double *mdust, double *sfr, double *emlines,
+               double *indx, double *young, double *old, double *mass_young, double *mass_old, double *lbol_young,
+               double *lbol_old, double *params_bar, int params_bar_rows, double *weights_bar,
+               double *weights_z_bar, std::string &err) {
+    Context *c = &cref;
+    if (n <= 0) return 0;
+    if (params_bar && params_bar_rows < OPENSPS_NBGRAD) {
+        err = "compute_csp_batch_grad: params_bar has " + std::to_string(params_bar_rows) + " rows, the library writes " +
+              std::to_string(OPENSPS_NBGRAD) + " (opensps_get_nbgrad)";
+        return ST_BAD_ARG;
+    }
+    if (!c->is_setup) { err = "context not set up"; return ST_NOT_SETUP; }
+    if (!mags && !c->fast_mode) { err = "mags is required"; return ST_BAD_ARG; }
+    if (indx) { err = "spectral indices are not computed on this path"; return ST_UNSUPPORTED; }
+    if (zred_mags) { err = "zred_mags is not supported on this path"; return ST_UNSUPPORTED; }
     std::vector<double> rows;
     int st = build_params(*c, n, n_params, names, values, rows, err);
-    if (st) return fail(status, st, err);
+    if (st) return st;
     // weights: the caller's over ages and metallicities, or over ages (blended at logzsol on the device), or the
     // SFH's (formed on the device, then blended)
     std::vector<double> sfhp;
     if (!ssp_weights_z) {
         if (!ssp_weights) {
-            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4)
-                return fail(status, ST_UNSUPPORTED, "sfh = " + std::to_string(c->sfh) +
-                                                        ": only 0 (SSP), 1 (tau) and 4 (delayed tau) on this path");
+            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4) {
+                err = "sfh = " + std::to_string(c->sfh) + ": only 0 (SSP), 1 (tau) and 4 (delayed tau) on this path";
+                return ST_UNSUPPORTED;
+            }
             for (int m = 0; m < n; ++m)
-                if (!(rows[(size_t)PF_COUNT * m + PF_TAGE] > 0.0))
-                    return fail(status, ST_UNSUPPORTED, "models with tage <= 0 are not supported");
+                if (!(rows[(size_t)PF_COUNT * m + PF_TAGE] > 0.0)) {
+                    err = "models with tage <= 0 are not supported";
+                    return ST_UNSUPPORTED;
+                }
         }
         sfhp.resize((size_t)SFH_NCOL * n);
         const int ids[SFH_NCOL] = {PF_TAGE, PF_TAU, PF_CONST, PF_FBURST, PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_LOGZSOL};
@@ -127,7 +141,38 @@ void batch_entry(int handle, int n, int n_params, const char *const *names, cons
     } else {
         st = run_batch(*c, io, err);
     }
-    if (st) return fail(status, st, err);
+    return st;
+}
+
+// A forward batch with the SFH (or the context's defaults) for magnitudes only; the caller holds the lock.
+int csp_batch_mags(Context &c, int n, int n_params, const char *const *names, const double *const *values,
+                   double *mags, std::string &err) {
+    return batch_core(c, n, n_params, names, values, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      mags, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, nullptr, 0, nullptr, nullptr, err);
+}
+}  // namespace sps
+
+namespace {
+
+void batch_entry(int handle, int n, int n_params, const char *const *names, const double *const *values,
+                 const double *ssp_weights, const double *ssp_weights_z, const double *zred_mags,
+                 const double *mags_bar, const double *spec_bar, const double *mass_bar, const double *lbol_bar,
+                 double *mags, double *spec, double *mass, double *lbol, double *mdust, double *sfr, double *emlines,
+                 double *indx, double *young, double *old, double *mass_young, double *mass_old, double *lbol_young,
+                 double *lbol_old, double *params_bar, int params_bar_rows, double *weights_bar,
+                 double *weights_z_bar, int *status) {
+    if (!status) return;
+    *status = 0;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::string err;
+    const int st = batch_core(*c, n, n_params, names, values, ssp_weights, ssp_weights_z, zred_mags, mags_bar,
+                              spec_bar, mass_bar, lbol_bar, mags, spec, mass, lbol, mdust, sfr, emlines, indx, young,
+                              old, mass_young, mass_old, lbol_young, lbol_old, params_bar, params_bar_rows,
+                              weights_bar, weights_z_bar, err);
+    if (st) fail(status, st, err);
 }
 
 }  // namespace
@@ -547,6 +592,97 @@ void opensps_gb300_last_launches(int handle, int *launches, int *status) {
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
     if (launches) *launches = c->last_launches;
     if (status) *status = 0;
+}
+
+// ---------------------------------------------------------------------------------------------- the emulator
+#define EMU_ENTRY_PROLOGUE()                                                          \
+    Context *c = lookup(handle);                                                      \
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");             \
+    std::lock_guard<std::mutex> lk(c->mu);                                            \
+    if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");        \
+    std::string err;                                                                  \
+    if (status) *status = 0;
+
+void opensps_gb300_emulator_train(int handle, const char *path, long long n_train, int n_val, int epochs, int batch,
+                                  int seed, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (int st = emu_train(*c, n_train, n_val, epochs, batch, seed, path ? path : "", err)) fail(status, st, err);
+}
+
+void opensps_gb300_emulator_load(int handle, const char *path, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (!path) return fail(status, ST_BAD_ARG, "NULL path");
+    if (int st = emu_load(*c, path, err)) fail(status, st, err);
+}
+
+void opensps_gb300_emulator_free(int handle, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    c->emu.release();
+}
+
+void opensps_gb300_emulator_info(int handle, double *info, int max_n, int *n, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (!c->emu.ready) return fail(status, ST_NO_OPERATOR, "no emulator on the context");
+    int k = 0;
+    for (; k < (int)c->emu.info.size() && k < max_n; ++k)
+        if (info) info[k] = c->emu.info[k];
+    if (n) *n = k;
+}
+
+void opensps_gb300_emulator_predict(int handle, int n, const double *inputs, int fallback, double *mags, double *pca,
+                                    double *spread, int *source, int *n_fallback, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (int st = emu_predict(*c, n, inputs, fallback, mags, pca, spread, source, n_fallback, err)) fail(status, st, err);
+}
+
+void opensps_gb300_emulator_predict_device(int handle, int n, const float *d_inputs, float *d_mags, float *d_pca,
+                                           float *d_spread, int *d_flag, int *d_flagged, int *n_flagged, int sync,
+                                           int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (n <= 0) { if (n_flagged) *n_flagged = 0; return; }
+    if (!d_inputs || !d_mags || !d_flag || !d_flagged) return fail(status, ST_BAD_ARG, "NULL device array");
+    if (!c->emu.d_nflag && cudaMalloc(&c->emu.d_nflag, sizeof(int)) != cudaSuccess)
+        return fail(status, ST_DATA_MISSING, "device memory");
+    if (int st = emu_infer_device(*c, n, d_inputs, d_mags, d_pca, d_spread, d_flag, c->emu.d_nflag, d_flagged, err))
+        return fail(status, st, err);
+    if (n_flagged || sync) {
+        int s = 0, nf = 0;
+        cudaMemcpyAsync(&s, c->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        cudaMemcpyAsync(&nf, c->emu.d_nflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+        const cudaError_t e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return fail(status, ST_DATA_MISSING, std::string("emulator: ") + cudaGetErrorString(e));
+        if (s != 0) return fail(status, ST_DATA_MISSING, "emulator kernel gave up waiting");
+        if (n_flagged) *n_flagged = nf;
+    }
+}
+
+void opensps_gb300_emulator_set_threshold(int handle, double spread_max, double faint, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (!(spread_max > 0.0) || !(faint > 0.0)) return fail(status, ST_BAD_ARG, "thresholds must be positive");
+    c->emu.spread_max = (float)spread_max;
+    c->emu.faint = (float)faint;
+}
+
+void opensps_gb300_emulator_init(int handle, int seed, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (int st = emu_init(*c, seed, err)) fail(status, st, err);
+}
+
+void opensps_gb300_emulator_param_count(long long *count) {
+    if (count) *count = emu_param_count();
+}
+
+void opensps_gb300_emulator_params(int handle, int set, float *params, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (!params) return fail(status, ST_BAD_ARG, "NULL params");
+    if (int st = emu_params(*c, set, params, err)) fail(status, st, err);
+}
+
+void opensps_gb300_emulator_grads(int handle, int n, const float *x_std, const float *y_std,
+                                  const float *loss_weights, float *loss, float *grads, int *status) {
+    EMU_ENTRY_PROLOGUE();
+    if (!x_std || !y_std || !loss_weights || !loss || !grads) return fail(status, ST_BAD_ARG, "NULL argument");
+    if (int st = emu_grads(*c, n, x_std, y_std, loss_weights, loss, grads, err)) fail(status, st, err);
 }
 
 }  // extern "C"

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 #include "csp_kernels.h"
+#include "emulator.h"
 
 namespace sps {
 
@@ -150,6 +151,7 @@ struct Context {
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
     DevBuf<unsigned char> d_dual;
     SspOps ops;
+    Emulator emu;                // the learned emulator (emulator.cu, emulator_train.cu)
     DevBuf<double> d_w64, d_y64, d_bc64, d_igm_a64;
     DevBuf<double> d_alpha;
     DevBuf<__nv_bfloat16> d_vhi, d_vlo;
@@ -224,5 +226,7 @@ void prof_mark(Context &c, int k);
 
 cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
                                 uint32_t box_outer);
+cudaError_t encode_tmap_2d_16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
+                              uint32_t box_outer, bool f16);
 
 }  // namespace sps

@@ -138,6 +138,10 @@ struct GemmArgs {
     int M, N, K, ldd, b_row0;
     float *D;
     int *status;
+    int groups = 1, ksplit = 1;                  // see gemm_bf16x3.cu: groups of rows, partial sums over K splits
+    long long a_grp = 0, b_grp = 0;              // rows between the groups' A / B operands
+    long long d_grp = 0, d_split = 0;            // elements between the groups' / splits' D
+    int f16 = 0;                                 // one-product kind: operands f16 (else bf16)
 };
 struct GemmPlan {
     CUtensorMap tm_a_hi, tm_a_lo, tm_b_hi, tm_b_lo;
@@ -146,7 +150,8 @@ struct GemmPlan {
 int gemm_bk();
 int gemm_bm();
 int gemm_bn();
-cudaError_t run_gemm_bf16x3(const GemmPlan &pl, const GemmArgs &g, cudaStream_t st);
+cudaError_t run_gemm_bf16x3(const GemmPlan &pl, const GemmArgs &g, cudaStream_t st);   // three products (hi / lo)
+cudaError_t run_gemm_bf16(const GemmPlan &pl, const GemmArgs &g, cudaStream_t st);     // one product (hi only)
 
 // The reverse pass per model (adjoint.cu): from the forward's young / old sums, band fluxes and the cotangents, the
 // cotangents of the young and old sums (bf16 hi / lo operands of the weight GEMM) and the parameter gradients.

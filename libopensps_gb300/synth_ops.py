@@ -5,7 +5,8 @@ available here. This dataset stands in for them with the shapes of the operator 
 2000 spectra on a grid of 50 effective temperatures (log-uniform 2500 .. 50000 K) x 40 surface gravities (0 .. 5),
 and, for each of the 107 ages x 12 metallicities of the SSP grid, 1500 isochrone points with initial masses
 log-uniform in [0.08, 100] M_sun, each mapped bilinearly (in log Teff and log g) to 4 library entries, about 7.7M
-operator entries in all.
+operator entries in all. The 1500 stars (masses, giant temperatures, scatter) are one seeded draw shared by every
+grid point, so that the points move smoothly with age and metallicity as on real isochrones.
 
 Contents of ``<root>/ssp_op/`` (little-endian; grid point g = age + 107 metallicity):
 
@@ -37,7 +38,7 @@ NPT = 1500
 TEFF_LO, TEFF_HI = 2500.0, 50000.0
 LOGG_LO, LOGG_HI = 0.0, 5.0
 M_LO, M_HI = 0.08, 100.0
-VERSION = 1
+VERSION = 2
 
 
 def _library(rng: np.random.Generator, lam: np.ndarray) -> np.ndarray:
@@ -65,15 +66,18 @@ def _library(rng: np.random.Generator, lam: np.ndarray) -> np.ndarray:
 def _points(rng: np.random.Generator, log_age: np.ndarray, logz: np.ndarray):
     nt, nz = log_age.size, logz.size
     lt_lo, lt_hi = np.log10(TEFF_LO), np.log10(TEFF_HI)
-    mini = np.sort(10.0 ** rng.uniform(np.log10(M_LO), np.log10(M_HI), size=(nz, nt, NPT)), axis=2)
+    # one set of stars for every grid point (the masses, the giants' temperatures and the scatter): as a real
+    # isochrone set, the points then move smoothly with age and metallicity
+    shape = (nz, nt, NPT)
+    mini = np.broadcast_to(np.sort(10.0 ** rng.uniform(np.log10(M_LO), np.log10(M_HI), size=NPT)), shape).copy()
     lm = np.log10(mini)
     mto = 10.0 ** (-0.4 * (log_age - 10.0))[None, :, None] * np.ones_like(mini)
     ms = mini <= mto
-    u = rng.uniform(size=mini.shape)
+    u = np.broadcast_to(rng.uniform(size=NPT), shape)
     logt = np.where(ms, 3.76 + 0.55 * lm - 0.03 * logz[:, None, None], 3.62 + 0.1 * u)
     logg = np.where(ms, 4.44 - 0.55 * lm, 1.5 - np.log10(mini / mto))
-    logt = logt + 0.01 * rng.standard_normal(mini.shape)
-    logg = logg + 0.05 * rng.standard_normal(mini.shape)
+    logt = logt + 0.01 * np.broadcast_to(rng.standard_normal(NPT), shape)
+    logg = logg + 0.05 * np.broadcast_to(rng.standard_normal(NPT), shape)
     lum = np.where(ms, mini ** 3.5, 100.0 * mto ** 2.5)
     mcur = np.where(ms, mini, 0.6 * mto ** 0.9)
     # bilinear position on the library grid (log Teff, log g), clamped to it

@@ -1,0 +1,174 @@
+"""The learned emulator (include/opensps_gb300.h): its training kernels' loss and gradients and its fused inference
+kernel against the CPU MLP oracle (oracle/mlp_oracle.py); the fallback to the plain CSP; a short training run end
+to end (training set from the CSP, PCA, training, weights file, reload).
+
+Tolerances: losses and gradients <= 1e-2 relative (L2 over each tensor) and inference outputs <= 2e-2 absolute in
+standardised units (median <= 2e-3): the device and the oracle round to bf16 at the same points and differ only by
+f32 against f64 sums and the hardware tanh, which flip an occasional bf16 rounding.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BOX_LO = np.array([0.1, 1.0, -2.0, 0.0, -1.0, 0.0, 50.0, 0.3, 1.3, 1.8])     # the training box (raw values)
+BOX_HI = np.array([10.0, 13.7, 0.5, 3.0, -0.4, 6.0, 300.0, 1.8, 2.8, 3.3])
+
+
+def features(x):
+    """The network's features of the inputs: log10 tau, log10 tage, log10(1 + zred), the others as they are."""
+    v = np.array(x, dtype=np.float32).astype(np.float64)
+    v[..., 0] = np.log10(v[..., 0])
+    v[..., 1] = np.log10(v[..., 1])
+    v[..., 5] = np.log10(1.0 + v[..., 5])
+    return v
+
+
+def standardise(x, ctx):
+    """The twelve standardised features (emu_features): the ten inputs', then the log-age and log-Z grid clocks."""
+    flo, fhi = features(BOX_LO), features(BOX_HI)
+    f = np.empty((x.shape[0], 12))
+    f[:, :10] = (features(x) - 0.5 * (flo + fhi)) * (2.0 / (fhi - flo))
+    la = ctx.ages()
+    lz = np.log10(ctx.zlegend() / 0.0142)
+    age = np.maximum(x[:, 1] - 2.0 * x[:, 0], 0.5 * x[:, 1])
+    da = (9.0 + np.log10(age) - la[0]) / ((la[-1] - la[0]) / (la.size - 1))
+    dz = (x[:, 2] - lz[0]) / ((lz[-1] - lz[0]) / (lz.size - 1))
+    f[:, 10] = (np.abs(np.sin(np.pi * da)) - 0.5) * 2.0
+    f[:, 11] = (np.abs(np.sin(np.pi * dz)) - 0.5) * 2.0
+    return f
+
+
+def draw_inputs(n, seed, zred=None):
+    rng = np.random.default_rng(seed)
+    u = BOX_LO + (BOX_HI - BOX_LO) * rng.uniform(size=(n, 10))
+    u[:, 0] = 10.0 ** rng.uniform(np.log10(BOX_LO[0]), np.log10(BOX_HI[0]), size=n)
+    if zred is not None:
+        u[:, 5] = zred
+    return u
+
+
+@pytest.fixture(scope="module")
+def ectx(data, built_lib):
+    from libopensps_gb300.capi import Context
+    c = Context()
+    c.set_int("add_igm_absorption", 1)
+    c.build_ssp_ops()
+    c.set_int("sfh", 4)
+    yield c
+    c.close()
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_training_gradients_match_oracle(ectx):
+    from oracle import mlp_oracle as mo
+    ectx.emulator_init(seed=3)
+    p = ectx.emulator_params()
+    rng = np.random.default_rng(4)
+    n = 256
+    x = rng.uniform(-1.0, 1.0, size=(n, 12))
+    y = rng.normal(size=(n, 128))
+    w = np.zeros(128)
+    w[:64 + ectx.nbands] = 1.0
+    y[:, 64 + ectx.nbands:] = 0.0
+    loss, g = ectx.emulator_grads(x, y, w)
+    ref_loss, ref_g = mo.loss_and_grads(p, x.astype(np.float32).astype(np.float64), y.astype(np.float32), w)
+    np.testing.assert_allclose(loss, ref_loss, rtol=1e-2)
+    H, K, NO, M = mo.H, mo.KIN, mo.NOUT, mo.MEMBERS
+    segs = {"w0": M * H * K, "wh0": M * H * H, "wh1": M * H * H, "wh2": M * H * H, "w4": M * NO * H, "bias": M * mo.NBIAS}
+    o = 0
+    for name, size in segs.items():
+        e = rel_l2(g[o:o + size].astype(np.float64), ref_g[o:o + size])
+        assert e <= 1e-2, f"{name}: relative L2 error {e:.2e}"
+        o += size
+    assert o == g.size
+
+
+def test_inference_kernel_matches_oracle(ectx):
+    from oracle import mlp_oracle as mo
+    ectx.emulator_init(seed=5)
+    p = ectx.emulator_params()
+    n, nb = 300, ectx.nbands                     # three tiles, the last partial
+    x = draw_inputs(n, seed=6, zred=0.0)         # z = 0: no distance term
+    got = ectx.emulator_predict(x, fallback=False, pca=True)
+    outs = mo.ensemble(p, standardise(x, ectx).astype(np.float32).astype(np.float64))     # (5, n, 128)
+    mean = outs.mean(axis=0)
+    spread = outs[:, :, 64:64 + nb].std(axis=0)
+    for key, ref in (("mags", mean[:, 64:64 + nb]), ("pca", mean[:, :64])):
+        d = np.abs(got[key] - ref)
+        assert float(d.max()) <= 2e-2, f"{key}: max {d.max():.3e}"
+        assert float(np.median(d)) <= 2e-3, f"{key}: median {np.median(d):.3e}"
+    mmin = mean[:, 64:64 + nb].min(axis=1, keepdims=True)
+    ref_spread = np.where(mean[:, 64:64 + nb] < mmin + 15.0, spread, 0.0).max(axis=1)
+    assert float(np.max(np.abs(got["spread"] - ref_spread))) <= 2e-2
+
+
+def test_outside_the_box_and_spread_fall_back_to_the_csp(ectx):
+    ectx.emulator_init(seed=7)                   # untrained: most models flagged by their spread
+    x = draw_inputs(64, seed=8)
+    x[:8, 1] = 14.0                              # tage outside the box
+    x[8:12, 5] = 6.5                             # zred outside the box
+    got = ectx.emulator_predict(x, fallback=True)
+    assert np.all(got["source"][:12] == 1)
+    flagged = got["source"] != 0
+    assert got["n_fallback"] == int(flagged.sum())
+    from libopensps_gb300.capi import EMU_INPUTS
+    ref = ectx.csp_batch({k: x[flagged, i] for i, k in enumerate(EMU_INPUTS)})
+    # the same CSP batch; the operator fold's shared-memory float atomics make repeated runs differ at FP32 rounding
+    np.testing.assert_allclose(got["mags"][flagged], ref["mags"], rtol=0, atol=1e-6)
+
+
+def test_training_end_to_end(ectx, tmp_path):
+    path = tmp_path / "emu.bin"
+    ectx.emulator_train(path, n_train=8192, n_val=1024, epochs=3, batch=1024, seed=9)
+    info = ectx.emulator_info()
+    assert info["n_train"] == 8192 and info["epochs"] == 3
+    assert 0.5 < info["pca_explained"] <= 1.0 + 1e-9
+    assert np.isfinite(info["val_rms_mag"])
+    x = draw_inputs(500, seed=10)
+    before = ectx.emulator_predict(x, fallback=False, pca=True)
+    ectx.emulator_free()
+    ectx.emulator_load(path)
+    after = ectx.emulator_predict(x, fallback=False, pca=True)
+    for k in ("mags", "pca", "spread", "source"):
+        np.testing.assert_array_equal(before[k], after[k])
+
+
+def test_trained_emulator_accuracy_fallback_and_gain(ectx):
+    """The shipped ensemble against the plain CSP on models it was not trained on: the emulated models' magnitudes
+    (bands less than 15 mag fainter than the model's brightest) within 0.01 mag for at least 99% of them, at most
+    5% routed to the CSP, the routed ones equal to the CSP's, and the emulator at least 10x faster than the CSP on
+    the same models (the speed-up the network buys; both timed end to end from host arrays)."""
+    import time
+    from libopensps_gb300.capi import EMU_INPUTS
+    from libopensps_gb300.emulator import WEIGHTS
+    if not WEIGHTS.exists():
+        pytest.skip("no trained weights file")
+    ectx.emulator_load(WEIGHTS)
+    ectx.emulator_set_threshold(0.01, 15.0)
+    n = 4096
+    x = draw_inputs(n, seed=2024)
+    params = {k: x[:, i] for i, k in enumerate(EMU_INPUTS)}
+    ectx.emulator_predict(x[:256], fallback=False)           # warm-up
+    ectx.csp_batch({k: v[:256] for k, v in params.items()}, spec=False)
+    t0 = time.perf_counter()
+    emu = ectx.emulator_predict(x, fallback=False)
+    t_emu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    csp = ectx.csp_batch(params, spec=False)
+    t_csp = time.perf_counter() - t0
+    ref = csp["mags"]
+    mmin = np.min(np.where(np.isfinite(ref), ref, np.inf), axis=1, keepdims=True)
+    gate = np.isfinite(ref) & (ref < mmin + 15.0)
+    err = np.where(gate, np.abs(emu["mags"] - ref), 0.0).max(axis=1)
+    ok = emu["source"] == 0
+    assert ok.mean() >= 0.95, f"routed to the CSP: {1 - ok.mean():.3f}"
+    assert float(np.mean(err[ok] <= 0.01)) >= 0.99, f"within 0.01 mag: {np.mean(err[ok] <= 0.01):.4f}"
+    assert float(err[ok].max()) <= 0.05
+    both = ectx.emulator_predict(x, fallback=True)
+    np.testing.assert_allclose(both["mags"][~ok], ref[~ok], rtol=0, atol=1e-6)
+    np.testing.assert_array_equal(both["mags"][ok], emu["mags"][ok])
+    assert t_csp / t_emu >= 10.0, f"emulator {t_emu * 1e3:.1f} ms, CSP {t_csp * 1e3:.1f} ms"
