@@ -266,6 +266,98 @@ def fp64_measure(args, torch, barrier) -> dict | None:
             "dtype": "f64"}
 
 
+def emulator_measure(args, torch, barrier) -> dict | None:
+    """The learned emulator (the shipped five-member ensemble) at B = --emu-batch: inputs drawn over its training box
+    (seed 77). Device-resident timing of the fused inference kernel (CUDA events on the library's stream; inputs
+    42 MB, outputs 0.44 GB per step: larger than L2), the flagged fraction (ensemble spread > 0.01 mag or outside the
+    box), end to end through the C API from host arrays with the flagged models computed by the plain CSP, the
+    accuracy against the plain CSP on a 4096-model sample, and the plain CSP of the same physics (the SSP operator
+    with the IMF per model, the delayed-tau SFH) on 65536 of the models."""
+    from libopensps_gb300.capi import EMU_INPUTS
+    from libopensps_gb300.emulator import WEIGHTS, training_context
+    n = args.emu_batch
+    if n <= 0 or not WEIGHTS.exists():
+        return None
+    ctx = training_context()
+    ctx.emulator_load(WEIGHTS)
+    ctx.emulator_set_threshold(0.01, 15.0)
+    lo = np.array([0.1, 1.0, -2.0, 0.0, -1.0, 0.0, 50.0, 0.3, 1.3, 1.8])
+    hi = np.array([10.0, 13.7, 0.5, 3.0, -0.4, 6.0, 300.0, 1.8, 2.8, 3.3])
+    rng = np.random.default_rng(77)
+    x = lo + (hi - lo) * rng.uniform(size=(n, 10))
+    x[:, 0] = 10.0 ** rng.uniform(-1.0, 1.0, size=n)
+    nb = ctx.nbands
+    dev = torch.device("cuda")
+    d_x = torch.from_numpy(x.astype(np.float32)).to(dev)
+    d_mags = torch.empty((n, nb), dtype=torch.float32, device=dev)
+    d_pca = torch.empty((n, 64), dtype=torch.float32, device=dev)
+    d_spread = torch.empty(n, dtype=torch.float32, device=dev)
+    d_flag = torch.empty(n, dtype=torch.int32, device=dev)
+    d_flagged = torch.empty(n, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+
+    def call(count=False):
+        return ctx.emulator_predict_device(n, d_x.data_ptr(), d_mags.data_ptr(), d_flag.data_ptr(),
+                                           d_flagged.data_ptr(), d_pca.data_ptr(), d_spread.data_ptr(),
+                                           count=count, sync=False)
+
+    nflag = call(count=True)
+    for _ in range(max(args.warmup, 3)):
+        call()
+    st = torch.cuda.ExternalStream(ctx.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.emu_steps):
+        call()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.emu_steps
+    value = n / (ms * 1e-3)
+    flops = 5 * 2.0 * (512 * 32 + 3 * 512 * 512 + 128 * 512) * n
+    pk = _peaks()
+    # end to end from host arrays, the flagged models through the plain CSP
+    ctx.emulator_predict(x[:4096], fallback=True)
+    t0 = time.perf_counter()
+    for _ in range(args.emu_e2e_steps):
+        out = ctx.emulator_predict(x, fallback=True)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.emu_e2e_steps
+    # accuracy against the plain CSP, and the plain CSP's own rate on the same physics
+    ns = 4096
+    ref = ctx.csp_batch({k: x[:ns, i] for i, k in enumerate(EMU_INPUTS)}, spec=False)["mags"]
+    emu = ctx.emulator_predict(x[:ns], fallback=False)
+    mmin = np.min(np.where(np.isfinite(ref), ref, np.inf), axis=1, keepdims=True)
+    gate = np.isfinite(ref) & (ref < mmin + 15.0)
+    err = np.where(gate, np.abs(emu["mags"] - ref), 0.0).max(axis=1)
+    ok = emu["source"] == 0
+    nc = min(n, 65536)
+    params = {k: x[:nc, i] for i, k in enumerate(EMU_INPUTS)}
+    ctx.csp_batch({k: v[:1024] for k, v in params.items()}, spec=False)
+    t0 = time.perf_counter()
+    ctx.csp_batch(params, spec=False)
+    csp_rate = nc / (time.perf_counter() - t0)
+    ctx.close()
+    return {"batch": n, "value": value, "unit": "models/s", "ms_per_step": ms, "steps": args.emu_steps,
+            "dtype": "f16 weights and activations (inputs split hi + lo), f32 accumulate",
+            "roofline": {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": pk["bf16_tflops_sustained"],
+                         "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / pk["bf16_tflops_sustained"],
+                         "kernel": "emu_infer_kernel", "flop_per_model": flops / n,
+                         "peak_src": f"{pk['src']} sustained dense bf16 (f16 runs at the same rate)"},
+            "flagged_frac": nflag / n,
+            "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "models/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(n * 10 * 4), "d2h_bytes_per_step": int(n * (nb + 1) * 4 + n * 4),
+                    "fallback_models": int(out["n_fallback"]),
+                    "outputs": "mags (flagged models from the plain CSP)"},
+            "accuracy_vs_csp": {"sample": ns, "unflagged_within_0.01_mag": float(np.mean(err[ok] <= 0.01)),
+                                "unflagged_max_mag": float(err[ok].max()), "all_p99_mag": float(np.percentile(err, 99)),
+                                "flagged_frac": float(1 - ok.mean()),
+                                "bands": "less than 15 mag fainter than the model's brightest"},
+            "csp_same_physics": {"batch": nc, "value": csp_rate, "unit": "models/s",
+                                 "workload": "SSP operator with the Kroupa slopes per model, delayed-tau SFH on the "
+                                             "device, dust, z 0-6 with IGM, smoothing, 40 filters (end to end)"},
+            "speedup_vs_same_physics_csp": value / csp_rate, "e2e_speedup_vs_same_physics_csp": (n / (e2e_ms * 1e-3)) / csp_rate}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -346,6 +438,9 @@ def run_ours(args) -> None:
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
+    emulator = emulator_measure(args, torch, barrier) if rank == 0 else None
+    if emulator:
+        emulator["speedup_vs_mixed_csp"] = emulator["value"] / value
 
     # roofline of the contraction
     pk = _peaks()
@@ -380,6 +475,7 @@ def run_ours(args) -> None:
             "ssp_operator": ssp_ops,
             "fp64_path": fp64,
             "mixed_over_fp64": (value / fp64["device_value"]) if fp64 and fp64.get("device_value") else None,
+            "emulator": emulator,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -403,6 +499,9 @@ def main():
     ap.add_argument("--ops-steps", type=int, default=10)
     ap.add_argument("--fp64-batch", type=int, default=65536)
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--emu-batch", type=int, default=1048576)
+    ap.add_argument("--emu-steps", type=int, default=20)
+    ap.add_argument("--emu-e2e-steps", type=int, default=2)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
