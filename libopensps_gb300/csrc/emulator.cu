@@ -1,27 +1,31 @@
 // The emulator's inference: one fused persistent kernel per SM that runs the five members of the ensemble over a
 // tile of 128 models, layer after layer, without leaving the SM.
 //
-// Per tile and member, five dense layers (64 -> 512 -> 512 -> 512 -> 512 -> 128). Each layer is four (the output
-// layer: one) N chunks of 128 outputs, D(models x 128) = A(models x K) W_chunk(128 x K)^T on tcgen05 (M = 128 models,
-// N = 128, f16, f32 accumulator in TMEM). The activations never leave the SM and alternate between two homes:
-//   input (S, K block 0) -> h1 (T) -> h2 (S) -> h3 (T) -> h4 (S) -> outputs (registers)
+// Per tile and member, five dense layers (12 features -> 512 -> 512 -> 512 -> 512 -> 128 outputs). Each hidden layer
+// is two N chunks of 256 outputs (the output layer one chunk of 128): D(models x 256) = A(models x K) W(256 x K)^T
+// on tcgen05 (M = 128 models, f16, f32 accumulator in TMEM). N = 256: on this GPU an N = 128 MMA takes as long as
+// an N = 256 one. The activations never leave the SM and alternate between two homes:
+//   input (S, K block 0) -> h1 (T) -> h2 (S) -> h3 (T) -> h4 (S) -> outputs (scratch)
 // where S is shared memory (128 x 512 f16, eight 16 KB K blocks in the 128-byte swizzle: the MMA's A descriptor)
 // and T is tensor memory (256 columns, two f16 per column: the MMA's A operand from TMEM). A layer reads one home
-// and its epilogue writes the other, so the epilogue of chunk c (TMEM accumulator -> bias, SiLU -> f16) runs
-// while the MMAs of chunk c + 1 read the unchanged input. The accumulators are double-buffered (2 x 128 columns),
-// and the next layer's first chunk starts on the K blocks already written (a ready barrier per 128 features).
-// The weights stream through a six-stage TMA ring (128 x 64 f16 tiles, 16 KB).
+// and its epilogue writes the other. The accumulator (256 columns) is single-buffered: the epilogue first drains
+// its 64 columns of the chunk into registers and releases the accumulator, so that the next chunk's MMAs run while
+// it adds the biases, applies SiLU and stores the f16 activations; the next layer's first chunk starts on the
+// 256 features already written (a ready barrier per 256 features).
+// The weights stream through a three-stage TMA ring of 256 x 64 f16 tiles (32 KB): the two CTAs of a cluster load
+// one half each and multicast it to both.
 //
-// Warp 0: TMA producer; warp 1: MMA issuer (one thread) and TMEM owner; warps 2..9: epilogue, two warps per TMEM
-// lane quarter (one model row per thread, 64 of the 128 columns each). The output epilogue keeps, per model, the
-// members' sum of the PCA coefficients and a running mean and M2 (Welford) of the magnitudes, then writes the
-// ensemble mean, the spread (the population standard deviation over the members, the largest over the bands that
-// are less than `faint` mag fainter than the brightest) and the flag.
+// Warp 0: TMA producer; warp 1: MMA issuer (one thread) and TMEM owner; warps 2..17: epilogue, four warps per
+// TMEM lane quarter (one model row per thread, 64 of a chunk's 256 columns each). Each member's outputs go to the
+// CTA's scratch (L2-resident); after the last member, each row's ensemble mean, spread (the population standard
+// deviation over the members, the largest over the bands that are less than `faint` mag fainter than the
+// brightest) and flag are formed from there.
 //
 // Every mbarrier wait is bounded (status word, no hang); drains wait for the copies and MMAs in flight.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include "sm103_ptx.cuh"
@@ -30,13 +34,18 @@
 
 namespace sps {
 
-constexpr int EI_THREADS = 320;
-constexpr int EI_NS = 6;                          // weight stages
-constexpr int EI_TILE = 128 * 64 * 2;             // one 128 x 64 f16 tile (16 KB)
-constexpr int EI_S_BYTES = 8 * EI_TILE;           // activations: 8 K blocks
-constexpr int EI_SMEM = EI_S_BYTES + EI_NS * EI_TILE + 256 + 1024;
-constexpr uint32_t EI_IDESC = idesc_f16_f32(128, 128);
+constexpr int EI_EPI_WARPS = 16;
+constexpr int EI_THREADS = (2 + EI_EPI_WARPS) * 32;
+constexpr int EI_NS = 3;                          // weight stages
+constexpr int EI_KBLK = 128 * 64 * 2;             // one 128-row x 64 f16 K block of the activations (16 KB)
+constexpr int EI_STAGE = 256 * 64 * 2;            // one 256 x 64 f16 weight tile (32 KB)
+constexpr int EI_S_BYTES = 8 * EI_KBLK;           // activations: 8 K blocks
+constexpr int EI_SMEM = EI_S_BYTES + EI_NS * EI_STAGE + 256 + 1024;
+constexpr uint32_t EI_IDESC256 = idesc_f16_f32(128, 256), EI_IDESC128 = idesc_f16_f32(128, 128);
 constexpr uint32_t EI_T_COL = 0, EI_ACC_COL = 256;
+constexpr int EI_CS = 2;                          // CTAs per cluster sharing each weight tile (multicast)
+constexpr int EI_ROWS = 256 / EI_CS;              // rows of a hidden-layer weight tile each CTA of the cluster loads
+constexpr int EI_ROWS4 = 128 / EI_CS;             // the same for the output layer's 128-row tiles
 
 __device__ __forceinline__ float silu_fast(float z) {
     const float hz = 0.5f * z;
@@ -74,175 +83,231 @@ __device__ __forceinline__ float emu_distance(float z, const float *zt, const fl
     return 5.f * log10f(dm * 0.1f) - 2.5f * log10f(1.f + z);
 }
 
+// The member a CTA runs at step mem of each tile: the order is rotated by the CTA index, so that the CTAs stream
+// different members' weights at a time instead of all reading the same tiles from the same L2 lines.
+__device__ __forceinline__ int emu_member(int mem) { return (mem + (int)blockIdx.x / EI_CS) % EMU_MEMBERS; }
+// Tiles per CTA: the same count in every CTA (a cluster's CTAs load the weights together), the ones past the last
+// tile are run with no valid model.
+__device__ __forceinline__ int emu_iters(int ntiles) { return (ntiles + (int)gridDim.x - 1) / (int)gridDim.x; }
+
 // A warp-uniform bounded wait (every lane polls; the warp goes on only if all saw the phase complete).
 __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, int *status, int code) {
     const bool w = mbar_wait(bar, parity, status, code);
     return __all_sync(0xffffffffu, w);
 }
 
-// The epilogue warps of one column half H (H = 0: columns 0..63 of each chunk, the PCA outputs of the last layer;
-// H = 1: columns 64..127, the magnitudes), one model row per thread.
-template <int H>
+// 32 consecutive 32-bit TMEM columns without the wait (the caller waits once for several loads).
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// The epilogue warps: lane quarter q (TMEM lanes 32q..32q+31, model rows), column slice cs (64 of a hidden chunk's
+// 256 columns; 32 of the output chunk's 128).
 __device__ __forceinline__ void emu_epilogue(const EmuInferArgs &a, uint8_t *S, uint64_t *bars, uint32_t tmem_base,
-                                             int q, int lane) {
-    uint64_t *afull = bars + 2 * EI_NS, *aempty = afull + 2, *hrdy = aempty + 2, *inrdy = hrdy + 4;
+                                             int q, int cs, int lane) {
+    uint64_t *afull = bars + 2 * EI_NS, *aempty = afull + 1, *hrdy = aempty + 1, *inrdy = hrdy + 2;
     const int r = q * 32 + lane;
     const uint32_t lane_base = (uint32_t)(q * 32) << 16;
     const uint32_t s_base = smem_u32(S);
     const float *par = a.par;
     const int ntiles = (a.n + 127) / 128;
+    const int iters = emu_iters(ntiles);
     int *status = a.status;
+    // this row's outputs of each member: scratch[cta][member][row][128]
+    float *scr_row = a.scratch + ((size_t)blockIdx.x * EMU_MEMBERS * 128 + r) * EMU_NOUT;
+    constexpr size_t SCR_MEM = (size_t)128 * EMU_NOUT;
     uint32_t g = 0;
     bool ok = true;
-    constexpr int NACC = H == 0 ? EMU_NPC : EMU_MAX_BANDS;
-    float acc1[NACC];            // H = 0: the members' sum (standardised); H = 1: Welford mean
-    float acc2[H == 0 ? 1 : EMU_MAX_BANDS];   // H = 1: Welford M2
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int m = tile * 128 + r;
-        const bool valid = m < a.n;
-        float xs[EMU_NFEAT];
-        bool outside = false, bad = false;
-        float zred = 0.f;
-        if (valid) {
-            float x[EMU_NIN];
+    // the input row of tile `tile` (K block 0 of S, f16: the features' hi parts at K 0..11, lo parts at 16..27),
+    // written by the cs = 0 warps; every epilogue warp arrives
+    auto put_input = [&](int tile) {
+        if (cs == 0) {
+            const int m = tile * 128 + r;
+            float xs[EMU_NFEAT];
+            bool use = m < a.n;
+            if (use) {
+                float x[EMU_NIN];
 #pragma unroll
-            for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
-            zred = x[5];
-            outside = !emu_features(x, par, xs);
+                for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
+                emu_features(x, par, xs);
 #pragma unroll
-            for (int i = 0; i < EMU_NFEAT; ++i)
-                if (!isfinite(xs[i])) bad = true;
-        }
-        if (!valid || bad) {
-#pragma unroll
-            for (int i = 0; i < EMU_NFEAT; ++i) xs[i] = 0.f;
-        }
-        // the input row as f16 words: the features' hi parts (K 0..11), then their lo parts (K 16..27)
-        uint32_t xin[12];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            xin[i] = pack_f16(xs[2 * i], xs[2 * i + 1]);
-            xin[6 + i] = pack_f16(f16_lo(xs[2 * i]), f16_lo(xs[2 * i + 1]));
-        }
-#pragma unroll
-        for (int j = 0; j < NACC; ++j) acc1[j] = 0.f;
-        if (H == 1) {
-#pragma unroll
-            for (int j = 0; j < EMU_MAX_BANDS; ++j) acc2[j] = 0.f;
-        }
-        for (int mem = 0; mem < EMU_MEMBERS && ok; ++mem) {
-            // the input row (K block 0 of S, f16): K 0..11 the features' hi parts, K 16..27 their lo parts, zeros
-            if (H == 0) {
-                st_shared_v4(s_base + sw128_off(r, 0), xin[0], xin[1], xin[2], xin[3]);
-                st_shared_v4(s_base + sw128_off(r, 1), xin[4], xin[5], 0u, 0u);
-                st_shared_v4(s_base + sw128_off(r, 2), xin[6], xin[7], xin[8], xin[9]);
-                st_shared_v4(s_base + sw128_off(r, 3), xin[10], xin[11], 0u, 0u);
-                fence_proxy_async_smem();
+                for (int i = 0; i < EMU_NFEAT; ++i)
+                    if (!isfinite(xs[i])) use = false;
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(inrdy);
-            const float *bm = a.bias + (size_t)mem * EMU_NBIAS;
+            if (!use) {
+#pragma unroll
+                for (int i = 0; i < EMU_NFEAT; ++i) xs[i] = 0.f;
+            }
+            uint32_t w[12];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                w[i] = pack_f16(xs[2 * i], xs[2 * i + 1]);
+                w[6 + i] = pack_f16(f16_lo(xs[2 * i]), f16_lo(xs[2 * i + 1]));
+            }
+            st_shared_v4(s_base + sw128_off(r, 0), w[0], w[1], w[2], w[3]);
+            st_shared_v4(s_base + sw128_off(r, 1), w[4], w[5], 0u, 0u);
+            st_shared_v4(s_base + sw128_off(r, 2), w[6], w[7], w[8], w[9]);
+            st_shared_v4(s_base + sw128_off(r, 3), w[10], w[11], 0u, 0u);
+            fence_proxy_async_smem();
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(inrdy);
+    };
+    put_input(blockIdx.x);
+    for (int it = 0; it < iters && ok; ++it) {
+        const int tile = blockIdx.x + it * gridDim.x;
+        const int m = tile * 128 + r;
+        for (int mem = 0; mem < EMU_MEMBERS && ok; ++mem) {
+            const float *bm = a.bias + (size_t)emu_member(mem) * EMU_NBIAS;
             for (int L = 0; L < 5 && ok; ++L) {
-                const int nch = L == 4 ? 1 : 4;
+                const int nch = L == 4 ? 1 : 2;
                 for (int c = 0; c < nch; ++c) {
-                    const uint32_t buf = g & 1u;
-                    if (!warp_wait(&afull[buf], (g >> 1) & 1u, status, ERR_TIMEOUT_EPILOGUE)) { ok = false; break; }
+                    if (!warp_wait(afull, g & 1u, status, ERR_TIMEOUT_EPILOGUE)) { ok = false; break; }
                     ++g;
                     tc_fence_after();
-                    const uint32_t ta = tmem_base + lane_base + EI_ACC_COL + buf * 128 + H * 64;
-                    float v[32];
                     if (L < 4) {
-                        const float *b = bm + L * EMU_H + c * 128 + H * 64;
-                        uint32_t p[32];
-#pragma unroll
-                        for (int half = 0; half < 2; ++half) {
-                            tmem_ld32(ta + half * 32, v);
-#pragma unroll
-                            for (int i = 0; i < 16; ++i)
-                                p[half * 16 + i] = pack_f16(silu_fast(v[2 * i] + __ldg(b + half * 32 + 2 * i)),
-                                                            silu_fast(v[2 * i + 1] + __ldg(b + half * 32 + 2 * i + 1)));
-                        }
+                        // drain this slice (64 columns) and release the accumulator
+                        uint32_t v[64];
+                        const uint32_t ta = tmem_base + lane_base + EI_ACC_COL + cs * 64;
+                        tmem_ld32_nowait(ta, v);
+                        tmem_ld32_nowait(ta + 32, v + 32);
+                        tmem_wait_ld();
                         tc_fence_before();
                         __syncwarp();
-                        if (lane == 0) mbar_arrive(&aempty[buf]);
+                        if (lane == 0) mbar_arrive(aempty);
+                        // bias, SiLU, f16 in groups of 16 features
+                        const float4 *b4 = reinterpret_cast<const float4 *>(bm + L * EMU_H + c * 256 + cs * 64);
+                        const uint32_t blk = s_base + (uint32_t)(c * 4 + cs) * EI_KBLK;   // h2, h4: K block 4c + cs
+#pragma unroll
+                        for (int grp = 0; grp < 4; ++grp) {
+                            float b[16];
+#pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const float4 t = __ldg(b4 + grp * 4 + i);
+                                b[4 * i] = t.x; b[4 * i + 1] = t.y; b[4 * i + 2] = t.z; b[4 * i + 3] = t.w;
+                            }
+                            uint32_t pk[8];
+#pragma unroll
+                            for (int i = 0; i < 8; ++i)
+                                pk[i] = pack_f16(silu_fast(__uint_as_float(v[grp * 16 + 2 * i]) + b[2 * i]),
+                                                 silu_fast(__uint_as_float(v[grp * 16 + 2 * i + 1]) + b[2 * i + 1]));
+                            if ((L & 1) == 0) {
+                                // h1 (L = 0), h3 (L = 2) into tensor memory: features c*256 + cs*64 + grp*16 ...
+                                tmem_st8(tmem_base + lane_base + EI_T_COL + c * 128 + cs * 32 + grp * 8, pk);
+                            } else {
+                                // h2 (L = 1), h4 (L = 3) into shared memory: 16-byte chunks 2 grp, 2 grp + 1
+                                st_shared_v4(blk + sw128_off(r, 2 * grp), pk[0], pk[1], pk[2], pk[3]);
+                                st_shared_v4(blk + sw128_off(r, 2 * grp + 1), pk[4], pk[5], pk[6], pk[7]);
+                            }
+                        }
                         if ((L & 1) == 0) {
-                            // h1 (L = 0) and h3 (L = 2) into tensor memory
-                            tmem_st32(tmem_base + lane_base + EI_T_COL + c * 64 + H * 32, p);
                             tmem_wait_st();
                             tc_fence_before();
                         } else {
-                            // h2 (L = 1) and h4 (L = 3) into shared memory, K block 2c + H
-                            const uint32_t blk = s_base + (uint32_t)(2 * c + H) * EI_TILE;
-#pragma unroll
-                            for (int j = 0; j < 8; ++j)
-                                st_shared_v4(blk + sw128_off(r, j), p[4 * j], p[4 * j + 1], p[4 * j + 2], p[4 * j + 3]);
                             fence_proxy_async_smem();
                         }
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&hrdy[c]);
                     } else {
-                        const float *b = bm + 4 * EMU_H + H * 64;
-                        const float inv = 1.f / (float)(mem + 1);
-#pragma unroll
-                        for (int half = 0; half < 2; ++half) {
-                            tmem_ld32(ta + half * 32, v);
-#pragma unroll
-                            for (int i = 0; i < 32; ++i) {
-                                const int j = half * 32 + i;
-                                if (H == 0) {
-                                    acc1[j < NACC ? j : 0] += v[i] + __ldg(b + j);
-                                } else if (j < EMU_MAX_BANDS) {
-                                    const float z = v[i] + __ldg(b + j);
-                                    const float d = z - acc1[j];
-                                    acc1[j] += d * inv;
-                                    acc2[j] = fmaf(d, z - acc1[j], acc2[j]);
-                                }
-                            }
-                        }
+                        // the output chunk (128 columns): this slice's 32
+                        uint32_t v[32];
+                        tmem_ld32_nowait(tmem_base + lane_base + EI_ACC_COL + cs * 32, v);
+                        tmem_wait_ld();
                         tc_fence_before();
                         __syncwarp();
-                        if (lane == 0) mbar_arrive(&aempty[buf]);
+                        if (lane == 0) mbar_arrive(aempty);
+                        // S is free (the output layer's MMAs are done): the next member's input row, or the next
+                        // tile's after the last member
+                        if (mem + 1 < EMU_MEMBERS) put_input(tile);
+                        else if (it + 1 < iters) put_input(tile + gridDim.x);
+                        const float4 *b4 = reinterpret_cast<const float4 *>(bm + 4 * EMU_H + cs * 32);
+                        float4 *dst = reinterpret_cast<float4 *>(scr_row + mem * SCR_MEM + cs * 32);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const float4 t = __ldg(b4 + i);
+                            dst[i] = make_float4(__uint_as_float(v[4 * i]) + t.x, __uint_as_float(v[4 * i + 1]) + t.y,
+                                                 __uint_as_float(v[4 * i + 2]) + t.z, __uint_as_float(v[4 * i + 3]) + t.w);
+                        }
                     }
                 }
             }
         }
-        if (!ok || !valid) continue;
-        // ---- the ensemble's outputs of model m
+        // ---- the ensemble's outputs of the quarter's rows: the four slices' scratch writes are in. The barrier is
+        // passed by all four warps whatever happened, and they stop together if any of them, or the status word,
+        // says so (a wait that gave up)
+        if (named_bar_or(1 + q, 128, !ok || *(volatile int *)status != 0)) break;
+        if (m >= a.n) continue;
         const float invm = 1.f / (float)EMU_MEMBERS;
-        if (H == 0) {
+        if (cs < 2) {
             if (a.coef) {
-                float *dst = a.coef + (size_t)m * EMU_NPC;
+                float *dst = a.coef + (size_t)m * EMU_NPC + cs * 32;
+#pragma unroll 2
+                for (int j = 0; j < 32; j += 4) {
+                    const int col = cs * 32 + j;
+                    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-                for (int j = 0; j < EMU_NPC; j += 4) {
+                    for (int k = 0; k < EMU_MEMBERS; ++k) {
+                        const float4 t = *reinterpret_cast<const float4 *>(scr_row + k * SCR_MEM + col);
+                        sum.x += t.x; sum.y += t.y; sum.z += t.z; sum.w += t.w;
+                    }
                     float4 o;
-                    o.x = par[EMU_P_OMU + j] + par[EMU_P_OSIG + j] * acc1[j] * invm;
-                    o.y = par[EMU_P_OMU + j + 1] + par[EMU_P_OSIG + j + 1] * acc1[j + 1] * invm;
-                    o.z = par[EMU_P_OMU + j + 2] + par[EMU_P_OSIG + j + 2] * acc1[j + 2] * invm;
-                    o.w = par[EMU_P_OMU + j + 3] + par[EMU_P_OSIG + j + 3] * acc1[j + 3] * invm;
+                    o.x = par[EMU_P_OMU + col] + par[EMU_P_OSIG + col] * sum.x * invm;
+                    o.y = par[EMU_P_OMU + col + 1] + par[EMU_P_OSIG + col + 1] * sum.y * invm;
+                    o.z = par[EMU_P_OMU + col + 2] + par[EMU_P_OSIG + col + 2] * sum.z * invm;
+                    o.w = par[EMU_P_OMU + col + 3] + par[EMU_P_OSIG + col + 3] * sum.w * invm;
                     *reinterpret_cast<float4 *>(dst + j) = o;
                 }
             }
-        } else {
-            const float dd = emu_distance(zred, par + EMU_P_ZT, par + EMU_P_DL);
+        } else if (cs == 2) {
+            float x[EMU_NIN], xs[EMU_NFEAT];
+#pragma unroll
+            for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
+            const bool outside = !emu_features(x, par, xs);
+            bool bad = false;
+#pragma unroll
+            for (int i = 0; i < EMU_NFEAT; ++i)
+                if (!isfinite(xs[i])) bad = true;
+            const float dd = emu_distance(x[5], par + EMU_P_ZT, par + EMU_P_DL);
+            const float *scr = scr_row + EMU_NPC;
+            // pass 1: the ensemble mean of each band (its magnitude) and the brightest band
             float mmin = INFINITY;
             bool finite = true;
+            float *mdst = a.mags + (size_t)m * a.nb;
+            for (int j = 0; j < a.nb; ++j) {
+                float sum = 0.f;
 #pragma unroll
-            for (int j = 0; j < EMU_MAX_BANDS; ++j)
-                if (j < a.nb) {
-                    const int o = EMU_NPC + j;
-                    acc1[j] = par[EMU_P_OMU + o] + par[EMU_P_OSIG + o] * acc1[j] + dd;     // the magnitude
-                    acc2[j] = par[EMU_P_OSIG + o] * sqrtf(fmaxf(acc2[j] * invm, 0.f));     // its spread
-                    if (!isfinite(acc1[j]) || !isfinite(acc2[j])) finite = false;
-                    mmin = fminf(mmin, acc1[j]);
-                }
+                for (int k = 0; k < EMU_MEMBERS; ++k) sum += scr[k * SCR_MEM + j];
+                const int o = EMU_NPC + j;
+                const float mag = par[EMU_P_OMU + o] + par[EMU_P_OSIG + o] * sum * invm + dd;
+                if (!isfinite(mag)) finite = false;
+                mmin = fminf(mmin, mag);
+                mdst[j] = mag;
+            }
+            // pass 2: the spread of the bands that count
             float spread = 0.f;
-            float *dst = a.mags + (size_t)m * a.nb;
+            for (int j = 0; j < a.nb; ++j) {
+                float z[EMU_MEMBERS], mean = 0.f;
 #pragma unroll
-            for (int j = 0; j < EMU_MAX_BANDS; ++j)
-                if (j < a.nb) {
-                    if (acc1[j] < mmin + a.faint) spread = fmaxf(spread, acc2[j]);
-                    dst[j] = acc1[j];
-                }
+                for (int k = 0; k < EMU_MEMBERS; ++k) { z[k] = scr[k * SCR_MEM + j]; mean += z[k]; }
+                mean *= invm;
+                float var = 0.f;
+#pragma unroll
+                for (int k = 0; k < EMU_MEMBERS; ++k) var += (z[k] - mean) * (z[k] - mean);
+                const int o = EMU_NPC + j;
+                const float sd = par[EMU_P_OSIG + o] * sqrtf(var * invm);
+                const float mag = par[EMU_P_OMU + o] + par[EMU_P_OSIG + o] * mean + dd;
+                if (!isfinite(sd)) finite = false;
+                if (mag < mmin + a.faint) spread = fmaxf(spread, sd);
+            }
             const int f = outside ? 1 : (bad || !finite) ? 3 : (spread > a.spread_max) ? 2 : 0;
             if (a.spread) a.spread[m] = spread;
             a.flag[m] = f;
@@ -261,9 +326,9 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *S = smem;
     uint8_t *W = smem + EI_S_BYTES;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(W + EI_NS * EI_TILE);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(W + EI_NS * EI_STAGE);
     uint64_t *full = bars, *empty = bars + EI_NS;
-    uint64_t *afull = bars + 2 * EI_NS, *aempty = afull + 2, *hrdy = aempty + 2, *inrdy = hrdy + 4;
+    uint64_t *afull = bars + 2 * EI_NS, *aempty = afull + 1, *hrdy = aempty + 1, *inrdy = hrdy + 2;
     uint64_t *mma_done = inrdy + 1;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -271,18 +336,23 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
     int *status = a.status;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < EI_NS; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(&afull[b], 1); mbar_init(&aempty[b], 8); }
-        for (int c = 0; c < 4; ++c) mbar_init(&hrdy[c], 8);
-        mbar_init(inrdy, 8);
+        for (int s = 0; s < EI_NS; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], EI_CS); }
+        mbar_init(afull, 1);
+        mbar_init(aempty, EI_EPI_WARPS);
+        for (int c = 0; c < 2; ++c) mbar_init(&hrdy[c], EI_EPI_WARPS);
+        mbar_init(inrdy, EI_EPI_WARPS);
         mbar_init(mma_done, 1);
         fence_mbar_init();
     }
     if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
     tc_fence_before();
     __syncthreads();
+    cluster_sync();      // the partner's barriers are initialised before any multicast reaches them
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    const uint32_t rank = cluster_ctarank();
+    const uint16_t cmask = (uint16_t)((1u << EI_CS) - 1u);
+    const int iters = emu_iters(ntiles);
 
     if (warp == 0) {
         if (lane == 0) {
@@ -290,21 +360,31 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
             int last_fill[EI_NS];
             for (int i = 0; i < EI_NS; ++i) last_fill[i] = -1;
             bool ok = true;
-            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
+            for (int it = 0; it < iters && ok; ++it)
                 for (int mem = 0; mem < EMU_MEMBERS && ok; ++mem)
                     for (int L = 0; L < 5 && ok; ++L) {
-                        const int nch = L == 4 ? 1 : 4, nkb = L == 0 ? 1 : 8;
+                        const int nch = L == 4 ? 1 : 2, nkb = L == 0 ? 1 : 8;
                         for (int c = 0; c < nch && ok; ++c)
                             for (int kb = 0; kb < nkb; ++kb) {
+                                // the stage is free once every CTA of the cluster has consumed it
                                 if (!mbar_wait(&empty[s], ph ^ 1u, status, ERR_TIMEOUT_PRODUCER)) { ok = false; break; }
-                                uint8_t *dst = W + s * EI_TILE;
-                                mbar_arrive_expect_tx(&full[s], EI_TILE);
-                                if (L == 0)
-                                    tma_load_2d(dst, &tm_w0, 0, mem * EMU_H + c * 128, &full[s]);
-                                else if (L < 4)
-                                    tma_load_2d(dst, &tm_wh, kb * 64, ((L - 1) * EMU_MEMBERS + mem) * EMU_H + c * 128, &full[s]);
-                                else
-                                    tma_load_2d(dst, &tm_w4, kb * 64, mem * EMU_NOUT, &full[s]);
+                                const int mw = emu_member(mem);
+                                uint8_t *st = W + s * EI_STAGE;
+                                if (L < 4) {
+                                    mbar_arrive_expect_tx(&full[s], EI_STAGE);
+                                    const int row = (int)rank * EI_ROWS;
+                                    uint8_t *dst = st + rank * (EI_ROWS * 128);
+                                    if (L == 0)
+                                        tma_load_2d_mc(dst, &tm_w0, 0, mw * EMU_H + c * 256 + row, &full[s], cmask);
+                                    else
+                                        tma_load_2d_mc(dst, &tm_wh, kb * 64, ((L - 1) * EMU_MEMBERS + mw) * EMU_H + c * 256 + row,
+                                                       &full[s], cmask);
+                                } else {
+                                    mbar_arrive_expect_tx(&full[s], EI_STAGE / 2);
+                                    const int row = (int)rank * EI_ROWS4;
+                                    tma_load_2d_mc(st + rank * (EI_ROWS4 * 128), &tm_w4, kb * 64, mw * EMU_NOUT + row,
+                                                   &full[s], cmask);
+                                }
                                 last_fill[s] = (int)ph;
                                 if (++s == EI_NS) { s = 0; ph ^= 1u; }
                             }
@@ -318,46 +398,47 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
             uint32_t g = 0, icnt = 0, hcnt = 0;
             bool ok = true;
             const uint32_t s_base = smem_u32(S);
-            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
+            const uint32_t d = tmem_base + EI_ACC_COL;
+            for (int it = 0; it < iters && ok; ++it)
                 for (int mem = 0; mem < EMU_MEMBERS && ok; ++mem) {
                     if (!mbar_wait(inrdy, icnt & 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                     ++icnt;
                     tc_fence_after();
                     for (int L = 0; L < 5 && ok; ++L) {
-                        const int nch = L == 4 ? 1 : 4, nkb = L == 0 ? 1 : 8;
+                        const int nch = L == 4 ? 1 : 2, nkb = L == 0 ? 1 : 8;
+                        const uint32_t idesc = L == 4 ? EI_IDESC128 : EI_IDESC256;
                         for (int c = 0; c < nch && ok; ++c) {
-                            const uint32_t buf = g & 1u;
-                            if (!mbar_wait(&aempty[buf], ((g >> 1) & 1u) ^ 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
+                            // the accumulator is free once the epilogue has drained the previous chunk
+                            if (!mbar_wait(aempty, (g & 1u) ^ 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                             tc_fence_after();
-                            const uint32_t d = tmem_base + EI_ACC_COL + buf * 128;
                             for (int kb = 0; kb < nkb; ++kb) {
-                                if (L >= 1 && c == 0 && (kb & 1) == 0) {
-                                    if (!mbar_wait(&hrdy[kb >> 1], hcnt & 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
+                                if (L >= 1 && c == 0 && (kb & 3) == 0) {
+                                    if (!mbar_wait(&hrdy[kb >> 2], hcnt & 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                                     tc_fence_after();
                                 }
                                 if (!mbar_wait(&full[s], ph, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                                 tc_fence_after();
-                                const uint32_t b0 = smem_u32(W + s * EI_TILE);
+                                const uint32_t b0 = smem_u32(W + s * EI_STAGE);
                                 if (L == 0) {
                                     // the input layer: two K steps (the features' hi parts, then their lo parts
                                     // against the same weights repeated in W0's columns 16..27)
-                                    mma_bf16(d, sw128_desc(s_base), sw128_desc(b0), EI_IDESC, 0u);
-                                    mma_bf16(d, sw128_desc(s_base + 32), sw128_desc(b0 + 32), EI_IDESC, 1u);
+                                    mma_bf16(d, sw128_desc(s_base), sw128_desc(b0), idesc, 0u);
+                                    mma_bf16(d, sw128_desc(s_base + 32), sw128_desc(b0 + 32), idesc, 1u);
                                 } else {
 #pragma unroll
                                     for (int k = 0; k < 4; ++k) {
                                         const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
                                         if (L & 1)   // h1, h3 in tensor memory
-                                            mma_bf16_ts(d, tmem_base + EI_T_COL + kb * 32 + k * 8, sw128_desc(b0 + k * 32), EI_IDESC, acc);
+                                            mma_bf16_ts(d, tmem_base + EI_T_COL + kb * 32 + k * 8, sw128_desc(b0 + k * 32), idesc, acc);
                                         else         // h2, h4 in shared memory
-                                            mma_bf16(d, sw128_desc(s_base + kb * EI_TILE + k * 32), sw128_desc(b0 + k * 32), EI_IDESC, acc);
+                                            mma_bf16(d, sw128_desc(s_base + kb * EI_KBLK + k * 32), sw128_desc(b0 + k * 32), idesc, acc);
                                     }
                                 }
-                                mma_commit(&empty[s]);
+                                mma_commit_mc(&empty[s], cmask);   // frees the stage in every CTA
                                 if (++s == EI_NS) { s = 0; ph ^= 1u; }
                             }
                             if (!ok) break;
-                            mma_commit(&afull[buf]);
+                            mma_commit(afull);
                             ++g;
                         }
                         if (L >= 1) ++hcnt;
@@ -367,9 +448,7 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
             mbar_wait(mma_done, 0, status, ERR_TIMEOUT_MMA, false);
         }
     } else {
-        const int q = warp & 3;
-        if (warp < 6) emu_epilogue<0>(a, S, bars, tmem_base, q, lane);
-        else emu_epilogue<1>(a, S, bars, tmem_base, q, lane);
+        emu_epilogue(a, S, bars, tmem_base, warp & 3, (warp - 2) >> 2, lane);
     }
     tc_fence_before();
     __syncthreads();
@@ -377,18 +456,43 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
     }
+    cluster_sync();      // no CTA leaves while its partner may still write into its shared memory or barriers
 }
 
 int emu_infer_smem() { return EI_SMEM; }
+// rows of the inference kernel's weight boxes: hidden layers (one CTA's share of a 256-row tile), output layer
+int emu_weight_box_rows() { return EI_ROWS; }
+int emu_weight_box_rows4() { return EI_ROWS4; }
 
 cudaError_t run_emu_infer(const Emulator &e, const EmuInferArgs &a, int num_sms, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
     if (a.nb < 1 || a.nb > EMU_MAX_BANDS) return cudaErrorInvalidValue;
     cudaError_t err = cudaFuncSetAttribute(emu_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EI_SMEM);
     if (err != cudaSuccess) return err;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = EI_CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(EI_THREADS);
+    cfg.dynamicSmemBytes = EI_SMEM;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    // persistent: as many clusters as fit at once (at most one CTA per SM), no more than the tiles need
+    static int max_clusters = 0;
+    if (max_clusters == 0) {
+        cfg.gridDim = dim3(num_sms / EI_CS * EI_CS);
+        int mc = 0;
+        if (cudaOccupancyMaxActiveClusters(&mc, emu_infer_kernel, &cfg) != cudaSuccess || mc <= 0) mc = num_sms / EI_CS;
+        max_clusters = mc;
+    }
     const int ntiles = (a.n + 127) / 128;
-    const int grid = ntiles < num_sms ? ntiles : num_sms;
-    emu_infer_kernel<<<grid, EI_THREADS, EI_SMEM, st>>>(e.tm_w0, e.tm_wh, e.tm_w4, a);
+    const int clusters = std::min(max_clusters, (ntiles + EI_CS - 1) / EI_CS);
+    cfg.gridDim = dim3(clusters * EI_CS);
+    err = cudaLaunchKernelEx(&cfg, emu_infer_kernel, e.tm_w0, e.tm_wh, e.tm_w4, a);
+    if (err != cudaSuccess) return err;
     return cudaGetLastError();
 }
 

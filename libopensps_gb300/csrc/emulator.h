@@ -82,6 +82,7 @@ struct EmuInferArgs {
     float *spread;               // n, or null
     int *flag;                   // n: 0 emulated, 1 outside the training box, 2 spread, 3 not finite
     int *nflag, *flagged;        // count and indices of the flagged models
+    float *scratch;              // grid x EMU_MEMBERS x 128 x EMU_NOUT: the members' outputs of each CTA's tile
     int *status;
 };
 
@@ -109,6 +110,7 @@ struct Emulator {
     // predict scratch
     float *d_x = nullptr, *d_mags = nullptr, *d_coef = nullptr, *d_spread = nullptr;
     int *d_flag = nullptr, *d_nflag = nullptr, *d_flagged = nullptr;
+    float *d_scratch = nullptr;                  // the inference kernel's per-CTA member outputs
     int cap = 0;
     void release();
 };

@@ -28,6 +28,8 @@
 namespace sps {
 
 cudaError_t run_emu_infer(const Emulator &e, const EmuInferArgs &a, int num_sms, cudaStream_t st);
+int emu_weight_box_rows();
+int emu_weight_box_rows4();
 int csp_batch_mags(Context &c, int n, int n_params, const char *const *names, const double *const *values,
                    double *mags, std::string &err);
 
@@ -53,12 +55,12 @@ void Emulator::release() {
     for (void *p : {(void *)w0, (void *)wh, (void *)w4, (void *)wht, (void *)w4t, (void *)bias, (void *)d_par,
                     (void *)d_pca_mean, (void *)d_pca_basis, (void *)master, (void *)adam_m, (void *)adam_v,
                     (void *)d_x, (void *)d_mags, (void *)d_coef, (void *)d_spread, (void *)d_flag, (void *)d_nflag,
-                    (void *)d_flagged})
+                    (void *)d_flagged, (void *)d_scratch})
         if (p) cudaFree(p);
     w0 = wh = w4 = nullptr;
     wht = w4t = nullptr;
     bias = d_par = d_pca_mean = d_pca_basis = master = adam_m = adam_v = nullptr;
-    d_x = d_mags = d_coef = d_spread = nullptr;
+    d_x = d_mags = d_coef = d_spread = d_scratch = nullptr;
     d_flag = d_nflag = d_flagged = nullptr;
     cap = 0;
     ready = trainable = false;
@@ -480,9 +482,11 @@ static int emu_alloc(Emulator &e, bool trainable, std::string &err) {
         e.trainable = true;
         e.adam_t = 0;
     }
-    cudaError_t r1 = encode_tmap_2d_16(&e.tm_w0, e.w0, EMU_KIN, (uint64_t)EMU_MEMBERS * EMU_H, 64, 128, true);
-    cudaError_t r2 = encode_tmap_2d_16(&e.tm_wh, e.wh, EMU_H, 3ull * EMU_MEMBERS * EMU_H, 64, 128, true);
-    cudaError_t r3 = encode_tmap_2d_16(&e.tm_w4, e.w4, EMU_H, (uint64_t)EMU_MEMBERS * EMU_NOUT, 64, 128, true);
+    // the inference kernel's boxes: its share of a 128-row weight tile (the cluster's CTAs load one share each)
+    const uint32_t rows = (uint32_t)emu_weight_box_rows(), rows4 = (uint32_t)emu_weight_box_rows4();
+    cudaError_t r1 = encode_tmap_2d_16(&e.tm_w0, e.w0, EMU_KIN, (uint64_t)EMU_MEMBERS * EMU_H, 64, rows, true);
+    cudaError_t r2 = encode_tmap_2d_16(&e.tm_wh, e.wh, EMU_H, 3ull * EMU_MEMBERS * EMU_H, 64, rows, true);
+    cudaError_t r3 = encode_tmap_2d_16(&e.tm_w4, e.w4, EMU_H, (uint64_t)EMU_MEMBERS * EMU_NOUT, 64, rows4, true);
     if (r1 != cudaSuccess || r2 != cudaSuccess || r3 != cudaSuccess) {
         err = "emulator weight tensor maps";
         return ST_DATA_MISSING;
@@ -772,8 +776,13 @@ int emu_infer_device(Context &c, int n, const float *d_x, float *d_mags, float *
     Emulator &e = c.emu;
     if (!e.ready) { err = "no emulator on the context (opensps_gb300_emulator_load / _train)"; return ST_NO_OPERATOR; }
     if (e.nb != c.nbands) { err = "the emulator was trained for another band set"; return ST_UNSUPPORTED; }
+    if (!e.d_scratch) {
+        const cudaError_t r = dalloc(&e.d_scratch, (size_t)c.num_sms * EMU_MEMBERS * 128 * EMU_NOUT);
+        if (r != cudaSuccess) { err = cmsg("emulator scratch", r); return ST_DATA_MISSING; }
+    }
     EmuInferArgs a;
     a.n = n; a.nb = e.nb; a.x = d_x; a.bias = e.bias; a.par = e.d_par; a.spread_max = e.spread_max; a.faint = e.faint;
+    a.scratch = e.d_scratch;
     a.mags = d_mags; a.coef = d_coef; a.spread = d_spread; a.flag = d_flag; a.nflag = d_nflag; a.flagged = d_flagged;
     a.status = c.d_status.p;
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), c.stream);
