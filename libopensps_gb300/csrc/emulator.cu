@@ -122,47 +122,66 @@ __device__ __forceinline__ void emu_epilogue(const EmuInferArgs &a, uint8_t *S, 
     const int ntiles = (a.n + 127) / 128;
     const int iters = emu_iters(ntiles);
     int *status = a.status;
-    // this row's outputs of each member: scratch[cta][member][row][128]
-    float *scr_row = a.scratch + ((size_t)blockIdx.x * EMU_MEMBERS * 128 + r) * EMU_NOUT;
+    // this row's outputs of each member: scratch[cta][member][row][128]; then, per CTA, two slots x 128 rows x 16
+    // words of tile inputs (the input row's 12 f16 words, zred, the flags)
+    float *scr_row = a.scratch + ((size_t)blockIdx.x * EMU_SCRATCH_CTA + (size_t)r * EMU_NOUT);
+    uint4 *in_row = reinterpret_cast<uint4 *>(a.scratch + (size_t)blockIdx.x * EMU_SCRATCH_CTA +
+                                             (size_t)EMU_MEMBERS * 128 * EMU_NOUT) + (size_t)r * 4;
     constexpr size_t SCR_MEM = (size_t)128 * EMU_NOUT;
     uint32_t g = 0;
     bool ok = true;
-    // the input row of tile `tile` (K block 0 of S, f16: the features' hi parts at K 0..11, lo parts at 16..27),
-    // written by the cs = 0 warps; every epilogue warp arrives
-    auto put_input = [&](int tile) {
+    // the input words and flags of tile `tile` into slot `slot` (cs = 0 warps, one row each)
+    auto prepare_input = [&](int tile, int slot) {
+        if (cs != 0) return;
+        const int m = tile * 128 + r;
+        float xs[EMU_NFEAT];
+        float zred = 0.f;
+        uint32_t flags = 0;                      // bit 0: outside the box, bit 1: not finite
+        bool use = m < a.n;
+        if (use) {
+            float x[EMU_NIN];
+#pragma unroll
+            for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
+            zred = x[5];
+            if (!emu_features(x, par, xs)) flags |= 1u;
+#pragma unroll
+            for (int i = 0; i < EMU_NFEAT; ++i)
+                if (!isfinite(xs[i])) use = false;
+            if (!use) flags |= 2u;
+        }
+        if (!use) {
+#pragma unroll
+            for (int i = 0; i < EMU_NFEAT; ++i) xs[i] = 0.f;
+        }
+        uint32_t w[12];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            w[i] = pack_f16(xs[2 * i], xs[2 * i + 1]);
+            w[6 + i] = pack_f16(f16_lo(xs[2 * i]), f16_lo(xs[2 * i + 1]));
+        }
+        uint4 *dst = in_row + (size_t)slot * 128 * 4;
+        dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+        dst[2] = make_uint4(w[8], w[9], w[10], w[11]);
+        dst[3] = make_uint4(__float_as_uint(zred), flags, 0u, 0u);
+    };
+    // the input row into K block 0 of S (f16: the features' hi parts at K 0..11, lo parts at 16..27), from slot
+    // `slot`; every epilogue warp arrives
+    auto put_input = [&](int slot) {
         if (cs == 0) {
-            const int m = tile * 128 + r;
-            float xs[EMU_NFEAT];
-            bool use = m < a.n;
-            if (use) {
-                float x[EMU_NIN];
-#pragma unroll
-                for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
-                emu_features(x, par, xs);
-#pragma unroll
-                for (int i = 0; i < EMU_NFEAT; ++i)
-                    if (!isfinite(xs[i])) use = false;
-            }
-            if (!use) {
-#pragma unroll
-                for (int i = 0; i < EMU_NFEAT; ++i) xs[i] = 0.f;
-            }
-            uint32_t w[12];
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                w[i] = pack_f16(xs[2 * i], xs[2 * i + 1]);
-                w[6 + i] = pack_f16(f16_lo(xs[2 * i]), f16_lo(xs[2 * i + 1]));
-            }
-            st_shared_v4(s_base + sw128_off(r, 0), w[0], w[1], w[2], w[3]);
-            st_shared_v4(s_base + sw128_off(r, 1), w[4], w[5], 0u, 0u);
-            st_shared_v4(s_base + sw128_off(r, 2), w[6], w[7], w[8], w[9]);
-            st_shared_v4(s_base + sw128_off(r, 3), w[10], w[11], 0u, 0u);
+            const uint4 *src = in_row + (size_t)slot * 128 * 4;
+            const uint4 w0 = src[0], w1 = src[1], w2 = src[2];
+            st_shared_v4(s_base + sw128_off(r, 0), w0.x, w0.y, w0.z, w0.w);
+            st_shared_v4(s_base + sw128_off(r, 1), w1.x, w1.y, 0u, 0u);
+            st_shared_v4(s_base + sw128_off(r, 2), w1.z, w1.w, w2.x, w2.y);
+            st_shared_v4(s_base + sw128_off(r, 3), w2.z, w2.w, 0u, 0u);
             fence_proxy_async_smem();
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(inrdy);
     };
-    put_input(blockIdx.x);
+    prepare_input(blockIdx.x, 0);
+    put_input(0);
     for (int it = 0; it < iters && ok; ++it) {
         const int tile = blockIdx.x + it * gridDim.x;
         const int m = tile * 128 + r;
@@ -217,6 +236,8 @@ __device__ __forceinline__ void emu_epilogue(const EmuInferArgs &a, uint8_t *S, 
                         }
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&hrdy[c]);
+                        // the next tile's inputs, where the epilogue has time to spare
+                        if (mem == 0 && L == 1 && c == 0 && it + 1 < iters) prepare_input(tile + gridDim.x, (it + 1) & 1);
                     } else {
                         // the output chunk (128 columns): this slice's 32
                         uint32_t v[32];
@@ -227,8 +248,8 @@ __device__ __forceinline__ void emu_epilogue(const EmuInferArgs &a, uint8_t *S, 
                         if (lane == 0) mbar_arrive(aempty);
                         // S is free (the output layer's MMAs are done): the next member's input row, or the next
                         // tile's after the last member
-                        if (mem + 1 < EMU_MEMBERS) put_input(tile);
-                        else if (it + 1 < iters) put_input(tile + gridDim.x);
+                        if (mem + 1 < EMU_MEMBERS) put_input(it & 1);
+                        else if (it + 1 < iters) put_input((it + 1) & 1);
                         const float4 *b4 = reinterpret_cast<const float4 *>(bm + 4 * EMU_H + cs * 32);
                         float4 *dst = reinterpret_cast<float4 *>(scr_row + mem * SCR_MEM + cs * 32);
 #pragma unroll
@@ -268,15 +289,10 @@ __device__ __forceinline__ void emu_epilogue(const EmuInferArgs &a, uint8_t *S, 
                 }
             }
         } else if (cs == 2) {
-            float x[EMU_NIN], xs[EMU_NFEAT];
-#pragma unroll
-            for (int i = 0; i < EMU_NIN; ++i) x[i] = __ldg(a.x + (size_t)m * EMU_NIN + i);
-            const bool outside = !emu_features(x, par, xs);
-            bool bad = false;
-#pragma unroll
-            for (int i = 0; i < EMU_NFEAT; ++i)
-                if (!isfinite(xs[i])) bad = true;
-            const float dd = emu_distance(x[5], par + EMU_P_ZT, par + EMU_P_DL);
+            // the row's zred and flags from the tile's input slot (written by this quarter's cs = 0 warp)
+            const uint4 info = in_row[(size_t)(it & 1) * 128 * 4 + 3];
+            const bool outside = (info.y & 1u) != 0, bad = (info.y & 2u) != 0;
+            const float dd = emu_distance(__uint_as_float(info.x), par + EMU_P_ZT, par + EMU_P_DL);
             const float *scr = scr_row + EMU_NPC;
             // pass 1: the ensemble mean of each band (its magnitude) and the brightest band
             float mmin = INFINITY;

@@ -37,6 +37,9 @@ constexpr int EMU_NBIAS = 4 * EMU_H + EMU_NOUT;     // biases of one member: fou
 constexpr int EMU_P_INC = 0, EMU_P_INS = EMU_NFEAT, EMU_P_OMU = 2 * EMU_NFEAT, EMU_P_OSIG = EMU_P_OMU + EMU_NOUT;
 constexpr int EMU_P_CLK = EMU_P_OSIG + EMU_NOUT, EMU_P_ZT = EMU_P_CLK + 4, EMU_P_DL = EMU_P_ZT + 500;
 constexpr int EMU_PAR = EMU_P_DL + 500;
+// floats of the inference kernel's scratch per CTA: the members' outputs (5 x 128 rows x 128), then two slots of
+// tile inputs (128 rows x 16 words)
+constexpr long long EMU_SCRATCH_CTA = (long long)EMU_MEMBERS * 128 * EMU_NOUT + 2 * 128 * 16;
 // element counts of one member's weights
 constexpr long long EMU_W0 = (long long)EMU_H * EMU_KIN, EMU_WH = (long long)EMU_H * EMU_H,
                     EMU_W4 = (long long)EMU_NOUT * EMU_H;
@@ -82,7 +85,7 @@ struct EmuInferArgs {
     float *spread;               // n, or null
     int *flag;                   // n: 0 emulated, 1 outside the training box, 2 spread, 3 not finite
     int *nflag, *flagged;        // count and indices of the flagged models
-    float *scratch;              // grid x EMU_MEMBERS x 128 x EMU_NOUT: the members' outputs of each CTA's tile
+    float *scratch;              // grid x EMU_SCRATCH_CTA: each CTA's members' outputs and tile inputs
     int *status;
 };
 

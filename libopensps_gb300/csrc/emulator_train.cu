@@ -777,7 +777,7 @@ int emu_infer_device(Context &c, int n, const float *d_x, float *d_mags, float *
     if (!e.ready) { err = "no emulator on the context (opensps_gb300_emulator_load / _train)"; return ST_NO_OPERATOR; }
     if (e.nb != c.nbands) { err = "the emulator was trained for another band set"; return ST_UNSUPPORTED; }
     if (!e.d_scratch) {
-        const cudaError_t r = dalloc(&e.d_scratch, (size_t)c.num_sms * EMU_MEMBERS * 128 * EMU_NOUT);
+        const cudaError_t r = dalloc(&e.d_scratch, (size_t)c.num_sms * EMU_SCRATCH_CTA);
         if (r != cudaSuccess) { err = cmsg("emulator scratch", r); return ST_DATA_MISSING; }
     }
     EmuInferArgs a;
