@@ -43,7 +43,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     objdir = OUT / "obj"
     objdir.mkdir(exist_ok=True)
     cc = nvcc()
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-fopenmp", "--expt-relaxed-constexpr",
                     "-I", str(CSRC), "-I", str(HERE.parent / "include")]
     if verbose:
         flags += ["-Xptxas", "-v"]
@@ -65,7 +65,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [cc, "-shared", "-o", str(tmp)] + [str(o) for o in objs] + ARCH + [
-            "-lcudart_static", "-lrt", "-lpthread", "-ldl", "-lcublas", "-Xlinker", "-rpath=" + CUDA_LIB]
+            "-lcudart_static", "-lrt", "-lpthread", "-ldl", "-lcublas", "-lgomp", "-Xlinker", "-rpath=" + CUDA_LIB]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

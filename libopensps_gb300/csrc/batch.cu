@@ -349,12 +349,17 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const double minl = par(0, PF_MIN_WAVE_SMOOTH), maxl = par(0, PF_MAX_WAVE_SMOOTH);
     int itesc = -1;
     bool nacc2 = false, any_smooth = false;
+    double last_tesc = std::nan("");
     for (int m = 0; m < n; ++m) {
-        const double dla = par(m, PF_DUST_TESC) > SAFE_FLOOR ? par(m, PF_DUST_TESC) : 7.0;
-        int it = find_interval0(c.log_age.data(), nt, dla) + 1;
-        it = std::max(1, std::min(it, nt));
-        if (itesc < 0) itesc = it;
-        else if (it != itesc) { err = "dust_tesc must select the same age for every model of a batch on this path"; return ST_UNSUPPORTED; }
+        const double tesc = par(m, PF_DUST_TESC);
+        if (!(tesc == last_tesc)) {        // the age search once per distinct dust_tesc
+            last_tesc = tesc;
+            const double dla = tesc > SAFE_FLOOR ? tesc : 7.0;
+            int it = find_interval0(c.log_age.data(), nt, dla) + 1;
+            it = std::max(1, std::min(it, nt));
+            if (itesc < 0) itesc = it;
+            else if (it != itesc) { err = "dust_tesc must select the same age for every model of a batch on this path"; return ST_UNSUPPORTED; }
+        }
         if (par(m, PF_MIN_WAVE_SMOOTH) != minl || par(m, PF_MAX_WAVE_SMOOTH) != maxl) {
             err = "models must share min_wave_smooth and max_wave_smooth";
             return ST_UNSUPPORTED;
@@ -489,6 +494,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return ST_DATA_MISSING;
     }
     cudaStream_t st = c.stream;
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
+    // host weights over ages and metallicities on the mixed path go up in chunks, each chunk's kernels running
+    // while the next chunk's weights are copied
+    constexpr int CHUNK = 16384;
+    const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && !fp64 && !ops && !parts && n >= 2 * CHUNK;
     const double *d_wz = io.wz;
     const double *d_par = nullptr;
     std::vector<double> hp;
@@ -513,17 +523,30 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         if ((e = run_sfh_forward(sa, st)) != cudaSuccess) { err = cuda_msg("SFH weights kernel", e); return ST_DATA_MISSING; }
         d_wz = c.d_wz.p;
     } else {
-        if ((e = cudaMemcpyAsync(c.d_wz.p, io.wz, sizeof(double) * nwz, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+        if (!chunked && (e = cudaMemcpyAsync(c.d_wz.p, io.wz, sizeof(double) * nwz, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
             err = cuda_msg("weights copy", e);
             return ST_DATA_MISSING;
         }
         d_wz = c.d_wz.p;
     }
     if (!io.dev_inputs) {
-        hp.resize((size_t)PAR_DEVICE * n);
+        // the device table from the parameter rows, through a page-locked staging buffer
+        const size_t np = (size_t)PAR_DEVICE * n;
+        if (c.pinned_par_n < np) {
+            if (c.pinned_par) cudaFreeHost(c.pinned_par);
+            c.pinned_par = nullptr;
+            c.pinned_par_n = 0;
+            if ((e = cudaMallocHost(&c.pinned_par, sizeof(double) * np)) != cudaSuccess) {
+                err = cuda_msg("page-locked parameters", e);
+                return ST_DATA_MISSING;
+            }
+            c.pinned_par_n = np;
+        }
+        double *hpp = c.pinned_par;
+#pragma omp parallel for schedule(static) if (n >= 8192)
         for (int m = 0; m < n; ++m)
-            for (int k = 0; k < PAR_DEVICE; ++k) hp[(size_t)PAR_DEVICE * m + k] = par(m, k);
-        if ((e = cudaMemcpyAsync(c.d_params.p, hp.data(), sizeof(double) * hp.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            for (int k = 0; k < PAR_DEVICE; ++k) hpp[(size_t)PAR_DEVICE * m + k] = par(m, k);
+        if ((e = cudaMemcpyAsync(c.d_params.p, hpp, sizeof(double) * np, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
             err = cuda_msg("parameter copy", e);
             return ST_DATA_MISSING;
         }
@@ -534,26 +557,22 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // ---- the per-model parameters, then the weight operand (one stream: run side by side they took longer than in
     // turn)
     prof_mark(c, 0);
-    ModelParamArgs ma;
-    ma.n = n; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
-    ma.i0 = i0; ma.par = d_par; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p; ma.zt = c.d_zt.p; ma.dl = c.d_dl.p;
-    ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p; ma.zinfo = c.d_zinfo.p; ma.dist = c.d_dist.p;
-    ma.lnlam = c.d_lnlam.p;
-    {
-        const int smem = (c.add_igm_absorption == 1 ? c.jtop : 0) * 6 * (int)sizeof(float);
-        if (smem > 48 * 1024 &&
-            (e = cudaFuncSetAttribute(model_params_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess) {
-            err = cuda_msg("model parameter kernel", e);
-            return ST_DATA_MISSING;
-        }
-        model_params_kernel<<<(n + 255) / 256, 256, smem, st>>>(ma);
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) {
+    const int smem_mp = (c.add_igm_absorption == 1 ? c.jtop : 0) * 6 * (int)sizeof(float);
+    if (smem_mp > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(model_params_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_mp)) != cudaSuccess) {
         err = cuda_msg("model parameter kernel", e);
         return ST_DATA_MISSING;
     }
-    prof_mark(c, 1);
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
+    // per-model parameters of models [off, off + nk)
+    auto model_params = [&](int off, int nk) -> cudaError_t {
+        ModelParamArgs ma;
+        ma.n = nk; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
+        ma.i0 = i0; ma.par = d_par + (size_t)PAR_DEVICE * off; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p;
+        ma.zt = c.d_zt.p; ma.dl = c.d_dl.p; ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
+        ma.zinfo = c.d_zinfo.p + off; ma.dist = c.d_dist.p + off; ma.lnlam = c.d_lnlam.p;
+        model_params_kernel<<<(nk + 255) / 256, 256, smem_mp, st>>>(ma);
+        return cudaGetLastError();
+    };
     int launches = 0;
     WeightsArgs wa;
     wa.n_models = n; wa.nt = nt; wa.nz = nz; wa.kpad = kpad; wa.kmap = bop ? bop->kmap.p : nullptr;
@@ -563,78 +582,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.itesc = itesc;
     wa.grid = 0;
     float *d_y = c.d_young.p, *d_o = c.d_old.p;
-    if (fp64) {
-        // ---- the plain FP64 path: DGEMM age sums, then the rest in FP64 (spectra into d_spec64, magnitudes)
-        const int rc = run_fp64_tail(c, io, bop, d_wz, d_par, nacc, any_smooth ? sm_lo : ns, any_smooth ? sm_hi : -1,
-                                     i0, err);
-        if (rc) return rc;
-        prof_mark(c, 2);
-        prof_mark(c, 3);
-        launches = 5;   // model parameters, weights gather, two DGEMMs, the FP64 tail
-    } else if (ops) {
-        // ---- the operator: the IMF weights folded with the SFH weights, the template GEMM, then the epilogue
-        std::vector<double> al((size_t)3 * n);
-        for (int m = 0; m < n; ++m) {
-            al[3 * m] = par(m, PF_IMF1); al[3 * m + 1] = par(m, PF_IMF2); al[3 * m + 2] = par(m, PF_IMF3);
-        }
-        if ((e = c.d_alpha.reserve(al.size())) != cudaSuccess || (e = c.d_yo.reserve((size_t)2 * n * ns + 4)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(c.d_alpha.p, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
-            err = cuda_msg("operator inputs", e);
-            return ST_DATA_MISSING;
-        }
-        d_y = c.d_yo.p;
-        d_o = c.d_yo.p + (size_t)n * ns;
-        const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, itesc, d_y, d_o, err);
-        if (rc) return rc;
-        prof_mark(c, 2);
-        PartsEpilogueArgs pe;
-        pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
-        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = d_y; pe.old = d_o;
-        pe.spec = c.d_spec.p;
-        if ((e = run_parts_epilogue(pe, st)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
-        prof_mark(c, 3);
-        launches = 5;   // model parameters, fold, template GEMM, epilogue (+ the parameter upload)
-    } else {
-    if ((e = run_weights_convert(wa, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
-    prof_mark(c, 2);
-
-    // ---- contraction + epilogue
-    ContractPlan pl;
-    pl.tm_a_hi = bop->tm_hi;
-    pl.tm_a_lo = bop->tm_lo;
-    pl.num_sms = c.num_sms;
-    if ((e = encode_tmap_2d_bf16(&pl.tm_b_hi, c.d_whi.p, kpad, n, contract_bk(), bn)) != cudaSuccess ||
-        (e = encode_tmap_2d_bf16(&pl.tm_b_lo, c.d_wlo.p, kpad, n, contract_bk(), bn)) != cudaSuccess) {
-        err = cuda_msg("weights tensor map", e);
-        return ST_DATA_MISSING;
-    }
-    ContractArgs ca;
-    ca.nspec = ns; ca.n_models = n;
-    ca.n_ptiles = (ns + contract_out_rows() - 1) / contract_out_rows();
-    ca.n_mtiles = n_mtiles;
-    ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
-    ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
-    ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p; ca.spec = c.d_spec.p;
-    ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
-    ca.young = ca.old = nullptr;
-    if (parts) {
-        // (4 floats of padding: the reverse pass copies whole 16-byte units of each row)
-        if ((e = c.d_young.reserve((size_t)n * ns + 4)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns + 4)) != cudaSuccess) {
-            err = cuda_msg("device memory", e);
-            return ST_DATA_MISSING;
-        }
-        ca.young = c.d_young.p;
-        ca.old = c.d_old.p;
-        d_y = c.d_young.p;
-        d_o = c.d_old.p;
-    }
-    ca.status = c.d_status.p;
-    if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
-    prof_mark(c, 3);
-    launches = 3;   // weight operand, model parameters, contraction
-    }
-
-    // ---- bands and magnitudes
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
     if (want_mags && !fp64) {
         std::vector<int> do_band(nb, 1);
@@ -644,26 +591,155 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("band mask", e);
             return ST_DATA_MISSING;
         }
+    }
+    // bands and magnitudes of models [off, off + nk)
+    auto bands = [&](int off, int nk) -> cudaError_t {
         BandGemmArgs ba;
-        ba.n_models = n; ba.nspec = ns; ba.nbands = nb; ba.npad = c.band_npad; ba.nkb = c.band_nkb; ba.j0 = c.band_j0;
-        ba.ld_spec = ns; ba.spec = c.d_spec.p; ba.zinfo = c.d_zinfo.p; ba.wl = c.d_wl.p; ba.dlnl = c.dlnl;
-        ba.dist = c.d_dist.p;
+        ba.n_models = nk; ba.nspec = ns; ba.nbands = nb; ba.npad = c.band_npad; ba.nkb = c.band_nkb; ba.j0 = c.band_j0;
+        ba.ld_spec = ns; ba.spec = c.d_spec.p + (size_t)ns * off; ba.zinfo = c.d_zinfo.p + off; ba.wl = c.d_wl.p;
+        ba.dlnl = c.dlnl; ba.dist = c.d_dist.p + off;
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
-        ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev; ba.mags = io.dev_inputs ? io.mags : c.d_mags.p;
+        ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev ? io.fband_dev + (size_t)nb * off : nullptr;
+        ba.mags = (io.dev_inputs ? io.mags : c.d_mags.p) + (size_t)nb * off;
         ba.status = c.d_status.p;
-        ba.wz = d_wz; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = nullptr; ba.nt = nt; ba.ntz = nt * nz;
-        ba.parts = wa.parts; ba.itesc = itesc;
-        if ((e = run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
-        ++launches;
+        ba.wz = d_wz + (size_t)nt * nz * off; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = nullptr; ba.nt = nt;
+        ba.ntz = nt * nz; ba.parts = wa.parts; ba.itesc = itesc;
+        return run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st);
+    };
+    if (!fp64 && !ops) {
+        // ---- the mixed path over models [off, off + nk): weight operand, contraction with its epilogue, bands,
+        // FP64 sums (stage marks on the first range)
+        auto run_range = [&](int off, int nk, bool marks, bool tail) -> int {
+            if ((e = model_params(off, nk)) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
+            if (marks) prof_mark(c, 1);
+            WeightsArgs w = wa;
+            w.n_models = nk; w.wz = d_wz + (size_t)nt * nz * off; w.w_hi = c.d_whi.p + (size_t)kpad * off;
+            w.w_lo = c.d_wlo.p + (size_t)kpad * off; w.sums = c.d_sums.p + (size_t)6 * off;
+            if ((e = run_weights_convert(w, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
+            if (marks) prof_mark(c, 2);
+            ContractPlan pl;
+            pl.tm_a_hi = bop->tm_hi;
+            pl.tm_a_lo = bop->tm_lo;
+            pl.num_sms = c.num_sms;
+            if ((e = encode_tmap_2d_bf16(&pl.tm_b_hi, w.w_hi, kpad, nk, contract_bk(), bn)) != cudaSuccess ||
+                (e = encode_tmap_2d_bf16(&pl.tm_b_lo, w.w_lo, kpad, nk, contract_bk(), bn)) != cudaSuccess) {
+                err = cuda_msg("weights tensor map", e);
+                return ST_DATA_MISSING;
+            }
+            ContractArgs ca;
+            ca.nspec = ns; ca.n_models = nk;
+            ca.n_ptiles = (ns + contract_out_rows() - 1) / contract_out_rows();
+            ca.n_mtiles = (nk + bn - 1) / bn;
+            ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
+            ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
+            ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
+            ca.spec = c.d_spec.p + (size_t)ns * off;
+            ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
+            ca.young = ca.old = nullptr;
+            if (parts) {
+                ca.young = d_y + (size_t)ns * off;
+                ca.old = d_o + (size_t)ns * off;
+            }
+            ca.status = c.d_status.p;
+            if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
+            if (marks) prof_mark(c, 3);
+            launches += 3;
+            if (!tail) return 0;
+            if (want_mags) {
+                if ((e = bands(off, nk)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+                ++launches;
+            }
+            if (marks) prof_mark(c, 4);
+            if ((e = run_weights_prep(w, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+            ++launches;
+            return 0;
+        };
+        if (parts) {
+            // (4 floats of padding: the reverse pass copies whole 16-byte units of each row)
+            if ((e = c.d_young.reserve((size_t)n * ns + 4)) != cudaSuccess || (e = c.d_old.reserve((size_t)n * ns + 4)) != cudaSuccess) {
+                err = cuda_msg("device memory", e);
+                return ST_DATA_MISSING;
+            }
+            d_y = c.d_young.p;
+            d_o = c.d_old.p;
+        }
+        if (!chunked) {
+            if (int rc = run_range(0, n, true, true)) return rc;
+        } else {
+            // chunks: the weight operand and the contraction (which hide the copies); then the bands and the FP64
+            // sums over the whole batch (efficient only at full size)
+            const int nch = (n + CHUNK - 1) / CHUNK;
+            for (int k = 0; k < nch; ++k) {
+                const int off = k * CHUNK, nk = std::min(CHUNK, n - off);
+                cudaEvent_t &ev = c.chunk_ev[k % Context::NCHUNK_EV];
+                if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+                    err = cuda_msg("chunk event", e);
+                    return ST_DATA_MISSING;
+                }
+                if ((e = cudaMemcpyAsync(c.d_wz.p + (size_t)nt * nz * off, io.wz + (size_t)nt * nz * off,
+                                         sizeof(double) * nt * nz * nk, cudaMemcpyHostToDevice, c.side)) != cudaSuccess ||
+                    (e = cudaEventRecord(ev, c.side)) != cudaSuccess || (e = cudaStreamWaitEvent(st, ev, 0)) != cudaSuccess) {
+                    err = cuda_msg("weights copy", e);
+                    return ST_DATA_MISSING;
+                }
+                if (int rc = run_range(off, nk, k == 0, false)) return rc;
+            }
+            if (want_mags) {
+                if ((e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+                ++launches;
+            }
+            prof_mark(c, 4);
+            if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+            ++launches;
+        }
+        prof_mark(c, 5);
+    } else {
+        if ((e = model_params(0, n)) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
+        prof_mark(c, 1);
+        if (fp64) {
+            // ---- the plain FP64 path: DGEMM age sums, then the rest in FP64 (spectra into d_spec64, magnitudes)
+            const int rc = run_fp64_tail(c, io, bop, d_wz, d_par, nacc, any_smooth ? sm_lo : ns, any_smooth ? sm_hi : -1,
+                                         i0, err);
+            if (rc) return rc;
+            prof_mark(c, 2);
+            prof_mark(c, 3);
+            launches = 5;   // model parameters, weights gather, two DGEMMs, the FP64 tail
+        } else if (ops) {
+            // ---- the operator: the IMF weights folded with the SFH weights, the template GEMM, then the epilogue
+            std::vector<double> al((size_t)3 * n);
+            for (int m = 0; m < n; ++m) {
+                al[3 * m] = par(m, PF_IMF1); al[3 * m + 1] = par(m, PF_IMF2); al[3 * m + 2] = par(m, PF_IMF3);
+            }
+            if ((e = c.d_alpha.reserve(al.size())) != cudaSuccess || (e = c.d_yo.reserve((size_t)2 * n * ns + 4)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(c.d_alpha.p, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+                err = cuda_msg("operator inputs", e);
+                return ST_DATA_MISSING;
+            }
+            d_y = c.d_yo.p;
+            d_o = c.d_yo.p + (size_t)n * ns;
+            const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, itesc, d_y, d_o, err);
+            if (rc) return rc;
+            prof_mark(c, 2);
+            PartsEpilogueArgs pe;
+            pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
+            pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = d_y; pe.old = d_o;
+            pe.spec = c.d_spec.p;
+            if ((e = run_parts_epilogue(pe, st)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+            prof_mark(c, 3);
+            launches = 5;   // model parameters, fold, template GEMM, epilogue (+ the parameter upload)
+        }
+        if (want_mags && !fp64) {
+            if ((e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+            ++launches;
+        }
+        prof_mark(c, 4);
+        // the FP64 mass and L_bol sums (the operator's fold forms its own)
+        if (fp64) {
+            if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
+            ++launches;
+        }
+        prof_mark(c, 5);
     }
-    prof_mark(c, 4);
-    // the FP64 mass and L_bol sums (alone: beside the contraction or the band GEMM they slow those more than they take;
-    // the operator's fold forms its own)
-    if (!ops) {
-        if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
-        ++launches;
-    }
-    prof_mark(c, 5);
     c.last_launches = launches + ((io.spec && !io.dev_inputs) ? 1 : 0);
     if (io.dev_inputs) {
         c.last_n = n;
@@ -749,11 +825,23 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             return ST_DATA_MISSING;
         }
     }
-    std::vector<double> sums;
     const bool want_sums = io.mass || io.lbol || io.mass_young || io.mass_old || io.lbol_young || io.lbol_old;
+    const double *sums = nullptr;
     if (want_sums && !io.dev_inputs) {
-        sums.resize((size_t)6 * n);
-        if ((e = cudaMemcpyAsync(sums.data(), c.d_sums.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
+        // through a page-locked buffer kept by the context
+        const size_t ns6 = (size_t)6 * n;
+        if (c.pinned_sums_n < ns6) {
+            if (c.pinned_sums) cudaFreeHost(c.pinned_sums);
+            c.pinned_sums = nullptr;
+            c.pinned_sums_n = 0;
+            if ((e = cudaMallocHost(&c.pinned_sums, sizeof(double) * ns6)) != cudaSuccess) {
+                err = cuda_msg("page-locked sums", e);
+                return ST_DATA_MISSING;
+            }
+            c.pinned_sums_n = ns6;
+        }
+        sums = c.pinned_sums;
+        if ((e = cudaMemcpyAsync(c.pinned_sums, c.d_sums.p, sizeof(double) * ns6, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
             err = cuda_msg("sums copy", e);
             return ST_DATA_MISSING;
         }
@@ -786,8 +874,9 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.last_n = n;
     c.geom.n = n;
     if (want_sums && !io.dev_inputs) {
+#pragma omp parallel for schedule(static) if (n >= 8192)
         for (int m = 0; m < n; ++m) {
-            const double *s = sums.data() + (size_t)6 * m;
+            const double *s = sums + (size_t)6 * m;
             if (io.mass) io.mass[m] = s[0];
             if (io.lbol) io.lbol[m] = s[1] > SAFE_FLOOR ? std::log10(s[1]) : 0.0;
             if (io.mass_young) io.mass_young[m] = s[2];

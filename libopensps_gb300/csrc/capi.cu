@@ -62,8 +62,10 @@ const char *const GRAD_NAMES[OPENSPS_NBGRAD] = {
 // names / values -> PF_COUNT x n rows (the context's values, with the named ones per model). 0, or a status.
 int build_params(Context &c, int n, int n_params, const char *const *names, const double *const *values,
                  std::vector<double> &rows, std::string &err) {
-    rows.resize((size_t)PF_COUNT * n);
-    for (int m = 0; m < n; ++m) std::memcpy(rows.data() + (size_t)PF_COUNT * m, c.pdef, sizeof(double) * PF_COUNT);
+    if (rows.size() < (size_t)PF_COUNT * n) rows.resize((size_t)PF_COUNT * n);
+    double *rp = rows.data();
+#pragma omp parallel for schedule(static) if (n >= 8192)
+    for (int m = 0; m < n; ++m) std::memcpy(rp + (size_t)PF_COUNT * m, c.pdef, sizeof(double) * PF_COUNT);
     if (n_params < 0) { err = "n_params < 0"; return ST_BAD_ARG; }
     if (n_params > 0 && (!names || !values)) { err = "names / values are NULL"; return ST_BAD_ARG; }
     for (int i = 0; i < n_params; ++i) {
@@ -74,7 +76,10 @@ int build_params(Context &c, int n, int n_params, const char *const *names, cons
             return ST_UNSUPPORTED;
         }
         if (!values[i]) { err = std::string("compute_csp_batch: no values for ") + pi->name; return ST_BAD_ARG; }
-        for (int m = 0; m < n; ++m) rows[(size_t)PF_COUNT * m + pi->id] = values[i][m];
+        const double *v = values[i];
+        const int id = pi->id;
+#pragma omp parallel for schedule(static) if (n >= 8192)
+        for (int m = 0; m < n; ++m) rp[(size_t)PF_COUNT * m + id] = v[m];
     }
     return 0;
 }
@@ -102,7 +107,7 @@ int batch_core(Context &cref, int n, int n_params, const char *const *names, con
     if (!mags && !c->fast_mode) { err = "mags is required"; return ST_BAD_ARG; }
     if (indx) { err = "spectral indices are not computed on this path"; return ST_UNSUPPORTED; }
     if (zred_mags) { err = "zred_mags is not supported on this path"; return ST_UNSUPPORTED; }
-    std::vector<double> rows;
+    std::vector<double> &rows = c->param_rows;     // kept between calls (no fresh pages per batch)
     int st = build_params(*c, n, n_params, names, values, rows, err);
     if (st) return st;
     // weights: the caller's over ages and metallicities, or over ages (blended at logzsol on the device), or the

@@ -174,6 +174,16 @@ Context::~Context() {
     fp64_release(*this);
     emu.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
+    if (pinned_par) cudaFreeHost(pinned_par);
+    pinned_par = nullptr;
+    pinned_par_n = 0;
+    if (pinned_sums) cudaFreeHost(pinned_sums);
+    pinned_sums = nullptr;
+    pinned_sums_n = 0;
+    for (int i = 0; i < NCHUNK_EV; ++i) {
+        if (chunk_ev[i]) cudaEventDestroy(chunk_ev[i]);
+        chunk_ev[i] = nullptr;
+    }
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
     if (ev_fork) cudaEventDestroy(ev_fork);
