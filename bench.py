@@ -358,6 +358,51 @@ def emulator_measure(args, torch, barrier) -> dict | None:
             "speedup_vs_same_physics_csp": value / csp_rate, "e2e_speedup_vs_same_physics_csp": (n / (e2e_ms * 1e-3)) / csp_rate}
 
 
+def sfh_config_measure(args, torch, barrier) -> dict | None:
+    """The plain batched CSP of the delayed-tau configuration at B = --sfh-batch (256): tau log-uniform 0.1-10 Gyr,
+    tage uniform 1-13.7 Gyr, logZ uniform -2..0.5 (the two-slab blend), power-law dust tau_V uniform 0-2 with slope
+    -0.7, z = 0, no nebular emission, 20 Gaussian filters; spectra (FP64) and magnitudes to the host. Timed through the
+    C API on the mixed path and on the plain FP64 GPU path (SFH weights formed on the device in both), and the FP64 CPU
+    oracle (OpenMP, the machine's cores) on the same models."""
+    from libopensps_gb300 import synthdata
+    from libopensps_gb300.capi import Context
+    from oracle.oracle import Oracle, SFH_NAMES, blend_at_logzsol, sfh_weights
+    n = args.sfh_batch
+    if n <= 0:
+        return None
+    rng = np.random.default_rng(0)
+    params = {"tau": 10.0 ** rng.uniform(-1.0, 1.0, n), "tage": rng.uniform(1.0, 13.7, n),
+              "logzsol": rng.uniform(-2.0, 0.5, n), "dust2": rng.uniform(0.0, 2.0, n), "dust_index": np.full(n, -0.7)}
+    out = {}
+    for name, fp64 in (("mixed", 0), ("fp64", 1)):
+        ctx = Context()
+        ctx.set_filters_library("gauss20")
+        ctx.set_int("sfh", 4)
+        ctx.set_int("gb300_fp64", fp64)
+        try:
+            for _ in range(max(args.warmup, 1)):
+                ctx.csp_batch(params)
+            t0 = time.perf_counter()
+            for _ in range(args.sfh_steps):
+                ctx.csp_batch(params)
+            out[name] = n / ((time.perf_counter() - t0) / args.sfh_steps)
+        except Exception as exc:          # a path that refuses the configuration: reported, not fatal
+            out[name] = f"unavailable: {exc}"
+        ctx.close()
+    data = synthdata.load()
+    o = Oracle(data, nbands=20, add_neb=False, add_igm=False)
+    t0 = time.perf_counter()
+    w, _ = sfh_weights(data["log_age"], 4, params, n)
+    wz, _ = blend_at_logzsol(data, w, params["logzsol"])
+    o.csp_batch({k: v for k, v in params.items() if k not in SFH_NAMES and k != "logzsol"}, wz)
+    cpu = n / (time.perf_counter() - t0)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"batch": n, "unit": "models/s", "mixed_e2e": out["mixed"], "fp64_gpu_e2e": out["fp64"],
+            "cpu_oracle": {"value": cpu, "cores": cores, "kind": "port"},
+            "outputs": "spectra (FP64) and 20 magnitudes to the host",
+            "workload": "delayed-tau SFH on the device, logZ blend, power-law dust, z = 0, no nebular emission"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -438,6 +483,7 @@ def run_ours(args) -> None:
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
+    sfh_cfg = sfh_config_measure(args, torch, barrier) if rank == 0 else None
     emulator = emulator_measure(args, torch, barrier) if rank == 0 else None
     if emulator:
         emulator["speedup_vs_mixed_csp"] = emulator["value"] / value
@@ -475,6 +521,7 @@ def run_ours(args) -> None:
             "ssp_operator": ssp_ops,
             "fp64_path": fp64,
             "mixed_over_fp64": (value / fp64["device_value"]) if fp64 and fp64.get("device_value") else None,
+            "sfh_config": sfh_cfg,
             "emulator": emulator,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
@@ -499,6 +546,8 @@ def main():
     ap.add_argument("--ops-steps", type=int, default=10)
     ap.add_argument("--fp64-batch", type=int, default=65536)
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--sfh-batch", type=int, default=256)
+    ap.add_argument("--sfh-steps", type=int, default=20)
     ap.add_argument("--emu-batch", type=int, default=1048576)
     ap.add_argument("--emu-steps", type=int, default=20)
     ap.add_argument("--emu-e2e-steps", type=int, default=2)

@@ -60,22 +60,9 @@ def rel_err_spec(got: np.ndarray, ref: np.ndarray, floor: float = 1e-6) -> float
 
 
 def blend_at_logzsol(data, w, logzsol):
-    """Weights over ages (n, nt) blended between the two metallicities bracketing logzsol (not clamped), and the
-    log-blended L_bol (total, young ages <= 7.0 dex, old) of the model_sums MSUMS_BLEND form."""
-    n, nt = w.shape
-    lz = np.log10(data["zlegend"] / 0.0142)
-    nz = lz.size
-    wz = np.zeros((n, nz, nt))
-    lb = np.zeros((n, 3))
-    young = data["log_age"] <= 7.0
-    for m in range(n):
-        zlo = min(max(np.searchsorted(lz, logzsol[m], side="right") - 1, 0), nz - 2)
-        dz = (logzsol[m] - lz[zlo]) / (lz[zlo + 1] - lz[zlo])
-        wz[m, zlo] = (1 - dz) * w[m]
-        wz[m, zlo + 1] = dz * w[m]
-        lk = np.where(w[m] > 0, w[m] * 10.0 ** ((1 - dz) * data["ssp_lbol"][zlo] + dz * data["ssp_lbol"][zlo + 1]), 0.0)
-        lb[m] = [lk.sum(), lk[young].sum(), lk[~young].sum()]
-    return wz, lb
+    """The oracle's metallicity blend (oracle.oracle.blend_at_logzsol)."""
+    from oracle.oracle import blend_at_logzsol as blend
+    return blend(data, w, logzsol)
 
 
 def oracle_sfh_csp(oracle, data, sfh, params):
