@@ -589,13 +589,41 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     io.fband_dev = nb > 0 ? c.d_fband.p : nullptr;
     int st = run_batch(c, io, err);
     if (st) return st;
+    // with the SSP operators the age sums came from the operator (no basis operand): the reverse pass goes through
+    // the transposed library and the reverse fold instead
+    const bool ops = c.ops.ready;
     BasisOperand *bop = c.geom.bop;
-    if (!bop || c.geom.nacc != 2 || c.geom.n != n) { err = "reverse pass: the forward's state is missing"; return ST_DATA_MISSING; }
+    if ((!ops && !bop) || (ops && !c.geom.wz) || c.geom.nacc != 2 || c.geom.n != n) {
+        err = "reverse pass: the forward's state is missing";
+        return ST_DATA_MISSING;
+    }
     cudaStream_t s = c.stream;
-    const int kpad = bop->kpad;
+    const int kpad = ops ? 0 : bop->kpad;
 
+    // ---- the transposed library (once per operator): the B operand of the template cotangents' GEMM
+    if (ops && !c.ops.lib_thi.p) {
+        SspOps &o = c.ops;
+        const int ppad = (ns + gemm_bk() - 1) / gemm_bk() * gemm_bk();
+        if ((e = o.lib_thi.reserve((size_t)o.ntpad * ppad)) != cudaSuccess ||
+            (e = o.lib_tlo.reserve((size_t)o.ntpad * ppad)) != cudaSuccess) {
+            err = msg("device memory", e);
+            o.lib_thi.release(); o.lib_tlo.release();
+            return ST_DATA_MISSING;
+        }
+        const dim3 grid((o.ntpad + 31) / 32, (ppad + 31) / 32), block(32, 8);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_hi.p, o.lib_thi.p, ns, o.ntpad, ppad);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_lo.p, o.lib_tlo.p, ns, o.ntpad, ppad);
+        if ((e = cudaGetLastError()) != cudaSuccess ||
+            (e = encode_tmap_2d_bf16(&o.tm_lib_thi, o.lib_thi.p, ppad, o.ntpad, gemm_bk(), gemm_bn())) != cudaSuccess ||
+            (e = encode_tmap_2d_bf16(&o.tm_lib_tlo, o.lib_tlo.p, ppad, o.ntpad, gemm_bk(), gemm_bn())) != cudaSuccess) {
+            err = msg("transposed library", e);
+            o.lib_thi.release(); o.lib_tlo.release();
+            return ST_DATA_MISSING;
+        }
+        o.ppad = ppad;
+    }
     // ---- the transposed basis (once per operand) and its column map
-    if (!bop->thi.p) {
+    if (!ops && !bop->thi.p) {
         const int ppad = (ns + gemm_bk() - 1) / gemm_bk() * gemm_bk();
         std::vector<int> kmap(kpad), col_of(ntz, 0);
         if ((e = cudaMemcpy(kmap.data(), bop->kmap.p, sizeof(int) * kpad, cudaMemcpyDeviceToHost)) != cudaSuccess) {
@@ -624,7 +652,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         }
         bop->ppad = ppad;
     }
-    const int ppad = bop->ppad;
+    const int ppad = ops ? c.ops.ppad : bop->ppad;
 
     // ---- cotangents to the device
     auto put = [&](DevBuf<double> &d, const double *h, size_t cnt) -> cudaError_t {
@@ -658,7 +686,9 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     a.j0 = c.band_j0; a.j1 = nb > 0 ? c.band_j1 : c.band_j0 - 1;
     a.sm_lo = c.geom.sm_lo; a.sm_hi = c.geom.sm_hi; a.uniform_index = c.geom.uniform_index;
     a.dl2 = (float)(c.dlnl * 1.4426950408889634); a.inv_em1 = (float)(1.0 / std::expm1(c.dlnl));
-    a.young = c.d_young.p; a.old = c.d_old.p; a.mpar = c.d_mpar.p; a.apar = c.d_apar.p; a.par = c.d_params.p;
+    a.young = ops ? c.d_yo.p : c.d_young.p;
+    a.old = ops ? c.d_yo.p + (size_t)n * ns : c.d_old.p;
+    a.mpar = c.d_mpar.p; a.apar = c.d_apar.p; a.par = c.d_params.p;
     a.zinfo = c.d_zinfo.p; a.fband = c.d_fband.p;
     a.mags_bar = mags_bar ? c.d_mags_bar.p : nullptr;
     a.spec_bar = spec_bar ? c.d_spec_bar.p : nullptr;
@@ -677,7 +707,55 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     // metallicities; with weights formed on the device, then through the blend and the SFH below)
     const bool dev_blend = io_in.sfh_par != nullptr;
     const bool sfh_rev = dev_blend && (weights_bar || params_bar);
-    if (weights_z_bar || sfh_rev) {
+    if (ops) {
+        // ---- the operator: template cotangents (young and old pixel cotangents against the transposed library),
+        // then the reverse fold: the weights' cotangent at every grid point (when wanted) and the slopes' rows
+        const SspOps &o = c.ops;
+        const bool want_wzb = weights_z_bar || sfh_rev;
+        if ((e = c.d_vbar.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
+            (e = c.d_apart.reserve((size_t)c.nz * n * 3)) != cudaSuccess ||
+            (want_wzb && (e = c.d_wzbar.reserve((size_t)n * ntz)) != cudaSuccess)) {
+            err = msg("device memory", e);
+            return ST_DATA_MISSING;
+        }
+        for (int part = 0; part < 2; ++part) {
+            GemmArgs g;
+            g.M = n; g.N = o.ntpad; g.K = ppad; g.ldd = o.ntpad; g.b_row0 = 0; g.status = c.d_status.p;
+            g.D = c.d_vbar.p + (size_t)part * n * o.ntpad;
+            GemmPlan pl;
+            pl.num_sms = c.num_sms;
+            pl.tm_b_hi = o.tm_lib_thi;
+            pl.tm_b_lo = o.tm_lib_tlo;
+            const __nv_bfloat16 *ah = part == 0 ? c.d_ybh.p : c.d_obh.p, *al = part == 0 ? c.d_ybl.p : c.d_obl.p;
+            if ((e = encode_tmap_2d_bf16(&pl.tm_a_hi, ah, ppad, n, gemm_bk(), gemm_bm())) != cudaSuccess ||
+                (e = encode_tmap_2d_bf16(&pl.tm_a_lo, al, ppad, n, gemm_bk(), gemm_bm())) != cudaSuccess) {
+                err = msg("cotangent tensor map", e);
+                return ST_DATA_MISSING;
+            }
+            if ((e = run_gemm_bf16x3(pl, g, s)) != cudaSuccess) { err = msg("template cotangent GEMM", e); return ST_DATA_MISSING; }
+            ++launches;
+        }
+        prof_mark(c, 8);
+        OpsRevArgs r;
+        r.n = n; r.nt = c.nt; r.nz = c.nz; r.npt = o.npt; r.ntpad = o.ntpad; r.itesc = c.geom.itesc;
+        r.lim_lo = 0.08f; r.lim_hi = 120.f;
+        r.wz = c.geom.wz; r.alpha = c.d_alpha.p; r.pts = o.pts.p; r.pidx = o.pidx.p; r.pcoef = o.pcoef.p;
+        r.vbar = c.d_vbar.p; r.cscale = c.d_cscale.p;
+        r.mass_bar = mass_bar ? c.d_mass_bar.p : nullptr;
+        r.lbol_bar = lbol_bar ? c.d_lbol_bar.p : nullptr;   // (L_bol with the operators: the linear row, always)
+        r.sums = c.d_sums.p;
+        r.wzb = want_wzb ? c.d_wzbar.p : nullptr;
+        r.apart = c.d_apart.p;
+        r.params_bar = c.d_pbar.p; r.rows = NBGRAD; r.row_imf1 = PB_IMF1;
+        if ((e = run_ops_reverse(r, s)) != cudaSuccess) { err = msg("operator reverse kernel", e); return ST_DATA_MISSING; }
+        prof_mark(c, 9);
+        launches += 2;
+        if (weights_z_bar &&
+            (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * n * ntz, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+            err = msg("weights cotangent copy", e);
+            return ST_DATA_MISSING;
+        }
+    } else if (weights_z_bar || sfh_rev) {
         if ((e = c.d_wzb32.reserve((size_t)n * kpad)) != cudaSuccess || (e = c.d_wzbar.reserve((size_t)n * ntz)) != cudaSuccess) {
             err = msg("device memory", e);
             return ST_DATA_MISSING;
@@ -734,7 +812,8 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         r.n = n; r.nt = nt; r.nz = c.nz; r.sfh = io_in.sfh_type; r.rows = NBGRAD; r.has_logzsol = 1;
         r.sfh_tangents = tangents ? 1 : 0;
         r.tf = c.d_logage.p; r.lz = c.d_lz.p; r.lbol = c.d_lbol.p; r.par = c.d_sfhpar.p; r.w = c.d_w.p;
-        r.lblend = c.d_lblend.p; r.lbol_bar = lbol_bar ? c.d_lbol_bar.p : nullptr; r.wzb = c.d_wzbar.p;
+        // (with the operators L_bol is the linear row, whose cotangent the reverse fold took)
+        r.lblend = c.d_lblend.p; r.lbol_bar = (lbol_bar && !ops) ? c.d_lbol_bar.p : nullptr; r.wzb = c.d_wzbar.p;
         r.weights_bar = c.d_wbar.p; r.scratch = c.d_sfh_scratch.p; r.params_bar = c.d_pbar.p;
         r.dual = tangents ? (void *)c.d_dual.p : nullptr;
         if ((e = run_sfh_reverse(r, s)) != cudaSuccess) { err = msg("SFH reverse kernel", e); return ST_DATA_MISSING; }

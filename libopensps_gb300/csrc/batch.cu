@@ -424,7 +424,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts) { err = "gradients with the SSP operators are not supported on this path"; return ST_UNSUPPORTED; }
         if (c.imf_type != 2) { err = "imf_type " + std::to_string(c.imf_type) + ": only 2 (Kroupa) with the operators"; return ST_UNSUPPORTED; }
         nacc2 = true;
     } else {
@@ -476,6 +475,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.geom.sm_lo = any_smooth ? sm_lo : ns;
     c.geom.sm_hi = any_smooth ? sm_hi : -1;
     c.geom.uniform_index = uniform_index ? 1 : 0;
+    c.geom.itesc = itesc;
+    c.geom.wz = nullptr;
     c.geom.n = 0;
 
     // ---- scratch
@@ -717,6 +718,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
             d_y = c.d_yo.p;
             d_o = c.d_yo.p + (size_t)n * ns;
+            c.geom.wz = d_wz;
             const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, itesc, d_y, d_o, err);
             if (rc) return rc;
             prof_mark(c, 2);

@@ -82,13 +82,27 @@ struct SspOps {
     DevBuf<float> ent_c;
     DevBuf<__nv_bfloat16> lib_hi, lib_lo;
     CUtensorMap tm_lib_hi, tm_lib_lo;
-    void release() { pts.release(); ent.release(); ent_c.release(); lib_hi.release(); lib_lo.release(); ready = false; }
+    // the reverse pass: each point's four templates and coefficients (point-major), and the library transposed
+    // (ntpad x ppad, bf16 hi / lo: the B operand of the template cotangents' GEMM, built on first use)
+    DevBuf<ushort4> pidx;
+    DevBuf<float4> pcoef;
+    DevBuf<__nv_bfloat16> lib_thi, lib_tlo;
+    CUtensorMap tm_lib_thi, tm_lib_tlo;
+    int ppad = 0;
+    void release() {
+        pts.release(); ent.release(); ent_c.release(); lib_hi.release(); lib_lo.release();
+        pidx.release(); pcoef.release(); lib_thi.release(); lib_tlo.release();
+        ppad = 0;
+        ready = false;
+    }
 };
 
 // What the reverse pass needs of the forward batch it follows.
 struct BatchGeom {
     BasisOperand *bop = nullptr;
     int nacc = 0, sm_lo = 0, sm_hi = -1, uniform_index = 0, n = 0;
+    int itesc = 0;               // the first old age
+    const double *wz = nullptr;  // the weights over ages and metallicities on the device (with the operators)
 };
 
 struct Context {
@@ -157,6 +171,8 @@ struct Context {
     DevBuf<__nv_bfloat16> d_vhi, d_vlo;
     DevBuf<float> d_yo, d_vpart;
     DevBuf<double> d_spart;
+    DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
+    DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab
     DevBuf<int> d_vflag;
     DevBuf<int> d_status;
     int last_n = 0;              // models of the last batch (device spectra valid for these)

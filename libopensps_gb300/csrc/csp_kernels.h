@@ -195,7 +195,7 @@ enum { SFH_TAGE = 0, SFH_TAU, SFH_CONST, SFH_FBURST, SFH_TBURST, SFH_SF_START, S
        SFH_LOGZSOL = 7, SFH_NCOL = 8 };
 // their params_bar rows (opensps.h)
 enum { PB_LOGZSOL = 15, PB_TAGE = 16, PB_TAU = 17, PB_CONST = 18, PB_FBURST = 19, PB_TBURST = 20, PB_SF_START = 21,
-       PB_SF_TRUNC = 24 };
+       PB_SF_TRUNC = 24, PB_IMF1 = 26 };
 struct SfhArgs {
     int n, nt, nz, sfh, itesc;
     const double *tf;        // nt: log10(age / yr) of the grid
@@ -244,6 +244,26 @@ struct OpsFoldArgs {
     int *flag;                // nz x ceil(n / 4): the slab has weight for some model of the group
 };
 cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
+// The operator's reverse pass: from the template cotangents, the cotangents of the SFH weights over ages and
+// metallicities and of the three Kroupa slopes.
+struct OpsRevArgs {
+    int n, nt, nz, npt, ntpad, itesc;
+    float lim_lo, lim_hi;
+    const double *wz;         // n x nt x nz SFH weights (age fastest)
+    const double *alpha;      // n x 3 Kroupa slopes
+    const OpsPoint *pts;      // (nt x nz) x npt
+    const ushort4 *pidx;      // (nt x nz) x npt: each point's four templates
+    const float4 *pcoef;      // and their coefficients
+    const float *vbar;        // 2n x ntpad: the template weights' cotangents / cscale (young rows, then old)
+    const double *cscale;     // n: the reverse pass's cotangent scale
+    const double *mass_bar, *lbol_bar;   // n each, or null
+    const double *sums;       // n x 6: the forward's mass and linear L_bol
+    double *wzb;              // n x nt x nz: the weights' cotangent (every grid point), or null (slopes only)
+    double *apart;            // nz x n x 3: each slab's slope cotangents / cscale
+    double *params_bar;       // n x rows: the slopes' rows row_imf1 .. row_imf1 + 2 (written), or null
+    int rows, row_imf1;
+};
+cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);
 // The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;

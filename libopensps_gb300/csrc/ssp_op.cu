@@ -74,6 +74,120 @@ __device__ __forceinline__ float imf_weight(const KroupaSeg &k, const OpsPoint &
     return v;
 }
 
+constexpr double KR_LN2 = 0.6931471805599453;
+
+// g2(x) = int_0^1 s e^(x s) ds = (e^x (x - 1) + 1) / x^2, with its Taylor series sum_k x^k / (k! (k + 2)) near 0
+// (FP64 and FP32); g1(x) = (e^x - 1) / x
+__device__ inline double kr_g1(double x) { return x == 0.0 ? 1.0 : expm1(x) / x; }
+__device__ inline double kr_g2(double x) {
+    if (fabs(x) < 0.25) {
+        const double cf[11] = {1.0 / 2, 1.0 / 3, 1.0 / 8, 1.0 / 30, 1.0 / 144, 1.0 / 840, 1.0 / 5760, 1.0 / 45360,
+                               1.0 / 403200, 1.0 / 3991680, 1.0 / 43545600};
+        double r = cf[10];
+        for (int k = 9; k >= 0; --k) r = fma(r, x, cf[k]);
+        return r;
+    }
+    return (exp(x) * (x - 1.0) + 1.0) / (x * x);
+}
+__device__ __forceinline__ float ops_g1(float x) { return x == 0.f ? 1.f : ops_expm1(x) / x; }
+__device__ __forceinline__ float ops_g2(float x) {
+    if (fabsf(x) < 0.5f) {
+        float r = 1.f / 403200.f;
+        r = fmaf(r, x, 1.f / 45360.f);
+        r = fmaf(r, x, 1.f / 5760.f);
+        r = fmaf(r, x, 1.f / 840.f);
+        r = fmaf(r, x, 1.f / 144.f);
+        r = fmaf(r, x, 1.f / 30.f);
+        r = fmaf(r, x, 1.f / 8.f);
+        r = fmaf(r, x, 1.f / 3.f);
+        return fmaf(r, x, 0.5f);
+    }
+    return fmaf(ops_ex2(x * 1.4426950408889634f), x - 1.f, 1.f) / (x * x);
+}
+
+// One model's Kroupa segments (c = 1, c2, c2 with c2 = 0.5^(alpha2 - alpha1): continuous at 0.5 and 1 Msun; the
+// FP32 constants of the bin weights) and 1 / (the IMF's mass between its limits: imf_integral, mass-weighted), in
+// FP64. With dlnT non-null also d ln(mass) / d alpha_j, j = 1..3, for the reverse pass: a segment's piece
+// P = c lo^em expm1(em dl) / em (em = 2 - alpha, dl = ln(hi / lo)) has dP/dem = c lo^em dl (ln lo g1 + dl g2)(em dl)
+// and c2 the factor 2^(alpha1 - alpha2).
+__device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
+                                    double *dlnT) {
+    const double a1 = al3[0], a2 = al3[1], a3 = al3[2];
+    const double c2 = pow(0.5, -a1 + a2);
+    const double al[3] = {a1, a2, a3}, cs[3] = {1.0, c2, c2};
+    const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
+    double total = 0.0, t12 = 0.0, dp[3] = {0.0, 0.0, 0.0};
+    for (int sg = 0; sg < 3; ++sg) {
+        const double e = 1.0 - al[sg];
+        k.e[sg] = (float)e;
+        k.c[sg] = (float)cs[sg];
+        k.ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
+        k.lo[sg] = (float)slo[sg];
+        k.hi[sg] = (float)shi[sg];
+        const double lo = fmax((double)lim_lo, slo[sg]), hi = fmin((double)lim_hi, shi[sg]);
+        if (hi > lo) {
+            const double em = 2.0 - al[sg];   // mass-weighted: int c m^(1 - alpha) dm
+            const double piece = (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
+            total += piece;
+            if (dlnT) {
+                if (sg > 0) t12 += piece;
+                const double ll = log(lo), dl = log(hi / lo), x = em * dl;
+                dp[sg] = cs[sg] * pow(lo, em) * dl * (ll * kr_g1(x) + dl * kr_g2(x));
+            }
+        }
+    }
+    inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
+    if (dlnT) {
+        const double it = total > 0.0 ? 1.0 / total : 0.0;
+        dlnT[0] = (-dp[0] + KR_LN2 * t12) * it;
+        dlnT[1] = (-dp[1] - KR_LN2 * t12) * it;
+        dlnT[2] = -dp[2] * it;
+    }
+}
+
+// A point's IMF bin weight (before the normalisation) and its derivatives: phi = sum of its segments' pieces
+// P_s = c_s lo^e dl g1(e dl), D_s = dP_s / de_s = c_s lo^e dl (ln lo g1 + dl g2), and p12 the pieces in segments 2
+// and 3 (those scaled by c2). Then dphi/dalpha1 = -D_1 + ln 2 p12, dphi/dalpha2 = -D_2 - ln 2 p12,
+// dphi/dalpha3 = -D_3.
+struct ImfTan {
+    float phi, d0, d1, d2, p12;
+};
+__device__ __forceinline__ void seg_piece_tan(const KroupaSeg &k, int s, float ln_lo, float dl, float &P, float &D) {
+    const float x = k.e[s] * dl;
+    const float b = k.c[s] * ops_ex2(k.e[s] * ln_lo * 1.4426950408889634f) * dl;
+    const float g1 = ops_g1(x);
+    P = b * g1;
+    D = b * fmaf(ln_lo, g1, dl * ops_g2(x));
+}
+__device__ __forceinline__ ImfTan imf_weight_tan(const KroupaSeg &k, const OpsPoint &q) {
+    ImfTan r = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (q.seg < 0) return r;
+    float P, D;
+    if (q.seg > 0) {
+        const int s = q.seg - 1;
+        seg_piece_tan(k, s, q.ln_lo, q.dl, P, D);
+        r.phi = P;
+        r.d0 = s == 0 ? D : 0.f;
+        r.d1 = s == 1 ? D : 0.f;
+        r.d2 = s == 2 ? D : 0.f;
+        r.p12 = s > 0 ? P : 0.f;
+        return r;
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
+        if (hi > lo) {
+            seg_piece_tan(k, s, logf(lo), logf(hi / lo), P, D);
+            r.phi += P;
+            if (s == 0) r.d0 += D;
+            else if (s == 1) r.d1 += D;
+            else r.d2 += D;
+            if (s > 0) r.p12 += P;
+        }
+    }
+    return r;
+}
+
 // OPS_K models per CTA: every point record and entry is read once for all of them. A CTA takes one metallicity slab
 // (blockIdx.y) of its OPS_K models; the slabs' template weights are summed after (ops_reduce_kernel), in slab order.
 constexpr int OPS_K = 4;
@@ -108,30 +222,8 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_fold_kernel(OpsFoldArgs a)
         const double sw = k < nk ? a.wz[(size_t)ng * (m0 + k) + t + (size_t)a.nt * z] : 0.0;
         sw_s[t][k] = (sw > SAFE_FLOOR) ? (float)sw : 0.f;
     }
-    if (tid < OPS_K) {
-        const int k = tid;
-        // the segments' constants and the IMF's mass over its limits (imf_integral, mass-weighted), in FP64
-        const int m = min(m0 + k, a.n - 1);
-        const double a1 = a.alpha[3 * m], a2 = a.alpha[3 * m + 1], a3 = a.alpha[3 * m + 2];
-        const double c2 = pow(0.5, -a1 + a2);
-        const double al[3] = {a1, a2, a3}, cs[3] = {1.0, c2, c2};
-        const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
-        double total = 0.0;
-        for (int sg = 0; sg < 3; ++sg) {
-            const double e = 1.0 - al[sg];
-            kseg[k].e[sg] = (float)e;
-            kseg[k].c[sg] = (float)cs[sg];
-            kseg[k].ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
-            kseg[k].lo[sg] = (float)slo[sg];
-            kseg[k].hi[sg] = (float)shi[sg];
-            const double lo = fmax((double)a.lim_lo, slo[sg]), hi = fmin((double)a.lim_hi, shi[sg]);
-            if (hi > lo) {
-                const double em = 2.0 - al[sg];   // mass-weighted: int c m^(1 - alpha) dm
-                total += (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
-            }
-        }
-        inv_total[k] = total > 0.0 ? (float)(1.0 / total) : 1.f;
-    }
+    if (tid < OPS_K)
+        kroupa_setup(a.alpha + 3 * min(m0 + tid, a.n - 1), a.lim_lo, a.lim_hi, kseg[tid], inv_total[tid], nullptr);
     __syncthreads();
     if (tid == 0) {
         int na = 0;
@@ -321,6 +413,193 @@ cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------- the reverse fold
+// The transpose of the fold for OPS_K models and one metallicity slab per CTA (the layout of ops_fold_kernel), after
+// ssp_batch_age_sums_adjoint (src/physics/opensps_ssp_batch.f90:991) and the IMF rows of the batch gradient
+// (params_bar(BGRAD_IMF1:, m) = imf_bar cscale, src/physics/opensps_csp_batch.f90:5115). With Vbar the template
+// weights' cotangents (the pixel cotangents against the library, divided by cscale), each point p of grid point g
+// has the cotangent of its IMF weight
+//     q_p = sum over its four entries of coef Vbar(template) + mass_bar / cscale mcur_p
+//           + lbol_bar / (ln 10 L_bol cscale) lum_p
+// (L_bol with the operators is the linear row of the sums), and then
+//     wz_bar(g)  = cscale sum_p w_p q_p                                   (w_p = phi_p / T: the bin weight)
+//     alpha_bar_j = cscale sum_g sw(g) sum_p q_p dw_p / dalpha_j,  dw_p / dalpha_j = dphi_p/dalpha_j / T - w_p dlnT_j
+// (forward-mode derivatives of the bin weights and of their normalisation T, the IMF's mass). Every grid point of
+// the slab is visited when wz_bar is wanted, else only those with weight. Per grid point the threads take its
+// points, gather the four models' Vbar of the point's templates from shared memory (one float4 per template), and
+// keep per-warp sums of q w (wz_bar) and per-thread sums of sw q dphi (flushed to FP64 every 16 grid points).
+__global__ void __launch_bounds__(OPS_THREADS, 2) ops_rev_kernel(OpsRevArgs a) {
+    extern __shared__ float4 rsm4[];
+    float4 *V4 = rsm4;                                 // ntpad: the four models' Vbar of the current part
+    float4 *wpart = rsm4 + a.ntpad;                    // n_active x warps: per warp, sum of q phi
+    __shared__ KroupaSeg kseg[OPS_K];
+    __shared__ float inv_total[OPS_K], qm_s[OPS_K], ql_s[OPS_K];
+    __shared__ double dlnT_s[OPS_K][3];
+    __shared__ float sw_s[OPS_MAXT][OPS_K];
+    __shared__ int tlist[OPS_MAXT];
+    __shared__ int n_active;
+    __shared__ double ured[OPS_THREADS / 32][OPS_K][4];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = blockIdx.x, z = blockIdx.y;
+    const int m0 = grp * OPS_K;
+    const int nk = min(OPS_K, a.n - m0);
+    const int ng = a.nt * a.nz;
+    const bool all_points = a.wzb != nullptr;
+    for (int i = tid; i < a.nt * OPS_K; i += OPS_THREADS) {
+        const int t = i / OPS_K, k = i % OPS_K;
+        const double sw = k < nk ? a.wz[(size_t)ng * (m0 + k) + t + (size_t)a.nt * z] : 0.0;
+        sw_s[t][k] = (sw > SAFE_FLOOR) ? (float)sw : 0.f;
+    }
+    if (tid < OPS_K) {
+        const int k = tid, m = min(m0 + k, a.n - 1);
+        double dl[3];
+        kroupa_setup(a.alpha + 3 * m, a.lim_lo, a.lim_hi, kseg[k], inv_total[k], dl);
+        for (int j = 0; j < 3; ++j) dlnT_s[k][j] = dl[j];
+        const double cs = a.cscale[m];
+        const double ls = a.sums[(size_t)6 * m + 1];
+        qm_s[k] = (k < nk && a.mass_bar) ? (float)(a.mass_bar[m] / cs) : 0.f;
+        ql_s[k] = (k < nk && a.lbol_bar && ls > SAFE_FLOOR) ? (float)(a.lbol_bar[m] / (ls * 2.302585092994046 * cs)) : 0.f;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int na = 0;
+        for (int t = 0; t < a.nt; ++t) {
+            bool any = all_points;
+            for (int k = 0; k < OPS_K; ++k) any = any || sw_s[t][k] != 0.f;
+            if (any) tlist[na++] = t;
+        }
+        n_active = na;
+    }
+    __syncthreads();
+    const int na = n_active;
+    double U[OPS_K][4];
+    float G[OPS_K][4];
+#pragma unroll
+    for (int k = 0; k < OPS_K; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) { U[k][i] = 0.0; G[k][i] = 0.f; }
+    int vpart_of = -1;
+    for (int it = 0; it < na; ++it) {
+        const int t = tlist[it];
+        const int part = t < a.itesc ? 0 : 1;
+        if (part != vpart_of) {
+            __syncthreads();                   // every thread done with the previous part's V4 (uniform branch)
+            for (int e = tid; e < a.ntpad; e += OPS_THREADS) {
+                float v[OPS_K];
+#pragma unroll
+                for (int k = 0; k < OPS_K; ++k)
+                    v[k] = k < nk ? a.vbar[((size_t)part * a.n + m0 + k) * a.ntpad + e] : 0.f;
+                V4[e] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+            __syncthreads();
+            vpart_of = part;
+        }
+        const size_t g = (size_t)t + (size_t)a.nt * z;
+        const OpsPoint *pts = a.pts + g * a.npt;
+        const ushort4 *pix = a.pidx + g * a.npt;
+        const float4 *pco = a.pcoef + g * a.npt;
+        float sw[OPS_K], wzp[OPS_K];
+#pragma unroll
+        for (int k = 0; k < OPS_K; ++k) { sw[k] = sw_s[t][k]; wzp[k] = 0.f; }
+#pragma unroll 2
+        for (int u = 0; u < OPS_PT_PER; ++u) {
+            const int p = tid + u * OPS_THREADS;
+            if (p >= a.npt) break;
+            const OpsPoint q = pts[p];
+            const ushort4 id = __ldg(pix + p);
+            const float4 cf = __ldg(pco + p);
+            const float4 v0 = V4[id.x], v1 = V4[id.y], v2 = V4[id.z], v3 = V4[id.w];
+            const float gq[OPS_K] = {
+                fmaf(cf.x, v0.x, fmaf(cf.y, v1.x, fmaf(cf.z, v2.x, cf.w * v3.x))),
+                fmaf(cf.x, v0.y, fmaf(cf.y, v1.y, fmaf(cf.z, v2.y, cf.w * v3.y))),
+                fmaf(cf.x, v0.z, fmaf(cf.y, v1.z, fmaf(cf.z, v2.z, cf.w * v3.z))),
+                fmaf(cf.x, v0.w, fmaf(cf.y, v1.w, fmaf(cf.z, v2.w, cf.w * v3.w)))};
+#pragma unroll
+            for (int k = 0; k < OPS_K; ++k) {
+                const float qk = fmaf(qm_s[k], q.mcur, fmaf(ql_s[k], q.lum, gq[k]));
+                const ImfTan r = imf_weight_tan(kseg[k], q);
+                wzp[k] = fmaf(qk, r.phi, wzp[k]);
+                const float qs = qk * sw[k];
+                G[k][0] = fmaf(qs, r.d0, G[k][0]);
+                G[k][1] = fmaf(qs, r.d1, G[k][1]);
+                G[k][2] = fmaf(qs, r.d2, G[k][2]);
+                G[k][3] = fmaf(qs, r.p12, G[k][3]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < OPS_K; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) wzp[k] += __shfl_xor_sync(0xffffffffu, wzp[k], off);
+        if (lane == 0) wpart[(size_t)it * (OPS_THREADS / 32) + warp] = make_float4(wzp[0], wzp[1], wzp[2], wzp[3]);
+        if ((it & 15) == 15 || it == na - 1) {
+#pragma unroll
+            for (int k = 0; k < OPS_K; ++k)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) { U[k][i] += (double)G[k][i]; G[k][i] = 0.f; }
+        }
+    }
+    // the threads' sums of sw q dphi, per warp, then per model
+#pragma unroll
+    for (int k = 0; k < OPS_K; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            double v = U[k][i];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) ured[warp][k][i] = v;
+        }
+    __syncthreads();
+    // warp k: model m0 + k's wz_bar over the slab's visited grid points, B = sum_g sw(g) wz_bar(g) / cscale, and the
+    // slab's slope cotangents
+    if (warp < nk) {
+        const int k = warp, m = m0 + k;
+        const double cs = a.cscale[m], it_k = (double)inv_total[k];
+        double b = 0.0;
+        for (int it = lane; it < na; it += 32) {
+            const int t = tlist[it];
+            double s = 0.0;
+            for (int w = 0; w < OPS_THREADS / 32; ++w)
+                s += (double)reinterpret_cast<const float *>(wpart + (size_t)it * (OPS_THREADS / 32) + w)[k];
+            s *= it_k;
+            if (a.wzb) a.wzb[(size_t)ng * m + t + (size_t)a.nt * z] = cs * s;
+            b += (double)sw_s[t][k] * s;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) b += __shfl_xor_sync(0xffffffffu, b, off);
+        if (lane == 0) {
+            double u[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int w = 0; w < OPS_THREADS / 32; ++w)
+                for (int i = 0; i < 4; ++i) u[i] += ured[w][k][i];
+            const double A[3] = {-u[0] + KR_LN2 * u[3], -u[1] - KR_LN2 * u[3], -u[2]};
+            for (int j = 0; j < 3; ++j)
+                a.apart[((size_t)z * a.n + m) * 3 + j] = it_k * A[j] - dlnT_s[k][j] * b;
+        }
+    }
+}
+
+// The slabs' slope cotangents summed in slab order, times cscale, into the params_bar rows.
+__global__ void ops_rev_finish_kernel(OpsRevArgs a) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n || !a.params_bar) return;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int z = 0; z < a.nz; ++z)
+        for (int j = 0; j < 3; ++j) s[j] += a.apart[((size_t)z * a.n + m) * 3 + j];
+    for (int j = 0; j < 3; ++j) a.params_bar[(size_t)a.rows * m + a.row_imf1 + j] = a.cscale[m] * s[j];
+}
+
+cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
+    if (a.n <= 0) return cudaSuccess;
+    if (a.npt > OPS_THREADS * OPS_PT_PER || a.nt > OPS_MAXT || a.ntpad > 65536) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float4) * ((size_t)a.ntpad + (size_t)a.nt * (OPS_THREADS / 32));
+    cudaError_t e = cudaFuncSetAttribute(ops_rev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((a.n + OPS_K - 1) / OPS_K, a.nz);
+    ops_rev_kernel<<<grid, OPS_THREADS, smem, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ops_rev_finish_kernel<<<(a.n + 255) / 256, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------- the epilogue
 __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a) {
     extern __shared__ float tsm[];
@@ -412,6 +691,11 @@ int ops_build(Context &c, std::string &err) {
         err = "SSP operator data under " + dir + " does not match the context's grid";
         return ST_DATA_MISSING;
     }
+    for (size_t i = 0; i < idx.size(); ++i)
+        if (idx[i] < 0 || idx[i] >= ntempl) {
+            err = "SSP operator data under " + dir + ": a template index outside the library";
+            return ST_DATA_MISSING;
+        }
     const double lower_bound = 0.08, lim_lo = 0.08, lim_hi = 120.0;
     // data layout: grid point (z, t) z-major in the files: g_file = z nt + t == t + nt z (age fastest)
     std::vector<OpsPoint> pts(np);
@@ -451,6 +735,14 @@ int ops_build(Context &c, std::string &err) {
             ent_c[(size_t)g * nent + i] = tmp[i].second;
         }
     }
+    // point-major templates and coefficients (the reverse fold gathers per point)
+    std::vector<ushort4> pidx(np);
+    std::vector<float4> pcoef(np);
+    for (size_t i = 0; i < np; ++i) {
+        pidx[i] = make_ushort4((unsigned short)idx[4 * i], (unsigned short)idx[4 * i + 1], (unsigned short)idx[4 * i + 2],
+                               (unsigned short)idx[4 * i + 3]);
+        pcoef[i] = make_float4((float)coef[4 * i], (float)coef[4 * i + 1], (float)coef[4 * i + 2], (float)coef[4 * i + 3]);
+    }
     const int ntpad = (ntempl + 63) / 64 * 64;
     std::vector<uint16_t> lh((size_t)ns * ntpad, 0), ll((size_t)ns * ntpad, 0);
     for (int e = 0; e < ntempl; ++e)
@@ -464,7 +756,10 @@ int ops_build(Context &c, std::string &err) {
     cudaError_t e;
     if ((e = o.pts.reserve(np)) != cudaSuccess || (e = o.ent.reserve(ent.size())) != cudaSuccess ||
         (e = o.ent_c.reserve(ent_c.size())) != cudaSuccess || (e = o.lib_hi.reserve(lh.size())) != cudaSuccess ||
-        (e = o.lib_lo.reserve(ll.size())) != cudaSuccess ||
+        (e = o.lib_lo.reserve(ll.size())) != cudaSuccess || (e = o.pidx.reserve(np)) != cudaSuccess ||
+        (e = o.pcoef.reserve(np)) != cudaSuccess ||
+        (e = cudaMemcpy(o.pidx.p, pidx.data(), sizeof(ushort4) * np, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o.pcoef.p, pcoef.data(), sizeof(float4) * np, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(o.pts.p, pts.data(), sizeof(OpsPoint) * np, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(o.ent.p, ent.data(), sizeof(uint32_t) * ent.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(o.ent_c.p, ent_c.data(), sizeof(float) * ent_c.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
