@@ -221,12 +221,23 @@ def ssp_operator_measure(args, torch, barrier) -> dict | None:
     barrier()
     ms = (time.perf_counter() - t0) * 1e3 / args.ops_steps
     kt = ctx.kernel_times()
+    interp = ctx.ops_last_interpolated()
+    ctx.set_profiling(False)
+    # the exact fold on the same batch, for comparison (a few steps)
+    ctx.set_int("gb300_ops_exact", 1)
+    ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    ctx.set_profiling(True)
+    for _ in range(3):
+        ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    kt_exact = ctx.kernel_times()
     ctx.set_profiling(False)
     ctx.close()
     names = ["model_params", "fold_and_template_gemm", "epilogue", "bands"]
     stages = dict(zip(names, kt))
     dev = sum(stages.values())
     return {"batch": n, "value": n / (ms * 1e-3), "unit": "models/s", "ms_per_step": ms, "steps": args.ops_steps,
+            "fold": "interpolated (tcgen05 GEMM against the Lagrange basis in ln m)" if interp else "exact",
+            "exact_fold_stage_ms": dict(zip(names, kt_exact)),
             "device_ms": dev, "device_value": n / (dev * 1e-3) if dev > 0 else None, "stage_ms": stages,
             "imf_bin_weights_per_model": K_AGES * N_Z * 1500, "operator_entries": K_AGES * N_Z * 1500 * 4,
             "workload": "IMF-free CSP through the SSP operator (Kroupa slopes per model), mixed-workload weights, "

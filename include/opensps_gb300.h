@@ -39,6 +39,11 @@ void opensps_gb300_kernel_times(int handle, double *ms, int max_n, int *n, int *
 /* Kernel launches of the last batch on the handle (for the benchmark's launch count). */
 void opensps_gb300_last_launches(int handle, int *launches, int *status);
 
+/* 1 when the last batch through the SSP operator took the interpolated fold (a tcgen05 GEMM against the operator's
+ * Lagrange basis in ln m: every model's |imf1| <= 2.6, |imf2| <= 3.0, |imf3| <= 3.5 and the setting "gb300_ops_exact"
+ * 0), 0 when it took the exact fold. */
+void opensps_gb300_ops_last_fold(int handle, int *interpolated, int *status);
+
 /* Maximum n of opensps_gb300_spec_mags_noalloc. */
 #define OPENSPS_GB300_NOALLOC_MAX_MODELS 65536
 

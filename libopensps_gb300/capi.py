@@ -72,6 +72,7 @@ SIGNATURES = {
     "opensps_gb300_batch_device": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
+    "opensps_gb300_ops_last_fold": (None, [C.c_int, _ip, _ip]),
     "opensps_gb300_spec_mags_noalloc": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
     "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
@@ -403,6 +404,10 @@ class Context:
 
     def last_launches(self) -> int:
         return self._get_int("opensps_gb300_last_launches")
+
+    def ops_last_interpolated(self) -> bool:
+        """Whether the last batch through the SSP operator took the interpolated fold (else the exact one)."""
+        return bool(self._get_int("opensps_gb300_ops_last_fold"))
 
     def set_profiling(self, on: bool):
         st = C.c_int(0)

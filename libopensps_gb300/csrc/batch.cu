@@ -719,7 +719,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             d_y = c.d_yo.p;
             d_o = c.d_yo.p + (size_t)n * ns;
             c.geom.wz = d_wz;
-            const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, itesc, d_y, d_o, err);
+            const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, al.data(), itesc, d_y, d_o, err);
             if (rc) return rc;
             prof_mark(c, 2);
             PartsEpilogueArgs pe;

@@ -276,6 +276,7 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "nebemlineinspec") c->nebemlineinspec = value;
     else if (k == "zmet") c->zmet = value;
     else if (k == "gb300_fp64") c->fp64 = value;   // extension: the plain FP64 path
+    else if (k == "gb300_ops_exact") c->ops_exact = value;   // extension: the operator's exact fold only
     else if (k == "imf_type") c->imf_type = value;
     else if (k == "keep_maggies") c->keep_maggies = value;
     else if (k == "add_dust_emission" || k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_stellar_remnants" ||
@@ -596,6 +597,13 @@ void opensps_gb300_last_launches(int handle, int *launches, int *status) {
     Context *c = lookup(handle);
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
     if (launches) *launches = c->last_launches;
+    if (status) *status = 0;
+}
+
+void opensps_gb300_ops_last_fold(int handle, int *interpolated, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (interpolated) *interpolated = c->ops_last_interp ? 1 : 0;
     if (status) *status = 0;
 }
 

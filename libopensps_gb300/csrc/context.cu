@@ -106,10 +106,15 @@ cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner,
 // The same over 16-bit elements that are bf16 (f16 = false) or f16.
 cudaError_t encode_tmap_2d_16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
                               uint32_t box_outer, bool f16) {
+    return encode_tmap_2d_16s(m, ptr, inner, outer, inner, box_inner, box_outer, f16);
+}
+// The same with rows row_elems elements apart (a column range of a wider matrix).
+cudaError_t encode_tmap_2d_16s(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint64_t row_elems,
+                               uint32_t box_inner, uint32_t box_outer, bool f16) {
     PFN_encodeTiled fn = get_encode_fn();
     if (!fn) return cudaErrorNotSupported;
     cuuint64_t dims[2] = {inner, outer};
-    cuuint64_t strides[1] = {inner * 2};
+    cuuint64_t strides[1] = {row_elems * 2};
     cuuint32_t box[2] = {box_inner, box_outer};
     cuuint32_t es[2] = {1, 1};
     CUresult r = fn(m, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
@@ -170,7 +175,7 @@ Context::~Context() {
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
     ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
-    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
+    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);
     emu.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);

@@ -89,10 +89,21 @@ struct SspOps {
     DevBuf<__nv_bfloat16> lib_thi, lib_tlo;
     CUtensorMap tm_lib_thi, tm_lib_tlo;
     int ppad = 0;
+    // the interpolated fold: each bin weight as Lagrange weights (degree 9 in ln m) on fixed mass nodes of its
+    // Kroupa segment, so that a model's IMF enters only through the node values mu^-alpha; the fold is then a
+    // tcgen05 GEMM of the models' node values x SFH weights against this operator basis (ntempl x nt nz R, columns
+    // (t nz + z) R + r), with the mass and L_bol rows beside it
+    bool interp_ready = false;
+    int interp_R = 0, interp_noff[3] = {}, interp_nn[3] = {};
+    double interp_x0[3] = {}, interp_h[3] = {};
+    DevBuf<__nv_bfloat16> ib_hi, ib_lo;
+    DevBuf<float> i_mrow, i_lrow;
     void release() {
         pts.release(); ent.release(); ent_c.release(); lib_hi.release(); lib_lo.release();
         pidx.release(); pcoef.release(); lib_thi.release(); lib_tlo.release();
+        ib_hi.release(); ib_lo.release(); i_mrow.release(); i_lrow.release();
         ppad = 0;
+        interp_ready = false;
         ready = false;
     }
 };
@@ -112,6 +123,8 @@ struct Context {
     int add_neb_emission = 0, add_igm_absorption = 0, smooth_velocity = 1, dust_type = 0, compute_vega_mags = 0;
     int sfh = 0, nebemlineinspec = 1, fast_mode = 0, zmet = 1, imf_type = 2;
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
+    int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
+    bool ops_last_interp = false;   // the last operator batch took the interpolated fold
     void *cublas = nullptr;      // cublasHandle_t of the FP64 path
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];
@@ -171,6 +184,8 @@ struct Context {
     DevBuf<__nv_bfloat16> d_vhi, d_vlo;
     DevBuf<float> d_yo, d_vpart;
     DevBuf<double> d_spart;
+    DevBuf<__nv_bfloat16> d_ix_hi, d_ix_lo;   // the interpolated fold's operand: node values x SFH weights
+    DevBuf<float> d_ipart;       // and its GEMM's split-K partial sums
     DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
     DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab
     DevBuf<int> d_vflag;
@@ -238,8 +253,8 @@ void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<
 int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,
                   int sm_lo, int sm_hi, int i0, std::string &err);
 void fp64_release(Context &c);
-int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, float *d_young,
-                  float *d_old, std::string &err);
+int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, const double *h_alpha, int itesc,
+                  float *d_young, float *d_old, std::string &err);
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err);
 // With profiling on: records event k on the context's stream (0 starts a batch's set).
@@ -249,5 +264,7 @@ cudaError_t encode_tmap_2d_bf16(CUtensorMap *m, const void *ptr, uint64_t inner,
                                 uint32_t box_outer);
 cudaError_t encode_tmap_2d_16(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint32_t box_inner,
                               uint32_t box_outer, bool f16);
+cudaError_t encode_tmap_2d_16s(CUtensorMap *m, const void *ptr, uint64_t inner, uint64_t outer, uint64_t row_elems,
+                               uint32_t box_inner, uint32_t box_outer, bool f16);
 
 }  // namespace sps

@@ -244,6 +244,22 @@ struct OpsFoldArgs {
     int *flag;                // nz x ceil(n / 4): the slab has weight for some model of the group
 };
 cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
+// The interpolated fold's operand (one row per model of a chunk) and its GEMM's reduction.
+struct OpsInterpArgs {
+    int m0, nt, nz, R, ktot, itesc;          // models m0 .. m0 + gridDim.x - 1; ktot = nt nz R columns
+    int noff[3], nn[3];                      // the segments' node columns: noff[s] .. noff[s] + nn[s] - 1
+    double x0[3], h[3];                      // node j of segment s at ln m = x0[s] + (j - 4) h[s]
+    float lim_lo, lim_hi;
+    const double *wz, *alpha;                // n x nt x nz SFH weights; n x 3 slopes
+    const float *mrow, *lrow;                // ktot: the operator basis's mass and L_bol rows
+    __nv_bfloat16 *x_hi, *x_lo;              // chunk rows x ktot
+    double *sums;                            // n x 6
+};
+struct OpsInterpReduceArgs {
+    int n, m0, rows, ntpad, ntempl, ks_young, ks_old;
+    const float *part_young, *part_old;      // ks x rows x ntpad split-K partial sums
+    __nv_bfloat16 *v_hi, *v_lo;              // 2n x ntpad
+};
 // The operator's reverse pass: from the template cotangents, the cotangents of the SFH weights over ages and
 // metallicities and of the three Kroupa slopes.
 struct OpsRevArgs {

@@ -111,7 +111,7 @@ __device__ __forceinline__ float ops_g2(float x) {
 // P = c lo^em expm1(em dl) / em (em = 2 - alpha, dl = ln(hi / lo)) has dP/dem = c lo^em dl (ln lo g1 + dl g2)(em dl)
 // and c2 the factor 2^(alpha1 - alpha2).
 __device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
-                                    double *dlnT) {
+                                    double *dlnT, double *total_out = nullptr) {
     const double a1 = al3[0], a2 = al3[1], a3 = al3[2];
     const double c2 = pow(0.5, -a1 + a2);
     const double al[3] = {a1, a2, a3}, cs[3] = {1.0, c2, c2};
@@ -137,6 +137,7 @@ __device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_h
         }
     }
     inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
+    if (total_out) *total_out = total;
     if (dlnT) {
         const double it = total > 0.0 ? 1.0 / total : 0.0;
         dlnT[0] = (-dp[0] + KR_LN2 * t12) * it;
@@ -413,6 +414,135 @@ cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------- the interpolated fold
+// The fold as a GEMM. In x = ln m a bin piece's weight in Kroupa segment s is int e^((1 - alpha_s) x) dx; e^(-alpha_s x)
+// interpolated by a degree-9 Lagrange polynomial on equispaced nodes x_j of the segment (the piece in the middle
+// interval of its ten nodes) turns it into sum_j L_pj mu_j^-alpha_s, L_pj = int L_j(x) e^x dx over the piece. So
+//     V(e, m) = sum_{g, s, j} [sw(g, m) c_s(m) / T(m) mu_j^-alpha_s(m)] B(e, (g, s, j)),
+//     B(e, (g, s, j)) = sum over the points p of g and their entries of template e: coef L_pj,
+// the bracket (the operand X, one row per model, all entries >= 0) formed per batch and B (the operator basis) once
+// per operator: a split-BF16 tcgen05 GEMM over K = (grid point, node), young ages and old apart as two column ranges.
+// With the node spacing h_s = 0.44 / |alpha|max_s the interpolation's relative error per bin is below 2e-7 for
+// |alpha_1| <= 2.6, |alpha_2| <= 3.0, |alpha_3| <= 3.5; a batch with a slope outside takes the exact fold. The mass
+// and L_bol rows go through the same expansion (rows of B over mcur and lum), summed per model in FP64.
+constexpr int OPS_IDEG = 9;                          // Lagrange degree (ten nodes per piece)
+constexpr double OPS_IH = 0.44;                      // node spacing x the largest |alpha| of the segment
+constexpr double OPS_AMAX[3] = {2.6, 3.0, 3.5};      // |alpha_s| of the interpolated fold
+constexpr int OPS_IX_THREADS = 256;
+constexpr int OPS_IMAXR = 256;                       // nodes per grid point (R <= OPS_IMAXR)
+
+// One model per CTA: its node values c_s / T mu_j^-alpha_s, then the row of X (bf16 hi / lo) over every grid
+// point, eight columns (one grid point) per thread step, and the model's FP64 mass and L_bol sums, young and old.
+__global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpArgs a) {
+    __shared__ float ctk[OPS_IMAXR];
+    __shared__ KroupaSeg ks;
+    __shared__ float inv_t_f;
+    __shared__ double total_s;
+    __shared__ double red[OPS_IX_THREADS / 32][4];
+    const int row = blockIdx.x, m = a.m0 + row, tid = threadIdx.x;
+    const double *al = a.alpha + 3 * (size_t)m;
+    if (tid == 0) kroupa_setup(al, a.lim_lo, a.lim_hi, ks, inv_t_f, nullptr, &total_s);
+    __syncthreads();
+    const double it = total_s > 0.0 ? 1.0 / total_s : 1.0;
+    const double c2 = pow(0.5, -al[0] + al[1]);
+    for (int r = tid; r < a.R; r += OPS_IX_THREADS) {
+        float v = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int j = r - a.noff[q];
+            if (j >= 0 && j < a.nn[q]) {
+                const double x = a.x0[q] + (double)(j - OPS_IDEG / 2) * a.h[q];
+                v = (float)((q == 0 ? 1.0 : c2) * it * exp(-al[q] * x));
+            }
+        }
+        ctk[r] = v;
+    }
+    __syncthreads();
+    const int ng = a.nt * a.nz, ngrp = a.ktot >> 3, kyoung = a.itesc * a.nz * a.R;
+    const double *wzm = a.wz + (size_t)ng * m;
+    uint4 *xh = reinterpret_cast<uint4 *>(a.x_hi + (size_t)row * a.ktot);
+    uint4 *xl = reinterpret_cast<uint4 *>(a.x_lo + (size_t)row * a.ktot);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};            // mass young, mass old, L_bol young, L_bol old
+    for (int q = tid; q < ngrp; q += OPS_IX_THREADS) {
+        const int col0 = q << 3;
+        const int gp = col0 / a.R, r0 = col0 - gp * a.R;
+        const int t = gp / a.nz, z = gp - t * a.nz;
+        const double swd = wzm[t + (size_t)a.nt * z];
+        const float sw = swd > SAFE_FLOOR ? (float)swd : 0.f;
+        const float4 ma = __ldg(reinterpret_cast<const float4 *>(a.mrow + col0));
+        const float4 mb = __ldg(reinterpret_cast<const float4 *>(a.mrow + col0) + 1);
+        const float4 la = __ldg(reinterpret_cast<const float4 *>(a.lrow + col0));
+        const float4 lb = __ldg(reinterpret_cast<const float4 *>(a.lrow + col0) + 1);
+        const float mr[8] = {ma.x, ma.y, ma.z, ma.w, mb.x, mb.y, mb.z, mb.w};
+        const float lr[8] = {la.x, la.y, la.z, la.w, lb.x, lb.y, lb.z, lb.w};
+        uint32_t hw[4], lw[4];
+        float ms = 0.f, ls = 0.f;
+#pragma unroll
+        for (int i = 0; i < 8; i += 2) {
+            const float v0 = sw * ctk[r0 + i], v1 = sw * ctk[r0 + i + 1];
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(v0 - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(v1 - __bfloat162float(h1));
+            hw[i >> 1] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            lw[i >> 1] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+            ms = fmaf(v0, mr[i], fmaf(v1, mr[i + 1], ms));
+            ls = fmaf(v0, lr[i], fmaf(v1, lr[i + 1], ls));
+        }
+        xh[q] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        xl[q] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        const int part = col0 < kyoung ? 0 : 1;
+        acc[part] += (double)ms;
+        acc[2 + part] += (double)ls;
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+        if (lane == 0) red[warp][i] = acc[i];
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int w = 0; w < OPS_IX_THREADS / 32; ++w)
+            for (int i = 0; i < 4; ++i) s[i] += red[w][i];
+        double *o = a.sums + (size_t)6 * m;
+        o[0] = s[0] + s[1];
+        o[1] = s[2] + s[3];
+        o[2] = s[0]; o[3] = s[1]; o[4] = s[2]; o[5] = s[3];
+    }
+}
+
+// The split-K partial sums of the young and old GEMMs added in split order, as the template GEMM's bf16 hi / lo A
+// operand (rows m0 .. m0 + rows - 1 young, n + m0 .. old; columns from ntempl on zero).
+__global__ void ops_interp_reduce_kernel(OpsInterpReduceArgs a) {
+    const size_t per4 = (size_t)a.rows * a.ntpad / 4;
+    const float4 *py = reinterpret_cast<const float4 *>(a.part_young);
+    const float4 *po = reinterpret_cast<const float4 *>(a.part_old);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < 2 * per4; i += (size_t)gridDim.x * blockDim.x) {
+        const int part = i >= per4 ? 1 : 0;
+        const size_t j = i - (size_t)part * per4;
+        const int row = (int)(j * 4 / a.ntpad), e = (int)(j * 4 - (size_t)row * a.ntpad);
+        const float4 *P = part ? po : py;
+        const int ks = part ? a.ks_old : a.ks_young;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e < a.ntempl)
+            for (int s = 0; s < ks; ++s) {
+                const float4 p = P[(size_t)s * per4 + j];
+                v.x += p.x; v.y += p.y; v.z += p.z; v.w += p.w;
+            }
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+        const size_t o = ((size_t)(part ? a.n : 0) + a.m0 + row) * a.ntpad + e;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float x = e + k < a.ntempl ? vv[k] : 0.f;
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            a.v_hi[o + k] = h;
+            a.v_lo[o + k] = __float2bfloat16_rn(x - __bfloat162float(h));
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------------- the reverse fold
 // The transpose of the fold for OPS_K models and one metallicity slab per CTA (the layout of ops_fold_kernel), after
 // ssp_batch_age_sums_adjoint (src/physics/opensps_ssp_batch.f90:991) and the IMF rows of the batch gradient
@@ -672,6 +802,152 @@ static bool read_raw(const std::string &path, std::vector<T> &out, size_t count)
 
 static std::string cmsg(const char *what, cudaError_t e) { return std::string(what) + ": " + cudaGetErrorString(e); }
 
+// The interpolated fold's operator basis (ops_interp_x_kernel): per segment equispaced nodes over the x = ln m range
+// of its bin pieces (the pieces as imf_weight splits a bin), per piece the Lagrange weights int L_j(x) e^x dx
+// (6-point Gauss-Legendre in each node interval the piece meets), summed per grid point in FP64 into B (templates x
+// R node columns, then bf16 hi / lo) and into the mass and L_bol rows; uploaded in blocks of grid points. Returns
+// false, leaving the exact fold the only one, when memory runs short or the nodes do not fit.
+static bool ops_interp_build(Context &c, const std::vector<double> &mini, const std::vector<int> &idx,
+                             const std::vector<double> &coef, const std::vector<double> &mcur,
+                             const std::vector<double> &lum, int ntempl, int npt, double lower_bound) {
+    SspOps &o = c.ops;
+    o.interp_ready = false;
+    const int nt = c.nt, nz = c.nz, ng = nt * nz;
+    const double lim_lo = 0.08, lim_hi = 120.0;
+    const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
+    auto pieces = [&](const double *mi, int i, int *sg, double *lo, double *hi) -> int {
+        const double m1 = (i == 0) ? lower_bound : mi[i] - 0.5 * (mi[i] - mi[i - 1]);
+        const double m2 = (i == npt - 1) ? mi[i] : mi[i] + 0.5 * (mi[i + 1] - mi[i]);
+        if (mi[i] < lim_lo || mi[i] > lim_hi || m2 <= m1) return 0;
+        int np = 0;
+        for (int s = 0; s < 3; ++s) {
+            const double a = std::max(m1, slo[s]), b = std::min(m2, shi[s]);
+            if (b > a) { sg[np] = s; lo[np] = a; hi[np] = b; ++np; }
+        }
+        return np;
+    };
+    double xlo[3] = {1e300, 1e300, 1e300}, xhi[3] = {-1e300, -1e300, -1e300};
+    for (int g = 0; g < ng; ++g) {
+        const double *mi = mini.data() + (size_t)g * npt;
+        for (int i = 0; i < npt; ++i) {
+            int sg[3]; double lo[3], hi[3];
+            const int np = pieces(mi, i, sg, lo, hi);
+            for (int k = 0; k < np; ++k) {
+                xlo[sg[k]] = std::min(xlo[sg[k]], std::log(lo[k]));
+                xhi[sg[k]] = std::max(xhi[sg[k]], std::log(hi[k]));
+            }
+        }
+    }
+    int R = 0, nint[3];
+    for (int s = 0; s < 3; ++s) {
+        if (!(xhi[s] > xlo[s])) { o.interp_nn[s] = 0; o.interp_noff[s] = R; nint[s] = 0; o.interp_x0[s] = 0.0; o.interp_h[s] = 1.0; continue; }
+        nint[s] = std::max(1, (int)std::ceil((xhi[s] - xlo[s]) * OPS_AMAX[s] / OPS_IH));
+        o.interp_h[s] = (xhi[s] - xlo[s]) / nint[s];
+        o.interp_x0[s] = xlo[s];
+        o.interp_nn[s] = nint[s] + OPS_IDEG;
+        o.interp_noff[s] = R;
+        R += o.interp_nn[s];
+    }
+    R = (R + 7) / 8 * 8;
+    if (R > OPS_IMAXR || R == 0) return false;
+    o.interp_R = R;
+    const size_t ktot = (size_t)ng * R;
+    if (o.ib_hi.reserve((size_t)ntempl * ktot) != cudaSuccess || o.ib_lo.reserve((size_t)ntempl * ktot) != cudaSuccess ||
+        o.i_mrow.reserve(ktot) != cudaSuccess || o.i_lrow.reserve(ktot) != cudaSuccess) {
+        o.ib_hi.release(); o.ib_lo.release(); o.i_mrow.release(); o.i_lrow.release();
+        cudaGetLastError();
+        return false;
+    }
+    static const double GX[6] = {-0.9324695142031521, -0.6612093864662645, -0.2386191860831969,
+                                 0.2386191860831969, 0.6612093864662645, 0.9324695142031521};
+    static const double GW[6] = {0.1713244923791704, 0.3607615730481386, 0.4679139345726910,
+                                 0.4679139345726910, 0.3607615730481386, 0.1713244923791704};
+    double inv_den[OPS_IDEG + 1];
+    for (int k = 0; k <= OPS_IDEG; ++k) {
+        double d = 1.0;
+        for (int l = 0; l <= OPS_IDEG; ++l)
+            if (l != k) d *= (double)(k - l);
+        inv_den[k] = 1.0 / d;
+    }
+    std::vector<float> mrow(ktot), lrow(ktot);
+    constexpr int BLK = 64;                              // grid points per upload
+    std::vector<uint16_t> sh((size_t)ntempl * BLK * R), sl((size_t)ntempl * BLK * R);
+    bool ok = true;
+    for (int g0 = 0; g0 < ng && ok; g0 += BLK) {
+        const int nb = std::min(BLK, ng - g0);
+        const size_t w = (size_t)nb * R;                  // staging row length
+#pragma omp parallel
+        {
+            std::vector<double> acc((size_t)ntempl * R), am(R), al(R);
+#pragma omp for schedule(dynamic, 1)
+            for (int b = 0; b < nb; ++b) {
+                const int gp = g0 + b, t = gp / nz, z = gp - t * nz;   // column order (t nz + z)
+                const size_t gf = (size_t)t + (size_t)nt * z;         // the files' order (age fastest)
+                std::fill(acc.begin(), acc.end(), 0.0);
+                std::fill(am.begin(), am.end(), 0.0);
+                std::fill(al.begin(), al.end(), 0.0);
+                const double *mi = mini.data() + gf * npt;
+                for (int i = 0; i < npt; ++i) {
+                    int sg[3]; double lo[3], hi[3];
+                    const int np = pieces(mi, i, sg, lo, hi);
+                    const size_t q = gf * npt + i;
+                    for (int k = 0; k < np; ++k) {
+                        const int s = sg[k];
+                        const double xa = std::log(lo[k]), xb = std::log(hi[k]), h = o.interp_h[s], x0 = o.interp_x0[s];
+                        const int ia = std::min(std::max((int)std::floor((xa - x0) / h), 0), nint[s] - 1);
+                        const int ib = std::min(std::max((int)std::floor((xb - x0) / h), 0), nint[s] - 1);
+                        for (int iv = ia; iv <= ib; ++iv) {
+                            const double a = iv == ia ? xa : x0 + iv * h, bb = iv == ib ? xb : x0 + (iv + 1) * h;
+                            if (!(bb > a)) continue;
+                            const double xs = x0 + (iv - OPS_IDEG / 2) * h;   // the stencil's first node
+                            double wl[OPS_IDEG + 1] = {};
+                            for (int gq = 0; gq < 6; ++gq) {
+                                const double x = 0.5 * (a + bb) + 0.5 * (bb - a) * GX[gq];
+                                const double u = (x - xs) / h, ex = std::exp(x) * 0.5 * (bb - a) * GW[gq];
+                                for (int kk = 0; kk <= OPS_IDEG; ++kk) {
+                                    double p = inv_den[kk];
+                                    for (int l = 0; l <= OPS_IDEG; ++l)
+                                        if (l != kk) p *= (u - l);
+                                    wl[kk] += ex * p;
+                                }
+                            }
+                            const int c0 = o.interp_noff[s] + iv;
+                            for (int kk = 0; kk <= OPS_IDEG; ++kk) {
+                                am[c0 + kk] += mcur[q] * wl[kk];
+                                al[c0 + kk] += lum[q] * wl[kk];
+                                for (int j = 0; j < 4; ++j)
+                                    acc[(size_t)idx[4 * q + j] * R + c0 + kk] += coef[4 * q + j] * wl[kk];
+                            }
+                        }
+                    }
+                }
+                for (int r = 0; r < R; ++r) {
+                    mrow[(size_t)gp * R + r] = (float)am[r];
+                    lrow[(size_t)gp * R + r] = (float)al[r];
+                }
+                for (int e = 0; e < ntempl; ++e)
+                    for (int r = 0; r < R; ++r) {
+                        const double v = acc[(size_t)e * R + r];
+                        const uint16_t hb = f32_to_bf16_bits((float)v);
+                        sh[(size_t)e * w + (size_t)b * R + r] = hb;
+                        sl[(size_t)e * w + (size_t)b * R + r] = f32_to_bf16_bits((float)(v - (double)bf16_bits_to_f32(hb)));
+                    }
+            }
+        }
+        ok = cudaMemcpy2D(o.ib_hi.p + (size_t)g0 * R, ktot * 2, sh.data(), w * 2, w * 2, ntempl, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy2D(o.ib_lo.p + (size_t)g0 * R, ktot * 2, sl.data(), w * 2, w * 2, ntempl, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    ok = ok && cudaMemcpy(o.i_mrow.p, mrow.data(), sizeof(float) * ktot, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(o.i_lrow.p, lrow.data(), sizeof(float) * ktot, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        o.ib_hi.release(); o.ib_lo.release(); o.i_mrow.release(); o.i_lrow.release();
+        cudaGetLastError();
+        return false;
+    }
+    o.interp_ready = true;
+    return true;
+}
+
 // The operator from the data root's ssp_op dataset (the reference's ssp_operator_build from isochrones and
 // libraries; here its synthetic stand-in): points with their bins and Kroupa segments, entries sorted by template per
 // grid point, the library transposed to pixels x ntpad in bf16 hi / lo.
@@ -777,26 +1053,119 @@ int ops_build(Context &c, std::string &err) {
     o.nent = nent;
     o.lower_bound = lower_bound;
     o.ready = true;
+    ops_interp_build(c, mini, idx, coef, mcur, lum, ntempl, npt, lower_bound);
     return 0;
 }
 
-// The young and old sums of n models (d_wz: their SFH weights over ages and metallicities, d_alpha: n x 3 Kroupa
-// slopes) through the operator: the fold, then the template GEMM into d_young / d_old (n x nspec each, contiguous:
-// d_old = d_young + n nspec); the mass and L_bol sums into the context's sums (n x 6).
-int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, float *d_young,
-                  float *d_old, std::string &err) {
+// Whether the interpolated fold holds for every model's slopes (and is built and not switched off).
+static bool ops_interp_ok(const Context &c, const double *h_alpha, int n) {
+    if (!c.ops.interp_ready || c.ops_exact || !h_alpha) return false;
+    for (int m = 0; m < n; ++m)
+        for (int s = 0; s < 3; ++s)
+            if (!(std::fabs(h_alpha[3 * (size_t)m + s]) <= OPS_AMAX[s])) return false;
+    return true;
+}
+
+// K splits for a GEMM of tiles_mn output tiles over nkb K blocks: the fewest giving at least two waves over the SMs
+// with the last wave at least 85% full (else the fullest last wave), each split keeping 8 or more K blocks.
+static int choose_ksplit(int tiles_mn, int nkb, int num_sms) {
+    int best = 1;
+    double best_eff = -1.0;
+    const int cap = std::max(1, std::min(64, nkb / 8));
+    for (int ks = 1; ks <= cap; ++ks) {
+        const long long tiles = (long long)tiles_mn * ks, waves = (tiles + num_sms - 1) / num_sms;
+        const double eff = (double)tiles / (double)(waves * num_sms);
+        if (tiles >= 2LL * num_sms && eff >= 0.85) return ks;
+        if (eff > best_eff + 1e-9) { best_eff = eff; best = ks; }
+    }
+    return best;
+}
+
+// The interpolated fold of n models into the template GEMM's operand (d_vhi / d_vlo) and the sums: per chunk of
+// models the operand X, the young and old split-K GEMMs against the operator basis, their reduction.
+static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, std::string &err) {
+    SspOps &o = c.ops;
+    cudaStream_t st = c.stream;
+    cudaError_t e;
+    const int nt = c.nt, nz = c.nz, R = o.interp_R;
+    const size_t ktot = (size_t)nt * nz * R;
+    const int chunk = std::min(n, 4096);
+    const int ky = itesc * nz * R, ko = (nt - itesc) * nz * R;
+    const int tiles_mn = ((chunk + gemm_bm() - 1) / gemm_bm()) * ((o.ntempl + gemm_bn() - 1) / gemm_bn());
+    const int ks_y = ky > 0 ? choose_ksplit(tiles_mn, (ky + gemm_bk() - 1) / gemm_bk(), c.num_sms) : 0;
+    const int ks_o = ko > 0 ? choose_ksplit(tiles_mn, (ko + gemm_bk() - 1) / gemm_bk(), c.num_sms) : 0;
+    if ((e = c.d_ix_hi.reserve((size_t)chunk * ktot)) != cudaSuccess || (e = c.d_ix_lo.reserve((size_t)chunk * ktot)) != cudaSuccess ||
+        (e = c.d_ipart.reserve((size_t)std::max(ks_y + ks_o, 1) * chunk * o.ntpad)) != cudaSuccess) {
+        err = cmsg("device memory", e);
+        return ST_DATA_MISSING;
+    }
+    for (int m0 = 0; m0 < n; m0 += chunk) {
+        const int rows = std::min(chunk, n - m0);
+        OpsInterpArgs xa;
+        xa.m0 = m0; xa.nt = nt; xa.nz = nz; xa.R = R; xa.ktot = (int)ktot; xa.itesc = itesc;
+        for (int s = 0; s < 3; ++s) {
+            xa.noff[s] = o.interp_noff[s]; xa.nn[s] = o.interp_nn[s]; xa.x0[s] = o.interp_x0[s]; xa.h[s] = o.interp_h[s];
+        }
+        xa.lim_lo = 0.08f; xa.lim_hi = 120.f;
+        xa.wz = d_wz; xa.alpha = d_alpha; xa.mrow = o.i_mrow.p; xa.lrow = o.i_lrow.p;
+        xa.x_hi = c.d_ix_hi.p; xa.x_lo = c.d_ix_lo.p; xa.sums = c.d_sums.p;
+        ops_interp_x_kernel<<<rows, OPS_IX_THREADS, 0, st>>>(xa);
+        if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated fold operand kernel", e); return ST_DATA_MISSING; }
+        const size_t per = (size_t)rows * o.ntpad;
+        for (int part = 0; part < 2; ++part) {
+            const int K = part ? ko : ky, ks = part ? ks_o : ks_y;
+            if (K <= 0) continue;
+            const size_t c0 = part ? (size_t)ky : 0;
+            GemmPlan pl;
+            pl.num_sms = c.num_sms;
+            if ((e = encode_tmap_2d_16s(&pl.tm_a_hi, c.d_ix_hi.p + c0, K, rows, ktot, gemm_bk(), gemm_bm(), false)) != cudaSuccess ||
+                (e = encode_tmap_2d_16s(&pl.tm_a_lo, c.d_ix_lo.p + c0, K, rows, ktot, gemm_bk(), gemm_bm(), false)) != cudaSuccess ||
+                (e = encode_tmap_2d_16s(&pl.tm_b_hi, o.ib_hi.p + c0, K, o.ntempl, ktot, gemm_bk(), gemm_bn(), false)) != cudaSuccess ||
+                (e = encode_tmap_2d_16s(&pl.tm_b_lo, o.ib_lo.p + c0, K, o.ntempl, ktot, gemm_bk(), gemm_bn(), false)) != cudaSuccess) {
+                err = cmsg("interpolated fold tensor map", e);
+                return ST_DATA_MISSING;
+            }
+            GemmArgs g;
+            g.M = rows; g.N = o.ntempl; g.K = K; g.ldd = o.ntpad; g.b_row0 = 0; g.status = c.d_status.p;
+            g.D = c.d_ipart.p + (part ? (size_t)ks_y * per : 0);
+            g.ksplit = ks; g.d_split = (long long)per;
+            if ((e = run_gemm_bf16x3(pl, g, st)) != cudaSuccess) { err = cmsg("interpolated fold GEMM", e); return ST_DATA_MISSING; }
+        }
+        OpsInterpReduceArgs ra;
+        ra.n = n; ra.m0 = m0; ra.rows = rows; ra.ntpad = o.ntpad; ra.ntempl = o.ntempl;
+        ra.ks_young = ks_y; ra.ks_old = ks_o;
+        ra.part_young = c.d_ipart.p; ra.part_old = c.d_ipart.p + (size_t)ks_y * per;
+        ra.v_hi = c.d_vhi.p; ra.v_lo = c.d_vlo.p;
+        const size_t n4 = 2 * per / 4;
+        ops_interp_reduce_kernel<<<(unsigned)std::min<size_t>((n4 + 255) / 256, 4096), 256, 0, st>>>(ra);
+        if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated fold reduce kernel", e); return ST_DATA_MISSING; }
+    }
+    return 0;
+}
+
+// The young and old sums of n models (d_wz: their SFH weights over ages and metallicities, d_alpha / h_alpha: n x 3
+// Kroupa slopes on the device / host) through the operator: the fold (interpolated when every model's slopes allow,
+// else exact), then the template GEMM into d_young / d_old (n x nspec each, contiguous: d_old = d_young + n nspec);
+// the mass and L_bol sums into the context's sums (n x 6).
+int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, const double *h_alpha, int itesc,
+                  float *d_young, float *d_old, std::string &err) {
     SspOps &o = c.ops;
     cudaStream_t st = c.stream;
     cudaError_t e;
     const int ngroups = (n + 3) / 4;
+    const bool interp = ops_interp_ok(c, h_alpha, n);
     if ((e = c.d_vhi.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
         (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess ||
-        (e = c.d_vpart.reserve((size_t)c.nz * 2 * n * o.ntpad)) != cudaSuccess ||
-        (e = c.d_spart.reserve((size_t)c.nz * n * 4)) != cudaSuccess ||
-        (e = c.d_vflag.reserve((size_t)c.nz * ngroups)) != cudaSuccess) {
+        (!interp && (e = c.d_vpart.reserve((size_t)c.nz * 2 * n * o.ntpad)) != cudaSuccess) ||
+        (!interp && (e = c.d_spart.reserve((size_t)c.nz * n * 4)) != cudaSuccess) ||
+        (!interp && (e = c.d_vflag.reserve((size_t)c.nz * ngroups)) != cudaSuccess)) {
         err = cmsg("device memory", e);
         return ST_DATA_MISSING;
     }
+    c.ops_last_interp = interp;
+    if (interp) {
+        if (int rc = run_ops_interp(c, n, d_wz, d_alpha, itesc, err)) return rc;
+    } else {
     OpsFoldArgs fa;
     fa.n = n; fa.nt = c.nt; fa.nz = c.nz; fa.npt = o.npt; fa.nent = o.nent; fa.ntpad = o.ntpad; fa.itesc = itesc;
     fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;
@@ -804,6 +1173,7 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     fa.v_hi = c.d_vhi.p; fa.v_lo = c.d_vlo.p; fa.sums = c.d_sums.p;
     fa.vpart = c.d_vpart.p; fa.spart = c.d_spart.p; fa.flag = c.d_vflag.p;
     if ((e = run_ops_fold(fa, st)) != cudaSuccess) { err = cmsg("operator fold kernel", e); return ST_DATA_MISSING; }
+    }
     GemmPlan pl;
     pl.num_sms = c.num_sms;
     pl.tm_b_hi = o.tm_lib_hi;
@@ -845,7 +1215,7 @@ int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mas
     }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
     // every age young (itesc = nt): the spectra are the young sums
-    int rc = run_ops_parts(c, nt, c.d_wz.p, c.d_alpha.p, nt, c.d_yo.p, c.d_yo.p + (size_t)nt * ns, err);
+    int rc = run_ops_parts(c, nt, c.d_wz.p, c.d_alpha.p, alpha.data(), nt, c.d_yo.p, c.d_yo.p + (size_t)nt * ns, err);
     if (rc) return rc;
     std::vector<float> y((size_t)nt * ns);
     std::vector<double> sums((size_t)6 * nt);

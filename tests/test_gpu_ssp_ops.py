@@ -56,6 +56,7 @@ def test_batch_with_imf_per_model_matches_oracle(octx, data, ops_data):
     alpha = np.stack([rng.uniform(0.3, 1.8, n), rng.uniform(1.3, 2.8, n), rng.uniform(1.8, 3.3, n)], axis=1)
     params = dict(params, imf1=alpha[:, 0], imf2=alpha[:, 1], imf3=alpha[:, 2], dust1=rng.uniform(0.0, 1.0, n))
     got = octx.csp_batch(params, ssp_weights_z=wz)
+    assert octx.ops_last_interpolated()          # every slope inside the interpolated fold's range
     itesc = int(np.clip(np.searchsorted(data["log_age"], 7.0, side="right"), 1, data["log_age"].size))
     y, o, mass, ls = OpsOracle(ops_data).parts(alpha, wz, itesc)
     ora = Oracle(data, nbands=40, add_neb=False).csp_from_parts(
@@ -65,6 +66,40 @@ def test_batch_with_imf_per_model_matches_oracle(octx, data, ops_data):
     assert float(np.nanmax(np.abs(got["mags"] - ora["mags"]))) <= 1e-3
     np.testing.assert_allclose(got["mass"], mass, rtol=1e-5)
     np.testing.assert_allclose(got["lbol"], np.log10(ls), rtol=1e-5)
+
+
+def test_interpolated_and_exact_folds_agree(octx, data, ops_data):
+    """The interpolated fold (the GEMM against the Lagrange basis in ln m) against the exact fold on the same batch:
+    spectra within 2e-5 relative (above 1e-6 of the peak), mass and L_bol within 1e-6; a batch with one slope
+    outside the interpolated range (imf1 = 2.8) takes the exact fold and matches the oracle."""
+    from oracle.oracle import Oracle, OpsOracle
+    n = 40
+    wz, params = config3_inputs(n, seed=311)
+    rng = np.random.default_rng(312)
+    alpha = np.stack([rng.uniform(-0.5, 2.6, n), rng.uniform(0.5, 3.0, n), rng.uniform(1.0, 3.5, n)], axis=1)
+    params = dict(params, imf1=alpha[:, 0], imf2=alpha[:, 1], imf3=alpha[:, 2])
+    a = octx.csp_batch(params, ssp_weights_z=wz)
+    assert octx.ops_last_interpolated()
+    octx.set_int("gb300_ops_exact", 1)
+    try:
+        b = octx.csp_batch(params, ssp_weights_z=wz)
+        assert not octx.ops_last_interpolated()
+    finally:
+        octx.set_int("gb300_ops_exact", 0)
+    assert rel_err_spec(a["spec"], b["spec"]) <= 2e-5
+    np.testing.assert_allclose(a["mass"], b["mass"], rtol=1e-6)
+    np.testing.assert_allclose(a["lbol"], b["lbol"], rtol=1e-6)
+    # outside the range: the exact fold, against the oracle
+    alpha[3, 0] = 2.8
+    params["imf1"] = alpha[:, 0]
+    got = octx.csp_batch(params, ssp_weights_z=wz)
+    assert not octx.ops_last_interpolated()
+    itesc = int(np.clip(np.searchsorted(data["log_age"], 7.0, side="right"), 1, data["log_age"].size))
+    y, o, mass, ls = OpsOracle(ops_data).parts(alpha, wz, itesc)
+    ora = Oracle(data, nbands=40, add_neb=False).csp_from_parts(
+        {k: v for k, v in params.items() if not k.startswith("imf")}, y, o)
+    assert rel_err_spec(got["spec"], ora["spec"]) <= 1e-4
+    np.testing.assert_allclose(got["mass"], mass, rtol=1e-5)
 
 
 def test_operator_refusals(data, built_lib, ops_data):
