@@ -16,6 +16,7 @@
 // With args.sums set, warps 8 and 9 form the FP64 sums of model_sums_zw (src/physics/opensps_csp_batch.f90:2090-2120)
 // for the CTA's 128 models (measured slower than the separate sums kernel; the batch does not set it).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cfloat>
 #include <cstdint>
@@ -96,6 +97,9 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 5);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * BG_M;
+    // this CTA's pixel blocks: split blockIdx.y of gridDim.y
+    const int kb0 = (int)((long long)blockIdx.y * a.nkb / gridDim.y), kb1 = (int)((long long)(blockIdx.y + 1) * a.nkb / gridDim.y);
+    const bool split = gridDim.y > 1;
     int *status = a.status;
     const uint32_t tcols = npad <= 32 ? 32 : (npad <= 64 ? 64 : (npad <= 128 ? 128 : 256));
     __shared__ float4 zsm[BG_M];     // the observed-frame shift of the CTA's models (w = 2: no model in this row)
@@ -117,7 +121,7 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
 
     if (warp >= BG_BUILD_WARPS) {
         // ---------------------------------------------------------------- FP64 sums of the CTA's models
-        if (a.sums) {
+        if (a.sums && blockIdx.y == 0) {
             for (int r = warp - BG_BUILD_WARPS; r < BG_M; r += BG_SUM_WARPS)
                 if (m0 + r < a.n_models) model_sums_warp(a, m0 + r, lane);
         }
@@ -127,10 +131,11 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         const float dl2 = (float)(a.dlnl * 1.4426950408889634);   // grid step in log2 units
         const float inv_em1 = (float)(1.0 / expm1(a.dlnl));
         // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
-        for (int kb = 0; kb < a.nkb; ++kb) {
-            const int s = kb & 1;
+        for (int kb = kb0; kb < kb1; ++kb) {
+            const int li = kb - kb0;                          // this CTA's stage count
+            const int s = li & 1;
             uint8_t *st = smem + s * stage_bytes;
-            if (kb >= 2) mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+            if (li >= 2) mbar_wait(&bar_mma[s], ((li - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
             if (tid == 0) {
                 mbar_arrive_expect_tx(&bar_tma[s], 2 * b_bytes);
                 tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &bar_tma[s]);
@@ -192,14 +197,14 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             fence_proxy_async_smem();
             named_bar_sync(1, BG_BUILD_THREADS);
             if (tid == 0) {
-                mbar_wait(&bar_tma[s], (kb >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+                mbar_wait(&bar_tma[s], (li >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
                 tc_fence_after();
                 const uint32_t sa = smem_u32(st);
                 const uint32_t ahi = sa, alo = sa + BG_A_BYTES, bhi = sa + 2 * BG_A_BYTES, blo = bhi + b_bytes;
 #pragma unroll
                 for (int k = 0; k < BG_K / 16; ++k) {
                     const uint32_t o = k * 32;
-                    mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                    mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(bhi + o), idesc, (li > 0 || k > 0) ? 1u : 0u);
                     mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
                     mma_bf16(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
                 }
@@ -217,6 +222,17 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             for (int c0 = 0; c0 < npad; c0 += 32) {
                 float v[32];
                 tmem_ld32(trow + c0, v);
+                if (split) {
+                    // the split's partial fluxes (band_finish_kernel sums them and forms the magnitudes)
+                    if (m < a.n_models) {
+                        float *dst = a.fpart + ((size_t)blockIdx.y * a.n_models + m) * npad + c0;
+#pragma unroll
+                        for (int i = 0; i < 32; i += 4)   // (npad is a multiple of 16)
+                            if (c0 + i < npad)
+                                *reinterpret_cast<float4 *>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    }
+                    continue;
+                }
                 if (m < a.n_models) {
 #pragma unroll
                     for (int i = 0; i < 32; ++i) {
@@ -247,14 +263,45 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
 
 int band_gemm_npad(int nbands) { return (nbands + 15) / 16 * 16 < 32 ? 32 : (nbands + 15) / 16 * 16; }
 
-cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
+// The split partial fluxes summed in split order, then the fluxes and magnitudes as the GEMM's epilogue forms them.
+__global__ void band_finish_kernel(BandGemmArgs a) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)a.n_models * a.nbands) return;
+    const int m = (int)(i / a.nbands), b = (int)(i % a.nbands);
+    float v = 0.f;
+    for (int s = 0; s < a.ksplit; ++s) v += a.fpart[((size_t)s * a.n_models + m) * a.npad + b];
+    const double f = (double)v;
+    if (a.fband) a.fband[i] = f;
+    if (a.mags) {
+        double mg = __longlong_as_double(0x7ff8000000000000LL);
+        if (a.do_band == nullptr || a.do_band[b] != 0)
+            mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) - a.zp + a.dist[m];
+        a.mags[i] = mg;
+    }
+}
+
+// Splits of the pixel blocks when the batch's 128-model tiles fill less than half the SMs: up to one CTA per SM,
+// each split keeping at least 4 pixel blocks.
+int band_gemm_ksplit(int n_models, int nkb, int num_sms) {
+    const int tiles = (n_models + BG_M - 1) / BG_M;
+    if (2 * tiles >= num_sms || nkb < 8) return 1;
+    return std::max(1, std::min((num_sms + tiles - 1) / tiles, nkb / 4));
+}
+
+cudaError_t run_band_gemm(const BandGemmArgs &a_in, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
                           cudaStream_t st) {
-    if (a.n_models <= 0 || a.nkb <= 0) return cudaSuccess;
+    if (a_in.n_models <= 0 || a_in.nkb <= 0) return cudaSuccess;
+    BandGemmArgs a = a_in;
+    a.ksplit = a.fpart ? band_gemm_ksplit(a.n_models, a.nkb, a.num_sms) : 1;
+    if (a.ksplit > 1 && (size_t)a.ksplit * a.n_models * a.npad > a.fpart_cap) a.ksplit = 1;
     const int smem = BandGemmSmem::total(a.npad);
     cudaError_t e = cudaFuncSetAttribute(band_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    const int grid = (a.n_models + BG_M - 1) / BG_M;
+    const dim3 grid((a.n_models + BG_M - 1) / BG_M, a.ksplit);
     band_gemm_kernel<<<grid, BG_THREADS, smem, st>>>(tm_hi, tm_lo, a);
+    if ((e = cudaGetLastError()) != cudaSuccess || a.ksplit == 1) return e;
+    const size_t tot = (size_t)a.n_models * a.nbands;
+    band_finish_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@ namespace sps {
 // ---------------------------------------------------------------------------------------------- model params
 struct ModelParamArgs {
     int n, nspec, jtop, add_igm, smooth, i0;   // i0: the pixel whose smoothing row gives the model's taps
+    int mpw = 32;            // models per warp (1 .. 32)
     const double *par;       // PAR_DEVICE x n
     const float *igm_a;      // jtop x 6
     const double *lam;       // nspec
@@ -28,9 +29,11 @@ struct ModelParamArgs {
 // cap's search for the largest optical depth over the pixels below Lyman alpha is shared by the warp's lanes, model
 // after model.
 __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    // a.mpw models per warp (lanes 0 .. mpw - 1): fewer than 32 when the batch is small, so that more warps share
+    // the cap searches
     const int lane = threadIdx.x & 31;
-    const bool live = m < a.n;
+    const int m = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * a.mpw + lane;
+    const bool live = lane < a.mpw && m < a.n;
     const double LOG2E = 1.4426950408889634;
     const double *p = a.par + (size_t)PAR_DEVICE * (live ? m : 0);
     const double z = live ? p[PF_ZRED] : 0.0;
@@ -59,7 +62,7 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     float my_tmax = 0.f;
     int my_jmax = 1;
     const unsigned todo = __ballot_sync(0xffffffffu, igm);
-    for (int i = 0; i < 32; ++i) {
+    for (int i = 0; i < a.mpw; ++i) {
         if (!((todo >> i) & 1u)) continue;
         float bb[6];
 #pragma unroll
@@ -571,7 +574,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ma.i0 = i0; ma.par = d_par + (size_t)PAR_DEVICE * off; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p;
         ma.zt = c.d_zt.p; ma.dl = c.d_dl.p; ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
         ma.zinfo = c.d_zinfo.p + off; ma.dist = c.d_dist.p + off; ma.lnlam = c.d_lnlam.p;
-        model_params_kernel<<<(nk + 255) / 256, 256, smem_mp, st>>>(ma);
+        int mpw = 32;
+        while (mpw > 4 && (nk + mpw - 1) / mpw < 8 * c.num_sms) mpw >>= 1;
+        ma.mpw = mpw;
+        const long long warps = (nk + mpw - 1) / mpw;
+        model_params_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, smem_mp, st>>>(ma);
         return cudaGetLastError();
     };
     int launches = 0;
@@ -605,6 +612,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ba.status = c.d_status.p;
         ba.wz = d_wz + (size_t)nt * nz * off; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = nullptr; ba.nt = nt;
         ba.ntz = nt * nz; ba.parts = wa.parts; ba.itesc = itesc;
+        ba.num_sms = c.num_sms;
+        const int ks = band_gemm_ksplit(nk, c.band_nkb, c.num_sms);
+        if (ks > 1) {
+            const size_t cap = (size_t)ks * nk * c.band_npad;
+            if (c.d_bpart.reserve(cap) == cudaSuccess) { ba.fpart = c.d_bpart.p; ba.fpart_cap = cap; }
+            else cudaGetLastError();
+        }
         return run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st);
     };
     if (!fp64 && !ops) {
@@ -728,11 +742,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             pe.spec = c.d_spec.p;
             if ((e = run_parts_epilogue(pe, st)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
             prof_mark(c, 3);
-            launches = 5;   // model parameters, fold, template GEMM, epilogue (+ the parameter upload)
+            launches = 2 + c.ops_launches;   // model parameters, the operator's kernels, the epilogue
         }
         if (want_mags && !fp64) {
             if ((e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
-            ++launches;
+            launches += band_gemm_ksplit(n, c.band_nkb, c.num_sms) > 1 ? 2 : 1;
         }
         prof_mark(c, 4);
         // the FP64 mass and L_bol sums (the operator's fold forms its own)

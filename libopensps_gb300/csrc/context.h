@@ -125,6 +125,7 @@ struct Context {
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     bool ops_last_interp = false;   // the last operator batch took the interpolated fold
+    int ops_launches = 0;        // kernels the last run_ops_parts launched
     void *cublas = nullptr;      // cublasHandle_t of the FP64 path
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];
@@ -186,6 +187,7 @@ struct Context {
     DevBuf<double> d_spart;
     DevBuf<__nv_bfloat16> d_ix_hi, d_ix_lo;   // the interpolated fold's operand: node values x SFH weights
     DevBuf<float> d_ipart;       // and its GEMM's split-K partial sums
+    DevBuf<float> d_bpart;       // the band GEMM's partial fluxes when it splits the pixels (few models)
     DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
     DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab
     DevBuf<int> d_vflag;

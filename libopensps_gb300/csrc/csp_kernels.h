@@ -118,8 +118,16 @@ struct BandGemmArgs {
     const double *mass, *llin;   // ntz
     double *sums;           // n_models x 6 (as WeightsArgs::sums)
     int nt, ntz, parts, itesc;
+    // with few models, the pixels split over CTAs: partial band fluxes (ksplit x n_models x npad floats, at most
+    // fpart_cap) summed by a second kernel that forms the magnitudes (fpart null: no split)
+    float *fpart = nullptr;
+    size_t fpart_cap = 0;
+    int num_sms = 148;
+    int ksplit = 1;         // set by run_band_gemm
 };
 int band_gemm_npad(int nbands);
+// The pixel splits run_band_gemm takes for n_models (1: none).
+int band_gemm_ksplit(int n_models, int nkb, int num_sms);
 cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
                           cudaStream_t st);
 
@@ -247,6 +255,7 @@ cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
 // The interpolated fold's operand (one row per model of a chunk) and its GEMM's reduction.
 struct OpsInterpArgs {
     int m0, nt, nz, R, ktot, itesc;          // models m0 .. m0 + gridDim.x - 1; ktot = nt nz R columns
+    unsigned rg_magic;                       // 2^32 / (R / 8), rounded up
     int noff[3], nn[3];                      // the segments' node columns: noff[s] .. noff[s] + nn[s] - 1
     double x0[3], h[3];                      // node j of segment s at ln m = x0[s] + (j - 4) h[s]
     float lim_lo, lim_hi;

@@ -431,17 +431,28 @@ constexpr double OPS_AMAX[3] = {2.6, 3.0, 3.5};      // |alpha_s| of the interpo
 constexpr int OPS_IX_THREADS = 256;
 constexpr int OPS_IMAXR = 256;                       // nodes per grid point (R <= OPS_IMAXR)
 
-// One model per CTA: its node values c_s / T mu_j^-alpha_s, then the row of X (bf16 hi / lo) over every grid
-// point, eight columns (one grid point) per thread step, and the model's FP64 mass and L_bol sums, young and old.
+// One model per CTA: its node values c_s / T mu_j^-alpha_s and its SFH weights (as the fold takes them: FP32, zero
+// at or below SAFE_FLOOR) in shared memory, then the row of X (bf16 hi / lo) over every grid point, eight columns
+// (one grid point) per thread step, and the model's FP64 mass and L_bol sums, young and old. Column group q of grid
+// point gp = q / (R / 8) (by a multiply-high with rg_magic = 2^32 / (R / 8) rounded up; exact for q < 2^20).
+constexpr int OPS_IMAXG = 4096;                      // grid points (nt nz <= OPS_IMAXG)
 __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpArgs a) {
-    __shared__ float ctk[OPS_IMAXR];
+    __shared__ __align__(16) float ctk[OPS_IMAXR];
+    __shared__ float sws[OPS_IMAXG];
     __shared__ KroupaSeg ks;
     __shared__ float inv_t_f;
     __shared__ double total_s;
     __shared__ double red[OPS_IX_THREADS / 32][4];
     const int row = blockIdx.x, m = a.m0 + row, tid = threadIdx.x;
+    const int ng = a.nt * a.nz;
     const double *al = a.alpha + 3 * (size_t)m;
     if (tid == 0) kroupa_setup(al, a.lim_lo, a.lim_hi, ks, inv_t_f, nullptr, &total_s);
+    const double *wzm = a.wz + (size_t)ng * m;
+    for (int g = tid; g < ng; g += OPS_IX_THREADS) {
+        const int t = g % a.nt, z = g / a.nt;                 // the weights' order: age fastest
+        const double sw = wzm[g];
+        sws[t * a.nz + z] = sw > SAFE_FLOOR ? (float)sw : 0.f;   // the columns' order: (t nz + z)
+    }
     __syncthreads();
     const double it = total_s > 0.0 ? 1.0 / total_s : 1.0;
     const double c2 = pow(0.5, -al[0] + al[1]);
@@ -458,39 +469,37 @@ __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpA
         ctk[r] = v;
     }
     __syncthreads();
-    const int ng = a.nt * a.nz, ngrp = a.ktot >> 3, kyoung = a.itesc * a.nz * a.R;
-    const double *wzm = a.wz + (size_t)ng * m;
+    const int rg = a.R >> 3, ngrp = ng * rg, gyoung = a.itesc * a.nz;
     uint4 *xh = reinterpret_cast<uint4 *>(a.x_hi + (size_t)row * a.ktot);
     uint4 *xl = reinterpret_cast<uint4 *>(a.x_lo + (size_t)row * a.ktot);
+    const float4 *mr4 = reinterpret_cast<const float4 *>(a.mrow), *lr4 = reinterpret_cast<const float4 *>(a.lrow);
+    const float4 *ct4 = reinterpret_cast<const float4 *>(ctk);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};            // mass young, mass old, L_bol young, L_bol old
     for (int q = tid; q < ngrp; q += OPS_IX_THREADS) {
-        const int col0 = q << 3;
-        const int gp = col0 / a.R, r0 = col0 - gp * a.R;
-        const int t = gp / a.nz, z = gp - t * a.nz;
-        const double swd = wzm[t + (size_t)a.nt * z];
-        const float sw = swd > SAFE_FLOOR ? (float)swd : 0.f;
-        const float4 ma = __ldg(reinterpret_cast<const float4 *>(a.mrow + col0));
-        const float4 mb = __ldg(reinterpret_cast<const float4 *>(a.mrow + col0) + 1);
-        const float4 la = __ldg(reinterpret_cast<const float4 *>(a.lrow + col0));
-        const float4 lb = __ldg(reinterpret_cast<const float4 *>(a.lrow + col0) + 1);
-        const float mr[8] = {ma.x, ma.y, ma.z, ma.w, mb.x, mb.y, mb.z, mb.w};
-        const float lr[8] = {la.x, la.y, la.z, la.w, lb.x, lb.y, lb.z, lb.w};
+        const int gp = (int)__umulhi((unsigned)q, a.rg_magic);
+        const int rq = q - gp * rg;
+        const float sw = sws[gp];
+        const float4 c0 = ct4[2 * rq], c1 = ct4[2 * rq + 1];
+        const float4 ma = __ldg(mr4 + 2 * (size_t)q), mb = __ldg(mr4 + 2 * (size_t)q + 1);
+        const float4 la = __ldg(lr4 + 2 * (size_t)q), lb = __ldg(lr4 + 2 * (size_t)q + 1);
+        const float v[8] = {sw * c0.x, sw * c0.y, sw * c0.z, sw * c0.w, sw * c1.x, sw * c1.y, sw * c1.z, sw * c1.w};
+        const float mrv[8] = {ma.x, ma.y, ma.z, ma.w, mb.x, mb.y, mb.z, mb.w};
+        const float lrv[8] = {la.x, la.y, la.z, la.w, lb.x, lb.y, lb.z, lb.w};
         uint32_t hw[4], lw[4];
         float ms = 0.f, ls = 0.f;
 #pragma unroll
         for (int i = 0; i < 8; i += 2) {
-            const float v0 = sw * ctk[r0 + i], v1 = sw * ctk[r0 + i + 1];
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(v0), h1 = __float2bfloat16_rn(v1);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn(v0 - __bfloat162float(h0));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn(v1 - __bfloat162float(h1));
-            hw[i >> 1] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-            lw[i >> 1] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-            ms = fmaf(v0, mr[i], fmaf(v1, mr[i + 1], ms));
-            ls = fmaf(v0, lr[i], fmaf(v1, lr[i + 1], ls));
+            const __nv_bfloat162 h = __floats2bfloat162_rn(v[i], v[i + 1]);
+            const float2 hf = __bfloat1622float2(h);
+            const __nv_bfloat162 l = __floats2bfloat162_rn(v[i] - hf.x, v[i + 1] - hf.y);
+            hw[i >> 1] = *reinterpret_cast<const uint32_t *>(&h);
+            lw[i >> 1] = *reinterpret_cast<const uint32_t *>(&l);
+            ms = fmaf(v[i], mrv[i], fmaf(v[i + 1], mrv[i + 1], ms));
+            ls = fmaf(v[i], lrv[i], fmaf(v[i + 1], lrv[i + 1], ls));
         }
         xh[q] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         xl[q] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-        const int part = col0 < kyoung ? 0 : 1;
+        const int part = gp < gyoung ? 0 : 1;
         acc[part] += (double)ms;
         acc[2 + part] += (double)ls;
     }
@@ -813,6 +822,7 @@ static bool ops_interp_build(Context &c, const std::vector<double> &mini, const 
     SspOps &o = c.ops;
     o.interp_ready = false;
     const int nt = c.nt, nz = c.nz, ng = nt * nz;
+    if (ng > OPS_IMAXG) return false;
     const double lim_lo = 0.08, lim_hi = 120.0;
     const double slo[3] = {0.08, 0.5, 1.0}, shi[3] = {0.5, 1.0, 1.0e30};
     auto pieces = [&](const double *mi, int i, int *sg, double *lo, double *hi) -> int {
@@ -1089,6 +1099,7 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
     cudaError_t e;
     const int nt = c.nt, nz = c.nz, R = o.interp_R;
     const size_t ktot = (size_t)nt * nz * R;
+    if (nt * nz > OPS_IMAXG || (size_t)nt * nz * (R / 8) >= (1u << 20)) { err = "operator grid too large for the interpolated fold"; return ST_UNSUPPORTED; }
     const int chunk = std::min(n, 4096);
     const int ky = itesc * nz * R, ko = (nt - itesc) * nz * R;
     const int tiles_mn = ((chunk + gemm_bm() - 1) / gemm_bm()) * ((o.ntempl + gemm_bn() - 1) / gemm_bn());
@@ -1103,6 +1114,7 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
         const int rows = std::min(chunk, n - m0);
         OpsInterpArgs xa;
         xa.m0 = m0; xa.nt = nt; xa.nz = nz; xa.R = R; xa.ktot = (int)ktot; xa.itesc = itesc;
+        xa.rg_magic = (unsigned)((0x100000000ULL + (unsigned)(R / 8) - 1) / (unsigned)(R / 8));
         for (int s = 0; s < 3; ++s) {
             xa.noff[s] = o.interp_noff[s]; xa.nn[s] = o.interp_nn[s]; xa.x0[s] = o.interp_x0[s]; xa.h[s] = o.interp_h[s];
         }
@@ -1110,6 +1122,7 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
         xa.wz = d_wz; xa.alpha = d_alpha; xa.mrow = o.i_mrow.p; xa.lrow = o.i_lrow.p;
         xa.x_hi = c.d_ix_hi.p; xa.x_lo = c.d_ix_lo.p; xa.sums = c.d_sums.p;
         ops_interp_x_kernel<<<rows, OPS_IX_THREADS, 0, st>>>(xa);
+        c.ops_launches += 2 + (ky > 0 ? 1 : 0) + (ko > 0 ? 1 : 0);   // operand, GEMMs, reduction
         if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated fold operand kernel", e); return ST_DATA_MISSING; }
         const size_t per = (size_t)rows * o.ntpad;
         for (int part = 0; part < 2; ++part) {
@@ -1163,9 +1176,11 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
         return ST_DATA_MISSING;
     }
     c.ops_last_interp = interp;
+    c.ops_launches = 1;                  // (the template GEMM)
     if (interp) {
         if (int rc = run_ops_interp(c, n, d_wz, d_alpha, itesc, err)) return rc;
     } else {
+    c.ops_launches += 2;                 // the fold and its slab reduction
     OpsFoldArgs fa;
     fa.n = n; fa.nt = c.nt; fa.nz = c.nz; fa.npt = o.npt; fa.nent = o.nent; fa.ntpad = o.ntpad; fa.itesc = itesc;
     fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;

@@ -117,8 +117,9 @@ def test_outside_the_box_and_spread_fall_back_to_the_csp(ectx):
     assert got["n_fallback"] == int(flagged.sum())
     from libopensps_gb300.capi import EMU_INPUTS
     ref = ectx.csp_batch({k: x[flagged, i] for i, k in enumerate(EMU_INPUTS)})
-    # the same CSP batch; the operator fold's shared-memory float atomics make repeated runs differ at FP32 rounding
-    np.testing.assert_allclose(got["mags"][flagged], ref["mags"], rtol=0, atol=1e-6)
+    # the same CSP on the same models: the split-K reductions of the operator's GEMM and of the band GEMM depend on
+    # the batch size, so the magnitudes agree to FP32 rounding (2e-5 mag), not bit for bit
+    np.testing.assert_allclose(got["mags"][flagged], ref["mags"], rtol=0, atol=2e-5)
 
 
 def test_training_end_to_end(ectx, tmp_path):
@@ -140,7 +141,7 @@ def test_training_end_to_end(ectx, tmp_path):
 def test_trained_emulator_accuracy_fallback_and_gain(ectx):
     """The shipped ensemble against the plain CSP on models it was not trained on: the emulated models' magnitudes
     (bands less than 15 mag fainter than the model's brightest) within 0.01 mag for at least 99% of them, at most
-    5% routed to the CSP, the routed ones equal to the CSP's, and the emulator at least 10x faster than the CSP on
+    5% routed to the CSP, the routed ones equal to the CSP's (to FP32 rounding), and the emulator at least 10x faster than the CSP on
     the same models (the speed-up the network buys; both timed end to end from host arrays)."""
     import time
     from libopensps_gb300.capi import EMU_INPUTS
@@ -169,6 +170,6 @@ def test_trained_emulator_accuracy_fallback_and_gain(ectx):
     assert float(np.mean(err[ok] <= 0.01)) >= 0.99, f"within 0.01 mag: {np.mean(err[ok] <= 0.01):.4f}"
     assert float(err[ok].max()) <= 0.05
     both = ectx.emulator_predict(x, fallback=True)
-    np.testing.assert_allclose(both["mags"][~ok], ref[~ok], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(both["mags"][~ok], ref[~ok], rtol=0, atol=2e-5)   # (FP32 rounding, as above)
     np.testing.assert_array_equal(both["mags"][ok], emu["mags"][ok])
     assert t_csp / t_emu >= 10.0, f"emulator {t_emu * 1e3:.1f} ms, CSP {t_csp * 1e3:.1f} ms"
