@@ -512,6 +512,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         // the weights over ages (the SFH's, or the caller's) and their blend at logzsol, formed on the device
         if ((e = c.d_sfhpar.reserve((size_t)SFH_NCOL * n)) != cudaSuccess || (e = c.d_w.reserve((size_t)nt * n)) != cudaSuccess ||
             (e = c.d_sfh_scratch.reserve((size_t)2 * nt * n)) != cudaSuccess ||
+            (e = c.d_sfh_mtab.reserve((size_t)nt * n)) != cudaSuccess ||
             (e = c.d_lblend.reserve((size_t)3 * n)) != cudaSuccess || (e = c.d_sfr.reserve(n)) != cudaSuccess ||
             (io.given_w && (e = c.d_wgiven.reserve((size_t)nt * n)) != cudaSuccess) ||
             (e = cudaMemcpyAsync(c.d_sfhpar.p, io.sfh_par, sizeof(double) * SFH_NCOL * n, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
@@ -524,6 +525,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         sa.tf = c.d_logage.p; sa.lz = c.d_lz.p; sa.lbol = c.d_lbol.p; sa.par = c.d_sfhpar.p;
         sa.given = io.given_w ? c.d_wgiven.p : nullptr;
         sa.w = c.d_w.p; sa.scratch = c.d_sfh_scratch.p; sa.wz = c.d_wz.p; sa.lblend = c.d_lblend.p; sa.sfr = c.d_sfr.p;
+        sa.mtab = c.d_sfh_mtab.p;
         if ((e = run_sfh_forward(sa, st)) != cudaSuccess) { err = cuda_msg("SFH weights kernel", e); return ST_DATA_MISSING; }
         d_wz = c.d_wz.p;
     } else {

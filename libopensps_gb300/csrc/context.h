@@ -177,6 +177,7 @@ struct Context {
     // SFH weights: grid tables, per-model parameters, weights over ages, log-blended L_bol, SFR; reverse-pass scratch
     DevBuf<double> d_logage, d_lz, d_lbol;
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
+    DevBuf<double2> d_sfh_mtab;  // the SFH's moments at the grid ages (n x nt)
     DevBuf<unsigned char> d_dual;
     SspOps ops;
     Emulator emu;                // the learned emulator (emulator.cu, emulator_train.cu)

@@ -216,6 +216,8 @@ struct SfhArgs {
     double *wz;              // n x nt x nz: the weights over ages and metallicities
     double *lblend;          // n x 3: log-blended L_bol (total, young, old)
     double *sfr;             // n, or null
+    double2 *mtab = nullptr; // n x nt: the main component's moments at the grid ages (sfh 1, 4; null: formed
+                             // serially per model)
 };
 cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st);
 struct SfhRevArgs {

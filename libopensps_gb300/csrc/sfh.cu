@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cfloat>
+#include <mutex>
 #include "context.h"
 
 namespace sps {
@@ -100,6 +101,11 @@ template <class T> __device__ __forceinline__ T slog10(const T &x) {
 template <class T> __device__ __forceinline__ T smax(const T &a, const T &b) { return val(a) >= val(b) ? a : b; }
 template <class T> __device__ __forceinline__ T smin(const T &a, const T &b) { return val(a) <= val(b) ? a : b; }
 
+// 1 / (k + 1)^2, k = 0 .. 1000: the power series' term ratio without an FP64 division per term (GB300's FP64 pipe is
+// narrow and the series' terms form one dependent chain)
+constexpr int SFH_NSER = 1001;
+__constant__ double c_inv_sq[SFH_NSER];
+
 // Ei(x) (expi, src/math/opensps_special_functions.f90:62-122): the power series about 0 for x <= 40, the
 // asymptotic series (20 terms) beyond; d Ei / dx = e^x / x.
 __device__ double expi_d(double x) {
@@ -108,8 +114,7 @@ __device__ double expi_d(double x) {
     if (fabs(x) <= 40.0) {
         double res = 1.0, r = 1.0;
         for (int k = 1; k <= 1000; ++k) {
-            const double dd = (double)k + 1.0;
-            r = (r * (double)k * x) / (dd * dd);
+            r = (r * (double)k * x) * c_inv_sq[k];
             res += r;
             if (fabs(r) <= 1.0e-20 * fabs(res)) break;
             if (k == 1000) return NAN;
@@ -168,8 +173,22 @@ __device__ void moments_log(const T &log_t, const SfhT<T> &s, T &m0, T &m1) {
 
 // compute_ssp_weights (src/physics/opensps_sfh.f90:97-257) with log-age interpolation: w (nt, strided) += the hat
 // kernel masses; idx_min / idx_max 1-based as the reference's. w must start at zero.
+// The moments at limit lim = the grid age tf[j] clamped to [lts, lte]: from the table when tf[j] lies strictly
+// inside (the table's entries are moments_log at tf[j] itself), else formed here.
 template <class T>
-__device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_min, int idx_max, T *w, int ws) {
+__device__ __forceinline__ void moments_at(const T &lim, int j, const double *tf, const T &lts, const T &lte,
+                                           const SfhT<T> &s, const double2 *mtab, T &m0, T &m1) {
+    if (mtab && val(lim) == tf[j] && tf[j] > val(lts) && tf[j] < val(lte)) {
+        m0 = lift<T>(mtab[j].x);
+        m1 = lift<T>(mtab[j].y);
+        return;
+    }
+    moments_log(lim, s, m0, m1);
+}
+
+template <class T>
+__device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_min, int idx_max, T *w, int ws,
+                            const double2 *mtab = nullptr) {
     const double tiny_logt = 0.0;
     if (s.type == -1) {
         if (val(s.tb) < 0.0) return;
@@ -191,12 +210,12 @@ __device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_
     if (je > hi_bound) je = hi_bound;
     T lim_prev = smin(smax(lift<T>(tf[js - 1]), lts), lte);
     T m0p, m1p;
-    moments_log(lim_prev, s, m0p, m1p);
+    moments_at(lim_prev, js - 1, tf, lts, lte, s, mtab, m0p, m1p);
     for (int j = js; j <= je; ++j) {
         const T lim2 = smin(smax(lift<T>(tf[j]), lts), lte);
         if (val(lim2) <= val(lim_prev)) { lim_prev = lim2; continue; }
         T m0c, m1c;
-        moments_log(lim2, s, m0c, m1c);
+        moments_at(lim2, j, tf, lts, lte, s, mtab, m0c, m1c);
         const T m0 = m0c - m0p, m1 = m1c - m1p;
         m0p = m0c;
         m1p = m1c;
@@ -219,7 +238,8 @@ __device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_
 // sfh_weights_core_pc for one metallicity (src/physics/opensps_sfh.f90:1077-1160; convert_sfhparams_pc :1306-1360).
 // p: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr). w, t1, t2: nt entries at stride ws, zeroed here.
 template <class T>
-__device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, T *w, T *t1, T *t2, int ws) {
+__device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, T *w, T *t1, T *t2, int ws,
+                                 const double2 *mtab = nullptr) {
     for (int i = 0; i < nt; ++i) { w[i * ws] = lift<T>(0.0); t1[i * ws] = lift<T>(0.0); t2[i * ws] = lift<T>(0.0); }
     SfhT<T> s;
     const T start = (sfh == 1 || sfh == 4) ? p[SFH_SF_START] * 1.0e9 : lift<T>(0.0);
@@ -238,7 +258,7 @@ __device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, 
         return;
     }
     s.type = sfh;
-    ssp_weights(tf, nt, s, 0, imax, w, ws);
+    ssp_weights(tf, nt, s, 0, imax, w, ws, mtab);
     T mass1 = lift<T>(0.0);
     for (int i = 0; i < imax; ++i) mass1 = mass1 + w[i * ws];
     if (val(mass1) < SAFE_FLOOR) mass1 = lift<T>(1.0);
@@ -304,51 +324,238 @@ __device__ __forceinline__ void zinterval(const double *lz, int nz, double x, in
     dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
 }
 
-// One thread per model: the weights over ages (w, n x nt), the SFR, the blend over metallicities (wz, n x nt x nz,
-// age fastest: the other slabs are zeroed) and the log-blended L_bol sums (total, young, old).
-__global__ void __launch_bounds__(128) sfh_forward_kernel(SfhArgs a) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+// One thread per (model, grid age): the main component's moments (sfh 1, 4) at the grid ages strictly inside the
+// model's [log t_start, log t_age], the SFH set up as sfh_weights_core sets it, for sfh_forward_kernel's table.
+__global__ void __launch_bounds__(128) sfh_moments_kernel(SfhArgs a) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)a.n * a.nt) return;
+    const int m = (int)(i / a.nt), j = (int)(i % a.nt);
+    const double *p = a.par + (size_t)SFH_NCOL * m;
+    SfhT<double> s;
+    const double start = p[SFH_SF_START] * 1.0e9;
+    s.type = a.sfh;
+    s.tage = p[SFH_TAGE] * 1.0e9 - start;
+    s.tau = p[SFH_TAU] * 1.0e9;
+    const double trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
+    s.tq = (trunc <= 0.0 || trunc > s.tage) ? 0.0 : s.tage - trunc;
+    s.tb = 0.0;
+    const double lts = log10(fmax(s.tq, 1.0)), lte = log10(fmax(s.tage, 1.0));
+    const double x = a.tf[j];
+    double2 r = make_double2(0.0, 0.0);
+    if (x > lts && x < lte) moments_log(x, s, r.x, r.y);
+    a.mtab[i] = r;
+}
+
+// One component's weights over ages by a warp (ssp_weights for T = double, idx_min 0 or the SSP's window): the
+// moments at every boundary of its intervals (the table's, or formed here at the clamped ends), then per age
+// w[i] = B_i + A_(i+1), interval j's shares A_j = (hi d0 - d1) / dt to w[j - 1] and B_j = (d1 - lo d0) / dt to w[j]
+// (d0, d1 the moments' differences over the interval; intervals of zero width skipped): the sums the serial loop
+// forms, in its order. wout[0 .. nt) is written in full; M0s / M1s are the warp's scratch.
+__device__ void warp_component(const double *tf, int nt, const SfhT<double> &s, int idx_min, int idx_max,
+                               const double2 *mtab, double *M0s, double *M1s, double *wout, int lane) {
+    for (int i = lane; i < nt; i += 32) wout[i] = 0.0;
+    __syncwarp();
+    if (s.type == -1) {
+        if (lane == 0 && s.tb >= 0.0) {
+            const double log_tb = log10(fmax(s.tb, 1.0));
+            if (log_tb <= tf[0]) {
+                wout[0] += 1.0;
+            } else {
+                int j = find_interval0(tf, nt, log_tb) + 1;
+                j = j < 1 ? 1 : (j > nt - 1 ? nt - 1 : j);
+                const double dt = tf[j] - tf[j - 1];
+                wout[j - 1] += (tf[j] - log_tb) / dt;
+                wout[j] += (log_tb - tf[j - 1]) / dt;
+            }
+        }
+        __syncwarp();
+        return;
+    }
+    const double lts = log10(fmax(s.tq, 1.0)), lte = log10(fmax(s.tage, 1.0));
+    int js = find_interval0(tf, nt, lts) + 1;
+    int je = find_interval0(tf, nt, lte) + 2;
+    const int lo_bound = idx_min > 1 ? idx_min : 1, hi_bound = idx_max < nt - 1 ? idx_max : nt - 1;
+    if (js < lo_bound) js = lo_bound;
+    if (je > hi_bound) je = hi_bound;
+    for (int j = lane; j < nt; j += 32)
+        if (j >= js - 1 && j <= je) {
+            const double lim = fmin(fmax(tf[j], lts), lte);
+            double m0, m1;
+            moments_at(lim, j, tf, lts, lte, s, mtab, m0, m1);
+            M0s[j] = m0;
+            M1s[j] = m1;
+        }
+    __syncwarp();
+    for (int i = lane; i < nt; i += 32) {
+        double v = 0.0;
+        if (i >= js && i <= je) {                          // B_i
+            const double lp = fmin(fmax(tf[i - 1], lts), lte), lc = fmin(fmax(tf[i], lts), lte);
+            if (lc > lp) {
+                const double d0 = M0s[i] - M0s[i - 1], d1 = M1s[i] - M1s[i - 1];
+                const double lo = tf[i - 1], hi = tf[i], inv = 1.0 / (hi - lo);
+                v = v + (d1 - lo * d0) * inv;
+            }
+        }
+        const int j = i + 1;
+        if (j >= js && j <= je && j < nt) {                // A_(i+1)
+            const double lp = fmin(fmax(tf[j - 1], lts), lte), lc = fmin(fmax(tf[j], lts), lte);
+            if (lc > lp) {
+                const double d0 = M0s[j] - M0s[j - 1], d1 = M1s[j] - M1s[j - 1];
+                const double lo = tf[j - 1], hi = tf[j], inv = 1.0 / (hi - lo);
+                v = v + (hi * d0 - d1) * inv;
+            }
+        }
+        wout[i] = v;
+    }
+    __syncwarp();
+    if (idx_min == 0 && lane == 0) {
+        const double l1 = fmin(fmax(0.0, lts), lte), l2 = fmin(fmax(tf[0], lts), lte);
+        if (l1 < l2) {
+            double a0, a1, b0, b1;
+            moments_log(l2, s, a0, a1);
+            moments_log(l1, s, b0, b1);
+            wout[0] = wout[0] + (a0 - b0);
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// One warp per model (SFH_WARPS models per CTA): the weights over ages (sfh_weights_core: the main component
+// normalised to one solar mass formed, then the constant and burst components), the SFR, the blend over
+// metallicities (wz, n x nt x nz, age fastest: the other slabs zeroed) and the log-blended L_bol sums (total, young,
+// old). The ages are spread over the lanes (GB300's FP64 pipe is narrow: one model per thread left the SMs idle on
+// small batches); the warp's weights live in shared memory.
+constexpr int SFH_WARPS = 4;
+constexpr int SFH_WMAXT = 128;
+__global__ void __launch_bounds__(SFH_WARPS * 32) sfh_forward_kernel(SfhArgs a) {
+    __shared__ double sm[SFH_WARPS][5][SFH_WMAXT];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const int m = blockIdx.x * SFH_WARPS + wi;
     if (m >= a.n) return;
     const double *p = a.par + (size_t)SFH_NCOL * m;
     const int nt = a.nt, nz = a.nz;
-    double *w = a.w + (size_t)nt * m;
-    double *t1 = a.scratch + (size_t)2 * nt * m, *t2 = t1 + nt;
-    if (a.given == nullptr) {
-        sfh_weights_core<double>(a.tf, nt, a.sfh, p, w, t1, t2, 1);
-        if (a.sfr) a.sfr[m] = sfh_sfr(a.tf, nt, a.sfh, p);
+    double *w = sm[wi][0], *t1 = sm[wi][1], *t2 = sm[wi][2], *M0s = sm[wi][3], *M1s = sm[wi][4];
+    if (a.given) {
+        for (int i = lane; i < nt; i += 32) w[i] = a.given[(size_t)nt * m + i];
+        if (lane == 0 && a.sfr) a.sfr[m] = NAN;
+        __syncwarp();
     } else {
-        for (int i = 0; i < nt; ++i) w[i] = a.given[(size_t)nt * m + i];
-        if (a.sfr) a.sfr[m] = NAN;
+        const int sfh = a.sfh;
+        SfhT<double> s;
+        const double start = (sfh == 1 || sfh == 4) ? p[SFH_SF_START] * 1.0e9 : 0.0;
+        s.tage = p[SFH_TAGE] * 1.0e9 - start;
+        const double tburst = p[SFH_TBURST] * 1.0e9 - start;
+        const double trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
+        s.tau = p[SFH_TAU] * 1.0e9;
+        s.tb = s.tage - tburst;
+        s.tq = (trunc <= 0.0 || trunc > s.tage) ? 0.0 : s.tage - trunc;
+        int imax = find_interval0(a.tf, nt, log10(s.tage)) + 1 + 2;
+        imax = imax < 1 ? 1 : (imax > nt ? nt : imax);
+        if (sfh == 0) {
+            s.type = -1;
+            s.tb = s.tage;
+            warp_component(a.tf, nt, s, imax - 2 > 1 ? imax - 2 : 1, imax, nullptr, M0s, M1s, w, lane);
+        } else {
+            s.type = sfh;
+            warp_component(a.tf, nt, s, 0, imax, a.mtab ? a.mtab + (size_t)nt * m : nullptr, M0s, M1s, w, lane);
+            double part = 0.0;
+            for (int i = lane; i < imax; i += 32) part += w[i];
+            double mass1 = warp_sum(part);
+            if (mass1 < SAFE_FLOOR) mass1 = 1.0;
+            for (int i = lane; i < nt; i += 32) w[i] = w[i] / mass1;
+            __syncwarp();
+            const double cst = p[SFH_CONST], fb_in = p[SFH_FBURST];
+            if (cst > 0.0 || fb_in > SAFE_FLOOR) {
+                s.type = 0;
+                warp_component(a.tf, nt, s, 0, imax, nullptr, M0s, M1s, t1, lane);
+                part = 0.0;
+                for (int i = lane; i < imax; i += 32) part += t1[i];
+                double m1 = warp_sum(part);
+                if (m1 < SAFE_FLOOR) m1 = 1.0;
+                double fb = 0.0;
+                if (s.tb >= 0.0) {
+                    s.type = -1;
+                    warp_component(a.tf, nt, s, 0, imax, nullptr, M0s, M1s, t2, lane);
+                    fb = fb_in;
+                } else {
+                    for (int i = lane; i < nt; i += 32) t2[i] = 0.0;
+                    __syncwarp();
+                }
+                for (int i = lane; i < nt; i += 32) w[i] = (1.0 - cst - fb) * w[i] + cst * (t1[i] / m1) + fb * t2[i];
+                __syncwarp();
+            }
+        }
+        if (lane == 0 && a.sfr) a.sfr[m] = sfh_sfr(a.tf, nt, sfh, p);
     }
+    double *wg = a.w + (size_t)nt * m;
+    for (int i = lane; i < nt; i += 32) wg[i] = w[i];
     int zlo;
     double dz;
     zinterval(a.lz, nz, p[SFH_LOGZSOL], zlo, dz);
     double *wz = a.wz + (size_t)nt * nz * m;
-    double ls = 0.0, ly = 0.0, lo = 0.0;
-    for (int z = 0; z < nz; ++z)
-        for (int t = 0; t < nt; ++t) {
-            const double wt = w[t];
-            double v = 0.0;
-            if (z == zlo) v = (1.0 - dz) * wt;
-            else if (z == zlo + 1) v = dz * wt;
-            wz[t + (size_t)nt * z] = v;
-        }
+    for (int k = lane; k < nt * nz; k += 32) {
+        const int z = k / nt, t = k - z * nt;
+        const double wt = w[t];
+        double v = 0.0;
+        if (z == zlo) v = (1.0 - dz) * wt;
+        else if (z == zlo + 1) v = dz * wt;
+        wz[k] = v;
+    }
     // log L_bol blended between the slabs, then exponentiated (the SSP's own interpolation); ages <= dust_tesc young
-    for (int t = 0; t < nt; ++t) {
+    double ls = 0.0, ly = 0.0, lo = 0.0;
+    for (int t = lane; t < nt; t += 32) {
         const double wt = w[t];
         if (!(wt > SAFE_FLOOR)) continue;
         const double lk = wt * pow(10.0, (1.0 - dz) * a.lbol[t + (size_t)nt * zlo] + dz * a.lbol[t + (size_t)nt * (zlo + 1)]);
         ls += lk;
         if (t < a.itesc) ly += lk; else lo += lk;
     }
-    a.lblend[3 * m] = ls;
-    a.lblend[3 * m + 1] = ly;
-    a.lblend[3 * m + 2] = lo;
+    ls = warp_sum(ls);
+    ly = warp_sum(ly);
+    lo = warp_sum(lo);
+    if (lane == 0) {
+        a.lblend[3 * m] = ls;
+        a.lblend[3 * m + 1] = ly;
+        a.lblend[3 * m + 2] = lo;
+    }
+}
+
+// The series' reciprocal table in constant memory, once per device.
+static cudaError_t sfh_init_tables(cudaStream_t st) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 64 && done[dev]) return cudaSuccess;
+    static double h[SFH_NSER];
+    for (int k = 0; k < SFH_NSER; ++k) h[k] = 1.0 / (((double)k + 1.0) * ((double)k + 1.0));
+    if ((e = cudaMemcpyToSymbolAsync(c_inv_sq, h, sizeof(h), 0, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    if (dev < 64) done[dev] = true;
+    return cudaSuccess;
 }
 
 cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
-    sfh_forward_kernel<<<(a.n + 127) / 128, 128, 0, st>>>(a);
+    cudaError_t e = sfh_init_tables(st);
+    if (e != cudaSuccess) return e;
+    SfhArgs b = a;
+    if (a.given || (a.sfh != 1 && a.sfh != 4)) b.mtab = nullptr;
+    if (b.mtab) {
+        const size_t tot = (size_t)a.n * a.nt;
+        sfh_moments_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, st>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (a.nt > SFH_WMAXT) return cudaErrorInvalidValue;
+    sfh_forward_kernel<<<(a.n + SFH_WARPS - 1) / SFH_WARPS, SFH_WARPS * 32, 0, st>>>(b);
     return cudaGetLastError();
 }
 
@@ -411,6 +618,8 @@ __global__ void __launch_bounds__(64) sfh_reverse_kernel(SfhRevArgs a) {
 
 cudaError_t run_sfh_reverse(const SfhRevArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
+    cudaError_t e0 = sfh_init_tables(st);
+    if (e0 != cudaSuccess) return e0;
     sfh_reverse_kernel<<<(a.n + 63) / 64, 64, 0, st>>>(a);
     return cudaGetLastError();
 }
