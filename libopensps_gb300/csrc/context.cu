@@ -175,7 +175,7 @@ Context::~Context() {
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
     ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
-    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
+    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);
     emu.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);

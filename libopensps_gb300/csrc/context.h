@@ -188,6 +188,7 @@ struct Context {
     DevBuf<double> d_spart;
     DevBuf<__nv_bfloat16> d_ix_hi, d_ix_lo;   // the interpolated fold's operand: node values x SFH weights
     DevBuf<float> d_ipart;       // and its GEMM's split-K partial sums
+    DevBuf<double2> d_ix_const;  // and each model's 1 / T and c2
     DevBuf<float> d_bpart;       // the band GEMM's partial fluxes when it splits the pixels (few models)
     DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
     DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab

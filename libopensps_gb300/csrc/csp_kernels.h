@@ -262,6 +262,7 @@ struct OpsInterpArgs {
     double x0[3], h[3];                      // node j of segment s at ln m = x0[s] + (j - 4) h[s]
     float lim_lo, lim_hi;
     const double *wz, *alpha;                // n x nt x nz SFH weights; n x 3 slopes
+    const double2 *kconst;                   // n: 1 / T and c2 of each model
     const float *mrow, *lrow;                // ktot: the operator basis's mass and L_bol rows
     __nv_bfloat16 *x_hi, *x_lo;              // chunk rows x ktot
     double *sums;                            // n x 6

@@ -436,26 +436,34 @@ constexpr int OPS_IMAXR = 256;                       // nodes per grid point (R 
 // (one grid point) per thread step, and the model's FP64 mass and L_bol sums, young and old. Column group q of grid
 // point gp = q / (R / 8) (by a multiply-high with rg_magic = 2^32 / (R / 8) rounded up; exact for q < 2^20).
 constexpr int OPS_IMAXG = 4096;                      // grid points (nt nz <= OPS_IMAXG)
+
+// One thread per model: 1 / T (the IMF's mass between its limits, FP64) and c2 = 0.5^(alpha2 - alpha1), for
+// ops_interp_x_kernel (formed there by one thread per CTA, the FP64 work ran as one-lane warps).
+__global__ void ops_interp_const_kernel(const double *alpha, int n, float lim_lo, float lim_hi, double2 *out) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    KroupaSeg ks;
+    float itf;
+    double total;
+    const double *al = alpha + 3 * (size_t)m;
+    kroupa_setup(al, lim_lo, lim_hi, ks, itf, nullptr, &total);
+    out[m] = make_double2(total > 0.0 ? 1.0 / total : 1.0, pow(0.5, -al[0] + al[1]));
+}
 __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpArgs a) {
     __shared__ __align__(16) float ctk[OPS_IMAXR];
     __shared__ float sws[OPS_IMAXG];
-    __shared__ KroupaSeg ks;
-    __shared__ float inv_t_f;
-    __shared__ double total_s;
     __shared__ double red[OPS_IX_THREADS / 32][4];
     const int row = blockIdx.x, m = a.m0 + row, tid = threadIdx.x;
     const int ng = a.nt * a.nz;
     const double *al = a.alpha + 3 * (size_t)m;
-    if (tid == 0) kroupa_setup(al, a.lim_lo, a.lim_hi, ks, inv_t_f, nullptr, &total_s);
     const double *wzm = a.wz + (size_t)ng * m;
     for (int g = tid; g < ng; g += OPS_IX_THREADS) {
         const int t = g % a.nt, z = g / a.nt;                 // the weights' order: age fastest
         const double sw = wzm[g];
         sws[t * a.nz + z] = sw > SAFE_FLOOR ? (float)sw : 0.f;   // the columns' order: (t nz + z)
     }
-    __syncthreads();
-    const double it = total_s > 0.0 ? 1.0 / total_s : 1.0;
-    const double c2 = pow(0.5, -al[0] + al[1]);
+    const double2 kc = a.kconst[m];                  // 1 / T, c2
+    const double it = kc.x, c2 = kc.y;
     for (int r = tid; r < a.R; r += OPS_IX_THREADS) {
         float v = 0.f;
 #pragma unroll
@@ -474,7 +482,11 @@ __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpA
     uint4 *xl = reinterpret_cast<uint4 *>(a.x_lo + (size_t)row * a.ktot);
     const float4 *mr4 = reinterpret_cast<const float4 *>(a.mrow), *lr4 = reinterpret_cast<const float4 *>(a.lrow);
     const float4 *ct4 = reinterpret_cast<const float4 *>(ctk);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};            // mass young, mass old, L_bol young, L_bol old
+    // mass young, mass old, L_bol young, L_bol old: FP32 over up to 16 thread steps, then FP64 (GB300's FP64 pipe
+    // is narrow: one FP64 add per step was a third of the kernel)
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float fac[4] = {0.f, 0.f, 0.f, 0.f};
+    int nstep = 0;
     for (int q = tid; q < ngrp; q += OPS_IX_THREADS) {
         const int gp = (int)__umulhi((unsigned)q, a.rg_magic);
         const int rq = q - gp * rg;
@@ -500,9 +512,16 @@ __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpA
         xh[q] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         xl[q] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         const int part = gp < gyoung ? 0 : 1;
-        acc[part] += (double)ms;
-        acc[2 + part] += (double)ls;
+        fac[part] += ms;
+        fac[2 + part] += ls;
+        if (++nstep == 16) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) { acc[i] += (double)fac[i]; fac[i] = 0.f; }
+            nstep = 0;
+        }
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i] += (double)fac[i];
     const int warp = tid >> 5, lane = tid & 31;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -1106,10 +1125,14 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
     const int ks_y = ky > 0 ? choose_ksplit(tiles_mn, (ky + gemm_bk() - 1) / gemm_bk(), c.num_sms) : 0;
     const int ks_o = ko > 0 ? choose_ksplit(tiles_mn, (ko + gemm_bk() - 1) / gemm_bk(), c.num_sms) : 0;
     if ((e = c.d_ix_hi.reserve((size_t)chunk * ktot)) != cudaSuccess || (e = c.d_ix_lo.reserve((size_t)chunk * ktot)) != cudaSuccess ||
+        (e = c.d_ix_const.reserve((size_t)n)) != cudaSuccess ||
         (e = c.d_ipart.reserve((size_t)std::max(ks_y + ks_o, 1) * chunk * o.ntpad)) != cudaSuccess) {
         err = cmsg("device memory", e);
         return ST_DATA_MISSING;
     }
+    ops_interp_const_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_alpha, n, 0.08f, 120.f, c.d_ix_const.p);
+    if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated fold constants kernel", e); return ST_DATA_MISSING; }
+    c.ops_launches += 1;
     for (int m0 = 0; m0 < n; m0 += chunk) {
         const int rows = std::min(chunk, n - m0);
         OpsInterpArgs xa;
@@ -1119,7 +1142,7 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
             xa.noff[s] = o.interp_noff[s]; xa.nn[s] = o.interp_nn[s]; xa.x0[s] = o.interp_x0[s]; xa.h[s] = o.interp_h[s];
         }
         xa.lim_lo = 0.08f; xa.lim_hi = 120.f;
-        xa.wz = d_wz; xa.alpha = d_alpha; xa.mrow = o.i_mrow.p; xa.lrow = o.i_lrow.p;
+        xa.wz = d_wz; xa.alpha = d_alpha; xa.kconst = c.d_ix_const.p; xa.mrow = o.i_mrow.p; xa.lrow = o.i_lrow.p;
         xa.x_hi = c.d_ix_hi.p; xa.x_lo = c.d_ix_lo.p; xa.sums = c.d_sums.p;
         ops_interp_x_kernel<<<rows, OPS_IX_THREADS, 0, st>>>(xa);
         c.ops_launches += 2 + (ky > 0 ? 1 : 0) + (ko > 0 ? 1 : 0);   // operand, GEMMs, reduction
