@@ -280,12 +280,12 @@ __global__ void band_finish_kernel(BandGemmArgs a) {
     }
 }
 
-// Splits of the pixel blocks when the batch's 128-model tiles fill less than half the SMs: up to one CTA per SM,
-// each split keeping at least 4 pixel blocks.
+// Splits of the pixel blocks when the batch's 128-model tiles give fewer than two CTAs per SM (two fit on an SM):
+// up to two CTAs per SM, each split keeping at least 4 pixel blocks.
 int band_gemm_ksplit(int n_models, int nkb, int num_sms) {
     const int tiles = (n_models + BG_M - 1) / BG_M;
-    if (2 * tiles >= num_sms || nkb < 8) return 1;
-    return std::max(1, std::min((num_sms + tiles - 1) / tiles, nkb / 4));
+    if (tiles >= 2 * num_sms || nkb < 8) return 1;
+    return std::max(1, std::min((2 * num_sms + tiles - 1) / tiles, nkb / 4));
 }
 
 cudaError_t run_band_gemm(const BandGemmArgs &a_in, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,

@@ -345,6 +345,49 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const double *P = io.params;   // PF_COUNT x n
     auto par = [&](int m, int id) { return P[(size_t)PF_COUNT * m + id]; };
 
+    // host weights over ages and metallicities on the mixed path go up in chunks on the side stream, each chunk's
+    // kernels running while the next chunk's weights are copied. The first chunk's copy starts here, under the
+    // host's checks and parameter staging; the parameter table follows it on the same stream, then the other chunks
+    // (the first kernels need the table)
+    constexpr int CHUNK = 16384;
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
+    const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts &&
+                         n >= 2 * CHUNK;
+    // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
+    // more on the small chunk than its shorter copy saves)
+    const int nch = chunked ? (n + CHUNK - 1) / CHUNK : 1;
+    auto chunk_off = [&](int k) { return k * CHUNK; };
+    auto chunk_len = [&](int k) { return std::min(CHUNK, n - k * CHUNK); };
+    auto chunk_copy = [&](int k) -> cudaError_t {
+        const int off = chunk_off(k), nk = chunk_len(k);
+        cudaEvent_t &ev = c.chunk_ev[k % Context::NCHUNK_EV];
+        cudaError_t r = cudaSuccess;
+        if (!ev) r = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (r == cudaSuccess)
+            r = cudaMemcpyAsync(c.d_wz.p + (size_t)nt * nz * off, io.wz + (size_t)nt * nz * off,
+                                sizeof(double) * nt * nz * nk, cudaMemcpyHostToDevice, c.side);
+        if (r == cudaSuccess) r = cudaEventRecord(ev, c.side);
+        return r;
+    };
+    // the band mask on the device (when it changed; before any weight copy, which would queue it)
+    if (nb > 0) {
+        std::vector<int> do_band(nb, 1);
+        for (int b = 0; b < nb && b < (int)c.mag_mask.size(); ++b) do_band[b] = c.mag_mask[b];
+        if (do_band != c.do_band_h || !c.d_do_band.p) {
+            cudaError_t e1 = c.d_do_band.reserve(nb);
+            if (e1 == cudaSuccess)
+                e1 = cudaMemcpyAsync(c.d_do_band.p, do_band.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream);
+            if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(c.stream);
+            if (e1 != cudaSuccess) { err = cuda_msg("band mask", e1); return ST_DATA_MISSING; }
+            c.do_band_h = do_band;
+        }
+    }
+    if (chunked) {
+        cudaError_t e0 = c.d_wz.reserve((size_t)n * nt * nz);
+        if (e0 == cudaSuccess) e0 = chunk_copy(0);
+        if (e0 != cudaSuccess) { err = cuda_msg("weights copy", e0); return ST_DATA_MISSING; }
+    }
+
     // ---- checks shared by the batch (the reference's batch_check_models / plan_smoothing rules)
     if (c.dust_type != 0) { err = "dust_type " + std::to_string(c.dust_type) + ": only the power law (0) on this path"; return ST_UNSUPPORTED; }
     if (c.compute_vega_mags != 0) { err = "compute_vega_mags = 1 is not supported on this path"; return ST_UNSUPPORTED; }
@@ -498,11 +541,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return ST_DATA_MISSING;
     }
     cudaStream_t st = c.stream;
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
-    // host weights over ages and metallicities on the mixed path go up in chunks, each chunk's kernels running
-    // while the next chunk's weights are copied
-    constexpr int CHUNK = 16384;
-    const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && !fp64 && !ops && !parts && n >= 2 * CHUNK;
     const double *d_wz = io.wz;
     const double *d_par = nullptr;
     std::vector<double> hp;
@@ -552,12 +590,25 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
 #pragma omp parallel for schedule(static) if (n >= 8192)
         for (int m = 0; m < n; ++m)
             for (int k = 0; k < PAR_DEVICE; ++k) hpp[(size_t)PAR_DEVICE * m + k] = par(m, k);
-        if ((e = cudaMemcpyAsync(c.d_params.p, hpp, sizeof(double) * np, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+        // (with the weights in chunks the table goes up on the side stream between the first chunk and the others:
+        // a copy on the batch's stream was served only after all the side stream's copies)
+        cudaStream_t cs = chunked ? c.side : st;
+        if ((e = cudaMemcpyAsync(c.d_params.p, hpp, sizeof(double) * np, cudaMemcpyHostToDevice, cs)) != cudaSuccess) {
             err = cuda_msg("parameter copy", e);
             return ST_DATA_MISSING;
         }
+        if (chunked) {
+            if ((!c.par_ev && (e = cudaEventCreateWithFlags(&c.par_ev, cudaEventDisableTiming)) != cudaSuccess) ||
+                (e = cudaEventRecord(c.par_ev, c.side)) != cudaSuccess || (e = cudaStreamWaitEvent(st, c.par_ev, 0)) != cudaSuccess) {
+                err = cuda_msg("parameter copy", e);
+                return ST_DATA_MISSING;
+            }
+        }
         d_par = c.d_params.p;
     }
+    if (chunked)
+        for (int k = 1; k < nch; ++k)
+            if ((e = chunk_copy(k)) != cudaSuccess) { err = cuda_msg("weights copy", e); return ST_DATA_MISSING; }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
 
     // ---- the per-model parameters, then the weight operand (one stream: run side by side they took longer than in
@@ -593,15 +644,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.grid = 0;
     float *d_y = c.d_young.p, *d_o = c.d_old.p;
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
-    if (want_mags && !fp64) {
-        std::vector<int> do_band(nb, 1);
-        for (int b = 0; b < nb && b < (int)c.mag_mask.size(); ++b) do_band[b] = c.mag_mask[b];
-        if ((e = c.d_do_band.reserve(nb)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(c.d_do_band.p, do_band.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
-            err = cuda_msg("band mask", e);
-            return ST_DATA_MISSING;
-        }
-    }
     // bands and magnitudes of models [off, off + nk)
     auto bands = [&](int off, int nk) -> cudaError_t {
         BandGemmArgs ba;
@@ -683,31 +725,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         if (!chunked) {
             if (int rc = run_range(0, n, true, true)) return rc;
         } else {
-            // chunks: the weight operand and the contraction (which hide the copies); then the bands and the FP64
-            // sums over the whole batch (efficient only at full size)
-            const int nch = (n + CHUNK - 1) / CHUNK;
+            // chunks: each chunk's weight operand, contraction, bands and FP64 sums run while the next chunk's
+            // weights are copied (the copies are the longer part: the kernels hide under them)
             for (int k = 0; k < nch; ++k) {
-                const int off = k * CHUNK, nk = std::min(CHUNK, n - off);
-                cudaEvent_t &ev = c.chunk_ev[k % Context::NCHUNK_EV];
-                if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
-                    err = cuda_msg("chunk event", e);
-                    return ST_DATA_MISSING;
-                }
-                if ((e = cudaMemcpyAsync(c.d_wz.p + (size_t)nt * nz * off, io.wz + (size_t)nt * nz * off,
-                                         sizeof(double) * nt * nz * nk, cudaMemcpyHostToDevice, c.side)) != cudaSuccess ||
-                    (e = cudaEventRecord(ev, c.side)) != cudaSuccess || (e = cudaStreamWaitEvent(st, ev, 0)) != cudaSuccess) {
+                const int off = chunk_off(k), nk = chunk_len(k);
+                // (the copies were enqueued above; beyond NCHUNK_EV chunks a slot's event was recorded again by a
+                // later chunk's copy, and waiting for that later copy is waiting for this one too)
+                if ((e = cudaStreamWaitEvent(st, c.chunk_ev[k % Context::NCHUNK_EV], 0)) != cudaSuccess) {
                     err = cuda_msg("weights copy", e);
                     return ST_DATA_MISSING;
                 }
-                if (int rc = run_range(off, nk, k == 0, false)) return rc;
+                if (int rc = run_range(off, nk, k == 0, true)) return rc;
             }
-            if (want_mags) {
-                if ((e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
-                ++launches;
-            }
-            prof_mark(c, 4);
-            if ((e = run_weights_prep(wa, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
-            ++launches;
         }
         prof_mark(c, 5);
     } else {

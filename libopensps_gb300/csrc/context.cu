@@ -191,6 +191,8 @@ Context::~Context() {
     }
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);
+    if (par_ev) cudaEventDestroy(par_ev);
+    par_ev = nullptr;
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_params) cudaEventDestroy(ev_params);
     if (ev_sums) cudaEventDestroy(ev_sums);
