@@ -82,6 +82,14 @@ __device__ __forceinline__ void model_sums_warp(const BandGemmArgs &a, int m, in
     }
 }
 
+// AB magnitude of an FP32 band flux (NaN when not positive): -2.5 log10 f in FP32 (the flux carries FP32's precision
+// already; an FP64 logarithm per band was most of the epilogue's time on GB300's narrow FP64 pipe), then the zero
+// point and the model's distance term in FP64.
+__device__ __forceinline__ double band_mag(float f, double zp, double dist) {
+    if (!(f > 0.f)) return __longlong_as_double(0x7ff8000000000000LL);
+    return (double)(-2.5f * log10f(f)) - zp + dist;
+}
+
 __global__ void __launch_bounds__(BG_THREADS, 2)
 band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_constant__ CUtensorMap tm_c_lo,
                  BandGemmArgs a) {
@@ -215,11 +223,12 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
         tc_fence_after();
 
-        // epilogue: warps 0..3 read their lane quarter (one model per thread)
-        if (warp < 4) {
-            const int r = warp * 32 + lane, m = m0 + r;
-            const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-            for (int c0 = 0; c0 < npad; c0 += 32) {
+        // epilogue: warps w and w + 4 read lane quarter w % 4 (one model per thread), columns 32 (w / 4) + 64 i
+        {
+            const int q = warp & 3;
+            const int r = q * 32 + lane, m = m0 + r;
+            const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+            for (int c0 = (warp >> 2) * 32; c0 < npad; c0 += 64) {
                 float v[32];
                 tmem_ld32(trow + c0, v);
                 if (split) {
@@ -243,8 +252,7 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                             if (a.mags) {
                                 double mg = __longlong_as_double(0x7ff8000000000000LL);
                                 if (a.do_band == nullptr || a.do_band[b] != 0)
-                                    mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) -
-                                         a.zp + a.dist[m];
+                                    mg = band_mag(v[i], a.zp, a.dist[m]);
                                 a.mags[(size_t)m * a.nbands + b] = mg;
                             }
                         }
@@ -270,12 +278,10 @@ __global__ void band_finish_kernel(BandGemmArgs a) {
     const int m = (int)(i / a.nbands), b = (int)(i % a.nbands);
     float v = 0.f;
     for (int s = 0; s < a.ksplit; ++s) v += a.fpart[((size_t)s * a.n_models + m) * a.npad + b];
-    const double f = (double)v;
-    if (a.fband) a.fband[i] = f;
+    if (a.fband) a.fband[i] = (double)v;
     if (a.mags) {
         double mg = __longlong_as_double(0x7ff8000000000000LL);
-        if (a.do_band == nullptr || a.do_band[b] != 0)
-            mg = (f > 0.0 ? -2.5 * log10(f) : __longlong_as_double(0x7ff8000000000000LL)) - a.zp + a.dist[m];
+        if (a.do_band == nullptr || a.do_band[b] != 0) mg = band_mag(v, a.zp, a.dist[m]);
         a.mags[i] = mg;
     }
 }
