@@ -342,8 +342,9 @@ static std::string cuda_msg(const char *what, cudaError_t e) { return std::strin
 int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const int n = io.n, ns = c.nspec, nt = c.nt, nz = c.nz, nb = c.nbands;
     if (n <= 0) return 0;
-    const double *P = io.params;   // PF_COUNT x n
-    auto par = [&](int m, int id) { return P[(size_t)PF_COUNT * m + id]; };
+    const double *P = io.params;   // params_cols x n
+    const int pc = io.params_cols;
+    auto par = [&](int m, int id) { return id < pc ? P[(size_t)pc * m + id] : io.param_defaults[id]; };
 
     // host weights over ages and metallicities on the mixed path go up in chunks on the side stream, each chunk's
     // kernels running while the next chunk's weights are copied. The first chunk's copy starts here, under the

@@ -485,17 +485,25 @@ void opensps_gb300_batch_device(int handle, int n, const double *d_params, const
     std::lock_guard<std::mutex> lk(c->mu);
     if (!c->is_setup) return fail(status, ST_NOT_SETUP, "context not set up");
     if (n <= 0) return;
-    // the batch-wide settings come from the context; the per-model table is on the device (a copy is read here
-    // for the batch's checks: 88 bytes per model)
-    std::vector<double> rows((size_t)PF_COUNT * n), dp((size_t)PAR_DEVICE * n);
-    cudaError_t e = cudaMemcpy(dp.data(), d_params, sizeof(double) * dp.size(), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return fail(status, ST_BAD_ARG, std::string("d_params: ") + cudaGetErrorString(e));
-    for (int m = 0; m < n; ++m) {
-        std::memcpy(rows.data() + (size_t)PF_COUNT * m, c->pdef, sizeof(double) * PF_COUNT);
-        std::memcpy(rows.data() + (size_t)PF_COUNT * m, dp.data() + (size_t)PAR_DEVICE * m, sizeof(double) * PAR_DEVICE);
+    // the batch-wide settings come from the context; the per-model table is on the device: a copy is read here for
+    // the batch's checks (88 bytes per model, into the page-locked staging buffer, on a stream of its own so that it
+    // does not wait for the previous batch's kernels)
+    const size_t np = (size_t)PAR_DEVICE * n;
+    cudaError_t e = cudaSuccess;
+    if (c->pinned_par_n < np) {
+        if (c->pinned_par) cudaFreeHost(c->pinned_par);
+        c->pinned_par = nullptr;
+        c->pinned_par_n = 0;
+        if ((e = cudaMallocHost(&c->pinned_par, sizeof(double) * np)) != cudaSuccess)
+            return fail(status, ST_DATA_MISSING, std::string("page-locked parameters: ") + cudaGetErrorString(e));
+        c->pinned_par_n = np;
     }
+    if ((e = cudaMemcpyAsync(c->pinned_par, d_params, sizeof(double) * np, cudaMemcpyDeviceToHost, c->side2)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(c->side2)) != cudaSuccess)
+        return fail(status, ST_BAD_ARG, std::string("d_params: ") + cudaGetErrorString(e));
     BatchIO io;
-    io.n = n; io.params = rows.data(); io.wz = d_wz; io.dev_inputs = true; io.dev_params = d_params;
+    io.n = n; io.params = c->pinned_par; io.params_cols = PAR_DEVICE; io.param_defaults = c->pdef;
+    io.wz = d_wz; io.dev_inputs = true; io.dev_params = d_params;
     io.mags = d_mags; io.dev_sync = sync != 0;
     std::string err;
     const int st = run_batch(*c, io, err);

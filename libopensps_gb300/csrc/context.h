@@ -233,8 +233,11 @@ float bf16_bits_to_f32(uint16_t b);
 // are device pointers and the spectra stay on the device.
 struct BatchIO {
     int n = 0;
-    // per-model parameters: PF_COUNT x n (host), built from names / values and the context's defaults
+    // per-model parameters (host): params_cols x n, the first params_cols of the ParamId order, the others the
+    // context's defaults (param_defaults, PF_COUNT; with params_cols = PF_COUNT none)
     const double *params = nullptr;
+    int params_cols = PF_COUNT;
+    const double *param_defaults = nullptr;
     const double *wz = nullptr;      // nt x nz x n
     bool dev_inputs = false;         // wz, dev_params and mags are device pointers; outputs stay on the device
     const double *dev_params = nullptr;   // PAR_DEVICE x n on the device (dev_inputs)
