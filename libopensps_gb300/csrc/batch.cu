@@ -52,11 +52,13 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     }
     // the cap (apply_igm_z :4272-4299): the first pixel of the largest optical depth, searched by the whole warp for
     // each of its models in turn, over the wavelength factors staged in shared memory (one array per factor)
-    extern __shared__ float sa[];    // 6 x jtop
+    extern __shared__ float4 sa4[];  // jtop float4 (factors 0..3), then jtop float2 (factors 4, 5)
     const int nj = a.add_igm ? a.jtop : 0;
-    for (int i = threadIdx.x; i < 6 * nj; i += blockDim.x) {
-        const int j = i / 6, k = i % 6;
-        sa[k * nj + j] = a.igm_a[i];
+    float2 *sa2 = reinterpret_cast<float2 *>(sa4 + nj);
+    for (int j = threadIdx.x; j < nj; j += blockDim.x) {
+        const float *g = a.igm_a + 6 * (size_t)j;
+        sa4[j] = make_float4(g[0], g[1], g[2], g[3]);
+        sa2[j] = make_float2(g[4], g[5]);
     }
     __syncthreads();
     float my_tmax = 0.f;
@@ -70,8 +72,9 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
         float tmax = 0.f;
         int jmax = 1;
         for (int j = lane; j < nj; j += 32) {
-            const float t = sa[j] * bb[0] + sa[nj + j] * bb[1] + sa[2 * nj + j] * bb[2] + sa[3 * nj + j] * bb[3] +
-                            sa[4 * nj + j] * bb[4] + sa[5 * nj + j] * bb[5];
+            const float4 f = sa4[j];
+            const float2 g = sa2[j];
+            const float t = f.x * bb[0] + f.y * bb[1] + f.z * bb[2] + f.w * bb[3] + g.x * bb[4] + g.y * bb[5];
             if (t > tmax) { tmax = t; jmax = j + 1; }
         }
 #pragma unroll
@@ -675,7 +678,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             WeightsArgs w = wa;
             w.n_models = nk; w.wz = d_wz + (size_t)nt * nz * off; w.w_hi = c.d_whi.p + (size_t)kpad * off;
             w.w_lo = c.d_wlo.p + (size_t)kpad * off; w.sums = c.d_sums.p + (size_t)6 * off;
-            if ((e = run_weights_convert(w, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
+            // (the operand and, in the same pass over the FP64 weights, the FP64 mass and L_bol sums)
+            if ((e = run_weights_convert_sums(w, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
             if (marks) prof_mark(c, 2);
             ContractPlan pl;
             pl.tm_a_hi = bop->tm_hi;
@@ -710,8 +714,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                 ++launches;
             }
             if (marks) prof_mark(c, 4);
-            if ((e = run_weights_prep(w, st)) != cudaSuccess) { err = cuda_msg("weights sums kernel", e); return ST_DATA_MISSING; }
-            ++launches;
             return 0;
         };
         if (parts) {

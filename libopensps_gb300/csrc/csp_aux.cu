@@ -1,8 +1,9 @@
 // The prologue kernels of the batched CSP path.
 //
-// weights_prep: model_sums_zw (OpenSPS src/physics/opensps_csp_batch.f90:2090-2120) per model: the weights floored
-//   at SAFE_FLOOR, the FP64 mass and L_bol sums (young and old parts apart when asked), and the weights cast once to
-//   the contraction's operand (bf16 hi + lo, in its K order, through the operand's column map).
+// weights_convert_sums: model_sums_zw (OpenSPS src/physics/opensps_csp_batch.f90:2090-2120) per model: the weights
+//   floored at SAFE_FLOOR, the FP64 mass and L_bol sums (young and old parts apart when asked), and the weights cast
+//   once to the contraction's operand (bf16 hi + lo, in its K order, through the operand's column map), in one pass.
+// weights_prep: the FP64 sums alone (the plain FP64 path).
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cfloat>
@@ -28,27 +29,62 @@ __device__ __forceinline__ float weight_to_f32(double w) {
     return __uint_as_float(((uint32_t)fe << 23) + m);                  // a mantissa carry moves into the exponent
 }
 
-// The contraction's weight operand: one warp per model, lane l takes operand columns l, l + 32, ...
-__global__ void __launch_bounds__(256) weights_convert_kernel(WeightsArgs a) {
+// The operand and, from the same FP64 weights, the FP64 sums of model_sums_zw (one warp per model, the sums in the
+// operand's column order; young ages by the column map's bit 30): the sums ride the FP64 pipe while the conversion
+// waits on memory, instead of a second pass over the weights bound by that pipe.
+template <bool PARTS>
+__global__ void __launch_bounds__(256) weights_convert_sums_kernel(WeightsArgs a) {
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (m >= a.n_models) return;
     const double *w = a.wz + (size_t)m * a.nt * a.nz;
     __nv_bfloat16 *hi = a.w_hi + (size_t)m * a.kpad, *lo = a.w_lo + (size_t)m * a.kpad;
+    double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
 #pragma unroll 4
     for (int k = lane; k < a.kpad; k += 32) {
         const int code = __ldg(a.kmap + k);
-        const float wf = (code >= 0) ? weight_to_f32(__ldg(w + (code & 0x3fffffff))) : 0.f;
+        float wf = 0.f;
+        if (code >= 0) {
+            const int idx = code & 0x3fffffff;
+            const double wv = __ldg(w + idx);
+            wf = weight_to_f32(wv);
+            if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
+                const double mk = __ldg(a.mass + idx), lk = __ldg(a.llin + idx);
+                ms = fma(wv, mk, ms);
+                ls = fma(wv, lk, ls);
+                if (PARTS) {
+                    if (code & 0x40000000) { msy = fma(wv, mk, msy); lsy = fma(wv, lk, lsy); }
+                    else { mso = fma(wv, mk, mso); lso = fma(wv, lk, lso); }
+                }
+            }
+        }
         const __nv_bfloat16 h = __float2bfloat16_rn(wf);
         hi[k] = h;
         lo[k] = __float2bfloat16_rn(wf - __bfloat162float(h));
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ms += __shfl_xor_sync(0xffffffffu, ms, off);
+        ls += __shfl_xor_sync(0xffffffffu, ls, off);
+        if (PARTS) {
+            msy += __shfl_xor_sync(0xffffffffu, msy, off);
+            lsy += __shfl_xor_sync(0xffffffffu, lsy, off);
+            mso += __shfl_xor_sync(0xffffffffu, mso, off);
+            lso += __shfl_xor_sync(0xffffffffu, lso, off);
+        }
+    }
+    if (lane == 0 && a.sums) {
+        double *o = a.sums + (size_t)m * 6;
+        o[0] = ms; o[1] = ls;
+        if (PARTS) { o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso; }
+    }
 }
 
-cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st) {
+cudaError_t run_weights_convert_sums(const WeightsArgs &a, cudaStream_t st) {
     if (a.n_models <= 0) return cudaSuccess;
-    const int threads = 256, per_block = threads / 32;
-    weights_convert_kernel<<<(a.n_models + per_block - 1) / per_block, threads, 0, st>>>(a);
+    const int threads = 256, per_block = threads / 32, blocks = (a.n_models + per_block - 1) / per_block;
+    if (a.parts) weights_convert_sums_kernel<true><<<blocks, threads, 0, st>>>(a);
+    else weights_convert_sums_kernel<false><<<blocks, threads, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -66,11 +102,13 @@ __global__ void __launch_bounds__(256) weights_prep_kernel(WeightsArgs a) {
     for (int k = lane; k < ntz; k += 32) {
         const double wv = __ldg(w + k);
         if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
-            const double mk = wv * __ldg(a.mass + k), lk = wv * __ldg(a.llin + k);
-            ms += mk;
-            ls += lk;
+            // (fused multiply-adds: the kernel is bound by GB300's FP64 pipe, and one FMA is half a multiply and an add)
+            const double mk = __ldg(a.mass + k), lk = __ldg(a.llin + k);
+            ms = fma(wv, mk, ms);
+            ls = fma(wv, lk, ls);
             if (PARTS) {
-                if (t < a.itesc) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
+                if (t < a.itesc) { msy = fma(wv, mk, msy); lsy = fma(wv, lk, lsy); }
+                else { mso = fma(wv, mk, mso); lso = fma(wv, lk, lso); }
             }
         }
         if (PARTS) { t += 32; while (t >= a.nt) t -= a.nt; }

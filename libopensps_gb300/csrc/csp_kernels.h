@@ -95,8 +95,8 @@ struct WeightsArgs {
     int itesc;              // ages t < itesc (0-based) are young
     int grid;               // blocks of the FP64 sums kernel (0: one warp per model)
 };
-// the bf16 hi / lo operand (no FP64 arithmetic), and the FP64 sums (run beside the contraction)
-cudaError_t run_weights_convert(const WeightsArgs &a, cudaStream_t st);
+// the bf16 hi / lo operand with the FP64 sums in one pass over the weights; the FP64 sums alone (the FP64 path)
+cudaError_t run_weights_convert_sums(const WeightsArgs &a, cudaStream_t st);
 cudaError_t run_weights_prep(const WeightsArgs &a, cudaStream_t st);
 
 // Band fluxes (observed frame at each model's redshift, trapezoid filter integrals) and AB magnitudes, as a
