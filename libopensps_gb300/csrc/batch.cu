@@ -712,6 +712,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if (want_mags) {
                 if ((e = bands(off, nk)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
                 ++launches;
+                if (chunked) {
+                    // this chunk's magnitudes to the page-locked staging buffer on the third stream, beside the next
+                    // chunk's kernels (the end of the batch then copies only into the caller's array on the host)
+                    cudaEvent_t &ev = c.mag_ev[(off / CHUNK) % Context::NCHUNK_EV];
+                    if ((!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) ||
+                        (e = cudaEventRecord(ev, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side2, ev, 0)) != cudaSuccess ||
+                        (e = cudaMemcpyAsync(c.pinned_mags + (size_t)nb * off, c.d_mags.p + (size_t)nb * off,
+                                             sizeof(double) * nb * nk, cudaMemcpyDeviceToHost, c.side2)) != cudaSuccess) {
+                        err = cuda_msg("magnitudes copy", e);
+                        return ST_DATA_MISSING;
+                    }
+                }
             }
             if (marks) prof_mark(c, 4);
             return 0;
@@ -724,6 +736,16 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
             d_y = c.d_young.p;
             d_o = c.d_old.p;
+        }
+        if (chunked && want_mags && c.pinned_mags_n < (size_t)n * nb) {
+            if (c.pinned_mags) cudaFreeHost(c.pinned_mags);
+            c.pinned_mags = nullptr;
+            c.pinned_mags_n = 0;
+            if ((e = cudaMallocHost(&c.pinned_mags, sizeof(double) * n * nb)) != cudaSuccess) {
+                err = cuda_msg("page-locked magnitudes", e);
+                return ST_DATA_MISSING;
+            }
+            c.pinned_mags_n = (size_t)n * nb;
         }
         if (!chunked) {
             if (int rc = run_range(0, n, true, true)) return rc;
@@ -869,7 +891,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             return ST_DATA_MISSING;
         }
     }
-    if (want_mags && !io.dev_inputs) {
+    if (want_mags && !io.dev_inputs && !chunked) {
         if ((e = cudaMemcpyAsync(io.mags, c.d_mags.p, sizeof(double) * n * nb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) {
             err = cuda_msg("magnitudes copy", e);
             return ST_DATA_MISSING;
@@ -923,6 +945,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     c.last_n = n;
     c.geom.n = n;
+    if (want_mags && chunked) {
+        // (the chunks' magnitude copies on the third stream: waited for, then spread over the host threads)
+        if ((e = cudaStreamSynchronize(c.side2)) != cudaSuccess) { err = cuda_msg("magnitudes copy", e); return ST_DATA_MISSING; }
+        const double *src = c.pinned_mags;
+#pragma omp parallel for schedule(static)
+        for (int m = 0; m < n; ++m) std::memcpy(io.mags + (size_t)nb * m, src + (size_t)nb * m, sizeof(double) * nb);
+    }
     if (want_sums && !io.dev_inputs) {
 #pragma omp parallel for schedule(static) if (n >= 8192)
         for (int m = 0; m < n; ++m) {

@@ -185,9 +185,14 @@ Context::~Context() {
     if (pinned_sums) cudaFreeHost(pinned_sums);
     pinned_sums = nullptr;
     pinned_sums_n = 0;
+    if (pinned_mags) cudaFreeHost(pinned_mags);
+    pinned_mags = nullptr;
+    pinned_mags_n = 0;
     for (int i = 0; i < NCHUNK_EV; ++i) {
         if (chunk_ev[i]) cudaEventDestroy(chunk_ev[i]);
         chunk_ev[i] = nullptr;
+        if (mag_ev[i]) cudaEventDestroy(mag_ev[i]);
+        mag_ev[i] = nullptr;
     }
     for (int s = 0; s < 2; ++s)
         for (int i = 0; i < NPROF; ++i) if (prof_ev[s][i]) cudaEventDestroy(prof_ev[s][i]);

@@ -206,10 +206,12 @@ struct Context {
     double *pinned_par = nullptr; size_t pinned_par_n = 0;   // page-locked staging of the per-model parameter table
     double *pinned_sums = nullptr; size_t pinned_sums_n = 0; // page-locked copy of the mass and L_bol sums
     std::vector<int> do_band_h;                               // the band mask last uploaded to d_do_band
+    double *pinned_mags = nullptr; size_t pinned_mags_n = 0; // page-locked staging of the chunked batch's magnitudes
     std::vector<double> param_rows;                          // the batch's parameter rows (PF_COUNT x n)
     static constexpr int NCHUNK_EV = 64;
     cudaEvent_t chunk_ev[NCHUNK_EV] = {};                    // the chunked batch's weight copies
     cudaEvent_t par_ev = nullptr;                            // and its parameter table's copy
+    cudaEvent_t mag_ev[NCHUNK_EV] = {};                      // and its chunks' band kernels (magnitude copies)
     std::vector<double> last_maggies;
     int keep_maggies = 0;
 
