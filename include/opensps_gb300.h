@@ -44,6 +44,11 @@ void opensps_gb300_last_launches(int handle, int *launches, int *status);
  * 0), 0 when it took the exact fold. */
 void opensps_gb300_ops_last_fold(int handle, int *interpolated, int *status);
 
+/* 1 when the last batch's weights over ages and metallicities were read in place from the caller's pageable host
+ * memory (a chunked batch on a device that reads pageable memory, as Grace systems do over NVLink-C2C), 0 when they
+ * were copied. */
+void opensps_gb300_last_input_in_place(int handle, int *in_place, int *status);
+
 /* Maximum n of opensps_gb300_spec_mags_noalloc. */
 #define OPENSPS_GB300_NOALLOC_MAX_MODELS 65536
 

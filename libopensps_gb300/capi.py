@@ -73,6 +73,7 @@ SIGNATURES = {
     "opensps_gb300_context_stream": (None, [C.c_int, C.POINTER(C.c_void_p), _ip, _ip]),
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
     "opensps_gb300_ops_last_fold": (None, [C.c_int, _ip, _ip]),
+    "opensps_gb300_last_input_in_place": (None, [C.c_int, _ip, _ip]),
     "opensps_gb300_spec_mags_noalloc": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
     "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
@@ -404,6 +405,10 @@ class Context:
 
     def last_launches(self) -> int:
         return self._get_int("opensps_gb300_last_launches")
+
+    def last_input_in_place(self) -> bool:
+        """Whether the last batch read the caller's pageable weights in place (else they were copied)."""
+        return bool(self._get_int("opensps_gb300_last_input_in_place"))
 
     def ops_last_interpolated(self) -> bool:
         """Whether the last batch through the SSP operator took the interpolated fold (else the exact one)."""

@@ -362,6 +362,23 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const int nch = chunked ? (n + CHUNK - 1) / CHUNK : 1;
     auto chunk_off = [&](int k) { return k * CHUNK; };
     auto chunk_len = [&](int k) { return std::min(CHUNK, n - k * CHUNK); };
+    // pageable host weights on a device that reads pageable memory (Grace's address translation over NVLink-C2C):
+    // the operand kernel reads each chunk in place (the link's rate, against about a fifth of it for a copy from
+    // pageable memory); page-locked weights still go up by copies, which overlap the kernels on the copy engine
+    bool direct = false;
+    if (chunked) {
+        if (c.pageable_access < 0) {
+            int dev = 0, v = 0;
+            c.pageable_access = (cudaGetDevice(&dev) == cudaSuccess &&
+                                 cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v == 1) ? 1 : 0;
+        }
+        cudaPointerAttributes pa;
+        if (c.pageable_access == 1 && cudaPointerGetAttributes(&pa, io.wz) == cudaSuccess &&
+            pa.type == cudaMemoryTypeUnregistered)
+            direct = true;
+        cudaGetLastError();
+    }
+    c.last_direct = direct;
     auto chunk_copy = [&](int k) -> cudaError_t {
         const int off = chunk_off(k), nk = chunk_len(k);
         cudaEvent_t &ev = c.chunk_ev[k % Context::NCHUNK_EV];
@@ -386,7 +403,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             c.do_band_h = do_band;
         }
     }
-    if (chunked) {
+    if (chunked && !direct) {
         cudaError_t e0 = c.d_wz.reserve((size_t)n * nt * nz);
         if (e0 == cudaSuccess) e0 = chunk_copy(0);
         if (e0 != cudaSuccess) { err = cuda_msg("weights copy", e0); return ST_DATA_MISSING; }
@@ -575,7 +592,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("weights copy", e);
             return ST_DATA_MISSING;
         }
-        d_wz = c.d_wz.p;
+        d_wz = direct ? io.wz : c.d_wz.p;
     }
     if (!io.dev_inputs) {
         // the device table from the parameter rows, through a page-locked staging buffer
@@ -610,7 +627,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         d_par = c.d_params.p;
     }
-    if (chunked)
+    if (chunked && !direct)
         for (int k = 1; k < nch; ++k)
             if ((e = chunk_copy(k)) != cudaSuccess) { err = cuda_msg("weights copy", e); return ST_DATA_MISSING; }
     cudaMemsetAsync(c.d_status.p, 0, sizeof(int), st);
@@ -678,8 +695,20 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             WeightsArgs w = wa;
             w.n_models = nk; w.wz = d_wz + (size_t)nt * nz * off; w.w_hi = c.d_whi.p + (size_t)kpad * off;
             w.w_lo = c.d_wlo.p + (size_t)kpad * off; w.sums = c.d_sums.p + (size_t)6 * off;
-            // (the operand and, in the same pass over the FP64 weights, the FP64 mass and L_bol sums)
-            if ((e = run_weights_convert_sums(w, st)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
+            // (the operand and, in the same pass over the FP64 weights, the FP64 mass and L_bol sums; reading the
+            // caller's pageable weights in place, on the side stream beside the previous chunk's kernels)
+            if (direct) {
+                cudaEvent_t &ev = c.chunk_ev[(off / CHUNK) % Context::NCHUNK_EV];
+                if ((!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) ||
+                    (e = run_weights_convert_sums(w, c.side)) != cudaSuccess || (e = cudaEventRecord(ev, c.side)) != cudaSuccess ||
+                    (e = cudaStreamWaitEvent(st, ev, 0)) != cudaSuccess) {
+                    err = cuda_msg("weights kernel", e);
+                    return ST_DATA_MISSING;
+                }
+            } else if ((e = run_weights_convert_sums(w, st)) != cudaSuccess) {
+                err = cuda_msg("weights kernel", e);
+                return ST_DATA_MISSING;
+            }
             if (marks) prof_mark(c, 2);
             ContractPlan pl;
             pl.tm_a_hi = bop->tm_hi;
@@ -756,7 +785,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                 const int off = chunk_off(k), nk = chunk_len(k);
                 // (the copies were enqueued above; beyond NCHUNK_EV chunks a slot's event was recorded again by a
                 // later chunk's copy, and waiting for that later copy is waiting for this one too)
-                if ((e = cudaStreamWaitEvent(st, c.chunk_ev[k % Context::NCHUNK_EV], 0)) != cudaSuccess) {
+                if (!direct && (e = cudaStreamWaitEvent(st, c.chunk_ev[k % Context::NCHUNK_EV], 0)) != cudaSuccess) {
                     err = cuda_msg("weights copy", e);
                     return ST_DATA_MISSING;
                 }

@@ -608,6 +608,13 @@ void opensps_gb300_last_launches(int handle, int *launches, int *status) {
     if (status) *status = 0;
 }
 
+void opensps_gb300_last_input_in_place(int handle, int *in_place, int *status) {
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (in_place) *in_place = c->last_direct ? 1 : 0;
+    if (status) *status = 0;
+}
+
 void opensps_gb300_ops_last_fold(int handle, int *interpolated, int *status) {
     Context *c = lookup(handle);
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");

@@ -126,6 +126,8 @@ struct Context {
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     bool ops_last_interp = false;   // the last operator batch took the interpolated fold
     int ops_launches = 0;        // kernels the last run_ops_parts launched
+    int pageable_access = -1;    // the device reads pageable host memory (-1: not asked yet)
+    bool last_direct = false;    // the last batch read the caller's pageable weights in place
     void *cublas = nullptr;      // cublasHandle_t of the FP64 path
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];

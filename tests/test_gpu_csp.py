@@ -139,3 +139,24 @@ def test_parts_and_emission_lines(ctx, oracle40, data):
                                                             data["ssp_mass"][:, young_ages]), rtol=1e-12)
     np.testing.assert_allclose(got["mass_young"] + got["mass_old"], got["mass"], rtol=1e-12)
     np.testing.assert_allclose(got["emlines"], ora["emlines"], rtol=1e-5)
+
+
+def test_chunked_batch_pageable_and_page_locked_weights(ctx, oracle40):
+    """A batch large enough to go up in chunks (40,000 models): from pageable weights (read in place where the device
+    reads pageable memory) and from page-locked weights (copied) the outputs are identical, and a sample of models
+    matches the oracle."""
+    import torch
+    n = 40000
+    wz, params = config3_inputs(n, seed=77)
+    a = ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
+    in_place = ctx.last_input_in_place()
+    pinned = torch.from_numpy(wz).pin_memory()
+    b = ctx.csp_batch(params, ssp_weights_z=pinned.numpy(), spec=False)
+    assert not ctx.last_input_in_place()
+    for k in ("mags", "mass", "lbol"):
+        np.testing.assert_array_equal(a[k], b[k])
+    idx = np.arange(0, n, 4999)
+    ref = oracle40.csp_batch({k: v[idx] for k, v in params.items()}, wz[idx])
+    assert float(np.nanmax(np.abs(a["mags"][idx] - ref["mags"]))) <= 1e-3
+    np.testing.assert_allclose(a["mass"][idx], ref["mass"], rtol=1e-12)
+    assert in_place in (True, False)
