@@ -194,6 +194,10 @@ class Context:
 
     # -- settings
     def set_int(self, key: str, value: int):
+        if key == "add_dust_emission" and int(value) == 1:
+            # the dust emission templates in the data root (written first if missing)
+            from . import synth_dust
+            synth_dust.generate(Path(os.environ["OPENSPS_DATA_HOME"]))
         st = C.c_int(0)
         self.lib.opensps_context_set_int(self.handle, key.encode(), int(value), C.byref(st))
         _check(st, self.lib)

@@ -354,7 +354,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // host's checks and parameter staging; the parameter table follows it on the same stream, then the other chunks
     // (the first kernels need the table)
     constexpr int CHUNK = 16384;
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;
+    // dust emission (add_dust_emission, for models with dust1 or dust2 above SAFE_FLOOR: batch_model_indices
+    // :1569-1570): the per-model epilogue forms it from the young and old sums
+    bool any_emis = false;
+    if (c.add_dust_emission == 1)
+        for (int m = 0; m < n && !any_emis; ++m)
+            any_emis = par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR;
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts || any_emis;
     const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts &&
                          n >= 2 * CHUNK;
     // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
@@ -433,7 +439,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
         if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
-        if (io.young || io.old || io.keep_parts) nacc2 = true;   // the parts need the young and old sums apart
+        if (io.young || io.old || io.keep_parts || any_emis) nacc2 = true;   // the parts need the young and old sums apart
         const double sig = par(m, PF_SIGMA_SMOOTH);
         if (sig > SAFE_FLOOR) {
             any_smooth = true;
@@ -488,6 +494,30 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     if (fp64 && (io.dev_inputs || io.keep_parts || io.young || io.old)) {
         err = "the plain FP64 path computes host-input batches' outputs only (no parts, device inputs or gradients)";
         return ST_UNSUPPORTED;
+    }
+    std::vector<DustEmModel> dem;
+    if (any_emis) {
+        if (fp64) { err = "dust emission is not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts) { err = "gradients with dust emission are not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.dev_inputs) { err = "dust emission needs host inputs on this path"; return ST_UNSUPPORTED; }
+        if (int rc = dustem_load(c, err)) return rc;
+        // dl07_indices (src/physics/opensps_csp_batch.f90:1622-1634): the grid cell in q_PAH and U_min (clamped to
+        // the grid) and the weights, clamped to [0, 1]; gamma clamped to [0, 1]
+        const DustEmission &d = c.dustem;
+        auto cell = [](const std::vector<double> &g, double x, int &i, float &w) {
+            int k = (int)(std::upper_bound(g.begin(), g.end(), x) - g.begin());   // entries <= x (find_interval)
+            k = std::max(1, std::min(k, (int)g.size() - 1));
+            i = k - 1;
+            w = (float)std::max(0.0, std::min((x - g[i]) / (g[i + 1] - g[i]), 1.0));
+        };
+        dem.resize(n);
+        for (int m = 0; m < n; ++m) {
+            DustEmModel &q = dem[m];
+            q.on = (par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR) ? 1 : 0;
+            cell(d.qpah, par(m, PF_DUSTE_QPAH), q.iq, q.wq);
+            cell(d.umin, par(m, PF_DUSTE_UMIN), q.iu, q.wu);
+            q.gam = (float)std::max(0.0, std::min(par(m, PF_DUSTE_GAMMA), 1.0));
+        }
     }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
@@ -686,6 +716,25 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         return run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st);
     };
+    // the per-model epilogue from the young and old sums (the operator's path, and any batch with dust emission)
+    const DustEmModel *d_dem = nullptr;
+    if (any_emis) {
+        if ((e = c.d_dem.reserve(n)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c.d_dem.p, dem.data(), sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+            err = cuda_msg("dust emission inputs", e);
+            return ST_DATA_MISSING;
+        }
+        d_dem = c.d_dem.p;
+    }
+    auto epilogue = [&](const float *y, const float *o) -> cudaError_t {
+        PartsEpilogueArgs pe;
+        pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
+        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = y; pe.old = o;
+        pe.spec = c.d_spec.p;
+        pe.dem = d_dem;
+        pe.dtab = c.dustem.tab.p; pe.cnu = c.dustem.cnu.p; pe.nqpah = c.dustem.nqpah;
+        return run_parts_epilogue(pe, st);
+    };
     if (!fp64 && !ops) {
         // ---- the mixed path over models [off, off + nk): weight operand, contraction with its epilogue, bands,
         // FP64 sums (stage marks on the first range)
@@ -776,7 +825,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
             c.pinned_mags_n = (size_t)n * nb;
         }
-        if (!chunked) {
+        if (!chunked && any_emis) {
+            // (the contraction's own epilogue has no energy balance: the spectra again from the young and old sums)
+            if (int rc = run_range(0, n, true, false)) return rc;
+            if ((e = epilogue(d_y, d_o)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+            if (want_mags && (e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
+            launches += 1 + (want_mags ? 1 : 0);
+        } else if (!chunked) {
             if (int rc = run_range(0, n, true, true)) return rc;
         } else {
             // chunks: each chunk's weight operand, contraction, bands and FP64 sums run while the next chunk's
@@ -821,11 +876,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, al.data(), itesc, d_y, d_o, err);
             if (rc) return rc;
             prof_mark(c, 2);
-            PartsEpilogueArgs pe;
-            pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
-            pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = d_y; pe.old = d_o;
-            pe.spec = c.d_spec.p;
-            if ((e = run_parts_epilogue(pe, st)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+            if ((e = epilogue(d_y, d_o)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
             prof_mark(c, 3);
             launches = 2 + c.ops_launches;   // model parameters, the operator's kernels, the epilogue
         }

@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <sstream>
 #include "context.h"
 
@@ -22,13 +23,14 @@ static const ParamInfo PARAMS[] = {
     {"min_wave_smooth", PF_MIN_WAVE_SMOOTH, 1.0e3}, {"max_wave_smooth", PF_MAX_WAVE_SMOOTH, 1.0e4},
     {"const", PF_CONST, 0.0}, {"fburst", PF_FBURST, 0.0}, {"tburst", PF_TBURST, 11.0},
     {"sf_start", PF_SF_START, 0.0}, {"sf_trunc", PF_SF_TRUNC, 0.0}, {"imf1", PF_IMF1, 1.3},
-    {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3},
+    {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3}, {"duste_qpah", PF_DUSTE_QPAH, 3.5},
+    {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01},
     // known to the reference, not varied per model by this path
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
     {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
     {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
     {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
-    {"duste_gamma", -1, 0.01}, {"duste_umin", -1, 1.0}, {"duste_qpah", -1, 3.5}, {"gas_logu", -1, -2.0},
+    {"gas_logu", -1, -2.0},
     {"gas_logz", -1, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
     {"fagn", -1, 0.0}, {"agn_tau", -1, 10.0}, {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
     {"wgp1", -1, 1.0}, {"wgp2", -1, 1.0}, {"wgp3", -1, 1.0}, {"compute_mags", -1, 1.0},
@@ -174,8 +176,8 @@ Context::~Context() {
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
-    ops.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
-    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
+    ops.release(); dustem.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
+    d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_dem.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);
     emu.release();
     if (pinned_spec) cudaFreeHost(pinned_spec);
@@ -263,6 +265,50 @@ static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
     cudaError_t e = b.reserve(n);
     if (e != cudaSuccess) return e;
     return cudaMemcpy(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+}
+
+// The dust emission templates from the data root's dust_dl07 dataset (the reference reads its Draine & Li files at
+// setup; here the synthetic stand-in): q_PAH and U_min grids, the templates on the context's wavelength grid, and
+// the per-pixel frequency trapezoid weights of the energy sums (dust_emission_reductions' wt, the grid's
+// prepare_batch_grid :262-265).
+int dustem_load(Context &c, std::string &err) {
+    if (c.dustem.ready) return 0;
+    const std::string dir = data_root() + "/dust_dl07/";
+    std::ifstream mf(dir + "manifest.json");
+    if (!mf) { err = "dust emission data missing under " + dir; return ST_DATA_MISSING; }
+    const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
+    long long nq = 0, nu = 0, ns = 0;
+    if (!manifest_int(text, "nqpah", nq) || !manifest_int(text, "numin", nu) || !manifest_int(text, "nspec", ns) ||
+        ns != c.nspec || nq < 2 || nu < 2) {
+        err = "dust emission data under " + dir + " does not match the context's grid";
+        return ST_DATA_MISSING;
+    }
+    DustEmission &d = c.dustem;
+    std::vector<float> tab((size_t)ns * nq * 2 * nu);
+    std::ifstream tf(dir + "dustem.f32", std::ios::binary);
+    if (!read_f64(dir + "qpah.f64", d.qpah, (size_t)nq) || !read_f64(dir + "umin.f64", d.umin, (size_t)nu) || !tf ||
+        !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
+        err = "dust emission data under " + dir + " is incomplete";
+        return ST_DATA_MISSING;
+    }
+    std::vector<float> cnu((size_t)ns, 0.f);
+    for (int i = 0; i + 1 < ns; ++i) {
+        const double wt = 0.5 * std::fabs(C_LIGHT / c.lam[i + 1] - C_LIGHT / c.lam[i]);
+        cnu[i] += (float)wt;
+        cnu[i + 1] += (float)wt;
+    }
+    cudaError_t e;
+    if ((e = d.tab.reserve(tab.size())) != cudaSuccess || (e = d.cnu.reserve(cnu.size())) != cudaSuccess ||
+        (e = cudaMemcpy(d.tab.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(d.cnu.p, cnu.data(), sizeof(float) * cnu.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        err = std::string("dust emission upload: ") + cudaGetErrorString(e);
+        d.release();
+        return ST_DATA_MISSING;
+    }
+    d.nqpah = (int)nq;
+    d.numin = (int)nu;
+    d.ready = true;
+    return 0;
 }
 
 int context_load_filters(Context &c, const std::string &name, std::string &err) {

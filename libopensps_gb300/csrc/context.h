@@ -24,7 +24,7 @@ enum ParamId {
     PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC,
     PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
-    PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3,
+    PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
     PF_COUNT
 };
 
@@ -108,6 +108,18 @@ struct SspOps {
     }
 };
 
+// The dust emission's template grid (dust_emission_reductions / add_dust_emission / dl07_shape of OpenSPS): on
+// the device nspec x nqpah x 2 numin FP32 templates (pixel fastest; column 2 u + c, c = 0 the U_min
+// delta-function, 1 the power law) and per pixel the trapezoid weight in frequency of the energy sums, c(p) =
+// wt(p) + wt(p - 1), wt(i) = |nu(i + 1) - nu(i)| / 2 (wt beyond the last pixel 0).
+struct DustEmission {
+    bool ready = false;
+    int nqpah = 0, numin = 0;
+    std::vector<double> qpah, umin;
+    DevBuf<float> tab, cnu;
+    void release() { tab.release(); cnu.release(); ready = false; }
+};
+
 // What the reverse pass needs of the forward batch it follows.
 struct BatchGeom {
     BasisOperand *bop = nullptr;
@@ -124,6 +136,7 @@ struct Context {
     int sfh = 0, nebemlineinspec = 1, fast_mode = 0, zmet = 1, imf_type = 2;
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
+    int add_dust_emission = 0;   // the energy-balance dust emission (Draine & Li templates)
     bool ops_last_interp = false;   // the last operator batch took the interpolated fold
     int ops_launches = 0;        // kernels the last run_ops_parts launched
     int pageable_access = -1;    // the device reads pageable host memory (-1: not asked yet)
@@ -181,6 +194,8 @@ struct Context {
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
     DevBuf<double2> d_sfh_mtab;  // the SFH's moments at the grid ages (n x nt)
     DevBuf<unsigned char> d_dual;
+    // the dust emission templates (Draine & Li shapes) and the frequency trapezoid weights of the grid
+    DustEmission dustem;
     SspOps ops;
     Emulator emu;                // the learned emulator (emulator.cu, emulator_train.cu)
     DevBuf<double> d_w64, d_y64, d_bc64, d_igm_a64;
@@ -191,6 +206,7 @@ struct Context {
     DevBuf<__nv_bfloat16> d_ix_hi, d_ix_lo;   // the interpolated fold's operand: node values x SFH weights
     DevBuf<float> d_ipart;       // and its GEMM's split-K partial sums
     DevBuf<double2> d_ix_const;  // and each model's 1 / T and c2
+    DevBuf<DustEmModel> d_dem;   // the batch's dust emission cells (one per model)
     DevBuf<float> d_bpart;       // the band GEMM's partial fluxes when it splits the pixels (few models)
     DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
     DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab
@@ -261,6 +277,7 @@ struct BatchIO {
 int run_batch(Context &c, const BatchIO &io, std::string &err);
 // The SSP operator (ssp_op.cu): build from the data root, the young / old sums of a batch, one IMF's SSP grid.
 int ops_build(Context &c, std::string &err);
+int dustem_load(Context &c, std::string &err);
 // The plain FP64 path (fp64_path.cu): the age sums by DGEMM and the rest in FP64, into the host outputs of io.
 void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<double> &b);
 int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,

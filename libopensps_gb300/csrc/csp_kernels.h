@@ -293,11 +293,22 @@ struct OpsRevArgs {
 };
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);
 // The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).
+// A model's dust emission: on, the Draine & Li grid cell (iq, iu: 0-based lower corner) with its weights and gamma
+// (dl07_indices, src/physics/opensps_csp_batch.f90:1622-1634).
+struct DustEmModel {
+    int on, iq, iu;
+    float wq, wu, gam;
+};
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
     const float *pix, *mpar;
     const float *young, *old;     // n x nspec
     float *spec;                  // n x nspec
+    // dust emission (dem null: none): per model its cell; the templates (nspec x nqpah x 2 numin) and the frequency
+    // trapezoid weights per pixel
+    const DustEmModel *dem = nullptr;
+    const float *dtab = nullptr, *cnu = nullptr;
+    int nqpah = 0;
 };
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
 

@@ -759,8 +759,25 @@ cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------------------------- the epilogue
+// One model per CTA from its young and old sums: the attenuation (attenuate_batch, power law), with dust emission
+// the energy balance (dust_emission_reductions / add_dust_emission, src/physics/opensps_csp_batch.f90:3963-4099:
+// the light the screens absorb, summed with the grid's frequency trapezoid weights, re-emitted as the Draine & Li
+// shape times the diffuse transmission, scaled so that its escaping part carries the absorbed luminosity; dl07_shape
+// :4103-4122), then the IGM (apply_igm_z) and the velocity smoothing.
+__device__ __forceinline__ float dl07_shape(const float *tab, int ns, int nq, int i, const DustEmModel &d) {
+    const int k0 = 2 * d.iu, k1 = 2 * (d.iu + 1);
+    const float *a = tab + (size_t)i;
+    auto T = [&](int k, int q) { return __ldg(a + ((size_t)k * nq + q) * ns); };
+    const float w00 = (1.f - d.wq) * (1.f - d.wu), w10 = d.wq * (1.f - d.wu), w11 = d.wq * d.wu, w01 = (1.f - d.wq) * d.wu;
+    const float lo = w00 * T(k0, d.iq) + w10 * T(k0, d.iq + 1) + w11 * T(k1, d.iq + 1) + w01 * T(k1, d.iq);
+    const float hi = w00 * T(k0 + 1, d.iq) + w10 * T(k0 + 1, d.iq + 1) + w11 * T(k1 + 1, d.iq + 1) + w01 * T(k1 + 1, d.iq);
+    return fmaxf((1.f - d.gam) * lo + d.gam * hi, FLT_MIN);
+}
+
 __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a) {
-    extern __shared__ float tsm[];
+    extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
+    float *esm = tsm + a.nspec;
+    __shared__ float red[2][8];
     const int ns = a.nspec, m = blockIdx.x;
     const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
     const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
@@ -768,24 +785,63 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     const float kd1 = mp[MP_KD1], d1i = mp[MP_DUST1_INDEX], one_m_fo = mp[MP_ONE_M_FO], fo = mp[MP_FO];
     const float kd3 = mp[MP_KD3], igm_on = mp[MP_IGM_ON], kcap = mp[MP_IGM_KCAP];
     const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
-    float kb[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) kb[k] = mp[MP_IGM_KB + k];
+    const bool emis = a.dem != nullptr && a.dem[m].on != 0;
+    DustEmModel dm;
+    if (emis) dm = a.dem[m];
+    constexpr float LN2 = 0.6931471805599453f;
+    float sa = 0.f, se = 0.f;
     for (int p = threadIdx.x; p < ns; p += blockDim.x) {
         const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
         const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
-        const float tb = (kd1 != 0.f) ? ops_ex2(kd1 * ops_ex2(d1i * v0.x)) : 1.f;
-        const float to = (kd3 != 0.f) ? ops_ex2(kd3 * curve) : 1.f;
-        const float y = yv[p];
+        const float lb = (kd1 != 0.f) ? kd1 * ops_ex2(d1i * v0.x) : 0.f;   // log2 of the transmissions
+        const float lo2 = kd3 * curve, ld2 = kd2 * curve;
+        const float tb = (kd1 != 0.f) ? ops_ex2(lb) : 1.f;
+        const float to = (kd3 != 0.f) ? ops_ex2(lo2) : 1.f;
+        const float td = ops_ex2(ld2);
+        const float y = yv[p], o = ov[p];
         const float ss = (y * tb * one_m_fo + y * fo) + ov[p] * to;
-        float tot = ss * fmaf(ops_ex2(kd2 * curve), one_m_fnd, fnd);
+        tsm[p] = ss * fmaf(td, one_m_fnd, fnd);
+        if (emis) {
+            // 1 - T of each screen from its exponent (no cancellation at small optical depth)
+            const float omb = (kd1 != 0.f) ? -expm1f(lb * LN2) : 0.f;
+            const float omo = (kd3 != 0.f) ? -expm1f(lo2 * LN2) : 0.f;
+            const float omd = one_m_fnd * -expm1f(ld2 * LN2);
+            const float ay = tb * one_m_fo + fo;
+            const float absorbed = y * (one_m_fo * omb + ay * omd) + o * (omo + to * omd);
+            const float esc = dl07_shape(a.dtab, ns, a.nqpah, p, dm) * td;
+            const float c = __ldg(a.cnu + p);
+            sa = fmaf(c, absorbed, sa);
+            se = fmaf(c, esc, se);
+            esm[p] = esc;
+        }
+    }
+    float rn = 0.f;
+    if (emis) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            sa += __shfl_xor_sync(0xffffffffu, sa, off);
+            se += __shfl_xor_sync(0xffffffffu, se, off);
+        }
+        if (lane == 0) { red[0][warp] = sa; red[1][warp] = se; }
+        __syncthreads();
+        float ta = 0.f, te = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { ta += red[0][w]; te += red[1][w]; }
+        rn = te > SAFE_FLOOR ? ta / te : 0.f;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
+        float tot = tsm[p];
+        if (emis) tot = fmaf(esm[p], rn, tot);
         if (igm_on != 0.f && p < a.jtop) {
             float arg;
             if (p < jmax) {
                 arg = kcap;
             } else {
+                const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
                 const float4 v1 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[1];
-                arg = v0.z * kb[0] + v0.w * kb[1] + v1.x * kb[2] + v1.y * kb[3] + v1.z * kb[4] + v1.w * kb[5];
+                arg = v0.z * mp[MP_IGM_KB] + v0.w * mp[MP_IGM_KB + 1] + v1.x * mp[MP_IGM_KB + 2] +
+                      v1.y * mp[MP_IGM_KB + 3] + v1.z * mp[MP_IGM_KB + 4] + v1.w * mp[MP_IGM_KB + 5];
             }
             tot *= ops_ex2(arg);
         }
@@ -811,7 +867,7 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
 
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (size_t)a.nspec;
+    const size_t smem = sizeof(float) * (size_t)a.nspec * (a.dem ? 2 : 1);
     cudaError_t e = cudaFuncSetAttribute(parts_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     parts_epilogue_kernel<<<a.n, 256, smem, st>>>(a);

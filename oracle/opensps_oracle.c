@@ -298,7 +298,7 @@ int oracle_velocity_row(int n, const double *lam, double sigma, double minl, dou
 
 /* Per-model parameters, in this order (doubles): */
 enum { P_DUST1, P_DUST2, P_DUST3, P_DUST_INDEX, P_DUST1_INDEX, P_FRAC_NODUST, P_FRAC_OBRUN, P_ZRED,
-       P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_NPAR };
+       P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_DUSTE_QPAH, P_DUSTE_UMIN, P_DUSTE_GAMMA, P_NPAR };
 
 typedef struct {
     int nspec, nt, nz, nbands;
@@ -314,6 +314,10 @@ typedef struct {
     int add_igm;             /* add_igm_absorption */
     int smooth;              /* velocity smoothing on (smooth_velocity = 1, smoothspec_fast = 1) */
     double min_wave_smooth, max_wave_smooth;
+    /* dust emission (add_dust_emission; dustem NULL: off): the Draine & Li grid, templates nspec x nqpah x 2 numin
+     * (pixel fastest; column 2 u + c, c = 0 the U_min delta function, 1 the power law) */
+    int nqpah, numin;
+    const double *qpah, *umin, *dustem;
 } oracle_grid_t;
 
 /* One model of compute_csp_batch (src/physics/opensps_csp_batch.f90:431-1214) with a weight matrix over
@@ -362,24 +366,82 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
     (void)ab_only;
 }
 
-/* From the young and old age sums of a model: attenuation, IGM, smoothing, the spectrum and the magnitudes
- * (the stages of compute_csp_batch after the age sums). tot, tmp: nspec doubles of work. */
+/* dl07_indices (src/physics/opensps_csp_batch.f90:1622-1634): the cell of x in the grid g (n values; the lower
+ * corner's 0-based index, clamped so that the cell lies in the grid) and the weight, clamped to [0, 1]. */
+static void dl07_cell(const double *gr, int n, double x, int *i, double *w) {
+    int k = 0;
+    while (k < n && gr[k] <= x) ++k;       /* entries <= x (find_interval) */
+    if (k < 1) k = 1;
+    if (k > n - 1) k = n - 1;
+    *i = k - 1;
+    double t = (x - gr[k - 1]) / (gr[k] - gr[k - 1]);
+    *w = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+}
+
+/* From the young and old age sums of a model: attenuation, dust emission, IGM, smoothing, the spectrum and the
+ * magnitudes (the stages of compute_csp_batch after the age sums). tot, tmp: nspec doubles of work; with dust
+ * emission two more (emis). */
 static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double *spec,
                        double *mags, double *fband_out, double *tot, double *tmp) {
     const int ns = g->nspec;
     /* attenuation, dust_type 0 (power law) */
     double d1 = par[P_DUST1], d2 = par[P_DUST2], d3 = par[P_DUST3], di = par[P_DUST_INDEX], d1i = par[P_DUST1_INDEX];
     double fnd = par[P_FRAC_NODUST], fo = par[P_FRAC_OBRUN];
+    /* dust emission (batch_model_indices :1569-1570): models with dust1 or dust2 above SAFE_FLOOR */
+    const int emis = g->dustem != NULL && (d1 > SAFE_FLOOR || d2 > SAFE_FLOOR);
+    double s_abs = 0.0, s_esc = 0.0, prev_abs = 0.0, prev_esc = 0.0;
+    int iq = 0, iu = 0;
+    double wq = 0.0, wu = 0.0, gam = 0.0;
+    double *esc = NULL;
+    if (emis) {
+        dl07_cell(g->qpah, g->nqpah, par[P_DUSTE_QPAH], &iq, &wq);
+        dl07_cell(g->umin, g->numin, par[P_DUSTE_UMIN], &iu, &wu);
+        gam = par[P_DUSTE_GAMMA] < 0.0 ? 0.0 : (par[P_DUSTE_GAMMA] > 1.0 ? 1.0 : par[P_DUSTE_GAMMA]);
+        esc = (double *)malloc(sizeof(double) * (size_t)ns);
+    }
     for (int i = 0; i < ns; ++i) {
         double ltab = log(g->lam[i] / V_BAND);
         double curve = 1.0;
         if (di != 0.0) curve = curve * exp(di * ltab);
         double tau_d = d2 * curve, td = exp(-tau_d);
-        double tb = 1.0, too = 1.0;
-        if (!(d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR)) tb = exp(-(d1 * exp(d1i * ltab)));
-        if (!(fabs(d3) <= SAFE_FLOOR)) too = exp(-(d3 * curve));
+        double tb = 1.0, too = 1.0, tau_b = 0.0, tau_o = 0.0;
+        if (!(d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR)) { tau_b = d1 * exp(d1i * ltab); tb = exp(-tau_b); }
+        if (!(fabs(d3) <= SAFE_FLOOR)) { tau_o = d3 * curve; too = exp(-tau_o); }
         double ss = (y[i] * tb * (1.0 - fo) + y[i] * fo) + o[i] * too;
         tot[i] = (1.0 - fnd <= SAFE_FLOOR) ? ss : ss * (td * (1.0 - fnd) + fnd);
+        if (emis) {
+            /* attenuate_batch :3640-3655: the absorbed light (1 - T of each screen, here -expm1(-tau)), the
+             * dl07_shape template :4103-4122 times the diffuse transmission */
+            double omb = -expm1(-tau_b), omo = -expm1(-tau_o);
+            double omd = (1.0 - fnd <= SAFE_FLOOR) ? 0.0 : (1.0 - fnd) * -expm1(-tau_d);
+            double ay = tb * (1.0 - fo) + fo;
+            double absorbed = y[i] * ((1.0 - fo) * omb + ay * omd) + o[i] * (omo + too * omd);
+            const double *T = g->dustem;
+            const size_t sq = (size_t)ns, su = (size_t)ns * g->nqpah;
+            const size_t k0 = (size_t)(2 * iu), k1 = (size_t)(2 * (iu + 1));
+            double lo = (1 - wq) * (1 - wu) * T[i + sq * iq + su * k0] + wq * (1 - wu) * T[i + sq * (iq + 1) + su * k0] +
+                        wq * wu * T[i + sq * (iq + 1) + su * k1] + (1 - wq) * wu * T[i + sq * iq + su * k1];
+            double hi = (1 - wq) * (1 - wu) * T[i + sq * iq + su * (k0 + 1)] +
+                        wq * (1 - wu) * T[i + sq * (iq + 1) + su * (k0 + 1)] + wq * wu * T[i + sq * (iq + 1) + su * (k1 + 1)] +
+                        (1 - wq) * wu * T[i + sq * iq + su * (k1 + 1)];
+            double shape = (1.0 - gam) * lo + gam * hi;
+            if (shape < DBL_MIN) shape = DBL_MIN;
+            esc[i] = shape * td;
+            /* dust_emission_reductions :3963-4042: trapezoids in frequency, wt = |nu(i + 1) - nu(i)| / 2 */
+            if (i > 0) {
+                double wt = 0.5 * fabs(C_LIGHT / g->lam[i] - C_LIGHT / g->lam[i - 1]);
+                s_abs += wt * (prev_abs + absorbed);
+                s_esc += wt * (prev_esc + esc[i]);
+            }
+            prev_abs = absorbed;
+            prev_esc = esc[i];
+        }
+    }
+    if (emis) {
+        /* add_dust_emission :4045-4099 */
+        double rn = s_esc > SAFE_FLOOR ? s_abs / s_esc : 0.0;
+        if (rn != 0.0) for (int i = 0; i < ns; ++i) tot[i] += esc[i] * rn;
+        free(esc);
     }
     /* IGM per model */
     double zr = par[P_ZRED];

@@ -15,10 +15,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 PAR_NAMES = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
-             "igm_factor", "sigma_smooth", "dust_tesc")
+             "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma")
 PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
                 "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
-                "dust_tesc": 7.0}
+                "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01}
 _dp = C.POINTER(C.c_double)
 
 
@@ -33,7 +33,8 @@ class _Grid(C.Structure):
     _fields_ = [("nspec", C.c_int), ("nt", C.c_int), ("nz", C.c_int), ("nbands", C.c_int),
                 ("lam", _dp), ("log_age", _dp), ("basis", _dp), ("mass", _dp), ("lbol", _dp), ("bands", _dp),
                 ("zt", _dp), ("dl", _dp), ("nline", C.c_int), ("line_lum", _dp), ("add_igm", C.c_int),
-                ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double)]
+                ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double),
+                ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp)]
 
 
 class _OpsT(C.Structure):
@@ -126,7 +127,8 @@ class Oracle:
 
     def __init__(self, data: dict, nbands: int = 40, add_neb: bool = True, add_igm: bool = True,
                  smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
-                 line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73):
+                 line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73,
+                 dust_emission: dict | None = None):
         L = lib()
         self.d = data
         self.lam = np.ascontiguousarray(data["lambda"])
@@ -157,6 +159,14 @@ class Oracle:
         g.line_lum = _p(self.line_lum) if add_neb else None
         g.add_igm, g.smooth = int(add_igm), int(smooth)
         g.min_wave_smooth, g.max_wave_smooth = min_wave_smooth, max_wave_smooth
+        g.dustem = None
+        if dust_emission is not None:
+            # the Draine & Li grid (synth_dust.load()): templates (2 numin, nqpah, nspec) C order
+            self._dq = np.ascontiguousarray(dust_emission["qpah"], dtype=np.float64)
+            self._du = np.ascontiguousarray(dust_emission["umin"], dtype=np.float64)
+            self._dt = np.ascontiguousarray(dust_emission["dustem"], dtype=np.float64)
+            g.nqpah, g.numin = self._dq.size, self._du.size
+            g.qpah, g.umin, g.dustem = _p(self._dq), _p(self._du), _p(self._dt)
         self.grid = g
         self.nline = nl
 
