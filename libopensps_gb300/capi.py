@@ -194,10 +194,11 @@ class Context:
 
     # -- settings
     def set_int(self, key: str, value: int):
-        if key == "add_dust_emission" and int(value) == 1:
-            # the dust emission templates in the data root (written first if missing)
+        if key in ("add_dust_emission", "add_agn_dust") and int(value) == 1:
+            # the dust emission / AGN torus templates in the data root (written first if missing)
             from . import synth_dust
-            synth_dust.generate(Path(os.environ["OPENSPS_DATA_HOME"]))
+            gen = synth_dust.generate if key == "add_dust_emission" else synth_dust.generate_agn
+            gen(Path(os.environ["OPENSPS_DATA_HOME"]))
         st = C.c_int(0)
         self.lib.opensps_context_set_int(self.handle, key.encode(), int(value), C.byref(st))
         _check(st, self.lib)

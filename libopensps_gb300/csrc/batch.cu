@@ -356,11 +356,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     constexpr int CHUNK = 16384;
     // dust emission (add_dust_emission, for models with dust1 or dust2 above SAFE_FLOOR: batch_model_indices
     // :1569-1570): the per-model epilogue forms it from the young and old sums
-    bool any_emis = false;
+    bool any_emis = false, any_agn = false;
     if (c.add_dust_emission == 1)
         for (int m = 0; m < n && !any_emis; ++m)
             any_emis = par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR;
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts || any_emis;
+    // the AGN torus (add_agn_dust, for models with fagn above SAFE_FLOOR: agn_indices :1575-1589), in the same epilogue
+    if (c.add_agn_dust == 1)
+        for (int m = 0; m < n && !any_agn; ++m) any_agn = par(m, PF_FAGN) > SAFE_FLOOR;
+    const bool epi_terms = any_emis || any_agn;
+    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts || epi_terms;
     const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts &&
                          n >= 2 * CHUNK;
     // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
@@ -439,7 +443,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
         if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
-        if (io.young || io.old || io.keep_parts || any_emis) nacc2 = true;   // the parts need the young and old sums apart
+        if (io.young || io.old || io.keep_parts || epi_terms) nacc2 = true;   // the parts need the young and old sums apart
         const double sig = par(m, PF_SIGMA_SMOOTH);
         if (sig > SAFE_FLOOR) {
             any_smooth = true;
@@ -496,11 +500,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return ST_UNSUPPORTED;
     }
     std::vector<DustEmModel> dem;
-    if (any_emis) {
-        if (fp64) { err = "dust emission is not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts) { err = "gradients with dust emission are not supported on this path"; return ST_UNSUPPORTED; }
-        if (io.dev_inputs) { err = "dust emission needs host inputs on this path"; return ST_UNSUPPORTED; }
-        if (int rc = dustem_load(c, err)) return rc;
+    if (epi_terms) {
+        if (fp64) { err = "dust emission and AGN are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts) { err = "gradients with dust emission or AGN are not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.dev_inputs) { err = "dust emission and AGN need host inputs on this path"; return ST_UNSUPPORTED; }
+        if (any_emis) { if (int rc = dustem_load(c, err)) return rc; }
+        if (any_agn) { if (int rc = agn_load(c, err)) return rc; }
         // dl07_indices (src/physics/opensps_csp_batch.f90:1622-1634): the grid cell in q_PAH and U_min (clamped to
         // the grid) and the weights, clamped to [0, 1]; gamma clamped to [0, 1]
         const DustEmission &d = c.dustem;
@@ -513,10 +518,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         dem.resize(n);
         for (int m = 0; m < n; ++m) {
             DustEmModel &q = dem[m];
-            q.on = (par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR) ? 1 : 0;
-            cell(d.qpah, par(m, PF_DUSTE_QPAH), q.iq, q.wq);
-            cell(d.umin, par(m, PF_DUSTE_UMIN), q.iu, q.wu);
-            q.gam = (float)std::max(0.0, std::min(par(m, PF_DUSTE_GAMMA), 1.0));
+            q = DustEmModel{};
+            q.on = (any_emis && (par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR)) ? 1 : 0;
+            if (q.on) {
+                cell(d.qpah, par(m, PF_DUSTE_QPAH), q.iq, q.wq);
+                cell(d.umin, par(m, PF_DUSTE_UMIN), q.iu, q.wu);
+                q.gam = (float)std::max(0.0, std::min(par(m, PF_DUSTE_GAMMA), 1.0));
+            }
+            q.agn = (any_agn && par(m, PF_FAGN) > SAFE_FLOOR) ? 1 : 0;
+            if (q.agn) {
+                cell(c.agn.tau, par(m, PF_AGN_TAU), q.ita, q.wta);
+                q.fagn = (float)par(m, PF_FAGN);
+            }
         }
     }
     if (ops) {
@@ -718,7 +731,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     };
     // the per-model epilogue from the young and old sums (the operator's path, and any batch with dust emission)
     const DustEmModel *d_dem = nullptr;
-    if (any_emis) {
+    if (epi_terms) {
         if ((e = c.d_dem.reserve(n)) != cudaSuccess ||
             (e = cudaMemcpyAsync(c.d_dem.p, dem.data(), sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
             err = cuda_msg("dust emission inputs", e);
@@ -733,6 +746,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         pe.spec = c.d_spec.p;
         pe.dem = d_dem;
         pe.dtab = c.dustem.tab.p; pe.cnu = c.dustem.cnu.p; pe.nqpah = c.dustem.nqpah;
+        pe.agn_spec = c.agn.spec.p;
+        // (the model's L_bol output: log-blended between the slabs for weights formed on the device, except with
+        // the operators, whose L_bol is their linear row)
+        const bool blend = io.sfh_par != nullptr && !ops;
+        pe.lsum = blend ? c.d_lblend.p : c.d_sums.p + 1;
+        pe.lsum_stride = blend ? 3 : 6;
         return run_parts_epilogue(pe, st);
     };
     if (!fp64 && !ops) {
@@ -825,7 +844,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
             c.pinned_mags_n = (size_t)n * nb;
         }
-        if (!chunked && any_emis) {
+        if (!chunked && epi_terms) {
             // (the contraction's own epilogue has no energy balance: the spectra again from the young and old sums)
             if (int rc = run_range(0, n, true, false)) return rc;
             if ((e = epilogue(d_y, d_o)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }

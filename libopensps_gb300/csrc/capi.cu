@@ -280,12 +280,13 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "imf_type") c->imf_type = value;
     else if (k == "keep_maggies") c->keep_maggies = value;
     else if (k == "add_dust_emission") c->add_dust_emission = value;
-    else if (k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_stellar_remnants" ||
+    else if (k == "add_agn_dust") c->add_agn_dust = value;
+    else if (k == "add_neb_continuum" || k == "add_stellar_remnants" ||
              k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" ||
              k == "redshift_colors" || k == "cloudy_dust" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
              k == "vactoair_flag") {
         // known settings this path keeps at the values it implements; other values are refused at batch time
-        if ((k == "add_agn_dust" || k == "add_neb_continuum" || k == "add_xrb_emission" ||
+        if ((k == "add_neb_continuum" || k == "add_xrb_emission" ||
              k == "redshift_colors") && value != 0)
             return fail(status, 104, k + " = 1 is not supported on this path");
     } else {

@@ -24,7 +24,8 @@ static const ParamInfo PARAMS[] = {
     {"const", PF_CONST, 0.0}, {"fburst", PF_FBURST, 0.0}, {"tburst", PF_TBURST, 11.0},
     {"sf_start", PF_SF_START, 0.0}, {"sf_trunc", PF_SF_TRUNC, 0.0}, {"imf1", PF_IMF1, 1.3},
     {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3}, {"duste_qpah", PF_DUSTE_QPAH, 3.5},
-    {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01},
+    {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01}, {"fagn", PF_FAGN, 0.0},
+    {"agn_tau", PF_AGN_TAU, 10.0},
     // known to the reference, not varied per model by this path
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
     {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
@@ -32,7 +33,7 @@ static const ParamInfo PARAMS[] = {
     {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
     {"gas_logu", -1, -2.0},
     {"gas_logz", -1, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
-    {"fagn", -1, 0.0}, {"agn_tau", -1, 10.0}, {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
+    {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
     {"wgp1", -1, 1.0}, {"wgp2", -1, 1.0}, {"wgp3", -1, 1.0}, {"compute_mags", -1, 1.0},
     {"compute_indices", -1, 1.0},
 };
@@ -176,7 +177,7 @@ Context::~Context() {
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
-    ops.release(); dustem.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
+    ops.release(); dustem.release(); agn.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
     d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_dem.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);
     emu.release();
@@ -308,6 +309,38 @@ int dustem_load(Context &c, std::string &err) {
     d.nqpah = (int)nq;
     d.numin = (int)nu;
     d.ready = true;
+    return 0;
+}
+
+// The AGN torus templates from the data root's agn_torus dataset (the reference reads its torus library at setup;
+// here the synthetic stand-in), on the context's wavelength grid.
+int agn_load(Context &c, std::string &err) {
+    if (c.agn.ready) return 0;
+    const std::string dir = data_root() + "/agn_torus/";
+    std::ifstream mf(dir + "manifest.json");
+    if (!mf) { err = "AGN torus data missing under " + dir; return ST_DATA_MISSING; }
+    const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
+    long long ntau = 0, ns = 0;
+    if (!manifest_int(text, "ntau", ntau) || !manifest_int(text, "nspec", ns) || ns != c.nspec || ntau < 2) {
+        err = "AGN torus data under " + dir + " does not match the context's grid";
+        return ST_DATA_MISSING;
+    }
+    AgnTorus &a = c.agn;
+    std::vector<float> tab((size_t)ntau * ns);
+    std::ifstream tf(dir + "agnspec.f32", std::ios::binary);
+    if (!read_f64(dir + "tau.f64", a.tau, (size_t)ntau) || !tf ||
+        !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
+        err = "AGN torus data under " + dir + " is incomplete";
+        return ST_DATA_MISSING;
+    }
+    cudaError_t e;
+    if ((e = a.spec.reserve(tab.size())) != cudaSuccess ||
+        (e = cudaMemcpy(a.spec.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        err = std::string("AGN torus upload: ") + cudaGetErrorString(e);
+        a.release();
+        return ST_DATA_MISSING;
+    }
+    a.ready = true;
     return 0;
 }
 

@@ -25,6 +25,7 @@ enum ParamId {
     PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
     PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
+    PF_FAGN, PF_AGN_TAU,
     PF_COUNT
 };
 
@@ -120,6 +121,15 @@ struct DustEmission {
     void release() { tab.release(); cnu.release(); ready = false; }
 };
 
+// The AGN torus templates over the torus optical depth (add_agn_batch's agndust_spec(i, ita) over agndust_tau): on
+// the device ntau x nspec FP32 (a template per row).
+struct AgnTorus {
+    bool ready = false;
+    std::vector<double> tau;
+    DevBuf<float> spec;
+    void release() { spec.release(); ready = false; }
+};
+
 // What the reverse pass needs of the forward batch it follows.
 struct BatchGeom {
     BasisOperand *bop = nullptr;
@@ -137,6 +147,7 @@ struct Context {
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     int add_dust_emission = 0;   // the energy-balance dust emission (Draine & Li templates)
+    int add_agn_dust = 0;        // the AGN torus emission
     bool ops_last_interp = false;   // the last operator batch took the interpolated fold
     int ops_launches = 0;        // kernels the last run_ops_parts launched
     int pageable_access = -1;    // the device reads pageable host memory (-1: not asked yet)
@@ -194,8 +205,10 @@ struct Context {
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
     DevBuf<double2> d_sfh_mtab;  // the SFH's moments at the grid ages (n x nt)
     DevBuf<unsigned char> d_dual;
-    // the dust emission templates (Draine & Li shapes) and the frequency trapezoid weights of the grid
+    // the dust emission templates (Draine & Li shapes) and the frequency trapezoid weights of the grid; the AGN torus
+    // templates
     DustEmission dustem;
+    AgnTorus agn;
     SspOps ops;
     Emulator emu;                // the learned emulator (emulator.cu, emulator_train.cu)
     DevBuf<double> d_w64, d_y64, d_bc64, d_igm_a64;
@@ -278,6 +291,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err);
 // The SSP operator (ssp_op.cu): build from the data root, the young / old sums of a batch, one IMF's SSP grid.
 int ops_build(Context &c, std::string &err);
 int dustem_load(Context &c, std::string &err);
+int agn_load(Context &c, std::string &err);
 // The plain FP64 path (fp64_path.cu): the age sums by DGEMM and the rest in FP64, into the host outputs of io.
 void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<double> &b);
 int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,

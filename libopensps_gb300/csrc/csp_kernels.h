@@ -293,11 +293,14 @@ struct OpsRevArgs {
 };
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);
 // The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).
-// A model's dust emission: on, the Draine & Li grid cell (iq, iu: 0-based lower corner) with its weights and gamma
-// (dl07_indices, src/physics/opensps_csp_batch.f90:1622-1634).
+// A model's emission terms of the per-model epilogue: dust emission (on, the Draine & Li grid cell iq, iu: 0-based
+// lower corner, with its weights and gamma: dl07_indices, src/physics/opensps_csp_batch.f90:1622-1634) and the AGN
+// torus (agn, the template interval ita with its weight and fagn: agn_indices :1575-1589).
 struct DustEmModel {
     int on, iq, iu;
     float wq, wu, gam;
+    int agn, ita;
+    float wta, fagn;
 };
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
@@ -309,6 +312,11 @@ struct PartsEpilogueArgs {
     const DustEmModel *dem = nullptr;
     const float *dtab = nullptr, *cnu = nullptr;
     int nqpah = 0;
+    // the AGN torus: the templates (ntau x nspec) and each model's L_bol as the batch outputs it (linear), at
+    // lsum[lsum_stride m]: the FP64 sums' L_bol, or with weights blended at logzsol on the device the log-blended one
+    const float *agn_spec = nullptr;
+    const double *lsum = nullptr;
+    int lsum_stride = 6;
 };
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
 

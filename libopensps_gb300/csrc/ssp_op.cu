@@ -763,7 +763,8 @@ cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
 // the energy balance (dust_emission_reductions / add_dust_emission, src/physics/opensps_csp_batch.f90:3963-4099:
 // the light the screens absorb, summed with the grid's frequency trapezoid weights, re-emitted as the Draine & Li
 // shape times the diffuse transmission, scaled so that its escaping part carries the absorbed luminosity; dl07_shape
-// :4103-4122), then the IGM (apply_igm_z) and the velocity smoothing.
+// :4103-4122), then the IGM (apply_igm_z), the AGN torus (add_agn_batch :4342-4433: fagn L_bol times the template
+// interpolated in the torus optical depth, through the diffuse dust) and the velocity smoothing.
 __device__ __forceinline__ float dl07_shape(const float *tab, int ns, int nq, int i, const DustEmModel &d) {
     const int k0 = 2 * d.iu, k1 = 2 * (d.iu + 1);
     const float *a = tab + (size_t)i;
@@ -785,9 +786,17 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     const float kd1 = mp[MP_KD1], d1i = mp[MP_DUST1_INDEX], one_m_fo = mp[MP_ONE_M_FO], fo = mp[MP_FO];
     const float kd3 = mp[MP_KD3], igm_on = mp[MP_IGM_ON], kcap = mp[MP_IGM_KCAP];
     const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
-    const bool emis = a.dem != nullptr && a.dem[m].on != 0;
     DustEmModel dm;
-    if (emis) dm = a.dem[m];
+    if (a.dem) dm = a.dem[m];
+    const bool emis = a.dem != nullptr && dm.on != 0;
+    const bool agn = a.dem != nullptr && dm.agn != 0;
+    // the AGN's luminosity: fagn times the model's L_bol (add_agn_batch :4342-4433, the value the batch outputs;
+    // 1 when it is not above SAFE_FLOOR, as log10 L_bol is then 0)
+    float lagn = 0.f;
+    if (agn) {
+        const double ls = a.lsum[(size_t)a.lsum_stride * m];
+        lagn = (float)((ls > SAFE_FLOOR ? ls : 1.0) * (double)dm.fagn);
+    }
     constexpr float LN2 = 0.6931471805599453f;
     float sa = 0.f, se = 0.f;
     for (int p = threadIdx.x; p < ns; p += blockDim.x) {
@@ -844,6 +853,13 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
                       v1.y * mp[MP_IGM_KB + 3] + v1.z * mp[MP_IGM_KB + 4] + v1.w * mp[MP_IGM_KB + 5];
             }
             tot *= ops_ex2(arg);
+        }
+        if (agn) {
+            // the torus template between the two bracketing optical depths, through the diffuse dust
+            const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
+            const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
+            const float t0 = __ldg(a.agn_spec + (size_t)dm.ita * ns + p), t1 = __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p);
+            tot = fmaf(lagn * fmaf(dm.wta, t1 - t0, t0), ops_ex2(kd2 * curve), tot);
         }
         tsm[p] = tot;
     }

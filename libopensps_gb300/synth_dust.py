@@ -1,4 +1,5 @@
-"""Synthetic dust emission templates (the Draine & Li 2007 grid's shape), in this package's data-root format.
+"""Synthetic dust emission templates (the Draine & Li 2007 grid's shape) and AGN torus templates, in this package's
+data-root format.
 
 OpenSPS reads the DL07 templates (dust emission per unit dust mass as a function of the PAH mass fraction q_PAH and
 the minimum starlight intensity U_min, each as a delta-function and a power-law distribution of U) from its data
@@ -85,6 +86,56 @@ def generate(root: Path | None = None, force: bool = False) -> Path:
     tab.astype("<f4").tofile(out / "dustem.f32")
     man.write_text(json.dumps({"version": VERSION, "nqpah": nq, "numin": nu, "nspec": int(lam.size)}, indent=1))
     return out
+
+
+# The AGN torus templates (OpenSPS's agndust_spec over agndust_tau: the Nenkova clumpy-torus grid in the torus'
+# optical depth): here hot-dust bodies (1500, 1000, 600, 300 K) whose mix cools as tau grows, with the 9.7 um silicate
+# feature in emission at low tau and in absorption at high tau, each normalised to unit luminosity on the grid.
+AGN_TAU = np.array([5.0, 10.0, 20.0, 30.0, 40.0, 60.0, 80.0, 100.0, 150.0])
+AGN_VERSION = 1
+
+
+def _agn_template(lam: np.ndarray, tau: float) -> np.ndarray:
+    nu = synthdata.C_LIGHT / lam
+    lam_um = lam * 1e-4
+    x = np.log10(tau / 5.0) / np.log10(30.0)                  # 0 .. 1 over the grid
+    temps = (1500.0, 1000.0, 600.0, 300.0)
+    mix = np.array([1.0 - 0.7 * x, 0.8, 0.5 + 0.5 * x, 0.2 + 0.8 * x])
+    body = sum(w * _mbb(nu, t) / _mbb(nu, t).max() for w, t in zip(mix, temps))
+    sil = 1.0 + (0.6 - 1.4 * x) * np.exp(-0.5 * ((lam_um - 9.7) / 0.9) ** 2)
+    t = np.maximum(body * sil, 0.0)
+    return t / max(np.sum(0.5 * (t[1:] + t[:-1]) * np.abs(np.diff(nu))), 1e-300)
+
+
+def generate_agn(root: Path | None = None, force: bool = False) -> Path:
+    """Write the AGN torus templates under ``root/agn_torus`` (``tau.f64``, ``agnspec.f32``: nspec x ntau,
+    column-major; once; ``force`` rewrites)."""
+    root = Path(root) if root is not None else synthdata.default_root()
+    synthdata.generate(root)
+    out = root / "agn_torus"
+    man = out / "manifest.json"
+    if man.exists() and not force:
+        try:
+            if json.loads(man.read_text()).get("version") == AGN_VERSION:
+                return out
+        except (OSError, ValueError):
+            pass
+    out.mkdir(parents=True, exist_ok=True)
+    lam = synthdata.wavelength_grid()
+    tab = np.stack([_agn_template(lam, t) for t in AGN_TAU])  # (ntau, nspec)
+    AGN_TAU.astype("<f8").tofile(out / "tau.f64")
+    tab.astype("<f4").tofile(out / "agnspec.f32")
+    man.write_text(json.dumps({"version": AGN_VERSION, "ntau": int(AGN_TAU.size), "nspec": int(lam.size)}, indent=1))
+    return out
+
+
+def load_agn(root: Path | None = None) -> dict:
+    d = generate_agn(root)
+    man = json.loads((d / "manifest.json").read_text())
+    nt, ns = man["ntau"], man["nspec"]
+    return {"tau": np.fromfile(d / "tau.f64", dtype="<f8"),
+            "agnspec": np.fromfile(d / "agnspec.f32", dtype="<f4").reshape(nt, ns).astype(np.float64),
+            "manifest": man}
 
 
 def load(root: Path | None = None) -> dict:

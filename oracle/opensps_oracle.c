@@ -298,7 +298,8 @@ int oracle_velocity_row(int n, const double *lam, double sigma, double minl, dou
 
 /* Per-model parameters, in this order (doubles): */
 enum { P_DUST1, P_DUST2, P_DUST3, P_DUST_INDEX, P_DUST1_INDEX, P_FRAC_NODUST, P_FRAC_OBRUN, P_ZRED,
-       P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_DUSTE_QPAH, P_DUSTE_UMIN, P_DUSTE_GAMMA, P_NPAR };
+       P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_DUSTE_QPAH, P_DUSTE_UMIN, P_DUSTE_GAMMA, P_FAGN, P_AGN_TAU,
+       P_NPAR };
 
 typedef struct {
     int nspec, nt, nz, nbands;
@@ -318,6 +319,9 @@ typedef struct {
      * (pixel fastest; column 2 u + c, c = 0 the U_min delta function, 1 the power law) */
     int nqpah, numin;
     const double *qpah, *umin, *dustem;
+    /* the AGN torus (add_agn_dust; agn_spec NULL: off): ntau templates of nspec over the optical depth agn_tau */
+    int ntau;
+    const double *agn_tau, *agn_spec;
 } oracle_grid_t;
 
 /* One model of compute_csp_batch (src/physics/opensps_csp_batch.f90:431-1214) with a weight matrix over
@@ -330,8 +334,8 @@ typedef struct {
  *   compute_magnitudes_columns (src/spectra/opensps_batch_photometry.f90:53-180): observed_frame_z :819-903,
  *   band_fluxes :1049-1171 (trapezoid per band support), magnitudes_from_fluxes :185-232 (AB, distance term).
  * work: 4 * nspec doubles. */
-static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double *spec,
-                       double *mags, double *fband_out, double *tot, double *tmp);
+static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double lsum,
+                       double *spec, double *mags, double *fband_out, double *tot, double *tmp);
 
 static void csp_one(const oracle_grid_t *g, const double *wz, const double *par, double *spec, double *mags,
                     double *mass, double *lbol, double *emlines, double *young, double *old, double *fband_out,
@@ -362,7 +366,7 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
     if (lbol) *lbol = ls > SAFE_FLOOR ? log10(ls) : 0.0;
     if (young) memcpy(young, y, sizeof(double) * ns);
     if (old) memcpy(old, o, sizeof(double) * ns);
-    post_parts(g, y, o, par, spec, mags, fband_out, tot, tmp);
+    post_parts(g, y, o, par, ls, spec, mags, fband_out, tot, tmp);
     (void)ab_only;
 }
 
@@ -378,11 +382,11 @@ static void dl07_cell(const double *gr, int n, double x, int *i, double *w) {
     *w = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
 }
 
-/* From the young and old age sums of a model: attenuation, dust emission, IGM, smoothing, the spectrum and the
- * magnitudes (the stages of compute_csp_batch after the age sums). tot, tmp: nspec doubles of work; with dust
- * emission two more (emis). */
-static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double *spec,
-                       double *mags, double *fband_out, double *tot, double *tmp) {
+/* From the young and old age sums of a model (and its linear L_bol lsum): attenuation, dust emission, IGM, the AGN
+ * torus, smoothing, the spectrum and the magnitudes (the stages of compute_csp_batch after the age sums). tot, tmp:
+ * nspec doubles of work. */
+static void post_parts(const oracle_grid_t *g, const double *y, const double *o, const double *par, double lsum,
+                       double *spec, double *mags, double *fband_out, double *tot, double *tmp) {
     const int ns = g->nspec;
     /* attenuation, dust_type 0 (power law) */
     double d1 = par[P_DUST1], d2 = par[P_DUST2], d3 = par[P_DUST3], di = par[P_DUST_INDEX], d1i = par[P_DUST1_INDEX];
@@ -462,6 +466,20 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
             for (int j = 0; j < jtop; ++j) tot[j] *= exp(-tmp[j] * par[P_IGM_FACTOR]);
         }
     }
+    /* the AGN torus (add_agn_batch :4342-4433; agn_indices :1575-1589): fagn L_bol times the template interpolated
+     * in the torus optical depth, times the diffuse transmission */
+    if (g->agn_spec != NULL && par[P_FAGN] > SAFE_FLOOR) {
+        int ita;
+        double wta;
+        dl07_cell(g->agn_tau, g->ntau, par[P_AGN_TAU], &ita, &wta);
+        double lagn = (lsum > SAFE_FLOOR ? lsum : 1.0) * par[P_FAGN];
+        for (int i = 0; i < ns; ++i) {
+            double ltab = log(g->lam[i] / V_BAND);
+            double curve = (di != 0.0) ? exp(di * ltab) : 1.0;
+            double tmpl = (1.0 - wta) * g->agn_spec[(size_t)ns * ita + i] + wta * g->agn_spec[(size_t)ns * (ita + 1) + i];
+            tot[i] += lagn * tmpl * exp(-d2 * curve);
+        }
+    }
     /* velocity smoothing */
     double *fin = tot;
     if (g->smooth && par[P_SIGMA_SMOOTH] > SAFE_FLOOR) {
@@ -512,14 +530,14 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
 
 /* The batch from given young and old age sums (young, old: nspec x n): spectra, magnitudes, band fluxes. */
 void oracle_csp_from_parts(const oracle_grid_t *g, int n, const double *young, const double *old, const double *par,
-                           double *spec, double *mags, double *fband) {
+                           const double *lsum, double *spec, double *mags, double *fband) {
     const int ns = g->nspec;
 #pragma omp parallel
     {
         double *work = (double *)malloc(sizeof(double) * 2 * (size_t)ns);
 #pragma omp for schedule(dynamic, 4)
         for (int m = 0; m < n; ++m)
-            post_parts(g, young + (size_t)ns * m, old + (size_t)ns * m, par + (size_t)P_NPAR * m,
+            post_parts(g, young + (size_t)ns * m, old + (size_t)ns * m, par + (size_t)P_NPAR * m, lsum ? lsum[m] : 0.0,
                        spec ? spec + (size_t)ns * m : NULL, mags ? mags + (size_t)g->nbands * m : NULL,
                        fband ? fband + (size_t)g->nbands * m : NULL, work, work + ns);
         free(work);

@@ -15,10 +15,11 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 PAR_NAMES = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
-             "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma")
+             "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma", "fagn", "agn_tau")
 PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
                 "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
-                "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01}
+                "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01, "fagn": 0.0,
+                "agn_tau": 10.0}
 _dp = C.POINTER(C.c_double)
 
 
@@ -34,7 +35,8 @@ class _Grid(C.Structure):
                 ("lam", _dp), ("log_age", _dp), ("basis", _dp), ("mass", _dp), ("lbol", _dp), ("bands", _dp),
                 ("zt", _dp), ("dl", _dp), ("nline", C.c_int), ("line_lum", _dp), ("add_igm", C.c_int),
                 ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double),
-                ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp)]
+                ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp),
+                ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp)]
 
 
 class _OpsT(C.Structure):
@@ -68,7 +70,7 @@ def lib() -> C.CDLL:
         _lib.oracle_expi.restype = C.c_double
         _lib.oracle_expi.argtypes = [C.c_double]
         _lib.oracle_sfh_batch.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
-        _lib.oracle_csp_from_parts.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        _lib.oracle_csp_from_parts.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         _lib.oracle_ops_csp.argtypes = [C.POINTER(_OpsT), C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp]
         _lib.oracle_kroupa_integral.restype = C.c_double
         _lib.oracle_kroupa_integral.argtypes = [_dp, C.c_double, C.c_double, C.c_int]
@@ -128,7 +130,7 @@ class Oracle:
     def __init__(self, data: dict, nbands: int = 40, add_neb: bool = True, add_igm: bool = True,
                  smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
                  line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73,
-                 dust_emission: dict | None = None):
+                 dust_emission: dict | None = None, agn: dict | None = None):
         L = lib()
         self.d = data
         self.lam = np.ascontiguousarray(data["lambda"])
@@ -167,6 +169,12 @@ class Oracle:
             self._dt = np.ascontiguousarray(dust_emission["dustem"], dtype=np.float64)
             g.nqpah, g.numin = self._dq.size, self._du.size
             g.qpah, g.umin, g.dustem = _p(self._dq), _p(self._du), _p(self._dt)
+        g.agn_spec = None
+        if agn is not None:
+            # the AGN torus templates (synth_dust.load_agn()): (ntau, nspec)
+            self._at = np.ascontiguousarray(agn["tau"], dtype=np.float64)
+            self._as = np.ascontiguousarray(agn["agnspec"], dtype=np.float64)
+            g.ntau, g.agn_tau, g.agn_spec = self._at.size, _p(self._at), _p(self._as)
         self.grid = g
         self.nline = nl
 
@@ -193,16 +201,17 @@ class Oracle:
                                _p(out.get("old")), _p(out.get("fband")))
         return out
 
-    def csp_from_parts(self, params: dict, young: np.ndarray, old: np.ndarray) -> dict:
-        """The batch's stages after the age sums (attenuation, IGM, smoothing, magnitudes) from given young and old
-        spectra (n, nspec)."""
+    def csp_from_parts(self, params: dict, young: np.ndarray, old: np.ndarray, lsum: np.ndarray | None = None) -> dict:
+        """The batch's stages after the age sums (attenuation, dust emission, IGM, AGN, smoothing, magnitudes) from
+        given young and old spectra (n, nspec); lsum (n,): the models' linear L_bol (the AGN's scale)."""
         y = np.ascontiguousarray(young, dtype=np.float64)
         o = np.ascontiguousarray(old, dtype=np.float64)
         n = y.shape[0]
         par = self.pack_params(params, n)
+        ls = None if lsum is None else np.ascontiguousarray(lsum, dtype=np.float64)
         out = {"mags": np.empty((n, self.nbands)), "spec": np.empty((n, self.nspec)), "fband": np.empty((n, self.nbands))}
-        lib().oracle_csp_from_parts(C.byref(self.grid), n, _p(y), _p(o), _p(par), _p(out["spec"]), _p(out["mags"]),
-                                    _p(out["fband"]))
+        lib().oracle_csp_from_parts(C.byref(self.grid), n, _p(y), _p(o), _p(par), _p(ls), _p(out["spec"]),
+                                    _p(out["mags"]), _p(out["fband"]))
         return out
 
     def velocity_row(self, sigma: float, i: int, minl: float = 1.0e3, maxl: float = 1.0e4):
