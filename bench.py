@@ -414,6 +414,39 @@ def sfh_config_measure(args, torch, barrier) -> dict | None:
             "workload": "delayed-tau SFH on the device, logZ blend, power-law dust, z = 0, no nebular emission"}
 
 
+def dust_emission_measure(ctx, params, h_wz, args, barrier) -> dict | None:
+    """The headline batch (B = --batch, nebular lines, IGM) with dust emission (the Draine & Li energy balance) and
+    the AGN torus switched on: per-model q_PAH, U_min, gamma, fagn and tau_AGN, and the birth-cloud, diffuse and
+    extra screens that set what is absorbed. Timed end to end through the C API from the same pinned host weights as
+    the headline e2e (magnitudes, mass and L_bol back to the host)."""
+    from libopensps_gb300 import synth_dust
+    n = h_wz.shape[0]
+    if args.dust_steps <= 0:
+        return None
+    synth_dust.generate()
+    synth_dust.generate_agn()
+    rng = np.random.default_rng(77)
+    p = dict(params, dust1=rng.uniform(0.1, 1.0, n), dust3=rng.uniform(0.0, 0.4, n),
+             frac_obrun=rng.uniform(0.0, 0.3, n), duste_qpah=rng.uniform(0.5, 4.5, n),
+             duste_umin=rng.uniform(0.1, 25.0, n), duste_gamma=rng.uniform(0.0, 0.5, n),
+             fagn=rng.uniform(0.0, 1.0, n), agn_tau=rng.uniform(5.0, 150.0, n))
+    ctx.set_int("add_dust_emission", 1)
+    ctx.set_int("add_agn_dust", 1)
+    try:
+        for i in range(args.warmup + args.dust_steps):
+            if i == args.warmup:
+                barrier()
+                t0 = time.perf_counter()
+            ctx.csp_batch(p, ssp_weights_z=h_wz, spec=False)
+        barrier()
+        ms = (time.perf_counter() - t0) * 1e3 / args.dust_steps
+    finally:
+        ctx.set_int("add_dust_emission", 0)
+        ctx.set_int("add_agn_dust", 0)
+    return {"batch": n, "unit": "models/s", "e2e": n / (ms * 1e-3), "ms_per_step": ms,
+            "workload": "headline batch + dust emission (7 q_PAH x 22 U_min templates) + AGN torus (9 tau)"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -503,6 +536,7 @@ def run_ours(args) -> None:
     e2e_pageable_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     in_place = ctx.last_input_in_place()
     del h_wz_pageable
+    dust_em = dust_emission_measure(ctx, params, h_wz_np, args, barrier)
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
@@ -548,6 +582,7 @@ def run_ours(args) -> None:
             "mixed_over_fp64": (value / fp64["device_value"]) if fp64 and fp64.get("device_value") else None,
             "sfh_config": sfh_cfg,
             "emulator": emulator,
+            "dust_emission": dict(dust_em, over_plain_e2e=dust_em["e2e"] / (n / (e2e_ms * 1e-3))) if dust_em else None,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -576,6 +611,7 @@ def main():
     ap.add_argument("--emu-batch", type=int, default=1048576)
     ap.add_argument("--emu-steps", type=int, default=20)
     ap.add_argument("--emu-e2e-steps", type=int, default=2)
+    ap.add_argument("--dust-steps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -364,8 +364,9 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     if (c.add_agn_dust == 1)
         for (int m = 0; m < n && !any_agn; ++m) any_agn = par(m, PF_FAGN) > SAFE_FLOOR;
     const bool epi_terms = any_emis || any_agn;
-    const bool parts = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts || epi_terms;
-    const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts &&
+    const bool parts_kept = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;   // the caller wants the parts
+    const bool parts = parts_kept || epi_terms;
+    const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts_kept &&
                          n >= 2 * CHUNK;
     // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
     // more on the small chunk than its shorter copy saves)
@@ -499,7 +500,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         err = "the plain FP64 path computes host-input batches' outputs only (no parts, device inputs or gradients)";
         return ST_UNSUPPORTED;
     }
-    std::vector<DustEmModel> dem;
+    DustEmModel *dem = nullptr;            // the per-model cells, page-locked (uploaded beside the parameter table)
     if (epi_terms) {
         if (fp64) { err = "dust emission and AGN are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
         if (io.keep_parts) { err = "gradients with dust emission or AGN are not supported on this path"; return ST_UNSUPPORTED; }
@@ -515,7 +516,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             i = k - 1;
             w = (float)std::max(0.0, std::min((x - g[i]) / (g[i + 1] - g[i]), 1.0));
         };
-        dem.resize(n);
+        if (c.pinned_dem_n < (size_t)n) {
+            if (c.pinned_dem) cudaFreeHost(c.pinned_dem);
+            c.pinned_dem = nullptr;
+            c.pinned_dem_n = 0;
+            if (cudaMallocHost(&c.pinned_dem, sizeof(DustEmModel) * n) != cudaSuccess) {
+                cudaGetLastError();
+                err = "page-locked dust emission inputs: out of memory";
+                return ST_DATA_MISSING;
+            }
+            c.pinned_dem_n = (size_t)n;
+        }
+        dem = c.pinned_dem;
         for (int m = 0; m < n; ++m) {
             DustEmModel &q = dem[m];
             q = DustEmModel{};
@@ -661,6 +673,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("parameter copy", e);
             return ST_DATA_MISSING;
         }
+        if (dem && ((e = c.d_dem.reserve(n)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(c.d_dem.p, dem, sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, cs)) != cudaSuccess)) {
+            err = cuda_msg("dust emission inputs", e);
+            return ST_DATA_MISSING;
+        }
         if (chunked) {
             if ((!c.par_ev && (e = cudaEventCreateWithFlags(&c.par_ev, cudaEventDisableTiming)) != cudaSuccess) ||
                 (e = cudaEventRecord(c.par_ev, c.side)) != cudaSuccess || (e = cudaStreamWaitEvent(st, c.par_ev, 0)) != cudaSuccess) {
@@ -730,34 +747,28 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         return run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st);
     };
     // the per-model epilogue from the young and old sums (the operator's path, and any batch with dust emission)
-    const DustEmModel *d_dem = nullptr;
-    if (epi_terms) {
-        if ((e = c.d_dem.reserve(n)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(c.d_dem.p, dem.data(), sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
-            err = cuda_msg("dust emission inputs", e);
-            return ST_DATA_MISSING;
-        }
-        d_dem = c.d_dem.p;
-    }
-    auto epilogue = [&](const float *y, const float *o) -> cudaError_t {
+    const DustEmModel *d_dem = epi_terms ? c.d_dem.p : nullptr;
+    // (models [off, off + nk))
+    auto epilogue = [&](const float *y, const float *o, int off, int nk) -> cudaError_t {
         PartsEpilogueArgs pe;
-        pe.n = n; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
-        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p; pe.young = y; pe.old = o;
-        pe.spec = c.d_spec.p;
-        pe.dem = d_dem;
+        pe.n = nk; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
+        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
+        pe.young = y + (size_t)ns * off; pe.old = o + (size_t)ns * off;
+        pe.spec = c.d_spec.p + (size_t)ns * off;
+        pe.dem = d_dem ? d_dem + off : nullptr;
         pe.dtab = c.dustem.tab.p; pe.cnu = c.dustem.cnu.p; pe.nqpah = c.dustem.nqpah;
         pe.agn_spec = c.agn.spec.p;
         // (the model's L_bol output: log-blended between the slabs for weights formed on the device, except with
         // the operators, whose L_bol is their linear row)
         const bool blend = io.sfh_par != nullptr && !ops;
-        pe.lsum = blend ? c.d_lblend.p : c.d_sums.p + 1;
+        pe.lsum = (blend ? c.d_lblend.p : c.d_sums.p + 1) + (size_t)(blend ? 3 : 6) * off;
         pe.lsum_stride = blend ? 3 : 6;
         return run_parts_epilogue(pe, st);
     };
     if (!fp64 && !ops) {
         // ---- the mixed path over models [off, off + nk): weight operand, contraction with its epilogue, bands,
         // FP64 sums (stage marks on the first range)
-        auto run_range = [&](int off, int nk, bool marks, bool tail) -> int {
+        auto run_range = [&](int off, int nk, bool marks) -> int {
             if ((e = model_params(off, nk)) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
             if (marks) prof_mark(c, 1);
             WeightsArgs w = wa;
@@ -794,7 +805,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
             ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
             ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
-            ca.spec = c.d_spec.p + (size_t)ns * off;
+            // (with dust emission or AGN the per-model epilogue forms the spectra from the young and old sums)
+            ca.spec = epi_terms ? nullptr : c.d_spec.p + (size_t)ns * off;
             ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
             ca.young = ca.old = nullptr;
             if (parts) {
@@ -805,7 +817,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
             if (marks) prof_mark(c, 3);
             launches += 3;
-            if (!tail) return 0;
+            if (epi_terms) {
+                if ((e = epilogue(d_y, d_o, off, nk)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+                ++launches;
+                if (marks) prof_mark(c, 4);
+            }
             if (want_mags) {
                 if ((e = bands(off, nk)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
                 ++launches;
@@ -822,7 +838,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                     }
                 }
             }
-            if (marks) prof_mark(c, 4);
+            if (marks && !epi_terms) prof_mark(c, 4);
             return 0;
         };
         if (parts) {
@@ -844,14 +860,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
             c.pinned_mags_n = (size_t)n * nb;
         }
-        if (!chunked && epi_terms) {
-            // (the contraction's own epilogue has no energy balance: the spectra again from the young and old sums)
-            if (int rc = run_range(0, n, true, false)) return rc;
-            if ((e = epilogue(d_y, d_o)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
-            if (want_mags && (e = bands(0, n)) != cudaSuccess) { err = cuda_msg("band kernel", e); return ST_DATA_MISSING; }
-            launches += 1 + (want_mags ? 1 : 0);
-        } else if (!chunked) {
-            if (int rc = run_range(0, n, true, true)) return rc;
+        if (!chunked) {
+            if (int rc = run_range(0, n, true)) return rc;
         } else {
             // chunks: each chunk's weight operand, contraction, bands and FP64 sums run while the next chunk's
             // weights are copied (the copies are the longer part: the kernels hide under them)
@@ -863,7 +873,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                     err = cuda_msg("weights copy", e);
                     return ST_DATA_MISSING;
                 }
-                if (int rc = run_range(off, nk, k == 0, true)) return rc;
+                if (int rc = run_range(off, nk, k == 0)) return rc;
             }
         }
         prof_mark(c, 5);
@@ -895,7 +905,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             const int rc = run_ops_parts(c, n, d_wz, c.d_alpha.p, al.data(), itesc, d_y, d_o, err);
             if (rc) return rc;
             prof_mark(c, 2);
-            if ((e = epilogue(d_y, d_o)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
+            if ((e = epilogue(d_y, d_o, 0, n)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
             prof_mark(c, 3);
             launches = 2 + c.ops_launches;   // model parameters, the operator's kernels, the epilogue
         }

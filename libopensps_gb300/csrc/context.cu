@@ -185,6 +185,9 @@ Context::~Context() {
     if (pinned_par) cudaFreeHost(pinned_par);
     pinned_par = nullptr;
     pinned_par_n = 0;
+    if (pinned_dem) cudaFreeHost(pinned_dem);
+    pinned_dem = nullptr;
+    pinned_dem_n = 0;
     if (pinned_sums) cudaFreeHost(pinned_sums);
     pinned_sums = nullptr;
     pinned_sums_n = 0;

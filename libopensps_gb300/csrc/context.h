@@ -235,6 +235,7 @@ struct Context {
     cudaEvent_t prof_ev[2][NPROF] = {};
     void *pinned_spec = nullptr; size_t pinned_bytes = 0;
     double *pinned_par = nullptr; size_t pinned_par_n = 0;   // page-locked staging of the per-model parameter table
+    DustEmModel *pinned_dem = nullptr; size_t pinned_dem_n = 0;   // page-locked staging of the dust emission / AGN cells
     double *pinned_sums = nullptr; size_t pinned_sums_n = 0; // page-locked copy of the mass and L_bol sums
     std::vector<int> do_band_h;                               // the band mask last uploaded to d_do_band
     double *pinned_mags = nullptr; size_t pinned_mags_n = 0; // page-locked staging of the chunked batch's magnitudes

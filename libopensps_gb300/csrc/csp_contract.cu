@@ -290,8 +290,9 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
                     stageT[j * TROW + r] = tot;
                 }
                 named_bar_sync(bar_id, 128);
-                // ---- phase 2: warp wg takes models 4 wg .. 4 wg + 3; lane l the output rows 4 + 4l .. 7 + 4l
-                if (lane < OUT_ROWS / 4) {
+                // ---- phase 2: warp wg takes models 4 wg .. 4 wg + 3; lane l the output rows 4 + 4l .. 7 + 4l (no
+                // spectra when a per-model epilogue forms them from the young and old sums)
+                if (args.spec != nullptr && lane < OUT_ROWS / 4) {
                     const int row0 = HALO + 4 * lane;
                     const int pq = p0 + row0;                      // first output pixel of this lane
 #pragma unroll 1

@@ -64,7 +64,7 @@ struct ContractArgs {
     int uniform_index;   // every model has the dust_index of the pixel table's curve
     const float *pix;    // nspec x PIX_FLOATS
     const float *mpar;   // n_models x MODEL_PAR_FLOATS
-    float *spec;         // n_models x ld_spec (pixel fastest)
+    float *spec;         // n_models x ld_spec (pixel fastest); null: not written (NACC = 2 with the parts)
     float *young, *old;  // NACC = 2 only, may be null: the age sums before dust (n_models x ld_spec)
     int *status;
 };

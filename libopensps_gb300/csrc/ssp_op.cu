@@ -775,6 +775,26 @@ __device__ __forceinline__ float dl07_shape(const float *tab, int ns, int nq, in
     return fmaxf((1.f - d.gam) * lo + d.gam * hi, FLT_MIN);
 }
 
+// The same for the pixel pair (i, i + 1), i even, nspec even (8-byte loads of the eight template rows).
+__device__ __forceinline__ float2 dl07_shape2(const float *tab, int ns, int nq, int i, const DustEmModel &d) {
+    const int k0 = 2 * d.iu, k1 = 2 * (d.iu + 1);
+    const float *a = tab + (size_t)i;
+    auto T = [&](int k, int q) { return __ldg(reinterpret_cast<const float2 *>(a + ((size_t)k * nq + q) * ns)); };
+    const float w00 = (1.f - d.wq) * (1.f - d.wu), w10 = d.wq * (1.f - d.wu), w11 = d.wq * d.wu, w01 = (1.f - d.wq) * d.wu;
+    const float2 a0 = T(k0, d.iq), a1 = T(k0, d.iq + 1), a2 = T(k1, d.iq + 1), a3 = T(k1, d.iq);
+    const float2 b0 = T(k0 + 1, d.iq), b1 = T(k0 + 1, d.iq + 1), b2 = T(k1 + 1, d.iq + 1), b3 = T(k1 + 1, d.iq);
+    const float lx = w00 * a0.x + w10 * a1.x + w11 * a2.x + w01 * a3.x, ly = w00 * a0.y + w10 * a1.y + w11 * a2.y + w01 * a3.y;
+    const float hx = w00 * b0.x + w10 * b1.x + w11 * b2.x + w01 * b3.x, hy = w00 * b0.y + w10 * b1.y + w11 * b2.y + w01 * b3.y;
+    return make_float2(fmaxf((1.f - d.gam) * lx + d.gam * hx, FLT_MIN), fmaxf((1.f - d.gam) * ly + d.gam * hy, FLT_MIN));
+}
+
+// One CTA per model, three passes over its pixels (the spectrum in shared memory): the attenuated sum (with dust
+// emission also the escaping template and the frequency-trapezoid sums of the absorbed and escaping light, reduced
+// over the block), then the emission, the IGM and the AGN, then the smoothing. Each thread issues the global loads of
+// EPI_U pixel pairs (young and old sums, templates) before it uses them: one pair at a time left the kernel waiting on
+// memory latency at a fraction of the HBM rate.
+constexpr int EPI_U = 4;
+
 __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a) {
     extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
     float *esm = tsm + a.nspec;
@@ -799,17 +819,16 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     }
     constexpr float LN2 = 0.6931471805599453f;
     float sa = 0.f, se = 0.f;
-    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
-        const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
+    auto pix0 = [&](int p) { return __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)); };
+    // pass 1 at one pixel: the attenuated young + old sum; with emission the escaping template (esc) and the sums
+    auto pass1 = [&](const float4 v0, float y, float o, float shape, float cn, float &esc) -> float {
         const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
         const float lb = (kd1 != 0.f) ? kd1 * ops_ex2(d1i * v0.x) : 0.f;   // log2 of the transmissions
         const float lo2 = kd3 * curve, ld2 = kd2 * curve;
         const float tb = (kd1 != 0.f) ? ops_ex2(lb) : 1.f;
         const float to = (kd3 != 0.f) ? ops_ex2(lo2) : 1.f;
         const float td = ops_ex2(ld2);
-        const float y = yv[p], o = ov[p];
-        const float ss = (y * tb * one_m_fo + y * fo) + ov[p] * to;
-        tsm[p] = ss * fmaf(td, one_m_fnd, fnd);
+        const float ss = (y * tb * one_m_fo + y * fo) + o * to;
         if (emis) {
             // 1 - T of each screen from its exponent (no cancellation at small optical depth)
             const float omb = (kd1 != 0.f) ? -expm1f(lb * LN2) : 0.f;
@@ -817,11 +836,46 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
             const float omd = one_m_fnd * -expm1f(ld2 * LN2);
             const float ay = tb * one_m_fo + fo;
             const float absorbed = y * (one_m_fo * omb + ay * omd) + o * (omo + to * omd);
-            const float esc = dl07_shape(a.dtab, ns, a.nqpah, p, dm) * td;
-            const float c = __ldg(a.cnu + p);
-            sa = fmaf(c, absorbed, sa);
-            se = fmaf(c, esc, se);
-            esm[p] = esc;
+            esc = shape * td;
+            sa = fmaf(cn, absorbed, sa);
+            se = fmaf(cn, esc, se);
+        }
+        return ss * fmaf(td, one_m_fnd, fnd);
+    };
+    const int bd = (int)blockDim.x;
+    if ((ns & 1) == 0) {
+        const int np2 = ns >> 1;
+        const float2 *y2 = reinterpret_cast<const float2 *>(yv), *o2 = reinterpret_cast<const float2 *>(ov);
+        for (int q0 = threadIdx.x; q0 < np2; q0 += EPI_U * bd) {
+            float2 yy[EPI_U], oo[EPI_U];
+#pragma unroll
+            for (int u = 0; u < EPI_U; ++u) {
+                const int q = min(q0 + u * bd, np2 - 1);      // (past the end: the last pair again, not used)
+                yy[u] = __ldg(y2 + q);
+                oo[u] = __ldg(o2 + q);
+            }
+#pragma unroll
+            for (int u = 0; u < EPI_U; ++u) {
+                const int q = q0 + u * bd;
+                if (q >= np2) break;
+                float2 sh = make_float2(0.f, 0.f), cn = make_float2(0.f, 0.f);
+                if (emis) {
+                    sh = dl07_shape2(a.dtab, ns, a.nqpah, 2 * q, dm);
+                    cn = __ldg(reinterpret_cast<const float2 *>(a.cnu) + q);
+                }
+                float e0 = 0.f, e1 = 0.f;
+                const float t0 = pass1(pix0(2 * q), yy[u].x, oo[u].x, sh.x, cn.x, e0);
+                const float t1 = pass1(pix0(2 * q + 1), yy[u].y, oo[u].y, sh.y, cn.y, e1);
+                reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
+                if (emis) reinterpret_cast<float2 *>(esm)[q] = make_float2(e0, e1);
+            }
+        }
+    } else {
+        for (int p = threadIdx.x; p < ns; p += bd) {
+            float esc = 0.f;
+            tsm[p] = pass1(pix0(p), __ldg(yv + p), __ldg(ov + p), emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
+                           emis ? __ldg(a.cnu + p) : 0.f, esc);
+            if (emis) esm[p] = esc;
         }
     }
     float rn = 0.f;
@@ -835,33 +889,43 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
         if (lane == 0) { red[0][warp] = sa; red[1][warp] = se; }
         __syncthreads();
         float ta = 0.f, te = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { ta += red[0][w]; te += red[1][w]; }
+        for (int w = 0; w < (bd >> 5); ++w) { ta += red[0][w]; te += red[1][w]; }
         rn = te > SAFE_FLOOR ? ta / te : 0.f;
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
-        float tot = tsm[p];
-        if (emis) tot = fmaf(esm[p], rn, tot);
-        if (igm_on != 0.f && p < a.jtop) {
-            float arg;
-            if (p < jmax) {
-                arg = kcap;
-            } else {
-                const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
-                const float4 v1 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[1];
-                arg = v0.z * mp[MP_IGM_KB] + v0.w * mp[MP_IGM_KB + 1] + v1.x * mp[MP_IGM_KB + 2] +
-                      v1.y * mp[MP_IGM_KB + 3] + v1.z * mp[MP_IGM_KB + 4] + v1.w * mp[MP_IGM_KB + 5];
+    // pass 2: the emission, the IGM, the AGN (the torus template between the two bracketing optical depths, through
+    // the diffuse dust); the global loads of EPI_U pixels first
+    const bool igm = igm_on != 0.f;
+    for (int p0 = threadIdx.x; p0 < ns; p0 += EPI_U * bd) {
+        float4 v0[EPI_U], v1[EPI_U];
+        float g0[EPI_U], g1[EPI_U];
+#pragma unroll
+        for (int u = 0; u < EPI_U; ++u) {
+            const int p = min(p0 + u * bd, ns - 1);
+            v0[u] = pix0(p);
+            v1[u] = (igm && p < a.jtop && p >= jmax) ? __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS) + 1)
+                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+            g0[u] = agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f;
+            g1[u] = agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < EPI_U; ++u) {
+            const int p = p0 + u * bd;
+            if (p >= ns) break;
+            float tot = tsm[p];
+            if (emis) tot = fmaf(esm[p], rn, tot);
+            if (igm && p < a.jtop) {
+                const float arg = (p < jmax) ? kcap
+                                             : v0[u].z * mp[MP_IGM_KB] + v0[u].w * mp[MP_IGM_KB + 1] + v1[u].x * mp[MP_IGM_KB + 2] +
+                                                   v1[u].y * mp[MP_IGM_KB + 3] + v1[u].z * mp[MP_IGM_KB + 4] + v1[u].w * mp[MP_IGM_KB + 5];
+                tot *= ops_ex2(arg);
             }
-            tot *= ops_ex2(arg);
+            if (agn) {
+                const float curve = a.uniform_index ? v0[u].y : ops_ex2(di * v0[u].x);
+                tot = fmaf(lagn * fmaf(dm.wta, g1[u] - g0[u], g0[u]), ops_ex2(kd2 * curve), tot);
+            }
+            tsm[p] = tot;
         }
-        if (agn) {
-            // the torus template between the two bracketing optical depths, through the diffuse dust
-            const float4 v0 = reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)[0];
-            const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
-            const float t0 = __ldg(a.agn_spec + (size_t)dm.ita * ns + p), t1 = __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p);
-            tot = fmaf(lagn * fmaf(dm.wta, t1 - t0, t0), ops_ex2(kd2 * curve), tot);
-        }
-        tsm[p] = tot;
     }
     __syncthreads();
     const int R = __float_as_int(mp[MP_SMOOTH_R]);
@@ -869,7 +933,7 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
 #pragma unroll
     for (int d = 0; d < 9; ++d) tap[d] = mp[MP_TAPS + d];
     float *out = a.spec + (size_t)m * ns;
-    for (int p = threadIdx.x; p < ns; p += blockDim.x) {
+    for (int p = threadIdx.x; p < ns; p += bd) {
         float v = tsm[p];
         if (R >= 0 && p >= a.sm_lo && p <= a.sm_hi) {
             float s = 0.f;
