@@ -788,14 +788,15 @@ __device__ __forceinline__ float2 dl07_shape2(const float *tab, int ns, int nq, 
     return make_float2(fmaxf((1.f - d.gam) * lx + d.gam * hx, FLT_MIN), fmaxf((1.f - d.gam) * ly + d.gam * hy, FLT_MIN));
 }
 
-// One CTA per model, three passes over its pixels (the spectrum in shared memory): the attenuated sum (with dust
-// emission also the escaping template and the frequency-trapezoid sums of the absorbed and escaping light, reduced
-// over the block), then the emission, the IGM and the AGN, then the smoothing. Each thread issues the global loads of
-// EPI_U pixel pairs (young and old sums, templates) before it uses them: one pair at a time left the kernel waiting on
-// memory latency at a fraction of the HBM rate.
+// One CTA per model, two passes over its pixels (the spectrum in shared memory). Pass 1 reads everything from global
+// memory: the attenuated sum through the IGM with the AGN added (the AGN does not depend on the energy balance), and
+// with dust emission the escaping template through the IGM and the frequency-trapezoid sums of the absorbed and
+// escaping light (before the IGM), reduced over the block; the emission scaled by their ratio then joins the
+// spectrum. Pass 2 smooths from shared memory. Each thread issues the young and old loads of EPI_U pixel pairs before
+// it uses them.
 constexpr int EPI_U = 4;
 
-__global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a) {
+__global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArgs a) {
     extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
     float *esm = tsm + a.nspec;
     __shared__ float red[2][8];
@@ -804,8 +805,9 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
     const float kd2 = mp[MP_KD2], one_m_fnd = mp[MP_ONE_M_FND], fnd = mp[MP_FND], di = mp[MP_DUST_INDEX];
     const float kd1 = mp[MP_KD1], d1i = mp[MP_DUST1_INDEX], one_m_fo = mp[MP_ONE_M_FO], fo = mp[MP_FO];
-    const float kd3 = mp[MP_KD3], igm_on = mp[MP_IGM_ON], kcap = mp[MP_IGM_KCAP];
+    const float kd3 = mp[MP_KD3], kcap = mp[MP_IGM_KCAP];
     const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
+    const int igm_top = mp[MP_IGM_ON] != 0.f ? a.jtop : 0;     // pixels below carry the IGM
     DustEmModel dm;
     if (a.dem) dm = a.dem[m];
     const bool emis = a.dem != nullptr && dm.on != 0;
@@ -819,9 +821,13 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     }
     constexpr float LN2 = 0.6931471805599453f;
     float sa = 0.f, se = 0.f;
-    auto pix0 = [&](int p) { return __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS)); };
-    // pass 1 at one pixel: the attenuated young + old sum; with emission the escaping template (esc) and the sums
-    auto pass1 = [&](const float4 v0, float y, float o, float shape, float cn, float &esc) -> float {
+    // (ln lambda log2 e, the shared diffuse curve) of a pixel
+    auto pix0 = [&](int p) { return __ldg(reinterpret_cast<const float2 *>(a.pix + (size_t)p * PIX_FLOATS)); };
+    // pass 1 at pixel p: the attenuated young + old sum through the IGM plus the AGN (the torus template between the
+    // two bracketing optical depths, through the diffuse dust); with emission the escaping template through the IGM
+    // (esc) and the sums
+    auto pass1 = [&](int p, float y, float o, float shape, float cn, float t0, float t1, float &esc) -> float {
+        const float2 v0 = pix0(p);
         const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
         const float lb = (kd1 != 0.f) ? kd1 * ops_ex2(d1i * v0.x) : 0.f;   // log2 of the transmissions
         const float lo2 = kd3 * curve, ld2 = kd2 * curve;
@@ -829,23 +835,40 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
         const float to = (kd3 != 0.f) ? ops_ex2(lo2) : 1.f;
         const float td = ops_ex2(ld2);
         const float ss = (y * tb * one_m_fo + y * fo) + o * to;
+        float g = 1.f;
+        if (p < igm_top) {
+            float arg = kcap;
+            if (p >= jmax) {
+                const float2 va = __ldg(reinterpret_cast<const float2 *>(a.pix + (size_t)p * PIX_FLOATS + PIX_IGM_A));
+                const float4 vb = __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS + PIX_IGM_A + 2));
+                arg = va.x * mp[MP_IGM_KB] + va.y * mp[MP_IGM_KB + 1] + vb.x * mp[MP_IGM_KB + 2] + vb.y * mp[MP_IGM_KB + 3] +
+                      vb.z * mp[MP_IGM_KB + 4] + vb.w * mp[MP_IGM_KB + 5];
+            }
+            g = ops_ex2(arg);
+        }
         if (emis) {
             // 1 - T of each screen from its exponent (no cancellation at small optical depth)
-            const float omb = (kd1 != 0.f) ? -expm1f(lb * LN2) : 0.f;
-            const float omo = (kd3 != 0.f) ? -expm1f(lo2 * LN2) : 0.f;
-            const float omd = one_m_fnd * -expm1f(ld2 * LN2);
+            const float omb = (kd1 != 0.f) ? -ops_expm1(lb * LN2) : 0.f;
+            const float omo = (kd3 != 0.f) ? -ops_expm1(lo2 * LN2) : 0.f;
+            const float omd = one_m_fnd * -ops_expm1(ld2 * LN2);
             const float ay = tb * one_m_fo + fo;
             const float absorbed = y * (one_m_fo * omb + ay * omd) + o * (omo + to * omd);
-            esc = shape * td;
+            const float e = shape * td;
             sa = fmaf(cn, absorbed, sa);
-            se = fmaf(cn, esc, se);
+            se = fmaf(cn, e, se);
+            esc = e * g;
         }
-        return ss * fmaf(td, one_m_fnd, fnd);
+        float tot = ss * fmaf(td, one_m_fnd, fnd) * g;
+        if (agn) tot = fmaf(lagn * fmaf(dm.wta, t1 - t0, t0), td, tot);
+        return tot;
     };
     const int bd = (int)blockDim.x;
-    if ((ns & 1) == 0) {
+    const bool pairs = (ns & 1) == 0;
+    if (pairs) {
         const int np2 = ns >> 1;
         const float2 *y2 = reinterpret_cast<const float2 *>(yv), *o2 = reinterpret_cast<const float2 *>(ov);
+        const float2 *ga = reinterpret_cast<const float2 *>(a.agn_spec + (size_t)dm.ita * ns);
+        const float2 *gb = reinterpret_cast<const float2 *>(a.agn_spec + (size_t)(dm.ita + 1) * ns);
         for (int q0 = threadIdx.x; q0 < np2; q0 += EPI_U * bd) {
             float2 yy[EPI_U], oo[EPI_U];
 #pragma unroll
@@ -858,14 +881,18 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
             for (int u = 0; u < EPI_U; ++u) {
                 const int q = q0 + u * bd;
                 if (q >= np2) break;
-                float2 sh = make_float2(0.f, 0.f), cn = make_float2(0.f, 0.f);
+                float2 sh = make_float2(0.f, 0.f), cn = make_float2(0.f, 0.f), g0 = make_float2(0.f, 0.f), g1 = g0;
                 if (emis) {
                     sh = dl07_shape2(a.dtab, ns, a.nqpah, 2 * q, dm);
                     cn = __ldg(reinterpret_cast<const float2 *>(a.cnu) + q);
                 }
+                if (agn) {
+                    g0 = __ldg(ga + q);
+                    g1 = __ldg(gb + q);
+                }
                 float e0 = 0.f, e1 = 0.f;
-                const float t0 = pass1(pix0(2 * q), yy[u].x, oo[u].x, sh.x, cn.x, e0);
-                const float t1 = pass1(pix0(2 * q + 1), yy[u].y, oo[u].y, sh.y, cn.y, e1);
+                const float t0 = pass1(2 * q, yy[u].x, oo[u].x, sh.x, cn.x, g0.x, g1.x, e0);
+                const float t1 = pass1(2 * q + 1, yy[u].y, oo[u].y, sh.y, cn.y, g0.y, g1.y, e1);
                 reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
                 if (emis) reinterpret_cast<float2 *>(esm)[q] = make_float2(e0, e1);
             }
@@ -873,12 +900,12 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
     } else {
         for (int p = threadIdx.x; p < ns; p += bd) {
             float esc = 0.f;
-            tsm[p] = pass1(pix0(p), __ldg(yv + p), __ldg(ov + p), emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
-                           emis ? __ldg(a.cnu + p) : 0.f, esc);
+            tsm[p] = pass1(p, __ldg(yv + p), __ldg(ov + p), emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
+                           emis ? __ldg(a.cnu + p) : 0.f, agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f,
+                           agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f, esc);
             if (emis) esm[p] = esc;
         }
     }
-    float rn = 0.f;
     if (emis) {
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
@@ -890,41 +917,15 @@ __global__ void __launch_bounds__(256) parts_epilogue_kernel(PartsEpilogueArgs a
         __syncthreads();
         float ta = 0.f, te = 0.f;
         for (int w = 0; w < (bd >> 5); ++w) { ta += red[0][w]; te += red[1][w]; }
-        rn = te > SAFE_FLOOR ? ta / te : 0.f;
-    }
-    __syncthreads();
-    // pass 2: the emission, the IGM, the AGN (the torus template between the two bracketing optical depths, through
-    // the diffuse dust); the global loads of EPI_U pixels first
-    const bool igm = igm_on != 0.f;
-    for (int p0 = threadIdx.x; p0 < ns; p0 += EPI_U * bd) {
-        float4 v0[EPI_U], v1[EPI_U];
-        float g0[EPI_U], g1[EPI_U];
-#pragma unroll
-        for (int u = 0; u < EPI_U; ++u) {
-            const int p = min(p0 + u * bd, ns - 1);
-            v0[u] = pix0(p);
-            v1[u] = (igm && p < a.jtop && p >= jmax) ? __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS) + 1)
-                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
-            g0[u] = agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f;
-            g1[u] = agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < EPI_U; ++u) {
-            const int p = p0 + u * bd;
-            if (p >= ns) break;
-            float tot = tsm[p];
-            if (emis) tot = fmaf(esm[p], rn, tot);
-            if (igm && p < a.jtop) {
-                const float arg = (p < jmax) ? kcap
-                                             : v0[u].z * mp[MP_IGM_KB] + v0[u].w * mp[MP_IGM_KB + 1] + v1[u].x * mp[MP_IGM_KB + 2] +
-                                                   v1[u].y * mp[MP_IGM_KB + 3] + v1[u].z * mp[MP_IGM_KB + 4] + v1[u].w * mp[MP_IGM_KB + 5];
-                tot *= ops_ex2(arg);
+        const float rn = te > SAFE_FLOOR ? ta / te : 0.f;
+        // the emission joins the spectrum (each thread its own pass-1 pixels)
+        if (pairs) {
+            for (int q = threadIdx.x; q < (ns >> 1); q += bd) {
+                const float2 t = reinterpret_cast<const float2 *>(tsm)[q], e = reinterpret_cast<const float2 *>(esm)[q];
+                reinterpret_cast<float2 *>(tsm)[q] = make_float2(fmaf(e.x, rn, t.x), fmaf(e.y, rn, t.y));
             }
-            if (agn) {
-                const float curve = a.uniform_index ? v0[u].y : ops_ex2(di * v0[u].x);
-                tot = fmaf(lagn * fmaf(dm.wta, g1[u] - g0[u], g0[u]), ops_ex2(kd2 * curve), tot);
-            }
-            tsm[p] = tot;
+        } else {
+            for (int p = threadIdx.x; p < ns; p += bd) tsm[p] = fmaf(esm[p], rn, tsm[p]);
         }
     }
     __syncthreads();
