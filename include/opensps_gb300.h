@@ -49,6 +49,18 @@ void opensps_gb300_ops_last_fold(int handle, int *interpolated, int *status);
  * were copied. */
 void opensps_gb300_last_input_in_place(int handle, int *in_place, int *status);
 
+/* A data library in OpenSPS's standard format (root/libraries/<kind>/<name>/manifest.json plus raw arrays), processed
+ * as opensps_context_setup processes it, without a device or a context (replaces nothing in opensps.h: the
+ * reference's readers run inside its setup, src/io/opensps_io.f90:991-1318,3131-3155). kind "ssp": log10 L_bol per
+ * grid point (nz x nt, the trapezoid integral of each SSP spectrum over frequency; lam unused); "dust_emission": the
+ * templates interpolated onto lam (2 numin x nqpah columns of nspec, column (2 u + c) nqpah + q); "agn_torus": the 9
+ * templates on lam (9 x nspec); "filters": the bands on lam normalised to int T / lambda = 1 and calibrated where
+ * the library says so (nb x nspec). name may
+ * carry axis selections ("name:axis=value"). *n_out receives the table's length; out may be NULL to query it.
+ * Status 4 with the message for a missing or malformed library. */
+void opensps_gb300_data_table(const char *root, const char *kind, const char *name, const double *lam, int nspec,
+                              double *out, long long out_cap, long long *n_out, int *status);
+
 /* Maximum n of opensps_gb300_spec_mags_noalloc. */
 #define OPENSPS_GB300_NOALLOC_MAX_MODELS 65536
 

@@ -74,6 +74,8 @@ SIGNATURES = {
     "opensps_gb300_last_launches": (None, [C.c_int, _ip, _ip]),
     "opensps_gb300_ops_last_fold": (None, [C.c_int, _ip, _ip]),
     "opensps_gb300_last_input_in_place": (None, [C.c_int, _ip, _ip]),
+    "opensps_gb300_data_table": (None, [C.c_char_p, C.c_char_p, C.c_char_p, _dp, C.c_int, _dp, C.c_longlong,
+                                        C.POINTER(C.c_longlong), _ip]),
     "opensps_gb300_spec_mags_noalloc": (None, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _ip]),
     "opensps_gb300_set_profiling": (None, [C.c_int, C.c_int, _ip]),
     "opensps_gb300_kernel_times": (None, [C.c_int, _dp, C.c_int, _ip, _ip]),
@@ -157,6 +159,23 @@ def _names_values(params: dict[str, np.ndarray], n: int):
     c_names = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
     c_vals = (_dp * max(1, len(names)))(*[a.ctypes.data_as(_dp) for a in arrs])
     return len(names), c_names, c_vals, arrs
+
+
+def data_table(root: str | os.PathLike, kind: str, name: str, lam: np.ndarray | None = None) -> np.ndarray:
+    """opensps_gb300_data_table: a standard-format library processed as the context's setup processes it (host only).
+    ssp: log L_bol (nz nt,); dust_emission: (2 numin nqpah, nspec) in column order (2 u + c) nqpah + q; agn_torus:
+    (9, nspec); filters: (nb, nspec)."""
+    lib = load_library()
+    g = np.ascontiguousarray(lam if lam is not None else np.zeros(0), dtype=np.float64)
+    gp = g.ctypes.data_as(_dp) if g.size else None
+    n, st = C.c_longlong(0), C.c_int(0)
+    args = (str(root).encode(), kind.encode(), name.encode(), gp, int(g.size))
+    lib.opensps_gb300_data_table(*args, None, 0, C.byref(n), C.byref(st))
+    _check(st, lib)
+    out = np.empty(n.value)
+    lib.opensps_gb300_data_table(*args, out.ctypes.data_as(_dp), n.value, C.byref(n), C.byref(st))
+    _check(st, lib)
+    return out if kind == "ssp" else out.reshape(-1, g.size)
 
 
 class Context:

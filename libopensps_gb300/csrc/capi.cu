@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 #include "context.h"
+#include "datalib.h"
 #include "../../include/opensps.h"
 #include "../../include/opensps_gb300.h"
 
@@ -614,6 +615,44 @@ void opensps_gb300_last_input_in_place(int handle, int *in_place, int *status) {
     Context *c = lookup(handle);
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
     if (in_place) *in_place = c->last_direct ? 1 : 0;
+    if (status) *status = 0;
+}
+
+// A standard-format library of the kinds this path reads, processed as the context's setup processes it (host only;
+// no device or context needed): "ssp" -> log L_bol per grid point (nz x nt; lam unused), "dust_emission" -> the
+// templates on lam (2 numin x nqpah columns of nspec), "agn_torus" -> ntau x nspec, "filters" -> nb x nspec bands.
+void opensps_gb300_data_table(const char *root, const char *kind, const char *name, const double *lam, int nspec,
+                              double *out, long long out_cap, long long *n_out, int *status) {
+    if (!root || !kind || !name) return fail(status, ST_BAD_ARG, "NULL argument");
+    const std::string k(kind);
+    std::vector<double> grid;
+    if (k != "ssp") {
+        if (!lam || nspec < 2) return fail(status, ST_BAD_ARG, "a wavelength grid of at least 2 points is required");
+        grid.assign(lam, lam + nspec);
+    }
+    std::string err;
+    std::vector<double> tab, a, b;
+    std::vector<std::string> names;
+    int rc = 0;
+    if (k == "ssp") {
+        SspLibrary L;
+        rc = std_load_ssp(root, name, L, err);
+        tab.swap(L.lbol);
+    } else if (k == "dust_emission") {
+        rc = std_load_dust_emission(root, name, grid, a, b, tab, err);
+    } else if (k == "agn_torus") {
+        rc = std_load_agn(root, grid, a, tab, err);
+    } else if (k == "filters") {
+        rc = std_load_filters(root, name, grid, tab, a, names, err);
+    } else {
+        return fail(status, ST_BAD_ARG, "kind must be ssp, dust_emission, agn_torus or filters");
+    }
+    if (rc) return fail(status, rc, err);
+    if (n_out) *n_out = (long long)tab.size();
+    if (out) {
+        if (out_cap < (long long)tab.size()) return fail(status, ST_BAD_ARG, "output buffer too small");
+        std::copy(tab.begin(), tab.end(), out);
+    }
     if (status) *status = 0;
 }
 

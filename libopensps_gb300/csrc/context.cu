@@ -8,6 +8,7 @@
 #include <iterator>
 #include <sstream>
 #include "context.h"
+#include "datalib.h"
 
 namespace sps {
 
@@ -277,23 +278,35 @@ static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
 // prepare_batch_grid :262-265).
 int dustem_load(Context &c, std::string &err) {
     if (c.dustem.ready) return 0;
-    const std::string dir = data_root() + "/dust_dl07/";
-    std::ifstream mf(dir + "manifest.json");
-    if (!mf) { err = "dust emission data missing under " + dir; return ST_DATA_MISSING; }
-    const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
-    long long nq = 0, nu = 0, ns = 0;
-    if (!manifest_int(text, "nqpah", nq) || !manifest_int(text, "numin", nu) || !manifest_int(text, "nspec", ns) ||
-        ns != c.nspec || nq < 2 || nu < 2) {
-        err = "dust emission data under " + dir + " does not match the context's grid";
-        return ST_DATA_MISSING;
-    }
     DustEmission &d = c.dustem;
-    std::vector<float> tab((size_t)ns * nq * 2 * nu);
-    std::ifstream tf(dir + "dustem.f32", std::ios::binary);
-    if (!read_f64(dir + "qpah.f64", d.qpah, (size_t)nq) || !read_f64(dir + "umin.f64", d.umin, (size_t)nu) || !tf ||
-        !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
-        err = "dust emission data under " + dir + " is incomplete";
-        return ST_DATA_MISSING;
+    const std::string root = data_root();
+    long long nq = 0, nu = 0, ns = c.nspec;
+    std::vector<float> tab;
+    if (datalib_available(root, "dust_emission", c.dust_emission_lib)) {
+        // the standard format's dust_emission/<name> library, interpolated onto the grid
+        std::vector<double> t64;
+        if (int rc = std_load_dust_emission(root, c.dust_emission_lib, c.lam, d.qpah, d.umin, t64, err)) return rc;
+        nq = (long long)d.qpah.size();
+        nu = (long long)d.umin.size();
+        tab.assign(t64.begin(), t64.end());
+    } else {
+        const std::string dir = root + "/dust_dl07/";
+        std::ifstream mf(dir + "manifest.json");
+        if (!mf) { err = "dust emission data missing under " + dir; return ST_DATA_MISSING; }
+        const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
+        long long nsf = 0;
+        if (!manifest_int(text, "nqpah", nq) || !manifest_int(text, "numin", nu) || !manifest_int(text, "nspec", nsf) ||
+            nsf != c.nspec || nq < 2 || nu < 2) {
+            err = "dust emission data under " + dir + " does not match the context's grid";
+            return ST_DATA_MISSING;
+        }
+        tab.resize((size_t)ns * nq * 2 * nu);
+        std::ifstream tf(dir + "dustem.f32", std::ios::binary);
+        if (!read_f64(dir + "qpah.f64", d.qpah, (size_t)nq) || !read_f64(dir + "umin.f64", d.umin, (size_t)nu) || !tf ||
+            !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
+            err = "dust emission data under " + dir + " is incomplete";
+            return ST_DATA_MISSING;
+        }
     }
     std::vector<float> cnu((size_t)ns, 0.f);
     for (int i = 0; i + 1 < ns; ++i) {
@@ -319,22 +332,31 @@ int dustem_load(Context &c, std::string &err) {
 // here the synthetic stand-in), on the context's wavelength grid.
 int agn_load(Context &c, std::string &err) {
     if (c.agn.ready) return 0;
-    const std::string dir = data_root() + "/agn_torus/";
-    std::ifstream mf(dir + "manifest.json");
-    if (!mf) { err = "AGN torus data missing under " + dir; return ST_DATA_MISSING; }
-    const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
-    long long ntau = 0, ns = 0;
-    if (!manifest_int(text, "ntau", ntau) || !manifest_int(text, "nspec", ns) || ns != c.nspec || ntau < 2) {
-        err = "AGN torus data under " + dir + " does not match the context's grid";
-        return ST_DATA_MISSING;
-    }
     AgnTorus &a = c.agn;
-    std::vector<float> tab((size_t)ntau * ns);
-    std::ifstream tf(dir + "agnspec.f32", std::ios::binary);
-    if (!read_f64(dir + "tau.f64", a.tau, (size_t)ntau) || !tf ||
-        !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
-        err = "AGN torus data under " + dir + " is incomplete";
-        return ST_DATA_MISSING;
+    const std::string root = data_root();
+    std::vector<float> tab;
+    if (datalib_available(root, "agn_torus", "clumpy")) {
+        // the standard format's agn_torus/clumpy library, interpolated onto the grid
+        std::vector<double> t64;
+        if (int rc = std_load_agn(root, c.lam, a.tau, t64, err)) return rc;
+        tab.assign(t64.begin(), t64.end());
+    } else {
+        const std::string dir = root + "/agn_torus/";
+        std::ifstream mf(dir + "manifest.json");
+        if (!mf) { err = "AGN torus data missing under " + dir; return ST_DATA_MISSING; }
+        const std::string text((std::istreambuf_iterator<char>(mf)), std::istreambuf_iterator<char>());
+        long long ntau = 0, ns = 0;
+        if (!manifest_int(text, "ntau", ntau) || !manifest_int(text, "nspec", ns) || ns != c.nspec || ntau < 2) {
+            err = "AGN torus data under " + dir + " does not match the context's grid";
+            return ST_DATA_MISSING;
+        }
+        tab.resize((size_t)ntau * ns);
+        std::ifstream tf(dir + "agnspec.f32", std::ios::binary);
+        if (!read_f64(dir + "tau.f64", a.tau, (size_t)ntau) || !tf ||
+            !tf.read(reinterpret_cast<char *>(tab.data()), (std::streamsize)(sizeof(float) * tab.size()))) {
+            err = "AGN torus data under " + dir + " is incomplete";
+            return ST_DATA_MISSING;
+        }
     }
     cudaError_t e;
     if ((e = a.spec.reserve(tab.size())) != cudaSuccess ||
@@ -349,15 +371,24 @@ int agn_load(Context &c, std::string &err) {
 
 int context_load_filters(Context &c, const std::string &name, std::string &err) {
     int nb = 0;
-    if (name == "gauss20") nb = 20;
-    else if (name == "gauss40") nb = 40;
-    else { err = "unknown filter library " + name; return 324; }
-    const std::string dir = data_root() + "/synthetic/";
     std::vector<double> bands, centers;
-    if (!read_f64(dir + "filters_" + std::to_string(nb) + ".f64", bands, (size_t)nb * c.nspec) ||
-        !read_f64(dir + "filters_" + std::to_string(nb) + "_center.f64", centers, nb)) {
-        err = "filter library " + name + " missing under " + dir;
-        return 324;
+    const std::string root = data_root();
+    if (datalib_available(root, "filters", name)) {
+        // the standard format's filters/<name> library: curves resampled onto the grid, pivot wavelengths
+        std::vector<std::string> names;
+        if (int rc = std_load_filters(root, name, c.lam, bands, centers, names, err)) return rc;
+        nb = (int)centers.size();
+        if (nb < 1) { err = "filter library " + name + " has no filters"; return 324; }
+    } else {
+        if (name == "gauss20") nb = 20;
+        else if (name == "gauss40") nb = 40;
+        else { err = "unknown filter library " + name; return 324; }
+        const std::string dir = root + "/synthetic/";
+        if (!read_f64(dir + "filters_" + std::to_string(nb) + ".f64", bands, (size_t)nb * c.nspec) ||
+            !read_f64(dir + "filters_" + std::to_string(nb) + "_center.f64", centers, nb)) {
+            err = "filter library " + name + " missing under " + dir;
+            return 324;
+        }
     }
     c.bands.swap(bands);
     c.band_center.swap(centers);
@@ -454,15 +485,34 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
 }
 
 int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err) {
-    (void)dust;
-    const std::string iso = isoc ? isoc : "", sp = spec ? spec : "";
-    if (!(iso.empty() || iso == "synthetic") || !(sp.empty() || sp == "synthetic")) {
-        err = "only the synthetic libraries of the data root are available (isoc_type / spec_type \"synthetic\")";
-        return ST_DATA_MISSING;
-    }
+    const std::string iso = isoc && *isoc ? isoc : "synthetic", sp = spec ? spec : "";
     const std::string root = data_root();
     if (root.empty()) {
         err = "OPENSPS_DATA_HOME is not set";
+        return ST_DATA_MISSING;
+    }
+    if (data_format_from_env() == DF_BAD) {
+        err = "OPENSPS_DATA_FORMAT must be legacy, standard or auto";
+        return ST_BAD_ARG;
+    }
+    // the dust emission library of the batches' add_dust_emission (DL07 unless named)
+    const std::string dn = dust ? dust : "";
+    c.dust_emission_lib = (dn == "DL07" || dn == "THEMIS") ? dn : "DL07";
+    c.dustem.release();
+    c.agn.release();
+    if (datalib_available(root, "ssp", iso)) {
+        // an SSP library in the standard format (kind ssp, the isochrone name: read_bpass_standard); its spectra
+        // are the basis, so spec_type is not read
+        SspLibrary L;
+        if (int rc = std_load_ssp(root, iso, L, err)) return rc;
+        c.nspec = L.nspec; c.nt = L.nt; c.nz = L.nz; c.nline = L.nline; c.zsol = L.zsol;
+        c.lam.swap(L.lam); c.log_age.swap(L.log_age); c.zlegend.swap(L.zlegend); c.ssp.swap(L.spec);
+        c.mass.swap(L.mass); c.lbol.swap(L.lbol); c.line_lambda.swap(L.line_lambda); c.line_lum.swap(L.line_lum);
+        return context_setup_grid(c, err);
+    }
+    if (iso != "synthetic" || !(sp.empty() || sp == "synthetic")) {
+        err = "library ssp/" + iso + " not found under " + root +
+              "/libraries (standard format) and only the synthetic library is in the package's own layout";
         return ST_DATA_MISSING;
     }
     const std::string dir = root + "/synthetic/";
@@ -490,6 +540,12 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
         err = "missing or short array under " + dir;
         return ST_DATA_MISSING;
     }
+    return context_setup_grid(c, err);
+}
+
+// The rest of the setup from the loaded basis (grid checks, device tables, filters).
+int context_setup_grid(Context &c, std::string &err) {
+    const int ns = c.nspec;
     c.llin.resize(c.lbol.size());
     for (size_t i = 0; i < c.lbol.size(); ++i) c.llin[i] = std::pow(10.0, c.lbol[i]);
     // the observed-frame resampling and the smoothing taps take the grid as log-uniform: check it

@@ -156,6 +156,7 @@ struct Context {
     double h0 = 72.0, om0 = 0.27, ol0 = 0.73;
     double pdef[PF_COUNT];
     std::string filter_set = "gauss40";
+    std::string dust_emission_lib = "DL07";   // dust_emission/<name> of a standard-format data root
     std::vector<int> mag_mask;   // empty: all bands
 
     // libraries (host, FP64)
@@ -256,6 +257,7 @@ enum { ST_OK = 0, ST_BAD_HANDLE = 1, ST_UNSUPPORTED = 2, ST_BAD_ARG = 3, ST_DATA
 
 void set_error(int status, const std::string &msg);
 int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err);
+int context_setup_grid(Context &c, std::string &err);
 int context_load_filters(Context &c, const std::string &name, std::string &err);
 std::string data_root();
 
