@@ -426,8 +426,10 @@ def dust_emission_measure(ctx, params, h_wz, args, barrier) -> dict | None:
     synth_dust.generate()
     synth_dust.generate_agn()
     rng = np.random.default_rng(77)
+    # (frac_obrun stays 0 as in the headline batch: above 0, with nebular emission, the escaping ionizing light of
+    # the nebular ages takes the per-model epilogue path of its own)
     p = dict(params, dust1=rng.uniform(0.1, 1.0, n), dust3=rng.uniform(0.0, 0.4, n),
-             frac_obrun=rng.uniform(0.0, 0.3, n), duste_qpah=rng.uniform(0.5, 4.5, n),
+             duste_qpah=rng.uniform(0.5, 4.5, n),
              duste_umin=rng.uniform(0.1, 25.0, n), duste_gamma=rng.uniform(0.0, 0.5, n),
              fagn=rng.uniform(0.0, 1.0, n), agn_tau=rng.uniform(5.0, 150.0, n))
     ctx.set_int("add_dust_emission", 1)

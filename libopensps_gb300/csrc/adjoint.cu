@@ -555,6 +555,59 @@ __global__ void wzbar_kernel(WzbArgs a) {
     a.wzb[i] = v;
 }
 
+// The reverse of nebular emission's escaping ionizing light (the forward adds fesc sum_k w_k ion_k(p) to the young
+// or old sums at the ionizing pixels p, fesc = clamp(frac_obrun, 0, 1)): per model and nebular (age, metallicity) k
+// the sum s_k = sum_p ybar(p) ion_k(p) (obar for the old ages), one warp per k; the weights' cotangent gains
+// fesc s_k and the frac_obrun row sum_k w_k s_k (where 0 < frac_obrun < 1).
+struct IonRevArgs {
+    int whl, ntneb, nt, nz, itesc, ppad, ntz;
+    const float *ion;
+    const double *wz, *par, *cscale;
+    const __nv_bfloat16 *ybh, *ybl, *obh, *obl;
+    double *wzbar;         // n x ntz (source order t + nt z), or null
+    double *params_bar;    // n x NBGRAD
+};
+
+__global__ void __launch_bounds__(256) ion_rev_kernel(IonRevArgs a) {
+    extern __shared__ float sb[];          // the ionizing pixels' young then old cotangents (scaled by 1 / cscale)
+    __shared__ double red[8];
+    const int m = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const double fo = a.par[(size_t)PAR_DEVICE * m + PF_FRAC_OBRUN];
+    const double fesc = fmin(fmax(fo, 0.0), 1.0);
+    const bool dfo = fo > 0.0 && fo < 1.0;
+    if (fesc <= 0.0 && !dfo) return;
+    const __nv_bfloat16 *yh = a.ybh + (size_t)m * a.ppad, *yl = a.ybl + (size_t)m * a.ppad;
+    const __nv_bfloat16 *oh = a.obh + (size_t)m * a.ppad, *ol = a.obl + (size_t)m * a.ppad;
+    for (int p = tid; p < a.whl; p += blockDim.x) {
+        sb[p] = __bfloat162float(yh[p]) + __bfloat162float(yl[p]);
+        sb[a.whl + p] = __bfloat162float(oh[p]) + __bfloat162float(ol[p]);
+    }
+    __syncthreads();
+    const double cs = a.cscale[m];
+    double part = 0.0;
+    for (int k = warp; k < a.nz * a.ntneb; k += (int)(blockDim.x >> 5)) {
+        const int z = k / a.ntneb, t = k - z * a.ntneb;
+        const float *ik = a.ion + (size_t)k * a.whl, *bar = sb + (t < a.itesc ? 0 : a.whl);
+        float s = 0.f;
+        for (int p = lane; p < a.whl; p += 32) s = fmaf(bar[p], __ldg(ik + p), s);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) {
+            const double sk = (double)s * cs;
+            if (a.wzbar) a.wzbar[(size_t)m * a.ntz + t + (size_t)a.nt * z] += fesc * sk;
+            const double w = a.wz[(size_t)m * a.nz * a.nt + (size_t)z * a.nt + t];
+            if (w > SAFE_FLOOR) part += w * sk;
+        }
+    }
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (tid == 0 && dfo) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+        a.params_bar[(size_t)m * NBGRAD + R_FRAC_OBRUN] += v;
+    }
+}
+
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st) {
     if (a.n_models <= 0) return cudaSuccess;
     adjoint_prep_kernel<<<(pa.n_models + 255) / 256, 256, 0, st>>>(pa);
@@ -793,11 +846,29 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         if ((e = cudaGetLastError()) != cudaSuccess) { err = msg("weights cotangent kernel", e); return ST_DATA_MISSING; }
         prof_mark(c, 9);
         ++launches;
-        if (weights_z_bar &&
-            (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * tot, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
-            err = msg("weights cotangent copy", e);
+    }
+    // ---- nebular emission's escaping ionizing light (the forward added it at the ionizing pixels)
+    if (c.last_ion && !ops) {
+        IonRevArgs ia;
+        ia.whl = c.whlylim; ia.ntneb = c.nt_neb; ia.nt = c.nt; ia.nz = c.nz; ia.itesc = bop->itesc;
+        ia.ppad = (ns + gemm_bk() - 1) / gemm_bk() * gemm_bk(); ia.ntz = ntz;
+        ia.ion = c.d_ion.p; ia.wz = c.d_wz.p; ia.par = c.d_params.p; ia.cscale = c.d_cscale.p;
+        ia.ybh = c.d_ybh.p; ia.ybl = c.d_ybl.p; ia.obh = c.d_obh.p; ia.obl = c.d_obl.p;
+        ia.wzbar = (weights_z_bar || sfh_rev) ? c.d_wzbar.p : nullptr;
+        ia.params_bar = c.d_pbar.p;
+        const size_t smem = sizeof(float) * 2 * (size_t)c.whlylim;
+        if ((e = cudaFuncSetAttribute(ion_rev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) {
+            err = msg("ionizing light reverse kernel", e);
             return ST_DATA_MISSING;
         }
+        ion_rev_kernel<<<n, 256, smem, s>>>(ia);
+        if ((e = cudaGetLastError()) != cudaSuccess) { err = msg("ionizing light reverse kernel", e); return ST_DATA_MISSING; }
+        ++launches;
+    }
+    if (!ops && weights_z_bar &&
+        (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * (size_t)n * ntz, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+        err = msg("weights cotangent copy", e);
+        return ST_DATA_MISSING;
     }
     // ---- weights formed on the device: the cotangent of the weights over ages, logzsol's row and the SFH rows
     if (sfh_rev) {

@@ -242,6 +242,14 @@ void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<
                     for (int j = jlo; j <= jhi; ++j) col[j] += prof[j] * L;
                 }
         }
+        // the gas absorbs the nebular ages' ionizing light (nebular_kernels step 2, opensps_csp_batch.f90:2726-2750:
+        // the age sums at pixels 1..whlylim with the nebular ages times the escaping fraction; that fraction's share
+        // is added per model by the epilogue when frac_obrun > 0)
+        for (int z = 0; z < nz; ++z)
+            for (int t = 0; t < c.nt_neb; ++t) {
+                double *col = b.data() + (size_t)ns * (t + (size_t)nt * z);
+                for (int i = 0; i < c.whlylim && i < ns; ++i) col[i] = 0.0;
+            }
     }
 }
 
@@ -363,11 +371,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // the AGN torus (add_agn_dust, for models with fagn above SAFE_FLOOR: agn_indices :1575-1589), in the same epilogue
     if (c.add_agn_dust == 1)
         for (int m = 0; m < n && !any_agn; ++m) any_agn = par(m, PF_FAGN) > SAFE_FLOOR;
+    // nebular emission's escaping ionizing light (frac_obrun above zero: nebular_kernels step 2,
+    // opensps_csp_batch.f90:2726-2750, the basis holding the absorbed case), added per model by the epilogue from the
+    // weights on the device
+    bool ion_terms = false;
+    if (c.add_neb_emission == 1 && c.nebemlineinspec == 1 && c.nline > 0 && c.nt_neb > 0 && c.whlylim > 0 && c.d_ion.p)
+        for (int m = 0; m < n && !ion_terms; ++m) ion_terms = par(m, PF_FRAC_OBRUN) > 0.0;
     const bool epi_terms = any_emis || any_agn;
+    const bool epi = epi_terms || ion_terms;         // spectra from the per-model epilogue
     const bool parts_kept = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;   // the caller wants the parts
-    const bool parts = parts_kept || epi_terms;
+    const bool parts = parts_kept || epi;
     const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts_kept &&
-                         n >= 2 * CHUNK;
+                         !ion_terms && n >= 2 * CHUNK;
     // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
     // more on the small chunk than its shorter copy saves)
     const int nch = chunked ? (n + CHUNK - 1) / CHUNK : 1;
@@ -444,7 +459,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         }
         const double d1 = par(m, PF_DUST1), fo = par(m, PF_FRAC_OBRUN), d3 = par(m, PF_DUST3);
         if ((d1 > SAFE_FLOOR && 1.0 - fo > SAFE_FLOOR) || std::fabs(d3) > SAFE_FLOOR) nacc2 = true;
-        if (io.young || io.old || io.keep_parts || epi_terms) nacc2 = true;   // the parts need the young and old sums apart
+        if (io.young || io.old || io.keep_parts || epi) nacc2 = true;   // the parts need the young and old sums apart
         const double sig = par(m, PF_SIGMA_SMOOTH);
         if (sig > SAFE_FLOOR) {
             any_smooth = true;
@@ -500,6 +515,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         err = "the plain FP64 path computes host-input batches' outputs only (no parts, device inputs or gradients)";
         return ST_UNSUPPORTED;
     }
+    if (ion_terms && (c.fp64 != 0 || io.dev_inputs)) {
+        err = "nebular emission with frac_obrun above zero is supported by the mixed batch from host inputs only";
+        return ST_UNSUPPORTED;
+    }
+    c.last_ion = ion_terms;
     DustEmModel *dem = nullptr;            // the per-model cells, page-locked (uploaded beside the parameter table)
     if (epi_terms) {
         if (fp64) { err = "dust emission and AGN are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
@@ -751,6 +771,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // (models [off, off + nk))
     auto epilogue = [&](const float *y, const float *o, int off, int nk) -> cudaError_t {
         PartsEpilogueArgs pe;
+        if (ion_terms) {
+            pe.ion = c.d_ion.p; pe.wz = d_wz + (size_t)nt * nz * off; pe.whl = c.whlylim; pe.ntneb = c.nt_neb;
+            pe.nt = nt; pe.nz = nz; pe.itesc = itesc;
+            pe.ion_young = const_cast<float *>(y) + (size_t)ns * off;
+            pe.ion_old = const_cast<float *>(o) + (size_t)ns * off;
+        }
         pe.n = nk; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
         pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
         pe.young = y + (size_t)ns * off; pe.old = o + (size_t)ns * off;
@@ -806,7 +832,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
             ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
             // (with dust emission or AGN the per-model epilogue forms the spectra from the young and old sums)
-            ca.spec = epi_terms ? nullptr : c.d_spec.p + (size_t)ns * off;
+            ca.spec = epi ? nullptr : c.d_spec.p + (size_t)ns * off;
             ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
             ca.young = ca.old = nullptr;
             if (parts) {
@@ -817,7 +843,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if ((e = run_contract(nacc, pl, ca, st)) != cudaSuccess) { err = cuda_msg("contraction kernel", e); return ST_DATA_MISSING; }
             if (marks) prof_mark(c, 3);
             launches += 3;
-            if (epi_terms) {
+            if (epi) {
                 if ((e = epilogue(d_y, d_o, off, nk)) != cudaSuccess) { err = cuda_msg("epilogue kernel", e); return ST_DATA_MISSING; }
                 ++launches;
                 if (marks) prof_mark(c, 4);
@@ -838,7 +864,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                     }
                 }
             }
-            if (marks && !epi_terms) prof_mark(c, 4);
+            if (marks && !epi) prof_mark(c, 4);
             return 0;
         };
         if (parts) {

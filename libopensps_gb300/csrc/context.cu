@@ -168,7 +168,7 @@ Context::~Context() {
         kv.second->release();
         delete kv.second;
     }
-    d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
+    d_ion.release(); d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
     d_lam.release(); d_lnlam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
@@ -546,6 +546,15 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
 // The rest of the setup from the loaded basis (grid checks, device tables, filters).
 int context_setup_grid(Context &c, std::string &err) {
     const int ns = c.nspec;
+    // the nebular ranges: whlylim = find_interval(lambda, 912 A) (opensps_initialization.f90:866), and the ages with
+    // nebular emission (the nebular grid's age range, opensps_csp_batch.f90:1644-1645: here the ages up to the last
+    // one with line luminosity)
+    c.whlylim = std::max(find_interval0(c.lam.data(), ns, 912.0) + 1, 0);
+    c.nt_neb = 0;
+    for (int z = 0; z < c.nz; ++z)
+        for (int t = 0; t < c.nt; ++t)
+            for (int l = 0; l < c.nline; ++l)
+                if (c.line_lum[l + (size_t)c.nline * (t + (size_t)c.nt * z)] != 0.0) c.nt_neb = std::max(c.nt_neb, t + 1);
     c.llin.resize(c.lbol.size());
     for (size_t i = 0; i < c.lbol.size(); ++i) c.llin[i] = std::pow(10.0, c.lbol[i]);
     // the observed-frame resampling and the smoothing taps take the grid as log-uniform: check it
@@ -616,6 +625,20 @@ int context_setup_grid(Context &c, std::string &err) {
         (e = c.d_status.reserve(4)) != cudaSuccess) {
         err = std::string("device upload failed: ") + cudaGetErrorString(e);
         return ST_DATA_MISSING;
+    }
+    // the nebular ages' ionizing pixels (their escaping fraction is added per model when frac_obrun > 0)
+    c.d_ion.release();
+    if (c.nt_neb > 0 && c.whlylim > 0) {
+        const int whl = c.whlylim, ntn = c.nt_neb;
+        std::vector<float> ion((size_t)c.nz * ntn * whl);
+        for (int z = 0; z < c.nz; ++z)
+            for (int t = 0; t < ntn; ++t)
+                for (int i = 0; i < whl; ++i)
+                    ion[((size_t)z * ntn + t) * whl + i] = (float)c.ssp[i + (size_t)ns * (t + (size_t)c.nt * z)];
+        if ((e = upload(c.d_ion, ion.data(), ion.size())) != cudaSuccess) {
+            err = std::string("device upload failed: ") + cudaGetErrorString(e);
+            return ST_DATA_MISSING;
+        }
     }
     c.d_pix.release();   // rebuilt by the next batch (smoothing range)
     c.pix_index = -1e300;

@@ -157,6 +157,11 @@ struct Context {
     double pdef[PF_COUNT];
     std::string filter_set = "gauss40";
     std::string dust_emission_lib = "DL07";   // dust_emission/<name> of a standard-format data root
+    // nebular emission's gas absorption: ages 0..nt_neb-1 carry nebular emission, pixels 0..whlylim-1 are ionizing
+    // (below 912 A); d_ion holds those ages' ionizing pixels of the library, (z nt_neb + t) x whlylim FP32
+    int nt_neb = 0, whlylim = 0;
+    DevBuf<float> d_ion;
+    bool last_ion = false;           // the last batch added the escaping ionizing light (its reverse pass follows)
     std::vector<int> mag_mask;   // empty: all bands
 
     // libraries (host, FP64)

@@ -317,6 +317,13 @@ struct PartsEpilogueArgs {
     const float *agn_spec = nullptr;
     const double *lsum = nullptr;
     int lsum_stride = 6;
+    // nebular emission's escaping ionizing light (ion null: none): clamp(frac_obrun, 0, 1) times the nebular ages'
+    // sums over ion ((z ntneb + t) x whl, the library's pixels below 912 A) with the model's weights wz (n x nz x nt
+    // FP64), ages below itesc into the young sum
+    const float *ion = nullptr;
+    const double *wz = nullptr;
+    int whl = 0, ntneb = 0, nt = 0, nz = 0, itesc = 0;
+    float *ion_young = nullptr, *ion_old = nullptr;   // the young and old sums with it, written back at those pixels
 };
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
 

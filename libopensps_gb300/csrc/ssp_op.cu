@@ -812,6 +812,37 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     if (a.dem) dm = a.dem[m];
     const bool emis = a.dem != nullptr && dm.on != 0;
     const bool agn = a.dem != nullptr && dm.agn != 0;
+    // the escaping ionizing light of the nebular ages: the model's weights of those ages in shared memory (floored
+    // at SAFE_FLOOR as the sums' weights)
+    const float fesc = fminf(fmaxf(fo, 0.f), 1.f);
+    const bool ion = a.ion != nullptr && fesc > 0.f;
+    float *sw = tsm + (a.dem ? 2 : 1) * a.nspec;
+    if (ion) {
+        const double *wm = a.wz + (size_t)m * a.nz * a.nt;
+        for (int k = threadIdx.x; k < a.nz * a.ntneb; k += blockDim.x) {
+            const double w = wm[(size_t)(k / a.ntneb) * a.nt + k % a.ntneb];
+            sw[k] = w > SAFE_FLOOR ? (float)w : 0.f;
+        }
+        __syncthreads();
+    }
+    // fesc times the nebular ages' sums at ionizing pixel p, into y (ages below itesc) and o
+    auto ion_add = [&](int p, float &y, float &o) {
+        float ey = 0.f, eo = 0.f;
+        const int ty = min(a.ntneb, a.itesc);
+        for (int z = 0; z < a.nz; ++z) {
+            const float *iz = a.ion + (size_t)z * a.ntneb * a.whl + p;
+            const float *wz = sw + z * a.ntneb;
+            for (int t = 0; t < ty; ++t) ey = fmaf(wz[t], __ldg(iz + (size_t)t * a.whl), ey);
+            for (int t = ty; t < a.ntneb; ++t) eo = fmaf(wz[t], __ldg(iz + (size_t)t * a.whl), eo);
+        }
+        y = fmaf(fesc, ey, y);
+        o = fmaf(fesc, eo, o);
+        // (the stored sums as the reverse pass reads them: each pixel's own thread read it above)
+        if (a.ion_young) {
+            a.ion_young[(size_t)m * a.nspec + p] = y;
+            a.ion_old[(size_t)m * a.nspec + p] = o;
+        }
+    };
     // the AGN's luminosity: fagn times the model's L_bol (add_agn_batch :4342-4433, the value the batch outputs;
     // 1 when it is not above SAFE_FLOOR, as log10 L_bol is then 0)
     float lagn = 0.f;
@@ -891,6 +922,8 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
                     g1 = __ldg(gb + q);
                 }
                 float e0 = 0.f, e1 = 0.f;
+                if (ion && 2 * q < a.whl) ion_add(2 * q, yy[u].x, oo[u].x);
+                if (ion && 2 * q + 1 < a.whl) ion_add(2 * q + 1, yy[u].y, oo[u].y);
                 const float t0 = pass1(2 * q, yy[u].x, oo[u].x, sh.x, cn.x, g0.x, g1.x, e0);
                 const float t1 = pass1(2 * q + 1, yy[u].y, oo[u].y, sh.y, cn.y, g0.y, g1.y, e1);
                 reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
@@ -899,8 +932,9 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
         }
     } else {
         for (int p = threadIdx.x; p < ns; p += bd) {
-            float esc = 0.f;
-            tsm[p] = pass1(p, __ldg(yv + p), __ldg(ov + p), emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
+            float esc = 0.f, y = __ldg(yv + p), o = __ldg(ov + p);
+            if (ion && p < a.whl) ion_add(p, y, o);
+            tsm[p] = pass1(p, y, o, emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
                            emis ? __ldg(a.cnu + p) : 0.f, agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f,
                            agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f, esc);
             if (emis) esm[p] = esc;
@@ -948,7 +982,7 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
 
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (size_t)a.nspec * (a.dem ? 2 : 1);
+    const size_t smem = sizeof(float) * ((size_t)a.nspec * (a.dem ? 2 : 1) + (a.ion ? (size_t)a.nz * a.ntneb : 0));
     cudaError_t e = cudaFuncSetAttribute(parts_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     parts_epilogue_kernel<<<a.n, 256, smem, st>>>(a);

@@ -104,9 +104,32 @@ static void line_profile(int nspec, const double *lam, double line_pos, double s
  * adds the lines of each young SSP before the age sum; the batch path adds the same sum after it,
  * src/physics/opensps_csp_batch.f90:2565-2610 and line_profiles :3133-3166: linear in the weights, so both are
  * the same sums). ssp_in / ssp_out: nspec x nt x nz (pixel fastest); line_lum: nline x nt x nz. */
+/* The nebular ranges of a library: whlylim = find_interval(lambda, 912 A) (the pixels 1..whlylim below the Lyman
+ * limit, src/core/opensps_initialization.f90:866) and nt_neb, the ages 1..nt_neb with nebular emission (the nebular
+ * grid's age range, opensps_csp_batch.f90:1644-1645; here the ages up to the last one with line luminosity). */
+void oracle_neb_ranges(int nspec, int nt, int nz, const double *lam, int nline, const double *line_lum, int *nt_neb,
+                       int *whlylim) {
+    int w = oracle_find_interval(lam, nspec, 912.0);
+    *whlylim = w < 0 ? 0 : w;
+    int last = 0;
+    for (int z = 0; z < nz; ++z)
+        for (int t = 0; t < nt; ++t)
+            for (int l = 0; l < nline; ++l)
+                if (line_lum[l + (size_t)nline * (t + (size_t)nt * z)] != 0.0 && t + 1 > last) last = t + 1;
+    *nt_neb = last;
+}
+
 void oracle_line_basis(int nspec, int nt, int nz, const double *lam, int nline, const double *line_pos,
                        const double *line_lum, double sigma_kms, const double *ssp_in, double *ssp_out) {
     memcpy(ssp_out, ssp_in, sizeof(double) * (size_t)nspec * nt * nz);
+    /* the gas absorbs the ionizing light of the nebular ages (nebular_kernels step 2, opensps_csp_batch.f90:2726-
+     * 2750: the age sums at pixels 1..whlylim with the nebular ages times the escaping fraction; its fesc share is
+     * added per model in csp_one) */
+    int nt_neb = 0, whlylim = 0;
+    oracle_neb_ranges(nspec, nt, nz, lam, nline, line_lum, &nt_neb, &whlylim);
+    for (int z = 0; z < nz; ++z)
+        for (int t = 0; t < nt_neb; ++t)
+            for (int i = 0; i < whlylim && i < nspec; ++i) ssp_out[i + (size_t)nspec * (t + (size_t)nt * z)] = 0.0;
     double *prof = (double *)malloc(sizeof(double) * nspec);
     for (int l = 0; l < nline; ++l) {
         int jlo, jhi;
@@ -322,6 +345,10 @@ typedef struct {
     /* the AGN torus (add_agn_dust; agn_spec NULL: off): ntau templates of nspec over the optical depth agn_tau */
     int ntau;
     const double *agn_tau, *agn_spec;
+    /* nebular emission (ssp_ion NULL: off): the library's spectra before the lines and the gas absorption (nspec x
+     * nt x nz), the nebular ages 1..nt_neb and the ionizing pixels 1..whlylim */
+    const double *ssp_ion;
+    int nt_neb, whlylim;
 } oracle_grid_t;
 
 /* One model of compute_csp_batch (src/physics/opensps_csp_batch.f90:431-1214) with a weight matrix over
@@ -359,6 +386,13 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
             const double *b = g->basis + (size_t)ns * (k + (size_t)nt * z);
             double *col = (k + 1 <= itesc) ? y : o;
             for (int i = 0; i < ns; ++i) col[i] += w * b[i];
+            if (g->ssp_ion && k < g->nt_neb) {
+                /* the escaping fraction of the nebular ages' ionizing light, fesc = clamp(frac_obrun, 0, 1)
+                 * (batch_nebular_indices :1696) */
+                const double fesc = fmax(0.0, fmin(par[P_FRAC_OBRUN], 1.0));
+                const double *bi = g->ssp_ion + (size_t)ns * (k + (size_t)nt * z);
+                for (int i = 0; i < g->whlylim && i < ns; ++i) col[i] += fesc * w * bi[i];
+            }
             if (emlines && g->line_lum)
                 for (int l = 0; l < g->nline; ++l) emlines[l] += w * g->line_lum[l + (size_t)g->nline * (k + (size_t)nt * z)];
         }

@@ -21,6 +21,7 @@ PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "d
                 "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01, "fagn": 0.0,
                 "agn_tau": 10.0}
 _dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
 
 
 def build() -> Path:
@@ -36,7 +37,8 @@ class _Grid(C.Structure):
                 ("zt", _dp), ("dl", _dp), ("nline", C.c_int), ("line_lum", _dp), ("add_igm", C.c_int),
                 ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double),
                 ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp),
-                ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp)]
+                ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp), ("ssp_ion", _dp), ("nt_neb", C.c_int),
+                ("whlylim", C.c_int)]
 
 
 class _OpsT(C.Structure):
@@ -57,6 +59,7 @@ def lib() -> C.CDLL:
         _lib.oracle_find_interval.restype = C.c_int
         _lib.oracle_find_interval.argtypes = [_dp, C.c_int, C.c_double]
         _lib.oracle_line_basis.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, C.c_double, _dp, _dp]
+        _lib.oracle_neb_ranges.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _ip, _ip]
         _lib.oracle_cosmo_table.argtypes = [C.c_double, C.c_double, C.c_double, _dp, _dp]
         _lib.oracle_distance_term.restype = C.c_double
         _lib.oracle_distance_term.argtypes = [_dp, _dp, C.c_double]
@@ -159,6 +162,13 @@ class Oracle:
         g.zt, g.dl = _p(self.zt), _p(self.dl)
         g.nline = nl
         g.line_lum = _p(self.line_lum) if add_neb else None
+        g.ssp_ion = None
+        if add_neb:
+            self._ssp = ssp
+            a, b = C.c_int(0), C.c_int(0)
+            L.oracle_neb_ranges(ns, nt, nz, _p(self.lam), nl, _p(self.line_lum), C.byref(a), C.byref(b))
+            g.ssp_ion, g.nt_neb, g.whlylim = _p(ssp), a.value, b.value
+            self.nt_neb, self.whlylim = a.value, b.value
         g.add_igm, g.smooth = int(add_igm), int(smooth)
         g.min_wave_smooth, g.max_wave_smooth = min_wave_smooth, max_wave_smooth
         g.dustem = None

@@ -89,3 +89,25 @@ def test_igm_only_below_lyman_alpha(data):
     red = o.lam >= 1215.67
     np.testing.assert_array_equal(a["spec"][:, red], b["spec"][:, red])
     assert np.all(a["spec"][:, ~red] <= b["spec"][:, ~red])
+
+
+def test_oracle_escaping_ionizing_light(data):
+    """The oracle's gas absorption: with nebular emission and frac_obrun = 1 (fesc = 1) the ionizing pixels of the
+    young and old sums equal those without nebular emission; with frac_obrun = 0 the nebular ages' ionizing light is
+    gone (the sums there come from the older ages only)."""
+    from oracle.oracle import Oracle
+    n = 3
+    rng = np.random.default_rng(951)
+    wz = rng.dirichlet(np.ones(107 * 12), size=n).reshape(n, 12, 107)
+    on, off = Oracle(data, nbands=20), Oracle(data, nbands=20, add_neb=False)
+    whl = on.whlylim
+    a = on.csp_batch({"frac_obrun": np.ones(n)}, wz, young=True)
+    b = off.csp_batch({"frac_obrun": np.ones(n)}, wz, young=True)
+    np.testing.assert_allclose(a["young"][:, :whl], b["young"][:, :whl], rtol=1e-13, atol=1e-300)
+    np.testing.assert_allclose(a["old"][:, :whl], b["old"][:, :whl], rtol=1e-13, atol=1e-300)
+    c = on.csp_batch({"frac_obrun": np.zeros(n)}, wz, young=True)
+    wo = wz.copy()
+    wo[:, :, :on.nt_neb] = 0.0
+    d = off.csp_batch({"frac_obrun": np.zeros(n)}, wo, young=True)
+    np.testing.assert_allclose(c["young"][:, :whl] + c["old"][:, :whl], d["young"][:, :whl] + d["old"][:, :whl],
+                               rtol=1e-13, atol=1e-300)
