@@ -772,8 +772,16 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     auto epilogue = [&](const float *y, const float *o, int off, int nk) -> cudaError_t {
         PartsEpilogueArgs pe;
         if (ion_terms) {
-            pe.ion = c.d_ion.p; pe.wz = d_wz + (size_t)nt * nz * off; pe.whl = c.whlylim; pe.ntneb = c.nt_neb;
-            pe.nt = nt; pe.nz = nz; pe.itesc = itesc;
+            // the nebular ages' sums at the ionizing pixels of models [off, off + nk), then added in the epilogue
+            IonSumsArgs ia;
+            ia.n = nk; ia.whl = c.whlylim; ia.ntneb = c.nt_neb; ia.nt = nt; ia.nz = nz; ia.itesc = itesc;
+            ia.ion = c.d_ion.p; ia.wz = d_wz + (size_t)nt * nz * off;
+            cudaError_t r = c.d_ione.reserve((size_t)2 * nk * c.whlylim);
+            if (r != cudaSuccess) return r;
+            ia.ey = c.d_ione.p; ia.eo = c.d_ione.p + (size_t)nk * c.whlylim;
+            if ((r = run_ion_sums(ia, st)) != cudaSuccess) return r;
+            ++launches;
+            pe.ion_ey = ia.ey; pe.ion_eo = ia.eo; pe.whl = c.whlylim;
             pe.ion_young = const_cast<float *>(y) + (size_t)ns * off;
             pe.ion_old = const_cast<float *>(o) + (size_t)ns * off;
         }

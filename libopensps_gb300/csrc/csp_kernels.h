@@ -317,15 +317,23 @@ struct PartsEpilogueArgs {
     const float *agn_spec = nullptr;
     const double *lsum = nullptr;
     int lsum_stride = 6;
-    // nebular emission's escaping ionizing light (ion null: none): clamp(frac_obrun, 0, 1) times the nebular ages'
-    // sums over ion ((z ntneb + t) x whl, the library's pixels below 912 A) with the model's weights wz (n x nz x nt
-    // FP64), ages below itesc into the young sum
-    const float *ion = nullptr;
-    const double *wz = nullptr;
-    int whl = 0, ntneb = 0, nt = 0, nz = 0, itesc = 0;
+    // nebular emission's escaping ionizing light (ion_ey null: none): clamp(frac_obrun, 0, 1) times the nebular
+    // ages' sums at the ionizing pixels (n x whl, young and old: ion_sums_kernel)
+    const float *ion_ey = nullptr, *ion_eo = nullptr;
+    int whl = 0;
     float *ion_young = nullptr, *ion_old = nullptr;   // the young and old sums with it, written back at those pixels
 };
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
+
+// The nebular ages' sums at the ionizing pixels: ey / eo (n x whl) = sum over k = (z, t < ntneb) of the weights wz
+// (n x nz x nt FP64, floored at SAFE_FLOOR) times ion ((z ntneb + t) x whl), ages below itesc into ey.
+struct IonSumsArgs {
+    int n, whl, ntneb, nt, nz, itesc;
+    const float *ion;
+    const double *wz;
+    float *ey, *eo;
+};
+cudaError_t run_ion_sums(const IonSumsArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

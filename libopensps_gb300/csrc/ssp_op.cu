@@ -812,31 +812,13 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     if (a.dem) dm = a.dem[m];
     const bool emis = a.dem != nullptr && dm.on != 0;
     const bool agn = a.dem != nullptr && dm.agn != 0;
-    // the escaping ionizing light of the nebular ages: the model's weights of those ages in shared memory (floored
-    // at SAFE_FLOOR as the sums' weights)
+    // the escaping ionizing light of the nebular ages: fesc times their sums at ionizing pixel p (ion_sums_kernel),
+    // into y (ages below itesc) and o
     const float fesc = fminf(fmaxf(fo, 0.f), 1.f);
-    const bool ion = a.ion != nullptr && fesc > 0.f;
-    float *sw = tsm + (a.dem ? 2 : 1) * a.nspec;
-    if (ion) {
-        const double *wm = a.wz + (size_t)m * a.nz * a.nt;
-        for (int k = threadIdx.x; k < a.nz * a.ntneb; k += blockDim.x) {
-            const double w = wm[(size_t)(k / a.ntneb) * a.nt + k % a.ntneb];
-            sw[k] = w > SAFE_FLOOR ? (float)w : 0.f;
-        }
-        __syncthreads();
-    }
-    // fesc times the nebular ages' sums at ionizing pixel p, into y (ages below itesc) and o
+    const bool ion = a.ion_ey != nullptr && fesc > 0.f;
     auto ion_add = [&](int p, float &y, float &o) {
-        float ey = 0.f, eo = 0.f;
-        const int ty = min(a.ntneb, a.itesc);
-        for (int z = 0; z < a.nz; ++z) {
-            const float *iz = a.ion + (size_t)z * a.ntneb * a.whl + p;
-            const float *wz = sw + z * a.ntneb;
-            for (int t = 0; t < ty; ++t) ey = fmaf(wz[t], __ldg(iz + (size_t)t * a.whl), ey);
-            for (int t = ty; t < a.ntneb; ++t) eo = fmaf(wz[t], __ldg(iz + (size_t)t * a.whl), eo);
-        }
-        y = fmaf(fesc, ey, y);
-        o = fmaf(fesc, eo, o);
+        y = fmaf(fesc, __ldg(a.ion_ey + (size_t)m * a.whl + p), y);
+        o = fmaf(fesc, __ldg(a.ion_eo + (size_t)m * a.whl + p), o);
         // (the stored sums as the reverse pass reads them: each pixel's own thread read it above)
         if (a.ion_young) {
             a.ion_young[(size_t)m * a.nspec + p] = y;
@@ -980,9 +962,98 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     }
 }
 
+// The nebular ages' sums at the ionizing pixels, E(m, p) = sum_k w(m, k) ion(k, p) over k = (z, t < ntneb), split
+// into ages below itesc (young) and the rest (old): a tiled FP32 product, 128 pixels x 32 models per CTA, 32 k per
+// shared-memory step; thread (tx, ty) holds pixels tx + 32 j and models 4 ty + i. Weights floored at SAFE_FLOOR as
+// the batch's sums floor them.
+constexpr int ION_TP = 128, ION_TM = 32, ION_TK = 32;
+
+__global__ void __launch_bounds__(256) ion_sums_kernel(IonSumsArgs a) {
+    __shared__ float is[ION_TK][ION_TP];
+    __shared__ float ws[ION_TK][ION_TM];
+    __shared__ int young[ION_TK];
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int p0 = blockIdx.x * ION_TP, m0 = blockIdx.y * ION_TM;
+    const int K = a.nz * a.ntneb;
+    float ey[4][4], eo[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { ey[i][j] = 0.f; eo[i][j] = 0.f; }
+    for (int k0 = 0; k0 < K; k0 += ION_TK) {
+        __syncthreads();
+        for (int e = tid; e < ION_TK * ION_TP; e += 256) {
+            const int kk = e / ION_TP, pp = e - kk * ION_TP, k = k0 + kk, p = p0 + pp;
+            is[kk][pp] = (k < K && p < a.whl) ? __ldg(a.ion + (size_t)k * a.whl + p) : 0.f;
+        }
+        for (int e = tid; e < ION_TK * ION_TM; e += 256) {
+            const int kk = e / ION_TM, mm = e - kk * ION_TM, k = k0 + kk, m = m0 + mm;
+            float w = 0.f;
+            if (k < K && m < a.n) {
+                const int z = k / a.ntneb, t = k - z * a.ntneb;
+                const double v = a.wz[(size_t)m * a.nz * a.nt + (size_t)z * a.nt + t];
+                w = v > SAFE_FLOOR ? (float)v : 0.f;
+            }
+            ws[kk][mm] = w;
+        }
+        if (tid < ION_TK) young[tid] = ((k0 + tid) % a.ntneb) < a.itesc;
+        __syncthreads();
+        const int kn = min(ION_TK, K - k0);
+        for (int kk = 0; kk < kn; ++kk) {
+            float x[4], w[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) x[j] = is[kk][tx + 32 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) w[i] = ws[kk][4 * ty + i];
+            if (young[kk]) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) ey[i][j] = fmaf(w[i], x[j], ey[i][j]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) eo[i][j] = fmaf(w[i], x[j], eo[i][j]);
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = m0 + 4 * ty + i;
+        if (m >= a.n) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int p = p0 + tx + 32 * j;
+            if (p < a.whl) {
+                a.ey[(size_t)m * a.whl + p] = ey[i][j];
+                a.eo[(size_t)m * a.whl + p] = eo[i][j];
+            }
+        }
+    }
+}
+
+cudaError_t run_ion_sums(const IonSumsArgs &a, cudaStream_t st) {
+    if (a.n <= 0 || a.whl <= 0) return cudaSuccess;
+    // (slices of models within the grid's y limit)
+    const int slice = 65535 * ION_TM;
+    for (int s0 = 0; s0 < a.n; s0 += slice) {
+        IonSumsArgs b = a;
+        b.n = std::min(slice, a.n - s0);
+        b.wz = a.wz + (size_t)s0 * a.nz * a.nt;
+        b.ey = a.ey + (size_t)s0 * a.whl;
+        b.eo = a.eo + (size_t)s0 * a.whl;
+        const dim3 grid((a.whl + ION_TP - 1) / ION_TP, (b.n + ION_TM - 1) / ION_TM);
+        ion_sums_kernel<<<grid, 256, 0, st>>>(b);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * ((size_t)a.nspec * (a.dem ? 2 : 1) + (a.ion ? (size_t)a.nz * a.ntneb : 0));
+    const size_t smem = sizeof(float) * (size_t)a.nspec * (a.dem ? 2 : 1);
     cudaError_t e = cudaFuncSetAttribute(parts_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     parts_epilogue_kernel<<<a.n, 256, smem, st>>>(a);
