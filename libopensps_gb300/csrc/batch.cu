@@ -776,9 +776,10 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             IonSumsArgs ia;
             ia.n = nk; ia.whl = c.whlylim; ia.ntneb = c.nt_neb; ia.nt = nt; ia.nz = nz; ia.itesc = itesc;
             ia.ion = c.d_ion.p; ia.wz = d_wz + (size_t)nt * nz * off;
-            cudaError_t r = c.d_ione.reserve((size_t)2 * nk * c.whlylim);
+            const size_t nw = (size_t)nz * c.nt_neb * nk;
+            cudaError_t r = c.d_ione.reserve((size_t)2 * nk * c.whlylim + nw);
             if (r != cudaSuccess) return r;
-            ia.ey = c.d_ione.p; ia.eo = c.d_ione.p + (size_t)nk * c.whlylim;
+            ia.ey = c.d_ione.p; ia.eo = c.d_ione.p + (size_t)nk * c.whlylim; ia.wn = ia.eo + (size_t)nk * c.whlylim;
             if ((r = run_ion_sums(ia, st)) != cudaSuccess) return r;
             ++launches;
             pe.ion_ey = ia.ey; pe.ion_eo = ia.eo; pe.whl = c.whlylim;

@@ -160,7 +160,7 @@ struct Context {
     // nebular emission's gas absorption: ages 0..nt_neb-1 carry nebular emission, pixels 0..whlylim-1 are ionizing
     // (below 912 A); d_ion holds those ages' ionizing pixels of the library, (z nt_neb + t) x whlylim FP32
     int nt_neb = 0, whlylim = 0;
-    DevBuf<float> d_ion, d_ione;     // d_ione: a batch's sums of the nebular ages at those pixels (2 x n x whlylim)
+    DevBuf<float> d_ion, d_ione;     // d_ione: a batch's sums of the nebular ages at those pixels (2 x n x whlylim) and its compact weights
     bool last_ion = false;           // the last batch added the escaping ionizing light (its reverse pass follows)
     std::vector<int> mag_mask;   // empty: all bands
 

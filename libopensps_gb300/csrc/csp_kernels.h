@@ -332,6 +332,8 @@ struct IonSumsArgs {
     const float *ion;
     const double *wz;
     float *ey, *eo;
+    float *wn = nullptr;     // scratch: nz ntneb x n, the weights gathered compact (set by the caller)
+    int wn_ld = 0;           // its row stride (set by run_ion_sums)
 };
 cudaError_t run_ion_sums(const IonSumsArgs &a, cudaStream_t st);
 
