@@ -67,18 +67,22 @@ void opensps_gb300_data_table(const char *root, const char *kind, const char *na
 /* The magnitudes (nbands x n doubles, d_mags) of n rest-frame spectra already on the device (d_spec: nspec x n
  * floats, column-major, as opensps_context_batch_spec_device gives them) at redshifts d_zred (n doubles), through
  * the band GEMM of the batch, with no allocation: the call's scratch (observed-frame shifts, distance terms, band
- * mask, status word) is a fixed 2 MiB device array of the library, held on every device that loads the library
- * until the process exits. No counterpart in OpenSPS: it serves callers that may not allocate device memory.
- * n > OPENSPS_GB300_NOALLOC_MAX_MODELS: status 3 and nothing runs. The first call on a device looks the array's
- * address up (cudaGetSymbolAddress) and should come before any stream capture. Every call shares the array:
- * calls whose kernels overlap on the GPU (other streams, contexts or threads) race. Runs on the context's stream;
- * asynchronous unless sync != 0. The context's filter library and magnitude mask apply. */
+ * mask, status word) is a fixed 2 MiB device array of the library. No counterpart in OpenSPS: it serves callers that
+ * may not allocate device memory (a framework's custom-call handler handed preallocated buffers, where a cudaMalloc
+ * can fail and a cudaFree synchronises the device under the framework's stream).
+ * n > OPENSPS_GB300_NOALLOC_MAX_MODELS: status 3 and nothing runs.
+ * When the array comes into being: opensps_context_setup loads this entry point's kernels on the context's device,
+ * which creates the array there (held until the process exits), and looks its address up; the call itself loads and
+ * allocates nothing. A context that was not set up gives status 301. Every call shares the array: calls whose kernels
+ * overlap on the GPU (other streams, contexts or threads) race. Runs on the context's stream; asynchronous unless
+ * sync != 0. With sync = 0 a device wait that gave up (status 4 with sync != 0) is not reported. The context's
+ * filter library and magnitude mask apply. */
 void opensps_gb300_spec_mags_noalloc(int handle, int n, const float *d_spec, const double *d_zred, double *d_mags,
                                      int sync, int *status);
 
 /* ---- The learned emulator (no counterpart in OpenSPS, whose only network is the cue nebular MLP) ----------------
  * An ensemble of five MLPs, 10 inputs -> 4 x 512 SiLU -> the first 64 PCA coefficients of log10 of the spectrum and
- * the magnitudes less the distance term (bf16 weights and activations, f32 accumulation), trained on this
+ * the magnitudes less the distance term (f16 weights and activations, f32 accumulation), trained on this
  * library's own CSP through the SSP operators: a Kroupa IMF per model and the delayed-tau SFH (sfh = 4) on the
  * device. Inputs, column-major OPENSPS_GB300_EMU_INPUTS x n doubles, in this order: tau [Gyr], tage [Gyr], logzsol,
  * dust2, dust_index, zred, sigma_smooth [km/s], imf1, imf2, imf3. The training box: log10 tau in [-1, 1], tage in

@@ -294,6 +294,15 @@ int band_gemm_ksplit(int n_models, int nkb, int num_sms) {
     return std::max(1, std::min((2 * num_sms + tiles - 1) / tiles, nkb / 4));
 }
 
+// Loads the band GEMM's module on the current device (CUDA loads modules lazily, on first use), so that a later
+// launch loads nothing.
+cudaError_t band_gemm_load() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, band_gemm_kernel);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, band_finish_kernel);
+    return e;
+}
+
 cudaError_t run_band_gemm(const BandGemmArgs &a_in, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
                           cudaStream_t st) {
     if (a_in.n_models <= 0 || a_in.nkb <= 0) return cudaSuccess;

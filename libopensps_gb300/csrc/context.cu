@@ -647,6 +647,11 @@ int context_setup_grid(Context &c, std::string &err) {
     for (auto &kv : c.basis_cache) { kv.second->release(); delete kv.second; }
     c.basis_cache.clear();
     c.eml_nnz = -1;
+    // the no-allocation magnitudes' modules and scratch address on this device (so that its calls allocate nothing)
+    if ((e = noalloc_prepare(c.device)) != cudaSuccess) {
+        err = std::string("loading the no-allocation entry point's modules: ") + cudaGetErrorString(e);
+        return ST_DATA_MISSING;
+    }
     c.is_setup = true;
     return 0;
 }

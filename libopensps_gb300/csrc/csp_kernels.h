@@ -130,6 +130,10 @@ int band_gemm_npad(int nbands);
 int band_gemm_ksplit(int n_models, int nkb, int num_sms);
 cudaError_t run_band_gemm(const BandGemmArgs &a, const CUtensorMap &tm_hi, const CUtensorMap &tm_lo,
                           cudaStream_t st);
+// Loads the band GEMM's module on the current device (no launch).
+cudaError_t band_gemm_load();
+// Loads the no-allocation entry point's modules on `device` (current) and records its scratch's device address.
+cudaError_t noalloc_prepare(int device);
 
 // Emission-line luminosities: eml(l, m) = sum_k w(k, m) L(l, k) over the (age, metallicity) entries with lines.
 struct EmlineArgs {

@@ -12,8 +12,8 @@
 // its 64 columns of the chunk into registers and releases the accumulator, so that the next chunk's MMAs run while
 // it adds the biases, applies SiLU and stores the f16 activations; the next layer's first chunk starts on the
 // 256 features already written (a ready barrier per 256 features).
-// The weights stream through a three-stage TMA ring of 256 x 64 f16 tiles (32 KB): the two CTAs of a cluster load
-// one half each and multicast it to both.
+// The weights stream through a three-stage TMA ring of 256 x 64 f16 tiles (32 KB), each CTA loading its own tiles
+// (no clusters); the CTAs start on different members so that their reads spread over L2.
 //
 // Warp 0: TMA producer; warp 1: MMA issuer (one thread) and TMEM owner; warps 2..17: epilogue, four warps per
 // TMEM lane quarter (one model row per thread, 64 of a chunk's 256 columns each). Each member's outputs go to the
@@ -43,9 +43,8 @@ constexpr int EI_S_BYTES = 8 * EI_KBLK;           // activations: 8 K blocks
 constexpr int EI_SMEM = EI_S_BYTES + EI_NS * EI_STAGE + 256 + 1024;
 constexpr uint32_t EI_IDESC256 = idesc_f16_f32(128, 256), EI_IDESC128 = idesc_f16_f32(128, 128);
 constexpr uint32_t EI_T_COL = 0, EI_ACC_COL = 256;
-constexpr int EI_CS = 2;                          // CTAs per cluster sharing each weight tile (multicast)
-constexpr int EI_ROWS = 256 / EI_CS;              // rows of a hidden-layer weight tile each CTA of the cluster loads
-constexpr int EI_ROWS4 = 128 / EI_CS;             // the same for the output layer's 128-row tiles
+constexpr int EI_ROWS = 256;                      // rows of a hidden-layer weight tile (one TMA box)
+constexpr int EI_ROWS4 = 128;                     // the same for the output layer's 128-row tiles
 
 __device__ __forceinline__ float silu_fast(float z) {
     const float hz = 0.5f * z;
@@ -85,9 +84,8 @@ __device__ __forceinline__ float emu_distance(float z, const float *zt, const fl
 
 // The member a CTA runs at step mem of each tile: the order is rotated by the CTA index, so that the CTAs stream
 // different members' weights at a time instead of all reading the same tiles from the same L2 lines.
-__device__ __forceinline__ int emu_member(int mem) { return (mem + (int)blockIdx.x / EI_CS) % EMU_MEMBERS; }
-// Tiles per CTA: the same count in every CTA (a cluster's CTAs load the weights together), the ones past the last
-// tile are run with no valid model.
+__device__ __forceinline__ int emu_member(int mem) { return (mem + (int)blockIdx.x) % EMU_MEMBERS; }
+// Tiles per CTA: the same count in every CTA, the ones past the last tile are run with no valid model.
 __device__ __forceinline__ int emu_iters(int ntiles) { return (ntiles + (int)gridDim.x - 1) / (int)gridDim.x; }
 
 // A warp-uniform bounded wait (every lane polls; the warp goes on only if all saw the phase complete).
@@ -352,7 +350,7 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
     int *status = a.status;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < EI_NS; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], EI_CS); }
+        for (int s = 0; s < EI_NS; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         mbar_init(afull, 1);
         mbar_init(aempty, EI_EPI_WARPS);
         for (int c = 0; c < 2; ++c) mbar_init(&hrdy[c], EI_EPI_WARPS);
@@ -363,11 +361,8 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
     if (warp == 1) { tmem_alloc(tmem_slot, 512); tmem_relinquish(); }
     tc_fence_before();
     __syncthreads();
-    cluster_sync();      // the partner's barriers are initialised before any multicast reaches them
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    const uint32_t rank = cluster_ctarank();
-    const uint16_t cmask = (uint16_t)((1u << EI_CS) - 1u);
     const int iters = emu_iters(ntiles);
 
     if (warp == 0) {
@@ -382,24 +377,20 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
                         const int nch = L == 4 ? 1 : 2, nkb = L == 0 ? 1 : 8;
                         for (int c = 0; c < nch && ok; ++c)
                             for (int kb = 0; kb < nkb; ++kb) {
-                                // the stage is free once every CTA of the cluster has consumed it
+                                // the stage is free once the MMAs that read it have completed
                                 if (!mbar_wait(&empty[s], ph ^ 1u, status, ERR_TIMEOUT_PRODUCER)) { ok = false; break; }
                                 const int mw = emu_member(mem);
                                 uint8_t *st = W + s * EI_STAGE;
                                 if (L < 4) {
                                     mbar_arrive_expect_tx(&full[s], EI_STAGE);
-                                    const int row = (int)rank * EI_ROWS;
-                                    uint8_t *dst = st + rank * (EI_ROWS * 128);
                                     if (L == 0)
-                                        tma_load_2d_mc(dst, &tm_w0, 0, mw * EMU_H + c * 256 + row, &full[s], cmask);
+                                        tma_load_2d(st, &tm_w0, 0, mw * EMU_H + c * 256, &full[s]);
                                     else
-                                        tma_load_2d_mc(dst, &tm_wh, kb * 64, ((L - 1) * EMU_MEMBERS + mw) * EMU_H + c * 256 + row,
-                                                       &full[s], cmask);
+                                        tma_load_2d(st, &tm_wh, kb * 64, ((L - 1) * EMU_MEMBERS + mw) * EMU_H + c * 256,
+                                                    &full[s]);
                                 } else {
                                     mbar_arrive_expect_tx(&full[s], EI_STAGE / 2);
-                                    const int row = (int)rank * EI_ROWS4;
-                                    tma_load_2d_mc(st + rank * (EI_ROWS4 * 128), &tm_w4, kb * 64, mw * EMU_NOUT + row,
-                                                   &full[s], cmask);
+                                    tma_load_2d(st, &tm_w4, kb * 64, mw * EMU_NOUT, &full[s]);
                                 }
                                 last_fill[s] = (int)ph;
                                 if (++s == EI_NS) { s = 0; ph ^= 1u; }
@@ -450,7 +441,7 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
                                             mma_bf16(d, sw128_desc(s_base + kb * EI_KBLK + k * 32), sw128_desc(b0 + k * 32), idesc, acc);
                                     }
                                 }
-                                mma_commit_mc(&empty[s], cmask);   // frees the stage in every CTA
+                                mma_commit(&empty[s]);   // frees the stage once these MMAs complete
                                 if (++s == EI_NS) { s = 0; ph ^= 1u; }
                             }
                             if (!ok) break;
@@ -472,7 +463,6 @@ emu_infer_kernel(const __grid_constant__ CUtensorMap tm_w0, const __grid_constan
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
     }
-    cluster_sync();      // no CTA leaves while its partner may still write into its shared memory or barriers
 }
 
 int emu_infer_smem() { return EI_SMEM; }
@@ -486,27 +476,14 @@ cudaError_t run_emu_infer(const Emulator &e, const EmuInferArgs &a, int num_sms,
     cudaError_t err = cudaFuncSetAttribute(emu_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EI_SMEM);
     if (err != cudaSuccess) return err;
     cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = EI_CS;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
     cfg.blockDim = dim3(EI_THREADS);
     cfg.dynamicSmemBytes = EI_SMEM;
     cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    // persistent: as many clusters as fit at once (at most one CTA per SM), no more than the tiles need
-    static int max_clusters = 0;
-    if (max_clusters == 0) {
-        cfg.gridDim = dim3(num_sms / EI_CS * EI_CS);
-        int mc = 0;
-        if (cudaOccupancyMaxActiveClusters(&mc, emu_infer_kernel, &cfg) != cudaSuccess || mc <= 0) mc = num_sms / EI_CS;
-        max_clusters = mc;
-    }
+    cfg.attrs = nullptr;
+    cfg.numAttrs = 0;
+    // persistent: one CTA per SM (its shared memory allows no more), no more CTAs than tiles
     const int ntiles = (a.n + 127) / 128;
-    const int clusters = std::min(max_clusters, (ntiles + EI_CS - 1) / EI_CS);
-    cfg.gridDim = dim3(clusters * EI_CS);
+    cfg.gridDim = dim3(std::min(num_sms, ntiles));
     err = cudaLaunchKernelEx(&cfg, emu_infer_kernel, e.tm_w0, e.tm_wh, e.tm_w4, a);
     if (err != cudaSuccess) return err;
     return cudaGetLastError();

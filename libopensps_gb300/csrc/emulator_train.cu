@@ -482,7 +482,7 @@ static int emu_alloc(Emulator &e, bool trainable, std::string &err) {
         e.trainable = true;
         e.adam_t = 0;
     }
-    // the inference kernel's boxes: its share of a 128-row weight tile (the cluster's CTAs load one share each)
+    // the inference kernel's boxes: a whole hidden-layer tile (256 rows) and a whole output-layer tile (128 rows)
     const uint32_t rows = (uint32_t)emu_weight_box_rows(), rows4 = (uint32_t)emu_weight_box_rows4();
     cudaError_t r1 = encode_tmap_2d_16(&e.tm_w0, e.w0, EMU_KIN, (uint64_t)EMU_MEMBERS * EMU_H, 64, rows, true);
     cudaError_t r2 = encode_tmap_2d_16(&e.tm_wh, e.wh, EMU_H, 3ull * EMU_MEMBERS * EMU_H, 64, rows, true);

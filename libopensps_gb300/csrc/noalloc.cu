@@ -8,8 +8,14 @@
 //   [24 MAX_MODELS, + 4 MAX_BANDS)       int do_band per band
 //   [.., + 4)                            int status (cleared by every call)
 // Every call on a device shares the array and leaves its contents behind; two calls whose kernels overlap on the
-// GPU (other streams, other contexts, other threads) race on it. The device address of the array is looked up once
-// per device, by the first call on that device, with cudaGetSymbolAddress.
+// GPU (other streams, other contexts, other threads) race on it.
+//
+// When the array comes into being: the library's kernels sit in separately compiled modules that CUDA loads lazily,
+// on a module's first use on a device. Loading this file's module creates the array (and its code) in device memory,
+// and loading the band GEMM's module creates its code. So that a call of the entry point never does either, every
+// context set-up (opensps_context_setup) loads both modules on the context's device and looks the array's device
+// address up there with cudaGetSymbolAddress (noalloc_prepare); the call only reads that address. A set-up after a
+// device reset looks it up again.
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdint>
@@ -70,19 +76,29 @@ __global__ void obs_frame_kernel(ObsFrameArgs a) {
     a.dist[m] = dd;
 }
 
-// The scratch's device address on each device, looked up by the first call there.
+// The scratch's device address on each device, looked up by noalloc_prepare at every context set-up there.
 static std::mutex g_noalloc_mu;
 static unsigned char *g_noalloc_ptr[256] = {};
+
+// With `device` current: loads this file's module and the band GEMM's on it (the array is created then), and records
+// the array's device address. Called by the context's set-up, so that the entry point itself allocates nothing.
+cudaError_t noalloc_prepare(int device) {
+    if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, obs_frame_kernel);
+    if (e == cudaSuccess) e = band_gemm_load();
+    void *p = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
+    return cudaSuccess;
+}
 
 static cudaError_t noalloc_scratch(int device, unsigned char **out) {
     if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);   // the device is current here
-        if (e != cudaSuccess) return e;
-        g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
-    }
+    if (!g_noalloc_ptr[device]) return cudaErrorNotReady;   // the context was not set up on this device
     *out = g_noalloc_ptr[device];
     return cudaSuccess;
 }
@@ -104,7 +120,11 @@ int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zre
     cudaError_t e = cudaGetDevice(&prev);
     if (e == cudaSuccess && prev != c.device) e = cudaSetDevice(c.device);
     unsigned char *base = nullptr;
-    if (e == cudaSuccess) e = noalloc_scratch(c.device, &base);
+    if (e == cudaSuccess && noalloc_scratch(c.device, &base) != cudaSuccess) {
+        err = "spec_mags_noalloc: the context was not set up on its device";
+        if (prev >= 0 && prev != c.device) cudaSetDevice(prev);
+        return ST_NOT_SETUP;
+    }
     int rc = 0;
     if (e == cudaSuccess) {
         float4 *zinfo = reinterpret_cast<float4 *>(base + NOALLOC_ZINFO_OFF);

@@ -77,17 +77,6 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *m, int
         : "memory");
 }
 
-// The same, multicast: the box lands at the same offset in every CTA of ctamask (this GPU's cluster), completing
-// on the mbarrier at the same offset in each.
-__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *m, int x, int y, uint64_t *bar,
-                                               uint16_t ctamask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(ctamask)
-        : "memory");
-}
-
 // ---------------------------------------------------------------------------------------------- clusters
 __device__ __forceinline__ uint32_t cluster_ctarank() {
     uint32_t r;
@@ -143,13 +132,6 @@ __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, ui
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                      smem_u32(bar))
-                 : "memory");
-}
-// Arrive on the mbarrier at bar's offset in every CTA of ctamask when every MMA issued so far by this thread has
-// completed.
-__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t ctamask) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                     smem_u32(bar)), "h"(ctamask)
                  : "memory");
 }
 // 32 consecutive f32 columns of this warp's 32 TMEM lanes (thread i gets lane base+i).

@@ -1,6 +1,6 @@
 """The standard data format (doc/DATA_FORMAT.md sections 2-3 of the reference; its reader src/io/opensps_datalib.f90):
 the C-ABI library's loader (opensps_gb300_data_table, no device) against the numpy restatement in oracle/stdformat.py
-on libraries written by libopensps_gb300/stdformat.py and, when present in this container, on the reference's own
+on libraries written by libopensps_gb300/stdformat.py and, when OPENSPS_SOURCE_DIR names an OpenSPS source tree, on its own
 test library (real DL07, THEMIS, clumpy-torus and filter manifests and arrays); and the reader's refusals (truncated
 files, format versions, names, extra axes without a selection), selections and axis defaults.
 
@@ -8,6 +8,7 @@ Tolerances: relative 1e-13 (interpolations agree to rounding; the trapezoid sums
 values of the log-interpolated AGN templates below 1e-12 of their peak absolutely.
 """
 import json
+import os
 import shutil
 from pathlib import Path
 
@@ -18,7 +19,8 @@ from libopensps_gb300 import stdformat, synthdata
 from libopensps_gb300.capi import OpenSPSError, data_table
 from oracle import stdformat as ora
 
-REF_TEST_LIBRARY = Path("/root/reference/tests/data/opensps-test-data")
+# The OpenSPS source tree, when one is at hand (OPENSPS_SOURCE_DIR); its test library's cases skip otherwise.
+REF_TEST_LIBRARY = Path(os.environ.get("OPENSPS_SOURCE_DIR", "/nonexistent")) / "tests" / "data" / "opensps-test-data"
 
 
 @pytest.fixture(scope="module")
