@@ -166,6 +166,8 @@ static double lum_distance_pc(double h0, double om0, double ol0, double z) {
 }
 
 /* update_cosmology_table (src/physics/opensps_cosmology.f90:286-300): 500 scale factors; zt decreasing. */
+double oracle_lum_distance(double h0, double om0, double ol0, double z) { return lum_distance_pc(h0, om0, ol0, z); }
+
 void oracle_cosmo_table(double h0, double om0, double ol0, double *zt, double *dl) {
     for (int i = 1; i <= 500; ++i) {
         double a = (double)(i - 1) / 499.0 * (1.0 - 1.0 / 1001.0) + 1.0 / 1001.0;
@@ -351,6 +353,46 @@ typedef struct {
     int nt_neb, whlylim;
 } oracle_grid_t;
 
+/* observed_frame_z (src/spectra/opensps_batch_photometry.f90:819-903) for one model: the rest-frame spectrum fin at
+ * lambda / (1 + z) by linear interpolation in the interval find_interval gives (the end intervals extrapolate),
+ * NaN to 0, negatives to 0, times 1 / lambda; z with |z| <= SAFE_FLOOR reads the pixel itself. */
+void oracle_observed_frame(int ns, const double *lam, double zr, const double *fin, double *fobs) {
+    for (int j = 0; j < ns; ++j) {
+        double v;
+        if (fabs(zr) > SAFE_FLOOR) {
+            double target = lam[j] / (1.0 + zr);
+            int il = oracle_find_interval(lam, ns, target);
+            if (il < 1) il = 1;
+            if (il > ns - 1) il = ns - 1;
+            double t = (target - lam[il - 1]) / (lam[il] - lam[il - 1]);
+            v = fin[il - 1] + t * (fin[il] - fin[il - 1]);
+        } else {
+            v = fin[j];
+        }
+        if (v != v) v = 0.0;
+        fobs[j] = (v > 0.0 ? v : 0.0) * (lam[j] > DBL_MIN ? 1.0 / lam[j] : 0.0);
+    }
+}
+
+/* band_fluxes (src/spectra/opensps_batch_photometry.f90:1049-1171) for one model and nb bands: band b (its curve
+ * bands + ns b) sums the trapezoid terms wt(j) (fobs(j) T(j) + fobs(j + 1) T(j + 1)) over the 1-based pixels j =
+ * jlo[b] .. jhi[b] (pixel j + 1 is read, so jhi <= ns - 1); bands with do_band[b] = 0 are exactly 0. wt: ns weights,
+ * or NULL for the trapezoid's 0.5 |lambda(j + 1) - lambda(j)| from lam. */
+void oracle_band_fluxes(int ns, int nb, const double *bands, const int *jlo, const int *jhi, const int *do_band,
+                        const double *wt, const double *lam, const double *fobs, double *fband) {
+    for (int b = 0; b < nb; ++b) {
+        double s = 0.0;
+        if (do_band[b]) {
+            const double *bd = bands + (size_t)ns * b;
+            for (int j = jlo[b]; j <= jhi[b]; ++j) {
+                double w = wt ? wt[j - 1] : 0.5 * fabs(lam[j] - lam[j - 1]);
+                s += w * (fobs[j - 1] * bd[j - 1] + fobs[j] * bd[j]);
+            }
+        }
+        fband[b] = s;
+    }
+}
+
 /* One model of compute_csp_batch (src/physics/opensps_csp_batch.f90:431-1214) with a weight matrix over
  * ages and metallicities (weights_over_z):
  *   model_sums_zw           :2090-2120   mass, L_bol, weights floored at SAFE_FLOOR, young/old at it_tesc
@@ -528,21 +570,7 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
     /* magnitudes */
     if (mags || fband_out) {
         double *fobs = (fin == tmp) ? tot : tmp;   /* reuse the free buffer */
-        for (int j = 0; j < ns; ++j) {
-            double v;
-            if (fabs(zr) > SAFE_FLOOR) {
-                double target = g->lam[j] / (1.0 + zr);
-                int il = oracle_find_interval(g->lam, ns, target);
-                if (il < 1) il = 1;
-                if (il > ns - 1) il = ns - 1;
-                double t = (target - g->lam[il - 1]) / (g->lam[il] - g->lam[il - 1]);
-                v = fin[il - 1] + t * (fin[il] - fin[il - 1]);
-            } else {
-                v = fin[j];
-            }
-            if (v != v) v = 0.0;
-            fobs[j] = (v > 0.0 ? v : 0.0) * (g->lam[j] > DBL_MIN ? 1.0 / g->lam[j] : 0.0);
-        }
+        oracle_observed_frame(ns, g->lam, zr, fin, fobs);
         double dist = oracle_distance_term(g->zt, g->dl, zr);
         double zp = AB_ZEROPOINT + 2.5 * abs_mag_zeropoint_log();
         for (int b = 0; b < g->nbands; ++b) {
@@ -551,11 +579,9 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
             for (int j = 1; j <= ns; ++j) if (bd[j - 1] != 0.0) { if (j < ilo) ilo = j; if (j > ihi) ihi = j; }
             int jlo = ilo - 1 > 1 ? ilo - 1 : 1, jhi = ihi < ns - 1 ? ihi : ns - 1;
             if (ilo > ihi) { jlo = 1; jhi = 0; }
-            double s = 0.0;
-            for (int j = jlo; j <= jhi; ++j) {
-                double wtl = 0.5 * fabs(g->lam[j] - g->lam[j - 1]);
-                s += wtl * (fobs[j - 1] * bd[j - 1] + fobs[j] * bd[j]);
-            }
+            const int on = 1;
+            double s;
+            oracle_band_fluxes(ns, 1, bd, &jlo, &jhi, &on, NULL, g->lam, fobs, &s);
             if (fband_out) fband_out[b] = s;
             if (mags) mags[b] = (s > 0.0 ? -2.5 * log10(s) : NAN) - zp + dist;
         }

@@ -78,6 +78,12 @@ def lib() -> C.CDLL:
         _lib.oracle_kroupa_integral.restype = C.c_double
         _lib.oracle_kroupa_integral.argtypes = [_dp, C.c_double, C.c_double, C.c_int]
         _lib.oracle_abs_mag_zeropoint_log.restype = C.c_double
+        _lib.oracle_lum_distance.restype = C.c_double
+        _lib.oracle_lum_distance.argtypes = [C.c_double] * 4
+        _lib.oracle_observed_frame.argtypes = [C.c_int, _dp, C.c_double, _dp, _dp]
+        _lib.oracle_band_fluxes.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+        _lib.oracle_ssp_weights_raw.argtypes = [_dp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
+                                                C.c_double, C.c_double, C.c_int, C.c_int, _dp]
     return _lib
 
 
@@ -121,6 +127,111 @@ def blend_at_logzsol(data: dict, w: np.ndarray, logzsol: np.ndarray):
         lk = np.where(w[m] > 0, w[m] * 10.0 ** ((1 - dz) * data["ssp_lbol"][zlo] + dz * data["ssp_lbol"][zlo + 1]), 0.0)
         lb[m] = [lk.sum(), lk[young].sum(), lk[~young].sum()]
     return wz, lb
+
+
+def lum_distance(h0: float, om0: float, ol0: float, z: float) -> float:
+    """The luminosity distance [pc] of the oracle's cosmology table (get_luminosity_distance's trapezoid)."""
+    return lib().oracle_lum_distance(float(h0), float(om0), float(ol0), float(z))
+
+
+def observed_frame(lam: np.ndarray, z: float, spec: np.ndarray) -> np.ndarray:
+    """observed_frame_z for one rest-frame spectrum: the observed f_lambda / lambda at the grid's pixels."""
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    fin = np.ascontiguousarray(spec, dtype=np.float64)
+    out = np.empty_like(lam)
+    lib().oracle_observed_frame(lam.size, _p(lam), float(z), _p(fin), _p(out))
+    return out
+
+
+def band_fluxes(bands: np.ndarray, jlo, jhi, do_band, wt: np.ndarray | None, lam: np.ndarray | None,
+                fobs: np.ndarray) -> np.ndarray:
+    """band_fluxes for one model: bands (nb, ns), 1-based supports jlo / jhi, do_band flags, weights wt (ns) or the
+    trapezoid's from lam."""
+    b = np.ascontiguousarray(bands, dtype=np.float64)
+    nb, ns = b.shape
+    jl = np.ascontiguousarray(jlo, dtype=np.int32)
+    jh = np.ascontiguousarray(jhi, dtype=np.int32)
+    db = np.ascontiguousarray(do_band, dtype=np.int32)
+    w = None if wt is None else np.ascontiguousarray(wt, dtype=np.float64)
+    lm = None if lam is None else np.ascontiguousarray(lam, dtype=np.float64)
+    f = np.ascontiguousarray(fobs, dtype=np.float64)
+    out = np.empty(nb)
+    ip = C.POINTER(C.c_int)
+    lib().oracle_band_fluxes(ns, nb, _p(b), jl.ctypes.data_as(ip), jh.ctypes.data_as(ip), db.ctypes.data_as(ip),
+                             _p(w), _p(lm), _p(f), _p(out))
+    return out
+
+
+def ssp_weights_raw(log_t: np.ndarray, sfh_type: int, tage: float, tau: float, idx_min: int, idx_max: int,
+                    tiny_logt: float = 0.0, tq: float = 0.0, tb: float = 0.0) -> np.ndarray:
+    """compute_ssp_weights alone: the hat-kernel mass of SFH type -1/0/1/4 (times in years) on the log-age nodes."""
+    tf = np.ascontiguousarray(log_t, dtype=np.float64)
+    w = np.empty(tf.size)
+    lib().oracle_ssp_weights_raw(_p(tf), tf.size, float(tiny_logt), int(sfh_type), float(tage), float(tau), float(tq),
+                                 float(tb), int(idx_min), int(idx_max), _p(w))
+    return w
+
+
+def smooth_velocity_direct(lam: np.ndarray, spec: np.ndarray, sigma: float, minl: float, maxl: float) -> np.ndarray:
+    """The velocity smoothing as a direct integral (convolve_variable_resolution, the path of smooth_velocity,
+    src/spectra/opensps_smoothing.f90:132-139,365-546): per pixel inside [minl, maxl] the +-4 sigma window found by the
+    same hunting search, weights exp(-(ln lam_i - ln lam_j)^2 / (2 (sigma/c)^2)) / lam_j, the trapezoid integrals of
+    weights and weighted flux over the window, their ratio. Pixels outside, or with fewer than two window pixels,
+    keep their value. Plain loops: small grids only."""
+    lam = np.asarray(lam, dtype=np.float64)
+    spec = np.asarray(spec, dtype=np.float64)
+    n = lam.size
+    out = spec.copy()
+    if n < 2 or sigma <= np.finfo(np.float64).tiny:
+        return out
+    c_kms = 2.99792458e18 * 1.0e-13
+    sig_beta = sigma / c_kms
+    inv2 = 0.5 * (1.0 / sig_beta) ** 2
+    fb, fr = np.exp(-4.0 * sig_beta), np.exp(4.0 * sig_beta)
+    loglam = np.log(lam)
+    dl = lam[1:] - lam[:-1]
+    il = ih = 0                                       # 0-based window bounds
+    for i in range(n):
+        if lam[i] < minl or lam[i] > maxl:
+            continue
+        vl, vh = lam[i] * fb, lam[i] * fr
+        while il > 0 and lam[il] > vl:
+            il -= 1
+        while il < n - 1 and lam[il] < vl:
+            il += 1
+        if il > 0 and lam[il] > vl:
+            il -= 1
+        if ih < il:
+            ih = il
+        while ih > il and lam[ih] > vh:
+            ih -= 1
+        while ih < n - 1 and lam[ih] < vh:
+            ih += 1
+        if ih - il + 1 < 2:
+            continue
+        w = np.exp(-inv2 * (loglam[i] - loglam[il:ih + 1]) ** 2) / lam[il:ih + 1]
+        tw = 0.5 * np.dot(w[:-1] + w[1:], dl[il:ih])
+        if tw <= np.finfo(np.float64).tiny:
+            continue
+        wf = w * spec[il:ih + 1]
+        out[i] = 0.5 * np.dot(wf[:-1] + wf[1:], dl[il:ih]) / tw
+    return out
+
+
+def smooth_velocity_kernel(lam: np.ndarray, spec: np.ndarray, sigma: float, minl: float, maxl: float) -> np.ndarray:
+    """The same smoothing through the oracle's sparse velocity operator (build_velocity_kernel /
+    apply_velocity_kernel, opensps_smoothing.f90:553-651): rows of normalised trapezoid coefficients."""
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    spec = np.asarray(spec, dtype=np.float64)
+    out = spec.copy()
+    lo = C.c_int(0)
+    coef = np.empty(lam.size)
+    for i in range(lam.size):
+        nt = lib().oracle_velocity_row(lam.size, _p(lam), float(sigma), float(minl), float(maxl), i, C.byref(lo),
+                                       _p(coef), lam.size)
+        if nt > 0:
+            out[i] = np.dot(coef[:nt], spec[lo.value:lo.value + nt])
+    return out
 
 
 def expi(x: float) -> float:

@@ -142,6 +142,19 @@ static void ssp_weights(const double *tf, int nt, double tiny_logt, const sfh_t 
     }
 }
 
+/* compute_ssp_weights alone (tests): SFH type -1 (burst), 0, 1 or 4 with times in years (tage, tau, tq the truncation
+ * lookback, tb the burst lookback), the 1-based index range idx_min .. idx_max and tiny_logt; w has nt entries. */
+void oracle_ssp_weights_raw(const double *tf, int nt, double tiny_logt, int type, double tage, double tau, double tq,
+                            double tb, int idx_min, int idx_max, double *w) {
+    sfh_t s;
+    s.type = type;
+    s.tage = tage;
+    s.tau = tau;
+    s.tq = tq;
+    s.tb = tb;
+    ssp_weights(tf, nt, tiny_logt, &s, idx_min, idx_max, w);
+}
+
 /* SFH parameters per model, in this order (Gyr where timed): tage, tau, const, fburst, tburst, sf_start, sf_trunc. */
 enum { SP_TAGE = 0, SP_TAU, SP_CONST, SP_FBURST, SP_TBURST, SP_SF_START, SP_SF_TRUNC, SP_COUNT };
 
