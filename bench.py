@@ -439,8 +439,7 @@ def dust_emission_measure(ctx, params, h_wz, args, barrier) -> dict | None:
     synth_dust.generate()
     synth_dust.generate_agn()
     rng = np.random.default_rng(77)
-    # (frac_obrun stays 0 as in the headline batch: above 0, with nebular emission, the escaping ionizing light of
-    # the nebular ages takes the per-model epilogue path of its own)
+    # (frac_obrun stays 0 as in the headline batch; the escaping ionizing light above 0 has its own leg)
     p = dict(params, dust1=rng.uniform(0.1, 1.0, n), dust3=rng.uniform(0.0, 0.4, n),
              duste_qpah=rng.uniform(0.5, 4.5, n),
              duste_umin=rng.uniform(0.1, 25.0, n), duste_gamma=rng.uniform(0.0, 0.5, n),
@@ -460,6 +459,45 @@ def dust_emission_measure(ctx, params, h_wz, args, barrier) -> dict | None:
         ctx.set_int("add_agn_dust", 0)
     return {"batch": n, "unit": "models/s", "e2e": n / (ms * 1e-3), "ms_per_step": ms,
             "workload": "headline batch + dust emission (7 q_PAH x 22 U_min templates) + AGN torus (9 tau)"}
+
+
+def escaping_light_measure(ctx, params, h_wz, args, barrier, torch) -> dict | None:
+    """The headline batch with frac_obrun uniform in 0-0.5: the nebular ages' escaping ionizing light (nebular
+    emission's gas absorption with an escaping fraction per model) as extra K blocks of the contraction on the pixel
+    tiles below 912 A. Timed end to end through the C API from the same pinned host weights as the headline e2e, and
+    device-resident (opensps_gb300_batch_device, CUDA events on the library's stream)."""
+    from libopensps_gb300 import workloads
+    n = h_wz.shape[0]
+    if args.ion_steps <= 0:
+        return None
+    rng = np.random.default_rng(78)
+    p = dict(params, frac_obrun=rng.uniform(0.0, 0.5, n))
+    for i in range(args.warmup + args.ion_steps):
+        if i == args.warmup:
+            barrier()
+            t0 = time.perf_counter()
+        ctx.csp_batch(p, ssp_weights_z=h_wz, spec=False)
+    barrier()
+    ms = (time.perf_counter() - t0) * 1e3 / args.ion_steps
+    d_wz = torch.from_numpy(h_wz).to("cuda")
+    d_par = torch.from_numpy(workloads.device_param_table(p, n)).to("cuda")
+    d_mags = torch.empty((n, ctx.nbands), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        ctx.batch_device(n, d_par.data_ptr(), d_wz.data_ptr(), d_mags.data_ptr(), sync=False)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.ion_steps):
+        ctx.batch_device(n, d_par.data_ptr(), d_wz.data_ptr(), d_mags.data_ptr(), sync=False)
+    e1.record(stream)
+    barrier()
+    dms = e0.elapsed_time(e1) / args.ion_steps
+    del d_wz, d_par, d_mags
+    return {"batch": n, "unit": "models/s", "e2e": n / (ms * 1e-3), "ms_per_step": ms,
+            "device_value": n / (dms * 1e-3), "device_ms": dms,
+            "workload": "headline batch with frac_obrun uniform 0-0.5 (the nebular ages' escaping ionizing light: 420 "
+                        "more K columns of the contraction on the 17 pixel tiles below 912 A)"}
 
 
 def run_ours(args) -> None:
@@ -551,6 +589,7 @@ def run_ours(args) -> None:
     in_place = ctx.last_input_in_place()
     del h_wz_pageable
     dust_em = dust_emission_measure(ctx, params, h_wz_np, args, barrier)
+    esc = escaping_light_measure(ctx, params, h_wz_np, args, barrier, torch)
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
@@ -595,6 +634,8 @@ def run_ours(args) -> None:
             "sfh_config": sfh_cfg,
             "emulator": emulator,
             "dust_emission": dict(dust_em, over_plain_e2e=dust_em["e2e"] / (n / (e2e_ms * 1e-3))) if dust_em else None,
+            "escaping_light": dict(esc, e2e_ms_over_plain=esc["ms_per_step"] / e2e_ms,
+                                   device_ms_over_plain=esc["device_ms"] / ms_step) if esc else None,
             "gpu_launches": launches * args.steps,
             "clocks": clk,
         }
@@ -624,6 +665,7 @@ def main():
     ap.add_argument("--emu-steps", type=int, default=20)
     ap.add_argument("--emu-e2e-steps", type=int, default=2)
     ap.add_argument("--dust-steps", type=int, default=10)
+    ap.add_argument("--ion-steps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

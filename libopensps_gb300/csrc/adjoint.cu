@@ -515,14 +515,15 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
 __host__ __device__ int adj_row_pad(int ns) { return (ns + 8 + 3) / 4 * 4; }
 
 // ---------------------------------------------------------------------------------------------- transposed basis
-// t(k, p) = basis(p, k): kpad x ppad from ns x kpad (zero for p >= ns), 32 x 32 tiles through shared memory.
+// t(k, p) = basis(p, k): kpad x ppad from the first kpad columns of ns rows of ld (zero for p >= ns), 32 x 32 tiles
+// through shared memory.
 __global__ void transpose_bf16_kernel(const __nv_bfloat16 *__restrict__ src, __nv_bfloat16 *__restrict__ dst, int ns,
-                                      int kpad, int ppad) {
+                                      int kpad, int ld, int ppad) {
     __shared__ __nv_bfloat16 tile[32][33];
     const int k0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int p = p0 + r, k = k0 + threadIdx.x;
-        tile[r][threadIdx.x] = (p < ns && k < kpad) ? src[(size_t)p * kpad + k] : __float2bfloat16_rn(0.f);
+        tile[r][threadIdx.x] = (p < ns && k < kpad) ? src[(size_t)p * ld + k] : __float2bfloat16_rn(0.f);
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
@@ -651,7 +652,9 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         return ST_DATA_MISSING;
     }
     cudaStream_t s = c.stream;
-    const int kpad = ops ? 0 : bop->kpad;
+    // (the weights' cotangent is over the young and old columns: the escaping light's columns repeat nebular entries,
+    // whose reverse is ion_rev_kernel's; ld_basis is the forward operand's row length)
+    const int kpad = ops ? 0 : bop->kmain, ld_basis = ops ? 0 : bop->kpad;
 
     // ---- the transposed library (once per operator): the B operand of the template cotangents' GEMM
     if (ops && !c.ops.lib_thi.p) {
@@ -664,8 +667,8 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
             return ST_DATA_MISSING;
         }
         const dim3 grid((o.ntpad + 31) / 32, (ppad + 31) / 32), block(32, 8);
-        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_hi.p, o.lib_thi.p, ns, o.ntpad, ppad);
-        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_lo.p, o.lib_tlo.p, ns, o.ntpad, ppad);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_hi.p, o.lib_thi.p, ns, o.ntpad, o.ntpad, ppad);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(o.lib_lo.p, o.lib_tlo.p, ns, o.ntpad, o.ntpad, ppad);
         if ((e = cudaGetLastError()) != cudaSuccess ||
             (e = encode_tmap_2d_bf16(&o.tm_lib_thi, o.lib_thi.p, ppad, o.ntpad, gemm_bk(), gemm_bn())) != cudaSuccess ||
             (e = encode_tmap_2d_bf16(&o.tm_lib_tlo, o.lib_tlo.p, ppad, o.ntpad, gemm_bk(), gemm_bn())) != cudaSuccess) {
@@ -684,7 +687,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
             return ST_DATA_MISSING;
         }
         for (int k = 0; k < kpad; ++k)
-            if (kmap[k] >= 0) col_of[kmap[k] & 0x3fffffff] = k;
+            if (kmap[k] >= 0) col_of[kmap[k] & KMAP_SRC] = k;
         if ((e = bop->thi.reserve((size_t)kpad * ppad)) != cudaSuccess ||
             (e = bop->tlo.reserve((size_t)kpad * ppad)) != cudaSuccess ||
             (e = bop->col_of.reserve(ntz)) != cudaSuccess ||
@@ -694,8 +697,8 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
             return ST_DATA_MISSING;
         }
         const dim3 grid((kpad + 31) / 32, (ppad + 31) / 32), block(32, 8);
-        transpose_bf16_kernel<<<grid, block, 0, s>>>(bop->hi.p, bop->thi.p, ns, kpad, ppad);
-        transpose_bf16_kernel<<<grid, block, 0, s>>>(bop->lo.p, bop->tlo.p, ns, kpad, ppad);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(bop->hi.p, bop->thi.p, ns, kpad, ld_basis, ppad);
+        transpose_bf16_kernel<<<grid, block, 0, s>>>(bop->lo.p, bop->tlo.p, ns, kpad, ld_basis, ppad);
         if ((e = cudaGetLastError()) != cudaSuccess ||
             (e = encode_tmap_2d_bf16(&bop->tm_thi, bop->thi.p, ppad, kpad, gemm_bk(), gemm_bn())) != cudaSuccess ||
             (e = encode_tmap_2d_bf16(&bop->tm_tlo, bop->tlo.p, ppad, kpad, gemm_bk(), gemm_bn())) != cudaSuccess) {

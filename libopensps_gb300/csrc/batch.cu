@@ -253,10 +253,16 @@ void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<
     }
 }
 
-static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double line_sigma, std::string &err) {
+// The contraction's basis operand for a K order (accumulators, dust_tesc's age, nebular lines at a line width), cached
+// on the context. With ion (nebular emission and some model's frac_obrun above 0) two more K blocks follow the young
+// and old ones: the nebular ages' unabsorbed ionizing spectra (the library's spectra at pixels below whlylim, zero
+// above), ages below itesc then the rest, against the weights times each model's escaping fraction.
+static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double line_sigma, bool ion,
+                               std::string &err) {
     union { double d; long long i; } u;
     u.d = neb ? line_sigma : -1.0;
-    const long long key = (u.i * 31 + (long long)nacc) * 1009 + itesc;
+    ion = ion && neb && c.nt_neb > 0 && c.whlylim > 0;
+    const long long key = ((u.i * 31 + (long long)nacc) * 1009 + itesc) * 2 + (ion ? 1 : 0);
     auto it = c.basis_cache.find(key);
     if (it != c.basis_cache.end()) return it->second;
     const int ns = c.nspec, nt = c.nt, nz = c.nz;
@@ -272,16 +278,30 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
     if (nacc == 1) {
         op->nty = 0;
         op->ky_pad = 0;
-        op->kpad = pad(nt * nz);
+        op->kmain = pad(nt * nz);
     } else {
         op->nty = itesc;
         op->ky_pad = pad(itesc * nz);
-        op->kpad = op->ky_pad + pad((nt - itesc) * nz);
+        op->kmain = op->ky_pad + pad((nt - itesc) * nz);
     }
+    // the escaping light's blocks: nebular ages below itesc (ty_end of them), then the other nebular ages
+    const int ty_end = ion ? std::min(c.nt_neb, itesc) : 0, n_ion_old = ion ? c.nt_neb - ty_end : 0;
+    op->ion = ion;
+    op->kion_y = pad(ty_end * nz);
+    op->kion_o = pad(n_ion_old * nz);
+    op->kpad = op->kmain + op->kion_y + op->kion_o;
     const int kpad = op->kpad;
     std::vector<uint16_t> hi((size_t)ns * kpad, 0), lo((size_t)ns * kpad, 0);
-    std::vector<int> kmap(kpad, -1);   // operand column -> source index t + nt z, bit 30: a young age
-    for (int k = 0; k < kpad; ++k) {
+    std::vector<int> kmap(kpad, -1);   // operand column -> source index t + nt z with the KMAP_ flags
+    auto put = [&](int k, const double *col, int jn) {
+        for (int j = 0; j < jn; ++j) {
+            const float f = (float)col[j];
+            const uint16_t h = f32_to_bf16_bits(f);
+            hi[(size_t)j * kpad + k] = h;
+            lo[(size_t)j * kpad + k] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));
+        }
+    };
+    for (int k = 0; k < op->kmain; ++k) {
         int t = -1, z = -1;
         if (nacc == 1) {
             if (k < nt * nz) { t = k % nt; z = k / nt; }
@@ -292,14 +312,23 @@ static BasisOperand *get_basis(Context &c, int nacc, int itesc, bool neb, double
             if (nto > 0 && kk < nto * nz) { t = itesc + kk % nto; z = kk / nto; }
         }
         if (t < 0) continue;
-        kmap[k] = (t + nt * z) | ((t < itesc) ? 0x40000000 : 0);
-        const double *col = b.data() + (size_t)ns * (t + (size_t)nt * z);
-        for (int j = 0; j < ns; ++j) {
-            const float f = (float)col[j];
-            const uint16_t h = f32_to_bf16_bits(f);
-            hi[(size_t)j * kpad + k] = h;
-            lo[(size_t)j * kpad + k] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));
+        kmap[k] = (t + nt * z) | ((t < itesc) ? KMAP_YOUNG : 0);
+        put(k, b.data() + (size_t)ns * (t + (size_t)nt * z), ns);
+    }
+    // (the library's own spectra at the ionizing pixels: the lines lie above 912 A, and b has these pixels zeroed)
+    const int jion = std::min(c.whlylim, ns);
+    for (int kk = 0; kk < op->kion_y + op->kion_o; ++kk) {
+        int t = -1, z = -1;
+        if (kk < op->kion_y) {
+            if (kk < ty_end * nz) { t = kk % ty_end; z = kk / ty_end; }
+        } else {
+            const int j = kk - op->kion_y;
+            if (j < n_ion_old * nz) { t = ty_end + j % n_ion_old; z = j / n_ion_old; }
         }
+        if (t < 0) continue;
+        const int k = op->kmain + kk;
+        kmap[k] = (t + nt * z) | ((t < itesc) ? KMAP_YOUNG : 0) | KMAP_ION;
+        put(k, c.ssp.data() + (size_t)ns * (t + (size_t)nt * z), jion);
     }
     cudaError_t e;
     if ((e = op->hi.reserve(hi.size())) != cudaSuccess || (e = op->lo.reserve(lo.size())) != cudaSuccess ||
@@ -375,14 +404,14 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // opensps_csp_batch.f90:2726-2750, the basis holding the absorbed case), added per model by the epilogue from the
     // weights on the device
     bool ion_terms = false;
-    if (c.add_neb_emission == 1 && c.nebemlineinspec == 1 && c.nline > 0 && c.nt_neb > 0 && c.whlylim > 0 && c.d_ion.p)
+    if (c.add_neb_emission == 1 && c.nebemlineinspec == 1 && c.nline > 0 && c.nt_neb > 0 && c.whlylim > 0)
         for (int m = 0; m < n && !ion_terms; ++m) ion_terms = par(m, PF_FRAC_OBRUN) > 0.0;
     const bool epi_terms = any_emis || any_agn;
-    const bool epi = epi_terms || ion_terms;         // spectra from the per-model epilogue
+    const bool epi = epi_terms;                      // spectra from the per-model epilogue
     const bool parts_kept = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;   // the caller wants the parts
     const bool parts = parts_kept || epi;
     const bool chunked = !io.dev_inputs && !io.sfh_par && io.wz && c.fp64 == 0 && !c.ops.ready && !parts_kept &&
-                         !ion_terms && n >= 2 * CHUNK;
+                         n >= 2 * CHUNK;
     // chunk k's models (a smaller first chunk, to start the kernels earlier, measured slower: the kernels lose
     // more on the small chunk than its shorter copy saves)
     const int nch = chunked ? (n + CHUNK - 1) / CHUNK : 1;
@@ -515,8 +544,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         err = "the plain FP64 path computes host-input batches' outputs only (no parts, device inputs or gradients)";
         return ST_UNSUPPORTED;
     }
-    if (ion_terms && (c.fp64 != 0 || io.dev_inputs)) {
-        err = "nebular emission with frac_obrun above zero is supported by the mixed batch from host inputs only";
+    if (ion_terms && c.fp64 != 0) {
+        err = "nebular emission with frac_obrun above zero is supported by the mixed batch only";
         return ST_UNSUPPORTED;
     }
     c.last_ion = ion_terms;
@@ -579,7 +608,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const int nacc = nacc2 ? 2 : 1;
     BasisOperand *bop = nullptr;
     if (!ops) {
-        bop = get_basis(c, nacc, itesc, neb, line_sigma, err);
+        bop = get_basis(c, nacc, itesc, neb, line_sigma, ion_terms, err);
         if (!bop) return ST_DATA_MISSING;
     }
 
@@ -743,6 +772,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     wa.parts = (io.mass_young || io.mass_old || io.lbol_young || io.lbol_old) ? 1 : 0;
     wa.itesc = itesc;
     wa.grid = 0;
+    wa.mpar = (bop && bop->ion) ? c.d_mpar.p : nullptr;   // (the escaping fraction of the escaping-light columns)
     float *d_y = c.d_young.p, *d_o = c.d_old.p;
     const bool want_mags = io.mags != nullptr && !c.fast_mode && nb > 0;
     // bands and magnitudes of models [off, off + nk)
@@ -771,21 +801,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     // (models [off, off + nk))
     auto epilogue = [&](const float *y, const float *o, int off, int nk) -> cudaError_t {
         PartsEpilogueArgs pe;
-        if (ion_terms) {
-            // the nebular ages' sums at the ionizing pixels of models [off, off + nk), then added in the epilogue
-            IonSumsArgs ia;
-            ia.n = nk; ia.whl = c.whlylim; ia.ntneb = c.nt_neb; ia.nt = nt; ia.nz = nz; ia.itesc = itesc;
-            ia.ion = c.d_ion.p; ia.wz = d_wz + (size_t)nt * nz * off;
-            const size_t nw = (size_t)nz * c.nt_neb * nk;
-            cudaError_t r = c.d_ione.reserve((size_t)2 * nk * c.whlylim + nw);
-            if (r != cudaSuccess) return r;
-            ia.ey = c.d_ione.p; ia.eo = c.d_ione.p + (size_t)nk * c.whlylim; ia.wn = ia.eo + (size_t)nk * c.whlylim;
-            if ((r = run_ion_sums(ia, st)) != cudaSuccess) return r;
-            ++launches;
-            pe.ion_ey = ia.ey; pe.ion_eo = ia.eo; pe.whl = c.whlylim;
-            pe.ion_young = const_cast<float *>(y) + (size_t)ns * off;
-            pe.ion_old = const_cast<float *>(o) + (size_t)ns * off;
-        }
         pe.n = nk; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
         pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
         pe.young = y + (size_t)ns * off; pe.old = o + (size_t)ns * off;
@@ -809,10 +824,17 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             WeightsArgs w = wa;
             w.n_models = nk; w.wz = d_wz + (size_t)nt * nz * off; w.w_hi = c.d_whi.p + (size_t)kpad * off;
             w.w_lo = c.d_wlo.p + (size_t)kpad * off; w.sums = c.d_sums.p + (size_t)6 * off;
+            if (w.mpar) w.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
             // (the operand and, in the same pass over the FP64 weights, the FP64 mass and L_bol sums; reading the
             // caller's pageable weights in place, on the side stream beside the previous chunk's kernels)
             if (direct) {
                 cudaEvent_t &ev = c.chunk_ev[(off / CHUNK) % Context::NCHUNK_EV];
+                // (escaping-light columns read the chunk's model parameters, formed on the batch's stream)
+                if (w.mpar && ((e = cudaEventRecord(c.ev_params, st)) != cudaSuccess ||
+                               (e = cudaStreamWaitEvent(c.side, c.ev_params, 0)) != cudaSuccess)) {
+                    err = cuda_msg("weights kernel", e);
+                    return ST_DATA_MISSING;
+                }
                 if ((!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) ||
                     (e = run_weights_convert_sums(w, c.side)) != cudaSuccess || (e = cudaEventRecord(ev, c.side)) != cudaSuccess ||
                     (e = cudaStreamWaitEvent(st, ev, 0)) != cudaSuccess) {
@@ -837,8 +859,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             ca.nspec = ns; ca.n_models = nk;
             ca.n_ptiles = (ns + contract_out_rows() - 1) / contract_out_rows();
             ca.n_mtiles = (nk + bn - 1) / bn;
-            ca.nkb_young = (nacc == 1) ? kpad / contract_bk() : bop->ky_pad / contract_bk();
-            ca.nkb_old = (nacc == 1) ? 0 : (kpad - bop->ky_pad) / contract_bk();
+            ca.nkb_young = (nacc == 1) ? bop->kmain / contract_bk() : bop->ky_pad / contract_bk();
+            ca.nkb_old = (nacc == 1) ? 0 : (bop->kmain - bop->ky_pad) / contract_bk();
+            ca.nkb_ion_young = bop->kion_y / contract_bk();
+            ca.nkb_ion_old = bop->kion_o / contract_bk();
+            ca.ion_pix = bop->ion ? c.whlylim : 0;
             ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
             // (with dust emission or AGN the per-model epilogue forms the spectra from the young and old sums)
             ca.spec = epi ? nullptr : c.d_spec.p + (size_t)ns * off;

@@ -54,9 +54,12 @@ struct DevBuf {
 
 // The contraction's basis operand for one K order (bf16 hi and lo, pixels x kpad).
 struct BasisOperand {
-    int nacc = 0, itesc = 0, kpad = 0, ky_pad = 0, nty = 0;
+    // K columns: [young block (ky_pad) | old block | escaping-light young block (kion_y) | escaping-light old block
+    // (kion_o)]; kmain = the young and old blocks, kpad = all (the blocks padded to the contraction's K step)
+    int nacc = 0, itesc = 0, kpad = 0, ky_pad = 0, nty = 0, kmain = 0, kion_y = 0, kion_o = 0;
+    bool ion = false;
     DevBuf<__nv_bfloat16> hi, lo;
-    DevBuf<int> kmap;            // operand column -> source (age, metallicity) of the weights, bit 30: young
+    DevBuf<int> kmap;            // operand column -> source (age, metallicity) of the weights with the KMAP_ flags
     CUtensorMap tm_hi, tm_lo;
     bool neb = false;
     double line_sigma = 0.0;
@@ -160,7 +163,7 @@ struct Context {
     // nebular emission's gas absorption: ages 0..nt_neb-1 carry nebular emission, pixels 0..whlylim-1 are ionizing
     // (below 912 A); d_ion holds those ages' ionizing pixels of the library, (z nt_neb + t) x whlylim FP32
     int nt_neb = 0, whlylim = 0;
-    DevBuf<float> d_ion, d_ione;     // d_ione: a batch's sums of the nebular ages at those pixels (2 x n x whlylim) and its compact weights
+    DevBuf<float> d_ion;
     bool last_ion = false;           // the last batch added the escaping ionizing light (its reverse pass follows)
     std::vector<int> mag_mask;   // empty: all bands
 

@@ -30,8 +30,10 @@ __device__ __forceinline__ float weight_to_f32(double w) {
 }
 
 // The operand and, from the same FP64 weights, the FP64 sums of model_sums_zw (one warp per model, the sums in the
-// operand's column order; young ages by the column map's bit 30): the sums ride the FP64 pipe while the conversion
-// waits on memory, instead of a second pass over the weights bound by that pipe.
+// operand's column order; young ages by the column map's KMAP_YOUNG bit): the sums ride the FP64 pipe while the
+// conversion waits on memory, instead of a second pass over the weights bound by that pipe. Escaping-light columns
+// (KMAP_ION) carry the weight times the model's escaping fraction clamp(frac_obrun, 0, 1) (nebular_kernels step 2,
+// OpenSPS src/physics/opensps_csp_batch.f90:2726-2750, with fesc of batch_nebular_indices :1696) and join no sum.
 template <bool PARTS>
 __global__ void __launch_bounds__(256) weights_convert_sums_kernel(WeightsArgs a) {
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -40,20 +42,23 @@ __global__ void __launch_bounds__(256) weights_convert_sums_kernel(WeightsArgs a
     const double *w = a.wz + (size_t)m * a.nt * a.nz;
     __nv_bfloat16 *hi = a.w_hi + (size_t)m * a.kpad, *lo = a.w_lo + (size_t)m * a.kpad;
     double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
+    const float fesc = a.mpar ? fminf(fmaxf(__ldg(a.mpar + (size_t)m * MODEL_PAR_FLOATS + MP_FO), 0.f), 1.f) : 0.f;
 #pragma unroll 4
     for (int k = lane; k < a.kpad; k += 32) {
         const int code = __ldg(a.kmap + k);
         float wf = 0.f;
         if (code >= 0) {
-            const int idx = code & 0x3fffffff;
+            const int idx = code & KMAP_SRC;
             const double wv = __ldg(w + idx);
             wf = weight_to_f32(wv);
-            if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
+            if (code & KMAP_ION) {
+                wf *= fesc;
+            } else if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
                 const double mk = __ldg(a.mass + idx), lk = __ldg(a.llin + idx);
                 ms = fma(wv, mk, ms);
                 ls = fma(wv, lk, ls);
                 if (PARTS) {
-                    if (code & 0x40000000) { msy = fma(wv, mk, msy); lsy = fma(wv, lk, lsy); }
+                    if (code & KMAP_YOUNG) { msy = fma(wv, mk, msy); lsy = fma(wv, lk, lsy); }
                     else { mso = fma(wv, mk, mso); lso = fma(wv, lk, lso); }
                 }
             }

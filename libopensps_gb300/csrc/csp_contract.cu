@@ -23,6 +23,11 @@
 //
 // NACC = 1: one accumulator (no birth-cloud or old-star screen in the batch: young and old are only ever summed).
 // NACC = 2: young and old accumulators (the K range is ordered young block first, then old block).
+// Nebular emission's escaping ionizing light (frac_obrun above 0, nebular_kernels step 2 of OpenSPS,
+// src/physics/opensps_csp_batch.f90:2726-2750): the basis holds the nebular ages' ionizing pixels absorbed (zero), and
+// extra K blocks after the old block hold those ages' unabsorbed ionizing spectra against the weights times each
+// model's escaping fraction; the ion young blocks accumulate into the young sums and the ion old blocks into the old
+// ones. Only the pixel tiles that reach an ionizing pixel run them.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cstdint>
@@ -100,6 +105,9 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
     const int n_ptiles = args.n_ptiles;
     const int n_tiles = n_ptiles * args.n_mtiles;
     const int nkb = args.nkb_young + args.nkb_old;
+    const int nkb_ion = args.nkb_ion_young + args.nkb_ion_old;
+    // K blocks of pixel tile pt: the escaping-light blocks only where the tile reaches an ionizing pixel
+    auto tile_nkb = [&](int pt) { return (nkb_ion > 0 && pt * OUT_ROWS - HALO < args.ion_pix) ? nkb + nkb_ion : nkb; };
     int *status = args.status;
 
     if (threadIdx.x == 0) {
@@ -128,7 +136,8 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
             for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
                 const int mt = tile / n_ptiles, pt = tile % n_ptiles;
                 const int p0 = pt * OUT_ROWS - HALO, m0 = mt * C::BN;
-                for (int kb = 0; kb < nkb; ++kb) {
+                const int kbn = tile_nkb(pt);
+                for (int kb = 0; kb < kbn; ++kb) {
                     if (!mbar_wait(&empty[s], ph ^ 1u, status, ERR_TIMEOUT_PRODUCER)) { ok = false; break; }
                     uint8_t *st = stage_base + s * C::STAGE_BYTES;
                     mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
@@ -154,12 +163,17 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
                 if (!mbar_wait(&tempty[acc], aph ^ 1u, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t d_base = tmem_base + acc * C::ACC_COLS;
-                for (int kb = 0; kb < nkb; ++kb) {
+                const int kbn = tile_nkb(tile % n_ptiles);
+                for (int kb = 0; kb < kbn; ++kb) {
                     if (!mbar_wait(&full[s], ph, status, ERR_TIMEOUT_MMA)) { ok = false; break; }
                     tc_fence_after();
-                    const int which = (NACC == 2 && kb >= args.nkb_young) ? 1 : 0;
+                    // the accumulator of block kb: young / old blocks, then the escaping light's young / old blocks
+                    // (which always add to sums their own range has begun: a young ion block exists only with young
+                    // ages, an old one only with old ages)
+                    const bool ion_old = kb >= nkb + args.nkb_ion_young;
+                    const int which = (NACC == 2 && ((kb >= args.nkb_young && kb < nkb) || ion_old)) ? 1 : 0;
                     const uint32_t d = d_base + which * C::BN;
-                    const int kfirst = (which == 0) ? 0 : args.nkb_young;
+                    const int kfirst = kb >= nkb ? -1 : (which == 0) ? 0 : args.nkb_young;
                     const uint32_t sa = smem_u32(stage_base + s * C::STAGE_BYTES);
                     const uint32_t a_hi = sa, a_lo = sa + C::A_BYTES;
                     const uint32_t b_hi = sa + 2 * C::A_BYTES, b_lo = b_hi + C::B_BYTES;

@@ -58,8 +58,18 @@ enum {
     MODEL_PAR_FLOATS = 32
 };
 
+// The operand's column map (BasisOperand::kmap, WeightsArgs::kmap): per K column the source index t + nt z of the
+// weights, with flag bits; -1: padding.
+constexpr int KMAP_YOUNG = 0x40000000;   // a young age (t < itesc)
+constexpr int KMAP_ION = 0x20000000;     // an escaping-light column: the weight times the model's clamp(frac_obrun, 0, 1)
+constexpr int KMAP_SRC = 0x1fffffff;     // the source index
+
 struct ContractArgs {
     int nspec, n_models, n_ptiles, n_mtiles, nkb_young, nkb_old, jtop, ld_spec;
+    // nebular emission's escaping ionizing light: K blocks after the young and old ones (ion young blocks into the
+    // young accumulator, then ion old blocks into the old one), run only by the pixel tiles that reach a pixel below
+    // ion_pix (the ionizing pixels; the basis holds those columns' unabsorbed spectra there and zeros above)
+    int nkb_ion_young = 0, nkb_ion_old = 0, ion_pix = 0;
     int sm_lo, sm_hi;    // pixels smoothed (lambda within [min_wave_smooth, max_wave_smooth]); sm_lo > sm_hi: none
     int uniform_index;   // every model has the dust_index of the pixel table's curve
     const float *pix;    // nspec x PIX_FLOATS
@@ -85,7 +95,8 @@ cudaError_t run_contract(int nacc, const ContractPlan &pl, const ContractArgs &a
 // per-model sums (mass, L_bol linear, young and old parts).
 struct WeightsArgs {
     int n_models, nt, nz, kpad;
-    const int *kmap;        // kpad: source index t + nt z of operand column k (bit 30 set: a young age), -1: padding
+    const int *kmap;        // kpad: source index t + nt z of operand column k with the KMAP_ flags, -1: padding
+    const float *mpar = nullptr;   // n_models x MODEL_PAR_FLOATS: frac_obrun of the KMAP_ION columns (null: none)
     const double *wz;       // n_models x (nt x nz), age fastest
     const double *mass;     // nt x nz
     const double *llin;     // nt x nz: 10^log L_bol
@@ -321,25 +332,8 @@ struct PartsEpilogueArgs {
     const float *agn_spec = nullptr;
     const double *lsum = nullptr;
     int lsum_stride = 6;
-    // nebular emission's escaping ionizing light (ion_ey null: none): clamp(frac_obrun, 0, 1) times the nebular
-    // ages' sums at the ionizing pixels (n x whl, young and old: ion_sums_kernel)
-    const float *ion_ey = nullptr, *ion_eo = nullptr;
-    int whl = 0;
-    float *ion_young = nullptr, *ion_old = nullptr;   // the young and old sums with it, written back at those pixels
 };
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
-
-// The nebular ages' sums at the ionizing pixels: ey / eo (n x whl) = sum over k = (z, t < ntneb) of the weights wz
-// (n x nz x nt FP64, floored at SAFE_FLOOR) times ion ((z ntneb + t) x whl), ages below itesc into ey.
-struct IonSumsArgs {
-    int n, whl, ntneb, nt, nz, itesc;
-    const float *ion;
-    const double *wz;
-    float *ey, *eo;
-    float *wn = nullptr;     // scratch: nz ntneb x n, the weights gathered compact (set by the caller)
-    int wn_ld = 0;           // its row stride (set by run_ion_sums)
-};
-cudaError_t run_ion_sums(const IonSumsArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

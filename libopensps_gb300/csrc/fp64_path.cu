@@ -25,7 +25,7 @@ __global__ void gather_w64_kernel(int n, int kpad, int ntz, const int *kmap, con
     const int code = kmap[k];
     double v = 0.0;
     if (code >= 0) {
-        const double w = wz[(size_t)m * ntz + (code & 0x3fffffff)];
+        const double w = wz[(size_t)m * ntz + (code & KMAP_SRC)];
         v = (w > SAFE_FLOOR) ? w : 0.0;   // (model_sums_zw: weights at or below SAFE_FLOOR are skipped)
     }
     w64[i] = v;
@@ -234,7 +234,7 @@ int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double
         }
         for (int k = 0; k < kpad; ++k)
             if (kmap[k] >= 0)
-                std::copy(b.data() + (size_t)ns * (kmap[k] & 0x3fffffff), b.data() + (size_t)ns * ((kmap[k] & 0x3fffffff) + 1),
+                std::copy(b.data() + (size_t)ns * (kmap[k] & KMAP_SRC), b.data() + (size_t)ns * ((kmap[k] & KMAP_SRC) + 1),
                           kb.data() + (size_t)ns * k);
         if ((e = bop->b64.reserve(kb.size())) != cudaSuccess ||
             (e = cudaMemcpy(bop->b64.p, kb.data(), sizeof(double) * kb.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {

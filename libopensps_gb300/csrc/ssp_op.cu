@@ -812,19 +812,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     if (a.dem) dm = a.dem[m];
     const bool emis = a.dem != nullptr && dm.on != 0;
     const bool agn = a.dem != nullptr && dm.agn != 0;
-    // the escaping ionizing light of the nebular ages: fesc times their sums at ionizing pixel p (ion_sums_kernel),
-    // into y (ages below itesc) and o
-    const float fesc = fminf(fmaxf(fo, 0.f), 1.f);
-    const bool ion = a.ion_ey != nullptr && fesc > 0.f;
-    auto ion_add = [&](int p, float &y, float &o) {
-        y = fmaf(fesc, __ldg(a.ion_ey + (size_t)m * a.whl + p), y);
-        o = fmaf(fesc, __ldg(a.ion_eo + (size_t)m * a.whl + p), o);
-        // (the stored sums as the reverse pass reads them: each pixel's own thread read it above)
-        if (a.ion_young) {
-            a.ion_young[(size_t)m * a.nspec + p] = y;
-            a.ion_old[(size_t)m * a.nspec + p] = o;
-        }
-    };
     // the AGN's luminosity: fagn times the model's L_bol (add_agn_batch :4342-4433, the value the batch outputs;
     // 1 when it is not above SAFE_FLOOR, as log10 L_bol is then 0)
     float lagn = 0.f;
@@ -904,8 +891,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
                     g1 = __ldg(gb + q);
                 }
                 float e0 = 0.f, e1 = 0.f;
-                if (ion && 2 * q < a.whl) ion_add(2 * q, yy[u].x, oo[u].x);
-                if (ion && 2 * q + 1 < a.whl) ion_add(2 * q + 1, yy[u].y, oo[u].y);
                 const float t0 = pass1(2 * q, yy[u].x, oo[u].x, sh.x, cn.x, g0.x, g1.x, e0);
                 const float t1 = pass1(2 * q + 1, yy[u].y, oo[u].y, sh.y, cn.y, g0.y, g1.y, e1);
                 reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
@@ -915,7 +900,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     } else {
         for (int p = threadIdx.x; p < ns; p += bd) {
             float esc = 0.f, y = __ldg(yv + p), o = __ldg(ov + p);
-            if (ion && p < a.whl) ion_add(p, y, o);
             tsm[p] = pass1(p, y, o, emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
                            emis ? __ldg(a.cnu + p) : 0.f, agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f,
                            agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f, esc);
@@ -960,113 +944,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
         }
         out[p] = v;
     }
-}
-
-// The nebular ages' sums at the ionizing pixels, E(m, p) = sum_k w(m, k) ion(k, p) over k = (z, t < ntneb), split
-// into ages below itesc (young) and the rest (old): a tiled FP32 product, 128 pixels x 64 models per CTA of 128
-// threads, the young and then the old entries as two passes of 32 entries per shared-memory step; thread (tx, ty)
-// holds pixels tx + 16 j and models 8 ty + i (8 x 8 outputs: 16 shared loads per 64 FMA). Weights floored at
-// SAFE_FLOOR as the batch's sums floor them.
-constexpr int ION_TP = 128, ION_TM = 64, ION_TK = 32;
-
-__global__ void __launch_bounds__(128) ion_sums_kernel(IonSumsArgs a) {
-    __shared__ float is[ION_TK][ION_TP];
-    __shared__ float ws[ION_TK][ION_TM];
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int p0 = blockIdx.x * ION_TP, m0 = blockIdx.y * ION_TM;
-    const int ty_end = min(a.ntneb, a.itesc);
-    for (int pass = 0; pass < 2; ++pass) {
-        const int t0 = pass == 0 ? 0 : ty_end, t1 = pass == 0 ? ty_end : a.ntneb, nts = max(t1 - t0, 0);
-        const int K = a.nz * nts;          // this pass's entries: j -> (z = j / nts, t = t0 + j % nts)
-        float acc[8][8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-        for (int k0 = 0; k0 < K; k0 += ION_TK) {
-            __syncthreads();
-            for (int e = tid; e < ION_TK * ION_TP; e += 128) {
-                const int kk = e / ION_TP, pp = e - kk * ION_TP, k = k0 + kk, p = p0 + pp;
-                float v = 0.f;
-                if (k < K && p < a.whl) {
-                    const int z = k / nts, t = t0 + (k - z * nts);
-                    v = __ldg(a.ion + ((size_t)z * a.ntneb + t) * a.whl + p);
-                }
-                is[kk][pp] = v;
-            }
-            const float *wp = a.wn + (size_t)(pass == 0 ? 0 : a.nz * ty_end) * a.wn_ld;   // this pass's compact rows
-            for (int e = tid; e < ION_TK * ION_TM; e += 128) {
-                const int kk = e / ION_TM, mm = e - kk * ION_TM, k = k0 + kk, m = m0 + mm;
-                ws[kk][mm] = (k < K && m < a.n) ? __ldg(wp + (size_t)k * a.wn_ld + m) : 0.f;
-            }
-            __syncthreads();
-            const int kn = min(ION_TK, K - k0);
-            for (int kk = 0; kk < kn; ++kk) {
-                float x[8], w[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) x[j] = is[kk][tx + 16 * j];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) w[i] = ws[kk][8 * ty + i];
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(w[i], x[j], acc[i][j]);
-            }
-        }
-        float *out = pass == 0 ? a.ey : a.eo;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int m = m0 + 8 * ty + i;
-            if (m >= a.n) continue;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int p = p0 + tx + 16 * j;
-                if (p < a.whl) out[(size_t)m * a.whl + p] = acc[i][j];
-            }
-        }
-    }
-}
-
-// The nebular weights gathered once per batch, compact and floored: wn[c n + m], c over the young entries (z, t <
-// min(ntneb, itesc)) then the old ones (z, itesc <= t < ntneb), z outer (the order ion_sums_kernel's passes read).
-__global__ void ion_gather_kernel(IonSumsArgs a) {
-    const int ty_end = min(a.ntneb, a.itesc), K = a.nz * a.ntneb, K0 = a.nz * ty_end;
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (size_t)K * a.n) return;
-    const int c = (int)(i / a.n), m = (int)(i - (size_t)c * a.n);
-    int z, t;
-    if (c < K0) { z = c / ty_end; t = c - z * ty_end; }
-    else { const int nto = a.ntneb - ty_end, j = c - K0; z = j / nto; t = ty_end + (j - z * nto); }
-    const double v = a.wz[(size_t)m * a.nz * a.nt + (size_t)z * a.nt + t];
-    a.wn[(size_t)c * a.wn_ld + m] = v > SAFE_FLOOR ? (float)v : 0.f;
-}
-
-cudaError_t run_ion_sums(const IonSumsArgs &a_in, cudaStream_t st) {
-    if (a_in.n <= 0 || a_in.whl <= 0) return cudaSuccess;
-    IonSumsArgs a = a_in;
-    a.wn_ld = a.n;
-    {
-        const size_t tot = (size_t)a.nz * a.ntneb * a.n;
-        ion_gather_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    // (slices of models within the grid's y limit)
-    const int slice = 65535 * ION_TM;
-    for (int s0 = 0; s0 < a.n; s0 += slice) {
-        IonSumsArgs b = a;
-        b.n = std::min(slice, a.n - s0);
-        b.wz = a.wz + (size_t)s0 * a.nz * a.nt;
-        // (the compact rows keep the whole batch's stride: a slice reads its columns through an offset and n)
-        b.wn = a.wn + s0;
-        b.ey = a.ey + (size_t)s0 * a.whl;
-        b.eo = a.eo + (size_t)s0 * a.whl;
-        const dim3 grid((a.whl + ION_TP - 1) / ION_TP, (b.n + ION_TM - 1) / ION_TM);
-        ion_sums_kernel<<<grid, 128, 0, st>>>(b);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
 }
 
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {

@@ -15,18 +15,22 @@ from conftest import config3_inputs, rel_err_spec
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("igm", [0, 1])
-def test_ionizing_absorption_matches_oracle(data, built_lib, igm):
+@pytest.mark.parametrize("igm,n,birth,tesc", [(0, 32, True, 7.0), (1, 32, True, 7.0), (0, 300, False, 7.0),
+                                               (0, 300, True, 6.5), (1, 300, True, 6.5)])
+def test_ionizing_absorption_matches_oracle(data, built_lib, igm, n, birth, tesc):
     """With the IGM off the ionizing pixels themselves are compared (with it on they fall below the comparison's
-    floor at most redshifts)."""
+    floor at most redshifts). 300 models: several model tiles of the contraction and a ragged last one; without a
+    birth cloud one accumulator (the escaping light in the same sums), with it young and old ones; dust_tesc 7.0 puts
+    every nebular age among the young ones, 6.5 splits them (escaping-light blocks for both)."""
     from libopensps_gb300.capi import Context
     from oracle.oracle import Oracle
-    n = 32
-    wz, params = config3_inputs(n, seed=941)
+    wz, params = config3_inputs(n, seed=941 + n)
     rng = np.random.default_rng(942)
     fo = rng.uniform(0.0, 0.6, n)
     fo[:8] = 0.0
-    params = dict(params, frac_obrun=fo, dust1=rng.uniform(0.0, 0.8, n))
+    params = dict(params, frac_obrun=fo, dust_tesc=np.full(n, tesc))
+    if birth:
+        params["dust1"] = rng.uniform(0.0, 0.8, n)
     c = Context()
     c.set_int("add_neb_emission", 1)
     c.set_int("add_igm_absorption", igm)
@@ -35,6 +39,35 @@ def test_ionizing_absorption_matches_oracle(data, built_lib, igm):
     want = Oracle(data, nbands=40, add_igm=bool(igm)).csp_batch(params, wz)
     assert rel_err_spec(got["spec"], want["spec"]) <= 1e-4
     assert float(np.nanmax(np.abs(got["mags"] - want["mags"]))) <= 1e-3
+
+
+def test_escaping_light_in_chunks_and_from_device_inputs(data, built_lib):
+    """A batch large enough to go up in chunks (40,000 models) with frac_obrun above 0, against the oracle on a sample
+    of models; and the same inputs from device memory (opensps_gb300_batch_device) give the same magnitudes to FP32
+    rounding (1e-4 mag)."""
+    import torch
+    from libopensps_gb300 import workloads
+    from libopensps_gb300.capi import Context
+    from oracle.oracle import Oracle
+    n = 40000
+    wz, params = config3_inputs(n, seed=946)
+    rng = np.random.default_rng(947)
+    params = dict(params, frac_obrun=rng.uniform(0.0, 0.5, n))
+    c = Context()
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    got = c.csp_batch(params, ssp_weights_z=wz, spec=False)
+    idx = np.arange(0, n, 997)
+    want = Oracle(data, nbands=40).csp_batch({k: v[idx] for k, v in params.items()}, wz[idx])
+    assert float(np.nanmax(np.abs(got["mags"][idx] - want["mags"]))) <= 1e-3
+    d_wz = torch.from_numpy(wz).cuda()
+    d_par = torch.from_numpy(workloads.device_param_table(params, n)).cuda()
+    d_mags = torch.empty((n, c.nbands), dtype=torch.float64, device="cuda")
+    c.batch_device(n, d_par.data_ptr(), d_wz.data_ptr(), d_mags.data_ptr(), sync=True)
+    # (the band GEMM splits the pixels over CTAs by the batch's size: 16384-model chunks and one 40,000-model batch
+    # sum the band fluxes in different FP32 orders)
+    np.testing.assert_allclose(d_mags.cpu().numpy(), got["mags"], rtol=0, atol=1e-4)
+    c.close()
 
 
 def test_escaping_fraction_one_is_no_absorption(data, built_lib):
