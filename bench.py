@@ -500,6 +500,44 @@ def escaping_light_measure(ctx, params, h_wz, args, barrier, torch) -> dict | No
                         "more K columns of the contraction on the 17 pixel tiles below 912 A)"}
 
 
+def nebular_continuum_measure(params, h_wz, args, barrier) -> dict | None:
+    """The headline batch with the CLOUDY-grid nebular continuum: a standard-format data root holding the synthetic
+    libraries and a CLOUDY-style grid (nebular/synthetic_nodust, 11 log Z x 10 ages x 7 log U), gas_logz and gas_logu
+    per model, frac_obrun uniform 0-0.4. The continuum joins the young and old sums in the per-model epilogue (the
+    batch's parts path, in 16384-model chunks). Timed end to end through the C API from the same pinned host weights
+    as the headline e2e."""
+    import shutil
+    from libopensps_gb300 import stdformat, synthdata
+    from libopensps_gb300.capi import Context
+    n = h_wz.shape[0]
+    if args.neb_steps <= 0:
+        return None
+    root = Path(tempfile.mkdtemp(prefix="opensps_neb_"))
+    old = os.environ.get("OPENSPS_DATA_HOME")
+    try:
+        stdformat.convert_synthetic(root, src_root=synthdata.default_root(), dust=False, agn=False, nebular=True)
+        c = Context(data_root=root)
+        c.set_int("add_neb_emission", 1)
+        c.set_int("add_igm_absorption", 1)
+        rng = np.random.default_rng(79)
+        p = dict(params, gas_logz=rng.uniform(-2.0, 0.2, n), gas_logu=rng.uniform(-4.0, -1.0, n),
+                 frac_obrun=rng.uniform(0.0, 0.4, n))
+        for i in range(args.warmup + args.neb_steps):
+            if i == args.warmup:
+                barrier()
+                t0 = time.perf_counter()
+            c.csp_batch(p, ssp_weights_z=h_wz, spec=False)
+        barrier()
+        ms = (time.perf_counter() - t0) * 1e3 / args.neb_steps
+        c.close()
+    finally:
+        if old is not None:
+            os.environ["OPENSPS_DATA_HOME"] = old
+        shutil.rmtree(root, ignore_errors=True)
+    return {"batch": n, "unit": "models/s", "e2e": n / (ms * 1e-3), "ms_per_step": ms,
+            "workload": "headline batch + CLOUDY-grid nebular continuum (gas_logz, gas_logu, frac_obrun per model)"}
+
+
 def run_ours(args) -> None:
     import torch
     ws, rank = _dist()
@@ -590,6 +628,7 @@ def run_ours(args) -> None:
     del h_wz_pageable
     dust_em = dust_emission_measure(ctx, params, h_wz_np, args, barrier)
     esc = escaping_light_measure(ctx, params, h_wz_np, args, barrier, torch)
+    neb_cont = nebular_continuum_measure(params, h_wz_np, args, barrier)
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
@@ -634,6 +673,7 @@ def run_ours(args) -> None:
             "sfh_config": sfh_cfg,
             "emulator": emulator,
             "dust_emission": dict(dust_em, over_plain_e2e=dust_em["e2e"] / (n / (e2e_ms * 1e-3))) if dust_em else None,
+            "nebular_continuum": dict(neb_cont, e2e_ms_over_plain=neb_cont["ms_per_step"] / e2e_ms) if neb_cont else None,
             "escaping_light": dict(esc, e2e_ms_over_plain=esc["ms_per_step"] / e2e_ms,
                                    device_ms_over_plain=esc["device_ms"] / ms_step) if esc else None,
             "gpu_launches": launches * args.steps,
@@ -666,6 +706,7 @@ def main():
     ap.add_argument("--emu-e2e-steps", type=int, default=2)
     ap.add_argument("--dust-steps", type=int, default=10)
     ap.add_argument("--ion-steps", type=int, default=10)
+    ap.add_argument("--neb-steps", type=int, default=5)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -401,12 +401,25 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     if (c.add_agn_dust == 1)
         for (int m = 0; m < n && !any_agn; ++m) any_agn = par(m, PF_FAGN) > SAFE_FLOOR;
     // nebular emission's escaping ionizing light (frac_obrun above zero: nebular_kernels step 2,
-    // opensps_csp_batch.f90:2726-2750, the basis holding the absorbed case), added per model by the epilogue from the
-    // weights on the device
+    // opensps_csp_batch.f90:2726-2750, the basis holding the absorbed case): extra K blocks of the contraction
     bool ion_terms = false;
     if (c.add_neb_emission == 1 && c.nebemlineinspec == 1 && c.nline > 0 && c.nt_neb > 0 && c.whlylim > 0)
         for (int m = 0; m < n && !ion_terms; ++m) ion_terms = par(m, PF_FRAC_OBRUN) > 0.0;
-    const bool epi_terms = any_emis || any_agn;
+    // the CLOUDY-grid nebular continuum (nb%cont = neb .and. add_neb_continuum, :1646; nebular_kernels step 3): in the
+    // per-model epilogue, when the data root has the grid of the setup's isochrones (nebular/<isoc>_<nodust|dust>)
+    const int neb_table = c.cloudy_dust == 1 ? 1 : 0;
+    const bool neb_cont = c.add_neb_emission == 1 && c.add_neb_continuum == 1 && c.nt_neb > 0 &&
+                          (c.neb.have[0] || c.neb.have[1]);
+    if (neb_cont && !c.neb.have[neb_table]) {
+        err = "nebular/" + c.isoc + (neb_table ? "_dust" : "_nodust") + " is missing (cloudy_dust = " +
+              std::to_string(c.cloudy_dust) + ")";
+        return ST_DATA_MISSING;
+    }
+    if (neb_cont && c.nt_neb > NEB_MAX_AGES) {
+        err = "the nebular continuum takes at most " + std::to_string(NEB_MAX_AGES) + " nebular ages";
+        return ST_UNSUPPORTED;
+    }
+    const bool epi_terms = any_emis || any_agn || neb_cont;
     const bool epi = epi_terms;                      // spectra from the per-model epilogue
     const bool parts_kept = ((io.young || io.old) && !io.dev_inputs) || io.keep_parts;   // the caller wants the parts
     const bool parts = parts_kept || epi;
@@ -551,9 +564,10 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.last_ion = ion_terms;
     DustEmModel *dem = nullptr;            // the per-model cells, page-locked (uploaded beside the parameter table)
     if (epi_terms) {
-        if (fp64) { err = "dust emission and AGN are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts) { err = "gradients with dust emission or AGN are not supported on this path"; return ST_UNSUPPORTED; }
-        if (io.dev_inputs) { err = "dust emission and AGN need host inputs on this path"; return ST_UNSUPPORTED; }
+        if (fp64) { err = "dust emission, AGN and the nebular continuum are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts) { err = "gradients with dust emission, AGN or the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.dev_inputs) { err = "dust emission, AGN and the nebular continuum need host inputs on this path"; return ST_UNSUPPORTED; }
+        if (neb_cont && c.ops.ready) { err = "the nebular continuum with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
         if (any_emis) { if (int rc = dustem_load(c, err)) return rc; }
         if (any_agn) { if (int rc = agn_load(c, err)) return rc; }
         // dl07_indices (src/physics/opensps_csp_batch.f90:1622-1634): the grid cell in q_PAH and U_min (clamped to
@@ -590,6 +604,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if (q.agn) {
                 cell(c.agn.tau, par(m, PF_AGN_TAU), q.ita, q.wta);
                 q.fagn = (float)par(m, PF_FAGN);
+            }
+            if (neb_cont) {
+                // get_grid_indices_weights (opensps_gas.f90:394-412) in gas_logz and gas_logu; fabs = 1 - frac_obrun
+                // (:1697), its magnitude as the continuum's q = |q0 fabs| takes it (:2795)
+                cell(c.neb.logz, par(m, PF_GAS_LOGZ), q.neb_iz, q.neb_wz);
+                cell(c.neb.logu, par(m, PF_GAS_LOGU), q.neb_iu, q.neb_wu);
+                q.neb_fabs = (float)std::fabs(1.0 - par(m, PF_FRAC_OBRUN));
             }
         }
     }
@@ -808,6 +829,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         pe.dem = d_dem ? d_dem + off : nullptr;
         pe.dtab = c.dustem.tab.p; pe.cnu = c.dustem.cnu.p; pe.nqpah = c.dustem.nqpah;
         pe.agn_spec = c.agn.spec.p;
+        if (neb_cont) {
+            pe.neb_tab = c.neb.tab[neb_table].p; pe.neb_off = c.neb.off.p;
+            pe.neb_age4 = reinterpret_cast<const float4 *>(c.neb.age4.p); pe.neb_q0 = c.neb.q0.p;
+            pe.wz = d_wz + (size_t)nt * nz * off;
+            pe.nt = nt; pe.nz = nz; pe.nt_neb = c.nt_neb; pe.itesc = itesc;
+        }
         // (the model's L_bol output: log-blended between the slabs for weights formed on the device, except with
         // the operators, whose L_bol is their linear row)
         const bool blend = io.sfh_par != nullptr && !ops;

@@ -217,7 +217,7 @@ void opensps_context_create(int *handle, int *status) {
     // the defaults of the parameters this path reads
     const char *names[] = {"dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun",
                            "zred", "igm_factor", "sigma_smooth", "dust_tesc", "logzsol", "tage", "tau",
-                           "min_wave_smooth", "max_wave_smooth"};
+                           "min_wave_smooth", "max_wave_smooth", "gas_logz", "gas_logu"};
     for (const char *nm : names) {
         const ParamInfo *p = find_param(nm);
         c->pdef[p->id] = p->def;
@@ -282,13 +282,14 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "keep_maggies") c->keep_maggies = value;
     else if (k == "add_dust_emission") c->add_dust_emission = value;
     else if (k == "add_agn_dust") c->add_agn_dust = value;
-    else if (k == "add_neb_continuum" || k == "add_stellar_remnants" ||
+    else if (k == "add_neb_continuum") c->add_neb_continuum = value;
+    else if (k == "cloudy_dust") c->cloudy_dust = value;
+    else if (k == "add_stellar_remnants" ||
              k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" ||
-             k == "redshift_colors" || k == "cloudy_dust" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
+             k == "redshift_colors" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
              k == "vactoair_flag") {
         // known settings this path keeps at the values it implements; other values are refused at batch time
-        if ((k == "add_neb_continuum" || k == "add_xrb_emission" ||
-             k == "redshift_colors") && value != 0)
+        if ((k == "add_xrb_emission" || k == "redshift_colors") && value != 0)
             return fail(status, 104, k + " = 1 is not supported on this path");
     } else {
         return fail(status, 101, "unknown integer parameter " + k);
@@ -644,8 +645,11 @@ void opensps_gb300_data_table(const char *root, const char *kind, const char *na
         rc = std_load_agn(root, grid, a, tab, err);
     } else if (k == "filters") {
         rc = std_load_filters(root, name, grid, tab, a, names, err);
+    } else if (k == "nebular") {
+        std::vector<double> lu;
+        rc = std_load_nebular(root, name, grid, a, b, lu, tab, err);
     } else {
-        return fail(status, ST_BAD_ARG, "kind must be ssp, dust_emission, agn_torus or filters");
+        return fail(status, ST_BAD_ARG, "kind must be ssp, dust_emission, agn_torus, filters or nebular");
     }
     if (rc) return fail(status, rc, err);
     if (n_out) *n_out = (long long)tab.size();

@@ -27,13 +27,13 @@ static const ParamInfo PARAMS[] = {
     {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3}, {"duste_qpah", PF_DUSTE_QPAH, 3.5},
     {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01}, {"fagn", PF_FAGN, 0.0},
     {"agn_tau", PF_AGN_TAU, 10.0},
-    // known to the reference, not varied per model by this path
+    // known to the reference, not varied per model by this path (gas_logz and gas_logu are: the nebular continuum)
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
     {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
     {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
     {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
-    {"gas_logu", -1, -2.0},
-    {"gas_logz", -1, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
+    {"gas_logu", PF_GAS_LOGU, -2.0},
+    {"gas_logz", PF_GAS_LOGZ, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
     {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
     {"wgp1", -1, 1.0}, {"wgp2", -1, 1.0}, {"wgp3", -1, 1.0}, {"compute_mags", -1, 1.0},
     {"compute_indices", -1, 1.0},
@@ -178,7 +178,7 @@ Context::~Context() {
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
     d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release();
-    ops.release(); dustem.release(); agn.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
+    ops.release(); dustem.release(); agn.release(); neb.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
     d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_dem.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);
     emu.release();
@@ -484,6 +484,103 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
     return 0;
 }
 
+// The CLOUDY grid of the setup's isochrone set, when the data root has one: the continuum tables (nodust, dust), the
+// nebular ages, the ionizing photon rate of each of their SSPs (nebular_kernels step 1, opensps_csp_batch.f90:2662-2720:
+// the frequency trapezoid of L_nu / nu over pixels 1 .. whlylim, times L_sun / h) and per nebular age its CLOUDY age
+// interval (batch_nebular_indices :1651-1686). Called from the grid setup once the basis, the pixels below 912 A and
+// the line ages are known.
+int nebular_load(Context &c, std::string &err) {
+    c.neb.release();
+    const std::string root = data_root();
+    const int ns = c.nspec;
+    std::vector<double> tab[2];
+    for (int d = 0; d < 2; ++d) {
+        const std::string name = c.isoc + (d == 0 ? "_nodust" : "_dust");
+        if (!datalib_available(root, "nebular", name)) continue;
+        std::vector<double> lz, la, lu;
+        if (int rc = std_load_nebular(root, name, c.lam, lz, la, lu, tab[d], err)) return rc;
+        if (!c.neb.logz.empty() && (lz != c.neb.logz || la != c.neb.lage || lu != c.neb.logu)) {
+            err = "nebular/" + name + ": its axes differ from nebular/" + c.isoc + "_nodust";
+            return ST_DATA_MISSING;
+        }
+        c.neb.logz = lz; c.neb.lage = la; c.neb.logu = lu;
+        c.neb.have[d] = true;
+    }
+    if (!c.neb.have[0] && !c.neb.have[1]) return 0;
+    c.nt_neb = std::max(0, std::min(find_interval0(c.log_age.data(), c.nt, c.neb.lage[NEB_NAGE - 1]) + 1, c.nt));
+    // per pixel the offset: the grid's largest log2 value there, rounded up (the device tables hold the rest, <= 0)
+    const double L2 = 3.321928094887362;   // log2(10)
+    std::vector<float> off(ns, 0.f);
+    for (int j = 0; j < ns; ++j) {
+        double mx = -1e300;
+        for (int d = 0; d < 2; ++d)
+            if (c.neb.have[d])
+                for (size_t k = 0; k < (size_t)NEB_NZ * NEB_NAGE * NEB_NU; ++k) mx = std::max(mx, tab[d][k * ns + j] * L2);
+        off[j] = (float)std::ceil(mx);
+    }
+    cudaError_t e = cudaSuccess;
+    for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
+        if (!c.neb.have[d]) continue;
+        std::vector<float> t((size_t)ns * NEB_NZ * NEB_NAGE * NEB_NU);
+        for (int z = 0; z < NEB_NZ; ++z)
+            for (int u = 0; u < NEB_NU; ++u)
+                for (int a = 0; a < NEB_NAGE; ++a) {
+                    const double *src = tab[d].data() + (size_t)ns * (z + NEB_NZ * (a + (size_t)NEB_NAGE * u));
+                    float *dst = t.data() + (size_t)ns * (a + NEB_NAGE * (u + (size_t)NEB_NU * z));
+                    for (int j = 0; j < ns; ++j) dst[j] = (float)(src[j] * L2 - (double)off[j]);
+                }
+        e = upload(c.neb.tab[d], t.data(), t.size());
+    }
+    if (e == cudaSuccess) e = upload(c.neb.off, off.data(), off.size());
+    // the ionizing photon rate of each nebular age's SSPs (q0(t, z), metallicity fastest); nu = c / lambda
+    const int nn = std::max(c.nt_neb, 1);
+    std::vector<double> q0((size_t)nn * c.nz, 0.0);
+    if (c.whlylim >= 2)
+        for (int z = 0; z < c.nz; ++z)
+            for (int t = 0; t < c.nt_neb; ++t) {
+                const double *b = c.ssp.data() + (size_t)ns * (t + (size_t)c.nt * z);
+                double s = 0.0;
+                for (int i = 0; i + 1 < c.whlylim && i + 1 < ns; ++i) {
+                    const double n0 = C_LIGHT / c.lam[i], n1 = C_LIGHT / c.lam[i + 1];
+                    s += 0.5 * std::fabs(n1 - n0) * (b[i] / n0 + b[i + 1] / n1);
+                }
+                q0[(size_t)t * c.nz + z] = s / 6.62607015e-27 * 3.828e33;
+            }
+    if (e == cudaSuccess) e = upload(c.neb.q0, q0.data(), q0.size());
+    // per nebular age its CLOUDY interval: get_grid_indices_weights (opensps_gas.f90:394-412) on the log ages, then
+    // the steps of wa within an interval and where a new step starts
+    std::vector<int> ia(nn, 0);
+    std::vector<double> wa(nn, 0.0), dwa(nn, 0.0);
+    std::vector<int> newr(nn, 0);
+    for (int t = 0; t < c.nt_neb; ++t) {
+        int k = find_interval0(c.neb.lage.data(), NEB_NAGE, c.log_age[t]);
+        k = std::max(0, std::min(k, NEB_NAGE - 2));
+        ia[t] = k;
+        const double w = (c.log_age[t] - c.neb.lage[k]) / (c.neb.lage[k + 1] - c.neb.lage[k]);
+        wa[t] = std::max(0.0, std::min(w, 1.0));
+    }
+    for (int t = 1; t < c.nt_neb; ++t) {
+        if (ia[t] != ia[t - 1]) continue;
+        dwa[t] = wa[t] - wa[t - 1];
+        newr[t] = (ia[t - 1] != ia[std::max(0, t - 2)] || t == 1 || dwa[t] != dwa[t - 1]) ? 1 : 0;
+    }
+    std::vector<float> a4((size_t)4 * nn);
+    for (int t = 0; t < nn; ++t) {
+        int bits = ia[t];
+        std::memcpy(&a4[4 * t], &bits, 4);
+        a4[4 * t + 1] = (float)wa[t];
+        a4[4 * t + 2] = (float)dwa[t];
+        a4[4 * t + 3] = (float)newr[t];
+    }
+    if (e == cudaSuccess) e = upload(c.neb.age4, a4.data(), a4.size());
+    if (e != cudaSuccess) {
+        err = std::string("nebular grid: ") + cudaGetErrorString(e);
+        c.neb.release();
+        return ST_DATA_MISSING;
+    }
+    return 0;
+}
+
 int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err) {
     const std::string iso = isoc && *isoc ? isoc : "synthetic", sp = spec ? spec : "";
     const std::string root = data_root();
@@ -500,6 +597,8 @@ int context_setup(Context &c, const char *isoc, const char *spec, const char *du
     c.dust_emission_lib = (dn == "DL07" || dn == "THEMIS") ? dn : "DL07";
     c.dustem.release();
     c.agn.release();
+    c.neb.release();
+    c.isoc = iso;
     if (datalib_available(root, "ssp", iso)) {
         // an SSP library in the standard format (kind ssp, the isochrone name: read_bpass_standard); its spectra
         // are the basis, so spec_type is not read
@@ -555,6 +654,9 @@ int context_setup_grid(Context &c, std::string &err) {
         for (int t = 0; t < c.nt; ++t)
             for (int l = 0; l < c.nline; ++l)
                 if (c.line_lum[l + (size_t)c.nline * (t + (size_t)c.nt * z)] != 0.0) c.nt_neb = std::max(c.nt_neb, t + 1);
+    // with a CLOUDY grid (nebular/<isoc>_nodust or _dust of a standard-format root) its ages set the nebular ages:
+    // nt_neb = find_interval(time_full, nebem_age(NEBNAGE)) (batch_nebular_indices :1643-1644)
+    if (int rc = nebular_load(c, err)) return rc;
     c.llin.resize(c.lbol.size());
     for (size_t i = 0; i < c.lbol.size(); ++i) c.llin[i] = std::pow(10.0, c.lbol[i]);
     // the observed-frame resampling and the smoothing taps take the grid as log-uniform: check it

@@ -25,7 +25,7 @@ enum ParamId {
     PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
     PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
-    PF_FAGN, PF_AGN_TAU,
+    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU,
     PF_COUNT
 };
 
@@ -133,6 +133,21 @@ struct AgnTorus {
     void release() { spec.release(); ready = false; }
 };
 
+// The CLOUDY-grid nebular continuum (nebular/<isoc>_<nodust|dust>, nebular_kernels step 3 of OpenSPS,
+// src/physics/opensps_csp_batch.f90:2760-2910): the continuum per ionizing photon over 11 gas metallicities x 10 ages
+// x 7 ionization parameters at each pixel, with per nebular age of the SSP grid its CLOUDY age interval and the
+// ionizing photon rate of each (age, metallicity) SSP. On the device, per table (0: nodust, 1: dust) the log2 of
+// the continuum less a per-pixel offset (off: the largest log2 value of the pixel over the grid, rounded up to an
+// integer) as FP32, [logZ][logU][age][pixel]; q0 FP64 (nt_neb x nz, metallicity fastest); per nebular age t a
+// float4 (the interval's lower node as int bits, wa, dwa, newr) as batch_nebular_indices forms them (:1651-1686).
+struct NebularGrid {
+    bool have[2] = {false, false};
+    std::vector<double> logz, lage, logu;
+    DevBuf<float> tab[2], off, age4;
+    DevBuf<double> q0;
+    void release() { tab[0].release(); tab[1].release(); off.release(); age4.release(); q0.release(); have[0] = have[1] = false; }
+};
+
 // What the reverse pass needs of the forward batch it follows.
 struct BatchGeom {
     BasisOperand *bop = nullptr;
@@ -151,6 +166,8 @@ struct Context {
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     int add_dust_emission = 0;   // the energy-balance dust emission (Draine & Li templates)
     int add_agn_dust = 0;        // the AGN torus emission
+    int add_neb_continuum = 1;   // the CLOUDY-grid nebular continuum (with add_neb_emission, when the grid exists)
+    int cloudy_dust = 0;         // the continuum table with dust in the ionized gas (nebular/<isoc>_dust)
     bool ops_last_interp = false;   // the last operator batch took the interpolated fold
     int ops_launches = 0;        // kernels the last run_ops_parts launched
     int pageable_access = -1;    // the device reads pageable host memory (-1: not asked yet)
@@ -218,6 +235,8 @@ struct Context {
     // templates
     DustEmission dustem;
     AgnTorus agn;
+    NebularGrid neb;
+    std::string isoc = "synthetic";   // the isochrone set of the setup (names the nebular libraries)
     SspOps ops;
     Emulator emu;                // the learned emulator (emulator.cu, emulator_train.cu)
     DevBuf<double> d_w64, d_y64, d_bc64, d_igm_a64;

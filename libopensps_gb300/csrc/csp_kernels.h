@@ -316,6 +316,10 @@ struct DustEmModel {
     float wq, wu, gam;
     int agn, ita;
     float wta, fagn;
+    // the nebular continuum's CLOUDY cell: the lower corner (0-based, clamped so that the cell lies in the grid) and
+    // the weights (clamped to [0, 1]) in gas_logz and gas_logu, and |1 - frac_obrun|
+    int neb_iz, neb_iu;
+    float neb_wz, neb_wu, neb_fabs;
 };
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
@@ -332,7 +336,15 @@ struct PartsEpilogueArgs {
     const float *agn_spec = nullptr;
     const double *lsum = nullptr;
     int lsum_stride = 6;
+    // the CLOUDY-grid nebular continuum (neb_tab null: none): the table (log2 less the pixel's offset,
+    // [logZ][logU][age][pixel]), the offsets, per nebular age its interval float4 and q0 (nt_neb x nz), the FP64
+    // weights of the models (n x nz x nt), the ages below itesc young
+    const float *neb_tab = nullptr, *neb_off = nullptr;
+    const float4 *neb_age4 = nullptr;
+    const double *neb_q0 = nullptr, *wz = nullptr;
+    int nt = 0, nz = 0, nt_neb = 0, itesc = 0;
 };
+constexpr int NEB_MAX_AGES = 128;         // nebular ages the epilogue's continuum takes
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.

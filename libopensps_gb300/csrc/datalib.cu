@@ -627,6 +627,44 @@ int std_load_agn(const std::string &root, const std::vector<double> &lam, std::v
     return 0;
 }
 
+int std_load_nebular(const std::string &root, const std::string &spec, const std::vector<double> &lam,
+                     std::vector<double> &logz, std::vector<double> &lage, std::vector<double> &logu,
+                     std::vector<double> &tab, std::string &err) {
+    DataLib lib;
+    if (int rc = lib.open(root, "nebular", spec, err)) return rc;
+    std::vector<double> wl, age;
+    if (int rc = lib.axis_values("logZ", logz, err)) return rc;
+    if (int rc = lib.axis_values("age", age, err)) return rc;
+    if (int rc = lib.axis_values("logU", logu, err)) return rc;
+    if (int rc = lib.axis_values("wavelength", wl, err)) return rc;
+    if ((int)logz.size() != NEB_NZ || (int)age.size() != NEB_NAGE || (int)logu.size() != NEB_NU)
+        return bad(err, "library nebular/" + lib.name + ": the grid must be 11 logZ x 10 ages x 7 logU");
+    const long long nw = (long long)wl.size();
+    if (nw < 2) return bad(err, "library nebular/" + lib.name + ": too few wavelengths");
+    for (double a : age)
+        if (!(a > 0.0)) return bad(err, "library nebular/" + lib.name + ": ages must be positive");
+    long long off = 0;
+    if (int rc = lib.check_array("continuum", {"logZ", "age", "logU", "wavelength"}, {NEB_NZ, NEB_NAGE, NEB_NU, nw}, off,
+                                 err))
+        return rc;
+    std::vector<double> raw;
+    if (int rc = lib.read_real("continuum", (long long)NEB_NZ * NEB_NAGE * NEB_NU * nw, off, raw, err)) return rc;
+    const int ns = (int)lam.size();
+    tab.assign((size_t)ns * NEB_NZ * NEB_NAGE * NEB_NU, 0.0);
+    std::vector<double> ly((size_t)nw);
+    for (int z = 0; z < NEB_NZ; ++z)
+        for (int a = 0; a < NEB_NAGE; ++a)
+            for (int u = 0; u < NEB_NU; ++u) {
+                const double *y = raw.data() + (size_t)(((z * NEB_NAGE + a) * NEB_NU + u) * nw);
+                for (long long i = 0; i < nw; ++i) ly[(size_t)i] = std::log10(y[i] + 1.0e-95);
+                double *dst = tab.data() + (size_t)ns * (z + NEB_NZ * (a + (size_t)NEB_NAGE * u));
+                for (int p = 0; p < ns; ++p) dst[p] = interp_linear(wl.data(), ly.data(), (int)nw, lam[(size_t)p]);
+            }
+    lage.resize(age.size());
+    for (size_t i = 0; i < age.size(); ++i) lage[i] = std::log10(age[i]);
+    return 0;
+}
+
 int std_load_filters(const std::string &root, const std::string &spec, const std::vector<double> &lam,
                      std::vector<double> &bands, std::vector<double> &pivot, std::vector<std::string> &names,
                      std::string &err) {

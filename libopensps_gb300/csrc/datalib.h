@@ -79,6 +79,15 @@ int std_load_dust_emission(const std::string &root, const std::string &spec, con
 int std_load_agn(const std::string &root, const std::vector<double> &lam, std::vector<double> &tau,
                  std::vector<double> &tab, std::string &err);
 
+// nebular/<isoc>_<nodust|dust> (load_nebular_grid / read_nebular_standard, opensps_io.f90:749-827,910-933): the
+// continuum [logZ (11), age (10), logU (7), wavelength] as log10(f + 1e-95) interpolated linearly (extrapolated beyond
+// the table) at the grid's pixels; tab is nspec x 11 x 10 x 7, pixel fastest, then logZ, age, logU (nebem_cont(j, z,
+// a, u)); lage = log10 of the ages. The lines array is not read (this path's lines are the SSP library's).
+constexpr int NEB_NZ = 11, NEB_NAGE = 10, NEB_NU = 7;
+int std_load_nebular(const std::string &root, const std::string &spec, const std::vector<double> &lam,
+                     std::vector<double> &logz, std::vector<double> &lage, std::vector<double> &logu,
+                     std::vector<double> &tab, std::string &err);
+
 // filters/<name> (read_filter_library, opensps_io.f90:1247-1318, then filters_build with point resampling,
 // src/spectra/opensps_filters.f90:395-500): bands nb x nspec normalised to int T / lambda = 1 on the grid, their
 // pivot wavelengths and names; a filter with a calibration {lambda_ref, exponent} is then divided by

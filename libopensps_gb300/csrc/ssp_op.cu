@@ -800,6 +800,10 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
     float *esm = tsm + a.nspec;
     __shared__ float red[2][8];
+    __shared__ double ncs[NEB_MAX_AGES];   // the continuum's per-age weights C(t) (FP64)
+    __shared__ float ncn[NEB_MAX_AGES];    // C(t) / max C
+    __shared__ float4 nag[NEB_MAX_AGES];   // per nebular age: interval, wa, dwa, newr
+    __shared__ double nmax;
     const int ns = a.nspec, m = blockIdx.x;
     const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
     const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
@@ -808,7 +812,7 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     const float kd3 = mp[MP_KD3], kcap = mp[MP_IGM_KCAP];
     const int jmax = __float_as_int(mp[MP_IGM_JMAX]);
     const int igm_top = mp[MP_IGM_ON] != 0.f ? a.jtop : 0;     // pixels below carry the IGM
-    DustEmModel dm;
+    DustEmModel dm{};
     if (a.dem) dm = a.dem[m];
     const bool emis = a.dem != nullptr && dm.on != 0;
     const bool agn = a.dem != nullptr && dm.agn != 0;
@@ -819,6 +823,83 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
         const double ls = a.lsum[(size_t)a.lsum_stride * m];
         lagn = (float)((ls > SAFE_FLOOR ? ls : 1.0) * (double)dm.fagn);
     }
+    // the CLOUDY-grid nebular continuum (nebular_kernels step 3, src/physics/opensps_csp_batch.f90:2760-2910): per
+    // nebular age t the weight C(t) = |1 - frac_obrun| sum_z w(t, z) q0(t, z) (the SFH weight times the ionizing
+    // photon rate, over the model's metallicities), normalised by its largest value S (log2 S joins the exponent:
+    // its integer part with the pixel's integer offset exactly, the rest with the table); per pixel the sum over t of
+    // C(t) 2^lg(t) with lg the table interpolated bilinearly in (log Z, log U) at the model's cell and linearly in age
+    // within the CLOUDY age interval, where 2^lg advances geometrically (one exponential per interval and per step)
+    const bool nebc_in = a.neb_tab != nullptr && dm.neb_fabs > 0.f;
+    if (nebc_in) {
+        const double *w = a.wz + (size_t)m * a.nz * a.nt;
+        for (int t = threadIdx.x; t < a.nt_neb; t += blockDim.x) {
+            double cs = 0.0;
+            for (int z = 0; z < a.nz; ++z) {
+                const double wv = __ldg(w + (size_t)z * a.nt + t);
+                if (wv > SAFE_FLOOR) cs = fma(wv, __ldg(a.neb_q0 + (size_t)t * a.nz + z), cs);
+            }
+            ncs[t] = cs * (double)dm.neb_fabs;
+            nag[t] = __ldg(a.neb_age4 + t);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double mx = 0.0;
+            for (int t = threadIdx.x; t < a.nt_neb; t += 32) mx = fmax(mx, ncs[t]);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+            if (threadIdx.x == 0) nmax = mx;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < a.nt_neb; t += blockDim.x) ncn[t] = nmax > 0.0 ? (float)(ncs[t] / nmax) : 0.f;
+        __syncthreads();
+    }
+    const bool nebc = nebc_in && nmax > 0.0;
+    float n_sint = 0.f, n_sfrac = 0.f;
+    const float *nt00 = nullptr, *nt01 = nullptr, *nt10 = nullptr, *nt11 = nullptr;
+    float nc00 = 0.f, nc01 = 0.f, nc10 = 0.f, nc11 = 0.f;
+    if (nebc) {
+        const double s2 = log2(nmax), si = floor(s2);
+        n_sint = (float)si;
+        n_sfrac = (float)(s2 - si);
+        constexpr int NU = 7, NA = 10;     // the CLOUDY grid's logU and age counts
+        const size_t plane = (size_t)NA * ns;
+        nt00 = a.neb_tab + (size_t)(dm.neb_iz * NU + dm.neb_iu) * plane;
+        nt01 = nt00 + plane;
+        nt10 = a.neb_tab + (size_t)((dm.neb_iz + 1) * NU + dm.neb_iu) * plane;
+        nt11 = nt10 + plane;
+        nc00 = (1.f - dm.neb_wz) * (1.f - dm.neb_wu);
+        nc01 = (1.f - dm.neb_wz) * dm.neb_wu;
+        nc10 = dm.neb_wz * (1.f - dm.neb_wu);
+        nc11 = dm.neb_wz * dm.neb_wu;
+    }
+    // the continuum at pixel p into the young (t < itesc) and old sums
+    auto neb_add = [&](int p, float &y, float &o) {
+        auto bil = [&](int k) {
+            const size_t i = (size_t)k * ns + p;
+            return fmaf(nc00, __ldg(nt00 + i), fmaf(nc01, __ldg(nt01 + i), fmaf(nc10, __ldg(nt10 + i), nc11 * __ldg(nt11 + i))));
+        };
+        const float e_int = __ldg(a.neb_off + p) + n_sint;      // an integer: exact
+        float ys = 0.f, os = 0.f, sy = 0.f, so = 0.f, ra = 0.f, rb = 0.f, dl = 0.f, f = 0.f, r = 1.f;
+        int a_prev = -1;
+        for (int t = 0; t < a.nt_neb; ++t) {
+            const float4 ag = nag[t];
+            const int k = __float_as_int(ag.x);
+            if (k != a_prev) {
+                ys += sy; os += so; sy = 0.f; so = 0.f;
+                ra = (a_prev >= 0 && k == a_prev + 1) ? rb : bil(k);   // (the first interval has no predecessor)
+                rb = bil(k + 1);
+                a_prev = k;
+                dl = rb - ra;
+                f = ops_ex2((n_sfrac + fmaf(ag.y, dl, ra)) + e_int);
+            } else {
+                if (ag.w != 0.f) r = ops_ex2(ag.z * dl);
+                f *= r;
+            }
+            if (t < a.itesc) sy = fmaf(ncn[t], f, sy); else so = fmaf(ncn[t], f, so);
+        }
+        y += ys + sy;
+        o += os + so;
+    };
     constexpr float LN2 = 0.6931471805599453f;
     float sa = 0.f, se = 0.f;
     // (ln lambda log2 e, the shared diffuse curve) of a pixel
@@ -891,6 +972,10 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
                     g1 = __ldg(gb + q);
                 }
                 float e0 = 0.f, e1 = 0.f;
+                if (nebc) {
+                    neb_add(2 * q, yy[u].x, oo[u].x);
+                    neb_add(2 * q + 1, yy[u].y, oo[u].y);
+                }
                 const float t0 = pass1(2 * q, yy[u].x, oo[u].x, sh.x, cn.x, g0.x, g1.x, e0);
                 const float t1 = pass1(2 * q + 1, yy[u].y, oo[u].y, sh.y, cn.y, g0.y, g1.y, e1);
                 reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
@@ -900,6 +985,7 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     } else {
         for (int p = threadIdx.x; p < ns; p += bd) {
             float esc = 0.f, y = __ldg(yv + p), o = __ldg(ov + p);
+            if (nebc) neb_add(p, y, o);
             tsm[p] = pass1(p, y, o, emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
                            emis ? __ldg(a.cnu + p) : 0.f, agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f,
                            agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f, esc);

@@ -95,9 +95,10 @@ def gaussian_curves(centres: np.ndarray, npts: int = 81) -> tuple[np.ndarray, np
 
 
 def convert_synthetic(out_root: Path, src_root: Path | None = None, energy_every: int = 0, dust: bool = True,
-                      agn: bool = True, ssp_dtype: str = "<f8") -> Path:
+                      agn: bool = True, ssp_dtype: str = "<f8", nebular: bool = False) -> Path:
     """The synthetic libraries of ``src_root`` (written first if missing) as a standard-format root ``out_root``.
-    Libraries: ssp/synthetic, filters/gauss20, filters/gauss40, dust_emission/DL07, agn_torus/clumpy."""
+    Libraries: ssp/synthetic, filters/gauss20, filters/gauss40, dust_emission/DL07, agn_torus/clumpy, and with
+    ``nebular`` the CLOUDY-style grid nebular/synthetic_nodust (the nebular continuum of the setup's isochrones)."""
     out_root = Path(out_root)
     data = synthdata.load(src_root)
     man = data["manifest"]
@@ -150,5 +151,8 @@ def convert_synthetic(out_root: Path, src_root: Path | None = None, energy_every
                             "wavelength": {"units": "angstrom", "values": wl}},
                       arrays={"spectra": (tab, "<f4", ["tau", "wavelength"], "f_nu, normalized to unity")},
                       title="Synthetic AGN torus templates")
+    if nebular:
+        from . import synth_nebular
+        synth_nebular.write(out_root, "synthetic_nodust")
     write_root_index(out_root)
     return out_root

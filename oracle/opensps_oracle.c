@@ -18,6 +18,8 @@
 #define SAFE_FLOOR DBL_MIN                 /* src/core/opensps_constants.f90:192 tiny(1.0_wp) */
 #define C_LIGHT 2.99792458e18              /* src/core/opensps_constants.f90:41 [A/s] */
 #define V_BAND 5500.0                      /* src/physics/opensps_dust.f90:47 */
+#define H_PLANCK 6.62607015e-27            /* src/core/opensps_constants.f90:35 [erg s] */
+#define L_SUN 3.828e33                     /* src/core/opensps_constants.f90:50 [erg/s] */
 #define AB_ZEROPOINT 48.60                 /* src/spectra/opensps_batch_photometry.f90:40 */
 #define LINE_PROFILE_CUT 1.0e-14           /* src/physics/opensps_gas.f90:354 */
 #define N_SIGMA_RANGE 4.0                  /* src/spectra/opensps_smoothing.f90:28 */
@@ -324,7 +326,7 @@ int oracle_velocity_row(int n, const double *lam, double sigma, double minl, dou
 /* Per-model parameters, in this order (doubles): */
 enum { P_DUST1, P_DUST2, P_DUST3, P_DUST_INDEX, P_DUST1_INDEX, P_FRAC_NODUST, P_FRAC_OBRUN, P_ZRED,
        P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_DUSTE_QPAH, P_DUSTE_UMIN, P_DUSTE_GAMMA, P_FAGN, P_AGN_TAU,
-       P_NPAR };
+       P_GAS_LOGZ, P_GAS_LOGU, P_NPAR };
 
 typedef struct {
     int nspec, nt, nz, nbands;
@@ -351,7 +353,113 @@ typedef struct {
      * nt x nz), the nebular ages 1..nt_neb and the ionizing pixels 1..whlylim */
     const double *ssp_ion;
     int nt_neb, whlylim;
+    /* the CLOUDY-grid nebular continuum (neb_cont NULL: off): log10 of the continuum per ionizing photon on the
+     * spectral grid, nspec x 11 x 10 x 7 (pixel fastest, then log Z, age, log U: nebem_cont(j, z, a, u)), the grid's
+     * log Z, log10 age and log U values */
+    const double *neb_cont, *neb_logz, *neb_lage, *neb_logu;
 } oracle_grid_t;
+
+#define NEB_NZ 11
+#define NEB_NAGE 10
+#define NEB_NU 7
+
+/* get_grid_indices_weights (src/physics/opensps_gas.f90:394-412): the 0-based lower node of val's interval, clamped
+ * so that the interval lies in the grid, and the weight clamped to [0, 1]. */
+static void grid_cell(const double *grid, int n, double val, int *idx, double *w) {
+    int i = oracle_find_interval(grid, n, val);    /* 1-based */
+    if (i < 1) i = 1;
+    if (i > n - 1) i = n - 1;
+    double t = (val - grid[i - 1]) / (grid[i] - grid[i - 1]);
+    *idx = i - 1;
+    *w = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+}
+
+/* The CLOUDY-grid nebular continuum of one model into its young (y) and old (o) sums (compute_csp_batch's nebular
+ * stage with add_neb_continuum, src/physics/opensps_csp_batch.f90):
+ *   q0(t, z)          nebular_kernels step 1 (:2672-2712): the ionizing photon rate of each nebular age's SSP, the
+ *                     frequency trapezoid of L_nu / nu over pixels 1 .. whlylim, / H_PLANCK * L_SOL
+ *   ia, wa, dwa, newr batch_nebular_indices (:1651-1686): per nebular age its CLOUDY age interval, the weight in it,
+ *                     the weight's step within the interval and where a new step starts
+ *   iz, wz, iu, wu    (:1691-1693) the cell in gas_logz and gas_logu; fabs = 1 - frac_obrun (:1697)
+ *   C(t)              step 3 (:2781-2828): the weight times |q fabs| (here with weights over ages and metallicities,
+ *                     q0 summed against each age's metallicity weights), divided by its largest value S per model
+ *   the continuum     (:2839-2905): per pixel sum_t C(t) 10^lg(t), lg = ra + wa (rb - ra) with ra, rb the bilinear
+ *                     (log Z, log U) interpolation at the interval's nodes; exp(ra ln10 + wa dl + ln S) at an
+ *                     interval's first age, then times exp(dwa dl) per age (recomputed where a new step starts)
+ * wz: nt x nz of the model (age fastest); itesc 1-based (ages t <= itesc young). */
+static void neb_continuum(const oracle_grid_t *g, const double *wz, const double *par, int itesc, double *y, double *o) {
+    const int ns = g->nspec, nt = g->nt, nz = g->nz, nn = g->nt_neb;
+    if (nn < 1) return;
+    const double LN10 = log(10.0);
+    double *cy = (double *)calloc((size_t)nn, sizeof(double)), *co = (double *)calloc((size_t)nn, sizeof(double));
+    double *wa = (double *)calloc((size_t)nn, sizeof(double)), *dwa = (double *)calloc((size_t)nn, sizeof(double));
+    int *ia = (int *)calloc((size_t)nn, sizeof(int)), *newr = (int *)calloc((size_t)nn, sizeof(int));
+    for (int t = 0; t < nn; ++t) grid_cell(g->neb_lage, NEB_NAGE, g->log_age[t], &ia[t], &wa[t]);
+    for (int t = 1; t < nn; ++t) {
+        if (ia[t] != ia[t - 1]) continue;
+        dwa[t] = wa[t] - wa[t - 1];
+        newr[t] = ia[t - 1] != ia[t >= 2 ? t - 2 : 0] || t == 1 || dwa[t] != dwa[t - 1];
+    }
+    int iz, iu;
+    double wzg, wug;
+    grid_cell(g->neb_logz, NEB_NZ, par[P_GAS_LOGZ], &iz, &wzg);
+    grid_cell(g->neb_logu, NEB_NU, par[P_GAS_LOGU], &iu, &wug);
+    const double fabs_ = 1.0 - par[P_FRAC_OBRUN];
+    double cmax = 0.0;
+    for (int t = 0; t < nn; ++t) {
+        double c = 0.0;
+        for (int z = 0; z < nz; ++z) {
+            const double w = wz[t + (size_t)nt * z];
+            if (!(w > SAFE_FLOOR)) continue;
+            /* step 1: the photon-number trapezoid of this SSP below 912 A */
+            const double *b = g->ssp_ion + (size_t)ns * (t + (size_t)nt * z);
+            double s = 0.0;
+            for (int i = 0; i + 1 < g->whlylim && i + 1 < ns; ++i) {
+                const double n0 = C_LIGHT / g->lam[i], n1 = C_LIGHT / g->lam[i + 1];
+                s += 0.5 * fabs(n1 - n0) * (b[i] / n0 + b[i + 1] / n1);
+            }
+            const double q = fabs(s / H_PLANCK * L_SUN * fabs_);
+            if (q > SAFE_FLOOR) c += w * q;
+        }
+        if (t + 1 <= itesc) cy[t] = c; else co[t] = c;
+        if (c > cmax) cmax = c;
+    }
+    if (cmax > 0.0) {
+        const double lns = log(cmax);
+        for (int t = 0; t < nn; ++t) { cy[t] /= cmax; co[t] /= cmax; }
+        const double c00 = (1.0 - wzg) * (1.0 - wug), c01 = (1.0 - wzg) * wug, c10 = wzg * (1.0 - wug), c11 = wzg * wug;
+#define NEBC(j, z, a, u) g->neb_cont[(j) + (size_t)ns * ((z) + NEB_NZ * ((a) + (size_t)NEB_NAGE * (u)))]
+        for (int j = 0; j < ns; ++j) {
+            double ys = 0.0, os = 0.0, sy = 0.0, so = 0.0, ra = 0.0, rb = 0.0, dl = 0.0, f = 0.0, r = 1.0;
+            int a_prev = -1;
+            for (int t = 0; t < nn; ++t) {
+                const int a = ia[t];
+                if (a != a_prev) {
+                    ys += sy; os += so; sy = 0.0; so = 0.0;
+                    if (a_prev >= 0 && a == a_prev + 1)   /* (0-based intervals: the first one has no predecessor) */
+                        ra = rb;
+                    else
+                        ra = c00 * NEBC(j, iz, a, iu) + c01 * NEBC(j, iz, a, iu + 1) + c10 * NEBC(j, iz + 1, a, iu) +
+                             c11 * NEBC(j, iz + 1, a, iu + 1);
+                    rb = c00 * NEBC(j, iz, a + 1, iu) + c01 * NEBC(j, iz, a + 1, iu + 1) + c10 * NEBC(j, iz + 1, a + 1, iu) +
+                         c11 * NEBC(j, iz + 1, a + 1, iu + 1);
+                    a_prev = a;
+                    dl = (rb - ra) * LN10;
+                    f = exp(ra * LN10 + wa[t] * dl + lns);
+                } else {
+                    if (newr[t]) r = exp(dwa[t] * dl);
+                    f = f * r;
+                }
+                sy += cy[t] * f;
+                so += co[t] * f;
+            }
+            y[j] += ys + sy;
+            o[j] += os + so;
+        }
+#undef NEBC
+    }
+    free(cy); free(co); free(wa); free(dwa); free(ia); free(newr);
+}
 
 /* observed_frame_z (src/spectra/opensps_batch_photometry.f90:819-903) for one model: the rest-frame spectrum fin at
  * lambda / (1 + z) by linear interpolation in the interval find_interval gives (the end intervals extrapolate),
@@ -438,6 +546,7 @@ static void csp_one(const oracle_grid_t *g, const double *wz, const double *par,
             if (emlines && g->line_lum)
                 for (int l = 0; l < g->nline; ++l) emlines[l] += w * g->line_lum[l + (size_t)g->nline * (k + (size_t)nt * z)];
         }
+    if (g->neb_cont) neb_continuum(g, wz, par, itesc, y, o);
     if (mass) *mass = ms;
     if (lbol) *lbol = ls > SAFE_FLOOR ? log10(ls) : 0.0;
     if (young) memcpy(young, y, sizeof(double) * ns);

@@ -15,11 +15,12 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 PAR_NAMES = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
-             "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma", "fagn", "agn_tau")
+             "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma", "fagn", "agn_tau",
+             "gas_logz", "gas_logu")
 PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
                 "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
                 "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01, "fagn": 0.0,
-                "agn_tau": 10.0}
+                "agn_tau": 10.0, "gas_logz": 0.0, "gas_logu": -2.0}
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
@@ -38,7 +39,7 @@ class _Grid(C.Structure):
                 ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double),
                 ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp),
                 ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp), ("ssp_ion", _dp), ("nt_neb", C.c_int),
-                ("whlylim", C.c_int)]
+                ("whlylim", C.c_int), ("neb_cont", _dp), ("neb_logz", _dp), ("neb_lage", _dp), ("neb_logu", _dp)]
 
 
 class _OpsT(C.Structure):
@@ -244,7 +245,7 @@ class Oracle:
     def __init__(self, data: dict, nbands: int = 40, add_neb: bool = True, add_igm: bool = True,
                  smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
                  line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73,
-                 dust_emission: dict | None = None, agn: dict | None = None):
+                 dust_emission: dict | None = None, agn: dict | None = None, nebular: dict | None = None):
         L = lib()
         self.d = data
         self.lam = np.ascontiguousarray(data["lambda"])
@@ -296,6 +297,18 @@ class Oracle:
             self._at = np.ascontiguousarray(agn["tau"], dtype=np.float64)
             self._as = np.ascontiguousarray(agn["agnspec"], dtype=np.float64)
             g.ntau, g.agn_tau, g.agn_spec = self._at.size, _p(self._at), _p(self._as)
+        g.neb_cont = None
+        if nebular is not None and add_neb:
+            # the CLOUDY continuum (stdformat.nebular()); its last age sets the nebular ages:
+            # nt_neb = find_interval(time_full, nebem_age(NEBNAGE)) (batch_nebular_indices :1643-1644)
+            self._nc = np.ascontiguousarray(nebular["cont"], dtype=np.float64)
+            self._nz = np.ascontiguousarray(nebular["logz"], dtype=np.float64)
+            self._na = np.ascontiguousarray(nebular["lage"], dtype=np.float64)
+            self._nu = np.ascontiguousarray(nebular["logu"], dtype=np.float64)
+            g.neb_cont, g.neb_logz, g.neb_lage, g.neb_logu = _p(self._nc), _p(self._nz), _p(self._na), _p(self._nu)
+            k = L.oracle_find_interval(_p(self.log_age), nt, float(self._na[-1]))
+            g.nt_neb = max(0, min(k, nt))
+            self.nt_neb = g.nt_neb
         self.grid = g
         self.nline = nl
 

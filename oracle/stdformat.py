@@ -8,6 +8,8 @@ Follows the reference's readers:
   src/physics/opensps_ssp.f90:203-218 (log10 of the |d nu| trapezoid of the spectrum, floored at tiny);
 * dust_emission: opensps_io.f90:991-1060 (linear interpolation, extrapolated, at pixels from the one holding 1 um);
 * agn_torus/clumpy: load_agn_dust_models opensps_io.f90:1099-1157 (log-log interpolation over the table's range);
+* nebular: load_nebular_grid / read_nebular_standard opensps_io.f90:749-827,910-933 (the continuum's log10(f + 1e-95)
+  interpolated linearly onto the grid);
 * filters: read_filter_library opensps_io.f90:1247-1318, filters_build with point resampling
   src/spectra/opensps_filters.f90:186-230 (lenient filter_clean), :362-387 (resample_point), :395-500,
   filter_pivot :521-531, the calibration of apply_standard_filter_calibration opensps_io.f90:1465-1500;
@@ -114,6 +116,21 @@ def dust_emission(root: Path, lam: np.ndarray, name: str = "DL07") -> dict:
         for col in range(2 * u.size):
             tab[col, iq, start:] = interp_linear_at(wl, raw[iq, col // 2, col % 2], lam[start:])
     return {"qpah": q, "umin": u, "dustem": tab}
+
+
+def nebular(root: Path, lam: np.ndarray, name: str) -> dict:
+    """nebular/<name> (load_nebular_grid / read_nebular_standard, opensps_io.f90:749-827,910-933) in the oracle's
+    format: cont = log10(continuum + 1e-95) interpolated linearly onto the grid, (logU, age, logZ, nspec) C order
+    (nebem_cont(j, z, a, u) column-major); logz, lage (log10 of the ages), logu."""
+    L = Lib(root, "nebular", name)
+    lz, age, lu, wl = L.axis("logZ"), L.axis("age"), L.axis("logU"), L.axis("wavelength")
+    raw = L.array("continuum")                                 # (11, 10, 7, nw)
+    cont = np.empty((lu.size, age.size, lz.size, lam.size))
+    for z in range(lz.size):
+        for a in range(age.size):
+            for u in range(lu.size):
+                cont[u, a, z] = interp_linear_at(wl, np.log10(raw[z, a, u] + 1.0e-95), lam)
+    return {"cont": cont, "logz": lz, "lage": np.log10(age), "logu": lu}
 
 
 def agn(root: Path, lam: np.ndarray) -> dict:

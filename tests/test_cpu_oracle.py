@@ -111,3 +111,33 @@ def test_oracle_escaping_ionizing_light(data):
     d = off.csp_batch({"frac_obrun": np.zeros(n)}, wo, young=True)
     np.testing.assert_allclose(c["young"][:, :whl] + c["old"][:, :whl], d["young"][:, :whl] + d["old"][:, :whl],
                                rtol=1e-13, atol=1e-300)
+
+
+def test_oracle_nebular_continuum_closed_form(data):
+    """The oracle's CLOUDY continuum loop (intervals, geometric steps, the normalisation by the largest weight) on a
+    table constant over log Z, age and log U: the continuum is then 10^T(lambda) times sum_t C(t), C(t) the weights
+    times |1 - frac_obrun| times the ionizing photon rate of each nebular age's SSPs (computed here directly)."""
+    from oracle.oracle import Oracle
+    lam = data["lambda"]
+    T = -60.4 + 0.3 * np.sin(np.log(lam))
+    neb = {"cont": np.broadcast_to(T, (7, 10, 11, lam.size)).copy(), "logz": np.linspace(-2.0, 0.2, 11),
+           "lage": np.log10(np.array([0.5, 1, 2, 3, 4, 5, 6, 7, 8, 10]) * 1e6), "logu": np.linspace(-4, -1, 7)}
+    n = 3
+    rng = np.random.default_rng(5)
+    wz = rng.dirichlet(np.ones(107), size=(n, 12)) / 12.0
+    params = {"frac_obrun": np.array([0.0, 0.3, 0.9]), "gas_logz": rng.uniform(-2, 0.2, n),
+              "gas_logu": rng.uniform(-4, -1, n)}
+    on = Oracle(data, nbands=40, add_igm=False, smooth=False, nebular=neb).csp_batch(params, wz, young=True)
+    off = Oracle(data, nbands=40, add_igm=False, smooth=False).csp_batch(params, wz, young=True)
+    nn = on_nt = Oracle(data, nbands=40, nebular=neb).nt_neb
+    assert nn == 35
+    whl = int(np.searchsorted(lam, 912.0, side="right"))
+    nu = 2.99792458e18 / lam[:whl]
+    ssp = data["ssp_spec"]                           # (nz, nt, ns)
+    q0 = 0.5 * np.sum(np.abs(np.diff(nu))[None, None, :] * (ssp[:, :nn, 1:whl] / nu[1:] + ssp[:, :nn, :whl - 1] / nu[:-1]),
+                      axis=2) / 6.62607015e-27 * 3.828e33          # (nz, nn)
+    for m in range(n):
+        c = np.sum(wz[m, :, :nn] * q0, axis=0) * abs(1.0 - params["frac_obrun"][m])
+        want = 10.0 ** T * c.sum()
+        got = (on["young"][m] + on["old"][m]) - (off["young"][m] + off["old"][m])
+        np.testing.assert_allclose(got, want, rtol=1e-10)

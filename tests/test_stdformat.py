@@ -31,7 +31,7 @@ def lam():
 @pytest.fixture(scope="module")
 def std_root(tmp_path_factory):
     root = tmp_path_factory.mktemp("stdroot")
-    stdformat.convert_synthetic(root, energy_every=3)
+    stdformat.convert_synthetic(root, energy_every=3, nebular=True)
     return root
 
 
@@ -65,6 +65,13 @@ def test_agn(std_root, lam):
     np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-12 * np.abs(want).max())
 
 
+def test_nebular_continuum_table(std_root, lam):
+    got = data_table(std_root, "nebular", "synthetic_nodust", lam)
+    want = ora.nebular(std_root, lam, "synthetic_nodust")["cont"].reshape(-1, lam.size)
+    assert got.shape == (11 * 10 * 7, lam.size)
+    np.testing.assert_allclose(got, want, rtol=1e-13)
+
+
 def test_filters_with_energy_detectors(std_root, lam):
     got = data_table(std_root, "filters", "gauss20", lam)
     want, _ = ora.filters(std_root, "gauss20", lam)
@@ -76,7 +83,7 @@ def test_filters_with_energy_detectors(std_root, lam):
 
 @pytest.mark.skipif(not REF_TEST_LIBRARY.exists(), reason="the reference's test library is not in this container")
 @pytest.mark.parametrize("kind,name", [("dust_emission", "DL07"), ("dust_emission", "THEMIS"), ("agn_torus", "clumpy"),
-                                       ("filters", "allfilters")])
+                                       ("filters", "allfilters"), ("nebular", "mist_nodust")])
 def test_reference_test_library(lam, kind, name):
     """The reader on the reference's own standard-format files (FP32 arrays, file-held axes, labels, filter
     calibrations) against the numpy restatement."""
@@ -85,6 +92,9 @@ def test_reference_test_library(lam, kind, name):
         want = ora.dust_emission(REF_TEST_LIBRARY, lam, name)["dustem"].reshape(-1, lam.size)
     elif kind == "agn_torus":
         want = ora.agn(REF_TEST_LIBRARY, lam)["agnspec"]
+    elif kind == "nebular":
+        # (the test subset's FP32 continuum underflows to zero: the table is the floor, log10(1e-95), everywhere)
+        want = ora.nebular(REF_TEST_LIBRARY, lam, name)["cont"].reshape(-1, lam.size)
     else:
         want, _ = ora.filters(REF_TEST_LIBRARY, name, lam)
         meta = json.loads((REF_TEST_LIBRARY / "libraries/filters/allfilters/manifest.json").read_text())["metadata"]
