@@ -10,11 +10,11 @@
 // Per CTA: 128 models (MMA M). K = the pixels that any band reaches, 64 per stage. The A operand (observed frame
 // of 128 models x 64 pixels) is built by warps 0..7 in shared memory from the spectra, in the 128-byte swizzled
 // K-major layout, split into bf16 hi and lo; the B operand (band matrix, hi and lo, bands x pixels) comes by TMA.
-// fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes. Two stages:
-// the builders fill stage s + 1 while the tensor core works on stage s.
-//
-// With args.sums set, warps 8 and 9 form the FP64 sums of model_sums_zw (src/physics/opensps_csp_batch.f90:2090-2120)
-// for the CTA's 128 models (measured slower than the separate sums kernel; the batch does not set it).
+// fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes.
+// Warp roles: warps 0..7 build the A operand (16 model rows each), warp 8 issues the band matrix's TMA and the MMAs.
+// Two stages with mbarriers: a builder warp signals its rows of stage s on full_a[s] and goes on to the next stage as
+// soon as the MMAs that read that buffer have completed (empty[s], a tcgen05 commit), so that the warps do not wait
+// for one another between stages.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cuda_bf16.h>
@@ -29,8 +29,8 @@ constexpr int BG_M = 128;
 constexpr int BG_K = 64;
 constexpr int BG_BUILD_WARPS = 8;
 constexpr int BG_BUILD_THREADS = BG_BUILD_WARPS * 32;
-constexpr int BG_SUM_WARPS = 2;
-constexpr int BG_THREADS = BG_BUILD_THREADS + BG_SUM_WARPS * 32;
+constexpr int BG_MMA_WARP = BG_BUILD_WARPS;             // TMA of the band matrix and the MMAs
+constexpr int BG_THREADS = BG_BUILD_THREADS + 32;
 constexpr int BG_A_BYTES = BG_M * BG_K * 2;   // 16 KB
 
 struct BandGemmSmem {
@@ -43,43 +43,6 @@ __device__ __forceinline__ float bg_ex2(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
-}
-
-// The FP64 sums of one model (one warp): mass and L_bol over the weights above SAFE_FLOOR (the comparison on the
-// bit pattern: positive doubles order as their bits), young and old apart with parts.
-__device__ __forceinline__ void model_sums_warp(const BandGemmArgs &a, int m, int lane) {
-    const double *w = a.wz + (size_t)m * a.ntz;
-    double ms = 0.0, ls = 0.0, msy = 0.0, lsy = 0.0, mso = 0.0, lso = 0.0;
-    int t = lane % a.nt;
-#pragma unroll 4
-    for (int k = lane; k < a.ntz; k += 32) {
-        const double wv = __ldg(w + k);
-        if (__double_as_longlong(wv) > 0x0010000000000000LL) {   // wv > DBL_MIN (and not negative)
-            const double mk = wv * __ldg(a.mass + k), lk = wv * __ldg(a.llin + k);
-            ms += mk;
-            ls += lk;
-            if (a.parts) {
-                if (t < a.itesc) { msy += mk; lsy += lk; } else { mso += mk; lso += lk; }
-            }
-        }
-        if (a.parts) { t += 32; while (t >= a.nt) t -= a.nt; }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        ms += __shfl_xor_sync(0xffffffffu, ms, off);
-        ls += __shfl_xor_sync(0xffffffffu, ls, off);
-        if (a.parts) {
-            msy += __shfl_xor_sync(0xffffffffu, msy, off);
-            lsy += __shfl_xor_sync(0xffffffffu, lsy, off);
-            mso += __shfl_xor_sync(0xffffffffu, mso, off);
-            lso += __shfl_xor_sync(0xffffffffu, lso, off);
-        }
-    }
-    if (lane == 0) {
-        double *o = a.sums + (size_t)m * 6;
-        o[0] = ms; o[1] = ls;
-        if (a.parts) { o[2] = msy; o[3] = mso; o[4] = lsy; o[5] = lso; }
-    }
 }
 
 // AB magnitude of an FP32 band flux (NaN when not positive): -2.5 log10 f in FP32 (the flux carries FP32's precision
@@ -99,113 +62,60 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     const int b_bytes = npad * BG_K * 2;
     const int stage_bytes = 2 * BG_A_BYTES + 2 * b_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * stage_bytes);
-    uint64_t *bar_tma = bars;        // [2]
-    uint64_t *bar_mma = bars + 2;    // [2]
-    uint64_t *bar_done = bars + 4;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 5);
+    uint64_t *full_a = bars;         // [2] the builder warps' rows of a stage (8 arrivals)
+    uint64_t *full_b = bars + 2;     // [2] the band matrix's TMA of a stage
+    uint64_t *empty = bars + 4;      // [2] the MMAs that read a stage have completed
+    uint64_t *bar_done = bars + 6;   // every MMA has completed
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 7);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * BG_M;
     // this CTA's pixel blocks: split blockIdx.y of gridDim.y
     const int kb0 = (int)((long long)blockIdx.y * a.nkb / gridDim.y), kb1 = (int)((long long)(blockIdx.y + 1) * a.nkb / gridDim.y);
+    const int nst = kb1 - kb0;
     const bool split = gridDim.y > 1;
     int *status = a.status;
     const uint32_t tcols = npad <= 32 ? 32 : (npad <= 64 ? 64 : (npad <= 128 ? 128 : 256));
     __shared__ float4 zsm[BG_M];     // the observed-frame shift of the CTA's models (w = 2: no model in this row)
+    __shared__ int2 rsh[BG_M];       // per row: the rest-frame offset d (observed pixel j reads j - d, j - d + 1) and
+                                     // its kind (0 rest frame, 1 shifted, 2 no model)
 
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) { mbar_init(&bar_tma[s], 1); mbar_init(&bar_mma[s], 1); }
+        for (int s = 0; s < 2; ++s) { mbar_init(&full_a[s], BG_BUILD_WARPS); mbar_init(&full_b[s], 1); mbar_init(&empty[s], 1); }
         mbar_init(bar_done, 1);
         fence_mbar_init();
         tma_prefetch_desc(&tm_c_hi);
         tma_prefetch_desc(&tm_c_lo);
     }
     if (warp == 0) { tmem_alloc(tmem_slot, tcols); tmem_relinquish(); }
-    for (int i = tid; i < BG_M; i += BG_THREADS)
-        zsm[i] = (m0 + i < a.n_models) ? a.zinfo[m0 + i] : make_float4(0.f, 0.f, 0.f, 2.f);
+    for (int i = tid; i < BG_M; i += BG_THREADS) {
+        const float4 zs = (m0 + i < a.n_models) ? a.zinfo[m0 + i] : make_float4(0.f, 0.f, 0.f, 2.f);
+        zsm[i] = zs;
+        // the interior interpolation's first rest pixel: n0 + 1 below the observed one unless the shift is whole
+        const int kind = zs.w == 1.f ? 1 : (zs.w == 0.f ? 0 : 2);
+        rsh[i] = make_int2(kind == 1 ? __float_as_int(zs.x) + (zs.y > 0.f ? 1 : 0) : 0, kind);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp >= BG_BUILD_WARPS) {
-        // ---------------------------------------------------------------- FP64 sums of the CTA's models
-        if (a.sums && blockIdx.y == 0) {
-            for (int r = warp - BG_BUILD_WARPS; r < BG_M; r += BG_SUM_WARPS)
-                if (m0 + r < a.n_models) model_sums_warp(a, m0 + r, lane);
-        }
-    } else {
-        // ---------------------------------------------------------------- band GEMM (warps 0..7)
-        const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
-        const float dl2 = (float)(a.dlnl * 1.4426950408889634);   // grid step in log2 units
-        const float inv_em1 = (float)(1.0 / expm1(a.dlnl));
-        // each warp builds 16 model rows; lane l takes pixels 2l, 2l + 1 of the stage
-        for (int kb = kb0; kb < kb1; ++kb) {
-            const int li = kb - kb0;                          // this CTA's stage count
-            const int s = li & 1;
-            uint8_t *st = smem + s * stage_bytes;
-            if (li >= 2) mbar_wait(&bar_mma[s], ((li - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
-            if (tid == 0) {
-                mbar_arrive_expect_tx(&bar_tma[s], 2 * b_bytes);
-                tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &bar_tma[s]);
-                tma_load_2d(st + 2 * BG_A_BYTES + b_bytes, &tm_c_lo, kb * BG_K, 0, &bar_tma[s]);
-            }
-            const int j = a.j0 + kb * BG_K + 2 * lane;       // observed pixel of this lane (and j + 1)
-            float wl0 = 0.f, wl1 = 0.f;
-            if (j < a.nspec) wl0 = __ldg(a.wl + j);
-            if (j + 1 < a.nspec) wl1 = __ldg(a.wl + j + 1);
-            // rows in two halves of 8: each half's loads are all issued before any is used
-#pragma unroll 1
-            for (int h = 0; h < 2; ++h) {
-            float s00[8], s01[8], s10[8], s11[8], t0v[8], t1v[8];
-#pragma unroll
-            for (int rr = 0; rr < 8; ++rr) {
-                const int r = warp * 16 + h * 8 + rr;
-                const float4 zs = zsm[r];                     // n0, t, s, (0: rest frame, 2: no model)
-                const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec;
-                s00[rr] = s01[rr] = s10[rr] = s11[rr] = 0.f;
-                t0v[rr] = t1v[rr] = 0.f;
-                if (zs.w == 1.f) {
-                    const int n0 = __float_as_int(zs.x);
-                    const int sub = (zs.y > 0.f) ? 1 : 0;
-                    const int il0 = j - n0 - sub, il1 = il0 + 1;
-                    // intervals outside the grid extrapolate from the first / last one (the reference's clamped
-                    // find_interval): position t = (e^(x dlnl) - 1) / (e^dlnl - 1), x pixels from the interval start
-                    const int c0 = min(max(il0, 0), a.nspec - 2), c1 = min(max(il1, 0), a.nspec - 2);
-                    const float t0 = (c0 == il0) ? zs.y : (bg_ex2(((float)(j - c0) - zs.z) * dl2) - 1.f) * inv_em1;
-                    const float t1 = (c1 == il1) ? zs.y : (bg_ex2(((float)(j + 1 - c1) - zs.z) * dl2) - 1.f) * inv_em1;
-                    s00[rr] = __ldg(sp + c0); s01[rr] = __ldg(sp + c0 + 1);
-                    s10[rr] = __ldg(sp + c1); s11[rr] = __ldg(sp + c1 + 1);
-                    t0v[rr] = t0; t1v[rr] = t1;
-                } else if (zs.w == 0.f) {
-                    // rest frame: v = s00 (t = 0)
-                    if (j < a.nspec) s00[rr] = __ldg(sp + j);
-                    if (j + 1 < a.nspec) s10[rr] = __ldg(sp + j + 1);
-                }
-            }
-#pragma unroll
-            for (int rr = 0; rr < 8; ++rr) {
-                const int r = warp * 16 + h * 8 + rr;
-                float v0 = fmaf(t0v[rr], s01[rr] - s00[rr], s00[rr]);
-                float v1 = fmaf(t1v[rr], s11[rr] - s10[rr], s10[rr]);
-                if (v0 != v0) v0 = 0.f;
-                if (v1 != v1) v1 = 0.f;
-                const float f0 = fmaxf(v0, 0.f) * wl0;
-                const float f1 = fmaxf(v1, 0.f) * wl1;
-                const __nv_bfloat16 h0 = __float2bfloat16_rn(f0), h1 = __float2bfloat16_rn(f1);
-                const __nv_bfloat16 l0 = __float2bfloat16_rn(f0 - __bfloat162float(h0));
-                const __nv_bfloat16 l1 = __float2bfloat16_rn(f1 - __bfloat162float(h1));
-                const uint32_t off = r * 128 + ((((uint32_t)lane >> 2) ^ (r & 7)) << 4) + ((lane & 3) << 2);
-                __nv_bfloat162 hh, ll;
-                hh.x = h0; hh.y = h1;
-                ll.x = l0; ll.y = l1;
-                *reinterpret_cast<__nv_bfloat162 *>(st + off) = hh;
-                *reinterpret_cast<__nv_bfloat162 *>(st + BG_A_BYTES + off) = ll;
-            }
-            }
-            fence_proxy_async_smem();
-            named_bar_sync(1, BG_BUILD_THREADS);
-            if (tid == 0) {
-                mbar_wait(&bar_tma[s], (li >> 1) & 1, status, ERR_TIMEOUT_BAND, false);
+    if (warp == BG_MMA_WARP) {
+        // ---------------------------------------------------------------- band matrix TMA and MMAs (one thread)
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_f32(BG_M, npad);
+            int last_fill[2] = {-1, -1};      // parity of the last TMA issued into each stage, -1: none
+            bool ok = true;
+            for (int li = 0; li < nst && ok; ++li) {
+                const int s = li & 1, kb = kb0 + li;
+                uint8_t *st = smem + s * stage_bytes;
+                // the stage's B buffer is free once the MMAs of stage li - 2 have completed
+                if (li >= 2 && !mbar_wait(&empty[s], ((li - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND)) { ok = false; break; }
+                mbar_arrive_expect_tx(&full_b[s], 2 * b_bytes);
+                tma_load_2d(st + 2 * BG_A_BYTES, &tm_c_hi, kb * BG_K, 0, &full_b[s]);
+                tma_load_2d(st + 2 * BG_A_BYTES + b_bytes, &tm_c_lo, kb * BG_K, 0, &full_b[s]);
+                last_fill[s] = (li >> 1) & 1;
+                if (!mbar_wait(&full_a[s], (li >> 1) & 1, status, ERR_TIMEOUT_BAND) ||
+                    !mbar_wait(&full_b[s], (li >> 1) & 1, status, ERR_TIMEOUT_BAND)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t sa = smem_u32(st);
                 const uint32_t ahi = sa, alo = sa + BG_A_BYTES, bhi = sa + 2 * BG_A_BYTES, blo = bhi + b_bytes;
@@ -216,15 +126,103 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                     mma_bf16(tmem, sw128_desc(ahi + o), sw128_desc(blo + o), idesc, 1u);
                     mma_bf16(tmem, sw128_desc(alo + o), sw128_desc(bhi + o), idesc, 1u);
                 }
-                mma_commit(&bar_mma[s]);
+                mma_commit(&empty[s]);
             }
+            // every MMA issued completes on bar_done (the epilogue's wait, and the TMEM's release below); the copies
+            // still in flight land before the CTA may exit
+            mma_commit(bar_done);
+            for (int s = 0; s < 2; ++s)
+                if (last_fill[s] >= 0) mbar_wait(&full_b[s], (uint32_t)last_fill[s], status, ERR_TIMEOUT_BAND, false);
+            if (!ok) mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
         }
-        if (tid == 0) mma_commit(bar_done);
+    } else {
+        // ---------------------------------------------------------------- A operand builders (warps 0..7)
+        const float dl2 = (float)(a.dlnl * 1.4426950408889634);   // grid step in log2 units
+        const float inv_em1 = (float)(1.0 / expm1(a.dlnl));
+        // each warp builds 16 model rows, two at a time: lane l takes row parity l / 16 and pixels 4 (l % 16) ..
+        // 4 (l % 16) + 3 of the stage
+        const int q = lane & 15, hr = lane >> 4;
+        for (int li = 0; li < nst; ++li) {
+            const int s = li & 1, kb = kb0 + li;
+            uint8_t *st = smem + s * stage_bytes;
+            // the stage's A buffer is free once the MMAs of stage li - 2 have completed
+            if (li >= 2 && !mbar_wait(&empty[s], ((li - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND)) break;
+            const int j = a.j0 + kb * BG_K + 4 * q;          // first observed pixel of this lane
+            float wl[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) wl[u] = (j + u < a.nspec) ? __ldg(a.wl + j + u) : 0.f;
+            // the loads of all 8 rows first (rows whose 5 rest pixels lie inside the grid: the interior case), then
+            // the arithmetic
+            float sv[8][5];
+            bool inner[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = warp * 16 + 2 * i + hr;
+                const int2 rs = rsh[r];
+                const int c = j - rs.x;
+                inner[i] = rs.y != 2 && c >= 0 && c + 4 < a.nspec && j + 3 < a.nspec;
+                const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec + c;
+#pragma unroll
+                for (int u = 0; u < 5; ++u) sv[i][u] = inner[i] ? __ldg(sp + u) : 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = warp * 16 + 2 * i + hr;
+                float f[4];
+                if (inner[i]) {
+                    // v = s(c) + t (s(c + 1) - s(c)), t = 0 for whole shifts and the rest frame (v = s(c) exactly);
+                    // NaN -> 0 and negatives -> 0 in one fmaxf
+                    const float t = zsm[r].y;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float v = t > 0.f ? fmaf(t, sv[i][u + 1] - sv[i][u], sv[i][u]) : sv[i][u];
+                        f[u] = fmaxf(v, 0.f) * wl[u];
+                    }
+                } else {
+                    // the general case: no model, pixels past the grid's end, or intervals outside the grid (they
+                    // extrapolate from the first / last one, the reference's clamped find_interval: position
+                    // t = (e^(x dlnl) - 1) / (e^dlnl - 1), x pixels from the interval start)
+                    const float4 zs = zsm[r];
+                    const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int ju = j + u;
+                        float v = 0.f;
+                        if (zs.w == 1.f) {
+                            const int n0 = __float_as_int(zs.x);
+                            const int il = ju - n0 - ((zs.y > 0.f) ? 1 : 0);
+                            const int cc = min(max(il, 0), a.nspec - 2);
+                            const float tt = (cc == il) ? zs.y : (bg_ex2(((float)(ju - cc) - zs.z) * dl2) - 1.f) * inv_em1;
+                            const float x0 = __ldg(sp + cc), x1 = __ldg(sp + cc + 1);
+                            v = fmaf(tt, x1 - x0, x0);
+                        } else if (zs.w == 0.f && ju < a.nspec) {
+                            v = __ldg(sp + ju);
+                        }
+                        f[u] = fmaxf(v, 0.f) * wl[u];
+                    }
+                }
+                // bf16 hi and lo parts, four pixels = 8 bytes of the row's 128-byte swizzled line
+                const __nv_bfloat162 h01 = __floats2bfloat162_rn(f[0], f[1]), h23 = __floats2bfloat162_rn(f[2], f[3]);
+                const float2 g01 = __bfloat1622float2(h01), g23 = __bfloat1622float2(h23);
+                const __nv_bfloat162 l01 = __floats2bfloat162_rn(f[0] - g01.x, f[1] - g01.y);
+                const __nv_bfloat162 l23 = __floats2bfloat162_rn(f[2] - g23.x, f[3] - g23.y);
+                const uint32_t off = r * 128 + ((((uint32_t)q >> 1) ^ (r & 7)) << 4) + ((q & 1) << 3);
+                uint2 hv, lv;
+                hv.x = *reinterpret_cast<const uint32_t *>(&h01); hv.y = *reinterpret_cast<const uint32_t *>(&h23);
+                lv.x = *reinterpret_cast<const uint32_t *>(&l01); lv.y = *reinterpret_cast<const uint32_t *>(&l23);
+                *reinterpret_cast<uint2 *>(st + off) = hv;
+                *reinterpret_cast<uint2 *>(st + BG_A_BYTES + off) = lv;
+            }
+            // this warp's rows of the stage, visible to the tensor core's (async) reads
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full_a[s]);
+        }
         mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
         tc_fence_after();
 
         // epilogue: warps w and w + 4 read lane quarter w % 4 (one model per thread), columns 32 (w / 4) + 64 i
-        {
+        if (*(volatile int *)status == 0) {
             const int q = warp & 3;
             const int r = q * 32 + lane, m = m0 + r;
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);

@@ -806,8 +806,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev ? io.fband_dev + (size_t)nb * off : nullptr;
         ba.mags = (io.dev_inputs ? io.mags : c.d_mags.p) + (size_t)nb * off;
         ba.status = c.d_status.p;
-        ba.wz = d_wz + (size_t)nt * nz * off; ba.mass = c.d_mass.p; ba.llin = c.d_llin.p; ba.sums = nullptr; ba.nt = nt;
-        ba.ntz = nt * nz; ba.parts = wa.parts; ba.itesc = itesc;
         ba.num_sms = c.num_sms;
         const int ks = band_gemm_ksplit(nk, c.band_nkb, c.num_sms);
         if (ks > 1) {

@@ -124,11 +124,6 @@ struct BandGemmArgs {
     double *fband;          // n_models x nbands (may be null)
     double *mags;           // n_models x nbands (may be null)
     int *status;
-    // the FP64 mass / L_bol sums formed beside the GEMM (sums null: none)
-    const double *wz;       // n_models x ntz, age fastest
-    const double *mass, *llin;   // ntz
-    double *sums;           // n_models x 6 (as WeightsArgs::sums)
-    int nt, ntz, parts, itesc;
     // with few models, the pixels split over CTAs: partial band fluxes (ksplit x n_models x npad floats, at most
     // fpart_cap) summed by a second kernel that forms the magnitudes (fpart null: no split)
     float *fpart = nullptr;

@@ -150,8 +150,6 @@ int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zre
             ba.dlnl = c.dlnl; ba.dist = dist;
             ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
             ba.do_band = do_band; ba.fband = nullptr; ba.mags = d_mags; ba.status = status;
-            ba.wz = nullptr; ba.mass = nullptr; ba.llin = nullptr; ba.sums = nullptr;
-            ba.nt = c.nt; ba.ntz = c.nt * c.nz; ba.parts = 0; ba.itesc = 0;
             e = run_band_gemm(ba, c.tm_cb_hi, c.tm_cb_lo, st);
         }
         if (e == cudaSuccess && sync) {
