@@ -37,7 +37,9 @@ constexpr int NBGRAD = 44;
 enum { R_DUST1 = 1, R_DUST2 = 2, R_DUST3 = 3, R_DUST_INDEX = 4, R_DUST1_INDEX = 5, R_FRAC_OBRUN = 6,
        R_FRAC_NODUST = 7, R_ZRED = 22, R_SIGMA = 23, R_IGM_FACTOR = 32 };
 enum { G_DUST2 = 0, G_DUST_INDEX, G_FNODUST, G_DUST1, G_DUST1_INDEX, G_FOBRUN, G_DUST3, G_ZRED, G_IGMF, G_SIGMA,
-       G_OBS, NG };
+       G_OBS, G_WQ, G_WU, G_GAM, NG };
+// rows of the dust emission and the AGN torus (opensps.h)
+enum { R_FAGN = 0, R_DUSTE_QPAH = 10, R_DUSTE_UMIN = 11, R_DUSTE_GAMMA = 12, R_AGN_TAU = 31 };
 
 // The per-model block of the reverse pass (floats; KOBS and DDIST are doubles at 8-byte offsets), written by
 // adjoint_prep_kernel: the redshift factors b_k = (1 + z)^p_k and d b_k / dz, the smoothing taps' d / dsigma, the
@@ -48,6 +50,50 @@ __device__ __forceinline__ float adj_ex2(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// e^y - 1 as the forward's epilogue forms it: the Taylor series to y^6 below |y| = 1/8, else e^y - 1
+__device__ __forceinline__ float adj_expm1(float y) {
+    if (fabsf(y) < 0.125f) {
+        float r = 1.f + y * (1.f / 6.f);
+        r = 1.f + y * (1.f / 5.f) * r;
+        r = 1.f + y * (1.f / 4.f) * r;
+        r = 1.f + y * (1.f / 3.f) * r;
+        r = 1.f + y * (1.f / 2.f) * r;
+        return y * r;
+    }
+    return adj_ex2(y * 1.4426950408889634f) - 1.f;
+}
+
+// The dust emission's template at pixel i for a model's cell (dl07_shape, src/physics/opensps_csp_batch.f90:4103-4122:
+// bilinear in the q_PAH and U_min weights, the two components mixed by gamma, floored at the smallest normal), and
+// its derivatives in wq, wu and gamma (zero where the floor holds). tab: (2 numin x nqpah) columns of nspec, column
+// (2 u + c) nqpah + q.
+struct Dl07Val {
+    float shape, d_wq, d_wu, d_gam;
+};
+__device__ __forceinline__ Dl07Val dl07_eval(const float *tab, int ns, int nq, int i, const DustEmModel &d) {
+    const int k0 = 2 * d.iu, k1 = 2 * (d.iu + 1);
+    const float *a = tab + (size_t)i;
+    auto T = [&](int k, int q) { return __ldg(a + ((size_t)k * nq + q) * ns); };
+    const float a0 = T(k0, d.iq), a1 = T(k0, d.iq + 1), a2 = T(k1, d.iq + 1), a3 = T(k1, d.iq);
+    const float b0 = T(k0 + 1, d.iq), b1 = T(k0 + 1, d.iq + 1), b2 = T(k1 + 1, d.iq + 1), b3 = T(k1 + 1, d.iq);
+    const float wq = d.wq, wu = d.wu;
+    const float w00 = (1.f - wq) * (1.f - wu), w10 = wq * (1.f - wu), w11 = wq * wu, w01 = (1.f - wq) * wu;
+    const float lo = w00 * a0 + w10 * a1 + w11 * a2 + w01 * a3, hi = w00 * b0 + w10 * b1 + w11 * b2 + w01 * b3;
+    const float v = (1.f - d.gam) * lo + d.gam * hi;
+    Dl07Val r;
+    r.shape = fmaxf(v, FLT_MIN);
+    if (v < FLT_MIN) {
+        r.d_wq = r.d_wu = r.d_gam = 0.f;
+        return r;
+    }
+    const float lq = (1.f - wu) * (a1 - a0) + wu * (a2 - a3), hq = (1.f - wu) * (b1 - b0) + wu * (b2 - b3);
+    const float lu = (1.f - wq) * (a3 - a0) + wq * (a2 - a1), hu = (1.f - wq) * (b3 - b0) + wq * (b2 - b1);
+    r.d_wq = (1.f - d.gam) * lq + d.gam * hq;
+    r.d_wu = (1.f - d.gam) * lu + d.gam * hu;
+    r.d_gam = hi - lo;
+    return r;
 }
 
 // x 2^-k as FP32 on the integer pipes (GB300 has little FP64): round to nearest even on the dropped mantissa bits; a
@@ -172,17 +218,18 @@ __device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const ModelC
 
 // The reverse pass of one pixel: from dL / dTOT (tb), the forward's sums (y, o), the gradient accumulators and the
 // cotangents of y and o.
-__device__ __forceinline__ void pixel_adjoint(const AdjointArgs &a, const ModelConst &mc, int p, float y, float o,
-                                              float tb, float f_igm, float kf, float d1, float d2, float d3, float *g,
-                                              float &yb, float &ob) {
-    const PixFwd f = pix_forward(a, mc, p);
+__device__ __forceinline__ void pixel_adjoint(const AdjointArgs &a, const ModelConst &mc, const PixFwd &f, float y,
+                                              float o, float tb, float f_igm, float kf, float d1, float d2, float d3,
+                                              float pre_extra, float *g, float &yb, float &ob, float &T) {
     const float ss = y * f.ssfac_y + o * f.to;
     const float pre = ss * f.D;
     float pb = tb;
+    T = 1.f;
     if (f.igm) {
-        // T = exp(-igm_factor tau): dT/dz = -igm_factor T dtau/dz, dT/d igm_factor = -tau T
-        const float T = adj_ex2(f.tau * kf);
-        const float gT = pb * pre;
+        // T = exp(-igm_factor tau): dT/dz = -igm_factor T dtau/dz, dT/d igm_factor = -tau T (the dust emission's
+        // escaping light, pre_extra, passes through the IGM with the rest)
+        T = adj_ex2(f.tau * kf);
+        const float gT = pb * (pre + pre_extra);
         g[G_ZRED] = fmaf(gT, -f_igm * T * f.dtau, g[G_ZRED]);
         g[G_IGMF] = fmaf(gT, -f.tau * T, g[G_IGMF]);
         pb *= T;
@@ -222,6 +269,7 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     __shared__ float red[NG][ADJ_WARPS];
     __shared__ unsigned long long wmax[ADJ_WARPS];
     __shared__ double wsum[ADJ_WARPS];
+    __shared__ float emsum[3][ADJ_WARPS];   // the dust emission's and the AGN's per-warp sums
     const int m = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
     const float *ap = a.apar + (size_t)AP_FLOATS * m;
@@ -303,15 +351,71 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
         }
     const float f_igm = (float)pr[PF_IGM_FACTOR];
     const float kf = -f_igm * 1.4426950408889634f;
+    // dust emission and the AGN torus of this model (the forward's per-model epilogue, parts_epilogue_kernel)
+    DustEmModel dm{};
+    if (a.dem) dm = a.dem[m];
+    const bool emis = a.dem != nullptr && dm.on != 0;
+    const bool agn = a.dem != nullptr && dm.agn != 0;
+    double lsum_m = 1.0;
+    float lagn = 0.f;
+    if (agn) {
+        const double ls = a.lsum[(size_t)a.lsum_stride * m];
+        lsum_m = ls > SAFE_FLOOR ? ls : 1.0;
+        lagn = (float)(lsum_m * (double)dm.fagn);
+    }
+    const float *ag0 = agn ? a.agn_spec + (size_t)dm.ita * ns : nullptr, *ag1 = agn ? ag0 + ns : nullptr;
+    constexpr float LN2 = 0.6931471805599453f;
+    // 1 - T of each screen from its exponent (the forward's absorbed light, without cancellation)
+    auto one_minus = [&](const PixFwd &f, float &omb, float &omo, float &omd) {
+        omb = (mc.kd1 != 0.f) ? -adj_expm1(mc.kd1 * f.c1 * LN2) : 0.f;
+        omo = (mc.kd3 != 0.f) ? -adj_expm1(mc.kd3 * f.curve * LN2) : 0.f;
+        omd = mc.one_m_fnd * -adj_expm1(mc.kd2 * f.curve * LN2);
+    };
+    // block sums of up to three per-thread values into emsum, then every thread reads them
+    auto block_sums = [&](float v0, float v1, float v2, float *out) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            v0 += __shfl_xor_sync(0xffffffffu, v0, off);
+            v1 += __shfl_xor_sync(0xffffffffu, v1, off);
+            v2 += __shfl_xor_sync(0xffffffffu, v2, off);
+        }
+        if (lane == 0) { emsum[0][warp] = v0; emsum[1][warp] = v1; emsum[2][warp] = v2; }
+        __syncthreads();
+        out[0] = out[1] = out[2] = 0.f;
+        for (int w = 0; w < ADJ_WARPS; ++w) { out[0] += emsum[0][w]; out[1] += emsum[1][w]; out[2] += emsum[2][w]; }
+        __syncthreads();
+    };
 
-    // ---- pass 0: the pre-smoothing spectrum TOT = ss D T_igm (the forward's epilogue, recomputed)
+    // ---- pass 0: the pre-smoothing spectrum TOT = ss D T_igm (the forward's epilogue, recomputed), with dust
+    // emission the energy-balance sums and its escaping template through the IGM (in S, free until pass 1), with the
+    // AGN its template through the diffuse dust
     mbar_wait(&rows_bar, 0, a.status, ERR_TIMEOUT_ADJOINT, false);
+    float s_abs = 0.f, s_esc = 0.f, R_em = 0.f;
 #pragma unroll 2
     for (int p = tid; p < ns; p += ADJ_THREADS) {
         const PixFwd f = pix_forward(a, mc, p);
-        float tot = (yv[p] * f.ssfac_y + ov[p] * f.to) * f.D;
-        if (f.igm) tot *= adj_ex2(f.tau * kf);
+        const float T = f.igm ? adj_ex2(f.tau * kf) : 1.f;
+        float tot = (yv[p] * f.ssfac_y + ov[p] * f.to) * f.D * T;
+        if (emis) {
+            float omb, omo, omd;
+            one_minus(f, omb, omo, omd);
+            const float absorbed = yv[p] * (mc.one_m_fo * omb + f.ssfac_y * omd) + ov[p] * (omo + f.to * omd);
+            const float e = dl07_eval(a.dtab, ns, a.nqpah, p, dm).shape * f.td;
+            const float cn = __ldg(a.cnu + p);
+            s_abs = fmaf(cn, absorbed, s_abs);
+            s_esc = fmaf(cn, e, s_esc);
+            S[p] = e * T;
+        }
+        if (agn) tot = fmaf(lagn * fmaf(dm.wta, __ldg(ag1 + p) - __ldg(ag0 + p), __ldg(ag0 + p)), f.td, tot);
         TOT[p] = tot;
+    }
+    if (emis) {
+        float sums[3];
+        block_sums(s_abs, s_esc, 0.f, sums);
+        s_abs = sums[0];
+        s_esc = sums[1];
+        R_em = s_esc > SAFE_FLOOR ? s_abs / s_esc : 0.f;
+        for (int p = tid; p < ns; p += ADJ_THREADS) TOT[p] = fmaf(S[p], R_em, TOT[p]);
     }
     __syncthreads();
     // ---- pass 1: the smoothed spectrum S (pixels sm_lo .. sm_hi with the model's taps)
@@ -452,6 +556,31 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
 #pragma unroll
     for (int k = 0; k < NG; ++k) g[k] = 0.f;
     const float d2 = (float)pr[PF_DUST2], d3 = (float)pr[PF_DUST3], d1 = (float)pr[PF_DUST1];
+    // the dust emission's and the AGN's sums over the pixels (backward_emission_sums / backward_agn,
+    // src/physics/opensps_csp_batch.f90:6667-6845): R_bar = sum dL/dTOT T_igm shape T_d (E = R shape T_d T_igm is linear
+    // in R = s_abs / s_esc), s1 = sum dL/dTOT tmpl T_d, s2 = sum dL/dTOT (tmpl_hi - tmpl_lo) T_d
+    float em_sums[3] = {0.f, 0.f, 0.f};
+    if (emis || agn) {
+        float rb = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int p = tid; p < ns; p += ADJ_THREADS) {
+            const PixFwd f = pix_forward(a, mc, p);
+            const float sb = TOT[p];
+            if (emis) {
+                const float T = f.igm ? adj_ex2(f.tau * kf) : 1.f;
+                rb = fmaf(sb * T, dl07_eval(a.dtab, ns, a.nqpah, p, dm).shape * f.td, rb);
+            }
+            if (agn) {
+                const float t0 = __ldg(ag0 + p), t1 = __ldg(ag1 + p);
+                s1 = fmaf(sb, fmaf(dm.wta, t1 - t0, t0) * f.td, s1);
+                s2 = fmaf(sb, (t1 - t0) * f.td, s2);
+            }
+        }
+        block_sums(rb, s1, s2, em_sums);
+    }
+    // s_abs_bar = R_bar / s_esc, s_esc_bar = -R_bar s_abs / s_esc^2 (zero where the forward added no emission)
+    const bool em_on = emis && s_esc > SAFE_FLOOR;
+    const float sab = em_on ? em_sums[0] / s_esc : 0.f;
+    const float seb = em_on ? -em_sums[0] * (s_abs / s_esc) / s_esc : 0.f;
     __nv_bfloat162 *yh = reinterpret_cast<__nv_bfloat162 *>(a.ybar_hi + (size_t)m * a.ppad);
     __nv_bfloat162 *yl = reinterpret_cast<__nv_bfloat162 *>(a.ybar_lo + (size_t)m * a.ppad);
     __nv_bfloat162 *oh = reinterpret_cast<__nv_bfloat162 *>(a.obar_hi + (size_t)m * a.ppad);
@@ -463,7 +592,50 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
             for (int u2 = 0; u2 < 2; ++u2) {
                 const int q = p + u2;
                 if (q >= ns) break;
-                pixel_adjoint(a, mc, q, yv[q], ov[q], TOT[q], f_igm, kf, d1, d2, d3, g, yb[u2], ob[u2]);
+                const PixFwd f = pix_forward(a, mc, q);
+                const float y = yv[q], o = ov[q], sb = TOT[q];
+                Dl07Val dv{};
+                if (em_on) dv = dl07_eval(a.dtab, ns, a.nqpah, q, dm);
+                float T;
+                pixel_adjoint(a, mc, f, y, o, sb, f_igm, kf, d1, d2, d3, em_on ? R_em * dv.shape * f.td : 0.f, g,
+                              yb[u2], ob[u2], T);
+                if (em_on || agn) {
+                    float td_bar = 0.f;
+                    if (em_on) {
+                        // the escaping template E = R shape T_d T_igm, s_esc = sum cn shape T_d, and the absorbed
+                        // light in s_abs = sum cn (y A_y + o A_o), A_y = (1 - fo) (1 - T_b) + (T_b (1 - fo) + fo)
+                        // (1 - T_d) (1 - fnd), A_o = (1 - T_o) + T_o (1 - T_d) (1 - fnd)
+                        const float cn = __ldg(a.cnu + q), sbt = sb * T;
+                        td_bar = sbt * R_em * dv.shape + seb * cn * dv.shape;
+                        const float shape_bar = (sbt * R_em + seb * cn) * f.td;
+                        g[G_WQ] = fmaf(shape_bar, dv.d_wq, g[G_WQ]);
+                        g[G_WU] = fmaf(shape_bar, dv.d_wu, g[G_WU]);
+                        g[G_GAM] = fmaf(shape_bar, dv.d_gam, g[G_GAM]);
+                        float omb, omo, omd;
+                        one_minus(f, omb, omo, omd);
+                        const float A = sab * cn, yo = y * f.ssfac_y + o * f.to;
+                        yb[u2] = fmaf(A, mc.one_m_fo * omb + f.ssfac_y * omd, yb[u2]);
+                        ob[u2] = fmaf(A, omo + f.to * omd, ob[u2]);
+                        td_bar = fmaf(A * yo, -mc.one_m_fnd, td_bar);
+                        g[G_FOBRUN] = fmaf(A * y, omb * (omd - 1.f), g[G_FOBRUN]);
+                        g[G_FNODUST] = fmaf(A * yo, -(1.f - f.td), g[G_FNODUST]);
+                        if (mc.kd1 != 0.f) {
+                            const float tbb = A * y * mc.one_m_fo * (omd - 1.f);
+                            g[G_DUST1] = fmaf(tbb, -f.c1 * f.tb, g[G_DUST1]);
+                            g[G_DUST1_INDEX] = fmaf(tbb, -d1 * f.c1 * f.ltab * f.tb, g[G_DUST1_INDEX]);
+                        }
+                        if (mc.kd3 != 0.f) {
+                            const float tob = A * o * (omd - 1.f);
+                            g[G_DUST3] = fmaf(tob, -f.curve * f.to, g[G_DUST3]);
+                            g[G_DUST_INDEX] = fmaf(tob, -d3 * f.curve * f.ltab * f.to, g[G_DUST_INDEX]);
+                        }
+                    }
+                    // the AGN: lagn tmpl T_d
+                    if (agn) td_bar = fmaf(sb * lagn, fmaf(dm.wta, __ldg(ag1 + q) - __ldg(ag0 + q), __ldg(ag0 + q)), td_bar);
+                    // T_d = exp(-dust2 curve)
+                    g[G_DUST2] = fmaf(td_bar, -f.curve * f.td, g[G_DUST2]);
+                    g[G_DUST_INDEX] = fmaf(td_bar, -d2 * f.curve * f.ltab * f.td, g[G_DUST_INDEX]);
+                }
             }
         }
         const __nv_bfloat162 hy = bf16_hi2(yb[0], yb[1]), ho = bf16_hi2(ob[0], ob[1]);
@@ -484,17 +656,29 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     __syncthreads();
     if (tid < NBGRAD) {
         const double c = ldexp(1.0, ks);
-        const int row_of[NG - 1] = {R_DUST2, R_DUST_INDEX, R_FRAC_NODUST, R_DUST1, R_DUST1_INDEX, R_FRAC_OBRUN,
-                                    R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA};
+        constexpr int NROW = 10;
+        const int row_of[NROW] = {R_DUST2, R_DUST_INDEX, R_FRAC_NODUST, R_DUST1, R_DUST1_INDEX, R_FRAC_OBRUN,
+                                  R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA};
         double v = 0.0;
         int k = -1;
 #pragma unroll
-        for (int i = 0; i < NG - 1; ++i)
+        for (int i = 0; i < NROW; ++i)
             if (row_of[i] == tid) k = i;
+        // the dust emission's rows: d / d(wq, wu, gam) times the chain factors to q_PAH, U_min, gamma
+        float chain = 0.f;
+        if (emis && a.dchain) {
+            const float4 dc = a.dchain[m];
+            if (tid == R_DUSTE_QPAH) { k = G_WQ; chain = dc.x; }
+            if (tid == R_DUSTE_UMIN) { k = G_WU; chain = dc.y; }
+            if (tid == R_DUSTE_GAMMA) { k = G_GAM; chain = dc.z; }
+        }
         if (k >= 0) {
             for (int w = 0; w < ADJ_WARPS; ++w) v += (double)red[k][w];
             v *= c;
+            if (k >= G_WQ) v *= (double)chain;
         }
+        if (agn && tid == R_FAGN) v = c * lsum_m * (double)em_sums[1];
+        if (agn && tid == R_AGN_TAU && a.dchain) v = c * lsum_m * (double)dm.fagn * (double)em_sums[2] * (double)a.dchain[m].w;
         if (tid == R_ZRED) {
             // the observed frame's share (its factor formed in FP64 per model) and the distance term's
             double go = 0.0, ms = 0.0;
@@ -507,6 +691,11 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     }
     if (tid == 0) {
         a.cscale[m] = ldexp(1.0, ks);
+        // the AGN's cotangent of the linear L_bol (fagn s1 where the forward did not floor it), unscaled
+        if (a.lsum_bar) {
+            const double ls = agn ? a.lsum[(size_t)a.lsum_stride * m] : 0.0;
+            a.lsum_bar[m] = (agn && ls > SAFE_FLOOR) ? ldexp(1.0, ks) * (double)dm.fagn * (double)em_sums[1] : 0.0;
+        }
         // (a wait above that gave up leaves the bulk copies to be waited for here, before the CTA exits)
         mbar_wait(&rows_bar, 0, a.status, ERR_TIMEOUT_ADJOINT, false);
     }
@@ -534,12 +723,13 @@ __global__ void transpose_bf16_kernel(const __nv_bfloat16 *__restrict__ src, __n
 
 // ---------------------------------------------------------------------------------------------- weights' cotangent
 // wzb(t + nt z, m) = cscale_m D(m, col(t, z)) + mass_bar_m M(t, z) + lsum_bar_m L(t, z), lsum_bar = lbol_bar /
-// (ln 10 L_bol) (backward_age_sums_w; the ssp_weights_z branch of compute_csp_batch's reverse pass).
+// (ln 10 L_bol) plus the AGN's (backward_age_sums_w; the ssp_weights_z branch of compute_csp_batch's reverse pass).
 struct WzbArgs {
     int n_models, ntz, ldd;
     const float *D;
     const int *col_of;
     const double *cscale, *mass_bar, *lbol_bar, *sums, *mass, *llin;
+    const double *lsum_bar = nullptr;   // n_models: the AGN's cotangent of the linear L_bol (null: none)
     double *wzb;
 };
 __global__ void wzbar_kernel(WzbArgs a) {
@@ -553,6 +743,7 @@ __global__ void wzbar_kernel(WzbArgs a) {
         const double ls = a.sums[(size_t)6 * m + 1];
         if (ls > SAFE_FLOOR) v += a.lbol_bar[m] / (ls * 2.302585092994046) * a.llin[k];
     }
+    if (a.lsum_bar) v += a.lsum_bar[m] * a.llin[k];
     a.wzb[i] = v;
 }
 
@@ -754,6 +945,17 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     a.lt_step = (float)(c.dlnl * 1.4426950408889634);
     a.ybar_hi = c.d_ybh.p; a.ybar_lo = c.d_ybl.p; a.obar_hi = c.d_obh.p; a.obar_lo = c.d_obl.p;
     a.cscale = c.d_cscale.p; a.params_bar = c.d_pbar.p; a.status = c.d_status.p;
+    if (c.geom.emis || c.geom.agn) {
+        // the forward's dust emission / AGN (the AGN's L_bol: the batch's linear FP64 sum)
+        a.dem = c.d_dem.p; a.dchain = c.d_dchain.p;
+        a.dtab = c.dustem.tab.p; a.cnu = c.dustem.cnu.p; a.nqpah = c.dustem.nqpah;
+        a.agn_spec = c.agn.spec.p;
+        a.lsum = c.d_sums.p + 1; a.lsum_stride = 6;
+        if (c.geom.agn) {
+            if ((e = c.d_lsum_bar.reserve(n)) != cudaSuccess) { err = msg("device memory", e); return ST_DATA_MISSING; }
+            a.lsum_bar = c.d_lsum_bar.p;
+        }
+    }
     prof_mark(c, 6);
     if ((e = run_adjoint(pa, a, s)) != cudaSuccess) { err = msg("adjoint kernel", e); return ST_DATA_MISSING; }
     prof_mark(c, 7);
@@ -843,6 +1045,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         // (the log-blended L_bol of weights formed on the device has its own cotangent, in the SFH reverse pass)
         w.lbol_bar = (lbol_bar && !dev_blend) ? c.d_lbol_bar.p : nullptr;
         w.sums = c.d_sums.p; w.mass = c.d_mass.p; w.llin = c.d_llin.p;
+        w.lsum_bar = c.geom.agn ? c.d_lsum_bar.p : nullptr;
         w.wzb = c.d_wzbar.p;
         const size_t tot = (size_t)n * ntz;
         wzbar_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(w);

@@ -565,7 +565,13 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     DustEmModel *dem = nullptr;            // the per-model cells, page-locked (uploaded beside the parameter table)
     if (epi_terms) {
         if (fp64) { err = "dust emission, AGN and the nebular continuum are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts) { err = "gradients with dust emission, AGN or the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts && neb_cont) { err = "gradients with the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
+        if (io.keep_parts && any_agn && (c.ops.ready || io.sfh_par)) {
+            // (the AGN scales with the L_bol the batch outputs: its cotangent goes into the weights through the linear
+            // L_bol sum of weights over ages and metallicities only)
+            err = "gradients with the AGN torus need weights over ages and metallicities (ssp_weights_z) without SSP operators";
+            return ST_UNSUPPORTED;
+        }
         if (io.dev_inputs) { err = "dust emission, AGN and the nebular continuum need host inputs on this path"; return ST_UNSUPPORTED; }
         if (neb_cont && c.ops.ready) { err = "the nebular continuum with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
         if (any_emis) { if (int rc = dustem_load(c, err)) return rc; }
@@ -591,6 +597,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             c.pinned_dem_n = (size_t)n;
         }
         dem = c.pinned_dem;
+        if (io.keep_parts) c.h_dchain.assign((size_t)n, make_float4(0.f, 0.f, 0.f, 0.f));
         for (int m = 0; m < n; ++m) {
             DustEmModel &q = dem[m];
             q = DustEmModel{};
@@ -604,6 +611,25 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             if (q.agn) {
                 cell(c.agn.tau, par(m, PF_AGN_TAU), q.ita, q.wta);
                 q.fagn = (float)par(m, PF_FAGN);
+            }
+            if (io.keep_parts) {
+                // the reverse pass's chain factors (batch_chain_derivatives, opensps_csp_batch.f90:4701-4706; agn_tau_slope
+                // :1598-1608): 1 / the cell's width where the parameter lies in the cell (its ends included), gamma within
+                // [0, 1]; agn_tau within [tau_1, tau_n)
+                float4 dc = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (q.on) {
+                    const double xq = par(m, PF_DUSTE_QPAH), xu = par(m, PF_DUSTE_UMIN), xg = par(m, PF_DUSTE_GAMMA);
+                    if (xq >= d.qpah[q.iq] && xq <= d.qpah[q.iq + 1]) dc.x = (float)(1.0 / (d.qpah[q.iq + 1] - d.qpah[q.iq]));
+                    if (xu >= d.umin[q.iu] && xu <= d.umin[q.iu + 1]) dc.y = (float)(1.0 / (d.umin[q.iu + 1] - d.umin[q.iu]));
+                    if (xg >= 0.0 && xg <= 1.0) dc.z = 1.f;
+                }
+                if (q.agn) {
+                    const std::vector<double> &ta = c.agn.tau;
+                    const double xt = par(m, PF_AGN_TAU);
+                    if (ta.size() >= 2 && xt >= ta.front() && xt < ta.back())
+                        dc.w = (float)(1.0 / (ta[q.ita + 1] - ta[q.ita]));
+                }
+                c.h_dchain[m] = dc;
             }
             if (neb_cont) {
                 // get_grid_indices_weights (opensps_gas.f90:394-412) in gas_logz and gas_logu; fabs = 1 - frac_obrun
@@ -670,6 +696,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.geom.itesc = itesc;
     c.geom.wz = nullptr;
     c.geom.n = 0;
+    c.geom.emis = epi_terms && any_emis;
+    c.geom.agn = epi_terms && any_agn;
 
     // ---- scratch
     const int bn = contract_models_per_tile(nacc);
@@ -746,6 +774,12 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         if (dem && ((e = c.d_dem.reserve(n)) != cudaSuccess ||
                     (e = cudaMemcpyAsync(c.d_dem.p, dem, sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, cs)) != cudaSuccess)) {
             err = cuda_msg("dust emission inputs", e);
+            return ST_DATA_MISSING;
+        }
+        if (dem && io.keep_parts &&
+            ((e = c.d_dchain.reserve(n)) != cudaSuccess ||
+             (e = cudaMemcpyAsync(c.d_dchain.p, c.h_dchain.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, cs)) != cudaSuccess)) {
+            err = cuda_msg("dust emission chain factors", e);
             return ST_DATA_MISSING;
         }
         if (chunked) {

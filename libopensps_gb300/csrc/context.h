@@ -154,6 +154,7 @@ struct BatchGeom {
     int nacc = 0, sm_lo = 0, sm_hi = -1, uniform_index = 0, n = 0;
     int itesc = 0;               // the first old age
     const double *wz = nullptr;  // the weights over ages and metallicities on the device (with the operators)
+    bool emis = false, agn = false;   // the batch had dust emission / the AGN torus (cells in d_dem, chains in d_dchain)
 };
 
 struct Context {
@@ -235,6 +236,11 @@ struct Context {
     // templates
     DustEmission dustem;
     AgnTorus agn;
+    // the reverse pass with dust emission / AGN: per model the chain factors (d wq / d q_PAH, d wu / d U_min,
+    // d gam / d gamma, d wta / d agn_tau) and the AGN's cotangent of the linear L_bol
+    std::vector<float4> h_dchain;
+    DevBuf<float4> d_dchain;
+    DevBuf<double> d_lsum_bar;
     NebularGrid neb;
     std::string isoc = "synthetic";   // the isochrone set of the setup (names the nebular libraries)
     SspOps ops;

@@ -183,6 +183,16 @@ struct AdjointPrepArgs {
     const double *zt, *dl;           // cosmology table (500)
     float *apar;                     // n_models x 32: the per-model block of the reverse pass
 };
+struct DustEmModel {
+    int on, iq, iu;
+    float wq, wu, gam;
+    int agn, ita;
+    float wta, fagn;
+    // the nebular continuum's CLOUDY cell: the lower corner (0-based, clamped so that the cell lies in the grid) and
+    // the weights (clamped to [0, 1]) in gas_logz and gas_logu, and |1 - frac_obrun|
+    int neb_iz, neb_iu;
+    float neb_wz, neb_wu, neb_fabs;
+};
 struct AdjointArgs {
     int n_models, nspec, ppad, nbands, jtop, j0, j1, sm_lo, sm_hi, uniform_index;
     float dl2, inv_em1;              // dlnl log2(e), 1 / (e^dlnl - 1)
@@ -205,6 +215,18 @@ struct AdjointArgs {
     double *cscale;                  // n_models: the cotangent scale (the A operands are divided by it)
     double *params_bar;              // n_models x 44
     int *status;
+    // dust emission and the AGN torus (dem null: neither): per model the cells (DustEmModel), the Draine & Li
+    // templates and the frequency trapezoid weights (as PartsEpilogueArgs), the AGN templates, each model's linear
+    // L_bol (lsum at lsum_stride m: the AGN's scale), the chain factors (d wq / d q_PAH, d wu / d U_min, d gam / d gamma,
+    // d wta / d agn_tau) and the AGN's cotangent of the linear L_bol (lsum_bar, n_models, unscaled; null: not wanted)
+    const DustEmModel *dem = nullptr;
+    const float *dtab = nullptr, *cnu = nullptr;
+    int nqpah = 0;
+    const float *agn_spec = nullptr;
+    const double *lsum = nullptr;
+    int lsum_stride = 6;
+    const float4 *dchain = nullptr;
+    double *lsum_bar = nullptr;
 };
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 
@@ -306,16 +328,7 @@ cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);
 // A model's emission terms of the per-model epilogue: dust emission (on, the Draine & Li grid cell iq, iu: 0-based
 // lower corner, with its weights and gamma: dl07_indices, src/physics/opensps_csp_batch.f90:1622-1634) and the AGN
 // torus (agn, the template interval ita with its weight and fagn: agn_indices :1575-1589).
-struct DustEmModel {
-    int on, iq, iu;
-    float wq, wu, gam;
-    int agn, ita;
-    float wta, fagn;
-    // the nebular continuum's CLOUDY cell: the lower corner (0-based, clamped so that the cell lies in the grid) and
-    // the weights (clamped to [0, 1]) in gas_logz and gas_logu, and |1 - frac_obrun|
-    int neb_iz, neb_iu;
-    float neb_wz, neb_wu, neb_fabs;
-};
+
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
     const float *pix, *mpar;

@@ -109,9 +109,6 @@ def test_dust_emission_refusals(data, built_lib):
     params = dict(params, dust1=np.full(n, 0.3))
     c = Context()
     c.set_int("add_dust_emission", 1)
-    with pytest.raises(OpenSPSError) as e:
-        c.csp_batch_grad(params, wz, mags_bar=np.ones((n, c.nbands)))
-    assert e.value.status == 2
     c.set_int("gb300_fp64", 1)
     with pytest.raises(OpenSPSError) as e:
         c.csp_batch(params, ssp_weights_z=wz)
