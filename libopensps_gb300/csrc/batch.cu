@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 #include "context.h"
+#include "datalib.h"
 
 namespace sps {
 
@@ -563,6 +564,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     c.last_ion = ion_terms;
     DustEmModel *dem = nullptr;            // the per-model cells, page-locked (uploaded beside the parameter table)
+    std::vector<int2> neb_chunk_groups;    // the nebular continuum: per chunk its first group and group count
     if (epi_terms) {
         if (fp64) { err = "dust emission, AGN and the nebular continuum are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
         if (io.keep_parts && neb_cont) { err = "gradients with the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
@@ -637,6 +639,36 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                 cell(c.neb.logz, par(m, PF_GAS_LOGZ), q.neb_iz, q.neb_wz);
                 cell(c.neb.logu, par(m, PF_GAS_LOGU), q.neb_iu, q.neb_wu);
                 q.neb_fabs = (float)std::fabs(1.0 - par(m, PF_FRAC_OBRUN));
+            }
+        }
+        if (neb_cont) {
+            // per chunk, its models with a continuum sorted by their (gas_logz, gas_logu) cell (chunk-relative
+            // indices) and cut into groups of at most NEB_GROUP (cell z, cell u, first index into the order, count)
+            c.neb.h_order.clear();
+            c.neb.h_groups.clear();
+            const int ncell = (NEB_NZ - 1) * (NEB_NU - 1);
+            std::vector<int> cnt(ncell + 1);
+            for (int k = 0; k < nch; ++k) {
+                const int off = chunk_off(k), nk = chunk_len(k);
+                std::fill(cnt.begin(), cnt.end(), 0);
+                for (int i = 0; i < nk; ++i) {
+                    const DustEmModel &q = dem[off + i];
+                    if (q.neb_fabs > 0.f) ++cnt[q.neb_iz * (NEB_NU - 1) + q.neb_iu + 1];
+                }
+                for (int cc = 0; cc < ncell; ++cc) cnt[cc + 1] += cnt[cc];
+                const size_t base = c.neb.h_order.size();
+                c.neb.h_order.resize(base + (size_t)cnt[ncell]);
+                std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+                for (int i = 0; i < nk; ++i) {
+                    const DustEmModel &q = dem[off + i];
+                    if (q.neb_fabs > 0.f) c.neb.h_order[base + pos[q.neb_iz * (NEB_NU - 1) + q.neb_iu]++] = i;
+                }
+                const int g0 = (int)c.neb.h_groups.size();
+                for (int cc = 0; cc < ncell; ++cc)
+                    for (int j = cnt[cc]; j < cnt[cc + 1]; j += NEB_GROUP)
+                        c.neb.h_groups.push_back(make_int4(cc / (NEB_NU - 1), cc % (NEB_NU - 1), (int)base + j,
+                                                           std::min(NEB_GROUP, cnt[cc + 1] - j)));
+                neb_chunk_groups.push_back(make_int2(g0, (int)c.neb.h_groups.size() - g0));
             }
         }
     }
@@ -771,6 +803,17 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("parameter copy", e);
             return ST_DATA_MISSING;
         }
+        if (neb_cont && ((e = c.neb.order.reserve(std::max<size_t>(c.neb.h_order.size(), 1))) != cudaSuccess ||
+                         (e = c.neb.groups.reserve(std::max<size_t>(c.neb.h_groups.size(), 1))) != cudaSuccess ||
+                         (!c.neb.h_order.empty() &&
+                          (e = cudaMemcpyAsync(c.neb.order.p, c.neb.h_order.data(), sizeof(int) * c.neb.h_order.size(),
+                                               cudaMemcpyHostToDevice, cs)) != cudaSuccess) ||
+                         (!c.neb.h_groups.empty() &&
+                          (e = cudaMemcpyAsync(c.neb.groups.p, c.neb.h_groups.data(), sizeof(int4) * c.neb.h_groups.size(),
+                                               cudaMemcpyHostToDevice, cs)) != cudaSuccess))) {
+            err = cuda_msg("nebular continuum groups", e);
+            return ST_DATA_MISSING;
+        }
         if (dem && ((e = c.d_dem.reserve(n)) != cudaSuccess ||
                     (e = cudaMemcpyAsync(c.d_dem.p, dem, sizeof(DustEmModel) * n, cudaMemcpyHostToDevice, cs)) != cudaSuccess)) {
             err = cuda_msg("dust emission inputs", e);
@@ -862,10 +905,22 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         pe.dtab = c.dustem.tab.p; pe.cnu = c.dustem.cnu.p; pe.nqpah = c.dustem.nqpah;
         pe.agn_spec = c.agn.spec.p;
         if (neb_cont) {
-            pe.neb_tab = c.neb.tab[neb_table].p; pe.neb_off = c.neb.off.p;
-            pe.neb_age4 = reinterpret_cast<const float4 *>(c.neb.age4.p); pe.neb_q0 = c.neb.q0.p;
-            pe.wz = d_wz + (size_t)nt * nz * off;
-            pe.nt = nt; pe.nz = nz; pe.nt_neb = c.nt_neb; pe.itesc = itesc;
+            // the CLOUDY-grid continuum into the young and old sums of models [off, off + nk) (their groups by cell)
+            const int2 cg = neb_chunk_groups[chunked ? off / CHUNK : 0];
+            NebContArgs na;
+            na.n = nk; na.nspec = ns; na.nt = nt; na.nz = nz; na.nt_neb = c.nt_neb; na.itesc = itesc;
+            na.cw_ld = c.nt_neb + 2;
+            na.dem = d_dem + off; na.tab = c.neb.tab[neb_table].p; na.off = c.neb.off.p;
+            na.age4 = reinterpret_cast<const float4 *>(c.neb.age4.p); na.tstart = c.neb.tstart.p; na.q0 = c.neb.q0.p;
+            na.wz = d_wz + (size_t)nt * nz * off;
+            na.groups = c.neb.groups.p + cg.x; na.order = c.neb.order.p;
+            cudaError_t r = c.neb.cw.reserve((size_t)nk * na.cw_ld);
+            if (r != cudaSuccess) return r;
+            na.cw = c.neb.cw.p;
+            na.young = const_cast<float *>(y) + (size_t)ns * off;
+            na.old = const_cast<float *>(o) + (size_t)ns * off;
+            if ((r = run_nebular_continuum(na, cg.y, st)) != cudaSuccess) return r;
+            launches += 2;
         }
         // (the model's L_bol output: log-blended between the slabs for weights formed on the device, except with
         // the operators, whose L_bol is their linear row)

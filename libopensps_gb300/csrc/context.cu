@@ -573,6 +573,14 @@ int nebular_load(Context &c, std::string &err) {
         a4[4 * t + 3] = (float)newr[t];
     }
     if (e == cudaSuccess) e = upload(c.neb.age4, a4.data(), a4.size());
+    // the ages of each interval are a run (ia grows with t): tstart[k] = the first age with ia >= k, tstart[9] = nt_neb
+    std::vector<int> ts(NEB_NAGE, c.nt_neb);
+    for (int k = 0; k < NEB_NAGE - 1; ++k) {
+        int t = 0;
+        while (t < c.nt_neb && ia[t] < k) ++t;
+        ts[k] = t;
+    }
+    if (e == cudaSuccess) e = upload(c.neb.tstart, ts.data(), ts.size());
     if (e != cudaSuccess) {
         err = std::string("nebular grid: ") + cudaGetErrorString(e);
         c.neb.release();

@@ -145,7 +145,19 @@ struct NebularGrid {
     std::vector<double> logz, lage, logu;
     DevBuf<float> tab[2], off, age4;
     DevBuf<double> q0;
-    void release() { tab[0].release(); tab[1].release(); off.release(); age4.release(); q0.release(); have[0] = have[1] = false; }
+    DevBuf<int> tstart;          // NEB_NAGE ints: the first nebular age of each CLOUDY interval (the last: nt_neb)
+    // a batch's continuum: the models sorted by cell and their groups (host staging and device copies), the per-model
+    // weights (scratch)
+    std::vector<int> h_order;
+    std::vector<int4> h_groups;
+    DevBuf<int> order;
+    DevBuf<int4> groups;
+    DevBuf<float> cw;
+    void release() {
+        tab[0].release(); tab[1].release(); off.release(); age4.release(); q0.release(); tstart.release();
+        order.release(); groups.release(); cw.release();
+        have[0] = have[1] = false;
+    }
 };
 
 // What the reverse pass needs of the forward batch it follows.

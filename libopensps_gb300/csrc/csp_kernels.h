@@ -344,16 +344,29 @@ struct PartsEpilogueArgs {
     const float *agn_spec = nullptr;
     const double *lsum = nullptr;
     int lsum_stride = 6;
-    // the CLOUDY-grid nebular continuum (neb_tab null: none): the table (log2 less the pixel's offset,
-    // [logZ][logU][age][pixel]), the offsets, per nebular age its interval float4 and q0 (nt_neb x nz), the FP64
-    // weights of the models (n x nz x nt), the ages below itesc young
-    const float *neb_tab = nullptr, *neb_off = nullptr;
-    const float4 *neb_age4 = nullptr;
-    const double *neb_q0 = nullptr, *wz = nullptr;
-    int nt = 0, nz = 0, nt_neb = 0, itesc = 0;
 };
-constexpr int NEB_MAX_AGES = 128;         // nebular ages the epilogue's continuum takes
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
+
+// The CLOUDY-grid nebular continuum added to the young and old sums (ssp_op.cu): n models, their cells in dem, the
+// table (log2 less the pixel's integer offset, [logZ][logU][age][pixel]) and offsets, per nebular age its interval
+// float4 (lower node as int bits, wa, dwa, newr) and each CLOUDY interval's first nebular age (tstart), q0 (nt_neb x
+// nz), the FP64 weights (n x nz x nt), the ages below itesc young; groups: (cell z, cell u, first index into order,
+// count <= NEB_GROUP), order: the models sorted by cell; cw: scratch, n x cw_ld floats (cw_ld >= nt_neb + 2).
+constexpr int NEB_MAX_AGES = 128;         // nebular ages the continuum takes
+constexpr int NEB_GROUP = 32;             // models per group of one cell
+struct NebContArgs {
+    int n, nspec, nt, nz, nt_neb, itesc, cw_ld;
+    const DustEmModel *dem;
+    const float *tab, *off;
+    const float4 *age4;
+    const int *tstart;
+    const double *q0, *wz;
+    const int4 *groups;
+    const int *order;
+    float *cw;
+    float *young, *old;       // n x nspec
+};
+cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

@@ -800,10 +800,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
     float *esm = tsm + a.nspec;
     __shared__ float red[2][8];
-    __shared__ double ncs[NEB_MAX_AGES];   // the continuum's per-age weights C(t) (FP64)
-    __shared__ float ncn[NEB_MAX_AGES];    // C(t) / max C
-    __shared__ float4 nag[NEB_MAX_AGES];   // per nebular age: interval, wa, dwa, newr
-    __shared__ double nmax;
     const int ns = a.nspec, m = blockIdx.x;
     const float *mp = a.mpar + (size_t)MODEL_PAR_FLOATS * m;
     const float *yv = a.young + (size_t)m * ns, *ov = a.old + (size_t)m * ns;
@@ -823,83 +819,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
         const double ls = a.lsum[(size_t)a.lsum_stride * m];
         lagn = (float)((ls > SAFE_FLOOR ? ls : 1.0) * (double)dm.fagn);
     }
-    // the CLOUDY-grid nebular continuum (nebular_kernels step 3, src/physics/opensps_csp_batch.f90:2760-2910): per
-    // nebular age t the weight C(t) = |1 - frac_obrun| sum_z w(t, z) q0(t, z) (the SFH weight times the ionizing
-    // photon rate, over the model's metallicities), normalised by its largest value S (log2 S joins the exponent:
-    // its integer part with the pixel's integer offset exactly, the rest with the table); per pixel the sum over t of
-    // C(t) 2^lg(t) with lg the table interpolated bilinearly in (log Z, log U) at the model's cell and linearly in age
-    // within the CLOUDY age interval, where 2^lg advances geometrically (one exponential per interval and per step)
-    const bool nebc_in = a.neb_tab != nullptr && dm.neb_fabs > 0.f;
-    if (nebc_in) {
-        const double *w = a.wz + (size_t)m * a.nz * a.nt;
-        for (int t = threadIdx.x; t < a.nt_neb; t += blockDim.x) {
-            double cs = 0.0;
-            for (int z = 0; z < a.nz; ++z) {
-                const double wv = __ldg(w + (size_t)z * a.nt + t);
-                if (wv > SAFE_FLOOR) cs = fma(wv, __ldg(a.neb_q0 + (size_t)t * a.nz + z), cs);
-            }
-            ncs[t] = cs * (double)dm.neb_fabs;
-            nag[t] = __ldg(a.neb_age4 + t);
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            double mx = 0.0;
-            for (int t = threadIdx.x; t < a.nt_neb; t += 32) mx = fmax(mx, ncs[t]);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-            if (threadIdx.x == 0) nmax = mx;
-        }
-        __syncthreads();
-        for (int t = threadIdx.x; t < a.nt_neb; t += blockDim.x) ncn[t] = nmax > 0.0 ? (float)(ncs[t] / nmax) : 0.f;
-        __syncthreads();
-    }
-    const bool nebc = nebc_in && nmax > 0.0;
-    float n_sint = 0.f, n_sfrac = 0.f;
-    const float *nt00 = nullptr, *nt01 = nullptr, *nt10 = nullptr, *nt11 = nullptr;
-    float nc00 = 0.f, nc01 = 0.f, nc10 = 0.f, nc11 = 0.f;
-    if (nebc) {
-        const double s2 = log2(nmax), si = floor(s2);
-        n_sint = (float)si;
-        n_sfrac = (float)(s2 - si);
-        constexpr int NU = 7, NA = 10;     // the CLOUDY grid's logU and age counts
-        const size_t plane = (size_t)NA * ns;
-        nt00 = a.neb_tab + (size_t)(dm.neb_iz * NU + dm.neb_iu) * plane;
-        nt01 = nt00 + plane;
-        nt10 = a.neb_tab + (size_t)((dm.neb_iz + 1) * NU + dm.neb_iu) * plane;
-        nt11 = nt10 + plane;
-        nc00 = (1.f - dm.neb_wz) * (1.f - dm.neb_wu);
-        nc01 = (1.f - dm.neb_wz) * dm.neb_wu;
-        nc10 = dm.neb_wz * (1.f - dm.neb_wu);
-        nc11 = dm.neb_wz * dm.neb_wu;
-    }
-    // the continuum at pixel p into the young (t < itesc) and old sums
-    auto neb_add = [&](int p, float &y, float &o) {
-        auto bil = [&](int k) {
-            const size_t i = (size_t)k * ns + p;
-            return fmaf(nc00, __ldg(nt00 + i), fmaf(nc01, __ldg(nt01 + i), fmaf(nc10, __ldg(nt10 + i), nc11 * __ldg(nt11 + i))));
-        };
-        const float e_int = __ldg(a.neb_off + p) + n_sint;      // an integer: exact
-        float ys = 0.f, os = 0.f, sy = 0.f, so = 0.f, ra = 0.f, rb = 0.f, dl = 0.f, f = 0.f, r = 1.f;
-        int a_prev = -1;
-        for (int t = 0; t < a.nt_neb; ++t) {
-            const float4 ag = nag[t];
-            const int k = __float_as_int(ag.x);
-            if (k != a_prev) {
-                ys += sy; os += so; sy = 0.f; so = 0.f;
-                ra = (a_prev >= 0 && k == a_prev + 1) ? rb : bil(k);   // (the first interval has no predecessor)
-                rb = bil(k + 1);
-                a_prev = k;
-                dl = rb - ra;
-                f = ops_ex2((n_sfrac + fmaf(ag.y, dl, ra)) + e_int);
-            } else {
-                if (ag.w != 0.f) r = ops_ex2(ag.z * dl);
-                f *= r;
-            }
-            if (t < a.itesc) sy = fmaf(ncn[t], f, sy); else so = fmaf(ncn[t], f, so);
-        }
-        y += ys + sy;
-        o += os + so;
-    };
     constexpr float LN2 = 0.6931471805599453f;
     float sa = 0.f, se = 0.f;
     // (ln lambda log2 e, the shared diffuse curve) of a pixel
@@ -972,10 +891,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
                     g1 = __ldg(gb + q);
                 }
                 float e0 = 0.f, e1 = 0.f;
-                if (nebc) {
-                    neb_add(2 * q, yy[u].x, oo[u].x);
-                    neb_add(2 * q + 1, yy[u].y, oo[u].y);
-                }
                 const float t0 = pass1(2 * q, yy[u].x, oo[u].x, sh.x, cn.x, g0.x, g1.x, e0);
                 const float t1 = pass1(2 * q + 1, yy[u].y, oo[u].y, sh.y, cn.y, g0.y, g1.y, e1);
                 reinterpret_cast<float2 *>(tsm)[q] = make_float2(t0, t1);
@@ -985,7 +900,6 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     } else {
         for (int p = threadIdx.x; p < ns; p += bd) {
             float esc = 0.f, y = __ldg(yv + p), o = __ldg(ov + p);
-            if (nebc) neb_add(p, y, o);
             tsm[p] = pass1(p, y, o, emis ? dl07_shape(a.dtab, ns, a.nqpah, p, dm) : 0.f,
                            emis ? __ldg(a.cnu + p) : 0.f, agn ? __ldg(a.agn_spec + (size_t)dm.ita * ns + p) : 0.f,
                            agn ? __ldg(a.agn_spec + (size_t)(dm.ita + 1) * ns + p) : 0.f, esc);
@@ -1030,6 +944,143 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
         }
         out[p] = v;
     }
+}
+
+// ---------------------------------------------------------------------------------------------- nebular continuum
+// The CLOUDY-grid nebular continuum (nebular_kernels step 3, src/physics/opensps_csp_batch.f90:2760-2910), added to
+// the young and old sums before the per-model epilogue.
+//
+// neb_weights_kernel, one warp per model: per nebular age t the weight C(t) = |1 - frac_obrun| sum_z w(t, z) q0(t, z)
+// (the SFH weight times the ionizing photon rate, over the model's metallicities; FP64), normalised by its largest
+// value S; log2 S split into an integer part and the rest. Row m of cw: C(t) / S for t < nt_neb, then (S's integer
+// part, the rest).
+__global__ void __launch_bounds__(256) neb_weights_kernel(NebContArgs a) {
+    const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (m >= a.n) return;
+    const DustEmModel dm = a.dem[m];
+    const double *w = a.wz + (size_t)m * a.nz * a.nt;
+    double cs[(NEB_MAX_AGES + 31) / 32];
+    double mx = 0.0;
+#pragma unroll
+    for (int i = 0; i < (NEB_MAX_AGES + 31) / 32; ++i) {
+        const int t = lane + 32 * i;
+        double c = 0.0;
+        if (t < a.nt_neb) {
+            for (int z = 0; z < a.nz; ++z) {
+                const double wv = __ldg(w + (size_t)z * a.nt + t);
+                if (wv > SAFE_FLOOR) c = fma(wv, __ldg(a.q0 + (size_t)t * a.nz + z), c);
+            }
+            c *= (double)dm.neb_fabs;
+        }
+        cs[i] = c;
+        mx = fmax(mx, c);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    float *o = a.cw + (size_t)m * a.cw_ld;
+#pragma unroll
+    for (int i = 0; i < (NEB_MAX_AGES + 31) / 32; ++i) {
+        const int t = lane + 32 * i;
+        if (t < a.nt_neb) o[t] = mx > 0.0 ? (float)(cs[i] / mx) : 0.f;
+    }
+    if (lane == 0) {
+        const double s2 = mx > 0.0 ? log2(mx) : 0.0, si = floor(s2);
+        o[a.nt_neb] = (float)si;
+        o[a.nt_neb + 1] = mx > 0.0 ? (float)(s2 - si) : 0.f;
+    }
+}
+
+// neb_cont_kernel: a CTA per (pixel block, group of at most NEB_GROUP models of one (gas_logz, gas_logu) cell, the
+// models sorted by cell on the host): each thread holds its pixel's 4 corners x 10 CLOUDY ages of the table (log2
+// less the pixel's integer offset) in registers for every model of the group, and per model forms the bilinear values
+// at the ten ages, then per CLOUDY interval the run of nebular ages in it, where 2^lg advances geometrically (one
+// exponential at the interval's first age and one per step change), the young ages (t < itesc) and the others
+// summed apart and added to the model's young and old sums.
+constexpr int NEB_PIX = 128;
+
+__global__ void __launch_bounds__(NEB_PIX) neb_cont_kernel(NebContArgs a) {
+    constexpr int NU = 7, NA = 10;
+    __shared__ float cws[NEB_GROUP][NEB_MAX_AGES + 2];
+    __shared__ float4 nag[NEB_MAX_AGES];
+    __shared__ int nts[NA];
+    __shared__ int mids[NEB_GROUP];
+    __shared__ float4 mw[NEB_GROUP];        // per model: c00, c01, c10, c11 of its cell's weights
+    const int4 g = a.groups[blockIdx.y];    // (cell z, cell u, first model in order, count)
+    const int p = blockIdx.x * NEB_PIX + threadIdx.x;
+    const int cnt = g.w;
+    for (int i = threadIdx.x; i < a.nt_neb; i += NEB_PIX) nag[i] = __ldg(a.age4 + i);
+    if (threadIdx.x < NA) nts[threadIdx.x] = __ldg(a.tstart + threadIdx.x);
+    for (int j = threadIdx.x; j < cnt; j += NEB_PIX) {
+        const int m = __ldg(a.order + g.z + j);
+        mids[j] = m;
+        const DustEmModel dm = a.dem[m];
+        mw[j] = make_float4((1.f - dm.neb_wz) * (1.f - dm.neb_wu), (1.f - dm.neb_wz) * dm.neb_wu,
+                            dm.neb_wz * (1.f - dm.neb_wu), dm.neb_wz * dm.neb_wu);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cnt * (a.nt_neb + 2); e += NEB_PIX) {
+        const int j = e / (a.nt_neb + 2), k = e - j * (a.nt_neb + 2);
+        cws[j][k] = __ldg(a.cw + (size_t)mids[j] * a.cw_ld + k);
+    }
+    __syncthreads();
+    if (p >= a.nspec) return;
+    // the pixel's table at the cell's corners: t[corner][age]
+    const size_t plane = (size_t)NA * a.nspec;
+    const float *b00 = a.tab + (size_t)(g.x * NU + g.y) * plane + p, *b01 = b00 + plane;
+    const float *b10 = a.tab + (size_t)((g.x + 1) * NU + g.y) * plane + p, *b11 = b10 + plane;
+    float t00[NA], t01[NA], t10[NA], t11[NA];
+#pragma unroll
+    for (int k = 0; k < NA; ++k) {
+        t00[k] = __ldg(b00 + (size_t)k * a.nspec);
+        t01[k] = __ldg(b01 + (size_t)k * a.nspec);
+        t10[k] = __ldg(b10 + (size_t)k * a.nspec);
+        t11[k] = __ldg(b11 + (size_t)k * a.nspec);
+    }
+    const float off = __ldg(a.off + p);
+    for (int j = 0; j < cnt; ++j) {
+        const float *cw = cws[j];
+        const float4 c = mw[j];
+        const float e_int = off + cw[a.nt_neb];          // integers: exact
+        const float sfrac = cw[a.nt_neb + 1];
+        float L[NA];
+#pragma unroll
+        for (int k = 0; k < NA; ++k) L[k] = fmaf(c.x, t00[k], fmaf(c.y, t01[k], fmaf(c.z, t10[k], c.w * t11[k])));
+        float ys = 0.f, os = 0.f;
+#pragma unroll
+        for (int k = 0; k < NA - 1; ++k) {
+            const int t0 = nts[k], t1 = nts[k + 1];
+            if (t0 >= t1) continue;
+            const float ra = L[k], dl = L[k + 1] - L[k];
+            float f = ops_ex2((sfrac + fmaf(nag[t0].y, dl, ra)) + e_int), r = 1.f;
+            for (int t = t0; t < t1; ++t) {
+                if (t > t0) {
+                    const float4 ag = nag[t];
+                    if (ag.w != 0.f) r = ops_ex2(ag.z * dl);
+                    f *= r;
+                }
+                if (t < a.itesc) ys = fmaf(cw[t], f, ys); else os = fmaf(cw[t], f, os);
+            }
+        }
+        const size_t i = (size_t)mids[j] * a.nspec + p;
+        a.young[i] += ys;
+        a.old[i] += os;
+    }
+}
+
+cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_t st) {
+    if (a.n <= 0 || ngroups <= 0) return cudaSuccess;
+    neb_weights_kernel<<<(unsigned)((a.n * 32 + 255) / 256), 256, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // (the groups in slices within the grid's y limit)
+    for (int g0 = 0; g0 < ngroups; g0 += 65535) {
+        NebContArgs b = a;
+        b.groups = a.groups + g0;
+        const dim3 grid((a.nspec + NEB_PIX - 1) / NEB_PIX, std::min(65535, ngroups - g0));
+        neb_cont_kernel<<<grid, NEB_PIX, 0, st>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
