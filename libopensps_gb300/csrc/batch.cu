@@ -642,6 +642,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             }
         }
         if (neb_cont) {
+            if (int rc = nebular_runs(c, itesc, err)) return rc;
             // per chunk, its models with a continuum sorted by their (gas_logz, gas_logu) cell (chunk-relative
             // indices) and cut into groups of at most NEB_GROUP (cell z, cell u, first index into the order, count)
             c.neb.h_order.clear();
@@ -908,10 +909,11 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             // the CLOUDY-grid continuum into the young and old sums of models [off, off + nk) (their groups by cell)
             const int2 cg = neb_chunk_groups[chunked ? off / CHUNK : 0];
             NebContArgs na;
-            na.n = nk; na.nspec = ns; na.nt = nt; na.nz = nz; na.nt_neb = c.nt_neb; na.itesc = itesc;
-            na.cw_ld = c.nt_neb + 2;
+            na.n = nk; na.nspec = ns; na.nt = nt; na.nz = nz; na.nt_neb = c.nt_neb;
+            na.cw_ld = c.nt_neb + 2; na.nrun = c.neb.nrun;
             na.dem = d_dem + off; na.tab = c.neb.tab[neb_table].p; na.off = c.neb.off.p;
-            na.age4 = reinterpret_cast<const float4 *>(c.neb.age4.p); na.tstart = c.neb.tstart.p; na.q0 = c.neb.q0.p;
+            na.rfirst = c.neb.runs.p; na.runs = reinterpret_cast<const int4 *>(c.neb.runs.p + NEB_RUN_HEAD);
+            na.q0 = c.neb.q0.p;
             na.wz = d_wz + (size_t)nt * nz * off;
             na.groups = c.neb.groups.p + cg.x; na.order = c.neb.order.p;
             cudaError_t r = c.neb.cw.reserve((size_t)nk * na.cw_ld);

@@ -547,45 +547,72 @@ int nebular_load(Context &c, std::string &err) {
                 q0[(size_t)t * c.nz + z] = s / 6.62607015e-27 * 3.828e33;
             }
     if (e == cudaSuccess) e = upload(c.neb.q0, q0.data(), q0.size());
-    // per nebular age its CLOUDY interval: get_grid_indices_weights (opensps_gas.f90:394-412) on the log ages, then
-    // the steps of wa within an interval and where a new step starts
-    std::vector<int> ia(nn, 0);
-    std::vector<double> wa(nn, 0.0), dwa(nn, 0.0);
-    std::vector<int> newr(nn, 0);
+    // per nebular age its CLOUDY interval: get_grid_indices_weights (opensps_gas.f90:394-412) on the log ages
+    c.neb.ia.assign(nn, 0);
+    c.neb.wa.assign(nn, 0.0);
     for (int t = 0; t < c.nt_neb; ++t) {
         int k = find_interval0(c.neb.lage.data(), NEB_NAGE, c.log_age[t]);
         k = std::max(0, std::min(k, NEB_NAGE - 2));
-        ia[t] = k;
+        c.neb.ia[t] = k;
         const double w = (c.log_age[t] - c.neb.lage[k]) / (c.neb.lage[k + 1] - c.neb.lage[k]);
-        wa[t] = std::max(0.0, std::min(w, 1.0));
+        c.neb.wa[t] = std::max(0.0, std::min(w, 1.0));
     }
-    for (int t = 1; t < c.nt_neb; ++t) {
-        if (ia[t] != ia[t - 1]) continue;
-        dwa[t] = wa[t] - wa[t - 1];
-        newr[t] = (ia[t - 1] != ia[std::max(0, t - 2)] || t == 1 || dwa[t] != dwa[t - 1]) ? 1 : 0;
-    }
-    std::vector<float> a4((size_t)4 * nn);
-    for (int t = 0; t < nn; ++t) {
-        int bits = ia[t];
-        std::memcpy(&a4[4 * t], &bits, 4);
-        a4[4 * t + 1] = (float)wa[t];
-        a4[4 * t + 2] = (float)dwa[t];
-        a4[4 * t + 3] = (float)newr[t];
-    }
-    if (e == cudaSuccess) e = upload(c.neb.age4, a4.data(), a4.size());
-    // the ages of each interval are a run (ia grows with t): tstart[k] = the first age with ia >= k, tstart[9] = nt_neb
-    std::vector<int> ts(NEB_NAGE, c.nt_neb);
-    for (int k = 0; k < NEB_NAGE - 1; ++k) {
-        int t = 0;
-        while (t < c.nt_neb && ia[t] < k) ++t;
-        ts[k] = t;
-    }
-    if (e == cudaSuccess) e = upload(c.neb.tstart, ts.data(), ts.size());
     if (e != cudaSuccess) {
         err = std::string("nebular grid: ") + cudaGetErrorString(e);
         c.neb.release();
         return ST_DATA_MISSING;
     }
+    return 0;
+}
+
+// The nebular ages as runs for the continuum kernel: consecutive ages of one CLOUDY interval, on one side of itesc
+// (young below it), whose weights wa step uniformly (ages below the grid's first age, wa clamped to 0, form a run of
+// step 0). Each run: (first age, count | young << 16, wa of its last age, the step). Built once per itesc.
+int nebular_runs(Context &c, int itesc, std::string &err) {
+    static_assert(NEB_NAGE <= NEB_RUN_HEAD, "the runs' head holds one int per CLOUDY age");
+    if (c.neb.runs_itesc == itesc && c.neb.runs.p) return 0;
+    const int nn = c.nt_neb;
+    std::vector<int> head(NEB_RUN_HEAD, 0);
+    std::vector<int4> runs;
+    auto fbits = [](double x) { float f = (float)x; int b; std::memcpy(&b, &f, 4); return b; };
+    int t = 0;
+    for (int k = 0; k < NEB_NAGE - 1; ++k) {
+        head[k] = (int)runs.size();
+        while (t < nn && c.neb.ia[t] == k) {
+            // a run from t: as long as the interval, the side of itesc and the step hold
+            int u = t + 1;
+            const bool young = t < itesc;
+            double step = 0.0;
+            if (u < nn && c.neb.ia[u] == k && (u < itesc) == young) {
+                step = c.neb.wa[u] - c.neb.wa[t];
+                ++u;
+                while (u < nn && c.neb.ia[u] == k && (u < itesc) == young &&
+                       std::fabs((c.neb.wa[u] - c.neb.wa[u - 1]) - step) <= 1e-9)
+                    ++u;
+            }
+            const int cnt = u - t;
+            const double d = cnt > 1 ? (c.neb.wa[u - 1] - c.neb.wa[t]) / (cnt - 1) : 0.0;
+            runs.push_back(make_int4(t, cnt | (young ? 1 << 16 : 0), fbits(c.neb.wa[u - 1]), fbits(d)));
+            t = u;
+        }
+    }
+    head[NEB_NAGE - 1] = (int)runs.size();
+    if (t != nn || (int)runs.size() > NEB_MAX_RUNS) {
+        err = "nebular continuum: the nebular ages do not form runs by interval";
+        return ST_UNSUPPORTED;
+    }
+    c.neb.h_runs.assign(head.begin(), head.end());
+    for (const int4 &r : runs) c.neb.h_runs.insert(c.neb.h_runs.end(), {r.x, r.y, r.z, r.w});
+    cudaError_t e = c.neb.runs.reserve(c.neb.h_runs.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c.neb.runs.p, c.neb.h_runs.data(), sizeof(int) * c.neb.h_runs.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        err = std::string("nebular continuum runs: ") + cudaGetErrorString(e);
+        c.neb.runs_itesc = -1;
+        return ST_DATA_MISSING;
+    }
+    c.neb.runs_itesc = itesc;
+    c.neb.nrun = (int)runs.size();
     return 0;
 }
 

@@ -138,14 +138,20 @@ struct AgnTorus {
 // x 7 ionization parameters at each pixel, with per nebular age of the SSP grid its CLOUDY age interval and the
 // ionizing photon rate of each (age, metallicity) SSP. On the device, per table (0: nodust, 1: dust) the log2 of
 // the continuum less a per-pixel offset (off: the largest log2 value of the pixel over the grid, rounded up to an
-// integer) as FP32, [logZ][logU][age][pixel]; q0 FP64 (nt_neb x nz, metallicity fastest); per nebular age t a
-// float4 (the interval's lower node as int bits, wa, dwa, newr) as batch_nebular_indices forms them (:1651-1686).
+// integer) as FP32, [logZ][logU][age][pixel]; q0 FP64 (nt_neb x nz, metallicity fastest); per nebular age its
+// interval and weight as batch_nebular_indices forms them (:1651-1686).
 struct NebularGrid {
     bool have[2] = {false, false};
     std::vector<double> logz, lage, logu;
-    DevBuf<float> tab[2], off, age4;
+    DevBuf<float> tab[2], off;
     DevBuf<double> q0;
-    DevBuf<int> tstart;          // NEB_NAGE ints: the first nebular age of each CLOUDY interval (the last: nt_neb)
+    // per nebular age its CLOUDY interval (lower node, 0-based) and weight wa in it (clamped to [0, 1]); the ages as
+    // runs for the last itesc (NEB_RUN_HEAD ints: each interval's first run and the run count, then the runs as int4)
+    std::vector<int> ia;
+    std::vector<double> wa;
+    std::vector<int> h_runs;
+    int runs_itesc = -1, nrun = 0;
+    DevBuf<int> runs;
     // a batch's continuum: the models sorted by cell and their groups (host staging and device copies), the per-model
     // weights (scratch)
     std::vector<int> h_order;
@@ -154,7 +160,8 @@ struct NebularGrid {
     DevBuf<int4> groups;
     DevBuf<float> cw;
     void release() {
-        tab[0].release(); tab[1].release(); off.release(); age4.release(); q0.release(); tstart.release();
+        tab[0].release(); tab[1].release(); off.release(); q0.release(); runs.release();
+        ia.clear(); wa.clear(); h_runs.clear(); runs_itesc = -1; nrun = 0;
         order.release(); groups.release(); cw.release();
         have[0] = have[1] = false;
     }
@@ -340,6 +347,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err);
 int ops_build(Context &c, std::string &err);
 int dustem_load(Context &c, std::string &err);
 int agn_load(Context &c, std::string &err);
+// the nebular ages as the continuum kernel's runs for this itesc (context.cu; rebuilt when itesc changes)
+int nebular_runs(Context &c, int itesc, std::string &err);
 // The plain FP64 path (fp64_path.cu): the age sums by DGEMM and the rest in FP64, into the host outputs of io.
 void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<double> &b);
 int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,

@@ -348,18 +348,22 @@ struct PartsEpilogueArgs {
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st);
 
 // The CLOUDY-grid nebular continuum added to the young and old sums (ssp_op.cu): n models, their cells in dem, the
-// table (log2 less the pixel's integer offset, [logZ][logU][age][pixel]) and offsets, per nebular age its interval
-// float4 (lower node as int bits, wa, dwa, newr) and each CLOUDY interval's first nebular age (tstart), q0 (nt_neb x
-// nz), the FP64 weights (n x nz x nt), the ages below itesc young; groups: (cell z, cell u, first index into order,
-// count <= NEB_GROUP), order: the models sorted by cell; cw: scratch, n x cw_ld floats (cw_ld >= nt_neb + 2).
+// table (log2 less the pixel's integer offset, [logZ][logU][age][pixel]) and offsets, q0 (nt_neb x nz), the FP64
+// weights (n x nz x nt); the nebular ages as runs of one CLOUDY interval, one side of itesc and a uniform step in the
+// interval's weight wa: runs[r] = (first age, age count | young << 16, wa of the run's last age, the step), as int
+// bits; rfirst[k] = interval k's first run (k = 0 .. NEB_NAGE - 2), rfirst[NEB_NAGE - 1] = nrun; groups: (cell z,
+// cell u, first index into order, count <= NEB_GROUP), order: the models sorted by cell; cw: scratch, n x cw_ld floats
+// (cw_ld >= nt_neb + 2).
 constexpr int NEB_MAX_AGES = 128;         // nebular ages the continuum takes
-constexpr int NEB_GROUP = 32;             // models per group of one cell
+constexpr int NEB_GROUP = 64;             // models per group of one cell
+constexpr int NEB_MAX_RUNS = NEB_MAX_AGES + 16;
+constexpr int NEB_RUN_HEAD = 12;          // ints before the runs: the intervals' first runs, the run count
 struct NebContArgs {
-    int n, nspec, nt, nz, nt_neb, itesc, cw_ld;
+    int n, nspec, nt, nz, nt_neb, cw_ld, nrun;
     const DustEmModel *dem;
     const float *tab, *off;
-    const float4 *age4;
-    const int *tstart;
+    const int4 *runs;
+    const int *rfirst;
     const double *q0, *wz;
     const int4 *groups;
     const int *order;

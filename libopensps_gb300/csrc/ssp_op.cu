@@ -991,79 +991,161 @@ __global__ void __launch_bounds__(256) neb_weights_kernel(NebContArgs a) {
 }
 
 // neb_cont_kernel: a CTA per (pixel block, group of at most NEB_GROUP models of one (gas_logz, gas_logu) cell, the
-// models sorted by cell on the host): each thread holds its pixel's 4 corners x 10 CLOUDY ages of the table (log2
-// less the pixel's integer offset) in registers for every model of the group, and per model forms the bilinear values
-// at the ten ages, then per CLOUDY interval the run of nebular ages in it, where 2^lg advances geometrically (one
-// exponential at the interval's first age and one per step change), the young ages (t < itesc) and the others
-// summed apart and added to the model's young and old sums.
+// models sorted by cell on the host). Each thread holds its pixel's table at the cell's four corners for the ten
+// CLOUDY ages in registers, as the bilinear form L = c + w_z dz + w_u (du + w_z dzu), and takes the group's models four
+// at a time (their weights C(t) / S four to a 16-byte shared load). The ages of one CLOUDY interval k are runs in which
+// the exponent L_k + wa (L_k+1 - L_k) steps uniformly, so a run's sum is 2^(exponent at its last age) times a
+// polynomial in y = 2^(-step dl) in Horner form: one FMA per age and model, two exponentials per run and model. Where
+// the run spans more than NEB_STEEP in log2 with the flux falling (y > 1, which could overflow the polynomial) any
+// lane of the warp takes the run age by age instead. Sums are relative to 2^(pixel offset + S's integer part), that
+// scale applied last as exact powers of two; the young runs (ages below itesc) and the others are added to the young
+// and old sums.
 constexpr int NEB_PIX = 128;
+constexpr float NEB_STEEP = 64.f;
+
+__device__ __forceinline__ float pow2i(int e) {
+    e = max(-126, min(e, 127));
+    return __int_as_float((e + 127) << 23);
+}
+
+static size_t neb_cont_smem(int nt_neb, int nrun) {
+    return sizeof(float4) * (size_t)NEB_GROUP + sizeof(float) * (size_t)nt_neb * NEB_GROUP + sizeof(int4) * (size_t)nrun +
+           sizeof(int) * (size_t)(NEB_RUN_HEAD + NEB_GROUP);
+}
 
 __global__ void __launch_bounds__(NEB_PIX) neb_cont_kernel(NebContArgs a) {
-    constexpr int NU = 7, NA = 10;
-    __shared__ float cws[NEB_GROUP][NEB_MAX_AGES + 2];
-    __shared__ float4 nag[NEB_MAX_AGES];
-    __shared__ int nts[NA];
-    __shared__ int mids[NEB_GROUP];
-    __shared__ float4 mw[NEB_GROUP];        // per model: c00, c01, c10, c11 of its cell's weights
-    const int4 g = a.groups[blockIdx.y];    // (cell z, cell u, first model in order, count)
-    const int p = blockIdx.x * NEB_PIX + threadIdx.x;
+    constexpr int NU = 7, NA = 10, G = NEB_GROUP, G4 = NEB_GROUP / 4;
+    static_assert(G % 4 == 0 && (G & (G - 1)) == 0 && G <= NEB_PIX, "groups of a power of two models");
+    extern __shared__ float4 nsm[];
+    float4 *mp = nsm;                                                  // G: (w_z, w_u, S's fraction, S's integer part)
+    float4 *cws = mp + G;                                              // nt_neb x G / 4: C(t) / S, models fastest
+    int4 *runs = reinterpret_cast<int4 *>(cws + (size_t)a.nt_neb * G4);
+    int *rf = reinterpret_cast<int *>(runs + a.nrun);                  // NEB_RUN_HEAD
+    int *mids = rf + NEB_RUN_HEAD;                                     // G
+    const int4 g = a.groups[blockIdx.y];                               // (cell z, cell u, first in order, count)
     const int cnt = g.w;
-    for (int i = threadIdx.x; i < a.nt_neb; i += NEB_PIX) nag[i] = __ldg(a.age4 + i);
-    if (threadIdx.x < NA) nts[threadIdx.x] = __ldg(a.tstart + threadIdx.x);
-    for (int j = threadIdx.x; j < cnt; j += NEB_PIX) {
-        const int m = __ldg(a.order + g.z + j);
+    for (int i = threadIdx.x; i < a.nrun; i += NEB_PIX) runs[i] = __ldg(a.runs + i);
+    if (threadIdx.x < NEB_RUN_HEAD) rf[threadIdx.x] = __ldg(a.rfirst + threadIdx.x);
+    if (threadIdx.x < G) {
+        const int j = threadIdx.x;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        int m = 0;
+        if (j < cnt) {
+            m = __ldg(a.order + g.z + j);
+            const DustEmModel &dm = a.dem[m];
+            const float *cw = a.cw + (size_t)m * a.cw_ld;
+            v = make_float4(dm.neb_wz, dm.neb_wu, __ldg(cw + a.nt_neb + 1), __ldg(cw + a.nt_neb));
+        }
+        mp[j] = v;
         mids[j] = m;
-        const DustEmModel dm = a.dem[m];
-        mw[j] = make_float4((1.f - dm.neb_wz) * (1.f - dm.neb_wu), (1.f - dm.neb_wz) * dm.neb_wu,
-                            dm.neb_wz * (1.f - dm.neb_wu), dm.neb_wz * dm.neb_wu);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < cnt * (a.nt_neb + 2); e += NEB_PIX) {
-        const int j = e / (a.nt_neb + 2), k = e - j * (a.nt_neb + 2);
-        cws[j][k] = __ldg(a.cw + (size_t)mids[j] * a.cw_ld + k);
+    float *cwf = reinterpret_cast<float *>(cws);
+    for (int e = threadIdx.x; e < a.nt_neb * G; e += NEB_PIX) {
+        const int j = e & (G - 1), t = e / G;
+        cwf[e] = j < cnt ? __ldg(a.cw + (size_t)mids[j] * a.cw_ld + t) : 0.f;
     }
     __syncthreads();
-    if (p >= a.nspec) return;
-    // the pixel's table at the cell's corners: t[corner][age]
+    const int p = blockIdx.x * NEB_PIX + threadIdx.x;
+    const int pc = min(p, a.nspec - 1);                 // (lanes past the last pixel compute on it and store nothing)
     const size_t plane = (size_t)NA * a.nspec;
-    const float *b00 = a.tab + (size_t)(g.x * NU + g.y) * plane + p, *b01 = b00 + plane;
-    const float *b10 = a.tab + (size_t)((g.x + 1) * NU + g.y) * plane + p, *b11 = b10 + plane;
-    float t00[NA], t01[NA], t10[NA], t11[NA];
+    const float *b00 = a.tab + (size_t)(g.x * NU + g.y) * plane + pc, *b01 = b00 + plane;
+    const float *b10 = a.tab + (size_t)((g.x + 1) * NU + g.y) * plane + pc, *b11 = b10 + plane;
+    float c0[NA], dz[NA], du[NA], dzu[NA];
 #pragma unroll
     for (int k = 0; k < NA; ++k) {
-        t00[k] = __ldg(b00 + (size_t)k * a.nspec);
-        t01[k] = __ldg(b01 + (size_t)k * a.nspec);
-        t10[k] = __ldg(b10 + (size_t)k * a.nspec);
-        t11[k] = __ldg(b11 + (size_t)k * a.nspec);
+        const float t00 = __ldg(b00 + (size_t)k * a.nspec), t01 = __ldg(b01 + (size_t)k * a.nspec);
+        const float t10 = __ldg(b10 + (size_t)k * a.nspec), t11 = __ldg(b11 + (size_t)k * a.nspec);
+        c0[k] = t00;
+        dz[k] = t10 - t00;
+        du[k] = t01 - t00;
+        dzu[k] = (t11 - t10) - (t01 - t00);
     }
-    const float off = __ldg(a.off + p);
-    for (int j = 0; j < cnt; ++j) {
-        const float *cw = cws[j];
-        const float4 c = mw[j];
-        const float e_int = off + cw[a.nt_neb];          // integers: exact
-        const float sfrac = cw[a.nt_neb + 1];
-        float L[NA];
+    const int offp = (int)__ldg(a.off + pc);
+    for (int j0 = 0; j0 < cnt; j0 += 4) {
+        float4 P[4];
+        size_t idx[4];
+        bool st[4];
+        float yv[4], ov[4];
 #pragma unroll
-        for (int k = 0; k < NA; ++k) L[k] = fmaf(c.x, t00[k], fmaf(c.y, t01[k], fmaf(c.z, t10[k], c.w * t11[k])));
-        float ys = 0.f, os = 0.f;
+        for (int q = 0; q < 4; ++q) {
+            P[q] = mp[j0 + q];
+            st[q] = p < a.nspec && j0 + q < cnt;
+            idx[q] = (size_t)mids[j0 + q] * a.nspec + pc;
+            yv[q] = st[q] ? a.young[idx[q]] : 0.f;
+            ov[q] = st[q] ? a.old[idx[q]] : 0.f;
+        }
+        float ys[4] = {0.f, 0.f, 0.f, 0.f}, os[4] = {0.f, 0.f, 0.f, 0.f}, Lk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Lk[q] = fmaf(P[q].x, dz[0], fmaf(P[q].y, fmaf(P[q].x, dzu[0], du[0]), c0[0]));
 #pragma unroll
         for (int k = 0; k < NA - 1; ++k) {
-            const int t0 = nts[k], t1 = nts[k + 1];
-            if (t0 >= t1) continue;
-            const float ra = L[k], dl = L[k + 1] - L[k];
-            float f = ops_ex2((sfrac + fmaf(nag[t0].y, dl, ra)) + e_int), r = 1.f;
-            for (int t = t0; t < t1; ++t) {
-                if (t > t0) {
-                    const float4 ag = nag[t];
-                    if (ag.w != 0.f) r = ops_ex2(ag.z * dl);
-                    f *= r;
-                }
-                if (t < a.itesc) ys = fmaf(cw[t], f, ys); else os = fmaf(cw[t], f, os);
+            float L1[4], dl[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                L1[q] = fmaf(P[q].x, dz[k + 1], fmaf(P[q].y, fmaf(P[q].x, dzu[k + 1], du[k + 1]), c0[k + 1]));
+                dl[q] = L1[q] - Lk[q];
             }
+            const int r1 = rf[k + 1];
+            for (int r = rf[k]; r < r1; ++r) {
+                const int4 R = runs[r];
+                const int t0 = R.x, nr = R.y & 0xffff;
+                const float wtop = __int_as_float(R.z), del = __int_as_float(R.w);
+                const float span = (float)(nr - 1) * del;
+                bool steep = false;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) steep |= -dl[q] * span > NEB_STEEP;
+                const float4 *cr = cws + (size_t)t0 * G4 + (j0 >> 2);
+                float H[4];
+                if (__any_sync(0xffffffffu, steep)) {
+                    // age by age: each term 2^(S's fraction + L_k + wa dl) <= 2
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) H[q] = 0.f;
+                    for (int t = 0; t < nr; ++t) {
+                        const float4 cv = cr[(size_t)t * G4];
+                        const float wt = wtop - (float)(nr - 1 - t) * del;
+                        H[0] = fmaf(cv.x, ops_ex2(P[0].z + fmaf(wt, dl[0], Lk[0])), H[0]);
+                        H[1] = fmaf(cv.y, ops_ex2(P[1].z + fmaf(wt, dl[1], Lk[1])), H[1]);
+                        H[2] = fmaf(cv.z, ops_ex2(P[2].z + fmaf(wt, dl[2], Lk[2])), H[2]);
+                        H[3] = fmaf(cv.w, ops_ex2(P[3].z + fmaf(wt, dl[3], Lk[3])), H[3]);
+                    }
+                } else {
+                    float y[4] = {1.f, 1.f, 1.f, 1.f};
+                    if (nr > 1 && del != 0.f) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) y[q] = ops_ex2(-del * dl[q]);
+                    }
+                    float4 cv = cr[0];
+                    H[0] = cv.x; H[1] = cv.y; H[2] = cv.z; H[3] = cv.w;
+                    for (int t = 1; t < nr; ++t) {
+                        cv = cr[(size_t)t * G4];
+                        H[0] = fmaf(H[0], y[0], cv.x);
+                        H[1] = fmaf(H[1], y[1], cv.y);
+                        H[2] = fmaf(H[2], y[2], cv.z);
+                        H[3] = fmaf(H[3], y[3], cv.w);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) H[q] *= ops_ex2(P[q].z + fmaf(wtop, dl[q], Lk[q]));
+                }
+                if (R.y >> 16) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) ys[q] += H[q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) os[q] += H[q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) Lk[q] = L1[q];
         }
-        const size_t i = (size_t)mids[j] * a.nspec + p;
-        a.young[i] += ys;
-        a.old[i] += os;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (!st[q]) continue;
+            const int e = offp + (int)P[q].w, e1 = e >> 1;
+            const float s1 = pow2i(e1), s2 = pow2i(e - e1);
+            a.young[idx[q]] = fmaf(ys[q] * s1, s2, yv[q]);
+            a.old[idx[q]] = fmaf(os[q] * s1, s2, ov[q]);
+        }
     }
 }
 
@@ -1072,12 +1154,16 @@ cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_
     neb_weights_kernel<<<(unsigned)((a.n * 32 + 255) / 256), 256, 0, st>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    const size_t smem = neb_cont_smem(a.nt_neb, a.nrun);
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(neb_cont_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
     // (the groups in slices within the grid's y limit)
     for (int g0 = 0; g0 < ngroups; g0 += 65535) {
         NebContArgs b = a;
         b.groups = a.groups + g0;
         const dim3 grid((a.nspec + NEB_PIX - 1) / NEB_PIX, std::min(65535, ngroups - g0));
-        neb_cont_kernel<<<grid, NEB_PIX, 0, st>>>(b);
+        neb_cont_kernel<<<grid, NEB_PIX, smem, st>>>(b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;

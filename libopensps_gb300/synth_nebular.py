@@ -20,6 +20,9 @@ photon per second, underflows to zero). This grid stands in for them with the sa
 
 The last CLOUDY age, 10 Myr, is the synthetic line list's last age, so the nebular ages of the grid are those of the
 lines (log age <= 7).
+
+``steep`` (a test grid): the continuum falls by ``STEEP_DEX`` decades per dex of age past 1 Myr (floored as above),
+so that between some CLOUDY ages it drops by more than 2^64, the case the continuum kernel takes age by age.
 """
 from __future__ import annotations
 
@@ -35,6 +38,7 @@ NEMLINE = 166
 HC_OVER_K = 1.4387769e8          # h c / k [A K]
 EDGES = ((3646.0, 1.2), (8204.0, 0.6), (14584.0, 0.3))
 FLOOR = 1.0e-95
+STEEP_DEX = 80.0
 
 
 def wavelengths() -> np.ndarray:
@@ -53,7 +57,7 @@ def _continuum(lam: np.ndarray, logz: float, age: float, logu: float) -> np.ndar
     return np.where(lam >= 912.0, c, 0.0)
 
 
-def continuum_grid() -> tuple[np.ndarray, np.ndarray]:
+def continuum_grid(steep: bool = False) -> tuple[np.ndarray, np.ndarray]:
     """(wavelength, continuum[logZ, age, logU, wavelength]) in L_sun/Hz per ionizing photon per second."""
     lam = wavelengths()
     ref = _continuum(np.array([5000.0]), 0.0, 1.0e6, -2.0)[0]
@@ -63,6 +67,8 @@ def continuum_grid() -> tuple[np.ndarray, np.ndarray]:
         for j, a in enumerate(AGE):
             for k, u in enumerate(LOGU):
                 out[i, j, k] = scale * _continuum(lam, z, a, u)
+                if steep:
+                    out[i, j, k] *= 10.0 ** (-STEEP_DEX * max(0.0, np.log10(a) - 6.0))
     return lam, np.maximum(out, FLOOR)
 
 
@@ -79,10 +85,10 @@ def lines_grid() -> tuple[np.ndarray, np.ndarray]:
     return lw, out
 
 
-def write(root: Path, name: str = "synthetic_nodust") -> Path:
+def write(root: Path, name: str = "synthetic_nodust", steep: bool = False) -> Path:
     """The grid as the standard-format library ``nebular/<name>`` under ``root``."""
     from .stdformat import write_library
-    lam, cont = continuum_grid()
+    lam, cont = continuum_grid(steep)
     lw, lines = lines_grid()
     return write_library(
         root, "nebular", name,

@@ -98,6 +98,42 @@ def test_continuum_with_dust_emission(neb_root, built_lib, restore_root):
     assert float(np.nanmax(np.abs(got["mags"] - want["mags"]))) <= 1e-3
 
 
+def test_continuum_steep_grid(tmp_path, data, built_lib, restore_root):
+    """synth_nebular's steep test grid (the continuum falls by 80 decades per dex of age past 1 Myr, floored at
+    1e-95): between the CLOUDY ages 1 and 2 Myr it drops by 2^80, past the 2^64 the kernel's polynomial takes, so
+    those runs go age by age; the next intervals fall by 2^35 and 2^26 (the polynomial with its ratio above 1). The
+    weights sit on the ages 1-4 Myr (the others at 1e-6 of theirs): the continuum's part of the spectrum (the batch
+    less the same batch without it) against the oracle's within 1e-2 wherever it is at least 1e-3 of the spectrum
+    (FP32 spectra differenced), and the whole batch as the other tests."""
+    from libopensps_gb300 import stdformat, synth_nebular, synthdata
+    from libopensps_gb300.capi import Context
+    from oracle import stdformat as ora
+    from oracle.oracle import Oracle
+    root = tmp_path / "steep"
+    stdformat.convert_synthetic(root, src_root=synthdata.default_root(), dust=False, agn=False)
+    synth_nebular.write(root, "synthetic_nodust", steep=True)
+    n = 40
+    wz, params = _inputs(n, seed=1270)
+    la = data["log_age"]
+    wz[:, :, ~((la >= 6.0) & (la < 6.6))] *= 1e-6
+    c = Context(data_root=root)
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    got = c.csp_batch(params, ssp_weights_z=wz)
+    c.set_int("add_neb_continuum", 0)
+    plain = c.csp_batch(params, ssp_weights_z=wz)
+    c.close()
+    d = ora.load_data(root, filter_sets=("gauss40",))
+    want = Oracle(d, nbands=40, nebular=ora.nebular(root, d["lambda"], "synthetic_nodust")).csp_batch(params, wz)
+    want_plain = Oracle(d, nbands=40).csp_batch(params, wz)
+    assert rel_err_spec(got["spec"], want["spec"]) <= 1e-4
+    assert float(np.nanmax(np.abs(got["mags"] - want["mags"]))) <= 1e-3
+    cont, cont_want = got["spec"] - plain["spec"], want["spec"] - want_plain["spec"]
+    sel = cont_want >= 1e-3 * want["spec"]
+    assert sel.sum() > 1000
+    assert np.max(np.abs(cont[sel] - cont_want[sel]) / cont_want[sel]) <= 1e-2
+
+
 def test_continuum_refusals(neb_root, built_lib, restore_root):
     from libopensps_gb300.capi import Context, OpenSPSError
     n = 8
