@@ -257,6 +257,59 @@ def ssp_operator_measure(args, torch, barrier) -> dict | None:
                         "power-law dust, z 0-6 with IGM, smoothing 50-300 km/s, 40 filters"}
 
 
+def ssp_operator_grad_measure(args, torch, barrier) -> dict | None:
+    """The reverse pass through the SSP operator: the operator leg's batch (Kroupa slopes per model) at B =
+    --ops-grad-batch with N(0,1) magnitude cotangents (FP64, page-locked), params_bar with the imf1-3 rows and the
+    weights' cotangent over ages and metallicities, through compute_csp_batch_grad; wall time per call with the
+    device stage times (the forward's, the adjoint, the template-cotangent GEMMs and the reverse fold)."""
+    from libopensps_gb300 import workloads
+    from libopensps_gb300.capi import Context
+    n = args.ops_grad_batch
+    if n <= 0:
+        return None
+    ctx = Context()
+    ctx.set_int("add_igm_absorption", 1)
+    ctx.build_ssp_ops()
+    h_wz = torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True)
+    _, params = workloads.mixed_csp(n, seed=3100, out=h_wz.numpy())
+    rng = np.random.default_rng(3101)
+    params = dict(params, imf1=rng.uniform(0.3, 1.8, n), imf2=rng.uniform(1.3, 2.8, n), imf3=rng.uniform(1.8, 3.3, n))
+    h_mb = torch.empty((n, ctx.nbands), dtype=torch.float64, pin_memory=True).numpy()
+    h_mb[:] = rng.standard_normal(h_mb.shape)
+    out = {"mags": torch.empty((n, ctx.nbands), dtype=torch.float64, pin_memory=True).numpy(),
+           "mass": torch.empty(n, dtype=torch.float64, pin_memory=True).numpy(),
+           "lbol": torch.empty(n, dtype=torch.float64, pin_memory=True).numpy(),
+           "weights_z_bar": torch.empty((n, N_Z, K_AGES), dtype=torch.float64, pin_memory=True).numpy()}
+    wz = h_wz.numpy()
+
+    def call():
+        return ctx.csp_batch_grad(params, wz, mags_bar=h_mb, spec=False, out=out)
+
+    for _ in range(max(args.warmup, 1)):
+        call()
+    barrier()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    for _ in range(args.ops_grad_steps):
+        r = call()
+    barrier()
+    ms = (time.perf_counter() - t0) * 1e3 / args.ops_grad_steps
+    kt = ctx.kernel_times()
+    interp = ctx.ops_last_interpolated()
+    ctx.set_profiling(False)
+    ctx.close()
+    names = ["model_params", "fold_and_template_gemm", "epilogue", "bands", "-", "copies_host", "adjoint",
+             "template_cotangent_gemm", "reverse_fold"]
+    stages = dict(zip(names, kt))
+    dev = sum(v for k, v in stages.items() if k != "copies_host")
+    return {"batch": n, "value": n / (ms * 1e-3), "unit": "models/s", "ms_per_step": ms, "steps": args.ops_grad_steps,
+            "fold": "interpolated" if interp else "exact", "device_ms": dev,
+            "device_value": n / (dev * 1e-3) if dev > 0 else None, "stage_ms": stages,
+            "params_bar_rows": int(r["params_bar"].shape[1]),
+            "workload": "the operator leg's batch with N(0,1) cotangents on 40 magnitudes: params_bar (imf1-3 rows "
+                        "included) and weights_z_bar"}
+
+
 def fp64_measure(args, torch, barrier) -> dict | None:
     """The plain FP64 path of the same workload ("gb300_fp64": DGEMM age sums, every later stage in FP64) at B =
     --fp64-batch through the C API: the denominator of the mixed path's speed-up (device stage times alongside)."""
@@ -631,6 +684,7 @@ def run_ours(args) -> None:
     neb_cont = nebular_continuum_measure(params, h_wz_np, args, barrier)
     adjoint = adjoint_measure(ctx, args, rank, torch, barrier)
     ssp_ops = ssp_operator_measure(args, torch, barrier)
+    ssp_ops_grad = ssp_operator_grad_measure(args, torch, barrier)
     fp64 = fp64_measure(args, torch, barrier)
     sfh_cfg = sfh_config_measure(args, torch, barrier) if rank == 0 else None
     emulator = emulator_measure(args, torch, barrier) if rank == 0 else None
@@ -668,6 +722,7 @@ def run_ours(args) -> None:
             "cpu_baseline": cpu,
             "adjoint": adjoint,
             "ssp_operator": ssp_ops,
+            "ssp_operator_grad": ssp_ops_grad,
             "fp64_path": fp64,
             "mixed_over_fp64": (value / fp64["device_value"]) if fp64 and fp64.get("device_value") else None,
             "sfh_config": sfh_cfg,
@@ -697,6 +752,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=10)
     ap.add_argument("--ops-batch", type=int, default=1024)
     ap.add_argument("--ops-steps", type=int, default=10)
+    ap.add_argument("--ops-grad-batch", type=int, default=1024)
+    ap.add_argument("--ops-grad-steps", type=int, default=5)
     ap.add_argument("--fp64-batch", type=int, default=65536)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--sfh-batch", type=int, default=256)
