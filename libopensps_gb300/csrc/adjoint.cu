@@ -12,6 +12,7 @@
 // The cotangents of the young and old sums leave as the bf16 hi / lo A operands of the weight GEMM; the parameter
 // gradients are block reductions. Every cotangent is divided by a power of two at least the model's largest one
 // (cscale) so that the FP32 arithmetic stays in range; the results are multiplied back in FP64.
+#include <climits>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -721,6 +722,14 @@ __global__ void transpose_bf16_kernel(const __nv_bfloat16 *__restrict__ src, __n
     }
 }
 
+cudaError_t run_transpose_bf16(const __nv_bfloat16 *src, __nv_bfloat16 *dst, int ns, size_t kpad, size_t ld, int ppad,
+                               cudaStream_t st) {
+    if (kpad > (size_t)INT_MAX - 32 || ld > (size_t)INT_MAX) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)((kpad + 31) / 32), (unsigned)((ppad + 31) / 32)), block(32, 8);
+    transpose_bf16_kernel<<<grid, block, 0, st>>>(src, dst, ns, (int)kpad, (int)ld, ppad);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------------- weights' cotangent
 // wzb(t + nt z, m) = cscale_m D(m, col(t, z)) + mass_bar_m M(t, z) + lsum_bar_m L(t, z), lsum_bar = lbol_bar /
 // (ln 10 L_bol) plus the AGN's (backward_age_sums_w; the ssp_weights_z branch of compute_csp_batch's reverse pass).
@@ -1005,9 +1014,15 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         r.wzb = want_wzb ? c.d_wzbar.p : nullptr;
         r.apart = c.d_apart.p;
         r.params_bar = c.d_pbar.p; r.rows = NBGRAD; r.row_imf1 = PB_IMF1;
-        if ((e = run_ops_reverse(r, s)) != cudaSuccess) { err = msg("operator reverse kernel", e); return ST_DATA_MISSING; }
+        // (the reverse of the fold the forward took: the interpolated one as GEMMs against the transposed basis)
+        if (c.ops_last_interp) {
+            if (int rc = run_ops_interp_reverse(c, r, err)) return rc;
+            launches += 1 + (n + 2047) / 2048 * (1 + (r.itesc > 0 ? 1 : 0) + (r.itesc < c.nt ? 1 : 0));
+        } else {
+            if ((e = run_ops_reverse(r, s)) != cudaSuccess) { err = msg("operator reverse kernel", e); return ST_DATA_MISSING; }
+            launches += 2;
+        }
         prof_mark(c, 9);
-        launches += 2;
         if (weights_z_bar &&
             (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * n * ntz, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
             err = msg("weights cotangent copy", e);

@@ -102,10 +102,13 @@ struct SspOps {
     double interp_x0[3] = {}, interp_h[3] = {};
     DevBuf<__nv_bfloat16> ib_hi, ib_lo;
     DevBuf<float> i_mrow, i_lrow;
+    // the reverse of the interpolated fold: the basis transposed (nt nz R x ntpad, bf16 hi / lo, built on first use)
+    DevBuf<__nv_bfloat16> ibt_hi, ibt_lo;
+    CUtensorMap tm_ibt_hi, tm_ibt_lo;
     void release() {
         pts.release(); ent.release(); ent_c.release(); lib_hi.release(); lib_lo.release();
         pidx.release(); pcoef.release(); lib_thi.release(); lib_tlo.release();
-        ib_hi.release(); ib_lo.release(); i_mrow.release(); i_lrow.release();
+        ib_hi.release(); ib_lo.release(); i_mrow.release(); i_lrow.release(); ibt_hi.release(); ibt_lo.release();
         ppad = 0;
         interp_ready = false;
         ready = false;
@@ -275,6 +278,8 @@ struct Context {
     DevBuf<DustEmModel> d_dem;   // the batch's dust emission cells (one per model)
     DevBuf<float> d_bpart;       // the band GEMM's partial fluxes when it splits the pixels (few models)
     DevBuf<float> d_vbar;        // reverse pass with operators: 2n x ntpad template cotangents (young, old)
+    DevBuf<__nv_bfloat16> d_vbh, d_vbl;   // and as bf16 hi / lo (the interpolated reverse fold's A operand)
+    DevBuf<float> d_xbar;        // the interpolated reverse fold: a chunk's cotangents of the operand X
     DevBuf<double> d_apart;      // and nz x n x 3 IMF-slope cotangents per metallicity slab
     DevBuf<int> d_vflag;
     DevBuf<int> d_status;
@@ -354,6 +359,8 @@ void line_basis_host(const Context &c, bool neb, double line_sigma, std::vector<
 int run_fp64_tail(Context &c, const BatchIO &io, BasisOperand *bop, const double *d_wz, const double *d_par, int nacc,
                   int sm_lo, int sm_hi, int i0, std::string &err);
 void fp64_release(Context &c);
+// the reverse of the interpolated fold (ssp_op.cu): r as for run_ops_reverse, the template cotangents in r.vbar
+int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err);
 int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, const double *h_alpha, int itesc,
                   float *d_young, float *d_old, std::string &err);
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,

@@ -324,6 +324,9 @@ struct OpsRevArgs {
     int rows, row_imf1;
 };
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);
+// dst(k, p) = src(p, k) (adjoint.cu): kpad x ppad from the first kpad columns of ns rows of ld, zero for p >= ns
+cudaError_t run_transpose_bf16(const __nv_bfloat16 *src, __nv_bfloat16 *dst, int ns, size_t kpad, size_t ld, int ppad,
+                               cudaStream_t st);
 // The spectrum from the young and old sums (the contraction epilogue's attenuation, IGM and smoothing).
 // A model's emission terms of the per-model epilogue: dust emission (on, the Draine & Li grid cell iq, iu: 0-based
 // lower corner, with its weights and gamma: dl07_indices, src/physics/opensps_csp_batch.f90:1622-1634) and the AGN

@@ -758,6 +758,224 @@ cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------- interpolated reverse
+// The reverse of the interpolated fold. The forward is V = X B^T with X(m, (g, r)) = sw(g, m) ct_m(r), ct_m(r) =
+// c_s / T mu_r^-alpha_s (node r in Kroupa segment s), and the mass and L_bol rows m = X mrow, L = X lrow. With Vbar
+// the template weights' cotangents (divided by cscale), the operand's cotangent is Xbar = Vbar B (a split-BF16
+// tcgen05 GEMM against the transposed basis, young grid points against the young Vbar and the rest against the old)
+// plus mass_bar / cscale mrow + lbol_bar / (ln 10 L_bol cscale) lrow. Then per model
+//     wz_bar(g)   = cscale sum_r Xbar(g, r) ct(r)
+//     alpha_bar_j = cscale sum_r Y(r) ct(r) d ln ct(r) / d alpha_j,   Y(r) = sum_g sw(g) Xbar(g, r),
+//     d ln ct(r) / d alpha_j = -ln mu_r [s = j] + d ln c_s / d alpha_j - d ln T / d alpha_j
+// (c_2 = c_3 = 2^(alpha1 - alpha2); T the IMF's mass between its limits), the transposes of the same expansion the
+// forward's interpolated fold takes (its interpolation error carries over to the cotangents).
+struct OpsInterpRevArgs {
+    int m0, nt, nz, R;
+    size_t ktot;
+    int noff[3], nn[3];
+    double x0[3], h[3];
+    float lim_lo, lim_hi;
+    const double *wz, *alpha, *cscale, *mass_bar, *lbol_bar, *sums;
+    const double2 *kconst;                   // n: 1 / T and c2 (the forward's)
+    const float *xbar;                       // rows x ktot: Vbar B of the chunk
+    const float *mrow, *lrow;
+    double *wzb;                             // n x nt x nz, or null
+    double *params_bar;                      // n x rows, or null
+    int rows, row_imf1;
+};
+constexpr int OPS_IR_THREADS = 256, OPS_IR_WARPS = OPS_IR_THREADS / 32, OPS_IR_RI = OPS_IMAXR / 32;
+
+// One model per CTA: the node values and their log-derivatives in shared memory; warp w takes grid points w, w + 8,
+// ..., lane l the nodes l + 32 i of each (the row of Xbar read once, coalesced): wz_bar(g) by a warp sum, Y(r) in
+// FP32 per lane over 16 grid points at a time, then FP64; the slopes' sums over the nodes by a block reduction.
+__global__ void __launch_bounds__(OPS_IR_THREADS) ops_interp_rev_kernel(OpsInterpRevArgs a) {
+    __shared__ float ct[OPS_IMAXR];
+    __shared__ float dlc[3][OPS_IMAXR];
+    __shared__ float sws[OPS_IMAXG];
+    __shared__ double ypart[OPS_IR_WARPS][OPS_IMAXR];
+    __shared__ double red[OPS_IR_WARPS][3];
+    __shared__ double dlnT_s[3];
+    __shared__ float qm_s, ql_s;
+    const int row = blockIdx.x, m = a.m0 + row, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ng = a.nt * a.nz;
+    const double *al = a.alpha + 3 * (size_t)m;
+    const double *wzm = a.wz + (size_t)ng * m;
+    for (int g = tid; g < ng; g += OPS_IR_THREADS) {
+        const int t = g % a.nt, z = g / a.nt;                 // the weights' order: age fastest
+        const double sw = wzm[g];
+        sws[t * a.nz + z] = sw > SAFE_FLOOR ? (float)sw : 0.f;   // the columns' order: (t nz + z)
+    }
+    const double cs = a.cscale[m];
+    if (tid == 0) {
+        KroupaSeg ks;
+        float itf;
+        double dl[3];
+        kroupa_setup(al, a.lim_lo, a.lim_hi, ks, itf, dl);
+        for (int j = 0; j < 3; ++j) dlnT_s[j] = dl[j];
+        const double ls = a.sums[(size_t)6 * m + 1];
+        qm_s = a.mass_bar ? (float)(a.mass_bar[m] / cs) : 0.f;
+        ql_s = (a.lbol_bar && ls > SAFE_FLOOR) ? (float)(a.lbol_bar[m] / (ls * 2.302585092994046 * cs)) : 0.f;
+    }
+    __syncthreads();
+    const double2 kc = a.kconst[m];                  // 1 / T, c2
+    for (int r = tid; r < OPS_IMAXR; r += OPS_IR_THREADS) {
+        float v = 0.f, d[3] = {0.f, 0.f, 0.f};
+        if (r < a.R) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const int j = r - a.noff[q];
+                if (j >= 0 && j < a.nn[q]) {
+                    const double x = a.x0[q] + (double)(j - OPS_IDEG / 2) * a.h[q];
+                    v = (float)((q == 0 ? 1.0 : kc.y) * kc.x * exp(-al[q] * x));
+                    double g3[3] = {-dlnT_s[0], -dlnT_s[1], -dlnT_s[2]};
+                    g3[q] -= x;
+                    if (q > 0) { g3[0] += KR_LN2; g3[1] -= KR_LN2; }
+                    d[0] = (float)g3[0]; d[1] = (float)g3[1]; d[2] = (float)g3[2];
+                }
+            }
+        }
+        ct[r] = v;
+        dlc[0][r] = d[0]; dlc[1][r] = d[1]; dlc[2][r] = d[2];
+    }
+    __syncthreads();
+    const float qm = qm_s, ql = ql_s;
+    const float *xr = a.xbar + (size_t)row * a.ktot;
+    float y[OPS_IR_RI];
+    double yd[OPS_IR_RI];
+#pragma unroll
+    for (int i = 0; i < OPS_IR_RI; ++i) { y[i] = 0.f; yd[i] = 0.0; }
+    int nstep = 0;
+    for (int g = warp; g < ng; g += OPS_IR_WARPS) {
+        const float sw = sws[g];
+        const size_t base = (size_t)g * a.R;
+        float ws = 0.f;
+#pragma unroll
+        for (int i = 0; i < OPS_IR_RI; ++i) {
+            const int r = lane + 32 * i;
+            if (r < a.R) {
+                const float xt = fmaf(qm, __ldg(a.mrow + base + r), fmaf(ql, __ldg(a.lrow + base + r), __ldg(xr + base + r)));
+                ws = fmaf(xt, ct[r], ws);
+                y[i] = fmaf(sw, xt, y[i]);
+            }
+        }
+        if (a.wzb) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, off);
+            if (lane == 0) {
+                const int t = g / a.nz, z = g - t * a.nz;
+                a.wzb[(size_t)ng * m + t + (size_t)a.nt * z] = cs * (double)ws;
+            }
+        }
+        if (++nstep == 16) {
+#pragma unroll
+            for (int i = 0; i < OPS_IR_RI; ++i) { yd[i] += (double)y[i]; y[i] = 0.f; }
+            nstep = 0;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < OPS_IR_RI; ++i) {
+        const int r = lane + 32 * i;
+        ypart[warp][r] = yd[i] + (double)y[i];
+    }
+    __syncthreads();
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int r = tid; r < a.R; r += OPS_IR_THREADS) {
+        double yv = 0.0;
+        for (int w = 0; w < OPS_IR_WARPS; ++w) yv += ypart[w][r];
+        const double yc = yv * (double)ct[r];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) s[j] += yc * (double)dlc[j][r];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s[j] += __shfl_xor_sync(0xffffffffu, s[j], off);
+        if (lane == 0) red[warp][j] = s[j];
+    }
+    __syncthreads();
+    if (tid < 3 && a.params_bar) {
+        double v = 0.0;
+        for (int w = 0; w < OPS_IR_WARPS; ++w) v += red[w][tid];
+        a.params_bar[(size_t)a.rows * m + a.row_imf1 + tid] = cs * v;
+    }
+}
+
+// FP32 -> bf16 hi / lo, element-wise (count a multiple of 2).
+__global__ void split_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__restrict__ hi,
+                                  __nv_bfloat16 *__restrict__ lo, size_t count) {
+    for (size_t i = 2 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x); i < count; i += 2 * (size_t)gridDim.x * blockDim.x) {
+        const float2 v = *reinterpret_cast<const float2 *>(src + i);
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+        const float2 hf = __bfloat1622float2(h);
+        *reinterpret_cast<__nv_bfloat162 *>(hi + i) = h;
+        *reinterpret_cast<__nv_bfloat162 *>(lo + i) = __floats2bfloat162_rn(v.x - hf.x, v.y - hf.y);
+    }
+}
+
+static std::string cmsg(const char *what, cudaError_t e);
+
+int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err) {
+    SspOps &o = c.ops;
+    cudaStream_t st = c.stream;
+    cudaError_t e;
+    const int n = r.n, nt = c.nt, nz = c.nz, R = o.interp_R;
+    const size_t ktot = (size_t)nt * nz * R;
+    const size_t ky = (size_t)r.itesc * nz * R, ko = ktot - ky;
+    if (!o.interp_ready || ktot > (size_t)INT32_MAX) { err = "the interpolated reverse fold needs the interpolated operator"; return ST_UNSUPPORTED; }
+    // the transposed basis (once per operator)
+    if (!o.ibt_hi.p) {
+        if ((e = o.ibt_hi.reserve(ktot * o.ntpad)) != cudaSuccess || (e = o.ibt_lo.reserve(ktot * o.ntpad)) != cudaSuccess ||
+            (e = run_transpose_bf16(o.ib_hi.p, o.ibt_hi.p, o.ntempl, ktot, ktot, o.ntpad, st)) != cudaSuccess ||
+            (e = run_transpose_bf16(o.ib_lo.p, o.ibt_lo.p, o.ntempl, ktot, ktot, o.ntpad, st)) != cudaSuccess ||
+            (e = encode_tmap_2d_bf16(&o.tm_ibt_hi, o.ibt_hi.p, o.ntpad, ktot, gemm_bk(), gemm_bn())) != cudaSuccess ||
+            (e = encode_tmap_2d_bf16(&o.tm_ibt_lo, o.ibt_lo.p, o.ntpad, ktot, gemm_bk(), gemm_bn())) != cudaSuccess) {
+            err = cmsg("transposed operator basis", e);
+            o.ibt_hi.release(); o.ibt_lo.release();
+            return ST_DATA_MISSING;
+        }
+    }
+    const size_t nv = (size_t)2 * n * o.ntpad;
+    const int chunk = std::min(n, 2048);
+    if ((e = c.d_vbh.reserve(nv)) != cudaSuccess || (e = c.d_vbl.reserve(nv)) != cudaSuccess ||
+        (e = c.d_xbar.reserve((size_t)chunk * ktot)) != cudaSuccess) {
+        err = cmsg("device memory", e);
+        return ST_DATA_MISSING;
+    }
+    split_bf16_kernel<<<(unsigned)std::min<size_t>((nv / 2 + 255) / 256, 8192), 256, 0, st>>>(r.vbar, c.d_vbh.p, c.d_vbl.p, nv);
+    if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("template cotangent operand kernel", e); return ST_DATA_MISSING; }
+    for (int m0 = 0; m0 < n; m0 += chunk) {
+        const int rows = std::min(chunk, n - m0);
+        for (int part = 0; part < 2; ++part) {
+            const size_t N = part ? ko : ky;
+            if (N == 0) continue;
+            GemmPlan pl;
+            pl.num_sms = c.num_sms;
+            pl.tm_b_hi = o.tm_ibt_hi;
+            pl.tm_b_lo = o.tm_ibt_lo;
+            const size_t a0 = ((size_t)(part ? n : 0) + m0) * o.ntpad;
+            if ((e = encode_tmap_2d_bf16(&pl.tm_a_hi, c.d_vbh.p + a0, o.ntpad, rows, gemm_bk(), gemm_bm())) != cudaSuccess ||
+                (e = encode_tmap_2d_bf16(&pl.tm_a_lo, c.d_vbl.p + a0, o.ntpad, rows, gemm_bk(), gemm_bm())) != cudaSuccess) {
+                err = cmsg("template cotangent tensor map", e);
+                return ST_DATA_MISSING;
+            }
+            GemmArgs g;
+            g.M = rows; g.N = (int)N; g.K = o.ntpad; g.ldd = (int)ktot; g.b_row0 = part ? (int)ky : 0;
+            g.D = c.d_xbar.p + (part ? ky : 0); g.status = c.d_status.p;
+            if ((e = run_gemm_bf16x3(pl, g, st)) != cudaSuccess) { err = cmsg("interpolated reverse fold GEMM", e); return ST_DATA_MISSING; }
+        }
+        OpsInterpRevArgs a;
+        a.m0 = m0; a.nt = nt; a.nz = nz; a.R = R; a.ktot = ktot;
+        for (int s = 0; s < 3; ++s) { a.noff[s] = o.interp_noff[s]; a.nn[s] = o.interp_nn[s]; a.x0[s] = o.interp_x0[s]; a.h[s] = o.interp_h[s]; }
+        a.lim_lo = r.lim_lo; a.lim_hi = r.lim_hi;
+        a.wz = r.wz; a.alpha = r.alpha; a.cscale = r.cscale; a.mass_bar = r.mass_bar; a.lbol_bar = r.lbol_bar; a.sums = r.sums;
+        a.kconst = c.d_ix_const.p; a.xbar = c.d_xbar.p; a.mrow = o.i_mrow.p; a.lrow = o.i_lrow.p;
+        a.wzb = r.wzb; a.params_bar = r.params_bar; a.rows = r.rows; a.row_imf1 = r.row_imf1;
+        ops_interp_rev_kernel<<<rows, OPS_IR_THREADS, 0, st>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated reverse fold kernel", e); return ST_DATA_MISSING; }
+    }
+    return 0;
+}
+
 // ---------------------------------------------------------------------------------------------- the epilogue
 // One model per CTA from its young and old sums: the attenuation (attenuate_batch, power law), with dust emission
 // the energy balance (dust_emission_reductions / add_dust_emission, src/physics/opensps_csp_batch.f90:3963-4099:

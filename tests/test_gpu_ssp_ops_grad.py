@@ -78,13 +78,21 @@ def _check(g, fd, names):
     assert float(err.max()) <= RTOL, {names[i]: float(err[:, i].max()) for i in range(len(names))}
 
 
+@pytest.mark.parametrize("fold", ["interpolated", "exact"])
 @pytest.mark.parametrize("n,seed", [(5, 510), (6, 511)])
-def test_slope_rows_and_weights_cotangent(octx, oracles, data, n, seed):
+def test_slope_rows_and_weights_cotangent(octx, oracles, data, n, seed, fold):
+    """Both folds' reverses: the interpolated one (GEMMs against the transposed operator basis) and the exact one
+    (gb300_ops_exact = 1)."""
     wz, params = config3_inputs(n, seed=seed)
     rng = np.random.default_rng(seed + 5)
     params = dict(params, **_slopes(n, rng))
     mb, sb, massb, lbolb = _cot(octx, n, seed)
-    got = octx.csp_batch_grad(params, wz, mags_bar=mb, spec_bar=sb, mass_bar=massb, lbol_bar=lbolb)
+    octx.set_int("gb300_ops_exact", 1 if fold == "exact" else 0)
+    try:
+        got = octx.csp_batch_grad(params, wz, mags_bar=mb, spec_bar=sb, mass_bar=massb, lbol_bar=lbolb)
+        assert octx.ops_last_interpolated() == (fold == "interpolated")
+    finally:
+        octx.set_int("gb300_ops_exact", 0)
     rows = dict(IMF_ROWS, dust2=2)
     names = list(rows)
     g = np.stack([got["params_bar"][:, rows[k]] for k in names], axis=1)
@@ -103,6 +111,30 @@ def test_slope_rows_and_weights_cotangent(octx, oracles, data, n, seed):
     g_w = np.sum(got["weights_z_bar"] * dw, axis=(1, 2))
     err = np.abs(g_w - fd_w) / np.maximum(np.abs(fd_w), 1e-3 * np.max(np.abs(fd_w)))
     assert float(err.max()) <= RTOL, (g_w, fd_w)
+
+
+def test_interpolated_reverse_matches_exact(octx, data):
+    """The interpolated reverse fold against the exact one on 300 models of the operator leg's batch (slopes per
+    model, every grid point weighted): the slope rows and the weights' cotangent within 1e-4 of each row's largest
+    value (the interpolation and the split-BF16 GEMMs against FP32 sums)."""
+    from libopensps_gb300 import workloads
+    n = 300
+    wz, params = workloads.mixed_csp(n, seed=530)
+    rng = np.random.default_rng(531)
+    params = dict(params, **_slopes(n, rng))
+    mb, sb, massb, lbolb = _cot(octx, n, 532)
+    out = {}
+    for fold in ("interpolated", "exact"):
+        octx.set_int("gb300_ops_exact", 1 if fold == "exact" else 0)
+        try:
+            out[fold] = octx.csp_batch_grad(params, wz, mags_bar=mb, spec_bar=sb, mass_bar=massb, lbol_bar=lbolb)
+        finally:
+            octx.set_int("gb300_ops_exact", 0)
+    gi, ge = out["interpolated"]["params_bar"][:, 26:29], out["exact"]["params_bar"][:, 26:29]
+    assert np.all(np.abs(gi - ge) <= 1e-4 * np.max(np.abs(ge), axis=0))
+    wi, we = out["interpolated"]["weights_z_bar"], out["exact"]["weights_z_bar"]
+    scale = np.max(np.abs(we), axis=(1, 2), keepdims=True)
+    assert float(np.max(np.abs(wi - we) / scale)) <= 1e-4
 
 
 def test_slope_rows_without_weights_cotangent(octx, data):
