@@ -41,14 +41,23 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     const bool igm = live && a.add_igm && z > SAFE_FLOOR && a.jtop > 0;
     // redshift factors b_k = (1 + z)^p_k (igm_tau_z_terms, src/physics/opensps_cosmology.f90:497-508)
     float b[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const double l1z = live ? log1p(z) : 0.0;   // (also the observed frame's shift below)
     if (igm) {
-        // (1 + z)^p as exp(p ln(1 + z)): one FP64 logarithm for the six powers
-        const double l1z = log1p(z);
-        b[0] = (float)exp(3.46 * l1z);
-        b[1] = (float)exp(1.68 * l1z);
-        b[2] = (float)exp((3.0 + 0.46) * l1z);
-        b[3] = (float)exp((1.5 + 0.18) * l1z);
-        b[4] = (float)exp((3.0 - 1.32) * l1z);
+        // (1 + z)^p = 2^(p ln(1 + z) log2 e): the exponent formed and split in FP64 (x = n + r, |r| <= 1/2), 2^r
+        // by the SFU and 2^n exactly (the reference's exp_kp: FP64 argument, exponential at kernel precision; the
+        // factors are stored as FP32)
+        auto pw = [&](double pexp) {
+            const double x = pexp * l1z * LOG2E, n = rint(x);
+            float r;
+            asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)(x - n)));
+            const int ni = (int)n;
+            return (ni > -126 && ni < 128) ? r * __int_as_float((ni + 127) << 23) : (float)exp(pexp * l1z);
+        };
+        b[0] = pw(3.46);
+        b[1] = pw(1.68);
+        b[2] = pw(3.0 + 0.46);
+        b[3] = pw(1.5 + 0.18);
+        b[4] = pw(3.0 - 1.32);
         b[5] = b[1];
     }
     // the cap (apply_igm_z :4272-4299): the first pixel of the largest optical depth, searched by the whole warp for
@@ -167,7 +176,7 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     float4 zi = make_float4(__int_as_float(0), 0.f, 0.f, 0.f);
     double dd = 0.0;
     if (fabs(z) > SAFE_FLOOR) {
-        const double s = log1p(z) / a.dlnl;
+        const double s = l1z / a.dlnl;
         const double n0 = floor(s), phi = s - n0;
         zi.x = __int_as_float((int)n0);
         zi.y = phi > 0.0 ? (float)(expm1((1.0 - phi) * a.dlnl) / expm1(a.dlnl)) : 0.f;
