@@ -836,6 +836,26 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     }
     if (nb > ADJ_MAX_BANDS) { err = "more than 256 bands"; return ST_UNSUPPORTED; }
     cudaError_t e;
+    // ---- the cotangents to the device on their own stream, beside the forward (from page-locked memory the copies
+    // overlap its weight copy and kernels; the reverse pass waits for them on the batch's stream)
+    auto put = [&](DevBuf<double> &d, const double *h, size_t cnt) -> cudaError_t {
+        cudaError_t r = d.reserve(cnt);
+        if (r != cudaSuccess) return r;
+        return cudaMemcpyAsync(d.p, h, sizeof(double) * cnt, cudaMemcpyHostToDevice, c.side3);
+    };
+    // (every return waits for these copies first: the caller may reuse its buffers once the call returns)
+    struct CopiesDone {
+        cudaStream_t s;
+        ~CopiesDone() { cudaStreamSynchronize(s); }
+    } copies_done{c.side3};
+    if ((mags_bar && (e = put(c.d_mags_bar, mags_bar, (size_t)n * nb)) != cudaSuccess) ||
+        (spec_bar && (e = put(c.d_spec_bar, spec_bar, (size_t)n * ns)) != cudaSuccess) ||
+        (mass_bar && (e = put(c.d_mass_bar, mass_bar, n)) != cudaSuccess) ||
+        (lbol_bar && (e = put(c.d_lbol_bar, lbol_bar, n)) != cudaSuccess) ||
+        (e = cudaEventRecord(c.ev_cot, c.side3)) != cudaSuccess) {
+        err = msg("cotangent copy", e);
+        return ST_DATA_MISSING;
+    }
     // ---- the forward, keeping the young and old sums and the band fluxes on the device
     if ((e = c.d_fband.reserve((size_t)n * std::max(nb, 1))) != cudaSuccess) { err = msg("device memory", e); return ST_DATA_MISSING; }
     BatchIO io = io_in;
@@ -910,19 +930,8 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     }
     const int ppad = ops ? c.ops.ppad : bop->ppad;
 
-    // ---- cotangents to the device
-    auto put = [&](DevBuf<double> &d, const double *h, size_t cnt) -> cudaError_t {
-        cudaError_t r = d.reserve(cnt);
-        if (r != cudaSuccess) return r;
-        return cudaMemcpyAsync(d.p, h, sizeof(double) * cnt, cudaMemcpyHostToDevice, s);
-    };
-    if ((mags_bar && (e = put(c.d_mags_bar, mags_bar, (size_t)n * nb)) != cudaSuccess) ||
-        (spec_bar && (e = put(c.d_spec_bar, spec_bar, (size_t)n * ns)) != cudaSuccess) ||
-        (mass_bar && (e = put(c.d_mass_bar, mass_bar, n)) != cudaSuccess) ||
-        (lbol_bar && (e = put(c.d_lbol_bar, lbol_bar, n)) != cudaSuccess)) {
-        err = msg("cotangent copy", e);
-        return ST_DATA_MISSING;
-    }
+    // ---- the cotangents (copied beside the forward) before the reverse pass's kernels
+    if ((e = cudaStreamWaitEvent(s, c.ev_cot, 0)) != cudaSuccess) { err = msg("cotangent copy", e); return ST_DATA_MISSING; }
     if ((e = c.d_cscale.reserve(n)) != cudaSuccess || (e = c.d_pbar.reserve((size_t)NBGRAD * n)) != cudaSuccess ||
         (e = c.d_ybh.reserve((size_t)n * ppad)) != cudaSuccess || (e = c.d_ybl.reserve((size_t)n * ppad)) != cudaSuccess ||
         (e = c.d_obh.reserve((size_t)n * ppad)) != cudaSuccess || (e = c.d_obl.reserve((size_t)n * ppad)) != cudaSuccess) {

@@ -211,6 +211,8 @@ Context::~Context() {
     if (ev_contract) cudaEventDestroy(ev_contract);
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
+    if (side3) cudaStreamDestroy(side3);
+    if (ev_cot) cudaEventDestroy(ev_cot);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -720,6 +722,8 @@ int context_setup_grid(Context &c, std::string &err) {
     if ((!c.stream && (e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.side && (e = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.side2 && (e = cudaStreamCreateWithFlags(&c.side2, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.side3 && (e = cudaStreamCreateWithFlags(&c.side3, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.ev_cot && (e = cudaEventCreateWithFlags(&c.ev_cot, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_contract && (e = cudaEventCreateWithFlags(&c.ev_contract, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_fork && (e = cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_params && (e = cudaEventCreateWithFlags(&c.ev_params, cudaEventDisableTiming)) != cudaSuccess) ||
