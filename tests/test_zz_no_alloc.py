@@ -7,8 +7,9 @@ synchronises the device under the framework's stream. Its scratch is a fixed dev
 The batch (opensps_context_compute_csp_batch_grad with no cotangents) gives the magnitudes and leaves its FP32
 spectra on the device (opensps_context_batch_spec_device); the no-allocation entry point forms the magnitudes of
 those spectra at the same redshifts. Two calls in a row with different batches, each within the parity tests'
-magnitude tolerance (1e-3 mag) and with the same NaN pattern (bands not computed). A fresh process checks that the
-first call after the context's set-up changes no device memory (its kernels and array were loaded by the set-up).
+magnitude tolerance (1e-3 mag) and with the same NaN pattern (bands not computed); the first also against the FP64
+oracle's magnitudes of the same models (1e-3 mag). A fresh process checks that the first call after the context's
+set-up changes no device memory (its kernels and array were loaded by the set-up).
 """
 import os
 import subprocess
@@ -26,7 +27,7 @@ MAG_TOL = 1e-3
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def _check_against_batch(ctx, torch, n, seed, mask=None):
+def _check_against_batch(ctx, torch, n, seed, mask=None, oracle_data=None):
     wz, params = config3_inputs(n, seed=seed)
     ref = ctx.csp_batch(params, ssp_weights_z=wz, spec=False)
     p, ns, nlast, nbytes = ctx.spec_device()
@@ -39,6 +40,12 @@ def _check_against_batch(ctx, torch, n, seed, mask=None):
     assert np.array_equal(np.isnan(got), np.isnan(ref["mags"]))
     err = float(np.nanmax(np.abs(got - ref["mags"])))
     assert err <= MAG_TOL, err
+    if oracle_data is not None:
+        from oracle.oracle import Oracle
+        want = Oracle(oracle_data, nbands=ctx.nbands).csp_batch(params, wz)["mags"]
+        assert np.array_equal(np.isnan(got), np.isnan(want))
+        err = float(np.nanmax(np.abs(got - want)))
+        assert err <= MAG_TOL, err
     return got
 
 
@@ -48,7 +55,7 @@ def test_noalloc_mags_match_batch_entry_point(data, built_lib):
     c = Context()
     c.set_int("add_neb_emission", 1)
     c.set_int("add_igm_absorption", 1)
-    _check_against_batch(c, torch, 300, seed=501)
+    _check_against_batch(c, torch, 300, seed=501, oracle_data=data)
     # a second call, fewer models, on the scratch the first one left behind
     _check_against_batch(c, torch, 37, seed=502)
     c.close()
