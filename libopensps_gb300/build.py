@@ -19,7 +19,7 @@ OUT = HERE / "_lib"
 LIB = OUT / "libopensps_gb300.so"
 SOURCES = ["capi.cu", "context.cu", "batch.cu", "csp_contract.cu", "csp_aux.cu", "band_gemm.cu", "gemm_bf16x3.cu",
            "adjoint.cu", "noalloc.cu", "sfh.cu", "ssp_op.cu", "fp64_path.cu", "emulator.cu",
-           "emulator_train.cu", "datalib.cu"]
+           "emulator_train.cu", "datalib.cu", "dust_curves.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_LIB = "/usr/local/cuda/lib64"   # cuBLAS (the plain FP64 path's DGEMM)
 

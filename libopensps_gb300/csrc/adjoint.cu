@@ -36,9 +36,9 @@ constexpr int NBGRAD = 44;
 
 // gradient rows of params_bar (opensps.h)
 enum { R_DUST1 = 1, R_DUST2 = 2, R_DUST3 = 3, R_DUST_INDEX = 4, R_DUST1_INDEX = 5, R_FRAC_OBRUN = 6,
-       R_FRAC_NODUST = 7, R_ZRED = 22, R_SIGMA = 23, R_IGM_FACTOR = 32 };
+       R_FRAC_NODUST = 7, R_MWR = 8, R_UVB = 9, R_ZRED = 22, R_SIGMA = 23, R_IGM_FACTOR = 32 };
 enum { G_DUST2 = 0, G_DUST_INDEX, G_FNODUST, G_DUST1, G_DUST1_INDEX, G_FOBRUN, G_DUST3, G_ZRED, G_IGMF, G_SIGMA,
-       G_OBS, G_WQ, G_WU, G_GAM, NG };
+       G_OBS, G_MWR, G_UVB, G_WQ, G_WU, G_GAM, NG };
 // rows of the dust emission and the AGN torus (opensps.h)
 enum { R_FAGN = 0, R_DUSTE_QPAH = 10, R_DUSTE_UMIN = 11, R_DUSTE_GAMMA = 12, R_AGN_TAU = 31 };
 
@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(256) adjoint_prep_kernel(AdjointPrepArgs a) {
 // The forward's per-pixel factors of a model (as the contraction's epilogue forms them).
 struct PixFwd {
     float curve, ltab, td, c1, tb, to, D, ssfac_y;
+    float dci, dcm, dcu;   // the diffuse curve's derivatives in dust_index, mwr and uvb
     float tau, dtau;   // IGM optical depth at unit igm_factor and its derivative in z (0 without IGM)
     bool igm;
 };
@@ -192,7 +193,14 @@ __device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const ModelC
     PixFwd f;
     const float ltab2 = fmaf((float)p, a.lt_step, a.lt_base);   // ln(lambda / 5500) log2(e) on the log-uniform grid
     f.ltab = ltab2 * 0.6931471805599453f;                        // ln(lambda / 5500)
-    f.curve = adj_ex2(mc.dust_index * ltab2);
+    if (a.ctab) {
+        // the batch's tabulated curve (dust_type 1, 2, 4, 6) with its derivatives
+        const float4 ct = __ldg(a.ctab + p);
+        f.curve = ct.x; f.dci = ct.y; f.dcm = ct.z; f.dcu = ct.w;
+    } else {
+        f.curve = adj_ex2(mc.dust_index * ltab2);
+        f.dci = f.curve * f.ltab; f.dcm = 0.f; f.dcu = 0.f;
+    }
     f.td = adj_ex2(mc.kd2 * f.curve);
     f.c1 = adj_ex2(mc.dust1_index * ltab2);
     f.tb = (mc.kd1 != 0.f) ? adj_ex2(mc.kd1 * f.c1) : 1.f;
@@ -217,6 +225,13 @@ __device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const ModelC
     return f;
 }
 
+// A cotangent of the diffuse curve at one pixel into the dust_index, mwr and uvb rows.
+__device__ __forceinline__ void curve_rows(const PixFwd &f, float cbar, float *g) {
+    g[G_DUST_INDEX] = fmaf(cbar, f.dci, g[G_DUST_INDEX]);
+    g[G_MWR] = fmaf(cbar, f.dcm, g[G_MWR]);
+    g[G_UVB] = fmaf(cbar, f.dcu, g[G_UVB]);
+}
+
 // The reverse pass of one pixel: from dL / dTOT (tb), the forward's sums (y, o), the gradient accumulators and the
 // cotangents of y and o.
 __device__ __forceinline__ void pixel_adjoint(const AdjointArgs &a, const ModelConst &mc, const PixFwd &f, float y,
@@ -235,11 +250,10 @@ __device__ __forceinline__ void pixel_adjoint(const AdjointArgs &a, const ModelC
         g[G_IGMF] = fmaf(gT, -f.tau * T, g[G_IGMF]);
         pb *= T;
     }
-    // pre = ss D, D = T_d (1 - fnd) + fnd, ss = y (T_b (1 - fo) + fo) + o T_o
-    const float dcurve = f.curve * f.ltab;   // d curve / d dust_index
+    // pre = ss D, D = T_d (1 - fnd) + fnd, ss = y (T_b (1 - fo) + fo) + o T_o; the curve's cotangent through the
+    // diffuse and old-star screens into dust_index, mwr and uvb
     g[G_DUST2] = fmaf(pb * ss * mc.one_m_fnd, -f.td * f.curve, g[G_DUST2]);
-    g[G_DUST_INDEX] = fmaf(pb, ss * mc.one_m_fnd * f.td * (-d2 * dcurve) + f.D * o * f.to * (-d3 * dcurve),
-                           g[G_DUST_INDEX]);
+    curve_rows(f, pb * (ss * mc.one_m_fnd * f.td * -d2 + f.D * o * f.to * -d3), g);
     g[G_FNODUST] = fmaf(pb * ss, 1.f - f.td, g[G_FNODUST]);
     const float ybase = pb * f.D * y;
     g[G_DUST1] = fmaf(ybase * mc.one_m_fo, -f.tb * f.c1, g[G_DUST1]);
@@ -628,14 +642,14 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
                         if (mc.kd3 != 0.f) {
                             const float tob = A * o * (omd - 1.f);
                             g[G_DUST3] = fmaf(tob, -f.curve * f.to, g[G_DUST3]);
-                            g[G_DUST_INDEX] = fmaf(tob, -d3 * f.curve * f.ltab * f.to, g[G_DUST_INDEX]);
+                            curve_rows(f, tob * -d3 * f.to, g);
                         }
                     }
                     // the AGN: lagn tmpl T_d
                     if (agn) td_bar = fmaf(sb * lagn, fmaf(dm.wta, __ldg(ag1 + q) - __ldg(ag0 + q), __ldg(ag0 + q)), td_bar);
                     // T_d = exp(-dust2 curve)
                     g[G_DUST2] = fmaf(td_bar, -f.curve * f.td, g[G_DUST2]);
-                    g[G_DUST_INDEX] = fmaf(td_bar, -d2 * f.curve * f.ltab * f.td, g[G_DUST_INDEX]);
+                    curve_rows(f, td_bar * -d2 * f.td, g);
                 }
             }
         }
@@ -657,9 +671,11 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     __syncthreads();
     if (tid < NBGRAD) {
         const double c = ldexp(1.0, ks);
-        constexpr int NROW = 10;
+        // (row_of[k]: the params_bar row of accumulator k; G_OBS goes into the zred row below)
+        constexpr int NROW = 13;
         const int row_of[NROW] = {R_DUST2, R_DUST_INDEX, R_FRAC_NODUST, R_DUST1, R_DUST1_INDEX, R_FRAC_OBRUN,
-                                  R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA};
+                                  R_DUST3, R_ZRED, R_IGM_FACTOR, R_SIGMA, -1, R_MWR, R_UVB};
+        static_assert(G_OBS == 10 && G_MWR == 11 && G_UVB == 12, "row_of follows the accumulators' order");
         double v = 0.0;
         int k = -1;
 #pragma unroll
@@ -957,6 +973,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     a.zinfo = c.d_zinfo.p; a.fband = c.d_fband.p;
     a.mags_bar = mags_bar ? c.d_mags_bar.p : nullptr;
     a.spec_bar = spec_bar ? c.d_spec_bar.p : nullptr;
+    a.ctab = c.geom.ctab;
     a.do_band = c.mag_mask.empty() ? nullptr : c.d_do_band.p;
     a.pix = c.d_pix.p; a.wl = c.d_wl.p; a.bc = c.d_bc.p; a.bmeta = c.d_bmeta.p; a.bchunk = c.d_bchunk.p;
     a.lt_base = (float)(std::log(c.lam[0] / 5500.0) * 1.4426950408889634);

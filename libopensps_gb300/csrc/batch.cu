@@ -488,7 +488,10 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
 
     // ---- checks shared by the batch (the reference's batch_check_models / plan_smoothing rules)
-    if (c.dust_type != 0) { err = "dust_type " + std::to_string(c.dust_type) + ": only the power law (0) on this path"; return ST_UNSUPPORTED; }
+    if (!dust_type_supported(c.dust_type)) {
+        err = "dust_type " + std::to_string(c.dust_type) + ": the table lookups (3, 5) are not supported on this path";
+        return ST_UNSUPPORTED;
+    }
     if (c.compute_vega_mags != 0) { err = "compute_vega_mags = 1 is not supported on this path"; return ST_UNSUPPORTED; }
     if (c.smooth_velocity != 1) { err = "smooth_velocity = 0 is not supported on this path"; return ST_UNSUPPORTED; }
     const double minl = par(0, PF_MIN_WAVE_SMOOTH), maxl = par(0, PF_MAX_WAVE_SMOOTH);
@@ -701,30 +704,61 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         if (!bop) return ST_DATA_MISSING;
     }
 
-    // ---- per-pixel table (rebuilt when the batch's shared dust_index changes): ln(lambda / 5500) log2(e), the
-    // diffuse curve (lambda / 5500)^dust_index in FP64 (exp_kp of the reference: the argument formed in FP64), the
-    // Madau wavelength factors
+    // ---- per-pixel table (rebuilt when the batch's shared curve changes): ln(lambda / 5500) log2(e), the diffuse
+    // curve shared by the batch's models in FP64 (the reference's tables, attenuation_tables_cached :3494-3560, times
+    // exp_kp of the power law: the argument formed in FP64), the Madau wavelength factors. dust_type 0 with a
+    // dust_index per model forms its curve in the kernels instead; the other types need the curve's parameters (mwr
+    // and uvb for 1, dust_index for 4) the same for every model of a batch on this path.
     const double idx0 = par(0, PF_DUST_INDEX);
     bool uniform_index = true;
-    for (int m = 1; m < n && uniform_index; ++m) uniform_index = par(m, PF_DUST_INDEX) == idx0;
-    if (!c.d_pix.p || (uniform_index && c.pix_index != idx0)) {
+    double sc0[4];
+    dust_scalars(c.dust_type, idx0, par(0, PF_MWR), par(0, PF_UVB), sc0);
+    for (int m = 1; m < n && uniform_index; ++m) {
+        double sc[4];
+        dust_scalars(c.dust_type, par(m, PF_DUST_INDEX), par(m, PF_MWR), par(m, PF_UVB), sc);
+        uniform_index = sc[0] == sc0[0] && sc[1] == sc0[1] && sc[2] == sc0[2] && sc[3] == sc0[3];
+    }
+    if (!uniform_index && c.dust_type != 0) {
+        err = "dust_type " + std::to_string(c.dust_type) + ": " + (c.dust_type == 1 ? "mwr and uvb" : "dust_index") +
+              " must be the same for every model of a batch on this path";
+        return ST_UNSUPPORTED;
+    }
+    if (c.dust_type != 0 && fp64) {
+        err = "dust_type " + std::to_string(c.dust_type) + " is not supported on the plain FP64 path";
+        return ST_UNSUPPORTED;
+    }
+    const double key[5] = {(double)c.dust_type, sc0[0], sc0[1], sc0[2], sc0[3]};
+    bool same_key = true;
+    for (int k = 0; k < 5; ++k) same_key = same_key && c.pix_key[k] == key[k];
+    if (!c.d_pix.p || (uniform_index && !same_key)) {
+        std::vector<double> tab;
+        dust_tables(c.dust_type, c.lam, tab);
         std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
+        std::vector<float4> ctab(c.dust_type != 0 ? (size_t)ns : 0);
         for (int j = 0; j < ns; ++j) {
             float *px = pix.data() + (size_t)j * PIX_FLOATS;
             const double ltab = std::log(c.lam[j] / 5500.0);
+            double curve, dci, dcm, dcu;
+            dust_curve_row(tab.data() + 4 * (size_t)j, sc0, ltab, curve, dci, dcm, dcu, c.dust_type, par(0, PF_MWR),
+                           par(0, PF_UVB));
             px[PIX_LTAB2] = (float)(ltab * 1.4426950408889634);
-            px[PIX_CURVE] = (float)(idx0 != 0.0 ? std::exp(idx0 * ltab) : 1.0);
+            px[PIX_CURVE] = (float)curve;
+            if (c.dust_type != 0) ctab[j] = make_float4((float)curve, (float)dci, (float)dcm, (float)dcu);
             if (j < c.jtop)
                 for (int k = 0; k < 6; ++k) px[PIX_IGM_A + k] = c.igm_a[(size_t)j * 6 + k];
         }
         cudaError_t e;
         if ((e = c.d_pix.reserve(pix.size())) != cudaSuccess ||
-            (e = cudaMemcpy(c.d_pix.p, pix.data(), sizeof(float) * pix.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            (e = cudaMemcpy(c.d_pix.p, pix.data(), sizeof(float) * pix.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (!ctab.empty() && ((e = c.d_ctab.reserve(ctab.size())) != cudaSuccess ||
+                               (e = cudaMemcpy(c.d_ctab.p, ctab.data(), sizeof(float4) * ctab.size(),
+                                               cudaMemcpyHostToDevice)) != cudaSuccess))) {
             err = cuda_msg("pixel table", e);
             return ST_DATA_MISSING;
         }
-        c.pix_index = idx0;
+        for (int k = 0; k < 5; ++k) c.pix_key[k] = key[k];
     }
+    c.geom.ctab = c.dust_type != 0 ? c.d_ctab.p : nullptr;
     // the smoothed pixels: lambda within [min_wave_smooth, max_wave_smooth]
     int sm_lo = ns, sm_hi = -1;
     for (int j = 0; j < ns; ++j)

@@ -217,7 +217,7 @@ void opensps_context_create(int *handle, int *status) {
     // the defaults of the parameters this path reads
     const char *names[] = {"dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun",
                            "zred", "igm_factor", "sigma_smooth", "dust_tesc", "logzsol", "tage", "tau",
-                           "min_wave_smooth", "max_wave_smooth", "gas_logz", "gas_logu"};
+                           "min_wave_smooth", "max_wave_smooth", "gas_logz", "gas_logu", "mwr", "uvb"};
     for (const char *nm : names) {
         const ParamInfo *p = find_param(nm);
         c->pdef[p->id] = p->def;

@@ -27,11 +27,12 @@ static const ParamInfo PARAMS[] = {
     {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3}, {"duste_qpah", PF_DUSTE_QPAH, 3.5},
     {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01}, {"fagn", PF_FAGN, 0.0},
     {"agn_tau", PF_AGN_TAU, 10.0},
-    // known to the reference, not varied per model by this path (gas_logz and gas_logu are: the nebular continuum)
+    // known to the reference, not varied per model by this path (gas_logz and gas_logu are: the nebular continuum;
+    // mwr and uvb are, by the batch, with dust_type 1)
     {"sf_slope", -1, 0.0}, {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
     {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
     {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
-    {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", -1, 1.0}, {"mwr", -1, 3.1},
+    {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", PF_UVB, 1.0}, {"mwr", PF_MWR, 3.1},
     {"gas_logu", PF_GAS_LOGU, -2.0},
     {"gas_logz", PF_GAS_LOGZ, 0.0}, {"gas_logn", -1, 2.0}, {"gas_logno", -1, 0.0}, {"gas_logco", -1, 0.0},
     {"sfh", -1, 0.0}, {"zmet", -1, 1.0}, {"evtype", -1, -1.0},
@@ -168,7 +169,7 @@ Context::~Context() {
         kv.second->release();
         delete kv.second;
     }
-    d_ion.release(); d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
+    d_ion.release(); d_pix.release(); d_ctab.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
     d_lam.release(); d_lnlam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();
@@ -782,7 +783,7 @@ int context_setup_grid(Context &c, std::string &err) {
         }
     }
     c.d_pix.release();   // rebuilt by the next batch (smoothing range)
-    c.pix_index = -1e300;
+    c.pix_key[0] = -1e300;
     int st = context_load_filters(c, c.filter_set, err);
     if (st != 0) return st;
     for (auto &kv : c.basis_cache) { kv.second->release(); delete kv.second; }

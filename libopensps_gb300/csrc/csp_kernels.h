@@ -227,6 +227,9 @@ struct AdjointArgs {
     int lsum_stride = 6;
     const float4 *dchain = nullptr;
     double *lsum_bar = nullptr;
+    // the batch's tabulated diffuse curve (dust_type 1, 2, 4, 6; null: the power law of each model's dust_index): per
+    // pixel the curve and its derivatives in dust_index, mwr and uvb
+    const float4 *ctab = nullptr;
 };
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 

@@ -1366,6 +1366,7 @@ int emu_predict(Context &c, int n, const double *inputs, int fallback, double *m
                 double *spread, int *source, int *n_fallback, std::string &err) {
     Emulator &e = c.emu;
     if (!e.ready) { err = "no emulator on the context (opensps_gb300_emulator_load / _train)"; return ST_NO_OPERATOR; }
+    if (c.dust_type != 0) { err = "emulator: trained with the power-law dust curve (dust_type 0)"; return ST_UNSUPPORTED; }
     if (n <= 0) { if (n_fallback) *n_fallback = 0; return 0; }
     if (!inputs) { err = "emulator: inputs are NULL"; return ST_BAD_ARG; }
     if (int rc = emu_scratch(e, n, err)) return rc;

@@ -326,7 +326,7 @@ int oracle_velocity_row(int n, const double *lam, double sigma, double minl, dou
 /* Per-model parameters, in this order (doubles): */
 enum { P_DUST1, P_DUST2, P_DUST3, P_DUST_INDEX, P_DUST1_INDEX, P_FRAC_NODUST, P_FRAC_OBRUN, P_ZRED,
        P_IGM_FACTOR, P_SIGMA_SMOOTH, P_DUST_TESC, P_DUSTE_QPAH, P_DUSTE_UMIN, P_DUSTE_GAMMA, P_FAGN, P_AGN_TAU,
-       P_GAS_LOGZ, P_GAS_LOGU, P_NPAR };
+       P_GAS_LOGZ, P_GAS_LOGU, P_MWR, P_UVB, P_NPAR };
 
 typedef struct {
     int nspec, nt, nz, nbands;
@@ -357,7 +357,112 @@ typedef struct {
      * spectral grid, nspec x 11 x 10 x 7 (pixel fastest, then log Z, age, log U: nebem_cont(j, z, a, u)), the grid's
      * log Z, log10 age and log U values */
     const double *neb_cont, *neb_logz, *neb_lage, *neb_logu;
+    int dust_type;           /* the diffuse curve (dust_type 0, 1, 2, 4, 6) */
 } oracle_grid_t;
+
+/* ------------------------------------------------------------------------------------------ */
+/* The attenuation curves (compute_attenuation_curve_point, src/physics/opensps_dust.f90:237-269): A_lambda / A_V  */
+/* of the power law (0), Cardelli, Clayton & Mathis 1989 with R_V = mwr and the bump scaled by uvb (1), Calzetti   */
+/* et al. 2000 (2), Kriek & Conroy 2013 with slope dust_index (4), Reddy et al. 2015 (6); each as those papers'     */
+/* published forms, with the extensions beyond their ranges the reference takes (its constants, :47-160).          */
+/* ------------------------------------------------------------------------------------------ */
+
+/* CCM89 (get_ccm89_curve_point :424-556) at wavenumber x = 1 / lambda[um], as a + b / R_V in each region: the
+ * infrared power law from x = 0.1, the optical polynomial in x - 1.82 (1.1 <= x < 3.3), the ultraviolet's linear
+ * term with the 2175 A Drude bump scaled by uvb (3.3 <= x < 8) and its far-UV curvature from x = 5.9, the far-UV
+ * cubic in x - 8 (x held at 12 beyond); no extinction below x = 0.1. In the near UV (3.3 <= x < 5.9) the gap
+ * between the optical and ultraviolet forms at x = 3.3 is added, fading as (3.3 / x)^6. */
+static void ccm89_opt(double y, double *a, double *b) {
+    static const double ca[8] = {1.0, 0.17699, -0.50447, -0.02427, 0.72085, 0.01979, -0.77530, 0.32999};
+    static const double cb[8] = {0.0, 1.41338, 2.28305, 1.07233, -5.38434, -0.62251, 5.30260, -2.09002};
+    double pa = 0.0, pb = 0.0;
+    for (int k = 7; k >= 0; --k) { pa = pa * y + ca[k]; pb = pb * y + cb[k]; }
+    *a = pa;
+    *b = pb;
+}
+static void ccm89_uv(double x, double uvb, double *a, double *b) {
+    *a = 1.752 - 0.316 * x + (-0.104 / ((x - 4.67) * (x - 4.67) + 0.341)) * uvb;
+    *b = -3.09 + 1.825 * x + (1.206 / ((x - 4.62) * (x - 4.62) + 0.263)) * uvb;
+}
+double oracle_ccm89(double lam, double rv, double uvb) {
+    const double x = 1.0e4 / lam;
+    double a, b;
+    if (x >= 8.0) {
+        const double t = (x < 12.0 ? x : 12.0) - 8.0;
+        a = -1.073 + t * (-0.628 + t * (0.137 + t * -0.070));
+        b = 13.67 + t * (4.257 + t * (-0.42 + t * 0.374));
+        return a + b / rv;
+    }
+    if (x >= 3.3) {
+        ccm89_uv(x, uvb, &a, &b);
+        if (x >= 5.9) {
+            const double t = x - 5.9;
+            a += -0.04473 * t * t - 0.009779 * t * t * t;
+            b += 0.2130 * t * t + 0.1207 * t * t * t;
+            return a + b / rv;
+        }
+        double ao, bo, au, bu;
+        ccm89_opt(3.3 - 1.82, &ao, &bo);
+        ccm89_uv(3.3, uvb, &au, &bu);
+        const double gap = (ao + bo / rv) - (au + bu / rv);
+        return a + b / rv + gap * pow(3.3 / x, 6.0);
+    }
+    if (x >= 1.1) {
+        ccm89_opt(x - 1.82, &a, &b);
+        return a + b / rv;
+    }
+    if (x >= 0.1) {
+        const double p = pow(x, 1.61);
+        return 0.574 * p + (-0.527 * p) / rv;
+    }
+    return 0.0;
+}
+
+/* Calzetti et al. 2000 eq. 4 (get_calzetti_curve_point :567-594): k' = 2.659 (poly(x)) + R_V with R_V = 4.05, the
+ * UV-optical cubic below 0.63 um and the linear law above, both extended past 0.12-2.2 um, k' clipped at 0;
+ * A / A_V = k' / R_V. */
+double oracle_calzetti(double lam) {
+    const double x = 1.0e4 / lam;
+    const double k = lam > 6300.0 ? 2.659 * (-1.857 + 1.040 * x) + 4.05
+                                  : 4.05 + 2.659 * (-2.156 + x * (1.509 + x * (-0.198 + x * 0.011)));
+    return (k > 0.0 ? k : 0.0) / 4.05;
+}
+
+/* Kriek & Conroy 2013 (get_kriek_conroy_curve_point :598-626): (k'_Calzetti + E_b D(lambda)) / 4.05 times
+ * (lambda / 5500)^delta, the Drude bump D at 2175 A of width 350 A with E_b = 0.85 - 1.9 delta. */
+double oracle_kc13(double lam, double delta) {
+    const double w = lam * 350.0, d = lam * lam - 2175.0 * 2175.0;
+    const double drude = (0.85 - 1.9 * delta) * w * w / (d * d + w * w);
+    return (oracle_calzetti(lam) * 4.05 + drude) / 4.05 * pow(lam / V_BAND, delta);
+}
+
+/* Reddy et al. 2015 (get_reddy_curve_point :630-662): k = poly(x) + 2.505 (the UV cubic below 0.6 um, x held at
+ * 1 / 0.15 um shorter; the optical cubic from 0.6 to 2.85 um with the reference's continuity offset -0.036221981;
+ * 0 beyond), A / A_V = k / 2.505. */
+double oracle_reddy(double lam) {
+    const double x = 1.0e4 / lam;
+    double k = 0.0;
+    if (lam < 6000.0) {
+        const double xc = x < 1.0e4 / 1500.0 ? x : 1.0e4 / 1500.0;
+        k = -5.726 + xc * (4.004 + xc * (-0.525 + xc * 0.029)) + 2.505;
+    } else if (lam < 28500.0) {
+        k = -2.672 + x * (-0.010 + x * (1.532 + x * -0.412)) + 2.505 - 0.036221981;
+    }
+    return k / 2.505;
+}
+
+/* The diffuse curve of one model at lambda (dust_type 3 and 5, table lookups, are not restated). */
+double oracle_dust_curve(int dust_type, double lam, double dust_index, double mwr, double uvb) {
+    switch (dust_type) {
+    case 0: return pow(lam / V_BAND, dust_index);
+    case 1: return oracle_ccm89(lam, mwr, uvb);
+    case 2: return oracle_calzetti(lam);
+    case 4: return oracle_kc13(lam, dust_index);
+    case 6: return oracle_reddy(lam);
+    default: return NAN;
+    }
+}
+
 
 #define NEB_NZ 11
 #define NEB_NAGE 10
@@ -505,7 +610,7 @@ void oracle_band_fluxes(int ns, int nb, const double *bands, const int *jlo, con
  * ages and metallicities (weights_over_z):
  *   model_sums_zw           :2090-2120   mass, L_bol, weights floored at SAFE_FLOOR, young/old at it_tesc
  *   age_sums_w (CPU order)  :2269-2293   metallicities outer, ages inner
- *   attenuate_batch         :3576-3660 with pixel_transmissions :3765-3818 (power-law curve, dust_type 0)
+ *   attenuate_batch         :3576-3660 with pixel_transmissions :3765-3818 (the curve of dust_type 0, 1, 2, 4, 6)
  *   apply_igm_z             :4205-4299   Madau terms, the short-wavelength cap, exp(-tau igm_factor)
  *   smooth_columns / apply_velocity_kernel (src/spectra/opensps_smoothing.f90)
  *   compute_magnitudes_columns (src/spectra/opensps_batch_photometry.f90:53-180): observed_frame_z :819-903,
@@ -591,7 +696,8 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
     for (int i = 0; i < ns; ++i) {
         double ltab = log(g->lam[i] / V_BAND);
         double curve = 1.0;
-        if (di != 0.0) curve = curve * exp(di * ltab);
+        if (g->dust_type != 0) curve = oracle_dust_curve(g->dust_type, g->lam[i], di, par[P_MWR], par[P_UVB]);
+        else if (di != 0.0) curve = curve * exp(di * ltab);
         double tau_d = d2 * curve, td = exp(-tau_d);
         double tb = 1.0, too = 1.0, tau_b = 0.0, tau_o = 0.0;
         if (!(d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR)) { tau_b = d1 * exp(d1i * ltab); tb = exp(-tau_b); }
@@ -660,7 +766,8 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
         double lagn = (lsum > SAFE_FLOOR ? lsum : 1.0) * par[P_FAGN];
         for (int i = 0; i < ns; ++i) {
             double ltab = log(g->lam[i] / V_BAND);
-            double curve = (di != 0.0) ? exp(di * ltab) : 1.0;
+            double curve = g->dust_type != 0 ? oracle_dust_curve(g->dust_type, g->lam[i], di, par[P_MWR], par[P_UVB])
+                                             : ((di != 0.0) ? exp(di * ltab) : 1.0);
             double tmpl = (1.0 - wta) * g->agn_spec[(size_t)ns * ita + i] + wta * g->agn_spec[(size_t)ns * (ita + 1) + i];
             tot[i] += lagn * tmpl * exp(-d2 * curve);
         }

@@ -16,11 +16,11 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 PAR_NAMES = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
              "igm_factor", "sigma_smooth", "dust_tesc", "duste_qpah", "duste_umin", "duste_gamma", "fagn", "agn_tau",
-             "gas_logz", "gas_logu")
+             "gas_logz", "gas_logu", "mwr", "uvb")
 PAR_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
                 "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
                 "dust_tesc": 7.0, "duste_qpah": 3.5, "duste_umin": 1.0, "duste_gamma": 0.01, "fagn": 0.0,
-                "agn_tau": 10.0, "gas_logz": 0.0, "gas_logu": -2.0}
+                "agn_tau": 10.0, "gas_logz": 0.0, "gas_logu": -2.0, "mwr": 3.1, "uvb": 1.0}
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
@@ -39,7 +39,8 @@ class _Grid(C.Structure):
                 ("smooth", C.c_int), ("min_wave_smooth", C.c_double), ("max_wave_smooth", C.c_double),
                 ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp),
                 ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp), ("ssp_ion", _dp), ("nt_neb", C.c_int),
-                ("whlylim", C.c_int), ("neb_cont", _dp), ("neb_logz", _dp), ("neb_lage", _dp), ("neb_logu", _dp)]
+                ("whlylim", C.c_int), ("neb_cont", _dp), ("neb_logz", _dp), ("neb_lage", _dp), ("neb_logu", _dp),
+                ("dust_type", C.c_int)]
 
 
 class _OpsT(C.Structure):
@@ -57,6 +58,8 @@ def lib() -> C.CDLL:
     if _lib is None:
         build()
         _lib = C.CDLL(str(LIB))
+        _lib.oracle_dust_curve.restype = C.c_double
+        _lib.oracle_dust_curve.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib.oracle_find_interval.restype = C.c_int
         _lib.oracle_find_interval.argtypes = [_dp, C.c_int, C.c_double]
         _lib.oracle_line_basis.argtypes = [C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, C.c_double, _dp, _dp]
@@ -239,13 +242,22 @@ def expi(x: float) -> float:
     return lib().oracle_expi(float(x))
 
 
+def dust_curve(dust_type: int, lam, dust_index: float = -0.7, mwr: float = 3.1, uvb: float = 1.0) -> np.ndarray:
+    """The oracle's attenuation curve A_lambda / A_V (dust_type 0, 1, 2, 4, 6) at the wavelengths lam [A]."""
+    L = lib()
+    lam = np.atleast_1d(np.asarray(lam, dtype=np.float64))
+    return np.array([L.oracle_dust_curve(int(dust_type), float(x), float(dust_index), float(mwr), float(uvb))
+                     for x in lam])
+
+
 class Oracle:
     """The oracle over one synthetic library and filter set, with a context's batch-wide settings."""
 
     def __init__(self, data: dict, nbands: int = 40, add_neb: bool = True, add_igm: bool = True,
                  smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
                  line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73,
-                 dust_emission: dict | None = None, agn: dict | None = None, nebular: dict | None = None):
+                 dust_emission: dict | None = None, agn: dict | None = None, nebular: dict | None = None,
+                 dust_type: int = 0):
         L = lib()
         self.d = data
         self.lam = np.ascontiguousarray(data["lambda"])
@@ -282,6 +294,7 @@ class Oracle:
             g.ssp_ion, g.nt_neb, g.whlylim = _p(ssp), a.value, b.value
             self.nt_neb, self.whlylim = a.value, b.value
         g.add_igm, g.smooth = int(add_igm), int(smooth)
+        g.dust_type = int(dust_type)
         g.min_wave_smooth, g.max_wave_smooth = min_wave_smooth, max_wave_smooth
         g.dustem = None
         if dust_emission is not None:

@@ -1,0 +1,141 @@
+"""The diffuse dust curves other than the power law (dust_type 1 CCM89 with mwr and uvb, 2 Calzetti, 4 Kriek &
+Conroy with dust_index, 6 Reddy: the reference's tabulated curves, attenuation_tables_cached / pixel_transmissions,
+src/physics/opensps_csp_batch.f90:3494-3560,3765-3818) through the C API against the FP64 oracle, which evaluates
+the curve functions themselves (compute_attenuation_curve_point): the mixed batch (nebular lines, birth-cloud,
+diffuse and old-star screens, IGM, smoothing, 40 filters), with dust emission too; the reverse pass's dust rows
+(dust2, dust_index with type 4, mwr and uvb with type 1) against FP64 central differences; the refusals.
+
+Tolerances as the other tests: spectra <= 1e-4 relative (pixels above 1e-6 of the peak), magnitudes <= 1e-3 mag;
+gradients |g - g_fd| <= 2e-3 max(|g_fd|, 1e-3 max_rows |g_fd|).
+"""
+import numpy as np
+import pytest
+
+from conftest import config3_inputs, rel_err_spec
+
+pytestmark = pytest.mark.gpu
+
+CURVE = {1: dict(mwr=3.4, uvb=0.7), 2: {}, 4: dict(dust_index=-0.35), 6: {}}
+
+
+def _inputs(n, seed, dust_type):
+    wz, params = config3_inputs(n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    params = dict(params, dust1=rng.uniform(0.1, 1.0, n), dust3=rng.uniform(0.0, 0.4, n),
+                  frac_nodust=rng.uniform(0.0, 0.2, n), frac_obrun=rng.uniform(0.0, 0.3, n),
+                  dust_index=rng.uniform(-1.0, -0.3, n))
+    for k, v in CURVE[dust_type].items():
+        params[k] = np.full(n, v)
+    return wz, params
+
+
+def _ctx(dust_type, **flags):
+    from libopensps_gb300.capi import Context
+    c = Context()
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    c.set_int("dust_type", dust_type)
+    for k, v in flags.items():
+        c.set_int(k, v)
+    return c
+
+
+@pytest.mark.parametrize("dust_type", [1, 2, 4, 6])
+def test_dust_type_matches_oracle(data, built_lib, dust_type):
+    from oracle.oracle import Oracle
+    n = 60
+    wz, params = _inputs(n, 1400 + dust_type, dust_type)
+    c = _ctx(dust_type)
+    got = c.csp_batch(params, ssp_weights_z=wz)
+    plain = None
+    if dust_type == 2:
+        c.set_int("dust_type", 0)
+        plain = c.csp_batch(params, ssp_weights_z=wz)
+    c.close()
+    want = Oracle(data, nbands=40, dust_type=dust_type).csp_batch(params, wz)
+    assert rel_err_spec(got["spec"], want["spec"]) <= 1e-4
+    assert np.array_equal(np.isnan(got["mags"]), np.isnan(want["mags"]))
+    assert float(np.nanmax(np.abs(got["mags"] - want["mags"]))) <= 1e-3
+    if plain is not None:
+        # the curve is in effect: Calzetti and the power law differ
+        assert float(np.nanmax(np.abs(got["mags"] - plain["mags"]))) > 0.05
+
+
+def test_dust_type_with_dust_emission(data, built_lib):
+    """The absorbed light of the energy balance goes through the same curve (Calzetti)."""
+    from libopensps_gb300 import synth_dust
+    from oracle.oracle import Oracle
+    n = 24
+    wz, params = _inputs(n, 1450, 2)
+    rng = np.random.default_rng(1451)
+    params = dict(params, duste_qpah=rng.uniform(0.5, 4.5, n), duste_umin=rng.uniform(0.1, 20.0, n),
+                  duste_gamma=rng.uniform(0.0, 0.5, n))
+    c = _ctx(2, add_dust_emission=1)
+    got = c.csp_batch(params, ssp_weights_z=wz)
+    c.close()
+    want = Oracle(data, nbands=40, dust_type=2, dust_emission=synth_dust.load()).csp_batch(params, wz)
+    assert rel_err_spec(got["spec"], want["spec"]) <= 1e-4
+    assert float(np.nanmax(np.abs(got["mags"] - want["mags"]))) <= 1e-3
+
+
+def _loss(out, mb, sb):
+    return np.nansum(mb * out["mags"], axis=1) + np.sum(sb * out["spec"], axis=1)
+
+
+@pytest.mark.parametrize("dust_type,rows", [(1, {"dust2": 2, "dust3": 3, "mwr": 8, "uvb": 9}),
+                                            (2, {"dust2": 2, "dust3": 3}),
+                                            (4, {"dust2": 2, "dust3": 3, "dust_index": 4})])
+def test_dust_type_gradients(data, built_lib, dust_type, rows):
+    """Rows against FP64 central differences of the oracle (h = 1e-4 relative): each model's own parameter moved
+    (the batch itself keeps mwr, uvb and dust_index the same for every model). Without IGM and smoothing, at z = 0:
+    the curve's rows alone."""
+    from libopensps_gb300.workloads import adjoint_cotangents
+    from oracle.oracle import Oracle
+    n = 6
+    wz, params = _inputs(n, 1460 + dust_type, dust_type)
+    params = dict(params, zred=np.zeros(n), sigma_smooth=np.zeros(n))
+    mb, sb = adjoint_cotangents(n, data["lambda"].size, 40, seed=1470 + dust_type)
+    c = _ctx(dust_type)
+    got = c.csp_batch_grad(params, wz, mags_bar=mb, spec_bar=sb)
+    c.close()
+    o = Oracle(data, nbands=40, dust_type=dust_type)
+    names = list(rows)
+    g = np.stack([got["params_bar"][:, rows[k]] for k in names], axis=1)
+    fd = np.empty_like(g)
+    for i, k in enumerate(names):
+        h = 1e-4 * np.abs(params[k])
+        up = o.csp_batch(dict(params, **{k: params[k] + h}), wz)
+        dn = o.csp_batch(dict(params, **{k: params[k] - h}), wz)
+        fd[:, i] = (_loss(up, mb, sb) - _loss(dn, mb, sb)) / (2.0 * h)
+    scale = np.max(np.abs(fd), axis=1, keepdims=True)
+    err = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
+    assert float(err.max()) <= 2e-3, {names[i]: float(err[:, i].max()) for i in range(len(names))}
+    if dust_type != 4:
+        assert np.all(got["params_bar"][:, 4] == 0.0)     # dust_index does not act
+    if dust_type != 1:
+        assert np.all(got["params_bar"][:, 8:10] == 0.0)  # nor mwr and uvb
+
+
+def test_dust_type_refusals(data, built_lib):
+    from libopensps_gb300.capi import OpenSPSError
+    n = 8
+    wz, params = _inputs(n, 1480, 1)
+    c = _ctx(1)
+    with pytest.raises(OpenSPSError) as e:
+        c.csp_batch(dict(params, mwr=np.linspace(2.5, 4.0, n)), ssp_weights_z=wz)
+    assert e.value.status == 2 and "mwr" in e.value.message
+    c.set_int("dust_type", 4)
+    with pytest.raises(OpenSPSError) as e:
+        c.csp_batch(dict(params, dust_index=np.linspace(-1.0, -0.2, n)), ssp_weights_z=wz)
+    assert e.value.status == 2 and "dust_index" in e.value.message
+    for dt in (3, 5):
+        c.set_int("dust_type", dt)
+        with pytest.raises(OpenSPSError) as e:
+            c.csp_batch(params, ssp_weights_z=wz)
+        assert e.value.status == 2
+    c.set_int("dust_type", 2)
+    c.set_int("gb300_fp64", 1)
+    with pytest.raises(OpenSPSError) as e:
+        c.csp_batch(params, ssp_weights_z=wz)
+    assert e.value.status == 2
+    c.close()
