@@ -13,8 +13,8 @@ extern "C" {
 
 /* Number of doubles per model in the device parameter table of opensps_gb300_batch_device, and their order:
  * dust1, dust2, dust3, dust_index, dust1_index, frac_nodust, frac_obrun, zred, igm_factor, sigma_smooth,
- * dust_tesc. */
-#define OPENSPS_GB300_DEVICE_PARAMS 11
+ * dust_tesc, mwr, uvb. */
+#define OPENSPS_GB300_DEVICE_PARAMS 13
 
 /* A batch of n models whose inputs are already in device memory: d_params (OPENSPS_GB300_DEVICE_PARAMS x n
  * doubles, column-major) and d_wz (ntfull x nz x n doubles, the ssp_weights_z of the C API). The context's

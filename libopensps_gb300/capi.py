@@ -22,7 +22,7 @@ _lib = None
 
 NBGRAD = 44
 DEVICE_PARAMS = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
-                 "igm_factor", "sigma_smooth", "dust_tesc")
+                 "igm_factor", "sigma_smooth", "dust_tesc", "mwr", "uvb")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

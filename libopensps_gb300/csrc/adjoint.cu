@@ -184,6 +184,7 @@ struct PixFwd {
 
 struct ModelConst {
     float kd2, one_m_fnd, fnd, dust_index, kd1, dust1_index, one_m_fo, fo, kd3;
+    float cs1, cs2, cs3;   // the tabulated curve's scalars (dust_index: its power)
     float b[6], db[6];
     int jmax;
     bool igm_model;
@@ -193,10 +194,15 @@ __device__ __forceinline__ PixFwd pix_forward(const AdjointArgs &a, const ModelC
     PixFwd f;
     const float ltab2 = fmaf((float)p, a.lt_step, a.lt_base);   // ln(lambda / 5500) log2(e) on the log-uniform grid
     f.ltab = ltab2 * 0.6931471805599453f;                        // ln(lambda / 5500)
-    if (a.ctab) {
-        // the batch's tabulated curve (dust_type 1, 2, 4, 6) with its derivatives
-        const float4 ct = __ldg(a.ctab + p);
-        f.curve = ct.x; f.dci = ct.y; f.dcm = ct.z; f.dcu = ct.w;
+    if (a.dust_type != 0) {
+        // the tabulated curve (T0 + s1 T1 + s2 T2 + s3 T3) (lambda / 5500)^ed and its derivatives: in dust_index
+        // (Kriek & Conroy: s1 = ed = dust_index), in mwr and uvb (CCM89: s = (1 / mwr, uvb, uvb / mwr))
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS + PIX_T));
+        const float pl = mc.dust_index != 0.f ? adj_ex2(mc.dust_index * ltab2) : 1.f;
+        f.curve = fmaf(mc.cs1, t.y, fmaf(mc.cs2, t.z, fmaf(mc.cs3, t.w, t.x))) * pl;
+        f.dci = a.dust_type == 4 ? fmaf(t.y, pl, f.curve * f.ltab) : 0.f;
+        f.dcm = a.dust_type == 1 ? -(t.y + mc.cs2 * t.w) * mc.cs1 * mc.cs1 : 0.f;
+        f.dcu = a.dust_type == 1 ? fmaf(mc.cs1, t.w, t.z) : 0.f;
     } else {
         f.curve = adj_ex2(mc.dust_index * ltab2);
         f.dci = f.curve * f.ltab; f.dcm = 0.f; f.dcu = 0.f;
@@ -348,6 +354,7 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
         mc.kd2 = d0.x; mc.one_m_fnd = d0.y; mc.fnd = d0.z; mc.dust_index = d0.w;
         mc.kd1 = d1v.x; mc.dust1_index = d1v.y; mc.one_m_fo = d1v.z; mc.fo = d1v.w;
         mc.igm_model = d2v.x != 0.f; mc.jmax = __float_as_int(d2v.y); mc.kd3 = d2v.w;
+        mc.cs1 = __ldg(mp + MP_CS1); mc.cs2 = __ldg(mp + MP_CS1 + 1); mc.cs3 = __ldg(mp + MP_CS1 + 2);
 #pragma unroll
         for (int k = 0; k < 6; ++k) { mc.b[k] = __ldg(ap + AP_B + k); mc.db[k] = __ldg(ap + AP_DB + k); }
     }
@@ -973,7 +980,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     a.zinfo = c.d_zinfo.p; a.fband = c.d_fband.p;
     a.mags_bar = mags_bar ? c.d_mags_bar.p : nullptr;
     a.spec_bar = spec_bar ? c.d_spec_bar.p : nullptr;
-    a.ctab = c.geom.ctab;
+    a.dust_type = c.dust_type;
     a.do_band = c.mag_mask.empty() ? nullptr : c.d_do_band.p;
     a.pix = c.d_pix.p; a.wl = c.d_wl.p; a.bc = c.d_bc.p; a.bmeta = c.d_bmeta.p; a.bchunk = c.d_bchunk.p;
     a.lt_base = (float)(std::log(c.lam[0] / 5500.0) * 1.4426950408889634);

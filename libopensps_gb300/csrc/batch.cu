@@ -15,6 +15,7 @@ namespace sps {
 struct ModelParamArgs {
     int n, nspec, jtop, add_igm, smooth, i0;   // i0: the pixel whose smoothing row gives the model's taps
     int mpw = 32;            // models per warp (1 .. 32)
+    int dust_type = 0;       // the diffuse curve's scalars (MP_DUST_INDEX: its power, MP_CS1..: the tables' weights)
     const double *par;       // PAR_DEVICE x n
     const float *igm_a;      // jtop x 6
     const double *lam;       // nspec
@@ -106,7 +107,17 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     blk[MP_KD2] = (float)(-d2 * LOG2E);
     if (1.0 - fnd <= SAFE_FLOOR) { blk[MP_ONE_M_FND] = 0.f; blk[MP_FND] = 1.f; }
     else { blk[MP_ONE_M_FND] = (float)(1.0 - fnd); blk[MP_FND] = (float)fnd; }
-    blk[MP_DUST_INDEX] = (float)p[PF_DUST_INDEX];
+    // the diffuse curve (T0 + s1 T1 + s2 T2 + s3 T3) (lambda / 5500)^ed (pixel_transmissions :3765-3818): power law
+    // (0) ed = dust_index; CCM89 (1) s = (1 / mwr, uvb, uvb / mwr); Kriek & Conroy (4) s1 = ed = dust_index
+    {
+        const double di = p[PF_DUST_INDEX];
+        float ed = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        if (a.dust_type == 0) ed = (float)di;
+        else if (a.dust_type == 4) { ed = (float)di; s1 = (float)di; }
+        else if (a.dust_type == 1) { const double ir = 1.0 / p[PF_MWR], u = p[PF_UVB]; s1 = (float)ir; s2 = (float)u; s3 = (float)(u * ir); }
+        blk[MP_DUST_INDEX] = ed;
+        blk[MP_CS1] = s1; blk[MP_CS1 + 1] = s2; blk[MP_CS1 + 2] = s3;
+    }
     blk[MP_KD1] = (d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR) ? 0.f : (float)(-d1 * LOG2E);
     blk[MP_DUST1_INDEX] = (float)p[PF_DUST1_INDEX];
     blk[MP_ONE_M_FO] = (float)(1.0 - fo);
@@ -706,22 +717,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
 
     // ---- per-pixel table (rebuilt when the batch's shared curve changes): ln(lambda / 5500) log2(e), the diffuse
     // curve shared by the batch's models in FP64 (the reference's tables, attenuation_tables_cached :3494-3560, times
-    // exp_kp of the power law: the argument formed in FP64), the Madau wavelength factors. dust_type 0 with a
-    // dust_index per model forms its curve in the kernels instead; the other types need the curve's parameters (mwr
-    // and uvb for 1, dust_index for 4) the same for every model of a batch on this path.
-    const double idx0 = par(0, PF_DUST_INDEX);
-    bool uniform_index = true;
+    // exp_kp of the power law: the argument formed in FP64), the Madau wavelength factors, the curve tables T0..T3
+    // (FP32: the kernels form a model's own curve from them when the models' curves differ)
     double sc0[4];
-    dust_scalars(c.dust_type, idx0, par(0, PF_MWR), par(0, PF_UVB), sc0);
+    dust_scalars(c.dust_type, par(0, PF_DUST_INDEX), par(0, PF_MWR), par(0, PF_UVB), sc0);
+    bool uniform_index = true;
     for (int m = 1; m < n && uniform_index; ++m) {
         double sc[4];
         dust_scalars(c.dust_type, par(m, PF_DUST_INDEX), par(m, PF_MWR), par(m, PF_UVB), sc);
         uniform_index = sc[0] == sc0[0] && sc[1] == sc0[1] && sc[2] == sc0[2] && sc[3] == sc0[3];
-    }
-    if (!uniform_index && c.dust_type != 0) {
-        err = "dust_type " + std::to_string(c.dust_type) + ": " + (c.dust_type == 1 ? "mwr and uvb" : "dust_index") +
-              " must be the same for every model of a batch on this path";
-        return ST_UNSUPPORTED;
     }
     if (c.dust_type != 0 && fp64) {
         err = "dust_type " + std::to_string(c.dust_type) + " is not supported on the plain FP64 path";
@@ -730,35 +734,28 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     const double key[5] = {(double)c.dust_type, sc0[0], sc0[1], sc0[2], sc0[3]};
     bool same_key = true;
     for (int k = 0; k < 5; ++k) same_key = same_key && c.pix_key[k] == key[k];
-    if (!c.d_pix.p || (uniform_index && !same_key)) {
+    if (!c.d_pix.p || c.pix_key[0] != key[0] || (uniform_index && !same_key)) {
         std::vector<double> tab;
         dust_tables(c.dust_type, c.lam, tab);
         std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
-        std::vector<float4> ctab(c.dust_type != 0 ? (size_t)ns : 0);
         for (int j = 0; j < ns; ++j) {
             float *px = pix.data() + (size_t)j * PIX_FLOATS;
             const double ltab = std::log(c.lam[j] / 5500.0);
-            double curve, dci, dcm, dcu;
-            dust_curve_row(tab.data() + 4 * (size_t)j, sc0, ltab, curve, dci, dcm, dcu, c.dust_type, par(0, PF_MWR),
-                           par(0, PF_UVB));
             px[PIX_LTAB2] = (float)(ltab * 1.4426950408889634);
-            px[PIX_CURVE] = (float)curve;
-            if (c.dust_type != 0) ctab[j] = make_float4((float)curve, (float)dci, (float)dcm, (float)dcu);
+            px[PIX_CURVE] = (float)dust_curve_value(tab.data() + 4 * (size_t)j, sc0, ltab);
             if (j < c.jtop)
                 for (int k = 0; k < 6; ++k) px[PIX_IGM_A + k] = c.igm_a[(size_t)j * 6 + k];
+            for (int k = 0; k < 4; ++k) px[PIX_T + k] = (float)tab[4 * (size_t)j + k];
         }
         cudaError_t e;
         if ((e = c.d_pix.reserve(pix.size())) != cudaSuccess ||
-            (e = cudaMemcpy(c.d_pix.p, pix.data(), sizeof(float) * pix.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-            (!ctab.empty() && ((e = c.d_ctab.reserve(ctab.size())) != cudaSuccess ||
-                               (e = cudaMemcpy(c.d_ctab.p, ctab.data(), sizeof(float4) * ctab.size(),
-                                               cudaMemcpyHostToDevice)) != cudaSuccess))) {
+            (e = cudaMemcpy(c.d_pix.p, pix.data(), sizeof(float) * pix.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
             err = cuda_msg("pixel table", e);
             return ST_DATA_MISSING;
         }
         for (int k = 0; k < 5; ++k) c.pix_key[k] = key[k];
     }
-    c.geom.ctab = c.dust_type != 0 ? c.d_ctab.p : nullptr;
+    const int tab_curve = c.dust_type != 0 ? 1 : 0;   // (models' own curves from the tables, else the power law)
     // the smoothed pixels: lambda within [min_wave_smooth, max_wave_smooth]
     int sm_lo = ns, sm_hi = -1;
     for (int j = 0; j < ns; ++j)
@@ -769,6 +766,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.geom.sm_lo = any_smooth ? sm_lo : ns;
     c.geom.sm_hi = any_smooth ? sm_hi : -1;
     c.geom.uniform_index = uniform_index ? 1 : 0;
+    c.geom.tab_curve = tab_curve;
     c.geom.itesc = itesc;
     c.geom.wz = nullptr;
     c.geom.n = 0;
@@ -896,7 +894,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     auto model_params = [&](int off, int nk) -> cudaError_t {
         ModelParamArgs ma;
         ma.n = nk; ma.nspec = ns; ma.jtop = c.jtop; ma.add_igm = c.add_igm_absorption == 1; ma.smooth = any_smooth ? 1 : 0;
-        ma.i0 = i0; ma.par = d_par + (size_t)PAR_DEVICE * off; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p;
+        ma.i0 = i0; ma.dust_type = c.dust_type; ma.par = d_par + (size_t)PAR_DEVICE * off; ma.igm_a = c.d_igm_a.p; ma.lam = c.d_lam.p;
         ma.zt = c.d_zt.p; ma.dl = c.d_dl.p; ma.dlnl = c.dlnl; ma.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
         ma.zinfo = c.d_zinfo.p + off; ma.dist = c.d_dist.p + off; ma.lnlam = c.d_lnlam.p;
         int mpw = 32;
@@ -942,7 +940,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     auto epilogue = [&](const float *y, const float *o, int off, int nk) -> cudaError_t {
         PartsEpilogueArgs pe;
         pe.n = nk; pe.nspec = ns; pe.jtop = c.jtop; pe.sm_lo = any_smooth ? sm_lo : ns; pe.sm_hi = any_smooth ? sm_hi : -1;
-        pe.uniform_index = uniform_index ? 1 : 0; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
+        pe.uniform_index = uniform_index ? 1 : 0; pe.tab_curve = tab_curve; pe.pix = c.d_pix.p; pe.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
         pe.young = y + (size_t)ns * off; pe.old = o + (size_t)ns * off;
         pe.spec = c.d_spec.p + (size_t)ns * off;
         pe.dem = d_dem ? d_dem + off : nullptr;
@@ -1026,7 +1024,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             ca.jtop = c.jtop; ca.ld_spec = ns; ca.pix = c.d_pix.p; ca.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
             // (with dust emission or AGN the per-model epilogue forms the spectra from the young and old sums)
             ca.spec = epi ? nullptr : c.d_spec.p + (size_t)ns * off;
-            ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0;
+            ca.sm_lo = any_smooth ? sm_lo : ns; ca.sm_hi = any_smooth ? sm_hi : -1; ca.uniform_index = uniform_index ? 1 : 0; ca.tab_curve = tab_curve;
             ca.young = ca.old = nullptr;
             if (parts) {
                 ca.young = d_y + (size_t)ns * off;

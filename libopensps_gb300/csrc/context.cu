@@ -169,7 +169,7 @@ Context::~Context() {
         kv.second->release();
         delete kv.second;
     }
-    d_ion.release(); d_pix.release(); d_ctab.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
+    d_ion.release(); d_pix.release(); d_wl.release(); d_igm_a.release(); d_do_band.release(); d_cb_hi.release(); d_cb_lo.release();
     d_lam.release(); d_lnlam.release(); d_mass.release(); d_llin.release(); d_zt.release(); d_dl.release();
     d_wz.release(); d_params.release(); d_sums.release(); d_zinfo.release(); d_dist.release(); d_fband.release();
     d_mags.release(); d_spec64.release(); d_whi.release(); d_wlo.release(); d_mpar.release(); d_spec.release();

@@ -21,11 +21,11 @@ constexpr double C_LIGHT = 2.99792458e18;                 // A / s
 // (the first PAR_DEVICE of them), with the defaults of OpenSPS's PARAMS_CORE (src/core/opensps_types.f90:32-45).
 enum ParamId {
     PF_DUST1 = 0, PF_DUST2, PF_DUST3, PF_DUST_INDEX, PF_DUST1_INDEX, PF_FRAC_NODUST, PF_FRAC_OBRUN, PF_ZRED,
-    PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC,
-    PAR_DEVICE,                  // = 11: the per-model table of the device kernels stops here
+    PF_IGM_FACTOR, PF_SIGMA_SMOOTH, PF_DUST_TESC, PF_MWR, PF_UVB,
+    PAR_DEVICE,                  // = 13: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
     PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
-    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU, PF_MWR, PF_UVB,
+    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU,
     PF_COUNT
 };
 
@@ -174,10 +174,10 @@ struct NebularGrid {
 struct BatchGeom {
     BasisOperand *bop = nullptr;
     int nacc = 0, sm_lo = 0, sm_hi = -1, uniform_index = 0, n = 0;
+    int tab_curve = 0;           // the models' diffuse curves from the pixel table's T0..T3 (dust_type other than 0)
     int itesc = 0;               // the first old age
     const double *wz = nullptr;  // the weights over ages and metallicities on the device (with the operators)
     bool emis = false, agn = false;   // the batch had dust emission / the AGN torus (cells in d_dem, chains in d_dchain)
-    const float4 *ctab = nullptr;     // the batch's tabulated curve (dust_type 1, 2, 4, 6), or null: the power law
 };
 
 struct Context {
@@ -234,7 +234,6 @@ struct Context {
     DevBuf<double> d_lam, d_lnlam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
     double pix_key[5] = {-1e300, 0.0, 0.0, 0.0, 0.0};   // the device pixel table's curve: dust_type, its 4 scalars
-    DevBuf<float4> d_ctab;       // with dust_type 1, 2, 4, 6: per pixel the curve and its d / d(dust_index, mwr, uvb)
 
     // batch scratch
     DevBuf<double> d_wz, d_params, d_sums, d_dist, d_fband, d_mags, d_spec64;
@@ -357,12 +356,11 @@ int ops_build(Context &c, std::string &err);
 int dustem_load(Context &c, std::string &err);
 int agn_load(Context &c, std::string &err);
 // the diffuse dust curves (dust_curves.cu): per pixel the tables T0..T3 (4 x nspec, pixel-major) of dust_type, per
-// model its scalars (s1, s2, s3, ed); a pixel's curve and its derivatives in dust_index, mwr and uvb
+// model its scalars (s1, s2, s3, ed); a pixel's curve (T0 + s1 T1 + s2 T2 + s3 T3) exp(ed ltab)
 bool dust_type_supported(int dust_type);
 void dust_tables(int dust_type, const std::vector<double> &lam, std::vector<double> &tab);
 void dust_scalars(int dust_type, double dust_index, double mwr, double uvb, double s[4]);
-void dust_curve_row(const double *t, const double s[4], double ltab, double &curve, double &dc_idx, double &dc_mwr,
-                    double &dc_uvb, int dust_type, double mwr, double uvb);
+double dust_curve_value(const double *t, const double s[4], double ltab);
 // the nebular ages as the continuum kernel's runs for this itesc (context.cu; rebuilt when itesc changes)
 int nebular_runs(Context &c, int itesc, std::string &err);
 // The plain FP64 path (fp64_path.cu): the age sums by DGEMM and the rest in FP64, into the host outputs of io.

@@ -217,11 +217,13 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
             const bool inpix = (p >= 0 && p < args.nspec);
             // per-pixel data of this thread's row (phase 1)
             float ltab2 = 0.f, curve_u = 1.f, ia[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float4 tcv = make_float4(0.f, 0.f, 0.f, 0.f);   // the curve tables T0..T3 (models' own tabulated curves)
             if (inpix) {
                 const float4 *px = reinterpret_cast<const float4 *>(args.pix + (size_t)p * PIX_FLOATS);
                 const float4 v0 = px[0], v1 = px[1];
                 ltab2 = v0.x; curve_u = v0.y; ia[0] = v0.z; ia[1] = v0.w;
                 ia[2] = v1.x; ia[3] = v1.y; ia[4] = v1.z; ia[5] = v1.w;
+                if (args.tab_curve) tcv = px[PIX_T / 4];
             }
             const bool igm_pix = inpix && p < args.jtop;
 
@@ -269,7 +271,8 @@ csp_contract_kernel(const __grid_constant__ CUtensorMap tm_a_hi, const __grid_co
                 for (int j = 0; j < 16; ++j) {
                     const float *mp = par + j * MODEL_PAR_FLOATS;
                     const float4 d0 = *reinterpret_cast<const float4 *>(mp);          // kd2, 1-fnd, fnd, index
-                    const float curve = args.uniform_index ? curve_u : ex2(d0.w * ltab2);
+                    const float curve = pix_curve(args.uniform_index, args.tab_curve, curve_u, ltab2, tcv,
+                                                  make_float4(mp[MP_CS1], mp[MP_CS1 + 1], mp[MP_CS1 + 2], 0.f), d0.w);
                     float ss;
                     if constexpr (NACC == 2) {
                         if (args.young && inpix && r >= HALO && r < BM - HALO && m0 + col0 + j < args.n_models) {

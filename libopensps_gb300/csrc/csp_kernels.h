@@ -33,9 +33,21 @@ enum {
     ERR_TIMEOUT_ADJOINT = 0x105,
 };
 
-// Per-pixel table (floats per pixel): ln(lambda / 5500 A) log2(e), the diffuse curve (lambda / 5500)^dust_index of
-// the batch's shared dust_index (used when uniform_index), the six Madau wavelength factors a_k.
-enum { PIX_LTAB2 = 0, PIX_CURVE = 1, PIX_IGM_A = 2, PIX_FLOATS = 8 };
+// Per-pixel table (floats per pixel): ln(lambda / 5500 A) log2(e), the batch's shared diffuse curve (used when
+// uniform_index), the six Madau wavelength factors a_k, the curve tables T0..T3 (a model's curve is
+// (T0 + s1 T1 + s2 T2 + s3 T3) exp2(ed ln(lambda / 5500) log2 e) with its scalars MP_CS1.. and MP_DUST_INDEX).
+enum { PIX_LTAB2 = 0, PIX_CURVE = 1, PIX_IGM_A = 2, PIX_T = 8, PIX_FLOATS = 12 };
+
+// A model's diffuse curve at a pixel: the batch's shared one (uniform), its tabulated form (tab: the pixel's
+// T0..T3 with the model's s1..s3 = cs and power ed), or the power law exp2(ed ltab2). ex2: the SFU's 2^x.
+__device__ __forceinline__ float pix_curve(bool uniform, bool tab, float curve_u, float ltab2, float4 t, float4 cs,
+                                           float ed) {
+    if (uniform) return curve_u;
+    float pl;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(pl) : "f"(ed * ltab2));
+    if (!tab) return pl;
+    return fmaf(cs.x, t.y, fmaf(cs.y, t.z, fmaf(cs.z, t.w, t.x))) * (ed != 0.f ? pl : 1.f);
+}
 
 // Per-model parameter block (floats), written by the model-parameter prologue; exponents are pre-scaled by
 // log2(e) so that every transmission is one exp2. Groups of four start on 16-byte boundaries (vector loads).
@@ -43,7 +55,7 @@ enum {
     MP_KD2 = 0,          // -dust2 log2(e):            T_diffuse = exp2(MP_KD2 curve)
     MP_ONE_M_FND = 1,    // 1 - frac_nodust (0 when frac_nodust = 1)
     MP_FND = 2,          // frac_nodust (1 when frac_nodust = 1)
-    MP_DUST_INDEX = 3,   // dust_index (curve = exp2(dust_index ln(lambda/5500) log2 e) when not uniform)
+    MP_DUST_INDEX = 3,   // the curve's power ed (dust_index with dust_type 0 and 4, else 0)
     MP_KD1 = 4,          // -dust1 log2(e) (0: no birth-cloud screen)
     MP_DUST1_INDEX = 5,
     MP_ONE_M_FO = 6,     // 1 - frac_obrun
@@ -55,6 +67,7 @@ enum {
     MP_IGM_KB = 12,      // 6 redshift factors b_k(1 + z) times -igm_factor log2(e) (12..17)
     MP_SMOOTH_R = 18,    // smoothing half-width in pixels (int bits), -1: none
     MP_TAPS = 20,        // 9 normalised taps, offsets -4 .. 4 (zero beyond R)
+    MP_CS1 = 29,         // the curve's scalars s1, s2, s3 (29..31; the tables' weights)
     MODEL_PAR_FLOATS = 32
 };
 
@@ -71,7 +84,8 @@ struct ContractArgs {
     // ion_pix (the ionizing pixels; the basis holds those columns' unabsorbed spectra there and zeros above)
     int nkb_ion_young = 0, nkb_ion_old = 0, ion_pix = 0;
     int sm_lo, sm_hi;    // pixels smoothed (lambda within [min_wave_smooth, max_wave_smooth]); sm_lo > sm_hi: none
-    int uniform_index;   // every model has the dust_index of the pixel table's curve
+    int uniform_index;   // every model has the pixel table's curve
+    int tab_curve = 0;   // not uniform: each model's curve from the pixel table's T0..T3 (else its power law)
     const float *pix;    // nspec x PIX_FLOATS
     const float *mpar;   // n_models x MODEL_PAR_FLOATS
     float *spec;         // n_models x ld_spec (pixel fastest); null: not written (NACC = 2 with the parts)
@@ -195,6 +209,7 @@ struct DustEmModel {
 };
 struct AdjointArgs {
     int n_models, nspec, ppad, nbands, jtop, j0, j1, sm_lo, sm_hi, uniform_index;
+    int dust_type = 0;               // the diffuse curve (0: the power law; else from the pixel table's T0..T3)
     float dl2, inv_em1;              // dlnl log2(e), 1 / (e^dlnl - 1)
     const float *young, *old;        // n_models x nspec (+ 4 floats of padding): the forward's age sums before dust
     const float *mpar;               // n_models x MODEL_PAR_FLOATS
@@ -227,9 +242,6 @@ struct AdjointArgs {
     int lsum_stride = 6;
     const float4 *dchain = nullptr;
     double *lsum_bar = nullptr;
-    // the batch's tabulated diffuse curve (dust_type 1, 2, 4, 6; null: the power law of each model's dust_index): per
-    // pixel the curve and its derivatives in dust_index, mwr and uvb
-    const float4 *ctab = nullptr;
 };
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 
@@ -337,6 +349,7 @@ cudaError_t run_transpose_bf16(const __nv_bfloat16 *src, __nv_bfloat16 *dst, int
 
 struct PartsEpilogueArgs {
     int n, nspec, jtop, sm_lo, sm_hi, uniform_index;
+    int tab_curve = 0;            // not uniform: each model's curve from the pixel table's T0..T3 (else its power law)
     const float *pix, *mpar;
     const float *young, *old;     // n x nspec
     float *spec;                  // n x nspec

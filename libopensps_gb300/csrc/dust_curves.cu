@@ -143,21 +143,9 @@ void dust_scalars(int dust_type, double dust_index, double mwr, double uvb, doub
     }
 }
 
-void dust_curve_row(const double *t, const double s[4], double ltab, double &curve, double &dc_idx, double &dc_mwr,
-                    double &dc_uvb, int dust_type, double mwr, double uvb) {
+double dust_curve_value(const double *t, const double s[4], double ltab) {
     const double base = t[0] + s[0] * t[1] + s[1] * t[2] + s[2] * t[3];
-    const double pl = s[3] != 0.0 ? std::exp(s[3] * ltab) : 1.0;
-    curve = base * pl;
-    dc_idx = dc_mwr = dc_uvb = 0.0;
-    if (dust_type == 0) {
-        dc_idx = curve * ltab;
-    } else if (dust_type == 4) {
-        dc_idx = t[1] * pl + curve * ltab;
-    } else if (dust_type == 1) {
-        const double s1 = 1.0 / mwr;
-        dc_uvb = t[2] + s1 * t[3];
-        dc_mwr = -(t[1] + uvb * t[3]) * s1 * s1;
-    }
+    return s[3] != 0.0 ? base * std::exp(s[3] * ltab) : base;
 }
 
 }  // namespace sps

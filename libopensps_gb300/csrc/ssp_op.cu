@@ -1014,6 +1014,9 @@ __device__ __forceinline__ float2 dl07_shape2(const float *tab, int ns, int nq, 
 // it uses them.
 constexpr int EPI_U = 4;
 
+// TAB: the models' curves differ and are tabulated (dust_type other than 0): each from the pixel's T0..T3 and the
+// model's scalars (a separate instantiation keeps the others' registers as they were)
+template <bool TAB>
 __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArgs a) {
     extern __shared__ float tsm[];         // nspec: the spectrum; with dust emission a second nspec: its emission
     float *esm = tsm + a.nspec;
@@ -1046,7 +1049,13 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
     // (esc) and the sums
     auto pass1 = [&](int p, float y, float o, float shape, float cn, float t0, float t1, float &esc) -> float {
         const float2 v0 = pix0(p);
-        const float curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
+        float curve;
+        if constexpr (TAB) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(a.pix + (size_t)p * PIX_FLOATS + PIX_T));
+            curve = pix_curve(false, true, 0.f, v0.x, t, make_float4(mp[MP_CS1], mp[MP_CS1 + 1], mp[MP_CS1 + 2], 0.f), di);
+        } else {
+            curve = a.uniform_index ? v0.y : ops_ex2(di * v0.x);
+        }
         const float lb = (kd1 != 0.f) ? kd1 * ops_ex2(d1i * v0.x) : 0.f;   // log2 of the transmissions
         const float lo2 = kd3 * curve, ld2 = kd2 * curve;
         const float tb = (kd1 != 0.f) ? ops_ex2(lb) : 1.f;
@@ -1390,9 +1399,12 @@ cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_
 cudaError_t run_parts_epilogue(const PartsEpilogueArgs &a, cudaStream_t st) {
     if (a.n <= 0) return cudaSuccess;
     const size_t smem = sizeof(float) * (size_t)a.nspec * (a.dem ? 2 : 1);
-    cudaError_t e = cudaFuncSetAttribute(parts_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool tab = !a.uniform_index && a.tab_curve;
+    cudaError_t e = tab ? cudaFuncSetAttribute(parts_epilogue_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(parts_epilogue_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    parts_epilogue_kernel<<<a.n, 256, smem, st>>>(a);
+    if (tab) parts_epilogue_kernel<true><<<a.n, 256, smem, st>>>(a);
+    else parts_epilogue_kernel<false><<<a.n, 256, smem, st>>>(a);
     return cudaGetLastError();
 }
 

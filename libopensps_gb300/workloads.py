@@ -35,14 +35,14 @@ def mixed_csp(n: int, seed: int = 0, nt: int = NT, nz: int = NZ, out: np.ndarray
 
 
 DEVICE_PARAM_ORDER = ("dust1", "dust2", "dust3", "dust_index", "dust1_index", "frac_nodust", "frac_obrun", "zred",
-                      "igm_factor", "sigma_smooth", "dust_tesc")
+                      "igm_factor", "sigma_smooth", "dust_tesc", "mwr", "uvb")
 DEVICE_PARAM_DEFAULTS = {"dust1": 0.0, "dust2": 0.0, "dust3": 0.0, "dust_index": -0.7, "dust1_index": -1.0,
                          "frac_nodust": 0.0, "frac_obrun": 0.0, "zred": 0.0, "igm_factor": 1.0, "sigma_smooth": 0.0,
-                         "dust_tesc": 7.0}
+                         "dust_tesc": 7.0, "mwr": 3.1, "uvb": 1.0}
 
 
 def device_param_table(params: dict, n: int) -> np.ndarray:
-    """The (n, 11) float64 per-model table of opensps_gb300_batch_device (column-major 11 x n)."""
+    """The (n, 13) float64 per-model table of opensps_gb300_batch_device (column-major 13 x n)."""
     out = np.empty((n, len(DEVICE_PARAM_ORDER)))
     for i, k in enumerate(DEVICE_PARAM_ORDER):
         out[:, i] = np.broadcast_to(np.asarray(params.get(k, DEVICE_PARAM_DEFAULTS[k]), dtype=np.float64), (n,))

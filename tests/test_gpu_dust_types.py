@@ -2,8 +2,10 @@
 Conroy with dust_index, 6 Reddy: the reference's tabulated curves, attenuation_tables_cached / pixel_transmissions,
 src/physics/opensps_csp_batch.f90:3494-3560,3765-3818) through the C API against the FP64 oracle, which evaluates
 the curve functions themselves (compute_attenuation_curve_point): the mixed batch (nebular lines, birth-cloud,
-diffuse and old-star screens, IGM, smoothing, 40 filters), with dust emission too; the reverse pass's dust rows
-(dust2, dust_index with type 4, mwr and uvb with type 1) against FP64 central differences; the refusals.
+diffuse and old-star screens, IGM, smoothing, 40 filters) with the curve's parameters shared by the batch (the
+pixel table's FP64 curve) and per model (each model's curve from the FP32 tables), with dust emission too; the
+reverse pass's dust rows (dust2, dust3, dust_index with type 4, mwr and uvb with type 1) against FP64 central
+differences, shared and per model; the refusals.
 
 Tolerances as the other tests: spectra <= 1e-4 relative (pixels above 1e-6 of the peak), magnitudes <= 1e-3 mag;
 gradients |g - g_fd| <= 2e-3 max(|g_fd|, 1e-3 max_rows |g_fd|).
@@ -18,14 +20,17 @@ pytestmark = pytest.mark.gpu
 CURVE = {1: dict(mwr=3.4, uvb=0.7), 2: {}, 4: dict(dust_index=-0.35), 6: {}}
 
 
-def _inputs(n, seed, dust_type):
+def _inputs(n, seed, dust_type, per_model=False):
     wz, params = config3_inputs(n, seed=seed)
     rng = np.random.default_rng(seed + 1)
     params = dict(params, dust1=rng.uniform(0.1, 1.0, n), dust3=rng.uniform(0.0, 0.4, n),
                   frac_nodust=rng.uniform(0.0, 0.2, n), frac_obrun=rng.uniform(0.0, 0.3, n),
                   dust_index=rng.uniform(-1.0, -0.3, n))
-    for k, v in CURVE[dust_type].items():
-        params[k] = np.full(n, v)
+    if per_model:
+        params.update(mwr=rng.uniform(2.2, 5.0, n), uvb=rng.uniform(0.0, 1.5, n))
+    else:
+        for k, v in CURVE[dust_type].items():
+            params[k] = np.full(n, v)
     return wz, params
 
 
@@ -40,11 +45,12 @@ def _ctx(dust_type, **flags):
     return c
 
 
-@pytest.mark.parametrize("dust_type", [1, 2, 4, 6])
-def test_dust_type_matches_oracle(data, built_lib, dust_type):
+@pytest.mark.parametrize("dust_type,per_model", [(1, False), (2, False), (4, False), (6, False), (1, True),
+                                                 (4, True)])
+def test_dust_type_matches_oracle(data, built_lib, dust_type, per_model):
     from oracle.oracle import Oracle
     n = 60
-    wz, params = _inputs(n, 1400 + dust_type, dust_type)
+    wz, params = _inputs(n, 1400 + dust_type + (10 if per_model else 0), dust_type, per_model)
     c = _ctx(dust_type)
     got = c.csp_batch(params, ssp_weights_z=wz)
     plain = None
@@ -82,17 +88,18 @@ def _loss(out, mb, sb):
     return np.nansum(mb * out["mags"], axis=1) + np.sum(sb * out["spec"], axis=1)
 
 
-@pytest.mark.parametrize("dust_type,rows", [(1, {"dust2": 2, "dust3": 3, "mwr": 8, "uvb": 9}),
-                                            (2, {"dust2": 2, "dust3": 3}),
-                                            (4, {"dust2": 2, "dust3": 3, "dust_index": 4})])
-def test_dust_type_gradients(data, built_lib, dust_type, rows):
-    """Rows against FP64 central differences of the oracle (h = 1e-4 relative): each model's own parameter moved
-    (the batch itself keeps mwr, uvb and dust_index the same for every model). Without IGM and smoothing, at z = 0:
-    the curve's rows alone."""
+@pytest.mark.parametrize("dust_type,rows,per_model", [(1, {"dust2": 2, "dust3": 3, "mwr": 8, "uvb": 9}, False),
+                                                      (2, {"dust2": 2, "dust3": 3}, False),
+                                                      (4, {"dust2": 2, "dust3": 3, "dust_index": 4}, False),
+                                                      (1, {"dust2": 2, "mwr": 8, "uvb": 9}, True),
+                                                      (4, {"dust2": 2, "dust_index": 4}, True)])
+def test_dust_type_gradients(data, built_lib, dust_type, rows, per_model):
+    """Rows against FP64 central differences of the oracle (h = 1e-4 relative), each model's own parameter moved.
+    Without IGM and smoothing, at z = 0: the curve's rows alone."""
     from libopensps_gb300.workloads import adjoint_cotangents
     from oracle.oracle import Oracle
     n = 6
-    wz, params = _inputs(n, 1460 + dust_type, dust_type)
+    wz, params = _inputs(n, 1460 + dust_type + (10 if per_model else 0), dust_type, per_model)
     params = dict(params, zred=np.zeros(n), sigma_smooth=np.zeros(n))
     mb, sb = adjoint_cotangents(n, data["lambda"].size, 40, seed=1470 + dust_type)
     c = _ctx(dust_type)
@@ -121,13 +128,6 @@ def test_dust_type_refusals(data, built_lib):
     n = 8
     wz, params = _inputs(n, 1480, 1)
     c = _ctx(1)
-    with pytest.raises(OpenSPSError) as e:
-        c.csp_batch(dict(params, mwr=np.linspace(2.5, 4.0, n)), ssp_weights_z=wz)
-    assert e.value.status == 2 and "mwr" in e.value.message
-    c.set_int("dust_type", 4)
-    with pytest.raises(OpenSPSError) as e:
-        c.csp_batch(dict(params, dust_index=np.linspace(-1.0, -0.2, n)), ssp_weights_z=wz)
-    assert e.value.status == 2 and "dust_index" in e.value.message
     for dt in (3, 5):
         c.set_int("dust_type", dt)
         with pytest.raises(OpenSPSError) as e:
