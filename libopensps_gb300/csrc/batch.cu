@@ -954,7 +954,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             na.cw_ld = c.nt_neb + 2; na.nrun = c.neb.nrun;
             na.dem = d_dem + off; na.tab = c.neb.tab[neb_table].p; na.off = c.neb.off.p;
             na.rfirst = c.neb.runs.p; na.runs = reinterpret_cast<const int4 *>(c.neb.runs.p + NEB_RUN_HEAD);
-            na.q0 = c.neb.q0.p;
+            na.q0 = c.neb.q0.p; na.q0_exp = c.neb.q0_exp;
             na.wz = d_wz + (size_t)nt * nz * off;
             na.groups = c.neb.groups.p + cg.x; na.order = c.neb.order.p;
             cudaError_t r = c.neb.cw.reserve((size_t)nk * na.cw_ld);

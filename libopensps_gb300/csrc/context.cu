@@ -549,7 +549,15 @@ int nebular_load(Context &c, std::string &err) {
                 }
                 q0[(size_t)t * c.nz + z] = s / 6.62607015e-27 * 3.828e33;
             }
-    if (e == cudaSuccess) e = upload(c.neb.q0, q0.data(), q0.size());
+    // as FP32 scaled by a power of two (their largest in [0.5, 1)): the per-model weights' sums run in FP32
+    double qmax = 0.0;
+    for (double v : q0) qmax = std::max(qmax, v);
+    int qe = 0;
+    if (qmax > 0.0) std::frexp(qmax, &qe);
+    c.neb.q0_exp = qe;
+    std::vector<float> q0s(q0.size());
+    for (size_t i = 0; i < q0.size(); ++i) q0s[i] = (float)std::ldexp(q0[i], -qe);
+    if (e == cudaSuccess) e = upload(c.neb.q0, q0s.data(), q0s.size());
     // per nebular age its CLOUDY interval: get_grid_indices_weights (opensps_gas.f90:394-412) on the log ages
     c.neb.ia.assign(nn, 0);
     c.neb.wa.assign(nn, 0.0);

@@ -141,13 +141,14 @@ struct AgnTorus {
 // x 7 ionization parameters at each pixel, with per nebular age of the SSP grid its CLOUDY age interval and the
 // ionizing photon rate of each (age, metallicity) SSP. On the device, per table (0: nodust, 1: dust) the log2 of
 // the continuum less a per-pixel offset (off: the largest log2 value of the pixel over the grid, rounded up to an
-// integer) as FP32, [logZ][logU][age][pixel]; q0 FP64 (nt_neb x nz, metallicity fastest); per nebular age its
+// integer) as FP32, [logZ][logU][age][pixel]; q0 (nt_neb x nz, metallicity fastest; FP32 times 2^q0_exp); per nebular age its
 // interval and weight as batch_nebular_indices forms them (:1651-1686).
 struct NebularGrid {
     bool have[2] = {false, false};
     std::vector<double> logz, lage, logu;
     DevBuf<float> tab[2], off;
-    DevBuf<double> q0;
+    DevBuf<float> q0;            // the ionizing photon rates scaled by 2^-q0_exp (FP32; their largest in [0.5, 1))
+    int q0_exp = 0;
     // per nebular age its CLOUDY interval (lower node, 0-based) and weight wa in it (clamped to [0, 1]); the ages as
     // runs for the last itesc (NEB_RUN_HEAD ints: each interval's first run and the run count, then the runs as int4)
     std::vector<int> ia;

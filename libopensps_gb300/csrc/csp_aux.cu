@@ -13,22 +13,6 @@
 namespace sps {
 
 // ---------------------------------------------------------------------------------------------- weights
-// The weight as an FP32 value, 0 unless it is above SAFE_FLOOR (model_sums_zw's floor): the FP64 -> FP32 rounding
-// done on the integer pipes (round to nearest even on the 29 dropped mantissa bits) so that the cast keeps off the
-// FP64 unit, which GB300 has little of. Weights below FP32's smallest normal also give 0.
-__device__ __forceinline__ float weight_to_f32(double w) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(w);
-    const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
-    if (b <= 0x0010000000000000ull || (hi32 >> 31)) return 0.f;       // <= DBL_MIN, or negative
-    const int fe = (int)((hi32 >> 20) & 0x7ff) - 896;                  // FP32 biased exponent
-    if (fe < 1) return 0.f;
-    if (fe > 254) return __int_as_float(0x7f800000);
-    uint32_t m = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
-    const uint32_t rem = lo32 & 0x1fffffffu;
-    m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
-    return __uint_as_float(((uint32_t)fe << 23) + m);                  // a mantissa carry moves into the exponent
-}
-
 // The operand and, from the same FP64 weights, the FP64 sums of model_sums_zw (one warp per model, the sums in the
 // operand's column order; young ages by the column map's KMAP_YOUNG bit): the sums ride the FP64 pipe while the
 // conversion waits on memory, instead of a second pass over the weights bound by that pipe. Escaping-light columns

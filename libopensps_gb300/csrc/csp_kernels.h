@@ -38,6 +38,22 @@ enum {
 // (T0 + s1 T1 + s2 T2 + s3 T3) exp2(ed ln(lambda / 5500) log2 e) with its scalars MP_CS1.. and MP_DUST_INDEX).
 enum { PIX_LTAB2 = 0, PIX_CURVE = 1, PIX_IGM_A = 2, PIX_T = 8, PIX_FLOATS = 12 };
 
+// The weight as an FP32 value, 0 unless it is above SAFE_FLOOR (model_sums_zw's floor): the FP64 -> FP32 rounding
+// done on the integer pipes (round to nearest even on the 29 dropped mantissa bits) so that the cast keeps off the
+// FP64 unit, which GB300 has little of. Weights below FP32's smallest normal also give 0.
+__device__ __forceinline__ float weight_to_f32(double w) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+    const uint32_t hi32 = (uint32_t)(b >> 32), lo32 = (uint32_t)b;
+    if (b <= 0x0010000000000000ull || (hi32 >> 31)) return 0.f;       // <= DBL_MIN, or negative
+    const int fe = (int)((hi32 >> 20) & 0x7ff) - 896;                  // FP32 biased exponent
+    if (fe < 1) return 0.f;
+    if (fe > 254) return __int_as_float(0x7f800000);
+    uint32_t m = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+    const uint32_t rem = lo32 & 0x1fffffffu;
+    m += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(((uint32_t)fe << 23) + m);                  // a mantissa carry moves into the exponent
+}
+
 // A model's diffuse curve at a pixel: the batch's shared one (uniform), its tabulated form (tab: the pixel's
 // T0..T3 with the model's s1..s3 = cs and power ed), or the power law exp2(ed ltab2). ex2: the SFU's 2^x.
 __device__ __forceinline__ float pix_curve(bool uniform, bool tab, float curve_u, float ltab2, float4 t, float4 cs,
@@ -383,7 +399,9 @@ struct NebContArgs {
     const float *tab, *off;
     const int4 *runs;
     const int *rfirst;
-    const double *q0, *wz;
+    const float *q0;          // nt_neb x nz, times 2^q0_exp
+    int q0_exp;
+    const double *wz;
     const int4 *groups;
     const int *order;
     float *cw;

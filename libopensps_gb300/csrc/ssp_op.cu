@@ -787,7 +787,8 @@ constexpr int OPS_IR_THREADS = 256, OPS_IR_WARPS = OPS_IR_THREADS / 32, OPS_IR_R
 
 // One model per CTA: the node values and their log-derivatives in shared memory; warp w takes grid points w, w + 8,
 // ..., lane l the nodes l + 32 i of each (the row of Xbar read once, coalesced): wz_bar(g) by a warp sum, Y(r) in
-// FP32 per lane over 16 grid points at a time, then FP64; the slopes' sums over the nodes by a block reduction.
+// FP32 per lane over 64 grid points at a time (GB300's FP64 pipe is narrow), then FP64; the slopes' sums over the
+// nodes by a block reduction.
 __global__ void __launch_bounds__(OPS_IR_THREADS) ops_interp_rev_kernel(OpsInterpRevArgs a) {
     __shared__ float ct[OPS_IMAXR];
     __shared__ float dlc[3][OPS_IMAXR];
@@ -866,7 +867,7 @@ __global__ void __launch_bounds__(OPS_IR_THREADS) ops_interp_rev_kernel(OpsInter
                 a.wzb[(size_t)ng * m + t + (size_t)a.nt * z] = cs * (double)ws;
             }
         }
-        if (++nstep == 16) {
+        if (++nstep == 64) {
 #pragma unroll
             for (int i = 0; i < OPS_IR_RI; ++i) { yd[i] += (double)y[i]; y[i] = 0.f; }
             nstep = 0;
@@ -1178,42 +1179,43 @@ __global__ void __launch_bounds__(256, 3) parts_epilogue_kernel(PartsEpilogueArg
 // the young and old sums before the per-model epilogue.
 //
 // neb_weights_kernel, one warp per model: per nebular age t the weight C(t) = |1 - frac_obrun| sum_z w(t, z) q0(t, z)
-// (the SFH weight times the ionizing photon rate, over the model's metallicities; FP64), normalised by its largest
-// value S; log2 S split into an integer part and the rest. Row m of cw: C(t) / S for t < nt_neb, then (S's integer
-// part, the rest).
+// (the SFH weight times the ionizing photon rate, over the model's metallicities), normalised by its largest value S;
+// log2 S split into an integer part and the rest. Row m of cw: C(t) / S for t < nt_neb, then (S's integer part, the
+// rest). In FP32 (the weights rounded on the integer pipes, q0 scaled by 2^q0_exp, which goes into S's integer
+// part): the sums of up to a dozen positive terms keep ~1e-7 (the FP64 form held the kernel at GB300's FP64 rate).
 __global__ void __launch_bounds__(256) neb_weights_kernel(NebContArgs a) {
     const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (m >= a.n) return;
-    const DustEmModel dm = a.dem[m];
+    const float fabs_m = a.dem[m].neb_fabs;
     const double *w = a.wz + (size_t)m * a.nz * a.nt;
-    double cs[(NEB_MAX_AGES + 31) / 32];
-    double mx = 0.0;
+    float cs[(NEB_MAX_AGES + 31) / 32];
+    float mx = 0.f;
 #pragma unroll
     for (int i = 0; i < (NEB_MAX_AGES + 31) / 32; ++i) {
         const int t = lane + 32 * i;
-        double c = 0.0;
+        float c = 0.f;
         if (t < a.nt_neb) {
-            for (int z = 0; z < a.nz; ++z) {
-                const double wv = __ldg(w + (size_t)z * a.nt + t);
-                if (wv > SAFE_FLOOR) c = fma(wv, __ldg(a.q0 + (size_t)t * a.nz + z), c);
-            }
-            c *= (double)dm.neb_fabs;
+            for (int z = 0; z < a.nz; ++z)
+                c = fmaf(weight_to_f32(__ldg(w + (size_t)z * a.nt + t)), __ldg(a.q0 + (size_t)t * a.nz + z), c);
+            c *= fabs_m;
         }
         cs[i] = c;
-        mx = fmax(mx, c);
+        mx = fmaxf(mx, c);
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
     float *o = a.cw + (size_t)m * a.cw_ld;
 #pragma unroll
     for (int i = 0; i < (NEB_MAX_AGES + 31) / 32; ++i) {
         const int t = lane + 32 * i;
-        if (t < a.nt_neb) o[t] = mx > 0.0 ? (float)(cs[i] / mx) : 0.f;
+        if (t < a.nt_neb) o[t] = mx > 0.f ? cs[i] / mx : 0.f;
     }
     if (lane == 0) {
-        const double s2 = mx > 0.0 ? log2(mx) : 0.0, si = floor(s2);
-        o[a.nt_neb] = (float)si;
-        o[a.nt_neb + 1] = mx > 0.0 ? (float)(s2 - si) : 0.f;
+        // S = mx 2^q0_exp = f 2^(e + q0_exp), f in [0.5, 1): log2 S = (e - 1 + q0_exp) + log2(2 f)
+        int e = 0;
+        const float f = mx > 0.f ? frexpf(mx, &e) : 0.5f;
+        o[a.nt_neb] = mx > 0.f ? (float)(e - 1 + a.q0_exp) : 0.f;
+        o[a.nt_neb + 1] = mx > 0.f ? log2f(2.f * f) : 0.f;
     }
 }
 
