@@ -698,7 +698,10 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
-        if (c.imf_type != 2) { err = "imf_type " + std::to_string(c.imf_type) + ": only 2 (Kroupa) with the operators"; return ST_UNSUPPORTED; }
+        if (c.imf_type < 0 || c.imf_type > 2) {
+            err = "imf_type " + std::to_string(c.imf_type) + ": 0 (Salpeter), 1 (Chabrier) and 2 (Kroupa) with the operators";
+            return ST_UNSUPPORTED;
+        }
         nacc2 = true;
     } else {
         for (int m = 0; m < n; ++m)
@@ -1110,6 +1113,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             std::vector<double> al((size_t)3 * n);
             for (int m = 0; m < n; ++m) {
                 al[3 * m] = par(m, PF_IMF1); al[3 * m + 1] = par(m, PF_IMF2); al[3 * m + 2] = par(m, PF_IMF3);
+                // (Salpeter: the Kroupa form with the three slopes 2.35; Chabrier: not read)
+                if (c.imf_type != 2) al[3 * m] = al[3 * m + 1] = al[3 * m + 2] = 2.35;
             }
             if ((e = c.d_alpha.reserve(al.size())) != cudaSuccess || (e = c.d_yo.reserve((size_t)2 * n * ns + 4)) != cudaSuccess ||
                 (e = cudaMemcpyAsync(c.d_alpha.p, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {

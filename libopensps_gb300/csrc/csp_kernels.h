@@ -320,6 +320,7 @@ cudaError_t run_ops_fold(const OpsFoldArgs &a, cudaStream_t st);
 // The interpolated fold's operand (one row per model of a chunk) and its GEMM's reduction.
 struct OpsInterpArgs {
     int m0, nt, nz, R, ktot, itesc;          // models m0 .. m0 + gridDim.x - 1; ktot = nt nz R columns
+    int imf_type = 2;                        // 2 Kroupa (slopes per model; 0 Salpeter as Kroupa), 1 Chabrier
     unsigned rg_magic;                       // 2^32 / (R / 8), rounded up
     int noff[3], nn[3];                      // the segments' node columns: noff[s] .. noff[s] + nn[s] - 1
     double x0[3], h[3];                      // node j of segment s at ln m = x0[s] + (j - 4) h[s]
@@ -339,6 +340,7 @@ struct OpsInterpReduceArgs {
 // metallicities and of the three Kroupa slopes.
 struct OpsRevArgs {
     int n, nt, nz, npt, ntpad, itesc;
+    int imf_type = 2;         // the slopes' rows are written only for Kroupa (2); zero otherwise
     float lim_lo, lim_hi;
     const double *wz;         // n x nt x nz SFH weights (age fastest)
     const double *alpha;      // n x 3 Kroupa slopes

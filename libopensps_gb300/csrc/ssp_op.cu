@@ -439,9 +439,14 @@ constexpr int OPS_IMAXG = 4096;                      // grid points (nt nz <= OP
 
 // One thread per model: 1 / T (the IMF's mass between its limits, FP64) and c2 = 0.5^(alpha2 - alpha1), for
 // ops_interp_x_kernel (formed there by one thread per CTA, the FP64 work ran as one-lane warps).
-__global__ void ops_interp_const_kernel(const double *alpha, int n, float lim_lo, float lim_hi, double2 *out) {
+__global__ void ops_interp_const_kernel(const double *alpha, int n, float lim_lo, float lim_hi, double fixed_inv_total,
+                                        double2 *out) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
+    if (fixed_inv_total > 0.0) {   // an IMF without per-model parameters (Chabrier): its 1 / T, formed on the host
+        out[m] = make_double2(fixed_inv_total, 0.0);
+        return;
+    }
     KroupaSeg ks;
     float itf;
     double total;
@@ -449,6 +454,23 @@ __global__ void ops_interp_const_kernel(const double *alpha, int n, float lim_lo
     kroupa_setup(al, lim_lo, lim_hi, ks, itf, nullptr, &total);
     out[m] = make_double2(total > 0.0 ? 1.0 / total : 1.0, pow(0.5, -al[0] + al[1]));
 }
+// A node's value for the fold: the IMF per unit mass at mu = e^x of segment q, over T (it = 1 / T). Kroupa (and
+// Salpeter as Kroupa with equal slopes): c_q mu^-alpha_q (c = 1, c2, c2). Chabrier 2003 (imf_integral case 1,
+// src/physics/opensps_imf.f90:234-242): the lognormal exp(-(log10 mu - log10 0.08)^2 / (2 0.69^2)) / mu in segments 0
+// and 1 (below 1 M_sun, extended past it at the segment's outer nodes), exp(-(log10 0.08)^2 / (2 0.69^2)) mu^-2.3 in
+// segment 2 (continuous at 1 M_sun).
+__device__ __forceinline__ double ops_node_value(int imf_type, int q, double x, const double *al, double it, double c2) {
+    if (imf_type == 1) {
+        const double l0 = -1.0969100130080565, inv2s2 = 1.0 / (2.0 * 0.69 * 0.69);   // log10 0.08
+        if (q < 2) {
+            const double u = x * 0.43429448190325176 - l0;                          // log10 mu - log10 0.08
+            return it * exp(-u * u * inv2s2 - x);
+        }
+        return it * exp(-l0 * l0 * inv2s2 - 2.3 * x);
+    }
+    return (q == 0 ? 1.0 : c2) * it * exp(-al[q] * x);
+}
+
 __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpArgs a) {
     __shared__ __align__(16) float ctk[OPS_IMAXR];
     __shared__ float sws[OPS_IMAXG];
@@ -471,7 +493,7 @@ __global__ void __launch_bounds__(OPS_IX_THREADS) ops_interp_x_kernel(OpsInterpA
             const int j = r - a.noff[q];
             if (j >= 0 && j < a.nn[q]) {
                 const double x = a.x0[q] + (double)(j - OPS_IDEG / 2) * a.h[q];
-                v = (float)((q == 0 ? 1.0 : c2) * it * exp(-al[q] * x));
+                v = (float)ops_node_value(a.imf_type, q, x, al, it, c2);
             }
         }
         ctk[r] = v;
@@ -742,7 +764,8 @@ __global__ void ops_rev_finish_kernel(OpsRevArgs a) {
     double s[3] = {0.0, 0.0, 0.0};
     for (int z = 0; z < a.nz; ++z)
         for (int j = 0; j < 3; ++j) s[j] += a.apart[((size_t)z * a.n + m) * 3 + j];
-    for (int j = 0; j < 3; ++j) a.params_bar[(size_t)a.rows * m + a.row_imf1 + j] = a.cscale[m] * s[j];
+    // (the slopes are the Kroupa IMF's; with Salpeter, taken as Kroupa with fixed equal slopes, they are not parameters)
+    for (int j = 0; j < 3; ++j) a.params_bar[(size_t)a.rows * m + a.row_imf1 + j] = a.imf_type == 2 ? a.cscale[m] * s[j] : 0.0;
 }
 
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
@@ -771,6 +794,7 @@ cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
 // forward's interpolated fold takes (its interpolation error carries over to the cotangents).
 struct OpsInterpRevArgs {
     int m0, nt, nz, R;
+    int imf_type;
     size_t ktot;
     int noff[3], nn[3];
     double x0[3], h[3];
@@ -827,11 +851,13 @@ __global__ void __launch_bounds__(OPS_IR_THREADS) ops_interp_rev_kernel(OpsInter
                 const int j = r - a.noff[q];
                 if (j >= 0 && j < a.nn[q]) {
                     const double x = a.x0[q] + (double)(j - OPS_IDEG / 2) * a.h[q];
-                    v = (float)((q == 0 ? 1.0 : kc.y) * kc.x * exp(-al[q] * x));
-                    double g3[3] = {-dlnT_s[0], -dlnT_s[1], -dlnT_s[2]};
-                    g3[q] -= x;
-                    if (q > 0) { g3[0] += KR_LN2; g3[1] -= KR_LN2; }
-                    d[0] = (float)g3[0]; d[1] = (float)g3[1]; d[2] = (float)g3[2];
+                    v = (float)ops_node_value(a.imf_type, q, x, al, kc.x, kc.y);
+                    if (a.imf_type == 2) {   // (the slopes act with Kroupa only)
+                        double g3[3] = {-dlnT_s[0], -dlnT_s[1], -dlnT_s[2]};
+                        g3[q] -= x;
+                        if (q > 0) { g3[0] += KR_LN2; g3[1] -= KR_LN2; }
+                        d[0] = (float)g3[0]; d[1] = (float)g3[1]; d[2] = (float)g3[2];
+                    }
                 }
             }
         }
@@ -965,7 +991,7 @@ int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err) {
             if ((e = run_gemm_bf16x3(pl, g, st)) != cudaSuccess) { err = cmsg("interpolated reverse fold GEMM", e); return ST_DATA_MISSING; }
         }
         OpsInterpRevArgs a;
-        a.m0 = m0; a.nt = nt; a.nz = nz; a.R = R; a.ktot = ktot;
+        a.m0 = m0; a.nt = nt; a.nz = nz; a.R = R; a.ktot = ktot; a.imf_type = r.imf_type;
         for (int s = 0; s < 3; ++s) { a.noff[s] = o.interp_noff[s]; a.nn[s] = o.interp_nn[s]; a.x0[s] = o.interp_x0[s]; a.h[s] = o.interp_h[s]; }
         a.lim_lo = r.lim_lo; a.lim_hi = r.lim_hi;
         a.wz = r.wz; a.alpha = r.alpha; a.cscale = r.cscale; a.mass_bar = r.mass_bar; a.lbol_bar = r.lbol_bar; a.sums = r.sums;
@@ -1681,6 +1707,7 @@ int ops_build(Context &c, std::string &err) {
 // Whether the interpolated fold holds for every model's slopes (and is built and not switched off).
 static bool ops_interp_ok(const Context &c, const double *h_alpha, int n) {
     if (!c.ops.interp_ready || c.ops_exact || !h_alpha) return false;
+    if (c.imf_type == 1) return true;   // (Chabrier: no slopes)
     for (int m = 0; m < n; ++m)
         for (int s = 0; s < 3; ++s)
             if (!(std::fabs(h_alpha[3 * (size_t)m + s]) <= OPS_AMAX[s])) return false;
@@ -1704,6 +1731,24 @@ static int choose_ksplit(int tiles_mn, int nkb, int num_sms) {
 
 // The interpolated fold of n models into the template GEMM's operand (d_vhi / d_vlo) and the sums: per chunk of
 // models the operand X, the young and old split-K GEMMs against the operator basis, their reduction.
+// Chabrier 2003's mass between m1 and m2 (imf_integral case 1, mass-weighted: src/physics/opensps_imf.f90:234-242):
+// the lognormal per unit ln m, exp(-(log10 m - log10 0.08)^2 / (2 sigma^2)) with sigma = 0.69, below 1 M_sun (times m:
+// a lognormal of centre log10 0.08 + ln 10 sigma^2, scale exp(ln 10 log10 0.08 + (ln 10 sigma)^2 / 2), in closed form
+// with erf), and the power law exp(-(log10 0.08)^2 / (2 sigma^2)) m^-2.3 above. FP64, host.
+static double chabrier_mass(double m1, double m2) {
+    const double K = std::log(10.0), lmc = std::log10(0.08), s2 = 0.69 * 0.69, sig = 0.69;
+    double v = 0.0;
+    const double a = m1, b = std::min(m2, 1.0);
+    if (b > a) {
+        const double centre = lmc + K * s2, scale = std::exp(K * lmc + 0.5 * K * K * s2);
+        const double z1 = (std::log10(a) - centre) / (sig * std::sqrt(2.0)), z2 = (std::log10(b) - centre) / (sig * std::sqrt(2.0));
+        v += scale * K * sig * std::sqrt(0.5 * M_PI) * (std::erf(z2) - std::erf(z1));
+    }
+    const double lo = std::max(m1, 1.0);
+    if (m2 > lo) v += std::exp(-lmc * lmc / (2.0 * s2)) * (std::pow(m2, -0.3) - std::pow(lo, -0.3)) / -0.3;
+    return v;
+}
+
 static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d_alpha, int itesc, std::string &err) {
     SspOps &o = c.ops;
     cudaStream_t st = c.stream;
@@ -1722,7 +1767,8 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
         err = cmsg("device memory", e);
         return ST_DATA_MISSING;
     }
-    ops_interp_const_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_alpha, n, 0.08f, 120.f, c.d_ix_const.p);
+    const double fixed_it = c.imf_type == 1 ? 1.0 / chabrier_mass(0.08, 120.0) : 0.0;
+    ops_interp_const_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_alpha, n, 0.08f, 120.f, fixed_it, c.d_ix_const.p);
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cmsg("interpolated fold constants kernel", e); return ST_DATA_MISSING; }
     c.ops_launches += 1;
     for (int m0 = 0; m0 < n; m0 += chunk) {
@@ -1733,7 +1779,7 @@ static int run_ops_interp(Context &c, int n, const double *d_wz, const double *d
         for (int s = 0; s < 3; ++s) {
             xa.noff[s] = o.interp_noff[s]; xa.nn[s] = o.interp_nn[s]; xa.x0[s] = o.interp_x0[s]; xa.h[s] = o.interp_h[s];
         }
-        xa.lim_lo = 0.08f; xa.lim_hi = 120.f;
+        xa.lim_lo = 0.08f; xa.lim_hi = 120.f; xa.imf_type = c.imf_type;
         xa.wz = d_wz; xa.alpha = d_alpha; xa.kconst = c.d_ix_const.p; xa.mrow = o.i_mrow.p; xa.lrow = o.i_lrow.p;
         xa.x_hi = c.d_ix_hi.p; xa.x_lo = c.d_ix_lo.p; xa.sums = c.d_sums.p;
         ops_interp_x_kernel<<<rows, OPS_IX_THREADS, 0, st>>>(xa);
@@ -1782,6 +1828,10 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     cudaError_t e;
     const int ngroups = (n + 3) / 4;
     const bool interp = ops_interp_ok(c, h_alpha, n);
+    if (!interp && c.imf_type == 1) {
+        err = "the Chabrier IMF takes the interpolated fold (gb300_ops_exact off)";
+        return ST_UNSUPPORTED;
+    }
     if ((e = c.d_vhi.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
         (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess ||
         (!interp && (e = c.d_vpart.reserve((size_t)c.nz * 2 * n * o.ntpad)) != cudaSuccess) ||
@@ -1824,12 +1874,23 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err) {
     if (!c.ops.ready) { err = "no SSP operators on the context (opensps_context_build_ssp_ops)"; return ST_NO_OPERATOR; }
-    if (imf_type != 2) { err = "imf_type " + std::to_string(imf_type) + ": only 2 (Kroupa) on this path"; return ST_UNSUPPORTED; }
+    if (imf_type < 0 || imf_type > 2) {
+        err = "imf_type " + std::to_string(imf_type) + ": 0 (Salpeter), 1 (Chabrier) or 2 (Kroupa) on this path";
+        return ST_UNSUPPORTED;
+    }
+    // (the operator batch takes the context's imf_type: this IMF for the call)
+    struct ImfTypeScope {
+        Context &c;
+        int saved;
+        ~ImfTypeScope() { c.imf_type = saved; }
+    } imf_scope{c, c.imf_type};
+    c.imf_type = imf_type;
     const int nt = c.nt, nz = c.nz, ns = c.nspec;
     const int z = std::max(1, std::min(c.zmet, nz)) - 1;
     std::vector<double> wz((size_t)nt * nt * nz, 0.0), alpha((size_t)3 * nt);
-    const double a1 = imf_params ? imf_params[0] : c.pdef[PF_IMF1], a2 = imf_params ? imf_params[1] : c.pdef[PF_IMF2];
-    const double a3 = imf_params ? imf_params[2] : c.pdef[PF_IMF3];
+    double a1 = imf_params ? imf_params[0] : c.pdef[PF_IMF1], a2 = imf_params ? imf_params[1] : c.pdef[PF_IMF2];
+    double a3 = imf_params ? imf_params[2] : c.pdef[PF_IMF3];
+    if (imf_type != 2) a1 = a2 = a3 = 2.35;   // (Salpeter as Kroupa with equal slopes; Chabrier: not read)
     for (int t = 0; t < nt; ++t) {
         wz[(size_t)nt * nz * t + t + (size_t)nt * z] = 1.0;
         alpha[3 * t] = a1; alpha[3 * t + 1] = a2; alpha[3 * t + 2] = a3;

@@ -5,7 +5,9 @@
  *   compute_imf_weights      src/physics/opensps_imf.f90:111-172  (bin edges halfway between the isochrone masses,
  *                            the first from the IMF's lower bound, the last at the last mass; points outside the
  *                            IMF mass limits weigh nothing; normalised by the IMF's mass over the limits)
- *   imf_integral (Kroupa)    src/physics/opensps_imf.f90:206-315, case 2 (segments 0.08-0.5-1.0, slopes alpha1-3)
+ *   imf_integral             src/physics/opensps_imf.f90:206-315: case 2 Kroupa (segments 0.08-0.5-1.0, slopes
+ *                            alpha1-3), case 0 Salpeter (slope 2.35, opensps_context_types.f90:120), case 1 Chabrier
+ *                            2003 (the lognormal below 1 M_sun, integrate_lognormal :640-700, and the power law above)
  *   integrate_powerlaw       src/physics/opensps_imf.f90:725-748 (the expm1 form: oracle_powerlaw_bin)
  *   ssp_op_model_weights / ssp_op_spmv   src/physics/opensps_ssp_operator.f90:1296-1338: W = S . w_IMF with the
  *                            mass and L_bol rows
@@ -29,6 +31,7 @@ typedef struct {
     const double *coef;        /* nz x nt x npt x 4 */
     const double *mcur, *lum;  /* nz x nt x npt */
     double lower_bound, lim_lo, lim_hi;
+    int imf_type;              /* 0 Salpeter, 1 Chabrier, 2 Kroupa (alpha per model) */
 } oracle_ops_t;
 
 /* integrate_powerlaw(lo, hi, alpha, mass_weighted, c) */
@@ -52,6 +55,49 @@ double oracle_kroupa_integral(const double *a, double m1, double m2, int mass_we
     return v;
 }
 
+/* The lognormal piece of Chabrier 2003, N(m) = exp(-(log10 m - log10 0.08)^2 / (2 0.69^2)) per unit ln m: its number
+ * (or mass) over [m1, m2] in closed form, K sigma sqrt(pi / 2) (erf(z2) - erf(z1)) with z = (log10 m - centre) /
+ * (sigma sqrt 2) (the mass-weighted form shifts the centre by K sigma^2 and scales by exp(K log_mc + K^2 sigma^2 / 2),
+ * K = ln 10); for a bin narrower than 0.1 in z a 5-point Gauss-Legendre rule on exp(-z^2), and erfc in a tail, against
+ * the cancellation of erf near 1 (integrate_lognormal, src/physics/opensps_imf.f90:640-700). */
+static double lognormal(double m1, double m2, double log_mc, double sigma2, int mass_weighted) {
+    const double K = log(10.0), sig = sqrt(sigma2);
+    const double centre = mass_weighted ? log_mc + K * sigma2 : log_mc;
+    const double scale = mass_weighted ? exp(K * log_mc + 0.5 * K * K * sigma2) : 1.0;
+    const double z1 = (log10(m1) - centre) / (sig * sqrt(2.0)), z2 = (log10(m2) - centre) / (sig * sqrt(2.0));
+    if (z2 - z1 < 0.1) {
+        static const double x[3] = {0.0, 0.5384693101056831, 0.9061798459386640};
+        static const double w[3] = {0.5688888888888889, 0.4786286704993665, 0.2369268850561891};
+        const double zc = 0.5 * (z1 + z2), zh = 0.5 * (z2 - z1);
+        double q = w[0] * exp(-zc * zc);
+        for (int k = 1; k < 3; ++k) {
+            const double a = zc - zh * x[k], b = zc + zh * x[k];
+            q += w[k] * (exp(-a * a) + exp(-b * b));
+        }
+        return scale * K * sig * sqrt(2.0) * zh * q;
+    }
+    const double c = scale * K * sig * sqrt(0.5 * acos(-1.0));
+    if (z1 >= 0.0) return c * (erfc(z1) - erfc(z2));
+    if (z2 <= 0.0) return c * (erfc(-z2) - erfc(-z1));
+    return c * (erf(z2) - erf(z1));
+}
+
+/* imf_integral by type: number (mass_weighted 0) or mass over [m1, m2]; a: Kroupa slopes (type 2). */
+double oracle_imf_integral(int imf_type, const double *a, double m1, double m2, int mass_weighted) {
+    const double lo = fmin(m1, m2), hi = fmax(m1, m2);
+    if (hi <= lo) return 0.0;
+    if (imf_type == 2) return oracle_kroupa_integral(a, m1, m2, mass_weighted);
+    if (imf_type == 0) return powerlaw(lo, hi, 2.35, mass_weighted, 1.0);
+    if (imf_type == 1) {
+        const double lmc = log10(0.08), s2 = 0.69 * 0.69;
+        double v = 0.0;
+        if (fmin(hi, 1.0) > lo) v += lognormal(lo, fmin(hi, 1.0), lmc, s2, mass_weighted);
+        if (hi > fmax(lo, 1.0)) v += powerlaw(fmax(lo, 1.0), hi, 2.3, mass_weighted, exp(-lmc * lmc / (2.0 * s2)));
+        return v;
+    }
+    return 0.0;
+}
+
 /* The IMF weights of one grid point's isochrone points (npt), normalised by the IMF's mass over its limits. */
 static void imf_weights(const oracle_ops_t *op, const double *mini, const double *a, double inv_total, double *w) {
     const int n = op->npt;
@@ -61,7 +107,7 @@ static void imf_weights(const oracle_ops_t *op, const double *mini, const double
         const double m1 = (i == 0) ? op->lower_bound : mini[i] - 0.5 * (mini[i] - mini[i - 1]);
         const double m2 = (i == n - 1) ? mini[i] : mini[i] + 0.5 * (mini[i + 1] - mini[i]);
         if (m2 <= m1) continue;
-        w[i] = oracle_kroupa_integral(a, m1, m2, 0) * inv_total;
+        w[i] = oracle_imf_integral(op->imf_type, a, m1, m2, 0) * inv_total;
     }
 }
 
@@ -78,7 +124,7 @@ void oracle_ops_csp(const oracle_ops_t *op, int n, const double *alpha, const do
 #pragma omp for schedule(dynamic, 1)
         for (int m = 0; m < n; ++m) {
             const double *a = alpha + 3 * (size_t)m;
-            const double total = oracle_kroupa_integral(a, op->lim_lo, op->lim_hi, 1);
+            const double total = oracle_imf_integral(op->imf_type, a, op->lim_lo, op->lim_hi, 1);
             const double inv = total > 0.0 ? 1.0 / total : 1.0;
             memset(vy, 0, sizeof(double) * ne);
             memset(vo, 0, sizeof(double) * ne);

@@ -47,7 +47,7 @@ class _OpsT(C.Structure):
     _fields_ = [("nspec", C.c_int), ("nt", C.c_int), ("nz", C.c_int), ("npt", C.c_int), ("ntempl", C.c_int),
                 ("lib", C.POINTER(C.c_float)), ("mini", _dp), ("idx", C.POINTER(C.c_int)), ("coef", _dp),
                 ("mcur", _dp), ("lum", _dp), ("lower_bound", C.c_double), ("lim_lo", C.c_double),
-                ("lim_hi", C.c_double)]
+                ("lim_hi", C.c_double), ("imf_type", C.c_int)]
 
 
 _lib = None
@@ -58,6 +58,8 @@ def lib() -> C.CDLL:
     if _lib is None:
         build()
         _lib = C.CDLL(str(LIB))
+        _lib.oracle_imf_integral.restype = C.c_double
+        _lib.oracle_imf_integral.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_int]
         _lib.oracle_dust_curve.restype = C.c_double
         _lib.oracle_dust_curve.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib.oracle_find_interval.restype = C.c_int
@@ -371,9 +373,10 @@ class Oracle:
 
 
 class OpsOracle:
-    """The SSP operator applied to per-model Kroupa IMFs (ops_oracle.c) over the operator dataset (synth_ops)."""
+    """The SSP operator applied to per-model IMFs (ops_oracle.c) over the operator dataset (synth_ops): imf_type 2
+    Kroupa (alpha per model), 0 Salpeter, 1 Chabrier."""
 
-    def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0):
+    def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0, imf_type: int = 2):
         self.ops = ops
         man = ops["manifest"]
         self.nspec, self.nt, self.nz, self.npt, self.ntempl = man["nspec"], man["nt"], man["nz"], man["npt"], man["ntempl"]
@@ -385,6 +388,7 @@ class OpsOracle:
         t.mini, t.coef, t.mcur, t.lum = _p(mi), _p(co), _p(mc), _p(lu)
         t.idx = ix.ctypes.data_as(C.POINTER(C.c_int))
         t.lower_bound, t.lim_lo, t.lim_hi = man["imf_lower_bound"], lim_lo, lim_hi
+        t.imf_type = int(imf_type)
         self.t = t
 
     def parts(self, alpha: np.ndarray, wz: np.ndarray, itesc: int):
@@ -396,6 +400,11 @@ class OpsOracle:
         mass, ls = np.empty(n), np.empty(n)
         lib().oracle_ops_csp(C.byref(self.t), n, _p(a), _p(w), int(itesc), _p(y), _p(o), _p(mass), _p(ls))
         return y, o, mass, ls
+
+
+def imf_integral(imf_type: int, m1: float, m2: float, mass_weighted: bool, alpha=(1.3, 2.3, 2.3)) -> float:
+    a = np.ascontiguousarray(alpha, dtype=np.float64)
+    return lib().oracle_imf_integral(int(imf_type), _p(a), float(m1), float(m2), int(mass_weighted))
 
 
 def kroupa_integral(alpha, m1: float, m2: float, mass_weighted: bool) -> float:
