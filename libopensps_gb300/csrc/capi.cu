@@ -116,8 +116,9 @@ int batch_core(Context &cref, int n, int n_params, const char *const *names, con
     std::vector<double> sfhp;
     if (!ssp_weights_z) {
         if (!ssp_weights) {
-            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4) {
-                err = "sfh = " + std::to_string(c->sfh) + ": only 0 (SSP), 1 (tau) and 4 (delayed tau) on this path";
+            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4 && c->sfh != 5) {
+                err = "sfh = " + std::to_string(c->sfh) +
+                      ": only 0 (SSP), 1 (tau), 4 (delayed tau) and 5 (delayed tau with a linear ramp) on this path";
                 return ST_UNSUPPORTED;
             }
             for (int m = 0; m < n; ++m)
@@ -127,7 +128,8 @@ int batch_core(Context &cref, int n, int n_params, const char *const *names, con
                 }
         }
         sfhp.resize((size_t)SFH_NCOL * n);
-        const int ids[SFH_NCOL] = {PF_TAGE, PF_TAU, PF_CONST, PF_FBURST, PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_LOGZSOL};
+        const int ids[SFH_NCOL] = {PF_TAGE, PF_TAU, PF_CONST, PF_FBURST, PF_TBURST, PF_SF_START, PF_SF_TRUNC,
+                                   PF_SF_SLOPE, PF_LOGZSOL};
         for (int m = 0; m < n; ++m)
             for (int k = 0; k < SFH_NCOL; ++k) sfhp[(size_t)SFH_NCOL * m + k] = rows[(size_t)PF_COUNT * m + ids[k]];
     }

@@ -25,7 +25,7 @@ enum ParamId {
     PAR_DEVICE,                  // = 13: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
     PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
-    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU,
+    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU, PF_SF_SLOPE,
     PF_COUNT
 };
 

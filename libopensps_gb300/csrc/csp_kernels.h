@@ -261,12 +261,13 @@ struct AdjointArgs {
 };
 cudaError_t run_adjoint(const AdjointPrepArgs &pa, const AdjointArgs &a, cudaStream_t st);
 
-// SFH weights (sfh.cu). Per-model FP64 columns: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr), logzsol.
-enum { SFH_TAGE = 0, SFH_TAU, SFH_CONST, SFH_FBURST, SFH_TBURST, SFH_SF_START, SFH_SF_TRUNC, SFH_NPAR = 7,
-       SFH_LOGZSOL = 7, SFH_NCOL = 8 };
+// SFH weights (sfh.cu). Per-model FP64 columns: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr),
+// sf_slope (per Gyr), logzsol.
+enum { SFH_TAGE = 0, SFH_TAU, SFH_CONST, SFH_FBURST, SFH_TBURST, SFH_SF_START, SFH_SF_TRUNC, SFH_SF_SLOPE,
+       SFH_NPAR = 8, SFH_LOGZSOL = 8, SFH_NCOL = 9 };
 // their params_bar rows (opensps.h)
 enum { PB_LOGZSOL = 15, PB_TAGE = 16, PB_TAU = 17, PB_CONST = 18, PB_FBURST = 19, PB_TBURST = 20, PB_SF_START = 21,
-       PB_SF_TRUNC = 24, PB_IMF1 = 26 };
+       PB_SF_TRUNC = 24, PB_SF_SLOPE = 25, PB_IMF1 = 26 };
 struct SfhArgs {
     int n, nt, nz, sfh, itesc;
     const double *tf;        // nt: log10(age / yr) of the grid
@@ -279,8 +280,8 @@ struct SfhArgs {
     double *wz;              // n x nt x nz: the weights over ages and metallicities
     double *lblend;          // n x 3: log-blended L_bol (total, young, old)
     double *sfr;             // n, or null
-    double2 *mtab = nullptr; // n x nt: the main component's moments at the grid ages (sfh 1, 4; null: formed
-                             // serially per model)
+    double2 *mtab = nullptr; // n x nt: the main component's moments at the grid ages (sfh 1, 4, and 5's delayed
+                             // tau; null: formed serially per model)
 };
 cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st);
 struct SfhRevArgs {

@@ -1,12 +1,14 @@
 // SFH weights on the device, one thread per model in FP64 (OpenSPS batch_sfh_weights → sfh_weights_core,
-// src/physics/opensps_csp_batch.f90:1865-1917, src/physics/opensps_sfh.f90:1077-1160, compute_ssp_weights :97-257):
+// src/physics/opensps_csp_batch.f90:1865-1917, src/physics/opensps_sfh.f90:1077-1212, compute_ssp_weights :97-257):
 // the mass formed against the hat kernel of each grid age for SFH types 0 (SSP), 1 (tau) and 4 (delayed tau), with
-// the constant and burst components, normalised to one solar mass formed. Then the models' metallicity blend at
-// logzsol into the weights over ages and metallicities, the log-blended L_bol (model_sums MSUMS_BLEND :2129-2176) and
-// the current SFR (get_sfh_properties_at_age :281-486 over the mass fraction, batch_model_indices :1558-1567).
+// the constant and burst components, normalised to one solar mass formed, and 5 (Simha: the delayed tau up to the
+// truncation, then a linear ramp from its SFR there, the two normalised apart and mixed by the ramp's mass fraction).
+// Then the models' metallicity blend at logzsol into the weights over ages and metallicities, the log-blended L_bol
+// (model_sums MSUMS_BLEND :2129-2176) and the current SFR (get_sfh_properties_at_age :281-486 over the mass fraction,
+// batch_model_indices :1558-1567).
 //
-// The weights are written once as templates over the scalar type: double for the forward, Dual (value and seven
-// derivatives: tage, tau, const, fburst, tburst, sf_start, sf_trunc) for the tangents of the reverse pass
+// The weights are written once as templates over the scalar type: double for the forward, Dual (value and eight
+// derivatives: tage, tau, const, fburst, tburst, sf_start, sf_trunc, sf_slope) for the tangents of the reverse pass
 // (sfh_weights_tangent, src/physics/opensps_sfh_tangent.f90:61-198, forward mode; d Ei(x)/dx = e^x / x).
 #include <cuda_runtime.h>
 #include <cmath>
@@ -75,6 +77,13 @@ __device__ __forceinline__ Dual operator*(const Dual &a, double b) {
 }
 __device__ __forceinline__ Dual operator*(double b, const Dual &a) { return a * b; }
 __device__ __forceinline__ Dual operator/(const Dual &a, double b) { return a * (1.0 / b); }
+__device__ __forceinline__ Dual operator/(double a, const Dual &b) {
+    Dual r; r.v = a / b.v;
+    const double q = -r.v / b.v;
+#pragma unroll
+    for (int i = 0; i < SFH_NPAR; ++i) r.d[i] = q * b.d[i];
+    return r;
+}
 
 __device__ __forceinline__ double val(double x) { return x; }
 __device__ __forceinline__ double val(const Dual &x) { return x.v; }
@@ -91,6 +100,7 @@ __device__ __forceinline__ Dual chain(const Dual &x, double f, double df) {
     return r;
 }
 template <class T> __device__ __forceinline__ T sexp(const T &x) { const double e = exp(val(x)); return chain(x, e, e); }
+template <class T> __device__ __forceinline__ T sexpm1(const T &x) { return chain(x, expm1(val(x)), exp(val(x))); }
 template <class T> __device__ __forceinline__ T spow10(const T &x) {
     const double e = pow(10.0, val(x));
     return chain(x, e, e * SFH_LN10);
@@ -138,9 +148,38 @@ template <class T> __device__ __forceinline__ T sexpi(const T &x, bool &finite) 
 // ---------------------------------------------------------------------------------------------- the weights
 template <class T>
 struct SfhT {
-    int type;         // -1 burst, 0 constant, 1 tau, 4 delayed tau
+    int type;         // -1 burst, 0 constant, 1 tau, 4 delayed tau, 5 linear ramp
     T tage, tau, tb, tq;
+    T trunc, slope, t0;   // the truncation (years after the start), the ramp's slope in lookback time (per year), the
+                          // lookback time where the ramp reaches zero (0: none)
+    int simha;            // 1: the ramp's window [t0, tq], else [tq, tage]
 };
+
+// convert_sfhparams_pc (src/physics/opensps_sfh.f90:1306-1360): years, lookback times from the start of star
+// formation (sf_start for sfh 1, 4, 5).
+template <class T>
+__device__ __forceinline__ void sfh_setup(int sfh, const T *p, SfhT<T> &s) {
+    const T start = (sfh == 1 || sfh == 4 || sfh == 5) ? p[SFH_SF_START] * 1.0e9 : lift<T>(0.0);
+    s.tage = p[SFH_TAGE] * 1.0e9 - start;
+    const T tburst = p[SFH_TBURST] * 1.0e9 - start;
+    s.trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
+    s.tau = p[SFH_TAU] * 1.0e9;
+    s.slope = p[SFH_SF_SLOPE] * -1.0e-9;
+    s.tb = s.tage - tburst;
+    s.tq = (val(s.trunc) <= 0.0 || val(s.trunc) > val(s.tage)) ? lift<T>(0.0) : s.tage - s.trunc;
+    s.t0 = val(s.slope) > SAFE_FLOOR ? s.tq - 1.0 / s.slope : lift<T>(0.0);
+    if (val(s.t0) > val(s.tq) || val(s.t0) <= 0.0) s.t0 = lift<T>(0.0);
+    s.simha = 0;
+}
+
+// The integration window in log10 lookback years (clamp_integration_limits, src/physics/opensps_sfh.f90:969-1010,
+// tiny_logt = 0).
+template <class T>
+__device__ __forceinline__ void sfh_window(const SfhT<T> &s, T &lts, T &lte) {
+    const T one = lift<T>(1.0);
+    lts = slog10(smax(s.simha ? s.t0 : s.tq, one));
+    lte = slog10(smax(s.simha ? s.tq : s.tage, one));
+}
 
 // eval_indefinite_moments_log (src/physics/opensps_sfh.f90:852-905): M0 = int SFR dt, M1 = int SFR log10(t) dt
 template <class T>
@@ -167,6 +206,13 @@ __device__ void moments_log(const T &log_t, const SfhT<T> &s, T &m0, T &m1) {
         }
         return;
     }
+    if (s.type == 5) {   // SFR = 1 + slope (t - t'), t' = max(0, tage - trunc)
+        const T f = 1.0 - s.slope * smax(lift<T>(0.0), s.tage - s.trunc);
+        const T h = 0.5 * s.slope * t * t;
+        m0 = f * t + h;
+        m1 = f * t * (log_t - SFH_LOG_E) + h * (log_t - 0.5 * SFH_LOG_E);
+        return;
+    }
     m0 = lift<T>(0.0);
     m1 = lift<T>(0.0);
 }
@@ -187,7 +233,7 @@ __device__ __forceinline__ void moments_at(const T &lim, int j, const double *tf
 }
 
 template <class T>
-__device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_min, int idx_max, T *w, int ws,
+__device__ __forceinline__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_min, int idx_max, T *w, int ws,
                             const double2 *mtab = nullptr) {
     const double tiny_logt = 0.0;
     if (s.type == -1) {
@@ -201,8 +247,8 @@ __device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_
         w[j * ws] = w[j * ws] + (log_tb - tf[j - 1]) / dt;
         return;
     }
-    const T lmin = lift<T>(pow(10.0, tiny_logt));
-    const T lts = slog10(smax(s.tq, lmin)), lte = slog10(smax(s.tage, lmin));
+    T lts, lte;
+    sfh_window(s, lts, lte);
     int js = find_interval0(tf, nt, val(lts)) + 1;
     int je = find_interval0(tf, nt, val(lte)) + 2;
     const int lo_bound = idx_min > 1 ? idx_min : 1, hi_bound = idx_max < nt - 1 ? idx_max : nt - 1;
@@ -235,26 +281,108 @@ __device__ void ssp_weights(const double *tf, int nt, const SfhT<T> &s, int idx_
     }
 }
 
-// sfh_weights_core_pc for one metallicity (src/physics/opensps_sfh.f90:1077-1160; convert_sfhparams_pc :1306-1360).
-// p: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr). w, t1, t2: nt entries at stride ws, zeroed here.
+// The regularised lower incomplete gamma function of power 1 or 2 (gammainc, src/math/opensps_special_functions.f90:
+// 142-170); 0 below 0.
 template <class T>
-__device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, T *w, T *t1, T *t2, int ws,
+__device__ __forceinline__ T gammainc12(bool one, const T &x) {
+    if (val(x) < 0.0) return lift<T>(0.0);
+    const T g = -sexpm1(-x);
+    return one ? g : g - x * sexp(-x);
+}
+
+// get_sfh_properties_at_age_pc at tage (src/physics/opensps_sfh.f90:281-486, Gyr; sfh 0, 1, 4, 5): the mass fraction
+// formed, the normalised SFR (per Gyr) and, for sfh 5, the fraction of the mass formed by tage that formed on the ramp.
+template <class T>
+__device__ __forceinline__ void sfh_props(const double *tf, int nt, int sfh, const T *p, T &mass_frac, T &sfr, T &frac_linear) {
+    mass_frac = lift<T>(1.0);
+    sfr = lift<T>(0.0);
+    frac_linear = lift<T>(0.0);
+    if (sfh != 1 && sfh != 4 && sfh != 5) return;
+    const T tau = p[SFH_TAU], start = p[SFH_SF_START], trunc = p[SFH_SF_TRUNC];
+    const T t_max = pow(10.0, tf[nt - 1] - 9.0) - start;
+    const T t_prime = p[SFH_TAGE] - start;
+    const T t_trunc = (val(trunc) < SAFE_FLOOR || val(trunc) < val(start)) ? t_max : trunc - start;
+    const T tau_g = smax(tau, lift<T>(SAFE_FLOOR));
+    const bool one = sfh == 1;
+    const T total = tau_g * gammainc12(one, smin(t_max, t_trunc) / tau_g);
+    T mass_tau = lift<T>(0.0), sfr_tau = lift<T>(0.0);
+    if (val(t_prime) >= 0.0) {
+        const T r = smin(t_prime, t_trunc) / tau_g;
+        mass_tau = tau_g * gammainc12(one, r);
+        sfr_tau = (one ? lift<T>(1.0) : r) * sexp(-r);
+    }
+    if (sfh != 5) {
+        const T cst = p[SFH_CONST], fburst = p[SFH_FBURST];
+        const double mfrac_burst = (val(t_prime) > val(p[SFH_TBURST]) - val(start)) ? 1.0 : 0.0;
+        T sfr_const = lift<T>(0.0), mass_const = lift<T>(0.0);
+        if (val(t_prime) > 0.0) {
+            sfr_const = 1.0 / smin(t_max, t_trunc);
+            mass_const = smax(smin(t_prime, t_trunc), lift<T>(0.0)) * sfr_const;
+        }
+        const T norm = 1.0 - cst - fburst;
+        mass_frac = norm * mass_tau / total + cst * mass_const + fburst * mfrac_burst;
+        sfr = (val(t_prime) > val(t_trunc)) ? lift<T>(0.0) : norm * sfr_tau / total + cst * sfr_const;
+        return;
+    }
+    // the ramp after the truncation: SFR = sfr_tr (1 - k (t - t_tr)), k = -sf_slope, from the delayed tau's SFR at
+    // t_tr, down to its zero t_tr + 1 / k
+    const T k = -p[SFH_SF_SLOPE];
+    const T t_zero = val(k) > 0.0 ? t_trunc + 1.0 / k : t_max;
+    T total_lin = lift<T>(0.0), mass_lin = lift<T>(0.0);
+    if (val(t_trunc) <= 0.0 || val(t_trunc) > val(t_max)) {
+        sfr = sfr_tau / total;
+    } else {
+        const T sfr_tr = (t_trunc / tau) * sexp(-(t_trunc / tau));
+        T hi = smin(t_zero, t_max);
+        total_lin = sfr_tr * ((hi - t_trunc) - 0.5 * k * (hi * hi + t_trunc * t_trunc) + k * hi * t_trunc);
+        if (val(t_prime) <= val(t_trunc)) {
+            sfr = sfr_tau / (total + total_lin);
+        } else {
+            hi = smin(t_zero, t_prime);
+            mass_lin = sfr_tr * ((hi - t_trunc) - 0.5 * k * (hi * hi + t_trunc * t_trunc) + k * hi * t_trunc);
+            sfr = smax(sfr_tr * (1.0 - k * (t_prime - t_trunc)), lift<T>(0.0)) / (total + total_lin);
+        }
+    }
+    if (val(t_prime) >= 0.0) {
+        mass_frac = (mass_tau + mass_lin) / (total + total_lin);
+        if (val(mass_lin) + val(mass_tau) > SAFE_FLOOR) frac_linear = mass_lin / (mass_lin + mass_tau);
+    } else {
+        mass_frac = lift<T>(0.0);
+        sfr = lift<T>(0.0);
+    }
+}
+
+// sfh_weights_core_pc for one metallicity (src/physics/opensps_sfh.f90:1077-1212; convert_sfhparams_pc :1306-1360).
+// p: tage, tau, const, fburst, tburst, sf_start, sf_trunc (Gyr), sf_slope (per Gyr). w, t1, t2: nt entries at stride
+// ws, zeroed here.
+template <class T>
+__device__ __forceinline__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, T *w, T *t1, T *t2, int ws,
                                  const double2 *mtab = nullptr) {
     for (int i = 0; i < nt; ++i) { w[i * ws] = lift<T>(0.0); t1[i * ws] = lift<T>(0.0); t2[i * ws] = lift<T>(0.0); }
     SfhT<T> s;
-    const T start = (sfh == 1 || sfh == 4) ? p[SFH_SF_START] * 1.0e9 : lift<T>(0.0);
-    s.tage = p[SFH_TAGE] * 1.0e9 - start;
-    const T tburst = p[SFH_TBURST] * 1.0e9 - start;
-    const T trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
-    s.tau = p[SFH_TAU] * 1.0e9;
-    s.tb = s.tage - tburst;
-    s.tq = (val(trunc) <= 0.0 || val(trunc) > val(s.tage)) ? lift<T>(0.0) : s.tage - trunc;
+    sfh_setup(sfh, p, s);
     int imax = find_interval0(tf, nt, log10(val(s.tage))) + 1 + 2;
     imax = imax < 1 ? 1 : (imax > nt ? nt : imax);
     if (sfh == 0) {
         s.type = -1;
         s.tb = s.tage;
         ssp_weights(tf, nt, s, imax - 2 > 1 ? imax - 2 : 1, imax, w, ws);
+        return;
+    }
+    if (sfh == 5) {
+        s.type = 4;
+        ssp_weights(tf, nt, s, 0, imax, t1, ws, mtab);
+        s.type = 5;
+        s.simha = 1;
+        ssp_weights(tf, nt, s, 0, imax, t2, ws);
+        T mass1 = lift<T>(0.0), mass2 = lift<T>(0.0);
+        for (int i = 0; i < imax; ++i) { mass1 = mass1 + t1[i * ws]; mass2 = mass2 + t2[i * ws]; }
+        if (val(mass1) < SAFE_FLOOR) mass1 = lift<T>(1.0);
+        if (val(mass2) < SAFE_FLOOR) mass2 = lift<T>(1.0);
+        T mf, sfr, fl;
+        sfh_props(tf, nt, sfh, p, mf, sfr, fl);
+        const T a = (1.0 - fl) / mass1, b = fl / mass2;
+        for (int i = 0; i < nt; ++i) w[i * ws] = t1[i * ws] * a + t2[i * ws] * b;
         return;
     }
     s.type = sfh;
@@ -281,35 +409,10 @@ __device__ void sfh_weights_core(const double *tf, int nt, int sfh, const T *p, 
     }
 }
 
-// The current SFR per unit mass formed over the mass fraction formed by tage (per yr), sfh 0, 1, 4.
+// The current SFR per unit mass formed over the mass fraction formed by tage (per yr).
 __device__ double sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
-    double mass_frac = 1.0, sfr = 0.0;
-    if (sfh == 1 || sfh == 4) {
-        const double tage = p[SFH_TAGE], tau = p[SFH_TAU], cst = p[SFH_CONST], fburst = p[SFH_FBURST];
-        const double tburst = p[SFH_TBURST], start = p[SFH_SF_START], trunc = p[SFH_SF_TRUNC];
-        const double t_max = pow(10.0, tf[nt - 1] - 9.0) - start;
-        const double t_prime = tage - start;
-        const double t_trunc = (trunc < SAFE_FLOOR || trunc < start) ? t_max : trunc - start;
-        const double tau_g = fmax(tau, SAFE_FLOOR);
-        const bool one = sfh == 1;
-        const double rt = fmin(t_max, t_trunc) / tau_g;
-        const double total = tau_g * (one ? -expm1(-rt) : -expm1(-rt) - rt * exp(-rt));
-        double mass_tau = 0.0, sfr_tau = 0.0;
-        if (t_prime >= 0.0) {
-            const double r = fmin(t_prime, t_trunc) / tau_g;
-            mass_tau = tau_g * (one ? -expm1(-r) : -expm1(-r) - r * exp(-r));
-            sfr_tau = (one ? 1.0 : r) * exp(-r);
-        }
-        const double mfrac_burst = (t_prime > tburst - start) ? 1.0 : 0.0;
-        double sfr_const = 0.0, mass_const = 0.0;
-        if (t_prime > 0.0) {
-            sfr_const = 1.0 / fmin(t_max, t_trunc);
-            mass_const = fmax(fmin(t_prime, t_trunc), 0.0) * sfr_const;
-        }
-        const double norm = 1.0 - cst - fburst;
-        mass_frac = norm * mass_tau / total + cst * mass_const + fburst * mfrac_burst;
-        sfr = (t_prime > t_trunc) ? 0.0 : norm * sfr_tau / total + cst * sfr_const;
-    }
+    double mass_frac, sfr, fl;
+    sfh_props(tf, nt, sfh, p, mass_frac, sfr, fl);
     sfr /= 1.0e9;
     if (mass_frac > SAFE_FLOOR) sfr /= mass_frac;
     return sfr;
@@ -324,22 +427,19 @@ __device__ __forceinline__ void zinterval(const double *lz, int nz, double x, in
     dz = (x - lz[zlo]) / (lz[zlo + 1] - lz[zlo]);
 }
 
-// One thread per (model, grid age): the main component's moments (sfh 1, 4) at the grid ages strictly inside the
-// model's [log t_start, log t_age], the SFH set up as sfh_weights_core sets it, for sfh_forward_kernel's table.
+// One thread per (model, grid age): the main component's moments (sfh 1, 4; the delayed tau of sfh 5) at the grid
+// ages strictly inside the model's [log t_start, log t_age], the SFH set up as sfh_weights_core sets it, for
+// sfh_forward_kernel's table.
 __global__ void __launch_bounds__(128) sfh_moments_kernel(SfhArgs a) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (size_t)a.n * a.nt) return;
     const int m = (int)(i / a.nt), j = (int)(i % a.nt);
     const double *p = a.par + (size_t)SFH_NCOL * m;
     SfhT<double> s;
-    const double start = p[SFH_SF_START] * 1.0e9;
-    s.type = a.sfh;
-    s.tage = p[SFH_TAGE] * 1.0e9 - start;
-    s.tau = p[SFH_TAU] * 1.0e9;
-    const double trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
-    s.tq = (trunc <= 0.0 || trunc > s.tage) ? 0.0 : s.tage - trunc;
-    s.tb = 0.0;
-    const double lts = log10(fmax(s.tq, 1.0)), lte = log10(fmax(s.tage, 1.0));
+    sfh_setup(a.sfh, p, s);
+    s.type = a.sfh == 5 ? 4 : a.sfh;
+    double lts, lte;
+    sfh_window(s, lts, lte);
     const double x = a.tf[j];
     double2 r = make_double2(0.0, 0.0);
     if (x > lts && x < lte) moments_log(x, s, r.x, r.y);
@@ -371,7 +471,8 @@ __device__ void warp_component(const double *tf, int nt, const SfhT<double> &s, 
         __syncwarp();
         return;
     }
-    const double lts = log10(fmax(s.tq, 1.0)), lte = log10(fmax(s.tage, 1.0));
+    double lts, lte;
+    sfh_window(s, lts, lte);
     int js = find_interval0(tf, nt, lts) + 1;
     int je = find_interval0(tf, nt, lte) + 2;
     const int lo_bound = idx_min > 1 ? idx_min : 1, hi_bound = idx_max < nt - 1 ? idx_max : nt - 1;
@@ -448,19 +549,31 @@ __global__ void __launch_bounds__(SFH_WARPS * 32) sfh_forward_kernel(SfhArgs a) 
     } else {
         const int sfh = a.sfh;
         SfhT<double> s;
-        const double start = (sfh == 1 || sfh == 4) ? p[SFH_SF_START] * 1.0e9 : 0.0;
-        s.tage = p[SFH_TAGE] * 1.0e9 - start;
-        const double tburst = p[SFH_TBURST] * 1.0e9 - start;
-        const double trunc = p[SFH_SF_TRUNC] * 1.0e9 - start;
-        s.tau = p[SFH_TAU] * 1.0e9;
-        s.tb = s.tage - tburst;
-        s.tq = (trunc <= 0.0 || trunc > s.tage) ? 0.0 : s.tage - trunc;
+        sfh_setup(sfh, p, s);
         int imax = find_interval0(a.tf, nt, log10(s.tage)) + 1 + 2;
         imax = imax < 1 ? 1 : (imax > nt ? nt : imax);
         if (sfh == 0) {
             s.type = -1;
             s.tb = s.tage;
             warp_component(a.tf, nt, s, imax - 2 > 1 ? imax - 2 : 1, imax, nullptr, M0s, M1s, w, lane);
+        } else if (sfh == 5) {
+            // the delayed tau over [tq, tage] and the ramp over [t0, tq], each normalised, mixed by the ramp's
+            // mass fraction at tage
+            s.type = 4;
+            warp_component(a.tf, nt, s, 0, imax, a.mtab ? a.mtab + (size_t)nt * m : nullptr, M0s, M1s, t1, lane);
+            s.type = 5;
+            s.simha = 1;
+            warp_component(a.tf, nt, s, 0, imax, nullptr, M0s, M1s, t2, lane);
+            double p1 = 0.0, p2 = 0.0;
+            for (int i = lane; i < imax; i += 32) { p1 += t1[i]; p2 += t2[i]; }
+            double mass1 = warp_sum(p1), mass2 = warp_sum(p2);
+            if (mass1 < SAFE_FLOOR) mass1 = 1.0;
+            if (mass2 < SAFE_FLOOR) mass2 = 1.0;
+            double mf, sfr, fl;
+            sfh_props(a.tf, nt, sfh, p, mf, sfr, fl);
+            const double ca = (1.0 - fl) / mass1, cb = fl / mass2;
+            for (int i = lane; i < nt; i += 32) w[i] = t1[i] * ca + t2[i] * cb;
+            __syncwarp();
         } else {
             s.type = sfh;
             warp_component(a.tf, nt, s, 0, imax, a.mtab ? a.mtab + (size_t)nt * m : nullptr, M0s, M1s, w, lane);
@@ -548,7 +661,7 @@ cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st) {
     cudaError_t e = sfh_init_tables(st);
     if (e != cudaSuccess) return e;
     SfhArgs b = a;
-    if (a.given || (a.sfh != 1 && a.sfh != 4)) b.mtab = nullptr;
+    if (a.given || (a.sfh != 1 && a.sfh != 4 && a.sfh != 5)) b.mtab = nullptr;
     if (b.mtab) {
         const size_t tot = (size_t)a.n * a.nt;
         sfh_moments_kernel<<<(unsigned)((tot + 127) / 128), 128, 0, st>>>(b);
@@ -594,7 +707,7 @@ __global__ void __launch_bounds__(64) sfh_reverse_kernel(SfhRevArgs a) {
     double *pb = a.params_bar + (size_t)a.rows * m;
     pb[PB_LOGZSOL] = a.has_logzsol ? gz / (a.lz[zlo + 1] - a.lz[zlo]) : 0.0;
     if (!a.sfh_tangents) return;
-    // the tangents of the weights (all seven directions in one pass)
+    // the tangents of the weights (all eight directions in one pass)
     Dual pd[SFH_NPAR];
 #pragma unroll
     for (int i = 0; i < SFH_NPAR; ++i) {
@@ -611,7 +724,7 @@ __global__ void __launch_bounds__(64) sfh_reverse_kernel(SfhRevArgs a) {
 #pragma unroll
         for (int i = 0; i < SFH_NPAR; ++i) acc[i] += g * dw[t].d[i];
     }
-    const int row[SFH_NPAR] = {PB_TAGE, PB_TAU, PB_CONST, PB_FBURST, PB_TBURST, PB_SF_START, PB_SF_TRUNC};
+    const int row[SFH_NPAR] = {PB_TAGE, PB_TAU, PB_CONST, PB_FBURST, PB_TBURST, PB_SF_START, PB_SF_TRUNC, PB_SF_SLOPE};
 #pragma unroll
     for (int i = 0; i < SFH_NPAR; ++i) pb[row[i]] = acc[i];
 }

@@ -89,7 +89,9 @@ def lib() -> C.CDLL:
         _lib.oracle_observed_frame.argtypes = [C.c_int, _dp, C.c_double, _dp, _dp]
         _lib.oracle_band_fluxes.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         _lib.oracle_ssp_weights_raw.argtypes = [_dp, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double,
-                                                C.c_double, C.c_double, C.c_int, C.c_int, _dp]
+                                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                C.c_int, C.c_int, C.c_int, _dp]
+        _lib.oracle_sfh_props.argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_double, _dp]
     return _lib
 
 
@@ -97,14 +99,14 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
-SFH_NAMES = ("tage", "tau", "const", "fburst", "tburst", "sf_start", "sf_trunc")
+SFH_NAMES = ("tage", "tau", "const", "fburst", "tburst", "sf_start", "sf_trunc", "sf_slope")
 SFH_DEFAULTS = {"tage": 0.0, "tau": 1.0, "const": 0.0, "fburst": 0.0, "tburst": 11.0, "sf_start": 0.0,
-                "sf_trunc": 0.0}
+                "sf_trunc": 0.0, "sf_slope": 0.0}
 
 
 def sfh_weights(log_age: np.ndarray, sfh: int, params: dict, n: int):
-    """The SFH weights over the ages (n, nt) and the current SFR per unit mass formed (n,) of SFH type sfh (0, 1, 4)
-    for per-model parameters (sfh_oracle.c)."""
+    """The SFH weights over the ages (n, nt) and the current SFR per unit mass formed (n,) of SFH type sfh (0, 1, 4,
+    5) for per-model parameters (sfh_oracle.c)."""
     tf = np.ascontiguousarray(log_age, dtype=np.float64)
     p = np.empty((n, len(SFH_NAMES)))
     for i, k in enumerate(SFH_NAMES):
@@ -169,13 +171,26 @@ def band_fluxes(bands: np.ndarray, jlo, jhi, do_band, wt: np.ndarray | None, lam
 
 
 def ssp_weights_raw(log_t: np.ndarray, sfh_type: int, tage: float, tau: float, idx_min: int, idx_max: int,
-                    tiny_logt: float = 0.0, tq: float = 0.0, tb: float = 0.0) -> np.ndarray:
-    """compute_ssp_weights alone: the hat-kernel mass of SFH type -1/0/1/4 (times in years) on the log-age nodes."""
+                    tiny_logt: float = 0.0, tq: float = 0.0, tb: float = 0.0, trunc: float = 0.0, slope: float = 0.0,
+                    t0: float = 0.0, simha: bool = False) -> np.ndarray:
+    """compute_ssp_weights alone: the hat-kernel mass of SFH type -1/0/1/4/5 (times in years, slope per year in
+    lookback time; simha integrates over [t0, tq]) on the log-age nodes."""
     tf = np.ascontiguousarray(log_t, dtype=np.float64)
     w = np.empty(tf.size)
     lib().oracle_ssp_weights_raw(_p(tf), tf.size, float(tiny_logt), int(sfh_type), float(tage), float(tau), float(tq),
-                                 float(tb), int(idx_min), int(idx_max), _p(w))
+                                 float(tb), float(trunc), float(slope), float(t0), int(bool(simha)), int(idx_min),
+                                 int(idx_max), _p(w))
     return w
+
+
+def sfh_properties(log_age: np.ndarray, sfh: int, params: dict, age: float):
+    """get_sfh_properties_at_age at age (Gyr) for one model: the mass fraction formed, the normalised SFR (per Gyr,
+    before the unit change and the division by the mass fraction) and the linear (ramp) mass fraction of sfh 5."""
+    tf = np.ascontiguousarray(log_age, dtype=np.float64)
+    p = np.array([float(params.get(k, SFH_DEFAULTS[k])) for k in SFH_NAMES])
+    out = np.empty(3)
+    lib().oracle_sfh_props(_p(tf), tf.size, int(sfh), _p(p), float(age), _p(out))
+    return float(out[0]), float(out[1]), float(out[2])
 
 
 def smooth_velocity_direct(lam: np.ndarray, spec: np.ndarray, sigma: float, minl: float, maxl: float) -> np.ndarray:

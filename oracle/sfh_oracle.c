@@ -5,10 +5,13 @@
  *   expi                       src/math/opensps_special_functions.f90:62-122
  *   gammainc (powers 1, 2)     src/math/opensps_special_functions.f90:142-170
  *   convert_sfhparams_pc       src/physics/opensps_sfh.f90:1306-1360
- *   eval_indefinite_moments_log (types 0, 1, 4)  src/physics/opensps_sfh.f90:852-905
- *   compute_ssp_weights        src/physics/opensps_sfh.f90:97-257 (log-age interpolation, interpolation_type 0)
- *   sfh_weights_core_pc        src/physics/opensps_sfh.f90:1077-1160 (sfh 0, 1, 4 with const / burst)
- *   get_sfh_properties_at_age_pc  src/physics/opensps_sfh.f90:281-486 (sfh 0, 1, 4), as batch_model_indices
+ *   eval_indefinite_moments_log (types 0, 1, 4, 5)  src/physics/opensps_sfh.f90:852-905
+ *   compute_ssp_weights        src/physics/opensps_sfh.f90:97-257 (log-age interpolation, interpolation_type 0; the
+ *                              Simha window [t0, tq] of clamp_integration_limits :969-1010)
+ *   sfh_weights_core_pc        src/physics/opensps_sfh.f90:1077-1212 (sfh 0, 1, 4 with const / burst; sfh 5, the
+ *                              delayed tau before the truncation and the linear ramp after it, mixed by the linear
+ *                              mass fraction)
+ *   get_sfh_properties_at_age_pc  src/physics/opensps_sfh.f90:281-486 (sfh 0, 1, 4, 5), as batch_model_indices
  *                              src/physics/opensps_csp_batch.f90:1558-1567 divides it by the mass fraction
  *
  * Times: time_full = log10(age / yr) of the SSP grid (ascending), tiny_logt = 0 (the context default), years in
@@ -56,8 +59,11 @@ static double gammainc12(int power, double x) {
 }
 
 typedef struct {
-    int type;                  /* -1 burst, 0 constant, 1 tau, 4 delayed tau */
+    int type;                  /* -1 burst, 0 constant, 1 tau, 4 delayed tau, 5 linear ramp (Simha) */
     double tage, tau, tb, tq;  /* years (lookback) */
+    double trunc, slope, t0;   /* the truncation (years after the start), the ramp's slope in lookback time (per
+                                  year), the lookback time where the ramp reaches zero (0: none) */
+    int simha;                 /* 1: integrate over [t0, tq] (the ramp), else over [tq, tage] */
 } sfh_t;
 
 /* Indefinite moments in log10 time: M0 = int SFR dt, M1 = int SFR log10(t) dt. */
@@ -86,6 +92,13 @@ static void moments_log(double log_t, const sfh_t *s, double *m0, double *m1) {
         *m1 = -((t - s->tage - s->tau) * log_t - s->tau * LOG_E) * exp(tt) - (s->tage + s->tau) * LOG_E * ei;
         return;
     }
+    case 5: {
+        /* SFR = 1 + slope (t - t'), t' = max(0, tage - trunc): M0 and M1 of the linear function */
+        const double tp = fmax(0.0, s->tage - s->trunc), f = 1.0 - s->slope * tp, h = 0.5 * s->slope * t * t;
+        *m0 = f * t + h;
+        *m1 = f * t * (log_t - LOG_E) + h * (log_t - 0.5 * LOG_E);
+        return;
+    }
     default:
         *m0 = 0.0;
         *m1 = 0.0;
@@ -109,7 +122,7 @@ static void ssp_weights(const double *tf, int nt, double tiny_logt, const sfh_t 
         return;
     }
     const double lmin = pow(10.0, tiny_logt);
-    const double lts = log10(fmax(s->tq, lmin)), lte = log10(fmax(s->tage, lmin));
+    const double lts = log10(fmax(s->simha ? s->t0 : s->tq, lmin)), lte = log10(fmax(s->simha ? s->tq : s->tage, lmin));
     int js = oracle_find_interval(tf, nt, lts);
     int je = oracle_find_interval(tf, nt, lte) + 1;
     const int lo_bound = idx_min > 1 ? idx_min : 1, hi_bound = idx_max < nt - 1 ? idx_max : nt - 1;
@@ -142,31 +155,47 @@ static void ssp_weights(const double *tf, int nt, double tiny_logt, const sfh_t 
     }
 }
 
-/* compute_ssp_weights alone (tests): SFH type -1 (burst), 0, 1 or 4 with times in years (tage, tau, tq the truncation
- * lookback, tb the burst lookback), the 1-based index range idx_min .. idx_max and tiny_logt; w has nt entries. */
+/* compute_ssp_weights alone (tests): SFH type -1 (burst), 0, 1, 4 or 5 with times in years (tage, tau, tq the
+ * truncation lookback, tb the burst lookback; for type 5 trunc, slope per year in lookback time, t0 and the window
+ * flag simha), the 1-based index range idx_min .. idx_max and tiny_logt; w has nt entries. */
 void oracle_ssp_weights_raw(const double *tf, int nt, double tiny_logt, int type, double tage, double tau, double tq,
-                            double tb, int idx_min, int idx_max, double *w) {
+                            double tb, double trunc, double slope, double t0, int simha, int idx_min, int idx_max,
+                            double *w) {
     sfh_t s;
     s.type = type;
     s.tage = tage;
     s.tau = tau;
     s.tq = tq;
     s.tb = tb;
+    s.trunc = trunc;
+    s.slope = slope;
+    s.t0 = t0;
+    s.simha = simha;
     ssp_weights(tf, nt, tiny_logt, &s, idx_min, idx_max, w);
 }
 
-/* SFH parameters per model, in this order (Gyr where timed): tage, tau, const, fburst, tburst, sf_start, sf_trunc. */
-enum { SP_TAGE = 0, SP_TAU, SP_CONST, SP_FBURST, SP_TBURST, SP_SF_START, SP_SF_TRUNC, SP_COUNT };
+/* SFH parameters per model, in this order (Gyr where timed): tage, tau, const, fburst, tburst, sf_start, sf_trunc,
+   sf_slope (per Gyr). */
+enum { SP_TAGE = 0, SP_TAU, SP_CONST, SP_FBURST, SP_TBURST, SP_SF_START, SP_SF_TRUNC, SP_SF_SLOPE, SP_COUNT };
 
 static void convert(int sfh, const double *p, sfh_t *s) {
     const double start = (sfh == 1 || sfh == 4 || sfh == 5) ? p[SP_SF_START] * 1.0e9 : 0.0;
     s->tage = p[SP_TAGE] * 1.0e9 - start;
     const double tburst = p[SP_TBURST] * 1.0e9 - start;
-    const double trunc = p[SP_SF_TRUNC] * 1.0e9 - start;
+    s->trunc = p[SP_SF_TRUNC] * 1.0e9 - start;
     s->tau = p[SP_TAU] * 1.0e9;
+    s->slope = -p[SP_SF_SLOPE] / 1.0e9;
     s->tb = s->tage - tburst;
-    s->tq = (trunc <= 0.0 || trunc > s->tage) ? 0.0 : s->tage - trunc;
+    s->tq = (s->trunc <= 0.0 || s->trunc > s->tage) ? 0.0 : s->tage - s->trunc;
+    s->t0 = s->slope > SAFE_FLOOR ? s->tq - 1.0 / s->slope : 0.0;
+    if (s->t0 > s->tq || s->t0 <= 0.0) s->t0 = 0.0;
+    s->simha = 0;
 }
+
+/* get_sfh_properties_at_age_pc (Gyr): the mass fraction formed by age, the SFR per unit mass formed (per Gyr) and,
+   for sfh 5, the fraction of the mass formed by age that formed on the ramp. */
+static void sfh_props(const double *tf, int nt, int sfh, const double *p, double age, double *mass_frac,
+                      double *sfr, double *frac_linear);
 
 /* sfh_weights_core_pc for one metallicity: w (nt) for SFH type sfh (0, 1 or 4) with the parameters p. */
 void oracle_sfh_weights(const double *tf, int nt, int sfh, const double *p, double *w, double *tmp1, double *tmp2) {
@@ -178,6 +207,21 @@ void oracle_sfh_weights(const double *tf, int nt, int sfh, const double *p, doub
         s.type = -1;
         s.tb = s.tage;
         ssp_weights(tf, nt, 0.0, &s, imax - 2 > 1 ? imax - 2 : 1, imax, w);
+        return;
+    }
+    if (sfh == 5) {
+        s.type = 4;
+        ssp_weights(tf, nt, 0.0, &s, 0, imax, tmp1);
+        s.type = 5;
+        s.simha = 1;
+        ssp_weights(tf, nt, 0.0, &s, 0, imax, tmp2);
+        double mass1 = 0.0, mass2 = 0.0;
+        for (int i = 0; i < imax; ++i) { mass1 += tmp1[i]; mass2 += tmp2[i]; }
+        if (mass1 < SAFE_FLOOR) mass1 = 1.0;
+        if (mass2 < SAFE_FLOOR) mass2 = 1.0;
+        double mf, sfr, fl;
+        sfh_props(tf, nt, sfh, p, p[SP_TAGE], &mf, &sfr, &fl);
+        for (int i = 0; i < nt; ++i) w[i] = tmp1[i] / mass1 * (1.0 - fl) + tmp2[i] / mass2 * fl;
         return;
     }
     s.type = sfh;
@@ -204,14 +248,14 @@ void oracle_sfh_weights(const double *tf, int nt, int sfh, const double *p, doub
     }
 }
 
-/* The current SFR per unit mass formed, normalised by the mass fraction formed by tage (per yr). */
-double oracle_sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
-    double mass_frac = 1.0, sfr = 0.0;
-    if (sfh == 1 || sfh == 4) {
-        const double tage = p[SP_TAGE], tau = p[SP_TAU], cst = p[SP_CONST], fburst = p[SP_FBURST];
+static void sfh_props(const double *tf, int nt, int sfh, const double *p, double age, double *mass_frac,
+                      double *sfr_out, double *frac_linear) {
+    double mass_frac_v = 1.0, sfr = 0.0, fl = 0.0;
+    if (sfh == 1 || sfh == 4 || sfh == 5) {
+        const double tau = p[SP_TAU], cst = p[SP_CONST], fburst = p[SP_FBURST];
         const double tburst = p[SP_TBURST], start = p[SP_SF_START], trunc = p[SP_SF_TRUNC];
         const double t_max = pow(10.0, tf[nt - 1] - 9.0) - start;
-        const double t_prime = tage - start;
+        const double t_prime = age - start;
         const double t_trunc = (trunc < SAFE_FLOOR || trunc < start) ? t_max : trunc - start;
         const double tau_g = fmax(tau, SAFE_FLOOR);
         const int pw = sfh == 1 ? 1 : 2;
@@ -222,16 +266,59 @@ double oracle_sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
             mass_tau = tau_g * gammainc12(pw, r);
             sfr_tau = (pw == 1 ? 1.0 : r) * exp(-r);
         }
-        const double mfrac_burst = (t_prime > tburst - start) ? 1.0 : 0.0;
-        double sfr_const = 0.0, mass_const = 0.0;
-        if (t_prime > 0.0) {
-            sfr_const = 1.0 / fmin(t_max, t_trunc);
-            mass_const = fmax(fmin(t_prime, t_trunc), 0.0) * sfr_const;
+        if (sfh != 5) {
+            const double mfrac_burst = (t_prime > tburst - start) ? 1.0 : 0.0;
+            double sfr_const = 0.0, mass_const = 0.0;
+            if (t_prime > 0.0) {
+                sfr_const = 1.0 / fmin(t_max, t_trunc);
+                mass_const = fmax(fmin(t_prime, t_trunc), 0.0) * sfr_const;
+            }
+            const double norm = 1.0 - cst - fburst;
+            mass_frac_v = norm * mass_tau / total + cst * mass_const + fburst * mfrac_burst;
+            sfr = (t_prime > t_trunc) ? 0.0 : norm * sfr_tau / total + cst * sfr_const;
+        } else {
+            /* the ramp after the truncation: SFR = sfr_tr (1 - s (t - t_tr)), s = -sf_slope, from the delayed tau's
+               SFR at t_tr, down to its zero t_tr + 1 / s */
+            const double s = -p[SP_SF_SLOPE];
+            const double t_zero = s > 0.0 ? t_trunc + 1.0 / s : t_max;
+            double total_lin = 0.0, mass_lin = 0.0;
+            if (t_trunc <= 0.0 || t_trunc > t_max) {
+                sfr = sfr_tau / total;
+            } else {
+                const double sfr_tr = (t_trunc / tau) * exp(-t_trunc / tau);
+                double hi = fmin(t_zero, t_max);
+                total_lin = sfr_tr * ((hi - t_trunc) - 0.5 * s * (hi * hi + t_trunc * t_trunc) + s * hi * t_trunc);
+                if (t_prime <= t_trunc) {
+                    sfr = sfr_tau / (total + total_lin);
+                } else {
+                    hi = fmin(t_zero, t_prime);
+                    mass_lin = sfr_tr * ((hi - t_trunc) - 0.5 * s * (hi * hi + t_trunc * t_trunc) + s * hi * t_trunc);
+                    sfr = fmax(sfr_tr * (1.0 - s * (t_prime - t_trunc)), 0.0) / (total + total_lin);
+                }
+            }
+            if (t_prime >= 0.0) {
+                mass_frac_v = (mass_tau + mass_lin) / (total + total_lin);
+                if (mass_lin + mass_tau > SAFE_FLOOR) fl = mass_lin / (mass_lin + mass_tau);
+            } else {
+                mass_frac_v = 0.0;
+                sfr = 0.0;
+            }
         }
-        const double norm = 1.0 - cst - fburst;
-        mass_frac = norm * mass_tau / total + cst * mass_const + fburst * mfrac_burst;
-        sfr = (t_prime > t_trunc) ? 0.0 : norm * sfr_tau / total + cst * sfr_const;
     }
+    *mass_frac = mass_frac_v;
+    *sfr_out = sfr;
+    *frac_linear = fl;
+}
+
+/* get_sfh_properties_at_age_pc alone (tests): age in Gyr, the SFR per Gyr before the unit change. */
+void oracle_sfh_props(const double *tf, int nt, int sfh, const double *p, double age, double *out3) {
+    sfh_props(tf, nt, sfh, p, age, out3, out3 + 1, out3 + 2);
+}
+
+/* The current SFR per unit mass formed, normalised by the mass fraction formed by tage (per yr). */
+double oracle_sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
+    double mass_frac, sfr, fl;
+    sfh_props(tf, nt, sfh, p, p[SP_TAGE], &mass_frac, &sfr, &fl);
     sfr /= 1.0e9;
     if (mass_frac > SAFE_FLOOR) sfr /= mass_frac;
     return sfr;

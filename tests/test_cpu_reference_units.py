@@ -5,8 +5,11 @@ inputs, the same closed forms or direct evaluations, the same tolerances as Open
   form at z = 2 (5e-4 relative) and the low-z Hubble law at z = 1e-3 (1e-3 relative).
 * SFH moment method (tests/physics/test_opensps_sfh.f90:158-278,1115-1243): the tau model's total mass against its
   integral (5e-3), the delayed tau's mass invariant under a grid refinement (1e-5), the youngest edge bin, and the
-  weights against Simpson quadrature of the SFR for the analytic types 0, 1 and 4 with tage on and off a node (mass
-  1e-6, mean log age 1e-8, weights non-negative).
+  weights against Simpson quadrature of the SFR for the analytic types 0, 1, 4 and 5 with tage on and off a node
+  (mass 1e-6, mean log age 1e-8, weights non-negative).
+* Simha SFH properties (tests/physics/test_opensps_sfh.f90:379-404,955-1016): the SFR is zero past the ramp's zero
+  and the ramp's mass fraction positive; a truncation past the grid's oldest age leaves no ramp; before sf_start the
+  mass fraction, SFR and ramp fraction are zero.
 * Velocity smoothing (tests/spectra/test_opensps_smoothing.f90:384-474,586-614): the sparse operator against the
   direct convolution integral on a grid with a spacing jump (1e-12 relative) and on the synthetic log-uniform grid;
   a flat spectrum stays flat; pixels outside [minl, maxl] pass through unchanged.
@@ -73,7 +76,7 @@ def test_youngest_edge_includes_zero_bin():
     assert w0[0] > w1[0]
 
 
-def _simpson_moments(sfh_type, tau, tage, t_lo, t_hi, n_steps=200000):
+def _simpson_moments(sfh_type, tau, tage, t_lo, t_hi, n_steps=200000, trunc=0.0, slope=0.0):
     """M0 = int SFR dt, M1 = int SFR log10(t) dt over lookback [t_lo, t_hi] by composite Simpson in u = log10 t (the
     reference test's sfh_moments_quadrature, log interpolation)."""
     u = np.log10(t_lo) + (np.log10(t_hi) - np.log10(t_lo)) * np.arange(n_steps + 1) / n_steps
@@ -82,6 +85,8 @@ def _simpson_moments(sfh_type, tau, tage, t_lo, t_hi, n_steps=200000):
         sfr = np.ones_like(t)
     elif sfh_type == 1:
         sfr = np.exp(t / tau) / tau
+    elif sfh_type == 5:
+        sfr = 1.0 - slope * max(0.0, tage - trunc) + slope * t
     else:
         sfr = (tage - t) * np.exp(t / tau) / tau
     c = np.where(np.arange(n_steps + 1) % 2 == 1, 4.0, 2.0)
@@ -91,17 +96,38 @@ def _simpson_moments(sfh_type, tau, tage, t_lo, t_hi, n_steps=200000):
     return float(np.sum(c * sfr * jac)) * du / 3.0, float(np.sum(c * sfr * u * jac)) * du / 3.0
 
 
-@pytest.mark.parametrize("sfh_type", [0, 1, 4])
+@pytest.mark.parametrize("sfh_type", [0, 1, 4, 5])
 @pytest.mark.parametrize("on_node", [True, False])
 def test_moments_match_quadrature(sfh_type, on_node):
     tf = log_grid(60, 6.0, 10.2)
     tau = 2.0e9
     tage = 10.0 ** tf[54] if on_node else 10.0 ** (0.3 * tf[54] + 0.7 * tf[55])
-    w = O.ssp_weights_raw(tf, sfh_type, tage=tage, tau=tau, idx_min=1, idx_max=tf.size, tiny_logt=4.0)
-    m0, m1 = _simpson_moments(sfh_type, tau, tage, 10.0 ** tf[0], tage)
+    trunc, slope = 2.0e9, 1.0e-10
+    w = O.ssp_weights_raw(tf, sfh_type, tage=tage, tau=tau, idx_min=1, idx_max=tf.size, tiny_logt=4.0, trunc=trunc,
+                          slope=slope)
+    m0, m1 = _simpson_moments(sfh_type, tau, tage, 10.0 ** tf[0], tage, trunc=trunc, slope=slope)
     assert abs(w.sum() / m0 - 1.0) <= 1.0e-6
     assert abs((np.sum(w * tf) / w.sum()) / (m1 / m0) - 1.0) <= 1.0e-8
     assert np.all(w >= 0.0)
+
+
+def test_simha_truncation_logic():
+    mf, sfr, fl = O.sfh_properties(log_grid(30, 6.0, 10.0), 5, {"tau": 1.0, "sf_start": 0.0, "sf_trunc": 2.0,
+                                                                 "sf_slope": -1.0}, 4.0)
+    assert abs(sfr) <= 1.0e-12
+    assert fl > 0.0
+
+
+def test_simha_no_truncation_effective():
+    mf, sfr, fl = O.sfh_properties(log_grid(10, 6.0, 10.0), 5, {"tau": 1.0, "sf_start": 0.0, "sf_trunc": 20.0,
+                                                                 "sf_slope": -1.0}, 5.0)
+    assert fl == 0.0
+
+
+def test_simha_before_sf_start():
+    mf, sfr, fl = O.sfh_properties(log_grid(10, 6.0, 10.0), 5, {"tau": 1.0, "sf_start": 5.0, "sf_trunc": 7.0,
+                                                                 "sf_slope": -1.0}, 3.0)
+    assert mf == 0.0 and sfr == 0.0 and fl == 0.0
 
 
 # ----------------------------------------------------------------------------------------------------- smoothing

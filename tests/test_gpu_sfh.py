@@ -1,4 +1,5 @@
-"""SFH weights formed on the device (sfh 0, 1, 4 with the constant and burst components), blended at logzsol,
+"""SFH weights formed on the device (sfh 0, 1, 4 with the constant and burst components; sfh 5, the delayed tau
+with a linear ramp after the truncation), blended at logzsol,
 through the batch, against the FP64 oracle: spectra <= 1e-4 relative, magnitudes <= 1e-3 mag, mass <= 1e-12
 relative, log L_bol <= 1e-9 relative, the SFR per unit mass formed <= 1e-12 relative.
 
@@ -80,6 +81,30 @@ def test_sfh_types_with_constant_and_burst(data, built_lib, sfh):
     c = _ctx(sfh, neb=True, igm=True)
     got = _forward(c, params, n)
     _check(got, oracle_sfh_csp(Oracle(data, nbands=40), data, sfh, params))
+    c.close()
+
+
+def test_simha_sfh(data, built_lib):
+    """sfh 5: truncations inside the star-forming age (and none), ramps falling to zero before tage, falling but not
+    to zero, and rising; sf_start and logzsol per model."""
+    from oracle.oracle import Oracle
+    n = 48
+    rng = np.random.default_rng(55)
+    tage = rng.uniform(1.0, 13.0, n)
+    start = rng.uniform(0.0, 0.3, n)
+    trunc = np.where(rng.uniform(size=n) < 0.2, 0.0, start + rng.uniform(0.2, 0.9, n) * (tage - start))
+    kind = rng.integers(0, 3, n)
+    ramp = np.maximum(tage - trunc, 0.05)
+    slope = np.select([kind == 0, kind == 1], [-1.0 / (rng.uniform(0.3, 0.9, n) * ramp),
+                                                -1.0 / (rng.uniform(1.2, 4.0, n) * ramp)], rng.uniform(0.05, 1.0, n))
+    params = {"tau": 10.0 ** rng.uniform(-0.5, 1.0, n), "tage": tage, "sf_start": start, "sf_trunc": trunc,
+              "sf_slope": slope, "logzsol": rng.uniform(-1.5, 0.3, n), "dust2": rng.uniform(0.0, 1.0, n),
+              "zred": rng.uniform(0.1, 3.0, n), "sigma_smooth": rng.uniform(60.0, 250.0, n)}
+    c = _ctx(5, neb=True, igm=True)
+    got = _forward(c, params, n)
+    ora = oracle_sfh_csp(Oracle(data, nbands=40), data, 5, params)
+    _check(got, ora)
+    assert np.any(ora["sfr"] == 0.0) and np.any(ora["sfr"] > 0.0)
     c.close()
 
 

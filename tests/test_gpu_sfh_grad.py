@@ -1,6 +1,6 @@
 """The reverse pass with weights formed on the device: the SFH parameters' rows (tage, tau, const, fburst, tburst,
-sf_start, sf_trunc: forward-mode tangents of the weights), logzsol's row and weights_bar (the cotangent of the
-weights over ages), against central differences (h = 1e-4 relative) of the FP64 oracle. Tolerance as the other
+sf_start, sf_trunc, and sf_slope for sfh 5: forward-mode tangents of the weights), logzsol's row and weights_bar (the
+cotangent of the weights over ages), against central differences (h = 1e-4 relative) of the FP64 oracle. Tolerance as the other
 gradient tests: |g - g_fd| <= 2e-3 max(|g_fd|, 1e-3 max_rows |g_fd|)."""
 import numpy as np
 import pytest
@@ -13,6 +13,7 @@ RTOL = 2e-3
 H_REL = 1e-4
 ROWS = {"logzsol": 15, "tage": 16, "tau": 17, "const": 18, "fburst": 19, "tburst": 20, "sf_start": 21,
         "sf_trunc": 24}
+ROWS_SIMHA = {"logzsol": 15, "tage": 16, "tau": 17, "sf_start": 21, "sf_trunc": 24, "sf_slope": 25}
 
 
 def _loss(out, mb, sb, massb, lbolb):
@@ -71,6 +72,46 @@ def test_sfh_rows_match_central_differences(data, built_lib):
     scale = np.max(np.abs(fd), axis=1, keepdims=True)
     err = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
     assert float(err.max()) <= RTOL, {names[i]: float(err[:, i].max()) for i in range(len(names))}
+    c.close()
+
+
+def test_simha_rows_match_central_differences(data, built_lib):
+    """sfh 5: the ramp's start (the truncation's lookback time tq), its zero t0 = tq - 1 / slope (for the falling
+    ramps) and the star-forming age each drawn away from the grid ages; half the ramps reach zero before tage."""
+    from libopensps_gb300.capi import Context
+    from oracle.oracle import Oracle
+    n = 6
+    rng = np.random.default_rng(83)
+    la = data["log_age"]
+    start = rng.uniform(0.05, 0.3, n)
+    age = _away_from_nodes(la, rng.uniform(4.0, 12.0, n), rng, 5e-3)
+    tq = _away_from_nodes(la, rng.uniform(1.0, 3.0, n), rng, 5e-3)
+    t0 = _away_from_nodes(la, tq * rng.uniform(0.2, 0.6, n), rng, 5e-3)
+    falling_to_zero = np.arange(n) % 2 == 0
+    slope = np.where(falling_to_zero, -1.0 / (tq - t0), -1.0 / (3.0 * tq))
+    params = {"tau": 10.0 ** rng.uniform(-0.3, 0.8, n), "tage": age + start, "sf_start": start,
+              "sf_trunc": age + start - tq, "sf_slope": slope, "logzsol": rng.uniform(-1.5, 0.3, n),
+              "dust2": rng.uniform(0.1, 1.0, n), "zred": rng.uniform(0.2, 2.0, n),
+              "sigma_smooth": rng.uniform(60.0, 250.0, n)}
+    c = Context()
+    c.set_int("sfh", 5)
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    mb, sb, massb, lbolb = _cot(c, n, 84)
+    got = c.csp_batch_grad(params, mags_bar=mb, spec_bar=sb, mass_bar=massb, lbol_bar=lbolb, n=n)
+    o = Oracle(data, nbands=40)
+    names = list(ROWS_SIMHA)
+    g = np.stack([got["params_bar"][:, ROWS_SIMHA[k]] for k in names], axis=1)
+    fd = np.empty_like(g)
+    for i, k in enumerate(names):
+        h = H_REL * np.maximum(np.abs(params[k]), 1e-2)
+        up = oracle_sfh_csp(o, data, 5, dict(params, **{k: params[k] + h}))
+        dn = oracle_sfh_csp(o, data, 5, dict(params, **{k: params[k] - h}))
+        fd[:, i] = (_loss(up, mb, sb, massb, lbolb) - _loss(dn, mb, sb, massb, lbolb)) / (2.0 * h)
+    scale = np.max(np.abs(fd), axis=1, keepdims=True)
+    err = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
+    assert float(err.max()) <= RTOL, {names[i]: float(err[:, i].max()) for i in range(len(names))}
+    assert np.all(np.abs(fd[:, names.index("sf_slope")]) > 1e-6 * scale[:, 0])
     c.close()
 
 
