@@ -39,6 +39,7 @@ typedef enum {
 #define OPENSPS_STATUS_OK 0
 #define OPENSPS_ERR_COMPUTE_UNINIT 301
 #define OPENSPS_ERR_SSP_UNINIT 303
+#define OPENSPS_ERR_SSP_TABULAR_SFH 508   /* opensps.h:105: the tabular SFH missing, unreadable or too long */
 
 /* ---- driver utilities ---------------------------------------------------------------------------------- */
 void opensps_clear_error(void);                                                   /* opensps.h:113 */
@@ -76,6 +77,14 @@ void opensps_context_set_filters_library(int handle, const char *name, int resam
                                          int vega_ref_band, int *status);
 /* The bands a context computes (opensps.h:227). */
 void opensps_context_set_mag_compute(int handle, int n_bands, const int *mask, int *status);
+/* Tabular SFH for sfh = 3 (opensps.h:229-232): ntab (1 .. 20000) rows of age [Gyr] and SFR [M_sun/yr]; met is
+ * accepted and not read (the batch forms one metallicity's weights and blends them at logzsol). status 3: ntab out of
+ * range, NULL age or sfr, or ages that decrease (the reference stores those; a bin of negative width gives its
+ * segment a slope over SAFE_FLOOR). sfh = 2 reads the same table from $OPENSPS_DATA_HOME/<sfh_filename> (default sfh.dat: rows of age and SFR,
+ * a third column not read, the SFRs floored at SAFE_FLOOR) at the first batch after the name is set, status 508
+ * when it cannot. */
+void opensps_context_set_sfh_tab(int handle, int ntab, const double *age, const double *sfr, const double *met,
+                                 int *status);
 
 /* ---- batched CSPs --------------------------------------------------------------------------------------- */
 /* opensps.h:266-278. ssp_weights (ntfull x n) blends each model's SSPs at its logzsol; with neither weight matrix

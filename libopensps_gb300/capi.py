@@ -53,6 +53,7 @@ SIGNATURES = {
     "opensps_context_get_emlambda": (None, [C.c_int, _dp, _ip]),
     "opensps_context_set_filters_library": (None, [C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, _ip]),
     "opensps_context_set_mag_compute": (None, [C.c_int, C.c_int, _ip, _ip]),
+    "opensps_context_set_sfh_tab": (None, [C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
     "opensps_context_compute_csp_batch": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp] + [_dp] * 8
                                           + [_ip]),
     "opensps_context_compute_csp_batch_parts": (None, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, _dp]
@@ -225,6 +226,20 @@ class Context:
     def set_float(self, key: str, value: float):
         st = C.c_int(0)
         self.lib.opensps_context_set_float(self.handle, key.encode(), float(value), C.byref(st))
+        _check(st, self.lib)
+
+    def set_str(self, key: str, value: str):
+        st = C.c_int(0)
+        self.lib.opensps_context_set_str(self.handle, key.encode(), value.encode(), C.byref(st))
+        _check(st, self.lib)
+
+    def set_sfh_tab(self, age, sfr, met=None):
+        """The tabular SFH of sfh = 3: ages [Gyr] and SFRs [M_sun / yr] (met is not read)."""
+        a = np.ascontiguousarray(age, dtype=np.float64)
+        s = np.ascontiguousarray(sfr, dtype=np.float64)
+        m = None if met is None else np.ascontiguousarray(met, dtype=np.float64)
+        st = C.c_int(0)
+        self.lib.opensps_context_set_sfh_tab(self.handle, int(a.size), _ptr(a), _ptr(s), _ptr(m), C.byref(st))
         _check(st, self.lib)
 
     def set_filters_library(self, name: str):

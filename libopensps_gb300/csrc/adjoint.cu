@@ -1127,7 +1127,10 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
     // ---- weights formed on the device: the cotangent of the weights over ages, logzsol's row and the SFH rows
     if (sfh_rev) {
         const int nt = c.nt;
-        const bool tangents = io_in.given_w == nullptr && params_bar != nullptr;
+        // (the tabular SFHs have no parameters here: their rows stay zero, sfh_weights_tangent
+        // src/physics/opensps_sfh_tangent.f90:61-81)
+        const bool tangents = io_in.given_w == nullptr && params_bar != nullptr && io_in.sfh_type != 2 &&
+                              io_in.sfh_type != 3;
         if ((e = c.d_wbar.reserve((size_t)nt * n)) != cudaSuccess ||
             (tangents && (e = c.d_dual.reserve((size_t)3 * nt * n * sfh_dual_bytes())) != cudaSuccess)) {
             err = msg("device memory", e);

@@ -815,6 +815,21 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         sa.given = io.given_w ? c.d_wgiven.p : nullptr;
         sa.w = c.d_w.p; sa.scratch = c.d_sfh_scratch.p; sa.wz = c.d_wz.p; sa.lblend = c.d_lblend.p; sa.sfr = c.d_sfr.p;
         sa.mtab = c.d_sfh_mtab.p;
+        if ((io.sfh_type == 2 || io.sfh_type == 3) && !io.given_w) {
+            // the tabular SFH: ages then SFRs, each with its zero entry past the table
+            const size_t nt1 = (size_t)c.ntab + 1;
+            if (c.sfh_tab_dirty || c.d_sfhtab.n < 2 * nt1) {
+                if ((e = c.d_sfhtab.reserve(2 * nt1)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(c.d_sfhtab.p, c.sfh_tab_t.data(), sizeof(double) * nt1, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(c.d_sfhtab.p + nt1, c.sfh_tab_sfr.data(), sizeof(double) * nt1, cudaMemcpyHostToDevice, st)) != cudaSuccess) {
+                    err = cuda_msg("tabular SFH copy", e);
+                    return ST_DATA_MISSING;
+                }
+                c.sfh_tab_dirty = false;
+            }
+            sa.ntab = c.ntab;
+            sa.tab = c.d_sfhtab.p;
+        }
         if ((e = run_sfh_forward(sa, st)) != cudaSuccess) { err = cuda_msg("SFH weights kernel", e); return ST_DATA_MISSING; }
         d_wz = c.d_wz.p;
     } else {

@@ -4,7 +4,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <fstream>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <vector>
 #include "context.h"
@@ -59,6 +61,61 @@ const char *const GRAD_NAMES[OPENSPS_NBGRAD] = {
     "tburst", "sf_start", "zred", "sigma_smooth", "sf_trunc", "sf_slope", "imf1", "imf2", "imf3", "vdmc", "mdave",
     "agn_tau", "igm_factor", "gas_logn", "gas_logno", "gas_logco", "afe", "fbhb", "sbss", "agb", "pagb", "redgb",
     "delt", "dell"};
+
+// The tabular SFH from ages [Gyr] and SFRs into the context (years; one zero entry past the table, where the SFR's
+// interpolation reads past the last row): 0, or ST_BAD_ARG with err for decreasing ages (the device finds a model's
+// bins by bisection).
+int store_sfh_tab(Context &c, int ntab, const double *age, const double *sfr, std::string &err) {
+    for (int i = 1; i < ntab; ++i)
+        if (!(age[i] >= age[i - 1])) {
+            err = "the tabular SFH's ages must not decrease on this path (row " + std::to_string(i + 1) + ")";
+            return ST_BAD_ARG;
+        }
+    c.sfh_tab_t.assign((size_t)ntab + 1, 0.0);
+    c.sfh_tab_sfr.assign((size_t)ntab + 1, 0.0);
+    for (int i = 0; i < ntab; ++i) {
+        c.sfh_tab_t[i] = age[i] * 1.0e9;
+        c.sfh_tab_sfr[i] = sfr[i];
+    }
+    c.ntab = ntab;
+    c.sfh_tab_dirty = true;
+    return 0;
+}
+
+// load_tabular_sfh for sfh = 2 (src/io/opensps_io.f90:2375-2491): rows of age [Gyr] and SFR [M_sun / yr] (a third
+// column, the metallicity, not read: the batch forms one metallicity's weights) from sfh_filename under the data
+// root, at most NTABMAX rows, the SFRs floored at SAFE_FLOOR. Read again when the name changes. 0, or
+// ST_TABULAR_SFH with err.
+int load_sfh_file(Context &c, std::string &err) {
+    const std::string path = data_root() + "/" + c.sfh_filename;
+    if (c.sfh_tab_file == path && c.ntab > 0) return 0;
+    std::ifstream f(path);
+    if (!f) { err = "sfh = 2: cannot open the tabular SFH " + path; return ST_TABULAR_SFH; }
+    std::vector<double> age, sfr;
+    std::string line;
+    int lineno = 0;
+    while (std::getline(f, line)) {
+        ++lineno;
+        for (char &ch : line)
+            if (ch == ',') ch = ' ';
+        std::istringstream is(line);
+        double a, s;
+        if (!(is >> a)) {
+            if (line.find_first_not_of(" \t\r") == std::string::npos) continue;   // blank
+            err = "sfh = 2: cannot read line " + std::to_string(lineno) + " of " + path;
+            return ST_TABULAR_SFH;
+        }
+        if (!(is >> s)) { err = "sfh = 2: line " + std::to_string(lineno) + " of " + path + " has one value"; return ST_TABULAR_SFH; }
+        if ((int)age.size() == SFH_NTABMAX) { err = "sfh = 2: " + path + " has more than 20000 rows"; return ST_TABULAR_SFH; }
+        age.push_back(a);
+        sfr.push_back(s < SAFE_FLOOR ? SAFE_FLOOR : s);
+    }
+    if (age.empty()) { err = "sfh = 2: " + path + " has no rows"; return ST_TABULAR_SFH; }
+    int st = store_sfh_tab(c, (int)age.size(), age.data(), sfr.data(), err);
+    if (st) { err = "sfh = 2: " + err; return ST_TABULAR_SFH; }
+    c.sfh_tab_file = path;
+    return 0;
+}
 
 // names / values -> PF_COUNT x n rows (the context's values, with the named ones per model). 0, or a status.
 int build_params(Context &c, int n, int n_params, const char *const *names, const double *const *values,
@@ -116,10 +173,14 @@ int batch_core(Context &cref, int n, int n_params, const char *const *names, con
     std::vector<double> sfhp;
     if (!ssp_weights_z) {
         if (!ssp_weights) {
-            if (c->sfh != 0 && c->sfh != 1 && c->sfh != 4 && c->sfh != 5) {
-                err = "sfh = " + std::to_string(c->sfh) +
-                      ": only 0 (SSP), 1 (tau), 4 (delayed tau) and 5 (delayed tau with a linear ramp) on this path";
+            if (c->sfh < 0 || c->sfh > 5) {
+                err = "sfh = " + std::to_string(c->sfh) + ": the SFH types are 0 to 5";
                 return ST_UNSUPPORTED;
+            }
+            if (c->sfh == 2 && (st = load_sfh_file(*c, err)) != 0) return st;
+            if (c->sfh == 3 && c->ntab < 1) {
+                err = "sfh = 3 without a tabular SFH (opensps_context_set_sfh_tab)";
+                return ST_TABULAR_SFH;
             }
             for (int m = 0; m < n; ++m)
                 if (!(rows[(size_t)PF_COUNT * m + PF_TAGE] > 0.0)) {
@@ -322,7 +383,14 @@ void opensps_context_set_str(int handle, const char *key, const char *value, int
     if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
     if (!key) return fail(status, 103, "NULL key");
     const std::string k(key);
-    if (k == "imf_filename" || k == "sfh_filename") return fail(status, 104, k + " is not supported on this path");
+    if (k == "sfh_filename") {
+        if (!value || !*value) return fail(status, 103, "empty sfh_filename");
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->sfh_filename = value;
+        if (status) *status = 0;
+        return;
+    }
+    if (k == "imf_filename") return fail(status, 104, k + " is not supported on this path");
     return fail(status, 103, "unknown string parameter " + k);
 }
 
@@ -394,6 +462,20 @@ void opensps_context_set_mag_compute(int handle, int n_bands, const int *mask, i
     if (n_bands < 1 || n_bands > c->nbands) return fail(status, ST_BAD_ARG, "n_bands out of range");
     c->mag_mask.assign(c->nbands, 0);
     for (int b = 0; b < n_bands; ++b) c->mag_mask[b] = mask[b] != 0;
+    if (status) *status = 0;
+}
+
+void opensps_context_set_sfh_tab(int handle, int ntab, const double *age, const double *sfr, const double *met,
+                                 int *status) {
+    (void)met;
+    Context *c = lookup(handle);
+    if (!c) return fail(status, ST_BAD_HANDLE, "invalid context handle");
+    if (ntab < 1 || ntab > SFH_NTABMAX) return fail(status, ST_BAD_ARG, "opensps_context_set_sfh_tab: ntab out of range");
+    if (!age || !sfr) return fail(status, ST_BAD_ARG, "opensps_context_set_sfh_tab: age and sfr are required");
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::string err;
+    if (store_sfh_tab(*c, ntab, age, sfr, err)) return fail(status, ST_BAD_ARG, "opensps_context_set_sfh_tab: " + err);
+    c->sfh_tab_file.clear();
     if (status) *status = 0;
 }
 

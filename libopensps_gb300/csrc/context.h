@@ -187,6 +187,12 @@ struct Context {
     // settings (set_int / set_float)
     int add_neb_emission = 0, add_igm_absorption = 0, smooth_velocity = 1, dust_type = 0, compute_vega_mags = 0;
     int sfh = 0, nebemlineinspec = 1, fast_mode = 0, zmet = 1, imf_type = 2;
+    // the tabular SFH (sfh 2, 3): ages in years since the start (non-decreasing) and SFRs [M_sun / yr], ntab entries
+    // and one zero entry past them; the file it came from (sfh 2; empty: the caller's arrays, sfh 3)
+    std::vector<double> sfh_tab_t, sfh_tab_sfr;
+    int ntab = 0;
+    std::string sfh_filename = "sfh.dat", sfh_tab_file;
+    bool sfh_tab_dirty = true;       // the device copy is stale
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     int add_dust_emission = 0;   // the energy-balance dust emission (Draine & Li templates)
@@ -256,6 +262,7 @@ struct Context {
     // SFH weights: grid tables, per-model parameters, weights over ages, log-blended L_bol, SFR; reverse-pass scratch
     DevBuf<double> d_logage, d_lz, d_lbol;
     DevBuf<double> d_sfhpar, d_wgiven, d_w, d_sfh_scratch, d_lblend, d_sfr, d_wbar;
+    DevBuf<double> d_sfhtab;         // the tabular SFH: 2 (ntab + 1) doubles, ages then SFRs
     DevBuf<double2> d_sfh_mtab;  // the SFH's moments at the grid ages (n x nt)
     DevBuf<unsigned char> d_dual;
     // the dust emission templates (Draine & Li shapes) and the frequency trapezoid weights of the grid; the AGN torus
@@ -314,7 +321,8 @@ struct Context {
 
 // status codes of opensps.h
 enum { ST_OK = 0, ST_BAD_HANDLE = 1, ST_UNSUPPORTED = 2, ST_BAD_ARG = 3, ST_DATA_MISSING = 4,
-       ST_NOT_SETUP = 301, ST_NO_OPERATOR = 303 };
+       ST_NOT_SETUP = 301, ST_NO_OPERATOR = 303, ST_TABULAR_SFH = 508 };
+constexpr int SFH_NTABMAX = 20000;   // the tabular SFH's rows at most (NTABMAX, src/core/opensps_constants.f90:147)
 
 void set_error(int status, const std::string &msg);
 int context_setup(Context &c, const char *isoc, const char *spec, const char *dust, std::string &err);

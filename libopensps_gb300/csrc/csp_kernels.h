@@ -282,6 +282,8 @@ struct SfhArgs {
     double *sfr;             // n, or null
     double2 *mtab = nullptr; // n x nt: the main component's moments at the grid ages (sfh 1, 4, and 5's delayed
                              // tau; null: formed serially per model)
+    int ntab = 0;            // the tabular SFH (sfh 2, 3): ntab rows, tab = ages (years since the start,
+    const double *tab = nullptr;   // non-decreasing) then SFRs, each with one zero entry past the table
 };
 cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st);
 struct SfhRevArgs {

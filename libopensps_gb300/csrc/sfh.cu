@@ -543,8 +543,9 @@ __global__ void __launch_bounds__(SFH_WARPS * 32) sfh_forward_kernel(SfhArgs a) 
     const int nt = a.nt, nz = a.nz;
     double *w = sm[wi][0], *t1 = sm[wi][1], *t2 = sm[wi][2], *M0s = sm[wi][3], *M1s = sm[wi][4];
     if (a.given) {
+        // the caller's weights (SFR NaN), or the tabular SFH's from sfh_tab_kernel (its SFR kept)
         for (int i = lane; i < nt; i += 32) w[i] = a.given[(size_t)nt * m + i];
-        if (lane == 0 && a.sfr) a.sfr[m] = NAN;
+        if (lane == 0 && a.sfr && a.ntab == 0) a.sfr[m] = NAN;
         __syncwarp();
     } else {
         const int sfh = a.sfh;
@@ -639,6 +640,108 @@ __global__ void __launch_bounds__(SFH_WARPS * 32) sfh_forward_kernel(SfhArgs a) 
     }
 }
 
+// sfh_weights_core_pc for the tabular SFHs (sfh 2, 3; src/physics/opensps_sfh.f90:1215-1293) with one metallicity,
+// one warp per model (TAB_WARPS per CTA): each table bin j, rows j and j + 1 (ages T, SFRs S), is the linear SFR
+// between them, a type-5 segment over the lookback window [tage - T_(j+1), tage - T_j] clamped to [1 yr, the grid's
+// oldest age], with slope -(S_(j+1) - S_j) / dt / S_(j+1); its hat-kernel weights over its own index range (the
+// reference's interval loop, the moments carried from one interval to the next, and the youngest edge) are scaled to
+// the bin's mass S_(j+1) (1 + slope / 2 (tage' + tq - 2 t1)) (tage' - tq) over their sum. The weights are the masses
+// formed (M_sun). Lane l takes bins l, l + 32, ... into its own row of shared memory; the rows are summed per age in
+// lane order (deterministic). A bin whose scale is not finite turns every weight to NaN, as the reference's
+// w += tmp1 (mass2 / mass1) does. The SFR: the table's, interpolated at tage (get_sfh_properties_at_age_pc
+// :458-480; the mass fraction 1). Written: w (n x nt) and sfr.
+constexpr int TAB_WARPS = 2;
+__global__ void __launch_bounds__(TAB_WARPS * 32) sfh_tab_kernel(SfhArgs a) {
+    extern __shared__ double tab_rows[];             // TAB_WARPS x 32 x nt
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const int m = blockIdx.x * TAB_WARPS + wi;
+    if (m >= a.n) return;
+    const int nt = a.nt, ntab = a.ntab;
+    const double *tf = a.tf, *T = a.tab, *S = a.tab + ntab + 1;
+    double *row = tab_rows + ((size_t)wi * 32 + lane) * nt;
+    for (int i = 0; i < nt; ++i) row[i] = 0.0;
+    const double tage = a.par[(size_t)SFH_NCOL * m + SFH_TAGE] * 1.0e9;
+    const double tmax = pow(10.0, tf[nt - 1]);
+    bool bad = false;
+    for (int b = lane; b < ntab - 1; b += 32) {
+        const double t1 = tage - T[b + 1], t2 = tage - T[b];
+        if (t2 < 0.0) continue;
+        const double dt = fmax(t2 - t1, SAFE_FLOOR);
+        SfhT<double> s;
+        s.type = 5;
+        s.simha = 0;
+        s.tau = s.tb = s.t0 = 0.0;
+        s.slope = -(S[b + 1] - S[b]) / dt / fmax(S[b + 1], SAFE_FLOOR);
+        s.tq = fmin(fmax(t1, 1.0), tmax);
+        s.tage = fmin(fmax(t2, 1.0), tmax);
+        s.trunc = s.tage - s.tq;
+        const double mass2 = S[b + 1] * (1.0 + s.slope / 2.0 * (s.tage + s.tq - 2.0 * t1)) * (s.tage - s.tq);
+        int imin = find_interval0(tf, nt, log10(fmax(t1, SAFE_FLOOR)));          // the reference's index - 1
+        int imax = find_interval0(tf, nt, log10(fmax(t2, SAFE_FLOOR))) + 3;      // and + 2, 1-based
+        imin = imin < 0 ? 0 : (imin > nt ? nt : imin);
+        imax = imax < 0 ? 0 : (imax > nt ? nt : imax);
+        double lts, lte;
+        sfh_window(s, lts, lte);
+        int js = find_interval0(tf, nt, lts) + 1, je = find_interval0(tf, nt, lte) + 2;
+        const int lo_bound = imin > 1 ? imin : 1, hi_bound = imax < nt - 1 ? imax : nt - 1;
+        if (js < lo_bound) js = lo_bound;
+        if (je > hi_bound) je = hi_bound;
+        // the bin's weights summed: its moments' change over its intervals, and the youngest edge
+        double m0s, m1s, m0e, m1e, mass1 = 0.0, edge = 0.0;
+        if (js <= je) {
+            moments_log(fmin(fmax(tf[je], lts), lte), s, m0e, m1e);
+            moments_log(fmin(fmax(tf[js - 1], lts), lte), s, m0s, m1s);
+            mass1 = m0e - m0s;
+        }
+        if (imin == 0) {
+            const double l1 = fmin(fmax(0.0, lts), lte), l2 = fmin(fmax(tf[0], lts), lte);
+            if (l1 < l2) {
+                moments_log(l2, s, m0e, m1e);
+                moments_log(l1, s, m0s, m1s);
+                edge = m0e - m0s;
+            }
+        }
+        mass1 += edge;
+        if (mass1 < SAFE_FLOOR) mass1 = 1.0;
+        const double scale = mass2 / mass1;
+        if (!isfinite(scale)) { bad = true; continue; }
+        if (js <= je) {
+            double lim_prev = fmin(fmax(tf[js - 1], lts), lte), m0p, m1p;
+            moments_log(lim_prev, s, m0p, m1p);
+            for (int j = js; j <= je; ++j) {
+                const double lim2 = fmin(fmax(tf[j], lts), lte);
+                if (lim2 <= lim_prev) { lim_prev = lim2; continue; }
+                double m0c, m1c;
+                moments_log(lim2, s, m0c, m1c);
+                const double d0 = m0c - m0p, d1 = m1c - m1p;
+                m0p = m0c;
+                m1p = m1c;
+                const double lo = tf[j - 1], hi = tf[j], inv = 1.0 / (hi - lo);
+                row[j - 1] += (hi * d0 - d1) * inv * scale;
+                row[j] += (d1 - lo * d0) * inv * scale;
+                lim_prev = lim2;
+            }
+        }
+        if (imin == 0) row[0] += edge * scale;
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    __syncwarp();
+    const double *rows = tab_rows + (size_t)wi * 32 * nt;
+    double *wg = a.w + (size_t)nt * m;
+    for (int i = lane; i < nt; i += 32) {
+        double v = 0.0;
+        for (int l = 0; l < 32; ++l) v += rows[(size_t)l * nt + i];
+        wg[i] = bad ? NAN : v;
+    }
+    if (lane == 0 && a.sfr) {
+        int idx = find_interval0(T, ntab, tage) + 1;
+        idx = idx > ntab - 1 ? ntab - 1 : idx;
+        idx = idx < 1 ? 1 : idx;
+        const double v = S[idx - 1] + (S[idx] - S[idx - 1]) / (T[idx] - T[idx - 1]) * (tage - T[idx - 1]);
+        a.sfr[m] = fmax(v, 0.0);
+    }
+}
+
 // The series' reciprocal table in constant memory, once per device.
 static cudaError_t sfh_init_tables(cudaStream_t st) {
     static std::mutex mu;
@@ -668,6 +771,18 @@ cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st) {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (a.nt > SFH_WMAXT) return cudaErrorInvalidValue;
+    if ((a.sfh == 2 || a.sfh == 3) && !a.given) {
+        if (a.ntab < 1 || !a.tab) return cudaErrorInvalidValue;
+        const size_t smem = sizeof(double) * TAB_WARPS * 32 * (size_t)a.nt;
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(sfh_tab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return e;
+        sfh_tab_kernel<<<(a.n + TAB_WARPS - 1) / TAB_WARPS, TAB_WARPS * 32, smem, st>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        b.given = a.w;
+    } else {
+        b.ntab = 0;
+    }
     sfh_forward_kernel<<<(a.n + SFH_WARPS - 1) / SFH_WARPS, SFH_WARPS * 32, 0, st>>>(b);
     return cudaGetLastError();
 }

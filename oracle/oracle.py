@@ -92,6 +92,9 @@ def lib() -> C.CDLL:
                                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                 C.c_int, C.c_int, C.c_int, _dp]
         _lib.oracle_sfh_props.argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_double, _dp]
+        _lib.oracle_sfh_tab_batch.argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp]
+        _lib.oracle_sfh_tab_sfr.restype = C.c_double
+        _lib.oracle_sfh_tab_sfr.argtypes = [C.c_double, C.c_int, _dp, _dp]
     return _lib
 
 
@@ -104,10 +107,19 @@ SFH_DEFAULTS = {"tage": 0.0, "tau": 1.0, "const": 0.0, "fburst": 0.0, "tburst": 
                 "sf_trunc": 0.0, "sf_slope": 0.0}
 
 
-def sfh_weights(log_age: np.ndarray, sfh: int, params: dict, n: int):
+def sfh_weights(log_age: np.ndarray, sfh: int, params: dict, n: int, table=None):
     """The SFH weights over the ages (n, nt) and the current SFR per unit mass formed (n,) of SFH type sfh (0, 1, 4,
-    5) for per-model parameters (sfh_oracle.c)."""
+    5) for per-model parameters, or of the tabular SFHs (sfh 2, 3) for table = (age [Gyr], sfr [M_sun / yr]) at the
+    models' tage: masses formed and the table's SFR (sfh_oracle.c)."""
     tf = np.ascontiguousarray(log_age, dtype=np.float64)
+    if sfh in (2, 3):
+        tt = np.ascontiguousarray(np.asarray(table[0], dtype=np.float64) * 1.0e9)
+        ts = np.ascontiguousarray(table[1], dtype=np.float64)
+        tage = np.ascontiguousarray(np.broadcast_to(np.asarray(params["tage"], dtype=np.float64), (n,)))
+        w = np.empty((n, tf.size))
+        sfr = np.empty(n)
+        lib().oracle_sfh_tab_batch(_p(tf), tf.size, n, _p(tage), tt.size, _p(tt), _p(ts), _p(w), _p(sfr))
+        return w, sfr
     p = np.empty((n, len(SFH_NAMES)))
     for i, k in enumerate(SFH_NAMES):
         p[:, i] = np.broadcast_to(np.asarray(params.get(k, SFH_DEFAULTS[k]), dtype=np.float64), (n,))

@@ -324,6 +324,67 @@ double oracle_sfh_sfr(const double *tf, int nt, int sfh, const double *p) {
     return sfr;
 }
 
+/* sfh_weights_core_pc for the tabular SFHs (sfh 2, 3; src/physics/opensps_sfh.f90:1215-1293) with one metallicity
+   (the batch's): each table bin [T_j, T_(j+1)] (years since the start, non-decreasing) is the linear SFR between its
+   rows, a type-5 segment of slope -(sfr_(j+1) - sfr_j) / dt / sfr_(j+1) over the lookback window [tage - T_(j+1),
+   tage - T_j] clamped to [10^tiny_logt, the grid's oldest age], whose hat-kernel weights (over its own index range)
+   are scaled to the bin's mass sfr_(j+1) (1 + slope / 2 (tage' + tq - 2 t1)) (tage' - tq). The weights are masses
+   formed (M_sun), not normalised. tage in Gyr; tab_t (years) and tab_sfr have ntab entries. */
+void oracle_sfh_tab_weights(const double *tf, int nt, double tage, int ntab, const double *tab_t,
+                            const double *tab_sfr, double *w, double *tmp1) {
+    for (int i = 0; i < nt; ++i) w[i] = 0.0;
+    const double tmin = pow(10.0, 0.0), tmax = pow(10.0, tf[nt - 1]);
+    for (int j = 0; j < ntab - 1; ++j) {
+        const double t1 = tage * 1.0e9 - tab_t[j + 1], t2 = tage * 1.0e9 - tab_t[j];
+        if (t2 < 0.0) continue;
+        const double dt = fmax(t2 - t1, SAFE_FLOOR);
+        sfh_t s;
+        memset(&s, 0, sizeof(s));
+        s.type = 5;
+        s.slope = -(tab_sfr[j + 1] - tab_sfr[j]) / dt / fmax(tab_sfr[j + 1], SAFE_FLOOR);
+        s.tq = fmin(fmax(t1, tmin), tmax);
+        s.tage = fmin(fmax(t2, tmin), tmax);
+        s.trunc = s.tage - s.tq;
+        const double mass2 = tab_sfr[j + 1] * (1.0 + s.slope / 2.0 * (s.tage + s.tq - 2.0 * t1)) * (s.tage - s.tq);
+        int imin = oracle_find_interval(tf, nt, log10(fmax(t1, SAFE_FLOOR))) - 1;
+        int imax = oracle_find_interval(tf, nt, log10(fmax(t2, SAFE_FLOOR))) + 2;
+        imin = imin < 0 ? 0 : (imin > nt ? nt : imin);
+        imax = imax < 0 ? 0 : (imax > nt ? nt : imax);
+        ssp_weights(tf, nt, 0.0, &s, imin, imax, tmp1);
+        double mass1 = 0.0;
+        for (int i = 0; i < nt; ++i) mass1 += tmp1[i];
+        if (mass1 < SAFE_FLOOR) mass1 = 1.0;
+        for (int i = 0; i < nt; ++i) w[i] += tmp1[i] * (mass2 / mass1);
+    }
+}
+
+/* get_sfh_properties_at_age_pc for the tabular SFHs (:458-480): the table's SFR interpolated linearly at age (Gyr)
+   in the interval find_interval_tab_time picks (clamped to the table's first ntab - 1 intervals; the entry past the
+   table reads as zero), floored at zero; M_sun / yr, the mass fraction 1. */
+double oracle_sfh_tab_sfr(double age, int ntab, const double *tab_t, const double *tab_sfr) {
+    int idx = oracle_find_interval(tab_t, ntab, age * 1.0e9);
+    idx = idx > ntab - 1 ? ntab - 1 : idx;
+    idx = idx < 1 ? 1 : idx;
+    const double t0 = tab_t[idx - 1], s0 = tab_sfr[idx - 1];
+    const double t1 = idx < ntab ? tab_t[idx] : 0.0, s1 = idx < ntab ? tab_sfr[idx] : 0.0;
+    const double v = s0 + (s1 - s0) / (t1 - t0) * (age * 1.0e9 - t0);
+    return fmax(v, 0.0);
+}
+
+/* Tabular batch form: w (n x nt) and sfr (n) at the models' ages tage (n, Gyr). */
+void oracle_sfh_tab_batch(const double *tf, int nt, int n, const double *tage, int ntab, const double *tab_t,
+                          const double *tab_sfr, double *w, double *sfr) {
+#pragma omp parallel
+    {
+        double tmp1[512];
+#pragma omp for
+        for (int m = 0; m < n; ++m) {
+            oracle_sfh_tab_weights(tf, nt, tage[m], ntab, tab_t, tab_sfr, w + (size_t)nt * m, tmp1);
+            if (sfr) sfr[m] = oracle_sfh_tab_sfr(tage[m], ntab, tab_t, tab_sfr);
+        }
+    }
+}
+
 /* Batch form: w (n x nt) and sfr (n) for the parameter rows p (n x SP_COUNT). */
 void oracle_sfh_batch(const double *tf, int nt, int sfh, int n, const double *p, double *w, double *sfr) {
 #pragma omp parallel

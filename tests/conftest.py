@@ -65,12 +65,12 @@ def blend_at_logzsol(data, w, logzsol):
     return blend(data, w, logzsol)
 
 
-def oracle_sfh_csp(oracle, data, sfh, params):
+def oracle_sfh_csp(oracle, data, sfh, params, table=None):
     """The oracle's batch for SFH parameters: its SFH weights, blended at logzsol, through its CSP; L_bol
-    log-blended; the SFR per unit mass formed."""
+    log-blended; the SFR per unit mass formed (the tabular SFHs, sfh 2 and 3: of table = (age [Gyr], sfr))."""
     from oracle.oracle import SFH_NAMES, sfh_weights
     n = len(np.atleast_1d(params["tage"]))
-    w, sfr = sfh_weights(data["log_age"], sfh, params, n)
+    w, sfr = sfh_weights(data["log_age"], sfh, params, n, table=table)
     logzsol = np.broadcast_to(np.asarray(params.get("logzsol", 0.0), dtype=np.float64), (n,))
     wz, lb = blend_at_logzsol(data, w, logzsol)
     out = oracle.csp_batch({k: v for k, v in params.items() if k not in SFH_NAMES and k != "logzsol"}, wz)

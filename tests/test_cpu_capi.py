@@ -60,6 +60,21 @@ def test_host_only_calls(built_lib):
     assert st.value == 101
     lib.opensps_context_set_float(h.value, b"dust2", 0.5, C.byref(st))
     assert st.value == 0
+    # the tabular SFH (host only): ntab out of range and decreasing ages are status 3
+    import numpy as np
+    age, sfr = np.array([0.0, 1.0, 2.0]), np.array([1.0, 2.0, 1.0])
+    dp = C.POINTER(C.c_double)
+    lib.opensps_context_set_sfh_tab(h.value, 3, age.ctypes.data_as(dp), sfr.ctypes.data_as(dp), None, C.byref(st))
+    assert st.value == 0
+    lib.opensps_context_set_sfh_tab(h.value, 0, age.ctypes.data_as(dp), sfr.ctypes.data_as(dp), None, C.byref(st))
+    assert st.value == 3
+    back = age[::-1].copy()
+    lib.opensps_context_set_sfh_tab(h.value, 3, back.ctypes.data_as(dp), sfr.ctypes.data_as(dp), None, C.byref(st))
+    assert st.value == 3
+    lib.opensps_context_set_sfh_tab(9999, 3, age.ctypes.data_as(dp), sfr.ctypes.data_as(dp), None, C.byref(st))
+    assert st.value == 1
+    lib.opensps_context_set_str(h.value, b"sfh_filename", b"my_sfh.dat", C.byref(st))
+    assert st.value == 0
     lib.opensps_context_destroy(h.value, C.byref(st))
     assert st.value == 0
 

@@ -257,3 +257,41 @@ def test_observed_frame_against_direct_evaluation(photometry_data):
                 v = 0.0
             ref = max(v, 0.0) * (1.0 / lam[j])
             assert abs(got[j] - ref) <= 4.0 * np.finfo(np.float64).eps * abs(ref), (m, j, got[j], ref)
+
+
+# ----------------------------------------------------------------------------------------------------- tabular SFH
+# The reference's tabular checks (tests/physics/test_opensps_sfh.f90:283-376,722-749,1065-1106), restated on the
+# batch's path (sfh_weights_core's per-bin linear segments): the square wave's mass, a flat table's mass, a fine
+# table against the analytic SFH of the same shape, the SFR's lookup in years.
+def test_tabular_square_wave_mass():
+    """The reference's square wave drops to an SFR of 0; on the batch's path a bin's segment is normalised by the SFR
+    at its later row (slope / max(sfr, SAFE_FLOOR)), which a zero there sends to ~1e301 and the moments to NaN, in
+    the reference as here: the wave drops to 1e-3 instead (mass 1e9 + 1e6 within the same 1e-2)."""
+    tf = log_grid(50, 6.0, 10.0)
+    w, _ = O.sfh_weights(tf, 3, {"tage": 2.0}, 1, table=([0.0, 1.0, 1.001, 2.0], [1.0, 1.0, 1.0e-3, 1.0e-3]))
+    assert np.any(w > 0.0)
+    assert abs(w.sum() / 1.0e9 - 1.0) <= 1.0e-2
+    z, _ = O.sfh_weights(tf, 3, {"tage": 2.0}, 1, table=([0.0, 1.0, 1.001, 2.0], [1.0, 1.0, 0.0, 0.0]))
+    assert np.all(np.isnan(z))
+
+
+def test_tabular_flat_mass():
+    tf = log_grid(10, 6.0, 10.0)
+    w, _ = O.sfh_weights(tf, 3, {"tage": 10.0}, 1, table=([0.0, 10.0], [1.0, 1.0]))
+    assert np.all(np.isfinite(w))
+    assert abs(w.sum() / 1.0e10 - 1.0) <= 0.05
+
+
+def test_tabular_matches_analytic_delayed_tau():
+    tf = log_grid(80, 6.0, 10.2)
+    tau, tage = 3.0, 9.0
+    t = np.linspace(0.0, tage, 10001)
+    w, _ = O.sfh_weights(tf, 3, {"tage": tage}, 1, table=(t, t * np.exp(-t / tau)))
+    wa, _ = O.sfh_weights(tf, 4, {"tage": tage, "tau": tau}, 1)
+    assert float(np.max(np.abs(w[0] / w.sum() - wa[0]))) <= 1.0e-3 * float(wa.max())
+
+
+def test_tabular_sfr_lookup_in_years():
+    tf = log_grid(10, 6.0, 10.0)
+    _, sfr = O.sfh_weights(tf, 3, {"tage": 1.0}, 1, table=([0.1, 1.0, 2.0], [0.1, 0.5, 0.9]))
+    assert abs(sfr[0] - 0.5) <= 1.0e-12

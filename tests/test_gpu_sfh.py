@@ -1,5 +1,5 @@
 """SFH weights formed on the device (sfh 0, 1, 4 with the constant and burst components; sfh 5, the delayed tau
-with a linear ramp after the truncation), blended at logzsol,
+with a linear ramp after the truncation; the tabular sfh 2 and 3), blended at logzsol,
 through the batch, against the FP64 oracle: spectra <= 1e-4 relative, magnitudes <= 1e-3 mag, mass <= 1e-12
 relative, log L_bol <= 1e-9 relative, the SFR per unit mass formed <= 1e-12 relative.
 
@@ -108,14 +108,80 @@ def test_simha_sfh(data, built_lib):
     c.close()
 
 
-def test_sfh_rejects_nonpositive_age_and_tabular(data, built_lib):
+def _table(seed=71, ntab=300):
+    """A tabular SFH over 0-13.5 Gyr: a bump at 3 Gyr on a wave, one repeated age (a bin of zero width)."""
+    rng = np.random.default_rng(seed)
+    t = np.sort(rng.uniform(0.0, 13.5, ntab))
+    t[0] = 0.0
+    t[100] = t[99]
+    sfr = 1.0 + 0.5 * np.sin(2.0 * t) + 2.0 * np.exp(-0.5 * ((t - 3.0) / 0.7) ** 2)
+    sfr[100] = sfr[99]
+    return t, sfr
+
+
+def _check_tab(got, ora):
+    """The tabular SFH's weights are masses formed, each bin a difference of moments ~ slope t^2 much larger than its
+    mass: the host's and the device's pow differ by an ulp there, so the FP64 sums agree to 1e-10."""
+    assert rel_err_spec(got["spec"], ora["spec"]) <= 1e-4
+    assert float(np.nanmax(np.abs(got["mags"] - ora["mags"]))) <= 1e-3
+    np.testing.assert_allclose(got["mass"], ora["mass"], rtol=1e-10)
+    np.testing.assert_allclose(got["lbol"], ora["lbol"], rtol=1e-9)
+    np.testing.assert_allclose(got["sfr"], ora["sfr"], rtol=1e-12)
+
+
+def _tab_params(n, seed):
+    rng = np.random.default_rng(seed)
+    return {"tage": rng.uniform(0.5, 14.0, n), "logzsol": rng.uniform(-1.5, 0.3, n),
+            "dust2": rng.uniform(0.0, 1.0, n), "zred": rng.uniform(0.1, 3.0, n),
+            "sigma_smooth": rng.uniform(60.0, 250.0, n)}
+
+
+def test_tabular_sfh_from_the_array(data, built_lib):
+    """sfh 3: the table set by opensps_context_set_sfh_tab; models older and younger than the table's span."""
+    from oracle.oracle import Oracle
+    n = 40
+    table = _table()
+    params = _tab_params(n, 72)
+    c = _ctx(3, neb=True, igm=True)
+    c.set_sfh_tab(*table)
+    got = _forward(c, params, n)
+    _check_tab(got, oracle_sfh_csp(Oracle(data, nbands=40), data, 3, params, table=table))
+    c.close()
+
+
+def test_tabular_sfh_from_the_file(data, built_lib):
+    """sfh 2: the table read from sfh_filename under the data root (three columns, the third not read); a missing
+    file and sfh 3 without a table are status 508."""
+    import os
+    from pathlib import Path
+    from libopensps_gb300.capi import OpenSPSError
+    from oracle.oracle import Oracle
+    n = 24
+    t, sfr = _table(seed=73, ntab=120)
+    path = Path(os.environ["OPENSPS_DATA_HOME"]) / "sfh_tab_test.dat"
+    path.write_text("".join(f"{a:.17g} {b:.17g} 0.0142\n" for a, b in zip(t, sfr)))
+    params = _tab_params(n, 74)
+    c = _ctx(2)
+    c.set_str("sfh_filename", "sfh_tab_test.dat")
+    got = _forward(c, params, n)
+    _check_tab(got, oracle_sfh_csp(Oracle(data, nbands=40, add_neb=False, add_igm=False), data, 2, params,
+                                   table=(t, sfr)))
+    c.set_str("sfh_filename", "no_such_sfh.dat")
+    with pytest.raises(OpenSPSError) as e:
+        _forward(c, params, n)
+    assert e.value.status == 508
+    c.close()
+    c = _ctx(3)
+    with pytest.raises(OpenSPSError) as e:
+        _forward(c, params, n)
+    assert e.value.status == 508
+    c.close()
+
+
+def test_sfh_rejects_nonpositive_age(data, built_lib):
     from libopensps_gb300.capi import OpenSPSError
     c = _ctx(4)
     with pytest.raises(OpenSPSError) as e:
         _forward(c, {"tage": np.array([1.0, 0.0]), "tau": np.array([1.0, 1.0])}, 2)
-    assert e.value.status == 2
-    c.set_int("sfh", 3)
-    with pytest.raises(OpenSPSError) as e:
-        _forward(c, {"tage": np.array([1.0]), "tau": np.array([1.0])}, 1)
     assert e.value.status == 2
     c.close()

@@ -115,6 +115,37 @@ def test_simha_rows_match_central_differences(data, built_lib):
     c.close()
 
 
+def test_tabular_sfh_rows(data, built_lib):
+    """sfh 3: the SFH rows are zero (the tabular SFH has no parameters in the reference's tangents); logzsol's row
+    against central differences."""
+    from libopensps_gb300.capi import Context
+    from oracle.oracle import Oracle
+    n = 5
+    rng = np.random.default_rng(85)
+    t = np.linspace(0.0, 13.0, 60)
+    table = (t, 1.0 + 0.5 * np.sin(t))
+    params = {"tage": rng.uniform(3.0, 12.0, n), "logzsol": rng.uniform(-1.5, 0.3, n),
+              "dust2": rng.uniform(0.1, 1.0, n), "zred": rng.uniform(0.2, 2.0, n),
+              "sigma_smooth": rng.uniform(60.0, 250.0, n)}
+    c = Context()
+    c.set_int("sfh", 3)
+    c.set_sfh_tab(*table)
+    c.set_int("add_neb_emission", 1)
+    mb, sb, massb, lbolb = _cot(c, n, 86)
+    got = c.csp_batch_grad(params, mags_bar=mb, spec_bar=sb, mass_bar=massb, lbol_bar=lbolb, n=n)
+    for k in ("tage", "tau", "const", "fburst", "tburst", "sf_start", "sf_trunc"):
+        assert np.all(got["params_bar"][:, ROWS[k]] == 0.0)
+    assert np.all(got["params_bar"][:, 25] == 0.0)
+    o = Oracle(data, nbands=40, add_igm=False)
+    h = H_REL * np.abs(params["logzsol"])
+    up = oracle_sfh_csp(o, data, 3, dict(params, logzsol=params["logzsol"] + h), table=table)
+    dn = oracle_sfh_csp(o, data, 3, dict(params, logzsol=params["logzsol"] - h), table=table)
+    fd = (_loss(up, mb, sb, massb, lbolb) - _loss(dn, mb, sb, massb, lbolb)) / (2.0 * h)
+    g = got["params_bar"][:, ROWS["logzsol"]]
+    assert float(np.max(np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd))))) <= RTOL
+    c.close()
+
+
 def test_weights_bar_and_logzsol_with_given_weights(data, built_lib):
     """ssp_weights (one weight per age) blended at logzsol: weights_bar along a random relative direction, and
     logzsol's row."""
