@@ -698,14 +698,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
-        if (c.imf_type < 0 || c.imf_type > 2) {
-            err = "imf_type " + std::to_string(c.imf_type) + ": 0 (Salpeter), 1 (Chabrier) and 2 (Kroupa) with the operators";
+        if (c.imf_type < 0 || c.imf_type > 4) {
+            err = "imf_type " + std::to_string(c.imf_type) +
+                  ": 0 (Salpeter), 1 (Chabrier), 2 (Kroupa), 3 (van Dokkum) and 4 (Dave) with the operators";
             return ST_UNSUPPORTED;
         }
         nacc2 = true;
     } else {
         for (int m = 0; m < n; ++m)
-            for (int id : {PF_IMF1, PF_IMF2, PF_IMF3})
+            for (int id : {PF_IMF1, PF_IMF2, PF_IMF3, PF_VDMC, PF_MDAVE})
                 if (par(m, id) != c.pdef[id]) {
                     err = "an IMF per model needs the SSP operators (opensps_context_build_ssp_ops)";
                     return ST_UNSUPPORTED;
@@ -1127,9 +1128,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             // ---- the operator: the IMF weights folded with the SFH weights, the template GEMM, then the epilogue
             std::vector<double> al((size_t)3 * n);
             for (int m = 0; m < n; ++m) {
-                al[3 * m] = par(m, PF_IMF1); al[3 * m + 1] = par(m, PF_IMF2); al[3 * m + 2] = par(m, PF_IMF3);
-                // (Salpeter: the Kroupa form with the three slopes 2.35; Chabrier: not read)
-                if (c.imf_type != 2) al[3 * m] = al[3 * m + 1] = al[3 * m + 2] = 2.35;
+                const double pv[5] = {par(m, PF_IMF1), par(m, PF_IMF2), par(m, PF_IMF3), par(m, PF_VDMC), par(m, PF_MDAVE)};
+                imf_pack(c.imf_type, pv, al.data() + 3 * m);
             }
             if ((e = c.d_alpha.reserve(al.size())) != cudaSuccess || (e = c.d_yo.reserve((size_t)2 * n * ns + 4)) != cudaSuccess ||
                 (e = cudaMemcpyAsync(c.d_alpha.p, al.data(), sizeof(double) * al.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) {

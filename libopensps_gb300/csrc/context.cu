@@ -27,10 +27,11 @@ static const ParamInfo PARAMS[] = {
     {"imf2", PF_IMF2, 2.3}, {"imf3", PF_IMF3, 2.3}, {"duste_qpah", PF_DUSTE_QPAH, 3.5},
     {"duste_umin", PF_DUSTE_UMIN, 1.0}, {"duste_gamma", PF_DUSTE_GAMMA, 0.01}, {"fagn", PF_FAGN, 0.0},
     {"agn_tau", PF_AGN_TAU, 10.0}, {"sf_slope", PF_SF_SLOPE, 0.0},
+    {"vdmc", PF_VDMC, 0.08}, {"mdave", PF_MDAVE, 0.5},
     // known to the reference, not varied per model by this path (gas_logz and gas_logu are: the nebular continuum;
     // mwr and uvb are, by the batch, with dust_type 1)
     {"afe", -1, 0.0}, {"fbhb", -1, 0.0}, {"sbss", -1, 0.0}, {"agb", -1, 1.0},
-    {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"vdmc", -1, 0.08}, {"mdave", -1, 0.5}, {"imf_lower_limit", -1, 0.08},
+    {"pagb", -1, 1.0}, {"redgb", -1, 1.0}, {"delt", -1, 0.0}, {"dell", -1, 0.0}, {"imf_lower_limit", -1, 0.08},
     {"imf_upper_limit", -1, 120.0}, {"masscut", -1, 150.0}, {"agb_dust", -1, 1.0}, {"pmetals", -1, 0.02},
     {"fcstar", -1, 1.0}, {"frac_xrb", -1, 1.0}, {"dust_clumps", -1, -99.0}, {"uvb", PF_UVB, 1.0}, {"mwr", PF_MWR, 3.1},
     {"gas_logu", PF_GAS_LOGU, -2.0},

@@ -25,7 +25,7 @@ enum ParamId {
     PAR_DEVICE,                  // = 13: the per-model table of the device kernels stops here
     PF_LOGZSOL = PAR_DEVICE, PF_TAGE, PF_TAU, PF_MIN_WAVE_SMOOTH, PF_MAX_WAVE_SMOOTH, PF_CONST, PF_FBURST,
     PF_TBURST, PF_SF_START, PF_SF_TRUNC, PF_IMF1, PF_IMF2, PF_IMF3, PF_DUSTE_QPAH, PF_DUSTE_UMIN, PF_DUSTE_GAMMA,
-    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU, PF_SF_SLOPE,
+    PF_FAGN, PF_AGN_TAU, PF_GAS_LOGZ, PF_GAS_LOGU, PF_SF_SLOPE, PF_VDMC, PF_MDAVE,
     PF_COUNT
 };
 
@@ -381,6 +381,7 @@ void fp64_release(Context &c);
 int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err);
 int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, const double *h_alpha, int itesc,
                   float *d_young, float *d_old, std::string &err);
+void imf_pack(int imf_type, const double *pv, double *ap);
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err);
 // With profiling on: records event k on the context's stream (0 starts a batch's set).

@@ -307,9 +307,11 @@ struct OpsPoint {
 };
 struct OpsFoldArgs {
     int n, nt, nz, npt, nent, ntpad, itesc;
+    int imf_type = 2;         // 0 Salpeter (as Kroupa), 2 Kroupa, 3 van Dokkum, 4 Dave
     float lower_bound, lim_lo, lim_hi;
     const double *wz;         // n x nt x nz SFH weights (age fastest)
-    const double *alpha;      // n x 3: the Kroupa slopes (imf1, imf2, imf3)
+    const double *alpha;      // n x 3: the IMF's parameters (Kroupa: imf1-3; van Dokkum: vdmc; Dave: imf1, imf2,
+                              // mdave)
     const OpsPoint *pts;      // (nt x nz) x npt
     const uint32_t *ent;      // (nt x nz) x nent: template << 16 | point, sorted by template within a grid point
     const float *ent_c;       // the entries' coefficients
@@ -343,10 +345,10 @@ struct OpsInterpReduceArgs {
 // metallicities and of the three Kroupa slopes.
 struct OpsRevArgs {
     int n, nt, nz, npt, ntpad, itesc;
-    int imf_type = 2;         // the slopes' rows are written only for Kroupa (2); zero otherwise
+    int imf_type = 2;         // the IMF's rows: Kroupa (2) imf1-3, Dave (4) imf1, imf2, mdave; zero otherwise
     float lim_lo, lim_hi;
     const double *wz;         // n x nt x nz SFH weights (age fastest)
-    const double *alpha;      // n x 3 Kroupa slopes
+    const double *alpha;      // n x 3: the IMF's parameters (as OpsFoldArgs)
     const OpsPoint *pts;      // (nt x nz) x npt
     const ushort4 *pidx;      // (nt x nz) x npt: each point's four templates
     const float4 *pcoef;      // and their coefficients
@@ -356,7 +358,7 @@ struct OpsRevArgs {
     const double *sums;       // n x 6: the forward's mass and linear L_bol
     double *wzb;              // n x nt x nz: the weights' cotangent (every grid point), or null (slopes only)
     double *apart;            // nz x n x 3: each slab's slope cotangents / cscale
-    double *params_bar;       // n x rows: the slopes' rows row_imf1 .. row_imf1 + 2 (written), or null
+    double *params_bar;       // n x rows: the IMF's rows from row_imf1 (imf1-3, vdmc, mdave; written), or null
     int rows, row_imf1;
 };
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st);

@@ -3,9 +3,12 @@
 // as a split-BF16 tcgen05 GEMM.
 //
 //   IMF bin weights  compute_imf_weights / imf_bin_weights_tab (src/physics/opensps_imf.f90:111-172, 439-559): per
-//                    isochrone point the Kroupa IMF's number of stars over its mass bin, over the IMF's mass between
-//                    its limits; inside one power-law segment c lo^e expm1(e ln(hi / lo)) / e (e = 1 - alpha), in FP32
+//                    isochrone point the IMF's number of stars over its mass bin, over the IMF's mass between its
+//                    limits; inside one power-law segment c lo^e expm1(e ln(hi / lo)) / e (e = 1 - alpha), in FP32
 //                    with the segment's constants (FP64) formed once per model, as the reference's FP32 kernels do.
+//                    Kroupa (and Salpeter as Kroupa with equal slopes) with its fixed breaks; van Dokkum 2008 (a
+//                    lognormal up to 25 vdmc, a power law above) and Dave 2008 (slopes imf1 below mdave, imf2 above)
+//                    with breaks per model (imf_integral :206-315).
 //   fold             fold_multi (src/physics/opensps_ssp_batch.f90:3095-3188): V(e, m) = sum over points of S(e, p)
 //                    w_IMF(p, m) wsfh(age(p), m), young ages and old apart, with the mass and L_bol rows.
 //   template product template_columns (:3247-3385): spectra(pixel, m) = sum_e library(pixel, e) V(e, m).
@@ -50,9 +53,19 @@ __device__ __forceinline__ float ops_expm1(float y) {
     return ops_ex2(y * 1.4426950408889634f) - 1.f;
 }
 
+// One model's IMF as the fold kernels take it: up to three segments [lo, hi], each a power law c m^-alpha (e = 1 -
+// alpha, ce = c / e). Kroupa's breaks are fixed (each point's segment found once, OpsPoint::seg); van Dokkum's and
+// Dave's move with the model (generic: every bin split at the model's breaks). For van Dokkum segment 0 is the
+// lognormal A exp(-z^2) per unit ln m, z = (log10 m - u0) zs (zs = 1 / (sigma sqrt 2)), whose bin integral is
+// la int e^(-z^2) dz (la = A ln 10 sigma sqrt 2). For the reverse pass: lnb = ln b of the continuity factor
+// c2 = b^(alpha2 - alpha1) (Kroupa b = 0.5, Dave b = mdave) and d3 = d ln c2 / d(third parameter) (Dave:
+// (alpha2 - alpha1) / mdave; Kroupa: 0, its third slope acts through segment 3).
 struct KroupaSeg {
     float e[3], ce[3], c[3];
     float lo[3], hi[3];
+    int generic, logn;
+    float la, u0, zs;
+    double lnb, d3;
 };
 
 // c lo^e expm1(e dl) / e over one segment (e = 0: c dl)
@@ -61,15 +74,32 @@ __device__ __forceinline__ float seg_piece(const KroupaSeg &k, int s, float ln_l
     return k.ce[s] * ops_ex2(k.e[s] * ln_lo * 1.4426950408889634f) * ops_expm1(k.e[s] * dl);
 }
 
+// van Dokkum's lognormal over [lo, hi] (integrate_lognormal, src/physics/opensps_imf.f90:677-722, number): la times
+// int e^(-z^2) dz, by 3-point Gauss-Legendre on a bin narrower than 0.1 in z (erf's difference would cancel), else
+// by the difference of erf (erfc in a tail).
+__device__ __forceinline__ float logn_piece(const KroupaSeg &k, float lo, float hi) {
+    const float z1 = (log10f(lo) - k.u0) * k.zs, z2 = (log10f(hi) - k.u0) * k.zs;
+    if (z2 - z1 < 0.1f) {
+        const float zc = 0.5f * (z1 + z2), zh = 0.5f * (z2 - z1), x = 0.7745966692414834f * zh;
+        const float q = (8.f / 9.f) * __expf(-zc * zc) +
+                        (5.f / 9.f) * (__expf(-(zc - x) * (zc - x)) + __expf(-(zc + x) * (zc + x)));
+        return k.la * zh * q;
+    }
+    const float c = k.la * 0.8862269254527580f;   // sqrt(pi) / 2
+    if (z1 >= 0.f) return c * (erfcf(z1) - erfcf(z2));
+    if (z2 <= 0.f) return c * (erfcf(-z2) - erfcf(-z1));
+    return c * (erff(z2) - erff(z1));
+}
+
 __device__ __forceinline__ float imf_weight(const KroupaSeg &k, const OpsPoint &q) {
-    if (q.seg > 0) return seg_piece(k, q.seg - 1, q.ln_lo, q.dl);
     if (q.seg < 0) return 0.f;
-    // a bin across a segment boundary: its pieces in each segment
+    if (q.seg > 0 && !k.generic) return seg_piece(k, q.seg - 1, q.ln_lo, q.dl);
+    // a bin across a segment boundary (or any bin with the breaks per model): its pieces in each segment
     float v = 0.f;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
-        if (hi > lo) v += seg_piece(k, s, logf(lo), logf(hi / lo));
+        if (hi > lo) v += (s == 0 && k.logn) ? logn_piece(k, lo, hi) : seg_piece(k, s, logf(lo), logf(hi / lo));
     }
     return v;
 }
@@ -138,12 +168,111 @@ __device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_h
     }
     inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
     if (total_out) *total_out = total;
+    k.generic = 0;
+    k.logn = 0;
+    k.la = k.u0 = k.zs = 0.f;
+    k.lnb = -KR_LN2;
+    k.d3 = 0.0;
     if (dlnT) {
         const double it = total > 0.0 ? 1.0 / total : 0.0;
         dlnT[0] = (-dp[0] + KR_LN2 * t12) * it;
         dlnT[1] = (-dp[1] - KR_LN2 * t12) * it;
         dlnT[2] = -dp[2] * it;
     }
+}
+
+// Dave 2008 (p = alpha1, alpha2, mdave): m^-alpha1 over [0.08, mdave], mdave^(alpha2 - alpha1) m^-alpha2 above
+// (imf_integral case 4); 1 / T and, with dlnT, d ln T / d(alpha1, alpha2, mdave) (imf_integral_dp case 4: the
+// moving break's edge terms cancel, the IMF being continuous there).
+__device__ inline void dave_setup(const double *p, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
+                                  double *dlnT, double *total_out = nullptr) {
+    const double a1 = p[0], a2 = p[1], md = p[2];
+    const double c2 = pow(md, -a1 + a2);
+    const double al[2] = {a1, a2}, cs[2] = {1.0, c2}, slo[2] = {0.08, md}, shi[2] = {md, 1.0e30};
+    double total = 0.0, t12 = 0.0, dp[2] = {0.0, 0.0};
+    for (int sg = 0; sg < 2; ++sg) {
+        const double e = 1.0 - al[sg];
+        k.e[sg] = (float)e;
+        k.c[sg] = (float)cs[sg];
+        k.ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
+        k.lo[sg] = (float)slo[sg];
+        k.hi[sg] = (float)shi[sg];
+        const double lo = fmax((double)lim_lo, slo[sg]), hi = fmin((double)lim_hi, shi[sg]);
+        if (hi > lo) {
+            const double em = 2.0 - al[sg];
+            const double piece = (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
+            total += piece;
+            if (sg == 1) t12 = piece;
+            const double ll = log(lo), dl = log(hi / lo), x = em * dl;
+            dp[sg] = cs[sg] * pow(lo, em) * dl * (ll * kr_g1(x) + dl * kr_g2(x));
+        }
+    }
+    k.e[2] = k.c[2] = k.ce[2] = 0.f;
+    k.lo[2] = k.hi[2] = 1.0e30f;
+    inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
+    if (total_out) *total_out = total;
+    k.generic = 1;
+    k.logn = 0;
+    k.la = k.u0 = k.zs = 0.f;
+    k.lnb = log(md);
+    k.d3 = (a2 - a1) / md;
+    if (dlnT) {
+        const double it = total > 0.0 ? 1.0 / total : 0.0;
+        dlnT[0] = (-dp[0] - k.lnb * t12) * it;
+        dlnT[1] = (-dp[1] + k.lnb * t12) * it;
+        dlnT[2] = k.d3 * t12 * it;
+    }
+}
+
+// van Dokkum 2008 (p[0] = vdmc): the lognormal 0.14 (12.5 vdmc)^-1.3 exp(-(log10 m - log10 vdmc)^2 / (2 0.69^2)) per
+// unit ln m up to 25 vdmc, 0.0443 m^-2.3 above (imf_integral case 3, constants src/physics/opensps_imf.f90:39-44);
+// 1 / T with the lognormal's mass in closed form (its centre shifted by ln 10 sigma^2). No parameters in the reverse
+// pass (imf_integral_dp has none for it): dlnT zero.
+__device__ inline void vd_setup(const double *p, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
+                                double *dlnT, double *total_out = nullptr) {
+    const double vdmc = p[0], br = 25.0 * vdmc, s2 = 0.69 * 0.69, sig = 0.69, K = 2.302585092994046;
+    const double A = 0.14 * pow(0.5 * br, -1.3), u0 = log10(vdmc);
+    double total = 0.0;
+    // the lognormal's mass over [lim_lo, min(lim_hi, 25 vdmc)]: A e^(K u0 + K^2 sigma^2 / 2) K sigma sqrt(pi / 2)
+    // (erf(z2) - erf(z1)), z about the shifted centre
+    double lo = (double)lim_lo, hi = fmin((double)lim_hi, br);
+    if (hi > lo) {
+        const double cen = u0 + K * s2, sc = exp(K * u0 + 0.5 * K * K * s2) * K * sig * sqrt(0.5 * 3.141592653589793);
+        const double z1 = (log10(lo) - cen) / (sig * 1.4142135623730951), z2 = (log10(hi) - cen) / (sig * 1.4142135623730951);
+        const double d = z1 >= 0.0 ? erfc(z1) - erfc(z2) : (z2 <= 0.0 ? erfc(-z2) - erfc(-z1) : erf(z2) - erf(z1));
+        total += A * sc * d;
+    }
+    lo = fmax((double)lim_lo, br);
+    hi = (double)lim_hi;
+    if (hi > lo) total += 0.0443 * pow(lo, -0.3) * expm1(-0.3 * log(hi / lo)) / -0.3;
+    k.e[0] = k.c[0] = k.ce[0] = 0.f;
+    k.lo[0] = 0.f;
+    k.hi[0] = (float)br;
+    k.e[1] = -1.3f;
+    k.c[1] = 0.0443f;
+    k.ce[1] = (float)(0.0443 / -1.3);
+    k.lo[1] = (float)br;
+    k.hi[1] = 1.0e30f;
+    k.e[2] = k.c[2] = k.ce[2] = 0.f;
+    k.lo[2] = k.hi[2] = 1.0e30f;
+    inv_total = total > 0.0 ? (float)(1.0 / total) : 1.f;
+    if (total_out) *total_out = total;
+    k.generic = 1;
+    k.logn = 1;
+    k.la = (float)(A * K * sig * 1.4142135623730951);
+    k.u0 = (float)u0;
+    k.zs = (float)(1.0 / (sig * 1.4142135623730951));
+    k.lnb = 0.0;
+    k.d3 = 0.0;
+    if (dlnT) dlnT[0] = dlnT[1] = dlnT[2] = 0.0;
+}
+
+// The model's IMF by type (0 Salpeter and 2 Kroupa through the Kroupa form, 3 van Dokkum, 4 Dave).
+__device__ inline void imf_setup(int imf_type, const double *p, float lim_lo, float lim_hi, KroupaSeg &k,
+                                 float &inv_total, double *dlnT) {
+    if (imf_type == 3) vd_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
+    else if (imf_type == 4) dave_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
+    else kroupa_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
 }
 
 // A point's IMF bin weight (before the normalisation) and its derivatives: phi = sum of its segments' pieces
@@ -164,7 +293,7 @@ __device__ __forceinline__ ImfTan imf_weight_tan(const KroupaSeg &k, const OpsPo
     ImfTan r = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (q.seg < 0) return r;
     float P, D;
-    if (q.seg > 0) {
+    if (q.seg > 0 && !k.generic) {
         const int s = q.seg - 1;
         seg_piece_tan(k, s, q.ln_lo, q.dl, P, D);
         r.phi = P;
@@ -178,7 +307,12 @@ __device__ __forceinline__ ImfTan imf_weight_tan(const KroupaSeg &k, const OpsPo
     for (int s = 0; s < 3; ++s) {
         const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
         if (hi > lo) {
-            seg_piece_tan(k, s, logf(lo), logf(hi / lo), P, D);
+            if (s == 0 && k.logn) {   // (van Dokkum's lognormal: no parameter of the reverse pass)
+                P = logn_piece(k, lo, hi);
+                D = 0.f;
+            } else {
+                seg_piece_tan(k, s, logf(lo), logf(hi / lo), P, D);
+            }
             r.phi += P;
             if (s == 0) r.d0 += D;
             else if (s == 1) r.d1 += D;
@@ -224,7 +358,7 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_fold_kernel(OpsFoldArgs a)
         sw_s[t][k] = (sw > SAFE_FLOOR) ? (float)sw : 0.f;
     }
     if (tid < OPS_K)
-        kroupa_setup(a.alpha + 3 * min(m0 + tid, a.n - 1), a.lim_lo, a.lim_hi, kseg[tid], inv_total[tid], nullptr);
+        imf_setup(a.imf_type, a.alpha + 3 * min(m0 + tid, a.n - 1), a.lim_lo, a.lim_hi, kseg[tid], inv_total[tid], nullptr);
     __syncthreads();
     if (tid == 0) {
         int na = 0;
@@ -633,7 +767,7 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_rev_kernel(OpsRevArgs a) {
     if (tid < OPS_K) {
         const int k = tid, m = min(m0 + k, a.n - 1);
         double dl[3];
-        kroupa_setup(a.alpha + 3 * m, a.lim_lo, a.lim_hi, kseg[k], inv_total[k], dl);
+        imf_setup(a.imf_type, a.alpha + 3 * m, a.lim_lo, a.lim_hi, kseg[k], inv_total[k], dl);
         for (int j = 0; j < 3; ++j) dlnT_s[k][j] = dl[j];
         const double cs = a.cscale[m];
         const double ls = a.sums[(size_t)6 * m + 1];
@@ -750,7 +884,9 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_rev_kernel(OpsRevArgs a) {
             double u[4] = {0.0, 0.0, 0.0, 0.0};
             for (int w = 0; w < OPS_THREADS / 32; ++w)
                 for (int i = 0; i < 4; ++i) u[i] += ured[w][k][i];
-            const double A[3] = {-u[0] + KR_LN2 * u[3], -u[1] - KR_LN2 * u[3], -u[2]};
+            // d phi / d(alpha1, alpha2, third) = (-D_1 - ln b p12, -D_2 + ln b p12, -D_3 + d3 p12)
+            const double lnb = kseg[k].lnb, d3 = kseg[k].d3;
+            const double A[3] = {-u[0] - lnb * u[3], -u[1] + lnb * u[3], -u[2] + d3 * u[3]};
             for (int j = 0; j < 3; ++j)
                 a.apart[((size_t)z * a.n + m) * 3 + j] = it_k * A[j] - dlnT_s[k][j] * b;
         }
@@ -764,8 +900,17 @@ __global__ void ops_rev_finish_kernel(OpsRevArgs a) {
     double s[3] = {0.0, 0.0, 0.0};
     for (int z = 0; z < a.nz; ++z)
         for (int j = 0; j < 3; ++j) s[j] += a.apart[((size_t)z * a.n + m) * 3 + j];
-    // (the slopes are the Kroupa IMF's; with Salpeter, taken as Kroupa with fixed equal slopes, they are not parameters)
-    for (int j = 0; j < 3; ++j) a.params_bar[(size_t)a.rows * m + a.row_imf1 + j] = a.imf_type == 2 ? a.cscale[m] * s[j] : 0.0;
+    // Kroupa: imf1-3; Dave: imf1, imf2 and mdave (row_imf1 + 4); the others (Salpeter as Kroupa with fixed equal
+    // slopes, van Dokkum) have none: zero
+    double *pb = a.params_bar + (size_t)a.rows * m + a.row_imf1;
+    for (int j = 0; j < 5; ++j) pb[j] = 0.0;
+    if (a.imf_type == 2)
+        for (int j = 0; j < 3; ++j) pb[j] = a.cscale[m] * s[j];
+    if (a.imf_type == 4) {
+        pb[0] = a.cscale[m] * s[0];
+        pb[1] = a.cscale[m] * s[1];
+        pb[4] = a.cscale[m] * s[2];
+    }
 }
 
 cudaError_t run_ops_reverse(const OpsRevArgs &a, cudaStream_t st) {
@@ -1708,6 +1853,7 @@ int ops_build(Context &c, std::string &err) {
 static bool ops_interp_ok(const Context &c, const double *h_alpha, int n) {
     if (!c.ops.interp_ready || c.ops_exact || !h_alpha) return false;
     if (c.imf_type == 1) return true;   // (Chabrier: no slopes)
+    if (c.imf_type == 3 || c.imf_type == 4) return false;   // (breaks per model: the exact fold)
     for (int m = 0; m < n; ++m)
         for (int s = 0; s < 3; ++s)
             if (!(std::fabs(h_alpha[3 * (size_t)m + s]) <= OPS_AMAX[s])) return false;
@@ -1848,6 +1994,7 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     c.ops_launches += 2;                 // the fold and its slab reduction
     OpsFoldArgs fa;
     fa.n = n; fa.nt = c.nt; fa.nz = c.nz; fa.npt = o.npt; fa.nent = o.nent; fa.ntpad = o.ntpad; fa.itesc = itesc;
+    fa.imf_type = c.imf_type;
     fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;
     fa.wz = d_wz; fa.alpha = d_alpha; fa.pts = o.pts.p; fa.ent = o.ent.p; fa.ent_c = o.ent_c.p;
     fa.v_hi = c.d_vhi.p; fa.v_lo = c.d_vlo.p; fa.sums = c.d_sums.p;
@@ -1870,12 +2017,22 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     return 0;
 }
 
+// The operator kernels' three IMF parameters of a model from imf1, imf2, imf3, vdmc, mdave (pv): Kroupa the slopes,
+// Salpeter the Kroupa form with the slopes 2.35 (Chabrier: not read), van Dokkum vdmc, Dave imf1, imf2 and mdave.
+void imf_pack(int imf_type, const double *pv, double *ap) {
+    ap[0] = pv[0]; ap[1] = pv[1]; ap[2] = pv[2];
+    if (imf_type == 0 || imf_type == 1) ap[0] = ap[1] = ap[2] = 2.35;
+    else if (imf_type == 3) { ap[0] = pv[3]; ap[1] = ap[2] = 0.0; }
+    else if (imf_type == 4) ap[2] = pv[4];
+}
+
 // One IMF's SSP grid at the context's metallicity zmet: every age as a "model" with a unit weight there.
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err) {
     if (!c.ops.ready) { err = "no SSP operators on the context (opensps_context_build_ssp_ops)"; return ST_NO_OPERATOR; }
-    if (imf_type < 0 || imf_type > 2) {
-        err = "imf_type " + std::to_string(imf_type) + ": 0 (Salpeter), 1 (Chabrier) or 2 (Kroupa) on this path";
+    if (imf_type < 0 || imf_type > 4) {
+        err = "imf_type " + std::to_string(imf_type) +
+              ": 0 (Salpeter), 1 (Chabrier), 2 (Kroupa), 3 (van Dokkum) or 4 (Dave) on this path";
         return ST_UNSUPPORTED;
     }
     // (the operator batch takes the context's imf_type: this IMF for the call)
@@ -1888,9 +2045,13 @@ int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mas
     const int nt = c.nt, nz = c.nz, ns = c.nspec;
     const int z = std::max(1, std::min(c.zmet, nz)) - 1;
     std::vector<double> wz((size_t)nt * nt * nz, 0.0), alpha((size_t)3 * nt);
-    double a1 = imf_params ? imf_params[0] : c.pdef[PF_IMF1], a2 = imf_params ? imf_params[1] : c.pdef[PF_IMF2];
-    double a3 = imf_params ? imf_params[2] : c.pdef[PF_IMF3];
-    if (imf_type != 2) a1 = a2 = a3 = 2.35;   // (Salpeter as Kroupa with equal slopes; Chabrier: not read)
+    // imf_params: imf1, imf2, imf3, vdmc, mdave
+    double pv[5] = {c.pdef[PF_IMF1], c.pdef[PF_IMF2], c.pdef[PF_IMF3], c.pdef[PF_VDMC], c.pdef[PF_MDAVE]};
+    if (imf_params)
+        for (int j = 0; j < 5; ++j) pv[j] = imf_params[j];
+    double ap[3];
+    imf_pack(imf_type, pv, ap);
+    const double a1 = ap[0], a2 = ap[1], a3 = ap[2];
     for (int t = 0; t < nt; ++t) {
         wz[(size_t)nt * nz * t + t + (size_t)nt * z] = 1.0;
         alpha[3 * t] = a1; alpha[3 * t + 1] = a2; alpha[3 * t + 2] = a3;

@@ -7,7 +7,9 @@
  *                            IMF mass limits weigh nothing; normalised by the IMF's mass over the limits)
  *   imf_integral             src/physics/opensps_imf.f90:206-315: case 2 Kroupa (segments 0.08-0.5-1.0, slopes
  *                            alpha1-3), case 0 Salpeter (slope 2.35, opensps_context_types.f90:120), case 1 Chabrier
- *                            2003 (the lognormal below 1 M_sun, integrate_lognormal :640-700, and the power law above)
+ *                            2003 (the lognormal below 1 M_sun, integrate_lognormal :677-722, and the power law above),
+ *                            case 3 van Dokkum 2008 (the scaled lognormal up to 25 vdmc, the power law above; constants
+ *                            :39-44), case 4 Dave 2008 (slopes alpha1 below mdave and alpha2 above, continuous)
  *   integrate_powerlaw       src/physics/opensps_imf.f90:725-748 (the expm1 form: oracle_powerlaw_bin)
  *   ssp_op_model_weights / ssp_op_spmv   src/physics/opensps_ssp_operator.f90:1296-1338: W = S . w_IMF with the
  *                            mass and L_bol rows
@@ -31,7 +33,8 @@ typedef struct {
     const double *coef;        /* nz x nt x npt x 4 */
     const double *mcur, *lum;  /* nz x nt x npt */
     double lower_bound, lim_lo, lim_hi;
-    int imf_type;              /* 0 Salpeter, 1 Chabrier, 2 Kroupa (alpha per model) */
+    int imf_type;              /* 0 Salpeter, 1 Chabrier, 2 Kroupa (alpha per model: imf1-3), 3 van Dokkum (alpha[0]
+                                  = vdmc), 4 Dave (alpha = imf1, imf2, mdave) */
 } oracle_ops_t;
 
 /* integrate_powerlaw(lo, hi, alpha, mass_weighted, c) */
@@ -59,7 +62,7 @@ double oracle_kroupa_integral(const double *a, double m1, double m2, int mass_we
  * (or mass) over [m1, m2] in closed form, K sigma sqrt(pi / 2) (erf(z2) - erf(z1)) with z = (log10 m - centre) /
  * (sigma sqrt 2) (the mass-weighted form shifts the centre by K sigma^2 and scales by exp(K log_mc + K^2 sigma^2 / 2),
  * K = ln 10); for a bin narrower than 0.1 in z a 5-point Gauss-Legendre rule on exp(-z^2), and erfc in a tail, against
- * the cancellation of erf near 1 (integrate_lognormal, src/physics/opensps_imf.f90:640-700). */
+ * the cancellation of erf near 1 (integrate_lognormal, src/physics/opensps_imf.f90:677-722). */
 static double lognormal(double m1, double m2, double log_mc, double sigma2, int mass_weighted) {
     const double K = log(10.0), sig = sqrt(sigma2);
     const double centre = mass_weighted ? log_mc + K * sigma2 : log_mc;
@@ -82,7 +85,8 @@ static double lognormal(double m1, double m2, double log_mc, double sigma2, int 
     return c * (erf(z2) - erf(z1));
 }
 
-/* imf_integral by type: number (mass_weighted 0) or mass over [m1, m2]; a: Kroupa slopes (type 2). */
+/* imf_integral by type: number (mass_weighted 0) or mass over [m1, m2]; a: the Kroupa slopes (type 2), vdmc (a[0],
+ * type 3) or the Dave slopes and break mass (type 4). */
 double oracle_imf_integral(int imf_type, const double *a, double m1, double m2, int mass_weighted) {
     const double lo = fmin(m1, m2), hi = fmax(m1, m2);
     if (hi <= lo) return 0.0;
@@ -93,6 +97,22 @@ double oracle_imf_integral(int imf_type, const double *a, double m1, double m2, 
         double v = 0.0;
         if (fmin(hi, 1.0) > lo) v += lognormal(lo, fmin(hi, 1.0), lmc, s2, mass_weighted);
         if (hi > fmax(lo, 1.0)) v += powerlaw(fmax(lo, 1.0), hi, 2.3, mass_weighted, exp(-lmc * lmc / (2.0 * s2)));
+        return v;
+    }
+    if (imf_type == 3) {
+        const double vdmc = a[0], br = 25.0 * vdmc, s2 = 0.69 * 0.69;
+        double v = 0.0;
+        if (fmin(hi, br) > lo)
+            v += 0.14 * pow(0.5 * br, -1.3) * lognormal(lo, fmin(hi, br), log10(vdmc), s2, mass_weighted);
+        if (hi > fmax(lo, br)) v += powerlaw(fmax(lo, br), hi, 2.3, mass_weighted, 0.0443);
+        return v;
+    }
+    if (imf_type == 4) {
+        const double md = a[2];
+        double v = 0.0, sl = fmax(lo, 0.08), sh = fmin(hi, md);
+        if (sh > sl) v += powerlaw(sl, sh, a[0], mass_weighted, 1.0);
+        sl = fmax(lo, md);
+        if (hi > sl) v += powerlaw(sl, hi, a[1], mass_weighted, pow(md, -a[0] + a[1]));
         return v;
     }
     return 0.0;

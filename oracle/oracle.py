@@ -401,7 +401,8 @@ class Oracle:
 
 class OpsOracle:
     """The SSP operator applied to per-model IMFs (ops_oracle.c) over the operator dataset (synth_ops): imf_type 2
-    Kroupa (alpha per model), 0 Salpeter, 1 Chabrier."""
+    Kroupa (alpha per model: imf1-3), 0 Salpeter, 1 Chabrier, 3 van Dokkum (alpha[:, 0] = vdmc), 4 Dave (alpha =
+    imf1, imf2, mdave)."""
 
     def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0, imf_type: int = 2):
         self.ops = ops

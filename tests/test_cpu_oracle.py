@@ -3,6 +3,10 @@
 * the IMF power-law bin integrals against the reference's 60-digit known-answer table
   (tests/golden/imf_powerlaw_bins.txt, made by the reference's own generator), within 1e-14 as the reference's
   test_powerlaw_bin_worst_cases;
+* the IMF integrals of every analytic type (Salpeter, Chabrier, Kroupa, van Dokkum, Dave) against Simpson quadrature
+  of the IMF's density, number and mass weighted, on the reference's intervals within its 1e-8
+  (tests/physics/test_opensps_imf.f90:236-255,383-408, the density of get_imf_value src/physics/opensps_imf.f90:
+  903-1010), and a wide lognormal bin equal to the sum of its narrow bins within 1e-13 (:344-381);
 * identities the reference's batch tests use (tests/test_csp_batch.f90): with no dust, IGM, lines or smoothing the
   spectrum is sum_k w_k SSP_k; linearity in the weights; the velocity-smoothing rows sum to one; the distance term.
 """
@@ -39,6 +43,57 @@ def test_imf_powerlaw_bins_known_answers(olib):
 def _oracle(data, **kw):
     from oracle.oracle import Oracle
     return Oracle(data, **kw)
+
+
+def _imf_density(t, m, vdmc=0.3, mdave=0.7, alpha=(1.3, 2.3, 2.3)):
+    """get_imf_value (number per unit mass) restated for the test: the analytic types 0-4."""
+    m = np.asarray(m, dtype=np.float64)
+    if t == 0:
+        return m ** -2.35
+    if t == 1:
+        lmc, s2 = np.log10(0.08), 0.69 ** 2
+        high = np.exp(-lmc ** 2 / (2 * s2)) * m ** -2.3
+        return np.where(m < 1.0, np.exp(-(np.log10(m) - lmc) ** 2 / (2 * s2)) / m, high)
+    if t == 2:
+        c2 = 0.5 ** (-alpha[0] + alpha[1])
+        return np.where(m < 0.08, 0.0, np.where(m < 0.5, m ** -alpha[0], np.where(m < 1.0, c2 * m ** -alpha[1],
+                                                                                 c2 * m ** -alpha[2])))
+    if t == 3:
+        br = 25.0 * vdmc
+        low = 0.14 * (0.5 * br) ** -1.3 * np.exp(-(np.log10(m) - np.log10(vdmc)) ** 2 / (2 * 0.69 ** 2))
+        return np.where(m <= br, low, 0.0443 * m ** -1.3) / m
+    return np.where(m < 0.08, 0.0, np.where(m < mdave, m ** -alpha[0], mdave ** (-alpha[0] + alpha[1]) * m ** -alpha[1]))
+
+
+@pytest.mark.parametrize("imf_type", [0, 1, 2, 3, 4])
+def test_imf_integrals_match_quadrature(imf_type):
+    from oracle.oracle import imf_integral
+    a = {3: (0.3, 0.0, 0.0), 4: (1.3, 2.3, 0.7)}.get(imf_type, (1.3, 2.3, 2.3))
+    for lo, hi in ((0.08, 0.3), (0.3, 0.7), (0.4, 2.0), (0.9, 1.1), (5.0, 120.0), (0.08, 120.0)):
+        n = 200000
+        u = np.log(lo) + (np.log(hi) - np.log(lo)) * np.arange(n + 1) / n
+        m = np.exp(u)
+        m[0], m[-1] = lo, hi
+        c = np.where(np.arange(n + 1) % 2 == 1, 4.0, 2.0)
+        c[0] = c[-1] = 1.0
+        f = _imf_density(imf_type, m) * m
+        du = (u[-1] - u[0]) / n
+        for mw in (False, True):
+            q = float(np.sum(c * f * (m if mw else 1.0))) * du / 3.0
+            got = imf_integral(imf_type, lo, hi, mw, alpha=a)
+            assert abs(got / q - 1.0) <= 1.0e-8, (imf_type, lo, hi, mw, got, q)
+
+
+@pytest.mark.parametrize("imf_type", [1, 3])
+def test_lognormal_wide_bin_is_the_sum_of_narrow_bins(imf_type):
+    from oracle.oracle import imf_integral
+    a = (0.13, 0.0, 0.0) if imf_type == 3 else (1.3, 2.3, 2.3)
+    for lo, hi in ((0.1, 0.9), (0.2, 1.0), (0.5, 0.95), (30.0, 100.0), (1.0e-4, 1.0e-3)):
+        e = lo * (hi / lo) ** (np.arange(4001) / 4000)
+        for mw in (False, True):
+            whole = imf_integral(imf_type, e[0], e[-1], mw, alpha=a)
+            parts = sum(imf_integral(imf_type, e[k - 1], e[k], mw, alpha=a) for k in range(1, e.size))
+            assert abs(parts / whole - 1.0) < 1.0e-13
 
 
 def test_no_dust_sum_of_ssps(data):
