@@ -11,7 +11,8 @@
 // of 128 models x 64 pixels) is built by warps 0..7 in shared memory from the spectra, in the 128-byte swizzled
 // K-major layout, split into bf16 hi and lo; the B operand (band matrix, hi and lo, bands x pixels) comes by TMA.
 // fband = A_hi B_hi + A_hi B_lo + A_lo B_hi in f32 in tensor memory; the epilogue forms the magnitudes.
-// Warp roles: warps 0..7 build the A operand (16 model rows each), warp 8 issues the band matrix's TMA and the MMAs.
+// Warp roles: warps 0..15 build the A operand (8 model rows each: two CTAs of 17 warps per SM at 56 registers, against
+// 9 warps of 16 rows at 92), warp 16 issues the band matrix's TMA and the MMAs.
 // Two stages with mbarriers: a builder warp signals its rows of stage s on full_a[s] and goes on to the next stage as
 // soon as the MMAs that read that buffer have completed (empty[s], a tcgen05 commit), so that the warps do not wait
 // for one another between stages.
@@ -27,7 +28,7 @@ namespace sps {
 
 constexpr int BG_M = 128;
 constexpr int BG_K = 64;
-constexpr int BG_BUILD_WARPS = 8;
+constexpr int BG_BUILD_WARPS = 16;
 constexpr int BG_BUILD_THREADS = BG_BUILD_WARPS * 32;
 constexpr int BG_MMA_WARP = BG_BUILD_WARPS;             // TMA of the band matrix and the MMAs
 constexpr int BG_THREADS = BG_BUILD_THREADS + 32;
@@ -136,10 +137,10 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             if (!ok) mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
         }
     } else {
-        // ---------------------------------------------------------------- A operand builders (warps 0..7)
+        // ---------------------------------------------------------------- A operand builders (warps 0..15)
         const float dl2 = (float)(a.dlnl * 1.4426950408889634);   // grid step in log2 units
         const float inv_em1 = (float)(1.0 / expm1(a.dlnl));
-        // each warp builds 16 model rows, two at a time: lane l takes row parity l / 16 and pixels 4 (l % 16) ..
+        // each warp builds 8 model rows, two at a time: lane l takes row parity l / 16 and pixels 4 (l % 16) ..
         // 4 (l % 16) + 3 of the stage
         const int q = lane & 15, hr = lane >> 4;
         for (int li = 0; li < nst; ++li) {
@@ -151,13 +152,13 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             float wl[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) wl[u] = (j + u < a.nspec) ? __ldg(a.wl + j + u) : 0.f;
-            // the loads of all 8 rows first (rows whose 5 rest pixels lie inside the grid: the interior case), then
-            // the arithmetic
-            float sv[8][5];
-            bool inner[8];
+            // the loads of all 4 row pairs first (rows whose 5 rest pixels lie inside the grid: the interior case),
+            // then the arithmetic
+            float sv[4][5];
+            bool inner[4];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int r = warp * 16 + 2 * i + hr;
+            for (int i = 0; i < 4; ++i) {
+                const int r = warp * 8 + 2 * i + hr;
                 const int2 rs = rsh[r];
                 const int c = j - rs.x;
                 inner[i] = rs.y != 2 && c >= 0 && c + 4 < a.nspec && j + 3 < a.nspec;
@@ -166,8 +167,8 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                 for (int u = 0; u < 5; ++u) sv[i][u] = inner[i] ? __ldg(sp + u) : 0.f;
             }
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int r = warp * 16 + 2 * i + hr;
+            for (int i = 0; i < 4; ++i) {
+                const int r = warp * 8 + 2 * i + hr;
                 float f[4];
                 if (inner[i]) {
                     // v = s(c) + t (s(c + 1) - s(c)), t = 0 for whole shifts and the rest frame (v = s(c) exactly);
@@ -221,8 +222,9 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         mbar_wait(bar_done, 0, status, ERR_TIMEOUT_BAND, false);
         tc_fence_after();
 
-        // epilogue: warps w and w + 4 read lane quarter w % 4 (one model per thread), columns 32 (w / 4) + 64 i
-        if (*(volatile int *)status == 0) {
+        // epilogue (warps 0..7): warps w and w + 4 read lane quarter w % 4 (one model per thread), columns
+        // 32 (w / 4) + 64 i
+        if (warp < 8 && *(volatile int *)status == 0) {
             const int q = warp & 3;
             const int r = q * 32 + lane, m = m0 + r;
             const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
