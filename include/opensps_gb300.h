@@ -56,7 +56,9 @@ void opensps_gb300_last_input_in_place(int handle, int *in_place, int *status);
  * templates interpolated onto lam (2 numin x nqpah columns of nspec, column (2 u + c) nqpah + q); "agn_torus": the 9
  * templates on lam (9 x nspec); "filters": the bands on lam normalised to int T / lambda = 1 and calibrated where
  * the library says so (nb x nspec); "nebular": log10(continuum + 1e-95) on lam (11 logZ x 10 ages x 7 logU columns of
- * nspec, column z + 11 (a + 10 u), src/io/opensps_io.f90:749-827,910-933). name may
+ * nspec, column z + 11 (a + 10 u), src/io/opensps_io.f90:749-827,910-933); "attenuation": smc_bar's A(lambda) / A(V)
+ * on lam (nspec) or dirty's optical depths (2 structures x 18 tau_v x 6 models curves of nspec, in that order;
+ * load_attenuation_curves :2079-2234). name may
  * carry axis selections ("name:axis=value"). *n_out receives the table's length; out may be NULL to query it.
  * Status 4 with the message for a missing or malformed library. */
 void opensps_gb300_data_table(const char *root, const char *kind, const char *name, const double *lam, int nspec,

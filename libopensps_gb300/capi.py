@@ -219,6 +219,10 @@ class Context:
             from . import synth_dust
             gen = synth_dust.generate if key == "add_dust_emission" else synth_dust.generate_agn
             gen(Path(os.environ["OPENSPS_DATA_HOME"]))
+        if key == "dust_type" and int(value) in (3, 5):
+            # the attenuation libraries in the data root (the synthetic stand-ins written first if missing)
+            from . import synth_attenuation
+            synth_attenuation.generate(Path(os.environ["OPENSPS_DATA_HOME"]))
         st = C.c_int(0)
         self.lib.opensps_context_set_int(self.handle, key.encode(), int(value), C.byref(st))
         _check(st, self.lib)

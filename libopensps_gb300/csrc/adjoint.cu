@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
     float g[NG];
 #pragma unroll
     for (int k = 0; k < NG; ++k) g[k] = 0.f;
-    const float d2 = (float)pr[PF_DUST2], d3 = (float)pr[PF_DUST3], d1 = (float)pr[PF_DUST1];
+    const float d2 = a.dust_type == 3 ? 1.f : (float)pr[PF_DUST2], d3 = (float)pr[PF_DUST3], d1 = (float)pr[PF_DUST1];
     // the dust emission's and the AGN's sums over the pixels (backward_emission_sums / backward_agn,
     // src/physics/opensps_csp_batch.f90:6667-6845): R_bar = sum dL/dTOT T_igm shape T_d (E = R shape T_d T_igm is linear
     // in R = s_abs / s_esc), s1 = sum dL/dTOT tmpl T_d, s2 = sum dL/dTOT (tmpl_hi - tmpl_lo) T_d
@@ -703,6 +703,8 @@ __global__ void __launch_bounds__(ADJ_THREADS, 2) adjoint_kernel(AdjointArgs a) 
         }
         if (agn && tid == R_FAGN) v = c * lsum_m * (double)em_sums[1];
         if (agn && tid == R_AGN_TAU && a.dchain) v = c * lsum_m * (double)dm.fagn * (double)em_sums[2] * (double)a.dchain[m].w;
+        // (dust_type 3: the optical depth is the curve itself, dust2 has no effect: its row zero)
+        if (tid == R_DUST2 && a.dust_type == 3) v = 0.0;
         if (tid == R_ZRED) {
             // the observed frame's share (its factor formed in FP64 per model) and the distance term's
             double go = 0.0, ms = 0.0;

@@ -102,7 +102,9 @@ __global__ void __launch_bounds__(256) model_params_kernel(ModelParamArgs a) {
     float blk[MODEL_PAR_FLOATS];
 #pragma unroll
     for (int i = 0; i < MODEL_PAR_FLOATS; ++i) blk[i] = 0.f;
-    const double d1 = p[PF_DUST1], d2 = p[PF_DUST2], d3 = p[PF_DUST3], fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
+    // (dust_type 3: the diffuse optical depth is the curve itself, pixel_transmissions :3798-3801)
+    const double d1 = p[PF_DUST1], d2 = a.dust_type == 3 ? 1.0 : p[PF_DUST2], d3 = p[PF_DUST3];
+    const double fnd = p[PF_FRAC_NODUST], fo = p[PF_FRAC_OBRUN];
     // attenuate_batch / pixel_transmissions (src/physics/opensps_csp_batch.f90:3576-3660, 3765-3818)
     blk[MP_KD2] = (float)(-d2 * LOG2E);
     if (1.0 - fnd <= SAFE_FLOOR) { blk[MP_ONE_M_FND] = 0.f; blk[MP_FND] = 1.f; }
@@ -417,7 +419,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     bool any_emis = false, any_agn = false;
     if (c.add_dust_emission == 1)
         for (int m = 0; m < n && !any_emis; ++m)
-            any_emis = par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR;
+            any_emis = par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR || c.dust_type == 3;
     // the AGN torus (add_agn_dust, for models with fagn above SAFE_FLOOR: agn_indices :1575-1589), in the same epilogue
     if (c.add_agn_dust == 1)
         for (int m = 0; m < n && !any_agn; ++m) any_agn = par(m, PF_FAGN) > SAFE_FLOOR;
@@ -500,9 +502,16 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
 
     // ---- checks shared by the batch (the reference's batch_check_models / plan_smoothing rules)
     if (!dust_type_supported(c.dust_type)) {
-        err = "dust_type " + std::to_string(c.dust_type) + ": the table lookups (3, 5) are not supported on this path";
+        err = "dust_type " + std::to_string(c.dust_type) + ": the types are 0 to 6";
         return ST_UNSUPPORTED;
     }
+    if (c.dust_type == 3 && (c.wgp[0] < 1 || c.wgp[0] > WG_NTAU || c.wgp[1] < 1 || c.wgp[1] > WG_NMODEL || c.wgp[2] < 1 ||
+                             c.wgp[2] > WG_NSTRUCT)) {
+        err = "dust_type 3: wgp1 (1-18), wgp2 (1-6) and wgp3 (1-2) select the curve";
+        return ST_BAD_ARG;
+    }
+    if (c.dust_type == 3 || c.dust_type == 5)
+        if (int rc = attenuation_load(c, err)) return rc;
     if (c.compute_vega_mags != 0) { err = "compute_vega_mags = 1 is not supported on this path"; return ST_UNSUPPORTED; }
     if (c.smooth_velocity != 1) { err = "smooth_velocity = 0 is not supported on this path"; return ST_UNSUPPORTED; }
     const double minl = par(0, PF_MIN_WAVE_SMOOTH), maxl = par(0, PF_MAX_WAVE_SMOOTH);
@@ -626,7 +635,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         for (int m = 0; m < n; ++m) {
             DustEmModel &q = dem[m];
             q = DustEmModel{};
-            q.on = (any_emis && (par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR)) ? 1 : 0;
+            q.on = (any_emis && (par(m, PF_DUST1) > SAFE_FLOOR || par(m, PF_DUST2) > SAFE_FLOOR || c.dust_type == 3)) ? 1 : 0;
             if (q.on) {
                 cell(d.qpah, par(m, PF_DUSTE_QPAH), q.iq, q.wq);
                 cell(d.umin, par(m, PF_DUSTE_UMIN), q.iu, q.wu);
@@ -735,12 +744,18 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         err = "dust_type " + std::to_string(c.dust_type) + " is not supported on the plain FP64 path";
         return ST_UNSUPPORTED;
     }
-    const double key[5] = {(double)c.dust_type, sc0[0], sc0[1], sc0[2], sc0[3]};
+    // (the dusty environments' curve: structure wgp3, tau_v wgp1, model wgp2)
+    const double *lookup = c.dust_type == 5 ? c.att_smc.data()
+                         : (c.dust_type == 3 ? c.att_wg.data() + (size_t)ns * (((c.wgp[2] - 1) * WG_NTAU + (c.wgp[0] - 1)) *
+                                                                              WG_NMODEL + (c.wgp[1] - 1))
+                                             : nullptr);
+    const double key[6] = {(double)c.dust_type, sc0[0], sc0[1], sc0[2], sc0[3],
+                           c.dust_type == 3 ? (double)(c.wgp[0] + 100 * c.wgp[1] + 10000 * c.wgp[2]) : 0.0};
     bool same_key = true;
-    for (int k = 0; k < 5; ++k) same_key = same_key && c.pix_key[k] == key[k];
-    if (!c.d_pix.p || c.pix_key[0] != key[0] || (uniform_index && !same_key)) {
+    for (int k = 0; k < 6; ++k) same_key = same_key && c.pix_key[k] == key[k];
+    if (!c.d_pix.p || c.pix_key[0] != key[0] || c.pix_key[5] != key[5] || (uniform_index && !same_key)) {
         std::vector<double> tab;
-        dust_tables(c.dust_type, c.lam, tab);
+        dust_tables(c.dust_type, c.lam, lookup, tab);
         std::vector<float> pix((size_t)ns * PIX_FLOATS, 0.f);
         for (int j = 0; j < ns; ++j) {
             float *px = pix.data() + (size_t)j * PIX_FLOATS;
@@ -757,7 +772,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
             err = cuda_msg("pixel table", e);
             return ST_DATA_MISSING;
         }
-        for (int k = 0; k < 5; ++k) c.pix_key[k] = key[k];
+        for (int k = 0; k < 6; ++k) c.pix_key[k] = key[k];
     }
     const int tab_curve = c.dust_type != 0 ? 1 : 0;   // (models' own curves from the tables, else the power law)
     // the smoothed pixels: lambda within [min_wave_smooth, max_wave_smooth]

@@ -347,6 +347,9 @@ void opensps_context_set_int(int handle, const char *key, int value, int *status
     else if (k == "add_agn_dust") c->add_agn_dust = value;
     else if (k == "add_neb_continuum") c->add_neb_continuum = value;
     else if (k == "cloudy_dust") c->cloudy_dust = value;
+    else if (k == "wgp1") c->wgp[0] = value;   // dust_type 3: tau_v, model, structure of the curve
+    else if (k == "wgp2") c->wgp[1] = value;
+    else if (k == "wgp3") c->wgp[2] = value;
     else if (k == "add_stellar_remnants" ||
              k == "smoothspec_fast" || k == "compute_mags" || k == "compute_indices" ||
              k == "redshift_colors" || k == "add_xrb_emission" || k == "tpagb_norm_type" ||
@@ -732,8 +735,10 @@ void opensps_gb300_data_table(const char *root, const char *kind, const char *na
     } else if (k == "nebular") {
         std::vector<double> lu;
         rc = std_load_nebular(root, name, grid, a, b, lu, tab, err);
+    } else if (k == "attenuation") {
+        rc = std_load_attenuation(root, name, grid, tab, err);
     } else {
-        return fail(status, ST_BAD_ARG, "kind must be ssp, dust_emission, agn_torus, filters or nebular");
+        return fail(status, ST_BAD_ARG, "kind must be ssp, dust_emission, agn_torus, filters, nebular or attenuation");
     }
     if (rc) return fail(status, rc, err);
     if (n_out) *n_out = (long long)tab.size();

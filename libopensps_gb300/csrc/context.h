@@ -240,7 +240,12 @@ struct Context {
     int band_j0 = 0, band_nkb = 0, band_npad = 0;
     DevBuf<double> d_lam, d_lnlam, d_mass, d_llin, d_zt, d_dl;
     std::map<long long, BasisOperand *> basis_cache;   // key: nacc, itesc, line-width key
-    double pix_key[5] = {-1e300, 0.0, 0.0, 0.0, 0.0};   // the device pixel table's curve: dust_type, its 4 scalars
+    double pix_key[6] = {-1e300, 0.0, 0.0, 0.0, 0.0, 0.0};   // the device pixel table's curve: dust_type, its 4
+                                                               // scalars, the dusty environments' curve (type 3)
+    // dust types 3 and 5 (attenuation/dirty and attenuation/smc_bar of the data root, on the grid): wgp1 (tau_v),
+    // wgp2 (model), wgp3 (structure) choose the dirty curve
+    int wgp[3] = {1, 1, 1};
+    std::vector<double> att_smc, att_wg;
 
     // batch scratch
     DevBuf<double> d_wz, d_params, d_sums, d_dist, d_fband, d_mags, d_spec64;
@@ -366,8 +371,11 @@ int dustem_load(Context &c, std::string &err);
 int agn_load(Context &c, std::string &err);
 // the diffuse dust curves (dust_curves.cu): per pixel the tables T0..T3 (4 x nspec, pixel-major) of dust_type, per
 // model its scalars (s1, s2, s3, ed); a pixel's curve (T0 + s1 T1 + s2 T2 + s3 T3) exp(ed ltab)
+// (types 3 and 5: T0 the table lookup's curve on the grid, lookup)
 bool dust_type_supported(int dust_type);
-void dust_tables(int dust_type, const std::vector<double> &lam, std::vector<double> &tab);
+void dust_tables(int dust_type, const std::vector<double> &lam, const double *lookup, std::vector<double> &tab);
+// the curves of dust types 3 and 5 from the data root (once per context): 0 or a status with err
+int attenuation_load(Context &c, std::string &err);
 void dust_scalars(int dust_type, double dust_index, double mwr, double uvb, double s[4]);
 double dust_curve_value(const double *t, const double s[4], double ltab);
 // the nebular ages as the continuum kernel's runs for this itesc (context.cu; rebuilt when itesc changes)

@@ -627,6 +627,41 @@ int std_load_agn(const std::string &root, const std::vector<double> &lam, std::v
     return 0;
 }
 
+int std_load_attenuation(const std::string &root, const std::string &name, const std::vector<double> &lam,
+                         std::vector<double> &tab, std::string &err) {
+    const bool smc = name == "smc_bar";
+    if (!smc && name != "dirty") return bad(err, "attenuation libraries: smc_bar or dirty", ST_BAD_ARG);
+    DataLib lib;
+    if (int rc = lib.open(root, "attenuation", name, err)) return rc;
+    std::vector<double> wl;
+    if (int rc = lib.axis_values("wavelength", wl, err)) return rc;
+    const long long nw = (long long)wl.size();
+    if (nw < 2) return bad(err, "library attenuation/" + name + ": too few wavelengths");
+    if (!smc && nw != WG_NLAM) return bad(err, "library attenuation/dirty: 25 wavelengths are required");
+    long long off = 0, ncurve = smc ? 1 : (long long)WG_NSTRUCT * WG_NTAU * WG_NMODEL;
+    std::vector<double> raw;
+    if (smc) {
+        if (int rc = lib.check_array("extinction", {"wavelength"}, {nw}, off, err)) return rc;
+        if (int rc = lib.read_real("extinction", nw, off, raw, err)) return rc;
+    } else {
+        if (int rc = lib.check_array("attenuation", {"structure", "tau_v", "model", "wavelength"},
+                                     {WG_NSTRUCT, WG_NTAU, WG_NMODEL, nw}, off, err))
+            return rc;
+        if (int rc = lib.read_real("attenuation", ncurve * nw, off, raw, err)) return rc;
+    }
+    const size_t ns = lam.size();
+    tab.assign((size_t)ncurve * ns, 0.0);
+    for (long long k = 0; k < ncurve; ++k) {
+        const double *y = raw.data() + (size_t)(k * nw);
+        double *dst = tab.data() + (size_t)k * ns;
+        for (size_t p = 0; p < ns; ++p) {
+            const double l = lam[p];
+            dst[p] = l > wl[(size_t)nw - 1] ? 0.0 : (l < wl[0] ? y[0] : interp_linear(wl.data(), y, (int)nw, l));
+        }
+    }
+    return 0;
+}
+
 int std_load_nebular(const std::string &root, const std::string &spec, const std::vector<double> &lam,
                      std::vector<double> &logz, std::vector<double> &lage, std::vector<double> &logu,
                      std::vector<double> &tab, std::string &err) {

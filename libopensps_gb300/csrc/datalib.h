@@ -88,6 +88,15 @@ int std_load_nebular(const std::string &root, const std::string &spec, const std
                      std::vector<double> &logz, std::vector<double> &lage, std::vector<double> &logu,
                      std::vector<double> &tab, std::string &err);
 
+// attenuation/smc_bar and attenuation/dirty (load_attenuation_curves, src/io/opensps_io.f90:2079-2234): the SMC bar's
+// A(lambda) / A(V) over its wavelength axis, or the dusty environments' optical depths [structure (2), tau_v (18),
+// model (6), wavelength (25)]; each curve interpolated linearly at the grid's pixels inside the table's range, its
+// first value below it and zero above. tab: the smc_bar curve (nspec), or the dirty curves (2 x 18 x 6 curves of
+// nspec pixels, in the array's order: structure, then tau_v, then model).
+constexpr int WG_NSTRUCT = 2, WG_NTAU = 18, WG_NMODEL = 6, WG_NLAM = 25;
+int std_load_attenuation(const std::string &root, const std::string &name, const std::vector<double> &lam,
+                         std::vector<double> &tab, std::string &err);
+
 // filters/<name> (read_filter_library, opensps_io.f90:1247-1318, then filters_build with point resampling,
 // src/spectra/opensps_filters.f90:395-500): bands nb x nspec normalised to int T / lambda = 1 on the grid, their
 // pivot wavelengths and names; a filter with a calibration {lambda_ref, exponent} is then divided by

@@ -5,7 +5,9 @@
 // dust_type 0 (power law): T0 = 1, ed = dust_index. 1 (Cardelli, Clayton & Mathis 1989 with R_V = mwr and the 2175 A
 // bump scaled by uvb): the curve is bilinear in 1 / R_V and uvb, s = (1 / mwr, uvb, uvb / mwr). 2 (Calzetti et al.
 // 2000) and 6 (Reddy et al. 2015): T0 alone. 4 (Kriek & Conroy 2013): linear in delta once its power law is factored
-// out, s1 = ed = dust_index. Types 3 (Witt & Gordon) and 5 (SMC) are table lookups of data this path does not read.
+// out, s1 = ed = dust_index. Types 3 (Witt & Gordon's dusty environments: the optical depth itself, dust2 not applied)
+// and 5 (the SMC bar) are table lookups (compute_attenuation_curve_point :237-270) of the data root's
+// attenuation/dirty and attenuation/smc_bar libraries on the grid: T0 alone.
 //
 // The curve functions restate the published forms with the reference's constants and extensions beyond their ranges
 // (src/physics/opensps_dust.f90:47-160 constants; get_ccm89_curve_point :424-556, get_calzetti_curve_point :567-594,
@@ -13,6 +15,7 @@
 #include <cmath>
 #include <vector>
 #include "context.h"
+#include "datalib.h"
 
 namespace sps {
 
@@ -101,11 +104,22 @@ double reddy(double lam) {
 
 }  // namespace
 
-bool dust_type_supported(int dust_type) {
-    return dust_type == 0 || dust_type == 1 || dust_type == 2 || dust_type == 4 || dust_type == 6;
+bool dust_type_supported(int dust_type) { return dust_type >= 0 && dust_type <= 6; }
+
+int attenuation_load(Context &c, std::string &err) {
+    const std::string root = data_root();
+    const char *name = c.dust_type == 5 ? "smc_bar" : "dirty";
+    std::vector<double> &dst = c.dust_type == 5 ? c.att_smc : c.att_wg;
+    if (!dst.empty()) return 0;
+    if (!datalib_available(root, "attenuation", name)) {
+        err = std::string("dust_type ") + std::to_string(c.dust_type) + ": the attenuation/" + name +
+              " library is missing under the data root " + root;
+        return ST_DATA_MISSING;
+    }
+    return std_load_attenuation(root, name, c.lam, dst, err);
 }
 
-void dust_tables(int dust_type, const std::vector<double> &lam, std::vector<double> &tab) {
+void dust_tables(int dust_type, const std::vector<double> &lam, const double *lookup, std::vector<double> &tab) {
     const size_t ns = lam.size();
     tab.assign(4 * ns, 0.0);
     const double R_BIG = 1.0e30;   // 1 / R_V = 1e-30: the terms without 1 / R_V
@@ -127,6 +141,8 @@ void dust_tables(int dust_type, const std::vector<double> &lam, std::vector<doub
             break;
         }
         case 6: t[0] = reddy(l); break;
+        case 3:
+        case 5: t[0] = lookup ? lookup[i] : 0.0; break;
         default: break;
         }
     }

@@ -357,7 +357,9 @@ typedef struct {
      * spectral grid, nspec x 11 x 10 x 7 (pixel fastest, then log Z, age, log U: nebem_cont(j, z, a, u)), the grid's
      * log Z, log10 age and log U values */
     const double *neb_cont, *neb_logz, *neb_lage, *neb_logu;
-    int dust_type;           /* the diffuse curve (dust_type 0, 1, 2, 4, 6) */
+    int dust_type;           /* the diffuse curve (dust_type 0 to 6) */
+    const double *att_curve; /* dust_type 3 and 5: the table lookup's curve on the grid (nspec; the dusty
+                                environments' chosen curve, or the SMC bar), compute_attenuation_curve_point :256-263 */
 } oracle_grid_t;
 
 /* ------------------------------------------------------------------------------------------ */
@@ -672,6 +674,14 @@ static void dl07_cell(const double *gr, int n, double x, int *i, double *w) {
     *w = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
 }
 
+/* The diffuse curve of a model at pixel i: the table lookup (types 3, 5), the curve functions (1, 2, 4, 6) or the
+ * power law (0). */
+static double curve_at(const oracle_grid_t *g, int i, const double *par) {
+    if (g->dust_type == 3 || g->dust_type == 5) return g->att_curve[i];
+    if (g->dust_type != 0) return oracle_dust_curve(g->dust_type, g->lam[i], par[P_DUST_INDEX], par[P_MWR], par[P_UVB]);
+    return par[P_DUST_INDEX] != 0.0 ? exp(par[P_DUST_INDEX] * log(g->lam[i] / V_BAND)) : 1.0;
+}
+
 /* From the young and old age sums of a model (and its linear L_bol lsum): attenuation, dust emission, IGM, the AGN
  * torus, smoothing, the spectrum and the magnitudes (the stages of compute_csp_batch after the age sums). tot, tmp:
  * nspec doubles of work. */
@@ -679,7 +689,8 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
                        double *spec, double *mags, double *fband_out, double *tot, double *tmp) {
     const int ns = g->nspec;
     /* attenuation, dust_type 0 (power law) */
-    double d1 = par[P_DUST1], d2 = par[P_DUST2], d3 = par[P_DUST3], di = par[P_DUST_INDEX], d1i = par[P_DUST1_INDEX];
+    /* (dust_type 3: the diffuse optical depth is the curve itself, pixel_transmissions :3798-3801) */
+    double d1 = par[P_DUST1], d2 = g->dust_type == 3 ? 1.0 : par[P_DUST2], d3 = par[P_DUST3], d1i = par[P_DUST1_INDEX];
     double fnd = par[P_FRAC_NODUST], fo = par[P_FRAC_OBRUN];
     /* dust emission (batch_model_indices :1569-1570): models with dust1 or dust2 above SAFE_FLOOR */
     const int emis = g->dustem != NULL && (d1 > SAFE_FLOOR || d2 > SAFE_FLOOR);
@@ -695,9 +706,7 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
     }
     for (int i = 0; i < ns; ++i) {
         double ltab = log(g->lam[i] / V_BAND);
-        double curve = 1.0;
-        if (g->dust_type != 0) curve = oracle_dust_curve(g->dust_type, g->lam[i], di, par[P_MWR], par[P_UVB]);
-        else if (di != 0.0) curve = curve * exp(di * ltab);
+        const double curve = curve_at(g, i, par);
         double tau_d = d2 * curve, td = exp(-tau_d);
         double tb = 1.0, too = 1.0, tau_b = 0.0, tau_o = 0.0;
         if (!(d1 <= SAFE_FLOOR || 1.0 - fo <= SAFE_FLOOR)) { tau_b = d1 * exp(d1i * ltab); tb = exp(-tau_b); }
@@ -765,9 +774,7 @@ static void post_parts(const oracle_grid_t *g, const double *y, const double *o,
         dl07_cell(g->agn_tau, g->ntau, par[P_AGN_TAU], &ita, &wta);
         double lagn = (lsum > SAFE_FLOOR ? lsum : 1.0) * par[P_FAGN];
         for (int i = 0; i < ns; ++i) {
-            double ltab = log(g->lam[i] / V_BAND);
-            double curve = g->dust_type != 0 ? oracle_dust_curve(g->dust_type, g->lam[i], di, par[P_MWR], par[P_UVB])
-                                             : ((di != 0.0) ? exp(di * ltab) : 1.0);
+            const double curve = curve_at(g, i, par);
             double tmpl = (1.0 - wta) * g->agn_spec[(size_t)ns * ita + i] + wta * g->agn_spec[(size_t)ns * (ita + 1) + i];
             tot[i] += lagn * tmpl * exp(-d2 * curve);
         }

@@ -40,7 +40,7 @@ class _Grid(C.Structure):
                 ("nqpah", C.c_int), ("numin", C.c_int), ("qpah", _dp), ("umin", _dp), ("dustem", _dp),
                 ("ntau", C.c_int), ("agn_tau", _dp), ("agn_spec", _dp), ("ssp_ion", _dp), ("nt_neb", C.c_int),
                 ("whlylim", C.c_int), ("neb_cont", _dp), ("neb_logz", _dp), ("neb_lage", _dp), ("neb_logu", _dp),
-                ("dust_type", C.c_int)]
+                ("dust_type", C.c_int), ("att_curve", _dp)]
 
 
 class _OpsT(C.Structure):
@@ -286,7 +286,7 @@ class Oracle:
                  smooth: bool = True, min_wave_smooth: float = 1.0e3, max_wave_smooth: float = 1.0e4,
                  line_sigma: float = 0.0, h0: float = 72.0, om0: float = 0.27, ol0: float = 0.73,
                  dust_emission: dict | None = None, agn: dict | None = None, nebular: dict | None = None,
-                 dust_type: int = 0):
+                 dust_type: int = 0, att_curve: np.ndarray | None = None):
         L = lib()
         self.d = data
         self.lam = np.ascontiguousarray(data["lambda"])
@@ -324,6 +324,9 @@ class Oracle:
             self.nt_neb, self.whlylim = a.value, b.value
         g.add_igm, g.smooth = int(add_igm), int(smooth)
         g.dust_type = int(dust_type)
+        # dust_type 3, 5: the table lookup's curve on the grid (nspec)
+        self._att = None if att_curve is None else np.ascontiguousarray(att_curve, dtype=np.float64)
+        g.att_curve = _p(self._att) if self._att is not None else None
         g.min_wave_smooth, g.max_wave_smooth = min_wave_smooth, max_wave_smooth
         g.dustem = None
         if dust_emission is not None:

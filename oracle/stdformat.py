@@ -8,6 +8,8 @@ Follows the reference's readers:
   src/physics/opensps_ssp.f90:203-218 (log10 of the |d nu| trapezoid of the spectrum, floored at tiny);
 * dust_emission: opensps_io.f90:991-1060 (linear interpolation, extrapolated, at pixels from the one holding 1 um);
 * agn_torus/clumpy: load_agn_dust_models opensps_io.f90:1099-1157 (log-log interpolation over the table's range);
+* attenuation/smc_bar and attenuation/dirty: load_attenuation_curves opensps_io.f90:2079-2234 (linear interpolation
+  inside the table's range, its first value below, zero above);
 * nebular: load_nebular_grid / read_nebular_standard opensps_io.f90:749-827,910-933 (the continuum's log10(f + 1e-95)
   interpolated linearly onto the grid);
 * filters: read_filter_library opensps_io.f90:1247-1318, filters_build with point resampling
@@ -148,6 +150,20 @@ def agn(root: Path, lam: np.ndarray) -> dict:
         if hi > i1:
             tab[t, i1:hi] = 10.0 ** interp_linear_at(lw, ly, np.log10(lam[i1:hi])) - SAFE_FLOOR
     return {"tau": tau, "agnspec": tab}
+
+
+def attenuation(root: Path, name: str, lam: np.ndarray) -> np.ndarray:
+    """attenuation/smc_bar (1, nspec) or attenuation/dirty (2 x 18 x 6, nspec): each curve interpolated linearly at
+    the pixels inside its wavelength range, its first value below and zero above (load_attenuation_curves,
+    opensps_io.f90:2079-2234)."""
+    L = Lib(root, "attenuation", name)
+    wl = L.axis("wavelength")
+    raw = L.array("extinction" if name == "smc_bar" else "attenuation").reshape(-1, wl.size)
+    out = np.empty((raw.shape[0], lam.size))
+    for k in range(raw.shape[0]):
+        v = interp_linear_at(wl, raw[k], lam)
+        out[k] = np.where(lam > wl[-1], 0.0, np.where(lam < wl[0], raw[k, 0], v))
+    return out
 
 
 def filters(root: Path, name: str, lam: np.ndarray) -> tuple[np.ndarray, np.ndarray]:

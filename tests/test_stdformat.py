@@ -83,7 +83,8 @@ def test_filters_with_energy_detectors(std_root, lam):
 
 @pytest.mark.skipif(not REF_TEST_LIBRARY.exists(), reason="the reference's test library is not in this container")
 @pytest.mark.parametrize("kind,name", [("dust_emission", "DL07"), ("dust_emission", "THEMIS"), ("agn_torus", "clumpy"),
-                                       ("filters", "allfilters"), ("nebular", "mist_nodust")])
+                                       ("filters", "allfilters"), ("nebular", "mist_nodust"),
+                                       ("attenuation", "smc_bar"), ("attenuation", "dirty")])
 def test_reference_test_library(lam, kind, name):
     """The reader on the reference's own standard-format files (FP32 arrays, file-held axes, labels, filter
     calibrations) against the numpy restatement."""
@@ -92,6 +93,8 @@ def test_reference_test_library(lam, kind, name):
         want = ora.dust_emission(REF_TEST_LIBRARY, lam, name)["dustem"].reshape(-1, lam.size)
     elif kind == "agn_torus":
         want = ora.agn(REF_TEST_LIBRARY, lam)["agnspec"]
+    elif kind == "attenuation":
+        want = ora.attenuation(REF_TEST_LIBRARY, name, lam)
     elif kind == "nebular":
         # (the test subset's FP32 continuum underflows to zero: the table is the floor, log10(1e-95), everywhere)
         want = ora.nebular(REF_TEST_LIBRARY, lam, name)["cont"].reshape(-1, lam.size)
