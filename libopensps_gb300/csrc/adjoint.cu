@@ -994,7 +994,10 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         a.dem = c.d_dem.p; a.dchain = c.d_dchain.p;
         a.dtab = c.dustem.tab.p; a.cnu = c.dustem.cnu.p; a.nqpah = c.dustem.nqpah;
         a.agn_spec = c.agn.spec.p;
-        a.lsum = c.d_sums.p + 1; a.lsum_stride = 6;
+        // (weights blended on the device without the operators: the log-blended L_bol the forward's AGN took)
+        const bool blend = io_in.sfh_par != nullptr && !ops;
+        a.lsum = blend ? c.d_lblend.p : c.d_sums.p + 1;
+        a.lsum_stride = blend ? 3 : 6;
         if (c.geom.agn) {
             if ((e = c.d_lsum_bar.reserve(n)) != cudaSuccess) { err = msg("device memory", e); return ST_DATA_MISSING; }
             a.lsum_bar = c.d_lsum_bar.p;
@@ -1045,6 +1048,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         r.vbar = c.d_vbar.p; r.cscale = c.d_cscale.p;
         r.mass_bar = mass_bar ? c.d_mass_bar.p : nullptr;
         r.lbol_bar = lbol_bar ? c.d_lbol_bar.p : nullptr;   // (L_bol with the operators: the linear row, always)
+        r.lsum_bar = c.geom.agn ? c.d_lsum_bar.p : nullptr;
         r.sums = c.d_sums.p;
         r.wzb = want_wzb ? c.d_wzbar.p : nullptr;
         r.apart = c.d_apart.p;
@@ -1095,7 +1099,9 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         // (the log-blended L_bol of weights formed on the device has its own cotangent, in the SFH reverse pass)
         w.lbol_bar = (lbol_bar && !dev_blend) ? c.d_lbol_bar.p : nullptr;
         w.sums = c.d_sums.p; w.mass = c.d_mass.p; w.llin = c.d_llin.p;
-        w.lsum_bar = c.geom.agn ? c.d_lsum_bar.p : nullptr;
+        // (the AGN's L_bol: the linear sum over ages and metallicities, unless blended on the device, whose
+        // log-blended L_bol takes it in the SFH reverse below)
+        w.lsum_bar = (c.geom.agn && !dev_blend) ? c.d_lsum_bar.p : nullptr;
         w.wzb = c.d_wzbar.p;
         const size_t tot = (size_t)n * ntz;
         wzbar_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(w);
@@ -1144,6 +1150,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         r.tf = c.d_logage.p; r.lz = c.d_lz.p; r.lbol = c.d_lbol.p; r.par = c.d_sfhpar.p; r.w = c.d_w.p;
         // (with the operators L_bol is the linear row, whose cotangent the reverse fold took)
         r.lblend = c.d_lblend.p; r.lbol_bar = (lbol_bar && !ops) ? c.d_lbol_bar.p : nullptr; r.wzb = c.d_wzbar.p;
+        r.lsum_bar = (c.geom.agn && !ops) ? c.d_lsum_bar.p : nullptr;
         r.weights_bar = c.d_wbar.p; r.scratch = c.d_sfh_scratch.p; r.params_bar = c.d_pbar.p;
         r.dual = tangents ? (void *)c.d_dual.p : nullptr;
         if ((e = run_sfh_reverse(r, s)) != cudaSuccess) { err = msg("SFH reverse kernel", e); return ST_DATA_MISSING; }

@@ -600,12 +600,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     if (epi_terms) {
         if (fp64) { err = "dust emission, AGN and the nebular continuum are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
         if (io.keep_parts && neb_cont) { err = "gradients with the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts && any_agn && (c.ops.ready || io.sfh_par)) {
-            // (the AGN scales with the L_bol the batch outputs: its cotangent goes into the weights through the linear
-            // L_bol sum of weights over ages and metallicities only)
-            err = "gradients with the AGN torus need weights over ages and metallicities (ssp_weights_z) without SSP operators";
-            return ST_UNSUPPORTED;
-        }
         if (io.dev_inputs) { err = "dust emission, AGN and the nebular continuum need host inputs on this path"; return ST_UNSUPPORTED; }
         if (neb_cont && c.ops.ready) { err = "the nebular continuum with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
         if (any_emis) { if (int rc = dustem_load(c, err)) return rc; }

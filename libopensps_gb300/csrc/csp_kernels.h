@@ -289,6 +289,7 @@ cudaError_t run_sfh_forward(const SfhArgs &a, cudaStream_t st);
 struct SfhRevArgs {
     int n, nt, nz, sfh, rows, has_logzsol, sfh_tangents;
     const double *tf, *lz, *lbol, *par, *w, *lblend, *lbol_bar;
+    const double *lsum_bar = nullptr;   // n: the AGN's cotangent of the log-blended L_bol (linear, absolute), or null
     const double *wzb;       // n x nt x nz: dL / dwz without the L_bol term
     double *weights_bar;     // n x nt, or null
     double *scratch;         // n x nt
@@ -355,6 +356,7 @@ struct OpsRevArgs {
     const float *vbar;        // 2n x ntpad: the template weights' cotangents / cscale (young rows, then old)
     const double *cscale;     // n: the reverse pass's cotangent scale
     const double *mass_bar, *lbol_bar;   // n each, or null
+    const double *lsum_bar = nullptr;    // n: the AGN's cotangent of the linear L_bol row (absolute), or null
     const double *sums;       // n x 6: the forward's mass and linear L_bol
     double *wzb;              // n x nt x nz: the weights' cotangent (every grid point), or null (slopes only)
     double *apart;            // nz x n x 3: each slab's slope cotangents / cscale

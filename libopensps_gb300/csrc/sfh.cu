@@ -803,7 +803,8 @@ __global__ void __launch_bounds__(64) sfh_reverse_kernel(SfhRevArgs a) {
     double dz;
     zinterval(a.lz, nz, p[SFH_LOGZSOL], zlo, dz);
     const double ls = a.lblend[3 * m];
-    const double lbar = (a.lbol_bar && ls > SAFE_FLOOR) ? a.lbol_bar[m] / (ls * SFH_LN10) : 0.0;
+    double lbar = (a.lbol_bar && ls > SAFE_FLOOR) ? a.lbol_bar[m] / (ls * SFH_LN10) : 0.0;
+    if (a.lsum_bar) lbar += a.lsum_bar[m];   // (the AGN's scale: this log-blended L_bol, linear)
     double gz = 0.0;   // dL / d dz
     double *wb = a.weights_bar ? a.weights_bar + (size_t)nt * m : nullptr;
     for (int t = 0; t < nt; ++t) {

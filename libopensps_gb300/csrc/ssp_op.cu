@@ -772,7 +772,9 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_rev_kernel(OpsRevArgs a) {
         const double cs = a.cscale[m];
         const double ls = a.sums[(size_t)6 * m + 1];
         qm_s[k] = (k < nk && a.mass_bar) ? (float)(a.mass_bar[m] / cs) : 0.f;
-        ql_s[k] = (k < nk && a.lbol_bar && ls > SAFE_FLOOR) ? (float)(a.lbol_bar[m] / (ls * 2.302585092994046 * cs)) : 0.f;
+        double qlv = (a.lbol_bar && ls > SAFE_FLOOR) ? a.lbol_bar[m] / (ls * 2.302585092994046) : 0.0;
+        if (a.lsum_bar) qlv += a.lsum_bar[m];   // (the AGN's L_bol scale)
+        ql_s[k] = k < nk ? (float)(qlv / cs) : 0.f;
     }
     __syncthreads();
     if (tid == 0) {
@@ -944,7 +946,7 @@ struct OpsInterpRevArgs {
     int noff[3], nn[3];
     double x0[3], h[3];
     float lim_lo, lim_hi;
-    const double *wz, *alpha, *cscale, *mass_bar, *lbol_bar, *sums;
+    const double *wz, *alpha, *cscale, *mass_bar, *lbol_bar, *lsum_bar, *sums;
     const double2 *kconst;                   // n: 1 / T and c2 (the forward's)
     const float *xbar;                       // rows x ktot: Vbar B of the chunk
     const float *mrow, *lrow;
@@ -984,7 +986,9 @@ __global__ void __launch_bounds__(OPS_IR_THREADS) ops_interp_rev_kernel(OpsInter
         for (int j = 0; j < 3; ++j) dlnT_s[j] = dl[j];
         const double ls = a.sums[(size_t)6 * m + 1];
         qm_s = a.mass_bar ? (float)(a.mass_bar[m] / cs) : 0.f;
-        ql_s = (a.lbol_bar && ls > SAFE_FLOOR) ? (float)(a.lbol_bar[m] / (ls * 2.302585092994046 * cs)) : 0.f;
+        double qlv = (a.lbol_bar && ls > SAFE_FLOOR) ? a.lbol_bar[m] / (ls * 2.302585092994046) : 0.0;
+        if (a.lsum_bar) qlv += a.lsum_bar[m];   // (the AGN's L_bol scale)
+        ql_s = (float)(qlv / cs);
     }
     __syncthreads();
     const double2 kc = a.kconst[m];                  // 1 / T, c2
@@ -1139,7 +1143,7 @@ int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err) {
         a.m0 = m0; a.nt = nt; a.nz = nz; a.R = R; a.ktot = ktot; a.imf_type = r.imf_type;
         for (int s = 0; s < 3; ++s) { a.noff[s] = o.interp_noff[s]; a.nn[s] = o.interp_nn[s]; a.x0[s] = o.interp_x0[s]; a.h[s] = o.interp_h[s]; }
         a.lim_lo = r.lim_lo; a.lim_hi = r.lim_hi;
-        a.wz = r.wz; a.alpha = r.alpha; a.cscale = r.cscale; a.mass_bar = r.mass_bar; a.lbol_bar = r.lbol_bar; a.sums = r.sums;
+        a.wz = r.wz; a.alpha = r.alpha; a.cscale = r.cscale; a.mass_bar = r.mass_bar; a.lbol_bar = r.lbol_bar; a.lsum_bar = r.lsum_bar; a.sums = r.sums;
         a.kconst = c.d_ix_const.p; a.xbar = c.d_xbar.p; a.mrow = o.i_mrow.p; a.lrow = o.i_lrow.p;
         a.wzb = r.wzb; a.params_bar = r.params_bar; a.rows = r.rows; a.row_imf1 = r.row_imf1;
         ops_interp_rev_kernel<<<rows, OPS_IR_THREADS, 0, st>>>(a);
