@@ -1127,6 +1127,36 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         if ((e = cudaGetLastError()) != cudaSuccess) { err = msg("ionizing light reverse kernel", e); return ST_DATA_MISSING; }
         ++launches;
     }
+    // ---- the nebular continuum (added to the young and old sums by the forward): into the weights' cotangent and
+    // the gas_logz, gas_logu and frac_obrun rows
+    if (c.geom.neb && !ops) {
+        NebContRevArgs na;
+        na.n = n; na.nspec = ns; na.nt = c.nt; na.nz = c.nz; na.nt_neb = c.nt_neb; na.cw_ld = c.nt_neb + 2;
+        na.itesc = c.geom.itesc; na.ppad = (ns + gemm_bk() - 1) / gemm_bk() * gemm_bk(); na.ntz = ntz;
+        // the nebular ages by CLOUDY interval (ascending with the ages)
+        for (int k = 0; k < 10; ++k) {
+            int t = 0;
+            while (t < c.nt_neb && c.neb.ia[t] < k) ++t;
+            na.kfirst[k] = t;
+        }
+        c.neb.h_wa.assign(c.neb.wa.begin(), c.neb.wa.end());
+        if ((e = c.neb.d_wa.reserve(std::max<size_t>(c.neb.h_wa.size(), 1))) != cudaSuccess ||
+            (e = cudaMemcpyAsync(c.neb.d_wa.p, c.neb.h_wa.data(), sizeof(float) * c.neb.h_wa.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+            err = msg("nebular continuum reverse inputs", e);
+            return ST_DATA_MISSING;
+        }
+        na.dem = c.d_dem.p; na.tab = c.neb.tab[c.geom.neb_table].p; na.off = c.neb.off.p; na.wa = c.neb.d_wa.p;
+        na.cw = c.neb.cw.p; na.q0 = c.neb.q0.p; na.q0_exp = c.neb.q0_exp;
+        na.ybh = c.d_ybh.p; na.ybl = c.d_ybl.p; na.obh = c.d_obh.p; na.obl = c.d_obl.p; na.cscale = c.d_cscale.p;
+        na.wzbar = (weights_z_bar || sfh_rev) ? c.d_wzbar.p : nullptr;
+        na.params_bar = c.d_pbar.p; na.rows = NBGRAD;
+        na.row_gas_logz = 13; na.row_gas_logu = 14; na.row_frac_obrun = 6;
+        if ((e = run_nebular_continuum_reverse(na, s)) != cudaSuccess) {
+            err = msg("nebular continuum reverse kernel", e);
+            return ST_DATA_MISSING;
+        }
+        ++launches;
+    }
     if (!ops && weights_z_bar &&
         (e = cudaMemcpyAsync(weights_z_bar, c.d_wzbar.p, sizeof(double) * (size_t)n * ntz, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
         err = msg("weights cotangent copy", e);

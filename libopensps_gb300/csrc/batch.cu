@@ -599,7 +599,6 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     std::vector<int2> neb_chunk_groups;    // the nebular continuum: per chunk its first group and group count
     if (epi_terms) {
         if (fp64) { err = "dust emission, AGN and the nebular continuum are not supported on the plain FP64 path"; return ST_UNSUPPORTED; }
-        if (io.keep_parts && neb_cont) { err = "gradients with the nebular continuum are not supported on this path"; return ST_UNSUPPORTED; }
         if (io.dev_inputs) { err = "dust emission, AGN and the nebular continuum need host inputs on this path"; return ST_UNSUPPORTED; }
         if (neb_cont && c.ops.ready) { err = "the nebular continuum with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
         if (any_emis) { if (int rc = dustem_load(c, err)) return rc; }
@@ -665,6 +664,15 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                 cell(c.neb.logz, par(m, PF_GAS_LOGZ), q.neb_iz, q.neb_wz);
                 cell(c.neb.logu, par(m, PF_GAS_LOGU), q.neb_iu, q.neb_wu);
                 q.neb_fabs = (float)std::fabs(1.0 - par(m, PF_FRAC_OBRUN));
+                // the reverse pass's chain factors (batch_chain_derivatives :4686-4697: inside the cell, its
+                // inverse width; zero where the weight is clamped) and d|1 - fo| / dfo
+                auto chain = [](const std::vector<double> &g, double x, int i) {
+                    return (x >= g[i] && x <= g[i + 1]) ? (float)(1.0 / (g[i + 1] - g[i])) : 0.f;
+                };
+                q.neb_dz = chain(c.neb.logz, par(m, PF_GAS_LOGZ), q.neb_iz);
+                q.neb_du = chain(c.neb.logu, par(m, PF_GAS_LOGU), q.neb_iu);
+                const double om = 1.0 - par(m, PF_FRAC_OBRUN);
+                q.neb_dfo = om > 0.0 ? -1.f : (om < 0.0 ? 1.f : 0.f);
             }
         }
         if (neb_cont) {
@@ -785,6 +793,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     c.geom.n = 0;
     c.geom.emis = epi_terms && any_emis;
     c.geom.agn = epi_terms && any_agn;
+    c.geom.neb = neb_cont;
+    c.geom.neb_table = neb_table;
 
     // ---- scratch
     const int bn = contract_models_per_tile(nacc);

@@ -163,10 +163,12 @@ struct NebularGrid {
     DevBuf<int> order;
     DevBuf<int4> groups;
     DevBuf<float> cw;
+    std::vector<float> h_wa;     // wa in FP32 (the reverse pass's copy, d_wa)
+    DevBuf<float> d_wa;
     void release() {
         tab[0].release(); tab[1].release(); off.release(); q0.release(); runs.release();
         ia.clear(); wa.clear(); h_runs.clear(); runs_itesc = -1; nrun = 0;
-        order.release(); groups.release(); cw.release();
+        order.release(); groups.release(); cw.release(); d_wa.release(); h_wa.clear();
         have[0] = have[1] = false;
     }
 };
@@ -179,6 +181,8 @@ struct BatchGeom {
     int itesc = 0;               // the first old age
     const double *wz = nullptr;  // the weights over ages and metallicities on the device (with the operators)
     bool emis = false, agn = false;   // the batch had dust emission / the AGN torus (cells in d_dem, chains in d_dchain)
+    bool neb = false;                 // the batch had the nebular continuum (cells in d_dem, C(t) / S in neb.cw)
+    int neb_table = 0;                // its table (nebular/<isoc>_nodust or _dust)
 };
 
 struct Context {

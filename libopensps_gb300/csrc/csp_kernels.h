@@ -222,6 +222,9 @@ struct DustEmModel {
     // the weights (clamped to [0, 1]) in gas_logz and gas_logu, and |1 - frac_obrun|
     int neb_iz, neb_iu;
     float neb_wz, neb_wu, neb_fabs;
+    // for the reverse pass: d w_z / d gas_logz and d w_u / d gas_logu (zero where the weight is clamped), and
+    // d |1 - frac_obrun| / d frac_obrun
+    float neb_dz, neb_du, neb_dfo;
 };
 struct AdjointArgs {
     int n_models, nspec, ppad, nbands, jtop, j0, j1, sm_lo, sm_hi, uniform_index;
@@ -417,6 +420,24 @@ struct NebContArgs {
     float *young, *old;       // n x nspec
 };
 cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_t st);
+// The continuum's reverse pass (ssp_op.cu): the young and old sums' cotangents (bf16 hi / lo, scaled by 1 / cscale)
+// against the forward's terms, into the weights' cotangent and the gas_logz, gas_logu and frac_obrun rows.
+struct NebContRevArgs {
+    int n, nspec, nt, nz, nt_neb, cw_ld, itesc, ppad, ntz;
+    int kfirst[10];           // the nebular ages in CLOUDY interval k: kfirst[k] .. kfirst[k + 1] - 1 (k < 9)
+    const DustEmModel *dem;
+    const float *tab, *off;   // the forward's table (log2, relative to the pixel offsets off)
+    const float *wa;          // nt_neb: each nebular age's weight in its CLOUDY interval
+    const float *cw;          // n x cw_ld: the forward's C(t) / S, then log2 S (integer part, rest)
+    const float *q0;          // nt_neb x nz, times 2^q0_exp
+    int q0_exp;
+    const __nv_bfloat16 *ybh, *ybl, *obh, *obl;   // n x ppad
+    const double *cscale;
+    double *wzbar;            // n x ntz (age t + nt z), or null
+    double *params_bar;       // n x rows
+    int rows, row_gas_logz, row_gas_logu, row_frac_obrun;
+};
+cudaError_t run_nebular_continuum_reverse(const NebContRevArgs &a, cudaStream_t st);
 
 // Casts the FP32 spectra to FP64 (the C API's double outputs), n_models x nspec from ld-strided rows.
 cudaError_t run_spec_to_f64(const float *src, int ld, int nspec, int n_models, double *dst, cudaStream_t st);

@@ -1553,6 +1553,117 @@ __global__ void __launch_bounds__(NEB_PIX) neb_cont_kernel(NebContArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------- its reverse pass
+// backward_nebular's continuum (src/physics/opensps_csp_batch.f90:5334-5606). With g the young or old sums' cotangent
+// (as the forward added age t's term), per model and nebular age t the pixel sums
+//     A_t  = sum_j g_j 2^(E + off_j + L_t(j)),     E = log2 S,   L_t = L_k + wa_t (L_k+1 - L_k),
+//     Az_t = sum_j g_j 2^(...) dL_t/dw_z (j),      Au_t = sum_j g_j 2^(...) dL_t/dw_u (j),
+// (L_k the cell's bilinear form c + w_z dz + w_u (du + w_z dzu) of CLOUDY age k, in log2, as the forward forms it),
+// so that dL / dC_t = A_t / S. Then the weights' cotangent gains dL/dC_t |1 - frac_obrun| q0(t, z); the gas_logz and
+// gas_logu rows ln 2 sum_t (C_t / S) Az_t (Au_t) times the cell's chain factor; frac_obrun's row sum_t (C_t / S) A_t
+// d|1 - fo|/dfo / |1 - fo|. One CTA per model: a thread takes a pixel per step, every age's three sums go over the
+// warp's lanes and lane 0 adds them to its warp's row in shared memory.
+constexpr int NEB_REV_THREADS = 256;
+__global__ void __launch_bounds__(NEB_REV_THREADS) neb_cont_rev_kernel(NebContRevArgs a) {
+    constexpr int NU = 7, NA = 10, NW = NEB_REV_THREADS / 32;
+    __shared__ float acc[NW][NEB_MAX_AGES][3];
+    __shared__ float wa_s[NEB_MAX_AGES];
+    __shared__ double red[NW][3];
+    const int m = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const DustEmModel dm = a.dem[m];
+    if (!(dm.neb_fabs > 0.f)) return;                  // (the forward added no continuum)
+    for (int i = tid; i < NW * NEB_MAX_AGES * 3; i += NEB_REV_THREADS) (&acc[0][0][0])[i] = 0.f;
+    for (int t = tid; t < a.nt_neb; t += NEB_REV_THREADS) wa_s[t] = __ldg(a.wa + t);
+    __syncthreads();
+    const float *cw = a.cw + (size_t)m * a.cw_ld;
+    const float E = __ldg(cw + a.nt_neb) + __ldg(cw + a.nt_neb + 1);
+    const size_t plane = (size_t)NA * a.nspec;
+    const float *b00 = a.tab + (size_t)(dm.neb_iz * NU + dm.neb_iu) * plane, *b01 = b00 + plane;
+    const float *b10 = a.tab + (size_t)((dm.neb_iz + 1) * NU + dm.neb_iu) * plane, *b11 = b10 + plane;
+    const float wz = dm.neb_wz, wu = dm.neb_wu;
+    const __nv_bfloat16 *yh = a.ybh + (size_t)m * a.ppad, *yl = a.ybl + (size_t)m * a.ppad;
+    const __nv_bfloat16 *oh = a.obh + (size_t)m * a.ppad, *ol = a.obl + (size_t)m * a.ppad;
+    for (int p0 = 0; p0 < a.nspec; p0 += NEB_REV_THREADS) {
+        const int p = p0 + tid;
+        const bool ok = p < a.nspec;
+        const int pc = ok ? p : a.nspec - 1;
+        const float gy = ok ? __bfloat162float(yh[p]) + __bfloat162float(yl[p]) : 0.f;
+        const float go = ok ? __bfloat162float(oh[p]) + __bfloat162float(ol[p]) : 0.f;
+        const float base = E + __ldg(a.off + pc);
+        float L[NA], Lz[NA], Lu[NA];
+#pragma unroll
+        for (int k = 0; k < NA; ++k) {
+            const float t00 = __ldg(b00 + (size_t)k * a.nspec + pc), t01 = __ldg(b01 + (size_t)k * a.nspec + pc);
+            const float t10 = __ldg(b10 + (size_t)k * a.nspec + pc), t11 = __ldg(b11 + (size_t)k * a.nspec + pc);
+            const float dz = t10 - t00, du = t01 - t00, dzu = (t11 - t10) - (t01 - t00);
+            L[k] = fmaf(wz, dz, fmaf(wu, fmaf(wz, dzu, du), t00));
+            Lz[k] = fmaf(wu, dzu, dz);
+            Lu[k] = fmaf(wz, dzu, du);
+        }
+#pragma unroll
+        for (int k = 0; k < NA - 1; ++k) {
+            const int t1 = a.kfirst[k + 1];
+            for (int t = a.kfirst[k]; t < t1; ++t) {
+                const float w = wa_s[t];
+                const float g = t < a.itesc ? gy : go;
+                const float e = ops_ex2(base + fmaf(w, L[k + 1] - L[k], L[k]));
+                float v0 = g != 0.f ? g * e : 0.f;
+                float v1 = v0 * fmaf(w, Lz[k + 1] - Lz[k], Lz[k]);
+                float v2 = v0 * fmaf(w, Lu[k + 1] - Lu[k], Lu[k]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    v0 += __shfl_xor_sync(0xffffffffu, v0, o);
+                    v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                    v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+                }
+                if (lane == 0) { acc[warp][t][0] += v0; acc[warp][t][1] += v1; acc[warp][t][2] += v2; }
+            }
+        }
+    }
+    __syncthreads();
+    const double cs = a.cscale[m], fab = (double)dm.neb_fabs;
+    const double inv_s = exp2(-(double)E), qs = ldexp(1.0, a.q0_exp);
+    double gz = 0.0, gu = 0.0, gfo = 0.0;
+    for (int t = tid; t < a.nt_neb; t += NEB_REV_THREADS) {
+        double A = 0.0, Az = 0.0, Au = 0.0;
+        for (int w = 0; w < NW; ++w) { A += acc[w][t][0]; Az += acc[w][t][1]; Au += acc[w][t][2]; }
+        const double ct = (double)__ldg(cw + t);       // C_t / S
+        gz += ct * Az;
+        gu += ct * Au;
+        gfo += ct * A;
+        if (a.wzbar) {
+            const double dc = A * inv_s * cs * fab * qs;
+            for (int z = 0; z < a.nz; ++z)
+                a.wzbar[(size_t)m * a.ntz + t + (size_t)a.nt * z] += dc * (double)__ldg(a.q0 + (size_t)t * a.nz + z);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        gz += __shfl_xor_sync(0xffffffffu, gz, o);
+        gu += __shfl_xor_sync(0xffffffffu, gu, o);
+        gfo += __shfl_xor_sync(0xffffffffu, gfo, o);
+    }
+    if (lane == 0) { red[warp][0] = gz; red[warp][1] = gu; red[warp][2] = gfo; }
+    __syncthreads();
+    if (tid == 0) {
+        double s[3] = {0.0, 0.0, 0.0};
+        for (int w = 0; w < NW; ++w)
+            for (int i = 0; i < 3; ++i) s[i] += red[w][i];
+        double *pb = a.params_bar + (size_t)a.rows * m;
+        const double ln2 = 0.6931471805599453;
+        pb[a.row_gas_logz] += cs * ln2 * s[0] * (double)dm.neb_dz;
+        pb[a.row_gas_logu] += cs * ln2 * s[1] * (double)dm.neb_du;
+        pb[a.row_frac_obrun] += cs * s[2] * (double)dm.neb_dfo / fab;
+    }
+}
+
+cudaError_t run_nebular_continuum_reverse(const NebContRevArgs &a, cudaStream_t st) {
+    if (a.n <= 0 || a.nt_neb <= 0) return cudaSuccess;
+    if (a.nt_neb > NEB_MAX_AGES) return cudaErrorInvalidValue;
+    neb_cont_rev_kernel<<<a.n, NEB_REV_THREADS, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t run_nebular_continuum(const NebContArgs &a, int ngroups, cudaStream_t st) {
     if (a.n <= 0 || ngroups <= 0) return cudaSuccess;
     neb_weights_kernel<<<(unsigned)((a.n * 32 + 255) / 256), 256, 0, st>>>(a);

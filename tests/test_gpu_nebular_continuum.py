@@ -3,7 +3,9 @@ a standard-format data root with the grid of the setup's isochrones (nebular/syn
 libopensps_gb300.synth_nebular), add_neb_emission and add_neb_continuum on, gas_logz, gas_logu and frac_obrun per
 model, through the whole mixed batch (lines, the escaping ionizing light, birth-cloud and diffuse dust, IGM,
 smoothing, 40 filters) against the FP64 oracle fed the numpy restatement of the grid's loader; with dust emission on
-as well; the continuum's share of the spectrum; and the refusals (gradients, the missing _dust table).
+as well; the continuum's share of the spectrum; its reverse pass (the gas_logz, gas_logu and frac_obrun rows and the
+weights' cotangent against central differences of the oracle, backward_nebular :5334-5606); and the refusal of the
+missing _dust table.
 
 Tolerances as the batch's other tests: spectra <= 1e-4 relative (pixels above 1e-6 of the peak), magnitudes
 <= 1e-3 mag, mass 1e-12 relative.
@@ -140,11 +142,54 @@ def test_continuum_refusals(neb_root, built_lib, restore_root):
     wz, params = _inputs(n, seed=1260)
     c = Context(data_root=neb_root)
     c.set_int("add_neb_emission", 1)
-    with pytest.raises(OpenSPSError) as e:
-        c.csp_batch_grad(params, wz, mags_bar=np.ones((n, c.nbands)))
-    assert e.value.status == 2
     c.set_int("cloudy_dust", 1)
     with pytest.raises(OpenSPSError) as e:
         c.csp_batch(params, ssp_weights_z=wz)
     assert e.value.status == 4 and "synthetic_dust" in e.value.message
     c.close()
+
+
+def test_continuum_reverse_pass(neb_root, built_lib, restore_root):
+    """gas_logz and gas_logu inside a cell of the grid (0.2 .. 0.8 of it), frac_obrun 0.05-0.4: the gas_logz (13),
+    gas_logu (14), frac_obrun (6) and dust2 (2) rows and the weights' cotangent along a random direction against
+    central differences (h = 1e-4 relative) of the oracle. Tolerance |g - g_fd| <= 2e-3 max(|g_fd|, 1e-3 max_rows)."""
+    from libopensps_gb300.capi import Context
+    from libopensps_gb300.workloads import adjoint_cotangents
+    from oracle import stdformat as ora
+    n = 5
+    wz, params = _inputs(n, seed=1280)
+    o, d = _oracle(neb_root)
+    grid = ora.nebular(neb_root, d["lambda"], "synthetic_nodust")
+    rng = np.random.default_rng(1281)
+
+    def mid(g):
+        i = rng.integers(0, g.size - 1, n)
+        return g[i] + rng.uniform(0.2, 0.8, n) * (g[i + 1] - g[i])
+
+    params = dict(params, gas_logz=mid(grid["logz"]), gas_logu=mid(grid["logu"]),
+                  frac_obrun=rng.uniform(0.05, 0.4, n), dust2=rng.uniform(0.1, 1.0, n))
+    c = Context(data_root=neb_root)
+    c.set_int("add_neb_emission", 1)
+    c.set_int("add_igm_absorption", 1)
+    mb, sb = adjoint_cotangents(n, c.nspec, c.nbands, seed=1282)
+    got = c.csp_batch_grad(params, wz, mags_bar=mb, spec_bar=sb)
+    c.close()
+
+    def loss(out):
+        return np.nansum(mb * out["mags"], axis=1) + np.sum(sb * out["spec"], axis=1)
+
+    rows = {"gas_logz": 13, "gas_logu": 14, "frac_obrun": 6, "dust2": 2}
+    g = np.stack([got["params_bar"][:, r] for r in rows.values()], axis=1)
+    fd = np.empty_like(g)
+    for i, k in enumerate(rows):
+        h = 1e-4 * np.abs(params[k])
+        fd[:, i] = (loss(o.csp_batch(dict(params, **{k: params[k] + h}), wz))
+                    - loss(o.csp_batch(dict(params, **{k: params[k] - h}), wz))) / (2.0 * h)
+    scale = np.max(np.abs(fd), axis=1, keepdims=True)
+    err = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * scale)
+    assert float(err.max()) <= 2e-3, {k: float(err[:, i].max()) for i, k in enumerate(rows)}
+    dw = wz * rng.standard_normal(wz.shape)
+    fdw = (loss(o.csp_batch(params, wz + 1e-4 * dw)) - loss(o.csp_batch(params, wz - 1e-4 * dw))) / 2e-4
+    gw = np.sum(got["weights_z_bar"] * dw, axis=(1, 2))
+    e = np.abs(gw - fdw) / np.maximum(np.abs(fdw), 1e-3 * np.max(np.abs(fdw)))
+    assert float(e.max()) <= 2e-3, (gw, fdw)
