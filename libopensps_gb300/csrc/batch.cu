@@ -1014,12 +1014,21 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
         // ---- the mixed path over models [off, off + nk): weight operand, contraction with its epilogue, bands,
         // FP64 sums (stage marks on the first range)
         auto run_range = [&](int off, int nk, bool marks) -> int {
-            if ((e = model_params(off, nk)) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
-            if (marks) prof_mark(c, 1);
             WeightsArgs w = wa;
             w.n_models = nk; w.wz = d_wz + (size_t)nt * nz * off; w.w_hi = c.d_whi.p + (size_t)kpad * off;
             w.w_lo = c.d_wlo.p + (size_t)kpad * off; w.sums = c.d_sums.p + (size_t)6 * off;
             if (w.mpar) w.mpar = c.d_mpar.p + (size_t)MODEL_PAR_FLOATS * off;
+            // the operand (which does not read the model parameters unless it forms escaping-light columns) on its
+            // own stream beside the model parameters, forked from the batch's stream and joined before the
+            // contraction
+            const bool fork_w = !direct && !w.mpar;
+            if (fork_w && ((e = cudaEventRecord(c.ev_w0, st)) != cudaSuccess || (e = cudaStreamWaitEvent(c.side4, c.ev_w0, 0)) != cudaSuccess ||
+                           (e = run_weights_convert_sums(w, c.side4)) != cudaSuccess || (e = cudaEventRecord(c.ev_w1, c.side4)) != cudaSuccess)) {
+                err = cuda_msg("weights kernel", e);
+                return ST_DATA_MISSING;
+            }
+            if ((e = model_params(off, nk)) != cudaSuccess) { err = cuda_msg("model parameter kernel", e); return ST_DATA_MISSING; }
+            if (marks) prof_mark(c, 1);
             // (the operand and, in the same pass over the FP64 weights, the FP64 mass and L_bol sums; reading the
             // caller's pageable weights in place, on the side stream beside the previous chunk's kernels)
             if (direct) {
@@ -1036,6 +1045,8 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
                     err = cuda_msg("weights kernel", e);
                     return ST_DATA_MISSING;
                 }
+            } else if (fork_w) {
+                if ((e = cudaStreamWaitEvent(st, c.ev_w1, 0)) != cudaSuccess) { err = cuda_msg("weights kernel", e); return ST_DATA_MISSING; }
             } else if ((e = run_weights_convert_sums(w, st)) != cudaSuccess) {
                 err = cuda_msg("weights kernel", e);
                 return ST_DATA_MISSING;

@@ -214,7 +214,10 @@ Context::~Context() {
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
     if (side3) cudaStreamDestroy(side3);
+    if (side4) cudaStreamDestroy(side4);
     if (ev_cot) cudaEventDestroy(ev_cot);
+    if (ev_w0) cudaEventDestroy(ev_w0);
+    if (ev_w1) cudaEventDestroy(ev_w1);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -733,7 +736,10 @@ int context_setup_grid(Context &c, std::string &err) {
         (!c.side && (e = cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.side2 && (e = cudaStreamCreateWithFlags(&c.side2, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.side3 && (e = cudaStreamCreateWithFlags(&c.side3, cudaStreamNonBlocking)) != cudaSuccess) ||
+        (!c.side4 && (e = cudaStreamCreateWithFlags(&c.side4, cudaStreamNonBlocking)) != cudaSuccess) ||
         (!c.ev_cot && (e = cudaEventCreateWithFlags(&c.ev_cot, cudaEventDisableTiming)) != cudaSuccess) ||
+        (!c.ev_w0 && (e = cudaEventCreateWithFlags(&c.ev_w0, cudaEventDisableTiming)) != cudaSuccess) ||
+        (!c.ev_w1 && (e = cudaEventCreateWithFlags(&c.ev_w1, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_contract && (e = cudaEventCreateWithFlags(&c.ev_contract, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_fork && (e = cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming)) != cudaSuccess) ||
         (!c.ev_params && (e = cudaEventCreateWithFlags(&c.ev_params, cudaEventDisableTiming)) != cudaSuccess) ||

@@ -234,7 +234,8 @@ struct Context {
     cudaStream_t side = nullptr;                 // the per-model parameters run here
     cudaStream_t side2 = nullptr;                // the FP64 sums run here (after the contraction)
     cudaStream_t side3 = nullptr;                // a reverse pass's cotangents go up here, beside its forward
-    cudaEvent_t ev_cot = nullptr;
+    cudaStream_t side4 = nullptr;                // the weight operand, beside the per-model parameters
+    cudaEvent_t ev_cot = nullptr, ev_w0 = nullptr, ev_w1 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_params = nullptr, ev_contract = nullptr, ev_sums = nullptr;
     DevBuf<float> d_pix, d_wl, d_igm_a;
     DevBuf<int> d_do_band;
