@@ -39,6 +39,7 @@ typedef enum {
 #define OPENSPS_STATUS_OK 0
 #define OPENSPS_ERR_COMPUTE_UNINIT 301
 #define OPENSPS_ERR_SSP_UNINIT 303
+#define OPENSPS_ERR_SSP_IMF_FILE 504       /* opensps.h:101: the user IMF file missing, unreadable or empty */
 #define OPENSPS_ERR_SSP_TABULAR_SFH 508   /* opensps.h:105: the tabular SFH missing, unreadable or too long */
 
 /* ---- driver utilities ---------------------------------------------------------------------------------- */

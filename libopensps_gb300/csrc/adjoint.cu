@@ -1043,7 +1043,7 @@ int run_grad_batch(Context &c, const BatchIO &io_in, const double *mags_bar, con
         prof_mark(c, 8);
         OpsRevArgs r;
         r.n = n; r.nt = c.nt; r.nz = c.nz; r.npt = o.npt; r.ntpad = o.ntpad; r.itesc = c.geom.itesc; r.imf_type = c.imf_type;
-        r.lim_lo = 0.08f; r.lim_hi = 120.f;
+        if (int rc = ops_imf_limits(c, c.imf_type, r.lim, err)) return rc;   // (the forward's limits and user IMF)
         r.wz = c.geom.wz; r.alpha = c.d_alpha.p; r.pts = o.pts.p; r.pidx = o.pidx.p; r.pcoef = o.pcoef.p;
         r.vbar = c.d_vbar.p; r.cscale = c.d_cscale.p;
         r.mass_bar = mass_bar ? c.d_mass_bar.p : nullptr;

@@ -709,13 +709,20 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     }
     if (ops) {
         if (neb) { err = "nebular emission with the SSP operators is not supported on this path"; return ST_UNSUPPORTED; }
-        if (c.imf_type < 0 || c.imf_type > 4) {
-            err = "imf_type " + std::to_string(c.imf_type) +
-                  ": 0 (Salpeter), 1 (Chabrier), 2 (Kroupa), 3 (van Dokkum) and 4 (Dave) with the operators";
+        if (c.imf_type < 0 || c.imf_type > 5) {
+            err = "imf_type " + std::to_string(c.imf_type) + ": the IMF types are 0 to 5";
             return ST_UNSUPPORTED;
+        }
+        if (!(c.imf_lim_lo > 0.0 && c.imf_lim_hi > c.imf_lim_lo)) {
+            err = "the IMF's mass limits must satisfy 0 < imf_lower_limit < imf_upper_limit";
+            return ST_BAD_ARG;
         }
         nacc2 = true;
     } else {
+        if (c.imf_lim_lo != 0.08 || c.imf_lim_hi != 120.0) {
+            err = "IMF mass limits other than 0.08 - 120 M_sun need the SSP operators (opensps_context_build_ssp_ops)";
+            return ST_UNSUPPORTED;
+        }
         for (int m = 0; m < n; ++m)
             for (int id : {PF_IMF1, PF_IMF2, PF_IMF3, PF_VDMC, PF_MDAVE})
                 if (par(m, id) != c.pdef[id]) {

@@ -372,6 +372,8 @@ void opensps_context_set_float(int handle, const char *key, double value, int *s
     if (k == "H0") c->h0 = value;
     else if (k == "om0") c->om0 = value;
     else if (k == "ol0") c->ol0 = value;
+    else if (k == "imf_lower_limit") c->imf_lim_lo = value;   // (the SSP operators' IMF mass limits)
+    else if (k == "imf_upper_limit") c->imf_lim_hi = value;
     else {
         const ParamInfo *p = find_param(key);
         if (!p) return fail(status, 102, "unknown float parameter " + k);
@@ -393,7 +395,12 @@ void opensps_context_set_str(int handle, const char *key, const char *value, int
         if (status) *status = 0;
         return;
     }
-    if (k == "imf_filename") return fail(status, 104, k + " is not supported on this path");
+    if (k == "imf_filename") {   // (the user IMF's file under the data root; read when a batch takes imf_type 5)
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->imf_filename = value ? value : "";
+        if (status) *status = 0;
+        return;
+    }
     return fail(status, 103, "unknown string parameter " + k);
 }
 

@@ -179,7 +179,7 @@ Context::~Context() {
     d_lbol_bar.release(); d_cscale.release(); d_pbar.release(); d_wzbar.release(); d_ybh.release(); d_ybl.release();
     d_obh.release(); d_obl.release(); d_wzb32.release(); d_apar.release();
     d_logage.release(); d_lz.release(); d_lbol.release(); d_sfhpar.release(); d_wgiven.release(); d_w.release();
-    d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release(); d_sfhtab.release();
+    d_sfh_scratch.release(); d_lblend.release(); d_sfr.release(); d_wbar.release(); d_dual.release(); d_sfhtab.release(); d_user_imf.release();
     ops.release(); dustem.release(); agn.release(); neb.release(); d_alpha.release(); d_vhi.release(); d_vlo.release(); d_yo.release(); d_vpart.release();
     d_spart.release(); d_vflag.release(); d_vbar.release(); d_apart.release(); d_ix_hi.release(); d_ix_lo.release(); d_ipart.release(); d_bpart.release(); d_sfh_mtab.release(); d_ix_const.release(); d_dem.release(); d_w64.release(); d_y64.release(); d_bc64.release(); d_igm_a64.release();
     fp64_release(*this);

@@ -197,6 +197,13 @@ struct Context {
     int ntab = 0;
     std::string sfh_filename = "sfh.dat", sfh_tab_file;
     bool sfh_tab_dirty = true;       // the device copy is stale
+    // the IMF's mass limits (imf_lower_limit, imf_upper_limit) and the user IMF (imf_type 5): its file under the data
+    // root (imf.dat when no name is set) and its segments as read (lower mass, upper mass, slope)
+    double imf_lim_lo = 0.08, imf_lim_hi = 120.0;
+    std::string imf_filename, user_imf_file;
+    std::vector<double> user_imf;
+    DevBuf<float> d_user_imf;        // nuser x 5: lo, hi, 1 - alpha, c / (1 - alpha), c
+    bool user_imf_dirty = true;      // the device table is stale
     int fp64 = 0;                // the plain FP64 path (an extension setting, "gb300_fp64")
     int ops_exact = 0;           // the SSP operator's exact fold only ("gb300_ops_exact"), never the interpolated one
     int add_dust_emission = 0;   // the energy-balance dust emission (Draine & Li templates)
@@ -331,7 +338,7 @@ struct Context {
 
 // status codes of opensps.h
 enum { ST_OK = 0, ST_BAD_HANDLE = 1, ST_UNSUPPORTED = 2, ST_BAD_ARG = 3, ST_DATA_MISSING = 4,
-       ST_NOT_SETUP = 301, ST_NO_OPERATOR = 303, ST_TABULAR_SFH = 508 };
+       ST_NOT_SETUP = 301, ST_NO_OPERATOR = 303, ST_IMF_FILE = 504, ST_TABULAR_SFH = 508 };
 constexpr int SFH_NTABMAX = 20000;   // the tabular SFH's rows at most (NTABMAX, src/core/opensps_constants.f90:147)
 
 void set_error(int status, const std::string &msg);
@@ -395,6 +402,9 @@ int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err);
 int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, const double *h_alpha, int itesc,
                   float *d_young, float *d_old, std::string &err);
 void imf_pack(int imf_type, const double *pv, double *ap);
+// The IMF's limits and user segments for the operator kernels (the user IMF read and uploaded when imf_type is 5): 0,
+// or ST_IMF_FILE / ST_DATA_MISSING with err.
+int ops_imf_limits(Context &c, int imf_type, OpsImfLim &lim, std::string &err);
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err);
 // With profiling on: records event k on the context's stream (0 starts a batch's set).

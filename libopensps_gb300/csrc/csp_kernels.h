@@ -304,15 +304,29 @@ size_t sfh_dual_bytes();
 
 // The SSP operator applied to per-model IMFs (ssp_op.cu). A point of the isochrones of one grid point: the IMF bin
 // [lo, hi] (ln lo and ln(hi / lo) for the bins inside one power-law segment of the IMF), the Kroupa segment (1 .. 3,
-// 0: the bin crosses a segment boundary, -1: no stars), the star's current mass and L_bol.
+// 0: the bin crosses a segment boundary, -1: no stars within the mass limits 0.08 - 120 M_sun the operator is built
+// with), the star's current mass and L_bol, and its initial mass (negative for the first point of its age, whose bin
+// starts at the IMF's lower edge).
 struct OpsPoint {
     float ln_lo, dl, mcur, lum, lo, hi;
-    int seg, pad;
+    int seg;
+    float mini;
+};
+// The IMF's mass limits and the user IMF as the exact fold and its reverse take them. custom: limits or a lower edge
+// other than the build's (0.08, 120, 0.08 M_sun), or the user IMF: every bin then takes the generic path, gated by
+// its point's initial mass (compute_imf_weights, src/physics/opensps_imf.f90:111-172).
+struct OpsImfLim {
+    double lim_lo = 0.08, lim_hi = 120.0;    // the normalisation's mass range and the points' gate
+    float lb = 0.08f;                        // the lower edge of each age's first bin
+    int custom = 0;
+    const float *user = nullptr;             // nuser x 5: lo, hi, e = 1 - alpha, c / e (0 for e = 0), c
+    int nuser = 0;
+    double user_inv_total = 1.0;             // 1 / (the user IMF's mass between the limits), FP64 on the host
 };
 struct OpsFoldArgs {
     int n, nt, nz, npt, nent, ntpad, itesc;
-    int imf_type = 2;         // 0 Salpeter (as Kroupa), 2 Kroupa, 3 van Dokkum, 4 Dave
-    float lower_bound, lim_lo, lim_hi;
+    int imf_type = 2;         // 0 Salpeter, 1 Chabrier, 2 Kroupa, 3 van Dokkum, 4 Dave, 5 the user's segments
+    OpsImfLim lim;
     const double *wz;         // n x nt x nz SFH weights (age fastest)
     const double *alpha;      // n x 3: the IMF's parameters (Kroupa: imf1-3; van Dokkum: vdmc; Dave: imf1, imf2,
                               // mdave)
@@ -350,7 +364,7 @@ struct OpsInterpReduceArgs {
 struct OpsRevArgs {
     int n, nt, nz, npt, ntpad, itesc;
     int imf_type = 2;         // the IMF's rows: Kroupa (2) imf1-3, Dave (4) imf1, imf2, mdave; zero otherwise
-    float lim_lo, lim_hi;
+    OpsImfLim lim;
     const double *wz;         // n x nt x nz SFH weights (age fastest)
     const double *alpha;      // n x 3: the IMF's parameters (as OpsFoldArgs)
     const OpsPoint *pts;      // (nt x nz) x npt

@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <fstream>
+#include <sstream>
 #include <string>
 #include <vector>
 #include "context.h"
@@ -55,17 +56,22 @@ __device__ __forceinline__ float ops_expm1(float y) {
 
 // One model's IMF as the fold kernels take it: up to three segments [lo, hi], each a power law c m^-alpha (e = 1 -
 // alpha, ce = c / e). Kroupa's breaks are fixed (each point's segment found once, OpsPoint::seg); van Dokkum's and
-// Dave's move with the model (generic: every bin split at the model's breaks). For van Dokkum segment 0 is the
-// lognormal A exp(-z^2) per unit ln m, z = (log10 m - u0) zs (zs = 1 / (sigma sqrt 2)), whose bin integral is
+// Dave's move with the model (generic: every bin split at the model's breaks). For van Dokkum and Chabrier segment 0
+// is the lognormal A exp(-z^2) per unit ln m, z = (log10 m - u0) zs (zs = 1 / (sigma sqrt 2)), whose bin integral is
 // la int e^(-z^2) dz (la = A ln 10 sigma sqrt 2). For the reverse pass: lnb = ln b of the continuity factor
 // c2 = b^(alpha2 - alpha1) (Kroupa b = 0.5, Dave b = mdave) and d3 = d ln c2 / d(third parameter) (Dave:
-// (alpha2 - alpha1) / mdave; Kroupa: 0, its third slope acts through segment 3).
+// (alpha2 - alpha1) / mdave; Kroupa: 0, its third slope acts through segment 3). With custom limits (OpsImfLim)
+// the points are gated by initial mass against [glo, ghi] and an age's first bin starts at lb; the user IMF's
+// segments (nuser, the table user) replace the three.
 struct KroupaSeg {
     float e[3], ce[3], c[3];
     float lo[3], hi[3];
     int generic, logn;
     float la, u0, zs;
     double lnb, d3;
+    int custom, nuser;
+    float glo, ghi, lb;
+    const float *user;
 };
 
 // c lo^e expm1(e dl) / e over one segment (e = 0: c dl)
@@ -91,14 +97,47 @@ __device__ __forceinline__ float logn_piece(const KroupaSeg &k, float lo, float 
     return c * (erff(z2) - erff(z1));
 }
 
+// The user IMF over [lo, hi] (imf_integral case 5, src/physics/opensps_imf.f90:287-305): each segment's power law
+// c_s m^-alpha_s over its own [lo_s, hi_s] (c_s continuous at each segment's lower mass); overlapping segments add,
+// gaps weigh nothing. The table is the same for every lane (broadcast loads).
+__device__ __forceinline__ float user_piece(const KroupaSeg &k, float lo, float hi) {
+    float v = 0.f;
+    for (int s = 0; s < k.nuser; ++s) {
+        const float *u = k.user + 5 * s;
+        const float a = fmaxf(lo, __ldg(u)), b = fminf(hi, __ldg(u + 1));
+        if (b > a) {
+            const float e = __ldg(u + 2), dl = logf(b / a);
+            v += e == 0.f ? __ldg(u + 4) * dl
+                          : __ldg(u + 3) * ops_ex2(e * logf(a) * 1.4426950408889634f) * ops_expm1(e * dl);
+        }
+    }
+    return v;
+}
+
+// With custom limits: the bin's lower edge, or a negative value when the point weighs nothing (its initial mass
+// outside the limits, or an empty bin).
+__device__ __forceinline__ float custom_lo(const KroupaSeg &k, const OpsPoint &q) {
+    const float mi = fabsf(q.mini);
+    if (mi < k.glo || mi > k.ghi) return -1.f;
+    const float lo = q.mini < 0.f ? k.lb : q.lo;
+    return q.hi > lo ? lo : -1.f;
+}
+
 __device__ __forceinline__ float imf_weight(const KroupaSeg &k, const OpsPoint &q) {
-    if (q.seg < 0) return 0.f;
-    if (q.seg > 0 && !k.generic) return seg_piece(k, q.seg - 1, q.ln_lo, q.dl);
+    float qlo = q.lo;
+    if (k.custom) {
+        qlo = custom_lo(k, q);
+        if (qlo < 0.f) return 0.f;
+        if (k.nuser) return user_piece(k, qlo, q.hi);
+    } else {
+        if (q.seg < 0) return 0.f;
+        if (q.seg > 0 && !k.generic) return seg_piece(k, q.seg - 1, q.ln_lo, q.dl);
+    }
     // a bin across a segment boundary (or any bin with the breaks per model): its pieces in each segment
     float v = 0.f;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-        const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
+        const float lo = fmaxf(qlo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
         if (hi > lo) v += (s == 0 && k.logn) ? logn_piece(k, lo, hi) : seg_piece(k, s, logf(lo), logf(hi / lo));
     }
     return v;
@@ -140,7 +179,7 @@ __device__ __forceinline__ float ops_g2(float x) {
 // FP64. With dlnT non-null also d ln(mass) / d alpha_j, j = 1..3, for the reverse pass: a segment's piece
 // P = c lo^em expm1(em dl) / em (em = 2 - alpha, dl = ln(hi / lo)) has dP/dem = c lo^em dl (ln lo g1 + dl g2)(em dl)
 // and c2 the factor 2^(alpha1 - alpha2).
-__device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
+__device__ inline void kroupa_setup(const double *al3, double lim_lo, double lim_hi, KroupaSeg &k, float &inv_total,
                                     double *dlnT, double *total_out = nullptr) {
     const double a1 = al3[0], a2 = al3[1], a3 = al3[2];
     const double c2 = pow(0.5, -a1 + a2);
@@ -154,7 +193,7 @@ __device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_h
         k.ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
         k.lo[sg] = (float)slo[sg];
         k.hi[sg] = (float)shi[sg];
-        const double lo = fmax((double)lim_lo, slo[sg]), hi = fmin((double)lim_hi, shi[sg]);
+        const double lo = fmax(lim_lo, slo[sg]), hi = fmin(lim_hi, shi[sg]);
         if (hi > lo) {
             const double em = 2.0 - al[sg];   // mass-weighted: int c m^(1 - alpha) dm
             const double piece = (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
@@ -184,7 +223,7 @@ __device__ inline void kroupa_setup(const double *al3, float lim_lo, float lim_h
 // Dave 2008 (p = alpha1, alpha2, mdave): m^-alpha1 over [0.08, mdave], mdave^(alpha2 - alpha1) m^-alpha2 above
 // (imf_integral case 4); 1 / T and, with dlnT, d ln T / d(alpha1, alpha2, mdave) (imf_integral_dp case 4: the
 // moving break's edge terms cancel, the IMF being continuous there).
-__device__ inline void dave_setup(const double *p, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
+__device__ inline void dave_setup(const double *p, double lim_lo, double lim_hi, KroupaSeg &k, float &inv_total,
                                   double *dlnT, double *total_out = nullptr) {
     const double a1 = p[0], a2 = p[1], md = p[2];
     const double c2 = pow(md, -a1 + a2);
@@ -197,7 +236,7 @@ __device__ inline void dave_setup(const double *p, float lim_lo, float lim_hi, K
         k.ce[sg] = e != 0.0 ? (float)(cs[sg] / e) : 0.f;
         k.lo[sg] = (float)slo[sg];
         k.hi[sg] = (float)shi[sg];
-        const double lo = fmax((double)lim_lo, slo[sg]), hi = fmin((double)lim_hi, shi[sg]);
+        const double lo = fmax(lim_lo, slo[sg]), hi = fmin(lim_hi, shi[sg]);
         if (hi > lo) {
             const double em = 2.0 - al[sg];
             const double piece = (em == 0.0) ? cs[sg] * log(hi / lo) : cs[sg] * pow(lo, em) * expm1(em * log(hi / lo)) / em;
@@ -224,33 +263,33 @@ __device__ inline void dave_setup(const double *p, float lim_lo, float lim_hi, K
     }
 }
 
-// van Dokkum 2008 (p[0] = vdmc): the lognormal 0.14 (12.5 vdmc)^-1.3 exp(-(log10 m - log10 vdmc)^2 / (2 0.69^2)) per
-// unit ln m up to 25 vdmc, 0.0443 m^-2.3 above (imf_integral case 3, constants src/physics/opensps_imf.f90:39-44);
-// 1 / T with the lognormal's mass in closed form (its centre shifted by ln 10 sigma^2). No parameters in the reverse
-// pass (imf_integral_dp has none for it): dlnT zero.
-__device__ inline void vd_setup(const double *p, float lim_lo, float lim_hi, KroupaSeg &k, float &inv_total,
-                                double *dlnT, double *total_out = nullptr) {
-    const double vdmc = p[0], br = 25.0 * vdmc, s2 = 0.69 * 0.69, sig = 0.69, K = 2.302585092994046;
-    const double A = 0.14 * pow(0.5 * br, -1.3), u0 = log10(vdmc);
+// A lognormal A exp(-(log10 m - u0)^2 / (2 0.69^2)) per unit ln m up to the break br, c_hi m^-2.3 above: van Dokkum
+// 2008 (imf_integral case 3; A = 0.14 (12.5 vdmc)^-1.3, u0 = log10 vdmc, br = 25 vdmc, c_hi = 0.0443, constants
+// src/physics/opensps_imf.f90:39-44) and Chabrier 2003 (case 1: A = 1, u0 = log10 0.08, br = 1 M_sun,
+// c_hi = exp(-u0^2 / (2 0.69^2))). 1 / T with the lognormal's mass in closed form (its centre shifted by
+// ln 10 sigma^2). No parameters in the reverse pass (imf_integral_dp has none for either): dlnT zero.
+__device__ inline void logn_setup(double A, double u0, double br, double c_hi, double lim_lo, double lim_hi,
+                                  KroupaSeg &k, float &inv_total, double *dlnT, double *total_out = nullptr) {
+    const double s2 = 0.69 * 0.69, sig = 0.69, K = 2.302585092994046;
     double total = 0.0;
-    // the lognormal's mass over [lim_lo, min(lim_hi, 25 vdmc)]: A e^(K u0 + K^2 sigma^2 / 2) K sigma sqrt(pi / 2)
+    // the lognormal's mass over [lim_lo, min(lim_hi, br)]: A e^(K u0 + K^2 sigma^2 / 2) K sigma sqrt(pi / 2)
     // (erf(z2) - erf(z1)), z about the shifted centre
-    double lo = (double)lim_lo, hi = fmin((double)lim_hi, br);
+    double lo = lim_lo, hi = fmin(lim_hi, br);
     if (hi > lo) {
         const double cen = u0 + K * s2, sc = exp(K * u0 + 0.5 * K * K * s2) * K * sig * sqrt(0.5 * 3.141592653589793);
         const double z1 = (log10(lo) - cen) / (sig * 1.4142135623730951), z2 = (log10(hi) - cen) / (sig * 1.4142135623730951);
         const double d = z1 >= 0.0 ? erfc(z1) - erfc(z2) : (z2 <= 0.0 ? erfc(-z2) - erfc(-z1) : erf(z2) - erf(z1));
         total += A * sc * d;
     }
-    lo = fmax((double)lim_lo, br);
-    hi = (double)lim_hi;
-    if (hi > lo) total += 0.0443 * pow(lo, -0.3) * expm1(-0.3 * log(hi / lo)) / -0.3;
+    lo = fmax(lim_lo, br);
+    hi = lim_hi;
+    if (hi > lo) total += c_hi * pow(lo, -0.3) * expm1(-0.3 * log(hi / lo)) / -0.3;
     k.e[0] = k.c[0] = k.ce[0] = 0.f;
     k.lo[0] = 0.f;
     k.hi[0] = (float)br;
     k.e[1] = -1.3f;
-    k.c[1] = 0.0443f;
-    k.ce[1] = (float)(0.0443 / -1.3);
+    k.c[1] = (float)c_hi;
+    k.ce[1] = (float)(c_hi / -1.3);
     k.lo[1] = (float)br;
     k.hi[1] = 1.0e30f;
     k.e[2] = k.c[2] = k.ce[2] = 0.f;
@@ -267,12 +306,47 @@ __device__ inline void vd_setup(const double *p, float lim_lo, float lim_hi, Kro
     if (dlnT) dlnT[0] = dlnT[1] = dlnT[2] = 0.0;
 }
 
-// The model's IMF by type (0 Salpeter and 2 Kroupa through the Kroupa form, 3 van Dokkum, 4 Dave).
-__device__ inline void imf_setup(int imf_type, const double *p, float lim_lo, float lim_hi, KroupaSeg &k,
-                                 float &inv_total, double *dlnT) {
-    if (imf_type == 3) vd_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
-    else if (imf_type == 4) dave_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
-    else kroupa_setup(p, lim_lo, lim_hi, k, inv_total, dlnT);
+// The model's IMF by type (0 Salpeter and 2 Kroupa through the Kroupa form, 1 Chabrier, 3 van Dokkum, 4 Dave, 5 the
+// user's segments with 1 / T from the host), then the limits and the user table of L.
+__device__ inline void imf_setup(int imf_type, const double *p, const OpsImfLim &L, KroupaSeg &k, float &inv_total,
+                                 double *dlnT) {
+    if (imf_type == 3) {
+        const double vdmc = p[0];
+        logn_setup(0.14 * pow(12.5 * vdmc, -1.3), log10(vdmc), 25.0 * vdmc, 0.0443, L.lim_lo, L.lim_hi, k, inv_total,
+                   dlnT);
+    } else if (imf_type == 1) {
+        const double u0 = -1.0969100130080565;   // log10 0.08
+        logn_setup(1.0, u0, 1.0, exp(-u0 * u0 / (2.0 * 0.69 * 0.69)), L.lim_lo, L.lim_hi, k, inv_total, dlnT);
+    } else if (imf_type == 4) {
+        dave_setup(p, L.lim_lo, L.lim_hi, k, inv_total, dlnT);
+    } else if (imf_type == 5) {
+        for (int s = 0; s < 3; ++s) {
+            k.e[s] = k.c[s] = k.ce[s] = 0.f;
+            k.lo[s] = k.hi[s] = 1.0e30f;
+        }
+        k.generic = 1;
+        k.logn = 0;
+        k.la = k.u0 = k.zs = 0.f;
+        k.lnb = k.d3 = 0.0;
+        inv_total = (float)L.user_inv_total;
+        if (dlnT) dlnT[0] = dlnT[1] = dlnT[2] = 0.0;
+    } else {
+        kroupa_setup(p, L.lim_lo, L.lim_hi, k, inv_total, dlnT);
+        if (imf_type == 0) {
+            // Salpeter (imf_integral case 0): m^-2.35 with no cut at 0.08 M_sun (the Kroupa form's equal segments,
+            // the first opened down to 0); its mass between the limits in closed form
+            k.lo[0] = 0.f;
+            const double total = (pow(L.lim_hi, -0.35) - pow(L.lim_lo, -0.35)) / -0.35;
+            inv_total = L.lim_hi > L.lim_lo ? (float)(1.0 / total) : 1.f;
+        }
+    }
+    k.custom = L.custom;
+    k.glo = (float)L.lim_lo;
+    k.ghi = (float)L.lim_hi;
+    k.lb = L.lb;
+    k.user = L.user;
+    k.nuser = imf_type == 5 ? L.nuser : 0;
+    if (L.custom) k.generic = 1;
 }
 
 // A point's IMF bin weight (before the normalisation) and its derivatives: phi = sum of its segments' pieces
@@ -291,7 +365,17 @@ __device__ __forceinline__ void seg_piece_tan(const KroupaSeg &k, int s, float l
 }
 __device__ __forceinline__ ImfTan imf_weight_tan(const KroupaSeg &k, const OpsPoint &q) {
     ImfTan r = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (q.seg < 0) return r;
+    float qlo = q.lo;
+    if (k.custom) {
+        qlo = custom_lo(k, q);
+        if (qlo < 0.f) return r;
+        if (k.nuser) {   // (the user IMF: no parameter of the reverse pass)
+            r.phi = user_piece(k, qlo, q.hi);
+            return r;
+        }
+    } else if (q.seg < 0) {
+        return r;
+    }
     float P, D;
     if (q.seg > 0 && !k.generic) {
         const int s = q.seg - 1;
@@ -305,9 +389,9 @@ __device__ __forceinline__ ImfTan imf_weight_tan(const KroupaSeg &k, const OpsPo
     }
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-        const float lo = fmaxf(q.lo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
+        const float lo = fmaxf(qlo, k.lo[s]), hi = fminf(q.hi, k.hi[s]);
         if (hi > lo) {
-            if (s == 0 && k.logn) {   // (van Dokkum's lognormal: no parameter of the reverse pass)
+            if (s == 0 && k.logn) {   // (van Dokkum's and Chabrier's lognormal: no parameter of the reverse pass)
                 P = logn_piece(k, lo, hi);
                 D = 0.f;
             } else {
@@ -358,7 +442,7 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_fold_kernel(OpsFoldArgs a)
         sw_s[t][k] = (sw > SAFE_FLOOR) ? (float)sw : 0.f;
     }
     if (tid < OPS_K)
-        imf_setup(a.imf_type, a.alpha + 3 * min(m0 + tid, a.n - 1), a.lim_lo, a.lim_hi, kseg[tid], inv_total[tid], nullptr);
+        imf_setup(a.imf_type, a.alpha + 3 * min(m0 + tid, a.n - 1), a.lim, kseg[tid], inv_total[tid], nullptr);
     __syncthreads();
     if (tid == 0) {
         int na = 0;
@@ -767,7 +851,7 @@ __global__ void __launch_bounds__(OPS_THREADS, 2) ops_rev_kernel(OpsRevArgs a) {
     if (tid < OPS_K) {
         const int k = tid, m = min(m0 + k, a.n - 1);
         double dl[3];
-        imf_setup(a.imf_type, a.alpha + 3 * m, a.lim_lo, a.lim_hi, kseg[k], inv_total[k], dl);
+        imf_setup(a.imf_type, a.alpha + 3 * m, a.lim, kseg[k], inv_total[k], dl);
         for (int j = 0; j < 3; ++j) dlnT_s[k][j] = dl[j];
         const double cs = a.cscale[m];
         const double ls = a.sums[(size_t)6 * m + 1];
@@ -1142,7 +1226,7 @@ int run_ops_interp_reverse(Context &c, const OpsRevArgs &r, std::string &err) {
         OpsInterpRevArgs a;
         a.m0 = m0; a.nt = nt; a.nz = nz; a.R = R; a.ktot = ktot; a.imf_type = r.imf_type;
         for (int s = 0; s < 3; ++s) { a.noff[s] = o.interp_noff[s]; a.nn[s] = o.interp_nn[s]; a.x0[s] = o.interp_x0[s]; a.h[s] = o.interp_h[s]; }
-        a.lim_lo = r.lim_lo; a.lim_hi = r.lim_hi;
+        a.lim_lo = (float)r.lim.lim_lo; a.lim_hi = (float)r.lim.lim_hi;
         a.wz = r.wz; a.alpha = r.alpha; a.cscale = r.cscale; a.mass_bar = r.mass_bar; a.lbol_bar = r.lbol_bar; a.lsum_bar = r.lsum_bar; a.sums = r.sums;
         a.kconst = c.d_ix_const.p; a.xbar = c.d_xbar.p; a.mrow = o.i_mrow.p; a.lrow = o.i_lrow.p;
         a.wzb = r.wzb; a.params_bar = r.params_bar; a.rows = r.rows; a.row_imf1 = r.row_imf1;
@@ -1898,7 +1982,7 @@ int ops_build(Context &c, std::string &err) {
             q.hi = (float)m2;
             q.ln_lo = (float)std::log(m1);
             q.dl = (float)std::log1p((m2 - m1) / m1);
-            q.pad = 0;
+            q.mini = (float)(i == 0 ? -mi[i] : mi[i]);
             if (mi[i] < lim_lo || mi[i] > lim_hi || m2 <= m1) q.seg = -1;
             else if (m1 >= 0.08 && m2 <= 0.5) q.seg = 1;
             else if (m1 >= 0.5 && m2 <= 1.0) q.seg = 2;
@@ -1967,6 +2051,8 @@ int ops_build(Context &c, std::string &err) {
 // Whether the interpolated fold holds for every model's slopes (and is built and not switched off).
 static bool ops_interp_ok(const Context &c, const double *h_alpha, int n) {
     if (!c.ops.interp_ready || c.ops_exact || !h_alpha) return false;
+    // (the basis holds the build's mass limits 0.08 - 120 M_sun and the fixed breaks of Kroupa's form)
+    if (c.imf_type == 5 || c.imf_lim_lo != 0.08 || c.imf_lim_hi != 120.0) return false;
     if (c.imf_type == 1) return true;   // (Chabrier: no slopes)
     if (c.imf_type == 3 || c.imf_type == 4) return false;   // (breaks per model: the exact fold)
     for (int m = 0; m < n; ++m)
@@ -2089,10 +2175,9 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     cudaError_t e;
     const int ngroups = (n + 3) / 4;
     const bool interp = ops_interp_ok(c, h_alpha, n);
-    if (!interp && c.imf_type == 1) {
-        err = "the Chabrier IMF takes the interpolated fold (gb300_ops_exact off)";
-        return ST_UNSUPPORTED;
-    }
+    OpsImfLim lim;
+    if (!interp)
+        if (int rc = ops_imf_limits(c, c.imf_type, lim, err)) return rc;
     if ((e = c.d_vhi.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess ||
         (e = c.d_vlo.reserve((size_t)2 * n * o.ntpad)) != cudaSuccess || (e = c.d_sums.reserve((size_t)6 * n)) != cudaSuccess ||
         (!interp && (e = c.d_vpart.reserve((size_t)c.nz * 2 * n * o.ntpad)) != cudaSuccess) ||
@@ -2110,7 +2195,7 @@ int run_ops_parts(Context &c, int n, const double *d_wz, const double *d_alpha, 
     OpsFoldArgs fa;
     fa.n = n; fa.nt = c.nt; fa.nz = c.nz; fa.npt = o.npt; fa.nent = o.nent; fa.ntpad = o.ntpad; fa.itesc = itesc;
     fa.imf_type = c.imf_type;
-    fa.lower_bound = (float)o.lower_bound; fa.lim_lo = 0.08f; fa.lim_hi = 120.f;
+    fa.lim = lim;
     fa.wz = d_wz; fa.alpha = d_alpha; fa.pts = o.pts.p; fa.ent = o.ent.p; fa.ent_c = o.ent_c.p;
     fa.v_hi = c.d_vhi.p; fa.v_lo = c.d_vlo.p; fa.sums = c.d_sums.p;
     fa.vpart = c.d_vpart.p; fa.spart = c.d_spart.p; fa.flag = c.d_vflag.p;
@@ -2141,13 +2226,78 @@ void imf_pack(int imf_type, const double *pv, double *ap) {
     else if (imf_type == 4) ap[2] = pv[4];
 }
 
+// The user IMF (imf_type 5) from imf_filename under the data root, imf.dat when none is set (ssp_gen,
+// src/physics/opensps_ssp.f90:1756-1808): rows of lower mass, upper mass and slope, read up to the first row that
+// does not hold three numbers, at most 100. Read again when the name changes. 0, or ST_IMF_FILE with err.
+static int load_user_imf(Context &c, std::string &err) {
+    const std::string path = data_root() + "/" + (c.imf_filename.empty() ? std::string("imf.dat") : c.imf_filename);
+    if (c.user_imf_file == path && !c.user_imf.empty()) return 0;
+    std::ifstream f(path);
+    if (!f) { err = "imf_type 5: cannot open the user IMF " + path; return ST_IMF_FILE; }
+    std::vector<double> seg;
+    std::string line;
+    while (seg.size() < 300 && std::getline(f, line)) {
+        if (line.find_first_not_of(" \t\r") == std::string::npos) continue;   // (a blank line: the next is read)
+        for (char &ch : line)
+            if (ch == ',') ch = ' ';
+        std::istringstream is(line);
+        double lo, hi, al;
+        if (!(is >> lo >> hi >> al)) break;
+        seg.insert(seg.end(), {lo, hi, al});
+    }
+    if (seg.empty()) { err = "imf_type 5: the user IMF " + path + " has no segments"; return ST_IMF_FILE; }
+    c.user_imf.swap(seg);
+    c.user_imf_file = path;
+    c.user_imf_dirty = true;
+    return 0;
+}
+
+int ops_imf_limits(Context &c, int imf_type, OpsImfLim &lim, std::string &err) {
+    lim = OpsImfLim();
+    lim.lim_lo = c.imf_lim_lo;
+    lim.lim_hi = c.imf_lim_hi;
+    lim.lb = (float)c.imf_lim_lo;   // (each age's first bin starts at the lower limit: non-Geneva isochrones)
+    lim.custom = (c.imf_lim_lo != 0.08 || c.imf_lim_hi != 120.0) ? 1 : 0;
+    if (imf_type != 5) return 0;
+    if (int rc = load_user_imf(c, err)) return rc;
+    const int n = (int)(c.user_imf.size() / 3);
+    const double *u = c.user_imf.data();
+    // the limits become the first segment's lower and the last one's upper mass (the first bin's edge stays)
+    lim.lim_lo = u[0];
+    lim.lim_hi = u[3 * (n - 1) + 1];
+    std::vector<float> t((size_t)5 * n);
+    double cu = 1.0, total = 0.0;
+    for (int s = 0; s < n; ++s) {
+        const double lo = u[3 * s], hi = u[3 * s + 1], al = u[3 * s + 2];
+        if (s > 0) cu *= std::pow(lo, -u[3 * s - 1] + al);   // continuous at the segment's lower mass
+        const double e = 1.0 - al;
+        t[5 * s] = (float)lo; t[5 * s + 1] = (float)hi; t[5 * s + 2] = (float)e;
+        t[5 * s + 3] = e != 0.0 ? (float)(cu / e) : 0.f; t[5 * s + 4] = (float)cu;
+        const double a = std::max(lo, lim.lim_lo), b = std::min(hi, lim.lim_hi), em = 2.0 - al;
+        if (b > a) total += em == 0.0 ? cu * std::log(b / a) : cu * (std::pow(b, em) - std::pow(a, em)) / em;
+    }
+    cudaError_t e;
+    // (a new table once the stream's earlier work, which may read the old one, is done)
+    if (c.user_imf_dirty &&
+        ((e = cudaStreamSynchronize(c.stream)) != cudaSuccess || (e = c.d_user_imf.reserve(t.size())) != cudaSuccess ||
+         (e = cudaMemcpy(c.d_user_imf.p, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice)) != cudaSuccess)) {
+        err = cmsg("user IMF upload", e);
+        return ST_DATA_MISSING;
+    }
+    c.user_imf_dirty = false;
+    lim.user = c.d_user_imf.p;
+    lim.nuser = n;
+    lim.user_inv_total = total > 0.0 ? 1.0 / total : 1.0;
+    lim.custom = 1;
+    return 0;
+}
+
 // One IMF's SSP grid at the context's metallicity zmet: every age as a "model" with a unit weight there.
 int ops_evaluate(Context &c, int imf_type, const double *imf_params, double *mass_grid, double *lbol_grid,
                  double *spec_grid, std::string &err) {
     if (!c.ops.ready) { err = "no SSP operators on the context (opensps_context_build_ssp_ops)"; return ST_NO_OPERATOR; }
-    if (imf_type < 0 || imf_type > 4) {
-        err = "imf_type " + std::to_string(imf_type) +
-              ": 0 (Salpeter), 1 (Chabrier), 2 (Kroupa), 3 (van Dokkum) or 4 (Dave) on this path";
+    if (imf_type < 0 || imf_type > 5) {
+        err = "imf_type " + std::to_string(imf_type) + ": the IMF types are 0 to 5";
         return ST_UNSUPPORTED;
     }
     // (the operator batch takes the context's imf_type: this IMF for the call)

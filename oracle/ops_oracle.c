@@ -9,7 +9,10 @@
  *                            alpha1-3), case 0 Salpeter (slope 2.35, opensps_context_types.f90:120), case 1 Chabrier
  *                            2003 (the lognormal below 1 M_sun, integrate_lognormal :677-722, and the power law above),
  *                            case 3 van Dokkum 2008 (the scaled lognormal up to 25 vdmc, the power law above; constants
- *                            :39-44), case 4 Dave 2008 (slopes alpha1 below mdave and alpha2 above, continuous)
+ *                            :39-44), case 4 Dave 2008 (slopes alpha1 below mdave and alpha2 above, continuous),
+ *                            case 5 the user's segments (:287-305: each a power law over its own mass range, scaled
+ *                            to be continuous at its lower mass; the limits the first lower and last upper mass,
+ *                            src/physics/opensps_ssp.f90:1756-1808)
  *   integrate_powerlaw       src/physics/opensps_imf.f90:725-748 (the expm1 form: oracle_powerlaw_bin)
  *   ssp_op_model_weights / ssp_op_spmv   src/physics/opensps_ssp_operator.f90:1296-1338: W = S . w_IMF with the
  *                            mass and L_bol rows
@@ -34,7 +37,9 @@ typedef struct {
     const double *mcur, *lum;  /* nz x nt x npt */
     double lower_bound, lim_lo, lim_hi;
     int imf_type;              /* 0 Salpeter, 1 Chabrier, 2 Kroupa (alpha per model: imf1-3), 3 van Dokkum (alpha[0]
-                                  = vdmc), 4 Dave (alpha = imf1, imf2, mdave) */
+                                  = vdmc), 4 Dave (alpha = imf1, imf2, mdave), 5 the user's segments */
+    int nuser;
+    const double *user;        /* nuser x 3: lower mass, upper mass, slope */
 } oracle_ops_t;
 
 /* integrate_powerlaw(lo, hi, alpha, mass_weighted, c) */
@@ -118,6 +123,24 @@ double oracle_imf_integral(int imf_type, const double *a, double m1, double m2, 
     return 0.0;
 }
 
+/* imf_integral case 5: the user's segments (n x 3: lower mass, upper mass, slope) over [m1, m2] */
+double oracle_user_imf_integral(int n, const double *u, double m1, double m2, int mass_weighted) {
+    const double lo = fmin(m1, m2), hi = fmax(m1, m2);
+    double v = 0.0, cu = 1.0;
+    if (hi <= lo) return 0.0;
+    for (int s = 0; s < n; ++s) {
+        if (s > 0) cu *= pow(u[3 * s], -u[3 * s - 1] + u[3 * s + 2]);
+        const double a = fmax(lo, u[3 * s]), b = fmin(hi, u[3 * s + 1]);
+        if (b > a) v += powerlaw(a, b, u[3 * s + 2], mass_weighted, cu);
+    }
+    return v;
+}
+
+static double imf_int(const oracle_ops_t *op, const double *a, double m1, double m2, int mass_weighted) {
+    if (op->imf_type == 5) return oracle_user_imf_integral(op->nuser, op->user, m1, m2, mass_weighted);
+    return oracle_imf_integral(op->imf_type, a, m1, m2, mass_weighted);
+}
+
 /* The IMF weights of one grid point's isochrone points (npt), normalised by the IMF's mass over its limits. */
 static void imf_weights(const oracle_ops_t *op, const double *mini, const double *a, double inv_total, double *w) {
     const int n = op->npt;
@@ -127,7 +150,7 @@ static void imf_weights(const oracle_ops_t *op, const double *mini, const double
         const double m1 = (i == 0) ? op->lower_bound : mini[i] - 0.5 * (mini[i] - mini[i - 1]);
         const double m2 = (i == n - 1) ? mini[i] : mini[i] + 0.5 * (mini[i + 1] - mini[i]);
         if (m2 <= m1) continue;
-        w[i] = oracle_imf_integral(op->imf_type, a, m1, m2, 0) * inv_total;
+        w[i] = imf_int(op, a, m1, m2, 0) * inv_total;
     }
 }
 
@@ -144,7 +167,7 @@ void oracle_ops_csp(const oracle_ops_t *op, int n, const double *alpha, const do
 #pragma omp for schedule(dynamic, 1)
         for (int m = 0; m < n; ++m) {
             const double *a = alpha + 3 * (size_t)m;
-            const double total = oracle_imf_integral(op->imf_type, a, op->lim_lo, op->lim_hi, 1);
+            const double total = imf_int(op, a, op->lim_lo, op->lim_hi, 1);
             const double inv = total > 0.0 ? 1.0 / total : 1.0;
             memset(vy, 0, sizeof(double) * ne);
             memset(vo, 0, sizeof(double) * ne);

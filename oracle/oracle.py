@@ -47,7 +47,7 @@ class _OpsT(C.Structure):
     _fields_ = [("nspec", C.c_int), ("nt", C.c_int), ("nz", C.c_int), ("npt", C.c_int), ("ntempl", C.c_int),
                 ("lib", C.POINTER(C.c_float)), ("mini", _dp), ("idx", C.POINTER(C.c_int)), ("coef", _dp),
                 ("mcur", _dp), ("lum", _dp), ("lower_bound", C.c_double), ("lim_lo", C.c_double),
-                ("lim_hi", C.c_double), ("imf_type", C.c_int)]
+                ("lim_hi", C.c_double), ("imf_type", C.c_int), ("nuser", C.c_int), ("user", _dp)]
 
 
 _lib = None
@@ -60,6 +60,8 @@ def lib() -> C.CDLL:
         _lib = C.CDLL(str(LIB))
         _lib.oracle_imf_integral.restype = C.c_double
         _lib.oracle_imf_integral.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_int]
+        _lib.oracle_user_imf_integral.restype = C.c_double
+        _lib.oracle_user_imf_integral.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_int]
         _lib.oracle_dust_curve.restype = C.c_double
         _lib.oracle_dust_curve.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
         _lib.oracle_find_interval.restype = C.c_int
@@ -405,9 +407,11 @@ class Oracle:
 class OpsOracle:
     """The SSP operator applied to per-model IMFs (ops_oracle.c) over the operator dataset (synth_ops): imf_type 2
     Kroupa (alpha per model: imf1-3), 0 Salpeter, 1 Chabrier, 3 van Dokkum (alpha[:, 0] = vdmc), 4 Dave (alpha =
-    imf1, imf2, mdave)."""
+    imf1, imf2, mdave), 5 the user's segments (user: rows of lower mass, upper mass, slope; the limits become its
+    first lower and last upper mass). lower_bound: the lower edge of each age's first bin (the dataset's when None)."""
 
-    def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0, imf_type: int = 2):
+    def __init__(self, ops: dict, lim_lo: float = 0.08, lim_hi: float = 120.0, imf_type: int = 2, user=None,
+                 lower_bound=None):
         self.ops = ops
         man = ops["manifest"]
         self.nspec, self.nt, self.nz, self.npt, self.ntempl = man["nspec"], man["nt"], man["nz"], man["npt"], man["ntempl"]
@@ -418,8 +422,14 @@ class OpsOracle:
         t.lib = lb.ctypes.data_as(C.POINTER(C.c_float))
         t.mini, t.coef, t.mcur, t.lum = _p(mi), _p(co), _p(mc), _p(lu)
         t.idx = ix.ctypes.data_as(C.POINTER(C.c_int))
-        t.lower_bound, t.lim_lo, t.lim_hi = man["imf_lower_bound"], lim_lo, lim_hi
+        t.lower_bound, t.lim_lo, t.lim_hi = man["imf_lower_bound"] if lower_bound is None else lower_bound, lim_lo, lim_hi
         t.imf_type = int(imf_type)
+        if user is not None:
+            u = np.ascontiguousarray(user, dtype=np.float64).reshape(-1, 3)
+            self._keep.append(u)
+            t.nuser, t.user = u.shape[0], _p(u)
+            if imf_type == 5:
+                t.lim_lo, t.lim_hi = float(u[0, 0]), float(u[-1, 1])
         self.t = t
 
     def parts(self, alpha: np.ndarray, wz: np.ndarray, itesc: int):
@@ -436,6 +446,11 @@ class OpsOracle:
 def imf_integral(imf_type: int, m1: float, m2: float, mass_weighted: bool, alpha=(1.3, 2.3, 2.3)) -> float:
     a = np.ascontiguousarray(alpha, dtype=np.float64)
     return lib().oracle_imf_integral(int(imf_type), _p(a), float(m1), float(m2), int(mass_weighted))
+
+
+def user_imf_integral(user, m1: float, m2: float, mass_weighted: bool) -> float:
+    u = np.ascontiguousarray(user, dtype=np.float64).reshape(-1, 3)
+    return lib().oracle_user_imf_integral(u.shape[0], _p(u), float(m1), float(m2), int(mass_weighted))
 
 
 def kroupa_integral(alpha, m1: float, m2: float, mass_weighted: bool) -> float:

@@ -84,6 +84,45 @@ def test_imf_integrals_match_quadrature(imf_type):
             assert abs(got / q - 1.0) <= 1.0e-8, (imf_type, lo, hi, mw, got, q)
 
 
+def _user_density(user, m):
+    """get_imf_value case 5 restated for the test: each segment c_s m^-alpha_s on [lo_s, hi_s), c_s continuous at
+    lo_s; overlapping segments add."""
+    v, cu = np.zeros_like(m), 1.0
+    for s, (lo, hi, al) in enumerate(user):
+        if s:
+            cu *= lo ** (-user[s - 1][2] + al)
+        v += np.where((m >= lo) & (m < hi), cu * m ** -al, 0.0)
+    return v
+
+
+def test_user_imf_integral_matches_quadrature():
+    """imf_integral case 5 (src/physics/opensps_imf.f90:287-305) against Simpson's rule between the segments'
+    edges: a chain with a gap (0.4 - 0.5 M_sun empty) and a segment overlapping another (3 - 10 M_sun); with the rows
+    of the reference's test imf.dat (Kroupa's slopes to 100 M_sun) it is the Kroupa integral."""
+    from oracle.oracle import imf_integral, user_imf_integral
+    user = [(0.1, 0.4, 1.1), (0.5, 2.0, 2.0), (2.0, 60.0, 2.6), (3.0, 10.0, 1.0)]
+    edges = sorted({e for r in user for e in r[:2]})
+    for lo, hi in ((0.08, 0.3), (0.2, 0.7), (0.45, 2.5), (2.5, 12.0), (0.05, 100.0), (0.1, 60.0)):
+        cuts = [lo] + [e for e in edges if lo < e < hi] + [hi]
+        for mw in (False, True):
+            q = 0.0
+            for a, b in zip(cuts[:-1], cuts[1:]):
+                n = 20000
+                u = np.log(a) + (np.log(b) - np.log(a)) * np.arange(n + 1) / n
+                m = np.exp(u)
+                m[0], m[-1] = a, b * (1.0 - 1e-15)   # (the piece's own side of its upper edge)
+                c = np.where(np.arange(n + 1) % 2 == 1, 4.0, 2.0)
+                c[0] = c[-1] = 1.0
+                f = _user_density(user, m) * m * (m if mw else 1.0)
+                q += float(np.sum(c * f)) * (u[-1] - u[0]) / n / 3.0
+            got = user_imf_integral(user, lo, hi, mw)
+            assert abs(got / q - 1.0) <= 1.0e-8, (lo, hi, mw, got, q)
+    kroupa_rows = [(0.08, 0.5, 1.3), (0.5, 1.0, 2.3), (1.0, 100.0, 2.3)]
+    for lo, hi in ((0.08, 100.0), (0.3, 0.7), (0.9, 40.0)):
+        for mw in (False, True):
+            assert user_imf_integral(kroupa_rows, lo, hi, mw) == pytest.approx(imf_integral(2, lo, hi, mw), rel=1e-14)
+
+
 @pytest.mark.parametrize("imf_type", [1, 3])
 def test_lognormal_wide_bin_is_the_sum_of_narrow_bins(imf_type):
     from oracle.oracle import imf_integral

@@ -117,9 +117,9 @@ def test_operator_refusals(data, built_lib, ops_data):
         c.csp_batch(params, ssp_weights_z=wz)
     assert e.value.status == 2
     c.set_int("add_neb_emission", 0)
-    # an IMF type the operators do not take (the user IMF)
+    # an IMF type beyond the reference's 0 - 5
     with pytest.raises(OpenSPSError) as e:
-        c.evaluate_ssp_op([1.3, 2.3, 2.3, 0.08, 0.5], imf_type=5)
+        c.evaluate_ssp_op([1.3, 2.3, 2.3, 0.08, 0.5], imf_type=6)
     assert e.value.status == 2
     c.free_ssp_ops()
     assert not c.has_ssp_ops

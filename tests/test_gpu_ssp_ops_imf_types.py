@@ -6,7 +6,8 @@ oracle's bin integrals of the same IMFs (ops_oracle.c, imf_integral cases 0, 1, 
 src/physics/opensps_imf.f90:206-315): evaluate_ssp_op at every age, the batch through the operator, the reverse
 pass's weights' cotangent along a random direction against central differences, the IMF's rows (zero for
 Salpeter, Chabrier and van Dokkum, which have no parameters there; Dave's imf1, imf2 and mdave against central
-differences, imf_integral_dp :833-900), and the refusals (imf_type 5; Chabrier with the exact fold forced).
+differences, imf_integral_dp :833-900), Chabrier's exact fold against its interpolated one, and the refusal of
+an IMF type beyond 5 (the user IMF, type 5, and other mass limits: test_gpu_ssp_ops_user_imf.py).
 
 Tolerances as the Kroupa tests: spectra <= 1e-4 relative (pixels above 1e-6 of the peak), magnitudes <= 1e-3 mag,
 mass and L_bol <= 1e-5 relative; gradients 2e-3.
@@ -206,21 +207,29 @@ def test_breaks_per_model_reverse(octx, data, ops_data, imf_type):
         assert float(e.max()) <= 2e-3, (k, pb[:, row], fdk)
 
 
-def test_refusals(octx, data):
+def test_chabrier_exact_fold_and_refusal(octx, data):
+    """Chabrier through the exact fold (its lognormal's bin integrals as van Dokkum's, the power law above 1 M_sun)
+    against the interpolated fold; an IMF type beyond 5 refused."""
     from libopensps_gb300.capi import OpenSPSError
-    n = 4
+    n = 24
     wz, params = config3_inputs(n, seed=350)
-    for t in (5,):
-        octx.set_int("imf_type", t)
-        with pytest.raises(OpenSPSError) as e:
-            octx.csp_batch(params, ssp_weights_z=wz)
-        assert e.value.status == 2
     octx.set_int("imf_type", 1)
-    octx.set_int("gb300_ops_exact", 1)
+    try:
+        a = octx.csp_batch(params, ssp_weights_z=wz)
+        assert octx.ops_last_interpolated()
+        octx.set_int("gb300_ops_exact", 1)
+        b = octx.csp_batch(params, ssp_weights_z=wz)
+        assert not octx.ops_last_interpolated()
+    finally:
+        octx.set_int("gb300_ops_exact", 0)
+        octx.set_int("imf_type", 2)
+    assert rel_err_spec(a["spec"], b["spec"]) <= 5e-5
+    np.testing.assert_allclose(a["mass"], b["mass"], rtol=2e-6)
+    np.testing.assert_allclose(a["lbol"], b["lbol"], rtol=2e-6)
+    octx.set_int("imf_type", 6)
     try:
         with pytest.raises(OpenSPSError) as e:
             octx.csp_batch(params, ssp_weights_z=wz)
-        assert e.value.status == 2 and "Chabrier" in e.value.message
+        assert e.value.status == 2
     finally:
-        octx.set_int("gb300_ops_exact", 0)
         octx.set_int("imf_type", 2)
