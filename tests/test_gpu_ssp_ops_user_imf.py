@@ -27,6 +27,8 @@ pytestmark = pytest.mark.gpu
 
 # four segments: a gap-free chain to 60 M_sun and a fourth overlapping the third over 3 - 10 M_sun
 USER = np.array([[0.1, 0.4, 1.1], [0.4, 2.0, 2.0], [2.0, 60.0, 2.6], [3.0, 10.0, 1.0]])
+# three segments with an empty gap over 0.4 - 0.5 M_sun, to 80 M_sun
+USER_GAP = np.array([[0.1, 0.4, 1.1], [0.5, 2.0, 2.0], [2.0, 80.0, 2.6]])
 # the rows of the reference's test imf.dat: Kroupa's slopes, to 100 M_sun
 KROUPA_ROWS = np.array([[0.08, 0.5, 1.3], [0.5, 1.0, 2.3], [1.0, 100.0, 2.3]])
 
@@ -114,15 +116,21 @@ def _imf_params(n, seed):
             "vdmc": 10.0 ** rng.uniform(-1.2, 0.0, n), "mdave": 10.0 ** rng.uniform(-0.6, 0.4, n)}
 
 
-def test_user_imf_evaluate(octx, ops_data):
+@pytest.mark.parametrize("table", ["overlap", "gap"])
+def test_user_imf_evaluate(octx, ops_data, table):
     from oracle.oracle import OpsOracle
+    rows = USER if table == "overlap" else USER_GAP
+    if table == "gap":
+        _write("imf_gap_test.dat", USER_GAP)
+        octx.set_str("imf_filename", "imf_gap_test.dat")
     octx.set_int("zmet", 4)
     try:
         got = octx.evaluate_ssp_op(imf_type=5)
     finally:
         octx.set_int("zmet", 1)
+        octx.set_str("imf_filename", "imf_user_test.dat")
     nt, nz = octx.ntfull, octx.nz
-    y, o, mass, ls = OpsOracle(ops_data, imf_type=5, user=USER).parts(np.zeros((nt, 3)), _grid_weights(nt, nz, 3), nt)
+    y, o, mass, ls = OpsOracle(ops_data, imf_type=5, user=rows).parts(np.zeros((nt, 3)), _grid_weights(nt, nz, 3), nt)
     assert np.all(o == 0.0)
     assert rel_err_spec(got["spec"], y) <= 1e-4
     np.testing.assert_allclose(got["mass"], mass, rtol=1e-5)
