@@ -5,7 +5,8 @@
 // spectrum resampled to the observed frame at its redshift, divided by lambda (observed_frame_z :819-903), then the
 // trapezoid filter integrals regrouped by pixel, C(j, b) = band(j, b) (wtl(j - 1) + wtl(j)) (the split-K product
 // :1002-1044, prepare_batch_grid :375-392), then magnitudes_from_fluxes :185-232 (AB, distance term, NaN for bands
-// not computed).
+// not computed). The division by lambda is folded into the band matrix (C(j, b) / lambda(j), formed in FP64 on the
+// host), so the A operand is the resampled spectrum itself.
 //
 // Per CTA: 128 models (MMA M). K = the pixels that any band reaches, 64 per stage. The A operand (observed frame
 // of 128 models x 64 pixels) is built by warps 0..7 in shared memory from the spectra, in the 128-byte swizzled
@@ -149,9 +150,6 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             // the stage's A buffer is free once the MMAs of stage li - 2 have completed
             if (li >= 2 && !mbar_wait(&empty[s], ((li - 2) >> 1) & 1, status, ERR_TIMEOUT_BAND)) break;
             const int j = a.j0 + kb * BG_K + 4 * q;          // first observed pixel of this lane
-            float wl[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) wl[u] = (j + u < a.nspec) ? __ldg(a.wl + j + u) : 0.f;
             // the loads of all 4 row pairs first (rows whose 5 rest pixels lie inside the grid: the interior case),
             // then the arithmetic
             float sv[4][5];
@@ -171,14 +169,11 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                 const int r = warp * 8 + 2 * i + hr;
                 float f[4];
                 if (inner[i]) {
-                    // v = s(c) + t (s(c + 1) - s(c)), t = 0 for whole shifts and the rest frame (v = s(c) exactly);
-                    // NaN -> 0 and negatives -> 0 in one fmaxf
+                    // v = s(c) + t (s(c + 1) - s(c)), t = 0 for whole shifts and the rest frame (v = s(c) exactly
+                    // for finite spectra); NaN -> 0 and negatives -> 0 in one fmaxf
                     const float t = zsm[r].y;
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float v = t > 0.f ? fmaf(t, sv[i][u + 1] - sv[i][u], sv[i][u]) : sv[i][u];
-                        f[u] = fmaxf(v, 0.f) * wl[u];
-                    }
+                    for (int u = 0; u < 4; ++u) f[u] = fmaxf(fmaf(t, sv[i][u + 1] - sv[i][u], sv[i][u]), 0.f);
                 } else {
                     // the general case: no model, pixels past the grid's end, or intervals outside the grid (they
                     // extrapolate from the first / last one, the reference's clamped find_interval: position
@@ -199,7 +194,7 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
                         } else if (zs.w == 0.f && ju < a.nspec) {
                             v = __ldg(sp + ju);
                         }
-                        f[u] = fmaxf(v, 0.f) * wl[u];
+                        f[u] = fmaxf(v, 0.f);
                     }
                 }
                 // bf16 hi and lo parts, four pixels = 8 bytes of the row's 128-byte swizzled line

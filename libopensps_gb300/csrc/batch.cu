@@ -964,7 +964,7 @@ int run_batch(Context &c, const BatchIO &io, std::string &err) {
     auto bands = [&](int off, int nk) -> cudaError_t {
         BandGemmArgs ba;
         ba.n_models = nk; ba.nspec = ns; ba.nbands = nb; ba.npad = c.band_npad; ba.nkb = c.band_nkb; ba.j0 = c.band_j0;
-        ba.ld_spec = ns; ba.spec = c.d_spec.p + (size_t)ns * off; ba.zinfo = c.d_zinfo.p + off; ba.wl = c.d_wl.p;
+        ba.ld_spec = ns; ba.spec = c.d_spec.p + (size_t)ns * off; ba.zinfo = c.d_zinfo.p + off;
         ba.dlnl = c.dlnl; ba.dist = c.d_dist.p + off;
         ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
         ba.do_band = c.d_do_band.p; ba.fband = io.fband_dev ? io.fband_dev + (size_t)nb * off : nullptr;

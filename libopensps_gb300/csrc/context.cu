@@ -428,7 +428,9 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
         j1 = std::max(j1, jhi + 1);
     }
     if (j1 < j0) { j0 = 0; j1 = -1; }
-    // the band GEMM's B operand: rows = bands (padded to npad), columns = pixels j0 .. j0 + 64 nkb - 1, bf16 hi + lo
+    // the band GEMM's B operand: rows = bands (padded to npad), columns = pixels j0 .. j0 + 64 nkb - 1, bf16 hi + lo;
+    // each pixel's 1 / lambda (the observed-frame spectrum's division by the wavelength) folded in here, in FP64, so
+    // that the kernel's operand builders do not multiply by it
     const int npad = band_gemm_npad(nb);
     if (npad > 256) { err = "more than 256 bands"; return ST_BAD_ARG; }
     const int nkb = (j1 - j0 + 1 + 63) / 64, kpad = 64 * nkb;
@@ -437,7 +439,8 @@ int context_load_filters(Context &c, const std::string &name, std::string &err) 
         for (int k = 0; k < kpad; ++k) {
             const int j = j0 + k;
             if (j >= ns) break;
-            const float f = (float)cm[(size_t)b * ns + j];
+            const double inv_l = c.lam[j] > 2.2250738585072014e-308 ? 1.0 / c.lam[j] : 0.0;
+            const float f = (float)(cm[(size_t)b * ns + j] * inv_l);
             const uint16_t h = f32_to_bf16_bits(f);
             hi[(size_t)b * kpad + k] = h;
             lo[(size_t)b * kpad + k] = f32_to_bf16_bits(f - bf16_bits_to_f32(h));

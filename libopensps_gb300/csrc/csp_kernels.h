@@ -146,7 +146,6 @@ struct BandGemmArgs {
     int n_models, nspec, nbands, npad, nkb, j0, ld_spec;
     const float *spec;      // n_models x ld_spec rest-frame spectra
     const float4 *zinfo;    // n_models: (n0 as int bits, t of the interior interpolation, shift s in pixels, 0 at z = 0)
-    const float *wl;        // nspec: 1 / lambda
     double dlnl;            // grid step in ln lambda
     const double *dist;     // n_models: distance term
     double zp;              // 48.60 + 2.5 ABS_MAG_ZEROPOINT_LOG

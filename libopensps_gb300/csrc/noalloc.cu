@@ -146,7 +146,7 @@ int run_mags_noalloc(Context &c, int n, const float *d_spec, const double *d_zre
         if (e == cudaSuccess) {
             BandGemmArgs ba{};
             ba.n_models = n; ba.nspec = c.nspec; ba.nbands = c.nbands; ba.npad = c.band_npad; ba.nkb = c.band_nkb;
-            ba.j0 = c.band_j0; ba.ld_spec = c.nspec; ba.spec = d_spec; ba.zinfo = zinfo; ba.wl = c.d_wl.p;
+            ba.j0 = c.band_j0; ba.ld_spec = c.nspec; ba.spec = d_spec; ba.zinfo = zinfo;
             ba.dlnl = c.dlnl; ba.dist = dist;
             ba.zp = 48.60 + 2.5 * std::log10(3.828e33 / (4.0 * M_PI * std::pow(10.0 * (648000.0 / M_PI) * 1.495978707e13, 2)));
             ba.do_band = do_band; ba.fband = nullptr; ba.mags = d_mags; ba.status = status;
