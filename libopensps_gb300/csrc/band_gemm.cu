@@ -79,7 +79,9 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
     const uint32_t tcols = npad <= 32 ? 32 : (npad <= 64 ? 64 : (npad <= 128 ? 128 : 256));
     __shared__ float4 zsm[BG_M];     // the observed-frame shift of the CTA's models (w = 2: no model in this row)
     __shared__ int2 rsh[BG_M];       // per row: the rest-frame offset d (observed pixel j reads j - d, j - d + 1) and
-                                     // its kind (0 rest frame, 1 shifted, 2 no model)
+                                     // the last first-pixel j of a lane whose five rest pixels j - d .. j - d + 4 and
+                                     // four observed ones lie inside the grid (the interior case: d <= j <= that;
+                                     // a row without a model has none)
 
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) { mbar_init(&full_a[s], BG_BUILD_WARPS); mbar_init(&full_b[s], 1); mbar_init(&empty[s], 1); }
@@ -94,7 +96,8 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
         zsm[i] = zs;
         // the interior interpolation's first rest pixel: n0 + 1 below the observed one unless the shift is whole
         const int kind = zs.w == 1.f ? 1 : (zs.w == 0.f ? 0 : 2);
-        rsh[i] = make_int2(kind == 1 ? __float_as_int(zs.x) + (zs.y > 0.f ? 1 : 0) : 0, kind);
+        const int d = kind == 1 ? __float_as_int(zs.x) + (zs.y > 0.f ? 1 : 0) : 0;
+        rsh[i] = make_int2(d, kind == 2 ? -1 : min(a.nspec - 5 + d, a.nspec - 4));
     }
     tc_fence_before();
     __syncthreads();
@@ -158,9 +161,8 @@ band_gemm_kernel(const __grid_constant__ CUtensorMap tm_c_hi, const __grid_const
             for (int i = 0; i < 4; ++i) {
                 const int r = warp * 8 + 2 * i + hr;
                 const int2 rs = rsh[r];
-                const int c = j - rs.x;
-                inner[i] = rs.y != 2 && c >= 0 && c + 4 < a.nspec && j + 3 < a.nspec;
-                const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec + c;
+                inner[i] = j >= rs.x && j <= rs.y;
+                const float *sp = a.spec + (size_t)(m0 + r) * a.ld_spec + (j - rs.x);
 #pragma unroll
                 for (int u = 0; u < 5; ++u) sv[i][u] = inner[i] ? __ldg(sp + u) : 0.f;
             }
